@@ -1,0 +1,137 @@
+// Shared device-side definitions of the GB300 dry dynamical core.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "geometry.h"
+
+namespace gb {
+
+// Device status word bits (read back by the host).
+enum : int { ST_TIMEOUT = 1, ST_NONFINITE = 2 };
+// Iteration limit of every bounded spin-wait on an mbarrier.
+constexpr long long WAIT_LIMIT = 1LL << 26;
+
+template <class FT>
+struct DevParams {
+  int Nh, Nv, Nf, ngroups;
+  FT grav, Rd, cpd, cvd, T0, pref, kappa, Tmin_ref, Tsfc_ref, Tmin_sgs;
+  FT nu_v, nu_s, div_damp, dt_model;
+  int upwinding;
+  FT W[NN];
+  FT D[NQ * NQ];  // D[i*4+k] = l_k'(xi_i)
+  const FT *hgeo;  // [Nh][HG_N][16]
+  const FT *levc;  // [LC_N][Nv]
+  const FT *levf;  // [LF_N][Nf]
+  const int *goff, *gcopy;
+  const FT *gw, *ecov, *econ;  // ecov/econ: [Nh*16][6]
+  int *status;
+};
+
+// ---------------------------------------------------------------- math
+__device__ __forceinline__ float gpow(float x, float y) { return powf(x, y); }
+__device__ __forceinline__ double gpow(double x, double y) { return pow(x, y); }
+__device__ __forceinline__ float glog(float x) { return logf(x); }
+__device__ __forceinline__ double glog(double x) { return log(x); }
+__device__ __forceinline__ float gsin(float x) { return sinf(x); }
+__device__ __forceinline__ double gsin(double x) { return sin(x); }
+
+template <class FT>
+__device__ __forceinline__ FT shfl(FT v, int src, int width) {
+  return __shfl_sync(0xffffffffu, v, src, width);
+}
+template <class FT>
+__device__ __forceinline__ FT shfl_up(FT v, int d) {
+  return __shfl_up_sync(0xffffffffu, v, d);
+}
+template <class FT>
+__device__ __forceinline__ FT shfl_down(FT v, int d) {
+  return __shfl_down_sync(0xffffffffu, v, d);
+}
+
+// Dry thermodynamics of Thermodynamics.jl with e_int = cv_d (T - T_0) - R_d T_0,
+// and the hydrostatic reference state of src/utils/refstate_thermodynamics.jl.
+template <class FT>
+struct Thermo {
+  FT T, p, h, Pi, thv, thvr, phir;
+};
+template <class FT>
+__device__ __forceinline__ void thermo(const DevParams<FT> &P, FT rho, FT rhoe, FT K, FT Phi, Thermo<FT> &o) {
+  FT e_tot = rhoe / rho;
+  FT eint = e_tot - K - Phi;
+  FT T = P.T0 + (eint + P.Rd * P.T0) / P.cvd;
+  T = T > P.Tmin_sgs ? T : P.Tmin_sgs;
+  FT p = rho * P.Rd * T;
+  FT Pi = gpow(p / P.pref, P.kappa);
+  FT Pi2 = Pi * Pi, Pi7 = Pi2 * Pi2 * Pi2 * Pi;
+  FT Tr = P.Tmin_ref + (P.Tsfc_ref - P.Tmin_ref) * Pi7;
+  o.T = T;
+  o.p = p;
+  o.h = e_tot + P.Rd * T;
+  o.Pi = Pi;
+  o.thv = T / Pi;
+  o.thvr = Tr / Pi;
+  o.phir = -P.cpd * (P.Tmin_ref * glog(Pi) + (P.Tsfc_ref - P.Tmin_ref) / FT(7) * (Pi7 - FT(1)));
+}
+template <class FT>
+__device__ __forceinline__ FT sd_r(const DevParams<FT> &P, FT Pi, FT phir) {
+  FT Pi2 = Pi * Pi, Pi7 = Pi2 * Pi2 * Pi2 * Pi;
+  return P.cpd * (P.Tmin_ref + (P.Tsfc_ref - P.Tmin_ref) * Pi7 - P.T0) + phir;
+}
+
+// ---------------------------------------------------------------- TMA (bulk copy) + mbarrier
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(uint64_t *bar, int count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void fence_mbar_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void fence_proxy_async() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+// 1-D TMA bulk copy global -> shared, completing on an mbarrier.  dst, src and
+// bytes must be multiples of 16.
+__device__ __forceinline__ void tma_load(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+// 1-D TMA bulk copy shared -> global (bulk-group completion).
+__device__ __forceinline__ void tma_store(void *dst, const void *src, uint32_t bytes) {
+  asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(dst), "r"(smem_u32(src)), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void tma_store_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void tma_store_wait_read() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
+__device__ __forceinline__ void tma_store_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// Bounded wait: returns false (and flags ST_TIMEOUT) if the phase did not
+// complete within WAIT_LIMIT polls; the caller then waits once more, with the
+// same limit, for its own copies and skips its work.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity, int *status) {
+  for (long long it = 0; it < WAIT_LIMIT; ++it)
+    if (mbar_try_wait(bar, parity)) return true;
+  if (status) atomicOr(status, ST_TIMEOUT);
+  for (long long it = 0; it < WAIT_LIMIT; ++it)
+    if (mbar_try_wait(bar, parity)) break;
+  return false;
+}
+
+__host__ __device__ constexpr size_t align16(size_t b) { return (b + 15) & ~size_t(15); }
+
+}  // namespace gb

@@ -1,0 +1,548 @@
+// C ABI of the GB300 dry dynamical core: context, hooks and the fused ARS343
+// step (see include/gbdycore.h for the interface and its reference citations).
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "gbdycore.h"
+#include "kernels.cuh"
+
+using namespace gb;
+
+namespace {
+
+struct DevBuf {
+  void *p = nullptr;
+  size_t bytes = 0;
+  ~DevBuf() { if (p) cudaFree(p); }
+};
+
+struct ImplBase {
+  virtual ~ImplBase() {}
+};
+
+template <class FT>
+struct Impl : ImplBase {
+  DevParams<FT> P{};
+  DevBuf hgeo, levc, levf, goff, gcopy, gw, ecov, econ, status;
+  DevBuf lap, U, Te[4], Ti[4], jac, rnorm, partials, sums, rsum;
+  size_t NC = 0, NF = 0, NR = 0;  // centre, face and reduced-centre element counts
+  int nsum_blocks = 0;
+  bool jac_valid = false;
+  // ARS343 tableau (explicit a~, implicit a, weights b~ = b)
+  double ae[4][4], ai[4][4], be[4], bi[4];
+  // captured step graph
+  cudaGraphExec_t gexec = nullptr;
+  void *g_c = nullptr, *g_f = nullptr;
+  double g_dt = 0;
+  ~Impl() {
+    if (gexec) cudaGraphExecDestroy(gexec);
+  }
+};
+
+}  // namespace
+
+struct gb_ctx {
+  gb_config cfg{};
+  HostGeometry geo;
+  cudaStream_t stream = nullptr;
+  ImplBase *impl = nullptr;
+  std::string err;
+  int last = GB_OK;
+  ~gb_ctx() { delete impl; }
+};
+
+namespace {
+
+int fail(gb_ctx *c, int code, const std::string &msg) {
+  if (c) {
+    c->err = msg;
+    c->last = code;
+  }
+  return code;
+}
+
+#define CK(call)                                                                                \
+  do {                                                                                          \
+    cudaError_t e_ = (call);                                                                    \
+    if (e_ != cudaSuccess) return fail(ctx, GB_ERR_CUDA, std::string(#call ": ") + cudaGetErrorString(e_)); \
+  } while (0)
+
+template <class FT>
+int upload(gb_ctx *ctx, DevBuf &b, const std::vector<double> &v) {
+  std::vector<FT> t(v.begin(), v.end());
+  b.bytes = t.size() * sizeof(FT);
+  if (cudaMalloc(&b.p, b.bytes ? b.bytes : 16) != cudaSuccess) return fail(ctx, GB_ERR_NOMEM, "cudaMalloc failed");
+  CK(cudaMemcpy(b.p, t.data(), b.bytes, cudaMemcpyHostToDevice));
+  return GB_OK;
+}
+int upload_i(gb_ctx *ctx, DevBuf &b, const std::vector<int> &v) {
+  b.bytes = v.size() * sizeof(int);
+  if (cudaMalloc(&b.p, b.bytes ? b.bytes : 16) != cudaSuccess) return fail(ctx, GB_ERR_NOMEM, "cudaMalloc failed");
+  CK(cudaMemcpy(b.p, v.data(), b.bytes, cudaMemcpyHostToDevice));
+  return GB_OK;
+}
+int alloc(gb_ctx *ctx, DevBuf &b, size_t bytes) {
+  b.bytes = bytes;
+  if (cudaMalloc(&b.p, bytes ? bytes : 16) != cudaSuccess)
+    return fail(ctx, GB_ERR_NOMEM, "cudaMalloc of " + std::to_string(bytes) + " bytes failed");
+  CK(cudaMemset(b.p, 0, bytes ? bytes : 16));
+  return GB_OK;
+}
+
+void ars343(double ae[4][4], double ai[4][4], double be[4], double bi[4]) {
+  // Ascher, Ruuth & Spiteri (1997), the (3,4,3) scheme
+  const double g = 0.4358665215084590;
+  const double a42 = 0.5529291480359398, a43 = a42;
+  const double b1 = -1.5 * g * g + 4 * g - 0.25, b2 = 1.5 * g * g - 5 * g + 1.25;
+  const double a31 = (1 - 4.5 * g + 1.5 * g * g) * a42 + (2.75 - 10.5 * g + 3.75 * g * g) * a43 - 3.5 + 13 * g - 4.5 * g * g;
+  const double a32 = (-1 + 4.5 * g - 1.5 * g * g) * a42 + (-2.75 + 10.5 * g - 3.75 * g * g) * a43 + 4 - 12.5 * g + 4.5 * g * g;
+  const double a41 = 1 - a42 - a43;
+  const double E[4][4] = {{0, 0, 0, 0}, {g, 0, 0, 0}, {a31, a32, 0, 0}, {a41, a42, a43, 0}};
+  const double I[4][4] = {{0, 0, 0, 0}, {0, g, 0, 0}, {0, (1 - g) / 2, g, 0}, {0, b1, b2, g}};
+  const double B[4] = {0, b1, b2, g};
+  for (int i = 0; i < 4; ++i) {
+    for (int j = 0; j < 4; ++j) { ae[i][j] = E[i][j]; ai[i][j] = I[i][j]; }
+    be[i] = B[i]; bi[i] = B[i];
+  }
+}
+
+template <class FT>
+int create_impl(gb_ctx *ctx) {
+  auto *I = new (std::nothrow) Impl<FT>();
+  if (!I) return fail(ctx, GB_ERR_NOMEM, "host allocation failed");
+  ctx->impl = I;
+  const HostGeometry &g = ctx->geo;
+  const gb_config &c = ctx->cfg;
+  int r;
+  if ((r = upload<FT>(ctx, I->hgeo, g.hgeo))) return r;
+  if ((r = upload<FT>(ctx, I->levc, g.levc))) return r;
+  if ((r = upload<FT>(ctx, I->levf, g.levf))) return r;
+  if ((r = upload_i(ctx, I->goff, g.grp_off))) return r;
+  if ((r = upload_i(ctx, I->gcopy, g.grp_copy))) return r;
+  if ((r = upload<FT>(ctx, I->gw, g.grp_w))) return r;
+  if ((r = upload<FT>(ctx, I->ecov, g.ecov))) return r;
+  if ((r = upload<FT>(ctx, I->econ, g.econ))) return r;
+  if ((r = alloc(ctx, I->status, 16))) return r;
+  const int Nh = g.Nh, Nv = g.Nv, Nf = Nv + 1;
+  I->NC = (size_t)Nh * 4 * NN * Nv;
+  I->NF = (size_t)Nh * NN * Nf;
+  I->NR = (size_t)Nh * 2 * NN * Nv;
+  if ((r = alloc(ctx, I->lap, I->NC * sizeof(FT)))) return r;
+  if ((r = alloc(ctx, I->U, (I->NC + I->NF) * sizeof(FT)))) return r;
+  for (int s = 0; s < 4; ++s)
+    if ((r = alloc(ctx, I->Te[s], (I->NC + I->NF) * sizeof(FT)))) return r;
+  for (int s = 1; s < 4; ++s)
+    if ((r = alloc(ctx, I->Ti[s], (I->NR + I->NF) * sizeof(FT)))) return r;
+  if ((r = alloc(ctx, I->rnorm, (size_t)Nh * NN * 3 * sizeof(double)))) return r;
+  I->nsum_blocks = 152 * 4;
+  if ((r = alloc(ctx, I->partials, (size_t)I->nsum_blocks * 4 * sizeof(double)))) return r;
+  if ((r = alloc(ctx, I->sums, 4 * sizeof(double)))) return r;
+  if ((r = alloc(ctx, I->rsum, 4 * sizeof(double)))) return r;
+  DevParams<FT> &P = I->P;
+  P.Nh = Nh; P.Nv = Nv; P.Nf = Nf; P.ngroups = (int)g.grp_off.size() - 1;
+  P.grav = (FT)c.grav; P.Rd = (FT)c.R_d; P.cpd = (FT)c.cp_d; P.cvd = (FT)c.cv_d; P.T0 = (FT)c.T_0;
+  P.pref = (FT)c.p_ref; P.kappa = (FT)c.R_d / (FT)c.cp_d; P.Tmin_ref = (FT)c.T_min_ref;
+  P.Tsfc_ref = (FT)c.T_surf_ref; P.Tmin_sgs = (FT)c.T_min_sgs;
+  P.nu_v = (FT)c.nu_v; P.nu_s = (FT)c.nu_s; P.div_damp = (FT)c.div_damp; P.dt_model = (FT)c.dt;
+  P.upwinding = c.upwinding;
+  for (int n = 0; n < NN; ++n) P.W[n] = (FT)g.W[n];
+  for (int i = 0; i < NQ; ++i)
+    for (int k = 0; k < NQ; ++k) P.D[i * NQ + k] = (FT)g.D[i][k];
+  P.hgeo = (const FT *)I->hgeo.p; P.levc = (const FT *)I->levc.p; P.levf = (const FT *)I->levf.p;
+  P.goff = (const int *)I->goff.p; P.gcopy = (const int *)I->gcopy.p; P.gw = (const FT *)I->gw.p;
+  P.ecov = (const FT *)I->ecov.p; P.econ = (const FT *)I->econ.p;
+  P.status = (int *)I->status.p;
+  ars343(I->ae, I->ai, I->be, I->bi);
+  int dev = 0, optin = 0;
+  CK(cudaGetDevice(&dev));
+  CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  if (passB_smem<FT>(Nv) > (size_t)optin)
+    return fail(ctx, GB_ERR_ARG, "z_elem too large for the element-slab kernels at this precision (shared memory)");
+  configure_se<FT>(Nv);
+  CK(cudaGetLastError());
+  return GB_OK;
+}
+
+template <class FT>
+Impl<FT> *impl(gb_ctx *ctx) { return static_cast<Impl<FT> *>(ctx->impl); }
+
+int check_launch(gb_ctx *ctx) {
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return fail(ctx, GB_ERR_CUDA, std::string("kernel launch: ") + cudaGetErrorString(e));
+  return GB_OK;
+}
+
+template <class FT>
+int remaining_tendency_t(gb_ctx *ctx, gb_fieldvec Yt, gb_fieldvec Y) {
+  Impl<FT> *I = impl<FT>(ctx);
+  launch_passA<FT>(I->P, (const FT *)Y.c, (const FT *)Y.f, (FT *)I->lap.p, ctx->stream);
+  launch_dss<FT>(I->P, (FT *)I->lap.p, nullptr, ctx->stream);
+  launch_passB<FT>(I->P, (const FT *)Y.c, (const FT *)Y.f, (const FT *)I->lap.p, (FT *)Yt.c, (FT *)Yt.f, ctx->stream);
+  return check_launch(ctx);
+}
+
+template <class FT>
+int column_hook_t(gb_ctx *ctx, int mode, gb_fieldvec O, gb_fieldvec Y, double dtg) {
+  Impl<FT> *I = impl<FT>(ctx);
+  if (mode == COL_JACOBIAN && !I->jac.p) {
+    int r = alloc(ctx, I->jac, (size_t)I->P.Nh * NN * JAC_Q * I->P.Nf * sizeof(FT));
+    if (r) return r;
+  }
+  if (mode == COL_LDIV && !I->jac_valid) return fail(ctx, GB_ERR_STATE, "gb_ldiv called before gb_update_jacobian");
+  ColArgs<FT> A{};
+  A.Y_c = (const FT *)Y.c; A.Y_f = (const FT *)Y.f;
+  A.O_c = (FT *)O.c; A.O_f = (FT *)O.f;
+  A.jac = (FT *)I->jac.p;
+  A.dtg = (FT)dtg;
+  launch_column<FT>(I->P, mode, A, ctx->stream);
+  if (mode == COL_JACOBIAN) I->jac_valid = true;
+  return check_launch(ctx);
+}
+
+// One fused ARS343 step (stage loop of ClimaTimeSteppers' IMEX ARK with one
+// Newton iteration per implicit stage); T_exp_j is DSSed once right after it
+// is computed, so every stage state assembled from u_n (continuous), DSSed
+// explicit tendencies and column-local implicit tendencies is continuous.
+template <class FT>
+void enqueue_step(gb_ctx *ctx, FT *Yc, FT *Yf, double dt_) {
+  Impl<FT> *I = impl<FT>(ctx);
+  const DevParams<FT> &P = I->P;
+  cudaStream_t s = ctx->stream;
+  const FT dt = (FT)dt_;
+  FT *lap = (FT *)I->lap.p;
+  auto tec = [&](int j) { return (FT *)I->Te[j].p; };
+  auto tef = [&](int j) { return (FT *)I->Te[j].p + I->NC; };
+  auto tic = [&](int j) { return (FT *)I->Ti[j].p; };
+  auto tif = [&](int j) { return (FT *)I->Ti[j].p + I->NR; };
+  FT *Uc = (FT *)I->U.p, *Uf = Uc + I->NC;
+  // stage 1: U_1 = u_n
+  launch_passA<FT>(P, Yc, Yf, lap, s);
+  launch_dss<FT>(P, lap, nullptr, s);
+  launch_passB<FT>(P, Yc, Yf, lap, tec(0), tef(0), s);
+  launch_dss<FT>(P, tec(0), tef(0), s);
+  for (int i = 1; i < 4; ++i) {
+    StageArgs<FT> A{};
+    A.un_c = Yc; A.un_f = Yf;
+    A.nsrc = i;
+    for (int j = 0; j < i; ++j) {
+      A.te_c[j] = I->ae[i][j] != 0 ? tec(j) : nullptr;
+      A.te_f[j] = I->ae[i][j] != 0 ? tef(j) : nullptr;
+      A.ce[j] = dt * (FT)I->ae[i][j];
+      A.ti_c[j] = I->ai[i][j] != 0 ? tic(j) : nullptr;
+      A.ti_f[j] = I->ai[i][j] != 0 ? tif(j) : nullptr;
+      A.ci[j] = dt * (FT)I->ai[i][j];
+    }
+    A.U_c = Uc; A.U_f = Uf;
+    A.Ti_c = tic(i); A.Ti_f = tif(i);
+    A.dtg = dt * (FT)I->ai[i][i];
+    A.rnorm = (double *)I->rnorm.p;
+    A.first = i == 1;
+    launch_column_stage<FT>(P, A, s);
+    launch_passA<FT>(P, Uc, Uf, lap, s);
+    launch_dss<FT>(P, lap, nullptr, s);
+    launch_passB<FT>(P, Uc, Uf, lap, tec(i), tef(i), s);
+    launch_dss<FT>(P, tec(i), tef(i), s);
+  }
+  StageArgs<FT> A{};
+  A.nsrc = 4;
+  for (int j = 0; j < 4; ++j) {
+    A.te_c[j] = I->be[j] != 0 ? tec(j) : nullptr;
+    A.te_f[j] = I->be[j] != 0 ? tef(j) : nullptr;
+    A.ce[j] = dt * (FT)I->be[j];
+    A.ti_c[j] = I->bi[j] != 0 ? tic(j) : nullptr;
+    A.ti_f[j] = I->bi[j] != 0 ? tif(j) : nullptr;
+    A.ci[j] = dt * (FT)I->bi[j];
+  }
+  launch_final<FT>(P, A, Yc, Yf, s);
+}
+
+template <class FT>
+int step_t(gb_ctx *ctx, gb_fieldvec Y, double dt, int nsteps, int use_graph) {
+  Impl<FT> *I = impl<FT>(ctx);
+  FT *Yc = (FT *)Y.c, *Yf = (FT *)Y.f;
+  if (!use_graph) {
+    for (int s = 0; s < nsteps; ++s) enqueue_step<FT>(ctx, Yc, Yf, dt);
+    return check_launch(ctx);
+  }
+  if (!I->gexec || I->g_c != Y.c || I->g_f != Y.f || I->g_dt != dt) {
+    if (I->gexec) { cudaGraphExecDestroy(I->gexec); I->gexec = nullptr; }
+    cudaGraph_t graph;
+    CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+    enqueue_step<FT>(ctx, Yc, Yf, dt);
+    cudaError_t le = cudaGetLastError();
+    cudaError_t ce = cudaStreamEndCapture(ctx->stream, &graph);
+    if (le != cudaSuccess) return fail(ctx, GB_ERR_CUDA, std::string("capture launch: ") + cudaGetErrorString(le));
+    if (ce != cudaSuccess) return fail(ctx, GB_ERR_CUDA, std::string("cudaStreamEndCapture: ") + cudaGetErrorString(ce));
+    cudaError_t ie = cudaGraphInstantiate(&I->gexec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (ie != cudaSuccess) { I->gexec = nullptr; return fail(ctx, GB_ERR_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(ie)); }
+    I->g_c = Y.c; I->g_f = Y.f; I->g_dt = dt;
+  }
+  for (int s = 0; s < nsteps; ++s) CK(cudaGraphLaunch(I->gexec, ctx->stream));
+  return GB_OK;
+}
+
+template <class FT>
+int read_status(gb_ctx *ctx) {
+  Impl<FT> *I = impl<FT>(ctx);
+  int st = 0;
+  CK(cudaMemcpyAsync(&st, I->status.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  if (st & ST_TIMEOUT) return fail(ctx, GB_ERR_TIMEOUT, "a bounded device wait timed out");
+  if (st & ST_NONFINITE) return fail(ctx, GB_ERR_NONFINITE, "non-finite Newton residual");
+  return GB_OK;
+}
+
+template <class FT>
+int global_sums_t(gb_ctx *ctx, gb_fieldvec Y, double *out) {
+  Impl<FT> *I = impl<FT>(ctx);
+  launch_global_sums<FT>(I->P, (const FT *)Y.c, (double *)I->partials.p, I->nsum_blocks, (double *)I->sums.p, ctx->stream);
+  int r = check_launch(ctx);
+  if (r) return r;
+  CK(cudaMemcpyAsync(out, I->sums.p, 2 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return GB_OK;
+}
+
+template <class FT>
+int residual_t(gb_ctx *ctx, double *out) {
+  Impl<FT> *I = impl<FT>(ctx);
+  launch_reduce_rnorm((const double *)I->rnorm.p, I->P.Nh * NN, (double *)I->rsum.p, ctx->stream);
+  int r = check_launch(ctx);
+  if (r) return r;
+  CK(cudaMemcpyAsync(out, I->rsum.p, 3 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return read_status<FT>(ctx);
+}
+
+template <class FT>
+int time_kernel_t(gb_ctx *ctx, int kernel, gb_fieldvec Y, int reps, double *ms) {
+  Impl<FT> *I = impl<FT>(ctx);
+  const DevParams<FT> &P = I->P;
+  cudaStream_t s = ctx->stream;
+  FT *Yc = (FT *)Y.c, *Yf = (FT *)Y.f;
+  FT *lap = (FT *)I->lap.p;
+  FT *Tc = (FT *)I->Te[0].p, *Tf = Tc + I->NC;
+  StageArgs<FT> A{};
+  const FT dt = (FT)ctx->cfg.dt;
+  if (kernel == GB_K_COLUMN || kernel == GB_K_FINAL) {
+    const int i = kernel == GB_K_COLUMN ? 3 : 4;
+    A.un_c = Yc; A.un_f = Yf; A.nsrc = i;
+    for (int j = 0; j < i; ++j) {
+      const double e = i < 4 ? I->ae[i][j] : I->be[j], m = i < 4 ? I->ai[i][j] : I->bi[j];
+      A.te_c[j] = e != 0 ? (FT *)I->Te[j].p : nullptr;
+      A.te_f[j] = e != 0 ? (FT *)I->Te[j].p + I->NC : nullptr;
+      A.ce[j] = dt * (FT)e;
+      A.ti_c[j] = m != 0 ? (FT *)I->Ti[j].p : nullptr;
+      A.ti_f[j] = m != 0 ? (FT *)I->Ti[j].p + I->NR : nullptr;
+      A.ci[j] = dt * (FT)m;
+    }
+    A.U_c = (FT *)I->U.p; A.U_f = (FT *)I->U.p + I->NC;
+    A.Ti_c = (FT *)I->Ti[3].p; A.Ti_f = (FT *)I->Ti[3].p + I->NR;
+    A.dtg = dt * (FT)I->ai[3][3];
+    A.rnorm = (double *)I->rnorm.p;
+    A.first = 1;
+  }
+  auto launch = [&]() {
+    switch (kernel) {
+      case GB_K_PASSA: launch_passA<FT>(P, Yc, Yf, lap, s); break;
+      case GB_K_PASSB: launch_passB<FT>(P, Yc, Yf, lap, Tc, Tf, s); break;
+      case GB_K_COLUMN: launch_column_stage<FT>(P, A, s); break;
+      case GB_K_DSS: launch_dss<FT>(P, Yc, Yf, s); break;
+      default: launch_final<FT>(P, A, (FT *)I->U.p, (FT *)I->U.p + I->NC, s); break;
+    }
+  };
+  launch();  // warm-up
+  cudaEvent_t a, b;
+  CK(cudaEventCreate(&a));
+  CK(cudaEventCreate(&b));
+  CK(cudaEventRecord(a, s));
+  for (int r = 0; r < reps; ++r) launch();
+  CK(cudaEventRecord(b, s));
+  int rc = check_launch(ctx);
+  CK(cudaEventSynchronize(b));
+  float t = 0;
+  CK(cudaEventElapsedTime(&t, a, b));
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  *ms = reps > 0 ? t / reps : 0.0;
+  return rc;
+}
+
+bool aligned(const void *p) { return ((uintptr_t)p & 15) == 0; }
+bool fv_ok(gb_fieldvec v) { return v.c && v.f && aligned(v.c) && aligned(v.f); }
+
+#define DISPATCH(ctx, fn, ...) ((ctx)->cfg.ft_bytes == 8 ? fn<double>(__VA_ARGS__) : fn<float>(__VA_ARGS__))
+
+#define GUARD(ctx)                                           \
+  do {                                                       \
+    if (!(ctx)) return GB_ERR_ARG;                           \
+  } while (0)
+
+}  // namespace
+
+extern "C" {
+
+int gb_sizes(const gb_config *cfg, size_t *n_center, size_t *n_face, int *n_groups, int *n_copies) {
+  if (!cfg) return GB_ERR_ARG;
+  const char *why = nullptr;
+  if (!validate_config(*cfg, &why)) return GB_ERR_ARG;
+  const size_t Nh = 6 * (size_t)cfg->h_elem * cfg->h_elem;
+  if (n_center) *n_center = Nh * 4 * NN * cfg->z_elem;
+  if (n_face) *n_face = Nh * NN * (cfg->z_elem + 1);
+  if (n_groups || n_copies) {
+    HostGeometry g;
+    build_geometry(*cfg, g);
+    if (n_groups) *n_groups = (int)g.grp_off.size() - 1;
+    if (n_copies) *n_copies = (int)g.grp_copy.size();
+  }
+  return GB_OK;
+}
+
+int gb_geometry_export(const gb_config *cfg, gb_geometry_host *out) {
+  if (!cfg || !out) return GB_ERR_ARG;
+  const char *why = nullptr;
+  if (!validate_config(*cfg, &why)) return GB_ERR_ARG;
+  try {
+    HostGeometry g;
+    build_geometry(*cfg, g);
+    auto cp = [](double *dst, const std::vector<double> &v) { if (dst) std::memcpy(dst, v.data(), v.size() * sizeof(double)); };
+    cp(out->xyz, g.xyz); cp(out->ecov, g.ecov); cp(out->Jh, g.Jh); cp(out->gup, g.gup); cp(out->fh0, g.fh0); cp(out->zf, g.zf);
+    if (out->dss_off) std::memcpy(out->dss_off, g.grp_off.data(), g.grp_off.size() * sizeof(int));
+    if (out->dss_copy) std::memcpy(out->dss_copy, g.grp_copy.data(), g.grp_copy.size() * sizeof(int));
+  } catch (...) {
+    return GB_ERR_NOMEM;
+  }
+  return GB_OK;
+}
+
+int gb_ctx_create(const gb_config *cfg, gb_ctx **out) {
+  if (!cfg || !out) return GB_ERR_ARG;
+  *out = nullptr;
+  const char *why = nullptr;
+  if (!validate_config(*cfg, &why)) return GB_ERR_ARG;
+  gb_ctx *ctx = new (std::nothrow) gb_ctx();
+  if (!ctx) return GB_ERR_NOMEM;
+  ctx->cfg = *cfg;
+  int r;
+  try {
+    build_geometry(*cfg, ctx->geo);
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) { delete ctx; return GB_ERR_CUDA; }
+    r = cfg->ft_bytes == 8 ? create_impl<double>(ctx) : create_impl<float>(ctx);
+  } catch (...) {
+    r = GB_ERR_NOMEM;
+  }
+  if (r) { delete ctx; return r; }
+  *out = ctx;
+  return GB_OK;
+}
+
+int gb_ctx_destroy(gb_ctx *ctx) {
+  if (!ctx) return GB_ERR_ARG;
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  else cudaDeviceSynchronize();
+  delete ctx;
+  return GB_OK;
+}
+
+int gb_set_stream(gb_ctx *ctx, void *stream) {
+  GUARD(ctx);
+  ctx->stream = (cudaStream_t)stream;
+  return GB_OK;
+}
+
+int gb_last_error(gb_ctx *ctx, char *buf, size_t len) {
+  GUARD(ctx);
+  if (buf && len) {
+    std::strncpy(buf, ctx->err.c_str(), len - 1);
+    buf[len - 1] = 0;
+  }
+  return ctx->last;
+}
+
+int gb_set_precomputed_quantities(gb_ctx *ctx, gb_fieldvec Y, double t) {
+  GUARD(ctx);
+  (void)t;
+  if (!fv_ok(Y)) return fail(ctx, GB_ERR_ARG, "Y: null or misaligned pointer");
+  if (ctx->cfg.ft_bytes == 8) launch_bc_filter<double>(impl<double>(ctx)->P, (double *)Y.f, ctx->stream);
+  else launch_bc_filter<float>(impl<float>(ctx)->P, (float *)Y.f, ctx->stream);
+  return check_launch(ctx);
+}
+
+int gb_remaining_tendency(gb_ctx *ctx, gb_fieldvec Yt, gb_fieldvec Y, double t) {
+  GUARD(ctx);
+  (void)t;
+  if (!fv_ok(Y) || !fv_ok(Yt)) return fail(ctx, GB_ERR_ARG, "null or misaligned pointer");
+  return DISPATCH(ctx, remaining_tendency_t, ctx, Yt, Y);
+}
+
+int gb_implicit_tendency(gb_ctx *ctx, gb_fieldvec Yt, gb_fieldvec Y, double t) {
+  GUARD(ctx);
+  (void)t;
+  if (!fv_ok(Y) || !fv_ok(Yt)) return fail(ctx, GB_ERR_ARG, "null or misaligned pointer");
+  return DISPATCH(ctx, column_hook_t, ctx, (int)COL_IMPLICIT, Yt, Y, 0.0);
+}
+
+int gb_update_jacobian(gb_ctx *ctx, gb_fieldvec Y, double dtgamma, double t) {
+  GUARD(ctx);
+  (void)t;
+  if (!fv_ok(Y)) return fail(ctx, GB_ERR_ARG, "null or misaligned pointer");
+  gb_fieldvec none{nullptr, nullptr};
+  return DISPATCH(ctx, column_hook_t, ctx, (int)COL_JACOBIAN, none, Y, dtgamma);
+}
+
+int gb_ldiv(gb_ctx *ctx, gb_fieldvec dY, gb_fieldvec R) {
+  GUARD(ctx);
+  if (!fv_ok(dY) || !fv_ok(R)) return fail(ctx, GB_ERR_ARG, "null or misaligned pointer");
+  return DISPATCH(ctx, column_hook_t, ctx, (int)COL_LDIV, dY, R, 0.0);
+}
+
+int gb_correct_implicit_advection_tendency(gb_ctx *ctx, gb_fieldvec Yt, gb_fieldvec Y, double t) {
+  GUARD(ctx);
+  (void)t;
+  if (!fv_ok(Y) || !fv_ok(Yt)) return fail(ctx, GB_ERR_ARG, "null or misaligned pointer");
+  return DISPATCH(ctx, column_hook_t, ctx, (int)COL_POSTIMP, Yt, Y, 0.0);
+}
+
+int gb_dss(gb_ctx *ctx, gb_fieldvec Y) {
+  GUARD(ctx);
+  if (!fv_ok(Y)) return fail(ctx, GB_ERR_ARG, "null or misaligned pointer");
+  if (ctx->cfg.ft_bytes == 8) launch_dss<double>(impl<double>(ctx)->P, (double *)Y.c, (double *)Y.f, ctx->stream);
+  else launch_dss<float>(impl<float>(ctx)->P, (float *)Y.c, (float *)Y.f, ctx->stream);
+  return check_launch(ctx);
+}
+
+int gb_step(gb_ctx *ctx, gb_fieldvec Y, double t, double dt, int nsteps, int use_graph) {
+  GUARD(ctx);
+  (void)t;
+  if (!fv_ok(Y)) return fail(ctx, GB_ERR_ARG, "null or misaligned pointer");
+  if (nsteps < 0 || !(dt > 0)) return fail(ctx, GB_ERR_ARG, "nsteps must be >= 0 and dt > 0");
+  if (dt != ctx->cfg.dt)
+    return fail(ctx, GB_ERR_ARG, "dt differs from gb_config.dt (the van Leer Courant factor uses the model time step)");
+  return DISPATCH(ctx, step_t, ctx, Y, dt, nsteps, use_graph);
+}
+
+int gb_global_sums(gb_ctx *ctx, gb_fieldvec Y, double out[2]) {
+  GUARD(ctx);
+  if (!fv_ok(Y) || !out) return fail(ctx, GB_ERR_ARG, "null or misaligned pointer");
+  return DISPATCH(ctx, global_sums_t, ctx, Y, out);
+}
+
+int gb_newton_residual(gb_ctx *ctx, double out[3]) {
+  GUARD(ctx);
+  if (!out) return fail(ctx, GB_ERR_ARG, "null pointer");
+  return DISPATCH(ctx, residual_t, ctx, out);
+}
+
+int gb_time_kernel(gb_ctx *ctx, int kernel, gb_fieldvec Y, int reps, double *ms) {
+  GUARD(ctx);
+  if (!fv_ok(Y) || !ms || reps < 0 || kernel < 0 || kernel > 4) return fail(ctx, GB_ERR_ARG, "bad gb_time_kernel arguments");
+  return DISPATCH(ctx, time_kernel_t, ctx, kernel, Y, reps, ms);
+}
+
+}  // extern "C"

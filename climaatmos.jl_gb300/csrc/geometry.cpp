@@ -1,0 +1,250 @@
+// Host-side grid generation (FP64): equiangular cubed sphere with Nq = 4 GLL
+// nodes, deep-atmosphere metric terms, vertical mesh, and the DSS plan.
+//
+// Restates what SphereGrid (src/simulation/grids.jl:42-89) obtains from
+// ClimaCore: EquiangularCubedSphere, nh_poly = 3, DeepSphericalGlobalGeometry
+// (horizontal metric scaled by (R + z) / R), and the tanh stretching of
+// get_stretching (grids.jl:356).  The DSS plan lists, for every set of
+// collocated element nodes, its copies in ascending element*16 + node order
+// with J-weights; collocated nodes are found exactly on the integer node
+// lattice of the cube (each coordinate in 0..3*h_elem).
+#include "geometry.h"
+
+#include <algorithm>
+#include <cmath>
+#include <numeric>
+
+namespace gb {
+
+namespace {
+// Panel frames (normal, t1, t2) with t1 x t2 = normal.
+const int PANEL[6][3][3] = {
+    {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}},  {{0, 1, 0}, {-1, 0, 0}, {0, 0, 1}},
+    {{-1, 0, 0}, {0, -1, 0}, {0, 0, 1}}, {{0, -1, 0}, {1, 0, 0}, {0, 0, 1}},
+    {{0, 0, 1}, {0, 1, 0}, {-1, 0, 0}}, {{0, 0, -1}, {0, 1, 0}, {1, 0, 0}},
+};
+
+void gll4(double *x, double *w, double D[NQ][NQ]) {
+  const double s = 1.0 / std::sqrt(5.0);
+  const double xs[NQ] = {-1.0, -s, s, 1.0};
+  const double ws[NQ] = {1.0 / 6.0, 5.0 / 6.0, 5.0 / 6.0, 1.0 / 6.0};
+  double lam[NQ];
+  for (int j = 0; j < NQ; ++j) {
+    double p = 1.0;
+    for (int m = 0; m < NQ; ++m)
+      if (m != j) p *= xs[j] - xs[m];
+    lam[j] = 1.0 / p;
+  }
+  for (int i = 0; i < NQ; ++i) {
+    x[i] = xs[i];
+    w[i] = ws[i];
+    double diag = 0;
+    for (int k = 0; k < NQ; ++k) {
+      if (k == i) continue;
+      D[i][k] = (lam[k] / lam[i]) / (xs[i] - xs[k]);
+      diag -= D[i][k];
+    }
+    D[i][i] = diag;
+  }
+}
+
+std::vector<double> faces(const gb_config &c) {
+  const int N = c.z_elem;
+  std::vector<double> zf(N + 1);
+  if (!c.z_stretch) {
+    for (int k = 0; k <= N; ++k) zf[k] = c.z_max * k / N;
+    return zf;
+  }
+  // z(zeta) = z_max (1 + tanh(gamma (zeta - 1)) / tanh(gamma)); gamma from z(1/N) = dz_bottom
+  const double target = c.dz_bottom / c.z_max;
+  auto first = [&](double g) { return 1.0 + std::tanh(g * (1.0 / N - 1.0)) / std::tanh(g); };
+  double lo = 1e-8, hi = 50.0;
+  for (int it = 0; it < 200; ++it) {
+    double mid = 0.5 * (lo + hi);
+    if (first(mid) > target) lo = mid; else hi = mid;
+  }
+  const double g = 0.5 * (lo + hi);
+  for (int k = 0; k <= N; ++k) zf[k] = c.z_max * (1.0 + std::tanh(g * ((double)k / N - 1.0)) / std::tanh(g));
+  zf[0] = 0.0;
+  zf[N] = c.z_max;
+  return zf;
+}
+
+double beta_sponge(double z, double zd, double zmax, double alpha) {
+  if (!(z > zd) || alpha == 0.0) return 0.0;
+  double s = std::sin(M_PI * (z - zd) / (zmax - zd) / 2.0);
+  return alpha * s * s;
+}
+}  // namespace
+
+bool validate_config(const gb_config &c, const char **why) {
+  if (c.h_elem < 1 || c.h_elem > 512) { *why = "h_elem must be in [1, 512]"; return false; }
+  if (c.z_elem < 2 || c.z_elem > 127) { *why = "z_elem must be in [2, 127]"; return false; }
+  if (c.ft_bytes != 4 && c.ft_bytes != 8) { *why = "ft_bytes must be 4 or 8"; return false; }
+  if (!(c.z_max > 0) || (c.z_stretch && !(c.dz_bottom > 0 && c.dz_bottom < c.z_max / c.z_elem))) {
+    *why = "invalid vertical mesh (z_max, dz_bottom)";
+    return false;
+  }
+  if (!(c.radius > 0) || !(c.R_d > 0) || !(c.cp_d > c.R_d) || !(c.cv_d > 0) || !(c.p_ref > 0)) {
+    *why = "invalid physical constants";
+    return false;
+  }
+  if (c.upwinding != 0 && c.upwinding != 1) { *why = "upwinding must be 0 or 1"; return false; }
+  return true;
+}
+
+void build_geometry(const gb_config &c, HostGeometry &g) {
+  const int h = c.h_elem, Nh = 6 * h * h, Nv = c.z_elem, Nf = Nv + 1;
+  const double R = c.radius;
+  g.h = h; g.Nh = Nh; g.Nv = Nv; g.R = R;
+  gll4(g.xg, g.wg, g.D);
+  for (int n = 0; n < NN; ++n) g.W[n] = g.wg[n % NQ] * g.wg[n / NQ];
+  const size_t H = (size_t)Nh * NN;
+  g.xyz.assign(H * 3, 0); g.ecov.assign(H * 6, 0); g.econ.assign(H * 6, 0);
+  g.Jh.assign(H, 0); g.gup.assign(H * 3, 0); g.gdn.assign(H * 3, 0);
+  g.sinlat.assign(H, 0); g.fh0.assign(H * 2, 0);
+  const double dal = (M_PI / 2.0) / h;
+  std::vector<long long> key(H);
+  const int M = 3 * h;
+  for (int p = 0; p < 6; ++p)
+    for (int ey = 0; ey < h; ++ey)
+      for (int ex = 0; ex < h; ++ex) {
+        const int e = (p * h + ey) * h + ex;
+        for (int j = 0; j < NQ; ++j)
+          for (int i = 0; i < NQ; ++i) {
+            const int n = i + NQ * j;
+            const size_t q = (size_t)e * NN + n;
+            const double al = -M_PI / 4 + (ex + (g.xg[i] + 1) / 2) * dal;
+            const double be = -M_PI / 4 + (ey + (g.xg[j] + 1) / 2) * dal;
+            const double ta = std::tan(al), tb = std::tan(be);
+            double P[3], t1[3], t2[3];
+            for (int d = 0; d < 3; ++d) {
+              t1[d] = PANEL[p][1][d];
+              t2[d] = PANEL[p][2][d];
+              P[d] = PANEL[p][0][d] + ta * t1[d] + tb * t2[d];
+            }
+            const double r2 = P[0] * P[0] + P[1] * P[1] + P[2] * P[2], rn = std::sqrt(r2);
+            for (int d = 0; d < 3; ++d) g.xyz[q * 3 + d] = P[d] / rn;
+            // e_k = R (dal/2) d(P/|P|)/dalpha_k with dP/dalpha = sec^2 * t
+            for (int k = 0; k < 2; ++k) {
+              const double *tv = k == 0 ? t1 : t2;
+              const double tt = k == 0 ? ta : tb;
+              double dP[3], pd = 0;
+              for (int d = 0; d < 3; ++d) { dP[d] = (1.0 + tt * tt) * tv[d]; pd += P[d] * dP[d]; }
+              for (int d = 0; d < 3; ++d)
+                g.ecov[q * 6 + k * 3 + d] = R * (dal / 2.0) * (dP[d] / rn - P[d] * pd / (rn * r2));
+            }
+            const double *e1 = &g.ecov[q * 6], *e2 = &g.ecov[q * 6 + 3];
+            const double g11 = e1[0] * e1[0] + e1[1] * e1[1] + e1[2] * e1[2];
+            const double g12 = e1[0] * e2[0] + e1[1] * e2[1] + e1[2] * e2[2];
+            const double g22 = e2[0] * e2[0] + e2[1] * e2[1] + e2[2] * e2[2];
+            const double det = g11 * g22 - g12 * g12;
+            g.Jh[q] = std::sqrt(det);
+            g.gdn[q * 3 + 0] = g11; g.gdn[q * 3 + 1] = g12; g.gdn[q * 3 + 2] = g22;
+            const double u11 = g22 / det, u12 = -g12 / det, u22 = g11 / det;
+            g.gup[q * 3 + 0] = u11; g.gup[q * 3 + 1] = u12; g.gup[q * 3 + 2] = u22;
+            for (int d = 0; d < 3; ++d) {
+              g.econ[q * 6 + d] = u11 * e1[d] + u12 * e2[d];
+              g.econ[q * 6 + 3 + d] = u12 * e1[d] + u22 * e2[d];
+            }
+            const double X = g.xyz[q * 3], Y = g.xyz[q * 3 + 1], Z = g.xyz[q * 3 + 2];
+            g.sinlat[q] = Z;
+            const double coslat = std::sqrt(std::max(X * X + Y * Y, 0.0));
+            const double lon = std::atan2(Y, X);
+            const double north[3] = {-Z * std::cos(lon), -Z * std::sin(lon), coslat};
+            // covariant components of 2 Omega cos(lat) north, raised with g^ij
+            double fc[2];
+            for (int k = 0; k < 2; ++k) {
+              const double *ek = &g.ecov[q * 6 + k * 3];
+              fc[k] = 2.0 * c.omega * coslat * (ek[0] * north[0] + ek[1] * north[1] + ek[2] * north[2]);
+            }
+            g.fh0[q * 2 + 0] = u11 * fc[0] + u12 * fc[1];
+            g.fh0[q * 2 + 1] = u12 * fc[0] + u22 * fc[1];
+            // integer lattice point of this node on the cube [0, M]^3
+            const int a = 3 * ex + i, b = 3 * ey + j;
+            int L[3];
+            for (int d = 0; d < 3; ++d) {
+              if (PANEL[p][0][d]) L[d] = PANEL[p][0][d] > 0 ? M : 0;
+              else if (PANEL[p][1][d]) L[d] = PANEL[p][1][d] > 0 ? a : M - a;
+              else L[d] = PANEL[p][2][d] > 0 ? b : M - b;
+            }
+            key[q] = ((long long)L[0] * (M + 1) + L[1]) * (M + 1) + L[2];
+          }
+      }
+  // DSS groups: copies sharing a lattice point, ordered by first copy
+  std::vector<int> order(H);
+  std::iota(order.begin(), order.end(), 0);
+  std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return key[x] < key[y]; });
+  std::vector<std::vector<int>> groups;
+  for (size_t s = 0; s < H;) {
+    size_t t = s;
+    while (t < H && key[order[t]] == key[order[s]]) ++t;
+    if (t - s > 1) {
+      std::vector<int> gset(order.begin() + s, order.begin() + t);
+      std::sort(gset.begin(), gset.end());
+      groups.push_back(gset);
+    }
+    s = t;
+  }
+  std::sort(groups.begin(), groups.end(), [](const std::vector<int> &x, const std::vector<int> &y) { return x[0] < y[0]; });
+  g.grp_off.assign(1, 0);
+  g.grp_copy.clear();
+  g.grp_w.clear();
+  for (auto &gs : groups) {
+    double s = 0;
+    for (int idx : gs) s += g.Jh[idx];
+    for (int idx : gs) {
+      g.grp_copy.push_back(idx);
+      g.grp_w.push_back(g.Jh[idx] / s);
+    }
+    g.grp_off.push_back((int)g.grp_copy.size());
+  }
+  // vertical mesh
+  g.zf = faces(c);
+  g.zc.resize(Nv); g.dzc.resize(Nv); g.rc.resize(Nv); g.dzf.resize(Nf); g.rf.resize(Nf);
+  for (int v = 0; v < Nv; ++v) {
+    g.zc[v] = (g.zf[v] + g.zf[v + 1]) / 2;
+    g.dzc[v] = g.zf[v + 1] - g.zf[v];
+    g.rc[v] = (R + g.zc[v]) / R;
+  }
+  for (int k = 0; k < Nf; ++k) {
+    if (k == 0) g.dzf[k] = g.dzc[0];
+    else if (k == Nv) g.dzf[k] = g.dzc[Nv - 1];
+    else g.dzf[k] = g.zc[k] - g.zc[k - 1];
+    g.rf[k] = (R + g.zf[k]) / R;
+  }
+  // kernel-side arrays
+  g.hgeo.assign((size_t)Nh * HG_N * NN, 0);
+  for (int e = 0; e < Nh; ++e)
+    for (int n = 0; n < NN; ++n) {
+      const size_t q = (size_t)e * NN + n;
+      double *o = &g.hgeo[(size_t)e * HG_N * NN];
+      o[HG_JH * NN + n] = g.Jh[q];
+      for (int k = 0; k < 3; ++k) {
+        o[(HG_GU0 + k) * NN + n] = g.gup[q * 3 + k];
+        o[(HG_GD0 + k) * NN + n] = g.gdn[q * 3 + k];
+      }
+      o[HG_F3 * NN + n] = 2.0 * c.omega * g.sinlat[q];
+      o[HG_FH1 * NN + n] = g.fh0[q * 2];
+      o[HG_FH2 * NN + n] = g.fh0[q * 2 + 1];
+    }
+  g.levc.assign((size_t)LC_N * Nv, 0);
+  for (int v = 0; v < Nv; ++v) {
+    g.levc[LC_Z * Nv + v] = g.zc[v];
+    g.levc[LC_R2 * Nv + v] = g.rc[v] * g.rc[v];
+    g.levc[LC_DZ * Nv + v] = g.dzc[v];
+    g.levc[LC_PHI * Nv + v] = c.grav * g.zc[v];
+    g.levc[LC_BETA * Nv + v] = beta_sponge(g.zc[v], c.sponge_zd, c.z_max, c.alpha_uh);
+  }
+  g.levf.assign((size_t)LF_N * Nf, 0);
+  for (int k = 0; k < Nf; ++k) {
+    g.levf[LF_Z * Nf + k] = g.zf[k];
+    g.levf[LF_R2 * Nf + k] = g.rf[k] * g.rf[k];
+    g.levf[LF_DZ * Nf + k] = g.dzf[k];
+    g.levf[LF_RINV * Nf + k] = 1.0 / g.rf[k];
+    g.levf[LF_BETA * Nf + k] = beta_sponge(g.zf[k], c.sponge_zd, c.z_max, c.alpha_w);
+    g.levf[LF_DPHI * Nf + k] = (k > 0 && k < Nv) ? c.grav * (g.zc[k] - g.zc[k - 1]) : 0.0;
+  }
+}
+
+}  // namespace gb

@@ -1,0 +1,36 @@
+// Host-side (FP64) grid generation for the GB300 dry dynamical core.
+#pragma once
+#include <vector>
+
+#include "gbdycore.h"
+
+namespace gb {
+
+constexpr int NQ = 4;
+constexpr int NN = 16;
+
+// Per-node horizontal geometry quantities stored for the kernels ([elem][q][node]).
+enum HGeo { HG_JH = 0, HG_GU0, HG_GU1, HG_GU2, HG_GD0, HG_GD1, HG_GD2, HG_F3, HG_FH1, HG_FH2, HG_N };
+// Per-level centre quantities ([q][Nv]).
+enum LevC { LC_Z = 0, LC_R2, LC_DZ, LC_PHI, LC_BETA, LC_N };
+// Per-level face quantities ([q][Nv+1]).
+enum LevF { LF_Z = 0, LF_R2, LF_DZ, LF_RINV, LF_BETA, LF_DPHI, LF_N };
+
+struct HostGeometry {
+  int h = 0, Nh = 0, Nv = 0;
+  double R = 0;
+  double xg[NQ], wg[NQ], W[NN], D[NQ][NQ];
+  std::vector<double> xyz, ecov, econ, Jh, gup, gdn, sinlat, fh0;
+  std::vector<double> zf, zc, dzc, dzf, rc, rf;
+  std::vector<int> grp_off, grp_copy;
+  std::vector<double> grp_w;
+  std::vector<double> hgeo;  // [Nh][HG_N][16]
+  std::vector<double> levc;  // [LC_N][Nv]
+  std::vector<double> levf;  // [LF_N][Nv+1]
+};
+
+// Returns false (with a message) on an invalid configuration.
+bool validate_config(const gb_config &cfg, const char **why);
+void build_geometry(const gb_config &cfg, HostGeometry &g);
+
+}  // namespace gb

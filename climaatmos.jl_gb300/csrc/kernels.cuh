@@ -1,0 +1,90 @@
+// Launch wrappers of the GB300 dry dynamical-core kernels.
+#pragma once
+#include "common.cuh"
+
+namespace gb {
+
+// Shared-memory layouts of the element-slab kernels (byte offsets).
+template <class FT>
+struct PassALayout {
+  size_t y, f, g, u3, kv, out, bar, total;
+  __host__ __device__ PassALayout(int Nv) {
+    const int Nf = Nv + 1;
+    size_t o = 0;
+    y = o; o += align16(sizeof(FT) * 64 * Nv);
+    f = o; o += align16(sizeof(FT) * 16 * Nf);
+    g = o; o += align16(sizeof(FT) * HG_N * 16);
+    u3 = o; o += align16(sizeof(FT) * 16 * Nv);
+    kv = o; o += align16(sizeof(FT) * 16 * Nv);
+    out = o; o += align16(sizeof(FT) * 64 * Nv);
+    bar = o; o += 16;
+    total = o;
+  }
+};
+
+template <class FT>
+struct PassBLayout {
+  size_t y, f, g, lap, u3, kv, c1, c2, k, rj, l4, out, outf, bar, total;
+  __host__ __device__ PassBLayout(int Nv) {
+    const int Nf = Nv + 1;
+    size_t o = 0;
+    y = o; o += align16(sizeof(FT) * 64 * Nv);
+    f = o; o += align16(sizeof(FT) * 16 * Nf);
+    g = o; o += align16(sizeof(FT) * HG_N * 16);
+    lap = o; o += align16(sizeof(FT) * 64 * Nv);  // reused for the face cross products after use
+    u3 = o; o += align16(sizeof(FT) * 16 * Nv);   // reused for the centre cross terms
+    kv = o; o += align16(sizeof(FT) * 16 * Nv);
+    c1 = o; o += align16(sizeof(FT) * 16 * Nv);
+    c2 = o; o += align16(sizeof(FT) * 16 * Nv);
+    k = o; o += align16(sizeof(FT) * 16 * Nv);
+    rj = o; o += align16(sizeof(FT) * 16 * Nv);
+    l4 = o; o += align16(sizeof(FT) * 16 * Nv);
+    out = o; o += align16(sizeof(FT) * 64 * Nv);
+    outf = o; o += align16(sizeof(FT) * 16 * Nf);
+    bar = o; o += 16;
+    total = o;
+  }
+};
+
+// Sources of a stage assembly  U = u_n + sum_j (ce[j] T_exp[j] + ci[j] T_imp[j]).
+template <class FT>
+struct StageArgs {
+  const FT *un_c, *un_f;
+  const FT *te_c[4], *te_f[4];
+  const FT *ti_c[4], *ti_f[4];  // reduced implicit tendencies ([e][2][16][Nv], faces)
+  FT ce[4], ci[4];
+  int nsrc;
+  FT *U_c, *U_f;    // stage state out
+  FT *Ti_c, *Ti_f;  // implicit tendency of this stage out (reduced)
+  FT dtg;
+  double *rnorm;    // [ncols][3] residual sums of squares (accumulated)
+  int first;        // 1: overwrite rnorm, 0: accumulate
+};
+
+enum ColMode { COL_STAGE = 0, COL_IMPLICIT = 1, COL_JACOBIAN = 2, COL_LDIV = 3, COL_POSTIMP = 4 };
+constexpr int JAC_Q = 15;  // stored Jacobian quantities per level
+
+template <class FT>
+struct ColArgs {
+  const FT *Y_c, *Y_f;  // input state (or R for ldiv)
+  FT *O_c, *O_f;        // output (tendency, or dY for ldiv)
+  FT *jac;              // [ncols][JAC_Q][Nf]
+  FT dtg;
+};
+
+template <class FT> void launch_passA(const DevParams<FT> &P, const FT *Yc, const FT *Yf, FT *L, cudaStream_t s);
+template <class FT> void launch_passB(const DevParams<FT> &P, const FT *Yc, const FT *Yf, const FT *L, FT *Tc, FT *Tf, cudaStream_t s);
+template <class FT> void launch_dss(const DevParams<FT> &P, FT *C, FT *F, cudaStream_t s);
+template <class FT> void launch_column_stage(const DevParams<FT> &P, const StageArgs<FT> &A, cudaStream_t s);
+template <class FT> void launch_column(const DevParams<FT> &P, int mode, const ColArgs<FT> &A, cudaStream_t s);
+template <class FT> void launch_final(const DevParams<FT> &P, const StageArgs<FT> &A, FT *Yc, FT *Yf, cudaStream_t s);
+template <class FT> void launch_bc_filter(const DevParams<FT> &P, FT *Yf, cudaStream_t s);
+template <class FT> void launch_global_sums(const DevParams<FT> &P, const FT *Yc, double *partials, int nblocks, double *out, cudaStream_t s);
+void launch_reduce_rnorm(const double *rnorm, int ncols, double *out, cudaStream_t s);
+
+// Shared memory needed by the slab kernels (for cudaFuncSetAttribute).
+template <class FT> size_t passA_smem(int Nv);
+template <class FT> size_t passB_smem(int Nv);
+template <class FT> void configure_se(int Nv);
+
+}  // namespace gb

@@ -1,0 +1,592 @@
+// Column kernel of the implicit vertical-acoustic solve: one warp per column,
+// each lane owning M consecutive levels (level index = lane*M + k, centre and
+// face of the same index, the face below the centre).
+//
+// COL_STAGE fuses, for one implicit ARS343 stage, what ClimaTimeSteppers does
+// through the hooks (src/simulation/integrator.jl:189-225):
+//   stage assembly U^ = u_n + dt sum_j (a~_ij T_exp_j + a_ij T_imp_j),
+//   set_implicit_precomputed_quantities! (precomputed_quantities.jl:698-831,
+//     impenetrable filter :486-553),
+//   implicit_tendency! (implicit_tendency.jl:185-298) -> residual
+//     R = U^ + dtgamma T_imp(U) - U,
+//   update_jacobian! (manual_sparse_jacobian.jl:713-870, dry, no topography),
+//   ldiv! with BlockArrowheadSolve(rho, rho e_tot; alg2 = u_h)
+//     (manual_sparse_jacobian.jl:580-583): Schur complement onto u_3 (a
+//     tridiagonal face system), solved by parallel cyclic reduction across
+//     the warp, then back-substitution for rho and rho e_tot,
+//   U -= dY; filter; correct_implicit_advection_tendency! (van Leer minus
+//     central, implicit_tendency.jl:322-339) applied as U += dtgamma * corr,
+//   T_imp_i = (U - U^) / dtgamma, and the FP64 residual sums of squares.
+// The other modes are the individual hooks.
+#include "kernels.cuh"
+
+namespace gb {
+
+namespace {
+
+constexpr int COL_THREADS = 128;  // 4 columns per CTA
+
+// value of x at level (own level + D) for the compile-time slot K
+template <int M, int K, int D, class FT>
+__device__ __forceinline__ FT nb(const FT (&x)[M]) {
+  constexpr int kk = K + D;
+  if constexpr (kk >= 0 && kk < M) {
+    return x[kk];
+  } else if constexpr (kk < 0) {
+    constexpr int L = (-kk + M - 1) / M;
+    return shfl_up(x[kk + L * M], L);
+  } else {
+    constexpr int L = kk / M;
+    return shfl_down(x[kk - L * M], L);
+  }
+}
+
+template <int M, int D, class FT>
+__device__ __forceinline__ void nb_all(const FT (&x)[M], FT (&o)[M]) {
+  if constexpr (M >= 1) o[0] = nb<M, 0, D>(x);
+  if constexpr (M >= 2) o[1] = nb<M, 1, D>(x);
+  if constexpr (M >= 3) o[2] = nb<M, 2, D>(x);
+  if constexpr (M >= 4) o[3] = nb<M, 3, D>(x);
+}
+
+// Parallel cyclic reduction of the 32*M-row tridiagonal system held by the warp
+// (rows outside the column are identity rows).  Leaves x = d / b.
+template <class FT, int M, int S>
+__device__ __forceinline__ void pcr_level(FT (&a)[M], FT (&b)[M], FT (&c)[M], FT (&d)[M], int lane) {
+  FT am[M], bm[M], cm[M], dm[M], ap[M], bp[M], cp[M], dp[M];
+  nb_all<M, -S>(a, am); nb_all<M, -S>(b, bm); nb_all<M, -S>(c, cm); nb_all<M, -S>(d, dm);
+  nb_all<M, S>(a, ap); nb_all<M, S>(b, bp); nb_all<M, S>(c, cp); nb_all<M, S>(d, dp);
+#pragma unroll
+  for (int k = 0; k < M; ++k) {
+    const int r = lane * M + k;
+    const bool hm = r - S >= 0, hp = r + S < 32 * M;
+    const FT al = hm ? -a[k] / bm[k] : FT(0);
+    const FT ga = hp ? -c[k] / bp[k] : FT(0);
+    const FT na = hm ? al * am[k] : FT(0);
+    const FT nc = hp ? ga * cp[k] : FT(0);
+    FT nbv = b[k], ndv = d[k];
+    if (hm) { nbv += al * cm[k]; ndv += al * dm[k]; }
+    if (hp) { nbv += ga * ap[k]; ndv += ga * dp[k]; }
+    a[k] = na; b[k] = nbv; c[k] = nc; d[k] = ndv;
+  }
+}
+
+template <class FT, int M>
+__device__ __forceinline__ void pcr_solve(FT (&a)[M], FT (&b)[M], FT (&c)[M], FT (&d)[M], FT (&x)[M], int lane) {
+  pcr_level<FT, M, 1>(a, b, c, d, lane);
+  pcr_level<FT, M, 2>(a, b, c, d, lane);
+  pcr_level<FT, M, 4>(a, b, c, d, lane);
+  pcr_level<FT, M, 8>(a, b, c, d, lane);
+  pcr_level<FT, M, 16>(a, b, c, d, lane);
+  if constexpr (M >= 2) pcr_level<FT, M, 32>(a, b, c, d, lane);
+  if constexpr (M >= 4) pcr_level<FT, M, 64>(a, b, c, d, lane);
+#pragma unroll
+  for (int k = 0; k < M; ++k) x[k] = d[k] / b[k];
+}
+
+// Column-local thermodynamic state at the owned levels.
+template <class FT, int M>
+struct ColState {
+  FT rho[M], u1[M], u2[M], rhoe[M], u3[M];
+};
+template <class FT, int M>
+struct ColDiag {
+  FT c1[M], c2[M], K[M], T[M], h[M], Pi[M], thv[M], thvr[M], phir[M], rJ[M], u3c[M], J[M];
+};
+
+template <class FT>
+struct ColGeo {
+  FT Jh, gu0, gu1, gu2;
+};
+
+template <class FT, int M>
+__device__ __forceinline__ void col_diag(const DevParams<FT> &P, const ColGeo<FT> &G, const ColState<FT, M> &S,
+                                         ColDiag<FT, M> &Dg, int lane) {
+  const int Nv = P.Nv, Nf = P.Nf;
+#pragma unroll
+  for (int k = 0; k < M; ++k) {
+    const int f = min(lane * M + k, Nf - 1);
+    const FT dz = P.levf[LF_DZ * Nf + f];
+    Dg.u3c[k] = S.u3[k] / (dz * dz);
+  }
+  FT u3n[M], u3cn[M];
+  nb_all<M, 1>(S.u3, u3n);
+  nb_all<M, 1>(Dg.u3c, u3cn);
+#pragma unroll
+  for (int k = 0; k < M; ++k) {
+    const int v = min(lane * M + k, Nv - 1);
+    const FT r2 = P.levc[LC_R2 * Nv + v], dz = P.levc[LC_DZ * Nv + v], Phi = P.levc[LC_PHI * Nv + v];
+    const FT gu0 = G.gu0 / r2, gu1 = G.gu1 / r2, gu2 = G.gu2 / r2;
+    const FT c1 = gu0 * S.u1[k] + gu1 * S.u2[k], c2 = gu1 * S.u1[k] + gu2 * S.u2[k];
+    const FT kv = (S.u3[k] * Dg.u3c[k] + u3n[k] * u3cn[k]) / FT(2);
+    const FT K = (S.u1[k] * c1 + S.u2[k] * c2 + kv) / FT(2);
+    Thermo<FT> th;
+    thermo(P, S.rho[k], S.rhoe[k], K, Phi, th);
+    Dg.c1[k] = c1; Dg.c2[k] = c2; Dg.K[k] = K; Dg.T[k] = th.T; Dg.h[k] = th.h; Dg.Pi[k] = th.Pi;
+    Dg.thv[k] = th.thv; Dg.thvr[k] = th.thvr; Dg.phir[k] = th.phir;
+    Dg.J[k] = G.Jh * r2 * dz;
+    Dg.rJ[k] = S.rho[k] * Dg.J[k];
+  }
+}
+
+// implicit tendency (rho, rho e_tot, u_3) at the owned levels
+template <class FT, int M>
+__device__ __forceinline__ void col_implicit(const DevParams<FT> &P, const ColGeo<FT> &G, const ColState<FT, M> &S,
+                                             const ColDiag<FT, M> &Dg, FT (&Tr)[M], FT (&Te)[M], FT (&T3)[M], int lane) {
+  const int Nv = P.Nv, Nf = P.Nf;
+  FT rJm[M], hm[M], phm[M], Pim[M], thm[M], thrm[M];
+  nb_all<M, -1>(Dg.rJ, rJm); nb_all<M, -1>(Dg.h, hm); nb_all<M, -1>(Dg.phir, phm);
+  nb_all<M, -1>(Dg.Pi, Pim); nb_all<M, -1>(Dg.thv, thm); nb_all<M, -1>(Dg.thvr, thrm);
+  FT flux[M], fh[M];
+#pragma unroll
+  for (int k = 0; k < M; ++k) {
+    const int f = lane * M + k;
+    const bool inner = f > 0 && f < Nv;
+    const int fc = min(f, Nf - 1);
+    const FT dzf = P.levf[LF_DZ * Nf + fc], r2 = P.levf[LF_R2 * Nf + fc];
+    const FT Jf = G.Jh * r2 * dzf;
+    const FT rJ = (rJm[k] + Dg.rJ[k]) / FT(2);
+    const FT F = rJ / Jf * Dg.u3c[k];
+    const FT hb = (hm[k] + Dg.h[k]) / FT(2);
+    flux[k] = inner ? Jf * F : FT(0);
+    fh[k] = inner ? Jf * F * hb : FT(0);
+    FT val = 0;
+    if (inner) {
+      const FT gPhir = Dg.phir[k] - phm[k];
+      const FT thd = ((thm[k] - thrm[k]) + (Dg.thv[k] - Dg.thvr[k])) / FT(2);
+      const FT gPi = Dg.Pi[k] - Pim[k];
+      val = -(P.levf[LF_DPHI * Nf + fc] - gPhir + P.cpd * thd * gPi);
+    }
+    val -= P.levf[LF_BETA * Nf + fc] * S.u3[k];
+    T3[k] = val;
+  }
+  FT fln[M], fhn[M];
+  nb_all<M, 1>(flux, fln);
+  nb_all<M, 1>(fh, fhn);
+#pragma unroll
+  for (int k = 0; k < M; ++k) {
+    Tr[k] = -((fln[k] - flux[k]) / Dg.J[k]);
+    Te[k] = -((fhn[k] - fh[k]) / Dg.J[k]);
+  }
+}
+
+// Jacobian blocks at the owned levels (centre rows: Mru/Meu for faces v, v+1;
+// face rows: Mur/Mue/Muh for centres k-1, k, Muu for faces k-1, k, k+1).
+template <class FT, int M>
+struct ColJac {
+  FT ru0[M], ru1[M], eu0[M], eu1[M];
+  FT ur0[M], ur1[M], ue0[M], ue1[M], uh0[M], uh1[M], uh2[M], uh3[M], uu0[M], uu1[M], uu2[M];
+};
+
+template <class FT, int M>
+__device__ __forceinline__ void col_jacobian(const DevParams<FT> &P, const ColGeo<FT> &G, const ColState<FT, M> &S,
+                                             const ColDiag<FT, M> &Dg, FT dtg, ColJac<FT, M> &Jc, int lane) {
+  const int Nv = P.Nv, Nf = P.Nf;
+  const FT kap = P.Rd / P.cvd;
+  FT rJm[M], hm[M], rhom[M], Km[M], thm[M], Pim[M], c1m[M], c2m[M], u3cm[M], u3cp[M];
+  nb_all<M, -1>(Dg.rJ, rJm); nb_all<M, -1>(Dg.h, hm); nb_all<M, -1>(S.rho, rhom); nb_all<M, -1>(Dg.K, Km);
+  nb_all<M, -1>(Dg.thv, thm); nb_all<M, -1>(Dg.Pi, Pim); nb_all<M, -1>(Dg.c1, c1m); nb_all<M, -1>(Dg.c2, c2m);
+  nb_all<M, -1>(Dg.u3c, u3cm); nb_all<M, 1>(Dg.u3c, u3cp);
+  // face quantities needed by centre rows: rJbar*g33 and hbar at faces
+  FT fr[M], fhb[M];
+#pragma unroll
+  for (int k = 0; k < M; ++k) {
+    const int f = lane * M + k;
+    const bool inner = f > 0 && f < Nv;
+    const int fc = min(f, Nf - 1);
+    const FT dzf = P.levf[LF_DZ * Nf + fc];
+    const FT g33 = FT(1) / (dzf * dzf);
+    const FT rJ = (rJm[k] + Dg.rJ[k]) / FT(2);
+    fr[k] = inner ? rJ * g33 : FT(0);
+    fhb[k] = (hm[k] + Dg.h[k]) / FT(2);
+  }
+  FT frn[M], fhbn[M];
+  nb_all<M, 1>(fr, frn);
+  nb_all<M, 1>(fhb, fhbn);
+#pragma unroll
+  for (int k = 0; k < M; ++k) {
+    const FT J = Dg.J[k];
+    const FT v0 = fr[k] / J, v1 = -frn[k] / J;
+    Jc.ru0[k] = dtg * v0;
+    Jc.ru1[k] = dtg * v1;
+    Jc.eu0[k] = dtg * (v0 * fhb[k]);
+    Jc.eu1[k] = dtg * (v1 * fhbn[k]);
+    const int f = lane * M + k;
+    const int fc = min(f, Nf - 1);
+    const FT beta = P.levf[LF_BETA * Nf + fc];
+    if (f > 0 && f < Nv) {
+      const int va = f - 1;
+      const FT ra = rhom[k], rb = S.rho[k];
+      const FT rbar = (ra + rb) / FT(2);
+      const FT dpa = kap * (P.T0 * P.cpd - Km[k] - P.levc[LC_PHI * Nv + va]);
+      const FT dpb = kap * (P.T0 * P.cpd - Dg.K[k] - P.levc[LC_PHI * Nv + f]);
+      const FT thvb = (thm[k] + Dg.thv[k]) / FT(2);
+      const FT gPi = Dg.Pi[k] - Pim[k];
+      const FT buoy = P.cpd * thvb * gPi / rbar;
+      Jc.ur0[k] = dtg * (dpa / rbar + buoy / FT(2));
+      Jc.ur1[k] = dtg * (-dpb / rbar + buoy / FT(2));
+      Jc.ue0[k] = dtg * (kap / rbar);
+      Jc.ue1[k] = dtg * (-kap / rbar);
+      Jc.uh0[k] = dtg * (-kap * ra / rbar) * c1m[k];
+      Jc.uh1[k] = dtg * (-kap * ra / rbar) * c2m[k];
+      Jc.uh2[k] = dtg * (kap * rb / rbar) * Dg.c1[k];
+      Jc.uh3[k] = dtg * (kap * rb / rbar) * Dg.c2[k];
+      Jc.uu0[k] = dtg * (-kap * ra * u3cm[k] / (FT(2) * rbar));
+      Jc.uu1[k] = dtg * (kap * (rb - ra) * Dg.u3c[k] / (FT(2) * rbar) - beta) - FT(1);
+      Jc.uu2[k] = dtg * (kap * rb * u3cp[k] / (FT(2) * rbar));
+    } else {
+      Jc.ur0[k] = Jc.ur1[k] = Jc.ue0[k] = Jc.ue1[k] = FT(0);
+      Jc.uh0[k] = Jc.uh1[k] = Jc.uh2[k] = Jc.uh3[k] = FT(0);
+      Jc.uu0[k] = Jc.uu2[k] = FT(0);
+      Jc.uu1[k] = f <= Nv ? -dtg * beta - FT(1) : FT(1);  // identity rows beyond the column
+    }
+  }
+}
+
+// Solve W dY = R with the Schur complement onto u_3.
+template <class FT, int M>
+__device__ __forceinline__ void col_ldiv(const DevParams<FT> &P, const ColJac<FT, M> &Jc, const FT (&Rr)[M],
+                                         const FT (&Re)[M], const FT (&Ru1)[M], const FT (&Ru2)[M], const FT (&R3)[M],
+                                         FT (&Xr)[M], FT (&Xe)[M], FT (&X3)[M], int lane) {
+  const int Nv = P.Nv, Nf = P.Nf;
+  FT ru0m[M], ru1m[M], eu0m[M], eu1m[M], Rrm[M], Rem[M], Ru1m[M], Ru2m[M];
+  nb_all<M, -1>(Jc.ru0, ru0m); nb_all<M, -1>(Jc.ru1, ru1m); nb_all<M, -1>(Jc.eu0, eu0m); nb_all<M, -1>(Jc.eu1, eu1m);
+  nb_all<M, -1>(Rr, Rrm); nb_all<M, -1>(Re, Rem); nb_all<M, -1>(Ru1, Ru1m); nb_all<M, -1>(Ru2, Ru2m);
+  FT a[M], b[M], c[M], d[M], x[M];
+#pragma unroll
+  for (int k = 0; k < M; ++k) {
+    const int f = lane * M + k;
+    FT aa = Jc.uu0[k], bb = Jc.uu1[k], cc = Jc.uu2[k];
+    FT rhs = f < Nf ? R3[k] : FT(0);
+    if (f >= 1 && f - 1 < Nv) {  // centre f-1 (slot s = 0)
+      const FT cr = Jc.ur0[k], ce = Jc.ue0[k];
+      aa += cr * ru0m[k] + ce * eu0m[k];
+      bb += cr * ru1m[k] + ce * eu1m[k];
+      rhs += cr * Rrm[k] + ce * Rem[k];
+      rhs += Jc.uh0[k] * Ru1m[k] + Jc.uh1[k] * Ru2m[k];
+    }
+    if (f < Nv) {  // centre f (slot s = 1)
+      const FT cr = Jc.ur1[k], ce = Jc.ue1[k];
+      bb += cr * Jc.ru0[k] + ce * Jc.eu0[k];
+      cc += cr * Jc.ru1[k] + ce * Jc.eu1[k];
+      rhs += cr * Rr[k] + ce * Re[k];
+      rhs += Jc.uh2[k] * Ru1[k] + Jc.uh3[k] * Ru2[k];
+    }
+    if (f >= Nf) { aa = FT(0); bb = FT(1); cc = FT(0); rhs = FT(0); }
+    a[k] = aa; b[k] = bb; c[k] = cc; d[k] = rhs;
+  }
+  pcr_solve<FT, M>(a, b, c, d, x, lane);
+  FT xn[M];
+  nb_all<M, 1>(x, xn);
+#pragma unroll
+  for (int k = 0; k < M; ++k) {
+    X3[k] = x[k];
+    Xr[k] = Jc.ru0[k] * x[k] + Jc.ru1[k] * xn[k] - Rr[k];
+    Xe[k] = Jc.eu0[k] * x[k] + Jc.eu1[k] * xn[k] - Re[k];
+  }
+}
+
+// Lin et al. (1994) van Leer face value times u, with their monotonicity
+// constraint and first-order one-sided values next to the boundaries.
+template <class FT>
+__device__ __forceinline__ FT vanleer(FT u, FT am2, FT am1, FT a0, FT ap1, bool near, FT dtm) {
+  // face between centres (am1 below) and (a0 above); am2 below am1, ap1 above a0
+  if (u >= FT(0)) {
+    if (near) return u * am1;
+    const FT lo = am2, c = am1, hi = a0;
+    const FT da = (hi - lo) / FT(2);
+    const FT mn = fmin(lo, fmin(c, hi)), mx = fmax(lo, fmax(c, hi));
+    const FT sl = copysign(fmin(fabs(da), fmin(FT(2) * (c - mn), FT(2) * (mx - c))), da);
+    return u * (c + sl * (FT(1) - fabs(u) * dtm) / FT(2));
+  } else {
+    if (near) return u * a0;
+    const FT lo = am1, c = a0, hi = ap1;
+    const FT da = (hi - lo) / FT(2);
+    const FT mn = fmin(lo, fmin(c, hi)), mx = fmax(lo, fmax(c, hi));
+    const FT sl = copysign(fmin(fabs(da), fmin(FT(2) * (c - mn), FT(2) * (mx - c))), da);
+    return u * (c - sl * (FT(1) - fabs(u) * dtm) / FT(2));
+  }
+}
+
+template <class FT, int M>
+__device__ __forceinline__ void col_correction(const DevParams<FT> &P, const ColGeo<FT> &G, const ColDiag<FT, M> &Dg,
+                                               FT (&corr)[M], int lane) {
+  const int Nv = P.Nv, Nf = P.Nf;
+  FT hm1[M], hm2[M], hp1[M], rJm[M];
+  nb_all<M, -1>(Dg.h, hm1); nb_all<M, -2>(Dg.h, hm2); nb_all<M, 1>(Dg.h, hp1);
+  nb_all<M, -1>(Dg.rJ, rJm);
+  FT fup[M], fcen[M];
+#pragma unroll
+  for (int k = 0; k < M; ++k) {
+    const int f = lane * M + k;
+    const bool inner = f > 0 && f < Nv;
+    const int fc = min(f, Nf - 1);
+    const FT Jf = G.Jh * P.levf[LF_R2 * Nf + fc] * P.levf[LF_DZ * Nf + fc];
+    const FT rJ = (rJm[k] + Dg.rJ[k]) / FT(2);
+    const FT u = Dg.u3c[k];
+    const bool near = f == 1 || f == Nv - 1;
+    const FT vl = vanleer(u, hm2[k], hm1[k], Dg.h[k], hp1[k], near, P.dt_model);
+    fup[k] = inner ? Jf * (rJ / Jf * vl) : FT(0);
+    fcen[k] = inner ? Jf * (rJ / Jf * (u * (hm1[k] + Dg.h[k]) / FT(2))) : FT(0);
+  }
+  FT fupn[M], fcn[M];
+  nb_all<M, 1>(fup, fupn);
+  nb_all<M, 1>(fcen, fcn);
+#pragma unroll
+  for (int k = 0; k < M; ++k) {
+    const FT vup = -((fupn[k] - fup[k]) / Dg.J[k]);
+    const FT vc = -((fcn[k] - fcen[k]) / Dg.J[k]);
+    corr[k] = vup - vc;
+  }
+}
+
+template <class FT>
+__device__ __forceinline__ size_t cidx(int e, int c, int n, int v, int Nv) { return (((size_t)e * 4 + c) * NN + n) * Nv + v; }
+template <class FT>
+__device__ __forceinline__ size_t ridx(int e, int c, int n, int v, int Nv) { return (((size_t)e * 2 + c) * NN + n) * Nv + v; }
+
+template <class FT, int M>
+__global__ void __launch_bounds__(COL_THREADS) k_col_stage(DevParams<FT> P, StageArgs<FT> A) {
+  const int lane = threadIdx.x & 31;
+  const int col = blockIdx.x * (COL_THREADS / 32) + (threadIdx.x >> 5);
+  const int ncols = P.Nh * NN;
+  if (col >= ncols) return;
+  const int e = col >> 4, n = col & 15, Nv = P.Nv, Nf = P.Nf;
+  ColGeo<FT> G;
+  const FT *hg = P.hgeo + (size_t)e * HG_N * NN;
+  G.Jh = hg[HG_JH * NN + n]; G.gu0 = hg[HG_GU0 * NN + n]; G.gu1 = hg[HG_GU1 * NN + n]; G.gu2 = hg[HG_GU2 * NN + n];
+  // ---- stage assembly
+  ColState<FT, M> H;  // U^
+#pragma unroll
+  for (int k = 0; k < M; ++k) {
+    const int v = lane * M + k;
+    const bool cv = v < Nv, fv = v < Nf;
+    FT x[5] = {0, 0, 0, 0, 0};
+    if (cv) {
+      for (int c = 0; c < 4; ++c) {
+        const size_t q = cidx<FT>(e, c, n, v, Nv);
+        FT s = A.un_c[q];
+        for (int j = 0; j < A.nsrc; ++j) {
+          if (A.te_c[j]) s += A.ce[j] * A.te_c[j][q];
+          if (A.ti_c[j] && (c == 0 || c == 3)) s += A.ci[j] * A.ti_c[j][ridx<FT>(e, c == 3, n, v, Nv)];
+        }
+        x[c] = s;
+      }
+    }
+    if (fv) {
+      const size_t q = ((size_t)e * NN + n) * Nf + v;
+      FT s = A.un_f[q];
+      for (int j = 0; j < A.nsrc; ++j) {
+        if (A.te_f[j]) s += A.ce[j] * A.te_f[j][q];
+        if (A.ti_f[j]) s += A.ci[j] * A.ti_f[j][q];
+      }
+      x[4] = s;
+    }
+    H.rho[k] = cv ? x[0] : FT(1);
+    H.u1[k] = x[1]; H.u2[k] = x[2];
+    H.rhoe[k] = cv ? x[3] : FT(1);
+    H.u3[k] = x[4];
+  }
+  // ---- filter and precomputed quantities at U = filtered U^
+  ColState<FT, M> U = H;
+#pragma unroll
+  for (int k = 0; k < M; ++k) {
+    const int f = lane * M + k;
+    if (f == 0 || f >= Nv) U.u3[k] = FT(0);
+  }
+  ColDiag<FT, M> Dg;
+  col_diag<FT, M>(P, G, U, Dg, lane);
+  FT Tr[M], Te[M], T3[M];
+  col_implicit<FT, M>(P, G, U, Dg, Tr, Te, T3, lane);
+  const FT dtg = A.dtg;
+  FT Rr[M], Re[M], Ru1[M], Ru2[M], R3[M];
+  double ss[3] = {0, 0, 0};
+  bool finite = true;
+#pragma unroll
+  for (int k = 0; k < M; ++k) {
+    const int v = lane * M + k;
+    const bool cv = v < Nv, fv = v < Nf;
+    Rr[k] = cv ? H.rho[k] + dtg * Tr[k] - U.rho[k] : FT(0);
+    Re[k] = cv ? H.rhoe[k] + dtg * Te[k] - U.rhoe[k] : FT(0);
+    Ru1[k] = FT(0);
+    Ru2[k] = FT(0);
+    R3[k] = fv ? H.u3[k] + dtg * T3[k] - U.u3[k] : FT(0);
+    ss[0] += (double)Rr[k] * (double)Rr[k];
+    ss[1] += (double)Re[k] * (double)Re[k];
+    ss[2] += (double)R3[k] * (double)R3[k];
+    finite = finite && isfinite(Rr[k]) && isfinite(Re[k]) && isfinite(R3[k]);
+  }
+  ColJac<FT, M> Jc;
+  col_jacobian<FT, M>(P, G, U, Dg, dtg, Jc, lane);
+  FT Xr[M], Xe[M], X3[M];
+  col_ldiv<FT, M>(P, Jc, Rr, Re, Ru1, Ru2, R3, Xr, Xe, X3, lane);
+#pragma unroll
+  for (int k = 0; k < M; ++k) {
+    const int f = lane * M + k;
+    U.rho[k] -= Xr[k];
+    U.rhoe[k] -= Xe[k];
+    U.u3[k] -= X3[k];
+    if (f == 0 || f >= Nv) U.u3[k] = FT(0);  // filter after the solve (cache!)
+  }
+  if (P.upwinding) {
+    col_diag<FT, M>(P, G, U, Dg, lane);
+    FT corr[M];
+    col_correction<FT, M>(P, G, Dg, corr, lane);
+#pragma unroll
+    for (int k = 0; k < M; ++k) U.rhoe[k] += dtg * corr[k];
+  }
+  // ---- outputs: U, T_imp = (U - U^) / dtgamma, residual sums of squares
+#pragma unroll
+  for (int k = 0; k < M; ++k) {
+    const int v = lane * M + k;
+    if (v < Nv) {
+      A.U_c[cidx<FT>(e, 0, n, v, Nv)] = U.rho[k];
+      A.U_c[cidx<FT>(e, 1, n, v, Nv)] = U.u1[k];
+      A.U_c[cidx<FT>(e, 2, n, v, Nv)] = U.u2[k];
+      A.U_c[cidx<FT>(e, 3, n, v, Nv)] = U.rhoe[k];
+      A.Ti_c[ridx<FT>(e, 0, n, v, Nv)] = (U.rho[k] - H.rho[k]) / dtg;
+      A.Ti_c[ridx<FT>(e, 1, n, v, Nv)] = (U.rhoe[k] - H.rhoe[k]) / dtg;
+    }
+    if (v < Nf) {
+      const size_t q = ((size_t)e * NN + n) * Nf + v;
+      A.U_f[q] = U.u3[k];
+      A.Ti_f[q] = (U.u3[k] - H.u3[k]) / dtg;
+    }
+  }
+#pragma unroll
+  for (int c = 0; c < 3; ++c)
+    for (int o = 16; o > 0; o >>= 1) ss[c] += __shfl_xor_sync(0xffffffffu, ss[c], o);
+  finite = __all_sync(0xffffffffu, finite);
+  if (lane == 0) {
+    if (A.rnorm) {
+      for (int c = 0; c < 3; ++c) A.rnorm[(size_t)col * 3 + c] = (A.first ? 0.0 : A.rnorm[(size_t)col * 3 + c]) + ss[c];
+    }
+    if (!finite) atomicOr(P.status, ST_NONFINITE);
+  }
+}
+
+// Individual hooks: implicit tendency, Jacobian, ldiv, post-Newton correction.
+template <class FT, int M, int MODE>
+__global__ void __launch_bounds__(COL_THREADS) k_col_hook(DevParams<FT> P, ColArgs<FT> A) {
+  const int lane = threadIdx.x & 31;
+  const int col = blockIdx.x * (COL_THREADS / 32) + (threadIdx.x >> 5);
+  const int ncols = P.Nh * NN;
+  if (col >= ncols) return;
+  const int e = col >> 4, n = col & 15, Nv = P.Nv, Nf = P.Nf;
+  ColGeo<FT> G;
+  const FT *hg = P.hgeo + (size_t)e * HG_N * NN;
+  G.Jh = hg[HG_JH * NN + n]; G.gu0 = hg[HG_GU0 * NN + n]; G.gu1 = hg[HG_GU1 * NN + n]; G.gu2 = hg[HG_GU2 * NN + n];
+  ColState<FT, M> S;
+#pragma unroll
+  for (int k = 0; k < M; ++k) {
+    const int v = lane * M + k;
+    const bool cv = v < Nv, fv = v < Nf;
+    S.rho[k] = cv ? A.Y_c[cidx<FT>(e, 0, n, v, Nv)] : (MODE == COL_LDIV ? FT(0) : FT(1));
+    S.u1[k] = cv ? A.Y_c[cidx<FT>(e, 1, n, v, Nv)] : FT(0);
+    S.u2[k] = cv ? A.Y_c[cidx<FT>(e, 2, n, v, Nv)] : FT(0);
+    S.rhoe[k] = cv ? A.Y_c[cidx<FT>(e, 3, n, v, Nv)] : (MODE == COL_LDIV ? FT(0) : FT(1));
+    S.u3[k] = fv ? A.Y_f[((size_t)e * NN + n) * Nf + v] : FT(0);
+    if (MODE != COL_LDIV && (v == 0 || v >= Nv)) S.u3[k] = FT(0);  // impenetrable filter
+  }
+  FT *jac = A.jac + (size_t)col * JAC_Q * Nf;
+  FT o0[M], o1[M], o2[M], o3[M], o4[M];
+  if constexpr (MODE == COL_LDIV) {
+    ColJac<FT, M> Jc;
+#pragma unroll
+    for (int k = 0; k < M; ++k) {
+      const int f = lane * M + k;
+      const int fc = min(f, Nf - 1);
+      FT *q[JAC_Q] = {Jc.ru0, Jc.ru1, Jc.eu0, Jc.eu1, Jc.ur0, Jc.ur1, Jc.ue0, Jc.ue1,
+                      Jc.uh0, Jc.uh1, Jc.uh2, Jc.uh3, Jc.uu0, Jc.uu1, Jc.uu2};
+      for (int t = 0; t < JAC_Q; ++t) q[t][k] = jac[t * Nf + fc];
+      if (f >= Nf) {
+        for (int t = 0; t < JAC_Q; ++t) q[t][k] = FT(0);
+        Jc.uu1[k] = FT(1);
+      }
+    }
+    col_ldiv<FT, M>(P, Jc, S.rho, S.rhoe, S.u1, S.u2, S.u3, o0, o3, o4, lane);
+#pragma unroll
+    for (int k = 0; k < M; ++k) { o1[k] = -S.u1[k]; o2[k] = -S.u2[k]; }
+  } else {
+    ColDiag<FT, M> Dg;
+    col_diag<FT, M>(P, G, S, Dg, lane);
+    if constexpr (MODE == COL_IMPLICIT) {
+      col_implicit<FT, M>(P, G, S, Dg, o0, o3, o4, lane);
+#pragma unroll
+      for (int k = 0; k < M; ++k) { o1[k] = FT(0); o2[k] = FT(0); }
+    } else if constexpr (MODE == COL_POSTIMP) {
+      FT corr[M];
+      if (P.upwinding) col_correction<FT, M>(P, G, Dg, corr, lane);
+#pragma unroll
+      for (int k = 0; k < M; ++k) {
+        o0[k] = o1[k] = o2[k] = o4[k] = FT(0);
+        o3[k] = P.upwinding ? corr[k] : FT(0);
+      }
+    } else {  // COL_JACOBIAN
+      ColJac<FT, M> Jc;
+      col_jacobian<FT, M>(P, G, S, Dg, A.dtg, Jc, lane);
+#pragma unroll
+      for (int k = 0; k < M; ++k) {
+        const int f = lane * M + k;
+        if (f < Nf) {
+          const FT q[JAC_Q] = {Jc.ru0[k], Jc.ru1[k], Jc.eu0[k], Jc.eu1[k], Jc.ur0[k], Jc.ur1[k], Jc.ue0[k], Jc.ue1[k],
+                               Jc.uh0[k], Jc.uh1[k], Jc.uh2[k], Jc.uh3[k], Jc.uu0[k], Jc.uu1[k], Jc.uu2[k]};
+          for (int t = 0; t < JAC_Q; ++t) jac[t * Nf + f] = q[t];
+        }
+      }
+      return;
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < M; ++k) {
+    const int v = lane * M + k;
+    if (v < Nv) {
+      A.O_c[cidx<FT>(e, 0, n, v, Nv)] = o0[k];
+      A.O_c[cidx<FT>(e, 1, n, v, Nv)] = o1[k];
+      A.O_c[cidx<FT>(e, 2, n, v, Nv)] = o2[k];
+      A.O_c[cidx<FT>(e, 3, n, v, Nv)] = o3[k];
+    }
+    if (v < Nf) A.O_f[((size_t)e * NN + n) * Nf + v] = o4[k];
+  }
+}
+
+inline int levels_per_lane(int Nf) { return Nf <= 32 ? 1 : (Nf <= 64 ? 2 : 4); }
+
+}  // namespace
+
+template <class FT>
+void launch_column_stage(const DevParams<FT> &P, const StageArgs<FT> &A, cudaStream_t s) {
+  const int ncols = P.Nh * NN, grid = (ncols + COL_THREADS / 32 - 1) / (COL_THREADS / 32);
+  switch (levels_per_lane(P.Nf)) {
+    case 1: k_col_stage<FT, 1><<<grid, COL_THREADS, 0, s>>>(P, A); break;
+    case 2: k_col_stage<FT, 2><<<grid, COL_THREADS, 0, s>>>(P, A); break;
+    default: k_col_stage<FT, 4><<<grid, COL_THREADS, 0, s>>>(P, A); break;
+  }
+}
+
+template <class FT, int M>
+void launch_hook_m(const DevParams<FT> &P, int mode, const ColArgs<FT> &A, int grid, cudaStream_t s) {
+  switch (mode) {
+    case COL_IMPLICIT: k_col_hook<FT, M, COL_IMPLICIT><<<grid, COL_THREADS, 0, s>>>(P, A); break;
+    case COL_JACOBIAN: k_col_hook<FT, M, COL_JACOBIAN><<<grid, COL_THREADS, 0, s>>>(P, A); break;
+    case COL_LDIV: k_col_hook<FT, M, COL_LDIV><<<grid, COL_THREADS, 0, s>>>(P, A); break;
+    default: k_col_hook<FT, M, COL_POSTIMP><<<grid, COL_THREADS, 0, s>>>(P, A); break;
+  }
+}
+
+template <class FT>
+void launch_column(const DevParams<FT> &P, int mode, const ColArgs<FT> &A, cudaStream_t s) {
+  const int ncols = P.Nh * NN, grid = (ncols + COL_THREADS / 32 - 1) / (COL_THREADS / 32);
+  switch (levels_per_lane(P.Nf)) {
+    case 1: launch_hook_m<FT, 1>(P, mode, A, grid, s); break;
+    case 2: launch_hook_m<FT, 2>(P, mode, A, grid, s); break;
+    default: launch_hook_m<FT, 4>(P, mode, A, grid, s); break;
+  }
+}
+
+template void launch_column_stage<float>(const DevParams<float> &, const StageArgs<float> &, cudaStream_t);
+template void launch_column_stage<double>(const DevParams<double> &, const StageArgs<double> &, cudaStream_t);
+template void launch_column<float>(const DevParams<float> &, int, const ColArgs<float> &, cudaStream_t);
+template void launch_column<double>(const DevParams<double> &, int, const ColArgs<double> &, cudaStream_t);
+
+}  // namespace gb

@@ -1,0 +1,200 @@
+// DSS, final stage combination, boundary filter and compensated global sums.
+#include "kernels.cuh"
+
+namespace gb {
+
+namespace {
+
+constexpr int DSS_THREADS = 256;  // 8 groups per CTA, one warp per group
+
+// Direct stiffness summation (Spaces.weighted_dss!, constrain_state.jl:59-64 and
+// remaining_tendency.jl:18-21): each group of collocated element nodes gets the
+// J-weighted average of its copies, summed in the fixed ascending copy order
+// (deterministic, no atomics).  Centre block components: 0 scalar, 1-2 covariant
+// horizontal vector (averaged in Cartesian components), 3 scalar.  One warp
+// per group, lanes over levels.
+template <class FT>
+__global__ void __launch_bounds__(DSS_THREADS) k_dss(DevParams<FT> P, FT *__restrict__ C, FT *__restrict__ F) {
+  const int lane = threadIdx.x & 31;
+  const int g = blockIdx.x * (DSS_THREADS / 32) + (threadIdx.x >> 5);
+  if (g >= P.ngroups) return;
+  const int Nv = P.Nv, Nf = P.Nf;
+  const int o0 = P.goff[g], o1 = P.goff[g + 1];
+  if (C) {
+    for (int v = lane; v < Nv; v += 32) {
+      FT s0 = 0, s3 = 0, X0 = 0, X1 = 0, X2 = 0;
+      for (int c = o0; c < o1; ++c) {
+        const int idx = P.gcopy[c], e = idx >> 4, n = idx & 15;
+        const FT w = P.gw[c];
+        const size_t b = ((size_t)e * 4 * NN + n) * Nv + v;
+        s0 += w * C[b];
+        s3 += w * C[b + 48 * Nv];
+        const FT u1 = C[b + 16 * Nv], u2 = C[b + 32 * Nv];
+        const FT *ec = P.econ + (size_t)idx * 6;
+        X0 += w * (u1 * ec[0] + u2 * ec[3]);
+        X1 += w * (u1 * ec[1] + u2 * ec[4]);
+        X2 += w * (u1 * ec[2] + u2 * ec[5]);
+      }
+      for (int c = o0; c < o1; ++c) {
+        const int idx = P.gcopy[c], e = idx >> 4, n = idx & 15;
+        const size_t b = ((size_t)e * 4 * NN + n) * Nv + v;
+        const FT *eo = P.ecov + (size_t)idx * 6;
+        C[b] = s0;
+        C[b + 48 * Nv] = s3;
+        C[b + 16 * Nv] = eo[0] * X0 + eo[1] * X1 + eo[2] * X2;
+        C[b + 32 * Nv] = eo[3] * X0 + eo[4] * X1 + eo[5] * X2;
+      }
+    }
+  }
+  if (F) {
+    for (int k = lane; k < Nf; k += 32) {
+      FT s = 0;
+      for (int c = o0; c < o1; ++c) {
+        const int idx = P.gcopy[c];
+        s += P.gw[c] * F[(size_t)idx * Nf + k];
+      }
+      for (int c = o0; c < o1; ++c) F[(size_t)P.gcopy[c] * Nf + k] = s;
+    }
+  }
+}
+
+// u_{n+1} = u_n + dt sum_j (b~_j T_exp_j + b_j T_imp_j), then the impenetrable filter.
+template <class FT>
+__global__ void k_final(DevParams<FT> P, StageArgs<FT> A, FT *__restrict__ Yc, FT *__restrict__ Yf) {
+  const int Nv = P.Nv, Nf = P.Nf;
+  const size_t NC = (size_t)P.Nh * 4 * NN * Nv, NF = (size_t)P.Nh * NN * Nf;
+  for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < NC + NF; q += (size_t)gridDim.x * blockDim.x) {
+    if (q < NC) {
+      const size_t row = q / Nv;
+      const int v = (int)(q - row * Nv);
+      const int n = (int)(row % NN), c = (int)((row / NN) % 4);
+      const size_t e = row / (4 * NN);
+      FT s = Yc[q];
+      for (int j = 0; j < A.nsrc; ++j) {
+        if (A.te_c[j]) s += A.ce[j] * A.te_c[j][q];
+        if (A.ti_c[j] && (c == 0 || c == 3)) s += A.ci[j] * A.ti_c[j][((e * 2 + (c == 3)) * NN + n) * Nv + v];
+      }
+      Yc[q] = s;
+    } else {
+      const size_t r = q - NC;
+      const int k = (int)(r % Nf);
+      FT s = Yf[r];
+      for (int j = 0; j < A.nsrc; ++j) {
+        if (A.te_f[j]) s += A.ce[j] * A.te_f[j][r];
+        if (A.ti_f[j]) s += A.ci[j] * A.ti_f[j][r];
+      }
+      Yf[r] = (k == 0 || k == Nv) ? FT(0) : s;
+    }
+  }
+}
+
+template <class FT>
+__global__ void k_bc_filter(int ncols, int Nf, FT *__restrict__ Yf) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c < ncols) {
+    Yf[(size_t)c * Nf] = FT(0);
+    Yf[(size_t)c * Nf + Nf - 1] = FT(0);
+  }
+}
+
+// Neumaier (compensated) FP64 summation
+__device__ __forceinline__ void two_sum_acc(double &s, double &cmp, double x) {
+  const double t = s + x;
+  if (fabs(s) >= fabs(x)) cmp += (s - t) + x; else cmp += (x - t) + s;
+  s = t;
+}
+
+constexpr int SUM_THREADS = 256;
+
+// Block partial sums of rho*WJ and rhoe*WJ (fixed order -> deterministic).
+template <class FT>
+__global__ void __launch_bounds__(SUM_THREADS) k_sums_partial(DevParams<FT> P, const FT *__restrict__ Yc, double *__restrict__ part) {
+  __shared__ double sh[4][SUM_THREADS];
+  const int Nv = P.Nv;
+  const size_t npt = (size_t)P.Nh * NN * Nv;
+  double s[2] = {0, 0}, c[2] = {0, 0};
+  for (size_t p = blockIdx.x * (size_t)SUM_THREADS + threadIdx.x; p < npt; p += (size_t)gridDim.x * SUM_THREADS) {
+    const size_t col = p / Nv;
+    const int v = (int)(p - col * Nv);
+    const int n = (int)(col % NN);
+    const size_t e = col / NN;
+    const double Jh = (double)P.hgeo[(e * HG_N + HG_JH) * NN + n];
+    const double WJ = (double)P.W[n] * (Jh * (double)P.levc[LC_R2 * Nv + v] * (double)P.levc[LC_DZ * Nv + v]);
+    const size_t b = (e * 4 * NN + n) * Nv + v;
+    two_sum_acc(s[0], c[0], (double)Yc[b] * WJ);
+    two_sum_acc(s[1], c[1], (double)Yc[b + 48 * Nv] * WJ);
+  }
+  sh[0][threadIdx.x] = s[0]; sh[1][threadIdx.x] = c[0];
+  sh[2][threadIdx.x] = s[1]; sh[3][threadIdx.x] = c[1];
+  __syncthreads();
+  if (threadIdx.x < 2) {
+    double ss = 0, cc = 0;
+    for (int t = 0; t < SUM_THREADS; ++t) {
+      two_sum_acc(ss, cc, sh[2 * threadIdx.x][t]);
+      cc += sh[2 * threadIdx.x + 1][t];
+    }
+    part[blockIdx.x * 4 + 2 * threadIdx.x] = ss;
+    part[blockIdx.x * 4 + 2 * threadIdx.x + 1] = cc;
+  }
+}
+
+__global__ void k_sums_final(const double *__restrict__ part, int nblocks, double *__restrict__ out) {
+  if (threadIdx.x < 2) {
+    double ss = 0, cc = 0;
+    for (int b = 0; b < nblocks; ++b) {
+      two_sum_acc(ss, cc, part[b * 4 + 2 * threadIdx.x]);
+      cc += part[b * 4 + 2 * threadIdx.x + 1];
+    }
+    out[threadIdx.x] = ss + cc;
+  }
+}
+
+__global__ void k_reduce_rnorm(const double *__restrict__ r, int ncols, double *__restrict__ out) {
+  __shared__ double sh[3][256];
+  double s[3] = {0, 0, 0};
+  for (int c = threadIdx.x; c < ncols; c += blockDim.x)
+    for (int q = 0; q < 3; ++q) s[q] += r[(size_t)c * 3 + q];
+  for (int q = 0; q < 3; ++q) sh[q][threadIdx.x] = s[q];
+  __syncthreads();
+  if (threadIdx.x < 3) {
+    double t = 0;
+    for (int i = 0; i < (int)blockDim.x; ++i) t += sh[threadIdx.x][i];
+    out[threadIdx.x] = t;
+  }
+}
+
+}  // namespace
+
+template <class FT>
+void launch_dss(const DevParams<FT> &P, FT *C, FT *F, cudaStream_t s) {
+  const int grid = (P.ngroups + DSS_THREADS / 32 - 1) / (DSS_THREADS / 32);
+  if (grid > 0) k_dss<FT><<<grid, DSS_THREADS, 0, s>>>(P, C, F);
+}
+template <class FT>
+void launch_final(const DevParams<FT> &P, const StageArgs<FT> &A, FT *Yc, FT *Yf, cudaStream_t s) {
+  k_final<FT><<<152 * 8, 256, 0, s>>>(P, A, Yc, Yf);
+}
+template <class FT>
+void launch_bc_filter(const DevParams<FT> &P, FT *Yf, cudaStream_t s) {
+  const int ncols = P.Nh * NN;
+  k_bc_filter<FT><<<(ncols + 255) / 256, 256, 0, s>>>(ncols, P.Nf, Yf);
+}
+template <class FT>
+void launch_global_sums(const DevParams<FT> &P, const FT *Yc, double *partials, int nblocks, double *out, cudaStream_t s) {
+  k_sums_partial<FT><<<nblocks, SUM_THREADS, 0, s>>>(P, Yc, partials);
+  k_sums_final<<<1, 32, 0, s>>>(partials, nblocks, out);
+}
+void launch_reduce_rnorm(const double *rnorm, int ncols, double *out, cudaStream_t s) {
+  k_reduce_rnorm<<<1, 256, 0, s>>>(rnorm, ncols, out);
+}
+
+#define INST(FT)                                                                                          \
+  template void launch_dss<FT>(const DevParams<FT> &, FT *, FT *, cudaStream_t);                          \
+  template void launch_final<FT>(const DevParams<FT> &, const StageArgs<FT> &, FT *, FT *, cudaStream_t); \
+  template void launch_bc_filter<FT>(const DevParams<FT> &, FT *, cudaStream_t);                          \
+  template void launch_global_sums<FT>(const DevParams<FT> &, const FT *, double *, int, double *, cudaStream_t);
+INST(float)
+INST(double)
+#undef INST
+
+}  // namespace gb

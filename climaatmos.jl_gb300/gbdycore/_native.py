@@ -1,0 +1,110 @@
+"""ctypes binding of the C ABI in include/gbdycore.h (libgbdycore.so).
+
+This is the Python counterpart of the ``ccall((:gb_*, libgbdycore), ...)``
+stubs of the Julia shim.  Loading fails loudly if the library has not been
+built; there is no CPU fallback.
+"""
+import ctypes
+import os
+
+from . import build as _build
+
+_c_int, _c_double, _vp = ctypes.c_int, ctypes.c_double, ctypes.c_void_p
+
+GB_OK, GB_ERR_ARG, GB_ERR_CUDA, GB_ERR_NOMEM, GB_ERR_NONFINITE, GB_ERR_TIMEOUT, GB_ERR_STATE = 0, -1, -2, -3, -4, -5, -6
+STATUS_NAMES = {0: "GB_OK", -1: "GB_ERR_ARG", -2: "GB_ERR_CUDA", -3: "GB_ERR_NOMEM", -4: "GB_ERR_NONFINITE",
+                -5: "GB_ERR_TIMEOUT", -6: "GB_ERR_STATE"}
+
+# Every symbol the header declares (checked by the CPU test suite).
+SYMBOLS = [
+    "gb_sizes", "gb_geometry_export", "gb_ctx_create", "gb_ctx_destroy", "gb_set_stream", "gb_last_error",
+    "gb_set_precomputed_quantities", "gb_remaining_tendency", "gb_implicit_tendency", "gb_update_jacobian",
+    "gb_ldiv", "gb_correct_implicit_advection_tendency", "gb_dss", "gb_step", "gb_global_sums",
+    "gb_newton_residual", "gb_time_kernel",
+]
+
+
+class GBConfig(ctypes.Structure):
+    _fields_ = [("h_elem", _c_int), ("z_elem", _c_int), ("ft_bytes", _c_int), ("z_stretch", _c_int),
+                ("z_max", _c_double), ("dz_bottom", _c_double), ("dt", _c_double),
+                ("nu_v", _c_double), ("nu_s", _c_double), ("div_damp", _c_double),
+                ("sponge_zd", _c_double), ("alpha_uh", _c_double), ("alpha_w", _c_double),
+                ("upwinding", _c_int)] + [(n, _c_double) for n in (
+                    "grav", "omega", "R_d", "cp_d", "cv_d", "T_0", "p_ref", "T_min_ref", "T_surf_ref",
+                    "T_min_sgs", "radius")]
+
+
+class GBFieldVec(ctypes.Structure):
+    _fields_ = [("c", _vp), ("f", _vp)]
+
+
+_dp = ctypes.POINTER(ctypes.c_double)
+_ip = ctypes.POINTER(ctypes.c_int)
+
+
+class GBGeometryHost(ctypes.Structure):
+    _fields_ = [("xyz", _dp), ("ecov", _dp), ("Jh", _dp), ("gup", _dp), ("fh0", _dp), ("zf", _dp),
+                ("dss_off", _ip), ("dss_copy", _ip)]
+
+
+class GBError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("%s: %s" % (STATUS_NAMES.get(code, code), msg))
+        self.code = code
+
+
+_lib = None
+
+
+def lib_path():
+    return _build.LIB
+
+
+def load(build_if_missing=True):
+    """Load libgbdycore.so (building it with nvcc first if it is missing or stale)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = _build.build() if build_if_missing else _build.LIB
+    if not os.path.exists(path):
+        raise RuntimeError("libgbdycore.so is not built (run __graft_entry__.build())")
+    L = ctypes.CDLL(path)
+    fv = GBFieldVec
+    cfgp = ctypes.POINTER(GBConfig)
+    L.gb_sizes.argtypes = [cfgp, ctypes.POINTER(ctypes.c_size_t), ctypes.POINTER(ctypes.c_size_t), _ip, _ip]
+    L.gb_geometry_export.argtypes = [cfgp, ctypes.POINTER(GBGeometryHost)]
+    L.gb_ctx_create.argtypes = [cfgp, ctypes.POINTER(_vp)]
+    L.gb_ctx_destroy.argtypes = [_vp]
+    L.gb_set_stream.argtypes = [_vp, _vp]
+    L.gb_last_error.argtypes = [_vp, ctypes.c_char_p, ctypes.c_size_t]
+    L.gb_set_precomputed_quantities.argtypes = [_vp, fv, _c_double]
+    L.gb_remaining_tendency.argtypes = [_vp, fv, fv, _c_double]
+    L.gb_implicit_tendency.argtypes = [_vp, fv, fv, _c_double]
+    L.gb_update_jacobian.argtypes = [_vp, fv, _c_double, _c_double]
+    L.gb_ldiv.argtypes = [_vp, fv, fv]
+    L.gb_correct_implicit_advection_tendency.argtypes = [_vp, fv, fv, _c_double]
+    L.gb_dss.argtypes = [_vp, fv]
+    L.gb_step.argtypes = [_vp, fv, _c_double, _c_double, _c_int, _c_int]
+    L.gb_global_sums.argtypes = [_vp, fv, _dp]
+    L.gb_newton_residual.argtypes = [_vp, _dp]
+    L.gb_time_kernel.argtypes = [_vp, _c_int, fv, _c_int, _dp]
+    for s in SYMBOLS:
+        getattr(L, s).restype = _c_int
+    _lib = L
+    return L
+
+
+def make_config(cfg):
+    """gb_config from a gbdycore.config.DycoreConfig."""
+    import numpy as np
+    c = GBConfig()
+    c.h_elem, c.z_elem = cfg.h_elem, cfg.z_elem
+    c.ft_bytes = np.dtype(cfg.ft).itemsize
+    c.z_stretch = 1 if cfg.z_stretch else 0
+    c.z_max, c.dz_bottom, c.dt = cfg.z_max, cfg.dz_bottom, cfg.dt
+    c.nu_v, c.nu_s, c.div_damp = cfg.nu, cfg.nu_s, cfg.divergence_damping
+    c.sponge_zd, c.alpha_uh, c.alpha_w = cfg.sponge_zd, cfg.alpha_uh, cfg.alpha_w
+    c.upwinding = 1 if cfg.upwinding == "vanleer" else 0
+    for k, v in cfg.constants.items():
+        setattr(c, k, float(v))
+    return c

@@ -1,0 +1,284 @@
+"""Host-side mirror of the reference's API for the dry dynamical-core path.
+
+Names follow the reference (with Julia's ``!`` dropped):
+
+* ``AtmosSimulation`` / ``solve_atmos``  (src/simulation/AtmosSimulations.jl:307,
+  src/simulation/solve.jl:119; SYPD as in solve.jl:40-45),
+* the ClimaODEFunction hooks wired in src/simulation/integrator.jl:189-225:
+  ``remaining_tendency``, ``implicit_tendency``, ``update_jacobian``, ``ldiv``,
+  ``correct_implicit_advection_tendency``, ``dss``,
+  ``set_precomputed_quantities``,
+* ``ars343_step_via_hooks``: the ClimaTimeSteppers IMEX ARK stage loop
+  (ARS343, one Newton iteration, Jacobian refreshed every iteration)
+  expressed through those hooks.
+
+Every hook is one C-ABI call into libgbdycore.so on the GPU; state buffers
+are torch CUDA tensors in the layout of include/gbdycore.h.  PyTorch only
+provides device memory, streams and the elementwise stage algebra of the
+hook-level loop.
+"""
+import ctypes
+import time
+
+import numpy as np
+
+from . import _native as N
+from . import config as C
+from . import setups as S
+
+
+class Geometry:
+    """Host copy of the library's grid (gb_geometry_export; no GPU needed)."""
+
+    def __init__(self, cfg):
+        L = N.load()
+        c = N.make_config(cfg)
+        nc, nf = ctypes.c_size_t(), ctypes.c_size_t()
+        ng, ncp = ctypes.c_int(), ctypes.c_int()
+        _check(None, L.gb_sizes(ctypes.byref(c), ctypes.byref(nc), ctypes.byref(nf), ctypes.byref(ng), ctypes.byref(ncp)))
+        self.Nh, self.Nv = 6 * cfg.h_elem * cfg.h_elem, cfg.z_elem
+        self.R = float(cfg.constants["radius"])
+        H = self.Nh * 16
+        self.xyz = np.zeros((self.Nh, 16, 3))
+        self.ecov = np.zeros((self.Nh, 16, 2, 3))
+        self.Jh = np.zeros((self.Nh, 16))
+        self.gup = np.zeros((self.Nh, 16, 3))
+        self.fh0 = np.zeros((self.Nh, 16, 2))
+        self.zf = np.zeros(self.Nv + 1)
+        self.dss_off = np.zeros(ng.value + 1, np.int32)
+        self.dss_copy = np.zeros(ncp.value, np.int32)
+        g = N.GBGeometryHost()
+        dp = lambda a: a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+        ip = lambda a: a.ctypes.data_as(ctypes.POINTER(ctypes.c_int))
+        g.xyz, g.ecov, g.Jh, g.gup, g.fh0, g.zf = dp(self.xyz), dp(self.ecov), dp(self.Jh), dp(self.gup), dp(self.fh0), dp(self.zf)
+        g.dss_off, g.dss_copy = ip(self.dss_off), ip(self.dss_copy)
+        _check(None, L.gb_geometry_export(ctypes.byref(c), ctypes.byref(g)))
+        self.zc = 0.5 * (self.zf[1:] + self.zf[:-1])
+        self.n_center, self.n_face = nc.value, nf.value
+        assert H * 4 * self.Nv == self.n_center
+
+
+def _check(ctx, rc):
+    if rc != N.GB_OK:
+        msg = ""
+        if ctx:
+            buf = ctypes.create_string_buffer(512)
+            N.load().gb_last_error(ctx, buf, 512)
+            msg = buf.value.decode(errors="replace")
+        raise N.GBError(rc, msg or "call failed")
+
+
+class FieldVector:
+    """Device state: ``c`` [Nh,4,16,Nv] (rho, u_1, u_2, rho e_tot), ``f`` [Nh,16,Nv+1] (u_3)."""
+
+    def __init__(self, c, f):
+        self.c, self.f = c, f
+
+    @classmethod
+    def from_numpy(cls, Yc, Yf, device="cuda"):
+        import torch
+        return cls(torch.from_numpy(np.ascontiguousarray(Yc)).to(device), torch.from_numpy(np.ascontiguousarray(Yf)).to(device))
+
+    def similar(self):
+        import torch
+        return FieldVector(torch.zeros_like(self.c), torch.zeros_like(self.f))
+
+    def copy(self):
+        return FieldVector(self.c.clone(), self.f.clone())
+
+    def numpy(self):
+        return self.c.cpu().numpy(), self.f.cpu().numpy()
+
+    def gb(self):
+        assert self.c.is_contiguous() and self.f.is_contiguous()
+        return N.GBFieldVec(self.c.data_ptr(), self.f.data_ptr())
+
+    # elementwise algebra used by the hook-level stage loop
+    def axpy_(self, a, X):
+        self.c.add_(X.c, alpha=a)
+        self.f.add_(X.f, alpha=a)
+        return self
+
+    def assign_(self, X):
+        self.c.copy_(X.c)
+        self.f.copy_(X.f)
+        return self
+
+
+class AtmosCache:
+    """The library context (gb_ctx): geometry, Coriolis, DSS plan, scratch and
+    the Jacobian blocks, i.e. the parts of the reference's cache ``p``
+    (src/cache/cache.jl:165-305) that the hot path reads."""
+
+    def __init__(self, cfg, stream=None):
+        import torch
+        self.cfg = cfg
+        self.L = N.load()
+        self._c = N.make_config(cfg)
+        h = ctypes.c_void_p()
+        _check(None, self.L.gb_ctx_create(ctypes.byref(self._c), ctypes.byref(h)))
+        self.h = h
+        self.stream = stream if stream is not None else torch.cuda.current_stream()
+        _check(self.h, self.L.gb_set_stream(self.h, ctypes.c_void_p(self.stream.cuda_stream)))
+        self.dt = cfg.dt
+
+    def close(self):
+        if self.h:
+            self.L.gb_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def call(self, name, *args):
+        _check(self.h, getattr(self.L, name)(self.h, *args))
+
+    def global_sums(self, Y):
+        out = (ctypes.c_double * 2)()
+        self.call("gb_global_sums", Y.gb(), out)
+        return np.array(out[:])
+
+    def newton_residual(self):
+        out = (ctypes.c_double * 3)()
+        self.call("gb_newton_residual", out)
+        return np.array(out[:])
+
+
+class Jacobian:
+    """Handle of the Jacobian blocks, which live in the context (manual_sparse_jacobian.jl:603)."""
+
+    def __init__(self, p):
+        self.p = p
+
+
+# ---------------------------------------------------------------- hooks
+def set_precomputed_quantities(Y, p, t):
+    p.call("gb_set_precomputed_quantities", Y.gb(), float(t))
+
+
+def remaining_tendency(Yt, Yt_lim, Y, p, t):
+    p.call("gb_remaining_tendency", Yt.gb(), Y.gb(), float(t))
+    return Yt
+
+
+def implicit_tendency(Yt, Y, p, t):
+    p.call("gb_implicit_tendency", Yt.gb(), Y.gb(), float(t))
+
+
+def update_jacobian(jacobian, Y, p, dtgamma, t):
+    p.call("gb_update_jacobian", Y.gb(), float(dtgamma), float(t))
+
+
+def ldiv(dY, jacobian, R):
+    jacobian.p.call("gb_ldiv", dY.gb(), R.gb())
+
+
+def correct_implicit_advection_tendency(Yt, Y, p, t):
+    p.call("gb_correct_implicit_advection_tendency", Yt.gb(), Y.gb(), float(t))
+
+
+def dss(Y, p, t):
+    p.call("gb_dss", Y.gb())
+
+
+def ars343_tableau():
+    """Ascher, Ruuth & Spiteri (1997) ARS(3,4,3): (a_exp, a_imp, b_exp, b_imp)."""
+    g = 0.4358665215084590
+    a42 = a43 = 0.5529291480359398
+    b1 = -1.5 * g * g + 4 * g - 0.25
+    b2 = 1.5 * g * g - 5 * g + 1.25
+    a31 = (1 - 4.5 * g + 1.5 * g * g) * a42 + (2.75 - 10.5 * g + 3.75 * g * g) * a43 - 3.5 + 13 * g - 4.5 * g * g
+    a32 = (-1 + 4.5 * g - 1.5 * g * g) * a42 + (-2.75 + 10.5 * g - 3.75 * g * g) * a43 + 4 - 12.5 * g + 4.5 * g * g
+    ae = np.array([[0, 0, 0, 0], [g, 0, 0, 0], [a31, a32, 0, 0], [1 - a42 - a43, a42, a43, 0]])
+    ai = np.array([[0, 0, 0, 0], [0, g, 0, 0], [0, (1 - g) / 2, g, 0], [0, b1, b2, g]])
+    b = np.array([0, b1, b2, g])
+    return ae, ai, b, b.copy()
+
+
+def ars343_step_via_hooks(Y, p, t, dt, dss_first_stage=True):
+    """One ClimaTimeSteppers IMEX ARK step (ARS343, NewtonsMethod(max_iters=1))
+    driven through the hooks only, as CTS does (AtmosSimulations.jl:317-323)."""
+    ae, ai, be, bi = ars343_tableau()
+    jac = Jacobian(p)
+    Te = [Y.similar() for _ in range(4)]
+    Ti = [Y.similar() for _ in range(4)]
+    U, Uhat, R, dU, corr = Y.similar(), Y.similar(), Y.similar(), Y.similar(), Y.similar()
+    for i in range(4):
+        U.assign_(Y)
+        for j in range(i):
+            if ae[i, j]:
+                U.axpy_(dt * ae[i, j], Te[j])
+            if ai[i, j]:
+                U.axpy_(dt * ai[i, j], Ti[j])
+        if i > 0 or dss_first_stage:
+            dss(U, p, t)
+        if ai[i, i]:
+            dtg = dt * ai[i, i]
+            Uhat.assign_(U)
+            set_precomputed_quantities(U, p, t)           # cache_imp!
+            implicit_tendency(R, U, p, t)                  # R = U^ + dtg T_imp(U) - U
+            R.c.mul_(dtg).add_(Uhat.c).sub_(U.c)
+            R.f.mul_(dtg).add_(Uhat.f).sub_(U.f)
+            update_jacobian(jac, U, p, dtg, t)
+            ldiv(dU, jac, R)
+            U.axpy_(-1.0, dU)
+            set_precomputed_quantities(U, p, t)           # cache! after the solve
+            if p.cfg.upwinding == "vanleer":
+                correct_implicit_advection_tendency(corr, U, p, t)
+                U.axpy_(dtg, corr)
+            Ti[i].assign_(U).axpy_(-1.0, Uhat)
+            Ti[i].c.mul_(1.0 / dtg)
+            Ti[i].f.mul_(1.0 / dtg)
+        else:
+            set_precomputed_quantities(U, p, t)
+        remaining_tendency(Te[i], None, U, p, t)
+    for j in range(4):
+        if be[j]:
+            Y.axpy_(dt * be[j], Te[j])
+        if bi[j]:
+            Y.axpy_(dt * bi[j], Ti[j])
+    dss(Y, p, t + dt)
+    set_precomputed_quantities(Y, p, t + dt)
+    return Y
+
+
+def simulated_years_per_day(dt, seconds_per_step):
+    """SYPD = (dt / year) / (wall seconds per step / day)  (src/simulation/solve.jl:40-45)."""
+    return (dt / C.SECONDS_PER_YEAR) / (seconds_per_step / 86400.0)
+
+
+class AtmosSimulation:
+    """State + cache + time of one dry dynamical-core run on the GPU."""
+
+    def __init__(self, config, workload="plain", state=None, device="cuda"):
+        self.config = config
+        self.geometry = Geometry(config)
+        if state is None:
+            Yc, Yf = S.workload_state(self.geometry, config, workload)
+        else:
+            Yc, Yf = state
+        self.Y = FieldVector.from_numpy(np.asarray(Yc, dtype=config.ft), np.asarray(Yf, dtype=config.ft), device)
+        self.p = AtmosCache(config)
+        self.t = 0.0
+        self.dt = config.dt
+
+    def step(self, nsteps=1, use_graph=True):
+        self.p.call("gb_step", self.Y.gb(), float(self.t), float(self.dt), int(nsteps), 1 if use_graph else 0)
+        self.t += nsteps * self.dt
+
+
+def solve_atmos(sim, nsteps, use_graph=True):
+    """Warm-up step, then ``nsteps`` timed steps (solve.jl:119-149); returns timing and SYPD."""
+    import torch
+    sim.step(1, use_graph)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    sim.step(nsteps, use_graph)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    sps = wall / max(nsteps, 1)
+    return {"walltime": wall, "seconds_per_step": sps, "sypd": simulated_years_per_day(sim.dt, sps),
+            "ret_code": "success"}

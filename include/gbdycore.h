@@ -1,0 +1,139 @@
+/*
+ * gbdycore: C ABI of the GB300 (sm_103a) dry dynamical-core IMEX step.
+ *
+ * The library replaces the hot path of ClimaAtmos.jl's dry dynamical core:
+ * the hooks that ClimaTimeSteppers calls through the ClimaODEFunction built in
+ * src/simulation/integrator.jl:189-225, plus a fused, graph-captured ARS343
+ * step.  Every entry point returns GB_OK (0) or a negative gb_status; no C++
+ * exception crosses the ABI.  Device work is queued on the context's stream
+ * (gb_set_stream) and is asynchronous unless stated otherwise.  A context is
+ * not thread-safe (one host thread drives it, as in the reference).
+ *
+ * State layout (a FieldVector with fields c and f, precision set by
+ * gb_config.ft_bytes; ClimaCore's VIJFH order with Nq = 4, i fastest in a slab):
+ *   c : [Nh][4][16][Nv]   components (rho, u_1, u_2, rho e_tot); u_h covariant
+ *   f : [Nh][16][Nv + 1]  covariant u_3
+ * with node n = i + 4 j and elements ordered panel-major, row-major within a
+ * panel (gb_geometry_export gives node positions for remapping).
+ * All pointers in gb_fieldvec are device pointers (e.g. CuArray / torch
+ * tensors), 16-byte aligned.
+ */
+#ifndef GBDYCORE_H
+#define GBDYCORE_H
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct gb_ctx gb_ctx;
+
+enum gb_status {
+  GB_OK = 0,
+  GB_ERR_ARG = -1,        /* invalid argument or configuration */
+  GB_ERR_CUDA = -2,       /* a CUDA runtime call failed */
+  GB_ERR_NOMEM = -3,      /* device allocation failed */
+  GB_ERR_NONFINITE = -4,  /* a NaN/Inf was detected in the Newton residual */
+  GB_ERR_TIMEOUT = -5,    /* a bounded device wait gave up */
+  GB_ERR_STATE = -6       /* call out of order (e.g. ldiv before update_jacobian) */
+};
+
+typedef struct {
+  int h_elem;        /* elements per cubed-sphere panel edge (SphereGrid h_elem) */
+  int z_elem;        /* vertical levels (centres) */
+  int ft_bytes;      /* 4 = Float32, 8 = Float64 */
+  int z_stretch;     /* 0 uniform, 1 hyperbolic-tangent stretching (grids.jl:356) */
+  double z_max, dz_bottom;
+  double dt;         /* model time step: van Leer Courant factor (implicit_tendency.jl:131-139) */
+  double nu_v, nu_s; /* hyperdiffusivities nu_4_vorticity, nu_4_scalar (hyperdiffusion.jl:21-28) */
+  double div_damp;   /* divergence_damping_factor */
+  double sponge_zd, alpha_uh, alpha_w; /* Rayleigh sponge (rayleigh_sponge.jl:7-57); alpha = 0: off */
+  int upwinding;     /* energy_q_tot_upwinding: 0 none, 1 van Leer (types.jl:1916) */
+  /* physical constants (ClimaParams names) */
+  double grav, omega, R_d, cp_d, cv_d, T_0, p_ref, T_min_ref, T_surf_ref, T_min_sgs, radius;
+} gb_config;
+
+typedef struct {
+  void *c; /* centre block, see above */
+  void *f; /* face block */
+} gb_fieldvec;
+
+/* Host-side geometry export (no GPU needed); any pointer may be NULL. */
+typedef struct {
+  double *xyz;   /* [Nh*16*3] unit-sphere node positions */
+  double *ecov;  /* [Nh*16*2*3] covariant basis dX/dxi^i at radius R, Cartesian */
+  double *Jh;    /* [Nh*16] horizontal Jacobian at radius R */
+  double *gup;   /* [Nh*16*3] g^11, g^12, g^22 at radius R */
+  double *fh0;   /* [Nh*16*2] contravariant 2*Omega*cos(lat)*north at radius R */
+  double *zf;    /* [Nv+1] face heights */
+  int *dss_off;  /* [ngroups+1] */
+  int *dss_copy; /* [ncopies] element*16 + node, ascending within a group */
+} gb_geometry_host;
+
+/* Sizes for a configuration (no GPU needed). */
+int gb_sizes(const gb_config *cfg, size_t *n_center, size_t *n_face, int *n_dss_groups, int *n_dss_copies);
+int gb_geometry_export(const gb_config *cfg, gb_geometry_host *out);
+
+/* Context lifetime.  Replaces the library-owned parts of AtmosCache
+ * (src/cache/cache.jl:165-305: geometry, Coriolis, DSS buffers, scratch) and
+ * the Jacobian cache (manual_sparse_jacobian.jl:603). */
+int gb_ctx_create(const gb_config *cfg, gb_ctx **out);
+int gb_ctx_destroy(gb_ctx *ctx);
+int gb_set_stream(gb_ctx *ctx, void *cuda_stream);
+/* Copies the last error message; returns the last gb_status. */
+int gb_last_error(gb_ctx *ctx, char *buf, size_t len);
+
+/* set_precomputed_quantities!(Y, p, t)  src/cache/precomputed_quantities.jl:928
+ * Applies the impenetrable-boundary filter to Y.f (u^3 = 0 at the bottom and
+ * top faces); the other precomputed quantities are recomputed inside each
+ * kernel from Y. */
+int gb_set_precomputed_quantities(gb_ctx *ctx, gb_fieldvec Y, double t);
+
+/* remaining_tendency!(Yt, Yt_lim, Y, p, t)  src/prognostic_equations/remaining_tendency.jl:48
+ * (Yt_lim is empty for the dry model). */
+int gb_remaining_tendency(gb_ctx *ctx, gb_fieldvec Yt, gb_fieldvec Y, double t);
+
+/* implicit_tendency!(Yt, Y, p, t)  src/prognostic_equations/implicit/implicit_tendency.jl:36 */
+int gb_implicit_tendency(gb_ctx *ctx, gb_fieldvec Yt, gb_fieldvec Y, double t);
+
+/* update_jacobian!(jacobian, Y, p, dtgamma, t)  src/prognostic_equations/implicit/jacobian.jl:74
+ * -> manual_sparse_jacobian.jl:713-870; the blocks are kept in the context. */
+int gb_update_jacobian(gb_ctx *ctx, gb_fieldvec Y, double dtgamma, double t);
+
+/* LinearAlgebra.ldiv!(dY, jacobian, R)  src/prognostic_equations/implicit/jacobian.jl:78-82
+ * (BlockArrowheadSolve, manual_sparse_jacobian.jl:580-583). */
+int gb_ldiv(gb_ctx *ctx, gb_fieldvec dY, gb_fieldvec R);
+
+/* correct_implicit_advection_tendency!(Yt, Y, p, t)  implicit_tendency.jl:322-339 */
+int gb_correct_implicit_advection_tendency(gb_ctx *ctx, gb_fieldvec Yt, gb_fieldvec Y, double t);
+
+/* dss!(Y, p, t)  src/prognostic_equations/constrain_state.jl:59-64 */
+int gb_dss(gb_ctx *ctx, gb_fieldvec Y);
+
+/* One or more fused ARS343 steps with one Newton iteration per implicit stage
+ * (the ClimaTimeSteppers stage loop driven by solve_atmos!,
+ * src/simulation/solve.jl:57-63).  use_graph = 1 replays a captured CUDA
+ * graph of the whole step. */
+int gb_step(gb_ctx *ctx, gb_fieldvec Y, double t, double dt, int nsteps, int use_graph);
+
+/* Global integrals of rho and rho e_tot (sum of value * WJ), compensated FP64,
+ * as check_conservation does (src/simulation/solve.jl:216-265).  Synchronous. */
+int gb_global_sums(gb_ctx *ctx, gb_fieldvec Y, double out[2]);
+
+/* FP64 sums of squares of the Newton residual of the last gb_step (rho,
+ * rho e_tot, u_3 parts, summed over stages); synchronous. */
+int gb_newton_residual(gb_ctx *ctx, double out[3]);
+
+/* Measurement support (no counterpart in the reference): launches one of the
+ * step's kernels `reps` times on the context stream between CUDA events and
+ * returns the mean time per launch in milliseconds.  kernel: 0 pass A
+ * (Laplacians), 1 pass B (explicit tendency), 2 column stage (stage 4: five
+ * sources), 3 state DSS, 4 final combination.  Y is read (and, for 3/4,
+ * written); synchronous. */
+enum gb_kernel_id { GB_K_PASSA = 0, GB_K_PASSB = 1, GB_K_COLUMN = 2, GB_K_DSS = 3, GB_K_FINAL = 4 };
+int gb_time_kernel(gb_ctx *ctx, int kernel, gb_fieldvec Y, int reps, double *ms_per_launch);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,1017 @@
+// CPU ORACLE for the ClimaAtmos dry dynamical-core IMEX step.
+//
+// TEST INFRASTRUCTURE ONLY: the parity tests, __graft_entry__.smoke() and the
+// CPU-baseline leg of bench.py use this file as the checker and as the timed
+// CPU port.  Nothing in the product library links or calls it.
+//
+// Parity status: the reference's arithmetic lives in ClimaCore 0.15.1,
+// ClimaTimeSteppers 0.10.6 and Thermodynamics 1.3.0 (pinned in
+// .buildkite/Manifest-v1.11.toml, not vendored) and no Julia toolchain exists
+// here, so this restatement is pinned by the reference's own invariants
+// (sponge known answers, impenetrable-boundary filter, post-Newton identity,
+// mass/energy conservation, Jacobian vs finite differences) and NOT by
+// ClimaCore outputs: parity with ClimaCore itself is unpinned.
+//
+// The code follows the reference statement by statement, as full-field
+// operations, in the order the reference issues them:
+//   remaining_tendency!            src/prognostic_equations/remaining_tendency.jl:48-58
+//   horizontal_dynamics_tendency!  src/prognostic_equations/advection.jl:36-91
+//   prep/apply hyperdiffusion      src/prognostic_equations/hyperdiffusion.jl:116-147, 247-307
+//   explicit_vertical_advection!   src/prognostic_equations/advection.jl:205-290 (deep branch)
+//   Rayleigh sponge                src/parameterized_tendencies/sponge/rayleigh_sponge.jl:7-57
+//   implicit tendency              src/prognostic_equations/implicit/implicit_tendency.jl:185-298
+//   post-Newton correction         src/prognostic_equations/implicit/implicit_tendency.jl:322-339
+//   Jacobian blocks                src/prognostic_equations/implicit/manual_sparse_jacobian.jl:713-870
+//   BlockArrowheadSolve (dry)      src/prognostic_equations/implicit/manual_sparse_jacobian.jl:580-583
+//   precomputed quantities         src/cache/precomputed_quantities.jl:473-571, 698-831
+//   kinetic energy                 src/utils/utilities.jl:194-206
+//   reference state                src/utils/refstate_thermodynamics.jl:58-166
+//   operators and their BCs        src/utils/abbreviations.jl:72-290
+// Operators are restated from docs/src/discretization.md:60-420 and the
+// spectral-element weak/strong forms (Taylor & Fournier 2010); ARS343 is the
+// Ascher-Ruuth-Spiteri (1997) (3,4,3) tableau; the van Leer face
+// reconstruction is Lin et al. (1994) with their monotonicity constraint.
+//
+// Layout (same as the product's C-ABI): centre block [elem][comp][node][level]
+// with comp = (rho, u_1, u_2, rho e_tot); face block [elem][node][face].
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+#include <algorithm>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+extern "C" {
+struct OracleParams {
+  double grav, omega, R_d, cp_d, cv_d, T_0, p_ref, T_min_ref, T_surf_ref, T_min_sgs, radius;
+  double nu_v, nu_s, div_damp;
+  double sponge_zd, alpha_uh, alpha_w;
+  double z_max;
+  double dt_model;  // the model time step used by the van Leer Courant factor
+  int upwinding;    // 0: central only (no post-Newton correction), 1: van Leer
+  int dss_stage1;   // 1: DSS the first stage as well (ClimaTimeSteppers does)
+};
+struct OracleGeom {
+  int Nh, Nv, ngroups;
+  const double *W, *D, *Jh, *gup, *gdn, *sinlat, *fh0, *ecov, *econ, *zf;
+  const int *dss_off, *dss_copy;
+  const double *dss_w;
+};
+}
+
+namespace {
+
+constexpr int NQ = 4, NN = 16;
+
+template <class FT>
+struct Oracle {
+  int Nh, Nv, Nf;
+  // parameters
+  FT grav, omega, Rd, cpd, cvd, T0, pref, Tmin_ref, Tsfc_ref, Tmin_sgs, R;
+  FT nu_v, nu_s, div_damp, zd, a_uh, a_w, zmax, dt_model, kappa;
+  int upwinding, dss_stage1;
+  // geometry
+  FT W[NN], D[NQ][NQ];
+  std::vector<FT> Jh, gup, gdn, sinlat, fh0, ecov, econ;
+  std::vector<FT> zf, zc, dzc, dzf, rc, rf;
+  std::vector<int> goff, gcopy;
+  std::vector<FT> gw;
+
+  size_t ncen() const { return (size_t)Nh * 4 * NN * Nv; }
+  size_t nfac() const { return (size_t)Nh * NN * Nf; }
+  size_t npt() const { return (size_t)Nh * NN * Nv; }
+  size_t ci(int e, int c, int n, int v) const { return (((size_t)e * 4 + c) * NN + n) * Nv + v; }
+  size_t fi(int e, int n, int k) const { return ((size_t)e * NN + n) * Nf + k; }
+  size_t pi(int e, int n, int v) const { return ((size_t)e * NN + n) * Nv + v; }
+  size_t hn(int e, int n) const { return (size_t)e * NN + n; }
+
+  // ---- pointwise geometry ----
+  FT Jc(int e, int n, int v) const { return Jh[hn(e, n)] * rc[v] * rc[v] * dzc[v]; }
+  FT Jfc(int e, int n, int k) const { return Jh[hn(e, n)] * rf[k] * rf[k] * dzf[k]; }
+  FT gu(int e, int n, int c, FT r) const { return gup[hn(e, n) * 3 + c] / (r * r); }
+  FT gd(int e, int n, int c, FT r) const { return gdn[hn(e, n) * 3 + c] * (r * r); }
+
+  // ---- thermodynamics (Thermodynamics.jl dry air; e_int = cv_d (T - T_0) - R_d T_0) ----
+  FT exner(FT p) const { return std::pow(p / pref, kappa); }
+  FT T_ref(FT Pi) const { return Tmin_ref + (Tsfc_ref - Tmin_ref) * std::pow(Pi, FT(7)); }
+  FT phi_r(FT Pi) const {
+    return -cpd * (Tmin_ref * std::log(Pi) + (Tsfc_ref - Tmin_ref) / FT(7) * (std::pow(Pi, FT(7)) - FT(1)));
+  }
+  FT sd_r(FT Pi) const { return cpd * (T_ref(Pi) - T0) + phi_r(Pi); }
+  FT beta_sponge(FT z, FT alpha) const {
+    if (!(z > zd) || alpha == FT(0)) return FT(0);
+    FT s = std::sin(FT(M_PI) * (z - zd) / (zmax - zd) / FT(2));
+    return alpha * s * s;
+  }
+
+  // ---- precomputed quantities (set_implicit_precomputed_quantities!) ----
+  struct Pre {
+    std::vector<FT> ub3, K, T, p, h, Pi, thv, thvr, phir, uc1, uc2, u3c;  // u3c = contravariant u^3 at faces
+  } pre;
+
+  void alloc_pre() {
+    size_t P = npt();
+    for (auto *v : {&pre.ub3, &pre.K, &pre.T, &pre.p, &pre.h, &pre.Pi, &pre.thv, &pre.thvr, &pre.phir, &pre.uc1, &pre.uc2})
+      v->assign(P, FT(0));
+    pre.u3c.assign(nfac(), FT(0));
+  }
+
+  // impenetrable-boundary filter: u_3 = -u_h^3 / g^33 at the bottom and top
+  // faces; without topography u_h^3 = 0 (precomputed_quantities.jl:486-553).
+  void bc_filter(FT *Yf) const {
+#pragma omp parallel for
+    for (int e = 0; e < Nh; ++e)
+      for (int n = 0; n < NN; ++n) {
+        Yf[fi(e, n, 0)] = FT(0);
+        Yf[fi(e, n, Nv)] = FT(0);
+      }
+  }
+
+  void set_precomputed(FT *Yc, FT *Yf) {
+    bc_filter(Yf);
+#pragma omp parallel for
+    for (int e = 0; e < Nh; ++e)
+      for (int n = 0; n < NN; ++n) {
+        for (int k = 0; k < Nf; ++k) pre.u3c[fi(e, n, k)] = Yf[fi(e, n, k)] / (dzf[k] * dzf[k]);
+        for (int v = 0; v < Nv; ++v) {
+          size_t q = pi(e, n, v);
+          FT rho = Yc[ci(e, 0, n, v)], u1 = Yc[ci(e, 1, n, v)], u2 = Yc[ci(e, 2, n, v)], rhoe = Yc[ci(e, 3, n, v)];
+          FT r = rc[v];
+          FT c1 = gu(e, n, 0, r) * u1 + gu(e, n, 1, r) * u2;
+          FT c2 = gu(e, n, 1, r) * u1 + gu(e, n, 2, r) * u2;
+          FT a = Yf[fi(e, n, v)], b = Yf[fi(e, n, v + 1)];
+          pre.uc1[q] = c1;
+          pre.uc2[q] = c2;
+          pre.ub3[q] = (a + b) / FT(2);
+          // K = 1/2 (u_h . u_h + I^c(u_3 u^3) + 2 u_h^3 I^c(u_3)); u_h^3 = 0 here
+          FT kv = (a * pre.u3c[fi(e, n, v)] + b * pre.u3c[fi(e, n, v + 1)]) / FT(2);
+          FT K = (u1 * c1 + u2 * c2 + kv) / FT(2);
+          pre.K[q] = K;
+          FT Phi = grav * zc[v];
+          FT eint = rhoe / rho - K - Phi;
+          FT T = std::max(Tmin_sgs, T0 + (eint + Rd * T0) / cvd);
+          FT p = rho * Rd * T;
+          FT Pi = exner(p);
+          pre.T[q] = T;
+          pre.p[q] = p;
+          pre.h[q] = rhoe / rho + Rd * T;
+          pre.Pi[q] = Pi;
+          pre.thv[q] = T / Pi;
+          pre.thvr[q] = T_ref(Pi) / Pi;
+          pre.phir[q] = phi_r(Pi);
+        }
+      }
+  }
+
+  // ---- spectral-element operators on one (element, level) slab ----
+  // d1 f[i,j] = sum_k D[i][k] f[k,j]; d2 f[i,j] = sum_k D[j][k] f[i,k]
+  void d1(const FT *f, FT *o) const {
+    for (int j = 0; j < NQ; ++j)
+      for (int i = 0; i < NQ; ++i) {
+        FT s = 0;
+        for (int k = 0; k < NQ; ++k) s += D[i][k] * f[k + NQ * j];
+        o[i + NQ * j] = s;
+      }
+  }
+  void d2(const FT *f, FT *o) const {
+    for (int j = 0; j < NQ; ++j)
+      for (int i = 0; i < NQ; ++i) {
+        FT s = 0;
+        for (int k = 0; k < NQ; ++k) s += D[j][k] * f[i + NQ * k];
+        o[i + NQ * j] = s;
+      }
+  }
+  // transposes: t1 f[i,j] = sum_k D[k][i] f[k,j]; t2 f[i,j] = sum_k D[k][j] f[i,k]
+  void t1(const FT *f, FT *o) const {
+    for (int j = 0; j < NQ; ++j)
+      for (int i = 0; i < NQ; ++i) {
+        FT s = 0;
+        for (int k = 0; k < NQ; ++k) s += D[k][i] * f[k + NQ * j];
+        o[i + NQ * j] = s;
+      }
+  }
+  void t2(const FT *f, FT *o) const {
+    for (int j = 0; j < NQ; ++j)
+      for (int i = 0; i < NQ; ++i) {
+        FT s = 0;
+        for (int k = 0; k < NQ; ++k) s += D[k][j] * f[i + NQ * k];
+        o[i + NQ * j] = s;
+      }
+  }
+  struct Slab {  // geometry of one slab
+    FT J[NN], WJ[NN], gu0[NN], gu1[NN], gu2[NN], gd0[NN], gd1[NN], gd2[NN], g33, G33;
+  };
+  void slab(int e, FT r, FT dz, Slab &s) const {
+    for (int n = 0; n < NN; ++n) {
+      s.J[n] = Jh[hn(e, n)] * r * r * dz;
+      s.WJ[n] = W[n] * s.J[n];
+      s.gu0[n] = gu(e, n, 0, r); s.gu1[n] = gu(e, n, 1, r); s.gu2[n] = gu(e, n, 2, r);
+      s.gd0[n] = gd(e, n, 0, r); s.gd1[n] = gd(e, n, 1, r); s.gd2[n] = gd(e, n, 2, r);
+    }
+    s.g33 = FT(1) / (dz * dz);
+    s.G33 = dz * dz;
+  }
+  // strong divergence of contravariant (F1, F2): (1/J) d_i (J F^i)
+  void div_h(const Slab &s, const FT *F1, const FT *F2, FT *o) const {
+    FT a[NN], b[NN], da[NN], db[NN];
+    for (int n = 0; n < NN; ++n) { a[n] = s.J[n] * F1[n]; b[n] = s.J[n] * F2[n]; }
+    d1(a, da); d2(b, db);
+    for (int n = 0; n < NN; ++n) o[n] = (da[n] + db[n]) / s.J[n];
+  }
+  // weak divergence: -(1/WJ) sum D^T (WJ F)
+  void wdiv_h(const Slab &s, const FT *F1, const FT *F2, FT *o) const {
+    FT a[NN], b[NN], da[NN], db[NN];
+    for (int n = 0; n < NN; ++n) { a[n] = s.WJ[n] * F1[n]; b[n] = s.WJ[n] * F2[n]; }
+    t1(a, da); t2(b, db);
+    for (int n = 0; n < NN; ++n) o[n] = -(da[n] + db[n]) / s.WJ[n];
+  }
+  // strong gradient (covariant components)
+  void grad_h(const FT *f, FT *o1, FT *o2) const { d1(f, o1); d2(f, o2); }
+  // weak gradient (covariant components): -(1/W) sum D^T (W f)
+  void wgrad_h(const FT *f, FT *o1, FT *o2) const {
+    FT a[NN], da[NN], db[NN];
+    for (int n = 0; n < NN; ++n) a[n] = W[n] * f[n];
+    t1(a, da); t2(a, db);
+    for (int n = 0; n < NN; ++n) { o1[n] = -da[n] / W[n]; o2[n] = -db[n] / W[n]; }
+  }
+  // strong curl of a covariant (c1, c2, c3): contravariant result
+  void curl_h(const Slab &s, const FT *c1, const FT *c2, const FT *c3, FT *o1, FT *o2, FT *o3) const {
+    FT a[NN], b[NN];
+    d1(c2, a); d2(c1, b);
+    for (int n = 0; n < NN; ++n) o3[n] = (a[n] - b[n]) / s.J[n];
+    if (c3) {
+      d2(c3, a); d1(c3, b);
+      for (int n = 0; n < NN; ++n) { o1[n] = a[n] / s.J[n]; o2[n] = -b[n] / s.J[n]; }
+    }
+  }
+  // weak curl of a covariant (c1, c2, c3): contravariant result
+  void wcurl_h(const Slab &s, const FT *c1, const FT *c2, const FT *c3, FT *o1, FT *o2, FT *o3) const {
+    FT a[NN], b[NN], ta[NN], tb[NN];
+    if (c1 && c2) {
+      for (int n = 0; n < NN; ++n) { a[n] = W[n] * c2[n]; b[n] = W[n] * c1[n]; }
+      t1(a, ta); t2(b, tb);
+      for (int n = 0; n < NN; ++n) o3[n] = (-ta[n] + tb[n]) / s.WJ[n];
+    }
+    if (c3) {
+      for (int n = 0; n < NN; ++n) a[n] = W[n] * c3[n];
+      t2(a, tb); t1(a, ta);
+      for (int n = 0; n < NN; ++n) { o1[n] = -tb[n] / s.WJ[n]; o2[n] = ta[n] / s.WJ[n]; }
+    }
+  }
+
+  // ---- vector Laplacian  L(u) = C123(wgrad(div u)) * fdiv - C123(wcurl(C123(curl u))) ----
+  // input covariant (c1, c2, c3) on the slab; output covariant (o1, o2, o3)
+  void vec_lap(const Slab &s, const FT *c1, const FT *c2, const FT *c3, FT fdiv, FT *o1, FT *o2, FT *o3) const {
+    FT F1[NN], F2[NN], dv[NN], w1[NN], w2[NN];
+    for (int n = 0; n < NN; ++n) {
+      F1[n] = s.gu0[n] * c1[n] + s.gu1[n] * c2[n];
+      F2[n] = s.gu1[n] * c1[n] + s.gu2[n] * c2[n];
+    }
+    div_h(s, F1, F2, dv);
+    wgrad_h(dv, w1, w2);
+    FT k1[NN], k2[NN], k3[NN];
+    curl_h(s, c1, c2, c3, k1, k2, k3);
+    FT z1[NN], z2[NN], z3[NN];
+    for (int n = 0; n < NN; ++n) {  // C123 of the contravariant curl
+      z1[n] = s.gd0[n] * k1[n] + s.gd1[n] * k2[n];
+      z2[n] = s.gd1[n] * k1[n] + s.gd2[n] * k2[n];
+      z3[n] = s.G33 * k3[n];
+    }
+    FT q1[NN], q2[NN], q3[NN];
+    wcurl_h(s, z1, z2, z3, q1, q2, q3);
+    for (int n = 0; n < NN; ++n) {
+      o1[n] = fdiv * w1[n] - (s.gd0[n] * q1[n] + s.gd1[n] * q2[n]);
+      o2[n] = fdiv * w2[n] - (s.gd1[n] * q1[n] + s.gd2[n] * q2[n]);
+      o3[n] = -s.G33 * q3[n];
+    }
+  }
+
+  // ---- DSS (Spaces.weighted_dss!): J-weighted average over collocated nodes; the
+  // covariant horizontal vector (comps 1, 2 of a centre block) is averaged in
+  // Cartesian components.  Centre block comps: 0 scalar, 1-2 vector, 3 scalar.
+  void dss_center(FT *C, int levels) const {
+    int G = (int)goff.size() - 1;
+#pragma omp parallel for
+    for (int g = 0; g < G; ++g) {
+      for (int v = 0; v < levels; ++v) {
+        FT s0 = 0, s3 = 0, X[3] = {0, 0, 0};
+        for (int c = goff[g]; c < goff[g + 1]; ++c) {
+          int idx = gcopy[c], e = idx / NN, n = idx % NN;
+          FT w = gw[c];
+          s0 += w * C[ci(e, 0, n, v)];
+          s3 += w * C[ci(e, 3, n, v)];
+          FT u1 = C[ci(e, 1, n, v)], u2 = C[ci(e, 2, n, v)];
+          const FT *ec = &econ[hn(e, n) * 6];
+          for (int d = 0; d < 3; ++d) X[d] += w * (u1 * ec[d] + u2 * ec[3 + d]);
+        }
+        for (int c = goff[g]; c < goff[g + 1]; ++c) {
+          int idx = gcopy[c], e = idx / NN, n = idx % NN;
+          C[ci(e, 0, n, v)] = s0;
+          C[ci(e, 3, n, v)] = s3;
+          const FT *eo = &ecov[hn(e, n) * 6];
+          C[ci(e, 1, n, v)] = eo[0] * X[0] + eo[1] * X[1] + eo[2] * X[2];
+          C[ci(e, 2, n, v)] = eo[3] * X[0] + eo[4] * X[1] + eo[5] * X[2];
+        }
+      }
+    }
+  }
+  void dss_face(FT *F) const {
+    int G = (int)goff.size() - 1;
+#pragma omp parallel for
+    for (int g = 0; g < G; ++g)
+      for (int k = 0; k < Nf; ++k) {
+        FT s = 0;
+        for (int c = goff[g]; c < goff[g + 1]; ++c) {
+          int idx = gcopy[c];
+          s += gw[c] * F[fi(idx / NN, idx % NN, k)];
+        }
+        for (int c = goff[g]; c < goff[g + 1]; ++c) {
+          int idx = gcopy[c];
+          F[fi(idx / NN, idx % NN, k)] = s;
+        }
+      }
+  }
+  void dss(FT *Yc, FT *Yf) const { dss_center(Yc, Nv); dss_face(Yf); }
+
+  // ---- remaining_tendency! ----
+  std::vector<FT> Lap;  // [e][4][n][v]: (Ls, L1, L2, L3) so comps 1-2 are the C12 vector
+  void remaining_tendency(FT *Tc, FT *Tf, const FT *Yc, const FT *Yf) {
+    std::fill(Tc, Tc + ncen(), FT(0));
+    std::fill(Tf, Tf + nfac(), FT(0));
+    Lap.assign(ncen(), FT(0));
+    // horizontal_dynamics_tendency! + prep_hyperdiffusion_tendency! (element-local)
+#pragma omp parallel for
+    for (int e = 0; e < Nh; ++e) {
+      Slab s;
+      for (int v = 0; v < Nv; ++v) {
+        slab(e, rc[v], dzc[v], s);
+        FT rho[NN], F1[NN], F2[NN], h[NN], tmp[NN], a1[NN], a2[NN], u1[NN], u2[NN], u3[NN];
+        for (int n = 0; n < NN; ++n) {
+          size_t q = pi(e, n, v);
+          rho[n] = Yc[ci(e, 0, n, v)];
+          u1[n] = Yc[ci(e, 1, n, v)]; u2[n] = Yc[ci(e, 2, n, v)]; u3[n] = pre.ub3[q];
+          F1[n] = rho[n] * pre.uc1[q]; F2[n] = rho[n] * pre.uc2[q];
+          h[n] = pre.h[q];
+        }
+        // Yt.rho -= split_div(rho u, 1) = wdiv(rho u)
+        FT dm[NN];
+        wdiv_h(s, F1, F2, dm);
+        for (int n = 0; n < NN; ++n) Tc[ci(e, 0, n, v)] -= dm[n];
+        // Yt.rhoe -= split_div(rho u, h) = 1/2 wdiv(rho u h) + 1/2 (h wdiv(rho u) + rho u . grad h)
+        FT G1[NN], G2[NN], dmh[NN];
+        for (int n = 0; n < NN; ++n) { G1[n] = F1[n] * h[n]; G2[n] = F2[n] * h[n]; }
+        wdiv_h(s, G1, G2, dmh);
+        grad_h(h, a1, a2);
+        for (int n = 0; n < NN; ++n)
+          Tc[ci(e, 3, n, v)] -= (dmh[n] + h[n] * dm[n] + F1[n] * a1[n] + F2[n] * a2[n]) / FT(2);
+        // Yt.u_h -= grad(K + Phi - Phi_r) + cp_d (th' grad Pi + grad(th' Pi) - Pi grad th') / 2
+        FT Pi[NN], thp[NN], b1[NN], b2[NN], c1[NN], c2[NN], d1_[NN], d2_[NN];
+        for (int n = 0; n < NN; ++n) {
+          size_t q = pi(e, n, v);
+          tmp[n] = pre.K[q] + grav * zc[v] - pre.phir[q];
+          Pi[n] = pre.Pi[q];
+          thp[n] = pre.thv[q] - pre.thvr[q];
+        }
+        grad_h(tmp, a1, a2);
+        grad_h(Pi, b1, b2);
+        FT tp[NN];
+        for (int n = 0; n < NN; ++n) tp[n] = thp[n] * Pi[n];
+        grad_h(tp, c1, c2);
+        grad_h(thp, d1_, d2_);
+        for (int n = 0; n < NN; ++n) {
+          Tc[ci(e, 1, n, v)] -= a1[n] + cpd * (thp[n] * b1[n] + c1[n] - Pi[n] * d1_[n]) / FT(2);
+          Tc[ci(e, 2, n, v)] -= a2[n] + cpd * (thp[n] * b2[n] + c2[n] - Pi[n] * d2_[n]) / FT(2);
+        }
+        // prep hyperdiffusion: grad/curl Laplacian of u_bar, scalar Laplacian of s_d - s_d,r
+        FT o1[NN], o2[NN], o3[NN];
+        vec_lap(s, u1, u2, u3, FT(1), o1, o2, o3);
+        FT sd[NN], g1[NN], g2[NN], Ls[NN];
+        for (int n = 0; n < NN; ++n) {
+          size_t q = pi(e, n, v);
+          sd[n] = cpd * (pre.T[q] - T0) + grav * zc[v] - sd_r(pre.Pi[q]);
+        }
+        grad_h(sd, g1, g2);
+        for (int n = 0; n < NN; ++n) {
+          FT x1 = s.gu0[n] * g1[n] + s.gu1[n] * g2[n], x2 = s.gu1[n] * g1[n] + s.gu2[n] * g2[n];
+          g1[n] = x1; g2[n] = x2;
+        }
+        wdiv_h(s, g1, g2, Ls);
+        for (int n = 0; n < NN; ++n) {
+          Lap[ci(e, 0, n, v)] = Ls[n];
+          Lap[ci(e, 1, n, v)] = o1[n];
+          Lap[ci(e, 2, n, v)] = o2[n];
+          Lap[ci(e, 3, n, v)] = o3[n];
+        }
+      }
+    }
+    // weighted_dss! of the Laplacians (remaining_tendency.jl:18-21)
+    dss_center(Lap.data(), Nv);
+    // apply_hyperdiffusion_tendency!
+    std::vector<FT> L4u3(npt());
+#pragma omp parallel for
+    for (int e = 0; e < Nh; ++e) {
+      Slab s;
+      for (int v = 0; v < Nv; ++v) {
+        slab(e, rc[v], dzc[v], s);
+        FT l1[NN], l2[NN], l3[NN], ls[NN], o1[NN], o2[NN], o3[NN];
+        for (int n = 0; n < NN; ++n) {
+          ls[n] = Lap[ci(e, 0, n, v)]; l1[n] = Lap[ci(e, 1, n, v)];
+          l2[n] = Lap[ci(e, 2, n, v)]; l3[n] = Lap[ci(e, 3, n, v)];
+        }
+        vec_lap(s, l1, l2, l3, div_damp, o1, o2, o3);
+        FT g1[NN], g2[NN], hd[NN];
+        grad_h(ls, g1, g2);
+        for (int n = 0; n < NN; ++n) {
+          FT rho = Yc[ci(e, 0, n, v)];
+          FT x1 = s.gu0[n] * g1[n] + s.gu1[n] * g2[n], x2 = s.gu1[n] * g1[n] + s.gu2[n] * g2[n];
+          g1[n] = rho * x1; g2[n] = rho * x2;
+        }
+        wdiv_h(s, g1, g2, hd);
+        for (int n = 0; n < NN; ++n) {
+          Tc[ci(e, 1, n, v)] -= nu_v * o1[n];
+          Tc[ci(e, 2, n, v)] -= nu_v * o2[n];
+          Tc[ci(e, 3, n, v)] -= nu_s * hd[n];
+          L4u3[pi(e, n, v)] = o3[n];
+        }
+      }
+    }
+    // Yt.u3 -= nu ᶠwinterp(ᶜJ ρ, C3(∇⁴u))  (extrapolated at the boundary faces)
+#pragma omp parallel for
+    for (int e = 0; e < Nh; ++e)
+      for (int n = 0; n < NN; ++n) {
+        for (int k = 0; k < Nf; ++k) {
+          FT val;
+          if (k == 0) val = L4u3[pi(e, n, 0)];
+          else if (k == Nv) val = L4u3[pi(e, n, Nv - 1)];
+          else {
+            FT wa = Jc(e, n, k - 1) * Yc[ci(e, 0, n, k - 1)], wb = Jc(e, n, k) * Yc[ci(e, 0, n, k)];
+            val = (wa * L4u3[pi(e, n, k - 1)] + wb * L4u3[pi(e, n, k)]) / (wa + wb);
+          }
+          Tf[fi(e, n, k)] -= nu_v * val;
+        }
+      }
+    // explicit_vertical_advection_tendency! (deep atmosphere)
+    std::vector<FT> om3(npt()), fo1(nfac()), fo2(nfac());
+#pragma omp parallel for
+    for (int e = 0; e < Nh; ++e) {
+      Slab s;
+      for (int v = 0; v < Nv; ++v) {  // ᶜω³ = wcurl(u_h)
+        slab(e, rc[v], dzc[v], s);
+        FT u1[NN], u2[NN], o1[NN], o2[NN], o3[NN];
+        for (int n = 0; n < NN; ++n) { u1[n] = Yc[ci(e, 1, n, v)]; u2[n] = Yc[ci(e, 2, n, v)]; }
+        wcurl_h(s, u1, u2, nullptr, o1, o2, o3);
+        for (int n = 0; n < NN; ++n) om3[pi(e, n, v)] = o3[n];
+      }
+      for (int k = 0; k < Nf; ++k) {  // ᶠω¹² = ᶠcurlᵥ(u_h) + CT12(wcurl(u_3))
+        slab(e, rf[k], dzf[k], s);
+        FT w3[NN], o1[NN], o2[NN], o3[NN];
+        for (int n = 0; n < NN; ++n) w3[n] = Yf[fi(e, n, k)];
+        wcurl_h(s, nullptr, nullptr, w3, o1, o2, o3);
+        for (int n = 0; n < NN; ++n) {
+          FT cv1 = 0, cv2 = 0;
+          if (k > 0 && k < Nv) {
+            FT J = s.J[n];
+            cv1 = -(Yc[ci(e, 2, n, k)] - Yc[ci(e, 2, n, k - 1)]) / J;
+            cv2 = (Yc[ci(e, 1, n, k)] - Yc[ci(e, 1, n, k - 1)]) / J;
+          }
+          FT fh = FT(1) / rf[k];
+          fo1[fi(e, n, k)] = fh0[hn(e, n) * 2 + 0] * fh + cv1 + o1[n];
+          fo2[fi(e, n, k)] = fh0[hn(e, n) * 2 + 1] * fh + cv2 + o2[n];
+        }
+      }
+    }
+#pragma omp parallel for
+    for (int e = 0; e < Nh; ++e)
+      for (int n = 0; n < NN; ++n) {
+        // face cross product X = (f12 + w12) x (I^f(rho J) u^3)  -> C12, times face J
+        std::vector<FT> X1(Nf), X2(Nf);
+        for (int k = 0; k < Nf; ++k) {
+          FT rJ;
+          if (k == 0) rJ = Yc[ci(e, 0, n, 0)] * Jc(e, n, 0);
+          else if (k == Nv) rJ = Yc[ci(e, 0, n, Nv - 1)] * Jc(e, n, Nv - 1);
+          else rJ = (Yc[ci(e, 0, n, k - 1)] * Jc(e, n, k - 1) + Yc[ci(e, 0, n, k)] * Jc(e, n, k)) / FT(2);
+          FT b3 = rJ * pre.u3c[fi(e, n, k)];
+          FT Jf = Jfc(e, n, k);
+          X1[k] = Jf * (fo2[fi(e, n, k)] * b3);
+          X2[k] = Jf * (-fo1[fi(e, n, k)] * b3);
+        }
+        for (int v = 0; v < Nv; ++v) {
+          size_t q = pi(e, n, v);
+          FT rJ = Yc[ci(e, 0, n, v)] * Jc(e, n, v);
+          FT t1v = (X1[v] + X1[v + 1]) / FT(2) / rJ;
+          FT t2v = (X2[v] + X2[v + 1]) / FT(2) / rJ;
+          // (f3 + w3) x CT12(u) -> C12 = J (-a3 u^2, a3 u^1)
+          FT a3 = FT(2) * omega * sinlat[hn(e, n)] / dzc[v] + om3[q];
+          FT J = Jc(e, n, v);
+          t1v += J * (-a3 * pre.uc2[q]);
+          t2v += J * (a3 * pre.uc1[q]);
+          Tc[ci(e, 1, n, v)] -= t1v;
+          Tc[ci(e, 2, n, v)] -= t2v;
+        }
+        for (int k = 0; k < Nf; ++k) {
+          // (f12 + w12) x I^f(CT12(u)) -> C3 = J (a1 c2 - a2 c1); plus ᶠgradᵥ(K)
+          FT c1, c2, gK = 0;
+          if (k == 0) { c1 = pre.uc1[pi(e, n, 0)]; c2 = pre.uc2[pi(e, n, 0)]; }
+          else if (k == Nv) { c1 = pre.uc1[pi(e, n, Nv - 1)]; c2 = pre.uc2[pi(e, n, Nv - 1)]; }
+          else {
+            c1 = (pre.uc1[pi(e, n, k - 1)] + pre.uc1[pi(e, n, k)]) / FT(2);
+            c2 = (pre.uc2[pi(e, n, k - 1)] + pre.uc2[pi(e, n, k)]) / FT(2);
+            gK = pre.K[pi(e, n, k)] - pre.K[pi(e, n, k - 1)];
+          }
+          FT Jf = Jfc(e, n, k);
+          Tf[fi(e, n, k)] -= Jf * (fo1[fi(e, n, k)] * c2 - fo2[fi(e, n, k)] * c1) + gK;
+        }
+        // additional_tendency!: Rayleigh sponge on u_h
+        for (int v = 0; v < Nv; ++v) {
+          FT b = beta_sponge(zc[v], a_uh);
+          Tc[ci(e, 1, n, v)] -= b * Yc[ci(e, 1, n, v)];
+          Tc[ci(e, 2, n, v)] -= b * Yc[ci(e, 2, n, v)];
+        }
+      }
+  }
+
+  // ---- implicit_tendency! (implicit_vertical_advection_tendency!) ----
+  // needs set_precomputed at Y first
+  void implicit_tendency(FT *Tc, FT *Tf, const FT *Yc, const FT *Yf) {
+    std::fill(Tc, Tc + ncen(), FT(0));
+    std::fill(Tf, Tf + nfac(), FT(0));
+#pragma omp parallel for
+    for (int e = 0; e < Nh; ++e)
+      for (int n = 0; n < NN; ++n) {
+        std::vector<FT> flux(Nf), fh(Nf);
+        for (int k = 0; k < Nf; ++k) {
+          if (k == 0 || k == Nv) { flux[k] = 0; fh[k] = 0; continue; }
+          FT rJ = (Yc[ci(e, 0, n, k - 1)] * Jc(e, n, k - 1) + Yc[ci(e, 0, n, k)] * Jc(e, n, k)) / FT(2);
+          FT Jf = Jfc(e, n, k);
+          FT F = rJ / Jf * pre.u3c[fi(e, n, k)];
+          FT hb = (pre.h[pi(e, n, k - 1)] + pre.h[pi(e, n, k)]) / FT(2);
+          flux[k] = Jf * F;       // ᶜadvdivᵥ multiplies the face value by ᶠJ
+          fh[k] = Jf * F * hb;
+        }
+        for (int v = 0; v < Nv; ++v) {
+          FT J = Jc(e, n, v);
+          Tc[ci(e, 0, n, v)] -= (flux[v + 1] - flux[v]) / J;
+          Tc[ci(e, 3, n, v)] -= (fh[v + 1] - fh[v]) / J;
+        }
+        for (int k = 0; k < Nf; ++k) {
+          FT val = 0;
+          if (k > 0 && k < Nv) {
+            size_t a = pi(e, n, k - 1), b = pi(e, n, k);
+            FT gPhi = grav * (zc[k] - zc[k - 1]);
+            FT gPhir = pre.phir[b] - pre.phir[a];
+            FT thd = ((pre.thv[a] - pre.thvr[a]) + (pre.thv[b] - pre.thvr[b])) / FT(2);
+            FT gPi = pre.Pi[b] - pre.Pi[a];
+            val = -(gPhi - gPhir + cpd * thd * gPi);
+          }
+          val -= beta_sponge(zf[k], a_w) * Yf[fi(e, n, k)];
+          Tf[fi(e, n, k)] = val;
+        }
+      }
+  }
+
+  // ---- Jacobian (update_advection_jacobian!, dry, no topography) ----
+  struct Jac {
+    std::vector<FT> Mru, Meu;             // [col][v][2]  (u3 faces v, v+1)
+    std::vector<FT> Mur, Mue;             // [col][k][2]  (centres k-1, k)
+    std::vector<FT> Muh;                  // [col][k][2][2] (centres k-1, k; comps 1, 2)
+    std::vector<FT> Muu;                  // [col][k][3]  (faces k-1, k, k+1)
+  } jac;
+
+  void update_jacobian(const FT *Yc, const FT *Yf, FT dtg) {
+    size_t C = (size_t)Nh * NN;
+    jac.Mru.assign(C * Nv * 2, 0); jac.Meu.assign(C * Nv * 2, 0);
+    jac.Mur.assign(C * Nf * 2, 0); jac.Mue.assign(C * Nf * 2, 0);
+    jac.Muh.assign(C * Nf * 4, 0); jac.Muu.assign(C * Nf * 3, 0);
+    FT kap = Rd / cvd;  // kappa_m for dry air
+#pragma omp parallel for
+    for (int e = 0; e < Nh; ++e)
+      for (int n = 0; n < NN; ++n) {
+        size_t col = hn(e, n);
+        // centre rows: d(rho_t)/d(u3), d(rhoe_t)/d(u3)
+        for (int v = 0; v < Nv; ++v) {
+          FT J = Jc(e, n, v);
+          for (int s = 0; s < 2; ++s) {
+            int k = v + s;
+            FT val = 0, vh = 0;
+            if (k > 0 && k < Nv) {
+              FT rJ = (Yc[ci(e, 0, n, k - 1)] * Jc(e, n, k - 1) + Yc[ci(e, 0, n, k)] * Jc(e, n, k)) / FT(2);
+              FT g33 = FT(1) / (dzf[k] * dzf[k]);
+              FT sign = s ? FT(-1) : FT(1);  // -ᶜadvdivᵥ: -(+ at v+1, - at v)/J
+              val = sign * rJ * g33 / J;
+              FT hb = (pre.h[pi(e, n, k - 1)] + pre.h[pi(e, n, k)]) / FT(2);
+              vh = val * hb;
+            }
+            jac.Mru[(col * Nv + v) * 2 + s] = dtg * val;
+            jac.Meu[(col * Nv + v) * 2 + s] = dtg * vh;
+          }
+        }
+        for (int k = 0; k < Nf; ++k) {
+          FT beta = beta_sponge(zf[k], a_w);
+          if (k == 0 || k == Nv) {
+            jac.Muu[(col * Nf + k) * 3 + 1] = -dtg * beta - FT(1);
+            continue;
+          }
+          size_t a = pi(e, n, k - 1), b = pi(e, n, k);
+          FT ra = Yc[ci(e, 0, n, k - 1)], rb = Yc[ci(e, 0, n, k)];
+          FT rbar = (ra + rb) / FT(2);
+          auto dpdr = [&](size_t q) { return kap * (T0 * cpd - pre.K[q] - grav * zc[q % Nv]); };
+          FT thvb = (pre.thv[a] + pre.thv[b]) / FT(2);
+          FT gPi = pre.Pi[b] - pre.Pi[a];
+          FT buoy = cpd * thvb * gPi / rbar;  // times ᶠinterp_matrix (1/2, 1/2)
+          // ᶠp_grad_matrix = diag(-1/ρ̄) ᶠgradᵥ_matrix  (−1 at k−1, +1 at k)
+          jac.Mur[(col * Nf + k) * 2 + 0] = dtg * (dpdr(a) / rbar + buoy / FT(2));
+          jac.Mur[(col * Nf + k) * 2 + 1] = dtg * (-dpdr(b) / rbar + buoy / FT(2));
+          jac.Mue[(col * Nf + k) * 2 + 0] = dtg * (kap / rbar);
+          jac.Mue[(col * Nf + k) * 2 + 1] = dtg * (-kap / rbar);
+          // (u3, u_h): p_grad * diag(-kappa rho) * dK/du_h,  dK/du_i = u^i
+          jac.Muh[(col * Nf + k) * 4 + 0] = dtg * (-kap * ra / rbar) * pre.uc1[a];
+          jac.Muh[(col * Nf + k) * 4 + 1] = dtg * (-kap * ra / rbar) * pre.uc2[a];
+          jac.Muh[(col * Nf + k) * 4 + 2] = dtg * (kap * rb / rbar) * pre.uc1[b];
+          jac.Muh[(col * Nf + k) * 4 + 3] = dtg * (kap * rb / rbar) * pre.uc2[b];
+          // (u3, u3): p_grad * diag(-kappa rho) * dK/du3 - beta - I ; dK_v/du3_f = u^3_f / 2
+          FT um = pre.u3c[fi(e, n, k - 1)], u0 = pre.u3c[fi(e, n, k)], up = pre.u3c[fi(e, n, k + 1)];
+          jac.Muu[(col * Nf + k) * 3 + 0] = dtg * (-kap * ra * um / (FT(2) * rbar));
+          jac.Muu[(col * Nf + k) * 3 + 1] = dtg * (kap * (rb - ra) * u0 / (FT(2) * rbar) - beta) - FT(1);
+          jac.Muu[(col * Nf + k) * 3 + 2] = dtg * (kap * rb * up / (FT(2) * rbar));
+        }
+      }
+  }
+
+  // ---- ldiv!: BlockArrowheadSolve(rho, rhoe; alg2 = BlockLowerTriangularSolve(u_h)) ----
+  void ldiv(FT *Xc, FT *Xf, const FT *Rc, const FT *Rf) const {
+#pragma omp parallel for
+    for (int e = 0; e < Nh; ++e)
+      for (int n = 0; n < NN; ++n) {
+        size_t col = hn(e, n);
+        std::vector<FT> A(Nf), B(Nf), Cc(Nf), Dd(Nf);
+        // Δu_h = -R_uh
+        for (int v = 0; v < Nv; ++v) {
+          Xc[ci(e, 1, n, v)] = -Rc[ci(e, 1, n, v)];
+          Xc[ci(e, 2, n, v)] = -Rc[ci(e, 2, n, v)];
+        }
+        for (int k = 0; k < Nf; ++k) {
+          const FT *mu = &jac.Muu[(col * Nf + k) * 3];
+          const FT *mr = &jac.Mur[(col * Nf + k) * 2];
+          const FT *me = &jac.Mue[(col * Nf + k) * 2];
+          const FT *mh = &jac.Muh[(col * Nf + k) * 4];
+          FT a = mu[0], b = mu[1], c = mu[2];
+          FT rhs = Rf[fi(e, n, k)];
+          for (int s = 0; s < 2; ++s) {
+            int v = k - 1 + s;
+            if (v < 0 || v >= Nv) continue;
+            // S += M_u,x M_x,u ; rhs += M_u,x R_x
+            const FT *mru = &jac.Mru[(col * Nv + v) * 2];
+            const FT *meu = &jac.Meu[(col * Nv + v) * 2];
+            // centre v couples faces v (slot 0) and v+1 (slot 1)
+            FT cr = mr[s], ce = me[s];
+            // face v = k - 1 + s; offset of face v relative to k: s - 1
+            // face v+1 relative to k: s
+            FT t0 = cr * mru[0] + ce * meu[0];  // -> face v
+            FT t1 = cr * mru[1] + ce * meu[1];  // -> face v+1
+            if (s == 0) { a += t0; b += t1; } else { b += t0; c += t1; }
+            rhs += cr * Rc[ci(e, 0, n, v)] + ce * Rc[ci(e, 3, n, v)];
+            rhs += mh[2 * s] * Rc[ci(e, 1, n, v)] + mh[2 * s + 1] * Rc[ci(e, 2, n, v)];
+          }
+          A[k] = a; B[k] = b; Cc[k] = c; Dd[k] = rhs;
+        }
+        // Thomas algorithm
+        std::vector<FT> cp(Nf), dp(Nf), x(Nf);
+        cp[0] = Cc[0] / B[0]; dp[0] = Dd[0] / B[0];
+        for (int k = 1; k < Nf; ++k) {
+          FT m = B[k] - A[k] * cp[k - 1];
+          cp[k] = Cc[k] / m;
+          dp[k] = (Dd[k] - A[k] * dp[k - 1]) / m;
+        }
+        x[Nf - 1] = dp[Nf - 1];
+        for (int k = Nf - 2; k >= 0; --k) x[k] = dp[k] - cp[k] * x[k + 1];
+        for (int k = 0; k < Nf; ++k) Xf[fi(e, n, k)] = x[k];
+        for (int v = 0; v < Nv; ++v) {
+          const FT *mru = &jac.Mru[(col * Nv + v) * 2];
+          const FT *meu = &jac.Meu[(col * Nv + v) * 2];
+          Xc[ci(e, 0, n, v)] = mru[0] * x[v] + mru[1] * x[v + 1] - Rc[ci(e, 0, n, v)];
+          Xc[ci(e, 3, n, v)] = meu[0] * x[v] + meu[1] * x[v + 1] - Rc[ci(e, 3, n, v)];
+        }
+      }
+  }
+
+  // W V with the stored blocks (W = dtγ ∂T/∂Y − I restricted to the manual sparsity)
+  void jac_apply(FT *Oc, FT *Of, const FT *Vc, const FT *Vf) const {
+#pragma omp parallel for
+    for (int e = 0; e < Nh; ++e)
+      for (int n = 0; n < NN; ++n) {
+        size_t col = hn(e, n);
+        for (int v = 0; v < Nv; ++v) {
+          const FT *mru = &jac.Mru[(col * Nv + v) * 2];
+          const FT *meu = &jac.Meu[(col * Nv + v) * 2];
+          FT a = Vf[fi(e, n, v)], b = Vf[fi(e, n, v + 1)];
+          Oc[ci(e, 0, n, v)] = -Vc[ci(e, 0, n, v)] + mru[0] * a + mru[1] * b;
+          Oc[ci(e, 3, n, v)] = -Vc[ci(e, 3, n, v)] + meu[0] * a + meu[1] * b;
+          Oc[ci(e, 1, n, v)] = -Vc[ci(e, 1, n, v)];
+          Oc[ci(e, 2, n, v)] = -Vc[ci(e, 2, n, v)];
+        }
+        for (int k = 0; k < Nf; ++k) {
+          const FT *mu = &jac.Muu[(col * Nf + k) * 3];
+          const FT *mr = &jac.Mur[(col * Nf + k) * 2];
+          const FT *me = &jac.Mue[(col * Nf + k) * 2];
+          const FT *mh = &jac.Muh[(col * Nf + k) * 4];
+          FT s = mu[1] * Vf[fi(e, n, k)];
+          if (k > 0) s += mu[0] * Vf[fi(e, n, k - 1)];
+          if (k < Nv) s += mu[2] * Vf[fi(e, n, k + 1)];
+          for (int t = 0; t < 2; ++t) {
+            int v = k - 1 + t;
+            if (v < 0 || v >= Nv) continue;
+            s += mr[t] * Vc[ci(e, 0, n, v)] + me[t] * Vc[ci(e, 3, n, v)];
+            s += mh[2 * t] * Vc[ci(e, 1, n, v)] + mh[2 * t + 1] * Vc[ci(e, 2, n, v)];
+          }
+          Of[fi(e, n, k)] = s;
+        }
+      }
+  }
+
+  // ---- correct_implicit_advection_tendency! (van Leer minus central, ρe_tot only) ----
+  FT vanleer_face(FT u, const FT *a, int k) const {
+    // a: centre values of the column; face k between centres k-1 and k (interior)
+    bool near = (k == 1 || k == Nv - 1);
+    if (u >= 0) {
+      FT a0 = a[k - 1];
+      if (near) return u * a0;
+      FT am = a[k - 2], ap = a[k];
+      FT da = (ap - am) / FT(2);
+      FT mn = std::min(am, std::min(a0, ap)), mx = std::max(am, std::max(a0, ap));
+      FT sl = std::copysign(std::min(std::fabs(da), std::min(FT(2) * (a0 - mn), FT(2) * (mx - a0))), da);
+      return u * (a0 + sl * (FT(1) - std::fabs(u) * dt_model) / FT(2));
+    } else {
+      FT a0 = a[k];
+      if (near) return u * a0;
+      FT am = a[k - 1], ap = a[k + 1];
+      FT da = (ap - am) / FT(2);
+      FT mn = std::min(am, std::min(a0, ap)), mx = std::max(am, std::max(a0, ap));
+      FT sl = std::copysign(std::min(std::fabs(da), std::min(FT(2) * (a0 - mn), FT(2) * (mx - a0))), da);
+      return u * (a0 - sl * (FT(1) - std::fabs(u) * dt_model) / FT(2));
+    }
+  }
+  void correct_implicit(FT *Tc, FT *Tf, const FT *Yc, const FT *Yf) {
+    std::fill(Tc, Tc + ncen(), FT(0));
+    std::fill(Tf, Tf + nfac(), FT(0));
+    if (!upwinding) return;
+#pragma omp parallel for
+    for (int e = 0; e < Nh; ++e)
+      for (int n = 0; n < NN; ++n) {
+        std::vector<FT> h(Nv), fup(Nf, 0), fc(Nf, 0);
+        for (int v = 0; v < Nv; ++v) h[v] = pre.h[pi(e, n, v)];
+        for (int k = 1; k < Nv; ++k) {
+          FT rJ = (Yc[ci(e, 0, n, k - 1)] * Jc(e, n, k - 1) + Yc[ci(e, 0, n, k)] * Jc(e, n, k)) / FT(2);
+          FT u = pre.u3c[fi(e, n, k)];
+          FT Jf = Jfc(e, n, k);
+          fup[k] = Jf * (rJ / Jf * vanleer_face(u, h.data(), k));
+          fc[k] = Jf * (rJ / Jf * (u * (h[k - 1] + h[k]) / FT(2)));
+        }
+        for (int v = 0; v < Nv; ++v) {
+          FT J = Jc(e, n, v);
+          FT vup = -(fup[v + 1] - fup[v]) / J;
+          FT vc = -(fc[v + 1] - fc[v]) / J;
+          Tc[ci(e, 3, n, v)] = vup - vc;
+        }
+      }
+  }
+
+  // ---- ARS343 IMEX step with one Newton iteration (ClimaTimeSteppers stage loop) ----
+  FT ae[4][4], ai[4][4], be[4], bi[4];
+  void tableau() {
+    double g = 0.4358665215084590;
+    double a42 = 0.5529291480359398, a43 = a42;
+    double b1 = -1.5 * g * g + 4 * g - 0.25, b2 = 1.5 * g * g - 5 * g + 1.25;
+    double a31 = (1 - 4.5 * g + 1.5 * g * g) * a42 + (2.75 - 10.5 * g + 3.75 * g * g) * a43 - 3.5 + 13 * g - 4.5 * g * g;
+    double a32 = (-1 + 4.5 * g - 1.5 * g * g) * a42 + (-2.75 + 10.5 * g - 3.75 * g * g) * a43 + 4 - 12.5 * g + 4.5 * g * g;
+    double a41 = 1 - a42 - a43;
+    double E[4][4] = {{0, 0, 0, 0}, {g, 0, 0, 0}, {a31, a32, 0, 0}, {a41, a42, a43, 0}};
+    double I[4][4] = {{0, 0, 0, 0}, {0, g, 0, 0}, {0, (1 - g) / 2, g, 0}, {0, b1, b2, g}};
+    double B[4] = {0, b1, b2, g};
+    for (int i = 0; i < 4; ++i) {
+      for (int j = 0; j < 4; ++j) { ae[i][j] = (FT)E[i][j]; ai[i][j] = (FT)I[i][j]; }
+      be[i] = (FT)B[i]; bi[i] = (FT)B[i];
+    }
+  }
+
+  std::vector<FT> Te_c[4], Te_f[4], Ti_c[4], Ti_f[4], Uc, Uf, Hc, Hf, Rc_, Rf_, Xc_, Xf_, Kc, Kf;
+  void step(FT *Yc, FT *Yf, double dt_) {
+    FT dt = (FT)dt_;
+    size_t NC = ncen(), NF = nfac();
+    for (int i = 0; i < 4; ++i) {
+      Te_c[i].assign(NC, 0); Te_f[i].assign(NF, 0); Ti_c[i].assign(NC, 0); Ti_f[i].assign(NF, 0);
+    }
+    Uc.resize(NC); Uf.resize(NF); Hc.resize(NC); Hf.resize(NF);
+    Rc_.resize(NC); Rf_.resize(NF); Xc_.resize(NC); Xf_.resize(NF); Kc.resize(NC); Kf.resize(NF);
+    for (int i = 0; i < 4; ++i) {
+      // U = u + dt sum_j (ã_ij T_exp_j + a_ij T_imp_j)
+#pragma omp parallel for
+      for (size_t q = 0; q < NC; ++q) {
+        FT s = Yc[q];
+        for (int j = 0; j < i; ++j) {
+          if (ae[i][j] != FT(0)) s += dt * ae[i][j] * Te_c[j][q];
+          if (ai[i][j] != FT(0)) s += dt * ai[i][j] * Ti_c[j][q];
+        }
+        Uc[q] = s;
+      }
+#pragma omp parallel for
+      for (size_t q = 0; q < NF; ++q) {
+        FT s = Yf[q];
+        for (int j = 0; j < i; ++j) {
+          if (ae[i][j] != FT(0)) s += dt * ae[i][j] * Te_f[j][q];
+          if (ai[i][j] != FT(0)) s += dt * ai[i][j] * Ti_f[j][q];
+        }
+        Uf[q] = s;
+      }
+      if (i > 0 || dss_stage1) dss(Uc.data(), Uf.data());
+      FT aii = ai[i][i];
+      if (aii != FT(0)) {
+        FT dtg = dt * aii;
+        Hc = Uc; Hf = Uf;  // Û (temp)
+        // Newton, one iteration
+        set_precomputed(Uc.data(), Uf.data());  // cache_imp!
+        implicit_tendency(Kc.data(), Kf.data(), Uc.data(), Uf.data());
+        for (size_t q = 0; q < NC; ++q) Rc_[q] = Hc[q] + dtg * Kc[q] - Uc[q];
+        for (size_t q = 0; q < NF; ++q) Rf_[q] = Hf[q] + dtg * Kf[q] - Uf[q];
+        update_jacobian(Uc.data(), Uf.data(), dtg);
+        ldiv(Xc_.data(), Xf_.data(), Rc_.data(), Rf_.data());
+        for (size_t q = 0; q < NC; ++q) Uc[q] -= Xc_[q];
+        for (size_t q = 0; q < NF; ++q) Uf[q] -= Xf_[q];
+        set_precomputed(Uc.data(), Uf.data());  // cache! after the solve
+        if (upwinding) {
+          correct_implicit(Kc.data(), Kf.data(), Uc.data(), Uf.data());
+          for (size_t q = 0; q < NC; ++q) Uc[q] += dtg * Kc[q];
+          set_precomputed(Uc.data(), Uf.data());
+        }
+        for (size_t q = 0; q < NC; ++q) Ti_c[i][q] = (Uc[q] - Hc[q]) / dtg;
+        for (size_t q = 0; q < NF; ++q) Ti_f[i][q] = (Uf[q] - Hf[q]) / dtg;
+      } else {
+        set_precomputed(Uc.data(), Uf.data());  // cache!
+      }
+      remaining_tendency(Te_c[i].data(), Te_f[i].data(), Uc.data(), Uf.data());
+    }
+#pragma omp parallel for
+    for (size_t q = 0; q < NC; ++q) {
+      FT s = Yc[q];
+      for (int j = 0; j < 4; ++j) {
+        if (be[j] != FT(0)) s += dt * be[j] * Te_c[j][q];
+        if (bi[j] != FT(0)) s += dt * bi[j] * Ti_c[j][q];
+      }
+      Yc[q] = s;
+    }
+#pragma omp parallel for
+    for (size_t q = 0; q < NF; ++q) {
+      FT s = Yf[q];
+      for (int j = 0; j < 4; ++j) {
+        if (be[j] != FT(0)) s += dt * be[j] * Te_f[j][q];
+        if (bi[j] != FT(0)) s += dt * bi[j] * Ti_f[j][q];
+      }
+      Yf[q] = s;
+    }
+    dss(Yc, Yf);
+    set_precomputed(Yc, Yf);
+  }
+
+  // ∫ rho dV, ∫ rho e_tot dV with compensated (Neumaier) FP64 summation
+  void global_sums(const FT *Yc, double *out) const {
+    for (int c = 0; c < 2; ++c) {
+      int comp = c == 0 ? 0 : 3;
+      double s = 0, comp_ = 0;
+      for (int e = 0; e < Nh; ++e)
+        for (int n = 0; n < NN; ++n)
+          for (int v = 0; v < Nv; ++v) {
+            double x = (double)Yc[ci(e, comp, n, v)] * (double)W[n] * ((double)Jh[hn(e, n)] * rc[v] * rc[v] * dzc[v]);
+            double t = s + x;
+            if (std::fabs(s) >= std::fabs(x)) comp_ += (s - t) + x; else comp_ += (x - t) + s;
+            s = t;
+          }
+      out[c] = s + comp_;
+    }
+  }
+
+  void init(const OracleGeom *g, const OracleParams *p) {
+    Nh = g->Nh; Nv = g->Nv; Nf = Nv + 1;
+    grav = p->grav; omega = p->omega; Rd = p->R_d; cpd = p->cp_d; cvd = p->cv_d; T0 = p->T_0; pref = p->p_ref;
+    Tmin_ref = p->T_min_ref; Tsfc_ref = p->T_surf_ref; Tmin_sgs = p->T_min_sgs; R = p->radius;
+    nu_v = p->nu_v; nu_s = p->nu_s; div_damp = p->div_damp; zd = p->sponge_zd; a_uh = p->alpha_uh; a_w = p->alpha_w;
+    zmax = p->z_max; dt_model = p->dt_model; upwinding = p->upwinding; dss_stage1 = p->dss_stage1;
+    kappa = Rd / cpd;
+    for (int n = 0; n < NN; ++n) W[n] = g->W[n];
+    for (int i = 0; i < NQ; ++i) for (int k = 0; k < NQ; ++k) D[i][k] = g->D[i * NQ + k];
+    size_t H = (size_t)Nh * NN;
+    Jh.assign(g->Jh, g->Jh + H);
+    gup.assign(g->gup, g->gup + 3 * H); gdn.assign(g->gdn, g->gdn + 3 * H);
+    sinlat.assign(g->sinlat, g->sinlat + H); fh0.assign(g->fh0, g->fh0 + 2 * H);
+    ecov.assign(g->ecov, g->ecov + 6 * H); econ.assign(g->econ, g->econ + 6 * H);
+    zf.assign(g->zf, g->zf + Nf);
+    zc.resize(Nv); dzc.resize(Nv); rc.resize(Nv); dzf.resize(Nf); rf.resize(Nf);
+    for (int v = 0; v < Nv; ++v) {
+      zc[v] = (FT)((g->zf[v] + g->zf[v + 1]) / 2);
+      dzc[v] = (FT)(g->zf[v + 1] - g->zf[v]);
+      rc[v] = (FT)((p->radius + (g->zf[v] + g->zf[v + 1]) / 2) / p->radius);
+    }
+    for (int k = 0; k < Nf; ++k) {
+      double d;
+      if (k == 0) d = g->zf[1] - g->zf[0];
+      else if (k == Nv) d = g->zf[Nv] - g->zf[Nv - 1];
+      else d = (g->zf[k] + g->zf[k + 1]) / 2 - (g->zf[k - 1] + g->zf[k]) / 2;
+      dzf[k] = (FT)d;
+      rf[k] = (FT)((p->radius + g->zf[k]) / p->radius);
+    }
+    goff.assign(g->dss_off, g->dss_off + g->ngroups + 1);
+    gcopy.assign(g->dss_copy, g->dss_copy + goff.back());
+    gw.assign(g->dss_w, g->dss_w + goff.back());
+    tableau();
+    alloc_pre();
+  }
+};
+
+struct Handle {
+  int ft;
+  Oracle<double> *d = nullptr;
+  Oracle<float> *f = nullptr;
+};
+
+}  // namespace
+
+#define DISPATCH(h, CALL)                         \
+  do {                                            \
+    if ((h)->ft == 8) { auto &o = *(h)->d; CALL; } \
+    else { auto &o = *(h)->f; CALL; }             \
+  } while (0)
+
+extern "C" {
+
+void *oracle_create(const OracleGeom *g, const OracleParams *p, int ft_bytes) {
+  Handle *h = new Handle();
+  h->ft = ft_bytes;
+  if (ft_bytes == 8) { h->d = new Oracle<double>(); h->d->init(g, p); }
+  else { h->f = new Oracle<float>(); h->f->init(g, p); }
+  return h;
+}
+void oracle_destroy(void *hh) {
+  Handle *h = (Handle *)hh;
+  delete h->d; delete h->f; delete h;
+}
+void oracle_set_threads(int n) {
+#ifdef _OPENMP
+  omp_set_num_threads(n);
+#else
+  (void)n;
+#endif
+}
+int oracle_max_threads() {
+#ifdef _OPENMP
+  return omp_get_max_threads();
+#else
+  return 1;
+#endif
+}
+// All state pointers are FT arrays in the C-ABI layout; FT = ft_bytes of the handle.
+void oracle_set_precomputed(void *hh, void *Yc, void *Yf) {
+  Handle *h = (Handle *)hh;
+  DISPATCH(h, (o.set_precomputed((decltype(o.R) *)Yc, (decltype(o.R) *)Yf)));
+}
+void oracle_remaining_tendency(void *hh, void *Tc, void *Tf, void *Yc, void *Yf) {
+  Handle *h = (Handle *)hh;
+  DISPATCH(h, (o.set_precomputed((decltype(o.R) *)Yc, (decltype(o.R) *)Yf),
+               o.remaining_tendency((decltype(o.R) *)Tc, (decltype(o.R) *)Tf, (decltype(o.R) *)Yc, (decltype(o.R) *)Yf)));
+}
+void oracle_implicit_tendency(void *hh, void *Tc, void *Tf, void *Yc, void *Yf) {
+  Handle *h = (Handle *)hh;
+  DISPATCH(h, (o.set_precomputed((decltype(o.R) *)Yc, (decltype(o.R) *)Yf),
+               o.implicit_tendency((decltype(o.R) *)Tc, (decltype(o.R) *)Tf, (decltype(o.R) *)Yc, (decltype(o.R) *)Yf)));
+}
+void oracle_update_jacobian(void *hh, void *Yc, void *Yf, double dtg) {
+  Handle *h = (Handle *)hh;
+  DISPATCH(h, (o.set_precomputed((decltype(o.R) *)Yc, (decltype(o.R) *)Yf),
+               o.update_jacobian((decltype(o.R) *)Yc, (decltype(o.R) *)Yf, (decltype(o.R))dtg)));
+}
+void oracle_ldiv(void *hh, void *Xc, void *Xf, void *Rc, void *Rf) {
+  Handle *h = (Handle *)hh;
+  DISPATCH(h, (o.ldiv((decltype(o.R) *)Xc, (decltype(o.R) *)Xf, (const decltype(o.R) *)Rc, (const decltype(o.R) *)Rf)));
+}
+void oracle_correct_implicit(void *hh, void *Tc, void *Tf, void *Yc, void *Yf) {
+  Handle *h = (Handle *)hh;
+  DISPATCH(h, (o.set_precomputed((decltype(o.R) *)Yc, (decltype(o.R) *)Yf),
+               o.correct_implicit((decltype(o.R) *)Tc, (decltype(o.R) *)Tf, (decltype(o.R) *)Yc, (decltype(o.R) *)Yf)));
+}
+void oracle_jac_apply(void *hh, void *Oc, void *Of, void *Vc, void *Vf) {
+  Handle *h = (Handle *)hh;
+  DISPATCH(h, (o.jac_apply((decltype(o.R) *)Oc, (decltype(o.R) *)Of, (const decltype(o.R) *)Vc, (const decltype(o.R) *)Vf)));
+}
+void oracle_dss(void *hh, void *Yc, void *Yf) {
+  Handle *h = (Handle *)hh;
+  DISPATCH(h, (o.dss((decltype(o.R) *)Yc, (decltype(o.R) *)Yf)));
+}
+void oracle_step(void *hh, void *Yc, void *Yf, double dt, int nsteps) {
+  Handle *h = (Handle *)hh;
+  for (int s = 0; s < nsteps; ++s) DISPATCH(h, (o.step((decltype(o.R) *)Yc, (decltype(o.R) *)Yf, dt)));
+}
+void oracle_global_sums(void *hh, void *Yc, double *out) {
+  Handle *h = (Handle *)hh;
+  DISPATCH(h, (o.global_sums((const decltype(o.R) *)Yc, out)));
+}
+}

@@ -1,0 +1,61 @@
+"""Shared test helpers: oracle construction and field comparisons."""
+import numpy as np
+
+from geometry import OracleGeometry
+import oracle as O
+from gbdycore import config as C
+from gbdycore import setups as S
+
+_GEO = {}
+
+
+def oracle_geometry(cfg):
+    key = (cfg.h_elem, cfg.z_elem, cfg.z_max, cfg.z_stretch, cfg.dz_bottom, cfg.constants["radius"])
+    if key not in _GEO:
+        _GEO[key] = OracleGeometry(cfg.h_elem, cfg.z_elem, cfg.z_max, cfg.z_stretch, cfg.dz_bottom,
+                                   radius=cfg.constants["radius"], omega=cfg.constants["omega"])
+    return _GEO[key]
+
+
+def make_oracle(cfg, dtype=np.float64, dss_stage1=True):
+    return O.Oracle(oracle_geometry(cfg), cfg.oracle_params(dss_stage1=dss_stage1), dtype)
+
+
+def state(cfg, workload="plain", dtype=np.float64, geom=None):
+    g = geom or oracle_geometry(cfg)
+    Yc, Yf = S.workload_state(g, cfg, workload)
+    return Yc.astype(dtype), Yf.astype(dtype)
+
+
+def perturbed_state(cfg, seed=11, dtype=np.float64, w_amp=0.05):
+    """Balanced state plus nonzero u_3 (interior faces), so every operator is exercised."""
+    Yc, Yf = state(cfg, dtype=np.float64)
+    rng = np.random.default_rng(seed)
+    g = oracle_geometry(cfg)
+    w = rng.normal(0, w_amp, size=Yf.shape)
+    Yf = w * g.dzf[None, None, :]
+    Yf[:, :, 0] = 0
+    Yf[:, :, -1] = 0
+    Yc = Yc.copy()
+    Yc[:, 3] *= 1 + 1e-3 * rng.normal(size=Yc[:, 3].shape)
+    return Yc.astype(dtype), Yf.astype(dtype)
+
+
+def small_config(ft=np.float64, **kw):
+    base = dict(h_elem=3, z_elem=8, z_max=30000.0, z_stretch=True, dz_bottom=300.0, dt=300.0, ft=ft)
+    base.update(kw)
+    return C.DycoreConfig(**base)
+
+
+def rel_err(a, b):
+    """max-norm relative error per component (normalised by the component's max magnitude)."""
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    return np.abs(a - b).max() / max(np.abs(b).max(), 1e-300)
+
+
+def field_errors(Xc, Xf, Rc, Rf):
+    names = ["rho", "u_1", "u_2", "rho_e_tot"]
+    out = {names[c]: rel_err(Xc[:, c], Rc[:, c]) for c in range(4)}
+    out["u_3"] = rel_err(Xf, Rf)
+    return out

@@ -1,0 +1,206 @@
+"""GPU parity: every hook and the fused ARS343 step through the C ABI against the CPU oracle.
+
+Tolerances (max-norm error relative to each component's max magnitude):
+  FP64 hooks and steps: <= 1e-11 / 1e-10 (roundoff of a different but
+    equivalent evaluation order: FMA contraction, shuffle-based derivatives,
+    parallel cyclic reduction instead of the Thomas algorithm);
+  FP32 GPU against the FP32 oracle: <= 1e-4 for tendencies (cancellation in
+    the pressure-gradient terms), and the FP32 step against the FP64 oracle
+    per prognostic field with the bounds written in each test.
+"""
+import numpy as np
+import pytest
+import torch
+
+from gbdycore import config as C
+from gbdycore import simulation as sim
+from helpers import field_errors, make_oracle, perturbed_state, small_config, state
+
+pytestmark = pytest.mark.gpu
+
+
+def _dev(Yc, Yf):
+    return sim.FieldVector.from_numpy(Yc, Yf)
+
+
+def _cache(cfg):
+    return sim.AtmosCache(cfg)
+
+
+def _errs(gpu, ref):
+    Xc, Xf = gpu.numpy() if isinstance(gpu, sim.FieldVector) else gpu
+    return field_errors(Xc, Xf, ref[0], ref[1])
+
+
+def _assert_errs(errs, tol, skip=()):
+    bad = {k: v for k, v in errs.items() if k not in skip and not v <= tol}
+    assert not bad, "errors above %g: %s (all: %s)" % (tol, bad, errs)
+
+
+FT_CASES = [(np.float64, 1e-11), (np.float32, 1e-4)]
+
+
+@pytest.mark.parametrize("ft,tol", FT_CASES)
+def test_remaining_tendency(ft, tol):
+    cfg = small_config(ft=ft)
+    Yc, Yf = perturbed_state(cfg, dtype=ft)
+    ref = make_oracle(cfg, ft).remaining_tendency(Yc.copy(), Yf.copy())
+    p = _cache(cfg)
+    Y = _dev(Yc, Yf)
+    Yt = Y.similar()
+    sim.remaining_tendency(Yt, None, Y, p, 0.0)
+    _assert_errs(_errs(Yt, ref), tol)
+
+
+@pytest.mark.parametrize("ft,tol", FT_CASES)
+def test_implicit_tendency_and_correction(ft, tol):
+    cfg = small_config(ft=ft, z_elem=12)
+    Yc, Yf = perturbed_state(cfg, dtype=ft, w_amp=0.3)
+    o = make_oracle(cfg, ft)
+    ref = o.implicit_tendency(Yc.copy(), Yf.copy())
+    refc = o.correct_implicit(Yc.copy(), Yf.copy())
+    p = _cache(cfg)
+    Y = _dev(Yc, Yf)
+    Yt = Y.similar()
+    sim.implicit_tendency(Yt, Y, p, 0.0)
+    _assert_errs(_errs(Yt, ref), tol, skip=("u_1", "u_2"))
+    sim.correct_implicit_advection_tendency(Yt, Y, p, 0.0)
+    e = _errs(Yt, refc)
+    assert e["rho_e_tot"] <= tol, e
+    assert np.abs(Yt.c[:, :3].cpu().numpy()).max() == 0 and np.abs(Yt.f.cpu().numpy()).max() == 0
+
+
+@pytest.mark.parametrize("ft,tol", [(np.float64, 1e-10), (np.float32, 1e-3)])
+def test_jacobian_and_ldiv(ft, tol):
+    cfg = small_config(ft=ft, z_elem=40)   # two levels per lane
+    Yc, Yf = perturbed_state(cfg, dtype=ft, w_amp=0.3)
+    dtg = 0.4358665215084590 * cfg.dt
+    o = make_oracle(cfg, ft)
+    o.set_precomputed(Yc, Yf)
+    o.update_jacobian(Yc, Yf, dtg)
+    rng = np.random.default_rng(3)
+    Rc = (rng.normal(size=Yc.shape) * np.abs(Yc).max(axis=(0, 2, 3), keepdims=True) * 1e-3).astype(ft)
+    Rf = (rng.normal(size=Yf.shape) * 0.1).astype(ft)
+    ref = o.ldiv(Rc, Rf)
+    p = _cache(cfg)
+    Y = _dev(Yc, Yf)
+    jac = sim.Jacobian(p)
+    sim.update_jacobian(jac, Y, p, dtg, 0.0)
+    R = _dev(Rc, Rf)
+    dY = Y.similar()
+    sim.ldiv(dY, jac, R)
+    _assert_errs(_errs(dY, ref), tol)
+
+
+@pytest.mark.parametrize("ft,tol", [(np.float64, 0.0), (np.float32, 0.0)])
+def test_dss_matches_oracle_bitwise_order(ft, tol):
+    cfg = small_config(ft=ft)
+    Yc, Yf = perturbed_state(cfg, dtype=ft)
+    rng = np.random.default_rng(2)
+    Yc = (Yc * (1 + 1e-3 * rng.normal(size=Yc.shape))).astype(ft)   # break continuity
+    o = make_oracle(cfg, ft)
+    rc, rf = Yc.copy(), Yf.copy()
+    o.dss(rc, rf)
+    p = _cache(cfg)
+    Y = _dev(Yc, Yf)
+    sim.dss(Y, p, 0.0)
+    e = _errs(Y, (rc, rf))
+    lim = 1e-14 if ft == np.float64 else 1e-6
+    _assert_errs(e, lim)
+
+
+@pytest.mark.parametrize("stretch,z_elem", [(False, 10), (True, 40), (True, 70)])
+def test_fused_step_fp64_matches_oracle(stretch, z_elem):
+    cfg = small_config(ft=np.float64, z_stretch=stretch, z_elem=z_elem)
+    Yc, Yf = perturbed_state(cfg, w_amp=0.05)
+    o = make_oracle(cfg, np.float64, dss_stage1=False)
+    rc, rf = Yc.copy(), Yf.copy()
+    o.step(rc, rf, cfg.dt, 3)
+    s = sim.AtmosSimulation(cfg, state=(Yc, Yf))
+    s.step(3, use_graph=True)
+    _assert_errs(_errs(s.Y, (rc, rf)), 1e-10)
+
+
+def test_hook_loop_matches_fused_step():
+    cfg = small_config(ft=np.float64)
+    Yc, Yf = perturbed_state(cfg)
+    a = sim.AtmosSimulation(cfg, state=(Yc, Yf))
+    a.step(2, use_graph=False)
+    p = sim.AtmosCache(cfg)
+    Y = _dev(Yc, Yf)
+    for k in range(2):
+        sim.ars343_step_via_hooks(Y, p, k * cfg.dt, cfg.dt)
+    _assert_errs(_errs(Y, a.Y.numpy()), 1e-10)
+
+
+def test_plain_workload_fp32_against_fp64_oracle():
+    """Plain dry IMEX step (h_elem 6, z_elem 10, dt 400 s), 10 steps: FP32 GPU vs FP64 oracle."""
+    cfg64 = C.plain_h6().with_(ft=np.float64)
+    Yc, Yf = state(cfg64, "plain")
+    o = make_oracle(cfg64, np.float64, dss_stage1=False)
+    rc, rf = Yc.copy(), Yf.copy()
+    o.step(rc, rf, cfg64.dt, 10)
+    s = sim.AtmosSimulation(C.plain_h6(), state=(Yc.astype(np.float32), Yf.astype(np.float32)))
+    s.step(10)
+    e = _errs(s.Y, (rc, rf))
+    print("FP32 vs FP64 after 10 steps:", e)
+    # rho and rho e_tot to 1e-5; the covariant velocities carry the roundoff of
+    # the pressure-gradient cancellation, bounded here at 1e-3 of their range
+    assert e["rho"] <= 1e-5 and e["rho_e_tot"] <= 1e-5, e
+    assert e["u_1"] <= 1e-3 and e["u_2"] <= 1e-3 and e["u_3"] <= 1e-2, e
+
+
+def test_graph_replay_equals_eager_and_is_deterministic():
+    cfg = small_config(ft=np.float32)
+    Yc, Yf = perturbed_state(cfg, dtype=np.float32)
+    runs = []
+    for g in (True, False, True):
+        s = sim.AtmosSimulation(cfg, state=(Yc, Yf))
+        s.step(2, use_graph=g)
+        runs.append(s.Y.numpy())
+    for r in runs[1:]:
+        assert np.array_equal(r[0], runs[0][0]) and np.array_equal(r[1], runs[0][1])
+
+
+def test_global_sums_and_conservation():
+    cfg = small_config(ft=np.float64)
+    Yc, Yf = perturbed_state(cfg)
+    o = make_oracle(cfg, np.float64)
+    o.dss(Yc, Yf)
+    s = sim.AtmosSimulation(cfg, state=(Yc, Yf))
+    g0 = s.p.global_sums(s.Y)
+    ref = o.global_sums(Yc)
+    assert np.all(np.abs(g0 - ref) <= 1e-14 * np.abs(ref))
+    s.step(3)
+    g1 = s.p.global_sums(s.Y)
+    assert abs(g1[0] - g0[0]) <= 1e-13 * abs(g0[0])
+    assert abs(g1[1] - g0[1]) <= 1e-12 * abs(g0[1])
+    r = s.p.newton_residual()
+    assert np.all(np.isfinite(r)) and r[0] > 0
+
+
+def test_nonfinite_state_is_reported():
+    cfg = small_config(ft=np.float32)
+    Yc, Yf = perturbed_state(cfg, dtype=np.float32)
+    Yc[3, 0, 5, 2] = np.nan
+    s = sim.AtmosSimulation(cfg, state=(Yc, Yf))
+    s.step(1)
+    from gbdycore import _native as N
+    with pytest.raises(N.GBError) as ei:
+        s.p.newton_residual()
+    assert ei.value.code == N.GB_ERR_NONFINITE
+
+
+def test_production_size_step_conserves_mass():
+    """h_elem 30, z_elem 63 stretched, FP32: two fused steps; size-independent checks."""
+    cfg = C.production_h30()
+    s = sim.AtmosSimulation(cfg, workload="production")
+    g0 = s.p.global_sums(s.Y)
+    s.step(2)
+    torch.cuda.synchronize()
+    g1 = s.p.global_sums(s.Y)
+    Yc = s.Y.c
+    assert torch.isfinite(Yc).all() and torch.isfinite(s.Y.f).all()
+    assert abs(g1[0] - g0[0]) <= 2e-6 * abs(g0[0])
+    assert abs(g1[1] - g0[1]) <= 2e-5 * abs(g0[1])
+    assert float(s.Y.f[:, :, 0].abs().max()) == 0.0 and float(s.Y.f[:, :, -1].abs().max()) == 0.0

@@ -36,10 +36,12 @@ struct Impl : ImplBase {
   double ae[4][4], ai[4][4], be[4], bi[4];
   // captured step graph
   cudaGraphExec_t gexec = nullptr;
+  cudaStream_t cap = nullptr;  // private stream the step graph is captured on
   void *g_c = nullptr, *g_f = nullptr;
   double g_dt = 0;
   ~Impl() {
     if (gexec) cudaGraphExecDestroy(gexec);
+    if (cap) cudaStreamDestroy(cap);
   }
 };
 
@@ -208,10 +210,9 @@ int column_hook_t(gb_ctx *ctx, int mode, gb_fieldvec O, gb_fieldvec Y, double dt
 // is computed, so every stage state assembled from u_n (continuous), DSSed
 // explicit tendencies and column-local implicit tendencies is continuous.
 template <class FT>
-void enqueue_step(gb_ctx *ctx, FT *Yc, FT *Yf, double dt_) {
+void enqueue_step(gb_ctx *ctx, FT *Yc, FT *Yf, double dt_, cudaStream_t s) {
   Impl<FT> *I = impl<FT>(ctx);
   const DevParams<FT> &P = I->P;
-  cudaStream_t s = ctx->stream;
   const FT dt = (FT)dt_;
   FT *lap = (FT *)I->lap.p;
   auto tec = [&](int j) { return (FT *)I->Te[j].p; };
@@ -265,16 +266,19 @@ int step_t(gb_ctx *ctx, gb_fieldvec Y, double dt, int nsteps, int use_graph) {
   Impl<FT> *I = impl<FT>(ctx);
   FT *Yc = (FT *)Y.c, *Yf = (FT *)Y.f;
   if (!use_graph) {
-    for (int s = 0; s < nsteps; ++s) enqueue_step<FT>(ctx, Yc, Yf, dt);
+    for (int s = 0; s < nsteps; ++s) enqueue_step<FT>(ctx, Yc, Yf, dt, ctx->stream);
     return check_launch(ctx);
   }
   if (!I->gexec || I->g_c != Y.c || I->g_f != Y.f || I->g_dt != dt) {
     if (I->gexec) { cudaGraphExecDestroy(I->gexec); I->gexec = nullptr; }
+    // capture on a private stream (the caller's stream may be the legacy
+    // default stream, which cannot be captured); replay on the caller's stream
+    if (!I->cap) CK(cudaStreamCreateWithFlags(&I->cap, cudaStreamNonBlocking));
     cudaGraph_t graph;
-    CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
-    enqueue_step<FT>(ctx, Yc, Yf, dt);
+    CK(cudaStreamBeginCapture(I->cap, cudaStreamCaptureModeThreadLocal));
+    enqueue_step<FT>(ctx, Yc, Yf, dt, I->cap);
     cudaError_t le = cudaGetLastError();
-    cudaError_t ce = cudaStreamEndCapture(ctx->stream, &graph);
+    cudaError_t ce = cudaStreamEndCapture(I->cap, &graph);
     if (le != cudaSuccess) return fail(ctx, GB_ERR_CUDA, std::string("capture launch: ") + cudaGetErrorString(le));
     if (ce != cudaSuccess) return fail(ctx, GB_ERR_CUDA, std::string("cudaStreamEndCapture: ") + cudaGetErrorString(ce));
     cudaError_t ie = cudaGraphInstantiate(&I->gexec, graph, 0);
@@ -292,6 +296,7 @@ int read_status(gb_ctx *ctx) {
   int st = 0;
   CK(cudaMemcpyAsync(&st, I->status.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
+  if (st) CK(cudaMemsetAsync(I->status.p, 0, sizeof(int), ctx->stream));  // reported once
   if (st & ST_TIMEOUT) return fail(ctx, GB_ERR_TIMEOUT, "a bounded device wait timed out");
   if (st & ST_NONFINITE) return fail(ctx, GB_ERR_NONFINITE, "non-finite Newton residual");
   return GB_OK;

@@ -18,7 +18,8 @@ def oracle_geometry(cfg):
 
 
 def make_oracle(cfg, dtype=np.float64, dss_stage1=True):
-    return O.Oracle(oracle_geometry(cfg), cfg.oracle_params(dss_stage1=dss_stage1), dtype)
+    cfg64 = cfg.with_(ft=np.float64)
+    return O.Oracle(oracle_geometry(cfg64), cfg64.oracle_params(dss_stage1=dss_stage1), dtype)
 
 
 def state(cfg, workload="plain", dtype=np.float64, geom=None):
@@ -38,6 +39,7 @@ def perturbed_state(cfg, seed=11, dtype=np.float64, w_amp=0.05):
     Yf[:, :, -1] = 0
     Yc = Yc.copy()
     Yc[:, 3] *= 1 + 1e-3 * rng.normal(size=Yc[:, 3].shape)
+    make_oracle(cfg).dss(Yc, Yf)        # continuous, as every stage state of the step is
     return Yc.astype(dtype), Yf.astype(dtype)
 
 

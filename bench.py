@@ -166,7 +166,7 @@ def algorithmic_bytes(cfg, kid, fb=4):
     F = Nh * 16 * (Nv + 1)
     S = 4 * P + F
     T = 2 * P + F                  # implicit tendency (rho, rho e_tot, u_3)
-    geo = Nh * 10 * 16             # per-node metric terms
+    geo = Nh * 11 * 16             # per-node metric terms
     words = {
         0: S + 4 * P + geo,        # read state + geometry, write 4 Laplacian fields
         1: 2 * S + 4 * P + geo,    # read state + Laplacians + geometry, write tendency

@@ -15,10 +15,10 @@ constexpr long long WAIT_LIMIT = 1LL << 26;
 template <class FT>
 struct DevParams {
   int Nh, Nv, Nf, ngroups;
-  FT grav, Rd, cpd, cvd, T0, pref, kappa, Tmin_ref, Tsfc_ref, Tmin_sgs;
+  FT grav, Rd, cpd, cvd, T0, pref, kappa, Tmin_ref, Tsfc_ref, Tmin_sgs, icvd, ipref;
   FT nu_v, nu_s, div_damp, dt_model;
   int upwinding;
-  FT W[NN];
+  FT W[NN], iW[NN];
   FT D[NQ * NQ];  // D[i*4+k] = l_k'(xi_i)
   const FT *hgeo;  // [Nh][HG_N][16]
   const FT *levc;  // [LC_N][Nv]
@@ -29,10 +29,16 @@ struct DevParams {
 };
 
 // ---------------------------------------------------------------- math
-__device__ __forceinline__ float gpow(float x, float y) { return powf(x, y); }
+// FP32 uses the hardware approximations (ex2/lg2/rcp based, a few ulp); FP64
+// keeps the correctly rounded library functions and IEEE division.
+__device__ __forceinline__ float gpow(float x, float y) { return __powf(x, y); }
 __device__ __forceinline__ double gpow(double x, double y) { return pow(x, y); }
-__device__ __forceinline__ float glog(float x) { return logf(x); }
+__device__ __forceinline__ float glog(float x) { return __logf(x); }
 __device__ __forceinline__ double glog(double x) { return log(x); }
+__device__ __forceinline__ float gdiv(float a, float b) { return __fdividef(a, b); }
+__device__ __forceinline__ double gdiv(double a, double b) { return a / b; }
+__device__ __forceinline__ float grcp(float a) { return __fdividef(1.0f, a); }
+__device__ __forceinline__ double grcp(double a) { return 1.0 / a; }
 __device__ __forceinline__ float gsin(float x) { return sinf(x); }
 __device__ __forceinline__ double gsin(double x) { return sin(x); }
 
@@ -57,20 +63,21 @@ struct Thermo {
 };
 template <class FT>
 __device__ __forceinline__ void thermo(const DevParams<FT> &P, FT rho, FT rhoe, FT K, FT Phi, Thermo<FT> &o) {
-  FT e_tot = rhoe / rho;
+  FT e_tot = gdiv(rhoe, rho);
   FT eint = e_tot - K - Phi;
-  FT T = P.T0 + (eint + P.Rd * P.T0) / P.cvd;
+  FT T = P.T0 + (eint + P.Rd * P.T0) * P.icvd;
   T = T > P.Tmin_sgs ? T : P.Tmin_sgs;
   FT p = rho * P.Rd * T;
-  FT Pi = gpow(p / P.pref, P.kappa);
+  FT Pi = gpow(p * P.ipref, P.kappa);
   FT Pi2 = Pi * Pi, Pi7 = Pi2 * Pi2 * Pi2 * Pi;
   FT Tr = P.Tmin_ref + (P.Tsfc_ref - P.Tmin_ref) * Pi7;
+  FT iPi = grcp(Pi);
   o.T = T;
   o.p = p;
   o.h = e_tot + P.Rd * T;
   o.Pi = Pi;
-  o.thv = T / Pi;
-  o.thvr = Tr / Pi;
+  o.thv = T * iPi;
+  o.thvr = Tr * iPi;
   o.phir = -P.cpd * (P.Tmin_ref * glog(Pi) + (P.Tsfc_ref - P.Tmin_ref) / FT(7) * (Pi7 - FT(1)));
 }
 template <class FT>

@@ -149,9 +149,10 @@ int create_impl(gb_ctx *ctx) {
   P.grav = (FT)c.grav; P.Rd = (FT)c.R_d; P.cpd = (FT)c.cp_d; P.cvd = (FT)c.cv_d; P.T0 = (FT)c.T_0;
   P.pref = (FT)c.p_ref; P.kappa = (FT)c.R_d / (FT)c.cp_d; P.Tmin_ref = (FT)c.T_min_ref;
   P.Tsfc_ref = (FT)c.T_surf_ref; P.Tmin_sgs = (FT)c.T_min_sgs;
+  P.icvd = (FT)(1.0 / c.cv_d); P.ipref = (FT)(1.0 / c.p_ref);
   P.nu_v = (FT)c.nu_v; P.nu_s = (FT)c.nu_s; P.div_damp = (FT)c.div_damp; P.dt_model = (FT)c.dt;
   P.upwinding = c.upwinding;
-  for (int n = 0; n < NN; ++n) P.W[n] = (FT)g.W[n];
+  for (int n = 0; n < NN; ++n) { P.W[n] = (FT)g.W[n]; P.iW[n] = (FT)(1.0 / g.W[n]); }
   for (int i = 0; i < NQ; ++i)
     for (int k = 0; k < NQ; ++k) P.D[i * NQ + k] = (FT)g.D[i][k];
   P.hgeo = (const FT *)I->hgeo.p; P.levc = (const FT *)I->levc.p; P.levf = (const FT *)I->levf.p;
@@ -240,6 +241,7 @@ void enqueue_step(gb_ctx *ctx, FT *Yc, FT *Yf, double dt_, cudaStream_t s) {
     A.U_c = Uc; A.U_f = Uf;
     A.Ti_c = tic(i); A.Ti_f = tif(i);
     A.dtg = dt * (FT)I->ai[i][i];
+    A.idtg = (FT)1 / A.dtg;
     A.rnorm = (double *)I->rnorm.p;
     A.first = i == 1;
     launch_column_stage<FT>(P, A, s);
@@ -349,6 +351,7 @@ int time_kernel_t(gb_ctx *ctx, int kernel, gb_fieldvec Y, int reps, double *ms) 
     A.U_c = (FT *)I->U.p; A.U_f = (FT *)I->U.p + I->NC;
     A.Ti_c = (FT *)I->Ti[3].p; A.Ti_f = (FT *)I->Ti[3].p + I->NR;
     A.dtg = dt * (FT)I->ai[3][3];
+    A.idtg = (FT)1 / A.dtg;
     A.rnorm = (double *)I->rnorm.p;
     A.first = 1;
   }

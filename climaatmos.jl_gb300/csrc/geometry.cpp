@@ -227,6 +227,7 @@ void build_geometry(const gb_config &c, HostGeometry &g) {
       o[HG_F3 * NN + n] = 2.0 * c.omega * g.sinlat[q];
       o[HG_FH1 * NN + n] = g.fh0[q * 2];
       o[HG_FH2 * NN + n] = g.fh0[q * 2 + 1];
+      o[HG_IJH * NN + n] = 1.0 / g.Jh[q];
     }
   g.levc.assign((size_t)LC_N * Nv, 0);
   for (int v = 0; v < Nv; ++v) {
@@ -235,6 +236,8 @@ void build_geometry(const gb_config &c, HostGeometry &g) {
     g.levc[LC_DZ * Nv + v] = g.dzc[v];
     g.levc[LC_PHI * Nv + v] = c.grav * g.zc[v];
     g.levc[LC_BETA * Nv + v] = beta_sponge(g.zc[v], c.sponge_zd, c.z_max, c.alpha_uh);
+    g.levc[LC_IR2 * Nv + v] = 1.0 / (g.rc[v] * g.rc[v]);
+    g.levc[LC_IDZ * Nv + v] = 1.0 / g.dzc[v];
   }
   g.levf.assign((size_t)LF_N * Nf, 0);
   for (int k = 0; k < Nf; ++k) {
@@ -244,6 +247,9 @@ void build_geometry(const gb_config &c, HostGeometry &g) {
     g.levf[LF_RINV * Nf + k] = 1.0 / g.rf[k];
     g.levf[LF_BETA * Nf + k] = beta_sponge(g.zf[k], c.sponge_zd, c.z_max, c.alpha_w);
     g.levf[LF_DPHI * Nf + k] = (k > 0 && k < Nv) ? c.grav * (g.zc[k] - g.zc[k - 1]) : 0.0;
+    g.levf[LF_IR2 * Nf + k] = 1.0 / (g.rf[k] * g.rf[k]);
+    g.levf[LF_IDZ * Nf + k] = 1.0 / g.dzf[k];
+    g.levf[LF_G33 * Nf + k] = 1.0 / (g.dzf[k] * g.dzf[k]);
   }
 }
 

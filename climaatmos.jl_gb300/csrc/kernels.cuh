@@ -56,7 +56,7 @@ struct StageArgs {
   int nsrc;
   FT *U_c, *U_f;    // stage state out
   FT *Ti_c, *Ti_f;  // implicit tendency of this stage out (reduced)
-  FT dtg;
+  FT dtg, idtg;
   double *rnorm;    // [ncols][3] residual sums of squares (accumulated)
   int first;        // 1: overwrite rnorm, 0: accumulate
 };

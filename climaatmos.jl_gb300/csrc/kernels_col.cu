@@ -60,8 +60,8 @@ __device__ __forceinline__ void pcr_level(FT (&a)[M], FT (&b)[M], FT (&c)[M], FT
   for (int k = 0; k < M; ++k) {
     const int r = lane * M + k;
     const bool hm = r - S >= 0, hp = r + S < 32 * M;
-    const FT al = hm ? -a[k] / bm[k] : FT(0);
-    const FT ga = hp ? -c[k] / bp[k] : FT(0);
+    const FT al = hm ? -gdiv(a[k], bm[k]) : FT(0);
+    const FT ga = hp ? -gdiv(c[k], bp[k]) : FT(0);
     const FT na = hm ? al * am[k] : FT(0);
     const FT nc = hp ? ga * cp[k] : FT(0);
     FT nbv = b[k], ndv = d[k];
@@ -81,7 +81,42 @@ __device__ __forceinline__ void pcr_solve(FT (&a)[M], FT (&b)[M], FT (&c)[M], FT
   if constexpr (M >= 2) pcr_level<FT, M, 32>(a, b, c, d, lane);
   if constexpr (M >= 4) pcr_level<FT, M, 64>(a, b, c, d, lane);
 #pragma unroll
-  for (int k = 0; k < M; ++k) x[k] = d[k] / b[k];
+  for (int k = 0; k < M; ++k) x[k] = gdiv(d[k], b[k]);
+}
+
+// Two rows per lane: one cyclic-reduction level eliminates the odd rows
+// (row 2l-1 comes from the previous lane), parallel cyclic reduction solves
+// the 32 even rows across the warp, and the odd rows are back-substituted.
+template <class FT>
+__device__ __forceinline__ void crpcr_solve2(FT (&a)[2], FT (&b)[2], FT (&c)[2], FT (&d)[2], FT (&x)[2], int lane) {
+  const FT ap = shfl_up(a[1], 1), bp = shfl_up(b[1], 1), cp = shfl_up(c[1], 1), dp = shfl_up(d[1], 1);
+  const bool hm0 = lane > 0;
+  const FT al0 = hm0 ? -gdiv(a[0], bp) : FT(0);
+  const FT ga0 = -gdiv(c[0], b[1]);
+  FT A = hm0 ? al0 * ap : FT(0);
+  FT C = ga0 * c[1];
+  FT B = b[0] + ga0 * a[1];
+  FT Dd = d[0] + ga0 * d[1];
+  if (hm0) { B += al0 * cp; Dd += al0 * dp; }
+#pragma unroll
+  for (int s = 1; s < 32; s <<= 1) {
+    const FT Am = shfl_up(A, s), Bm = shfl_up(B, s), Cm = shfl_up(C, s), Dm = shfl_up(Dd, s);
+    const FT Ap = shfl_down(A, s), Bp = shfl_down(B, s), Cp = shfl_down(C, s), Dp = shfl_down(Dd, s);
+    const bool hm = lane >= s, hp = lane + s < 32;
+    const FT al = hm ? -gdiv(A, Bm) : FT(0);
+    const FT ga = hp ? -gdiv(C, Bp) : FT(0);
+    FT nB = B, nD = Dd;
+    if (hm) { nB += al * Cm; nD += al * Dm; }
+    if (hp) { nB += ga * Ap; nD += ga * Dp; }
+    A = hm ? al * Am : FT(0);
+    C = hp ? ga * Cp : FT(0);
+    B = nB;
+    Dd = nD;
+  }
+  const FT xe = gdiv(Dd, B);
+  const FT xn = shfl_down(xe, 1);
+  x[0] = xe;
+  x[1] = gdiv(d[1] - a[1] * xe - (lane < 31 ? c[1] * xn : FT(0)), b[1]);
 }
 
 // Column-local thermodynamic state at the owned levels.
@@ -91,12 +126,20 @@ struct ColState {
 };
 template <class FT, int M>
 struct ColDiag {
-  FT c1[M], c2[M], K[M], T[M], h[M], Pi[M], thv[M], thvr[M], phir[M], rJ[M], u3c[M], J[M];
+  FT c1[M], c2[M], K[M], T[M], h[M], Pi[M], thv[M], thvr[M], phir[M], rJ[M], u3c[M], J[M], iJ[M];
 };
 
 template <class FT>
 struct ColGeo {
-  FT Jh, gu0, gu1, gu2;
+  FT Jh, iJh, gu0, gu1, gu2;
+  __device__ void load(const DevParams<FT> &P, int e, int n) {
+    const FT *hg = P.hgeo + (size_t)e * HG_N * NN;
+    Jh = hg[HG_JH * NN + n];
+    iJh = hg[HG_IJH * NN + n];
+    gu0 = hg[HG_GU0 * NN + n];
+    gu1 = hg[HG_GU1 * NN + n];
+    gu2 = hg[HG_GU2 * NN + n];
+  }
 };
 
 template <class FT, int M>
@@ -106,8 +149,7 @@ __device__ __forceinline__ void col_diag(const DevParams<FT> &P, const ColGeo<FT
 #pragma unroll
   for (int k = 0; k < M; ++k) {
     const int f = min(lane * M + k, Nf - 1);
-    const FT dz = P.levf[LF_DZ * Nf + f];
-    Dg.u3c[k] = S.u3[k] / (dz * dz);
+    Dg.u3c[k] = S.u3[k] * P.levf[LF_G33 * Nf + f];
   }
   FT u3n[M], u3cn[M];
   nb_all<M, 1>(S.u3, u3n);
@@ -116,7 +158,8 @@ __device__ __forceinline__ void col_diag(const DevParams<FT> &P, const ColGeo<FT
   for (int k = 0; k < M; ++k) {
     const int v = min(lane * M + k, Nv - 1);
     const FT r2 = P.levc[LC_R2 * Nv + v], dz = P.levc[LC_DZ * Nv + v], Phi = P.levc[LC_PHI * Nv + v];
-    const FT gu0 = G.gu0 / r2, gu1 = G.gu1 / r2, gu2 = G.gu2 / r2;
+    const FT ir2 = P.levc[LC_IR2 * Nv + v];
+    const FT gu0 = G.gu0 * ir2, gu1 = G.gu1 * ir2, gu2 = G.gu2 * ir2;
     const FT c1 = gu0 * S.u1[k] + gu1 * S.u2[k], c2 = gu1 * S.u1[k] + gu2 * S.u2[k];
     const FT kv = (S.u3[k] * Dg.u3c[k] + u3n[k] * u3cn[k]) / FT(2);
     const FT K = (S.u1[k] * c1 + S.u2[k] * c2 + kv) / FT(2);
@@ -125,6 +168,7 @@ __device__ __forceinline__ void col_diag(const DevParams<FT> &P, const ColGeo<FT
     Dg.c1[k] = c1; Dg.c2[k] = c2; Dg.K[k] = K; Dg.T[k] = th.T; Dg.h[k] = th.h; Dg.Pi[k] = th.Pi;
     Dg.thv[k] = th.thv; Dg.thvr[k] = th.thvr; Dg.phir[k] = th.phir;
     Dg.J[k] = G.Jh * r2 * dz;
+    Dg.iJ[k] = G.iJh * ir2 * P.levc[LC_IDZ * Nv + v];
     Dg.rJ[k] = S.rho[k] * Dg.J[k];
   }
 }
@@ -143,13 +187,11 @@ __device__ __forceinline__ void col_implicit(const DevParams<FT> &P, const ColGe
     const int f = lane * M + k;
     const bool inner = f > 0 && f < Nv;
     const int fc = min(f, Nf - 1);
-    const FT dzf = P.levf[LF_DZ * Nf + fc], r2 = P.levf[LF_R2 * Nf + fc];
-    const FT Jf = G.Jh * r2 * dzf;
     const FT rJ = (rJm[k] + Dg.rJ[k]) / FT(2);
-    const FT F = rJ / Jf * Dg.u3c[k];
+    const FT F = rJ * Dg.u3c[k];   // ᶜadvdivᵥ(ᶠinterp(ρJ)/ᶠJ u³): the face Jacobian cancels
     const FT hb = (hm[k] + Dg.h[k]) / FT(2);
-    flux[k] = inner ? Jf * F : FT(0);
-    fh[k] = inner ? Jf * F * hb : FT(0);
+    flux[k] = inner ? F : FT(0);
+    fh[k] = inner ? F * hb : FT(0);
     FT val = 0;
     if (inner) {
       const FT gPhir = Dg.phir[k] - phm[k];
@@ -165,8 +207,8 @@ __device__ __forceinline__ void col_implicit(const DevParams<FT> &P, const ColGe
   nb_all<M, 1>(fh, fhn);
 #pragma unroll
   for (int k = 0; k < M; ++k) {
-    Tr[k] = -((fln[k] - flux[k]) / Dg.J[k]);
-    Te[k] = -((fhn[k] - fh[k]) / Dg.J[k]);
+    Tr[k] = -((fln[k] - flux[k]) * Dg.iJ[k]);
+    Te[k] = -((fhn[k] - fh[k]) * Dg.iJ[k]);
   }
 }
 
@@ -182,7 +224,7 @@ template <class FT, int M>
 __device__ __forceinline__ void col_jacobian(const DevParams<FT> &P, const ColGeo<FT> &G, const ColState<FT, M> &S,
                                              const ColDiag<FT, M> &Dg, FT dtg, ColJac<FT, M> &Jc, int lane) {
   const int Nv = P.Nv, Nf = P.Nf;
-  const FT kap = P.Rd / P.cvd;
+  const FT kap = P.Rd * P.icvd;
   FT rJm[M], hm[M], rhom[M], Km[M], thm[M], Pim[M], c1m[M], c2m[M], u3cm[M], u3cp[M];
   nb_all<M, -1>(Dg.rJ, rJm); nb_all<M, -1>(Dg.h, hm); nb_all<M, -1>(S.rho, rhom); nb_all<M, -1>(Dg.K, Km);
   nb_all<M, -1>(Dg.thv, thm); nb_all<M, -1>(Dg.Pi, Pim); nb_all<M, -1>(Dg.c1, c1m); nb_all<M, -1>(Dg.c2, c2m);
@@ -194,8 +236,7 @@ __device__ __forceinline__ void col_jacobian(const DevParams<FT> &P, const ColGe
     const int f = lane * M + k;
     const bool inner = f > 0 && f < Nv;
     const int fc = min(f, Nf - 1);
-    const FT dzf = P.levf[LF_DZ * Nf + fc];
-    const FT g33 = FT(1) / (dzf * dzf);
+    const FT g33 = P.levf[LF_G33 * Nf + fc];
     const FT rJ = (rJm[k] + Dg.rJ[k]) / FT(2);
     fr[k] = inner ? rJ * g33 : FT(0);
     fhb[k] = (hm[k] + Dg.h[k]) / FT(2);
@@ -205,8 +246,7 @@ __device__ __forceinline__ void col_jacobian(const DevParams<FT> &P, const ColGe
   nb_all<M, 1>(fhb, fhbn);
 #pragma unroll
   for (int k = 0; k < M; ++k) {
-    const FT J = Dg.J[k];
-    const FT v0 = fr[k] / J, v1 = -frn[k] / J;
+    const FT v0 = fr[k] * Dg.iJ[k], v1 = -frn[k] * Dg.iJ[k];
     Jc.ru0[k] = dtg * v0;
     Jc.ru1[k] = dtg * v1;
     Jc.eu0[k] = dtg * (v0 * fhb[k]);
@@ -218,22 +258,23 @@ __device__ __forceinline__ void col_jacobian(const DevParams<FT> &P, const ColGe
       const int va = f - 1;
       const FT ra = rhom[k], rb = S.rho[k];
       const FT rbar = (ra + rb) / FT(2);
+      const FT irb = grcp(rbar);
       const FT dpa = kap * (P.T0 * P.cpd - Km[k] - P.levc[LC_PHI * Nv + va]);
       const FT dpb = kap * (P.T0 * P.cpd - Dg.K[k] - P.levc[LC_PHI * Nv + f]);
       const FT thvb = (thm[k] + Dg.thv[k]) / FT(2);
       const FT gPi = Dg.Pi[k] - Pim[k];
-      const FT buoy = P.cpd * thvb * gPi / rbar;
-      Jc.ur0[k] = dtg * (dpa / rbar + buoy / FT(2));
-      Jc.ur1[k] = dtg * (-dpb / rbar + buoy / FT(2));
-      Jc.ue0[k] = dtg * (kap / rbar);
-      Jc.ue1[k] = dtg * (-kap / rbar);
-      Jc.uh0[k] = dtg * (-kap * ra / rbar) * c1m[k];
-      Jc.uh1[k] = dtg * (-kap * ra / rbar) * c2m[k];
-      Jc.uh2[k] = dtg * (kap * rb / rbar) * Dg.c1[k];
-      Jc.uh3[k] = dtg * (kap * rb / rbar) * Dg.c2[k];
-      Jc.uu0[k] = dtg * (-kap * ra * u3cm[k] / (FT(2) * rbar));
-      Jc.uu1[k] = dtg * (kap * (rb - ra) * Dg.u3c[k] / (FT(2) * rbar) - beta) - FT(1);
-      Jc.uu2[k] = dtg * (kap * rb * u3cp[k] / (FT(2) * rbar));
+      const FT buoy = P.cpd * thvb * gPi * irb;
+      Jc.ur0[k] = dtg * (dpa * irb + buoy / FT(2));
+      Jc.ur1[k] = dtg * (-dpb * irb + buoy / FT(2));
+      Jc.ue0[k] = dtg * (kap * irb);
+      Jc.ue1[k] = dtg * (-kap * irb);
+      Jc.uh0[k] = dtg * (-kap * ra * irb) * c1m[k];
+      Jc.uh1[k] = dtg * (-kap * ra * irb) * c2m[k];
+      Jc.uh2[k] = dtg * (kap * rb * irb) * Dg.c1[k];
+      Jc.uh3[k] = dtg * (kap * rb * irb) * Dg.c2[k];
+      Jc.uu0[k] = dtg * (-kap * ra * u3cm[k] * (irb / FT(2)));
+      Jc.uu1[k] = dtg * (kap * (rb - ra) * Dg.u3c[k] * (irb / FT(2)) - beta) - FT(1);
+      Jc.uu2[k] = dtg * (kap * rb * u3cp[k] * (irb / FT(2)));
     } else {
       Jc.ur0[k] = Jc.ur1[k] = Jc.ue0[k] = Jc.ue1[k] = FT(0);
       Jc.uh0[k] = Jc.uh1[k] = Jc.uh2[k] = Jc.uh3[k] = FT(0);
@@ -275,7 +316,8 @@ __device__ __forceinline__ void col_ldiv(const DevParams<FT> &P, const ColJac<FT
     if (f >= Nf) { aa = FT(0); bb = FT(1); cc = FT(0); rhs = FT(0); }
     a[k] = aa; b[k] = bb; c[k] = cc; d[k] = rhs;
   }
-  pcr_solve<FT, M>(a, b, c, d, x, lane);
+  if constexpr (M == 2) crpcr_solve2<FT>(a, b, c, d, x, lane);
+  else pcr_solve<FT, M>(a, b, c, d, x, lane);
   FT xn[M];
   nb_all<M, 1>(x, xn);
 #pragma unroll
@@ -320,22 +362,20 @@ __device__ __forceinline__ void col_correction(const DevParams<FT> &P, const Col
   for (int k = 0; k < M; ++k) {
     const int f = lane * M + k;
     const bool inner = f > 0 && f < Nv;
-    const int fc = min(f, Nf - 1);
-    const FT Jf = G.Jh * P.levf[LF_R2 * Nf + fc] * P.levf[LF_DZ * Nf + fc];
     const FT rJ = (rJm[k] + Dg.rJ[k]) / FT(2);
     const FT u = Dg.u3c[k];
     const bool near = f == 1 || f == Nv - 1;
     const FT vl = vanleer(u, hm2[k], hm1[k], Dg.h[k], hp1[k], near, P.dt_model);
-    fup[k] = inner ? Jf * (rJ / Jf * vl) : FT(0);
-    fcen[k] = inner ? Jf * (rJ / Jf * (u * (hm1[k] + Dg.h[k]) / FT(2))) : FT(0);
+    fup[k] = inner ? rJ * vl : FT(0);
+    fcen[k] = inner ? rJ * (u * (hm1[k] + Dg.h[k]) / FT(2)) : FT(0);
   }
   FT fupn[M], fcn[M];
   nb_all<M, 1>(fup, fupn);
   nb_all<M, 1>(fcen, fcn);
 #pragma unroll
   for (int k = 0; k < M; ++k) {
-    const FT vup = -((fupn[k] - fup[k]) / Dg.J[k]);
-    const FT vc = -((fcn[k] - fcen[k]) / Dg.J[k]);
+    const FT vup = -((fupn[k] - fup[k]) * Dg.iJ[k]);
+    const FT vc = -((fcn[k] - fcen[k]) * Dg.iJ[k]);
     corr[k] = vup - vc;
   }
 }
@@ -345,7 +385,10 @@ __device__ __forceinline__ size_t cidx(int e, int c, int n, int v, int Nv) { ret
 template <class FT>
 __device__ __forceinline__ size_t ridx(int e, int c, int n, int v, int Nv) { return (((size_t)e * 2 + c) * NN + n) * Nv + v; }
 
-template <class FT, int M>
+// STG = stage index i (1..3): explicit sources j < STG, implicit sources 1 <= j < STG
+// (the nonzero pattern of the ARS343 tableau).  All loads are issued before
+// the sums so that each lane has its ~50 independent loads in flight at once.
+template <class FT, int M, int STG>
 __global__ void __launch_bounds__(COL_THREADS) k_col_stage(DevParams<FT> P, StageArgs<FT> A) {
   const int lane = threadIdx.x & 31;
   const int col = blockIdx.x * (COL_THREADS / 32) + (threadIdx.x >> 5);
@@ -353,39 +396,52 @@ __global__ void __launch_bounds__(COL_THREADS) k_col_stage(DevParams<FT> P, Stag
   if (col >= ncols) return;
   const int e = col >> 4, n = col & 15, Nv = P.Nv, Nf = P.Nf;
   ColGeo<FT> G;
-  const FT *hg = P.hgeo + (size_t)e * HG_N * NN;
-  G.Jh = hg[HG_JH * NN + n]; G.gu0 = hg[HG_GU0 * NN + n]; G.gu1 = hg[HG_GU1 * NN + n]; G.gu2 = hg[HG_GU2 * NN + n];
-  // ---- stage assembly
+  G.load(P, e, n);
+  // ---- stage assembly U^ = u_n + sum_j (ce_j T_exp_j + ci_j T_imp_j), summed in j order
+  FT un[5][M], te[STG][5][M], ti[STG][3][M];
+  const size_t cb = (size_t)e * 4 * NN * Nv + (size_t)n * Nv;   // centre comp 0 of this column
+  const size_t rb = (size_t)e * 2 * NN * Nv + (size_t)n * Nv;   // reduced centre comp 0
+  const size_t fb = ((size_t)e * NN + n) * Nf;
+#pragma unroll
+  for (int k = 0; k < M; ++k) {
+    const int v = lane * M + k;
+    const int vc = min(v, Nv - 1), vf = min(v, Nf - 1);
+#pragma unroll
+    for (int c = 0; c < 4; ++c) un[c][k] = A.un_c[cb + (size_t)c * NN * Nv + vc];
+    un[4][k] = A.un_f[fb + vf];
+#pragma unroll
+    for (int j = 0; j < STG; ++j) {
+#pragma unroll
+      for (int c = 0; c < 4; ++c) te[j][c][k] = A.te_c[j][cb + (size_t)c * NN * Nv + vc];
+      te[j][4][k] = A.te_f[j][fb + vf];
+      if (j >= 1) {
+        ti[j][0][k] = A.ti_c[j][rb + vc];
+        ti[j][1][k] = A.ti_c[j][rb + (size_t)NN * Nv + vc];
+        ti[j][2][k] = A.ti_f[j][fb + vf];
+      }
+    }
+  }
   ColState<FT, M> H;  // U^
 #pragma unroll
   for (int k = 0; k < M; ++k) {
     const int v = lane * M + k;
     const bool cv = v < Nv, fv = v < Nf;
-    FT x[5] = {0, 0, 0, 0, 0};
-    if (cv) {
-      for (int c = 0; c < 4; ++c) {
-        const size_t q = cidx<FT>(e, c, n, v, Nv);
-        FT s = A.un_c[q];
-        for (int j = 0; j < A.nsrc; ++j) {
-          if (A.te_c[j]) s += A.ce[j] * A.te_c[j][q];
-          if (A.ti_c[j] && (c == 0 || c == 3)) s += A.ci[j] * A.ti_c[j][ridx<FT>(e, c == 3, n, v, Nv)];
-        }
-        x[c] = s;
+    FT x[5];
+#pragma unroll
+    for (int c = 0; c < 5; ++c) {
+      FT s = un[c][k];
+#pragma unroll
+      for (int j = 0; j < STG; ++j) {
+        s += A.ce[j] * te[j][c][k];
+        if (j >= 1 && c != 1 && c != 2) s += A.ci[j] * ti[j][c == 0 ? 0 : (c == 3 ? 1 : 2)][k];
       }
-    }
-    if (fv) {
-      const size_t q = ((size_t)e * NN + n) * Nf + v;
-      FT s = A.un_f[q];
-      for (int j = 0; j < A.nsrc; ++j) {
-        if (A.te_f[j]) s += A.ce[j] * A.te_f[j][q];
-        if (A.ti_f[j]) s += A.ci[j] * A.ti_f[j][q];
-      }
-      x[4] = s;
+      x[c] = s;
     }
     H.rho[k] = cv ? x[0] : FT(1);
-    H.u1[k] = x[1]; H.u2[k] = x[2];
+    H.u1[k] = cv ? x[1] : FT(0);
+    H.u2[k] = cv ? x[2] : FT(0);
     H.rhoe[k] = cv ? x[3] : FT(1);
-    H.u3[k] = x[4];
+    H.u3[k] = fv ? x[4] : FT(0);
   }
   // ---- filter and precomputed quantities at U = filtered U^
   ColState<FT, M> U = H;
@@ -411,9 +467,9 @@ __global__ void __launch_bounds__(COL_THREADS) k_col_stage(DevParams<FT> P, Stag
     Ru1[k] = FT(0);
     Ru2[k] = FT(0);
     R3[k] = fv ? H.u3[k] + dtg * T3[k] - U.u3[k] : FT(0);
-    ss[0] += (double)Rr[k] * (double)Rr[k];
-    ss[1] += (double)Re[k] * (double)Re[k];
-    ss[2] += (double)R3[k] * (double)R3[k];
+    ss[0] += (double)(Rr[k] * Rr[k]);
+    ss[1] += (double)(Re[k] * Re[k]);
+    ss[2] += (double)(R3[k] * R3[k]);
     finite = finite && isfinite(Rr[k]) && isfinite(Re[k]) && isfinite(R3[k]);
   }
   ColJac<FT, M> Jc;
@@ -436,6 +492,7 @@ __global__ void __launch_bounds__(COL_THREADS) k_col_stage(DevParams<FT> P, Stag
     for (int k = 0; k < M; ++k) U.rhoe[k] += dtg * corr[k];
   }
   // ---- outputs: U, T_imp = (U - U^) / dtgamma, residual sums of squares
+  const FT idtg = A.idtg;
 #pragma unroll
   for (int k = 0; k < M; ++k) {
     const int v = lane * M + k;
@@ -444,13 +501,13 @@ __global__ void __launch_bounds__(COL_THREADS) k_col_stage(DevParams<FT> P, Stag
       A.U_c[cidx<FT>(e, 1, n, v, Nv)] = U.u1[k];
       A.U_c[cidx<FT>(e, 2, n, v, Nv)] = U.u2[k];
       A.U_c[cidx<FT>(e, 3, n, v, Nv)] = U.rhoe[k];
-      A.Ti_c[ridx<FT>(e, 0, n, v, Nv)] = (U.rho[k] - H.rho[k]) / dtg;
-      A.Ti_c[ridx<FT>(e, 1, n, v, Nv)] = (U.rhoe[k] - H.rhoe[k]) / dtg;
+      A.Ti_c[ridx<FT>(e, 0, n, v, Nv)] = (U.rho[k] - H.rho[k]) * idtg;
+      A.Ti_c[ridx<FT>(e, 1, n, v, Nv)] = (U.rhoe[k] - H.rhoe[k]) * idtg;
     }
     if (v < Nf) {
       const size_t q = ((size_t)e * NN + n) * Nf + v;
       A.U_f[q] = U.u3[k];
-      A.Ti_f[q] = (U.u3[k] - H.u3[k]) / dtg;
+      A.Ti_f[q] = (U.u3[k] - H.u3[k]) * idtg;
     }
   }
 #pragma unroll
@@ -474,8 +531,7 @@ __global__ void __launch_bounds__(COL_THREADS) k_col_hook(DevParams<FT> P, ColAr
   if (col >= ncols) return;
   const int e = col >> 4, n = col & 15, Nv = P.Nv, Nf = P.Nf;
   ColGeo<FT> G;
-  const FT *hg = P.hgeo + (size_t)e * HG_N * NN;
-  G.Jh = hg[HG_JH * NN + n]; G.gu0 = hg[HG_GU0 * NN + n]; G.gu1 = hg[HG_GU1 * NN + n]; G.gu2 = hg[HG_GU2 * NN + n];
+  G.load(P, e, n);
   ColState<FT, M> S;
 #pragma unroll
   for (int k = 0; k < M; ++k) {
@@ -554,13 +610,24 @@ inline int levels_per_lane(int Nf) { return Nf <= 32 ? 1 : (Nf <= 64 ? 2 : 4); }
 
 }  // namespace
 
+template <class FT, int M>
+void launch_stage_m(const DevParams<FT> &P, const StageArgs<FT> &A, int grid, cudaStream_t s) {
+  switch (A.nsrc) {
+    case 1: k_col_stage<FT, M, 1><<<grid, COL_THREADS, 0, s>>>(P, A); break;
+    case 2: k_col_stage<FT, M, 2><<<grid, COL_THREADS, 0, s>>>(P, A); break;
+    default: k_col_stage<FT, M, 3><<<grid, COL_THREADS, 0, s>>>(P, A); break;
+  }
+}
+
+// A.nsrc = stage index (1..3); all explicit sources j < nsrc and implicit
+// sources 1 <= j < nsrc must be present (the ARS343 nonzero pattern).
 template <class FT>
 void launch_column_stage(const DevParams<FT> &P, const StageArgs<FT> &A, cudaStream_t s) {
   const int ncols = P.Nh * NN, grid = (ncols + COL_THREADS / 32 - 1) / (COL_THREADS / 32);
   switch (levels_per_lane(P.Nf)) {
-    case 1: k_col_stage<FT, 1><<<grid, COL_THREADS, 0, s>>>(P, A); break;
-    case 2: k_col_stage<FT, 2><<<grid, COL_THREADS, 0, s>>>(P, A); break;
-    default: k_col_stage<FT, 4><<<grid, COL_THREADS, 0, s>>>(P, A); break;
+    case 1: launch_stage_m<FT, 1>(P, A, grid, s); break;
+    case 2: launch_stage_m<FT, 2>(P, A, grid, s); break;
+    default: launch_stage_m<FT, 4>(P, A, grid, s); break;
   }
 }
 

@@ -67,9 +67,11 @@ struct Nodal {
 
 template <class FT>
 struct NodeGeo {
-  FT Jh, gu0, gu1, gu2, gd0, gd1, gd2, f3, fh1, fh2, W;
+  FT Jh, iJh, gu0, gu1, gu2, gd0, gd1, gd2, f3, fh1, fh2, W, iW;
   __device__ void load(const FT *sG, const DevParams<FT> &P, int n) {
     Jh = sG[HG_JH * NN + n];
+    iJh = sG[HG_IJH * NN + n];
+    iW = P.iW[n];
     gu0 = sG[HG_GU0 * NN + n]; gu1 = sG[HG_GU1 * NN + n]; gu2 = sG[HG_GU2 * NN + n];
     gd0 = sG[HG_GD0 * NN + n]; gd1 = sG[HG_GD1 * NN + n]; gd2 = sG[HG_GD2 * NN + n];
     f3 = sG[HG_F3 * NN + n]; fh1 = sG[HG_FH1 * NN + n]; fh2 = sG[HG_FH2 * NN + n];
@@ -80,11 +82,13 @@ struct NodeGeo {
 // Slab geometry at one level: full Jacobian and metric with deep-atmosphere scaling.
 template <class FT>
 struct LevGeo {
-  FT J, WJ, gu0, gu1, gu2, gd0, gd1, gd2, G33;
-  __device__ void set(const NodeGeo<FT> &g, FT r2, FT dz) {
+  FT J, iJ, WJ, iWJ, gu0, gu1, gu2, gd0, gd1, gd2, G33;
+  __device__ void set(const NodeGeo<FT> &g, FT r2, FT ir2, FT dz, FT idz) {
     J = g.Jh * r2 * dz;
+    iJ = g.iJh * ir2 * idz;
     WJ = g.W * J;
-    gu0 = g.gu0 / r2; gu1 = g.gu1 / r2; gu2 = g.gu2 / r2;
+    iWJ = g.iW * iJ;
+    gu0 = g.gu0 * ir2; gu1 = g.gu1 * ir2; gu2 = g.gu2 * ir2;
     gd0 = g.gd0 * r2; gd1 = g.gd1 * r2; gd2 = g.gd2 * r2;
     G33 = dz * dz;
   }
@@ -92,18 +96,18 @@ struct LevGeo {
 
 // C123(wgrad(div u)) * fdiv - C123(wcurl(C123(curl u))) for covariant (c1, c2, c3)
 template <class FT>
-__device__ __forceinline__ void vec_lap(const Nodal<FT> &N, const LevGeo<FT> &s, FT W, FT c1, FT c2, FT c3, FT fdiv,
-                                        FT &o1, FT &o2, FT &o3) {
+__device__ __forceinline__ void vec_lap(const Nodal<FT> &N, const LevGeo<FT> &s, FT W, FT iW, FT c1, FT c2, FT c3,
+                                        FT fdiv, FT &o1, FT &o2, FT &o3) {
   FT F1 = s.gu0 * c1 + s.gu1 * c2, F2 = s.gu1 * c1 + s.gu2 * c2;
-  FT dv = (N.d1(s.J * F1) + N.d2(s.J * F2)) / s.J;
+  FT dv = (N.d1(s.J * F1) + N.d2(s.J * F2)) * s.iJ;
   FT wdv = W * dv;
-  FT w1 = -N.t1(wdv) / W, w2 = -N.t2(wdv) / W;
-  FT k3 = (N.d1(c2) - N.d2(c1)) / s.J;
-  FT k1 = N.d2(c3) / s.J, k2 = -N.d1(c3) / s.J;
+  FT w1 = -N.t1(wdv) * iW, w2 = -N.t2(wdv) * iW;
+  FT k3 = (N.d1(c2) - N.d2(c1)) * s.iJ;
+  FT k1 = N.d2(c3) * s.iJ, k2 = -N.d1(c3) * s.iJ;
   FT z1 = s.gd0 * k1 + s.gd1 * k2, z2 = s.gd1 * k1 + s.gd2 * k2, z3 = s.G33 * k3;
-  FT q3 = (-N.t1(W * z2) + N.t2(W * z1)) / s.WJ;
+  FT q3 = (-N.t1(W * z2) + N.t2(W * z1)) * s.iWJ;
   FT Wz3 = W * z3;
-  FT q1 = -N.t2(Wz3) / s.WJ, q2 = N.t1(Wz3) / s.WJ;
+  FT q1 = -N.t2(Wz3) * s.iWJ, q2 = N.t1(Wz3) * s.iWJ;
   o1 = fdiv * w1 - (s.gd0 * q1 + s.gd1 * q2);
   o2 = fdiv * w2 - (s.gd1 * q1 + s.gd2 * q2);
   o3 = -s.G33 * q3;
@@ -149,8 +153,7 @@ __device__ void centre_from_faces(const DevParams<FT> &P, const FT *sF, FT *sU3,
     const int n = idx / Nv, v = idx - n * Nv;
     FT a = v == 0 ? FT(0) : sF[n * Nf + v];
     FT b = v + 1 == Nv ? FT(0) : sF[n * Nf + v + 1];
-    FT da = P.levf[LF_DZ * Nf + v], db = P.levf[LF_DZ * Nf + v + 1];
-    FT ua = a / (da * da), ub = b / (db * db);
+    FT ua = a * P.levf[LF_G33 * Nf + v], ub = b * P.levf[LF_G33 * Nf + v + 1];
     sU3[idx] = (a + b) / FT(2);
     sKv[idx] = (a * ua + b * ub) / FT(2);
   }
@@ -183,7 +186,7 @@ __global__ void __launch_bounds__(SE_THREADS) k_passA(DevParams<FT> P, const FT 
     const int v = min(v0 + vl, Nv - 1);
     const bool act = v0 + vl < Nv;
     LevGeo<FT> s;
-    s.set(g, P.levc[LC_R2 * Nv + v], P.levc[LC_DZ * Nv + v]);
+    s.set(g, P.levc[LC_R2 * Nv + v], P.levc[LC_IR2 * Nv + v], P.levc[LC_DZ * Nv + v], P.levc[LC_IDZ * Nv + v]);
     const FT Phi = P.levc[LC_PHI * Nv + v];
     const int q = n * Nv + v;
     const FT rho = sY[q], u1 = sY[16 * Nv + q], u2 = sY[32 * Nv + q], rhoe = sY[48 * Nv + q];
@@ -193,11 +196,11 @@ __global__ void __launch_bounds__(SE_THREADS) k_passA(DevParams<FT> P, const FT 
     Thermo<FT> th;
     thermo(P, rho, rhoe, K, Phi, th);
     FT o1, o2, o3;
-    vec_lap(N, s, g.W, u1, u2, ub3, FT(1), o1, o2, o3);
+    vec_lap(N, s, g.W, g.iW, u1, u2, ub3, FT(1), o1, o2, o3);
     const FT sd = P.cpd * (th.T - P.T0) + Phi - sd_r(P, th.Pi, th.phir);
     const FT g1 = N.d1(sd), g2 = N.d2(sd);
     const FT x1 = s.gu0 * g1 + s.gu1 * g2, x2 = s.gu1 * g1 + s.gu2 * g2;
-    const FT Ls = -(N.t1(s.WJ * x1) + N.t2(s.WJ * x2)) / s.WJ;
+    const FT Ls = -(N.t1(s.WJ * x1) + N.t2(s.WJ * x2)) * s.iWJ;
     if (act) {
       sO[q] = Ls;
       sO[16 * Nv + q] = o1;
@@ -246,8 +249,8 @@ __global__ void __launch_bounds__(SE_THREADS) k_passB(DevParams<FT> P, const FT 
     const int v = min(v0 + vl, Nv - 1);
     const bool act = v0 + vl < Nv;
     LevGeo<FT> s;
-    const FT dz = P.levc[LC_DZ * Nv + v];
-    s.set(g, P.levc[LC_R2 * Nv + v], dz);
+    const FT dz = P.levc[LC_DZ * Nv + v], idz = P.levc[LC_IDZ * Nv + v];
+    s.set(g, P.levc[LC_R2 * Nv + v], P.levc[LC_IR2 * Nv + v], dz, idz);
     const FT Phi = P.levc[LC_PHI * Nv + v];
     const int q = n * Nv + v;
     const FT rho = sY[q], u1 = sY[16 * Nv + q], u2 = sY[32 * Nv + q], rhoe = sY[48 * Nv + q];
@@ -259,10 +262,10 @@ __global__ void __launch_bounds__(SE_THREADS) k_passB(DevParams<FT> P, const FT 
     const FT h = th.h;
     // rho: -split_div(rho u, 1) = -wdiv(rho u)
     const FT F1 = rho * c1, F2 = rho * c2;
-    const FT dm = -(N.t1(s.WJ * F1) + N.t2(s.WJ * F2)) / s.WJ;
+    const FT dm = -(N.t1(s.WJ * F1) + N.t2(s.WJ * F2)) * s.iWJ;
     FT Trho = -dm;
     // rho e_tot: -split_div(rho u, h)
-    const FT dmh = -(N.t1(s.WJ * (F1 * h)) + N.t2(s.WJ * (F2 * h))) / s.WJ;
+    const FT dmh = -(N.t1(s.WJ * (F1 * h)) + N.t2(s.WJ * (F2 * h))) * s.iWJ;
     const FT ha = N.d1(h), hb = N.d2(h);
     FT Trhoe = -((dmh + h * dm + F1 * ha + F2 * hb) / FT(2));
     // u_h: -[grad(K + Phi - Phi_r) + cp_d (th' grad Pi + grad(th' Pi) - Pi grad th') / 2]
@@ -278,16 +281,16 @@ __global__ void __launch_bounds__(SE_THREADS) k_passB(DevParams<FT> P, const FT 
     // hyperdiffusion: nu (div_damp C123(wgrad div L) - C123(wcurl C123(curl L)))
     const FT Ls = sL[q], L1 = sL[16 * Nv + q], L2 = sL[32 * Nv + q], L3 = sL[48 * Nv + q];
     FT o1, o2, o3;
-    vec_lap(N, s, g.W, L1, L2, L3, P.div_damp, o1, o2, o3);
+    vec_lap(N, s, g.W, g.iW, L1, L2, L3, P.div_damp, o1, o2, o3);
     const FT g1 = N.d1(Ls), g2 = N.d2(Ls);
     const FT x1 = rho * (s.gu0 * g1 + s.gu1 * g2), x2 = rho * (s.gu1 * g1 + s.gu2 * g2);
-    const FT hd = -(N.t1(s.WJ * x1) + N.t2(s.WJ * x2)) / s.WJ;
+    const FT hd = -(N.t1(s.WJ * x1) + N.t2(s.WJ * x2)) * s.iWJ;
     Tu1 -= P.nu_v * o1;
     Tu2 -= P.nu_v * o2;
     Trhoe -= P.nu_s * hd;
     // vorticity: w^3 = wcurl(u_h); (f^3 + w^3) x CT12(u) -> C12
-    const FT om3 = (-N.t1(g.W * u2) + N.t2(g.W * u1)) / s.WJ;
-    const FT a3 = g.f3 / dz + om3;
+    const FT om3 = (-N.t1(g.W * u2) + N.t2(g.W * u1)) * s.iWJ;
+    const FT a3 = g.f3 * idz + om3;
     __syncwarp();
     if (act) {
       sO[q] = Trho;
@@ -311,19 +314,20 @@ __global__ void __launch_bounds__(SE_THREADS) k_passB(DevParams<FT> P, const FT 
     const bool inner = k > 0 && k < Nv;
     const FT u3 = inner ? sF[n * Nf + k] : FT(0);
     const FT r2 = P.levf[LF_R2 * Nf + k], dzf = P.levf[LF_DZ * Nf + k], rinv = P.levf[LF_RINV * Nf + k];
-    const FT Jf = g.Jh * r2 * dzf, WJf = g.W * Jf;
+    const FT Jf = g.Jh * r2 * dzf;
+    const FT iJf = g.iJh * P.levf[LF_IR2 * Nf + k] * P.levf[LF_IDZ * Nf + k], iWJf = g.iW * iJf;
     const FT Wu = g.W * u3;
-    const FT w1 = -N.t2(Wu) / WJf, w2 = N.t1(Wu) / WJf;
+    const FT w1 = -N.t2(Wu) * iWJf, w2 = N.t1(Wu) * iWJf;
     FT cv1 = 0, cv2 = 0, gK = 0, cc1, cc2, l4, rJ;
     const int qa = n * Nv + (k > 0 ? k - 1 : 0), qb = n * Nv + (k < Nv ? k : Nv - 1);
     if (inner) {
-      cv1 = -(sY[32 * Nv + qb] - sY[32 * Nv + qa]) / Jf;
-      cv2 = (sY[16 * Nv + qb] - sY[16 * Nv + qa]) / Jf;
+      cv1 = -(sY[32 * Nv + qb] - sY[32 * Nv + qa]) * iJf;
+      cv2 = (sY[16 * Nv + qb] - sY[16 * Nv + qa]) * iJf;
       cc1 = (sC1[qa] + sC1[qb]) / FT(2);
       cc2 = (sC2[qa] + sC2[qb]) / FT(2);
       gK = sK[qb] - sK[qa];
       const FT wa = sRJ[qa], wb = sRJ[qb];
-      l4 = (wa * sL4[qa] + wb * sL4[qb]) / (wa + wb);
+      l4 = gdiv(wa * sL4[qa] + wb * sL4[qb], wa + wb);
       rJ = (wa + wb) / FT(2);
     } else {
       const int qq = k == 0 ? qb : qa;
@@ -333,7 +337,7 @@ __global__ void __launch_bounds__(SE_THREADS) k_passB(DevParams<FT> P, const FT 
       rJ = sRJ[qq];
     }
     const FT fo1 = g.fh1 * rinv + cv1 + w1, fo2 = g.fh2 * rinv + cv2 + w2;
-    const FT b3 = rJ * (u3 / (dzf * dzf));
+    const FT b3 = rJ * (u3 * P.levf[LF_G33 * Nf + k]);
     FT T3 = -(P.nu_v * l4);
     T3 -= Jf * (fo1 * cc2 - fo2 * cc1) + gK;
     if (act) {
@@ -346,9 +350,9 @@ __global__ void __launch_bounds__(SE_THREADS) k_passB(DevParams<FT> P, const FT 
   // ---- P3: centre u_h part of the face cross products and the sponge (level-fastest)
   for (int idx = threadIdx.x; idx < NN * Nv; idx += blockDim.x) {
     const int nn = idx / Nv, v = idx - nn * Nv;
-    const FT rJ = sRJ[idx];
-    const FT t1v = (sX1[nn * Nf + v] + sX1[nn * Nf + v + 1]) / FT(2) / rJ + sCr1[idx];
-    const FT t2v = (sX2[nn * Nf + v] + sX2[nn * Nf + v + 1]) / FT(2) / rJ + sCr2[idx];
+    const FT irJ = grcp(sRJ[idx]);
+    const FT t1v = (sX1[nn * Nf + v] + sX1[nn * Nf + v + 1]) / FT(2) * irJ + sCr1[idx];
+    const FT t2v = (sX2[nn * Nf + v] + sX2[nn * Nf + v + 1]) / FT(2) * irJ + sCr2[idx];
     const FT beta = P.levc[LC_BETA * Nv + v];
     FT a = sO[16 * Nv + idx] - t1v;
     FT b = sO[32 * Nv + idx] - t2v;

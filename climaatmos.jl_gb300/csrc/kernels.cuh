@@ -4,16 +4,23 @@
 
 namespace gb {
 
-// Shared-memory layouts of the element-slab kernels (byte offsets).
+// Shared-memory layouts of the element-slab kernels (byte offsets).  The
+// input slabs are double-buffered (nbuf = 2) when they fit, else single.
 template <class FT>
 struct PassALayout {
-  size_t y, f, g, u3, kv, out, bar, total;
-  __host__ __device__ PassALayout(int Nv) {
+  size_t y[2], f[2], g[2], u3, kv, out, bar, total;
+  __host__ __device__ PassALayout(int Nv, int nbuf) {
     const int Nf = Nv + 1;
     size_t o = 0;
-    y = o; o += align16(sizeof(FT) * 64 * Nv);
-    f = o; o += align16(sizeof(FT) * 16 * Nf);
-    g = o; o += align16(sizeof(FT) * HG_N * 16);
+    for (int b = 0; b < 2; ++b) {
+      if (b < nbuf) {
+        y[b] = o; o += align16(sizeof(FT) * 64 * Nv);
+        f[b] = o; o += align16(sizeof(FT) * 16 * Nf);
+        g[b] = o; o += align16(sizeof(FT) * HG_N * 16);
+      } else {
+        y[b] = y[0]; f[b] = f[0]; g[b] = g[0];
+      }
+    }
     u3 = o; o += align16(sizeof(FT) * 16 * Nv);
     kv = o; o += align16(sizeof(FT) * 16 * Nv);
     out = o; o += align16(sizeof(FT) * 64 * Nv);
@@ -24,21 +31,30 @@ struct PassALayout {
 
 template <class FT>
 struct PassBLayout {
-  size_t y, f, g, lap, u3, kv, c1, c2, k, rj, l4, out, outf, bar, total;
-  __host__ __device__ PassBLayout(int Nv) {
+  size_t y[2], f[2], g[2], lap[2], kv, c1, c2, k, rj, l4, cr1, cr2, x1, x2, out, outf, bar, total;
+  __host__ __device__ PassBLayout(int Nv, int nbuf) {
     const int Nf = Nv + 1;
     size_t o = 0;
-    y = o; o += align16(sizeof(FT) * 64 * Nv);
-    f = o; o += align16(sizeof(FT) * 16 * Nf);
-    g = o; o += align16(sizeof(FT) * HG_N * 16);
-    lap = o; o += align16(sizeof(FT) * 64 * Nv);  // reused for the face cross products after use
-    u3 = o; o += align16(sizeof(FT) * 16 * Nv);   // reused for the centre cross terms
+    for (int b = 0; b < 2; ++b) {
+      if (b < nbuf) {
+        y[b] = o; o += align16(sizeof(FT) * 64 * Nv);
+        f[b] = o; o += align16(sizeof(FT) * 16 * Nf);
+        g[b] = o; o += align16(sizeof(FT) * HG_N * 16);
+        lap[b] = o; o += align16(sizeof(FT) * 64 * Nv);
+      } else {
+        y[b] = y[0]; f[b] = f[0]; g[b] = g[0]; lap[b] = lap[0];
+      }
+    }
     kv = o; o += align16(sizeof(FT) * 16 * Nv);
     c1 = o; o += align16(sizeof(FT) * 16 * Nv);
     c2 = o; o += align16(sizeof(FT) * 16 * Nv);
     k = o; o += align16(sizeof(FT) * 16 * Nv);
     rj = o; o += align16(sizeof(FT) * 16 * Nv);
     l4 = o; o += align16(sizeof(FT) * 16 * Nv);
+    cr1 = o; o += align16(sizeof(FT) * 16 * Nv);
+    cr2 = o; o += align16(sizeof(FT) * 16 * Nv);
+    x1 = o; o += align16(sizeof(FT) * 16 * Nf);
+    x2 = o; o += align16(sizeof(FT) * 16 * Nf);
     out = o; o += align16(sizeof(FT) * 64 * Nv);
     outf = o; o += align16(sizeof(FT) * 16 * Nf);
     bar = o; o += 16;
@@ -82,7 +98,8 @@ template <class FT> void launch_bc_filter(const DevParams<FT> &P, FT *Yf, cudaSt
 template <class FT> void launch_global_sums(const DevParams<FT> &P, const FT *Yc, double *partials, int nblocks, double *out, cudaStream_t s);
 void launch_reduce_rnorm(const double *rnorm, int ncols, double *out, cudaStream_t s);
 
-// Shared memory needed by the slab kernels (for cudaFuncSetAttribute).
+// Shared memory needed by the slab kernels with single input buffers (the
+// minimum; double buffering is used when it fits).
 template <class FT> size_t passA_smem(int Nv);
 template <class FT> size_t passB_smem(int Nv);
 template <class FT> void configure_se(int Nv);

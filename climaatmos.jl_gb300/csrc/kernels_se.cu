@@ -1,11 +1,17 @@
 // Spectral-element slab kernels of the explicit tendency (remaining_tendency!).
 //
-// One CTA per element: the Nq=4 GLL slab of all levels (state, DSSed
-// Laplacians, per-node metric terms) is staged into shared memory by 1-D TMA
-// bulk copies, horizontal derivatives apply the 4x4 derivative matrix with
-// warp shuffles inside 16-lane groups (one level of one element per group),
-// vertical (face/centre) operators read neighbouring levels from shared memory
-// in a level-fastest mapping, and the finished slab leaves by a TMA bulk store.
+// Persistent CTAs walk the elements.  For each element the Nq=4 GLL slab of
+// all levels (state, DSSed Laplacians, per-node metric terms) is staged into
+// shared memory by 1-D TMA bulk copies, double-buffered where shared memory
+// allows so that the next element's slab streams in while the current one is
+// computed; the finished slab leaves by a TMA bulk store.
+//
+// Thread mapping of the horizontal work: one thread per (level, row j),
+// holding the four nodes n = 4 j + i of that row.  Derivatives along xi^1 are
+// 4x4 matrix-vector products in registers (D from the constant bank);
+// derivatives along xi^2 gather the other rows with shuffles inside the 4-lane
+// group of the level.  Vertical (face/centre) operators read neighbouring
+// levels from shared memory in a level-fastest mapping.
 //
 // pass A = prep_hyperdiffusion_tendency! (src/prognostic_equations/hyperdiffusion.jl:116-147):
 //   L = (grad/curl Laplacian of u_bar, scalar Laplacian of s_d - s_d,r)
@@ -19,380 +25,604 @@ namespace gb {
 
 namespace {
 
-constexpr int SE_THREADS = 256;  // 16 nodes x 16 levels per sweep
+constexpr int SE_THREADS = 256;          // 64 level slots x 4 rows per sweep
+constexpr int SE_LEVELS = SE_THREADS / 4;
 
-// Per-lane nodal derivative helper (lane holds node n = i + 4 j of one level).
+// Row helper: the thread's row j and its xi^2 derivative coefficients.
 template <class FT>
-struct Nodal {
-  int i, j;
-  FT dA[NQ], dB[NQ], tA[NQ], tB[NQ];  // D[i][k], D[j][k], D[k][i], D[k][j]
-  __device__ void init(const DevParams<FT> &P, int n) {
-    i = n & 3;
-    j = n >> 2;
+struct Row {
+  int j;
+  FT dB[NQ], tB[NQ];  // D[j][k], D[k][j]
+  __device__ void init(const DevParams<FT> &P, int jj) {
+    j = jj;
 #pragma unroll
     for (int k = 0; k < NQ; ++k) {
-      dA[k] = P.D[i * NQ + k];
       dB[k] = P.D[j * NQ + k];
-      tA[k] = P.D[k * NQ + i];
       tB[k] = P.D[k * NQ + j];
     }
   }
-  // d1 f = sum_k D[i][k] f(k,j)
-  __device__ FT d1(FT f) const {
+};
+
+// o[i] = sum_k D[i][k] f[k]   (d/dxi^1, register-local)
+template <class FT>
+__device__ __forceinline__ void d1(const DevParams<FT> &P, const FT (&f)[4], FT (&o)[4]) {
+#pragma unroll
+  for (int i = 0; i < NQ; ++i) {
     FT s = 0;
 #pragma unroll
-    for (int k = 0; k < NQ; ++k) s += dA[k] * shfl(f, NQ * j + k, 16);
-    return s;
+    for (int k = 0; k < NQ; ++k) s += P.D[i * NQ + k] * f[k];
+    o[i] = s;
   }
-  __device__ FT d2(FT f) const {
+}
+// o[i] = sum_k D[k][i] f[k]   (transpose: weak forms)
+template <class FT>
+__device__ __forceinline__ void t1(const DevParams<FT> &P, const FT (&f)[4], FT (&o)[4]) {
+#pragma unroll
+  for (int i = 0; i < NQ; ++i) {
     FT s = 0;
 #pragma unroll
-    for (int k = 0; k < NQ; ++k) s += dB[k] * shfl(f, i + NQ * k, 16);
-    return s;
+    for (int k = 0; k < NQ; ++k) s += P.D[k * NQ + i] * f[k];
+    o[i] = s;
   }
-  // t1 f = sum_k D[k][i] f(k,j)
-  __device__ FT t1(FT f) const {
+}
+// o[i] = sum_k C[k] f(i, row k): the rows are gathered from the level's 4-lane group
+template <class FT>
+__device__ __forceinline__ void across(const FT (&C)[NQ], const FT (&f)[4], FT (&o)[4]) {
+#pragma unroll
+  for (int i = 0; i < NQ; ++i) {
     FT s = 0;
 #pragma unroll
-    for (int k = 0; k < NQ; ++k) s += tA[k] * shfl(f, NQ * j + k, 16);
-    return s;
+    for (int k = 0; k < NQ; ++k) s += C[k] * shfl(f[i], k, 4);
+    o[i] = s;
   }
-  __device__ FT t2(FT f) const {
-    FT s = 0;
+}
+template <class FT>
+__device__ __forceinline__ void d2(const Row<FT> &R, const FT (&f)[4], FT (&o)[4]) { across(R.dB, f, o); }
+template <class FT>
+__device__ __forceinline__ void t2(const Row<FT> &R, const FT (&f)[4], FT (&o)[4]) { across(R.tB, f, o); }
+
+// Per-node horizontal geometry of the thread's row (loaded once per element).
+template <class FT>
+struct RowGeo {
+  FT Jh[4], iJh[4], gu0[4], gu1[4], gu2[4], gd0[4], gd1[4], gd2[4], W[4], iW[4];
+  __device__ void load(const FT *sG, const DevParams<FT> &P, int j) {
 #pragma unroll
-    for (int k = 0; k < NQ; ++k) s += tB[k] * shfl(f, i + NQ * k, 16);
-    return s;
+    for (int i = 0; i < NQ; ++i) {
+      const int n = NQ * j + i;
+      Jh[i] = sG[HG_JH * NN + n];
+      iJh[i] = sG[HG_IJH * NN + n];
+      gu0[i] = sG[HG_GU0 * NN + n];
+      gu1[i] = sG[HG_GU1 * NN + n];
+      gu2[i] = sG[HG_GU2 * NN + n];
+      gd0[i] = sG[HG_GD0 * NN + n];
+      gd1[i] = sG[HG_GD1 * NN + n];
+      gd2[i] = sG[HG_GD2 * NN + n];
+      W[i] = P.W[n];
+      iW[i] = P.iW[n];
+    }
   }
 };
 
+// Geometry of the row at one level (deep-atmosphere scaling r^2, layer thickness dz).
 template <class FT>
-struct NodeGeo {
-  FT Jh, iJh, gu0, gu1, gu2, gd0, gd1, gd2, f3, fh1, fh2, W, iW;
-  __device__ void load(const FT *sG, const DevParams<FT> &P, int n) {
-    Jh = sG[HG_JH * NN + n];
-    iJh = sG[HG_IJH * NN + n];
-    iW = P.iW[n];
-    gu0 = sG[HG_GU0 * NN + n]; gu1 = sG[HG_GU1 * NN + n]; gu2 = sG[HG_GU2 * NN + n];
-    gd0 = sG[HG_GD0 * NN + n]; gd1 = sG[HG_GD1 * NN + n]; gd2 = sG[HG_GD2 * NN + n];
-    f3 = sG[HG_F3 * NN + n]; fh1 = sG[HG_FH1 * NN + n]; fh2 = sG[HG_FH2 * NN + n];
-    W = P.W[n];
-  }
-};
-
-// Slab geometry at one level: full Jacobian and metric with deep-atmosphere scaling.
-template <class FT>
-struct LevGeo {
-  FT J, iJ, WJ, iWJ, gu0, gu1, gu2, gd0, gd1, gd2, G33;
-  __device__ void set(const NodeGeo<FT> &g, FT r2, FT ir2, FT dz, FT idz) {
-    J = g.Jh * r2 * dz;
-    iJ = g.iJh * ir2 * idz;
-    WJ = g.W * J;
-    iWJ = g.iW * iJ;
-    gu0 = g.gu0 * ir2; gu1 = g.gu1 * ir2; gu2 = g.gu2 * ir2;
-    gd0 = g.gd0 * r2; gd1 = g.gd1 * r2; gd2 = g.gd2 * r2;
+struct LevRow {
+  FT J[4], iJ[4], WJ[4], iWJ[4];
+  FT ir2, r2, G33;
+  __device__ void set(const RowGeo<FT> &g, FT r2_, FT ir2_, FT dz, FT idz) {
+    r2 = r2_;
+    ir2 = ir2_;
     G33 = dz * dz;
+#pragma unroll
+    for (int i = 0; i < NQ; ++i) {
+      J[i] = g.Jh[i] * r2 * dz;
+      iJ[i] = g.iJh[i] * ir2 * idz;
+      WJ[i] = g.W[i] * J[i];
+      iWJ[i] = g.iW[i] * iJ[i];
+    }
   }
 };
 
 // C123(wgrad(div u)) * fdiv - C123(wcurl(C123(curl u))) for covariant (c1, c2, c3)
 template <class FT>
-__device__ __forceinline__ void vec_lap(const Nodal<FT> &N, const LevGeo<FT> &s, FT W, FT iW, FT c1, FT c2, FT c3,
-                                        FT fdiv, FT &o1, FT &o2, FT &o3) {
-  FT F1 = s.gu0 * c1 + s.gu1 * c2, F2 = s.gu1 * c1 + s.gu2 * c2;
-  FT dv = (N.d1(s.J * F1) + N.d2(s.J * F2)) * s.iJ;
-  FT wdv = W * dv;
-  FT w1 = -N.t1(wdv) * iW, w2 = -N.t2(wdv) * iW;
-  FT k3 = (N.d1(c2) - N.d2(c1)) * s.iJ;
-  FT k1 = N.d2(c3) * s.iJ, k2 = -N.d1(c3) * s.iJ;
-  FT z1 = s.gd0 * k1 + s.gd1 * k2, z2 = s.gd1 * k1 + s.gd2 * k2, z3 = s.G33 * k3;
-  FT q3 = (-N.t1(W * z2) + N.t2(W * z1)) * s.iWJ;
-  FT Wz3 = W * z3;
-  FT q1 = -N.t2(Wz3) * s.iWJ, q2 = N.t1(Wz3) * s.iWJ;
-  o1 = fdiv * w1 - (s.gd0 * q1 + s.gd1 * q2);
-  o2 = fdiv * w2 - (s.gd1 * q1 + s.gd2 * q2);
-  o3 = -s.G33 * q3;
+__device__ __forceinline__ void vec_lap(const DevParams<FT> &P, const Row<FT> &R, const RowGeo<FT> &g,
+                                        const LevRow<FT> &s, const FT (&c1)[4], const FT (&c2)[4],
+                                        const FT (&c3)[4], FT fdiv, FT (&o1)[4], FT (&o2)[4], FT (&o3)[4]) {
+  FT a[4], b[4], da[4], db[4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const FT gu0 = g.gu0[i] * s.ir2, gu1 = g.gu1[i] * s.ir2, gu2 = g.gu2[i] * s.ir2;
+    a[i] = s.J[i] * (gu0 * c1[i] + gu1 * c2[i]);
+    b[i] = s.J[i] * (gu1 * c1[i] + gu2 * c2[i]);
+  }
+  d1(P, a, da);
+  d2(R, b, db);
+  FT wdv[4], w1[4], w2[4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) wdv[i] = g.W[i] * ((da[i] + db[i]) * s.iJ[i]);
+  t1(P, wdv, w1);
+  t2(R, wdv, w2);
+  FT e1[4], e2[4], e3[4], e4[4];
+  d1(P, c2, e1);
+  d2(R, c1, e2);
+  d2(R, c3, e3);
+  d1(P, c3, e4);
+  FT Wz1[4], Wz2[4], Wz3[4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const FT k3 = (e1[i] - e2[i]) * s.iJ[i];
+    const FT k1 = e3[i] * s.iJ[i], k2 = -e4[i] * s.iJ[i];
+    const FT gd0 = g.gd0[i] * s.r2, gd1 = g.gd1[i] * s.r2, gd2 = g.gd2[i] * s.r2;
+    Wz1[i] = g.W[i] * (gd0 * k1 + gd1 * k2);
+    Wz2[i] = g.W[i] * (gd1 * k1 + gd2 * k2);
+    Wz3[i] = g.W[i] * (s.G33 * k3);
+  }
+  FT f1[4], f2[4], f3[4], f4[4];
+  t1(P, Wz2, f1);
+  t2(R, Wz1, f2);
+  t2(R, Wz3, f3);
+  t1(P, Wz3, f4);
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const FT q3 = (-f1[i] + f2[i]) * s.iWJ[i];
+    const FT q1 = -f3[i] * s.iWJ[i], q2 = f4[i] * s.iWJ[i];
+    const FT gd0 = g.gd0[i] * s.r2, gd1 = g.gd1[i] * s.r2, gd2 = g.gd2[i] * s.r2;
+    o1[i] = fdiv * (-w1[i] * g.iW[i]) - (gd0 * q1 + gd1 * q2);
+    o2[i] = fdiv * (-w2[i] * g.iW[i]) - (gd1 * q1 + gd2 * q2);
+    o3[i] = -s.G33 * q3;
+  }
 }
 
-// Stage one element's slabs into shared memory; returns false on a TMA timeout.
+// weak divergence -(1/WJ) (D^T (WJ F1) along xi^1 + along xi^2)
 template <class FT>
-__device__ bool stage_in(uint64_t *bar, int nbuf, void *const *dst, const void *const *src, const uint32_t *bytes,
-                         int *status) {
-  if (threadIdx.x == 0) {
-    mbar_init(bar, 1);
-    fence_mbar_init();
+__device__ __forceinline__ void wdiv(const DevParams<FT> &P, const Row<FT> &R, const LevRow<FT> &s,
+                                     const FT (&F1)[4], const FT (&F2)[4], FT (&o)[4]) {
+  FT a[4], b[4], ta[4], tb[4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    a[i] = s.WJ[i] * F1[i];
+    b[i] = s.WJ[i] * F2[i];
   }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    uint32_t tot = 0;
-    for (int b = 0; b < nbuf; ++b) tot += bytes[b];
-    mbar_expect_tx(bar, tot);
-    for (int b = 0; b < nbuf; ++b) tma_load(dst[b], src[b], bytes[b], bar);
-  }
-  bool ok = mbar_wait_bounded(bar, 0, status);
-  return __syncthreads_and(ok) != 0;
+  t1(P, a, ta);
+  t2(R, b, tb);
+#pragma unroll
+  for (int i = 0; i < 4; ++i) o[i] = -(ta[i] + tb[i]) * s.iWJ[i];
 }
 
+// u_bar_3 = I^c(u_3) and the face part of K, I^c(u_3 u^3), with the
+// impenetrable filter (u_3 = 0 on the boundary faces); level-fastest mapping.
 template <class FT>
-__device__ void stage_out(int nbuf, void *const *dst, const void *const *src, const uint32_t *bytes) {
-  fence_proxy_async();
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    for (int b = 0; b < nbuf; ++b) tma_store(dst[b], src[b], bytes[b]);
-    tma_store_commit();
-    tma_store_wait_all();
-  }
-  __syncthreads();
-}
-
-// u_bar_3 = I^c(u_3) and the face part of K, I^c(u_3 u^3) / ... with the
-// impenetrable filter (u_3 = 0 on the boundary faces), level-fastest mapping.
-template <class FT>
-__device__ void centre_from_faces(const DevParams<FT> &P, const FT *sF, FT *sU3, FT *sKv) {
+__device__ __forceinline__ void centre_from_faces(const DevParams<FT> &P, const FT *sF, FT *sU3, FT *sKv) {
   const int Nv = P.Nv, Nf = P.Nf;
   for (int idx = threadIdx.x; idx < NN * Nv; idx += blockDim.x) {
     const int n = idx / Nv, v = idx - n * Nv;
-    FT a = v == 0 ? FT(0) : sF[n * Nf + v];
-    FT b = v + 1 == Nv ? FT(0) : sF[n * Nf + v + 1];
-    FT ua = a * P.levf[LF_G33 * Nf + v], ub = b * P.levf[LF_G33 * Nf + v + 1];
-    sU3[idx] = (a + b) / FT(2);
+    const FT a = v == 0 ? FT(0) : sF[n * Nf + v];
+    const FT b = v + 1 == Nv ? FT(0) : sF[n * Nf + v + 1];
+    const FT ua = a * P.levf[LF_G33 * Nf + v], ub = b * P.levf[LF_G33 * Nf + v + 1];
+    if (sU3) sU3[idx] = (a + b) / FT(2);
     sKv[idx] = (a * ua + b * ub) / FT(2);
   }
 }
 
+// TMA loads of one element's input slabs into buffer set b (thread 0 only).
 template <class FT>
-__global__ void __launch_bounds__(SE_THREADS) k_passA(DevParams<FT> P, const FT *__restrict__ Yc,
-                                                      const FT *__restrict__ Yf, FT *__restrict__ Lout) {
+__device__ __forceinline__ void issue_slab(const DevParams<FT> &P, uint64_t *bar, int e, FT *sY, FT *sF, FT *sG,
+                                           FT *sL, const FT *Yc, const FT *Yf, const FT *Lin) {
+  const int Nv = P.Nv, Nf = P.Nf;
+  const uint32_t by = uint32_t(sizeof(FT) * 64 * Nv), bf = uint32_t(sizeof(FT) * 16 * Nf);
+  const uint32_t bg = uint32_t(sizeof(FT) * HG_N * 16);
+  mbar_expect_tx(bar, by + bf + bg + (sL ? by : 0u));
+  tma_load(sY, Yc + (size_t)e * 64 * Nv, by, bar);
+  tma_load(sF, Yf + (size_t)e * 16 * Nf, bf, bar);
+  tma_load(sG, P.hgeo + (size_t)e * HG_N * 16, bg, bar);
+  if (sL) tma_load(sL, Lin + (size_t)e * 64 * Nv, by, bar);
+}
+
+__device__ __forceinline__ void init_bars(uint64_t *bar) {
+  if (threadIdx.x == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+}
+
+// Start of one element iteration: prefetch the next element (double
+// buffering) or load this one (single buffering), retire the previous
+// output store, and wait for this element's slabs.  Returns false if a
+// bounded wait gave up (every thread then leaves the element loop).
+template <class T>
+__device__ __forceinline__ T *pick(int b, T *p0, T *p1) { return b ? p1 : p0; }
+
+template <class FT>
+__device__ __forceinline__ bool begin_element(const DevParams<FT> &P, uint64_t *bar, int nbuf, int it, int e,
+                                              FT *const (&sY)[2], FT *const (&sF)[2], FT *const (&sG)[2],
+                                              FT *const (&sL)[2], bool withL, const FT *Yc, const FT *Yf,
+                                              const FT *Lin, int &b) {
+  b = nbuf == 2 ? (it & 1) : 0;
+  if (threadIdx.x == 0) {
+    if (nbuf == 2) {
+      const int en = e + gridDim.x;
+      const int o = b ^ 1;
+      if (en < P.Nh)
+        issue_slab<FT>(P, &bar[o], en, pick(o, sY[0], sY[1]), pick(o, sF[0], sF[1]), pick(o, sG[0], sG[1]),
+                       withL ? pick(o, sL[0], sL[1]) : nullptr, Yc, Yf, Lin);
+    } else if (it > 0) {
+      issue_slab<FT>(P, &bar[0], e, sY[0], sF[0], sG[0], withL ? sL[0] : nullptr, Yc, Yf, Lin);
+    }
+    tma_store_wait_read();
+  }
+  const uint32_t parity = nbuf == 2 ? ((it >> 1) & 1) : (it & 1);
+  const bool ok = mbar_wait_bounded(pick(b, &bar[0], &bar[1]), parity, P.status);
+  return __syncthreads_and(ok) != 0;
+}
+
+template <class FT>
+__global__ void __launch_bounds__(SE_THREADS, 1) k_passA(DevParams<FT> P, int nbuf, const FT *__restrict__ Yc,
+                                                         const FT *__restrict__ Yf, FT *__restrict__ Lout) {
   extern __shared__ __align__(128) unsigned char sm[];
-  const int Nv = P.Nv, Nf = P.Nf, e = blockIdx.x;
-  const PassALayout<FT> Lo(Nv);
-  FT *sY = (FT *)(sm + Lo.y), *sF = (FT *)(sm + Lo.f), *sG = (FT *)(sm + Lo.g);
+  const int Nv = P.Nv;
+  const PassALayout<FT> Lo(Nv, nbuf);
+  FT *sYb[2] = {(FT *)(sm + Lo.y[0]), (FT *)(sm + Lo.y[1])};
+  FT *sFb[2] = {(FT *)(sm + Lo.f[0]), (FT *)(sm + Lo.f[1])};
+  FT *sGb[2] = {(FT *)(sm + Lo.g[0]), (FT *)(sm + Lo.g[1])};
   FT *sU3 = (FT *)(sm + Lo.u3), *sKv = (FT *)(sm + Lo.kv), *sO = (FT *)(sm + Lo.out);
   uint64_t *bar = (uint64_t *)(sm + Lo.bar);
-  {
-    void *dst[3] = {sY, sF, sG};
-    const void *src[3] = {Yc + (size_t)e * 64 * Nv, Yf + (size_t)e * 16 * Nf, P.hgeo + (size_t)e * HG_N * 16};
-    uint32_t by[3] = {uint32_t(sizeof(FT) * 64 * Nv), uint32_t(sizeof(FT) * 16 * Nf), uint32_t(sizeof(FT) * HG_N * 16)};
-    if (!stage_in<FT>(bar, 3, dst, src, by, P.status)) return;
-  }
-  centre_from_faces(P, sF, sU3, sKv);
-  __syncthreads();
-
-  const int n = threadIdx.x & 15, vl = threadIdx.x >> 4, nlev = blockDim.x >> 4;
-  Nodal<FT> N;
-  N.init(P, n);
-  NodeGeo<FT> g;
-  g.load(sG, P, n);
-  for (int v0 = 0; v0 < Nv; v0 += nlev) {
-    const int v = min(v0 + vl, Nv - 1);
-    const bool act = v0 + vl < Nv;
-    LevGeo<FT> s;
-    s.set(g, P.levc[LC_R2 * Nv + v], P.levc[LC_IR2 * Nv + v], P.levc[LC_DZ * Nv + v], P.levc[LC_IDZ * Nv + v]);
-    const FT Phi = P.levc[LC_PHI * Nv + v];
-    const int q = n * Nv + v;
-    const FT rho = sY[q], u1 = sY[16 * Nv + q], u2 = sY[32 * Nv + q], rhoe = sY[48 * Nv + q];
-    const FT ub3 = sU3[q], kv = sKv[q];
-    const FT c1 = s.gu0 * u1 + s.gu1 * u2, c2 = s.gu1 * u1 + s.gu2 * u2;
-    const FT K = (u1 * c1 + u2 * c2 + kv) / FT(2);
-    Thermo<FT> th;
-    thermo(P, rho, rhoe, K, Phi, th);
-    FT o1, o2, o3;
-    vec_lap(N, s, g.W, g.iW, u1, u2, ub3, FT(1), o1, o2, o3);
-    const FT sd = P.cpd * (th.T - P.T0) + Phi - sd_r(P, th.Pi, th.phir);
-    const FT g1 = N.d1(sd), g2 = N.d2(sd);
-    const FT x1 = s.gu0 * g1 + s.gu1 * g2, x2 = s.gu1 * g1 + s.gu2 * g2;
-    const FT Ls = -(N.t1(s.WJ * x1) + N.t2(s.WJ * x2)) * s.iWJ;
-    if (act) {
-      sO[q] = Ls;
-      sO[16 * Nv + q] = o1;
-      sO[32 * Nv + q] = o2;
-      sO[48 * Nv + q] = o3;
+  init_bars(bar);
+  int e = blockIdx.x;
+  if (threadIdx.x == 0 && e < P.Nh) issue_slab<FT>(P, &bar[0], e, sYb[0], sFb[0], sGb[0], nullptr, Yc, Yf, nullptr);
+  const int j = threadIdx.x & 3, vl = threadIdx.x >> 2;
+  Row<FT> R;
+  R.init(P, j);
+  for (int it = 0; e < P.Nh; ++it, e += gridDim.x) {
+    int b;
+    if (!begin_element<FT>(P, bar, nbuf, it, e, sYb, sFb, sGb, sGb, false, Yc, Yf, nullptr, b)) break;
+    const FT *sY = pick(b, sYb[0], sYb[1]), *sF = pick(b, sFb[0], sFb[1]), *sG = pick(b, sGb[0], sGb[1]);
+    centre_from_faces(P, sF, sU3, sKv);
+    __syncthreads();
+    RowGeo<FT> g;
+    g.load(sG, P, j);
+    for (int v0 = 0; v0 < Nv; v0 += SE_LEVELS) {
+      const int v = min(v0 + vl, Nv - 1);
+      const bool act = v0 + vl < Nv;
+      LevRow<FT> s;
+      s.set(g, P.levc[LC_R2 * Nv + v], P.levc[LC_IR2 * Nv + v], P.levc[LC_DZ * Nv + v], P.levc[LC_IDZ * Nv + v]);
+      const FT Phi = P.levc[LC_PHI * Nv + v];
+      FT u1[4], u2[4], ub3[4], sd[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        const int q = (NQ * j + i) * Nv + v;
+        const FT rho = sY[q], rhoe = sY[48 * Nv + q];
+        u1[i] = sY[16 * Nv + q];
+        u2[i] = sY[32 * Nv + q];
+        ub3[i] = sU3[q];
+        const FT gu0 = g.gu0[i] * s.ir2, gu1 = g.gu1[i] * s.ir2, gu2 = g.gu2[i] * s.ir2;
+        const FT c1 = gu0 * u1[i] + gu1 * u2[i], c2 = gu1 * u1[i] + gu2 * u2[i];
+        const FT K = (u1[i] * c1 + u2[i] * c2 + sKv[q]) / FT(2);
+        Thermo<FT> th;
+        thermo(P, rho, rhoe, K, Phi, th);
+        sd[i] = P.cpd * (th.T - P.T0) + Phi - sd_r(P, th.Pi, th.phir);
+      }
+      FT o1[4], o2[4], o3[4];
+      vec_lap(P, R, g, s, u1, u2, ub3, FT(1), o1, o2, o3);
+      FT g1[4], g2[4], x1[4], x2[4], Ls[4];
+      d1(P, sd, g1);
+      d2(R, sd, g2);
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        const FT gu0 = g.gu0[i] * s.ir2, gu1 = g.gu1[i] * s.ir2, gu2 = g.gu2[i] * s.ir2;
+        x1[i] = gu0 * g1[i] + gu1 * g2[i];
+        x2[i] = gu1 * g1[i] + gu2 * g2[i];
+      }
+      wdiv(P, R, s, x1, x2, Ls);
+      if (act) {
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          const int q = (NQ * j + i) * Nv + v;
+          sO[q] = Ls[i];
+          sO[16 * Nv + q] = o1[i];
+          sO[32 * Nv + q] = o2[i];
+          sO[48 * Nv + q] = o3[i];
+        }
+      }
+    }
+    fence_proxy_async();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      tma_store(Lout + (size_t)e * 64 * Nv, sO, uint32_t(sizeof(FT) * 64 * Nv));
+      tma_store_commit();
     }
   }
-  void *dst[1] = {Lout + (size_t)e * 64 * Nv};
-  const void *src[1] = {sO};
-  uint32_t by[1] = {uint32_t(sizeof(FT) * 64 * Nv)};
-  stage_out<FT>(1, dst, src, by);
+  if (threadIdx.x == 0) tma_store_wait_all();
 }
 
 template <class FT>
-__global__ void __launch_bounds__(SE_THREADS) k_passB(DevParams<FT> P, const FT *__restrict__ Yc,
-                                                      const FT *__restrict__ Yf, const FT *__restrict__ Lin,
-                                                      FT *__restrict__ Tc, FT *__restrict__ Tf) {
+__global__ void __launch_bounds__(SE_THREADS, 1) k_passB(DevParams<FT> P, int nbuf, const FT *__restrict__ Yc,
+                                                         const FT *__restrict__ Yf, const FT *__restrict__ Lin,
+                                                         FT *__restrict__ Tc, FT *__restrict__ Tf) {
   extern __shared__ __align__(128) unsigned char sm[];
-  const int Nv = P.Nv, Nf = P.Nf, e = blockIdx.x;
-  const PassBLayout<FT> Lo(Nv);
-  FT *sY = (FT *)(sm + Lo.y), *sF = (FT *)(sm + Lo.f), *sG = (FT *)(sm + Lo.g), *sL = (FT *)(sm + Lo.lap);
-  FT *sU3 = (FT *)(sm + Lo.u3), *sKv = (FT *)(sm + Lo.kv);
+  const int Nv = P.Nv, Nf = P.Nf;
+  const PassBLayout<FT> Lo(Nv, nbuf);
+  FT *sYb[2] = {(FT *)(sm + Lo.y[0]), (FT *)(sm + Lo.y[1])};
+  FT *sFb[2] = {(FT *)(sm + Lo.f[0]), (FT *)(sm + Lo.f[1])};
+  FT *sGb[2] = {(FT *)(sm + Lo.g[0]), (FT *)(sm + Lo.g[1])};
+  FT *sLb[2] = {(FT *)(sm + Lo.lap[0]), (FT *)(sm + Lo.lap[1])};
+  FT *sKv = (FT *)(sm + Lo.kv);
   FT *sC1 = (FT *)(sm + Lo.c1), *sC2 = (FT *)(sm + Lo.c2), *sK = (FT *)(sm + Lo.k), *sRJ = (FT *)(sm + Lo.rj);
   FT *sL4 = (FT *)(sm + Lo.l4), *sO = (FT *)(sm + Lo.out), *sOf = (FT *)(sm + Lo.outf);
-  FT *sCr1 = sU3, *sCr2 = sKv;          // centre cross terms overwrite u_bar_3 / K_v point by point
-  FT *sX1 = sL, *sX2 = sL + 16 * Nf;    // face cross products reuse the Laplacian buffer after P1
+  FT *sCr1 = (FT *)(sm + Lo.cr1), *sCr2 = (FT *)(sm + Lo.cr2);
+  FT *sX1 = (FT *)(sm + Lo.x1), *sX2 = (FT *)(sm + Lo.x2);
   uint64_t *bar = (uint64_t *)(sm + Lo.bar);
-  {
-    void *dst[4] = {sY, sF, sG, sL};
-    const void *src[4] = {Yc + (size_t)e * 64 * Nv, Yf + (size_t)e * 16 * Nf, P.hgeo + (size_t)e * HG_N * 16,
-                          Lin + (size_t)e * 64 * Nv};
-    uint32_t by[4] = {uint32_t(sizeof(FT) * 64 * Nv), uint32_t(sizeof(FT) * 16 * Nf),
-                      uint32_t(sizeof(FT) * HG_N * 16), uint32_t(sizeof(FT) * 64 * Nv)};
-    if (!stage_in<FT>(bar, 4, dst, src, by, P.status)) return;
-  }
-  centre_from_faces(P, sF, sU3, sKv);
-  __syncthreads();
-
-  const int n = threadIdx.x & 15, vl = threadIdx.x >> 4, nlev = blockDim.x >> 4;
-  Nodal<FT> N;
-  N.init(P, n);
-  NodeGeo<FT> g;
-  g.load(sG, P, n);
-  // ---- P1: centre-level horizontal work
-  for (int v0 = 0; v0 < Nv; v0 += nlev) {
-    const int v = min(v0 + vl, Nv - 1);
-    const bool act = v0 + vl < Nv;
-    LevGeo<FT> s;
-    const FT dz = P.levc[LC_DZ * Nv + v], idz = P.levc[LC_IDZ * Nv + v];
-    s.set(g, P.levc[LC_R2 * Nv + v], P.levc[LC_IR2 * Nv + v], dz, idz);
-    const FT Phi = P.levc[LC_PHI * Nv + v];
-    const int q = n * Nv + v;
-    const FT rho = sY[q], u1 = sY[16 * Nv + q], u2 = sY[32 * Nv + q], rhoe = sY[48 * Nv + q];
-    const FT kv = sKv[q];
-    const FT c1 = s.gu0 * u1 + s.gu1 * u2, c2 = s.gu1 * u1 + s.gu2 * u2;
-    const FT K = (u1 * c1 + u2 * c2 + kv) / FT(2);
-    Thermo<FT> th;
-    thermo(P, rho, rhoe, K, Phi, th);
-    const FT h = th.h;
-    // rho: -split_div(rho u, 1) = -wdiv(rho u)
-    const FT F1 = rho * c1, F2 = rho * c2;
-    const FT dm = -(N.t1(s.WJ * F1) + N.t2(s.WJ * F2)) * s.iWJ;
-    FT Trho = -dm;
-    // rho e_tot: -split_div(rho u, h)
-    const FT dmh = -(N.t1(s.WJ * (F1 * h)) + N.t2(s.WJ * (F2 * h))) * s.iWJ;
-    const FT ha = N.d1(h), hb = N.d2(h);
-    FT Trhoe = -((dmh + h * dm + F1 * ha + F2 * hb) / FT(2));
-    // u_h: -[grad(K + Phi - Phi_r) + cp_d (th' grad Pi + grad(th' Pi) - Pi grad th') / 2]
-    const FT tmp = K + Phi - th.phir;
-    const FT thp = th.thv - th.thvr;
-    const FT a1 = N.d1(tmp), a2 = N.d2(tmp);
-    const FT b1 = N.d1(th.Pi), b2 = N.d2(th.Pi);
-    const FT tp = thp * th.Pi;
-    const FT e1 = N.d1(tp), e2 = N.d2(tp);
-    const FT f1 = N.d1(thp), f2 = N.d2(thp);
-    FT Tu1 = -(a1 + P.cpd * (thp * b1 + e1 - th.Pi * f1) / FT(2));
-    FT Tu2 = -(a2 + P.cpd * (thp * b2 + e2 - th.Pi * f2) / FT(2));
-    // hyperdiffusion: nu (div_damp C123(wgrad div L) - C123(wcurl C123(curl L)))
-    const FT Ls = sL[q], L1 = sL[16 * Nv + q], L2 = sL[32 * Nv + q], L3 = sL[48 * Nv + q];
-    FT o1, o2, o3;
-    vec_lap(N, s, g.W, g.iW, L1, L2, L3, P.div_damp, o1, o2, o3);
-    const FT g1 = N.d1(Ls), g2 = N.d2(Ls);
-    const FT x1 = rho * (s.gu0 * g1 + s.gu1 * g2), x2 = rho * (s.gu1 * g1 + s.gu2 * g2);
-    const FT hd = -(N.t1(s.WJ * x1) + N.t2(s.WJ * x2)) * s.iWJ;
-    Tu1 -= P.nu_v * o1;
-    Tu2 -= P.nu_v * o2;
-    Trhoe -= P.nu_s * hd;
-    // vorticity: w^3 = wcurl(u_h); (f^3 + w^3) x CT12(u) -> C12
-    const FT om3 = (-N.t1(g.W * u2) + N.t2(g.W * u1)) * s.iWJ;
-    const FT a3 = g.f3 * idz + om3;
-    __syncwarp();
-    if (act) {
-      sO[q] = Trho;
-      sO[16 * Nv + q] = Tu1;
-      sO[32 * Nv + q] = Tu2;
-      sO[48 * Nv + q] = Trhoe;
-      sC1[q] = c1;
-      sC2[q] = c2;
-      sK[q] = K;
-      sRJ[q] = rho * s.J;
-      sL4[q] = o3;
-      sCr1[q] = s.J * (-a3 * c2);
-      sCr2[q] = s.J * (a3 * c1);
+  init_bars(bar);
+  int e = blockIdx.x;
+  if (threadIdx.x == 0 && e < P.Nh) issue_slab<FT>(P, &bar[0], e, sYb[0], sFb[0], sGb[0], sLb[0], Yc, Yf, Lin);
+  const int j = threadIdx.x & 3, vl = threadIdx.x >> 2;
+  Row<FT> R;
+  R.init(P, j);
+  for (int it = 0; e < P.Nh; ++it, e += gridDim.x) {
+    int b;
+    if (!begin_element<FT>(P, bar, nbuf, it, e, sYb, sFb, sGb, sLb, true, Yc, Yf, Lin, b)) break;
+    const FT *sY = pick(b, sYb[0], sYb[1]), *sF = pick(b, sFb[0], sFb[1]), *sG = pick(b, sGb[0], sGb[1]);
+    const FT *sL = pick(b, sLb[0], sLb[1]);
+    centre_from_faces<FT>(P, sF, nullptr, sKv);
+    __syncthreads();
+    RowGeo<FT> g;
+    g.load(sG, P, j);
+    // ---- P1: centre-level horizontal work
+    for (int v0 = 0; v0 < Nv; v0 += SE_LEVELS) {
+      const int v = min(v0 + vl, Nv - 1);
+      const bool act = v0 + vl < Nv;
+      LevRow<FT> s;
+      const FT idz = P.levc[LC_IDZ * Nv + v];
+      s.set(g, P.levc[LC_R2 * Nv + v], P.levc[LC_IR2 * Nv + v], P.levc[LC_DZ * Nv + v], idz);
+      const FT Phi = P.levc[LC_PHI * Nv + v];
+      FT rho[4], u1[4], u2[4], c1[4], c2[4], K[4], h[4], Pi[4], thp[4], tmp[4], tp[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        const int q = (NQ * j + i) * Nv + v;
+        rho[i] = sY[q];
+        u1[i] = sY[16 * Nv + q];
+        u2[i] = sY[32 * Nv + q];
+        const FT gu0 = g.gu0[i] * s.ir2, gu1 = g.gu1[i] * s.ir2, gu2 = g.gu2[i] * s.ir2;
+        c1[i] = gu0 * u1[i] + gu1 * u2[i];
+        c2[i] = gu1 * u1[i] + gu2 * u2[i];
+        K[i] = (u1[i] * c1[i] + u2[i] * c2[i] + sKv[q]) / FT(2);
+        Thermo<FT> th;
+        thermo(P, rho[i], sY[48 * Nv + q], K[i], Phi, th);
+        h[i] = th.h;
+        Pi[i] = th.Pi;
+        thp[i] = th.thv - th.thvr;
+        tmp[i] = K[i] + Phi - th.phir;
+        tp[i] = thp[i] * Pi[i];
+      }
+      // rho: -wdiv(rho u); rho e_tot: -split_div(rho u, h)
+      FT F1[4], F2[4], dm[4], Trho[4], Trhoe[4], Tu1[4], Tu2[4];
+      {
+        FT G1[4], G2[4], dmh[4], ha[4], hb[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          F1[i] = rho[i] * c1[i];
+          F2[i] = rho[i] * c2[i];
+          G1[i] = F1[i] * h[i];
+          G2[i] = F2[i] * h[i];
+        }
+        wdiv(P, R, s, F1, F2, dm);
+        wdiv(P, R, s, G1, G2, dmh);
+        d1(P, h, ha);
+        d2(R, h, hb);
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          Trho[i] = -dm[i];
+          Trhoe[i] = -((dmh[i] + h[i] * dm[i] + F1[i] * ha[i] + F2[i] * hb[i]) / FT(2));
+        }
+      }
+      // u_h: -[grad(K + Phi - Phi_r) + cp_d (th' grad Pi + grad(th' Pi) - Pi grad th') / 2]
+      {
+        FT a1[4], a2[4], b1[4], b2[4], e1[4], e2[4], f1[4], f2[4];
+        d1(P, tmp, a1);
+        d2(R, tmp, a2);
+        d1(P, Pi, b1);
+        d2(R, Pi, b2);
+        d1(P, tp, e1);
+        d2(R, tp, e2);
+        d1(P, thp, f1);
+        d2(R, thp, f2);
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          Tu1[i] = -(a1[i] + P.cpd * (thp[i] * b1[i] + e1[i] - Pi[i] * f1[i]) / FT(2));
+          Tu2[i] = -(a2[i] + P.cpd * (thp[i] * b2[i] + e2[i] - Pi[i] * f2[i]) / FT(2));
+        }
+      }
+      // hyperdiffusion: nu (div_damp C123(wgrad div L) - C123(wcurl C123(curl L)))
+      FT o3[4];
+      {
+        FT L1[4], L2[4], L3[4], Ls[4], o1[4], o2[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          const int q = (NQ * j + i) * Nv + v;
+          Ls[i] = sL[q];
+          L1[i] = sL[16 * Nv + q];
+          L2[i] = sL[32 * Nv + q];
+          L3[i] = sL[48 * Nv + q];
+        }
+        vec_lap(P, R, g, s, L1, L2, L3, P.div_damp, o1, o2, o3);
+        FT g1[4], g2[4], x1[4], x2[4], hd[4];
+        d1(P, Ls, g1);
+        d2(R, Ls, g2);
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          const FT gu0 = g.gu0[i] * s.ir2, gu1 = g.gu1[i] * s.ir2, gu2 = g.gu2[i] * s.ir2;
+          x1[i] = rho[i] * (gu0 * g1[i] + gu1 * g2[i]);
+          x2[i] = rho[i] * (gu1 * g1[i] + gu2 * g2[i]);
+        }
+        wdiv(P, R, s, x1, x2, hd);
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          Tu1[i] -= P.nu_v * o1[i];
+          Tu2[i] -= P.nu_v * o2[i];
+          Trhoe[i] -= P.nu_s * hd[i];
+        }
+      }
+      // vorticity: w^3 = wcurl(u_h); (f^3 + w^3) x CT12(u) -> C12
+      FT om[4];
+      {
+        FT Wu1[4], Wu2[4], ta[4], tb[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          Wu1[i] = g.W[i] * u1[i];
+          Wu2[i] = g.W[i] * u2[i];
+        }
+        t1(P, Wu2, ta);
+        t2(R, Wu1, tb);
+#pragma unroll
+        for (int i = 0; i < 4; ++i) om[i] = (-ta[i] + tb[i]) * s.iWJ[i];
+      }
+      if (act) {
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          const int n = NQ * j + i;
+          const int q = n * Nv + v;
+          const FT a3 = sG[HG_F3 * NN + n] * idz + om[i];
+          sO[q] = Trho[i];
+          sO[16 * Nv + q] = Tu1[i];
+          sO[32 * Nv + q] = Tu2[i];
+          sO[48 * Nv + q] = Trhoe[i];
+          sC1[q] = c1[i];
+          sC2[q] = c2[i];
+          sK[q] = K[i];
+          sRJ[q] = rho[i] * s.J[i];
+          sL4[q] = o3[i];
+          sCr1[q] = s.J[i] * (-a3 * c2[i]);
+          sCr2[q] = s.J[i] * (a3 * c1[i]);
+        }
+      }
+    }
+    __syncthreads();
+    // ---- P2: face-level work (f^12 + w^12, cross products, u_3 tendency)
+    for (int k0 = 0; k0 < Nf; k0 += SE_LEVELS) {
+      const int k = min(k0 + vl, Nf - 1);
+      const bool act = k0 + vl < Nf;
+      const bool inner = k > 0 && k < Nv;
+      const FT r2 = P.levf[LF_R2 * Nf + k], dzf = P.levf[LF_DZ * Nf + k], rinv = P.levf[LF_RINV * Nf + k];
+      const FT ir2f = P.levf[LF_IR2 * Nf + k], idzf = P.levf[LF_IDZ * Nf + k], g33 = P.levf[LF_G33 * Nf + k];
+      FT Wu[4], u3[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        u3[i] = inner ? sF[(NQ * j + i) * Nf + k] : FT(0);
+        Wu[i] = g.W[i] * u3[i];
+      }
+      FT ta[4], tb[4];
+      t2(R, Wu, tb);
+      t1(P, Wu, ta);
+      const int va = k > 0 ? k - 1 : 0, vb = k < Nv ? k : Nv - 1;
+      if (act) {
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          const int n = NQ * j + i;
+          const int qa = n * Nv + va, qb = n * Nv + vb;
+          const FT Jf = g.Jh[i] * r2 * dzf;
+          const FT iJf = g.iJh[i] * ir2f * idzf, iWJf = g.iW[i] * iJf;
+          const FT w1 = -tb[i] * iWJf, w2 = ta[i] * iWJf;
+          FT cv1 = 0, cv2 = 0, gK = 0, cc1, cc2, l4, rJ;
+          if (inner) {
+            cv1 = -(sY[32 * Nv + qb] - sY[32 * Nv + qa]) * iJf;
+            cv2 = (sY[16 * Nv + qb] - sY[16 * Nv + qa]) * iJf;
+            cc1 = (sC1[qa] + sC1[qb]) / FT(2);
+            cc2 = (sC2[qa] + sC2[qb]) / FT(2);
+            gK = sK[qb] - sK[qa];
+            const FT wa = sRJ[qa], wb = sRJ[qb];
+            l4 = gdiv(wa * sL4[qa] + wb * sL4[qb], wa + wb);
+            rJ = (wa + wb) / FT(2);
+          } else {
+            const int qq = k == 0 ? qb : qa;
+            cc1 = sC1[qq];
+            cc2 = sC2[qq];
+            l4 = sL4[qq];
+            rJ = sRJ[qq];
+          }
+          const FT fo1 = sG[HG_FH1 * NN + n] * rinv + cv1 + w1, fo2 = sG[HG_FH2 * NN + n] * rinv + cv2 + w2;
+          const FT b3 = rJ * (u3[i] * g33);
+          FT T3 = -(P.nu_v * l4);
+          T3 -= Jf * (fo1 * cc2 - fo2 * cc1) + gK;
+          sX1[n * Nf + k] = Jf * (fo2 * b3);
+          sX2[n * Nf + k] = Jf * (-fo1 * b3);
+          sOf[n * Nf + k] = T3;
+        }
+      }
+    }
+    __syncthreads();
+    // ---- P3: centre u_h part of the face cross products and the sponge (level-fastest)
+    for (int idx = threadIdx.x; idx < NN * Nv; idx += blockDim.x) {
+      const int nn = idx / Nv, v = idx - nn * Nv;
+      const FT irJ = grcp(sRJ[idx]);
+      const FT t1v = (sX1[nn * Nf + v] + sX1[nn * Nf + v + 1]) / FT(2) * irJ + sCr1[idx];
+      const FT t2v = (sX2[nn * Nf + v] + sX2[nn * Nf + v + 1]) / FT(2) * irJ + sCr2[idx];
+      const FT beta = P.levc[LC_BETA * Nv + v];
+      FT a = sO[16 * Nv + idx] - t1v;
+      FT bb = sO[32 * Nv + idx] - t2v;
+      a -= beta * sY[16 * Nv + idx];
+      bb -= beta * sY[32 * Nv + idx];
+      sO[16 * Nv + idx] = a;
+      sO[32 * Nv + idx] = bb;
+    }
+    fence_proxy_async();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      tma_store(Tc + (size_t)e * 64 * Nv, sO, uint32_t(sizeof(FT) * 64 * Nv));
+      tma_store(Tf + (size_t)e * 16 * Nf, sOf, uint32_t(sizeof(FT) * 16 * Nf));
+      tma_store_commit();
     }
   }
-  __syncthreads();
-  // ---- P2: face-level work (f^12 + w^12, cross products, u_3 tendency)
-  for (int k0 = 0; k0 < Nf; k0 += nlev) {
-    const int k = min(k0 + vl, Nf - 1);
-    const bool act = k0 + vl < Nf;
-    const bool inner = k > 0 && k < Nv;
-    const FT u3 = inner ? sF[n * Nf + k] : FT(0);
-    const FT r2 = P.levf[LF_R2 * Nf + k], dzf = P.levf[LF_DZ * Nf + k], rinv = P.levf[LF_RINV * Nf + k];
-    const FT Jf = g.Jh * r2 * dzf;
-    const FT iJf = g.iJh * P.levf[LF_IR2 * Nf + k] * P.levf[LF_IDZ * Nf + k], iWJf = g.iW * iJf;
-    const FT Wu = g.W * u3;
-    const FT w1 = -N.t2(Wu) * iWJf, w2 = N.t1(Wu) * iWJf;
-    FT cv1 = 0, cv2 = 0, gK = 0, cc1, cc2, l4, rJ;
-    const int qa = n * Nv + (k > 0 ? k - 1 : 0), qb = n * Nv + (k < Nv ? k : Nv - 1);
-    if (inner) {
-      cv1 = -(sY[32 * Nv + qb] - sY[32 * Nv + qa]) * iJf;
-      cv2 = (sY[16 * Nv + qb] - sY[16 * Nv + qa]) * iJf;
-      cc1 = (sC1[qa] + sC1[qb]) / FT(2);
-      cc2 = (sC2[qa] + sC2[qb]) / FT(2);
-      gK = sK[qb] - sK[qa];
-      const FT wa = sRJ[qa], wb = sRJ[qb];
-      l4 = gdiv(wa * sL4[qa] + wb * sL4[qb], wa + wb);
-      rJ = (wa + wb) / FT(2);
-    } else {
-      const int qq = k == 0 ? qb : qa;
-      cc1 = sC1[qq];
-      cc2 = sC2[qq];
-      l4 = sL4[qq];
-      rJ = sRJ[qq];
-    }
-    const FT fo1 = g.fh1 * rinv + cv1 + w1, fo2 = g.fh2 * rinv + cv2 + w2;
-    const FT b3 = rJ * (u3 * P.levf[LF_G33 * Nf + k]);
-    FT T3 = -(P.nu_v * l4);
-    T3 -= Jf * (fo1 * cc2 - fo2 * cc1) + gK;
-    if (act) {
-      sX1[n * Nf + k] = Jf * (fo2 * b3);
-      sX2[n * Nf + k] = Jf * (-fo1 * b3);
-      sOf[n * Nf + k] = T3;
-    }
-  }
-  __syncthreads();
-  // ---- P3: centre u_h part of the face cross products and the sponge (level-fastest)
-  for (int idx = threadIdx.x; idx < NN * Nv; idx += blockDim.x) {
-    const int nn = idx / Nv, v = idx - nn * Nv;
-    const FT irJ = grcp(sRJ[idx]);
-    const FT t1v = (sX1[nn * Nf + v] + sX1[nn * Nf + v + 1]) / FT(2) * irJ + sCr1[idx];
-    const FT t2v = (sX2[nn * Nf + v] + sX2[nn * Nf + v + 1]) / FT(2) * irJ + sCr2[idx];
-    const FT beta = P.levc[LC_BETA * Nv + v];
-    FT a = sO[16 * Nv + idx] - t1v;
-    FT b = sO[32 * Nv + idx] - t2v;
-    a -= beta * sY[16 * Nv + idx];
-    b -= beta * sY[32 * Nv + idx];
-    sO[16 * Nv + idx] = a;
-    sO[32 * Nv + idx] = b;
-  }
-  void *dst[2] = {Tc + (size_t)e * 64 * Nv, Tf + (size_t)e * 16 * Nf};
-  const void *src[2] = {sO, sOf};
-  uint32_t by[2] = {uint32_t(sizeof(FT) * 64 * Nv), uint32_t(sizeof(FT) * 16 * Nf)};
-  stage_out<FT>(2, dst, src, by);
+  if (threadIdx.x == 0) tma_store_wait_all();
 }
+
+struct SeLaunch {
+  int nsm = 0, optin = 0;
+};
+SeLaunch g_se;
+
+void se_device() {
+  if (!g_se.nsm) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&g_se.nsm, cudaDevAttrMultiProcessorCount, dev);
+    cudaDeviceGetAttribute(&g_se.optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    if (g_se.nsm <= 0) g_se.nsm = 1;
+  }
+}
+
+template <class L>
+int pick_nbuf(const L &two) { return two.total <= (size_t)g_se.optin ? 2 : 1; }
 
 }  // namespace
 
 template <class FT>
-size_t passA_smem(int Nv) { return PassALayout<FT>(Nv).total; }
+size_t passA_smem(int Nv) { return PassALayout<FT>(Nv, 1).total; }
 template <class FT>
-size_t passB_smem(int Nv) { return PassBLayout<FT>(Nv).total; }
+size_t passB_smem(int Nv) { return PassBLayout<FT>(Nv, 1).total; }
 
 // Raise the dynamic shared-memory limit of the slab kernels to the device's
 // opt-in maximum once (contexts with different level counts may coexist).
 template <class FT>
 void configure_se(int Nv) {
   (void)Nv;
-  int dev = 0, optin = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-  cudaFuncSetAttribute(k_passA<FT>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
-  cudaFuncSetAttribute(k_passB<FT>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+  se_device();
+  cudaFuncSetAttribute(k_passA<FT>, cudaFuncAttributeMaxDynamicSharedMemorySize, g_se.optin);
+  cudaFuncSetAttribute(k_passB<FT>, cudaFuncAttributeMaxDynamicSharedMemorySize, g_se.optin);
 }
 
 template <class FT>
 void launch_passA(const DevParams<FT> &P, const FT *Yc, const FT *Yf, FT *L, cudaStream_t s) {
-  k_passA<FT><<<P.Nh, SE_THREADS, passA_smem<FT>(P.Nv), s>>>(P, Yc, Yf, L);
+  se_device();
+  const int nbuf = pick_nbuf(PassALayout<FT>(P.Nv, 2));
+  const int grid = min(P.Nh, g_se.nsm);
+  k_passA<FT><<<grid, SE_THREADS, PassALayout<FT>(P.Nv, nbuf).total, s>>>(P, nbuf, Yc, Yf, L);
 }
 template <class FT>
 void launch_passB(const DevParams<FT> &P, const FT *Yc, const FT *Yf, const FT *L, FT *Tc, FT *Tf, cudaStream_t s) {
-  k_passB<FT><<<P.Nh, SE_THREADS, passB_smem<FT>(P.Nv), s>>>(P, Yc, Yf, L, Tc, Tf);
+  se_device();
+  const int nbuf = pick_nbuf(PassBLayout<FT>(P.Nv, 2));
+  const int grid = min(P.Nh, g_se.nsm);
+  k_passB<FT><<<grid, SE_THREADS, PassBLayout<FT>(P.Nv, nbuf).total, s>>>(P, nbuf, Yc, Yf, L, Tc, Tf);
 }
 
 #define INST(FT)                                                                                             \

@@ -1,0 +1,133 @@
+"""
+    GBDycore
+
+Julia binding of libgbdycore (the GB300 dry dynamical-core IMEX step).  The
+functions below have the signatures of the ClimaAtmos hooks they replace
+(src/simulation/integrator.jl:189-225), so `args_integrator` can pass them to
+`CTS.ClimaODEFunction` unchanged; each is one `ccall` into the C ABI declared in
+include/gbdycore.h.  `p.gb` holds the library context (a `GBContext`).
+
+State buffers are CuArrays in ClimaCore's VIJFH layout: `parent(Y.c)` is
+(Nv, 4, 4, 4, Nh) with components (ρ, uₕ₁, uₕ₂, ρe_tot) and `parent(Y.f)` is
+(Nv + 1, 4, 4, 1, Nh); their device pointers are passed without copies.
+"""
+module GBDycore
+
+import CUDA
+import LinearAlgebra
+
+const libgbdycore = get(ENV, "GBDYCORE_LIB", joinpath(@__DIR__, "..", "gbdycore", "libgbdycore.so"))
+
+const GB_OK = Cint(0)
+
+struct GBConfig
+    h_elem::Cint
+    z_elem::Cint
+    ft_bytes::Cint
+    z_stretch::Cint
+    z_max::Cdouble
+    dz_bottom::Cdouble
+    dt::Cdouble
+    nu_v::Cdouble
+    nu_s::Cdouble
+    div_damp::Cdouble
+    sponge_zd::Cdouble
+    alpha_uh::Cdouble
+    alpha_w::Cdouble
+    upwinding::Cint
+    grav::Cdouble
+    omega::Cdouble
+    R_d::Cdouble
+    cp_d::Cdouble
+    cv_d::Cdouble
+    T_0::Cdouble
+    p_ref::Cdouble
+    T_min_ref::Cdouble
+    T_surf_ref::Cdouble
+    T_min_sgs::Cdouble
+    radius::Cdouble
+end
+
+struct GBFieldVec
+    c::Ptr{Cvoid}
+    f::Ptr{Cvoid}
+end
+
+mutable struct GBContext
+    handle::Ptr{Cvoid}
+end
+
+fieldvec(Y) = GBFieldVec(
+    reinterpret(Ptr{Cvoid}, pointer(parent(Y.c))),
+    reinterpret(Ptr{Cvoid}, pointer(parent(Y.f))),
+)
+
+function check(ctx::GBContext, rc::Cint)
+    rc == GB_OK && return nothing
+    buf = Vector{UInt8}(undef, 512)
+    ccall((:gb_last_error, libgbdycore), Cint, (Ptr{Cvoid}, Ptr{UInt8}, Csize_t), ctx.handle, buf, length(buf))
+    error("libgbdycore status $rc: " * unsafe_string(pointer(buf)))
+end
+
+function GBContext(cfg::GBConfig)
+    h = Ref{Ptr{Cvoid}}(C_NULL)
+    rc = ccall((:gb_ctx_create, libgbdycore), Cint, (Ref{GBConfig}, Ref{Ptr{Cvoid}}), cfg, h)
+    rc == GB_OK || error("gb_ctx_create failed with status $rc")
+    ctx = GBContext(h[])
+    finalizer(c -> ccall((:gb_ctx_destroy, libgbdycore), Cint, (Ptr{Cvoid},), c.handle), ctx)
+    # work on CUDA.jl's task-local stream
+    stream = CUDA.stream().handle
+    check(ctx, ccall((:gb_set_stream, libgbdycore), Cint, (Ptr{Cvoid}, Ptr{Cvoid}), ctx.handle, stream))
+    return ctx
+end
+
+# ---- hooks (same signatures as the reference's) ----
+
+set_precomputed_quantities!(Y, p, t) =
+    check(p.gb, ccall((:gb_set_precomputed_quantities, libgbdycore), Cint,
+        (Ptr{Cvoid}, GBFieldVec, Cdouble), p.gb.handle, fieldvec(Y), t))
+
+function remaining_tendency!(Yₜ, Yₜ_lim, Y, p, t)
+    check(p.gb, ccall((:gb_remaining_tendency, libgbdycore), Cint,
+        (Ptr{Cvoid}, GBFieldVec, GBFieldVec, Cdouble), p.gb.handle, fieldvec(Yₜ), fieldvec(Y), t))
+    return Yₜ
+end
+
+implicit_tendency!(Yₜ, Y, p, t) =
+    check(p.gb, ccall((:gb_implicit_tendency, libgbdycore), Cint,
+        (Ptr{Cvoid}, GBFieldVec, GBFieldVec, Cdouble), p.gb.handle, fieldvec(Yₜ), fieldvec(Y), t))
+
+"""The Jacobian blocks live in the library context; this struct is the handle CTS carries."""
+struct GBJacobian
+    p::Any
+end
+Base.zero(j::GBJacobian) = j
+
+update_jacobian!(jacobian::GBJacobian, Y, p, dtγ, t) =
+    check(p.gb, ccall((:gb_update_jacobian, libgbdycore), Cint,
+        (Ptr{Cvoid}, GBFieldVec, Cdouble, Cdouble), p.gb.handle, fieldvec(Y), dtγ, t))
+
+LinearAlgebra.ldiv!(ΔY, jacobian::GBJacobian, R) =
+    check(jacobian.p.gb, ccall((:gb_ldiv, libgbdycore), Cint,
+        (Ptr{Cvoid}, GBFieldVec, GBFieldVec), jacobian.p.gb.handle, fieldvec(ΔY), fieldvec(R)))
+
+correct_implicit_advection_tendency!(Yₜ, Y, p, t) =
+    check(p.gb, ccall((:gb_correct_implicit_advection_tendency, libgbdycore), Cint,
+        (Ptr{Cvoid}, GBFieldVec, GBFieldVec, Cdouble), p.gb.handle, fieldvec(Yₜ), fieldvec(Y), t))
+
+dss!(Y, p, t) =
+    check(p.gb, ccall((:gb_dss, libgbdycore), Cint, (Ptr{Cvoid}, GBFieldVec), p.gb.handle, fieldvec(Y)))
+
+"""One or more fused ARS343 steps (graph-captured) in place of CTS's stage loop."""
+step!(Y, p, t, dt, nsteps = 1) =
+    check(p.gb, ccall((:gb_step, libgbdycore), Cint,
+        (Ptr{Cvoid}, GBFieldVec, Cdouble, Cdouble, Cint, Cint), p.gb.handle, fieldvec(Y), t, dt, nsteps, 1))
+
+function global_sums(Y, p)
+    out = zeros(Cdouble, 2)
+    check(p.gb, ccall((:gb_global_sums, libgbdycore), Cint,
+        (Ptr{Cvoid}, GBFieldVec, Ptr{Cdouble}), p.gb.handle, fieldvec(Y), out))
+    return out
+end
+
+end # module

@@ -3,6 +3,7 @@
 #include <cstdio>
 #include <cstring>
 #include <memory>
+#include <mutex>
 #include <new>
 #include <string>
 #include <vector>
@@ -11,6 +12,12 @@
 #include "kernels.cuh"
 
 using namespace gb;
+
+// Scratch of gb_jacobian_solve_noalloc: the Jacobian blocks live in this
+// file-scope device array instead of memory allocated by the library.  In
+// host code the name is only a stand-in; its device address comes from
+// cudaGetSymbolAddress (per device, see noalloc_scratch()).
+static __device__ __align__(256) unsigned char g_noalloc_scratch[GB_NOALLOC_SCRATCH_BYTES];
 
 namespace {
 
@@ -381,6 +388,50 @@ int time_kernel_t(gb_ctx *ctx, int kernel, gb_fieldvec Y, int reps, double *ms) 
   return rc;
 }
 
+// Device address of g_noalloc_scratch on the current device, resolved once per
+// device (with that device current) on the first call.
+constexpr int NOALLOC_MAX_DEVICES = 64;
+void *g_noalloc_ptr[NOALLOC_MAX_DEVICES] = {};
+std::mutex g_noalloc_mu;
+
+int noalloc_scratch(gb_ctx *ctx, void **out) {
+  int dev = 0;
+  CK(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= NOALLOC_MAX_DEVICES) return fail(ctx, GB_ERR_ARG, "device ordinal out of range");
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (!g_noalloc_ptr[dev]) {
+    void *p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p)
+      return fail(ctx, GB_ERR_CUDA, std::string("cudaGetSymbolAddress(g_noalloc_scratch): ") + cudaGetErrorString(e));
+    g_noalloc_ptr[dev] = p;
+  }
+  *out = g_noalloc_ptr[dev];
+  return GB_OK;
+}
+
+template <class FT>
+int jacobian_solve_noalloc_t(gb_ctx *ctx, gb_fieldvec dY, gb_fieldvec Y, gb_fieldvec R, double dtg) {
+  Impl<FT> *I = impl<FT>(ctx);
+  const size_t need = (size_t)I->P.Nh * NN * JAC_Q * I->P.Nf * sizeof(FT);
+  if (need > (size_t)GB_NOALLOC_SCRATCH_BYTES)
+    return fail(ctx, GB_ERR_ARG, "gb_jacobian_solve_noalloc: Jacobian needs " + std::to_string(need) +
+                                     " bytes, more than GB_NOALLOC_SCRATCH_BYTES (" +
+                                     std::to_string((size_t)GB_NOALLOC_SCRATCH_BYTES) + ")");
+  void *scratch = nullptr;
+  int r = noalloc_scratch(ctx, &scratch);
+  if (r) return r;
+  ColArgs<FT> A{};
+  A.jac = (FT *)scratch;
+  A.dtg = (FT)dtg;
+  A.Y_c = (const FT *)Y.c; A.Y_f = (const FT *)Y.f;
+  launch_column<FT>(I->P, COL_JACOBIAN, A, ctx->stream);
+  A.Y_c = (const FT *)R.c; A.Y_f = (const FT *)R.f;
+  A.O_c = (FT *)dY.c; A.O_f = (FT *)dY.f;
+  launch_column<FT>(I->P, COL_LDIV, A, ctx->stream);
+  return check_launch(ctx);
+}
+
 bool aligned(const void *p) { return ((uintptr_t)p & 15) == 0; }
 bool fv_ok(gb_fieldvec v) { return v.c && v.f && aligned(v.c) && aligned(v.f); }
 
@@ -545,6 +596,12 @@ int gb_newton_residual(gb_ctx *ctx, double out[3]) {
   GUARD(ctx);
   if (!out) return fail(ctx, GB_ERR_ARG, "null pointer");
   return DISPATCH(ctx, residual_t, ctx, out);
+}
+
+int gb_jacobian_solve_noalloc(gb_ctx *ctx, gb_fieldvec dY, gb_fieldvec Y, gb_fieldvec R, double dtgamma) {
+  GUARD(ctx);
+  if (!fv_ok(dY) || !fv_ok(Y) || !fv_ok(R)) return fail(ctx, GB_ERR_ARG, "null or misaligned pointer");
+  return DISPATCH(ctx, jacobian_solve_noalloc_t, ctx, dY, Y, R, dtgamma);
 }
 
 int gb_time_kernel(gb_ctx *ctx, int kernel, gb_fieldvec Y, int reps, double *ms) {

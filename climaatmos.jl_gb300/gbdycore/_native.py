@@ -20,8 +20,9 @@ SYMBOLS = [
     "gb_sizes", "gb_geometry_export", "gb_ctx_create", "gb_ctx_destroy", "gb_set_stream", "gb_last_error",
     "gb_set_precomputed_quantities", "gb_remaining_tendency", "gb_implicit_tendency", "gb_update_jacobian",
     "gb_ldiv", "gb_correct_implicit_advection_tendency", "gb_dss", "gb_step", "gb_global_sums",
-    "gb_newton_residual", "gb_time_kernel",
+    "gb_newton_residual", "gb_time_kernel", "gb_jacobian_solve_noalloc",
 ]
+GB_NOALLOC_SCRATCH_BYTES = 64 << 20
 
 
 class GBConfig(ctypes.Structure):
@@ -88,6 +89,7 @@ def load(build_if_missing=True):
     L.gb_global_sums.argtypes = [_vp, fv, _dp]
     L.gb_newton_residual.argtypes = [_vp, _dp]
     L.gb_time_kernel.argtypes = [_vp, _c_int, fv, _c_int, _dp]
+    L.gb_jacobian_solve_noalloc.argtypes = [_vp, fv, fv, fv, _c_double]
     for s in SYMBOLS:
         getattr(L, s).restype = _c_int
     _lib = L

@@ -41,6 +41,10 @@ def parse():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--plain-steps", type=int, default=3)
+    ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--precision-steps", type=int, default=20)
+    ap.add_argument("--no-precision", action="store_true")
     return ap.parse_args()
 
 
@@ -273,6 +277,44 @@ def run_gb300(args):
     e2e = {"value": sypd(cfg.dt, ms_e2e / 1e3) * world, "unit": UNIT, "h2d_bytes_per_step": nbytes,
            "d2h_bytes_per_step": nbytes, "ms_per_step": ms_e2e}
 
+    # plain form: the same step through the individual hooks (one C-ABI call per hook,
+    # unfused stage algebra in torch), as ClimaTimeSteppers drives the reference
+    plain_ms = None
+    if not args.no_plain:
+        Yp = s.Y.copy()
+        sim.ars343_step_via_hooks(Yp, s.p, 0.0, cfg.dt)
+        torch.cuda.synchronize()
+        e4, e5 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e4.record(stream)
+        for k in range(args.plain_steps):
+            sim.ars343_step_via_hooks(Yp, s.p, k * cfg.dt, cfg.dt)
+        e5.record(stream)
+        torch.cuda.synchronize()
+        plain_ms = e4.elapsed_time(e5) / args.plain_steps
+        del Yp
+
+    # precision: the FP32 step against the FP64 step of the same library (which
+    # matches the FP64 oracle to 1e-10), per prognostic field after n steps
+    prec = None
+    if not args.no_precision:
+        from gbdycore import setups as S
+        n = args.precision_steps
+        c64 = cfg.with_(ft=np.float64)
+        g = s.geometry
+        Yc, Yf = S.workload_state(g, c64, "production")
+        s64 = sim.AtmosSimulation(c64, state=(Yc, Yf))
+        s32 = sim.AtmosSimulation(cfg, state=(Yc.astype(np.float32), Yf.astype(np.float32)))
+        s64.step(n)
+        s32.step(n)
+        a, b = s32.Y.numpy(), s64.Y.numpy()
+        names = ["rho", "u_1", "u_2", "rho_e_tot"]
+        prec = {"steps": n}
+        for c in range(4):
+            prec[names[c]] = float(np.abs(a[0][:, c] - b[0][:, c]).max() / np.abs(b[0][:, c]).max())
+        prec["u_3"] = float(np.abs(a[1] - b[1]).max() / max(np.abs(b[1]).max(), 1e-300))
+        prec["norm"] = "max |FP32 - FP64| / max |FP64| per field"
+        del s64, s32
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         sec, cores = cpu_step_seconds(cfg, 2, 1)
@@ -287,6 +329,12 @@ def run_gb300(args):
                 "config": dict(workload_desc(cfg), parallelism="replicas" if world > 1 else "single GPU",
                                finite=finite),
                 "roofline": roof, "step_roofline": step_roof, "cpu_baseline": cpu, "e2e": e2e,
+                "plain_step": None if plain_ms is None else {
+                    "ms_per_step": plain_ms, "value": sypd(cfg.dt, plain_ms / 1e3), "unit": UNIT,
+                    "chosen_over_plain": plain_ms / ms,
+                    "what": "same step through the individual hooks (remaining/implicit tendency, Jacobian, ldiv, "
+                            "post-Newton correction, DSS) with unfused torch stage algebra"},
+                "fp32_vs_fp64": prec,
                 "clocks": clk, "gpu_launches": 20 * args.steps}
         print(json.dumps(line), flush=True)
     if world > 1:

@@ -9,8 +9,14 @@ namespace gb {
 
 // Device status word bits (read back by the host).
 enum : int { ST_TIMEOUT = 1, ST_NONFINITE = 2 };
-// Iteration limit of every bounded spin-wait on an mbarrier.
-constexpr long long WAIT_LIMIT = 1LL << 26;
+// Time limit (ns, device global timer) of every bounded wait on an mbarrier.
+constexpr unsigned long long WAIT_LIMIT_NS = 1000000000ull;
+
+// Four per-level values in one aligned 16-byte (FP32) or 32-byte (FP64) load.
+template <class FT>
+struct alignas(4 * sizeof(FT)) Lev4 {
+  FT x, y, z, w;
+};
 
 template <class FT>
 struct DevParams {
@@ -23,6 +29,8 @@ struct DevParams {
   const FT *hgeo;  // [Nh][HG_N][16]
   const FT *levc;  // [LC_N][Nv]
   const FT *levf;  // [LF_N][Nf]
+  const Lev4<FT> *lc4;  // [Nv] centres: {r^2 dz, 1 / (r^2 dz), 1 / r^2, Phi}
+  const Lev4<FT> *lf4;  // [Nf] faces: {g^33, beta_w, Phi_c(v) - Phi_c(v-1) (0 on the boundary faces), 0}
   const int *goff, *gcopy;
   const FT *gw, *ecov, *econ;  // ecov/econ: [Nh*16][6]
   int *status;
@@ -86,6 +94,20 @@ __device__ __forceinline__ FT sd_r(const DevParams<FT> &P, FT Pi, FT phir) {
   return P.cpd * (P.Tmin_ref + (P.Tsfc_ref - P.Tmin_ref) * Pi7 - P.T0) + phir;
 }
 
+// Per-column horizontal geometry (surface metric of one node).
+template <class FT>
+struct ColGeo {
+  FT Jh, iJh, gu0, gu1, gu2;
+  __device__ void load(const DevParams<FT> &P, int e, int n) {
+    const FT *hg = P.hgeo + (size_t)e * HG_N * NN;
+    Jh = hg[HG_JH * NN + n];
+    iJh = hg[HG_IJH * NN + n];
+    gu0 = hg[HG_GU0 * NN + n];
+    gu1 = hg[HG_GU1 * NN + n];
+    gu2 = hg[HG_GU2 * NN + n];
+  }
+};
+
 // ---------------------------------------------------------------- TMA (bulk copy) + mbarrier
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
   return static_cast<uint32_t>(__cvta_generic_to_shared(p));
@@ -127,14 +149,22 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
       : "memory");
   return ok != 0;
 }
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+  return t;
+}
 // Bounded wait: returns false (and flags ST_TIMEOUT) if the phase did not
-// complete within WAIT_LIMIT polls; the caller then waits once more, with the
+// complete within WAIT_LIMIT_NS; the caller then waits once more, with the
 // same limit, for its own copies and skips its work.
 __device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity, int *status) {
-  for (long long it = 0; it < WAIT_LIMIT; ++it)
+  if (mbar_try_wait(bar, parity)) return true;
+  const unsigned long long t0 = global_ns();
+  while (global_ns() - t0 < WAIT_LIMIT_NS)
     if (mbar_try_wait(bar, parity)) return true;
   if (status) atomicOr(status, ST_TIMEOUT);
-  for (long long it = 0; it < WAIT_LIMIT; ++it)
+  const unsigned long long t1 = global_ns();
+  while (global_ns() - t1 < WAIT_LIMIT_NS)
     if (mbar_try_wait(bar, parity)) break;
   return false;
 }

@@ -34,7 +34,7 @@ struct ImplBase {
 template <class FT>
 struct Impl : ImplBase {
   DevParams<FT> P{};
-  DevBuf hgeo, levc, levf, goff, gcopy, gw, ecov, econ, status;
+  DevBuf hgeo, levc, levf, lc4, lf4, goff, gcopy, gw, ecov, econ, status;
   DevBuf lap, U, Te[4], Ti[4], jac, rnorm, partials, sums, rsum;
   size_t NC = 0, NF = 0, NR = 0;  // centre, face and reduced-centre element counts
   int nsum_blocks = 0;
@@ -130,6 +130,24 @@ int create_impl(gb_ctx *ctx) {
   if ((r = upload<FT>(ctx, I->hgeo, g.hgeo))) return r;
   if ((r = upload<FT>(ctx, I->levc, g.levc))) return r;
   if ((r = upload<FT>(ctx, I->levf, g.levf))) return r;
+  {
+    const int nv = g.Nv, nf = nv + 1;
+    std::vector<double> c4((size_t)4 * nv), f4((size_t)4 * nf, 0.0);
+    for (int v = 0; v < nv; ++v) {
+      const double r2dz = g.levc[LC_R2 * nv + v] * g.levc[LC_DZ * nv + v];
+      c4[4 * v + 0] = r2dz;
+      c4[4 * v + 1] = 1.0 / r2dz;
+      c4[4 * v + 2] = g.levc[LC_IR2 * nv + v];
+      c4[4 * v + 3] = g.levc[LC_PHI * nv + v];
+    }
+    for (int f = 0; f < nf; ++f) {
+      f4[4 * f + 0] = g.levf[LF_G33 * nf + f];
+      f4[4 * f + 1] = g.levf[LF_BETA * nf + f];
+      f4[4 * f + 2] = g.levf[LF_DPHI * nf + f];
+    }
+    if ((r = upload<FT>(ctx, I->lc4, c4))) return r;
+    if ((r = upload<FT>(ctx, I->lf4, f4))) return r;
+  }
   if ((r = upload_i(ctx, I->goff, g.grp_off))) return r;
   if ((r = upload_i(ctx, I->gcopy, g.grp_copy))) return r;
   if ((r = upload<FT>(ctx, I->gw, g.grp_w))) return r;
@@ -163,6 +181,7 @@ int create_impl(gb_ctx *ctx) {
   for (int i = 0; i < NQ; ++i)
     for (int k = 0; k < NQ; ++k) P.D[i * NQ + k] = (FT)g.D[i][k];
   P.hgeo = (const FT *)I->hgeo.p; P.levc = (const FT *)I->levc.p; P.levf = (const FT *)I->levf.p;
+  P.lc4 = (const Lev4<FT> *)I->lc4.p; P.lf4 = (const Lev4<FT> *)I->lf4.p;
   P.goff = (const int *)I->goff.p; P.gcopy = (const int *)I->gcopy.p; P.gw = (const FT *)I->gw.p;
   P.ecov = (const FT *)I->ecov.p; P.econ = (const FT *)I->econ.p;
   P.status = (int *)I->status.p;

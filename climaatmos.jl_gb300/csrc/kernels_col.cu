@@ -129,18 +129,6 @@ struct ColDiag {
   FT c1[M], c2[M], K[M], T[M], h[M], Pi[M], thv[M], thvr[M], phir[M], rJ[M], u3c[M], J[M], iJ[M];
 };
 
-template <class FT>
-struct ColGeo {
-  FT Jh, iJh, gu0, gu1, gu2;
-  __device__ void load(const DevParams<FT> &P, int e, int n) {
-    const FT *hg = P.hgeo + (size_t)e * HG_N * NN;
-    Jh = hg[HG_JH * NN + n];
-    iJh = hg[HG_IJH * NN + n];
-    gu0 = hg[HG_GU0 * NN + n];
-    gu1 = hg[HG_GU1 * NN + n];
-    gu2 = hg[HG_GU2 * NN + n];
-  }
-};
 
 template <class FT, int M>
 __device__ __forceinline__ void col_diag(const DevParams<FT> &P, const ColGeo<FT> &G, const ColState<FT, M> &S,
@@ -385,143 +373,6 @@ __device__ __forceinline__ size_t cidx(int e, int c, int n, int v, int Nv) { ret
 template <class FT>
 __device__ __forceinline__ size_t ridx(int e, int c, int n, int v, int Nv) { return (((size_t)e * 2 + c) * NN + n) * Nv + v; }
 
-// STG = stage index i (1..3): explicit sources j < STG, implicit sources 1 <= j < STG
-// (the nonzero pattern of the ARS343 tableau).  All loads are issued before
-// the sums so that each lane has its ~50 independent loads in flight at once.
-template <class FT, int M, int STG>
-__global__ void __launch_bounds__(COL_THREADS) k_col_stage(DevParams<FT> P, StageArgs<FT> A) {
-  const int lane = threadIdx.x & 31;
-  const int col = blockIdx.x * (COL_THREADS / 32) + (threadIdx.x >> 5);
-  const int ncols = P.Nh * NN;
-  if (col >= ncols) return;
-  const int e = col >> 4, n = col & 15, Nv = P.Nv, Nf = P.Nf;
-  ColGeo<FT> G;
-  G.load(P, e, n);
-  // ---- stage assembly U^ = u_n + sum_j (ce_j T_exp_j + ci_j T_imp_j), summed in j order
-  FT un[5][M], te[STG][5][M], ti[STG][3][M];
-  const size_t cb = (size_t)e * 4 * NN * Nv + (size_t)n * Nv;   // centre comp 0 of this column
-  const size_t rb = (size_t)e * 2 * NN * Nv + (size_t)n * Nv;   // reduced centre comp 0
-  const size_t fb = ((size_t)e * NN + n) * Nf;
-#pragma unroll
-  for (int k = 0; k < M; ++k) {
-    const int v = lane * M + k;
-    const int vc = min(v, Nv - 1), vf = min(v, Nf - 1);
-#pragma unroll
-    for (int c = 0; c < 4; ++c) un[c][k] = A.un_c[cb + (size_t)c * NN * Nv + vc];
-    un[4][k] = A.un_f[fb + vf];
-#pragma unroll
-    for (int j = 0; j < STG; ++j) {
-#pragma unroll
-      for (int c = 0; c < 4; ++c) te[j][c][k] = A.te_c[j][cb + (size_t)c * NN * Nv + vc];
-      te[j][4][k] = A.te_f[j][fb + vf];
-      if (j >= 1) {
-        ti[j][0][k] = A.ti_c[j][rb + vc];
-        ti[j][1][k] = A.ti_c[j][rb + (size_t)NN * Nv + vc];
-        ti[j][2][k] = A.ti_f[j][fb + vf];
-      }
-    }
-  }
-  ColState<FT, M> H;  // U^
-#pragma unroll
-  for (int k = 0; k < M; ++k) {
-    const int v = lane * M + k;
-    const bool cv = v < Nv, fv = v < Nf;
-    FT x[5];
-#pragma unroll
-    for (int c = 0; c < 5; ++c) {
-      FT s = un[c][k];
-#pragma unroll
-      for (int j = 0; j < STG; ++j) {
-        s += A.ce[j] * te[j][c][k];
-        if (j >= 1 && c != 1 && c != 2) s += A.ci[j] * ti[j][c == 0 ? 0 : (c == 3 ? 1 : 2)][k];
-      }
-      x[c] = s;
-    }
-    H.rho[k] = cv ? x[0] : FT(1);
-    H.u1[k] = cv ? x[1] : FT(0);
-    H.u2[k] = cv ? x[2] : FT(0);
-    H.rhoe[k] = cv ? x[3] : FT(1);
-    H.u3[k] = fv ? x[4] : FT(0);
-  }
-  // ---- filter and precomputed quantities at U = filtered U^
-  ColState<FT, M> U = H;
-#pragma unroll
-  for (int k = 0; k < M; ++k) {
-    const int f = lane * M + k;
-    if (f == 0 || f >= Nv) U.u3[k] = FT(0);
-  }
-  ColDiag<FT, M> Dg;
-  col_diag<FT, M>(P, G, U, Dg, lane);
-  FT Tr[M], Te[M], T3[M];
-  col_implicit<FT, M>(P, G, U, Dg, Tr, Te, T3, lane);
-  const FT dtg = A.dtg;
-  FT Rr[M], Re[M], Ru1[M], Ru2[M], R3[M];
-  double ss[3] = {0, 0, 0};
-  bool finite = true;
-#pragma unroll
-  for (int k = 0; k < M; ++k) {
-    const int v = lane * M + k;
-    const bool cv = v < Nv, fv = v < Nf;
-    Rr[k] = cv ? H.rho[k] + dtg * Tr[k] - U.rho[k] : FT(0);
-    Re[k] = cv ? H.rhoe[k] + dtg * Te[k] - U.rhoe[k] : FT(0);
-    Ru1[k] = FT(0);
-    Ru2[k] = FT(0);
-    R3[k] = fv ? H.u3[k] + dtg * T3[k] - U.u3[k] : FT(0);
-    ss[0] += (double)(Rr[k] * Rr[k]);
-    ss[1] += (double)(Re[k] * Re[k]);
-    ss[2] += (double)(R3[k] * R3[k]);
-    finite = finite && isfinite(Rr[k]) && isfinite(Re[k]) && isfinite(R3[k]);
-  }
-  ColJac<FT, M> Jc;
-  col_jacobian<FT, M>(P, G, U, Dg, dtg, Jc, lane);
-  FT Xr[M], Xe[M], X3[M];
-  col_ldiv<FT, M>(P, Jc, Rr, Re, Ru1, Ru2, R3, Xr, Xe, X3, lane);
-#pragma unroll
-  for (int k = 0; k < M; ++k) {
-    const int f = lane * M + k;
-    U.rho[k] -= Xr[k];
-    U.rhoe[k] -= Xe[k];
-    U.u3[k] -= X3[k];
-    if (f == 0 || f >= Nv) U.u3[k] = FT(0);  // filter after the solve (cache!)
-  }
-  if (P.upwinding) {
-    col_diag<FT, M>(P, G, U, Dg, lane);
-    FT corr[M];
-    col_correction<FT, M>(P, G, Dg, corr, lane);
-#pragma unroll
-    for (int k = 0; k < M; ++k) U.rhoe[k] += dtg * corr[k];
-  }
-  // ---- outputs: U, T_imp = (U - U^) / dtgamma, residual sums of squares
-  const FT idtg = A.idtg;
-#pragma unroll
-  for (int k = 0; k < M; ++k) {
-    const int v = lane * M + k;
-    if (v < Nv) {
-      A.U_c[cidx<FT>(e, 0, n, v, Nv)] = U.rho[k];
-      A.U_c[cidx<FT>(e, 1, n, v, Nv)] = U.u1[k];
-      A.U_c[cidx<FT>(e, 2, n, v, Nv)] = U.u2[k];
-      A.U_c[cidx<FT>(e, 3, n, v, Nv)] = U.rhoe[k];
-      A.Ti_c[ridx<FT>(e, 0, n, v, Nv)] = (U.rho[k] - H.rho[k]) * idtg;
-      A.Ti_c[ridx<FT>(e, 1, n, v, Nv)] = (U.rhoe[k] - H.rhoe[k]) * idtg;
-    }
-    if (v < Nf) {
-      const size_t q = ((size_t)e * NN + n) * Nf + v;
-      A.U_f[q] = U.u3[k];
-      A.Ti_f[q] = (U.u3[k] - H.u3[k]) * idtg;
-    }
-  }
-#pragma unroll
-  for (int c = 0; c < 3; ++c)
-    for (int o = 16; o > 0; o >>= 1) ss[c] += __shfl_xor_sync(0xffffffffu, ss[c], o);
-  finite = __all_sync(0xffffffffu, finite);
-  if (lane == 0) {
-    if (A.rnorm) {
-      for (int c = 0; c < 3; ++c) A.rnorm[(size_t)col * 3 + c] = (A.first ? 0.0 : A.rnorm[(size_t)col * 3 + c]) + ss[c];
-    }
-    if (!finite) atomicOr(P.status, ST_NONFINITE);
-  }
-}
-
 // Individual hooks: implicit tendency, Jacobian, ldiv, post-Newton correction.
 template <class FT, int M, int MODE>
 __global__ void __launch_bounds__(COL_THREADS) k_col_hook(DevParams<FT> P, ColArgs<FT> A) {
@@ -611,27 +462,6 @@ inline int levels_per_lane(int Nf) { return Nf <= 32 ? 1 : (Nf <= 64 ? 2 : 4); }
 }  // namespace
 
 template <class FT, int M>
-void launch_stage_m(const DevParams<FT> &P, const StageArgs<FT> &A, int grid, cudaStream_t s) {
-  switch (A.nsrc) {
-    case 1: k_col_stage<FT, M, 1><<<grid, COL_THREADS, 0, s>>>(P, A); break;
-    case 2: k_col_stage<FT, M, 2><<<grid, COL_THREADS, 0, s>>>(P, A); break;
-    default: k_col_stage<FT, M, 3><<<grid, COL_THREADS, 0, s>>>(P, A); break;
-  }
-}
-
-// A.nsrc = stage index (1..3); all explicit sources j < nsrc and implicit
-// sources 1 <= j < nsrc must be present (the ARS343 nonzero pattern).
-template <class FT>
-void launch_column_stage(const DevParams<FT> &P, const StageArgs<FT> &A, cudaStream_t s) {
-  const int ncols = P.Nh * NN, grid = (ncols + COL_THREADS / 32 - 1) / (COL_THREADS / 32);
-  switch (levels_per_lane(P.Nf)) {
-    case 1: launch_stage_m<FT, 1>(P, A, grid, s); break;
-    case 2: launch_stage_m<FT, 2>(P, A, grid, s); break;
-    default: launch_stage_m<FT, 4>(P, A, grid, s); break;
-  }
-}
-
-template <class FT, int M>
 void launch_hook_m(const DevParams<FT> &P, int mode, const ColArgs<FT> &A, int grid, cudaStream_t s) {
   switch (mode) {
     case COL_IMPLICIT: k_col_hook<FT, M, COL_IMPLICIT><<<grid, COL_THREADS, 0, s>>>(P, A); break;
@@ -651,8 +481,6 @@ void launch_column(const DevParams<FT> &P, int mode, const ColArgs<FT> &A, cudaS
   }
 }
 
-template void launch_column_stage<float>(const DevParams<float> &, const StageArgs<float> &, cudaStream_t);
-template void launch_column_stage<double>(const DevParams<double> &, const StageArgs<double> &, cudaStream_t);
 template void launch_column<float>(const DevParams<float> &, int, const ColArgs<float> &, cudaStream_t);
 template void launch_column<double>(const DevParams<double> &, int, const ColArgs<double> &, cudaStream_t);
 

@@ -45,6 +45,9 @@ def parse():
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--precision-steps", type=int, default=20)
     ap.add_argument("--no-precision", action="store_true")
+    ap.add_argument("--batch-columns", type=int, default=20000)
+    ap.add_argument("--batch-reps", type=int, default=10)
+    ap.add_argument("--no-batching", action="store_true")
     return ap.parse_args()
 
 
@@ -315,6 +318,10 @@ def run_gb300(args):
         prec["norm"] = "max |FP32 - FP64| / max |FP64| per field"
         del s64, s32
 
+    batching = None
+    if not args.no_batching:
+        batching = measure_batching(args)
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         sec, cores = cpu_step_seconds(cfg, 2, 1)
@@ -334,12 +341,63 @@ def run_gb300(args):
                     "chosen_over_plain": plain_ms / ms,
                     "what": "same step through the individual hooks (remaining/implicit tendency, Jacobian, ldiv, "
                             "post-Newton correction, DSS) with unfused torch stage algebra"},
-                "fp32_vs_fp64": prec,
+                "fp32_vs_fp64": prec, "batching": batching,
                 "clocks": clk, "gpu_launches": 20 * args.steps}
         print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()
     return 0
+
+
+def measure_batching(args):
+    """Standalone columns of uneven height: 20,000 columns, z_elem ~ U{30..127}
+    (seed 2), z_max 30 km uniform, FP32 storage, 2 Newton iterations per column
+    (Jacobian build + block-tridiagonal solve each), dtgamma = gamma * 120 s.
+    One persistent graph-captured launch (variant chosen by the autotuner) vs
+    the plain form, one launch per height group."""
+    import torch
+    from gbdycore import columns as CB, config as C
+    cfg = C.DycoreConfig(h_elem=1, z_elem=10, z_max=30000.0, z_stretch=False, ft=np.float32, dt=120.0)
+    z = CB.batch_heights(args.batch_columns, 30, 127, seed=2)
+    Yc, Yf = CB.batch_state(cfg, z, seed=2)
+    B = CB.ColumnBatch(cfg, z)
+    Uh = B.state(Yc, Yf)
+    U = Uh.copy()
+    dtg = 0.4358665215084590 * 120.0
+    choice, tune_ms = B.autotune(U, Uh, dtg, 2, reps=3)
+    stream = torch.cuda.current_stream()
+
+    def timed(mode):
+        U.assign_(Uh)
+        B.solve(U, Uh, dtg, 2, mode, residual=False)   # warm-up (captures the graph)
+        torch.cuda.synchronize()
+        tot = 0.0
+        for _ in range(args.batch_reps):
+            U.assign_(Uh)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            B.solve(U, Uh, dtg, 2, mode, residual=False)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            tot += e0.elapsed_time(e1)
+        return tot / args.batch_reps
+
+    ms = {m: timed(m) for m in ("graph", "persistent", "per_height")}
+    U.assign_(Uh)
+    rn = B.solve(U, Uh, dtg, 2, "graph", residual=True)
+    C_tot = int(z.sum())
+    # compulsory traffic: read U^ and the initial iterate (4 centre + 1 face fields each), write the iterate
+    nbytes = 4 * (3 * (4 * C_tot + C_tot + len(z)))
+    return {"columns": int(len(z)), "z_elem": "U{30..127}, seed 2", "distinct_heights": int(len(np.unique(z))),
+            "newton_iters": 2, "centres": C_tot,
+            "ms": ms, "columns_per_s": len(z) / (ms["graph"] * 1e-3),
+            "persistent_graph_over_per_height": ms["per_height"] / ms["graph"],
+            "launches": {"graph": 3, "per_height": int(len(np.unique(z))) + 1},
+            "autotune": {"choice": int(choice), "variant_ms": [float(x) for x in tune_ms],
+                         "variants": ["128 thr/4 CTAs, 4 levels/lane", "128/4, 2 levels/lane (<=64 faces)",
+                                      "128/6, 2 levels/lane", "256/2, 2 levels/lane", "64/8, 2 levels/lane"]},
+            "GBps": nbytes / (ms["graph"] * 1e-3) / 1e9,
+            "residual_sq_fp64": rn.tolist()}
 
 
 def main():

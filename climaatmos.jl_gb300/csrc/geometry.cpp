@@ -48,7 +48,9 @@ void gll4(double *x, double *w, double D[NQ][NQ]) {
   }
 }
 
-std::vector<double> faces(const gb_config &c) {
+}  // namespace
+
+std::vector<double> vertical_faces(const gb_config &c) {
   const int N = c.z_elem;
   std::vector<double> zf(N + 1);
   if (!c.z_stretch) {
@@ -75,7 +77,6 @@ double beta_sponge(double z, double zd, double zmax, double alpha) {
   double s = std::sin(M_PI * (z - zd) / (zmax - zd) / 2.0);
   return alpha * s * s;
 }
-}  // namespace
 
 bool validate_config(const gb_config &c, const char **why) {
   if (c.h_elem < 1 || c.h_elem > 512) { *why = "h_elem must be in [1, 512]"; return false; }
@@ -200,7 +201,7 @@ void build_geometry(const gb_config &c, HostGeometry &g) {
     g.grp_off.push_back((int)g.grp_copy.size());
   }
   // vertical mesh
-  g.zf = faces(c);
+  g.zf = vertical_faces(c);
   g.zc.resize(Nv); g.dzc.resize(Nv); g.rc.resize(Nv); g.dzf.resize(Nf); g.rf.resize(Nf);
   for (int v = 0; v < Nv; ++v) {
     g.zc[v] = (g.zf[v] + g.zf[v + 1]) / 2;

@@ -33,4 +33,10 @@ struct HostGeometry {
 bool validate_config(const gb_config &cfg, const char **why);
 void build_geometry(const gb_config &cfg, HostGeometry &g);
 
+// Face heights z_0 = 0 .. z_{z_elem} = z_max: uniform, or tanh-stretched with the
+// first layer dz_bottom (ClimaCore's HyperbolicTangentStretching, grids.jl:356).
+std::vector<double> vertical_faces(const gb_config &cfg);
+// Rayleigh sponge rate alpha sin^2(pi/2 (z - z_d)/(z_max - z_d)) above z_d (rayleigh_sponge.jl:39-44).
+double beta_sponge(double z, double zd, double zmax, double alpha);
+
 }  // namespace gb

@@ -27,6 +27,13 @@ namespace {
 
 constexpr int SE_THREADS = 256;          // 64 level slots x 4 rows per sweep
 constexpr int SE_LEVELS = SE_THREADS / 4;
+// Resident CTAs per SM the slab kernels are compiled for: two in FP32 (a
+// 128-register cap; one CTA computes while the other's slabs stream in), one
+// in FP64 (whose register demand would spill heavily under the cap).
+template <class FT>
+struct SeMinBlocks {
+  static constexpr int value = sizeof(FT) == 4 ? 2 : 1;
+};
 
 // Row helper: the thread's row j and its xi^2 derivative coefficients.
 template <class FT>
@@ -257,7 +264,7 @@ __device__ __forceinline__ bool begin_element(const DevParams<FT> &P, uint64_t *
 }
 
 template <class FT>
-__global__ void __launch_bounds__(SE_THREADS, 1) k_passA(DevParams<FT> P, int nbuf, const FT *__restrict__ Yc,
+__global__ void __launch_bounds__(SE_THREADS, SeMinBlocks<FT>::value) k_passA(DevParams<FT> P, int nbuf, const FT *__restrict__ Yc,
                                                          const FT *__restrict__ Yf, FT *__restrict__ Lout) {
   extern __shared__ __align__(128) unsigned char sm[];
   const int Nv = P.Nv;
@@ -336,7 +343,7 @@ __global__ void __launch_bounds__(SE_THREADS, 1) k_passA(DevParams<FT> P, int nb
 }
 
 template <class FT>
-__global__ void __launch_bounds__(SE_THREADS, 1) k_passB(DevParams<FT> P, int nbuf, const FT *__restrict__ Yc,
+__global__ void __launch_bounds__(SE_THREADS, SeMinBlocks<FT>::value) k_passB(DevParams<FT> P, int nbuf, const FT *__restrict__ Yc,
                                                          const FT *__restrict__ Yf, const FT *__restrict__ Lin,
                                                          FT *__restrict__ Tc, FT *__restrict__ Tf) {
   extern __shared__ __align__(128) unsigned char sm[];
@@ -576,7 +583,7 @@ __global__ void __launch_bounds__(SE_THREADS, 1) k_passB(DevParams<FT> P, int nb
 }
 
 struct SeLaunch {
-  int nsm = 0, optin = 0;
+  int nsm = 0, optin = 0, per_sm = 0;
 };
 SeLaunch g_se;
 
@@ -586,12 +593,29 @@ void se_device() {
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&g_se.nsm, cudaDevAttrMultiProcessorCount, dev);
     cudaDeviceGetAttribute(&g_se.optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    cudaDeviceGetAttribute(&g_se.per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
     if (g_se.nsm <= 0) g_se.nsm = 1;
   }
 }
 
-template <class L>
-int pick_nbuf(const L &two) { return two.total <= (size_t)g_se.optin ? 2 : 1; }
+// Buffering and resident CTAs per SM of a slab kernel.  With two CTAs per SM
+// each CTA's slabs must leave room for the other's (1 KB per CTA is reserved
+// by the hardware): prefer double buffering if two such CTAs fit, else single
+// buffering at two CTAs, else one double- or single-buffered CTA.
+struct SeShape {
+  int nbuf, ctas;
+  size_t smem;
+};
+template <class FT, class L>
+SeShape se_shape(int Nv) {
+  const size_t two = L(Nv, 2).total, one = L(Nv, 1).total, per_sm = (size_t)g_se.per_sm;
+  if (SeMinBlocks<FT>::value >= 2) {
+    if (2 * (two + 1024) <= per_sm) return {2, 2, two};
+    if (2 * (one + 1024) <= per_sm) return {1, 2, one};
+  }
+  if (two <= (size_t)g_se.optin) return {2, 1, two};
+  return {1, 1, one};
+}
 
 }  // namespace
 
@@ -613,16 +637,16 @@ void configure_se(int Nv) {
 template <class FT>
 void launch_passA(const DevParams<FT> &P, const FT *Yc, const FT *Yf, FT *L, cudaStream_t s) {
   se_device();
-  const int nbuf = pick_nbuf(PassALayout<FT>(P.Nv, 2));
-  const int grid = min(P.Nh, g_se.nsm);
-  k_passA<FT><<<grid, SE_THREADS, PassALayout<FT>(P.Nv, nbuf).total, s>>>(P, nbuf, Yc, Yf, L);
+  const SeShape sh = se_shape<FT, PassALayout<FT>>(P.Nv);
+  const int grid = min(P.Nh, g_se.nsm * sh.ctas);
+  k_passA<FT><<<grid, SE_THREADS, sh.smem, s>>>(P, sh.nbuf, Yc, Yf, L);
 }
 template <class FT>
 void launch_passB(const DevParams<FT> &P, const FT *Yc, const FT *Yf, const FT *L, FT *Tc, FT *Tf, cudaStream_t s) {
   se_device();
-  const int nbuf = pick_nbuf(PassBLayout<FT>(P.Nv, 2));
-  const int grid = min(P.Nh, g_se.nsm);
-  k_passB<FT><<<grid, SE_THREADS, PassBLayout<FT>(P.Nv, nbuf).total, s>>>(P, nbuf, Yc, Yf, L, Tc, Tf);
+  const SeShape sh = se_shape<FT, PassBLayout<FT>>(P.Nv);
+  const int grid = min(P.Nh, g_se.nsm * sh.ctas);
+  k_passB<FT><<<grid, SE_THREADS, sh.smem, s>>>(P, sh.nbuf, Yc, Yf, L, Tc, Tf);
 }
 
 #define INST(FT)                                                                                             \

@@ -21,7 +21,11 @@ SYMBOLS = [
     "gb_set_precomputed_quantities", "gb_remaining_tendency", "gb_implicit_tendency", "gb_update_jacobian",
     "gb_ldiv", "gb_correct_implicit_advection_tendency", "gb_dss", "gb_step", "gb_global_sums",
     "gb_newton_residual", "gb_time_kernel", "gb_jacobian_solve_noalloc",
+    "gb_columns_create", "gb_columns_destroy", "gb_columns_set_stream", "gb_columns_size", "gb_columns_solve",
+    "gb_columns_autotune", "gb_columns_set_variant", "gb_columns_last_error",
 ]
+GB_COLUMNS_GRAPH, GB_COLUMNS_PERSISTENT, GB_COLUMNS_PER_HEIGHT = 0, 1, 2
+GB_COLUMNS_VARIANTS = 5
 GB_NOALLOC_SCRATCH_BYTES = 64 << 20
 
 
@@ -90,6 +94,15 @@ def load(build_if_missing=True):
     L.gb_newton_residual.argtypes = [_vp, _dp]
     L.gb_time_kernel.argtypes = [_vp, _c_int, fv, _c_int, _dp]
     L.gb_jacobian_solve_noalloc.argtypes = [_vp, fv, fv, fv, _c_double]
+    _llp = ctypes.POINTER(ctypes.c_longlong)
+    L.gb_columns_create.argtypes = [cfgp, _c_int, _ip, ctypes.POINTER(_vp)]
+    L.gb_columns_destroy.argtypes = [_vp]
+    L.gb_columns_set_stream.argtypes = [_vp, _vp]
+    L.gb_columns_size.argtypes = [_vp, _llp, _llp]
+    L.gb_columns_solve.argtypes = [_vp, fv, fv, _c_double, _c_int, _c_int, _dp]
+    L.gb_columns_autotune.argtypes = [_vp, fv, fv, _c_double, _c_int, _c_int, _ip, _dp]
+    L.gb_columns_set_variant.argtypes = [_vp, _c_int]
+    L.gb_columns_last_error.argtypes = [_vp, ctypes.c_char_p, ctypes.c_size_t]
     for s in SYMBOLS:
         getattr(L, s).restype = _c_int
     _lib = L

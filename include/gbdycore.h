@@ -151,6 +151,64 @@ int gb_jacobian_solve_noalloc(gb_ctx *ctx, gb_fieldvec dY, gb_fieldvec Y, gb_fie
 enum gb_kernel_id { GB_K_PASSA = 0, GB_K_PASSB = 1, GB_K_COLUMN = 2, GB_K_DSS = 3, GB_K_FINAL = 4 };
 int gb_time_kernel(gb_ctx *ctx, int kernel, gb_fieldvec Y, int reps, double *ms_per_launch);
 
+/* ---------------------------------------------------------------------------
+ * Batched standalone columns of uneven height.
+ *
+ * A batch of independent dry columns, each a ColumnGrid of its own z_elem
+ * (src/simulation/grids.jl:93-127: flat column metric, faces uniform or
+ * tanh-stretched as gb_config.z_stretch / dz_bottom / z_max say), solved by
+ * NewtonsMethod(max_iters = newton_iters, update_j =
+ * UpdateEvery(NewNewtonIteration)) (integrator.jl:63-120) on the implicit
+ * stage equation U = U^ + dtgamma T_imp(U): each iteration is
+ * implicit_tendency! (implicit_tendency.jl:185-298) for the residual,
+ * update_jacobian! (manual_sparse_jacobian.jl:713-870) and ldiv! with
+ * BlockArrowheadSolve (:580-583), with the impenetrable filter on u_3
+ * (precomputed_quantities.jl:486-553).  Columns do not interact.
+ *
+ * Layout (C_c = sum over d < c of z_elem_d, C = C_ncols):
+ *   c : [4][C]          (rho, u_1, u_2, rho e_tot), column c at C_c .. C_c + z_elem_c - 1
+ *   f : [C + ncols]     u_3, column c at C_c + c .. C_c + c + z_elem_c
+ * Precision and constants come from gb_config (h_elem, dt, hyperdiffusion,
+ * upwinding and the radius are unused; the column metric is flat).
+ *
+ * Modes of gb_columns_solve:
+ *   GB_COLUMNS_GRAPH       one persistent launch (warps take groups of
+ *                          columns of one height class from a work counter,
+ *                          tallest first), captured with its reset and the
+ *                          residual reduction as one CUDA graph and replayed;
+ *   GB_COLUMNS_PERSISTENT  the same launch sequence without the graph;
+ *   GB_COLUMNS_PER_HEIGHT  the plain form: one launch per distinct z_elem.
+ * The persistent kernel variant (columns per block, levels per lane) is the
+ * one gb_columns_autotune chose, else a default.
+ * ------------------------------------------------------------------------- */
+typedef struct gb_columns gb_columns;
+enum gb_columns_mode { GB_COLUMNS_GRAPH = 0, GB_COLUMNS_PERSISTENT = 1, GB_COLUMNS_PER_HEIGHT = 2 };
+#define GB_COLUMNS_VARIANTS 5
+
+/* z_elem[c] in [2, 127].  Builds the per-height level tables and the work
+ * lists; allocates device memory. */
+int gb_columns_create(const gb_config *cfg, int ncols, const int *z_elem, gb_columns **out);
+int gb_columns_destroy(gb_columns *cols);
+int gb_columns_set_stream(gb_columns *cols, void *cuda_stream);
+/* Total centres C (the component stride of the centre block). */
+int gb_columns_size(const gb_columns *cols, long long *centres, long long *faces);
+/* U: the initial iterate on entry (normally a copy of Uhat), the iterate after
+ * newton_iters iterations on return (u_h set to Uhat's, u_3 filtered).  rnorm, if
+ * not NULL, receives newton_iters x 3 FP64 sums over the batch of the squared
+ * residual (rho, rho e_tot, u_3) of each iteration, and the call synchronizes;
+ * otherwise it is asynchronous.  newton_iters in [1, 8]. */
+int gb_columns_solve(gb_columns *cols, gb_fieldvec U, gb_fieldvec Uhat, double dtgamma, int newton_iters, int mode,
+                     double *rnorm);
+/* Times every persistent kernel variant (each from the same initial iterate U,
+ * which is left unchanged) and keeps the fastest for later solves.  ms, if not
+ * NULL, receives GB_COLUMNS_VARIANTS mean times (negative: variant not
+ * applicable); *choice the chosen variant.  Synchronous. */
+int gb_columns_autotune(gb_columns *cols, gb_fieldvec U, gb_fieldvec Uhat, double dtgamma, int newton_iters,
+                        int reps, int *choice, double *ms);
+/* Sets the persistent kernel variant (0 .. GB_COLUMNS_VARIANTS - 1) directly. */
+int gb_columns_set_variant(gb_columns *cols, int variant);
+int gb_columns_last_error(const gb_columns *cols, char *buf, size_t len);
+
 #ifdef __cplusplus
 }
 #endif

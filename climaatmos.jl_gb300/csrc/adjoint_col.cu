@@ -1,0 +1,583 @@
+// Reverse (adjoint) kernel of the implicit column stage.
+//
+// The forward stage (kernels_colg.cu) maps the assembled stage state U^ to
+//   U   = filter(U^ - W(U^)^-1 R(U^)) with the van Leer minus central
+//         correction of rho e_tot added (implicit_tendency.jl:322-339),
+//   T_imp = (U - U^) / dtgamma,
+// where R = dtgamma T_imp(U0) + (U^ - U0), U0 = filter(U^), is the residual of
+// implicit_tendency! (implicit_tendency.jl:185-298) and W the manual Jacobian
+// (manual_sparse_jacobian.jl:713-870) solved by BlockArrowheadSolve (:580-583).
+// This kernel is the exact reverse mode of that map, including the
+// dependence of W on the state: with x = W^-1 R,
+//   cotangent(U^) = (dR/dU^)^T y - (d(W x)/dU^)^T y,   y = W^-T cotangent(x),
+// so it solves the transposed Schur-complement tridiagonal system and runs the
+// Jacobian-entry, residual and thermodynamic formulas backwards.  It then
+// distributes cotangent(U^) to u_n and to the stage tendencies it was
+// assembled from (U^ = u_n + dt sum_j (a~_ij T_exp_j + a_ij T_imp_j)) and
+// accumulates d/d(sponge rate) (beta_w = rate s(z)).
+//
+// One thread per column with serial sweeps over the levels (the forward and
+// transposed tridiagonal solves by the Thomas algorithm); the per-column
+// intermediates live in a column-major global scratch so that the threads of
+// a warp access consecutive words.
+#include "kernels.cuh"
+
+namespace gb {
+
+namespace {
+
+// scratch arrays (each [Nf][ncols])
+enum ColScr {
+  // centres
+  S_R0 = 0, S_RE, S_U1, S_U2, S_K, S_H, S_PI, S_THV, S_THVR, S_PHIR, S_RJ, S_IJ, S_RR, S_RES, S_RN, S_REN,
+  S_HN, S_RJN,
+  S_BR, S_BRE, S_BU1, S_BU2, S_BK, S_BH, S_BPI, S_BTHV, S_BTHVR, S_BPHIR, S_BRJ, S_BRN, S_BREN, S_BHN, S_BRJN,
+  S_BRR, S_BRES, S_BRU0, S_BRU1, S_BEU0, S_BEU1,
+  // faces (forward values, then the cotangents S_BU3 .. S_BFHB, which the reverse pass zeroes)
+  S_U3, S_H4, S_A, S_B, S_C, S_D, S_CP, S_DP, S_X, S_U3N, S_FR, S_FHB,
+  S_BU3, S_BH4, S_BX, S_BD, S_BU3N, S_BF, S_BFH, S_BFR, S_BFHB,
+  S_NUM
+};
+
+template <class FT>
+struct ColVjpArgs {
+  StageArgs<FT> A;        // the forward stage's sources and coefficients (U_c etc. unused)
+  const FT *Ub_c, *Ub_f;  // cotangent of U (4 centre fields, faces)
+  const FT *Tb_c, *Tb_f;  // cotangent of T_imp (rho, rho e_tot; faces)
+  FT *Yb_c, *Yb_f;        // cotangent of u_n (accumulated)
+  FT *Teb_c[4], *Teb_f[4];  // cotangents of the explicit tendencies (accumulated)
+  FT *Tib_c[4], *Tib_f[4];  // cotangents of the implicit tendencies (accumulated)
+  FT *scr;
+  double *dalpha;         // per-column d/d(sponge rate)
+};
+
+template <class FT>
+__device__ __forceinline__ FT vl_value(FT u, FT am2, FT am1, FT a0, FT ap1, bool near, FT dtm) {
+  const bool pos = u >= FT(0);
+  const FT lo = pos ? am2 : am1, c = pos ? am1 : a0, hi = pos ? a0 : ap1;
+  if (near) return u * c;
+  const FT da = (hi - lo) / FT(2);
+  const FT mn = fmin(lo, fmin(c, hi)), mx = fmax(lo, fmax(c, hi));
+  const FT sl = copysign(fmin(fabs(da), fmin(FT(2) * (c - mn), FT(2) * (mx - c))), da);
+  const FT half = sl * (FT(1) - fabs(u) * dtm) / FT(2);
+  return u * (pos ? c + half : c - half);
+}
+
+// Partial derivatives of vl_value (piecewise: the active branch of the limiter).
+// dh[0..3] are the derivatives with respect to (am2, am1, a0, ap1).
+template <class FT>
+__device__ __forceinline__ void vl_grad(FT u, FT am2, FT am1, FT a0, FT ap1, bool near, FT dtm, FT &du, FT (&dh)[4]) {
+  const bool pos = u >= FT(0);
+  const int ilo = pos ? 0 : 1, ic = pos ? 1 : 2, ihi = pos ? 2 : 3;
+  const FT lo = pos ? am2 : am1, c = pos ? am1 : a0, hi = pos ? a0 : ap1;
+  dh[0] = dh[1] = dh[2] = dh[3] = FT(0);
+  if (near) {
+    du = c;
+    dh[ic] = u;
+    return;
+  }
+  const FT da = (hi - lo) / FT(2);
+  const FT mn = fmin(lo, fmin(c, hi)), mx = fmax(lo, fmax(c, hi));
+  const FT m1 = fabs(da), m2 = FT(2) * (c - mn), m3 = FT(2) * (mx - c);
+  const FT sgn = copysign(FT(1), da);
+  // d sl / d (lo, c, hi)
+  FT dl[3] = {FT(0), FT(0), FT(0)};
+  FT sl;
+  if (m1 <= m2 && m1 <= m3) {
+    sl = da;
+    dl[0] = -FT(0.5);
+    dl[2] = FT(0.5);
+  } else if (m2 <= m3) {
+    sl = sgn * m2;
+    dl[1] += FT(2) * sgn;
+    const int imn = (lo <= c && lo <= hi) ? 0 : (c <= hi ? 1 : 2);
+    dl[imn] -= FT(2) * sgn;
+  } else {
+    sl = sgn * m3;
+    dl[1] -= FT(2) * sgn;
+    const int imx = (lo >= c && lo >= hi) ? 0 : (c >= hi ? 1 : 2);
+    dl[imx] += FT(2) * sgn;
+  }
+  const FT f = (FT(1) - fabs(u) * dtm) / FT(2);
+  const FT half = sl * f;
+  const FT s = pos ? FT(1) : FT(-1);  // value = u (c + s half)
+  du = c + s * half + u * s * sl * (-copysign(FT(1), u) * dtm / FT(2));
+  const FT k = u * s * f;  // d value / d sl
+  dh[ilo] += k * dl[0];
+  dh[ic] += u + k * dl[1];
+  dh[ihi] += k * dl[2];
+}
+
+template <class FT>
+__global__ void __launch_bounds__(128) k_col_stage_vjp(DevParams<FT> P, ColVjpArgs<FT> V) {
+  const int ncols = P.Nh * NN;
+  const int col = blockIdx.x * blockDim.x + threadIdx.x;
+  if (col >= ncols) return;
+  const StageArgs<FT> &A = V.A;
+  const int e = col >> 4, n = col & 15, Nv = P.Nv, Nf = P.Nf;
+  FT *const scr = V.scr;
+  auto S = [&](int q, int k) -> FT & { return scr[((size_t)q * Nf + k) * ncols + col]; };
+  ColGeo<FT> G;
+  G.load(P, e, n);
+  const FT dtg = A.dtg, idtg = A.idtg, kap = P.Rd * P.icvd;
+  const size_t cb = (size_t)e * 4 * NN * Nv + (size_t)n * Nv, rb = (size_t)e * 2 * NN * Nv + (size_t)n * Nv;
+  const size_t fb = ((size_t)e * NN + n) * Nf;
+  const int sc = NN * Nv;
+  // ------------------------------------------------ forward recompute
+  // stage assembly (the forward kernel's order of additions)
+  for (int v = 0; v < Nv; ++v) {
+    FT h[4];
+    for (int c = 0; c < 4; ++c) h[c] = A.un_c[cb + (size_t)c * sc + v];
+    for (int j = 0; j < A.nsrc; ++j) {
+      for (int c = 0; c < 4; ++c) {
+        h[c] += A.ce[j] * A.te_c[j][cb + (size_t)c * sc + v];
+        if (j >= 1 && (c == 0 || c == 3)) h[c] += A.ci[j] * A.ti_c[j][rb + (size_t)(c == 0 ? 0 : sc) + v];
+      }
+    }
+    S(S_R0, v) = h[0];
+    S(S_U1, v) = h[1];
+    S(S_U2, v) = h[2];
+    S(S_RE, v) = h[3];
+  }
+  for (int f = 0; f < Nf; ++f) {
+    FT h = A.un_f[fb + f];
+    for (int j = 0; j < A.nsrc; ++j) {
+      h += A.ce[j] * A.te_f[j][fb + f];
+      if (j >= 1) h += A.ci[j] * A.ti_f[j][fb + f];
+    }
+    S(S_H4, f) = h;
+    S(S_U3, f) = (f == 0 || f == Nv) ? FT(0) : h;
+  }
+  auto g33 = [&](int f) { return P.lf4[f].x; };
+  // centre diagnostics of U0
+  for (int v = 0; v < Nv; ++v) {
+    const Lev4<FT> L = P.lc4[v];
+    const FT u1 = S(S_U1, v), u2 = S(S_U2, v), a = S(S_U3, v), b = S(S_U3, v + 1);
+    const FT c1 = (G.gu0 * u1 + G.gu1 * u2) * L.z, c2 = (G.gu1 * u1 + G.gu2 * u2) * L.z;
+    const FT K = (u1 * c1 + u2 * c2 + (a * (a * g33(v)) + b * (b * g33(v + 1))) / FT(2)) / FT(2);
+    Thermo<FT> th;
+    thermo(P, S(S_R0, v), S(S_RE, v), K, L.w, th);
+    S(S_K, v) = K;
+    S(S_H, v) = th.h;
+    S(S_PI, v) = th.Pi;
+    S(S_THV, v) = th.thv;
+    S(S_THVR, v) = th.thvr;
+    S(S_PHIR, v) = th.phir;
+    S(S_RJ, v) = S(S_R0, v) * (G.Jh * L.x);
+    S(S_IJ, v) = G.iJh * L.y;
+  }
+  // face fluxes (zero on the boundary faces)
+  auto face_F = [&](int f, FT &F, FT &Fh, FT &fr, FT &fhb) {
+    if (f == 0 || f >= Nv) { F = Fh = fr = fhb = FT(0); return; }
+    const FT rJb = (S(S_RJ, f - 1) + S(S_RJ, f)) / FT(2), hb = (S(S_H, f - 1) + S(S_H, f)) / FT(2);
+    F = rJb * (S(S_U3, f) * g33(f));
+    Fh = F * hb;
+    fr = rJb * g33(f);
+    fhb = hb;
+  };
+  for (int f = 0; f < Nf; ++f) {
+    FT F, Fh, fr, fhb;
+    face_F(f, F, Fh, fr, fhb);
+    S(S_FR, f) = fr;
+    S(S_FHB, f) = fhb;
+  }
+  // centre rows: residual and (scalar, u_3) blocks
+  auto crow = [&](int v, FT &ru0, FT &ru1, FT &eu0, FT &eu1) {
+    const FT iJ = S(S_IJ, v);
+    ru0 = dtg * (S(S_FR, v) * iJ);
+    ru1 = dtg * (-S(S_FR, v + 1) * iJ);
+    eu0 = dtg * (S(S_FR, v) * iJ * S(S_FHB, v));
+    eu1 = dtg * (-S(S_FR, v + 1) * iJ * S(S_FHB, v + 1));
+  };
+  for (int v = 0; v < Nv; ++v) {
+    FT Fa, Fha, fra, fhba, Fb, Fhb, frb, fhbb;
+    face_F(v, Fa, Fha, fra, fhba);
+    face_F(v + 1, Fb, Fhb, frb, fhbb);
+    S(S_RR, v) = dtg * (-((Fb - Fa) * S(S_IJ, v)));
+    S(S_RES, v) = dtg * (-((Fhb - Fha) * S(S_IJ, v)));
+  }
+  // face rows of W and R, Schur complement onto u_3
+  struct FRow { FT ur0, ur1, ue0, uu0, uu1, uu2, T3; };
+  auto frow = [&](int f) {
+    FRow r;
+    const FT beta = P.lf4[f].y;
+    const FT u3 = S(S_U3, f);
+    if (f == 0 || f >= Nv) {
+      r.ur0 = r.ur1 = r.ue0 = r.uu0 = r.uu2 = FT(0);
+      r.uu1 = -dtg * beta - FT(1);
+      r.T3 = -beta * u3;
+      return r;
+    }
+    const int a = f - 1, b = f;
+    const FT ra = S(S_R0, a), rbv = S(S_R0, b);
+    const FT irb = FT(1) / ((ra + rbv) / FT(2));
+    const FT dpa = kap * (P.T0 * P.cpd - S(S_K, a) - P.lc4[a].w);
+    const FT dpb = kap * (P.T0 * P.cpd - S(S_K, b) - P.lc4[b].w);
+    const FT buoy = P.cpd * ((S(S_THV, a) + S(S_THV, b)) / FT(2)) * (S(S_PI, b) - S(S_PI, a)) * irb;
+    r.ur0 = dtg * (dpa * irb + buoy / FT(2));
+    r.ur1 = dtg * (-dpb * irb + buoy / FT(2));
+    r.ue0 = dtg * (kap * irb);
+    const FT u3cm = S(S_U3, f - 1) * g33(f - 1), u3c = u3 * g33(f), u3cp = S(S_U3, f + 1) * g33(f + 1);
+    r.uu0 = dtg * (-kap * ra * u3cm * (irb / FT(2)));
+    r.uu1 = dtg * (kap * (rbv - ra) * u3c * (irb / FT(2)) - beta) - FT(1);
+    r.uu2 = dtg * (kap * rbv * u3cp * (irb / FT(2)));
+    const FT thd = ((S(S_THV, a) - S(S_THVR, a)) + (S(S_THV, b) - S(S_THVR, b))) / FT(2);
+    r.T3 = -(P.lf4[f].z - (S(S_PHIR, b) - S(S_PHIR, a)) + P.cpd * thd * (S(S_PI, b) - S(S_PI, a))) - beta * u3;
+    return r;
+  };
+  for (int f = 0; f < Nf; ++f) {
+    const FRow r = frow(f);
+    FT aa = r.uu0, bb = r.uu1, cc = r.uu2, rhs = dtg * r.T3 + (S(S_H4, f) - S(S_U3, f));
+    if (f >= 1) {
+      FT ru0, ru1, eu0, eu1;
+      crow(f - 1, ru0, ru1, eu0, eu1);
+      aa += r.ur0 * ru0 + r.ue0 * eu0;
+      bb += r.ur0 * ru1 + r.ue0 * eu1;
+      rhs += r.ur0 * S(S_RR, f - 1) + r.ue0 * S(S_RES, f - 1);
+    }
+    if (f < Nv) {
+      FT ru0, ru1, eu0, eu1;
+      crow(f, ru0, ru1, eu0, eu1);
+      bb += r.ur1 * ru0 - r.ue0 * eu0;
+      cc += r.ur1 * ru1 - r.ue0 * eu1;
+      rhs += r.ur1 * S(S_RR, f) - r.ue0 * S(S_RES, f);
+    }
+    S(S_A, f) = aa;
+    S(S_B, f) = bb;
+    S(S_C, f) = cc;
+    S(S_D, f) = rhs;
+  }
+  // Thomas solve A x = D
+  {
+    FT cp = S(S_C, 0) / S(S_B, 0), dp = S(S_D, 0) / S(S_B, 0);
+    S(S_CP, 0) = cp;
+    S(S_DP, 0) = dp;
+    for (int f = 1; f < Nf; ++f) {
+      const FT m = S(S_B, f) - S(S_A, f) * cp;
+      cp = S(S_C, f) / m;
+      dp = (S(S_D, f) - S(S_A, f) * dp) / m;
+      S(S_CP, f) = cp;
+      S(S_DP, f) = dp;
+    }
+    FT x = dp;
+    S(S_X, Nf - 1) = x;
+    for (int f = Nf - 2; f >= 0; --f) {
+      x = S(S_DP, f) - S(S_CP, f) * x;
+      S(S_X, f) = x;
+    }
+  }
+  // back-substitution
+  for (int v = 0; v < Nv; ++v) {
+    FT ru0, ru1, eu0, eu1;
+    crow(v, ru0, ru1, eu0, eu1);
+    const FT xa = S(S_X, v), xb = S(S_X, v + 1);
+    S(S_RN, v) = S(S_R0, v) - (ru0 * xa + ru1 * xb - S(S_RR, v));
+    S(S_REN, v) = S(S_RE, v) - (eu0 * xa + eu1 * xb - S(S_RES, v));
+  }
+  for (int f = 0; f < Nf; ++f) S(S_U3N, f) = (f == 0 || f >= Nv) ? FT(0) : S(S_U3, f) - S(S_X, f);
+  // van Leer forward quantities at the Newton result
+  for (int v = 0; v < Nv; ++v) {
+    const Lev4<FT> L = P.lc4[v];
+    const FT u1 = S(S_U1, v), u2 = S(S_U2, v), a = S(S_U3N, v), b = S(S_U3N, v + 1);
+    const FT c1 = (G.gu0 * u1 + G.gu1 * u2) * L.z, c2 = (G.gu1 * u1 + G.gu2 * u2) * L.z;
+    const FT K = (u1 * c1 + u2 * c2 + (a * (a * g33(v)) + b * (b * g33(v + 1))) / FT(2)) / FT(2);
+    Thermo<FT> th;
+    thermo(P, S(S_RN, v), S(S_REN, v), K, L.w, th);
+    S(S_HN, v) = th.h;
+    S(S_RJN, v) = S(S_RN, v) * (G.Jh * L.x);
+  }
+  // ------------------------------------------------ reverse
+  for (int v = 0; v < Nv; ++v)
+    for (int q = S_BR; q <= S_BEU1; ++q) S(q, v) = FT(0);
+  for (int f = 0; f < Nf; ++f)
+    for (int q = S_BU3; q <= S_BFHB; ++q) S(q, f) = FT(0);
+  double dal = 0;
+  // output cotangents: U and T_imp = (U - U^) / dtgamma
+  for (int v = 0; v < Nv; ++v) {
+    S(S_BRN, v) = V.Ub_c[cb + v] + V.Tb_c[rb + v] * idtg;
+    S(S_BREN, v) = V.Ub_c[cb + (size_t)3 * sc + v] + V.Tb_c[rb + (size_t)sc + v] * idtg;
+  }
+  for (int f = 0; f < Nf; ++f) S(S_BU3N, f) = V.Ub_f[fb + f] + V.Tb_f[fb + f] * idtg;
+  // (a) van Leer correction: rhoe_out = rhoe_n + dtgamma corr(state_n)
+  if (P.upwinding) {
+    for (int f = 1; f < Nv; ++f) {
+      FT cb_ = FT(0);  // cotangent of fup(f); that of fcen(f) is -cb_
+      if (f < Nv) cb_ += dtg * S(S_BREN, f) * S(S_IJ, f);
+      cb_ -= dtg * S(S_BREN, f - 1) * S(S_IJ, f - 1);
+      const FT u = S(S_U3N, f) * g33(f);
+      const FT rJb = (S(S_RJN, f - 1) + S(S_RJN, f)) / FT(2);
+      const bool near = f == 1 || f == Nv - 1;
+      const FT hm2 = f >= 2 ? S(S_HN, f - 2) : FT(0), hm1 = S(S_HN, f - 1), h0 = S(S_HN, f);
+      const FT hp1 = f + 1 < Nv ? S(S_HN, f + 1) : FT(0);
+      const FT vl = vl_value(u, hm2, hm1, h0, hp1, near, P.dt_model);
+      FT du, dh[4];
+      vl_grad(u, hm2, hm1, h0, hp1, near, P.dt_model, du, dh);
+      const FT hm = (hm1 + h0) / FT(2);
+      const FT rJbb = cb_ * vl - cb_ * u * hm;
+      S(S_BRJN, f - 1) += rJbb / FT(2);
+      S(S_BRJN, f) += rJbb / FT(2);
+      const FT ub = cb_ * rJb * du - cb_ * rJb * hm;
+      S(S_BU3N, f) += ub * g33(f);
+      if (f >= 2) S(S_BHN, f - 2) += cb_ * rJb * dh[0];
+      S(S_BHN, f - 1) += cb_ * rJb * dh[1] - cb_ * rJb * u / FT(2);
+      S(S_BHN, f) += cb_ * rJb * dh[2] - cb_ * rJb * u / FT(2);
+      if (f + 1 < Nv) S(S_BHN, f + 1) += cb_ * rJb * dh[3];
+    }
+    for (int v = 0; v < Nv; ++v) {
+      const Lev4<FT> L = P.lc4[v];
+      const FT u1 = S(S_U1, v), u2 = S(S_U2, v), a = S(S_U3N, v), b = S(S_U3N, v + 1);
+      const FT c1 = (G.gu0 * u1 + G.gu1 * u2) * L.z, c2 = (G.gu1 * u1 + G.gu2 * u2) * L.z;
+      const FT K = (u1 * c1 + u2 * c2 + (a * (a * g33(v)) + b * (b * g33(v + 1))) / FT(2)) / FT(2);
+      ThermoBar<FT> tb{};
+      tb.h = S(S_BHN, v);
+      FT rb_, reb, Kb;
+      thermo_vjp(P, S(S_RN, v), S(S_REN, v), K, L.w, tb, rb_, reb, Kb);
+      S(S_BRN, v) += rb_ + (G.Jh * L.x) * S(S_BRJN, v);
+      S(S_BREN, v) += reb;
+      S(S_BU1, v) += c1 * Kb;
+      S(S_BU2, v) += c2 * Kb;
+      S(S_BU3N, v) += Kb * a * g33(v) / FT(2);
+      S(S_BU3N, v + 1) += Kb * b * g33(v + 1) / FT(2);
+    }
+  }
+  // (b) back-substitution
+  for (int v = 0; v < Nv; ++v) {
+    S(S_BR, v) += S(S_BRN, v);
+    S(S_BRE, v) += S(S_BREN, v);
+    S(S_BRR, v) += S(S_BRN, v);
+    S(S_BRES, v) += S(S_BREN, v);
+    S(S_BRU0, v) -= S(S_BRN, v) * S(S_X, v);
+    S(S_BRU1, v) -= S(S_BRN, v) * S(S_X, v + 1);
+    S(S_BEU0, v) -= S(S_BREN, v) * S(S_X, v);
+    S(S_BEU1, v) -= S(S_BREN, v) * S(S_X, v + 1);
+  }
+  for (int f = 0; f < Nf; ++f) {
+    FT xb = FT(0);
+    if (f < Nv) {
+      FT ru0, ru1, eu0, eu1;
+      crow(f, ru0, ru1, eu0, eu1);
+      xb -= S(S_BRN, f) * ru0 + S(S_BREN, f) * eu0;
+    }
+    if (f >= 1) {
+      FT ru0, ru1, eu0, eu1;
+      crow(f - 1, ru0, ru1, eu0, eu1);
+      xb -= S(S_BRN, f - 1) * ru1 + S(S_BREN, f - 1) * eu1;
+    }
+    const bool inner = f > 0 && f < Nv;
+    if (inner) {
+      xb -= S(S_BU3N, f);
+      S(S_BU3, f) += S(S_BU3N, f);
+    }
+    S(S_BX, f) = xb;
+  }
+  // (c) transposed solve A^T dbar = xbar  (A^T: sub C[f-1], diagonal B[f], super A[f+1])
+  {
+    FT cp = (Nf > 1 ? S(S_A, 1) : FT(0)) / S(S_B, 0), dp = S(S_BX, 0) / S(S_B, 0);
+    S(S_CP, 0) = cp;
+    S(S_DP, 0) = dp;
+    for (int f = 1; f < Nf; ++f) {
+      const FT sub = S(S_C, f - 1);
+      const FT m = S(S_B, f) - sub * cp;
+      cp = (f + 1 < Nf ? S(S_A, f + 1) : FT(0)) / m;
+      dp = (S(S_BX, f) - sub * dp) / m;
+      S(S_CP, f) = cp;
+      S(S_DP, f) = dp;
+    }
+    FT y = dp;
+    S(S_BD, Nf - 1) = y;
+    for (int f = Nf - 2; f >= 0; --f) {
+      y = S(S_DP, f) - S(S_CP, f) * y;
+      S(S_BD, f) = y;
+    }
+  }
+  // (d) Schur rows, Jacobian entries and the u_3 tendency
+  for (int f = 0; f < Nf; ++f) {
+    const FT db = S(S_BD, f);
+    const FT ab = f >= 1 ? -db * S(S_X, f - 1) : FT(0);
+    const FT bbb = -db * S(S_X, f);
+    const FT cbb = f + 1 < Nf ? -db * S(S_X, f + 1) : FT(0);
+    const FRow r = frow(f);
+    FT ur0b = FT(0), ur1b = FT(0), ue0b = FT(0);
+    if (f >= 1) {
+      FT ru0, ru1, eu0, eu1;
+      crow(f - 1, ru0, ru1, eu0, eu1);
+      ur0b += ru0 * ab + ru1 * bbb + S(S_RR, f - 1) * db;
+      ue0b += eu0 * ab + eu1 * bbb + S(S_RES, f - 1) * db;
+      S(S_BRU0, f - 1) += r.ur0 * ab;
+      S(S_BRU1, f - 1) += r.ur0 * bbb;
+      S(S_BEU0, f - 1) += r.ue0 * ab;
+      S(S_BEU1, f - 1) += r.ue0 * bbb;
+      S(S_BRR, f - 1) += r.ur0 * db;
+      S(S_BRES, f - 1) += r.ue0 * db;
+    }
+    if (f < Nv) {
+      FT ru0, ru1, eu0, eu1;
+      crow(f, ru0, ru1, eu0, eu1);
+      ur1b += ru0 * bbb + ru1 * cbb + S(S_RR, f) * db;
+      ue0b -= eu0 * bbb + eu1 * cbb + S(S_RES, f) * db;
+      S(S_BRU0, f) += r.ur1 * bbb;
+      S(S_BRU1, f) += r.ur1 * cbb;
+      S(S_BEU0, f) -= r.ue0 * bbb;
+      S(S_BEU1, f) -= r.ue0 * cbb;
+      S(S_BRR, f) += r.ur1 * db;
+      S(S_BRES, f) -= r.ue0 * db;
+    }
+    // rhs = dtgamma T3 + (U^_3 - U0_3)
+    const FT T3b = dtg * db;
+    S(S_BH4, f) += db;
+    S(S_BU3, f) -= db;
+    const FT spg = P.levf[LF_SPG * Nf + f], beta = P.lf4[f].y;
+    const FT u3 = S(S_U3, f);
+    S(S_BU3, f) -= beta * T3b;
+    dal -= (double)(spg * u3 * T3b);
+    dal -= (double)(dtg * spg * bbb);  // uu1 = dtgamma (... - beta) - 1
+    if (f == 0 || f >= Nv) continue;
+    const int a = f - 1, b = f;
+    // T3 = -(dPhi - (Phi_r(b) - Phi_r(a)) + cp thd (Pi(b) - Pi(a))) - beta u3
+    const FT dPi = S(S_PI, b) - S(S_PI, a);
+    const FT thd = ((S(S_THV, a) - S(S_THVR, a)) + (S(S_THV, b) - S(S_THVR, b))) / FT(2);
+    S(S_BPHIR, b) += T3b;
+    S(S_BPHIR, a) -= T3b;
+    const FT thdb = -P.cpd * dPi * T3b;
+    S(S_BPI, b) -= P.cpd * thd * T3b;
+    S(S_BPI, a) += P.cpd * thd * T3b;
+    S(S_BTHV, a) += thdb / FT(2);
+    S(S_BTHVR, a) -= thdb / FT(2);
+    S(S_BTHV, b) += thdb / FT(2);
+    S(S_BTHVR, b) -= thdb / FT(2);
+    // Jacobian entries
+    const FT uu0b = ab, uu1b = bbb, uu2b = cbb;
+    const FT ra = S(S_R0, a), rbv = S(S_R0, b);
+    const FT irb = FT(1) / ((ra + rbv) / FT(2));
+    const FT dpa = kap * (P.T0 * P.cpd - S(S_K, a) - P.lc4[a].w);
+    const FT dpb = kap * (P.T0 * P.cpd - S(S_K, b) - P.lc4[b].w);
+    const FT thvb = (S(S_THV, a) + S(S_THV, b)) / FT(2);
+    const FT buoy = P.cpd * thvb * dPi * irb;
+    const FT u3cm = S(S_U3, f - 1) * g33(f - 1), u3c = u3 * g33(f), u3cp = S(S_U3, f + 1) * g33(f + 1);
+    const FT dpab = dtg * irb * ur0b, dpbb = -dtg * irb * ur1b, buoyb = dtg * (ur0b + ur1b) / FT(2);
+    FT irbb = dtg * (dpa * ur0b - dpb * ur1b) + dtg * kap * ue0b;
+    irbb += dtg * (-kap * ra * u3cm / FT(2)) * uu0b + dtg * (kap * (rbv - ra) * u3c / FT(2)) * uu1b +
+            dtg * (kap * rbv * u3cp / FT(2)) * uu2b;
+    irbb += buoyb * P.cpd * thvb * dPi;
+    const FT thvbb = buoyb * P.cpd * dPi * irb, dPib = buoyb * P.cpd * thvb * irb;
+    S(S_BR, a) += dtg * (-kap * u3cm * irb / FT(2)) * uu0b - dtg * kap * u3c * irb / FT(2) * uu1b;
+    S(S_BR, b) += dtg * kap * u3c * irb / FT(2) * uu1b + dtg * kap * u3cp * irb / FT(2) * uu2b;
+    S(S_BU3, f - 1) += dtg * (-kap * ra * irb / FT(2)) * uu0b * g33(f - 1);
+    S(S_BU3, f) += dtg * kap * (rbv - ra) * irb / FT(2) * uu1b * g33(f);
+    S(S_BU3, f + 1) += dtg * kap * rbv * irb / FT(2) * uu2b * g33(f + 1);
+    S(S_BK, a) -= kap * dpab;
+    S(S_BK, b) -= kap * dpbb;
+    const FT rbarb = -irb * irb * irbb;
+    S(S_BR, a) += rbarb / FT(2);
+    S(S_BR, b) += rbarb / FT(2);
+    S(S_BTHV, a) += thvbb / FT(2);
+    S(S_BTHV, b) += thvbb / FT(2);
+    S(S_BPI, b) += dPib;
+    S(S_BPI, a) -= dPib;
+  }
+  // (e) centre rows: R_rho = dtgamma T_rho, blocks from fr, fhb
+  for (int v = 0; v < Nv; ++v) {
+    const FT iJ = S(S_IJ, v);
+    const FT Trb = dtg * S(S_BRR, v), Teb = dtg * S(S_BRES, v);
+    S(S_BF, v + 1) -= Trb * iJ;
+    S(S_BF, v) += Trb * iJ;
+    S(S_BFH, v + 1) -= Teb * iJ;
+    S(S_BFH, v) += Teb * iJ;
+    S(S_BFR, v) += dtg * iJ * S(S_BRU0, v) + dtg * iJ * S(S_FHB, v) * S(S_BEU0, v);
+    S(S_BFR, v + 1) -= dtg * iJ * S(S_BRU1, v) + dtg * iJ * S(S_FHB, v + 1) * S(S_BEU1, v);
+    S(S_BFHB, v) += dtg * S(S_FR, v) * iJ * S(S_BEU0, v);
+    S(S_BFHB, v + 1) -= dtg * S(S_FR, v + 1) * iJ * S(S_BEU1, v);
+  }
+  // (f) face fluxes F = rJb u3c, Fh = F hb, fr = rJb g33, fhb = hb
+  for (int f = 1; f < Nv; ++f) {
+    FT F, Fh, fr, fhb;
+    face_F(f, F, Fh, fr, fhb);
+    const FT rJb = (S(S_RJ, f - 1) + S(S_RJ, f)) / FT(2), hb = fhb;
+    const FT Fb = S(S_BF, f) + S(S_BFH, f) * hb;
+    const FT hbb = S(S_BFH, f) * F + S(S_BFHB, f);
+    const FT rJbb = Fb * (S(S_U3, f) * g33(f)) + S(S_BFR, f) * g33(f);
+    S(S_BU3, f) += Fb * rJb * g33(f);
+    S(S_BH, f - 1) += hbb / FT(2);
+    S(S_BH, f) += hbb / FT(2);
+    S(S_BRJ, f - 1) += rJbb / FT(2);
+    S(S_BRJ, f) += rJbb / FT(2);
+  }
+  // (g) centre diagnostics of U0
+  for (int v = 0; v < Nv; ++v) {
+    const Lev4<FT> L = P.lc4[v];
+    const FT u1 = S(S_U1, v), u2 = S(S_U2, v), a = S(S_U3, v), b = S(S_U3, v + 1);
+    const FT c1 = (G.gu0 * u1 + G.gu1 * u2) * L.z, c2 = (G.gu1 * u1 + G.gu2 * u2) * L.z;
+    ThermoBar<FT> tb{};
+    tb.h = S(S_BH, v);
+    tb.Pi = S(S_BPI, v);
+    tb.thv = S(S_BTHV, v);
+    tb.thvr = S(S_BTHVR, v);
+    tb.phir = S(S_BPHIR, v);
+    FT rb_, reb, Kb;
+    thermo_vjp(P, S(S_R0, v), S(S_RE, v), S(S_K, v), L.w, tb, rb_, reb, Kb);
+    S(S_BR, v) += rb_ + (G.Jh * L.x) * S(S_BRJ, v);
+    S(S_BRE, v) += reb;
+    const FT Kt = Kb + S(S_BK, v);
+    S(S_BU1, v) += c1 * Kt;
+    S(S_BU2, v) += c2 * Kt;
+    S(S_BU3, v) += Kt * a * g33(v) / FT(2);
+    S(S_BU3, v + 1) += Kt * b * g33(v + 1) / FT(2);
+  }
+  // ------------------------------------------------ cotangent of U^ and its distribution
+  for (int v = 0; v < Nv; ++v) {
+    const FT hb[4] = {S(S_BR, v) - V.Tb_c[rb + v] * idtg, S(S_BU1, v) + V.Ub_c[cb + (size_t)sc + v],
+                      S(S_BU2, v) + V.Ub_c[cb + (size_t)2 * sc + v], S(S_BRE, v) - V.Tb_c[rb + (size_t)sc + v] * idtg};
+    for (int c = 0; c < 4; ++c) V.Yb_c[cb + (size_t)c * sc + v] += hb[c];
+    for (int j = 0; j < A.nsrc; ++j) {
+      for (int c = 0; c < 4; ++c) V.Teb_c[j][cb + (size_t)c * sc + v] += A.ce[j] * hb[c];
+      if (j >= 1) {
+        V.Tib_c[j][rb + v] += A.ci[j] * hb[0];
+        V.Tib_c[j][rb + (size_t)sc + v] += A.ci[j] * hb[3];
+      }
+    }
+  }
+  for (int f = 0; f < Nf; ++f) {
+    const bool inner = f > 0 && f < Nv;
+    const FT hb = S(S_BH4, f) + (inner ? S(S_BU3, f) : FT(0)) - V.Tb_f[fb + f] * idtg;
+    V.Yb_f[fb + f] += hb;
+    for (int j = 0; j < A.nsrc; ++j) {
+      V.Teb_f[j][fb + f] += A.ce[j] * hb;
+      if (j >= 1) V.Tib_f[j][fb + f] += A.ci[j] * hb;
+    }
+  }
+  V.dalpha[col] = dal;
+}
+
+}  // namespace
+
+size_t col_vjp_scratch_words(int Nh, int Nv) { return (size_t)S_NUM * (Nv + 1) * (size_t)Nh * NN; }
+
+template <class FT>
+void launch_column_stage_vjp(const DevParams<FT> &P, const StageArgs<FT> &A, const FT *Ub_c, const FT *Ub_f,
+                             const FT *Tb_c, const FT *Tb_f, FT *Yb_c, FT *Yb_f, FT *const Teb[4], FT *const Tib[4],
+                             size_t NC, size_t NR, FT *scr, double *dalpha, cudaStream_t s) {
+  ColVjpArgs<FT> V{};
+  V.A = A;
+  V.Ub_c = Ub_c; V.Ub_f = Ub_f; V.Tb_c = Tb_c; V.Tb_f = Tb_f; V.Yb_c = Yb_c; V.Yb_f = Yb_f;
+  for (int j = 0; j < 4; ++j) {
+    V.Teb_c[j] = Teb[j];
+    V.Teb_f[j] = Teb[j] ? Teb[j] + NC : nullptr;
+    V.Tib_c[j] = Tib[j];
+    V.Tib_f[j] = Tib[j] ? Tib[j] + NR : nullptr;
+  }
+  V.scr = scr;
+  V.dalpha = dalpha;
+  const int ncols = P.Nh * NN;
+  k_col_stage_vjp<FT><<<(ncols + 127) / 128, 128, 0, s>>>(P, V);
+}
+
+template void launch_column_stage_vjp<float>(const DevParams<float> &, const StageArgs<float> &, const float *,
+                                             const float *, const float *, const float *, float *, float *,
+                                             float *const[4], float *const[4], size_t, size_t, float *, double *,
+                                             cudaStream_t);
+template void launch_column_stage_vjp<double>(const DevParams<double> &, const StageArgs<double> &, const double *,
+                                              const double *, const double *, const double *, double *, double *,
+                                              double *const[4], double *const[4], size_t, size_t, double *,
+                                              double *, cudaStream_t);
+
+}  // namespace gb

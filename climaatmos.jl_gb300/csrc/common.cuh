@@ -88,6 +88,42 @@ __device__ __forceinline__ void thermo(const DevParams<FT> &P, FT rho, FT rhoe, 
   o.thvr = Tr * iPi;
   o.phir = -P.cpd * (P.Tmin_ref * glog(Pi) + (P.Tsfc_ref - P.Tmin_ref) / FT(7) * (Pi7 - FT(1)));
 }
+// Reverse mode of thermo(): the cotangents of its outputs (T, p, h, Pi, thv,
+// thvr, phir) and of the reference temperature T_r(Pi) give those of
+// (rho, rho e_tot, K).  Uses dPi/dp = kappa Pi / p, dT_r/dPi = 7 (T_sfc - T_min) Pi^6,
+// dPhi_r/dPi = -cp T_r / Pi; T has no sensitivity where it is clamped at T_min_sgs.
+template <class FT>
+struct ThermoBar {
+  FT T, p, h, Pi, thv, thvr, phir, Tr;
+};
+template <class FT>
+__device__ __forceinline__ void thermo_vjp(const DevParams<FT> &P, FT rho, FT rhoe, FT K, FT Phi,
+                                           const ThermoBar<FT> &b, FT &rho_b, FT &rhoe_b, FT &K_b) {
+  const FT e = gdiv(rhoe, rho);
+  const FT Tu = P.T0 + (e - K - Phi + P.Rd * P.T0) * P.icvd;
+  const bool clamped = !(Tu > P.Tmin_sgs);
+  const FT T = clamped ? P.Tmin_sgs : Tu;
+  const FT p = rho * P.Rd * T;
+  const FT Pi = gpow(p * P.ipref, P.kappa);
+  const FT Pi2 = Pi * Pi, Pi7 = Pi2 * Pi2 * Pi2 * Pi;
+  const FT dT = P.Tsfc_ref - P.Tmin_ref;
+  const FT Tr = P.Tmin_ref + dT * Pi7;
+  const FT iPi = grcp(Pi), iPi2 = iPi * iPi;
+  const FT Pib = b.Pi - T * iPi2 * b.thv + (FT(7) * dT * Pi7 - Tr) * iPi2 * b.thvr - P.cpd * Tr * iPi * b.phir +
+                 FT(7) * dT * Pi7 * iPi * b.Tr;
+  const FT pb = b.p + P.kappa * Pi * gdiv(Pib, p);
+  const FT Tb = b.T + iPi * b.thv + P.Rd * b.h + rho * P.Rd * pb;
+  FT eb = b.h;
+  FT Kb = FT(0);
+  if (!clamped) {
+    eb += Tb * P.icvd;
+    Kb = -Tb * P.icvd;
+  }
+  rho_b = P.Rd * T * pb - gdiv(eb * e, rho);
+  rhoe_b = gdiv(eb, rho);
+  K_b = Kb;
+}
+
 template <class FT>
 __device__ __forceinline__ FT sd_r(const DevParams<FT> &P, FT Pi, FT phir) {
   FT Pi2 = Pi * Pi, Pi7 = Pi2 * Pi2 * Pi2 * Pi;

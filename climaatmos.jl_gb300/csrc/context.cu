@@ -1,5 +1,6 @@
 // C ABI of the GB300 dry dynamical core: context, hooks and the fused ARS343
 // step (see include/gbdycore.h for the interface and its reference citations).
+#include <algorithm>
 #include <cstdio>
 #include <cstring>
 #include <memory>
@@ -41,6 +42,20 @@ struct Impl : ImplBase {
   bool jac_valid = false;
   // ARS343 tableau (explicit a~, implicit a, weights b~ = b)
   double ae[4][4], ai[4][4], be[4], bi[4];
+  // reverse mode (allocated on first use)
+  struct Record {  // forward data of one step kept for its reverse pass
+    DevBuf Y, U[4], L[4], Te[4], Ti[4];
+  };
+  struct Adjoint {
+    std::vector<std::unique_ptr<Record>> rec;
+    std::vector<std::unique_ptr<DevBuf>> ckpt;
+    DevBuf Ub, Tb, Lb, Teb[4], Tib[4], zero, dummy, scr, dparB, dal, dacc, work;
+    int nsteps = 0, every = 0, grid = 0;
+    double dt = 0;
+    bool ready = false;
+    size_t bytes = 0, rec_bytes = 0;
+  };
+  std::unique_ptr<Adjoint> adj;
   // captured step graph
   cudaGraphExec_t gexec = nullptr;
   cudaStream_t cap = nullptr;  // private stream the step graph is captured on
@@ -413,6 +428,362 @@ constexpr int NOALLOC_MAX_DEVICES = 64;
 void *g_noalloc_ptr[NOALLOC_MAX_DEVICES] = {};
 std::mutex g_noalloc_mu;
 
+// ---------------------------------------------------------------- reverse mode
+template <class FT>
+int alloc_z(gb_ctx *ctx, DevBuf &b, size_t bytes, size_t &total) {
+  int r = alloc(ctx, b, bytes);
+  total += bytes;
+  return r;
+}
+
+template <class FT>
+int ensure_adjoint(gb_ctx *ctx) {
+  Impl<FT> *I = impl<FT>(ctx);
+  if (I->adj) return GB_OK;
+  int dev = 0, optin = 0, nsm = 0;
+  CK(cudaGetDevice(&dev));
+  CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  if (passB_vjp_smem<FT>(I->P.Nv) + 2 * 256 * sizeof(double) > (size_t)optin)
+    return fail(ctx, GB_ERR_ARG, "z_elem too large for the reverse-mode slab kernels at this precision (shared memory)");
+  configure_adjoint_se<FT>(I->P.Nv);
+  auto A = std::make_unique<typename Impl<FT>::Adjoint>();
+  const size_t S = (I->NC + I->NF) * sizeof(FT), R = (I->NR + I->NF) * sizeof(FT);
+  const int ncols = I->P.Nh * NN;
+  A->grid = std::min(I->P.Nh, nsm);
+  size_t &t = A->bytes;
+  int r;
+  if ((r = alloc_z<FT>(ctx, A->Ub, S, t)) || (r = alloc_z<FT>(ctx, A->Tb, S, t)) ||
+      (r = alloc_z<FT>(ctx, A->Lb, I->NC * sizeof(FT), t)) || (r = alloc_z<FT>(ctx, A->zero, S, t)) ||
+      (r = alloc_z<FT>(ctx, A->dummy, S, t)) || (r = alloc_z<FT>(ctx, A->work, S, t)) ||
+      (r = alloc_z<FT>(ctx, A->scr, col_vjp_scratch_words(I->P.Nh, I->P.Nv) * sizeof(FT), t)) ||
+      (r = alloc_z<FT>(ctx, A->dparB, (size_t)A->grid * 2 * sizeof(double), t)) ||
+      (r = alloc_z<FT>(ctx, A->dal, (size_t)ncols * sizeof(double), t)) ||
+      (r = alloc_z<FT>(ctx, A->dacc, 4 * sizeof(double), t)))
+    return r;
+  for (int j = 0; j < 4; ++j)
+    if ((r = alloc_z<FT>(ctx, A->Teb[j], S, t))) return r;
+  for (int j = 1; j < 4; ++j)
+    if ((r = alloc_z<FT>(ctx, A->Tib[j], R, t))) return r;
+  I->adj = std::move(A);
+  return GB_OK;
+}
+
+template <class FT>
+int ensure_records(gb_ctx *ctx, int n) {
+  Impl<FT> *I = impl<FT>(ctx);
+  auto &A = *I->adj;
+  const size_t S = (I->NC + I->NF) * sizeof(FT), R = (I->NR + I->NF) * sizeof(FT), L = I->NC * sizeof(FT);
+  while ((int)A.rec.size() < n) {
+    auto rc = std::make_unique<typename Impl<FT>::Record>();
+    size_t t = 0;
+    int r;
+    if ((r = alloc_z<FT>(ctx, rc->Y, S, t))) return r;
+    for (int i = 0; i < 4; ++i) {
+      if ((r = alloc_z<FT>(ctx, rc->L[i], L, t)) || (r = alloc_z<FT>(ctx, rc->Te[i], S, t))) return r;
+      if (i >= 1 && ((r = alloc_z<FT>(ctx, rc->U[i], S, t)) || (r = alloc_z<FT>(ctx, rc->Ti[i], R, t)))) return r;
+    }
+    A.rec_bytes = t;
+    A.bytes += t;
+    A.rec.push_back(std::move(rc));
+  }
+  return GB_OK;
+}
+
+// Sources of implicit stage i (1..3) as the fused step assembles them.
+template <class FT>
+StageArgs<FT> stage_args(Impl<FT> *I, int i, FT dt, const FT *Yc, const FT *Yf, FT *const Te[4], FT *const Ti[4]) {
+  StageArgs<FT> A{};
+  A.un_c = Yc; A.un_f = Yf;
+  A.nsrc = i;
+  for (int j = 0; j < i; ++j) {
+    A.te_c[j] = I->ae[i][j] != 0 ? Te[j] : nullptr;
+    A.te_f[j] = I->ae[i][j] != 0 ? Te[j] + I->NC : nullptr;
+    A.ce[j] = dt * (FT)I->ae[i][j];
+    A.ti_c[j] = I->ai[i][j] != 0 ? Ti[j] : nullptr;
+    A.ti_f[j] = I->ai[i][j] != 0 ? Ti[j] + I->NR : nullptr;
+    A.ci[j] = dt * (FT)I->ai[i][j];
+  }
+  A.dtg = dt * (FT)I->ai[i][i];
+  A.idtg = (FT)1 / A.dtg;
+  A.rnorm = (double *)I->rnorm.p;
+  A.first = i == 1;
+  return A;
+}
+
+// One fused ARS343 step on Y (the arithmetic of enqueue_step) that keeps the
+// stage states, Laplacians and tendencies in rec.
+template <class FT>
+void record_step(gb_ctx *ctx, FT *Yc, FT *Yf, double dt_, typename Impl<FT>::Record &rec, cudaStream_t s) {
+  Impl<FT> *I = impl<FT>(ctx);
+  const DevParams<FT> &P = I->P;
+  const FT dt = (FT)dt_;
+  cudaMemcpyAsync(rec.Y.p, Yc, I->NC * sizeof(FT), cudaMemcpyDeviceToDevice, s);
+  cudaMemcpyAsync((FT *)rec.Y.p + I->NC, Yf, I->NF * sizeof(FT), cudaMemcpyDeviceToDevice, s);
+  FT *Te[4], *Ti[4] = {nullptr, nullptr, nullptr, nullptr};
+  for (int j = 0; j < 4; ++j) {
+    Te[j] = (FT *)rec.Te[j].p;
+    if (j >= 1) Ti[j] = (FT *)rec.Ti[j].p;
+  }
+  for (int i = 0; i < 4; ++i) {
+    FT *Uc = Yc, *Uf = Yf;
+    if (i >= 1) {
+      StageArgs<FT> A = stage_args<FT>(I, i, dt, Yc, Yf, Te, Ti);
+      Uc = (FT *)rec.U[i].p;
+      Uf = Uc + I->NC;
+      A.U_c = Uc; A.U_f = Uf;
+      A.Ti_c = Ti[i]; A.Ti_f = Ti[i] + I->NR;
+      launch_column_stage<FT>(P, A, s);
+    }
+    FT *L = (FT *)rec.L[i].p;
+    launch_passA<FT>(P, Uc, Uf, L, s);
+    launch_dss<FT>(P, L, nullptr, s);
+    launch_passB<FT>(P, Uc, Uf, L, Te[i], Te[i] + I->NC, s);
+    launch_dss<FT>(P, Te[i], Te[i] + I->NC, s);
+  }
+  StageArgs<FT> A{};
+  A.nsrc = 4;
+  for (int j = 0; j < 4; ++j) {
+    A.te_c[j] = I->be[j] != 0 ? Te[j] : nullptr;
+    A.te_f[j] = I->be[j] != 0 ? Te[j] + I->NC : nullptr;
+    A.ce[j] = dt * (FT)I->be[j];
+    A.ti_c[j] = I->bi[j] != 0 && Ti[j] ? Ti[j] : nullptr;
+    A.ti_f[j] = I->bi[j] != 0 && Ti[j] ? Ti[j] + I->NR : nullptr;
+    A.ci[j] = dt * (FT)I->bi[j];
+  }
+  launch_final<FT>(P, A, Yc, Yf, s);
+}
+
+// Reverse of the explicit tendency of one stage state U: Ub += (dT/dU)^T Tb_in
+// where Tb_in (copied, not modified) is the cotangent of the DSSed tendency
+// (dss_out, as inside the step) or of the tendency as gb_remaining_tendency
+// returns it (not DSSed).
+template <class FT>
+void tendency_vjp(gb_ctx *ctx, const FT *Uc, const FT *Uf, const FT *L, const FT *Tb_c, const FT *Tb_f, FT *Ubc,
+                  FT *Ubf, bool dss_out, cudaStream_t s) {
+  Impl<FT> *I = impl<FT>(ctx);
+  auto &A = *I->adj;
+  const DevParams<FT> &P = I->P;
+  FT *Tb = (FT *)A.Tb.p, *Lb = (FT *)A.Lb.p;
+  cudaMemcpyAsync(Tb, Tb_c, I->NC * sizeof(FT), cudaMemcpyDeviceToDevice, s);
+  cudaMemcpyAsync(Tb + I->NC, Tb_f, I->NF * sizeof(FT), cudaMemcpyDeviceToDevice, s);
+  if (dss_out) launch_dss_transpose<FT>(P, Tb, Tb + I->NC, s);
+  launch_passB_vjp<FT>(P, Uc, Uf, L, Tb, Tb + I->NC, Ubc, Ubf, Lb, (double *)A.dparB.p, A.grid, s);
+  launch_accum((const double *)A.dparB.p, A.grid, 2, 2, (double *)A.dacc.p, s);
+  launch_dss_transpose<FT>(P, Lb, nullptr, s);
+  launch_passA_vjp<FT>(P, Uc, Uf, Lb, Ubc, Ubf, A.grid, s);
+}
+
+// Reverse of one recorded step: Yb holds the cotangent of u_{n+1} on entry and
+// that of u_n on return; d/dnu and d/d(sponge rate) accumulate in dacc.
+template <class FT>
+void reverse_step(gb_ctx *ctx, typename Impl<FT>::Record &rec, double dt_, FT *Ybc, FT *Ybf, cudaStream_t s) {
+  Impl<FT> *I = impl<FT>(ctx);
+  auto &A = *I->adj;
+  const DevParams<FT> &P = I->P;
+  const FT dt = (FT)dt_;
+  const size_t SB = (I->NC + I->NF) * sizeof(FT), RB = (I->NR + I->NF) * sizeof(FT);
+  FT *Teb[4], *Tib[4] = {nullptr, nullptr, nullptr, nullptr}, *Te[4], *Ti[4] = {nullptr, nullptr, nullptr, nullptr};
+  for (int j = 0; j < 4; ++j) {
+    Teb[j] = (FT *)A.Teb[j].p;
+    Te[j] = (FT *)rec.Te[j].p;
+    cudaMemsetAsync(Teb[j], 0, SB, s);
+    if (j >= 1) {
+      Tib[j] = (FT *)A.Tib[j].p;
+      Ti[j] = (FT *)rec.Ti[j].p;
+      cudaMemsetAsync(Tib[j], 0, RB, s);
+    }
+  }
+  // final combination u_{n+1} = u_n + dt sum_j b_j (T_exp_j + T_imp_j), filtered
+  CotArgs<FT> F{};
+  F.nsrc = 4;
+  for (int j = 0; j < 4; ++j) {
+    F.te_c[j] = I->be[j] != 0 ? Teb[j] : nullptr;
+    F.te_f[j] = I->be[j] != 0 ? Teb[j] + I->NC : nullptr;
+    F.ce[j] = dt * (FT)I->be[j];
+    F.ti_c[j] = I->bi[j] != 0 && Tib[j] ? Tib[j] : nullptr;
+    F.ti_f[j] = I->bi[j] != 0 && Tib[j] ? Tib[j] + I->NR : nullptr;
+    F.ci[j] = dt * (FT)I->bi[j];
+  }
+  launch_final_transpose<FT>(P, F, Ybc, Ybf, s);
+  const FT *Yc = (const FT *)rec.Y.p, *Yf = Yc + I->NC;
+  FT *Ubc = (FT *)A.Ub.p, *Ubf = Ubc + I->NC;
+  for (int i = 3; i >= 0; --i) {
+    const FT *Uc = i == 0 ? Yc : (const FT *)rec.U[i].p, *Uf = Uc + I->NC;
+    cudaMemsetAsync(Ubc, 0, SB, s);
+    tendency_vjp<FT>(ctx, Uc, Uf, (const FT *)rec.L[i].p, Teb[i], Teb[i] + I->NC, Ubc, Ubf, true, s);
+    if (i == 0) {
+      launch_axpy<FT>(I->NC, FT(1), Ubc, Ybc, s);  // the caller's c and f blocks are separate allocations
+      launch_axpy<FT>(I->NF, FT(1), Ubf, Ybf, s);
+    } else {
+      const StageArgs<FT> SA = stage_args<FT>(I, i, dt, Yc, Yf, Te, Ti);
+      launch_column_stage_vjp<FT>(P, SA, Ubc, Ubf, Tib[i], Tib[i] + I->NR, Ybc, Ybf, Teb, Tib, I->NC, I->NR,
+                                  (FT *)A.scr.p, (double *)A.dal.p, s);
+      launch_accum((const double *)A.dal.p, P.Nh * NN, 1, 1, (double *)A.dacc.p + 1, s);
+    }
+  }
+}
+
+template <class FT>
+int dss_transpose_t(gb_ctx *ctx, gb_fieldvec X) {
+  launch_dss_transpose<FT>(impl<FT>(ctx)->P, (FT *)X.c, (FT *)X.f, ctx->stream);
+  return check_launch(ctx);
+}
+
+template <class FT>
+int read_dacc(gb_ctx *ctx, double *dpar, bool add) {
+  Impl<FT> *I = impl<FT>(ctx);
+  double h[2];
+  CK(cudaMemcpyAsync(h, I->adj->dacc.p, 2 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  if (dpar) {
+    dpar[0] = (add ? dpar[0] : 0.0) + h[0];
+    dpar[1] = (add ? dpar[1] : 0.0) + h[1];
+  }
+  return GB_OK;
+}
+
+template <class FT>
+int remaining_tendency_vjp_t(gb_ctx *ctx, gb_fieldvec Yb, gb_fieldvec Tb, gb_fieldvec Y, double *dpar) {
+  int r = ensure_adjoint<FT>(ctx);
+  if (r) return r;
+  Impl<FT> *I = impl<FT>(ctx);
+  cudaStream_t s = ctx->stream;
+  CK(cudaMemsetAsync(I->adj->dacc.p, 0, 4 * sizeof(double), s));
+  // forward Laplacians at Y (DSSed), then the reverse
+  FT *L = (FT *)I->lap.p;
+  launch_passA<FT>(I->P, (const FT *)Y.c, (const FT *)Y.f, L, s);
+  launch_dss<FT>(I->P, L, nullptr, s);
+  tendency_vjp<FT>(ctx, (const FT *)Y.c, (const FT *)Y.f, L, (const FT *)Tb.c, (const FT *)Tb.f, (FT *)Yb.c,
+                   (FT *)Yb.f, false, s);
+  if ((r = check_launch(ctx))) return r;
+  return read_dacc<FT>(ctx, dpar, true);
+}
+
+template <class FT>
+StageArgs<FT> single_stage_args(Impl<FT> *I, const FT *Uhc, const FT *Uhf, double dtg) {
+  // U^ given directly: one source, the zero field, with coefficient 0
+  StageArgs<FT> A{};
+  A.un_c = Uhc; A.un_f = Uhf;
+  A.nsrc = 1;
+  A.te_c[0] = (const FT *)I->adj->zero.p;
+  A.te_f[0] = (const FT *)I->adj->zero.p + I->NC;
+  A.ce[0] = FT(0);
+  A.dtg = (FT)dtg;
+  A.idtg = (FT)1 / A.dtg;
+  A.rnorm = (double *)I->rnorm.p;
+  A.first = 1;
+  return A;
+}
+
+template <class FT>
+int implicit_stage_t(gb_ctx *ctx, gb_fieldvec U, gb_fieldvec Ti, gb_fieldvec Uh, double dtg) {
+  int r = ensure_adjoint<FT>(ctx);
+  if (r) return r;
+  Impl<FT> *I = impl<FT>(ctx);
+  StageArgs<FT> A = single_stage_args<FT>(I, (const FT *)Uh.c, (const FT *)Uh.f, dtg);
+  A.U_c = (FT *)U.c; A.U_f = (FT *)U.f;
+  A.Ti_c = (FT *)Ti.c; A.Ti_f = (FT *)Ti.f;
+  launch_column_stage<FT>(I->P, A, ctx->stream);
+  return check_launch(ctx);
+}
+
+template <class FT>
+int implicit_stage_vjp_t(gb_ctx *ctx, gb_fieldvec Uhb, gb_fieldvec Ub, gb_fieldvec Tib, gb_fieldvec Uh, double dtg,
+                         double *dpar) {
+  int r = ensure_adjoint<FT>(ctx);
+  if (r) return r;
+  Impl<FT> *I = impl<FT>(ctx);
+  cudaStream_t s = ctx->stream;
+  CK(cudaMemsetAsync(I->adj->dacc.p, 0, 4 * sizeof(double), s));
+  const StageArgs<FT> A = single_stage_args<FT>(I, (const FT *)Uh.c, (const FT *)Uh.f, dtg);
+  FT *Teb[4] = {(FT *)I->adj->dummy.p, nullptr, nullptr, nullptr}, *Tibs[4] = {nullptr, nullptr, nullptr, nullptr};
+  launch_column_stage_vjp<FT>(I->P, A, (const FT *)Ub.c, (const FT *)Ub.f, (const FT *)Tib.c, (const FT *)Tib.f,
+                              (FT *)Uhb.c, (FT *)Uhb.f, Teb, Tibs, I->NC, I->NR, (FT *)I->adj->scr.p,
+                              (double *)I->adj->dal.p, s);
+  launch_accum((const double *)I->adj->dal.p, I->P.Nh * NN, 1, 1, (double *)I->adj->dacc.p + 1, s);
+  if ((r = check_launch(ctx))) return r;
+  return read_dacc<FT>(ctx, dpar, true);
+}
+
+template <class FT>
+int step_vjp_t(gb_ctx *ctx, gb_fieldvec Yb, gb_fieldvec Y, double dt, double *dpar) {
+  int r = ensure_adjoint<FT>(ctx);
+  if (r || (r = ensure_records<FT>(ctx, 1))) return r;
+  Impl<FT> *I = impl<FT>(ctx);
+  cudaStream_t s = ctx->stream;
+  auto &A = *I->adj;
+  FT *W = (FT *)A.work.p;
+  CK(cudaMemcpyAsync(W, Y.c, I->NC * sizeof(FT), cudaMemcpyDeviceToDevice, s));
+  CK(cudaMemcpyAsync(W + I->NC, Y.f, I->NF * sizeof(FT), cudaMemcpyDeviceToDevice, s));
+  CK(cudaMemsetAsync(A.dacc.p, 0, 4 * sizeof(double), s));
+  record_step<FT>(ctx, W, W + I->NC, dt, *A.rec[0], s);
+  reverse_step<FT>(ctx, *A.rec[0], dt, (FT *)Yb.c, (FT *)Yb.f, s);
+  if ((r = check_launch(ctx))) return r;
+  if ((r = read_dacc<FT>(ctx, dpar, true))) return r;
+  return read_status<FT>(ctx);
+}
+
+template <class FT>
+int adjoint_forward_t(gb_ctx *ctx, gb_fieldvec Y, double dt, int nsteps, int every) {
+  int r = ensure_adjoint<FT>(ctx);
+  if (r) return r;
+  Impl<FT> *I = impl<FT>(ctx);
+  auto &A = *I->adj;
+  const size_t SB = (I->NC + I->NF) * sizeof(FT);
+  const int nck = (nsteps + every - 1) / every;
+  while ((int)A.ckpt.size() < nck) {
+    auto b = std::make_unique<DevBuf>();
+    if ((r = alloc_z<FT>(ctx, *b, SB, A.bytes))) return r;
+    A.ckpt.push_back(std::move(b));
+  }
+  cudaStream_t s = ctx->stream;
+  FT *Yc = (FT *)Y.c, *Yf = (FT *)Y.f;
+  for (int k = 0; k < nsteps; ++k) {
+    if (k % every == 0) {
+      FT *ck = (FT *)A.ckpt[k / every]->p;
+      CK(cudaMemcpyAsync(ck, Yc, I->NC * sizeof(FT), cudaMemcpyDeviceToDevice, s));
+      CK(cudaMemcpyAsync(ck + I->NC, Yf, I->NF * sizeof(FT), cudaMemcpyDeviceToDevice, s));
+    }
+    enqueue_step<FT>(ctx, Yc, Yf, dt, s);
+  }
+  A.nsteps = nsteps;
+  A.every = every;
+  A.dt = dt;
+  A.ready = true;
+  if ((r = check_launch(ctx))) return r;
+  return read_status<FT>(ctx);
+}
+
+template <class FT>
+int adjoint_reverse_t(gb_ctx *ctx, gb_fieldvec Yb, double *dpar, size_t *peak) {
+  Impl<FT> *I = impl<FT>(ctx);
+  if (!I->adj || !I->adj->ready) return fail(ctx, GB_ERR_STATE, "gb_adjoint_reverse called before gb_adjoint_forward");
+  auto &A = *I->adj;
+  int r = ensure_records<FT>(ctx, A.every);
+  if (r) return r;
+  cudaStream_t s = ctx->stream;
+  const size_t SB = (I->NC + I->NF) * sizeof(FT);
+  FT *W = (FT *)A.work.p;
+  CK(cudaMemsetAsync(A.dacc.p, 0, 4 * sizeof(double), s));
+  const int nseg = (A.nsteps + A.every - 1) / A.every;
+  for (int g = nseg - 1; g >= 0; --g) {
+    const int s0 = g * A.every, s1 = std::min(A.nsteps, s0 + A.every);
+    CK(cudaMemcpyAsync(W, A.ckpt[g]->p, SB, cudaMemcpyDeviceToDevice, s));
+    for (int k = s0; k < s1; ++k) record_step<FT>(ctx, W, W + I->NC, A.dt, *A.rec[k - s0], s);
+    for (int k = s1 - 1; k >= s0; --k) reverse_step<FT>(ctx, *A.rec[k - s0], A.dt, (FT *)Yb.c, (FT *)Yb.f, s);
+    if ((r = check_launch(ctx))) return r;
+  }
+  if ((r = read_dacc<FT>(ctx, dpar, false))) return r;
+  if (peak) {
+    size_t base = 0;
+    base += (I->NC + I->NF) * sizeof(FT) * (2 + 4) + (I->NR + I->NF) * sizeof(FT) * 3 + I->NC * sizeof(FT);
+    *peak = base + A.bytes;
+  }
+  A.ready = false;
+  return read_status<FT>(ctx);
+}
+
 int noalloc_scratch(gb_ctx *ctx, void **out) {
   int dev = 0;
   CK(cudaGetDevice(&dev));
@@ -621,6 +992,52 @@ int gb_jacobian_solve_noalloc(gb_ctx *ctx, gb_fieldvec dY, gb_fieldvec Y, gb_fie
   GUARD(ctx);
   if (!fv_ok(dY) || !fv_ok(Y) || !fv_ok(R)) return fail(ctx, GB_ERR_ARG, "null or misaligned pointer");
   return DISPATCH(ctx, jacobian_solve_noalloc_t, ctx, dY, Y, R, dtgamma);
+}
+
+int gb_dss_transpose(gb_ctx *ctx, gb_fieldvec X) {
+  if (!ctx || !X.c || !X.f) return GB_ERR_ARG;
+  return ctx->cfg.ft_bytes == 8 ? dss_transpose_t<double>(ctx, X) : dss_transpose_t<float>(ctx, X);
+}
+
+int gb_remaining_tendency_vjp(gb_ctx *ctx, gb_fieldvec Ybar, gb_fieldvec Tbar, gb_fieldvec Y, double t,
+                              double dparams[2]) {
+  (void)t;
+  if (!ctx || !Ybar.c || !Ybar.f || !Tbar.c || !Tbar.f || !Y.c || !Y.f) return GB_ERR_ARG;
+  return ctx->cfg.ft_bytes == 8 ? remaining_tendency_vjp_t<double>(ctx, Ybar, Tbar, Y, dparams)
+                                : remaining_tendency_vjp_t<float>(ctx, Ybar, Tbar, Y, dparams);
+}
+
+int gb_implicit_stage(gb_ctx *ctx, gb_fieldvec U, gb_fieldvec Timp, gb_fieldvec Uhat, double dtgamma) {
+  if (!ctx || !U.c || !U.f || !Timp.c || !Timp.f || !Uhat.c || !Uhat.f || !(dtgamma > 0)) return GB_ERR_ARG;
+  return ctx->cfg.ft_bytes == 8 ? implicit_stage_t<double>(ctx, U, Timp, Uhat, dtgamma)
+                                : implicit_stage_t<float>(ctx, U, Timp, Uhat, dtgamma);
+}
+
+int gb_implicit_stage_vjp(gb_ctx *ctx, gb_fieldvec Uhat_bar, gb_fieldvec Ubar, gb_fieldvec Timp_bar, gb_fieldvec Uhat,
+                          double dtgamma, double dparams[2]) {
+  if (!ctx || !Uhat_bar.c || !Ubar.c || !Timp_bar.c || !Uhat.c || !(dtgamma > 0)) return GB_ERR_ARG;
+  return ctx->cfg.ft_bytes == 8 ? implicit_stage_vjp_t<double>(ctx, Uhat_bar, Ubar, Timp_bar, Uhat, dtgamma, dparams)
+                                : implicit_stage_vjp_t<float>(ctx, Uhat_bar, Ubar, Timp_bar, Uhat, dtgamma, dparams);
+}
+
+int gb_step_vjp(gb_ctx *ctx, gb_fieldvec Ybar, gb_fieldvec Y, double t, double dt, double dparams[2]) {
+  (void)t;
+  if (!ctx || !Ybar.c || !Ybar.f || !Y.c || !Y.f || !(dt > 0)) return GB_ERR_ARG;
+  return ctx->cfg.ft_bytes == 8 ? step_vjp_t<double>(ctx, Ybar, Y, dt, dparams)
+                                : step_vjp_t<float>(ctx, Ybar, Y, dt, dparams);
+}
+
+int gb_adjoint_forward(gb_ctx *ctx, gb_fieldvec Y, double t0, double dt, int nsteps, int checkpoint_every) {
+  (void)t0;
+  if (!ctx || !Y.c || !Y.f || !(dt > 0) || nsteps < 1 || checkpoint_every < 1) return GB_ERR_ARG;
+  return ctx->cfg.ft_bytes == 8 ? adjoint_forward_t<double>(ctx, Y, dt, nsteps, checkpoint_every)
+                                : adjoint_forward_t<float>(ctx, Y, dt, nsteps, checkpoint_every);
+}
+
+int gb_adjoint_reverse(gb_ctx *ctx, gb_fieldvec Ybar, double dparams[2], size_t *peak_bytes) {
+  if (!ctx || !Ybar.c || !Ybar.f) return GB_ERR_ARG;
+  return ctx->cfg.ft_bytes == 8 ? adjoint_reverse_t<double>(ctx, Ybar, dparams, peak_bytes)
+                                : adjoint_reverse_t<float>(ctx, Ybar, dparams, peak_bytes);
 }
 
 int gb_time_kernel(gb_ctx *ctx, int kernel, gb_fieldvec Y, int reps, double *ms) {

@@ -239,6 +239,7 @@ void build_geometry(const gb_config &c, HostGeometry &g) {
     g.levc[LC_BETA * Nv + v] = beta_sponge(g.zc[v], c.sponge_zd, c.z_max, c.alpha_uh);
     g.levc[LC_IR2 * Nv + v] = 1.0 / (g.rc[v] * g.rc[v]);
     g.levc[LC_IDZ * Nv + v] = 1.0 / g.dzc[v];
+    g.levc[LC_SPG * Nv + v] = beta_sponge(g.zc[v], c.sponge_zd, c.z_max, 1.0);
   }
   g.levf.assign((size_t)LF_N * Nf, 0);
   for (int k = 0; k < Nf; ++k) {
@@ -251,6 +252,7 @@ void build_geometry(const gb_config &c, HostGeometry &g) {
     g.levf[LF_IR2 * Nf + k] = 1.0 / (g.rf[k] * g.rf[k]);
     g.levf[LF_IDZ * Nf + k] = 1.0 / g.dzf[k];
     g.levf[LF_G33 * Nf + k] = 1.0 / (g.dzf[k] * g.dzf[k]);
+    g.levf[LF_SPG * Nf + k] = beta_sponge(g.zf[k], c.sponge_zd, c.z_max, 1.0);
   }
 }
 

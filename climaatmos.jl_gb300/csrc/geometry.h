@@ -12,9 +12,10 @@ constexpr int NN = 16;
 // Per-node horizontal geometry quantities stored for the kernels ([elem][q][node]).
 enum HGeo { HG_JH = 0, HG_GU0, HG_GU1, HG_GU2, HG_GD0, HG_GD1, HG_GD2, HG_F3, HG_FH1, HG_FH2, HG_IJH, HG_N };
 // Per-level centre quantities ([q][Nv]).
-enum LevC { LC_Z = 0, LC_R2, LC_DZ, LC_PHI, LC_BETA, LC_IR2, LC_IDZ, LC_N };
+// LC_SPG / LF_SPG: the sponge shape s(z) (beta = alpha s(z)), for the sponge-rate derivative.
+enum LevC { LC_Z = 0, LC_R2, LC_DZ, LC_PHI, LC_BETA, LC_IR2, LC_IDZ, LC_SPG, LC_N };
 // Per-level face quantities ([q][Nv+1]).
-enum LevF { LF_Z = 0, LF_R2, LF_DZ, LF_RINV, LF_BETA, LF_DPHI, LF_IR2, LF_IDZ, LF_G33, LF_N };
+enum LevF { LF_Z = 0, LF_R2, LF_DZ, LF_RINV, LF_BETA, LF_DPHI, LF_IR2, LF_IDZ, LF_G33, LF_SPG, LF_N };
 
 struct HostGeometry {
   int h = 0, Nh = 0, Nv = 0;

@@ -77,6 +77,15 @@ struct StageArgs {
   int first;        // 1: overwrite rnorm, 0: accumulate
 };
 
+// Cotangents of the tendencies a transposed stage combination accumulates into.
+template <class FT>
+struct CotArgs {
+  FT *te_c[4], *te_f[4];
+  FT *ti_c[4], *ti_f[4];
+  FT ce[4], ci[4];
+  int nsrc;
+};
+
 enum ColMode { COL_STAGE = 0, COL_IMPLICIT = 1, COL_JACOBIAN = 2, COL_LDIV = 3, COL_POSTIMP = 4 };
 constexpr int JAC_Q = 15;  // stored Jacobian quantities per level
 
@@ -91,9 +100,21 @@ struct ColArgs {
 template <class FT> void launch_passA(const DevParams<FT> &P, const FT *Yc, const FT *Yf, FT *L, cudaStream_t s);
 template <class FT> void launch_passB(const DevParams<FT> &P, const FT *Yc, const FT *Yf, const FT *L, FT *Tc, FT *Tf, cudaStream_t s);
 template <class FT> void launch_dss(const DevParams<FT> &P, FT *C, FT *F, cudaStream_t s);
+template <class FT> void launch_dss_transpose(const DevParams<FT> &P, FT *C, FT *F, cudaStream_t s);
 template <class FT> void launch_column_stage(const DevParams<FT> &P, const StageArgs<FT> &A, cudaStream_t s);
 template <class FT> void launch_column(const DevParams<FT> &P, int mode, const ColArgs<FT> &A, cudaStream_t s);
 template <class FT> void launch_final(const DevParams<FT> &P, const StageArgs<FT> &A, FT *Yc, FT *Yf, cudaStream_t s);
+// ---- reverse (adjoint) kernels
+template <class FT> void launch_final_transpose(const DevParams<FT> &P, const CotArgs<FT> &A, FT *Ybc, FT *Ybf, cudaStream_t s);
+template <class FT> void launch_axpy(size_t n, FT a, const FT *x, FT *y, cudaStream_t s);
+void launch_accum(const double *part, int n, int stride, int nout, double *acc, cudaStream_t s);
+template <class FT> size_t passA_vjp_smem(int Nv);
+template <class FT> size_t passB_vjp_smem(int Nv);
+template <class FT> void configure_adjoint_se(int Nv);
+template <class FT> void launch_passA_vjp(const DevParams<FT> &P, const FT *Yc, const FT *Yf, const FT *Lb, FT *Ybc, FT *Ybf, int grid, cudaStream_t s);
+template <class FT> void launch_passB_vjp(const DevParams<FT> &P, const FT *Yc, const FT *Yf, const FT *L, const FT *Tbc, const FT *Tbf, FT *Ybc, FT *Ybf, FT *Lb, double *dpar, int grid, cudaStream_t s);
+size_t col_vjp_scratch_words(int Nh, int Nv);
+template <class FT> void launch_column_stage_vjp(const DevParams<FT> &P, const StageArgs<FT> &A, const FT *Ub_c, const FT *Ub_f, const FT *Tb_c, const FT *Tb_f, FT *Yb_c, FT *Yb_f, FT *const Teb[4], FT *const Tib[4], size_t NC, size_t NR, FT *scr, double *dalpha, cudaStream_t s);
 template <class FT> void launch_bc_filter(const DevParams<FT> &P, FT *Yf, cudaStream_t s);
 template <class FT> void launch_global_sums(const DevParams<FT> &P, const FT *Yc, double *partials, int nblocks, double *out, cudaStream_t s);
 void launch_reduce_rnorm(const double *rnorm, int ncols, double *out, cudaStream_t s);

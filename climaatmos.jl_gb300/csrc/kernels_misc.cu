@@ -58,6 +58,54 @@ __global__ void __launch_bounds__(DSS_THREADS) k_dss(DevParams<FT> P, FT *__rest
   }
 }
 
+// Transpose of k_dss (the reverse pass of the DSS projection).  The forward
+// map gives every copy c of a group out_c = sum_k w_k in_k (vectors: the
+// covariant basis of c applied to sum_k w_k (contravariant basis of k . u_k)),
+// so its transpose gives every copy k in_k = w_k sum_c out_c (vectors: w_k
+// times the contravariant basis of k applied to sum_c (covariant basis of c
+// . u_c)).  Same group order and summation order as k_dss.
+template <class FT>
+__global__ void __launch_bounds__(DSS_THREADS) k_dss_t(DevParams<FT> P, FT *__restrict__ C, FT *__restrict__ F) {
+  const int lane = threadIdx.x & 31;
+  const int g = blockIdx.x * (DSS_THREADS / 32) + (threadIdx.x >> 5);
+  if (g >= P.ngroups) return;
+  const int Nv = P.Nv, Nf = P.Nf;
+  const int o0 = P.goff[g], o1 = P.goff[g + 1];
+  if (C) {
+    for (int v = lane; v < Nv; v += 32) {
+      FT s0 = 0, s3 = 0, X0 = 0, X1 = 0, X2 = 0;
+      for (int c = o0; c < o1; ++c) {
+        const int idx = P.gcopy[c], e = idx >> 4, n = idx & 15;
+        const size_t b = ((size_t)e * 4 * NN + n) * Nv + v;
+        s0 += C[b];
+        s3 += C[b + 48 * Nv];
+        const FT u1 = C[b + 16 * Nv], u2 = C[b + 32 * Nv];
+        const FT *eo = P.ecov + (size_t)idx * 6;
+        X0 += u1 * eo[0] + u2 * eo[3];
+        X1 += u1 * eo[1] + u2 * eo[4];
+        X2 += u1 * eo[2] + u2 * eo[5];
+      }
+      for (int c = o0; c < o1; ++c) {
+        const int idx = P.gcopy[c], e = idx >> 4, n = idx & 15;
+        const size_t b = ((size_t)e * 4 * NN + n) * Nv + v;
+        const FT w = P.gw[c];
+        const FT *ec = P.econ + (size_t)idx * 6;
+        C[b] = w * s0;
+        C[b + 48 * Nv] = w * s3;
+        C[b + 16 * Nv] = w * (ec[0] * X0 + ec[1] * X1 + ec[2] * X2);
+        C[b + 32 * Nv] = w * (ec[3] * X0 + ec[4] * X1 + ec[5] * X2);
+      }
+    }
+  }
+  if (F) {
+    for (int k = lane; k < Nf; k += 32) {
+      FT s = 0;
+      for (int c = o0; c < o1; ++c) s += F[(size_t)P.gcopy[c] * Nf + k];
+      for (int c = o0; c < o1; ++c) F[(size_t)P.gcopy[c] * Nf + k] = P.gw[c] * s;
+    }
+  }
+}
+
 // u_{n+1} = u_n + dt sum_j (b~_j T_exp_j + b_j T_imp_j), then the impenetrable filter.
 template <class FT>
 __global__ void k_final(DevParams<FT> P, StageArgs<FT> A, FT *__restrict__ Yc, FT *__restrict__ Yf) {
@@ -85,6 +133,60 @@ __global__ void k_final(DevParams<FT> P, StageArgs<FT> A, FT *__restrict__ Yc, F
       }
       Yf[r] = (k == 0 || k == Nv) ? FT(0) : s;
     }
+  }
+}
+
+// Transpose of k_final: the filter zeroes the boundary-face cotangent of
+// u_{n+1}; u_n receives it unchanged and every tendency j its coefficient
+// times it (A.te_c/te_f/ti_c/ti_f point at the tendency cotangents).
+template <class FT>
+__global__ void k_final_t(DevParams<FT> P, CotArgs<FT> A, FT *__restrict__ Ybc, FT *__restrict__ Ybf) {
+  const int Nv = P.Nv, Nf = P.Nf;
+  const size_t NC = (size_t)P.Nh * 4 * NN * Nv, NF = (size_t)P.Nh * NN * Nf;
+  for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < NC + NF; q += (size_t)gridDim.x * blockDim.x) {
+    if (q < NC) {
+      const size_t row = q / Nv;
+      const int v = (int)(q - row * Nv);
+      const int n = (int)(row % NN), c = (int)((row / NN) % 4);
+      const size_t e = row / (4 * NN);
+      const FT yb = Ybc[q];
+      for (int j = 0; j < A.nsrc; ++j) {
+        if (A.te_c[j]) A.te_c[j][q] += A.ce[j] * yb;
+        if (A.ti_c[j] && (c == 0 || c == 3)) A.ti_c[j][((e * 2 + (c == 3)) * NN + n) * Nv + v] += A.ci[j] * yb;
+      }
+    } else {
+      const size_t r = q - NC;
+      const int k = (int)(r % Nf);
+      const FT yb = (k == 0 || k == Nv) ? FT(0) : Ybf[r];
+      Ybf[r] = yb;
+      for (int j = 0; j < A.nsrc; ++j) {
+        if (A.te_f[j]) A.te_f[j][r] += A.ce[j] * yb;
+        if (A.ti_f[j]) A.ti_f[j][r] += A.ci[j] * yb;
+      }
+    }
+  }
+}
+
+template <class FT>
+__global__ void k_axpy(size_t n, FT a, const FT *__restrict__ x, FT *__restrict__ y) {
+  for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x)
+    y[q] += a * x[q];
+}
+
+// acc[o] += sum_i part[i * stride + o] for o < nout, in a fixed order (one block).
+__global__ void k_accum(const double *__restrict__ part, int n, int stride, int nout, double *__restrict__ acc) {
+  __shared__ double sh[256];
+  for (int o = 0; o < nout; ++o) {
+    double s = 0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) s += part[(size_t)i * stride + o];
+    sh[threadIdx.x] = s;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+      if ((int)threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) acc[o] += sh[0];
+    __syncthreads();
   }
 }
 
@@ -171,8 +273,24 @@ void launch_dss(const DevParams<FT> &P, FT *C, FT *F, cudaStream_t s) {
   if (grid > 0) k_dss<FT><<<grid, DSS_THREADS, 0, s>>>(P, C, F);
 }
 template <class FT>
+void launch_dss_transpose(const DevParams<FT> &P, FT *C, FT *F, cudaStream_t s) {
+  const int grid = (P.ngroups + DSS_THREADS / 32 - 1) / (DSS_THREADS / 32);
+  if (grid > 0) k_dss_t<FT><<<grid, DSS_THREADS, 0, s>>>(P, C, F);
+}
+template <class FT>
 void launch_final(const DevParams<FT> &P, const StageArgs<FT> &A, FT *Yc, FT *Yf, cudaStream_t s) {
   k_final<FT><<<152 * 8, 256, 0, s>>>(P, A, Yc, Yf);
+}
+template <class FT>
+void launch_final_transpose(const DevParams<FT> &P, const CotArgs<FT> &A, FT *Ybc, FT *Ybf, cudaStream_t s) {
+  k_final_t<FT><<<152 * 8, 256, 0, s>>>(P, A, Ybc, Ybf);
+}
+template <class FT>
+void launch_axpy(size_t n, FT a, const FT *x, FT *y, cudaStream_t s) {
+  k_axpy<FT><<<152 * 8, 256, 0, s>>>(n, a, x, y);
+}
+void launch_accum(const double *part, int n, int stride, int nout, double *acc, cudaStream_t s) {
+  k_accum<<<1, 256, 0, s>>>(part, n, stride, nout, acc);
 }
 template <class FT>
 void launch_bc_filter(const DevParams<FT> &P, FT *Yf, cudaStream_t s) {
@@ -190,7 +308,10 @@ void launch_reduce_rnorm(const double *rnorm, int ncols, double *out, cudaStream
 
 #define INST(FT)                                                                                          \
   template void launch_dss<FT>(const DevParams<FT> &, FT *, FT *, cudaStream_t);                          \
+  template void launch_dss_transpose<FT>(const DevParams<FT> &, FT *, FT *, cudaStream_t);                \
   template void launch_final<FT>(const DevParams<FT> &, const StageArgs<FT> &, FT *, FT *, cudaStream_t); \
+  template void launch_final_transpose<FT>(const DevParams<FT> &, const CotArgs<FT> &, FT *, FT *, cudaStream_t); \
+  template void launch_axpy<FT>(size_t, FT, const FT *, FT *, cudaStream_t);                               \
   template void launch_bc_filter<FT>(const DevParams<FT> &, FT *, cudaStream_t);                          \
   template void launch_global_sums<FT>(const DevParams<FT> &, const FT *, double *, int, double *, cudaStream_t);
 INST(float)

@@ -1,0 +1,296 @@
+// Element-slab spectral-element operators shared by the forward slab kernels
+// and their reverse (adjoint) kernels.
+//
+// Thread mapping: one thread per (level, row j), holding the four nodes
+// n = 4 j + i of that row; xi^1 derivatives are register-local 4x4 products,
+// xi^2 derivatives gather the other rows with shuffles inside the level's
+// 4-lane group.  The transposes pair up: d1^T = t1 and d2^T = t2.
+#pragma once
+#include "kernels.cuh"
+
+namespace gb {
+namespace se {
+
+// Row helper: the thread's row j and its xi^2 derivative coefficients.
+template <class FT>
+struct Row {
+  int j;
+  FT dB[NQ], tB[NQ];  // D[j][k], D[k][j]
+  __device__ void init(const DevParams<FT> &P, int jj) {
+    j = jj;
+#pragma unroll
+    for (int k = 0; k < NQ; ++k) {
+      dB[k] = P.D[j * NQ + k];
+      tB[k] = P.D[k * NQ + j];
+    }
+  }
+};
+
+// o[i] = sum_k D[i][k] f[k]   (d/dxi^1, register-local)
+template <class FT>
+__device__ __forceinline__ void d1(const DevParams<FT> &P, const FT (&f)[4], FT (&o)[4]) {
+#pragma unroll
+  for (int i = 0; i < NQ; ++i) {
+    FT s = 0;
+#pragma unroll
+    for (int k = 0; k < NQ; ++k) s += P.D[i * NQ + k] * f[k];
+    o[i] = s;
+  }
+}
+// o[i] = sum_k D[k][i] f[k]   (transpose: weak forms)
+template <class FT>
+__device__ __forceinline__ void t1(const DevParams<FT> &P, const FT (&f)[4], FT (&o)[4]) {
+#pragma unroll
+  for (int i = 0; i < NQ; ++i) {
+    FT s = 0;
+#pragma unroll
+    for (int k = 0; k < NQ; ++k) s += P.D[k * NQ + i] * f[k];
+    o[i] = s;
+  }
+}
+// o[i] = sum_k C[k] f(i, row k): the rows are gathered from the level's 4-lane group
+template <class FT>
+__device__ __forceinline__ void across(const FT (&C)[NQ], const FT (&f)[4], FT (&o)[4]) {
+#pragma unroll
+  for (int i = 0; i < NQ; ++i) {
+    FT s = 0;
+#pragma unroll
+    for (int k = 0; k < NQ; ++k) s += C[k] * shfl(f[i], k, 4);
+    o[i] = s;
+  }
+}
+template <class FT>
+__device__ __forceinline__ void d2(const Row<FT> &R, const FT (&f)[4], FT (&o)[4]) { across(R.dB, f, o); }
+template <class FT>
+__device__ __forceinline__ void t2(const Row<FT> &R, const FT (&f)[4], FT (&o)[4]) { across(R.tB, f, o); }
+
+// Per-node horizontal geometry of the thread's row (loaded once per element).
+template <class FT>
+struct RowGeo {
+  FT Jh[4], iJh[4], gu0[4], gu1[4], gu2[4], gd0[4], gd1[4], gd2[4], W[4], iW[4];
+  __device__ void load(const FT *sG, const DevParams<FT> &P, int j) {
+#pragma unroll
+    for (int i = 0; i < NQ; ++i) {
+      const int n = NQ * j + i;
+      Jh[i] = sG[HG_JH * NN + n];
+      iJh[i] = sG[HG_IJH * NN + n];
+      gu0[i] = sG[HG_GU0 * NN + n];
+      gu1[i] = sG[HG_GU1 * NN + n];
+      gu2[i] = sG[HG_GU2 * NN + n];
+      gd0[i] = sG[HG_GD0 * NN + n];
+      gd1[i] = sG[HG_GD1 * NN + n];
+      gd2[i] = sG[HG_GD2 * NN + n];
+      W[i] = P.W[n];
+      iW[i] = P.iW[n];
+    }
+  }
+};
+
+// Geometry of the row at one level (deep-atmosphere scaling r^2, layer thickness dz).
+template <class FT>
+struct LevRow {
+  FT J[4], iJ[4], WJ[4], iWJ[4];
+  FT ir2, r2, G33;
+  __device__ void set(const RowGeo<FT> &g, FT r2_, FT ir2_, FT dz, FT idz) {
+    r2 = r2_;
+    ir2 = ir2_;
+    G33 = dz * dz;
+#pragma unroll
+    for (int i = 0; i < NQ; ++i) {
+      J[i] = g.Jh[i] * r2 * dz;
+      iJ[i] = g.iJh[i] * ir2 * idz;
+      WJ[i] = g.W[i] * J[i];
+      iWJ[i] = g.iW[i] * iJ[i];
+    }
+  }
+};
+
+// C123(wgrad(div u)) * fdiv - C123(wcurl(C123(curl u))) for covariant (c1, c2, c3)
+template <class FT>
+__device__ __forceinline__ void vec_lap(const DevParams<FT> &P, const Row<FT> &R, const RowGeo<FT> &g,
+                                        const LevRow<FT> &s, const FT (&c1)[4], const FT (&c2)[4],
+                                        const FT (&c3)[4], FT fdiv, FT (&o1)[4], FT (&o2)[4], FT (&o3)[4]) {
+  FT a[4], b[4], da[4], db[4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const FT gu0 = g.gu0[i] * s.ir2, gu1 = g.gu1[i] * s.ir2, gu2 = g.gu2[i] * s.ir2;
+    a[i] = s.J[i] * (gu0 * c1[i] + gu1 * c2[i]);
+    b[i] = s.J[i] * (gu1 * c1[i] + gu2 * c2[i]);
+  }
+  d1(P, a, da);
+  d2(R, b, db);
+  FT wdv[4], w1[4], w2[4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) wdv[i] = g.W[i] * ((da[i] + db[i]) * s.iJ[i]);
+  t1(P, wdv, w1);
+  t2(R, wdv, w2);
+  FT e1[4], e2[4], e3[4], e4[4];
+  d1(P, c2, e1);
+  d2(R, c1, e2);
+  d2(R, c3, e3);
+  d1(P, c3, e4);
+  FT Wz1[4], Wz2[4], Wz3[4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const FT k3 = (e1[i] - e2[i]) * s.iJ[i];
+    const FT k1 = e3[i] * s.iJ[i], k2 = -e4[i] * s.iJ[i];
+    const FT gd0 = g.gd0[i] * s.r2, gd1 = g.gd1[i] * s.r2, gd2 = g.gd2[i] * s.r2;
+    Wz1[i] = g.W[i] * (gd0 * k1 + gd1 * k2);
+    Wz2[i] = g.W[i] * (gd1 * k1 + gd2 * k2);
+    Wz3[i] = g.W[i] * (s.G33 * k3);
+  }
+  FT f1[4], f2[4], f3[4], f4[4];
+  t1(P, Wz2, f1);
+  t2(R, Wz1, f2);
+  t2(R, Wz3, f3);
+  t1(P, Wz3, f4);
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const FT q3 = (-f1[i] + f2[i]) * s.iWJ[i];
+    const FT q1 = -f3[i] * s.iWJ[i], q2 = f4[i] * s.iWJ[i];
+    const FT gd0 = g.gd0[i] * s.r2, gd1 = g.gd1[i] * s.r2, gd2 = g.gd2[i] * s.r2;
+    o1[i] = fdiv * (-w1[i] * g.iW[i]) - (gd0 * q1 + gd1 * q2);
+    o2[i] = fdiv * (-w2[i] * g.iW[i]) - (gd1 * q1 + gd2 * q2);
+    o3[i] = -s.G33 * q3;
+  }
+}
+
+// weak divergence -(1/WJ) (D^T (WJ F1) along xi^1 + along xi^2)
+template <class FT>
+__device__ __forceinline__ void wdiv(const DevParams<FT> &P, const Row<FT> &R, const LevRow<FT> &s,
+                                     const FT (&F1)[4], const FT (&F2)[4], FT (&o)[4]) {
+  FT a[4], b[4], ta[4], tb[4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    a[i] = s.WJ[i] * F1[i];
+    b[i] = s.WJ[i] * F2[i];
+  }
+  t1(P, a, ta);
+  t2(R, b, tb);
+#pragma unroll
+  for (int i = 0; i < 4; ++i) o[i] = -(ta[i] + tb[i]) * s.iWJ[i];
+}
+
+// u_bar_3 = I^c(u_3) and the face part of K, I^c(u_3 u^3), with the
+// impenetrable filter (u_3 = 0 on the boundary faces); level-fastest mapping.
+template <class FT>
+__device__ __forceinline__ void centre_from_faces(const DevParams<FT> &P, const FT *sF, FT *sU3, FT *sKv) {
+  const int Nv = P.Nv, Nf = P.Nf;
+  for (int idx = threadIdx.x; idx < NN * Nv; idx += blockDim.x) {
+    const int n = idx / Nv, v = idx - n * Nv;
+    const FT a = v == 0 ? FT(0) : sF[n * Nf + v];
+    const FT b = v + 1 == Nv ? FT(0) : sF[n * Nf + v + 1];
+    const FT ua = a * P.levf[LF_G33 * Nf + v], ub = b * P.levf[LF_G33 * Nf + v + 1];
+    if (sU3) sU3[idx] = (a + b) / FT(2);
+    sKv[idx] = (a * ua + b * ub) / FT(2);
+  }
+}
+
+
+// ---------------------------------------------------------------- reverse (adjoint) forms
+// Transpose of vec_lap: given the cotangents (ob1, ob2, ob3) of (o1, o2, o3),
+// returns the cotangents (cb1, cb2, cb3) of (c1, c2, c3).  The forward sequence
+// run backwards, with d1 <-> t1 and d2 <-> t2.
+template <class FT>
+__device__ __forceinline__ void vec_lap_t(const DevParams<FT> &P, const Row<FT> &R, const RowGeo<FT> &g,
+                                          const LevRow<FT> &s, const FT (&ob1)[4], const FT (&ob2)[4],
+                                          const FT (&ob3)[4], FT fdiv, FT (&cb1)[4], FT (&cb2)[4], FT (&cb3)[4]) {
+  FT f1b[4], f2b[4], f3b[4], f4b[4], w1b[4], w2b[4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const FT gd0 = g.gd0[i] * s.r2, gd1 = g.gd1[i] * s.r2, gd2 = g.gd2[i] * s.r2;
+    const FT q1b = -(gd0 * ob1[i] + gd1 * ob2[i]), q2b = -(gd1 * ob1[i] + gd2 * ob2[i]);
+    const FT q3b = -s.G33 * ob3[i];
+    w1b[i] = -fdiv * g.iW[i] * ob1[i];
+    w2b[i] = -fdiv * g.iW[i] * ob2[i];
+    f1b[i] = -q3b * s.iWJ[i];
+    f2b[i] = q3b * s.iWJ[i];
+    f3b[i] = -q1b * s.iWJ[i];
+    f4b[i] = q2b * s.iWJ[i];
+  }
+  FT Wz1b[4], Wz2b[4], Wz3b[4], tmp[4];
+  d1(P, f1b, Wz2b);
+  d2(R, f2b, Wz1b);
+  d2(R, f3b, Wz3b);
+  d1(P, f4b, tmp);
+  FT e1b[4], e2b[4], e3b[4], e4b[4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    Wz3b[i] += tmp[i];
+    const FT gd0 = g.gd0[i] * s.r2, gd1 = g.gd1[i] * s.r2, gd2 = g.gd2[i] * s.r2;
+    const FT k1b = g.W[i] * (gd0 * Wz1b[i] + gd1 * Wz2b[i]);
+    const FT k2b = g.W[i] * (gd1 * Wz1b[i] + gd2 * Wz2b[i]);
+    const FT k3b = g.W[i] * (s.G33 * Wz3b[i]);
+    e1b[i] = k3b * s.iJ[i];
+    e2b[i] = -k3b * s.iJ[i];
+    e3b[i] = k1b * s.iJ[i];
+    e4b[i] = -k2b * s.iJ[i];
+  }
+  t1(P, e1b, cb2);
+  t2(R, e2b, cb1);
+  t2(R, e3b, cb3);
+  t1(P, e4b, tmp);
+  FT wdvb[4], t2b[4];
+  d1(P, w1b, wdvb);
+  d2(R, w2b, t2b);
+  FT dab[4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    cb3[i] += tmp[i];
+    dab[i] = g.W[i] * s.iJ[i] * (wdvb[i] + t2b[i]);
+  }
+  FT ab[4], bb[4];
+  t1(P, dab, ab);
+  t2(R, dab, bb);
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const FT gu0 = g.gu0[i] * s.ir2, gu1 = g.gu1[i] * s.ir2, gu2 = g.gu2[i] * s.ir2;
+    cb1[i] += s.J[i] * (gu0 * ab[i] + gu1 * bb[i]);
+    cb2[i] += s.J[i] * (gu1 * ab[i] + gu2 * bb[i]);
+  }
+}
+
+// Transpose of wdiv: cotangents (Fb1, Fb2) of (F1, F2) from the cotangent ob of o.
+template <class FT>
+__device__ __forceinline__ void wdiv_t(const DevParams<FT> &P, const Row<FT> &R, const LevRow<FT> &s,
+                                       const FT (&ob)[4], FT (&Fb1)[4], FT (&Fb2)[4]) {
+  FT tb[4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) tb[i] = -ob[i] * s.iWJ[i];
+  d1(P, tb, Fb1);
+  d2(R, tb, Fb2);
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    Fb1[i] *= s.WJ[i];
+    Fb2[i] *= s.WJ[i];
+  }
+}
+
+// Transpose of the gradient (d1 f, d2 f): fb = t1(gb1) + t2(gb2).
+template <class FT>
+__device__ __forceinline__ void grad_t(const DevParams<FT> &P, const Row<FT> &R, const FT (&gb1)[4],
+                                       const FT (&gb2)[4], FT (&fb)[4]) {
+  FT a[4];
+  t1(P, gb1, fb);
+  t2(R, gb2, a);
+#pragma unroll
+  for (int i = 0; i < 4; ++i) fb[i] += a[i];
+}
+
+// Transpose of the scalar Laplacian Ls = wdiv(g^-1 grad sd) (with the row's g^ij / r^2).
+template <class FT>
+__device__ __forceinline__ void lap_t(const DevParams<FT> &P, const Row<FT> &R, const RowGeo<FT> &g,
+                                      const LevRow<FT> &s, const FT (&Lb)[4], FT (&sdb)[4]) {
+  FT xb1[4], xb2[4], gb1[4], gb2[4];
+  wdiv_t(P, R, s, Lb, xb1, xb2);
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const FT gu0 = g.gu0[i] * s.ir2, gu1 = g.gu1[i] * s.ir2, gu2 = g.gu2[i] * s.ir2;
+    gb1[i] = gu0 * xb1[i] + gu1 * xb2[i];
+    gb2[i] = gu1 * xb1[i] + gu2 * xb2[i];
+  }
+  grad_t(P, R, gb1, gb2, sdb);
+}
+
+}  // namespace se
+}  // namespace gb

@@ -21,6 +21,8 @@ SYMBOLS = [
     "gb_set_precomputed_quantities", "gb_remaining_tendency", "gb_implicit_tendency", "gb_update_jacobian",
     "gb_ldiv", "gb_correct_implicit_advection_tendency", "gb_dss", "gb_step", "gb_global_sums",
     "gb_newton_residual", "gb_time_kernel", "gb_jacobian_solve_noalloc",
+    "gb_dss_transpose", "gb_remaining_tendency_vjp", "gb_implicit_stage", "gb_implicit_stage_vjp", "gb_step_vjp",
+    "gb_adjoint_forward", "gb_adjoint_reverse",
     "gb_columns_create", "gb_columns_destroy", "gb_columns_set_stream", "gb_columns_size", "gb_columns_solve",
     "gb_columns_autotune", "gb_columns_set_variant", "gb_columns_last_error",
 ]
@@ -94,6 +96,13 @@ def load(build_if_missing=True):
     L.gb_newton_residual.argtypes = [_vp, _dp]
     L.gb_time_kernel.argtypes = [_vp, _c_int, fv, _c_int, _dp]
     L.gb_jacobian_solve_noalloc.argtypes = [_vp, fv, fv, fv, _c_double]
+    L.gb_dss_transpose.argtypes = [_vp, fv]
+    L.gb_remaining_tendency_vjp.argtypes = [_vp, fv, fv, fv, _c_double, _dp]
+    L.gb_implicit_stage.argtypes = [_vp, fv, fv, fv, _c_double]
+    L.gb_implicit_stage_vjp.argtypes = [_vp, fv, fv, fv, fv, _c_double, _dp]
+    L.gb_step_vjp.argtypes = [_vp, fv, fv, _c_double, _c_double, _dp]
+    L.gb_adjoint_forward.argtypes = [_vp, fv, _c_double, _c_double, _c_int, _c_int]
+    L.gb_adjoint_reverse.argtypes = [_vp, fv, _dp, ctypes.POINTER(ctypes.c_size_t)]
     _llp = ctypes.POINTER(ctypes.c_longlong)
     L.gb_columns_create.argtypes = [cfgp, _c_int, _ip, ctypes.POINTER(_vp)]
     L.gb_columns_destroy.argtypes = [_vp]

@@ -282,3 +282,60 @@ def solve_atmos(sim, nsteps, use_graph=True):
     sps = wall / max(nsteps, 1)
     return {"walltime": wall, "seconds_per_step": sps, "sypd": simulated_years_per_day(sim.dt, sps),
             "ret_code": "success"}
+
+
+# ---------------------------------------------------------------- reverse mode
+# Every *_vjp accumulates into its cotangent arguments; each returns the
+# (d/dnu, d/d sponge rate) contributions as a length-2 array.
+def _dpar():
+    return (ctypes.c_double * 2)(0.0, 0.0)
+
+
+def dss_transpose(X, p):
+    p.call("gb_dss_transpose", X.gb())
+
+
+def remaining_tendency_vjp(Ybar, Tbar, Y, p, t=0.0):
+    d = _dpar()
+    p.call("gb_remaining_tendency_vjp", Ybar.gb(), Tbar.gb(), Y.gb(), float(t), d)
+    return np.array(d[:])
+
+
+def reduced_like(Y):
+    """A zero implicit-tendency FieldVector: c [Nh, 2, 16, Nv] (rho, rho e_tot), f like Y.f."""
+    import torch
+    Nh, _, nn, Nv = Y.c.shape
+    return FieldVector(torch.zeros((Nh, 2, nn, Nv), dtype=Y.c.dtype, device=Y.c.device), torch.zeros_like(Y.f))
+
+
+def implicit_stage(U, Timp, Uhat, p, dtgamma):
+    p.call("gb_implicit_stage", U.gb(), Timp.gb(), Uhat.gb(), float(dtgamma))
+
+
+def implicit_stage_vjp(Uhat_bar, Ubar, Timp_bar, Uhat, p, dtgamma):
+    d = _dpar()
+    p.call("gb_implicit_stage_vjp", Uhat_bar.gb(), Ubar.gb(), Timp_bar.gb(), Uhat.gb(), float(dtgamma), d)
+    return np.array(d[:])
+
+
+def step_vjp(Ybar, Y, p, t, dt):
+    d = _dpar()
+    p.call("gb_step_vjp", Ybar.gb(), Y.gb(), float(t), float(dt), d)
+    return np.array(d[:])
+
+
+def gradient(p, Y0, nsteps, loss_and_grad, dt=None, checkpoint_every=5):
+    """Reverse-mode gradient of a loss of the state after ``nsteps`` steps from Y0.
+
+    The rrule pattern (ChainRulesCore.rrule of the solve): the forward half
+    advances a copy of Y0 keeping a checkpoint every ``checkpoint_every``
+    steps; ``loss_and_grad(Y_N) -> (J, dJ/dY_N FieldVector)``; the pullback
+    returns (J, dJ/dY0, dJ/dnu, dJ/d sponge rate, library bytes at the peak)."""
+    dt = p.dt if dt is None else dt
+    Y = Y0.copy()
+    p.call("gb_adjoint_forward", Y.gb(), 0.0, float(dt), int(nsteps), int(checkpoint_every))
+    J, Ybar = loss_and_grad(Y)
+    d = _dpar()
+    peak = ctypes.c_size_t(0)
+    p.call("gb_adjoint_reverse", Ybar.gb(), d, ctypes.byref(peak))
+    return J, Ybar, float(d[0]), float(d[1]), int(peak.value)

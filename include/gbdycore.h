@@ -152,6 +152,49 @@ enum gb_kernel_id { GB_K_PASSA = 0, GB_K_PASSB = 1, GB_K_COLUMN = 2, GB_K_DSS = 
 int gb_time_kernel(gb_ctx *ctx, int kernel, gb_fieldvec Y, int reps, double *ms_per_launch);
 
 /* ---------------------------------------------------------------------------
+ * Reverse mode (adjoint) of the step, for gradients with respect to the state
+ * and to two scalars: nu (nu_4_vorticity, with nu_4_scalar = nu / Prandtl
+ * following it) and the Rayleigh sponge rate alpha (alpha_uh = alpha_w =
+ * alpha, beta(z) = alpha s(z) above sponge_zd).  The reference exposes its
+ * differentiable step to Julia AD through ChainRulesCore; these entries are
+ * the forward and pullback halves of that rrule (the Julia shim defines
+ * ChainRulesCore.rrule(solve!, ...) on gb_adjoint_forward /
+ * gb_adjoint_reverse).  Every *_vjp entry ACCUMULATES into its cotangent
+ * outputs (+=) and into dparams[0] (d/dnu) and dparams[1] (d/dalpha); each
+ * is the exact reverse of the corresponding forward computation in this
+ * library.  Synchronous.  The reverse slab kernels keep an element's state,
+ * Laplacians and tendency cotangent in shared memory: FP64 contexts support
+ * z_elem up to ~50, FP32 up to 127 (else GB_ERR_ARG).
+ * ------------------------------------------------------------------------- */
+
+/* Transpose of gb_dss (in place). */
+int gb_dss_transpose(gb_ctx *ctx, gb_fieldvec X);
+/* Reverse of gb_remaining_tendency: Ybar += (dT/dY)^T Tbar (Tbar is not modified). */
+int gb_remaining_tendency_vjp(gb_ctx *ctx, gb_fieldvec Ybar, gb_fieldvec Tbar, gb_fieldvec Y, double t,
+                              double dparams[2]);
+/* One fused implicit stage on a given U^: one Newton iteration of the stage
+ * equation, the impenetrable filter and the van Leer post-Newton correction
+ * (as inside gb_step); writes U and T_imp = (U - U^)/dtgamma, the latter in
+ * the reduced layout c: [Nh][2][16][Nv] (rho, rho e_tot), f: faces. */
+int gb_implicit_stage(gb_ctx *ctx, gb_fieldvec U, gb_fieldvec Timp, gb_fieldvec Uhat, double dtgamma);
+/* Reverse of gb_implicit_stage, including the dependence of the Jacobian on
+ * the state: Uhat_bar += (dU/dU^)^T Ubar + (dT_imp/dU^)^T Timp_bar. */
+int gb_implicit_stage_vjp(gb_ctx *ctx, gb_fieldvec Uhat_bar, gb_fieldvec Ubar, gb_fieldvec Timp_bar, gb_fieldvec Uhat,
+                          double dtgamma, double dparams[2]);
+/* Reverse of one gb_step from u_n = Y (not modified): Ybar holds the cotangent
+ * of u_{n+1} on entry and that of u_n on return. */
+int gb_step_vjp(gb_ctx *ctx, gb_fieldvec Ybar, gb_fieldvec Y, double t, double dt, double dparams[2]);
+/* Forward half of the trajectory gradient: Y advances nsteps steps (as
+ * gb_step) and a copy of the state is kept every checkpoint_every steps. */
+int gb_adjoint_forward(gb_ctx *ctx, gb_fieldvec Y, double t0, double dt, int nsteps, int checkpoint_every);
+/* Pullback of the last gb_adjoint_forward: Ybar holds dJ/du_N on entry and
+ * dJ/du_0 on return; dparams receives (dJ/dnu, dJ/dalpha) (overwritten).
+ * Each segment between checkpoints is recomputed from its checkpoint with its
+ * stage data kept, then reversed.  peak_bytes (may be NULL) receives the
+ * device bytes the library held during the pass. */
+int gb_adjoint_reverse(gb_ctx *ctx, gb_fieldvec Ybar, double dparams[2], size_t *peak_bytes);
+
+/* ---------------------------------------------------------------------------
  * Batched standalone columns of uneven height.
  *
  * A batch of independent dry columns, each a ColumnGrid of its own z_elem

@@ -48,6 +48,11 @@ def parse():
     ap.add_argument("--batch-columns", type=int, default=20000)
     ap.add_argument("--batch-reps", type=int, default=10)
     ap.add_argument("--no-batching", action="store_true")
+    ap.add_argument("--adjoint-steps", type=int, default=10)
+    ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--fd-directions", type=int, default=32)
+    ap.add_argument("--no-differentiation", action="store_true")
+    ap.add_argument("--no-h60", action="store_true")
     return ap.parse_args()
 
 
@@ -310,17 +315,25 @@ def run_gb300(args):
         s64.step(n)
         s32.step(n)
         a, b = s32.Y.numpy(), s64.Y.numpy()
-        names = ["rho", "u_1", "u_2", "rho_e_tot"]
         prec = {"steps": n}
-        for c in range(4):
-            prec[names[c]] = float(np.abs(a[0][:, c] - b[0][:, c]).max() / np.abs(b[0][:, c]).max())
-        prec["u_3"] = float(np.abs(a[1] - b[1]).max() / max(np.abs(b[1]).max(), 1e-300))
-        prec["norm"] = "max |FP32 - FP64| / max |FP64| per field"
+        prec.update(field_errors(a, b))
         del s64, s32
 
     batching = None
     if not args.no_batching:
         batching = measure_batching(args)
+
+    adjoint = None
+    if not args.no_adjoint:
+        adjoint = measure_adjoint(args, s, ms)
+    differentiation = None
+    if not args.no_differentiation:
+        differentiation = measure_differentiation(args)
+    h60 = None
+    if not args.no_h60:
+        del s
+        torch.cuda.empty_cache()
+        h60 = measure_precision_h60(args)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -341,7 +354,8 @@ def run_gb300(args):
                     "chosen_over_plain": plain_ms / ms,
                     "what": "same step through the individual hooks (remaining/implicit tendency, Jacobian, ldiv, "
                             "post-Newton correction, DSS) with unfused torch stage algebra"},
-                "fp32_vs_fp64": prec, "batching": batching,
+                "fp32_vs_fp64": prec, "batching": batching, "adjoint": adjoint,
+                "differentiation": differentiation, "precision_h60": h60,
                 "clocks": clk, "gpu_launches": 20 * args.steps}
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -398,6 +412,185 @@ def measure_batching(args):
                                       "128/6, 2 levels/lane", "256/2, 2 levels/lane", "64/8, 2 levels/lane"]},
             "GBps": nbytes / (ms["graph"] * 1e-3) / 1e9,
             "residual_sq_fp64": rn.tolist()}
+
+
+def field_errors(a, b):
+    """FP32 (a) against FP64 (b) per prognostic field: max-norm and RMS relative errors."""
+    names = ["rho", "u_1", "u_2", "rho_e_tot"]
+    out, rms = {}, {}
+    for c in range(4):
+        d = a[0][:, c].astype(np.float64) - b[0][:, c]
+        out[names[c]] = float(np.abs(d).max() / np.abs(b[0][:, c]).max())
+        rms[names[c]] = float(np.sqrt(np.mean(d * d) / np.mean(b[0][:, c] ** 2)))
+    d = a[1].astype(np.float64) - b[1]
+    out["u_3"] = float(np.abs(d).max() / max(np.abs(b[1]).max(), 1e-300))
+    rms["u_3"] = float(np.sqrt(np.mean(d * d) / max(np.mean(b[1] ** 2), 1e-300)))
+    out["rms"] = rms
+    out["norm"] = "max |FP32 - FP64| / max |FP64| per field; rms: |FP32 - FP64|_2 / |FP64|_2"
+    return out
+
+
+def _timed(fn):
+    import torch
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    st = torch.cuda.current_stream()
+    e0.record(st)
+    out = fn()
+    e1.record(st)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1), out
+
+
+def _rhoe_loss(target):
+    """J = 1/2 |rho e_tot - target|^2 over the stored centre nodes and its gradient."""
+    def lg(YN):
+        d = YN.c[:, 3] - target
+        G = YN.similar()
+        G.c[:, 3] = d
+        return 0.5 * float((d.double() * d.double()).sum().item()), G
+    return lg
+
+
+def measure_adjoint(args, s, fwd_ms):
+    """Reverse-mode cost on the production workload (h_elem=30, z_elem=63, FP32):
+    gradient of 1/2 |rho e_tot(t_n) - target|^2 over n steps with a checkpoint
+    every 5 steps; the pullback recomputes each segment (one forward step per
+    step) and runs the reverse kernels."""
+    import torch
+    from gbdycore import simulation as sim
+    n = args.adjoint_steps
+    Y0 = s.Y.copy()
+    target = Y0.c[:, 3] * 1.001
+    lg = _rhoe_loss(target)
+    sim.gradient(s.p, Y0, 1, lg, checkpoint_every=1)          # warm-up, allocates the reverse buffers
+    Y = Y0.copy()
+    f_ms, _ = _timed(lambda: s.p.call("gb_adjoint_forward", Y.gb(), 0.0, float(s.dt), n, 5))
+    J, Ybar = lg(Y)
+    import ctypes
+    d = (ctypes.c_double * 2)()
+    peak = ctypes.c_size_t(0)
+    r_ms, _ = _timed(lambda: s.p.call("gb_adjoint_reverse", Ybar.gb(), d, ctypes.byref(peak)))
+    finite = bool(torch.isfinite(Ybar.c).all() and torch.isfinite(Ybar.f).all())
+    return {"steps": n, "checkpoint_every": 5, "forward_ms_per_step": fwd_ms,
+            "checkpointed_forward_ms_per_step": f_ms / n, "reverse_ms_per_step": r_ms / n,
+            "adjoint_over_forward": (r_ms / n) / fwd_ms,
+            "what": "reverse = per-segment recompute (1 forward step per step, stage data kept) + reverse kernels; "
+                    "ratio against the graph-replayed forward step",
+            "dJ_dnu": d[0], "dJ_drate": d[1], "library_bytes": int(peak.value), "finite": finite}
+
+
+def measure_differentiation(args):
+    """Gradient of J = 1/2 |rho e_tot(t_end) - rho e_tot*|^2 over 8 steps (dt 200 s)
+    on h_elem=16, z_elem=45 with a Rayleigh sponge of rate 1e-4 s^-1 above 20 km,
+    with respect to the initial state, nu and the sponge rate; target = the run
+    from a seed-3 perturbed state.  FP32 timing; FP64 gradient checked against
+    central differences (relative step eps, FP64) in random directions."""
+    import torch
+    from gbdycore import config as C, setups as S, simulation as sim
+    out = {}
+    cfg32 = C.differentiation_h16()
+    nsteps = 8
+    for ft in (np.float32, np.float64):
+        cfg = cfg32.with_(ft=ft)
+        g = sim.Geometry(cfg)
+        Yc, Yf = S.initial_state(g, cfg, seed=0, sigma=1.0, dtype=np.float64)
+        Tc, Tf = S.initial_state(g, cfg, seed=3, sigma=1.0, dtype=np.float64)
+        p = sim.AtmosCache(cfg)
+        T = sim.FieldVector.from_numpy(Tc.astype(ft), Tf.astype(ft))
+        p.call("gb_step", T.gb(), 0.0, float(cfg.dt), nsteps, 1)
+        lg = _rhoe_loss(T.c[:, 3].clone())
+        Y0 = sim.FieldVector.from_numpy(Yc.astype(ft), Yf.astype(ft))
+        ms, (J, G, dnu, drate, peak) = _timed(lambda: sim.gradient(p, Y0, nsteps, lg, checkpoint_every=4))
+        key = "fp32" if ft == np.float32 else "fp64"
+        out[key] = {"gradient_ms": ms, "J": J, "dJ_dnu": dnu, "dJ_drate": drate, "library_bytes": peak}
+        if ft == np.float64:
+            def fwd(Xc, Xf, q=p):
+                Z = sim.FieldVector.from_numpy(Xc, Xf)
+                q.call("gb_step", Z.gb(), 0.0, float(cfg.dt), nsteps, 0)
+                return lg(Z)[0]
+            rng = np.random.default_rng(3)
+            errs = {1e-6: [], 1e-8: []}
+            for k in range(args.fd_directions):
+                dc = rng.standard_normal(Yc.shape)
+                for c in range(4):
+                    dc[:, c] *= np.sqrt(np.mean(Yc[:, c] ** 2))
+                df = rng.standard_normal(Yf.shape) * max(np.sqrt(np.mean(Yf ** 2)), 1e-3 * np.sqrt(np.mean(Yc[:, 1] ** 2)))
+                ad = float((G.c.cpu().numpy() * dc).sum() + (G.f.cpu().numpy() * df).sum())
+                for eps in errs:
+                    fd = (fwd(Yc + eps * dc, Yf + eps * df) - fwd(Yc - eps * dc, Yf - eps * df)) / (2 * eps)
+                    errs[eps].append(abs(ad - fd) / abs(fd))
+            par = {}
+            for name, mk, val, scale in (("nu", lambda s_: cfg.with_(nu=cfg.nu * s_), dnu, cfg.nu),
+                                         ("rate", lambda s_: cfg.with_(alpha_uh=1e-4 * s_, alpha_w=1e-4 * s_), drate, 1e-4)):
+                vals = []
+                for s_ in (1 + 1e-4, 1 - 1e-4):
+                    q = sim.AtmosCache(mk(s_))
+                    vals.append(fwd(Yc, Yf, q))
+                fd = (vals[0] - vals[1]) / (2e-4 * scale)
+                par[name] = {"adjoint": val, "fd": fd, "rel": abs(val - fd) / abs(fd)}
+            out["fd_check_fp64"] = {
+                "directions": args.fd_directions,
+                "rel_err_eps_1e-6": {"median": float(np.median(errs[1e-6])), "max": float(np.max(errs[1e-6]))},
+                "rel_err_eps_1e-8": {"median": float(np.median(errs[1e-8])), "max": float(np.max(errs[1e-8]))},
+                "parameters_eps_1e-4": par,
+                "note": "the van Leer limiter makes the 8-step map piecewise smooth: central differences "
+                        "with eps = 1e-6 can straddle limiter branch switches; eps = 1e-8 shown beside it"}
+        del p
+    f32 = C.differentiation_h16()
+    s32 = sim.AtmosSimulation(f32, state=S.initial_state(sim.Geometry(f32), f32, seed=0, sigma=1.0))
+    s32.step(2)
+    fms, _ = _timed(lambda: s32.step(nsteps))
+    out["fp32"]["forward_ms"] = fms
+    out["fp32"]["gradient_over_forward"] = out["fp32"]["gradient_ms"] / fms
+    out["workload"] = "h_elem=16, z_elem=45 stretched (dz_bottom 500 m), dt=200 s, 8 steps, sponge 1e-4 s^-1 above 20 km"
+    return out
+
+
+def measure_precision_h60(args):
+    """h_elem=60 (21,600 elements), z_elem=63 stretched, dt=60 s: 20 FP32 steps
+    against the FP64 run of the same library (per-field max error / max |FP64|),
+    and the 20-step adjoint with a checkpoint every 5 steps (peak device memory)."""
+    import ctypes
+    import torch
+    from gbdycore import config as C, setups as S, simulation as sim
+    cfg = C.precision_h60()
+    g = sim.Geometry(cfg)
+    Yc, Yf = S.workload_state(g, cfg, "precision")
+    out = {"workload": "h_elem=60, z_elem=63 tanh-stretched (dz_bottom 30 m), dt=60 s, 20 steps, seed 4"}
+    s64 = sim.AtmosSimulation(cfg.with_(ft=np.float64), state=(Yc.astype(np.float64), Yf.astype(np.float64)))
+    s64.step(20)
+    a64 = s64.Y.numpy()
+    sums64 = s64.p.global_sums(s64.Y)
+    del s64
+    torch.cuda.empty_cache()
+    s32 = sim.AtmosSimulation(cfg, state=(Yc.astype(np.float32), Yf.astype(np.float32)))
+    Y0 = s32.Y.copy()
+    s32.step(20)                      # the same 20 steps as the FP64 run
+    a32 = s32.Y.numpy()
+    sums32 = s32.p.global_sums(s32.Y)
+    ms, _ = _timed(lambda: s32.step(20))   # timing (graph already captured)
+    err = field_errors(a32, a64)
+    out.update({"fp32_ms_per_step": ms / 20, "fp32_vs_fp64_after_20_steps": err,
+                "mass_energy_fp32_vs_fp64_rel": [float(abs(sums32[i] - sums64[i]) / abs(sums64[i])) for i in range(2)]})
+    del a64
+    target = Y0.c[:, 3] * 1.001
+    lg = _rhoe_loss(target)
+    torch.cuda.synchronize()
+    free0, total = torch.cuda.mem_get_info()
+    Y = Y0.copy()
+    fwd_ms, _ = _timed(lambda: s32.p.call("gb_adjoint_forward", Y.gb(), 0.0, float(cfg.dt), 20, 5))
+    J, Ybar = lg(Y)
+    d = (ctypes.c_double * 2)()
+    peak = ctypes.c_size_t(0)
+    rev_ms, _ = _timed(lambda: s32.p.call("gb_adjoint_reverse", Ybar.gb(), d, ctypes.byref(peak)))
+    free1, _ = torch.cuda.mem_get_info()
+    out["adjoint_20_steps"] = {"checkpoint_every": 5, "forward_ms": fwd_ms, "reverse_ms": rev_ms,
+                               "reverse_over_forward_steps": rev_ms / (20 * ms / 20),
+                               "library_bytes": int(peak.value),
+                               "device_bytes_in_use_after_reverse": int(total - free1),
+                               "finite": bool(torch.isfinite(Ybar.c).all() and torch.isfinite(Ybar.f).all())}
+    return out
 
 
 def main():

@@ -48,7 +48,7 @@ struct ColVjpArgs {
   FT *Teb_c[4], *Teb_f[4];  // cotangents of the explicit tendencies (accumulated)
   FT *Tib_c[4], *Tib_f[4];  // cotangents of the implicit tendencies (accumulated)
   FT *scr;
-  double *dalpha;         // per-column d/d(sponge rate)
+  double *dalpha;         // per-column d/d(sponge rate), accumulated
 };
 
 template <class FT>
@@ -545,7 +545,7 @@ __global__ void __launch_bounds__(128) k_col_stage_vjp(DevParams<FT> P, ColVjpAr
       if (j >= 1) V.Tib_f[j][fb + f] += A.ci[j] * hb;
     }
   }
-  V.dalpha[col] = dal;
+  V.dalpha[col] += dal;  // accumulated over the launches of a reverse pass (zeroed by the host)
 }
 
 }  // namespace

@@ -579,9 +579,9 @@ __global__ void __launch_bounds__(AD_THREADS) k_passB_vjp(DevParams<FT> P, const
     }
     __syncthreads();
   }
-  if (threadIdx.x == 0) {
-    dpar[2 * blockIdx.x] = red[0][0];
-    dpar[2 * blockIdx.x + 1] = red[1][0];
+  if (threadIdx.x == 0) {  // accumulated over the launches of a reverse pass (zeroed by the host)
+    dpar[2 * blockIdx.x] += red[0][0];
+    dpar[2 * blockIdx.x + 1] += red[1][0];
   }
 }
 

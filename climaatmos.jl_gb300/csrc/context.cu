@@ -569,7 +569,6 @@ void tendency_vjp(gb_ctx *ctx, const FT *Uc, const FT *Uf, const FT *L, const FT
   cudaMemcpyAsync(Tb + I->NC, Tb_f, I->NF * sizeof(FT), cudaMemcpyDeviceToDevice, s);
   if (dss_out) launch_dss_transpose<FT>(P, Tb, Tb + I->NC, s);
   launch_passB_vjp<FT>(P, Uc, Uf, L, Tb, Tb + I->NC, Ubc, Ubf, Lb, (double *)A.dparB.p, A.grid, s);
-  launch_accum((const double *)A.dparB.p, A.grid, 2, 2, (double *)A.dacc.p, s);
   launch_dss_transpose<FT>(P, Lb, nullptr, s);
   launch_passA_vjp<FT>(P, Uc, Uf, Lb, Ubc, Ubf, A.grid, s);
 }
@@ -619,7 +618,6 @@ void reverse_step(gb_ctx *ctx, typename Impl<FT>::Record &rec, double dt_, FT *Y
       const StageArgs<FT> SA = stage_args<FT>(I, i, dt, Yc, Yf, Te, Ti);
       launch_column_stage_vjp<FT>(P, SA, Ubc, Ubf, Tib[i], Tib[i] + I->NR, Ybc, Ybf, Teb, Tib, I->NC, I->NR,
                                   (FT *)A.scr.p, (double *)A.dal.p, s);
-      launch_accum((const double *)A.dal.p, P.Nh * NN, 1, 1, (double *)A.dacc.p + 1, s);
     }
   }
 }
@@ -630,9 +628,23 @@ int dss_transpose_t(gb_ctx *ctx, gb_fieldvec X) {
   return check_launch(ctx);
 }
 
+// Zero the parameter partials (per-CTA of the pass B reverse, per column of
+// the column reverse) at the start of a reverse pass.
+template <class FT>
+void zero_dpar(gb_ctx *ctx, cudaStream_t s) {
+  auto &A = *impl<FT>(ctx)->adj;
+  cudaMemsetAsync(A.dacc.p, 0, 4 * sizeof(double), s);
+  cudaMemsetAsync(A.dparB.p, 0, (size_t)A.grid * 2 * sizeof(double), s);
+  cudaMemsetAsync(A.dal.p, 0, (size_t)impl<FT>(ctx)->P.Nh * NN * sizeof(double), s);
+}
+
+// Reduce the partials (fixed order) and read (d/dnu, d/d rate).
 template <class FT>
 int read_dacc(gb_ctx *ctx, double *dpar, bool add) {
   Impl<FT> *I = impl<FT>(ctx);
+  auto &A = *I->adj;
+  launch_accum((const double *)A.dparB.p, A.grid, 2, 2, (double *)A.dacc.p, ctx->stream);
+  launch_accum((const double *)A.dal.p, I->P.Nh * NN, 1, 1, (double *)A.dacc.p + 1, ctx->stream);
   double h[2];
   CK(cudaMemcpyAsync(h, I->adj->dacc.p, 2 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
@@ -649,7 +661,7 @@ int remaining_tendency_vjp_t(gb_ctx *ctx, gb_fieldvec Yb, gb_fieldvec Tb, gb_fie
   if (r) return r;
   Impl<FT> *I = impl<FT>(ctx);
   cudaStream_t s = ctx->stream;
-  CK(cudaMemsetAsync(I->adj->dacc.p, 0, 4 * sizeof(double), s));
+  zero_dpar<FT>(ctx, s);
   // forward Laplacians at Y (DSSed), then the reverse
   FT *L = (FT *)I->lap.p;
   launch_passA<FT>(I->P, (const FT *)Y.c, (const FT *)Y.f, L, s);
@@ -695,13 +707,12 @@ int implicit_stage_vjp_t(gb_ctx *ctx, gb_fieldvec Uhb, gb_fieldvec Ub, gb_fieldv
   if (r) return r;
   Impl<FT> *I = impl<FT>(ctx);
   cudaStream_t s = ctx->stream;
-  CK(cudaMemsetAsync(I->adj->dacc.p, 0, 4 * sizeof(double), s));
+  zero_dpar<FT>(ctx, s);
   const StageArgs<FT> A = single_stage_args<FT>(I, (const FT *)Uh.c, (const FT *)Uh.f, dtg);
   FT *Teb[4] = {(FT *)I->adj->dummy.p, nullptr, nullptr, nullptr}, *Tibs[4] = {nullptr, nullptr, nullptr, nullptr};
   launch_column_stage_vjp<FT>(I->P, A, (const FT *)Ub.c, (const FT *)Ub.f, (const FT *)Tib.c, (const FT *)Tib.f,
                               (FT *)Uhb.c, (FT *)Uhb.f, Teb, Tibs, I->NC, I->NR, (FT *)I->adj->scr.p,
                               (double *)I->adj->dal.p, s);
-  launch_accum((const double *)I->adj->dal.p, I->P.Nh * NN, 1, 1, (double *)I->adj->dacc.p + 1, s);
   if ((r = check_launch(ctx))) return r;
   return read_dacc<FT>(ctx, dpar, true);
 }
@@ -716,7 +727,7 @@ int step_vjp_t(gb_ctx *ctx, gb_fieldvec Yb, gb_fieldvec Y, double dt, double *dp
   FT *W = (FT *)A.work.p;
   CK(cudaMemcpyAsync(W, Y.c, I->NC * sizeof(FT), cudaMemcpyDeviceToDevice, s));
   CK(cudaMemcpyAsync(W + I->NC, Y.f, I->NF * sizeof(FT), cudaMemcpyDeviceToDevice, s));
-  CK(cudaMemsetAsync(A.dacc.p, 0, 4 * sizeof(double), s));
+  zero_dpar<FT>(ctx, s);
   record_step<FT>(ctx, W, W + I->NC, dt, *A.rec[0], s);
   reverse_step<FT>(ctx, *A.rec[0], dt, (FT *)Yb.c, (FT *)Yb.f, s);
   if ((r = check_launch(ctx))) return r;
@@ -765,7 +776,7 @@ int adjoint_reverse_t(gb_ctx *ctx, gb_fieldvec Yb, double *dpar, size_t *peak) {
   cudaStream_t s = ctx->stream;
   const size_t SB = (I->NC + I->NF) * sizeof(FT);
   FT *W = (FT *)A.work.p;
-  CK(cudaMemsetAsync(A.dacc.p, 0, 4 * sizeof(double), s));
+  zero_dpar<FT>(ctx, s);
   const int nseg = (A.nsteps + A.every - 1) / A.every;
   for (int g = nseg - 1; g >= 0; --g) {
     const int s0 = g * A.every, s1 = std::min(A.nsteps, s0 + A.every);

@@ -20,7 +20,9 @@
 // transposed tridiagonal solves by the Thomas algorithm); the per-column
 // intermediates live in a column-major global scratch so that the threads of
 // a warp access consecutive words.
-#include "kernels.cuh"
+#include <cstdlib>
+
+#include "colcore.cuh"
 
 namespace gb {
 
@@ -548,6 +550,565 @@ __global__ void __launch_bounds__(128) k_col_stage_vjp(DevParams<FT> P, ColVjpAr
   V.dalpha[col] += dal;  // accumulated over the launches of a reverse pass (zeroed by the host)
 }
 
+
+// ============================================================================ lane-parallel form
+// The same reverse pass with a column held by G lanes, CM levels per lane (the
+// forward stage kernel's layout): the forward is recomputed in registers, the
+// transposed tridiagonal system is solved by the lane-parallel cyclic
+// reduction, and every scatter to a neighbouring level becomes a local add
+// plus one shuffle ("fold") per halo.
+namespace lp {
+
+using col::up;
+using col::down;
+
+// Value of level r0 - 1 (previous lane's last) and r0 + CM (next lane's first); 0 past the column.
+template <int G, int CM, class FT>
+__device__ __forceinline__ FT prv(const FT (&x)[CM], int gl) {
+  const FT v = up<G>(x[CM - 1], 1);
+  return gl > 0 ? v : FT(0);
+}
+template <int G, int CM, class FT>
+__device__ __forceinline__ FT prv2(const FT (&x)[CM], int gl) {
+  const FT v = up<G>(x[CM - 2], 1);
+  return gl > 0 ? v : FT(0);
+}
+template <int G, int CM, class FT>
+__device__ __forceinline__ FT nxt(const FT (&x)[CM], int gl) {
+  const FT v = down<G>(x[0], 1);
+  return gl + 1 < G ? v : FT(0);
+}
+template <int G, int CM, class FT>
+__device__ __forceinline__ FT nxt2(const FT (&x)[CM], int gl) {
+  const FT v = down<G>(x[1], 1);
+  return gl + 1 < G ? v : FT(0);
+}
+// own[] += the contributions neighbours computed for this lane's levels:
+// toPrev is this lane's contribution to level r0 - 1, toNext to level r0 + CM.
+template <int G, int CM, class FT>
+__device__ __forceinline__ void fold1(FT (&own)[CM], FT toPrev, FT toNext, int gl) {
+  const FT fn = down<G>(toPrev, 1), fp = up<G>(toNext, 1);
+  if (gl + 1 < G) own[CM - 1] += fn;
+  if (gl > 0) own[0] += fp;
+}
+// halo 2: toPrev2 -> r0 - 2, toPrev1 -> r0 - 1, toNext0 -> r0 + CM, toNext1 -> r0 + CM + 1
+template <int G, int CM, class FT>
+__device__ __forceinline__ void fold2(FT (&own)[CM], FT toPrev2, FT toPrev1, FT toNext0, FT toNext1, int gl) {
+  const FT a = down<G>(toPrev2, 1), b = down<G>(toPrev1, 1), c = up<G>(toNext0, 1), d = up<G>(toNext1, 1);
+  if (gl + 1 < G) { own[CM - 2] += a; own[CM - 1] += b; }
+  if (gl > 0) { own[0] += c; own[1] += d; }
+}
+
+template <class FT, int G, int CM>
+__global__ void __launch_bounds__(128) k_col_stage_vjp_g(DevParams<FT> P, ColVjpArgs<FT> V) {
+  const int lane = threadIdx.x & 31, gl = lane % G;
+  const int col0 = (blockIdx.x * 4 + (threadIdx.x >> 5)) * (32 / G) + lane / G;
+  const int ncols = P.Nh * NN;
+  const bool colv = col0 < ncols;
+  const int col = colv ? col0 : ncols - 1;
+  const StageArgs<FT> &A = V.A;
+  const int e = col >> 4, n = col & 15, Nv = P.Nv, Nf = P.Nf, r0 = gl * CM, sc = NN * Nv;
+  ColGeo<FT> Gm;
+  Gm.load(P, e, n);
+  const FT dtg = A.dtg, idtg = A.idtg, kap = P.Rd * P.icvd;
+  const size_t cb = (size_t)e * 4 * NN * Nv + (size_t)n * Nv + r0, rb = (size_t)e * 2 * NN * Nv + (size_t)n * Nv + r0;
+  const size_t fb = ((size_t)e * NN + n) * Nf + r0;
+  const col::ColLev<FT> L{P.lc4, P.lf4, Nv, Nf};
+  // ---------------------------------------------------------------- forward recompute
+  FT H[5][CM];
+#pragma unroll
+  for (int k = 0; k < CM; ++k) {
+    const bool okc = r0 + k < Nv, okf = r0 + k < Nf;
+#pragma unroll
+    for (int c = 0; c < 4; ++c) H[c][k] = okc ? A.un_c[cb + (size_t)c * sc + k] : FT(0);
+    H[4][k] = okf ? A.un_f[fb + k] : FT(0);
+  }
+  for (int j = 0; j < A.nsrc; ++j) {
+#pragma unroll
+    for (int k = 0; k < CM; ++k) {
+      const bool okc = r0 + k < Nv, okf = r0 + k < Nf;
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        H[c][k] += A.ce[j] * (okc ? A.te_c[j][cb + (size_t)c * sc + k] : FT(0));
+        if (j >= 1 && (c == 0 || c == 3))
+          H[c][k] += A.ci[j] * (okc ? A.ti_c[j][rb + (size_t)(c == 0 ? 0 : sc) + k] : FT(0));
+      }
+      H[4][k] += A.ce[j] * (okf ? A.te_f[j][fb + k] : FT(0));
+      if (j >= 1) H[4][k] += A.ci[j] * (okf ? A.ti_f[j][fb + k] : FT(0));
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < CM; ++k) {
+    if (r0 + k >= Nv) { H[0][k] = FT(1); H[1][k] = FT(0); H[2][k] = FT(0); H[3][k] = FT(1); }
+    if (r0 + k >= Nf) H[4][k] = FT(0);
+  }
+  FT u3[CM], g33[CM], beta[CM], spg[CM], dphi[CM];
+#pragma unroll
+  for (int k = 0; k < CM; ++k) {
+    const int f = r0 + k;
+    u3[k] = (f == 0 || f >= Nv) ? FT(0) : H[4][k];
+    const Lev4<FT> lf = P.lf4[min(f, Nf - 1)];
+    g33[k] = lf.x;
+    beta[k] = lf.y;
+    dphi[k] = lf.z;
+    spg[k] = P.levf[LF_SPG * Nf + min(f, Nf - 1)];
+  }
+  const FT u3n0 = nxt<G, CM>(u3, gl), g33n0 = nxt<G, CM>(g33, gl);
+  const FT u3p = prv<G, CM>(u3, gl), g33p = prv<G, CM>(g33, gl);
+  // centre diagnostics of U0
+  FT K[CM], h[CM], Pi[CM], thv[CM], thvr[CM], phir[CM], rJ[CM], iJ[CM], c1[CM], c2[CM], Jc[CM], phi[CM];
+#pragma unroll
+  for (int k = 0; k < CM; ++k) {
+    const int v = r0 + k;
+    const FT ub = k + 1 < CM ? u3[k + 1] : u3n0, gb = k + 1 < CM ? g33[k + 1] : g33n0;
+    const Lev4<FT> Lc = P.lc4[min(v, Nv - 1)];
+    c1[k] = (Gm.gu0 * H[1][k] + Gm.gu1 * H[2][k]) * Lc.z;
+    c2[k] = (Gm.gu1 * H[1][k] + Gm.gu2 * H[2][k]) * Lc.z;
+    const col::Cen<FT> cc = col::cdiag(P, Gm, L, v, H[0][k], H[1][k], H[2][k], H[3][k], u3[k], ub, g33[k], gb);
+    K[k] = cc.K; h[k] = cc.h; Pi[k] = cc.Pi; thv[k] = cc.thv; thvr[k] = cc.thvr; phir[k] = cc.phir;
+    rJ[k] = cc.rJ; iJ[k] = cc.iJ; Jc[k] = Gm.Jh * Lc.x; phi[k] = cc.phi;
+  }
+  // previous-level (centre r0 - 1) values
+  const FT rJp = prv<G, CM>(rJ, gl), hp = prv<G, CM>(h, gl), Kp = prv<G, CM>(K, gl), Pip = prv<G, CM>(Pi, gl);
+  const FT thvp = prv<G, CM>(thv, gl), thvrp = prv<G, CM>(thvr, gl), phirp = prv<G, CM>(phir, gl);
+  const FT rhop = prv<G, CM>(H[0], gl), phip = prv<G, CM>(phi, gl);
+  auto cprev = [&](const FT (&x)[CM], int k, FT pv) { return k > 0 ? x[k - 1] : pv; };
+  // face fluxes and rows
+  FT fr[CM], fhb[CM], F[CM], Fh[CM], T3[CM], ur0[CM], ur1[CM], ue0[CM], uu0[CM], uu1[CM], uu2[CM];
+#pragma unroll
+  for (int k = 0; k < CM; ++k) {
+    const int f = r0 + k;
+    const bool inner = f > 0 && f < Nv;
+    const FT rJa = cprev(rJ, k, rJp), ha = cprev(h, k, hp);
+    const FT rJb = (rJa + rJ[k]) / FT(2), hb = (ha + h[k]) / FT(2);
+    F[k] = inner ? rJb * (u3[k] * g33[k]) : FT(0);
+    Fh[k] = F[k] * hb;
+    fr[k] = inner ? rJb * g33[k] : FT(0);
+    fhb[k] = inner ? hb : FT(0);
+    if (inner) {
+      const FT ra = cprev(H[0], k, rhop), rbv = H[0][k];
+      const FT irb = FT(1) / ((ra + rbv) / FT(2));
+      const FT dpa = kap * (P.T0 * P.cpd - cprev(K, k, Kp) - cprev(phi, k, phip));
+      const FT dpb = kap * (P.T0 * P.cpd - K[k] - phi[k]);
+      const FT thva = cprev(thv, k, thvp), Pia = cprev(Pi, k, Pip);
+      const FT buoy = P.cpd * ((thva + thv[k]) / FT(2)) * (Pi[k] - Pia) * irb;
+      ur0[k] = dtg * (dpa * irb + buoy / FT(2));
+      ur1[k] = dtg * (-dpb * irb + buoy / FT(2));
+      ue0[k] = dtg * (kap * irb);
+      const FT u3cm = cprev(u3, k, u3p) * cprev(g33, k, g33p), u3c = u3[k] * g33[k];
+      const FT u3cp = (k + 1 < CM ? u3[k + 1] : u3n0) * (k + 1 < CM ? g33[k + 1] : g33n0);
+      uu0[k] = dtg * (-kap * ra * u3cm * (irb / FT(2)));
+      uu1[k] = dtg * (kap * (rbv - ra) * u3c * (irb / FT(2)) - beta[k]) - FT(1);
+      uu2[k] = dtg * (kap * rbv * u3cp * (irb / FT(2)));
+      const FT thd = ((thva - cprev(thvr, k, thvrp)) + (thv[k] - thvr[k])) / FT(2);
+      T3[k] = -(dphi[k] - (phir[k] - cprev(phir, k, phirp)) + P.cpd * thd * (Pi[k] - Pia)) - beta[k] * u3[k];
+    } else {
+      ur0[k] = ur1[k] = ue0[k] = uu0[k] = uu2[k] = FT(0);
+      uu1[k] = f <= Nv ? -dtg * beta[k] - FT(1) : FT(1);
+      T3[k] = -beta[k] * u3[k];
+    }
+  }
+  const FT Fn = nxt<G, CM>(F, gl), Fhn = nxt<G, CM>(Fh, gl), frn = nxt<G, CM>(fr, gl), fhbn = nxt<G, CM>(fhb, gl);
+  auto fnext = [&](const FT (&x)[CM], int k, FT nv) { return k + 1 < CM ? x[k + 1] : nv; };
+  FT Rr[CM], Re[CM], ru0[CM], ru1[CM], eu0[CM], eu1[CM];
+#pragma unroll
+  for (int k = 0; k < CM; ++k) {
+    const bool cv = r0 + k < Nv;
+    Rr[k] = cv ? dtg * (-((fnext(F, k, Fn) - F[k]) * iJ[k])) : FT(0);
+    Re[k] = cv ? dtg * (-((fnext(Fh, k, Fhn) - Fh[k]) * iJ[k])) : FT(0);
+    ru0[k] = cv ? dtg * (fr[k] * iJ[k]) : FT(0);
+    ru1[k] = cv ? dtg * (-fnext(fr, k, frn) * iJ[k]) : FT(0);
+    eu0[k] = cv ? dtg * (fr[k] * iJ[k] * fhb[k]) : FT(0);
+    eu1[k] = cv ? dtg * (-fnext(fr, k, frn) * iJ[k] * fnext(fhb, k, fhbn)) : FT(0);
+  }
+  const FT ru0p = prv<G, CM>(ru0, gl), ru1p = prv<G, CM>(ru1, gl), eu0p = prv<G, CM>(eu0, gl);
+  const FT eu1p = prv<G, CM>(eu1, gl), Rrp = prv<G, CM>(Rr, gl), Rep = prv<G, CM>(Re, gl);
+  FT Sa[CM], Sb[CM], Sc[CM], Sd[CM];
+#pragma unroll
+  for (int k = 0; k < CM; ++k) {
+    const int f = r0 + k;
+    FT aa = uu0[k], bb = uu1[k], cc = uu2[k], rhs = f < Nf ? dtg * T3[k] + (H[4][k] - u3[k]) : FT(0);
+    if (f >= 1 && f - 1 < Nv) {
+      aa += ur0[k] * cprev(ru0, k, ru0p) + ue0[k] * cprev(eu0, k, eu0p);
+      bb += ur0[k] * cprev(ru1, k, ru1p) + ue0[k] * cprev(eu1, k, eu1p);
+      rhs += ur0[k] * cprev(Rr, k, Rrp) + ue0[k] * cprev(Re, k, Rep);
+    }
+    if (f < Nv) {
+      bb += ur1[k] * ru0[k] - ue0[k] * eu0[k];
+      cc += ur1[k] * ru1[k] - ue0[k] * eu1[k];
+      rhs += ur1[k] * Rr[k] - ue0[k] * Re[k];
+    }
+    if (f >= Nf) { aa = FT(0); bb = FT(1); cc = FT(0); rhs = FT(0); }
+    Sa[k] = aa; Sb[k] = bb; Sc[k] = cc; Sd[k] = rhs;
+  }
+  FT x[CM];
+  {
+    FT a_[CM], b_[CM], c_[CM], d_[CM];
+#pragma unroll
+    for (int k = 0; k < CM; ++k) { a_[k] = Sa[k]; b_[k] = Sb[k]; c_[k] = Sc[k]; d_[k] = Sd[k]; }
+    col::solve_lanes<FT, G, CM>(a_, b_, c_, d_, x, gl);
+  }
+  const FT xn0 = nxt<G, CM>(x, gl), xp = prv<G, CM>(x, gl);
+  FT RN[CM], REN[CM], U3N[CM];
+#pragma unroll
+  for (int k = 0; k < CM; ++k) {
+    const int f = r0 + k;
+    const FT xu = fnext(x, k, xn0);
+    RN[k] = H[0][k] - (ru0[k] * x[k] + ru1[k] * xu - Rr[k]);
+    REN[k] = H[3][k] - (eu0[k] * x[k] + eu1[k] * xu - Re[k]);
+    if (f >= Nv) { RN[k] = FT(1); REN[k] = FT(1); }
+    U3N[k] = (f == 0 || f >= Nv) ? FT(0) : u3[k] - x[k];
+  }
+  // ---------------------------------------------------------------- reverse
+  FT bRN[CM], bREN[CM], bU3N[CM], bU1[CM], bU2[CM];
+#pragma unroll
+  for (int k = 0; k < CM; ++k) {
+    const bool okc = r0 + k < Nv, okf = r0 + k < Nf;
+    bRN[k] = okc ? V.Ub_c[cb + k] + V.Tb_c[rb + k] * idtg : FT(0);
+    bREN[k] = okc ? V.Ub_c[cb + (size_t)3 * sc + k] + V.Tb_c[rb + (size_t)sc + k] * idtg : FT(0);
+    bU3N[k] = okf ? V.Ub_f[fb + k] + V.Tb_f[fb + k] * idtg : FT(0);
+    bU1[k] = FT(0);
+    bU2[k] = FT(0);
+  }
+  // (a) van Leer minus central correction at the Newton result
+  if (P.upwinding) {
+    FT hn[CM], rJn[CM], cn1[CM], cn2[CM], Kn[CM];
+    const FT U3Nn = nxt<G, CM>(U3N, gl);
+#pragma unroll
+    for (int k = 0; k < CM; ++k) {
+      const FT wn = fnext(U3N, k, U3Nn), gb = fnext(g33, k, g33n0);
+      const col::Cen<FT> cc = col::cdiag(P, Gm, L, r0 + k, RN[k], H[1][k], H[2][k], REN[k], U3N[k], wn, g33[k], gb);
+      hn[k] = cc.h;
+      rJn[k] = cc.rJ;
+      Kn[k] = cc.K;
+      cn1[k] = c1[k];
+      cn2[k] = c2[k];
+    }
+    const FT hnp = prv<G, CM>(hn, gl), hnp2 = prv2<G, CM>(hn, gl), hnn = nxt<G, CM>(hn, gl), hnn2 = nxt2<G, CM>(hn, gl);
+    const FT rJnp = prv<G, CM>(rJn, gl);
+    const FT bRENp = prv<G, CM>(bREN, gl), iJp = prv<G, CM>(iJ, gl);
+    // contributions: h to levels f-2 .. f+1 (array index j + 2 -> level r0 + j), rJ to f-1, f
+    FT accH[CM + 4], accR[CM + 2];
+#pragma unroll
+    for (int j = 0; j < CM + 4; ++j) accH[j] = FT(0);
+#pragma unroll
+    for (int j = 0; j < CM + 2; ++j) accR[j] = FT(0);
+#pragma unroll
+    for (int k = 0; k < CM; ++k) {
+      const int f = r0 + k;
+      if (!(f >= 1 && f < Nv)) continue;
+      FT cbv = dtg * bREN[k] * iJ[k];
+      cbv -= dtg * cprev(bREN, k, bRENp) * cprev(iJ, k, iJp);
+      const FT u = U3N[k] * g33[k];
+      const FT hA1 = k >= 1 ? hn[k - 1] : hnp;
+      const FT hA2 = k >= 2 ? hn[k - 2] : (k == 1 ? hnp : hnp2);
+      const FT h0 = hn[k], hP1 = k + 1 < CM ? hn[k + 1] : hnn;
+      const FT rJb = (cprev(rJn, k, rJnp) + rJn[k]) / FT(2);
+      const bool near = f == 1 || f == Nv - 1;
+      const FT vl = vl_value(u, f >= 2 ? hA2 : FT(0), hA1, h0, f + 1 < Nv ? hP1 : FT(0), near, P.dt_model);
+      FT du, dh[4];
+      vl_grad(u, f >= 2 ? hA2 : FT(0), hA1, h0, f + 1 < Nv ? hP1 : FT(0), near, P.dt_model, du, dh);
+      const FT hm = (hA1 + h0) / FT(2);
+      const FT rJbb = cbv * vl - cbv * u * hm;
+      accR[k] += rJbb / FT(2);      // level f - 1 (index k - 1 + 1)
+      accR[k + 1] += rJbb / FT(2);  // level f
+      bU3N[k] += (cbv * rJb * du - cbv * rJb * hm) * g33[k];
+      if (f >= 2) accH[k] += cbv * rJb * dh[0];  // level f - 2 (index k - 2 + 2)
+      accH[k + 1] += cbv * rJb * dh[1] - cbv * rJb * u / FT(2);
+      accH[k + 2] += cbv * rJb * dh[2] - cbv * rJb * u / FT(2);
+      if (f + 1 < Nv) accH[k + 3] += cbv * rJb * dh[3];
+    }
+    FT bHN[CM], bRJN[CM];
+#pragma unroll
+    for (int k = 0; k < CM; ++k) { bHN[k] = accH[k + 2]; bRJN[k] = accR[k + 1]; }
+    fold2<G, CM>(bHN, accH[0], accH[1], accH[CM + 2], accH[CM + 3], gl);
+    fold1<G, CM>(bRJN, accR[0], accR[CM + 1], gl);
+    FT toNextU3 = FT(0);
+#pragma unroll
+    for (int k = 0; k < CM; ++k) {
+      if (r0 + k >= Nv) continue;
+      ThermoBar<FT> tb{};
+      tb.h = bHN[k];
+      FT rb_, reb, Kb;
+      thermo_vjp(P, RN[k], REN[k], Kn[k], phi[k], tb, rb_, reb, Kb);
+      bRN[k] += rb_ + Jc[k] * bRJN[k];
+      bREN[k] += reb;
+      bU1[k] += cn1[k] * Kb;
+      bU2[k] += cn2[k] * Kb;
+      bU3N[k] += Kb * U3N[k] * g33[k] / FT(2);
+      const FT cUp = Kb * fnext(U3N, k, U3Nn) * fnext(g33, k, g33n0) / FT(2);
+      if (k + 1 < CM) bU3N[k + 1] += cUp; else toNextU3 = cUp;
+    }
+    fold1<G, CM>(bU3N, FT(0), toNextU3, gl);
+  }
+  // (b) back-substitution: U = U0 - dY
+  FT bR0[CM], bRE0[CM], bRr[CM], bRe[CM], bru0[CM], bru1[CM], beu0[CM], beu1[CM], bX[CM], bU3[CM];
+  {
+    const FT bRNp = prv<G, CM>(bRN, gl), bRENp = prv<G, CM>(bREN, gl);
+#pragma unroll
+    for (int k = 0; k < CM; ++k) {
+      const int f = r0 + k;
+      const bool cv = f < Nv, inner = f > 0 && f < Nv;
+      const FT xu = fnext(x, k, xn0);
+      bR0[k] = cv ? bRN[k] : FT(0);
+      bRE0[k] = cv ? bREN[k] : FT(0);
+      bRr[k] = bR0[k];
+      bRe[k] = bRE0[k];
+      bru0[k] = -bR0[k] * x[k];
+      bru1[k] = -bR0[k] * xu;
+      beu0[k] = -bRE0[k] * x[k];
+      beu1[k] = -bRE0[k] * xu;
+      FT xb = FT(0);
+      if (cv) xb -= bRN[k] * ru0[k] + bREN[k] * eu0[k];
+      if (f >= 1 && f - 1 < Nv) xb -= cprev(bRN, k, bRNp) * cprev(ru1, k, ru1p) + cprev(bREN, k, bRENp) * cprev(eu1, k, eu1p);
+      bU3[k] = FT(0);
+      if (inner) {
+        xb -= bU3N[k];
+        bU3[k] = bU3N[k];
+      }
+      bX[k] = f < Nf ? xb : FT(0);
+    }
+  }
+  // (c) transposed solve A^T dbar = xbar (sub C[f-1], diagonal B[f], super A[f+1])
+  FT bD[CM];
+  {
+    const FT Scp = prv<G, CM>(Sc, gl), San = nxt<G, CM>(Sa, gl);
+    FT a_[CM], b_[CM], c_[CM], d_[CM];
+#pragma unroll
+    for (int k = 0; k < CM; ++k) {
+      const int f = r0 + k;
+      a_[k] = f >= 1 ? cprev(Sc, k, Scp) : FT(0);
+      b_[k] = Sb[k];
+      c_[k] = f + 1 < Nf ? fnext(Sa, k, San) : FT(0);
+      d_[k] = bX[k];
+      if (f >= Nf) { a_[k] = FT(0); b_[k] = FT(1); c_[k] = FT(0); d_[k] = FT(0); }
+    }
+    col::solve_lanes<FT, G, CM>(a_, b_, c_, d_, bD, gl);
+  }
+  // (d) Schur rows, Jacobian entries, u_3 tendency
+  FT bH4[CM], bK[CM], bH[CM], bPI[CM], bTHV[CM], bTHVR[CM], bPHIR[CM], bRJ[CM];
+#pragma unroll
+  for (int k = 0; k < CM; ++k) {
+    bH4[k] = bK[k] = bH[k] = bPI[k] = bTHV[k] = bTHVR[k] = bPHIR[k] = bRJ[k] = FT(0);
+  }
+  double dal = 0;
+  {
+    // contributions to the centre below the face (f - 1) go to the previous level
+    FT pR0 = 0, pK = 0, pTHV = 0, pTHVR = 0, pPI = 0, pPHIR = 0, pru0 = 0, pru1 = 0, peu0 = 0, peu1 = 0, pRr = 0, pRe = 0;
+    FT toPrevU3 = 0, toNextU3 = 0;
+    FT cR0[CM], cK[CM], cTHV[CM], cTHVR[CM], cPI[CM], cPHIR[CM], cru0[CM], cru1[CM], ceu0[CM], ceu1[CM], cRr[CM], cRe[CM];
+#pragma unroll
+    for (int k = 0; k < CM; ++k)
+      cR0[k] = cK[k] = cTHV[k] = cTHVR[k] = cPI[k] = cPHIR[k] = cru0[k] = cru1[k] = ceu0[k] = ceu1[k] = cRr[k] = cRe[k] = FT(0);
+    const FT xpv = xp;
+#pragma unroll
+    for (int k = 0; k < CM; ++k) {
+      const int f = r0 + k;
+      if (f >= Nf) continue;
+      const FT db = bD[k];
+      const FT ab = f >= 1 ? -db * cprev(x, k, xpv) : FT(0);
+      const FT bbb = -db * x[k];
+      const FT cbb = f + 1 < Nf ? -db * fnext(x, k, xn0) : FT(0);
+      FT ur0b = 0, ur1b = 0, ue0b = 0;
+      // (scalar, u_3) rows of the centre below (f - 1): its index is k - 1 (this lane) or the previous lane's last
+      auto addA = [&](FT (&arr)[CM], FT &pv, FT val) {
+        if (k >= 1) arr[k - 1] += val; else pv += val;
+      };
+      if (f >= 1 && f - 1 < Nv) {
+        ur0b += cprev(ru0, k, ru0p) * ab + cprev(ru1, k, ru1p) * bbb + cprev(Rr, k, Rrp) * db;
+        ue0b += cprev(eu0, k, eu0p) * ab + cprev(eu1, k, eu1p) * bbb + cprev(Re, k, Rep) * db;
+        addA(cru0, pru0, ur0[k] * ab);
+        addA(cru1, pru1, ur0[k] * bbb);
+        addA(ceu0, peu0, ue0[k] * ab);
+        addA(ceu1, peu1, ue0[k] * bbb);
+        addA(cRr, pRr, ur0[k] * db);
+        addA(cRe, pRe, ue0[k] * db);
+      }
+      if (f < Nv) {
+        ur1b += ru0[k] * bbb + ru1[k] * cbb + Rr[k] * db;
+        ue0b -= eu0[k] * bbb + eu1[k] * cbb + Re[k] * db;
+        cru0[k] += ur1[k] * bbb;
+        cru1[k] += ur1[k] * cbb;
+        ceu0[k] -= ue0[k] * bbb;
+        ceu1[k] -= ue0[k] * cbb;
+        cRr[k] += ur1[k] * db;
+        cRe[k] -= ue0[k] * db;
+      }
+      const FT T3b = dtg * db;
+      bH4[k] += db;
+      bU3[k] -= db;
+      bU3[k] -= beta[k] * T3b;
+      dal -= (double)(spg[k] * u3[k] * T3b);
+      dal -= (double)(dtg * spg[k] * bbb);
+      if (!(f > 0 && f < Nv)) continue;
+      // T3 = -(dPhi - (Phi_r(b) - Phi_r(a)) + cp thd (Pi(b) - Pi(a))) - beta u3
+      const FT Pia = cprev(Pi, k, Pip), dPi = Pi[k] - Pia;
+      const FT thva = cprev(thv, k, thvp), thvra = cprev(thvr, k, thvrp);
+      const FT thd = ((thva - thvra) + (thv[k] - thvr[k])) / FT(2);
+      cPHIR[k] += T3b;
+      addA(cPHIR, pPHIR, -T3b);
+      const FT thdb = -P.cpd * dPi * T3b;
+      cPI[k] -= P.cpd * thd * T3b;
+      addA(cPI, pPI, P.cpd * thd * T3b);
+      addA(cTHV, pTHV, thdb / FT(2));
+      addA(cTHVR, pTHVR, -thdb / FT(2));
+      cTHV[k] += thdb / FT(2);
+      cTHVR[k] -= thdb / FT(2);
+      // Jacobian entries
+      const FT uu0b = ab, uu1b = bbb, uu2b = cbb;
+      const FT ra = cprev(H[0], k, rhop), rbv = H[0][k];
+      const FT irb = FT(1) / ((ra + rbv) / FT(2));
+      const FT dpa = kap * (P.T0 * P.cpd - cprev(K, k, Kp) - cprev(phi, k, phip));
+      const FT dpb = kap * (P.T0 * P.cpd - K[k] - phi[k]);
+      const FT thvb = (thva + thv[k]) / FT(2);
+      const FT u3cm = cprev(u3, k, u3p) * cprev(g33, k, g33p), u3c = u3[k] * g33[k];
+      const FT u3cp = fnext(u3, k, u3n0) * fnext(g33, k, g33n0);
+      const FT dpab = dtg * irb * ur0b, dpbb = -dtg * irb * ur1b, buoyb = dtg * (ur0b + ur1b) / FT(2);
+      FT irbb = dtg * (dpa * ur0b - dpb * ur1b) + dtg * kap * ue0b;
+      irbb += dtg * (-kap * ra * u3cm / FT(2)) * uu0b + dtg * (kap * (rbv - ra) * u3c / FT(2)) * uu1b +
+              dtg * (kap * rbv * u3cp / FT(2)) * uu2b;
+      irbb += buoyb * P.cpd * thvb * dPi;
+      const FT thvbb = buoyb * P.cpd * dPi * irb, dPib = buoyb * P.cpd * thvb * irb;
+      const FT rbarb = -irb * irb * irbb;
+      addA(cR0, pR0, dtg * (-kap * u3cm * irb / FT(2)) * uu0b - dtg * kap * u3c * irb / FT(2) * uu1b + rbarb / FT(2));
+      cR0[k] += dtg * kap * u3c * irb / FT(2) * uu1b + dtg * kap * u3cp * irb / FT(2) * uu2b + rbarb / FT(2);
+      const FT tp = dtg * (-kap * ra * irb / FT(2)) * uu0b * cprev(g33, k, g33p);
+      if (k >= 1) bU3[k - 1] += tp; else toPrevU3 += tp;
+      bU3[k] += dtg * kap * (rbv - ra) * irb / FT(2) * uu1b * g33[k];
+      const FT tn = dtg * kap * rbv * irb / FT(2) * uu2b * fnext(g33, k, g33n0);
+      if (k + 1 < CM) bU3[k + 1] += tn; else toNextU3 += tn;
+      addA(cK, pK, -kap * dpab);
+      cK[k] -= kap * dpbb;
+      addA(cTHV, pTHV, thvbb / FT(2));
+      cTHV[k] += thvbb / FT(2);
+      cPI[k] += dPib;
+      addA(cPI, pPI, -dPib);
+    }
+    fold1<G, CM>(cR0, pR0, FT(0), gl);
+    fold1<G, CM>(cK, pK, FT(0), gl);
+    fold1<G, CM>(cTHV, pTHV, FT(0), gl);
+    fold1<G, CM>(cTHVR, pTHVR, FT(0), gl);
+    fold1<G, CM>(cPI, pPI, FT(0), gl);
+    fold1<G, CM>(cPHIR, pPHIR, FT(0), gl);
+    fold1<G, CM>(cru0, pru0, FT(0), gl);
+    fold1<G, CM>(cru1, pru1, FT(0), gl);
+    fold1<G, CM>(ceu0, peu0, FT(0), gl);
+    fold1<G, CM>(ceu1, peu1, FT(0), gl);
+    fold1<G, CM>(cRr, pRr, FT(0), gl);
+    fold1<G, CM>(cRe, pRe, FT(0), gl);
+    fold1<G, CM>(bU3, toPrevU3, toNextU3, gl);
+#pragma unroll
+    for (int k = 0; k < CM; ++k) {
+      bR0[k] += cR0[k]; bK[k] += cK[k]; bTHV[k] += cTHV[k]; bTHVR[k] += cTHVR[k]; bPI[k] += cPI[k];
+      bPHIR[k] += cPHIR[k]; bru0[k] += cru0[k]; bru1[k] += cru1[k]; beu0[k] += ceu0[k]; beu1[k] += ceu1[k];
+      bRr[k] += cRr[k]; bRe[k] += cRe[k];
+    }
+  }
+  // (e) centre rows: contributions to the face cotangents of F, F h, fr, fhb at faces v, v+1
+  FT bF[CM], bFh[CM], bfr[CM], bfhb[CM];
+  {
+    FT nF = 0, nFh = 0, nfr = 0, nfhb = 0;
+#pragma unroll
+    for (int k = 0; k < CM; ++k) bF[k] = bFh[k] = bfr[k] = bfhb[k] = FT(0);
+#pragma unroll
+    for (int k = 0; k < CM; ++k) {
+      if (r0 + k >= Nv) continue;
+      const FT Trb = dtg * bRr[k], Teb = dtg * bRe[k];
+      bF[k] += Trb * iJ[k];
+      bFh[k] += Teb * iJ[k];
+      bfr[k] += dtg * iJ[k] * bru0[k] + dtg * iJ[k] * fhb[k] * beu0[k];
+      bfhb[k] += dtg * fr[k] * iJ[k] * beu0[k];
+      const FT frU = fnext(fr, k, frn), fhbU = fnext(fhb, k, fhbn);
+      const FT uF = -Trb * iJ[k], uFh = -Teb * iJ[k];
+      const FT ufr = -(dtg * iJ[k] * bru1[k] + dtg * iJ[k] * fhbU * beu1[k]);
+      const FT ufhb = -dtg * frU * iJ[k] * beu1[k];
+      if (k + 1 < CM) { bF[k + 1] += uF; bFh[k + 1] += uFh; bfr[k + 1] += ufr; bfhb[k + 1] += ufhb; }
+      else { nF = uF; nFh = uFh; nfr = ufr; nfhb = ufhb; }
+    }
+    fold1<G, CM>(bF, FT(0), nF, gl);
+    fold1<G, CM>(bFh, FT(0), nFh, gl);
+    fold1<G, CM>(bfr, FT(0), nfr, gl);
+    fold1<G, CM>(bfhb, FT(0), nfhb, gl);
+  }
+  // (f) face fluxes F = rJb u3c, Fh = F hb, fr = rJb g33, fhb = hb -> rho J and h of the centres f-1, f
+  {
+    FT pH = 0, pRJ = 0;
+#pragma unroll
+    for (int k = 0; k < CM; ++k) {
+      const int f = r0 + k;
+      if (!(f > 0 && f < Nv)) continue;
+      const FT rJb = (cprev(rJ, k, rJp) + rJ[k]) / FT(2), hb = fhb[k];
+      const FT Fb = bF[k] + bFh[k] * hb;
+      const FT hbb = bFh[k] * F[k] + bfhb[k];
+      const FT rJbb = Fb * (u3[k] * g33[k]) + bfr[k] * g33[k];
+      bU3[k] += Fb * rJb * g33[k];
+      bH[k] += hbb / FT(2);
+      bRJ[k] += rJbb / FT(2);
+      if (k >= 1) { bH[k - 1] += hbb / FT(2); bRJ[k - 1] += rJbb / FT(2); }
+      else { pH += hbb / FT(2); pRJ += rJbb / FT(2); }
+    }
+    fold1<G, CM>(bH, pH, FT(0), gl);
+    fold1<G, CM>(bRJ, pRJ, FT(0), gl);
+  }
+  // (g) centre diagnostics of U0
+  {
+    FT toNextU3 = 0;
+#pragma unroll
+    for (int k = 0; k < CM; ++k) {
+      if (r0 + k >= Nv) continue;
+      ThermoBar<FT> tb{};
+      tb.h = bH[k];
+      tb.Pi = bPI[k];
+      tb.thv = bTHV[k];
+      tb.thvr = bTHVR[k];
+      tb.phir = bPHIR[k];
+      FT rb_, reb, Kb;
+      thermo_vjp(P, H[0][k], H[3][k], K[k], phi[k], tb, rb_, reb, Kb);
+      bR0[k] += rb_ + Jc[k] * bRJ[k];
+      bRE0[k] += reb;
+      const FT Kt = Kb + bK[k];
+      bU1[k] += c1[k] * Kt;
+      bU2[k] += c2[k] * Kt;
+      bU3[k] += Kt * u3[k] * g33[k] / FT(2);
+      const FT cu = Kt * fnext(u3, k, u3n0) * fnext(g33, k, g33n0) / FT(2);
+      if (k + 1 < CM) bU3[k + 1] += cu; else toNextU3 = cu;
+    }
+    fold1<G, CM>(bU3, FT(0), toNextU3, gl);
+  }
+  // ---------------------------------------------------------------- cotangent of U^ and its distribution
+#pragma unroll
+  for (int k = 0; k < CM; ++k) {
+    const int v = r0 + k;
+    if (colv && v < Nv) {
+      const FT hb[4] = {bR0[k] - V.Tb_c[rb + k] * idtg, bU1[k] + V.Ub_c[cb + (size_t)sc + k],
+                        bU2[k] + V.Ub_c[cb + (size_t)2 * sc + k], bRE0[k] - V.Tb_c[rb + (size_t)sc + k] * idtg};
+#pragma unroll
+      for (int c = 0; c < 4; ++c) V.Yb_c[cb + (size_t)c * sc + k] += hb[c];
+      for (int j = 0; j < A.nsrc; ++j) {
+#pragma unroll
+        for (int c = 0; c < 4; ++c) V.Teb_c[j][cb + (size_t)c * sc + k] += A.ce[j] * hb[c];
+        if (j >= 1) {
+          V.Tib_c[j][rb + k] += A.ci[j] * hb[0];
+          V.Tib_c[j][rb + (size_t)sc + k] += A.ci[j] * hb[3];
+        }
+      }
+    }
+    if (colv && v < Nf) {
+      const bool inner = v > 0 && v < Nv;
+      const FT hb = bH4[k] + (inner ? bU3[k] : FT(0)) - V.Tb_f[fb + k] * idtg;
+      V.Yb_f[fb + k] += hb;
+      for (int j = 0; j < A.nsrc; ++j) {
+        V.Teb_f[j][fb + k] += A.ce[j] * hb;
+        if (j >= 1) V.Tib_f[j][fb + k] += A.ci[j] * hb;
+      }
+    }
+  }
+  col::group_sum1<G>(dal);
+  if (gl == 0 && colv) V.dalpha[col] += dal;
+}
+
+}  // namespace lp
+
 }  // namespace
 
 size_t col_vjp_scratch_words(int Nh, int Nv) { return (size_t)S_NUM * (Nv + 1) * (size_t)Nh * NN; }
@@ -568,7 +1129,20 @@ void launch_column_stage_vjp(const DevParams<FT> &P, const StageArgs<FT> &A, con
   V.scr = scr;
   V.dalpha = dalpha;
   const int ncols = P.Nh * NN;
-  k_col_stage_vjp<FT><<<(ncols + 127) / 128, 128, 0, s>>>(P, V);
+  // lane-parallel form by default; GBDYCORE_COLUMN_VJP=serial selects the one-thread-per-column form
+  static const bool serial = [] {
+    const char *e = getenv("GBDYCORE_COLUMN_VJP");
+    return e && e[0] == 's';
+  }();
+  if (serial) {
+    k_col_stage_vjp<FT><<<(ncols + 127) / 128, 128, 0, s>>>(P, V);
+    return;
+  }
+  auto grid = [&](int G) { return (ncols + 4 * (32 / G) - 1) / (4 * (32 / G)); };
+  if (P.Nf <= 16) lp::k_col_stage_vjp_g<FT, 8, 2><<<grid(8), 128, 0, s>>>(P, V);
+  else if (P.Nf <= 32) lp::k_col_stage_vjp_g<FT, 16, 2><<<grid(16), 128, 0, s>>>(P, V);
+  else if (P.Nf <= 64) lp::k_col_stage_vjp_g<FT, 32, 2><<<grid(32), 128, 0, s>>>(P, V);
+  else lp::k_col_stage_vjp_g<FT, 32, 4><<<grid(32), 128, 0, s>>>(P, V);
 }
 
 template void launch_column_stage_vjp<float>(const DevParams<float> &, const StageArgs<float> &, const float *,

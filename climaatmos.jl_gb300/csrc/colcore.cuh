@@ -345,5 +345,10 @@ __device__ __forceinline__ void group_sum(double (&ss)[3]) {
     for (int o = G / 2; o > 0; o >>= 1) ss[q] += __shfl_xor_sync(0xffffffffu, ss[q], o, G);
 }
 
+template <int G>
+__device__ __forceinline__ void group_sum1(double &v) {
+  for (int o = G / 2; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o, G);
+}
+
 }  // namespace col
 }  // namespace gb

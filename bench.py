@@ -196,6 +196,10 @@ def contract_bytes_per_step(cfg, fb=4):
     return (51 * S + 56 * P) * fb
 
 
+# ncu-measured DRAM traffic per launch on the production FP32 workload (bytes)
+NCU_TRAFFIC = {"k_passB": 200255744 + 80094720, "k_col_stage": 572394240 + 153260544}
+
+
 def measured_peak():
     try:
         m = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
@@ -254,8 +258,12 @@ def run_gb300(args):
     share = {kid: ktime[kid] * KERNELS[kid][2] for kid in ktime}
     dom = max(share, key=share.get)
     ach = algorithmic_bytes(cfg, dom) / (ktime[dom] * 1e-3) / 1e9
+    # DRAM bytes (read + write) of one launch from an ncu capture of this workload
+    traffic = NCU_TRAFFIC.get(KERNELS[dom][1].split()[0]) if cfg == workload() else None
     roof = {"kernel": KERNELS[dom][1], "bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s",
-            "frac": ach / peak, "peak_kind": peak_kind, "traffic": None,
+            "frac": ach / peak, "peak_kind": peak_kind, "traffic": traffic,
+            "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, one launch "
+                              "(profiles/k_passB_h30z63_fp32.md, profiles/k_col_stage_g_h30z63_fp32.md)",
             "algorithmic_bytes_per_launch": algorithmic_bytes(cfg, dom), "ms_per_launch": ktime[dom],
             "kernels": {KERNELS[k][1]: {"ms": ktime[k], "launches_per_step": KERNELS[k][2],
                                         "GBps": algorithmic_bytes(cfg, k) / (ktime[k] * 1e-3) / 1e9}

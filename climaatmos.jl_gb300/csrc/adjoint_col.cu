@@ -599,8 +599,15 @@ __device__ __forceinline__ void fold2(FT (&own)[CM], FT toPrev2, FT toPrev1, FT 
   if (gl > 0) { own[0] += c; own[1] += d; }
 }
 
+// FP32 is capped at 128 registers (four resident 128-thread CTAs per SM; 60 B of spills measured at
+// z_elem = 63), FP64 runs uncapped.
+template <class FT>
+struct VjpMinBlocks {
+  static constexpr int value = sizeof(FT) == 4 ? 4 : 1;
+};
+
 template <class FT, int G, int CM>
-__global__ void __launch_bounds__(128) k_col_stage_vjp_g(DevParams<FT> P, ColVjpArgs<FT> V) {
+__global__ void __launch_bounds__(128, VjpMinBlocks<FT>::value) k_col_stage_vjp_g(DevParams<FT> P, ColVjpArgs<FT> V) {
   const int lane = threadIdx.x & 31, gl = lane % G;
   const int col0 = (blockIdx.x * 4 + (threadIdx.x >> 5)) * (32 / G) + lane / G;
   const int ncols = P.Nh * NN;

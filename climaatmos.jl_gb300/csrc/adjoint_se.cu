@@ -15,6 +15,8 @@
 // shared memory.  The state cotangent is accumulated (+=) element by element:
 // each element owns its nodes, so there are no write conflicts; the DSS
 // transpose that precedes/follows is a separate kernel.
+#include <algorithm>
+
 #include "se_ops.cuh"
 
 namespace gb {
@@ -25,6 +27,12 @@ using namespace se;
 
 constexpr int AD_THREADS = 256;
 constexpr int AD_LEVELS = AD_THREADS / 4;
+// Resident CTAs per SM the pass B reverse is compiled for: two in FP32 (a
+// 128-register cap), one in FP64.
+template <class FT>
+struct AdMinBlocks {
+  static constexpr int value = sizeof(FT) == 4 ? 2 : 1;
+};
 
 template <class FT>
 __device__ __forceinline__ void load_slab(FT *dst, const FT *src, int n) {
@@ -120,19 +128,19 @@ __global__ void __launch_bounds__(AD_THREADS) k_passA_vjp(DevParams<FT> P, const
 }
 
 // ----------------------------------------------------------------------------- pass B^T
-// Shared memory (FT words): Y 64Nv, L 64Nv, Tb 64Nv (centre cotangent), F 16Nf,
-// Tbf 16Nf (u_3 tendency cotangent), geometry HG_N*16; centre scratch
+// Shared memory (FT words): Y 64Nv, F 16Nf, geometry HG_N*16 (the Laplacians
+// and the tendency cotangent are read from global memory); centre scratch
 // Kv, c1, c2, K, rho J, o3, a3 (7 x 16Nv), lower/upper face parts (2 x 16Nv);
 // face scratch X1, X2, and the face cotangents cc1, cc2, gK, l4, rJ, cv1, cv2,
 // u3 (10 x 16Nf).
 template <class FT>
 __host__ __device__ inline size_t passB_vjp_words(int Nv) {
   const size_t Nf = Nv + 1;
-  return 3 * 64 * (size_t)Nv + 2 * 16 * Nf + HG_N * 16 + 9 * 16 * (size_t)Nv + 10 * 16 * Nf;
+  return 64 * (size_t)Nv + 16 * Nf + HG_N * 16 + 9 * 16 * (size_t)Nv + 10 * 16 * Nf;
 }
 
 template <class FT>
-__global__ void __launch_bounds__(AD_THREADS) k_passB_vjp(DevParams<FT> P, const FT *__restrict__ Yc,
+__global__ void __launch_bounds__(AD_THREADS, AdMinBlocks<FT>::value) k_passB_vjp(DevParams<FT> P, const FT *__restrict__ Yc,
                                                           const FT *__restrict__ Yf, const FT *__restrict__ Lc,
                                                           const FT *__restrict__ Tbc, const FT *__restrict__ Tbf,
                                                           FT *__restrict__ Ybc, FT *__restrict__ Ybf,
@@ -140,8 +148,8 @@ __global__ void __launch_bounds__(AD_THREADS) k_passB_vjp(DevParams<FT> P, const
   extern __shared__ __align__(16) unsigned char sm_raw[];
   FT *sm = (FT *)sm_raw;
   const int Nv = P.Nv, Nf = P.Nf;
-  FT *sY = sm, *sL = sY + 64 * Nv, *sT = sL + 64 * Nv, *sF = sT + 64 * Nv, *sTf = sF + 16 * Nf;
-  FT *sG = sTf + 16 * Nf;
+  FT *sY = sm, *sF = sY + 64 * Nv;
+  FT *sG = sF + 16 * Nf;
   FT *sKv = sG + HG_N * 16, *sC1 = sKv + 16 * Nv, *sC2 = sC1 + 16 * Nv, *sK = sC2 + 16 * Nv;
   FT *sRJ = sK + 16 * Nv, *sL4 = sRJ + 16 * Nv, *sA3 = sL4 + 16 * Nv, *sLo = sA3 + 16 * Nv, *sHi = sLo + 16 * Nv;
   FT *sX1 = sHi + 16 * Nv, *sX2 = sX1 + 16 * Nf, *bCc1 = sX2 + 16 * Nf, *bCc2 = bCc1 + 16 * Nf;
@@ -155,11 +163,10 @@ __global__ void __launch_bounds__(AD_THREADS) k_passB_vjp(DevParams<FT> P, const
   double dnu = 0, dal = 0;
   for (int e = blockIdx.x; e < P.Nh; e += gridDim.x) {
     load_slab(sY, Yc + (size_t)e * 64 * Nv, 64 * Nv);
-    load_slab(sL, Lc + (size_t)e * 64 * Nv, 64 * Nv);
-    load_slab(sT, Tbc + (size_t)e * 64 * Nv, 64 * Nv);
     load_slab(sF, Yf + (size_t)e * 16 * Nf, 16 * Nf);
-    load_slab(sTf, Tbf + (size_t)e * 16 * Nf, 16 * Nf);
     load_slab(sG, P.hgeo + (size_t)e * HG_N * 16, HG_N * 16);
+    // the Laplacians and the tendency cotangent are read in place (L1-cached)
+    const FT *sL = Lc + (size_t)e * 64 * Nv, *sT = Tbc + (size_t)e * 64 * Nv, *sTf = Tbf + (size_t)e * 16 * Nf;
     __syncthreads();
     centre_from_faces<FT>(P, sF, nullptr, sKv);
     __syncthreads();
@@ -610,15 +617,34 @@ void configure_adjoint_se(int Nv) {
   cudaFuncSetAttribute(k_passB_vjp<FT>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes);
 }
 
+// Persistent grids: the resident CTAs of each kernel at its shared-memory size.
+template <class K>
+int resident_grid(K kern, size_t smem, int Nh) {
+  static int nsm = 0;
+  if (!nsm) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  }
+  int b = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kern, AD_THREADS, smem);
+  return std::max(1, std::min(Nh, nsm * std::max(1, b)));
+}
+
 template <class FT>
 void launch_passA_vjp(const DevParams<FT> &P, const FT *Yc, const FT *Yf, const FT *Lb, FT *Ybc, FT *Ybf, int grid,
                       cudaStream_t s) {
-  k_passA_vjp<FT><<<grid, AD_THREADS, passA_vjp_smem<FT>(P.Nv), s>>>(P, Yc, Yf, Lb, Ybc, Ybf);
+  (void)grid;
+  const size_t sm = passA_vjp_smem<FT>(P.Nv);
+  k_passA_vjp<FT><<<resident_grid(k_passA_vjp<FT>, sm, P.Nh), AD_THREADS, sm, s>>>(P, Yc, Yf, Lb, Ybc, Ybf);
 }
+// grid: the number of parameter-partial slots (CTAs) the caller allocated.
 template <class FT>
 void launch_passB_vjp(const DevParams<FT> &P, const FT *Yc, const FT *Yf, const FT *L, const FT *Tbc, const FT *Tbf,
                       FT *Ybc, FT *Ybf, FT *Lb, double *dpar, int grid, cudaStream_t s) {
-  k_passB_vjp<FT><<<grid, AD_THREADS, passB_vjp_smem<FT>(P.Nv), s>>>(P, Yc, Yf, L, Tbc, Tbf, Ybc, Ybf, Lb, dpar);
+  const size_t sm = passB_vjp_smem<FT>(P.Nv);
+  const int g = std::min(grid, resident_grid(k_passB_vjp<FT>, sm, P.Nh));
+  k_passB_vjp<FT><<<g, AD_THREADS, sm, s>>>(P, Yc, Yf, L, Tbc, Tbf, Ybc, Ybf, Lb, dpar);
 }
 
 #define INST(FT)                                                                                             \

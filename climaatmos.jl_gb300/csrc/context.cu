@@ -450,7 +450,7 @@ int ensure_adjoint(gb_ctx *ctx) {
   auto A = std::make_unique<typename Impl<FT>::Adjoint>();
   const size_t S = (I->NC + I->NF) * sizeof(FT), R = (I->NR + I->NF) * sizeof(FT);
   const int ncols = I->P.Nh * NN;
-  A->grid = std::min(I->P.Nh, nsm);
+  A->grid = std::min(I->P.Nh, 4 * nsm);  // parameter-partial slots: at most 4 resident CTAs per SM
   size_t &t = A->bytes;
   int r;
   if ((r = alloc_z<FT>(ctx, A->Ub, S, t)) || (r = alloc_z<FT>(ctx, A->Tb, S, t)) ||

@@ -130,4 +130,32 @@ function global_sums(Y, p)
     return out
 end
 
+# ---- reverse mode (the pullback halves of ChainRulesCore.rrule(solve!, ...)) ----
+
+"""Advance Y by n fused steps (gb_step with graph replay)."""
+solve!(Y, p, dt, n) = step!(Y, p, 0.0, dt, n)
+
+"""Forward half of the trajectory gradient: Y advances n steps, a checkpoint every `every`."""
+adjoint_forward!(Y, p, dt, n, every) =
+    check(p.gb, ccall((:gb_adjoint_forward, libgbdycore), Cint,
+        (Ptr{Cvoid}, GBFieldVec, Cdouble, Cdouble, Cint, Cint), p.gb.handle, fieldvec(Y), 0.0, dt, n, every))
+
+"""Pullback of the last adjoint_forward!: Ybar (dJ/dY_n in, dJ/dY_0 out); returns (dJ/dnu, dJ/drate)."""
+function adjoint_reverse!(Ybar, p)
+    d = zeros(Cdouble, 2)
+    peak = Ref{Csize_t}(0)
+    check(p.gb, ccall((:gb_adjoint_reverse, libgbdycore), Cint,
+        (Ptr{Cvoid}, GBFieldVec, Ptr{Cdouble}, Ref{Csize_t}), p.gb.handle, fieldvec(Ybar), d, peak))
+    return d[1], d[2]
+end
+
+"""Pullback of one step from Y: Ybar (cotangent of the next state in, of Y out)."""
+function step_vjp!(Ybar, Y, p, t, dt)
+    d = zeros(Cdouble, 2)
+    check(p.gb, ccall((:gb_step_vjp, libgbdycore), Cint,
+        (Ptr{Cvoid}, GBFieldVec, GBFieldVec, Cdouble, Cdouble, Ptr{Cdouble}), p.gb.handle, fieldvec(Ybar),
+        fieldvec(Y), t, dt, d))
+    return d[1], d[2]
+end
+
 end # module

@@ -249,21 +249,22 @@ __global__ void __launch_bounds__(SE_THREADS, SeMinBlocks<FT>::value) k_passB(De
           Trhoe[i] = -((dmh[i] + h[i] * dm[i] + F1[i] * ha[i] + F2[i] * hb[i]) / FT(2));
         }
       }
-      // u_h: -[grad(K + Phi - Phi_r) + cp_d (th' grad Pi + grad(th' Pi) - Pi grad th') / 2]
+      // u_h: -[grad(K + Phi - Phi_r) + cp_d (th' grad Pi + grad(th' Pi) - Pi grad th') / 2];
+      // the two plain gradients are taken as one, grad(K + Phi - Phi_r + cp_d th' Pi / 2)
       {
-        FT a1[4], a2[4], b1[4], b2[4], e1[4], e2[4], f1[4], f2[4];
-        d1(P, tmp, a1);
-        d2(R, tmp, a2);
+        FT a1[4], a2[4], b1[4], b2[4], f1[4], f2[4], g[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) g[i] = tmp[i] + P.cpd * tp[i] / FT(2);
+        d1(P, g, a1);
+        d2(R, g, a2);
         d1(P, Pi, b1);
         d2(R, Pi, b2);
-        d1(P, tp, e1);
-        d2(R, tp, e2);
         d1(P, thp, f1);
         d2(R, thp, f2);
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
-          Tu1[i] = -(a1[i] + P.cpd * (thp[i] * b1[i] + e1[i] - Pi[i] * f1[i]) / FT(2));
-          Tu2[i] = -(a2[i] + P.cpd * (thp[i] * b2[i] + e2[i] - Pi[i] * f2[i]) / FT(2));
+          Tu1[i] = -(a1[i] + P.cpd * (thp[i] * b1[i] - Pi[i] * f1[i]) / FT(2));
+          Tu2[i] = -(a2[i] + P.cpd * (thp[i] * b2[i] - Pi[i] * f2[i]) / FT(2));
         }
       }
       // hyperdiffusion: nu (div_damp C123(wgrad div L) - C123(wcurl C123(curl L)))

@@ -15,13 +15,15 @@ namespace se {
 template <class FT>
 struct Row {
   int j;
-  FT dB[NQ], tB[NQ];  // D[j][k], D[k][j]
+  // xi^2 coefficients ordered by partner row j ^ m (m = 0: the thread's own row):
+  // dX[m] = D[j][j ^ m], tX[m] = D[j ^ m][j]
+  FT dX[NQ], tX[NQ];
   __device__ void init(const DevParams<FT> &P, int jj) {
     j = jj;
 #pragma unroll
-    for (int k = 0; k < NQ; ++k) {
-      dB[k] = P.D[j * NQ + k];
-      tB[k] = P.D[k * NQ + j];
+    for (int m = 0; m < NQ; ++m) {
+      dX[m] = P.D[j * NQ + (j ^ m)];
+      tX[m] = P.D[(j ^ m) * NQ + j];
     }
   }
 };
@@ -48,21 +50,22 @@ __device__ __forceinline__ void t1(const DevParams<FT> &P, const FT (&f)[4], FT 
     o[i] = s;
   }
 }
-// o[i] = sum_k C[k] f(i, row k): the rows are gathered from the level's 4-lane group
+// o[i] = sum_m C[m] f(i, row j ^ m): the thread's own row plus three xor
+// partners of its level's 4-lane group (12 shuffles for the 4 outputs)
 template <class FT>
 __device__ __forceinline__ void across(const FT (&C)[NQ], const FT (&f)[4], FT (&o)[4]) {
 #pragma unroll
   for (int i = 0; i < NQ; ++i) {
-    FT s = 0;
+    FT s = C[0] * f[i];
 #pragma unroll
-    for (int k = 0; k < NQ; ++k) s += C[k] * shfl(f[i], k, 4);
+    for (int m = 1; m < NQ; ++m) s += C[m] * __shfl_xor_sync(0xffffffffu, f[i], m, 4);
     o[i] = s;
   }
 }
 template <class FT>
-__device__ __forceinline__ void d2(const Row<FT> &R, const FT (&f)[4], FT (&o)[4]) { across(R.dB, f, o); }
+__device__ __forceinline__ void d2(const Row<FT> &R, const FT (&f)[4], FT (&o)[4]) { across(R.dX, f, o); }
 template <class FT>
-__device__ __forceinline__ void t2(const Row<FT> &R, const FT (&f)[4], FT (&o)[4]) { across(R.tB, f, o); }
+__device__ __forceinline__ void t2(const Row<FT> &R, const FT (&f)[4], FT (&o)[4]) { across(R.tX, f, o); }
 
 // Per-node horizontal geometry of the thread's row (loaded once per element).
 template <class FT>

@@ -29,9 +29,14 @@ struct PassALayout {
   }
 };
 
+// Level-major scratch rows of pass B: field f of level v, node n at
+// (f Nv + v) 16 + n, so the thread of (level v, row j) reads or writes its
+// four nodes as one 16-byte row vector (bank-conflict free).
+enum PassBScratch { SB_C1 = 0, SB_C2, SB_K, SB_RJ, SB_L4, SB_U1, SB_U2, SB_Q1, SB_Q2, SB_N };
+
 template <class FT>
 struct PassBLayout {
-  size_t y[2], f[2], g[2], lap[2], kv, c1, c2, k, rj, l4, cr1, cr2, x1, x2, out, outf, bar, total;
+  size_t y[2], f[2], g[2], lap[2], s, x1, x2, out, outf, bar, total;
   __host__ __device__ PassBLayout(int Nv, int nbuf) {
     const int Nf = Nv + 1;
     size_t o = 0;
@@ -45,15 +50,8 @@ struct PassBLayout {
         y[b] = y[0]; f[b] = f[0]; g[b] = g[0]; lap[b] = lap[0];
       }
     }
-    kv = o; o += align16(sizeof(FT) * 16 * Nv);
-    c1 = o; o += align16(sizeof(FT) * 16 * Nv);
-    c2 = o; o += align16(sizeof(FT) * 16 * Nv);
-    k = o; o += align16(sizeof(FT) * 16 * Nv);
-    rj = o; o += align16(sizeof(FT) * 16 * Nv);
-    l4 = o; o += align16(sizeof(FT) * 16 * Nv);
-    cr1 = o; o += align16(sizeof(FT) * 16 * Nv);
-    cr2 = o; o += align16(sizeof(FT) * 16 * Nv);
-    x1 = o; o += align16(sizeof(FT) * 16 * Nf);
+    s = o; o += align16(sizeof(FT) * SB_N * 16 * Nv);
+    x1 = o; o += align16(sizeof(FT) * 16 * Nf);   // face rows [Nf][16]
     x2 = o; o += align16(sizeof(FT) * 16 * Nf);
     out = o; o += align16(sizeof(FT) * 64 * Nv);
     outf = o; o += align16(sizeof(FT) * 16 * Nf);

@@ -180,16 +180,15 @@ __global__ void __launch_bounds__(SE_THREADS, SeMinBlocks<FT>::value) k_passB(De
   FT *sFb[2] = {(FT *)(sm + Lo.f[0]), (FT *)(sm + Lo.f[1])};
   FT *sGb[2] = {(FT *)(sm + Lo.g[0]), (FT *)(sm + Lo.g[1])};
   FT *sLb[2] = {(FT *)(sm + Lo.lap[0]), (FT *)(sm + Lo.lap[1])};
-  FT *sKv = (FT *)(sm + Lo.kv);
-  FT *sC1 = (FT *)(sm + Lo.c1), *sC2 = (FT *)(sm + Lo.c2), *sK = (FT *)(sm + Lo.k), *sRJ = (FT *)(sm + Lo.rj);
-  FT *sL4 = (FT *)(sm + Lo.l4), *sO = (FT *)(sm + Lo.out), *sOf = (FT *)(sm + Lo.outf);
-  FT *sCr1 = (FT *)(sm + Lo.cr1), *sCr2 = (FT *)(sm + Lo.cr2);
-  FT *sX1 = (FT *)(sm + Lo.x1), *sX2 = (FT *)(sm + Lo.x2);
+  FT *sS = (FT *)(sm + Lo.s), *sX1 = (FT *)(sm + Lo.x1), *sX2 = (FT *)(sm + Lo.x2);
+  FT *sO = (FT *)(sm + Lo.out), *sOf = (FT *)(sm + Lo.outf);
   uint64_t *bar = (uint64_t *)(sm + Lo.bar);
   init_bars(bar);
   int e = blockIdx.x;
   if (threadIdx.x == 0 && e < P.Nh) issue_slab<FT>(P, &bar[0], e, sYb[0], sFb[0], sGb[0], sLb[0], Yc, Yf, Lin);
   const int j = threadIdx.x & 3, vl = threadIdx.x >> 2;
+  // the thread's row of scratch field f at level (or face) v
+  auto row = [&](FT *base, int f, int v) { return base + ((size_t)f * Nv + v) * NN + NQ * j; };
   Row<FT> R;
   R.init(P, j);
   for (int it = 0; e < P.Nh; ++it, e += gridDim.x) {
@@ -197,11 +196,10 @@ __global__ void __launch_bounds__(SE_THREADS, SeMinBlocks<FT>::value) k_passB(De
     if (!begin_element<FT>(P, bar, nbuf, it, e, sYb, sFb, sGb, sLb, true, Yc, Yf, Lin, b)) break;
     const FT *sY = pick(b, sYb[0], sYb[1]), *sF = pick(b, sFb[0], sFb[1]), *sG = pick(b, sGb[0], sGb[1]);
     const FT *sL = pick(b, sLb[0], sLb[1]);
-    centre_from_faces<FT>(P, sF, nullptr, sKv);
-    __syncthreads();
     RowGeo<FT> g;
     g.load(sG, P, j);
-    // ---- P1: centre-level horizontal work
+    // ---- P1: centre-level horizontal work; per-level results go to the
+    // level-major scratch rows for the face pass
     for (int v0 = 0; v0 < Nv; v0 += SE_LEVELS) {
       const int v = min(v0 + vl, Nv - 1);
       const bool act = v0 + vl < Nv;
@@ -209,17 +207,23 @@ __global__ void __launch_bounds__(SE_THREADS, SeMinBlocks<FT>::value) k_passB(De
       const FT idz = P.levc[LC_IDZ * Nv + v];
       s.set(g, P.levc[LC_R2 * Nv + v], P.levc[LC_IR2 * Nv + v], P.levc[LC_DZ * Nv + v], idz);
       const FT Phi = P.levc[LC_PHI * Nv + v];
+      const FT g3a = P.levf[LF_G33 * Nf + v], g3b = P.levf[LF_G33 * Nf + v + 1];
       FT rho[4], u1[4], u2[4], c1[4], c2[4], K[4], h[4], Pi[4], thp[4], tmp[4], tp[4];
 #pragma unroll
       for (int i = 0; i < 4; ++i) {
-        const int q = (NQ * j + i) * Nv + v;
+        const int n = NQ * j + i;
+        const int q = n * Nv + v;
         rho[i] = sY[q];
         u1[i] = sY[16 * Nv + q];
         u2[i] = sY[32 * Nv + q];
         const FT gu0 = g.gu0[i] * s.ir2, gu1 = g.gu1[i] * s.ir2, gu2 = g.gu2[i] * s.ir2;
         c1[i] = gu0 * u1[i] + gu1 * u2[i];
         c2[i] = gu1 * u1[i] + gu2 * u2[i];
-        K[i] = (u1[i] * c1[i] + u2[i] * c2[i] + sKv[q]) / FT(2);
+        // face part of K, I^c(u_3 u^3), with u_3 = 0 on the boundary faces
+        const FT fa = v == 0 ? FT(0) : sF[n * Nf + v];
+        const FT fb = v + 1 == Nv ? FT(0) : sF[n * Nf + v + 1];
+        const FT kv = (fa * (fa * g3a) + fb * (fb * g3b)) / FT(2);
+        K[i] = (u1[i] * c1[i] + u2[i] * c2[i] + kv) / FT(2);
         Thermo<FT> th;
         thermo(P, rho[i], sY[48 * Nv + q], K[i], Phi, th);
         h[i] = th.h;
@@ -252,11 +256,11 @@ __global__ void __launch_bounds__(SE_THREADS, SeMinBlocks<FT>::value) k_passB(De
       // u_h: -[grad(K + Phi - Phi_r) + cp_d (th' grad Pi + grad(th' Pi) - Pi grad th') / 2];
       // the two plain gradients are taken as one, grad(K + Phi - Phi_r + cp_d th' Pi / 2)
       {
-        FT a1[4], a2[4], b1[4], b2[4], f1[4], f2[4], g[4];
+        FT a1[4], a2[4], b1[4], b2[4], f1[4], f2[4], gg[4];
 #pragma unroll
-        for (int i = 0; i < 4; ++i) g[i] = tmp[i] + P.cpd * tp[i] / FT(2);
-        d1(P, g, a1);
-        d2(R, g, a2);
+        for (int i = 0; i < 4; ++i) gg[i] = tmp[i] + P.cpd * tp[i] / FT(2);
+        d1(P, gg, a1);
+        d2(R, gg, a2);
         d1(P, Pi, b1);
         d2(R, Pi, b2);
         d1(P, thp, f1);
@@ -312,23 +316,29 @@ __global__ void __launch_bounds__(SE_THREADS, SeMinBlocks<FT>::value) k_passB(De
         for (int i = 0; i < 4; ++i) om[i] = (-ta[i] + tb[i]) * s.iWJ[i];
       }
       if (act) {
+        const FT beta = P.levc[LC_BETA * Nv + v];
+        FT rJ[4], Q1[4], Q2[4];
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
           const int n = NQ * j + i;
           const int q = n * Nv + v;
           const FT a3 = sG[HG_F3 * NN + n] * idz + om[i];
           sO[q] = Trho[i];
-          sO[16 * Nv + q] = Tu1[i];
-          sO[32 * Nv + q] = Tu2[i];
           sO[48 * Nv + q] = Trhoe[i];
-          sC1[q] = c1[i];
-          sC2[q] = c2[i];
-          sK[q] = K[i];
-          sRJ[q] = rho[i] * s.J[i];
-          sL4[q] = o3[i];
-          sCr1[q] = s.J[i] * (-a3 * c2[i]);
-          sCr2[q] = s.J[i] * (a3 * c1[i]);
+          rJ[i] = rho[i] * s.J[i];
+          // u_h tendency less the face cross products (added in P3) and the sponge
+          Q1[i] = (Tu1[i] - s.J[i] * (-a3 * c2[i])) - beta * u1[i];
+          Q2[i] = (Tu2[i] - s.J[i] * (a3 * c1[i])) - beta * u2[i];
         }
+        st_row(row(sS, SB_C1, v), c1);
+        st_row(row(sS, SB_C2, v), c2);
+        st_row(row(sS, SB_K, v), K);
+        st_row(row(sS, SB_RJ, v), rJ);
+        st_row(row(sS, SB_L4, v), o3);
+        st_row(row(sS, SB_U1, v), u1);
+        st_row(row(sS, SB_U2, v), u2);
+        st_row(row(sS, SB_Q1, v), Q1);
+        st_row(row(sS, SB_Q2, v), Q2);
       }
     }
     __syncthreads();
@@ -348,56 +358,79 @@ __global__ void __launch_bounds__(SE_THREADS, SeMinBlocks<FT>::value) k_passB(De
       FT ta[4], tb[4];
       t2(R, Wu, tb);
       t1(P, Wu, ta);
+      // the levels below and above the face (both the adjacent level on a boundary face)
       const int va = k > 0 ? k - 1 : 0, vb = k < Nv ? k : Nv - 1;
       if (act) {
+        FT C1a[4], C1b[4], C2a[4], C2b[4], Ka[4], Kb[4], Ra[4], Rb[4], La[4], Lb[4], U1a[4], U1b[4], U2a[4], U2b[4];
+        ld_row(row(sS, SB_C1, va), C1a);
+        ld_row(row(sS, SB_C1, vb), C1b);
+        ld_row(row(sS, SB_C2, va), C2a);
+        ld_row(row(sS, SB_C2, vb), C2b);
+        ld_row(row(sS, SB_K, va), Ka);
+        ld_row(row(sS, SB_K, vb), Kb);
+        ld_row(row(sS, SB_RJ, va), Ra);
+        ld_row(row(sS, SB_RJ, vb), Rb);
+        ld_row(row(sS, SB_L4, va), La);
+        ld_row(row(sS, SB_L4, vb), Lb);
+        ld_row(row(sS, SB_U1, va), U1a);
+        ld_row(row(sS, SB_U1, vb), U1b);
+        ld_row(row(sS, SB_U2, va), U2a);
+        ld_row(row(sS, SB_U2, vb), U2b);
+        FT X1[4], X2[4];
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
           const int n = NQ * j + i;
-          const int qa = n * Nv + va, qb = n * Nv + vb;
           const FT Jf = g.Jh[i] * r2 * dzf;
           const FT iJf = g.iJh[i] * ir2f * idzf, iWJf = g.iW[i] * iJf;
           const FT w1 = -tb[i] * iWJf, w2 = ta[i] * iWJf;
           FT cv1 = 0, cv2 = 0, gK = 0, cc1, cc2, l4, rJ;
           if (inner) {
-            cv1 = -(sY[32 * Nv + qb] - sY[32 * Nv + qa]) * iJf;
-            cv2 = (sY[16 * Nv + qb] - sY[16 * Nv + qa]) * iJf;
-            cc1 = (sC1[qa] + sC1[qb]) / FT(2);
-            cc2 = (sC2[qa] + sC2[qb]) / FT(2);
-            gK = sK[qb] - sK[qa];
-            const FT wa = sRJ[qa], wb = sRJ[qb];
-            l4 = gdiv(wa * sL4[qa] + wb * sL4[qb], wa + wb);
-            rJ = (wa + wb) / FT(2);
+            cv1 = -(U2b[i] - U2a[i]) * iJf;
+            cv2 = (U1b[i] - U1a[i]) * iJf;
+            cc1 = (C1a[i] + C1b[i]) / FT(2);
+            cc2 = (C2a[i] + C2b[i]) / FT(2);
+            gK = Kb[i] - Ka[i];
+            l4 = gdiv(Ra[i] * La[i] + Rb[i] * Lb[i], Ra[i] + Rb[i]);
+            rJ = (Ra[i] + Rb[i]) / FT(2);
           } else {
-            const int qq = k == 0 ? qb : qa;
-            cc1 = sC1[qq];
-            cc2 = sC2[qq];
-            l4 = sL4[qq];
-            rJ = sRJ[qq];
+            cc1 = C1a[i];
+            cc2 = C2a[i];
+            l4 = La[i];
+            rJ = Ra[i];
           }
           const FT fo1 = sG[HG_FH1 * NN + n] * rinv + cv1 + w1, fo2 = sG[HG_FH2 * NN + n] * rinv + cv2 + w2;
           const FT b3 = rJ * (u3[i] * g33);
           FT T3 = -(P.nu_v * l4);
           T3 -= Jf * (fo1 * cc2 - fo2 * cc1) + gK;
-          sX1[n * Nf + k] = Jf * (fo2 * b3);
-          sX2[n * Nf + k] = Jf * (-fo1 * b3);
+          X1[i] = Jf * (fo2 * b3);
+          X2[i] = Jf * (-fo1 * b3);
           sOf[n * Nf + k] = T3;
         }
+        st_row(sX1 + (size_t)k * NN + NQ * j, X1);
+        st_row(sX2 + (size_t)k * NN + NQ * j, X2);
       }
     }
     __syncthreads();
-    // ---- P3: centre u_h part of the face cross products and the sponge (level-fastest)
-    for (int idx = threadIdx.x; idx < NN * Nv; idx += blockDim.x) {
-      const int nn = idx / Nv, v = idx - nn * Nv;
-      const FT irJ = grcp(sRJ[idx]);
-      const FT t1v = (sX1[nn * Nf + v] + sX1[nn * Nf + v + 1]) / FT(2) * irJ + sCr1[idx];
-      const FT t2v = (sX2[nn * Nf + v] + sX2[nn * Nf + v + 1]) / FT(2) * irJ + sCr2[idx];
-      const FT beta = P.levc[LC_BETA * Nv + v];
-      FT a = sO[16 * Nv + idx] - t1v;
-      FT bb = sO[32 * Nv + idx] - t2v;
-      a -= beta * sY[16 * Nv + idx];
-      bb -= beta * sY[32 * Nv + idx];
-      sO[16 * Nv + idx] = a;
-      sO[32 * Nv + idx] = bb;
+    // ---- P3: centre u_h part of the face cross products (the sponge is in Q)
+    for (int v0 = 0; v0 < Nv; v0 += SE_LEVELS) {
+      const int v = v0 + vl;
+      if (v < Nv) {
+        FT Xa1[4], Xb1[4], Xa2[4], Xb2[4], rJ[4], Q1[4], Q2[4];
+        ld_row(sX1 + (size_t)v * NN + NQ * j, Xa1);
+        ld_row(sX1 + (size_t)(v + 1) * NN + NQ * j, Xb1);
+        ld_row(sX2 + (size_t)v * NN + NQ * j, Xa2);
+        ld_row(sX2 + (size_t)(v + 1) * NN + NQ * j, Xb2);
+        ld_row(row(sS, SB_RJ, v), rJ);
+        ld_row(row(sS, SB_Q1, v), Q1);
+        ld_row(row(sS, SB_Q2, v), Q2);
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          const int q = (NQ * j + i) * Nv + v;
+          const FT irJ = grcp(rJ[i]);
+          sO[16 * Nv + q] = Q1[i] - (Xa1[i] + Xb1[i]) / FT(2) * irJ;
+          sO[32 * Nv + q] = Q2[i] - (Xa2[i] + Xb2[i]) / FT(2) * irJ;
+        }
+      }
     }
     fence_proxy_async();
     __syncthreads();

@@ -67,6 +67,24 @@ __device__ __forceinline__ void d2(const Row<FT> &R, const FT (&f)[4], FT (&o)[4
 template <class FT>
 __device__ __forceinline__ void t2(const Row<FT> &R, const FT (&f)[4], FT (&o)[4]) { across(R.tX, f, o); }
 
+// The four nodes of a row as one 16-byte vector access (two in FP64);
+// p must be 16-byte aligned.
+__device__ __forceinline__ void st_row(float *p, const float (&a)[4]) {
+  *reinterpret_cast<float4 *>(p) = make_float4(a[0], a[1], a[2], a[3]);
+}
+__device__ __forceinline__ void st_row(double *p, const double (&a)[4]) {
+  reinterpret_cast<double2 *>(p)[0] = make_double2(a[0], a[1]);
+  reinterpret_cast<double2 *>(p)[1] = make_double2(a[2], a[3]);
+}
+__device__ __forceinline__ void ld_row(const float *p, float (&a)[4]) {
+  const float4 t = *reinterpret_cast<const float4 *>(p);
+  a[0] = t.x; a[1] = t.y; a[2] = t.z; a[3] = t.w;
+}
+__device__ __forceinline__ void ld_row(const double *p, double (&a)[4]) {
+  const double2 t0 = reinterpret_cast<const double2 *>(p)[0], t1 = reinterpret_cast<const double2 *>(p)[1];
+  a[0] = t0.x; a[1] = t0.y; a[2] = t1.x; a[3] = t1.y;
+}
+
 // Per-node horizontal geometry of the thread's row (loaded once per element).
 template <class FT>
 struct RowGeo {

@@ -8,7 +8,7 @@ namespace gb {
 // input slabs are double-buffered (nbuf = 2) when they fit, else single.
 template <class FT>
 struct PassALayout {
-  size_t y[2], f[2], g[2], u3, kv, out, bar, total;
+  size_t y[2], f[2], g[2], out, bar, total;
   __host__ __device__ PassALayout(int Nv, int nbuf) {
     const int Nf = Nv + 1;
     size_t o = 0;
@@ -21,8 +21,6 @@ struct PassALayout {
         y[b] = y[0]; f[b] = f[0]; g[b] = g[0];
       }
     }
-    u3 = o; o += align16(sizeof(FT) * 16 * Nv);
-    kv = o; o += align16(sizeof(FT) * 16 * Nv);
     out = o; o += align16(sizeof(FT) * 64 * Nv);
     bar = o; o += 16;
     total = o;

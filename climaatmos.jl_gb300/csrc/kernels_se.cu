@@ -95,43 +95,48 @@ __global__ void __launch_bounds__(SE_THREADS, SeMinBlocks<FT>::value) k_passA(De
                                                          const FT *__restrict__ Yf, FT *__restrict__ Lout) {
   extern __shared__ __align__(128) unsigned char sm[];
   const int Nv = P.Nv;
+  const int Nf = P.Nf;
   const PassALayout<FT> Lo(Nv, nbuf);
   FT *sYb[2] = {(FT *)(sm + Lo.y[0]), (FT *)(sm + Lo.y[1])};
   FT *sFb[2] = {(FT *)(sm + Lo.f[0]), (FT *)(sm + Lo.f[1])};
   FT *sGb[2] = {(FT *)(sm + Lo.g[0]), (FT *)(sm + Lo.g[1])};
-  FT *sU3 = (FT *)(sm + Lo.u3), *sKv = (FT *)(sm + Lo.kv), *sO = (FT *)(sm + Lo.out);
+  FT *sO = (FT *)(sm + Lo.out);
   uint64_t *bar = (uint64_t *)(sm + Lo.bar);
   init_bars(bar);
   int e = blockIdx.x;
   if (threadIdx.x == 0 && e < P.Nh) issue_slab<FT>(P, &bar[0], e, sYb[0], sFb[0], sGb[0], nullptr, Yc, Yf, nullptr);
-  const int j = threadIdx.x & 3, vl = threadIdx.x >> 2;
+  const int j = threadIdx.x & 3, vs = level_slot(threadIdx.x >> 2);
   Row<FT> R;
   R.init(P, j);
   for (int it = 0; e < P.Nh; ++it, e += gridDim.x) {
     int b;
     if (!begin_element<FT>(P, bar, nbuf, it, e, sYb, sFb, sGb, sGb, false, Yc, Yf, nullptr, b)) break;
     const FT *sY = pick(b, sYb[0], sYb[1]), *sF = pick(b, sFb[0], sFb[1]), *sG = pick(b, sGb[0], sGb[1]);
-    centre_from_faces(P, sF, sU3, sKv);
-    __syncthreads();
     RowGeo<FT> g;
     g.load(sG, P, j);
     for (int v0 = 0; v0 < Nv; v0 += SE_LEVELS) {
-      const int v = min(v0 + vl, Nv - 1);
-      const bool act = v0 + vl < Nv;
+      const int v = min(v0 + vs, Nv - 1);
+      const bool act = v0 + vs < Nv;
       LevRow<FT> s;
       s.set(g, P.levc[LC_R2 * Nv + v], P.levc[LC_IR2 * Nv + v], P.levc[LC_DZ * Nv + v], P.levc[LC_IDZ * Nv + v]);
       const FT Phi = P.levc[LC_PHI * Nv + v];
+      const FT g3a = P.levf[LF_G33 * Nf + v], g3b = P.levf[LF_G33 * Nf + v + 1];
       FT u1[4], u2[4], ub3[4], sd[4];
 #pragma unroll
       for (int i = 0; i < 4; ++i) {
-        const int q = (NQ * j + i) * Nv + v;
+        const int n = NQ * j + i;
+        const int q = n * Nv + v;
         const FT rho = sY[q], rhoe = sY[48 * Nv + q];
         u1[i] = sY[16 * Nv + q];
         u2[i] = sY[32 * Nv + q];
-        ub3[i] = sU3[q];
+        // u_bar_3 = I^c(u_3) and the face part of K, with u_3 = 0 on the boundary faces
+        const FT fa = v == 0 ? FT(0) : sF[n * Nf + v];
+        const FT fb = v + 1 == Nv ? FT(0) : sF[n * Nf + v + 1];
+        ub3[i] = (fa + fb) / FT(2);
+        const FT kv = (fa * (fa * g3a) + fb * (fb * g3b)) / FT(2);
         const FT gu0 = g.gu0[i] * s.ir2, gu1 = g.gu1[i] * s.ir2, gu2 = g.gu2[i] * s.ir2;
         const FT c1 = gu0 * u1[i] + gu1 * u2[i], c2 = gu1 * u1[i] + gu2 * u2[i];
-        const FT K = (u1[i] * c1 + u2[i] * c2 + sKv[q]) / FT(2);
+        const FT K = (u1[i] * c1 + u2[i] * c2 + kv) / FT(2);
         Thermo<FT> th;
         thermo(P, rho, rhoe, K, Phi, th);
         sd[i] = P.cpd * (th.T - P.T0) + Phi - sd_r(P, th.Pi, th.phir);
@@ -186,7 +191,7 @@ __global__ void __launch_bounds__(SE_THREADS, SeMinBlocks<FT>::value) k_passB(De
   init_bars(bar);
   int e = blockIdx.x;
   if (threadIdx.x == 0 && e < P.Nh) issue_slab<FT>(P, &bar[0], e, sYb[0], sFb[0], sGb[0], sLb[0], Yc, Yf, Lin);
-  const int j = threadIdx.x & 3, vl = threadIdx.x >> 2;
+  const int j = threadIdx.x & 3, vl = threadIdx.x >> 2, vs = level_slot(vl);
   // the thread's row of scratch field f at level (or face) v
   auto row = [&](FT *base, int f, int v) { return base + ((size_t)f * Nv + v) * NN + NQ * j; };
   Row<FT> R;
@@ -201,8 +206,8 @@ __global__ void __launch_bounds__(SE_THREADS, SeMinBlocks<FT>::value) k_passB(De
     // ---- P1: centre-level horizontal work; per-level results go to the
     // level-major scratch rows for the face pass
     for (int v0 = 0; v0 < Nv; v0 += SE_LEVELS) {
-      const int v = min(v0 + vl, Nv - 1);
-      const bool act = v0 + vl < Nv;
+      const int v = min(v0 + vs, Nv - 1);
+      const bool act = v0 + vs < Nv;
       LevRow<FT> s;
       const FT idz = P.levc[LC_IDZ * Nv + v];
       s.set(g, P.levc[LC_R2 * Nv + v], P.levc[LC_IR2 * Nv + v], P.levc[LC_DZ * Nv + v], idz);
@@ -413,7 +418,7 @@ __global__ void __launch_bounds__(SE_THREADS, SeMinBlocks<FT>::value) k_passB(De
     __syncthreads();
     // ---- P3: centre u_h part of the face cross products (the sponge is in Q)
     for (int v0 = 0; v0 < Nv; v0 += SE_LEVELS) {
-      const int v = v0 + vl;
+      const int v = v0 + vs;
       if (v < Nv) {
         FT Xa1[4], Xb1[4], Xa2[4], Xb2[4], rJ[4], Q1[4], Q2[4];
         ld_row(sX1 + (size_t)v * NN + NQ * j, Xa1);

@@ -67,6 +67,16 @@ __device__ __forceinline__ void d2(const Row<FT> &R, const FT (&f)[4], FT (&o)[4
 template <class FT>
 __device__ __forceinline__ void t2(const Row<FT> &R, const FT (&f)[4], FT (&o)[4]) { across(R.tX, f, o); }
 
+// Level slot of the 4-lane group vl (0..63) of a 256-thread slab sweep: warp
+// w takes levels 4 (w mod 4) + 32 (w / 4) + {0..3, 16..19}.  A [node][level]
+// slab with an odd level count Nv is then read and written without bank
+// conflicts: node rows are 4 Nv = 4 (Nv mod 8) banks apart, and the shifts of
+// the four rows carry the two 4-bank chunks onto all eight.
+__device__ __forceinline__ int level_slot(int vl) {
+  const int w = vl >> 3, g = vl & 7;
+  return ((w & 3) << 2) + ((w >> 2) << 5) + (g < 4 ? g : g + 12);
+}
+
 // The four nodes of a row as one 16-byte vector access (two in FP64);
 // p must be 16-byte aligned.
 __device__ __forceinline__ void st_row(float *p, const float (&a)[4]) {

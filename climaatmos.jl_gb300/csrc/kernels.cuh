@@ -34,7 +34,7 @@ enum PassBScratch { SB_C1 = 0, SB_C2, SB_K, SB_RJ, SB_L4, SB_U1, SB_U2, SB_Q1, S
 
 template <class FT>
 struct PassBLayout {
-  size_t y[2], f[2], g[2], lap[2], s, x1, x2, out, outf, bar, total;
+  size_t y[2], f[2], g[2], lap[2], s, x1, x2, out, outf, w, bar, total;
   __host__ __device__ PassBLayout(int Nv, int nbuf) {
     const int Nf = Nv + 1;
     size_t o = 0;
@@ -53,6 +53,7 @@ struct PassBLayout {
     x2 = o; o += align16(sizeof(FT) * 16 * Nf);
     out = o; o += align16(sizeof(FT) * 64 * Nv);
     outf = o; o += align16(sizeof(FT) * 16 * Nf);
+    w = o; o += align16(sizeof(FT) * 2 * 16);     // GLL weights W, 1/W
     bar = o; o += 16;
     total = o;
   }

@@ -186,8 +186,12 @@ __global__ void __launch_bounds__(SE_THREADS, SeMinBlocks<FT>::value) k_passB(De
   FT *sGb[2] = {(FT *)(sm + Lo.g[0]), (FT *)(sm + Lo.g[1])};
   FT *sLb[2] = {(FT *)(sm + Lo.lap[0]), (FT *)(sm + Lo.lap[1])};
   FT *sS = (FT *)(sm + Lo.s), *sX1 = (FT *)(sm + Lo.x1), *sX2 = (FT *)(sm + Lo.x2);
-  FT *sO = (FT *)(sm + Lo.out), *sOf = (FT *)(sm + Lo.outf);
+  FT *sO = (FT *)(sm + Lo.out), *sOf = (FT *)(sm + Lo.outf), *sW = (FT *)(sm + Lo.w);
   uint64_t *bar = (uint64_t *)(sm + Lo.bar);
+  if (threadIdx.x < NN) {
+    sW[threadIdx.x] = P.W[threadIdx.x];
+    sW[NN + threadIdx.x] = P.iW[threadIdx.x];
+  }
   init_bars(bar);
   int e = blockIdx.x;
   if (threadIdx.x == 0 && e < P.Nh) issue_slab<FT>(P, &bar[0], e, sYb[0], sFb[0], sGb[0], sLb[0], Yc, Yf, Lin);
@@ -201,50 +205,97 @@ __global__ void __launch_bounds__(SE_THREADS, SeMinBlocks<FT>::value) k_passB(De
     if (!begin_element<FT>(P, bar, nbuf, it, e, sYb, sFb, sGb, sLb, true, Yc, Yf, Lin, b)) break;
     const FT *sY = pick(b, sYb[0], sYb[1]), *sF = pick(b, sFb[0], sFb[1]), *sG = pick(b, sGb[0], sGb[1]);
     const FT *sL = pick(b, sLb[0], sLb[1]);
-    RowGeo<FT> g;
-    g.load(sG, P, j);
-    // ---- P1: centre-level horizontal work; per-level results go to the
-    // level-major scratch rows for the face pass
+    const SlabGeo<FT> g{sG + NQ * j, sW + NQ * j};
+    // ---- P1: centre-level horizontal work, ordered so that each group of
+    // intermediate fields dies before the next is formed; per-level results
+    // go to the level-major scratch rows for the face pass
     for (int v0 = 0; v0 < Nv; v0 += SE_LEVELS) {
       const int v = min(v0 + vs, Nv - 1);
       const bool act = v0 + vs < Nv;
-      LevRow<FT> s;
       const FT idz = P.levc[LC_IDZ * Nv + v];
-      s.set(g, P.levc[LC_R2 * Nv + v], P.levc[LC_IR2 * Nv + v], P.levc[LC_DZ * Nv + v], idz);
-      const FT Phi = P.levc[LC_PHI * Nv + v];
+      const FT Phi = P.levc[LC_PHI * Nv + v], beta = P.levc[LC_BETA * Nv + v];
       const FT g3a = P.levf[LF_G33 * Nf + v], g3b = P.levf[LF_G33 * Nf + v + 1];
-      FT rho[4], u1[4], u2[4], c1[4], c2[4], K[4], h[4], Pi[4], thp[4], tmp[4], tp[4];
-#pragma unroll
-      for (int i = 0; i < 4; ++i) {
-        const int n = NQ * j + i;
-        const int q = n * Nv + v;
-        rho[i] = sY[q];
-        u1[i] = sY[16 * Nv + q];
-        u2[i] = sY[32 * Nv + q];
-        const FT gu0 = g.gu0[i] * s.ir2, gu1 = g.gu1[i] * s.ir2, gu2 = g.gu2[i] * s.ir2;
-        c1[i] = gu0 * u1[i] + gu1 * u2[i];
-        c2[i] = gu1 * u1[i] + gu2 * u2[i];
-        // face part of K, I^c(u_3 u^3), with u_3 = 0 on the boundary faces
-        const FT fa = v == 0 ? FT(0) : sF[n * Nf + v];
-        const FT fb = v + 1 == Nv ? FT(0) : sF[n * Nf + v + 1];
-        const FT kv = (fa * (fa * g3a) + fb * (fb * g3b)) / FT(2);
-        K[i] = (u1[i] * c1[i] + u2[i] * c2[i] + kv) / FT(2);
-        Thermo<FT> th;
-        thermo(P, rho[i], sY[48 * Nv + q], K[i], Phi, th);
-        h[i] = th.h;
-        Pi[i] = th.Pi;
-        thp[i] = th.thv - th.thvr;
-        tmp[i] = K[i] + Phi - th.phir;
-        tp[i] = thp[i] * Pi[i];
-      }
-      // rho: -wdiv(rho u); rho e_tot: -split_div(rho u, h)
-      FT F1[4], F2[4], dm[4], Trho[4], Trhoe[4], Tu1[4], Tu2[4];
+      LevRow<FT> s;
       {
-        FT G1[4], G2[4], dmh[4], ha[4], hb[4];
+        FT Jh[4], iJh[4], W[4], iW[4];
+        g.row(HG_JH, Jh);
+        g.row(HG_IJH, iJh);
+        g.w(W);
+        g.iw(iW);
+        s.set_rows(Jh, iJh, W, iW, P.levc[LC_R2 * Nv + v], P.levc[LC_IR2 * Nv + v], P.levc[LC_DZ * Nv + v], idz);
+      }
+      // Q: the u_h tendency less the face cross products (added in P3)
+      FT rho[4], h[4], Pi[4], thp[4], gg[4], F1[4], F2[4], Q1[4], Q2[4];
+      {
+        FT u1[4], u2[4], c1[4], c2[4], K[4];
+        {
+          FT gu0[4], gu1[4], gu2[4];
+          g.gu(gu0, gu1, gu2);
+#pragma unroll
+          for (int i = 0; i < 4; ++i) {
+            const int n = NQ * j + i;
+            const int q = n * Nv + v;
+            rho[i] = sY[q];
+            u1[i] = sY[16 * Nv + q];
+            u2[i] = sY[32 * Nv + q];
+            const FT x0 = gu0[i] * s.ir2, x1 = gu1[i] * s.ir2, x2 = gu2[i] * s.ir2;
+            c1[i] = x0 * u1[i] + x1 * u2[i];
+            c2[i] = x1 * u1[i] + x2 * u2[i];
+            // face part of K, I^c(u_3 u^3), with u_3 = 0 on the boundary faces
+            const FT fa = v == 0 ? FT(0) : sF[n * Nf + v];
+            const FT fb = v + 1 == Nv ? FT(0) : sF[n * Nf + v + 1];
+            const FT kv = (fa * (fa * g3a) + fb * (fb * g3b)) / FT(2);
+            K[i] = (u1[i] * c1[i] + u2[i] * c2[i] + kv) / FT(2);
+            Thermo<FT> th;
+            thermo(P, rho[i], sY[48 * Nv + q], K[i], Phi, th);
+            h[i] = th.h;
+            Pi[i] = th.Pi;
+            thp[i] = th.thv - th.thvr;
+            // grad(K + Phi - Phi_r) and (cp_d / 2) grad(th' Pi) taken as one gradient
+            gg[i] = (K[i] + Phi - th.phir) + P.cpd * (thp[i] * Pi[i]) / FT(2);
+          }
+        }
+        // vorticity w^3 = wcurl(u_h); (f^3 + w^3) x CT12(u) -> C12, and the sponge
+        FT om[4];
+        {
+          FT W[4], Wu1[4], Wu2[4], ta[4], tb[4];
+          g.w(W);
+#pragma unroll
+          for (int i = 0; i < 4; ++i) {
+            Wu1[i] = W[i] * u1[i];
+            Wu2[i] = W[i] * u2[i];
+          }
+          t1(P, Wu2, ta);
+          t2(R, Wu1, tb);
+#pragma unroll
+          for (int i = 0; i < 4; ++i) om[i] = (-ta[i] + tb[i]) * s.iWJ[i];
+        }
+        FT f3[4], rJ[4];
+        g.row(HG_F3, f3);
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
+          const FT a3 = f3[i] * idz + om[i];
+          Q1[i] = -(s.J[i] * (-a3 * c2[i])) - beta * u1[i];
+          Q2[i] = -(s.J[i] * (a3 * c1[i])) - beta * u2[i];
           F1[i] = rho[i] * c1[i];
           F2[i] = rho[i] * c2[i];
+          rJ[i] = rho[i] * s.J[i];
+        }
+        if (act) {
+          st_row(row(sS, SB_C1, v), c1);
+          st_row(row(sS, SB_C2, v), c2);
+          st_row(row(sS, SB_K, v), K);
+          st_row(row(sS, SB_RJ, v), rJ);
+          st_row(row(sS, SB_U1, v), u1);
+          st_row(row(sS, SB_U2, v), u2);
+        }
+      }
+      // rho: -wdiv(rho u); rho e_tot: -split_div(rho u, h)
+      FT Trhoe[4];
+      {
+        FT G1[4], G2[4], dm[4], dmh[4], ha[4], hb[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
           G1[i] = F1[i] * h[i];
           G2[i] = F2[i] * h[i];
         }
@@ -254,16 +305,13 @@ __global__ void __launch_bounds__(SE_THREADS, SeMinBlocks<FT>::value) k_passB(De
         d2(R, h, hb);
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
-          Trho[i] = -dm[i];
           Trhoe[i] = -((dmh[i] + h[i] * dm[i] + F1[i] * ha[i] + F2[i] * hb[i]) / FT(2));
+          if (act) sO[(NQ * j + i) * Nv + v] = -dm[i];
         }
       }
-      // u_h: -[grad(K + Phi - Phi_r) + cp_d (th' grad Pi + grad(th' Pi) - Pi grad th') / 2];
-      // the two plain gradients are taken as one, grad(K + Phi - Phi_r + cp_d th' Pi / 2)
+      // u_h: -[grad(K + Phi - Phi_r) + cp_d (th' grad Pi + grad(th' Pi) - Pi grad th') / 2]
       {
-        FT a1[4], a2[4], b1[4], b2[4], f1[4], f2[4], gg[4];
-#pragma unroll
-        for (int i = 0; i < 4; ++i) gg[i] = tmp[i] + P.cpd * tp[i] / FT(2);
+        FT a1[4], a2[4], b1[4], b2[4], f1[4], f2[4];
         d1(P, gg, a1);
         d2(R, gg, a2);
         d1(P, Pi, b1);
@@ -272,78 +320,53 @@ __global__ void __launch_bounds__(SE_THREADS, SeMinBlocks<FT>::value) k_passB(De
         d2(R, thp, f2);
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
-          Tu1[i] = -(a1[i] + P.cpd * (thp[i] * b1[i] - Pi[i] * f1[i]) / FT(2));
-          Tu2[i] = -(a2[i] + P.cpd * (thp[i] * b2[i] - Pi[i] * f2[i]) / FT(2));
+          Q1[i] += -(a1[i] + P.cpd * (thp[i] * b1[i] - Pi[i] * f1[i]) / FT(2));
+          Q2[i] += -(a2[i] + P.cpd * (thp[i] * b2[i] - Pi[i] * f2[i]) / FT(2));
         }
       }
       // hyperdiffusion: nu (div_damp C123(wgrad div L) - C123(wcurl C123(curl L)))
-      FT o3[4];
       {
-        FT L1[4], L2[4], L3[4], Ls[4], o1[4], o2[4];
+        FT L1[4], L2[4], L3[4], o1[4], o2[4], o3[4];
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
           const int q = (NQ * j + i) * Nv + v;
-          Ls[i] = sL[q];
           L1[i] = sL[16 * Nv + q];
           L2[i] = sL[32 * Nv + q];
           L3[i] = sL[48 * Nv + q];
         }
         vec_lap(P, R, g, s, L1, L2, L3, P.div_damp, o1, o2, o3);
-        FT g1[4], g2[4], x1[4], x2[4], hd[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          Q1[i] -= P.nu_v * o1[i];
+          Q2[i] -= P.nu_v * o2[i];
+        }
+        if (act) {
+          st_row(row(sS, SB_L4, v), o3);
+          st_row(row(sS, SB_Q1, v), Q1);
+          st_row(row(sS, SB_Q2, v), Q2);
+        }
+      }
+      {
+        FT Ls[4], g1[4], g2[4], x1[4], x2[4], hd[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) Ls[i] = sL[(NQ * j + i) * Nv + v];
         d1(P, Ls, g1);
         d2(R, Ls, g2);
+        {
+          FT gu0[4], gu1[4], gu2[4];
+          g.gu(gu0, gu1, gu2);
 #pragma unroll
-        for (int i = 0; i < 4; ++i) {
-          const FT gu0 = g.gu0[i] * s.ir2, gu1 = g.gu1[i] * s.ir2, gu2 = g.gu2[i] * s.ir2;
-          x1[i] = rho[i] * (gu0 * g1[i] + gu1 * g2[i]);
-          x2[i] = rho[i] * (gu1 * g1[i] + gu2 * g2[i]);
+          for (int i = 0; i < 4; ++i) {
+            const FT y0 = gu0[i] * s.ir2, y1 = gu1[i] * s.ir2, y2 = gu2[i] * s.ir2;
+            x1[i] = rho[i] * (y0 * g1[i] + y1 * g2[i]);
+            x2[i] = rho[i] * (y1 * g1[i] + y2 * g2[i]);
+          }
         }
         wdiv(P, R, s, x1, x2, hd);
+        if (act) {
 #pragma unroll
-        for (int i = 0; i < 4; ++i) {
-          Tu1[i] -= P.nu_v * o1[i];
-          Tu2[i] -= P.nu_v * o2[i];
-          Trhoe[i] -= P.nu_s * hd[i];
+          for (int i = 0; i < 4; ++i) sO[48 * Nv + (NQ * j + i) * Nv + v] = Trhoe[i] - P.nu_s * hd[i];
         }
-      }
-      // vorticity: w^3 = wcurl(u_h); (f^3 + w^3) x CT12(u) -> C12
-      FT om[4];
-      {
-        FT Wu1[4], Wu2[4], ta[4], tb[4];
-#pragma unroll
-        for (int i = 0; i < 4; ++i) {
-          Wu1[i] = g.W[i] * u1[i];
-          Wu2[i] = g.W[i] * u2[i];
-        }
-        t1(P, Wu2, ta);
-        t2(R, Wu1, tb);
-#pragma unroll
-        for (int i = 0; i < 4; ++i) om[i] = (-ta[i] + tb[i]) * s.iWJ[i];
-      }
-      if (act) {
-        const FT beta = P.levc[LC_BETA * Nv + v];
-        FT rJ[4], Q1[4], Q2[4];
-#pragma unroll
-        for (int i = 0; i < 4; ++i) {
-          const int n = NQ * j + i;
-          const int q = n * Nv + v;
-          const FT a3 = sG[HG_F3 * NN + n] * idz + om[i];
-          sO[q] = Trho[i];
-          sO[48 * Nv + q] = Trhoe[i];
-          rJ[i] = rho[i] * s.J[i];
-          // u_h tendency less the face cross products (added in P3) and the sponge
-          Q1[i] = (Tu1[i] - s.J[i] * (-a3 * c2[i])) - beta * u1[i];
-          Q2[i] = (Tu2[i] - s.J[i] * (a3 * c1[i])) - beta * u2[i];
-        }
-        st_row(row(sS, SB_C1, v), c1);
-        st_row(row(sS, SB_C2, v), c2);
-        st_row(row(sS, SB_K, v), K);
-        st_row(row(sS, SB_RJ, v), rJ);
-        st_row(row(sS, SB_L4, v), o3);
-        st_row(row(sS, SB_U1, v), u1);
-        st_row(row(sS, SB_U2, v), u2);
-        st_row(row(sS, SB_Q1, v), Q1);
-        st_row(row(sS, SB_Q2, v), Q2);
       }
     }
     __syncthreads();
@@ -355,10 +378,14 @@ __global__ void __launch_bounds__(SE_THREADS, SeMinBlocks<FT>::value) k_passB(De
       const FT r2 = P.levf[LF_R2 * Nf + k], dzf = P.levf[LF_DZ * Nf + k], rinv = P.levf[LF_RINV * Nf + k];
       const FT ir2f = P.levf[LF_IR2 * Nf + k], idzf = P.levf[LF_IDZ * Nf + k], g33 = P.levf[LF_G33 * Nf + k];
       FT Wu[4], u3[4];
+      {
+        FT W[4];
+        g.w(W);
 #pragma unroll
-      for (int i = 0; i < 4; ++i) {
-        u3[i] = inner ? sF[(NQ * j + i) * Nf + k] : FT(0);
-        Wu[i] = g.W[i] * u3[i];
+        for (int i = 0; i < 4; ++i) {
+          u3[i] = inner ? sF[(NQ * j + i) * Nf + k] : FT(0);
+          Wu[i] = W[i] * u3[i];
+        }
       }
       FT ta[4], tb[4];
       t2(R, Wu, tb);
@@ -381,12 +408,18 @@ __global__ void __launch_bounds__(SE_THREADS, SeMinBlocks<FT>::value) k_passB(De
         ld_row(row(sS, SB_U1, vb), U1b);
         ld_row(row(sS, SB_U2, va), U2a);
         ld_row(row(sS, SB_U2, vb), U2b);
+        FT Jh[4], iJh[4], iW[4], fh1[4], fh2[4];
+        g.row(HG_JH, Jh);
+        g.row(HG_IJH, iJh);
+        g.iw(iW);
+        g.row(HG_FH1, fh1);
+        g.row(HG_FH2, fh2);
         FT X1[4], X2[4];
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
           const int n = NQ * j + i;
-          const FT Jf = g.Jh[i] * r2 * dzf;
-          const FT iJf = g.iJh[i] * ir2f * idzf, iWJf = g.iW[i] * iJf;
+          const FT Jf = Jh[i] * r2 * dzf;
+          const FT iJf = iJh[i] * ir2f * idzf, iWJf = iW[i] * iJf;
           const FT w1 = -tb[i] * iWJf, w2 = ta[i] * iWJf;
           FT cv1 = 0, cv2 = 0, gK = 0, cc1, cc2, l4, rJ;
           if (inner) {
@@ -403,7 +436,7 @@ __global__ void __launch_bounds__(SE_THREADS, SeMinBlocks<FT>::value) k_passB(De
             l4 = La[i];
             rJ = Ra[i];
           }
-          const FT fo1 = sG[HG_FH1 * NN + n] * rinv + cv1 + w1, fo2 = sG[HG_FH2 * NN + n] * rinv + cv2 + w2;
+          const FT fo1 = fh1[i] * rinv + cv1 + w1, fo2 = fh2[i] * rinv + cv2 + w2;
           const FT b3 = rJ * (u3[i] * g33);
           FT T3 = -(P.nu_v * l4);
           T3 -= Jf * (fo1 * cc2 - fo2 * cc1) + gK;

@@ -95,7 +95,24 @@ __device__ __forceinline__ void ld_row(const double *p, double (&a)[4]) {
   a[0] = t0.x; a[1] = t0.y; a[2] = t1.x; a[3] = t1.y;
 }
 
-// Per-node horizontal geometry of the thread's row (loaded once per element).
+// A row load that is issued at every use: the compiler may neither merge it
+// with an earlier load of the same row nor hold the value in registers
+// between uses (trading a 16-byte shared-memory read for register pressure).
+__device__ __forceinline__ void ld_row_v(const float *p, float (&a)[4]) {
+  const unsigned sa = static_cast<unsigned>(__cvta_generic_to_shared(p));
+  asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];"
+               : "=f"(a[0]), "=f"(a[1]), "=f"(a[2]), "=f"(a[3])
+               : "r"(sa));
+}
+__device__ __forceinline__ void ld_row_v(const double *p, double (&a)[4]) {
+  const unsigned sa = static_cast<unsigned>(__cvta_generic_to_shared(p));
+  asm volatile("ld.shared.v2.f64 {%0, %1}, [%2];" : "=d"(a[0]), "=d"(a[1]) : "r"(sa));
+  asm volatile("ld.shared.v2.f64 {%0, %1}, [%2+16];" : "=d"(a[2]), "=d"(a[3]) : "r"(sa));
+}
+
+// Per-node horizontal geometry of the thread's row (loaded once per element
+// and held in registers).  The accessors give the operators one interface
+// for this and for SlabGeo.
 template <class FT>
 struct RowGeo {
   FT Jh[4], iJh[4], gu0[4], gu1[4], gu2[4], gd0[4], gd1[4], gd2[4], W[4], iW[4];
@@ -115,6 +132,43 @@ struct RowGeo {
       iW[i] = P.iW[n];
     }
   }
+  __device__ void gu(FT (&a)[4], FT (&b)[4], FT (&c)[4]) const {
+#pragma unroll
+    for (int i = 0; i < 4; ++i) { a[i] = gu0[i]; b[i] = gu1[i]; c[i] = gu2[i]; }
+  }
+  __device__ void gd(FT (&a)[4], FT (&b)[4], FT (&c)[4]) const {
+#pragma unroll
+    for (int i = 0; i < 4; ++i) { a[i] = gd0[i]; b[i] = gd1[i]; c[i] = gd2[i]; }
+  }
+  __device__ void w(FT (&a)[4]) const {
+#pragma unroll
+    for (int i = 0; i < 4; ++i) a[i] = W[i];
+  }
+  __device__ void iw(FT (&a)[4]) const {
+#pragma unroll
+    for (int i = 0; i < 4; ++i) a[i] = iW[i];
+  }
+};
+
+// The same geometry re-read from the element's shared-memory slab at each use
+// (one 16-byte row per field; the GLL weights W and 1/W are staged per CTA).
+template <class FT>
+struct SlabGeo {
+  const FT *g;   // element slab + 4 j: field f of the row at g + 16 f
+  const FT *wt;  // W[16] then 1/W[16], + 4 j
+  __device__ void row(int f, FT (&a)[4]) const { ld_row_v(g + f * NN, a); }
+  __device__ void gu(FT (&a)[4], FT (&b)[4], FT (&c)[4]) const {
+    row(HG_GU0, a);
+    row(HG_GU1, b);
+    row(HG_GU2, c);
+  }
+  __device__ void gd(FT (&a)[4], FT (&b)[4], FT (&c)[4]) const {
+    row(HG_GD0, a);
+    row(HG_GD1, b);
+    row(HG_GD2, c);
+  }
+  __device__ void w(FT (&a)[4]) const { ld_row_v(wt, a); }
+  __device__ void iw(FT (&a)[4]) const { ld_row_v(wt + NN, a); }
 };
 
 // Geometry of the row at one level (deep-atmosphere scaling r^2, layer thickness dz).
@@ -122,37 +176,49 @@ template <class FT>
 struct LevRow {
   FT J[4], iJ[4], WJ[4], iWJ[4];
   FT ir2, r2, G33;
-  __device__ void set(const RowGeo<FT> &g, FT r2_, FT ir2_, FT dz, FT idz) {
+  __device__ void set_rows(const FT (&Jh)[4], const FT (&iJh)[4], const FT (&W)[4], const FT (&iW)[4], FT r2_,
+                           FT ir2_, FT dz, FT idz) {
     r2 = r2_;
     ir2 = ir2_;
     G33 = dz * dz;
 #pragma unroll
     for (int i = 0; i < NQ; ++i) {
-      J[i] = g.Jh[i] * r2 * dz;
-      iJ[i] = g.iJh[i] * ir2 * idz;
-      WJ[i] = g.W[i] * J[i];
-      iWJ[i] = g.iW[i] * iJ[i];
+      J[i] = Jh[i] * r2 * dz;
+      iJ[i] = iJh[i] * ir2 * idz;
+      WJ[i] = W[i] * J[i];
+      iWJ[i] = iW[i] * iJ[i];
     }
+  }
+  __device__ void set(const RowGeo<FT> &g, FT r2_, FT ir2_, FT dz, FT idz) {
+    set_rows(g.Jh, g.iJh, g.W, g.iW, r2_, ir2_, dz, idz);
   }
 };
 
 // C123(wgrad(div u)) * fdiv - C123(wcurl(C123(curl u))) for covariant (c1, c2, c3)
-template <class FT>
-__device__ __forceinline__ void vec_lap(const DevParams<FT> &P, const Row<FT> &R, const RowGeo<FT> &g,
+template <class FT, class G>
+__device__ __forceinline__ void vec_lap(const DevParams<FT> &P, const Row<FT> &R, const G &g,
                                         const LevRow<FT> &s, const FT (&c1)[4], const FT (&c2)[4],
                                         const FT (&c3)[4], FT fdiv, FT (&o1)[4], FT (&o2)[4], FT (&o3)[4]) {
   FT a[4], b[4], da[4], db[4];
+  {
+    FT gu0[4], gu1[4], gu2[4];
+    g.gu(gu0, gu1, gu2);
 #pragma unroll
-  for (int i = 0; i < 4; ++i) {
-    const FT gu0 = g.gu0[i] * s.ir2, gu1 = g.gu1[i] * s.ir2, gu2 = g.gu2[i] * s.ir2;
-    a[i] = s.J[i] * (gu0 * c1[i] + gu1 * c2[i]);
-    b[i] = s.J[i] * (gu1 * c1[i] + gu2 * c2[i]);
+    for (int i = 0; i < 4; ++i) {
+      const FT x0 = gu0[i] * s.ir2, x1 = gu1[i] * s.ir2, x2 = gu2[i] * s.ir2;
+      a[i] = s.J[i] * (x0 * c1[i] + x1 * c2[i]);
+      b[i] = s.J[i] * (x1 * c1[i] + x2 * c2[i]);
+    }
   }
   d1(P, a, da);
   d2(R, b, db);
   FT wdv[4], w1[4], w2[4];
+  {
+    FT W[4];
+    g.w(W);
 #pragma unroll
-  for (int i = 0; i < 4; ++i) wdv[i] = g.W[i] * ((da[i] + db[i]) * s.iJ[i]);
+    for (int i = 0; i < 4; ++i) wdv[i] = W[i] * ((da[i] + db[i]) * s.iJ[i]);
+  }
   t1(P, wdv, w1);
   t2(R, wdv, w2);
   FT e1[4], e2[4], e3[4], e4[4];
@@ -161,28 +227,38 @@ __device__ __forceinline__ void vec_lap(const DevParams<FT> &P, const Row<FT> &R
   d2(R, c3, e3);
   d1(P, c3, e4);
   FT Wz1[4], Wz2[4], Wz3[4];
+  {
+    FT gd0[4], gd1[4], gd2[4], W[4];
+    g.gd(gd0, gd1, gd2);
+    g.w(W);
 #pragma unroll
-  for (int i = 0; i < 4; ++i) {
-    const FT k3 = (e1[i] - e2[i]) * s.iJ[i];
-    const FT k1 = e3[i] * s.iJ[i], k2 = -e4[i] * s.iJ[i];
-    const FT gd0 = g.gd0[i] * s.r2, gd1 = g.gd1[i] * s.r2, gd2 = g.gd2[i] * s.r2;
-    Wz1[i] = g.W[i] * (gd0 * k1 + gd1 * k2);
-    Wz2[i] = g.W[i] * (gd1 * k1 + gd2 * k2);
-    Wz3[i] = g.W[i] * (s.G33 * k3);
+    for (int i = 0; i < 4; ++i) {
+      const FT k3 = (e1[i] - e2[i]) * s.iJ[i];
+      const FT k1 = e3[i] * s.iJ[i], k2 = -e4[i] * s.iJ[i];
+      const FT x0 = gd0[i] * s.r2, x1 = gd1[i] * s.r2, x2 = gd2[i] * s.r2;
+      Wz1[i] = W[i] * (x0 * k1 + x1 * k2);
+      Wz2[i] = W[i] * (x1 * k1 + x2 * k2);
+      Wz3[i] = W[i] * (s.G33 * k3);
+    }
   }
   FT f1[4], f2[4], f3[4], f4[4];
   t1(P, Wz2, f1);
   t2(R, Wz1, f2);
   t2(R, Wz3, f3);
   t1(P, Wz3, f4);
+  {
+    FT gd0[4], gd1[4], gd2[4], iW[4];
+    g.gd(gd0, gd1, gd2);
+    g.iw(iW);
 #pragma unroll
-  for (int i = 0; i < 4; ++i) {
-    const FT q3 = (-f1[i] + f2[i]) * s.iWJ[i];
-    const FT q1 = -f3[i] * s.iWJ[i], q2 = f4[i] * s.iWJ[i];
-    const FT gd0 = g.gd0[i] * s.r2, gd1 = g.gd1[i] * s.r2, gd2 = g.gd2[i] * s.r2;
-    o1[i] = fdiv * (-w1[i] * g.iW[i]) - (gd0 * q1 + gd1 * q2);
-    o2[i] = fdiv * (-w2[i] * g.iW[i]) - (gd1 * q1 + gd2 * q2);
-    o3[i] = -s.G33 * q3;
+    for (int i = 0; i < 4; ++i) {
+      const FT q3 = (-f1[i] + f2[i]) * s.iWJ[i];
+      const FT q1 = -f3[i] * s.iWJ[i], q2 = f4[i] * s.iWJ[i];
+      const FT x0 = gd0[i] * s.r2, x1 = gd1[i] * s.r2, x2 = gd2[i] * s.r2;
+      o1[i] = fdiv * (-w1[i] * iW[i]) - (x0 * q1 + x1 * q2);
+      o2[i] = fdiv * (-w2[i] * iW[i]) - (x1 * q1 + x2 * q2);
+      o3[i] = -s.G33 * q3;
+    }
   }
 }
 

@@ -169,6 +169,12 @@ KERNELS = [  # (id, name, launches per step)
     (3, "k_dss (direct stiffness summation)", 8),
     (4, "k_final (stage combination)", 1),
 ]
+REVERSE_KERNELS = [  # (id, name, launches per reverse step)
+    (6, "k_passB_vjp (explicit tendency transpose)", 4),
+    (5, "k_passA_vjp (Laplacian transpose)", 4),
+    (7, "k_col_stage_vjp (implicit column stage transpose)", 3),
+    (8, "k_dss_t (DSS transpose)", 8),
+]
 
 
 def algorithmic_bytes(cfg, kid, fb=4):
@@ -480,7 +486,13 @@ def measure_adjoint(args, s, fwd_ms):
     peak = ctypes.c_size_t(0)
     r_ms, _ = _timed(lambda: s.p.call("gb_adjoint_reverse", Ybar.gb(), d, ctypes.byref(peak)))
     finite = bool(torch.isfinite(Ybar.c).all() and torch.isfinite(Ybar.f).all())
-    return {"steps": n, "checkpoint_every": 5, "forward_ms_per_step": fwd_ms,
+    # per-kernel times of the reverse kernels (CUDA events inside the library)
+    kern = {}
+    for kid, name, per_step in REVERSE_KERNELS:
+        out = ctypes.c_double()
+        s.p.call("gb_time_kernel", kid, s.Y.gb(), 20, ctypes.byref(out))
+        kern[name] = {"ms": out.value, "launches_per_step": per_step}
+    return {"steps": n, "checkpoint_every": 5, "forward_ms_per_step": fwd_ms, "kernels": kern,
             "checkpointed_forward_ms_per_step": f_ms / n, "reverse_ms_per_step": r_ms / n,
             "adjoint_over_forward": (r_ms / n) / fwd_ms,
             "what": "reverse = per-segment recompute (1 forward step per step, stage data kept) + reverse kernels; "

@@ -46,36 +46,114 @@ __device__ __forceinline__ void level_geo(const DevParams<FT> &P, const RowGeo<F
   s.set(g, P.levc[LC_R2 * Nv + v], P.levc[LC_IR2 * Nv + v], P.levc[LC_DZ * Nv + v], P.levc[LC_IDZ * Nv + v]);
 }
 
+// Device shape shared by the reverse slab kernels.
+struct AdDev {
+  int nsm = 0, optin = 0, per_sm = 0;
+};
+AdDev &ad_dev() {
+  static AdDev d;
+  if (!d.nsm) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&d.nsm, cudaDevAttrMultiProcessorCount, dev);
+    cudaDeviceGetAttribute(&d.optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    cudaDeviceGetAttribute(&d.per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+    if (d.nsm <= 0) d.nsm = 1;
+  }
+  return d;
+}
+// Buffering and resident CTAs per SM of a TMA slab kernel (1 KB per CTA is
+// reserved by the hardware): double buffering at `minb` CTAs if it fits,
+// else single buffering at `minb`, else one double- or single-buffered CTA.
+struct AdShape {
+  int nbuf, ctas;
+  size_t smem;
+};
+template <class L>
+AdShape ad_shape(int Nv, int minb) {
+  const AdDev &d = ad_dev();
+  const size_t two = L(Nv, 2).total, one = L(Nv, 1).total, per_sm = (size_t)d.per_sm;
+  if (minb >= 2) {
+    if (2 * (two + 1024) <= per_sm) return {2, 2, two};
+    if (2 * (one + 1024) <= per_sm) return {1, 2, one};
+  }
+  if (two <= (size_t)d.optin) return {2, 1, two};
+  return {1, 1, one};
+}
+
 // ----------------------------------------------------------------------------- pass A^T
+// Per buffer: the state Y (64 Nv) and faces (16 Nf), the element geometry,
+// the Laplacian cotangent Lb (64 Nv) and the state cotangent (64 Nv, 16 Nf),
+// which is accumulated in place and stored back.  Scratch: the face parts of
+// each level's cotangent, level-major rows [Nv][16] (lower, upper face).
 template <class FT>
-__global__ void __launch_bounds__(AD_THREADS) k_passA_vjp(DevParams<FT> P, const FT *__restrict__ Yc,
-                                                          const FT *__restrict__ Yf, const FT *__restrict__ Lb,
-                                                          FT *__restrict__ Ybc, FT *__restrict__ Ybf) {
-  extern __shared__ __align__(16) unsigned char sm_raw[];
-  FT *sm = (FT *)sm_raw;
+struct AvLayout {
+  size_t y[2], f[2], g[2], lb[2], yb[2], fb[2], lo, hi, bar, total;
+  __host__ __device__ AvLayout(int Nv, int nbuf) {
+    const int Nf = Nv + 1;
+    size_t o = 0;
+    for (int b = 0; b < 2; ++b) {
+      if (b < nbuf) {
+        y[b] = o; o += align16(sizeof(FT) * 64 * Nv);
+        f[b] = o; o += align16(sizeof(FT) * 16 * Nf);
+        g[b] = o; o += align16(sizeof(FT) * HG_N * 16);
+        lb[b] = o; o += align16(sizeof(FT) * 64 * Nv);
+        yb[b] = o; o += align16(sizeof(FT) * 64 * Nv);
+        fb[b] = o; o += align16(sizeof(FT) * 16 * Nf);
+      } else {
+        y[b] = y[0]; f[b] = f[0]; g[b] = g[0]; lb[b] = lb[0]; yb[b] = yb[0]; fb[b] = fb[0];
+      }
+    }
+    lo = o; o += align16(sizeof(FT) * 16 * Nv);
+    hi = o; o += align16(sizeof(FT) * 16 * Nv);
+    bar = o; o += 16;
+    total = o;
+  }
+};
+
+template <class FT>
+__global__ void __launch_bounds__(AD_THREADS, AdMinBlocks<FT>::value)
+    k_passA_vjp(DevParams<FT> P, int nbuf, const FT *__restrict__ Yc, const FT *__restrict__ Yf,
+                const FT *__restrict__ Lb, FT *__restrict__ Ybc, FT *__restrict__ Ybf) {
+  extern __shared__ __align__(128) unsigned char sm[];
   const int Nv = P.Nv, Nf = P.Nf;
-  FT *sY = sm, *sL = sY + 64 * Nv, *sF = sL + 64 * Nv, *sG = sF + 16 * Nf;
-  FT *sU3 = sG + HG_N * 16, *sKv = sU3 + 16 * Nv, *sLo = sKv + 16 * Nv, *sHi = sLo + 16 * Nv;
-  const int j = threadIdx.x & 3, vl = threadIdx.x >> 2;
+  const AvLayout<FT> Lo(Nv, nbuf);
+  // slab x of buffer b (selects, not a runtime-indexed array)
+  auto at = [&](const size_t (&off)[2], int b) { return (FT *)(sm + (b ? off[1] : off[0])); };
+  FT *sLo = (FT *)(sm + Lo.lo), *sHi = (FT *)(sm + Lo.hi);
+  uint64_t *bar = (uint64_t *)(sm + Lo.bar);
+  const uint32_t by = uint32_t(sizeof(FT) * 64 * Nv), bf = uint32_t(sizeof(FT) * 16 * Nf);
+  const uint32_t bg = uint32_t(sizeof(FT) * HG_N * 16);
+  auto issue = [&](int b, int e) {
+    mbar_expect_tx(b ? &bar[1] : &bar[0], 3 * by + 2 * bf + bg);
+    uint64_t *bb = b ? &bar[1] : &bar[0];
+    tma_load(at(Lo.y, b), Yc + (size_t)e * 64 * Nv, by, bb);
+    tma_load(at(Lo.f, b), Yf + (size_t)e * 16 * Nf, bf, bb);
+    tma_load(at(Lo.g, b), P.hgeo + (size_t)e * HG_N * 16, bg, bb);
+    tma_load(at(Lo.lb, b), Lb + (size_t)e * 64 * Nv, by, bb);
+    tma_load(at(Lo.yb, b), Ybc + (size_t)e * 64 * Nv, by, bb);
+    tma_load(at(Lo.fb, b), Ybf + (size_t)e * 16 * Nf, bf, bb);
+  };
+  slab_init_bars(bar);
+  int e = blockIdx.x;
+  if (threadIdx.x == 0 && e < P.Nh) issue(0, e);
+  const int j = threadIdx.x & 3, vl = threadIdx.x >> 2, vs = level_slot(vl);
   Row<FT> R;
   R.init(P, j);
-  for (int e = blockIdx.x; e < P.Nh; e += gridDim.x) {
-    load_slab(sY, Yc + (size_t)e * 64 * Nv, 64 * Nv);
-    load_slab(sL, Lb + (size_t)e * 64 * Nv, 64 * Nv);
-    load_slab(sF, Yf + (size_t)e * 16 * Nf, 16 * Nf);
-    load_slab(sG, P.hgeo + (size_t)e * HG_N * 16, HG_N * 16);
-    __syncthreads();
-    centre_from_faces(P, sF, sU3, sKv);
-    __syncthreads();
+  for (int it = 0; e < P.Nh; ++it, e += gridDim.x) {
+    int b;
+    if (!slab_begin(bar, nbuf, it, e, P.Nh, P.status, issue, b)) break;
+    const FT *sY = at(Lo.y, b), *sF = at(Lo.f, b), *sG = at(Lo.g, b), *sL = at(Lo.lb, b);
+    FT *sB = at(Lo.yb, b), *sBf = at(Lo.fb, b);
     RowGeo<FT> g;
     g.load(sG, P, j);
-    FT *yb = Ybc + (size_t)e * 64 * Nv;
     for (int v0 = 0; v0 < Nv; v0 += AD_LEVELS) {
-      const int v = min(v0 + vl, Nv - 1);
-      const bool act = v0 + vl < Nv;
+      const int v = min(v0 + vs, Nv - 1);
+      const bool act = v0 + vs < Nv;
       LevRow<FT> s;
       level_geo(P, g, v, s);
       const FT Phi = P.levc[LC_PHI * Nv + v];
+      const FT g3a = P.levf[LF_G33 * Nf + v], g3b = P.levf[LF_G33 * Nf + v + 1];
       FT Lsb[4], L1b[4], L2b[4], L3b[4];
 #pragma unroll
       for (int i = 0; i < 4; ++i) {
@@ -88,43 +166,62 @@ __global__ void __launch_bounds__(AD_THREADS) k_passA_vjp(DevParams<FT> P, const
       FT u1b[4], u2b[4], ub3b[4], sdb[4];
       vec_lap_t(P, R, g, s, L1b, L2b, L3b, FT(1), u1b, u2b, ub3b);
       lap_t(P, R, g, s, Lsb, sdb);
-      if (act) {
+      FT lo[4], hi[4];
 #pragma unroll
-        for (int i = 0; i < 4; ++i) {
-          const int q = (NQ * j + i) * Nv + v;
-          const FT rho = sY[q], u1 = sY[16 * Nv + q], u2 = sY[32 * Nv + q], rhoe = sY[48 * Nv + q];
-          const FT gu0 = g.gu0[i] * s.ir2, gu1 = g.gu1[i] * s.ir2, gu2 = g.gu2[i] * s.ir2;
-          const FT c1 = gu0 * u1 + gu1 * u2, c2 = gu1 * u1 + gu2 * u2;
-          const FT K = (u1 * c1 + u2 * c2 + sKv[q]) / FT(2);
-          // sd = cp (T - T_r(Pi)) + Phi - Phi_r(Pi)
-          ThermoBar<FT> tb{};
-          tb.T = P.cpd * sdb[i];
-          tb.Tr = -P.cpd * sdb[i];
-          tb.phir = -sdb[i];
-          FT rb, reb, Kb;
-          thermo_vjp(P, rho, rhoe, K, Phi, tb, rb, reb, Kb);
-          // K = (u . c + Kv) / 2: dK/du_h = c, dK/dKv = 1/2
-          yb[q] += rb;
-          yb[16 * Nv + q] += u1b[i] + c1 * Kb;
-          yb[32 * Nv + q] += u2b[i] + c2 * Kb;
-          yb[48 * Nv + q] += reb;
-          // faces v, v+1: u_bar_3 = (a + b)/2, Kv = (a^2 g33_a + b^2 g33_b)/2 (filtered at the boundary)
-          const int n = NQ * j + i;
-          const FT a = v == 0 ? FT(0) : sF[n * Nf + v], bt = v + 1 == Nv ? FT(0) : sF[n * Nf + v + 1];
-          const FT Kvb = Kb / FT(2);
-          sLo[q] = v == 0 ? FT(0) : ub3b[i] / FT(2) + Kvb * a * P.levf[LF_G33 * Nf + v];
-          sHi[q] = v + 1 == Nv ? FT(0) : ub3b[i] / FT(2) + Kvb * bt * P.levf[LF_G33 * Nf + v + 1];
+      for (int i = 0; i < 4; ++i) {
+        const int n = NQ * j + i;
+        const int q = n * Nv + v;
+        const FT rho = sY[q], u1 = sY[16 * Nv + q], u2 = sY[32 * Nv + q], rhoe = sY[48 * Nv + q];
+        const FT gu0 = g.gu0[i] * s.ir2, gu1 = g.gu1[i] * s.ir2, gu2 = g.gu2[i] * s.ir2;
+        const FT c1 = gu0 * u1 + gu1 * u2, c2 = gu1 * u1 + gu2 * u2;
+        // faces v, v+1 (u_3 = 0 on the boundary faces): u_bar_3 = (a + b)/2, Kv = (a^2 g33_a + b^2 g33_b)/2
+        const FT fa = v == 0 ? FT(0) : sF[n * Nf + v], fb = v + 1 == Nv ? FT(0) : sF[n * Nf + v + 1];
+        const FT kv = (fa * (fa * g3a) + fb * (fb * g3b)) / FT(2);
+        const FT K = (u1 * c1 + u2 * c2 + kv) / FT(2);
+        // sd = cp (T - T_r(Pi)) + Phi - Phi_r(Pi)
+        ThermoBar<FT> tb{};
+        tb.T = P.cpd * sdb[i];
+        tb.Tr = -P.cpd * sdb[i];
+        tb.phir = -sdb[i];
+        FT rb, reb, Kb;
+        thermo_vjp(P, rho, rhoe, K, Phi, tb, rb, reb, Kb);
+        // K = (u . c + Kv) / 2: dK/du_h = c, dK/dKv = 1/2
+        if (act) {
+          sB[q] += rb;
+          sB[16 * Nv + q] += u1b[i] + c1 * Kb;
+          sB[32 * Nv + q] += u2b[i] + c2 * Kb;
+          sB[48 * Nv + q] += reb;
         }
+        const FT Kvb = Kb / FT(2);
+        lo[i] = v == 0 ? FT(0) : ub3b[i] / FT(2) + Kvb * fa * g3a;
+        hi[i] = v + 1 == Nv ? FT(0) : ub3b[i] / FT(2) + Kvb * fb * g3b;
+      }
+      if (act) {
+        st_row(sLo + (size_t)v * NN + NQ * j, lo);
+        st_row(sHi + (size_t)v * NN + NQ * j, hi);
       }
     }
     __syncthreads();
-    FT *fb = Ybf + (size_t)e * 16 * Nf;
-    for (int idx = threadIdx.x; idx < 16 * Nf; idx += blockDim.x) {
-      const int n = idx / Nf, f = idx - n * Nf;
-      if (f > 0 && f < Nv) fb[idx] += sHi[n * Nv + f - 1] + sLo[n * Nv + f];
+    // inner face k gathers the upper part of level k-1 and the lower part of level k
+    for (int k0 = 1; k0 < Nv; k0 += AD_LEVELS) {
+      const int k = k0 + vl;
+      if (k < Nv) {
+        FT hi[4], lo[4];
+        ld_row(sHi + (size_t)(k - 1) * NN + NQ * j, hi);
+        ld_row(sLo + (size_t)k * NN + NQ * j, lo);
+#pragma unroll
+        for (int i = 0; i < 4; ++i) sBf[(NQ * j + i) * Nf + k] += hi[i] + lo[i];
+      }
     }
+    fence_proxy_async();
     __syncthreads();
+    if (threadIdx.x == 0) {
+      tma_store(Ybc + (size_t)e * 64 * Nv, sB, by);
+      tma_store(Ybf + (size_t)e * 16 * Nf, sBf, bf);
+      tma_store_commit();
+    }
   }
+  if (threadIdx.x == 0) tma_store_wait_all();
 }
 
 // ----------------------------------------------------------------------------- pass B^T
@@ -596,7 +693,7 @@ __global__ void __launch_bounds__(AD_THREADS, AdMinBlocks<FT>::value) k_passB_vj
 
 template <class FT>
 size_t passA_vjp_smem(int Nv) {
-  return sizeof(FT) * (2 * 64 * (size_t)Nv + 16 * (size_t)(Nv + 1) + HG_N * 16 + 4 * 16 * (size_t)Nv);
+  return AvLayout<FT>(Nv, 1).total;
 }
 template <class FT>
 size_t passB_vjp_smem(int Nv) {
@@ -635,8 +732,9 @@ template <class FT>
 void launch_passA_vjp(const DevParams<FT> &P, const FT *Yc, const FT *Yf, const FT *Lb, FT *Ybc, FT *Ybf, int grid,
                       cudaStream_t s) {
   (void)grid;
-  const size_t sm = passA_vjp_smem<FT>(P.Nv);
-  k_passA_vjp<FT><<<resident_grid(k_passA_vjp<FT>, sm, P.Nh), AD_THREADS, sm, s>>>(P, Yc, Yf, Lb, Ybc, Ybf);
+  const AdShape sh = ad_shape<AvLayout<FT>>(P.Nv, AdMinBlocks<FT>::value);
+  const int g = std::max(1, std::min(P.Nh, ad_dev().nsm * sh.ctas));
+  k_passA_vjp<FT><<<g, AD_THREADS, sh.smem, s>>>(P, sh.nbuf, Yc, Yf, Lb, Ybc, Ybf);
 }
 // grid: the number of parameter-partial slots (CTAs) the caller allocated.
 template <class FT>

@@ -368,6 +368,11 @@ int residual_t(gb_ctx *ctx, double *out) {
 }
 
 template <class FT>
+int ensure_adjoint(gb_ctx *ctx);
+template <class FT>
+StageArgs<FT> single_stage_args(Impl<FT> *I, const FT *Uhc, const FT *Uhf, double dtg);
+
+template <class FT>
 int time_kernel_t(gb_ctx *ctx, int kernel, gb_fieldvec Y, int reps, double *ms) {
   Impl<FT> *I = impl<FT>(ctx);
   const DevParams<FT> &P = I->P;
@@ -396,12 +401,38 @@ int time_kernel_t(gb_ctx *ctx, int kernel, gb_fieldvec Y, int reps, double *ms) 
     A.rnorm = (double *)I->rnorm.p;
     A.first = 1;
   }
+  // reverse kernels: cotangent inputs are the tendency and Laplacian buffers of
+  // the last step (finite values), outputs the reverse-mode scratch
+  const bool rev = kernel >= GB_K_PASSA_VJP && kernel <= GB_K_DSS_T;
+  if (rev) {
+    int r = ensure_adjoint<FT>(ctx);
+    if (r) return r;
+  }
+  FT *Ubc = rev ? (FT *)I->adj->Ub.p : nullptr, *Ubf = rev ? Ubc + I->NC : nullptr;
+  FT *Lbc = rev ? (FT *)I->adj->Lb.p : nullptr;
+  StageArgs<FT> SA{};
+  // the implicit-tendency cotangent input: stage 1's buffer (stage 0 has no implicit tendency)
+  if (kernel == GB_K_COLUMN_VJP) {
+    if (!I->Ti[1].p) return fail(ctx, GB_ERR_ARG, "implicit tendency buffers not allocated");
+    SA = single_stage_args<FT>(I, Yc, Yf, (double)dt * I->ai[1][1]);
+  }
+  FT *Teb[4] = {rev ? (FT *)I->adj->dummy.p : nullptr, nullptr, nullptr, nullptr};
+  FT *Tibs[4] = {nullptr, nullptr, nullptr, nullptr};
   auto launch = [&]() {
     switch (kernel) {
       case GB_K_PASSA: launch_passA<FT>(P, Yc, Yf, lap, s); break;
       case GB_K_PASSB: launch_passB<FT>(P, Yc, Yf, lap, Tc, Tf, s); break;
       case GB_K_COLUMN: launch_column_stage<FT>(P, A, s); break;
       case GB_K_DSS: launch_dss<FT>(P, Yc, Yf, s); break;
+      case GB_K_PASSA_VJP: launch_passA_vjp<FT>(P, Yc, Yf, lap, Ubc, Ubf, I->adj->grid, s); break;
+      case GB_K_PASSB_VJP:
+        launch_passB_vjp<FT>(P, Yc, Yf, lap, Tc, Tf, Ubc, Ubf, Lbc, (double *)I->adj->dparB.p, I->adj->grid, s);
+        break;
+      case GB_K_COLUMN_VJP:
+        launch_column_stage_vjp<FT>(P, SA, Tc, Tf, (const FT *)I->Ti[1].p, (const FT *)I->Ti[1].p + I->NR, Ubc, Ubf,
+                                    Teb, Tibs, I->NC, I->NR, (FT *)I->adj->scr.p, (double *)I->adj->dal.p, s);
+        break;
+      case GB_K_DSS_T: launch_dss_transpose<FT>(P, Ubc, Ubf, s); break;
       default: launch_final<FT>(P, A, (FT *)I->U.p, (FT *)I->U.p + I->NC, s); break;
     }
   };
@@ -444,7 +475,8 @@ int ensure_adjoint(gb_ctx *ctx) {
   CK(cudaGetDevice(&dev));
   CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
   CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-  if (passB_vjp_smem<FT>(I->P.Nv) + 2 * 256 * sizeof(double) > (size_t)optin)
+  if (passB_vjp_smem<FT>(I->P.Nv) + 2 * 256 * sizeof(double) > (size_t)optin ||
+      passA_vjp_smem<FT>(I->P.Nv) > (size_t)optin)
     return fail(ctx, GB_ERR_ARG, "z_elem too large for the reverse-mode slab kernels at this precision (shared memory)");
   configure_adjoint_se<FT>(I->P.Nv);
   auto A = std::make_unique<typename Impl<FT>::Adjoint>();
@@ -1013,7 +1045,7 @@ int gb_dss_transpose(gb_ctx *ctx, gb_fieldvec X) {
 int gb_remaining_tendency_vjp(gb_ctx *ctx, gb_fieldvec Ybar, gb_fieldvec Tbar, gb_fieldvec Y, double t,
                               double dparams[2]) {
   (void)t;
-  if (!ctx || !Ybar.c || !Ybar.f || !Tbar.c || !Tbar.f || !Y.c || !Y.f) return GB_ERR_ARG;
+  if (!ctx || !fv_ok(Ybar) || !fv_ok(Tbar) || !fv_ok(Y)) return GB_ERR_ARG;
   return ctx->cfg.ft_bytes == 8 ? remaining_tendency_vjp_t<double>(ctx, Ybar, Tbar, Y, dparams)
                                 : remaining_tendency_vjp_t<float>(ctx, Ybar, Tbar, Y, dparams);
 }
@@ -1033,27 +1065,27 @@ int gb_implicit_stage_vjp(gb_ctx *ctx, gb_fieldvec Uhat_bar, gb_fieldvec Ubar, g
 
 int gb_step_vjp(gb_ctx *ctx, gb_fieldvec Ybar, gb_fieldvec Y, double t, double dt, double dparams[2]) {
   (void)t;
-  if (!ctx || !Ybar.c || !Ybar.f || !Y.c || !Y.f || !(dt > 0)) return GB_ERR_ARG;
+  if (!ctx || !fv_ok(Ybar) || !fv_ok(Y) || !(dt > 0)) return GB_ERR_ARG;
   return ctx->cfg.ft_bytes == 8 ? step_vjp_t<double>(ctx, Ybar, Y, dt, dparams)
                                 : step_vjp_t<float>(ctx, Ybar, Y, dt, dparams);
 }
 
 int gb_adjoint_forward(gb_ctx *ctx, gb_fieldvec Y, double t0, double dt, int nsteps, int checkpoint_every) {
   (void)t0;
-  if (!ctx || !Y.c || !Y.f || !(dt > 0) || nsteps < 1 || checkpoint_every < 1) return GB_ERR_ARG;
+  if (!ctx || !fv_ok(Y) || !(dt > 0) || nsteps < 1 || checkpoint_every < 1) return GB_ERR_ARG;
   return ctx->cfg.ft_bytes == 8 ? adjoint_forward_t<double>(ctx, Y, dt, nsteps, checkpoint_every)
                                 : adjoint_forward_t<float>(ctx, Y, dt, nsteps, checkpoint_every);
 }
 
 int gb_adjoint_reverse(gb_ctx *ctx, gb_fieldvec Ybar, double dparams[2], size_t *peak_bytes) {
-  if (!ctx || !Ybar.c || !Ybar.f) return GB_ERR_ARG;
+  if (!ctx || !fv_ok(Ybar)) return GB_ERR_ARG;
   return ctx->cfg.ft_bytes == 8 ? adjoint_reverse_t<double>(ctx, Ybar, dparams, peak_bytes)
                                 : adjoint_reverse_t<float>(ctx, Ybar, dparams, peak_bytes);
 }
 
 int gb_time_kernel(gb_ctx *ctx, int kernel, gb_fieldvec Y, int reps, double *ms) {
   GUARD(ctx);
-  if (!fv_ok(Y) || !ms || reps < 0 || kernel < 0 || kernel > 4) return fail(ctx, GB_ERR_ARG, "bad gb_time_kernel arguments");
+  if (!fv_ok(Y) || !ms || reps < 0 || kernel < 0 || kernel > GB_K_DSS_T) return fail(ctx, GB_ERR_ARG, "bad gb_time_kernel arguments");
   return DISPATCH(ctx, time_kernel_t, ctx, kernel, Y, reps, ms);
 }
 

@@ -401,3 +401,45 @@ __device__ __forceinline__ void lap_t(const DevParams<FT> &P, const Row<FT> &R, 
 
 }  // namespace se
 }  // namespace gb
+
+namespace gb {
+namespace se {
+
+// ---------------------------------------------------------------- TMA slab pipeline
+// Shared by slab kernels whose output store reads from a load buffer (an
+// input slab accumulated in place and stored back).  One mbarrier per buffer.
+__device__ __forceinline__ void slab_init_bars(uint64_t *bar) {
+  if (threadIdx.x == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+}
+
+// Start of element iteration `it` (element e): thread 0 first retires the
+// reads of the previous element's store (it may read the buffer about to be
+// refilled), then prefetches the next element into the other buffer (double
+// buffering) or loads this one (single buffering; iteration 0 was issued
+// before the loop).  issue(buffer, element) issues the TMA loads.  Returns
+// false, in every thread, if the bounded wait for this element gave up.
+template <class Issue>
+__device__ __forceinline__ bool slab_begin(uint64_t *bar, int nbuf, int it, int e, int Nh, int *status,
+                                           const Issue &issue, int &b) {
+  b = nbuf == 2 ? (it & 1) : 0;
+  if (threadIdx.x == 0) {
+    tma_store_wait_read();
+    if (nbuf == 2) {
+      const int en = e + (int)gridDim.x;
+      if (en < Nh) issue(b ^ 1, en);
+    } else if (it > 0) {
+      issue(0, e);
+    }
+  }
+  const uint32_t parity = nbuf == 2 ? ((it >> 1) & 1) : (it & 1);
+  const bool ok = mbar_wait_bounded(b ? &bar[1] : &bar[0], parity, status);
+  return __syncthreads_and(ok) != 0;
+}
+
+}  // namespace se
+}  // namespace gb

@@ -148,7 +148,11 @@ int gb_jacobian_solve_noalloc(gb_ctx *ctx, gb_fieldvec dY, gb_fieldvec Y, gb_fie
  * (Laplacians), 1 pass B (explicit tendency), 2 column stage (stage 4: five
  * sources), 3 state DSS, 4 final combination.  Y is read (and, for 3/4,
  * written); synchronous. */
-enum gb_kernel_id { GB_K_PASSA = 0, GB_K_PASSB = 1, GB_K_COLUMN = 2, GB_K_DSS = 3, GB_K_FINAL = 4 };
+enum gb_kernel_id {
+  GB_K_PASSA = 0, GB_K_PASSB = 1, GB_K_COLUMN = 2, GB_K_DSS = 3, GB_K_FINAL = 4,
+  /* reverse mode: pass A^T, pass B^T, the implicit column stage VJP, DSS^T */
+  GB_K_PASSA_VJP = 5, GB_K_PASSB_VJP = 6, GB_K_COLUMN_VJP = 7, GB_K_DSS_T = 8
+};
 int gb_time_kernel(gb_ctx *ctx, int kernel, gb_fieldvec Y, int reps, double *ms_per_launch);
 
 /* ---------------------------------------------------------------------------

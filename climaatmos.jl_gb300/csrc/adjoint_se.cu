@@ -34,11 +34,6 @@ struct AdMinBlocks {
   static constexpr int value = sizeof(FT) == 4 ? 2 : 1;
 };
 
-template <class FT>
-__device__ __forceinline__ void load_slab(FT *dst, const FT *src, int n) {
-  for (int q = threadIdx.x; q < n; q += blockDim.x) dst[q] = src[q];
-}
-
 // Per-level forward quantities of one row at centre level v.
 template <class FT>
 __device__ __forceinline__ void level_geo(const DevParams<FT> &P, const RowGeo<FT> &g, int v, LevRow<FT> &s) {
@@ -225,398 +220,562 @@ __global__ void __launch_bounds__(AD_THREADS, AdMinBlocks<FT>::value)
 }
 
 // ----------------------------------------------------------------------------- pass B^T
-// Shared memory (FT words): Y 64Nv, F 16Nf, geometry HG_N*16 (the Laplacians
-// and the tendency cotangent are read from global memory); centre scratch
-// Kv, c1, c2, K, rho J, o3, a3 (7 x 16Nv), lower/upper face parts (2 x 16Nv);
-// face scratch X1, X2, and the face cotangents cc1, cc2, gK, l4, rJ, cv1, cv2,
-// u3 (10 x 16Nf).
-template <class FT>
-__host__ __device__ inline size_t passB_vjp_words(int Nv) {
-  const size_t Nf = Nv + 1;
-  return 64 * (size_t)Nv + 16 * Nf + HG_N * 16 + 9 * 16 * (size_t)Nv + 10 * 16 * Nf;
-}
+// Per buffer: the state Y (64 Nv) and faces (16 Nf), the element geometry,
+// the DSSed Laplacians L (64 Nv) and the tendency cotangent Tb (64 Nv, 16 Nf).
+// Scratch, level-major rows ([Nv][16] or [Nf][16], one 16-byte row per
+// thread): the forward centre values c1, c2, K, rho J, o3; the forward face
+// cross products X1, X2 and the face cotangents; the K_v cotangent.  The
+// state cotangent is accumulated in global memory (each element owns its
+// nodes); the Laplacian cotangent is written.
+enum BvCentre { BC_C1 = 0, BC_C2, BC_K, BC_RJ, BC_L4, BC_N };
+enum BvFace { BF_X1 = 0, BF_X2, BF_CC1, BF_CC2, BF_RJ, BF_CV1, BF_CV2, BF_U3, BF_N };
 
 template <class FT>
-__global__ void __launch_bounds__(AD_THREADS, AdMinBlocks<FT>::value) k_passB_vjp(DevParams<FT> P, const FT *__restrict__ Yc,
-                                                          const FT *__restrict__ Yf, const FT *__restrict__ Lc,
-                                                          const FT *__restrict__ Tbc, const FT *__restrict__ Tbf,
-                                                          FT *__restrict__ Ybc, FT *__restrict__ Ybf,
-                                                          FT *__restrict__ Lbc, double *__restrict__ dpar) {
-  extern __shared__ __align__(16) unsigned char sm_raw[];
-  FT *sm = (FT *)sm_raw;
+struct BvLayout {
+  size_t y[2], f[2], g[2], lap[2], tb[2], tbf[2], c, fc, kvb, w, red, bar, total;
+  __host__ __device__ BvLayout(int Nv, int nbuf) {
+    const int Nf = Nv + 1;
+    size_t o = 0;
+    for (int b = 0; b < 2; ++b) {
+      if (b < nbuf) {
+        y[b] = o; o += align16(sizeof(FT) * 64 * Nv);
+        f[b] = o; o += align16(sizeof(FT) * 16 * Nf);
+        g[b] = o; o += align16(sizeof(FT) * HG_N * 16);
+        lap[b] = o; o += align16(sizeof(FT) * 64 * Nv);
+        tb[b] = o; o += align16(sizeof(FT) * 64 * Nv);
+        tbf[b] = o; o += align16(sizeof(FT) * 16 * Nf);
+      } else {
+        y[b] = y[0]; f[b] = f[0]; g[b] = g[0]; lap[b] = lap[0]; tb[b] = tb[0]; tbf[b] = tbf[0];
+      }
+    }
+    c = o; o += align16(sizeof(FT) * BC_N * 16 * Nv);
+    fc = o; o += align16(sizeof(FT) * BF_N * 16 * Nf);
+    kvb = o; o += align16(sizeof(FT) * 16 * Nv);
+    w = o; o += align16(sizeof(FT) * 2 * 16);
+    red = o; o += align16(sizeof(double) * 2 * (AD_THREADS / 32));
+    bar = o; o += 16;
+    total = o;
+  }
+};
+
+template <class FT>
+__global__ void __launch_bounds__(AD_THREADS, AdMinBlocks<FT>::value)
+    k_passB_vjp(DevParams<FT> P, int nbuf, const FT *__restrict__ Yc, const FT *__restrict__ Yf,
+                const FT *__restrict__ Lc, const FT *__restrict__ Tbc, const FT *__restrict__ Tbf,
+                FT *__restrict__ Ybc, FT *__restrict__ Ybf, FT *__restrict__ Lbc, double *__restrict__ dpar) {
+  extern __shared__ __align__(128) unsigned char sm[];
   const int Nv = P.Nv, Nf = P.Nf;
-  FT *sY = sm, *sF = sY + 64 * Nv;
-  FT *sG = sF + 16 * Nf;
-  FT *sKv = sG + HG_N * 16, *sC1 = sKv + 16 * Nv, *sC2 = sC1 + 16 * Nv, *sK = sC2 + 16 * Nv;
-  FT *sRJ = sK + 16 * Nv, *sL4 = sRJ + 16 * Nv, *sA3 = sL4 + 16 * Nv, *sLo = sA3 + 16 * Nv, *sHi = sLo + 16 * Nv;
-  FT *sX1 = sHi + 16 * Nv, *sX2 = sX1 + 16 * Nf, *bCc1 = sX2 + 16 * Nf, *bCc2 = bCc1 + 16 * Nf;
-  FT *bGK = bCc2 + 16 * Nf, *bL4 = bGK + 16 * Nf, *bRJ = bL4 + 16 * Nf, *bCv1 = bRJ + 16 * Nf;
-  FT *bCv2 = bCv1 + 16 * Nf, *bU3 = bCv2 + 16 * Nf;
-  const int j = threadIdx.x & 3, vl = threadIdx.x >> 2;
+  const BvLayout<FT> Lo(Nv, nbuf);
+  auto at = [&](const size_t (&off)[2], int b) { return (FT *)(sm + (b ? off[1] : off[0])); };
+  FT *sC = (FT *)(sm + Lo.c), *sFc = (FT *)(sm + Lo.fc), *sKvb = (FT *)(sm + Lo.kvb), *sW = (FT *)(sm + Lo.w);
+  double *red = (double *)(sm + Lo.red);
+  uint64_t *bar = (uint64_t *)(sm + Lo.bar);
+  const uint32_t by = uint32_t(sizeof(FT) * 64 * Nv), bf = uint32_t(sizeof(FT) * 16 * Nf);
+  const uint32_t bg = uint32_t(sizeof(FT) * HG_N * 16);
+  auto issue = [&](int b, int e) {
+    uint64_t *bb = b ? &bar[1] : &bar[0];
+    mbar_expect_tx(bb, 3 * by + 2 * bf + bg);
+    tma_load(at(Lo.y, b), Yc + (size_t)e * 64 * Nv, by, bb);
+    tma_load(at(Lo.f, b), Yf + (size_t)e * 16 * Nf, bf, bb);
+    tma_load(at(Lo.g, b), P.hgeo + (size_t)e * HG_N * 16, bg, bb);
+    tma_load(at(Lo.lap, b), Lc + (size_t)e * 64 * Nv, by, bb);
+    tma_load(at(Lo.tb, b), Tbc + (size_t)e * 64 * Nv, by, bb);
+    tma_load(at(Lo.tbf, b), Tbf + (size_t)e * 16 * Nf, bf, bb);
+  };
+  if (threadIdx.x < NN) {
+    sW[threadIdx.x] = P.W[threadIdx.x];
+    sW[NN + threadIdx.x] = P.iW[threadIdx.x];
+  }
+  slab_init_bars(bar);
+  int e = blockIdx.x;
+  if (threadIdx.x == 0 && e < P.Nh) issue(0, e);
+  const int j = threadIdx.x & 3, vl = threadIdx.x >> 2, vs = level_slot(vl);
+  // the thread's row of centre scratch field f at level v / face field f at face k
+  auto crow = [&](int f, int v) { return sC + ((size_t)f * Nv + v) * NN + NQ * j; };
+  auto frow = [&](int f, int k) { return sFc + ((size_t)f * Nf + k) * NN + NQ * j; };
   Row<FT> R;
   R.init(P, j);
   const FT nu = P.nu_v, nus = P.nu_s;
   const FT rpr = nu != FT(0) ? nus / nu : FT(1);  // d nu_s / d nu = 1 / Prandtl
+  const FT hc = P.cpd / FT(2);
   double dnu = 0, dal = 0;
-  for (int e = blockIdx.x; e < P.Nh; e += gridDim.x) {
-    load_slab(sY, Yc + (size_t)e * 64 * Nv, 64 * Nv);
-    load_slab(sF, Yf + (size_t)e * 16 * Nf, 16 * Nf);
-    load_slab(sG, P.hgeo + (size_t)e * HG_N * 16, HG_N * 16);
-    // the Laplacians and the tendency cotangent are read in place (L1-cached)
-    const FT *sL = Lc + (size_t)e * 64 * Nv, *sT = Tbc + (size_t)e * 64 * Nv, *sTf = Tbf + (size_t)e * 16 * Nf;
-    __syncthreads();
-    centre_from_faces<FT>(P, sF, nullptr, sKv);
-    __syncthreads();
-    RowGeo<FT> g;
-    g.load(sG, P, j);
-    // ---- C: forward centre quantities used by the face phase and the P3 transpose
+  for (int it = 0; e < P.Nh; ++it, e += gridDim.x) {
+    int b;
+    if (!slab_begin(bar, nbuf, it, e, P.Nh, P.status, issue, b)) break;
+    const FT *sY = at(Lo.y, b), *sF = at(Lo.f, b), *sG = at(Lo.g, b), *sL = at(Lo.lap, b);
+    const FT *sT = at(Lo.tb, b), *sTf = at(Lo.tbf, b);
+    const SlabGeo<FT> g{sG + NQ * j, sW + NQ * j};
+    auto levrow = [&](int v, LevRow<FT> &s) {
+      FT Jh[4], iJh[4], W[4], iW[4];
+      g.row(HG_JH, Jh);
+      g.row(HG_IJH, iJh);
+      g.w(W);
+      g.iw(iW);
+      s.set_rows(Jh, iJh, W, iW, P.levc[LC_R2 * Nv + v], P.levc[LC_IR2 * Nv + v], P.levc[LC_DZ * Nv + v],
+                 P.levc[LC_IDZ * Nv + v]);
+    };
+    // ---- C: forward centre values used by the face phase and the centre transpose
     for (int v0 = 0; v0 < Nv; v0 += AD_LEVELS) {
-      const int v = min(v0 + vl, Nv - 1);
-      const bool act = v0 + vl < Nv;
+      const int v = min(v0 + vs, Nv - 1);
+      const bool act = v0 + vs < Nv;
       LevRow<FT> s;
-      level_geo(P, g, v, s);
-      const FT idz = P.levc[LC_IDZ * Nv + v];
-      FT rho[4], u1[4], u2[4], L1[4], L2[4], L3[4], Ls[4];
-#pragma unroll
-      for (int i = 0; i < 4; ++i) {
-        const int q = (NQ * j + i) * Nv + v;
-        rho[i] = sY[q];
-        u1[i] = sY[16 * Nv + q];
-        u2[i] = sY[32 * Nv + q];
-        Ls[i] = sL[q];
-        L1[i] = sL[16 * Nv + q];
-        L2[i] = sL[32 * Nv + q];
-        L3[i] = sL[48 * Nv + q];
-      }
-      FT o1[4], o2[4], o3[4];
-      vec_lap(P, R, g, s, L1, L2, L3, P.div_damp, o1, o2, o3);
-      FT g1[4], g2[4], x1[4], x2[4], hd[4];
-      d1(P, Ls, g1);
-      d2(R, Ls, g2);
-#pragma unroll
-      for (int i = 0; i < 4; ++i) {
-        const FT gu0 = g.gu0[i] * s.ir2, gu1 = g.gu1[i] * s.ir2, gu2 = g.gu2[i] * s.ir2;
-        x1[i] = rho[i] * (gu0 * g1[i] + gu1 * g2[i]);
-        x2[i] = rho[i] * (gu1 * g1[i] + gu2 * g2[i]);
-      }
-      wdiv(P, R, s, x1, x2, hd);
-      FT om[4];
+      levrow(v, s);
+      const FT g3a = P.levf[LF_G33 * Nf + v], g3b = P.levf[LF_G33 * Nf + v + 1];
+      FT rho[4];
       {
-        FT Wu1[4], Wu2[4], ta[4], tb[4];
+        FT c1[4], c2[4], K[4], rJ[4], gu0[4], gu1[4], gu2[4];
+        g.gu(gu0, gu1, gu2);
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
-          Wu1[i] = g.W[i] * u1[i];
-          Wu2[i] = g.W[i] * u2[i];
+          const int n = NQ * j + i, q = n * Nv + v;
+          rho[i] = sY[q];
+          const FT u1 = sY[16 * Nv + q], u2 = sY[32 * Nv + q];
+          const FT x0 = gu0[i] * s.ir2, x1 = gu1[i] * s.ir2, x2 = gu2[i] * s.ir2;
+          c1[i] = x0 * u1 + x1 * u2;
+          c2[i] = x1 * u1 + x2 * u2;
+          const FT fa = v == 0 ? FT(0) : sF[n * Nf + v], fb = v + 1 == Nv ? FT(0) : sF[n * Nf + v + 1];
+          const FT kv = (fa * (fa * g3a) + fb * (fb * g3b)) / FT(2);
+          K[i] = (u1 * c1[i] + u2 * c2[i] + kv) / FT(2);
+          rJ[i] = rho[i] * s.J[i];
         }
-        t1(P, Wu2, ta);
-        t2(R, Wu1, tb);
+        if (act) {
+          st_row(crow(BC_C1, v), c1);
+          st_row(crow(BC_C2, v), c2);
+          st_row(crow(BC_K, v), K);
+          st_row(crow(BC_RJ, v), rJ);
+        }
+      }
+      FT o1[4], o2[4], o3[4];
+      {
+        FT L1[4], L2[4], L3[4];
 #pragma unroll
-        for (int i = 0; i < 4; ++i) om[i] = (-ta[i] + tb[i]) * s.iWJ[i];
+        for (int i = 0; i < 4; ++i) {
+          const int q = (NQ * j + i) * Nv + v;
+          L1[i] = sL[16 * Nv + q];
+          L2[i] = sL[32 * Nv + q];
+          L3[i] = sL[48 * Nv + q];
+        }
+        vec_lap(P, R, g, s, L1, L2, L3, P.div_damp, o1, o2, o3);
+      }
+      if (act) st_row(crow(BC_L4, v), o3);
+      FT hd[4];
+      {
+        FT Ls[4], g1[4], g2[4], x1[4], x2[4], gu0[4], gu1[4], gu2[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) Ls[i] = sL[(NQ * j + i) * Nv + v];
+        d1(P, Ls, g1);
+        d2(R, Ls, g2);
+        g.gu(gu0, gu1, gu2);
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          const FT y0 = gu0[i] * s.ir2, y1 = gu1[i] * s.ir2, y2 = gu2[i] * s.ir2;
+          x1[i] = rho[i] * (y0 * g1[i] + y1 * g2[i]);
+          x2[i] = rho[i] * (y1 * g1[i] + y2 * g2[i]);
+        }
+        wdiv(P, R, s, x1, x2, hd);
       }
       if (act) {
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
-          const int n = NQ * j + i, q = n * Nv + v;
-          const FT gu0 = g.gu0[i] * s.ir2, gu1 = g.gu1[i] * s.ir2, gu2 = g.gu2[i] * s.ir2;
-          const FT c1 = gu0 * u1[i] + gu1 * u2[i], c2 = gu1 * u1[i] + gu2 * u2[i];
-          sC1[q] = c1;
-          sC2[q] = c2;
-          sK[q] = (u1[i] * c1 + u2[i] * c2 + sKv[q]) / FT(2);
-          sRJ[q] = rho[i] * s.J[i];
-          sL4[q] = o3[i];
-          sA3[q] = sG[HG_F3 * NN + n] * idz + om[i];
+          const int q = (NQ * j + i) * Nv + v;
           dnu -= (double)(o1[i] * sT[16 * Nv + q] + o2[i] * sT[32 * Nv + q] + rpr * hd[i] * sT[48 * Nv + q]);
         }
       }
     }
     __syncthreads();
-    // ---- D: face phase, forward and reverse (the P3 cotangent of X is known from Tb and rho J)
+    // ---- D: face phase, forward and reverse (the cotangent of X follows from Tb and rho J)
     for (int k0 = 0; k0 < Nf; k0 += AD_LEVELS) {
       const int k = min(k0 + vl, Nf - 1);
       const bool act = k0 + vl < Nf;
       const bool inner = k > 0 && k < Nv;
       const FT r2 = P.levf[LF_R2 * Nf + k], dzf = P.levf[LF_DZ * Nf + k], rinv = P.levf[LF_RINV * Nf + k];
       const FT ir2f = P.levf[LF_IR2 * Nf + k], idzf = P.levf[LF_IDZ * Nf + k], g33 = P.levf[LF_G33 * Nf + k];
-      FT Wu[4], u3[4];
+      FT u3[4], ta[4], tb[4];
+      {
+        FT W[4], Wu[4];
+        g.w(W);
 #pragma unroll
-      for (int i = 0; i < 4; ++i) {
-        u3[i] = inner ? sF[(NQ * j + i) * Nf + k] : FT(0);
-        Wu[i] = g.W[i] * u3[i];
+        for (int i = 0; i < 4; ++i) {
+          u3[i] = inner ? sF[(NQ * j + i) * Nf + k] : FT(0);
+          Wu[i] = W[i] * u3[i];
+        }
+        t2(R, Wu, tb);
+        t1(P, Wu, ta);
       }
-      FT ta[4], tb[4];
-      t2(R, Wu, tb);
-      t1(P, Wu, ta);
+      // the levels below and above the face (both the adjacent level on a boundary face)
       const int va = k > 0 ? k - 1 : 0, vb = k < Nv ? k : Nv - 1;
-      FT tab[4], tbb[4], u3d[4];
-#pragma unroll
-      for (int i = 0; i < 4; ++i) {
-        const int n = NQ * j + i;
-        const int qa = n * Nv + va, qb = n * Nv + vb;
-        const FT Jf = g.Jh[i] * r2 * dzf;
-        const FT iJf = g.iJh[i] * ir2f * idzf, iWJf = g.iW[i] * iJf;
-        const FT w1 = -tb[i] * iWJf, w2 = ta[i] * iWJf;
-        FT cv1 = 0, cv2 = 0, cc1, cc2, l4, rJ;
-        if (inner) {
-          cv1 = -(sY[32 * Nv + qb] - sY[32 * Nv + qa]) * iJf;
-          cv2 = (sY[16 * Nv + qb] - sY[16 * Nv + qa]) * iJf;
-          cc1 = (sC1[qa] + sC1[qb]) / FT(2);
-          cc2 = (sC2[qa] + sC2[qb]) / FT(2);
-          const FT wa = sRJ[qa], wb = sRJ[qb];
-          l4 = gdiv(wa * sL4[qa] + wb * sL4[qb], wa + wb);
-          rJ = (wa + wb) / FT(2);
-        } else {
-          const int qq = k == 0 ? qb : qa;
-          cc1 = sC1[qq];
-          cc2 = sC2[qq];
-          l4 = sL4[qq];
-          rJ = sRJ[qq];
-        }
-        const FT fo1 = sG[HG_FH1 * NN + n] * rinv + cv1 + w1, fo2 = sG[HG_FH2 * NN + n] * rinv + cv2 + w2;
-        const FT b3 = rJ * (u3[i] * g33);
-        // X-cotangents from P3: t_i(v) = (X_i(v) + X_i(v+1)) / (2 rho J(v)) + ..., T_u_i -= t_i
-        FT Xb1 = 0, Xb2 = 0;
-        if (k >= 1) {
-          Xb1 -= sT[16 * Nv + qa] / (FT(2) * sRJ[qa]);
-          Xb2 -= sT[32 * Nv + qa] / (FT(2) * sRJ[qa]);
-        }
-        if (k < Nv) {
-          Xb1 -= sT[16 * Nv + qb] / (FT(2) * sRJ[qb]);
-          Xb2 -= sT[32 * Nv + qb] / (FT(2) * sRJ[qb]);
-        }
-        const FT T3b = sTf[n * Nf + k];
-        const FT b3b = Jf * (fo2 * Xb1 - fo1 * Xb2);
-        const FT fo1b = -Jf * b3 * Xb2 - Jf * cc2 * T3b;
-        const FT fo2b = Jf * b3 * Xb1 + Jf * cc1 * T3b;
-        if (act) {
-          sX1[n * Nf + k] = Jf * (fo2 * b3);
-          sX2[n * Nf + k] = Jf * (-fo1 * b3);
-          bCc1[n * Nf + k] = Jf * fo2 * T3b;
-          bCc2[n * Nf + k] = -Jf * fo1 * T3b;
-          bGK[n * Nf + k] = inner ? -T3b : FT(0);
-          bL4[n * Nf + k] = -nu * T3b;
-          bRJ[n * Nf + k] = b3b * u3[i] * g33;
-          bCv1[n * Nf + k] = inner ? fo1b * iJf : FT(0);
-          bCv2[n * Nf + k] = inner ? fo2b * iJf : FT(0);
-          dnu -= (double)(l4 * T3b);
-        }
-        u3d[i] = inner ? b3b * rJ * g33 : FT(0);
-        // w1 = -tb iWJf, w2 = ta iWJf  ->  cotangents of tb, ta
-        tbb[i] = -fo1b * iWJf;
-        tab[i] = fo2b * iWJf;
-      }
-      FT Wb[4], Wb2[4];
-      d1(P, tab, Wb);
-      d2(R, tbb, Wb2);
-      if (act) {
+      FT X1[4], X2[4], Cc1[4], Cc2[4], RJb[4], Cv1[4], Cv2[4], u3d[4], tab[4], tbb[4];
+      {
+        FT C1a[4], C1b[4], C2a[4], C2b[4], Ra[4], Rb[4], La[4], Lb[4];
+        ld_row(crow(BC_C1, va), C1a);
+        ld_row(crow(BC_C1, vb), C1b);
+        ld_row(crow(BC_C2, va), C2a);
+        ld_row(crow(BC_C2, vb), C2b);
+        ld_row(crow(BC_RJ, va), Ra);
+        ld_row(crow(BC_RJ, vb), Rb);
+        ld_row(crow(BC_L4, va), La);
+        ld_row(crow(BC_L4, vb), Lb);
+        FT Jh[4], iJh[4], iW[4], fh1[4], fh2[4];
+        g.row(HG_JH, Jh);
+        g.row(HG_IJH, iJh);
+        g.iw(iW);
+        g.row(HG_FH1, fh1);
+        g.row(HG_FH2, fh2);
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
           const int n = NQ * j + i;
-          bU3[n * Nf + k] = inner ? u3d[i] + g.W[i] * (Wb[i] + Wb2[i]) : FT(0);
+          const int qa = n * Nv + va, qb = n * Nv + vb;
+          const FT Jf = Jh[i] * r2 * dzf;
+          const FT iJf = iJh[i] * ir2f * idzf, iWJf = iW[i] * iJf;
+          const FT w1 = -tb[i] * iWJf, w2 = ta[i] * iWJf;
+          FT cv1 = 0, cv2 = 0, cc1, cc2, l4, rJ;
+          if (inner) {
+            cv1 = -(sY[32 * Nv + qb] - sY[32 * Nv + qa]) * iJf;
+            cv2 = (sY[16 * Nv + qb] - sY[16 * Nv + qa]) * iJf;
+            cc1 = (C1a[i] + C1b[i]) / FT(2);
+            cc2 = (C2a[i] + C2b[i]) / FT(2);
+            l4 = gdiv(Ra[i] * La[i] + Rb[i] * Lb[i], Ra[i] + Rb[i]);
+            rJ = (Ra[i] + Rb[i]) / FT(2);
+          } else {
+            cc1 = C1a[i];
+            cc2 = C2a[i];
+            l4 = La[i];
+            rJ = Ra[i];
+          }
+          const FT fo1 = fh1[i] * rinv + cv1 + w1, fo2 = fh2[i] * rinv + cv2 + w2;
+          const FT b3 = rJ * (u3[i] * g33);
+          // X-cotangents from P3: t_i(v) = (X_i(v) + X_i(v+1)) / (2 rho J(v)) + ..., T_u_i -= t_i
+          FT Xb1 = 0, Xb2 = 0;
+          if (k >= 1) {
+            Xb1 -= sT[16 * Nv + qa] / (FT(2) * Ra[i]);
+            Xb2 -= sT[32 * Nv + qa] / (FT(2) * Ra[i]);
+          }
+          if (k < Nv) {
+            Xb1 -= sT[16 * Nv + qb] / (FT(2) * Rb[i]);
+            Xb2 -= sT[32 * Nv + qb] / (FT(2) * Rb[i]);
+          }
+          const FT T3b = sTf[n * Nf + k];
+          const FT b3b = Jf * (fo2 * Xb1 - fo1 * Xb2);
+          const FT fo1b = -Jf * b3 * Xb2 - Jf * cc2 * T3b;
+          const FT fo2b = Jf * b3 * Xb1 + Jf * cc1 * T3b;
+          X1[i] = Jf * (fo2 * b3);
+          X2[i] = Jf * (-fo1 * b3);
+          Cc1[i] = Jf * fo2 * T3b;
+          Cc2[i] = -Jf * fo1 * T3b;
+          RJb[i] = b3b * u3[i] * g33;
+          Cv1[i] = inner ? fo1b * iJf : FT(0);
+          Cv2[i] = inner ? fo2b * iJf : FT(0);
+          if (act) dnu -= (double)(l4 * T3b);
+          u3d[i] = inner ? b3b * rJ * g33 : FT(0);
+          // w1 = -tb iWJf, w2 = ta iWJf  ->  cotangents of tb, ta
+          tbb[i] = -fo1b * iWJf;
+          tab[i] = fo2b * iWJf;
         }
+      }
+      FT Wb[4], Wb2[4], U3b[4];
+      d1(P, tab, Wb);
+      d2(R, tbb, Wb2);
+      {
+        FT W[4];
+        g.w(W);
+#pragma unroll
+        for (int i = 0; i < 4; ++i) U3b[i] = inner ? u3d[i] + W[i] * (Wb[i] + Wb2[i]) : FT(0);
+      }
+      if (act) {
+        st_row(frow(BF_X1, k), X1);
+        st_row(frow(BF_X2, k), X2);
+        st_row(frow(BF_CC1, k), Cc1);
+        st_row(frow(BF_CC2, k), Cc2);
+        st_row(frow(BF_RJ, k), RJb);
+        st_row(frow(BF_CV1, k), Cv1);
+        st_row(frow(BF_CV2, k), Cv2);
+        st_row(frow(BF_U3, k), U3b);
       }
     }
     __syncthreads();
-    // ---- G: centre phase: P3 and face gathers, then the P1 transpose
+    // ---- G: centre transpose (P3 and the face gathers, vorticity, hyperdiffusion,
+    // horizontal dynamics, thermodynamics), intermediates dying group by group
     FT *yb = Ybc + (size_t)e * 64 * Nv, *lb = Lbc + (size_t)e * 64 * Nv;
     for (int v0 = 0; v0 < Nv; v0 += AD_LEVELS) {
-      const int v = min(v0 + vl, Nv - 1);
-      const bool act = v0 + vl < Nv;
+      const int v = min(v0 + vs, Nv - 1);
+      const bool act = v0 + vs < Nv;
       LevRow<FT> s;
-      level_geo(P, g, v, s);
-      const FT Phi = P.levc[LC_PHI * Nv + v], beta = P.levc[LC_BETA * Nv + v], spg = P.levc[LC_SPG * Nv + v];
-      FT rho[4], u1[4], u2[4], rhoe[4], c1[4], c2[4], K[4];
-      FT Trb[4], Tu1b[4], Tu2b[4], Teb[4];
-      FT rhob[4], u1b[4], u2b[4], c1b[4], c2b[4], Kb[4], L4b[4], omb[4];
+      levrow(v, s);
+      const FT idz = P.levc[LC_IDZ * Nv + v];
+      const FT beta = P.levc[LC_BETA * Nv + v], spg = P.levc[LC_SPG * Nv + v];
+      const int vm = v > 0 ? v - 1 : v, vp = v + 1 < Nv ? v + 1 : v;
+      FT rhob[4], u1b[4], u2b[4], c1b[4], c2b[4], Kb[4], L4b[4];
+      {
+        FT Tu1b[4], Tu2b[4], RJv[4], RJb[4], omb[4];
 #pragma unroll
-      for (int i = 0; i < 4; ++i) {
-        const int n = NQ * j + i, q = n * Nv + v;
-        rho[i] = sY[q];
-        u1[i] = sY[16 * Nv + q];
-        u2[i] = sY[32 * Nv + q];
-        rhoe[i] = sY[48 * Nv + q];
-        c1[i] = sC1[q];
-        c2[i] = sC2[q];
-        K[i] = sK[q];
-        Trb[i] = sT[q];
-        Tu1b[i] = sT[16 * Nv + q];
-        Tu2b[i] = sT[32 * Nv + q];
-        Teb[i] = sT[48 * Nv + q];
-        const FT RJ = sRJ[q], iRJ = FT(1) / RJ;
+        for (int i = 0; i < 4; ++i) {
+          const int q = (NQ * j + i) * Nv + v;
+          Tu1b[i] = sT[16 * Nv + q];
+          Tu2b[i] = sT[32 * Nv + q];
+        }
+        ld_row(crow(BC_RJ, v), RJv);
         // P3: t_i = (X_i(v) + X_i(v+1)) / 2 / rho J + Cr_i, T_u_i -= t_i + beta u_i
-        const FT X1s = (sX1[n * Nf + v] + sX1[n * Nf + v + 1]) / FT(2);
-        const FT X2s = (sX2[n * Nf + v] + sX2[n * Nf + v + 1]) / FT(2);
-        const FT t1b = -Tu1b[i], t2b = -Tu2b[i];
-        FT RJb = -(X1s * t1b + X2s * t2b) * iRJ * iRJ;
-        const FT a3 = sA3[q];
-        // Cr1 = J (-a3 c2), Cr2 = J (a3 c1)
-        omb[i] = s.J[i] * (c1[i] * t2b - c2[i] * t1b);
-        c1b[i] = s.J[i] * a3 * t2b;
-        c2b[i] = -s.J[i] * a3 * t1b;
-        u1b[i] = -beta * Tu1b[i];
-        u2b[i] = -beta * Tu2b[i];
-        if (act) dal -= (double)(spg * (u1[i] * Tu1b[i] + u2[i] * Tu2b[i]));
-        Kb[i] = FT(0);
+        {
+          FT Xa1[4], Xb1[4], Xa2[4], Xb2[4];
+          ld_row(frow(BF_X1, v), Xa1);
+          ld_row(frow(BF_X1, v + 1), Xb1);
+          ld_row(frow(BF_X2, v), Xa2);
+          ld_row(frow(BF_X2, v + 1), Xb2);
+#pragma unroll
+          for (int i = 0; i < 4; ++i) {
+            const FT iRJ = FT(1) / RJv[i];
+            const FT X1s = (Xa1[i] + Xb1[i]) / FT(2), X2s = (Xa2[i] + Xb2[i]) / FT(2);
+            RJb[i] = -(X1s * (-Tu1b[i]) + X2s * (-Tu2b[i])) * iRJ * iRJ;
+          }
+        }
+        // Cr1 = J (-a3 c2), Cr2 = J (a3 c1) with a3 = f^3 + w^3, w^3 = wcurl(u_h) recomputed
+        {
+          FT u1[4], u2[4], om[4], C1v[4], C2v[4], f3[4];
+          {
+            FT W[4], Wu1[4], Wu2[4], ta[4], tb[4];
+            g.w(W);
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+              const int q = (NQ * j + i) * Nv + v;
+              u1[i] = sY[16 * Nv + q];
+              u2[i] = sY[32 * Nv + q];
+              Wu1[i] = W[i] * u1[i];
+              Wu2[i] = W[i] * u2[i];
+            }
+            t1(P, Wu2, ta);
+            t2(R, Wu1, tb);
+#pragma unroll
+            for (int i = 0; i < 4; ++i) om[i] = (-ta[i] + tb[i]) * s.iWJ[i];
+          }
+          ld_row(crow(BC_C1, v), C1v);
+          ld_row(crow(BC_C2, v), C2v);
+          g.row(HG_F3, f3);
+#pragma unroll
+          for (int i = 0; i < 4; ++i) {
+            const FT a3 = f3[i] * idz + om[i];
+            const FT t1b = -Tu1b[i], t2b = -Tu2b[i];
+            omb[i] = s.J[i] * (C1v[i] * t2b - C2v[i] * t1b);
+            c1b[i] = s.J[i] * a3 * t2b;
+            c2b[i] = -s.J[i] * a3 * t1b;
+            u1b[i] = -beta * Tu1b[i];
+            u2b[i] = -beta * Tu2b[i];
+            if (act) dal -= (double)(spg * (u1[i] * Tu1b[i] + u2[i] * Tu2b[i]));
+            Kb[i] = FT(0);
+          }
+        }
         // gathers from face v (this centre is its upper neighbour) and face v+1 (lower neighbour)
-        const int fl = n * Nf + v, fu = n * Nf + v + 1;
-        const FT L4v = sL4[q];
-        FT l4b = FT(0);
-        if (v > 0) {
-          const FT wa = sRJ[q - 1], wb = RJ, ws = wa + wb;
-          const FT l4 = (wa * sL4[q - 1] + wb * L4v) / ws;
-          c1b[i] += bCc1[fl] / FT(2);
-          c2b[i] += bCc2[fl] / FT(2);
-          Kb[i] += bGK[fl];
-          l4b += bL4[fl] * wb / ws;
-          RJb += bL4[fl] * (L4v - l4) / ws + bRJ[fl] / FT(2);
-          u1b[i] += bCv2[fl];
-          u2b[i] -= bCv1[fl];
-        } else {
-          c1b[i] += bCc1[fl];
-          c2b[i] += bCc2[fl];
-          l4b += bL4[fl];
-          RJb += bRJ[fl];
+        {
+          FT RJm[4], RJp[4], L4m[4], L4v[4], L4p[4];
+          ld_row(crow(BC_RJ, vm), RJm);
+          ld_row(crow(BC_RJ, vp), RJp);
+          ld_row(crow(BC_L4, vm), L4m);
+          ld_row(crow(BC_L4, v), L4v);
+          ld_row(crow(BC_L4, vp), L4p);
+          FT cc1l[4], cc1u[4], cc2l[4], cc2u[4], rjl[4], rju[4], cv1l[4], cv1u[4], cv2l[4], cv2u[4];
+          ld_row(frow(BF_CC1, v), cc1l);
+          ld_row(frow(BF_CC1, v + 1), cc1u);
+          ld_row(frow(BF_CC2, v), cc2l);
+          ld_row(frow(BF_CC2, v + 1), cc2u);
+          ld_row(frow(BF_RJ, v), rjl);
+          ld_row(frow(BF_RJ, v + 1), rju);
+          ld_row(frow(BF_CV1, v), cv1l);
+          ld_row(frow(BF_CV1, v + 1), cv1u);
+          ld_row(frow(BF_CV2, v), cv2l);
+          ld_row(frow(BF_CV2, v + 1), cv2u);
+#pragma unroll
+          for (int i = 0; i < 4; ++i) {
+            const int n = NQ * j + i;
+            // face cotangents of gK (-T3b on inner faces) and l4 (-nu T3b)
+            const FT T3l = sTf[n * Nf + v], T3u = sTf[n * Nf + v + 1];
+            const FT bl4l = -nu * T3l, bl4u = -nu * T3u;
+            FT l4b = FT(0);
+            if (v > 0) {
+              const FT wa = RJm[i], wb = RJv[i], ws = wa + wb;
+              const FT l4 = (wa * L4m[i] + wb * L4v[i]) / ws;
+              c1b[i] += cc1l[i] / FT(2);
+              c2b[i] += cc2l[i] / FT(2);
+              Kb[i] += -T3l;
+              l4b += bl4l * wb / ws;
+              RJb[i] += bl4l * (L4v[i] - l4) / ws + rjl[i] / FT(2);
+              u1b[i] += cv2l[i];
+              u2b[i] -= cv1l[i];
+            } else {
+              c1b[i] += cc1l[i];
+              c2b[i] += cc2l[i];
+              l4b += bl4l;
+              RJb[i] += rjl[i];
+            }
+            if (v + 1 < Nv) {
+              const FT wa = RJv[i], wb = RJp[i], ws = wa + wb;
+              const FT l4 = (wa * L4v[i] + wb * L4p[i]) / ws;
+              c1b[i] += cc1u[i] / FT(2);
+              c2b[i] += cc2u[i] / FT(2);
+              Kb[i] -= -T3u;
+              l4b += bl4u * wa / ws;
+              RJb[i] += bl4u * (L4v[i] - l4) / ws + rju[i] / FT(2);
+              u1b[i] -= cv2u[i];
+              u2b[i] += cv1u[i];
+            } else {
+              c1b[i] += cc1u[i];
+              c2b[i] += cc2u[i];
+              l4b += bl4u;
+              RJb[i] += rju[i];
+            }
+            L4b[i] = l4b;
+            rhob[i] = s.J[i] * RJb[i];
+          }
         }
-        if (v + 1 < Nv) {
-          const FT wa = RJ, wb = sRJ[q + 1], ws = wa + wb;
-          const FT l4 = (wa * L4v + wb * sL4[q + 1]) / ws;
-          c1b[i] += bCc1[fu] / FT(2);
-          c2b[i] += bCc2[fu] / FT(2);
-          Kb[i] -= bGK[fu];
-          l4b += bL4[fu] * wa / ws;
-          RJb += bL4[fu] * (L4v - l4) / ws + bRJ[fu] / FT(2);
-          u1b[i] -= bCv2[fu];
-          u2b[i] += bCv1[fu];
-        } else {
-          c1b[i] += bCc1[fu];
-          c2b[i] += bCc2[fu];
-          l4b += bL4[fu];
-          RJb += bRJ[fu];
+        // vorticity: om = (-t1(W u2) + t2(W u1)) / WJ
+        {
+          FT tab[4], tbb[4], da[4], db[4], W[4];
+#pragma unroll
+          for (int i = 0; i < 4; ++i) {
+            tab[i] = -omb[i] * s.iWJ[i];
+            tbb[i] = omb[i] * s.iWJ[i];
+          }
+          d1(P, tab, da);
+          d2(R, tbb, db);
+          g.w(W);
+#pragma unroll
+          for (int i = 0; i < 4; ++i) {
+            u2b[i] += W[i] * da[i];
+            u1b[i] += W[i] * db[i];
+          }
         }
-        L4b[i] = l4b;
-        rhob[i] = s.J[i] * RJb;
       }
       // ---- hyperdiffusion: T_u -= nu o(L), T_rhoe -= nu_s wdiv(rho g^-1 grad L_s), o3 -> faces (L4)
       {
         FT o1b[4], o2b[4], L1b[4], L2b[4], L3b[4];
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
-          o1b[i] = -nu * Tu1b[i];
-          o2b[i] = -nu * Tu2b[i];
+          const int q = (NQ * j + i) * Nv + v;
+          o1b[i] = -nu * sT[16 * Nv + q];
+          o2b[i] = -nu * sT[32 * Nv + q];
         }
         vec_lap_t(P, R, g, s, o1b, o2b, L4b, P.div_damp, L1b, L2b, L3b);
-        FT hdb[4], xb1[4], xb2[4], Ls[4], g1[4], g2[4];
-#pragma unroll
-        for (int i = 0; i < 4; ++i) {
-          hdb[i] = -nus * Teb[i];
-          Ls[i] = sL[(NQ * j + i) * Nv + v];
-        }
-        wdiv_t(P, R, s, hdb, xb1, xb2);
-        d1(P, Ls, g1);
-        d2(R, Ls, g2);
-        FT gb1[4], gb2[4], Lsb[4];
-#pragma unroll
-        for (int i = 0; i < 4; ++i) {
-          const FT gu0 = g.gu0[i] * s.ir2, gu1 = g.gu1[i] * s.ir2, gu2 = g.gu2[i] * s.ir2;
-          rhob[i] += (gu0 * g1[i] + gu1 * g2[i]) * xb1[i] + (gu1 * g1[i] + gu2 * g2[i]) * xb2[i];
-          gb1[i] = rho[i] * (gu0 * xb1[i] + gu1 * xb2[i]);
-          gb2[i] = rho[i] * (gu1 * xb1[i] + gu2 * xb2[i]);
-        }
-        grad_t(P, R, gb1, gb2, Lsb);
         if (act) {
 #pragma unroll
           for (int i = 0; i < 4; ++i) {
             const int q = (NQ * j + i) * Nv + v;
-            lb[q] = Lsb[i];
             lb[16 * Nv + q] = L1b[i];
             lb[32 * Nv + q] = L2b[i];
             lb[48 * Nv + q] = L3b[i];
           }
         }
       }
-      // ---- vorticity: om = (-t1(W u2) + t2(W u1)) / WJ
       {
-        FT tab[4], tbb[4], da[4], db[4];
+        FT hdb[4], xb1[4], xb2[4], Ls[4], g1[4], g2[4], gb1[4], gb2[4], Lsb[4];
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
-          tab[i] = -omb[i] * s.iWJ[i];
-          tbb[i] = omb[i] * s.iWJ[i];
+          const int q = (NQ * j + i) * Nv + v;
+          hdb[i] = -nus * sT[48 * Nv + q];
+          Ls[i] = sL[q];
         }
-        d1(P, tab, da);
-        d2(R, tbb, db);
+        wdiv_t(P, R, s, hdb, xb1, xb2);
+        d1(P, Ls, g1);
+        d2(R, Ls, g2);
+        FT gu0[4], gu1[4], gu2[4];
+        g.gu(gu0, gu1, gu2);
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
-          u2b[i] += g.W[i] * da[i];
-          u1b[i] += g.W[i] * db[i];
+          const FT rho = sY[(NQ * j + i) * Nv + v];
+          const FT x0 = gu0[i] * s.ir2, x1 = gu1[i] * s.ir2, x2 = gu2[i] * s.ir2;
+          rhob[i] += (x0 * g1[i] + x1 * g2[i]) * xb1[i] + (x1 * g1[i] + x2 * g2[i]) * xb2[i];
+          gb1[i] = rho * (x0 * xb1[i] + x1 * xb2[i]);
+          gb2[i] = rho * (x1 * xb1[i] + x2 * xb2[i]);
+        }
+        grad_t(P, R, gb1, gb2, Lsb);
+        if (act) {
+#pragma unroll
+          for (int i = 0; i < 4; ++i) lb[(NQ * j + i) * Nv + v] = Lsb[i];
         }
       }
       // ---- forward thermodynamics and the horizontal-dynamics transpose
-      FT h[4], Pi[4], thp[4], tp[4], F1[4], F2[4];
+      const FT Phi = P.levc[LC_PHI * Nv + v];
+      FT rho[4], rhoe[4], K[4], c1[4], c2[4], h[4], Pi[4], thp[4];
+      ld_row(crow(BC_K, v), K);
+      ld_row(crow(BC_C1, v), c1);
+      ld_row(crow(BC_C2, v), c2);
 #pragma unroll
       for (int i = 0; i < 4; ++i) {
+        const int q = (NQ * j + i) * Nv + v;
+        rho[i] = sY[q];
+        rhoe[i] = sY[48 * Nv + q];
         Thermo<FT> th;
         thermo(P, rho[i], rhoe[i], K[i], Phi, th);
         h[i] = th.h;
         Pi[i] = th.Pi;
         thp[i] = th.thv - th.thvr;
-        tp[i] = thp[i] * Pi[i];
-        F1[i] = rho[i] * c1[i];
-        F2[i] = rho[i] * c2[i];
       }
       FT hb_[4], Pib[4], thpb[4], phirb[4];
       {
-        // T_u_i = -(a_i + cp (thp b_i + e_i - Pi f_i) / 2), a = grad tmp, b = grad Pi, e = grad tp, f = grad thp
-        FT b1[4], b2[4], f1[4], f2[4];
+        // T_u_i = -(g_i + cp (thp b_i - Pi f_i) / 2), g = grad(K + Phi - Phi_r + cp thp Pi / 2),
+        // b = grad Pi, f = grad thp
+        FT Tu1b[4], Tu2b[4], b1[4], b2[4], f1[4], f2[4], x1[4], x2[4], x[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          const int q = (NQ * j + i) * Nv + v;
+          Tu1b[i] = sT[16 * Nv + q];
+          Tu2b[i] = sT[32 * Nv + q];
+        }
         d1(P, Pi, b1);
         d2(R, Pi, b2);
         d1(P, thp, f1);
         d2(R, thp, f2);
-        FT ab1[4], ab2[4], bb1[4], bb2[4], eb1[4], eb2[4], fb1[4], fb2[4];
-        const FT hc = P.cpd / FT(2);
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
-          ab1[i] = -Tu1b[i];
-          ab2[i] = -Tu2b[i];
-          bb1[i] = -hc * thp[i] * Tu1b[i];
-          bb2[i] = -hc * thp[i] * Tu2b[i];
-          eb1[i] = -hc * Tu1b[i];
-          eb2[i] = -hc * Tu2b[i];
-          fb1[i] = hc * Pi[i] * Tu1b[i];
-          fb2[i] = hc * Pi[i] * Tu2b[i];
           thpb[i] = -hc * (b1[i] * Tu1b[i] + b2[i] * Tu2b[i]);
           Pib[i] = hc * (f1[i] * Tu1b[i] + f2[i] * Tu2b[i]);
+          x1[i] = -Tu1b[i];
+          x2[i] = -Tu2b[i];
         }
-        FT tmpb[4], x[4], tpb[4];
-        grad_t(P, R, ab1, ab2, tmpb);
-        grad_t(P, R, bb1, bb2, x);
-        grad_t(P, R, eb1, eb2, tpb);
-#pragma unroll
-        for (int i = 0; i < 4; ++i) Pib[i] += x[i];
-        grad_t(P, R, fb1, fb2, x);
+        FT gb[4];  // cotangent of the fused gradient's argument
+        grad_t(P, R, x1, x2, gb);
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
-          thpb[i] += x[i] + Pi[i] * tpb[i];
-          Pib[i] += thp[i] * tpb[i];
-          Kb[i] += tmpb[i];
-          phirb[i] = -tmpb[i];
+          x1[i] = -hc * thp[i] * Tu1b[i];
+          x2[i] = -hc * thp[i] * Tu2b[i];
+        }
+        grad_t(P, R, x1, x2, x);
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          Pib[i] += x[i];
+          x1[i] = hc * Pi[i] * Tu1b[i];
+          x2[i] = hc * Pi[i] * Tu2b[i];
+        }
+        grad_t(P, R, x1, x2, x);
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          const FT tpb = hc * gb[i];  // of th' Pi
+          thpb[i] += x[i] + Pi[i] * tpb;
+          Pib[i] += thp[i] * tpb;
+          Kb[i] += gb[i];
+          phirb[i] = -gb[i];
         }
       }
       {
         // T_rho = -dm, T_rhoe = -(dmh + h dm + F . grad h) / 2, dm = wdiv(F), dmh = wdiv(F h)
-        FT dm[4], ha[4], hbv[4];
+        FT F1[4], F2[4], dm[4], ha[4], hbv[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          F1[i] = rho[i] * c1[i];
+          F2[i] = rho[i] * c2[i];
+        }
         wdiv(P, R, s, F1, F2, dm);
         d1(P, h, ha);
         d2(R, h, hbv);
         FT dmb[4], dmhb[4], hab[4], hbb[4], F1b[4], F2b[4];
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
-          const FT q = Teb[i] / FT(2);
-          dmb[i] = -Trb[i] - h[i] * q;
-          dmhb[i] = -q;
-          hb_[i] = -dm[i] * q;
-          F1b[i] = -ha[i] * q;
-          F2b[i] = -hbv[i] * q;
-          hab[i] = -F1[i] * q;
-          hbb[i] = -F2[i] * q;
+          const int q = (NQ * j + i) * Nv + v;
+          const FT qq = sT[48 * Nv + q] / FT(2);
+          dmb[i] = -sT[q] - h[i] * qq;
+          dmhb[i] = -qq;
+          hb_[i] = -dm[i] * qq;
+          F1b[i] = -ha[i] * qq;
+          F2b[i] = -hbv[i] * qq;
+          hab[i] = -F1[i] * qq;
+          hbb[i] = -F2[i] * qq;
         }
         FT x[4], y1[4], y2[4];
         grad_t(P, R, hab, hbb, x);
@@ -639,9 +798,11 @@ __global__ void __launch_bounds__(AD_THREADS, AdMinBlocks<FT>::value) k_passB_vj
         }
       }
       if (act) {
+        FT kvb[4], gu0[4], gu1[4], gu2[4];
+        g.gu(gu0, gu1, gu2);
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
-          const int n = NQ * j + i, q = n * Nv + v;
+          const int q = (NQ * j + i) * Nv + v;
           ThermoBar<FT> tb{};
           tb.h = hb_[i];
           tb.Pi = Pib[i];
@@ -651,41 +812,58 @@ __global__ void __launch_bounds__(AD_THREADS, AdMinBlocks<FT>::value) k_passB_vj
           FT rb, reb, kb;
           thermo_vjp(P, rho[i], rhoe[i], K[i], Phi, tb, rb, reb, kb);
           const FT Kt = Kb[i] + kb;
-          const FT gu0 = g.gu0[i] * s.ir2, gu1 = g.gu1[i] * s.ir2, gu2 = g.gu2[i] * s.ir2;
+          const FT x0 = gu0[i] * s.ir2, x1 = gu1[i] * s.ir2, x2 = gu2[i] * s.ir2;
           yb[q] += rhob[i] + rb;
-          yb[16 * Nv + q] += u1b[i] + c1[i] * Kt + gu0 * c1b[i] + gu1 * c2b[i];
-          yb[32 * Nv + q] += u2b[i] + c2[i] * Kt + gu1 * c1b[i] + gu2 * c2b[i];
+          yb[16 * Nv + q] += u1b[i] + c1[i] * Kt + x0 * c1b[i] + x1 * c2b[i];
+          yb[32 * Nv + q] += u2b[i] + c2[i] * Kt + x1 * c1b[i] + x2 * c2b[i];
           yb[48 * Nv + q] += reb;
-          const FT a = v == 0 ? FT(0) : sF[n * Nf + v], bt = v + 1 == Nv ? FT(0) : sF[n * Nf + v + 1];
-          const FT Kvb = Kt / FT(2);
-          sLo[q] = v == 0 ? FT(0) : Kvb * a * P.levf[LF_G33 * Nf + v];
-          sHi[q] = v + 1 == Nv ? FT(0) : Kvb * bt * P.levf[LF_G33 * Nf + v + 1];
+          kvb[i] = Kt / FT(2);
         }
+        st_row(sKvb + (size_t)v * NN + NQ * j, kvb);
       }
     }
     __syncthreads();
+    // inner face k: the face-phase cotangent of u_3 and the K_v cotangents of levels k-1, k
     FT *fb = Ybf + (size_t)e * 16 * Nf;
-    for (int idx = threadIdx.x; idx < 16 * Nf; idx += blockDim.x) {
-      const int n = idx / Nf, f = idx - n * Nf;
-      if (f > 0 && f < Nv) fb[idx] += bU3[idx] + sHi[n * Nv + f - 1] + sLo[n * Nv + f];
+    for (int k0 = 1; k0 < Nv; k0 += AD_LEVELS) {
+      const int k = k0 + vl;
+      if (k < Nv) {
+        FT U3b[4], Km[4], Kp[4];
+        ld_row(frow(BF_U3, k), U3b);
+        ld_row(sKvb + (size_t)(k - 1) * NN + NQ * j, Km);
+        ld_row(sKvb + (size_t)k * NN + NQ * j, Kp);
+        const FT g33 = P.levf[LF_G33 * Nf + k];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          const int idx = (NQ * j + i) * Nf + k;
+          const FT u3 = sF[idx];
+          fb[idx] += U3b[i] + Km[i] * u3 * g33 + Kp[i] * u3 * g33;
+        }
+      }
     }
+    // every thread is done with this element's slabs before they are refilled
     __syncthreads();
   }
-  // parameter cotangents: block sums in a fixed order, one slot per CTA
-  __shared__ double red[2][AD_THREADS];
-  red[0][threadIdx.x] = dnu;
-  red[1][threadIdx.x] = dal;
+  // parameter cotangents: warp sums, then the warps in a fixed order; one slot per CTA
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    dnu += __shfl_xor_sync(0xffffffffu, dnu, o);
+    dal += __shfl_xor_sync(0xffffffffu, dal, o);
+  }
+  const int warp = threadIdx.x >> 5;
+  if ((threadIdx.x & 31) == 0) {
+    red[warp] = dnu;
+    red[AD_THREADS / 32 + warp] = dal;
+  }
   __syncthreads();
-  for (int o = AD_THREADS / 2; o > 0; o >>= 1) {
-    if ((int)threadIdx.x < o) {
-      red[0][threadIdx.x] += red[0][threadIdx.x + o];
-      red[1][threadIdx.x] += red[1][threadIdx.x + o];
-    }
-    __syncthreads();
-  }
   if (threadIdx.x == 0) {  // accumulated over the launches of a reverse pass (zeroed by the host)
-    dpar[2 * blockIdx.x] += red[0][0];
-    dpar[2 * blockIdx.x + 1] += red[1][0];
+    double a = 0, c = 0;
+    for (int w = 0; w < AD_THREADS / 32; ++w) {
+      a += red[w];
+      c += red[AD_THREADS / 32 + w];
+    }
+    dpar[2 * blockIdx.x] += a;
+    dpar[2 * blockIdx.x + 1] += c;
   }
 }
 
@@ -697,7 +875,7 @@ size_t passA_vjp_smem(int Nv) {
 }
 template <class FT>
 size_t passB_vjp_smem(int Nv) {
-  return sizeof(FT) * passB_vjp_words<FT>(Nv);
+  return BvLayout<FT>(Nv, 1).total;
 }
 
 template <class FT>
@@ -714,20 +892,6 @@ void configure_adjoint_se(int Nv) {
   cudaFuncSetAttribute(k_passB_vjp<FT>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes);
 }
 
-// Persistent grids: the resident CTAs of each kernel at its shared-memory size.
-template <class K>
-int resident_grid(K kern, size_t smem, int Nh) {
-  static int nsm = 0;
-  if (!nsm) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-  }
-  int b = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kern, AD_THREADS, smem);
-  return std::max(1, std::min(Nh, nsm * std::max(1, b)));
-}
-
 template <class FT>
 void launch_passA_vjp(const DevParams<FT> &P, const FT *Yc, const FT *Yf, const FT *Lb, FT *Ybc, FT *Ybf, int grid,
                       cudaStream_t s) {
@@ -740,9 +904,9 @@ void launch_passA_vjp(const DevParams<FT> &P, const FT *Yc, const FT *Yf, const 
 template <class FT>
 void launch_passB_vjp(const DevParams<FT> &P, const FT *Yc, const FT *Yf, const FT *L, const FT *Tbc, const FT *Tbf,
                       FT *Ybc, FT *Ybf, FT *Lb, double *dpar, int grid, cudaStream_t s) {
-  const size_t sm = passB_vjp_smem<FT>(P.Nv);
-  const int g = std::min(grid, resident_grid(k_passB_vjp<FT>, sm, P.Nh));
-  k_passB_vjp<FT><<<g, AD_THREADS, sm, s>>>(P, Yc, Yf, L, Tbc, Tbf, Ybc, Ybf, Lb, dpar);
+  const AdShape sh = ad_shape<BvLayout<FT>>(P.Nv, AdMinBlocks<FT>::value);
+  const int g = std::max(1, std::min({grid, P.Nh, ad_dev().nsm * sh.ctas}));
+  k_passB_vjp<FT><<<g, AD_THREADS, sh.smem, s>>>(P, sh.nbuf, Yc, Yf, L, Tbc, Tbf, Ybc, Ybf, Lb, dpar);
 }
 
 #define INST(FT)                                                                                             \

@@ -475,7 +475,7 @@ int ensure_adjoint(gb_ctx *ctx) {
   CK(cudaGetDevice(&dev));
   CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
   CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-  if (passB_vjp_smem<FT>(I->P.Nv) + 2 * 256 * sizeof(double) > (size_t)optin ||
+  if (passB_vjp_smem<FT>(I->P.Nv) > (size_t)optin ||
       passA_vjp_smem<FT>(I->P.Nv) > (size_t)optin)
     return fail(ctx, GB_ERR_ARG, "z_elem too large for the reverse-mode slab kernels at this precision (shared memory)");
   configure_adjoint_se<FT>(I->P.Nv);

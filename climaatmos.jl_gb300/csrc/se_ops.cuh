@@ -298,22 +298,27 @@ __device__ __forceinline__ void centre_from_faces(const DevParams<FT> &P, const 
 // Transpose of vec_lap: given the cotangents (ob1, ob2, ob3) of (o1, o2, o3),
 // returns the cotangents (cb1, cb2, cb3) of (c1, c2, c3).  The forward sequence
 // run backwards, with d1 <-> t1 and d2 <-> t2.
-template <class FT>
-__device__ __forceinline__ void vec_lap_t(const DevParams<FT> &P, const Row<FT> &R, const RowGeo<FT> &g,
+template <class FT, class G>
+__device__ __forceinline__ void vec_lap_t(const DevParams<FT> &P, const Row<FT> &R, const G &g,
                                           const LevRow<FT> &s, const FT (&ob1)[4], const FT (&ob2)[4],
                                           const FT (&ob3)[4], FT fdiv, FT (&cb1)[4], FT (&cb2)[4], FT (&cb3)[4]) {
   FT f1b[4], f2b[4], f3b[4], f4b[4], w1b[4], w2b[4];
+  {
+    FT gd0[4], gd1[4], gd2[4], iW[4];
+    g.gd(gd0, gd1, gd2);
+    g.iw(iW);
 #pragma unroll
-  for (int i = 0; i < 4; ++i) {
-    const FT gd0 = g.gd0[i] * s.r2, gd1 = g.gd1[i] * s.r2, gd2 = g.gd2[i] * s.r2;
-    const FT q1b = -(gd0 * ob1[i] + gd1 * ob2[i]), q2b = -(gd1 * ob1[i] + gd2 * ob2[i]);
-    const FT q3b = -s.G33 * ob3[i];
-    w1b[i] = -fdiv * g.iW[i] * ob1[i];
-    w2b[i] = -fdiv * g.iW[i] * ob2[i];
-    f1b[i] = -q3b * s.iWJ[i];
-    f2b[i] = q3b * s.iWJ[i];
-    f3b[i] = -q1b * s.iWJ[i];
-    f4b[i] = q2b * s.iWJ[i];
+    for (int i = 0; i < 4; ++i) {
+      const FT x0 = gd0[i] * s.r2, x1 = gd1[i] * s.r2, x2 = gd2[i] * s.r2;
+      const FT q1b = -(x0 * ob1[i] + x1 * ob2[i]), q2b = -(x1 * ob1[i] + x2 * ob2[i]);
+      const FT q3b = -s.G33 * ob3[i];
+      w1b[i] = -fdiv * iW[i] * ob1[i];
+      w2b[i] = -fdiv * iW[i] * ob2[i];
+      f1b[i] = -q3b * s.iWJ[i];
+      f2b[i] = q3b * s.iWJ[i];
+      f3b[i] = -q1b * s.iWJ[i];
+      f4b[i] = q2b * s.iWJ[i];
+    }
   }
   FT Wz1b[4], Wz2b[4], Wz3b[4], tmp[4];
   d1(P, f1b, Wz2b);
@@ -321,17 +326,22 @@ __device__ __forceinline__ void vec_lap_t(const DevParams<FT> &P, const Row<FT> 
   d2(R, f3b, Wz3b);
   d1(P, f4b, tmp);
   FT e1b[4], e2b[4], e3b[4], e4b[4];
+  {
+    FT gd0[4], gd1[4], gd2[4], W[4];
+    g.gd(gd0, gd1, gd2);
+    g.w(W);
 #pragma unroll
-  for (int i = 0; i < 4; ++i) {
-    Wz3b[i] += tmp[i];
-    const FT gd0 = g.gd0[i] * s.r2, gd1 = g.gd1[i] * s.r2, gd2 = g.gd2[i] * s.r2;
-    const FT k1b = g.W[i] * (gd0 * Wz1b[i] + gd1 * Wz2b[i]);
-    const FT k2b = g.W[i] * (gd1 * Wz1b[i] + gd2 * Wz2b[i]);
-    const FT k3b = g.W[i] * (s.G33 * Wz3b[i]);
-    e1b[i] = k3b * s.iJ[i];
-    e2b[i] = -k3b * s.iJ[i];
-    e3b[i] = k1b * s.iJ[i];
-    e4b[i] = -k2b * s.iJ[i];
+    for (int i = 0; i < 4; ++i) {
+      Wz3b[i] += tmp[i];
+      const FT x0 = gd0[i] * s.r2, x1 = gd1[i] * s.r2, x2 = gd2[i] * s.r2;
+      const FT k1b = W[i] * (x0 * Wz1b[i] + x1 * Wz2b[i]);
+      const FT k2b = W[i] * (x1 * Wz1b[i] + x2 * Wz2b[i]);
+      const FT k3b = W[i] * (s.G33 * Wz3b[i]);
+      e1b[i] = k3b * s.iJ[i];
+      e2b[i] = -k3b * s.iJ[i];
+      e3b[i] = k1b * s.iJ[i];
+      e4b[i] = -k2b * s.iJ[i];
+    }
   }
   t1(P, e1b, cb2);
   t2(R, e2b, cb1);
@@ -341,19 +351,27 @@ __device__ __forceinline__ void vec_lap_t(const DevParams<FT> &P, const Row<FT> 
   d1(P, w1b, wdvb);
   d2(R, w2b, t2b);
   FT dab[4];
+  {
+    FT W[4];
+    g.w(W);
 #pragma unroll
-  for (int i = 0; i < 4; ++i) {
-    cb3[i] += tmp[i];
-    dab[i] = g.W[i] * s.iJ[i] * (wdvb[i] + t2b[i]);
+    for (int i = 0; i < 4; ++i) {
+      cb3[i] += tmp[i];
+      dab[i] = W[i] * s.iJ[i] * (wdvb[i] + t2b[i]);
+    }
   }
   FT ab[4], bb[4];
   t1(P, dab, ab);
   t2(R, dab, bb);
+  {
+    FT gu0[4], gu1[4], gu2[4];
+    g.gu(gu0, gu1, gu2);
 #pragma unroll
-  for (int i = 0; i < 4; ++i) {
-    const FT gu0 = g.gu0[i] * s.ir2, gu1 = g.gu1[i] * s.ir2, gu2 = g.gu2[i] * s.ir2;
-    cb1[i] += s.J[i] * (gu0 * ab[i] + gu1 * bb[i]);
-    cb2[i] += s.J[i] * (gu1 * ab[i] + gu2 * bb[i]);
+    for (int i = 0; i < 4; ++i) {
+      const FT x0 = gu0[i] * s.ir2, x1 = gu1[i] * s.ir2, x2 = gu2[i] * s.ir2;
+      cb1[i] += s.J[i] * (x0 * ab[i] + x1 * bb[i]);
+      cb2[i] += s.J[i] * (x1 * ab[i] + x2 * bb[i]);
+    }
   }
 }
 
@@ -385,16 +403,20 @@ __device__ __forceinline__ void grad_t(const DevParams<FT> &P, const Row<FT> &R,
 }
 
 // Transpose of the scalar Laplacian Ls = wdiv(g^-1 grad sd) (with the row's g^ij / r^2).
-template <class FT>
-__device__ __forceinline__ void lap_t(const DevParams<FT> &P, const Row<FT> &R, const RowGeo<FT> &g,
+template <class FT, class G>
+__device__ __forceinline__ void lap_t(const DevParams<FT> &P, const Row<FT> &R, const G &g,
                                       const LevRow<FT> &s, const FT (&Lb)[4], FT (&sdb)[4]) {
   FT xb1[4], xb2[4], gb1[4], gb2[4];
   wdiv_t(P, R, s, Lb, xb1, xb2);
+  {
+    FT gu0[4], gu1[4], gu2[4];
+    g.gu(gu0, gu1, gu2);
 #pragma unroll
-  for (int i = 0; i < 4; ++i) {
-    const FT gu0 = g.gu0[i] * s.ir2, gu1 = g.gu1[i] * s.ir2, gu2 = g.gu2[i] * s.ir2;
-    gb1[i] = gu0 * xb1[i] + gu1 * xb2[i];
-    gb2[i] = gu1 * xb1[i] + gu2 * xb2[i];
+    for (int i = 0; i < 4; ++i) {
+      const FT x0 = gu0[i] * s.ir2, x1 = gu1[i] * s.ir2, x2 = gu2[i] * s.ir2;
+      gb1[i] = x0 * xb1[i] + x1 * xb2[i];
+      gb2[i] = x1 * xb1[i] + x2 * xb2[i];
+    }
   }
   grad_t(P, R, gb1, gb2, sdb);
 }

@@ -11,10 +11,10 @@
 // Both recompute the forward intermediates of one element from the state
 // slab and run the forward sequence backwards (the SE operators transpose as
 // d1 <-> t1, d2 <-> t2).  One CTA per element at a time, 256 threads in the
-// forward (level, row) mapping; slabs are read with coalesced loads into
-// shared memory.  The state cotangent is accumulated (+=) element by element:
-// each element owns its nodes, so there are no write conflicts; the DSS
-// transpose that precedes/follows is a separate kernel.
+// forward (level, row) mapping; the slabs of each element arrive by TMA bulk
+// copies.  The state cotangent is accumulated (or, by pass B^T on request,
+// written) element by element: each element owns its nodes, so there are no
+// write conflicts; the DSS transposes before and after are separate kernels.
 #include <algorithm>
 
 #include "se_ops.cuh"
@@ -225,8 +225,8 @@ __global__ void __launch_bounds__(AD_THREADS, AdMinBlocks<FT>::value)
 // Scratch, level-major rows ([Nv][16] or [Nf][16], one 16-byte row per
 // thread): the forward centre values c1, c2, K, rho J, o3; the forward face
 // cross products X1, X2 and the face cotangents; the K_v cotangent.  The
-// state cotangent is accumulated in global memory (each element owns its
-// nodes); the Laplacian cotangent is written.
+// state cotangent goes to global memory, added (accum) or written; the
+// Laplacian cotangent is written.
 enum BvCentre { BC_C1 = 0, BC_C2, BC_K, BC_RJ, BC_L4, BC_N };
 enum BvFace { BF_X1 = 0, BF_X2, BF_CC1, BF_CC2, BF_RJ, BF_CV1, BF_CV2, BF_U3, BF_N };
 
@@ -262,7 +262,8 @@ template <class FT>
 __global__ void __launch_bounds__(AD_THREADS, AdMinBlocks<FT>::value)
     k_passB_vjp(DevParams<FT> P, int nbuf, const FT *__restrict__ Yc, const FT *__restrict__ Yf,
                 const FT *__restrict__ Lc, const FT *__restrict__ Tbc, const FT *__restrict__ Tbf,
-                FT *__restrict__ Ybc, FT *__restrict__ Ybf, FT *__restrict__ Lbc, double *__restrict__ dpar) {
+                FT *__restrict__ Ybc, FT *__restrict__ Ybf, FT *__restrict__ Lbc, double *__restrict__ dpar,
+                int accum) {
   extern __shared__ __align__(128) unsigned char sm[];
   const int Nv = P.Nv, Nf = P.Nf;
   const BvLayout<FT> Lo(Nv, nbuf);
@@ -813,10 +814,19 @@ __global__ void __launch_bounds__(AD_THREADS, AdMinBlocks<FT>::value)
           thermo_vjp(P, rho[i], rhoe[i], K[i], Phi, tb, rb, reb, kb);
           const FT Kt = Kb[i] + kb;
           const FT x0 = gu0[i] * s.ir2, x1 = gu1[i] * s.ir2, x2 = gu2[i] * s.ir2;
-          yb[q] += rhob[i] + rb;
-          yb[16 * Nv + q] += u1b[i] + c1[i] * Kt + x0 * c1b[i] + x1 * c2b[i];
-          yb[32 * Nv + q] += u2b[i] + c2[i] * Kt + x1 * c1b[i] + x2 * c2b[i];
-          yb[48 * Nv + q] += reb;
+          const FT o0 = rhob[i] + rb, o1 = u1b[i] + c1[i] * Kt + x0 * c1b[i] + x1 * c2b[i];
+          const FT o2 = u2b[i] + c2[i] * Kt + x1 * c1b[i] + x2 * c2b[i];
+          if (accum) {
+            yb[q] += o0;
+            yb[16 * Nv + q] += o1;
+            yb[32 * Nv + q] += o2;
+            yb[48 * Nv + q] += reb;
+          } else {
+            yb[q] = o0;
+            yb[16 * Nv + q] = o1;
+            yb[32 * Nv + q] = o2;
+            yb[48 * Nv + q] = reb;
+          }
           kvb[i] = Kt / FT(2);
         }
         st_row(sKvb + (size_t)v * NN + NQ * j, kvb);
@@ -837,8 +847,18 @@ __global__ void __launch_bounds__(AD_THREADS, AdMinBlocks<FT>::value)
         for (int i = 0; i < 4; ++i) {
           const int idx = (NQ * j + i) * Nf + k;
           const FT u3 = sF[idx];
-          fb[idx] += U3b[i] + Km[i] * u3 * g33 + Kp[i] * u3 * g33;
+          const FT o = U3b[i] + Km[i] * u3 * g33 + Kp[i] * u3 * g33;
+          if (accum) fb[idx] += o;
+          else fb[idx] = o;
         }
+      }
+    }
+    // overwrite: the boundary faces have no cotangent
+    if (!accum && vl == 0) {
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        fb[(NQ * j + i) * Nf] = FT(0);
+        fb[(NQ * j + i) * Nf + Nv] = FT(0);
       }
     }
     // every thread is done with this element's slabs before they are refilled
@@ -903,10 +923,10 @@ void launch_passA_vjp(const DevParams<FT> &P, const FT *Yc, const FT *Yf, const 
 // grid: the number of parameter-partial slots (CTAs) the caller allocated.
 template <class FT>
 void launch_passB_vjp(const DevParams<FT> &P, const FT *Yc, const FT *Yf, const FT *L, const FT *Tbc, const FT *Tbf,
-                      FT *Ybc, FT *Ybf, FT *Lb, double *dpar, int grid, cudaStream_t s) {
+                      FT *Ybc, FT *Ybf, FT *Lb, double *dpar, int grid, bool accum, cudaStream_t s) {
   const AdShape sh = ad_shape<BvLayout<FT>>(P.Nv, AdMinBlocks<FT>::value);
   const int g = std::max(1, std::min({grid, P.Nh, ad_dev().nsm * sh.ctas}));
-  k_passB_vjp<FT><<<g, AD_THREADS, sh.smem, s>>>(P, sh.nbuf, Yc, Yf, L, Tbc, Tbf, Ybc, Ybf, Lb, dpar);
+  k_passB_vjp<FT><<<g, AD_THREADS, sh.smem, s>>>(P, sh.nbuf, Yc, Yf, L, Tbc, Tbf, Ybc, Ybf, Lb, dpar, accum ? 1 : 0);
 }
 
 #define INST(FT)                                                                                             \
@@ -916,7 +936,7 @@ void launch_passB_vjp(const DevParams<FT> &P, const FT *Yc, const FT *Yf, const 
   template void launch_passA_vjp<FT>(const DevParams<FT> &, const FT *, const FT *, const FT *, FT *, FT *, int, \
                                      cudaStream_t);                                                          \
   template void launch_passB_vjp<FT>(const DevParams<FT> &, const FT *, const FT *, const FT *, const FT *,      \
-                                     const FT *, FT *, FT *, FT *, double *, int, cudaStream_t);
+                                     const FT *, FT *, FT *, FT *, double *, int, bool, cudaStream_t);
 INST(float)
 INST(double)
 #undef INST

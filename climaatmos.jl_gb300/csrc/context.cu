@@ -49,7 +49,7 @@ struct Impl : ImplBase {
   struct Adjoint {
     std::vector<std::unique_ptr<Record>> rec;
     std::vector<std::unique_ptr<DevBuf>> ckpt;
-    DevBuf Ub, Tb, Lb, Teb[4], Tib[4], zero, dummy, scr, dparB, dal, dacc, work;
+    DevBuf Ub, Lb, Teb[4], Tib[4], zero, dummy, scr, dparB, dal, dacc, work;
     int nsteps = 0, every = 0, grid = 0;
     double dt = 0;
     bool ready = false;
@@ -426,7 +426,7 @@ int time_kernel_t(gb_ctx *ctx, int kernel, gb_fieldvec Y, int reps, double *ms) 
       case GB_K_DSS: launch_dss<FT>(P, Yc, Yf, s); break;
       case GB_K_PASSA_VJP: launch_passA_vjp<FT>(P, Yc, Yf, lap, Ubc, Ubf, I->adj->grid, s); break;
       case GB_K_PASSB_VJP:
-        launch_passB_vjp<FT>(P, Yc, Yf, lap, Tc, Tf, Ubc, Ubf, Lbc, (double *)I->adj->dparB.p, I->adj->grid, s);
+        launch_passB_vjp<FT>(P, Yc, Yf, lap, Tc, Tf, Ubc, Ubf, Lbc, (double *)I->adj->dparB.p, I->adj->grid, false, s);
         break;
       case GB_K_COLUMN_VJP:
         launch_column_stage_vjp<FT>(P, SA, Tc, Tf, (const FT *)I->Ti[1].p, (const FT *)I->Ti[1].p + I->NR, Ubc, Ubf,
@@ -485,7 +485,7 @@ int ensure_adjoint(gb_ctx *ctx) {
   A->grid = std::min(I->P.Nh, 4 * nsm);  // parameter-partial slots: at most 4 resident CTAs per SM
   size_t &t = A->bytes;
   int r;
-  if ((r = alloc_z<FT>(ctx, A->Ub, S, t)) || (r = alloc_z<FT>(ctx, A->Tb, S, t)) ||
+  if ((r = alloc_z<FT>(ctx, A->Ub, S, t)) ||
       (r = alloc_z<FT>(ctx, A->Lb, I->NC * sizeof(FT), t)) || (r = alloc_z<FT>(ctx, A->zero, S, t)) ||
       (r = alloc_z<FT>(ctx, A->dummy, S, t)) || (r = alloc_z<FT>(ctx, A->work, S, t)) ||
       (r = alloc_z<FT>(ctx, A->scr, col_vjp_scratch_words(I->P.Nh, I->P.Nv) * sizeof(FT), t)) ||
@@ -586,21 +586,20 @@ void record_step(gb_ctx *ctx, FT *Yc, FT *Yf, double dt_, typename Impl<FT>::Rec
   launch_final<FT>(P, A, Yc, Yf, s);
 }
 
-// Reverse of the explicit tendency of one stage state U: Ub += (dT/dU)^T Tb_in
-// where Tb_in (copied, not modified) is the cotangent of the DSSed tendency
-// (dss_out, as inside the step) or of the tendency as gb_remaining_tendency
-// returns it (not DSSed).
+// Reverse of the explicit tendency of one stage state U: Ub (+)= (dT/dU)^T Tb,
+// where Tb is the cotangent of the DSSed tendency (dss_out, as inside the step;
+// Tb is then DSS-transposed in place) or of the tendency as
+// gb_remaining_tendency returns it (not DSSed; Tb is only read).  accum adds
+// to Ub, else Ub is overwritten.
 template <class FT>
-void tendency_vjp(gb_ctx *ctx, const FT *Uc, const FT *Uf, const FT *L, const FT *Tb_c, const FT *Tb_f, FT *Ubc,
-                  FT *Ubf, bool dss_out, cudaStream_t s) {
+void tendency_vjp(gb_ctx *ctx, const FT *Uc, const FT *Uf, const FT *L, FT *Tb_c, FT *Tb_f, FT *Ubc, FT *Ubf,
+                  bool dss_out, bool accum, cudaStream_t s) {
   Impl<FT> *I = impl<FT>(ctx);
   auto &A = *I->adj;
   const DevParams<FT> &P = I->P;
-  FT *Tb = (FT *)A.Tb.p, *Lb = (FT *)A.Lb.p;
-  cudaMemcpyAsync(Tb, Tb_c, I->NC * sizeof(FT), cudaMemcpyDeviceToDevice, s);
-  cudaMemcpyAsync(Tb + I->NC, Tb_f, I->NF * sizeof(FT), cudaMemcpyDeviceToDevice, s);
-  if (dss_out) launch_dss_transpose<FT>(P, Tb, Tb + I->NC, s);
-  launch_passB_vjp<FT>(P, Uc, Uf, L, Tb, Tb + I->NC, Ubc, Ubf, Lb, (double *)A.dparB.p, A.grid, s);
+  FT *Lb = (FT *)A.Lb.p;
+  if (dss_out) launch_dss_transpose<FT>(P, Tb_c, Tb_f, s);
+  launch_passB_vjp<FT>(P, Uc, Uf, L, Tb_c, Tb_f, Ubc, Ubf, Lb, (double *)A.dparB.p, A.grid, accum, s);
   launch_dss_transpose<FT>(P, Lb, nullptr, s);
   launch_passA_vjp<FT>(P, Uc, Uf, Lb, Ubc, Ubf, A.grid, s);
 }
@@ -613,27 +612,25 @@ void reverse_step(gb_ctx *ctx, typename Impl<FT>::Record &rec, double dt_, FT *Y
   auto &A = *I->adj;
   const DevParams<FT> &P = I->P;
   const FT dt = (FT)dt_;
-  const size_t SB = (I->NC + I->NF) * sizeof(FT), RB = (I->NR + I->NF) * sizeof(FT);
   FT *Teb[4], *Tib[4] = {nullptr, nullptr, nullptr, nullptr}, *Te[4], *Ti[4] = {nullptr, nullptr, nullptr, nullptr};
   for (int j = 0; j < 4; ++j) {
     Teb[j] = (FT *)A.Teb[j].p;
     Te[j] = (FT *)rec.Te[j].p;
-    cudaMemsetAsync(Teb[j], 0, SB, s);
     if (j >= 1) {
       Tib[j] = (FT *)A.Tib[j].p;
       Ti[j] = (FT *)rec.Ti[j].p;
-      cudaMemsetAsync(Tib[j], 0, RB, s);
     }
   }
-  // final combination u_{n+1} = u_n + dt sum_j b_j (T_exp_j + T_imp_j), filtered
+  // final combination u_{n+1} = u_n + dt sum_j b_j (T_exp_j + T_imp_j), filtered; its
+  // transpose writes every tendency cotangent (zero where b_j = 0)
   CotArgs<FT> F{};
   F.nsrc = 4;
   for (int j = 0; j < 4; ++j) {
-    F.te_c[j] = I->be[j] != 0 ? Teb[j] : nullptr;
-    F.te_f[j] = I->be[j] != 0 ? Teb[j] + I->NC : nullptr;
+    F.te_c[j] = Teb[j];
+    F.te_f[j] = Teb[j] + I->NC;
     F.ce[j] = dt * (FT)I->be[j];
-    F.ti_c[j] = I->bi[j] != 0 && Tib[j] ? Tib[j] : nullptr;
-    F.ti_f[j] = I->bi[j] != 0 && Tib[j] ? Tib[j] + I->NR : nullptr;
+    F.ti_c[j] = Tib[j];
+    F.ti_f[j] = Tib[j] ? Tib[j] + I->NR : nullptr;
     F.ci[j] = dt * (FT)I->bi[j];
   }
   launch_final_transpose<FT>(P, F, Ybc, Ybf, s);
@@ -641,8 +638,7 @@ void reverse_step(gb_ctx *ctx, typename Impl<FT>::Record &rec, double dt_, FT *Y
   FT *Ubc = (FT *)A.Ub.p, *Ubf = Ubc + I->NC;
   for (int i = 3; i >= 0; --i) {
     const FT *Uc = i == 0 ? Yc : (const FT *)rec.U[i].p, *Uf = Uc + I->NC;
-    cudaMemsetAsync(Ubc, 0, SB, s);
-    tendency_vjp<FT>(ctx, Uc, Uf, (const FT *)rec.L[i].p, Teb[i], Teb[i] + I->NC, Ubc, Ubf, true, s);
+    tendency_vjp<FT>(ctx, Uc, Uf, (const FT *)rec.L[i].p, Teb[i], Teb[i] + I->NC, Ubc, Ubf, true, false, s);
     if (i == 0) {
       launch_axpy<FT>(I->NC, FT(1), Ubc, Ybc, s);  // the caller's c and f blocks are separate allocations
       launch_axpy<FT>(I->NF, FT(1), Ubf, Ybf, s);
@@ -698,8 +694,8 @@ int remaining_tendency_vjp_t(gb_ctx *ctx, gb_fieldvec Yb, gb_fieldvec Tb, gb_fie
   FT *L = (FT *)I->lap.p;
   launch_passA<FT>(I->P, (const FT *)Y.c, (const FT *)Y.f, L, s);
   launch_dss<FT>(I->P, L, nullptr, s);
-  tendency_vjp<FT>(ctx, (const FT *)Y.c, (const FT *)Y.f, L, (const FT *)Tb.c, (const FT *)Tb.f, (FT *)Yb.c,
-                   (FT *)Yb.f, false, s);
+  tendency_vjp<FT>(ctx, (const FT *)Y.c, (const FT *)Y.f, L, (FT *)Tb.c, (FT *)Tb.f, (FT *)Yb.c, (FT *)Yb.f, false,
+                   true, s);
   if ((r = check_launch(ctx))) return r;
   return read_dacc<FT>(ctx, dpar, true);
 }

@@ -138,7 +138,8 @@ __global__ void k_final(DevParams<FT> P, StageArgs<FT> A, FT *__restrict__ Yc, F
 
 // Transpose of k_final: the filter zeroes the boundary-face cotangent of
 // u_{n+1}; u_n receives it unchanged and every tendency j its coefficient
-// times it (A.te_c/te_f/ti_c/ti_f point at the tendency cotangents).
+// times it.  The tendency cotangents are written (this is their first
+// contribution in a reverse step); a zero coefficient writes zeros.
 template <class FT>
 __global__ void k_final_t(DevParams<FT> P, CotArgs<FT> A, FT *__restrict__ Ybc, FT *__restrict__ Ybf) {
   const int Nv = P.Nv, Nf = P.Nf;
@@ -151,8 +152,8 @@ __global__ void k_final_t(DevParams<FT> P, CotArgs<FT> A, FT *__restrict__ Ybc, 
       const size_t e = row / (4 * NN);
       const FT yb = Ybc[q];
       for (int j = 0; j < A.nsrc; ++j) {
-        if (A.te_c[j]) A.te_c[j][q] += A.ce[j] * yb;
-        if (A.ti_c[j] && (c == 0 || c == 3)) A.ti_c[j][((e * 2 + (c == 3)) * NN + n) * Nv + v] += A.ci[j] * yb;
+        if (A.te_c[j]) A.te_c[j][q] = A.ce[j] * yb;
+        if (A.ti_c[j] && (c == 0 || c == 3)) A.ti_c[j][((e * 2 + (c == 3)) * NN + n) * Nv + v] = A.ci[j] * yb;
       }
     } else {
       const size_t r = q - NC;
@@ -160,8 +161,8 @@ __global__ void k_final_t(DevParams<FT> P, CotArgs<FT> A, FT *__restrict__ Ybc, 
       const FT yb = (k == 0 || k == Nv) ? FT(0) : Ybf[r];
       Ybf[r] = yb;
       for (int j = 0; j < A.nsrc; ++j) {
-        if (A.te_f[j]) A.te_f[j][r] += A.ce[j] * yb;
-        if (A.ti_f[j]) A.ti_f[j][r] += A.ci[j] * yb;
+        if (A.te_f[j]) A.te_f[j][r] = A.ce[j] * yb;
+        if (A.ti_f[j]) A.ti_f[j][r] = A.ci[j] * yb;
       }
     }
   }

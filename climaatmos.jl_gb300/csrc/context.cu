@@ -638,11 +638,11 @@ void reverse_step(gb_ctx *ctx, typename Impl<FT>::Record &rec, double dt_, FT *Y
   FT *Ubc = (FT *)A.Ub.p, *Ubf = Ubc + I->NC;
   for (int i = 3; i >= 0; --i) {
     const FT *Uc = i == 0 ? Yc : (const FT *)rec.U[i].p, *Uf = Uc + I->NC;
-    tendency_vjp<FT>(ctx, Uc, Uf, (const FT *)rec.L[i].p, Teb[i], Teb[i] + I->NC, Ubc, Ubf, true, false, s);
     if (i == 0) {
-      launch_axpy<FT>(I->NC, FT(1), Ubc, Ybc, s);  // the caller's c and f blocks are separate allocations
-      launch_axpy<FT>(I->NF, FT(1), Ubf, Ybf, s);
+      // stage 0 is u_n itself: its tendency cotangent adds straight into the caller's Yb
+      tendency_vjp<FT>(ctx, Uc, Uf, (const FT *)rec.L[i].p, Teb[i], Teb[i] + I->NC, Ybc, Ybf, true, true, s);
     } else {
+      tendency_vjp<FT>(ctx, Uc, Uf, (const FT *)rec.L[i].p, Teb[i], Teb[i] + I->NC, Ubc, Ubf, true, false, s);
       const StageArgs<FT> SA = stage_args<FT>(I, i, dt, Yc, Yf, Te, Ti);
       launch_column_stage_vjp<FT>(P, SA, Ubc, Ubf, Tib[i], Tib[i] + I->NR, Ybc, Ybf, Teb, Tib, I->NC, I->NR,
                                   (FT *)A.scr.p, (double *)A.dal.p, s);

@@ -30,11 +30,14 @@ struct PassALayout {
 // Level-major scratch rows of pass B: field f of level v, node n at
 // (f Nv + v) 16 + n, so the thread of (level v, row j) reads or writes its
 // four nodes as one 16-byte row vector (bank-conflict free).
-enum PassBScratch { SB_C1 = 0, SB_C2, SB_K, SB_RJ, SB_L4, SB_U1, SB_U2, SB_Q1, SB_Q2, SB_N };
+enum PassBScratch { SB_C1 = 0, SB_C2, SB_K, SB_RJ, SB_L4, SB_Q1, SB_Q2, SB_N };
 
+// Pass B's shared memory: per buffer the input slabs (state, faces, geometry,
+// Laplacians); the tendency is written in place over the state and face slabs
+// of the element being computed and stored from there.
 template <class FT>
 struct PassBLayout {
-  size_t y[2], f[2], g[2], lap[2], s, x1, x2, out, outf, w, bar, total;
+  size_t y[2], f[2], g[2], lap[2], s, x1, x2, w, bar, total;
   __host__ __device__ PassBLayout(int Nv, int nbuf) {
     const int Nf = Nv + 1;
     size_t o = 0;
@@ -51,8 +54,6 @@ struct PassBLayout {
     s = o; o += align16(sizeof(FT) * SB_N * 16 * Nv);
     x1 = o; o += align16(sizeof(FT) * 16 * Nf);   // face rows [Nf][16]
     x2 = o; o += align16(sizeof(FT) * 16 * Nf);
-    out = o; o += align16(sizeof(FT) * 64 * Nv);
-    outf = o; o += align16(sizeof(FT) * 16 * Nf);
     w = o; o += align16(sizeof(FT) * 2 * 16);     // GLL weights W, 1/W
     bar = o; o += 16;
     total = o;

@@ -181,20 +181,26 @@ __global__ void __launch_bounds__(SE_THREADS, SeMinBlocks<FT>::value) k_passB(De
   extern __shared__ __align__(128) unsigned char sm[];
   const int Nv = P.Nv, Nf = P.Nf;
   const PassBLayout<FT> Lo(Nv, nbuf);
-  FT *sYb[2] = {(FT *)(sm + Lo.y[0]), (FT *)(sm + Lo.y[1])};
-  FT *sFb[2] = {(FT *)(sm + Lo.f[0]), (FT *)(sm + Lo.f[1])};
-  FT *sGb[2] = {(FT *)(sm + Lo.g[0]), (FT *)(sm + Lo.g[1])};
-  FT *sLb[2] = {(FT *)(sm + Lo.lap[0]), (FT *)(sm + Lo.lap[1])};
-  FT *sS = (FT *)(sm + Lo.s), *sX1 = (FT *)(sm + Lo.x1), *sX2 = (FT *)(sm + Lo.x2);
-  FT *sO = (FT *)(sm + Lo.out), *sOf = (FT *)(sm + Lo.outf), *sW = (FT *)(sm + Lo.w);
+  auto at = [&](const size_t (&off)[2], int b) { return (FT *)(sm + (b ? off[1] : off[0])); };
+  FT *sS = (FT *)(sm + Lo.s), *sX1 = (FT *)(sm + Lo.x1), *sX2 = (FT *)(sm + Lo.x2), *sW = (FT *)(sm + Lo.w);
   uint64_t *bar = (uint64_t *)(sm + Lo.bar);
+  const uint32_t by = uint32_t(sizeof(FT) * 64 * Nv), bf = uint32_t(sizeof(FT) * 16 * Nf);
+  const uint32_t bg = uint32_t(sizeof(FT) * HG_N * 16);
+  auto issue = [&](int b, int e) {
+    uint64_t *bb = b ? &bar[1] : &bar[0];
+    mbar_expect_tx(bb, 2 * by + bf + bg);
+    tma_load(at(Lo.y, b), Yc + (size_t)e * 64 * Nv, by, bb);
+    tma_load(at(Lo.f, b), Yf + (size_t)e * 16 * Nf, bf, bb);
+    tma_load(at(Lo.g, b), P.hgeo + (size_t)e * HG_N * 16, bg, bb);
+    tma_load(at(Lo.lap, b), Lin + (size_t)e * 64 * Nv, by, bb);
+  };
   if (threadIdx.x < NN) {
     sW[threadIdx.x] = P.W[threadIdx.x];
     sW[NN + threadIdx.x] = P.iW[threadIdx.x];
   }
-  init_bars(bar);
+  slab_init_bars(bar);
   int e = blockIdx.x;
-  if (threadIdx.x == 0 && e < P.Nh) issue_slab<FT>(P, &bar[0], e, sYb[0], sFb[0], sGb[0], sLb[0], Yc, Yf, Lin);
+  if (threadIdx.x == 0 && e < P.Nh) issue(0, e);
   const int j = threadIdx.x & 3, vl = threadIdx.x >> 2, vs = level_slot(vl);
   // the thread's row of scratch field f at level (or face) v
   auto row = [&](FT *base, int f, int v) { return base + ((size_t)f * Nv + v) * NN + NQ * j; };
@@ -202,9 +208,12 @@ __global__ void __launch_bounds__(SE_THREADS, SeMinBlocks<FT>::value) k_passB(De
   R.init(P, j);
   for (int it = 0; e < P.Nh; ++it, e += gridDim.x) {
     int b;
-    if (!begin_element<FT>(P, bar, nbuf, it, e, sYb, sFb, sGb, sLb, true, Yc, Yf, Lin, b)) break;
-    const FT *sY = pick(b, sYb[0], sYb[1]), *sF = pick(b, sFb[0], sFb[1]), *sG = pick(b, sGb[0], sGb[1]);
-    const FT *sL = pick(b, sLb[0], sLb[1]);
+    if (!slab_begin(bar, nbuf, it, e, P.Nh, P.status, issue, b)) break;
+    // the tendency overwrites the state and face slabs in place: each entry is
+    // written by the thread that read it, after its last read
+    FT *sY = at(Lo.y, b), *sF = at(Lo.f, b);
+    const FT *sG = at(Lo.g, b), *sL = at(Lo.lap, b);
+    FT *sO = sY, *sOf = sF;
     const SlabGeo<FT> g{sG + NQ * j, sW + NQ * j};
     // ---- P1: centre-level horizontal work, ordered so that each group of
     // intermediate fields dies before the next is formed; per-level results
@@ -286,8 +295,6 @@ __global__ void __launch_bounds__(SE_THREADS, SeMinBlocks<FT>::value) k_passB(De
           st_row(row(sS, SB_C2, v), c2);
           st_row(row(sS, SB_K, v), K);
           st_row(row(sS, SB_RJ, v), rJ);
-          st_row(row(sS, SB_U1, v), u1);
-          st_row(row(sS, SB_U2, v), u2);
         }
       }
       // rho: -wdiv(rho u); rho e_tot: -split_div(rho u, h)
@@ -393,7 +400,7 @@ __global__ void __launch_bounds__(SE_THREADS, SeMinBlocks<FT>::value) k_passB(De
       // the levels below and above the face (both the adjacent level on a boundary face)
       const int va = k > 0 ? k - 1 : 0, vb = k < Nv ? k : Nv - 1;
       if (act) {
-        FT C1a[4], C1b[4], C2a[4], C2b[4], Ka[4], Kb[4], Ra[4], Rb[4], La[4], Lb[4], U1a[4], U1b[4], U2a[4], U2b[4];
+        FT C1a[4], C1b[4], C2a[4], C2b[4], Ka[4], Kb[4], Ra[4], Rb[4], La[4], Lb[4];
         ld_row(row(sS, SB_C1, va), C1a);
         ld_row(row(sS, SB_C1, vb), C1b);
         ld_row(row(sS, SB_C2, va), C2a);
@@ -404,10 +411,6 @@ __global__ void __launch_bounds__(SE_THREADS, SeMinBlocks<FT>::value) k_passB(De
         ld_row(row(sS, SB_RJ, vb), Rb);
         ld_row(row(sS, SB_L4, va), La);
         ld_row(row(sS, SB_L4, vb), Lb);
-        ld_row(row(sS, SB_U1, va), U1a);
-        ld_row(row(sS, SB_U1, vb), U1b);
-        ld_row(row(sS, SB_U2, va), U2a);
-        ld_row(row(sS, SB_U2, vb), U2b);
         FT Jh[4], iJh[4], iW[4], fh1[4], fh2[4];
         g.row(HG_JH, Jh);
         g.row(HG_IJH, iJh);
@@ -423,8 +426,10 @@ __global__ void __launch_bounds__(SE_THREADS, SeMinBlocks<FT>::value) k_passB(De
           const FT w1 = -tb[i] * iWJf, w2 = ta[i] * iWJf;
           FT cv1 = 0, cv2 = 0, gK = 0, cc1, cc2, l4, rJ;
           if (inner) {
-            cv1 = -(U2b[i] - U2a[i]) * iJf;
-            cv2 = (U1b[i] - U1a[i]) * iJf;
+            // u_h of the levels below and above (not yet overwritten: P3 writes them)
+            const int qa = n * Nv + va, qb = n * Nv + vb;
+            cv1 = -(sY[32 * Nv + qb] - sY[32 * Nv + qa]) * iJf;
+            cv2 = (sY[16 * Nv + qb] - sY[16 * Nv + qa]) * iJf;
             cc1 = (C1a[i] + C1b[i]) / FT(2);
             cc2 = (C2a[i] + C2b[i]) / FT(2);
             gK = Kb[i] - Ka[i];
@@ -473,8 +478,8 @@ __global__ void __launch_bounds__(SE_THREADS, SeMinBlocks<FT>::value) k_passB(De
     fence_proxy_async();
     __syncthreads();
     if (threadIdx.x == 0) {
-      tma_store(Tc + (size_t)e * 64 * Nv, sO, uint32_t(sizeof(FT) * 64 * Nv));
-      tma_store(Tf + (size_t)e * 16 * Nf, sOf, uint32_t(sizeof(FT) * 16 * Nf));
+      tma_store(Tc + (size_t)e * 64 * Nv, sO, by);
+      tma_store(Tf + (size_t)e * 16 * Nf, sOf, bf);
       tma_store_commit();
     }
   }

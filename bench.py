@@ -53,6 +53,9 @@ def parse():
     ap.add_argument("--fd-directions", type=int, default=32)
     ap.add_argument("--no-differentiation", action="store_true")
     ap.add_argument("--no-h60", action="store_true")
+    # bracket one forward step ("step") or one reverse pass ("reverse") by
+    # cudaProfilerStart/Stop, for `ncu --profile-from-start off`; no effect otherwise
+    ap.add_argument("--profile-region", default="none", choices=["none", "step", "reverse"])
     return ap.parse_args()
 
 
@@ -203,7 +206,7 @@ def contract_bytes_per_step(cfg, fb=4):
 
 
 # ncu-measured DRAM traffic per launch on the production FP32 workload (bytes)
-NCU_TRAFFIC = {"k_passB": 200255744 + 80094720, "k_col_stage": 572394240 + 153260544}
+NCU_TRAFFIC = {"k_passB": 200229376 + 72189440, "k_col_stage": 572394240 + 153260544}
 
 
 def measured_peak():
@@ -251,6 +254,11 @@ def run_gb300(args):
         ms = float(t.item())
         dist.barrier()
     finite = bool(torch.isfinite(s.Y.c).all() and torch.isfinite(s.Y.f).all())
+    if args.profile_region == "step":
+        torch.cuda.profiler.start()
+        s.step(1)
+        torch.cuda.synchronize()
+        torch.cuda.profiler.stop()
     v1 = sypd(cfg.dt, ms / 1e3)
     value = v1 * world        # independent replicas, one per GPU
 
@@ -484,7 +492,11 @@ def measure_adjoint(args, s, fwd_ms):
     import ctypes
     d = (ctypes.c_double * 2)()
     peak = ctypes.c_size_t(0)
+    if args.profile_region == "reverse":
+        torch.cuda.profiler.start()
     r_ms, _ = _timed(lambda: s.p.call("gb_adjoint_reverse", Ybar.gb(), d, ctypes.byref(peak)))
+    if args.profile_region == "reverse":
+        torch.cuda.profiler.stop()
     finite = bool(torch.isfinite(Ybar.c).all() and torch.isfinite(Ybar.f).all())
     # per-kernel times of the reverse kernels (CUDA events inside the library)
     kern = {}

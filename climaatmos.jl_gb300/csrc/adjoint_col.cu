@@ -621,6 +621,35 @@ __global__ void __launch_bounds__(128, VjpMinBlocks<FT>::value) k_col_stage_vjp_
   const size_t cb = (size_t)e * 4 * NN * Nv + (size_t)n * Nv + r0, rb = (size_t)e * 2 * NN * Nv + (size_t)n * Nv + r0;
   const size_t fb = ((size_t)e * NN + n) * Nf + r0;
   const col::ColLev<FT> L{P.lc4, P.lf4, Nv, Nf};
+  // The cotangent inputs and the accumulation targets are first touched after
+  // the forward recompute: start their lines towards L2 now (one prefetch per
+  // field and warp covers the column: the lanes' levels are contiguous).
+  if (r0 < Nv) {
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      prefetch_l2(V.Ub_c + cb + (size_t)c * sc);
+      prefetch_l2(V.Yb_c + cb + (size_t)c * sc);
+    }
+    prefetch_l2(V.Tb_c + rb);
+    prefetch_l2(V.Tb_c + rb + sc);
+    for (int j = 0; j < A.nsrc; ++j) {
+      if (V.Teb_c[j])
+        for (int c = 0; c < 4; ++c) prefetch_l2(V.Teb_c[j] + cb + (size_t)c * sc);
+      if (j >= 1 && V.Tib_c[j]) {
+        prefetch_l2(V.Tib_c[j] + rb);
+        prefetch_l2(V.Tib_c[j] + rb + sc);
+      }
+    }
+  }
+  if (r0 < Nf) {
+    prefetch_l2(V.Ub_f + fb);
+    prefetch_l2(V.Tb_f + fb);
+    prefetch_l2(V.Yb_f + fb);
+    for (int j = 0; j < A.nsrc; ++j) {
+      if (V.Teb_f[j]) prefetch_l2(V.Teb_f[j] + fb);
+      if (j >= 1 && V.Tib_f[j]) prefetch_l2(V.Tib_f[j] + fb);
+    }
+  }
   // ---------------------------------------------------------------- forward recompute
   FT H[5][CM];
 #pragma unroll

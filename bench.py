@@ -507,8 +507,9 @@ def measure_adjoint(args, s, fwd_ms):
     return {"steps": n, "checkpoint_every": 5, "forward_ms_per_step": fwd_ms, "kernels": kern,
             "checkpointed_forward_ms_per_step": f_ms / n, "reverse_ms_per_step": r_ms / n,
             "adjoint_over_forward": (r_ms / n) / fwd_ms,
-            "what": "reverse = per-segment recompute (1 forward step per step, stage data kept) + reverse kernels; "
-                    "ratio against the graph-replayed forward step",
+            "what": "reverse = per-segment recompute (1 forward step per step, stage data kept; the last "
+                    "segment is recorded by the checkpointed forward pass) + reverse kernels; ratio against "
+                    "the graph-replayed forward step",
             "dJ_dnu": d[0], "dJ_drate": d[1], "library_bytes": int(peak.value), "finite": finite}
 
 

@@ -51,6 +51,7 @@ struct Impl : ImplBase {
     std::vector<std::unique_ptr<DevBuf>> ckpt;
     DevBuf Ub, Lb, Teb[4], Tib[4], zero, dummy, scr, dparB, dal, dacc, work;
     int nsteps = 0, every = 0, grid = 0;
+    int rec_seg = -1;  // checkpoint segment whose stage records are valid (recorded by the forward pass)
     double dt = 0;
     bool ready = false;
     size_t bytes = 0, rec_bytes = 0;
@@ -756,6 +757,7 @@ int step_vjp_t(gb_ctx *ctx, gb_fieldvec Yb, gb_fieldvec Y, double dt, double *dp
   CK(cudaMemcpyAsync(W, Y.c, I->NC * sizeof(FT), cudaMemcpyDeviceToDevice, s));
   CK(cudaMemcpyAsync(W + I->NC, Y.f, I->NF * sizeof(FT), cudaMemcpyDeviceToDevice, s));
   zero_dpar<FT>(ctx, s);
+  A.rec_seg = -1;  // record 0 is reused here
   record_step<FT>(ctx, W, W + I->NC, dt, *A.rec[0], s);
   reverse_step<FT>(ctx, *A.rec[0], dt, (FT *)Yb.c, (FT *)Yb.f, s);
   if ((r = check_launch(ctx))) return r;
@@ -776,6 +778,11 @@ int adjoint_forward_t(gb_ctx *ctx, gb_fieldvec Y, double dt, int nsteps, int eve
     if ((r = alloc_z<FT>(ctx, *b, SB, A.bytes))) return r;
     A.ckpt.push_back(std::move(b));
   }
+  // the last segment's stage data is recorded on the way (the reverse pass starts
+  // there and needs no recompute for it); the same kernels in the same order as the step
+  if ((r = ensure_records<FT>(ctx, every))) return r;
+  const int last = (nck - 1) * every;
+  A.rec_seg = -1;
   cudaStream_t s = ctx->stream;
   FT *Yc = (FT *)Y.c, *Yf = (FT *)Y.f;
   for (int k = 0; k < nsteps; ++k) {
@@ -784,8 +791,10 @@ int adjoint_forward_t(gb_ctx *ctx, gb_fieldvec Y, double dt, int nsteps, int eve
       CK(cudaMemcpyAsync(ck, Yc, I->NC * sizeof(FT), cudaMemcpyDeviceToDevice, s));
       CK(cudaMemcpyAsync(ck + I->NC, Yf, I->NF * sizeof(FT), cudaMemcpyDeviceToDevice, s));
     }
-    enqueue_step<FT>(ctx, Yc, Yf, dt, s);
+    if (k >= last) record_step<FT>(ctx, Yc, Yf, dt, *A.rec[k - last], s);
+    else enqueue_step<FT>(ctx, Yc, Yf, dt, s);
   }
+  A.rec_seg = nck - 1;
   A.nsteps = nsteps;
   A.every = every;
   A.dt = dt;
@@ -808,8 +817,11 @@ int adjoint_reverse_t(gb_ctx *ctx, gb_fieldvec Yb, double *dpar, size_t *peak) {
   const int nseg = (A.nsteps + A.every - 1) / A.every;
   for (int g = nseg - 1; g >= 0; --g) {
     const int s0 = g * A.every, s1 = std::min(A.nsteps, s0 + A.every);
-    CK(cudaMemcpyAsync(W, A.ckpt[g]->p, SB, cudaMemcpyDeviceToDevice, s));
-    for (int k = s0; k < s1; ++k) record_step<FT>(ctx, W, W + I->NC, A.dt, *A.rec[k - s0], s);
+    if (g != A.rec_seg) {
+      CK(cudaMemcpyAsync(W, A.ckpt[g]->p, SB, cudaMemcpyDeviceToDevice, s));
+      for (int k = s0; k < s1; ++k) record_step<FT>(ctx, W, W + I->NC, A.dt, *A.rec[k - s0], s);
+    }
+    A.rec_seg = -1;
     for (int k = s1 - 1; k >= s0; --k) reverse_step<FT>(ctx, *A.rec[k - s0], A.dt, (FT *)Yb.c, (FT *)Yb.f, s);
     if ((r = check_launch(ctx))) return r;
   }

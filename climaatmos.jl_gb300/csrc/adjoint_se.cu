@@ -346,6 +346,16 @@ __global__ void __launch_bounds__(AD_THREADS, AdMinBlocks<FT>::value)
           st_row(crow(BC_RJ, v), rJ);
         }
       }
+      if (nu != FT(0)) {
+        // only o3 (face phase) is needed: the d/dnu terms of o1, o2 and the rho e_tot
+        // hyperdiffusion follow from the transposes in the centre phase (adjoint identity)
+        FT L3[4], o3[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) L3[i] = sL[48 * Nv + (NQ * j + i) * Nv + v];
+        vec_lap_o3(P, R, g, s, L3, o3);
+        if (act) st_row(crow(BC_L4, v), o3);
+        continue;
+      }
       FT o1[4], o2[4], o3[4];
       {
         FT L1[4], L2[4], L3[4];
@@ -655,13 +665,18 @@ __global__ void __launch_bounds__(AD_THREADS, AdMinBlocks<FT>::value)
         }
         vec_lap_t(P, R, g, s, o1b, o2b, L4b, P.div_damp, L1b, L2b, L3b);
         if (act) {
+          FT o3[4];
+          ld_row(crow(BC_L4, v), o3);
+          FT dl = 0;  // sum L . Lb - o3 . L4b = sum (o1 o1b + o2 o2b), o_ib = -nu T_u_i
 #pragma unroll
           for (int i = 0; i < 4; ++i) {
             const int q = (NQ * j + i) * Nv + v;
             lb[16 * Nv + q] = L1b[i];
             lb[32 * Nv + q] = L2b[i];
             lb[48 * Nv + q] = L3b[i];
+            dl += sL[16 * Nv + q] * L1b[i] + sL[32 * Nv + q] * L2b[i] + sL[48 * Nv + q] * L3b[i] - o3[i] * L4b[i];
           }
+          if (nu != FT(0)) dnu += (double)dl / (double)nu;
         }
       }
       {
@@ -687,8 +702,13 @@ __global__ void __launch_bounds__(AD_THREADS, AdMinBlocks<FT>::value)
         }
         grad_t(P, R, gb1, gb2, Lsb);
         if (act) {
+          FT dl = 0;  // sum Ls . Lsb = sum hd . hdb, hdb = -nu_s T_rhoe
 #pragma unroll
-          for (int i = 0; i < 4; ++i) lb[(NQ * j + i) * Nv + v] = Lsb[i];
+          for (int i = 0; i < 4; ++i) {
+            lb[(NQ * j + i) * Nv + v] = Lsb[i];
+            dl += Ls[i] * Lsb[i];
+          }
+          if (nu != FT(0)) dnu += (double)dl / (double)nu;
         }
       }
       // ---- forward thermodynamics and the horizontal-dynamics transpose

@@ -262,6 +262,36 @@ __device__ __forceinline__ void vec_lap(const DevParams<FT> &P, const Row<FT> &R
   }
 }
 
+// The third output of vec_lap alone (it depends on c3 only): the same
+// operations in the same order as in vec_lap.
+template <class FT, class G>
+__device__ __forceinline__ void vec_lap_o3(const DevParams<FT> &P, const Row<FT> &R, const G &g,
+                                           const LevRow<FT> &s, const FT (&c3)[4], FT (&o3)[4]) {
+  FT e3[4], e4[4], Wz1[4], Wz2[4];
+  d2(R, c3, e3);
+  d1(P, c3, e4);
+  {
+    FT gd0[4], gd1[4], gd2[4], W[4];
+    g.gd(gd0, gd1, gd2);
+    g.w(W);
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const FT k1 = e3[i] * s.iJ[i], k2 = -e4[i] * s.iJ[i];
+      const FT x0 = gd0[i] * s.r2, x1 = gd1[i] * s.r2, x2 = gd2[i] * s.r2;
+      Wz1[i] = W[i] * (x0 * k1 + x1 * k2);
+      Wz2[i] = W[i] * (x1 * k1 + x2 * k2);
+    }
+  }
+  FT f1[4], f2[4];
+  t1(P, Wz2, f1);
+  t2(R, Wz1, f2);
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const FT q3 = (-f1[i] + f2[i]) * s.iWJ[i];
+    o3[i] = -s.G33 * q3;
+  }
+}
+
 // weak divergence -(1/WJ) (D^T (WJ F1) along xi^1 + along xi^2)
 template <class FT>
 __device__ __forceinline__ void wdiv(const DevParams<FT> &P, const Row<FT> &R, const LevRow<FT> &s,

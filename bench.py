@@ -498,6 +498,13 @@ def measure_adjoint(args, s, fwd_ms):
     if args.profile_region == "reverse":
         torch.cuda.profiler.stop()
     finite = bool(torch.isfinite(Ybar.c).all() and torch.isfinite(Ybar.f).all())
+    # the pullback alone: one segment of 5 steps, recorded by the checkpointed forward
+    # pass, so the reverse pass recomputes nothing
+    Y1 = Y0.copy()
+    s.p.call("gb_adjoint_forward", Y1.gb(), 0.0, float(s.dt), 5, 5)
+    _, Ybar1 = lg(Y1)
+    d1 = (ctypes.c_double * 2)()
+    p_ms, _ = _timed(lambda: s.p.call("gb_adjoint_reverse", Ybar1.gb(), d1, None))
     # per-kernel times of the reverse kernels (CUDA events inside the library)
     kern = {}
     for kid, name, per_step in REVERSE_KERNELS:
@@ -505,6 +512,7 @@ def measure_adjoint(args, s, fwd_ms):
         s.p.call("gb_time_kernel", kid, s.Y.gb(), 20, ctypes.byref(out))
         kern[name] = {"ms": out.value, "launches_per_step": per_step}
     return {"steps": n, "checkpoint_every": 5, "forward_ms_per_step": fwd_ms, "kernels": kern,
+            "pullback_ms_per_step": p_ms / 5, "pullback_over_forward": (p_ms / 5) / fwd_ms,
             "checkpointed_forward_ms_per_step": f_ms / n, "reverse_ms_per_step": r_ms / n,
             "adjoint_over_forward": (r_ms / n) / fwd_ms,
             "what": "reverse = per-segment recompute (1 forward step per step, stage data kept; the last "

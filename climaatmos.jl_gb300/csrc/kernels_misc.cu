@@ -13,6 +13,9 @@ constexpr int DSS_THREADS = 256;  // 8 groups per CTA, one warp per group
 // (deterministic, no atomics).  Centre block components: 0 scalar, 1-2 covariant
 // horizontal vector (averaged in Cartesian components), 3 scalar.  One warp
 // per group, lanes over levels.
+// Two levels per lane (v0 + lane and v0 + 32 + lane), so that each lane has
+// two independent gathers in flight; per level the sums run in the same copy
+// order as with one level per lane.
 template <class FT>
 __global__ void __launch_bounds__(DSS_THREADS) k_dss(DevParams<FT> P, FT *__restrict__ C, FT *__restrict__ F) {
   const int lane = threadIdx.x & 31;
@@ -21,39 +24,61 @@ __global__ void __launch_bounds__(DSS_THREADS) k_dss(DevParams<FT> P, FT *__rest
   const int Nv = P.Nv, Nf = P.Nf;
   const int o0 = P.goff[g], o1 = P.goff[g + 1];
   if (C) {
-    for (int v = lane; v < Nv; v += 32) {
-      FT s0 = 0, s3 = 0, X0 = 0, X1 = 0, X2 = 0;
+    for (int v0 = 0; v0 < Nv; v0 += 64) {
+      const int v[2] = {v0 + lane, v0 + 32 + lane};
+      const bool ok[2] = {v[0] < Nv, v[1] < Nv};
+      FT s0[2] = {0, 0}, s3[2] = {0, 0}, X0[2] = {0, 0}, X1[2] = {0, 0}, X2[2] = {0, 0};
       for (int c = o0; c < o1; ++c) {
         const int idx = P.gcopy[c], e = idx >> 4, n = idx & 15;
         const FT w = P.gw[c];
-        const size_t b = ((size_t)e * 4 * NN + n) * Nv + v;
-        s0 += w * C[b];
-        s3 += w * C[b + 48 * Nv];
-        const FT u1 = C[b + 16 * Nv], u2 = C[b + 32 * Nv];
         const FT *ec = P.econ + (size_t)idx * 6;
-        X0 += w * (u1 * ec[0] + u2 * ec[3]);
-        X1 += w * (u1 * ec[1] + u2 * ec[4]);
-        X2 += w * (u1 * ec[2] + u2 * ec[5]);
+        const size_t b0 = ((size_t)e * 4 * NN + n) * Nv;
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          if (!ok[h]) continue;
+          const size_t b = b0 + v[h];
+          s0[h] += w * C[b];
+          s3[h] += w * C[b + 48 * Nv];
+          const FT u1 = C[b + 16 * Nv], u2 = C[b + 32 * Nv];
+          X0[h] += w * (u1 * ec[0] + u2 * ec[3]);
+          X1[h] += w * (u1 * ec[1] + u2 * ec[4]);
+          X2[h] += w * (u1 * ec[2] + u2 * ec[5]);
+        }
       }
       for (int c = o0; c < o1; ++c) {
         const int idx = P.gcopy[c], e = idx >> 4, n = idx & 15;
-        const size_t b = ((size_t)e * 4 * NN + n) * Nv + v;
         const FT *eo = P.ecov + (size_t)idx * 6;
-        C[b] = s0;
-        C[b + 48 * Nv] = s3;
-        C[b + 16 * Nv] = eo[0] * X0 + eo[1] * X1 + eo[2] * X2;
-        C[b + 32 * Nv] = eo[3] * X0 + eo[4] * X1 + eo[5] * X2;
+        const size_t b0 = ((size_t)e * 4 * NN + n) * Nv;
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          if (!ok[h]) continue;
+          const size_t b = b0 + v[h];
+          C[b] = s0[h];
+          C[b + 48 * Nv] = s3[h];
+          C[b + 16 * Nv] = eo[0] * X0[h] + eo[1] * X1[h] + eo[2] * X2[h];
+          C[b + 32 * Nv] = eo[3] * X0[h] + eo[4] * X1[h] + eo[5] * X2[h];
+        }
       }
     }
   }
   if (F) {
-    for (int k = lane; k < Nf; k += 32) {
-      FT s = 0;
+    for (int k0 = 0; k0 < Nf; k0 += 64) {
+      const int k[2] = {k0 + lane, k0 + 32 + lane};
+      const bool ok[2] = {k[0] < Nf, k[1] < Nf};
+      FT sf[2] = {0, 0};
       for (int c = o0; c < o1; ++c) {
-        const int idx = P.gcopy[c];
-        s += P.gw[c] * F[(size_t)idx * Nf + k];
+        const FT w = P.gw[c];
+        const size_t b0 = (size_t)P.gcopy[c] * Nf;
+#pragma unroll
+        for (int h = 0; h < 2; ++h)
+          if (ok[h]) sf[h] += w * F[b0 + k[h]];
       }
-      for (int c = o0; c < o1; ++c) F[(size_t)P.gcopy[c] * Nf + k] = s;
+      for (int c = o0; c < o1; ++c) {
+        const size_t b0 = (size_t)P.gcopy[c] * Nf;
+#pragma unroll
+        for (int h = 0; h < 2; ++h)
+          if (ok[h]) F[b0 + k[h]] = sf[h];
+      }
     }
   }
 }
@@ -72,36 +97,61 @@ __global__ void __launch_bounds__(DSS_THREADS) k_dss_t(DevParams<FT> P, FT *__re
   const int Nv = P.Nv, Nf = P.Nf;
   const int o0 = P.goff[g], o1 = P.goff[g + 1];
   if (C) {
-    for (int v = lane; v < Nv; v += 32) {
-      FT s0 = 0, s3 = 0, X0 = 0, X1 = 0, X2 = 0;
+    for (int v0 = 0; v0 < Nv; v0 += 64) {
+      const int v[2] = {v0 + lane, v0 + 32 + lane};
+      const bool ok[2] = {v[0] < Nv, v[1] < Nv};
+      FT s0[2] = {0, 0}, s3[2] = {0, 0}, X0[2] = {0, 0}, X1[2] = {0, 0}, X2[2] = {0, 0};
       for (int c = o0; c < o1; ++c) {
         const int idx = P.gcopy[c], e = idx >> 4, n = idx & 15;
-        const size_t b = ((size_t)e * 4 * NN + n) * Nv + v;
-        s0 += C[b];
-        s3 += C[b + 48 * Nv];
-        const FT u1 = C[b + 16 * Nv], u2 = C[b + 32 * Nv];
         const FT *eo = P.ecov + (size_t)idx * 6;
-        X0 += u1 * eo[0] + u2 * eo[3];
-        X1 += u1 * eo[1] + u2 * eo[4];
-        X2 += u1 * eo[2] + u2 * eo[5];
+        const size_t b0 = ((size_t)e * 4 * NN + n) * Nv;
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          if (!ok[h]) continue;
+          const size_t b = b0 + v[h];
+          s0[h] += C[b];
+          s3[h] += C[b + 48 * Nv];
+          const FT u1 = C[b + 16 * Nv], u2 = C[b + 32 * Nv];
+          X0[h] += u1 * eo[0] + u2 * eo[3];
+          X1[h] += u1 * eo[1] + u2 * eo[4];
+          X2[h] += u1 * eo[2] + u2 * eo[5];
+        }
       }
       for (int c = o0; c < o1; ++c) {
         const int idx = P.gcopy[c], e = idx >> 4, n = idx & 15;
-        const size_t b = ((size_t)e * 4 * NN + n) * Nv + v;
         const FT w = P.gw[c];
         const FT *ec = P.econ + (size_t)idx * 6;
-        C[b] = w * s0;
-        C[b + 48 * Nv] = w * s3;
-        C[b + 16 * Nv] = w * (ec[0] * X0 + ec[1] * X1 + ec[2] * X2);
-        C[b + 32 * Nv] = w * (ec[3] * X0 + ec[4] * X1 + ec[5] * X2);
+        const size_t b0 = ((size_t)e * 4 * NN + n) * Nv;
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          if (!ok[h]) continue;
+          const size_t b = b0 + v[h];
+          C[b] = w * s0[h];
+          C[b + 48 * Nv] = w * s3[h];
+          C[b + 16 * Nv] = w * (ec[0] * X0[h] + ec[1] * X1[h] + ec[2] * X2[h]);
+          C[b + 32 * Nv] = w * (ec[3] * X0[h] + ec[4] * X1[h] + ec[5] * X2[h]);
+        }
       }
     }
   }
   if (F) {
-    for (int k = lane; k < Nf; k += 32) {
-      FT s = 0;
-      for (int c = o0; c < o1; ++c) s += F[(size_t)P.gcopy[c] * Nf + k];
-      for (int c = o0; c < o1; ++c) F[(size_t)P.gcopy[c] * Nf + k] = P.gw[c] * s;
+    for (int k0 = 0; k0 < Nf; k0 += 64) {
+      const int k[2] = {k0 + lane, k0 + 32 + lane};
+      const bool ok[2] = {k[0] < Nf, k[1] < Nf};
+      FT sf[2] = {0, 0};
+      for (int c = o0; c < o1; ++c) {
+        const size_t b0 = (size_t)P.gcopy[c] * Nf;
+#pragma unroll
+        for (int h = 0; h < 2; ++h)
+          if (ok[h]) sf[h] += F[b0 + k[h]];
+      }
+      for (int c = o0; c < o1; ++c) {
+        const FT w = P.gw[c];
+        const size_t b0 = (size_t)P.gcopy[c] * Nf;
+#pragma unroll
+        for (int h = 0; h < 2; ++h)
+          if (ok[h]) F[b0 + k[h]] = w * sf[h];
+      }
     }
   }
 }

@@ -24,6 +24,10 @@ struct DevParams {
   FT grav, Rd, cpd, cvd, T0, pref, kappa, Tmin_ref, Tsfc_ref, Tmin_sgs, icvd, ipref;
   FT nu_v, nu_s, div_damp, dt_model;
   int upwinding;
+  // Held-Suarez forcing: k_a, k_s - k_a, k_f; sigma_b, 1 / (1 - sigma_b); Delta T_y, T_equator,
+  // Delta theta_z, T_min; 1 / p_ref_theta, 1 / MSLP
+  int hs;
+  FT hs_ka, hs_dk, hs_kf, hs_sb, hs_isb, hs_dTy, hs_Teq, hs_dthz, hs_Tmin, hs_ip0, hs_iMSLP;
   FT W[NN], iW[NN];
   FT D[NQ * NQ];  // D[i*4+k] = l_k'(xi_i)
   const FT *hgeo;  // [Nh][HG_N][16]

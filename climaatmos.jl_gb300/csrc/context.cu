@@ -192,6 +192,16 @@ int create_impl(gb_ctx *ctx) {
   P.Tsfc_ref = (FT)c.T_surf_ref; P.Tmin_sgs = (FT)c.T_min_sgs;
   P.icvd = (FT)(1.0 / c.cv_d); P.ipref = (FT)(1.0 / c.p_ref);
   P.nu_v = (FT)c.nu_v; P.nu_s = (FT)c.nu_s; P.div_damp = (FT)c.div_damp; P.dt_model = (FT)c.dt;
+  P.hs = c.held_suarez ? 1 : 0;
+  if (P.hs) {
+    P.hs_ka = (FT)(1.0 / (40.0 * c.hs_day));
+    P.hs_dk = (FT)(1.0 / (4.0 * c.hs_day) - 1.0 / (40.0 * c.hs_day));
+    P.hs_kf = (FT)(1.0 / c.hs_day);
+    P.hs_sb = (FT)c.hs_sigma_b;
+    P.hs_isb = (FT)(1.0 / (1.0 - c.hs_sigma_b));
+    P.hs_dTy = (FT)c.hs_dT_y; P.hs_Teq = (FT)c.hs_T_equator; P.hs_dthz = (FT)c.hs_dtheta_z;
+    P.hs_Tmin = (FT)c.hs_T_min; P.hs_ip0 = (FT)(1.0 / c.hs_p_ref_theta); P.hs_iMSLP = (FT)(1.0 / c.hs_MSLP);
+  }
   P.upwinding = c.upwinding;
   for (int n = 0; n < NN; ++n) { P.W[n] = (FT)g.W[n]; P.iW[n] = (FT)(1.0 / g.W[n]); }
   for (int i = 0; i < NQ; ++i)
@@ -472,6 +482,8 @@ template <class FT>
 int ensure_adjoint(gb_ctx *ctx) {
   Impl<FT> *I = impl<FT>(ctx);
   if (I->adj) return GB_OK;
+  if (ctx->cfg.held_suarez)
+    return fail(ctx, GB_ERR_ARG, "reverse mode does not cover the Held-Suarez forcing (configure held_suarez = 0)");
   int dev = 0, optin = 0, nsm = 0;
   CK(cudaGetDevice(&dev));
   CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));

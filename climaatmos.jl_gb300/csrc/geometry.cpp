@@ -91,6 +91,12 @@ bool validate_config(const gb_config &c, const char **why) {
     return false;
   }
   if (c.upwinding != 0 && c.upwinding != 1) { *why = "upwinding must be 0 or 1"; return false; }
+  if (c.held_suarez != 0 && c.held_suarez != 1) { *why = "held_suarez must be 0 or 1"; return false; }
+  if (c.held_suarez && (!(c.hs_day > 0) || !(c.hs_sigma_b >= 0 && c.hs_sigma_b < 1) || !(c.hs_p_ref_theta > 0) ||
+                        !(c.hs_MSLP > 0))) {
+    *why = "invalid Held-Suarez parameters";
+    return false;
+  }
   return true;
 }
 
@@ -229,6 +235,7 @@ void build_geometry(const gb_config &c, HostGeometry &g) {
       o[HG_FH1 * NN + n] = g.fh0[q * 2];
       o[HG_FH2 * NN + n] = g.fh0[q * 2 + 1];
       o[HG_IJH * NN + n] = 1.0 / g.Jh[q];
+      o[HG_S2 * NN + n] = g.sinlat[q] * g.sinlat[q];
     }
   g.levc.assign((size_t)LC_N * Nv, 0);
   for (int v = 0; v < Nv; ++v) {

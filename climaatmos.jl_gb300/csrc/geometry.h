@@ -10,7 +10,8 @@ constexpr int NQ = 4;
 constexpr int NN = 16;
 
 // Per-node horizontal geometry quantities stored for the kernels ([elem][q][node]).
-enum HGeo { HG_JH = 0, HG_GU0, HG_GU1, HG_GU2, HG_GD0, HG_GD1, HG_GD2, HG_F3, HG_FH1, HG_FH2, HG_IJH, HG_N };
+// HG_S2: sin^2 of the node's latitude (Held-Suarez forcing)
+enum HGeo { HG_JH = 0, HG_GU0, HG_GU1, HG_GU2, HG_GD0, HG_GD1, HG_GD2, HG_F3, HG_FH1, HG_FH2, HG_IJH, HG_S2, HG_N };
 // Per-level centre quantities ([q][Nv]).
 // LC_SPG / LF_SPG: the sponge shape s(z) (beta = alpha s(z)), for the sponge-rate derivative.
 enum LevC { LC_Z = 0, LC_R2, LC_DZ, LC_PHI, LC_BETA, LC_IR2, LC_IDZ, LC_SPG, LC_N };

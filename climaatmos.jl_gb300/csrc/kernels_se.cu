@@ -174,7 +174,9 @@ __global__ void __launch_bounds__(SE_THREADS, SeMinBlocks<FT>::value) k_passA(De
   if (threadIdx.x == 0) tma_store_wait_all();
 }
 
-template <class FT>
+// HS: the Held-Suarez forcing is compiled in (a separate instantiation, so that
+// the default kernel carries none of its registers or instructions).
+template <class FT, bool HS>
 __global__ void __launch_bounds__(SE_THREADS, SeMinBlocks<FT>::value) k_passB(DevParams<FT> P, int nbuf, const FT *__restrict__ Yc,
                                                          const FT *__restrict__ Yf, const FT *__restrict__ Lin,
                                                          FT *__restrict__ Tc, FT *__restrict__ Tf) {
@@ -235,11 +237,13 @@ __global__ void __launch_bounds__(SE_THREADS, SeMinBlocks<FT>::value) k_passB(De
       }
       // Q: the u_h tendency less the face cross products (added in P3)
       FT rho[4], h[4], Pi[4], thp[4], gg[4], F1[4], F2[4], Q1[4], Q2[4];
+      FT hsk[4] = {0, 0, 0, 0};  // Held-Suarez drag rate k_f max(0, (sigma - sigma_b) / (1 - sigma_b))
       {
         FT u1[4], u2[4], c1[4], c2[4], K[4];
         {
-          FT gu0[4], gu1[4], gu2[4];
+          FT gu0[4], gu1[4], gu2[4], s2[4];
           g.gu(gu0, gu1, gu2);
+          if (HS) g.row(HG_S2, s2);
 #pragma unroll
           for (int i = 0; i < 4; ++i) {
             const int n = NQ * j + i;
@@ -262,6 +266,19 @@ __global__ void __launch_bounds__(SE_THREADS, SeMinBlocks<FT>::value) k_passB(De
             thp[i] = th.thv - th.thvr;
             // grad(K + Phi - Phi_r) and (cp_d / 2) grad(th' Pi) taken as one gradient
             gg[i] = (K[i] + Phi - th.phir) + P.cpd * (thp[i] * Pi[i]) / FT(2);
+            if (HS) {
+              // Held-Suarez forcing (held_suarez.jl:98-141, 203-225, 279-295), flat surface:
+              // sigma = p / MSLP; rho e_tot relaxes with -cv_d k_T rho (p / (rho R_d) - T_eq)
+              const FT c2l = FT(1) - s2[i];
+              const FT hf = fmax(FT(0), (th.p * P.hs_iMSLP - P.hs_sb) * P.hs_isb);
+              const FT kT = P.hs_ka + P.hs_dk * hf * (c2l * c2l);
+              const FT pr = th.p * P.hs_ip0;
+              const FT Teq =
+                  fmax(P.hs_Tmin, (P.hs_Teq - P.hs_dTy * s2[i] - P.hs_dthz * glog(pr) * c2l) * gpow(pr, P.kappa));
+              hsk[i] = P.hs_kf * hf;
+              // parked in the (already read) rho e_tot entry of the slab until the tendency is written
+              if (act) sY[48 * Nv + q] = kT * rho[i] * (th.p / (rho[i] * P.Rd) - Teq) * P.cvd;
+            }
           }
         }
         // vorticity w^3 = wcurl(u_h); (f^3 + w^3) x CT12(u) -> C12, and the sponge
@@ -284,8 +301,9 @@ __global__ void __launch_bounds__(SE_THREADS, SeMinBlocks<FT>::value) k_passB(De
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
           const FT a3 = f3[i] * idz + om[i];
-          Q1[i] = -(s.J[i] * (-a3 * c2[i])) - beta * u1[i];
-          Q2[i] = -(s.J[i] * (a3 * c1[i])) - beta * u2[i];
+          const FT damp = HS ? beta + hsk[i] : beta;  // sponge (+ Held-Suarez drag)
+          Q1[i] = -(s.J[i] * (-a3 * c2[i])) - damp * u1[i];
+          Q2[i] = -(s.J[i] * (a3 * c1[i])) - damp * u2[i];
           F1[i] = rho[i] * c1[i];
           F2[i] = rho[i] * c2[i];
           rJ[i] = rho[i] * s.J[i];
@@ -372,7 +390,11 @@ __global__ void __launch_bounds__(SE_THREADS, SeMinBlocks<FT>::value) k_passB(De
         wdiv(P, R, s, x1, x2, hd);
         if (act) {
 #pragma unroll
-          for (int i = 0; i < 4; ++i) sO[48 * Nv + (NQ * j + i) * Nv + v] = Trhoe[i] - P.nu_s * hd[i];
+          for (int i = 0; i < 4; ++i) {
+            const int q = 48 * Nv + (NQ * j + i) * Nv + v;
+            const FT t = Trhoe[i] - P.nu_s * hd[i];
+            sO[q] = HS ? t - sO[q] : t;
+          }
         }
       }
     }
@@ -535,7 +557,8 @@ void configure_se(int Nv) {
   (void)Nv;
   se_device();
   cudaFuncSetAttribute(k_passA<FT>, cudaFuncAttributeMaxDynamicSharedMemorySize, g_se.optin);
-  cudaFuncSetAttribute(k_passB<FT>, cudaFuncAttributeMaxDynamicSharedMemorySize, g_se.optin);
+  cudaFuncSetAttribute(k_passB<FT, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, g_se.optin);
+  cudaFuncSetAttribute(k_passB<FT, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, g_se.optin);
 }
 
 template <class FT>
@@ -550,7 +573,8 @@ void launch_passB(const DevParams<FT> &P, const FT *Yc, const FT *Yf, const FT *
   se_device();
   const SeShape sh = se_shape<FT, PassBLayout<FT>>(P.Nv);
   const int grid = min(P.Nh, g_se.nsm * sh.ctas);
-  k_passB<FT><<<grid, SE_THREADS, sh.smem, s>>>(P, sh.nbuf, Yc, Yf, L, Tc, Tf);
+  if (P.hs) k_passB<FT, true><<<grid, SE_THREADS, sh.smem, s>>>(P, sh.nbuf, Yc, Yf, L, Tc, Tf);
+  else k_passB<FT, false><<<grid, SE_THREADS, sh.smem, s>>>(P, sh.nbuf, Yc, Yf, L, Tc, Tf);
 }
 
 #define INST(FT)                                                                                             \

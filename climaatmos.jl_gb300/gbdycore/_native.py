@@ -38,7 +38,9 @@ class GBConfig(ctypes.Structure):
                 ("sponge_zd", _c_double), ("alpha_uh", _c_double), ("alpha_w", _c_double),
                 ("upwinding", _c_int)] + [(n, _c_double) for n in (
                     "grav", "omega", "R_d", "cp_d", "cv_d", "T_0", "p_ref", "T_min_ref", "T_surf_ref",
-                    "T_min_sgs", "radius")]
+                    "T_min_sgs", "radius")] + [("held_suarez", _c_int)] + [(n, _c_double) for n in (
+                    "hs_day", "hs_sigma_b", "hs_dT_y", "hs_T_equator", "hs_dtheta_z", "hs_T_min",
+                    "hs_p_ref_theta", "hs_MSLP")]
 
 
 class GBFieldVec(ctypes.Structure):
@@ -131,4 +133,7 @@ def make_config(cfg):
     c.upwinding = 1 if cfg.upwinding == "vanleer" else 0
     for k, v in cfg.constants.items():
         setattr(c, k, float(v))
+    c.held_suarez = 1 if cfg.held_suarez else 0
+    for k, v in cfg.hs.items():
+        setattr(c, "hs_" + k, float(v))
     return c

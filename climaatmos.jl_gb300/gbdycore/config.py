@@ -27,6 +27,20 @@ CONSTANTS = dict(
     radius=6.371229e6,
 )
 
+# Held-Suarez forcing parameters (dry values; Held and Suarez 1994, the values
+# ClimaParams names day, sigma_b, Delta T_y (dry), T_equator (dry), Delta theta_z,
+# T_min_hs, p_ref_theta and MSLP; held_suarez.jl:40-70).
+HELD_SUAREZ = dict(
+    day=86400.0,
+    sigma_b=0.7,
+    dT_y=60.0,
+    T_equator=315.0,
+    dtheta_z=10.0,
+    T_min=200.0,
+    p_ref_theta=1.0e5,
+    MSLP=101325.0,
+)
+
 SECONDS_PER_YEAR = 3.1536e7  # 365-day year, as in simulated_years_per_day (src/simulation/solve.jl:40-45)
 
 
@@ -67,6 +81,8 @@ class DycoreConfig:
     alpha_w: float = 0.0
     upwinding: str = "vanleer"
     constants: dict = field(default_factory=lambda: dict(CONSTANTS))
+    held_suarez: bool = False        # rad: held_suarez (src/config/model_getters.jl:636)
+    hs: dict = field(default_factory=lambda: dict(HELD_SUAREZ))
 
     def __post_init__(self):
         if self.nu is None:
@@ -84,7 +100,9 @@ class DycoreConfig:
         p = dict(self.constants)
         p.update(nu_v=self.nu, nu_s=self.nu_s, div_damp=self.divergence_damping, sponge_zd=self.sponge_zd,
                  alpha_uh=self.alpha_uh, alpha_w=self.alpha_w, z_max=self.z_max, dt_model=self.dt,
-                 upwinding=1 if self.upwinding == "vanleer" else 0, dss_stage1=1 if dss_stage1 else 0)
+                 upwinding=1 if self.upwinding == "vanleer" else 0, dss_stage1=1 if dss_stage1 else 0,
+                 held_suarez=1 if self.held_suarez else 0)
+        p.update({"hs_" + k: v for k, v in self.hs.items()})
         return p
 
 

@@ -46,6 +46,16 @@ struct GBConfig
     T_surf_ref::Cdouble
     T_min_sgs::Cdouble
     radius::Cdouble
+    # Held-Suarez forcing (rad: held_suarez): 0 off, 1 on
+    held_suarez::Cint
+    hs_day::Cdouble
+    hs_sigma_b::Cdouble
+    hs_dT_y::Cdouble
+    hs_T_equator::Cdouble
+    hs_dtheta_z::Cdouble
+    hs_T_min::Cdouble
+    hs_p_ref_theta::Cdouble
+    hs_MSLP::Cdouble
 end
 
 struct GBFieldVec

@@ -51,6 +51,12 @@ typedef struct {
   int upwinding;     /* energy_q_tot_upwinding: 0 none, 1 van Leer (types.jl:1916) */
   /* physical constants (ClimaParams names) */
   double grav, omega, R_d, cp_d, cv_d, T_0, p_ref, T_min_ref, T_surf_ref, T_min_sgs, radius;
+  /* Held-Suarez forcing of the explicit tendency (rad: held_suarez; held_suarez.jl): 0 off, 1 on
+     (flat surface: sigma = p / MSLP); day length, boundary-layer top sigma_b, equator-to-pole
+     contrast Delta T_y, equatorial surface temperature, static stability Delta theta_z, the
+     equilibrium floor T_min, the potential-temperature reference pressure and MSLP */
+  int held_suarez;
+  double hs_day, hs_sigma_b, hs_dT_y, hs_T_equator, hs_dtheta_z, hs_T_min, hs_p_ref_theta, hs_MSLP;
 } gb_config;
 
 typedef struct {

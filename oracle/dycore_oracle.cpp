@@ -19,6 +19,7 @@
 //   prep/apply hyperdiffusion      src/prognostic_equations/hyperdiffusion.jl:116-147, 247-307
 //   explicit_vertical_advection!   src/prognostic_equations/advection.jl:205-290 (deep branch)
 //   Rayleigh sponge                src/parameterized_tendencies/sponge/rayleigh_sponge.jl:7-57
+//   Held-Suarez forcing            src/parameterized_tendencies/radiation/held_suarez.jl:98-296
 //   implicit tendency              src/prognostic_equations/implicit/implicit_tendency.jl:185-298
 //   post-Newton correction         src/prognostic_equations/implicit/implicit_tendency.jl:322-339
 //   Jacobian blocks                src/prognostic_equations/implicit/manual_sparse_jacobian.jl:713-870
@@ -53,6 +54,8 @@ struct OracleParams {
   double dt_model;  // the model time step used by the van Leer Courant factor
   int upwinding;    // 0: central only (no post-Newton correction), 1: van Leer
   int dss_stage1;   // 1: DSS the first stage as well (ClimaTimeSteppers does)
+  int held_suarez;  // 1: Held-Suarez forcing in the remaining tendency
+  double hs_day, hs_sigma_b, hs_dT_y, hs_T_equator, hs_dtheta_z, hs_T_min, hs_p_ref_theta, hs_MSLP;
 };
 struct OracleGeom {
   int Nh, Nv, ngroups;
@@ -73,6 +76,8 @@ struct Oracle {
   FT grav, omega, Rd, cpd, cvd, T0, pref, Tmin_ref, Tsfc_ref, Tmin_sgs, R;
   FT nu_v, nu_s, div_damp, zd, a_uh, a_w, zmax, dt_model, kappa;
   int upwinding, dss_stage1;
+  int hs = 0;  // Held-Suarez forcing
+  FT hs_day, hs_sb, hs_dTy, hs_Teq, hs_dthz, hs_Tmin, hs_p0, hs_MSLP;
   // geometry
   FT W[NN], D[NQ][NQ];
   std::vector<FT> Jh, gup, gdn, sinlat, fh0, ecov, econ;
@@ -530,6 +535,24 @@ struct Oracle {
           Tc[ci(e, 1, n, v)] -= b * Yc[ci(e, 1, n, v)];
           Tc[ci(e, 2, n, v)] -= b * Yc[ci(e, 2, n, v)];
         }
+        // Held-Suarez forcing (remaining_tendency.jl:154-172; held_suarez.jl:98-120 compute_dRhoT,
+        // :122-141 compute_sigma / height_factor, :160-225 the rho e_tot relaxation times cv_d,
+        // :230-296 the boundary-layer drag k_f = 1/day).  Flat surface: sigma = p / MSLP;
+        // T = p / (rho R_d); latitude from the node's sin(lat).
+        if (hs) {
+          const FT s2 = sinlat[hn(e, n)] * sinlat[hn(e, n)], c2 = FT(1) - s2;
+          const FT ka = FT(1) / (FT(40) * hs_day), ks = FT(1) / (FT(4) * hs_day), kf = FT(1) / hs_day;
+          for (int v = 0; v < Nv; ++v) {
+            const FT rho = Yc[ci(e, 0, n, v)], p = pre.p[pi(e, n, v)];
+            const FT hf = std::max(FT(0), (p / hs_MSLP - hs_sb) / (FT(1) - hs_sb));
+            const FT kT = ka + (ks - ka) * hf * (c2 * c2);
+            const FT pr = p / hs_p0;
+            const FT Teq = std::max(hs_Tmin, (hs_Teq - hs_dTy * s2 - hs_dthz * std::log(pr) * c2) * std::pow(pr, kappa));
+            Tc[ci(e, 3, n, v)] -= kT * rho * (p / (rho * Rd) - Teq) * cvd;
+            Tc[ci(e, 1, n, v)] -= kf * hf * Yc[ci(e, 1, n, v)];
+            Tc[ci(e, 2, n, v)] -= kf * hf * Yc[ci(e, 2, n, v)];
+          }
+        }
       }
   }
 
@@ -898,6 +921,8 @@ struct Oracle {
     nu_v = p->nu_v; nu_s = p->nu_s; div_damp = p->div_damp; zd = p->sponge_zd; a_uh = p->alpha_uh; a_w = p->alpha_w;
     zmax = p->z_max; dt_model = p->dt_model; upwinding = p->upwinding; dss_stage1 = p->dss_stage1;
     kappa = Rd / cpd;
+    hs = p->held_suarez; hs_day = p->hs_day; hs_sb = p->hs_sigma_b; hs_dTy = p->hs_dT_y; hs_Teq = p->hs_T_equator;
+    hs_dthz = p->hs_dtheta_z; hs_Tmin = p->hs_T_min; hs_p0 = p->hs_p_ref_theta; hs_MSLP = p->hs_MSLP;
     for (int n = 0; n < NN; ++n) W[n] = g->W[n];
     for (int i = 0; i < NQ; ++i) for (int k = 0; k < NQ; ++k) D[i][k] = g->D[i * NQ + k];
     size_t H = (size_t)Nh * NN;
@@ -973,6 +998,12 @@ int oracle_max_threads() {
 void oracle_set_precomputed(void *hh, void *Yc, void *Yf) {
   Handle *h = (Handle *)hh;
   DISPATCH(h, (o.set_precomputed((decltype(o.R) *)Yc, (decltype(o.R) *)Yf)));
+}
+// The precomputed pressure at Y (centres, [Nh][16][Nv] in the oracle's precision).
+void oracle_pressure(void *hh, void *Yc, void *Yf, void *p_out) {
+  Handle *h = (Handle *)hh;
+  DISPATCH(h, (o.set_precomputed((decltype(o.R) *)Yc, (decltype(o.R) *)Yf),
+               std::copy(o.pre.p.begin(), o.pre.p.end(), (decltype(o.R) *)p_out)));
 }
 void oracle_remaining_tendency(void *hh, void *Tc, void *Tf, void *Yc, void *Yf) {
   Handle *h = (Handle *)hh;

@@ -36,7 +36,9 @@ class _Params(ctypes.Structure):
     _fields_ = [(n, ctypes.c_double) for n in (
         "grav", "omega", "R_d", "cp_d", "cv_d", "T_0", "p_ref", "T_min_ref", "T_surf_ref", "T_min_sgs", "radius",
         "nu_v", "nu_s", "div_damp", "sponge_zd", "alpha_uh", "alpha_w", "z_max", "dt_model")] + [
-        ("upwinding", ctypes.c_int), ("dss_stage1", ctypes.c_int)]
+        ("upwinding", ctypes.c_int), ("dss_stage1", ctypes.c_int), ("held_suarez", ctypes.c_int)] + [
+        (n, ctypes.c_double) for n in ("hs_day", "hs_sigma_b", "hs_dT_y", "hs_T_equator", "hs_dtheta_z",
+                                       "hs_T_min", "hs_p_ref_theta", "hs_MSLP")]
 
 
 _dp = ctypes.POINTER(ctypes.c_double)
@@ -64,6 +66,7 @@ def lib():
                      "oracle_jac_apply"):
             getattr(_lib, name).argtypes = [v, v, v, v, v]
         _lib.oracle_set_precomputed.argtypes = [v, v, v]
+        _lib.oracle_pressure.argtypes = [v, v, v, v]
         _lib.oracle_dss.argtypes = [v, v, v]
         _lib.oracle_update_jacobian.argtypes = [v, v, v, ctypes.c_double]
         _lib.oracle_step.argtypes = [v, v, v, ctypes.c_double, ctypes.c_int]
@@ -113,7 +116,7 @@ class Oracle:
         g.dss_w = arr(geom.dss_w)
         p = _Params()
         for k, _ in _Params._fields_:
-            setattr(p, k, params[k])
+            setattr(p, k, params.get(k, 0))
         self._g, self._p = g, p
         self.h = L.oracle_create(ctypes.byref(g), ctypes.byref(p), self.dtype.itemsize)
         self.Nh, self.Nv = geom.Nh, geom.Nv
@@ -134,6 +137,14 @@ class Oracle:
     def set_precomputed(self, Yc, Yf):
         self._chk(Yc, Yf)
         lib().oracle_set_precomputed(self.h, _ptr(Yc), _ptr(Yf))
+
+    def pressure(self, Yc, Yf):
+        """The precomputed pressure at Y, [Nh, 16, Nv]."""
+        Yc = np.ascontiguousarray(Yc, self.dtype)
+        Yf = np.ascontiguousarray(Yf, self.dtype)
+        p = np.zeros((self.Nh, 16, self.Nv), self.dtype)
+        lib().oracle_pressure(self.h, _ptr(Yc), _ptr(Yf), _ptr(p))
+        return p
 
     def remaining_tendency(self, Yc, Yf):
         Tc, Tf = self.zeros()

@@ -53,6 +53,8 @@ def parse():
     ap.add_argument("--fd-directions", type=int, default=32)
     ap.add_argument("--no-differentiation", action="store_true")
     ap.add_argument("--no-h60", action="store_true")
+    ap.add_argument("--held-suarez-steps", type=int, default=20)
+    ap.add_argument("--no-held-suarez", action="store_true")
     # bracket one forward step ("step") or one reverse pass ("reverse") by
     # cudaProfilerStart/Stop, for `ncu --profile-from-start off`; no effect otherwise
     ap.add_argument("--profile-region", default="none", choices=["none", "step", "reverse"])
@@ -344,6 +346,9 @@ def run_gb300(args):
     batching = None
     if not args.no_batching:
         batching = measure_batching(args)
+    held_suarez = None
+    if not args.no_held_suarez:
+        held_suarez = measure_held_suarez(args, ms)
 
     adjoint = None
     if not args.no_adjoint:
@@ -377,7 +382,7 @@ def run_gb300(args):
                     "what": "same step through the individual hooks (remaining/implicit tendency, Jacobian, ldiv, "
                             "post-Newton correction, DSS) with unfused torch stage algebra"},
                 "fp32_vs_fp64": prec, "batching": batching, "adjoint": adjoint,
-                "differentiation": differentiation, "precision_h60": h60,
+                "differentiation": differentiation, "precision_h60": h60, "held_suarez": held_suarez,
                 "clocks": clk, "gpu_launches": 20 * args.steps}
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -519,6 +524,30 @@ def measure_adjoint(args, s, fwd_ms):
                     "segment is recorded by the checkpointed forward pass) + reverse kernels; ratio against "
                     "the graph-replayed forward step",
             "dJ_dnu": d[0], "dJ_drate": d[1], "library_bytes": int(peak.value), "finite": finite}
+
+
+def measure_held_suarez(args, fwd_ms):
+    """The production step with the Held-Suarez forcing in the explicit tendency
+    (rad: held_suarez): SYPD, the cost over the plain dry step, and the state
+    after the timed steps (finite, mass conserved)."""
+    import torch
+    from gbdycore import config as C, simulation as sim
+    cfg = C.production_h30().with_(held_suarez=True)
+    s = sim.AtmosSimulation(cfg, workload="production")
+    m0 = s.p.global_sums(s.Y)[0]
+    s.step(3)
+    torch.cuda.synchronize()
+    n = args.held_suarez_steps
+    ms, _ = _timed(lambda: s.step(n))
+    ms /= n
+    m1 = s.p.global_sums(s.Y)[0]
+    finite = bool(torch.isfinite(s.Y.c).all() and torch.isfinite(s.Y.f).all())
+    out = {"steps": n + 3, "ms_per_step": ms, "value": sypd(cfg.dt, ms / 1e3), "unit": UNIT,
+           "over_dry_step": ms / fwd_ms, "mass_rel_change": abs(m1 - m0) / abs(m0), "finite": finite,
+           "parameters": dict(cfg.hs)}
+    del s
+    torch.cuda.empty_cache()
+    return out
 
 
 def measure_differentiation(args):

@@ -258,7 +258,8 @@ struct BvLayout {
   }
 };
 
-template <class FT>
+// HS: the Held-Suarez forcing's pullback is compiled in (a separate instantiation).
+template <class FT, bool HS>
 __global__ void __launch_bounds__(AD_THREADS, AdMinBlocks<FT>::value)
     k_passB_vjp(DevParams<FT> P, int nbuf, const FT *__restrict__ Yc, const FT *__restrict__ Yf,
                 const FT *__restrict__ Lc, const FT *__restrict__ Tbc, const FT *__restrict__ Tbf,
@@ -713,7 +714,7 @@ __global__ void __launch_bounds__(AD_THREADS, AdMinBlocks<FT>::value)
       }
       // ---- forward thermodynamics and the horizontal-dynamics transpose
       const FT Phi = P.levc[LC_PHI * Nv + v];
-      FT rho[4], rhoe[4], K[4], c1[4], c2[4], h[4], Pi[4], thp[4];
+      FT rho[4], rhoe[4], K[4], c1[4], c2[4], h[4], Pi[4], thp[4], pH[4];
       ld_row(crow(BC_K, v), K);
       ld_row(crow(BC_C1, v), c1);
       ld_row(crow(BC_C2, v), c2);
@@ -727,6 +728,7 @@ __global__ void __launch_bounds__(AD_THREADS, AdMinBlocks<FT>::value)
         h[i] = th.h;
         Pi[i] = th.Pi;
         thp[i] = th.thv - th.thvr;
+        if (HS) pH[i] = th.p;
       }
       FT hb_[4], Pib[4], thpb[4], phirb[4];
       {
@@ -819,8 +821,9 @@ __global__ void __launch_bounds__(AD_THREADS, AdMinBlocks<FT>::value)
         }
       }
       if (act) {
-        FT kvb[4], gu0[4], gu1[4], gu2[4];
+        FT kvb[4], gu0[4], gu1[4], gu2[4], s2[4];
         g.gu(gu0, gu1, gu2);
+        if (HS) g.row(HG_S2, s2);
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
           const int q = (NQ * j + i) * Nv + v;
@@ -830,6 +833,26 @@ __global__ void __launch_bounds__(AD_THREADS, AdMinBlocks<FT>::value)
           tb.thv = thpb[i];
           tb.thvr = -thpb[i];
           tb.phir = phirb[i];
+          if (HS) {
+            // Held-Suarez: T_rhoe -= E = cv_d k_T (p / R_d - rho T_eq), T_u -= k_f hf u,
+            // hf = max(0, (p / MSLP - sigma_b) / (1 - sigma_b)); cotangents of p, rho and u_h
+            const FT p = pH[i], c2l = FT(1) - s2[i];
+            const FT xs = (p * P.hs_iMSLP - P.hs_sb) * P.hs_isb;
+            const FT hf = fmax(FT(0), xs), dhf = xs > FT(0) ? P.hs_isb * P.hs_iMSLP : FT(0);
+            const FT kT = P.hs_ka + P.hs_dk * hf * (c2l * c2l), dkT = P.hs_dk * (c2l * c2l) * dhf;
+            const FT pr = p * P.hs_ip0, pk = gpow(pr, P.kappa);
+            const FT A = P.hs_Teq - P.hs_dTy * s2[i] - P.hs_dthz * glog(pr) * c2l;
+            const FT raw = A * pk;
+            const FT Teq = fmax(P.hs_Tmin, raw);
+            const FT dTeq = raw > P.hs_Tmin ? P.hs_ip0 * gdiv(pk, pr) * (P.kappa * A - P.hs_dthz * c2l) : FT(0);
+            const FT Teb = sT[48 * Nv + q], Tu1b = sT[16 * Nv + q], Tu2b = sT[32 * Nv + q];
+            const FT u1 = sY[16 * Nv + q], u2 = sY[32 * Nv + q];
+            const FT dEdp = P.cvd * (dkT * (p / P.Rd - rho[i] * Teq) + kT * (FT(1) / P.Rd - rho[i] * dTeq));
+            tb.p = -Teb * dEdp - P.hs_kf * dhf * (u1 * Tu1b + u2 * Tu2b);
+            rhob[i] += Teb * P.cvd * kT * Teq;
+            u1b[i] -= P.hs_kf * hf * Tu1b;
+            u2b[i] -= P.hs_kf * hf * Tu2b;
+          }
           FT rb, reb, kb;
           thermo_vjp(P, rho[i], rhoe[i], K[i], Phi, tb, rb, reb, kb);
           const FT Kt = Kb[i] + kb;
@@ -928,8 +951,10 @@ void configure_adjoint_se(int Nv) {
   cudaFuncAttributes fa{};
   cudaFuncGetAttributes(&fa, k_passA_vjp<FT>);
   cudaFuncSetAttribute(k_passA_vjp<FT>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes);
-  cudaFuncGetAttributes(&fa, k_passB_vjp<FT>);
-  cudaFuncSetAttribute(k_passB_vjp<FT>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes);
+  cudaFuncGetAttributes(&fa, k_passB_vjp<FT, false>);
+  cudaFuncSetAttribute(k_passB_vjp<FT, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes);
+  cudaFuncGetAttributes(&fa, k_passB_vjp<FT, true>);
+  cudaFuncSetAttribute(k_passB_vjp<FT, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes);
 }
 
 template <class FT>
@@ -946,7 +971,10 @@ void launch_passB_vjp(const DevParams<FT> &P, const FT *Yc, const FT *Yf, const 
                       FT *Ybc, FT *Ybf, FT *Lb, double *dpar, int grid, bool accum, cudaStream_t s) {
   const AdShape sh = ad_shape<BvLayout<FT>>(P.Nv, AdMinBlocks<FT>::value);
   const int g = std::max(1, std::min({grid, P.Nh, ad_dev().nsm * sh.ctas}));
-  k_passB_vjp<FT><<<g, AD_THREADS, sh.smem, s>>>(P, sh.nbuf, Yc, Yf, L, Tbc, Tbf, Ybc, Ybf, Lb, dpar, accum ? 1 : 0);
+  if (P.hs)
+    k_passB_vjp<FT, true><<<g, AD_THREADS, sh.smem, s>>>(P, sh.nbuf, Yc, Yf, L, Tbc, Tbf, Ybc, Ybf, Lb, dpar, accum ? 1 : 0);
+  else
+    k_passB_vjp<FT, false><<<g, AD_THREADS, sh.smem, s>>>(P, sh.nbuf, Yc, Yf, L, Tbc, Tbf, Ybc, Ybf, Lb, dpar, accum ? 1 : 0);
 }
 
 #define INST(FT)                                                                                             \

@@ -482,8 +482,6 @@ template <class FT>
 int ensure_adjoint(gb_ctx *ctx) {
   Impl<FT> *I = impl<FT>(ctx);
   if (I->adj) return GB_OK;
-  if (ctx->cfg.held_suarez)
-    return fail(ctx, GB_ERR_ARG, "reverse mode does not cover the Held-Suarez forcing (configure held_suarez = 0)");
   int dev = 0, optin = 0, nsm = 0;
   CK(cudaGetDevice(&dev));
   CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));

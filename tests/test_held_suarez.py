@@ -9,8 +9,8 @@ surface pressure is MSLP, so sigma = p / MSLP.
 CPU: the oracle's forcing equals a numpy restatement of those formulas (the
 difference of the oracle's remaining tendency with and without the forcing);
 invalid parameters are rejected at the C ABI.  GPU: the remaining tendency and
-the fused IMEX step with the forcing on against the oracle, and reverse mode
-refusing the configuration.
+the fused IMEX step with the forcing on against the oracle, and the pullbacks of
+the tendency and of one step against central differences (FP64).
 """
 import ctypes
 
@@ -118,12 +118,74 @@ def test_gpu_fused_step_with_forcing_fp64():
     assert np.abs(r2c - rc).max() > 0
 
 
+def _fv(Yc, Yf):
+    from gbdycore import simulation as sim
+    return sim.FieldVector.from_numpy(np.ascontiguousarray(Yc), np.ascontiguousarray(Yf))
+
+
+def _dot(A, B):
+    return float((A.c * B.c).sum().item() + (A.f * B.f).sum().item())
+
+
+def _direction(Yc, Yf, seed):
+    rng = np.random.default_rng(seed)
+    dc = rng.standard_normal(Yc.shape)
+    for c in range(4):
+        dc[:, c] *= np.sqrt(np.mean(Yc[:, c] ** 2))
+    df = rng.standard_normal(Yf.shape) * np.sqrt(np.mean(Yf ** 2))
+    return dc, df
+
+
+def _cotangent(Xc, Xf, seed):
+    rng = np.random.default_rng(seed)
+    return _fv(rng.standard_normal(Xc.shape) / np.maximum(np.abs(Xc).max(axis=(0, 2, 3), keepdims=True), 1e-30),
+               rng.standard_normal(Xf.shape) / max(np.abs(Xf).max(), 1e-30))
+
+
+H = 1.0e-6
+
+
 @pytest.mark.gpu
-def test_gpu_reverse_mode_refuses_the_forcing():
+def test_gpu_remaining_tendency_vjp_with_forcing():
+    """<Tb, (T(Y + h d) - T(Y - h d)) / 2h> == <T^T Tb, d> with the forcing on (FP64)."""
     from gbdycore import simulation as sim
     cfg = hs_config(ft=np.float64)
     Yc, Yf = perturbed_state(cfg)
-    s = sim.AtmosSimulation(cfg, state=(Yc, Yf))
-    with pytest.raises(N.GBError) as ei:
-        s.p.call("gb_adjoint_forward", s.Y.gb(), 0.0, float(cfg.dt), 2, 1)
-    assert ei.value.code == N.GB_ERR_ARG
+    p = sim.AtmosCache(cfg)
+    Y = _fv(Yc, Yf)
+    T = Y.similar()
+    sim.remaining_tendency(T, None, Y, p, 0.0)
+    Tb = _cotangent(*T.numpy(), seed=2)
+    Yb = Y.similar()
+    sim.remaining_tendency_vjp(Yb, Tb, Y, p, 0.0)
+    for seed in (3, 4):
+        dc, df = _direction(Yc, Yf, seed)
+        Tp, Tm = Y.similar(), Y.similar()
+        sim.remaining_tendency(Tp, None, _fv(Yc + H * dc, Yf + H * df), p, 0.0)
+        sim.remaining_tendency(Tm, None, _fv(Yc - H * dc, Yf - H * df), p, 0.0)
+        fd = (_dot(Tb, Tp) - _dot(Tb, Tm)) / (2 * H)
+        got = _dot(Yb, _fv(dc, df))
+        assert abs(got - fd) <= 1e-6 * abs(fd), (got, fd)
+
+
+@pytest.mark.gpu
+def test_gpu_step_vjp_with_forcing():
+    from gbdycore import simulation as sim
+    cfg = hs_config(ft=np.float64)
+    Yc, Yf = perturbed_state(cfg, w_amp=0.05)
+    p = sim.AtmosCache(cfg)
+    Y = _fv(Yc, Yf)
+
+    def step(X):
+        Z = X.copy()
+        p.call("gb_step", Z.gb(), 0.0, float(cfg.dt), 1, 0)
+        return Z
+
+    Yb = _cotangent(*step(Y).numpy(), seed=8)
+    Ybar = Yb.copy()
+    sim.step_vjp(Ybar, Y, p, 0.0, cfg.dt)
+    for seed in (9, 10):
+        dc, df = _direction(Yc, Yf, seed)
+        fd = (_dot(Yb, step(_fv(Yc + H * dc, Yf + H * df))) - _dot(Yb, step(_fv(Yc - H * dc, Yf - H * df)))) / (2 * H)
+        got = _dot(Ybar, _fv(dc, df))
+        assert abs(got - fd) <= 1e-6 * abs(fd), (got, fd)

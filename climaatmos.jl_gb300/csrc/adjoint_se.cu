@@ -230,7 +230,9 @@ __global__ void __launch_bounds__(AD_THREADS, AdMinBlocks<FT>::value)
 enum BvCentre { BC_C1 = 0, BC_C2, BC_K, BC_RJ, BC_L4, BC_N };
 enum BvFace { BF_X1 = 0, BF_X2, BF_CC1, BF_CC2, BF_RJ, BF_CV1, BF_CV2, BF_U3, BF_N };
 
-template <class FT>
+// GL: the Laplacians and the tendency cotangent are read from global memory
+// instead of being staged (tall columns, where the staged slabs do not fit).
+template <class FT, bool GL = false>
 struct BvLayout {
   size_t y[2], f[2], g[2], lap[2], tb[2], tbf[2], c, fc, kvb, w, red, bar, total;
   __host__ __device__ BvLayout(int Nv, int nbuf) {
@@ -241,9 +243,12 @@ struct BvLayout {
         y[b] = o; o += align16(sizeof(FT) * 64 * Nv);
         f[b] = o; o += align16(sizeof(FT) * 16 * Nf);
         g[b] = o; o += align16(sizeof(FT) * HG_N * 16);
-        lap[b] = o; o += align16(sizeof(FT) * 64 * Nv);
-        tb[b] = o; o += align16(sizeof(FT) * 64 * Nv);
-        tbf[b] = o; o += align16(sizeof(FT) * 16 * Nf);
+        lap[b] = tb[b] = tbf[b] = 0;
+        if (!GL) {
+          lap[b] = o; o += align16(sizeof(FT) * 64 * Nv);
+          tb[b] = o; o += align16(sizeof(FT) * 64 * Nv);
+          tbf[b] = o; o += align16(sizeof(FT) * 16 * Nf);
+        }
       } else {
         y[b] = y[0]; f[b] = f[0]; g[b] = g[0]; lap[b] = lap[0]; tb[b] = tb[0]; tbf[b] = tbf[0];
       }
@@ -259,7 +264,7 @@ struct BvLayout {
 };
 
 // HS: the Held-Suarez forcing's pullback is compiled in (a separate instantiation).
-template <class FT, bool HS>
+template <class FT, bool HS, bool GL>
 __global__ void __launch_bounds__(AD_THREADS, AdMinBlocks<FT>::value)
     k_passB_vjp(DevParams<FT> P, int nbuf, const FT *__restrict__ Yc, const FT *__restrict__ Yf,
                 const FT *__restrict__ Lc, const FT *__restrict__ Tbc, const FT *__restrict__ Tbf,
@@ -267,7 +272,7 @@ __global__ void __launch_bounds__(AD_THREADS, AdMinBlocks<FT>::value)
                 int accum) {
   extern __shared__ __align__(128) unsigned char sm[];
   const int Nv = P.Nv, Nf = P.Nf;
-  const BvLayout<FT> Lo(Nv, nbuf);
+  const BvLayout<FT, GL> Lo(Nv, nbuf);
   auto at = [&](const size_t (&off)[2], int b) { return (FT *)(sm + (b ? off[1] : off[0])); };
   FT *sC = (FT *)(sm + Lo.c), *sFc = (FT *)(sm + Lo.fc), *sKvb = (FT *)(sm + Lo.kvb), *sW = (FT *)(sm + Lo.w);
   double *red = (double *)(sm + Lo.red);
@@ -276,13 +281,15 @@ __global__ void __launch_bounds__(AD_THREADS, AdMinBlocks<FT>::value)
   const uint32_t bg = uint32_t(sizeof(FT) * HG_N * 16);
   auto issue = [&](int b, int e) {
     uint64_t *bb = b ? &bar[1] : &bar[0];
-    mbar_expect_tx(bb, 3 * by + 2 * bf + bg);
+    mbar_expect_tx(bb, GL ? by + bf + bg : 3 * by + 2 * bf + bg);
     tma_load(at(Lo.y, b), Yc + (size_t)e * 64 * Nv, by, bb);
     tma_load(at(Lo.f, b), Yf + (size_t)e * 16 * Nf, bf, bb);
     tma_load(at(Lo.g, b), P.hgeo + (size_t)e * HG_N * 16, bg, bb);
-    tma_load(at(Lo.lap, b), Lc + (size_t)e * 64 * Nv, by, bb);
-    tma_load(at(Lo.tb, b), Tbc + (size_t)e * 64 * Nv, by, bb);
-    tma_load(at(Lo.tbf, b), Tbf + (size_t)e * 16 * Nf, bf, bb);
+    if (!GL) {
+      tma_load(at(Lo.lap, b), Lc + (size_t)e * 64 * Nv, by, bb);
+      tma_load(at(Lo.tb, b), Tbc + (size_t)e * 64 * Nv, by, bb);
+      tma_load(at(Lo.tbf, b), Tbf + (size_t)e * 16 * Nf, bf, bb);
+    }
   };
   if (threadIdx.x < NN) {
     sW[threadIdx.x] = P.W[threadIdx.x];
@@ -304,8 +311,10 @@ __global__ void __launch_bounds__(AD_THREADS, AdMinBlocks<FT>::value)
   for (int it = 0; e < P.Nh; ++it, e += gridDim.x) {
     int b;
     if (!slab_begin(bar, nbuf, it, e, P.Nh, P.status, issue, b)) break;
-    const FT *sY = at(Lo.y, b), *sF = at(Lo.f, b), *sG = at(Lo.g, b), *sL = at(Lo.lap, b);
-    const FT *sT = at(Lo.tb, b), *sTf = at(Lo.tbf, b);
+    const FT *sY = at(Lo.y, b), *sF = at(Lo.f, b), *sG = at(Lo.g, b);
+    const FT *sL = GL ? Lc + (size_t)e * 64 * Nv : at(Lo.lap, b);
+    const FT *sT = GL ? Tbc + (size_t)e * 64 * Nv : at(Lo.tb, b);
+    const FT *sTf = GL ? Tbf + (size_t)e * 16 * Nf : at(Lo.tbf, b);
     const SlabGeo<FT> g{sG + NQ * j, sW + NQ * j};
     auto levrow = [&](int v, LevRow<FT> &s) {
       FT Jh[4], iJh[4], W[4], iW[4];
@@ -936,9 +945,14 @@ template <class FT>
 size_t passA_vjp_smem(int Nv) {
   return AvLayout<FT>(Nv, 1).total;
 }
+// Whether pass B^T stages the Laplacians and the tendency cotangent (they fit).
+template <class FT>
+bool passB_vjp_staged(int Nv) {
+  return BvLayout<FT, false>(Nv, 1).total <= (size_t)ad_dev().optin;
+}
 template <class FT>
 size_t passB_vjp_smem(int Nv) {
-  return BvLayout<FT>(Nv, 1).total;
+  return passB_vjp_staged<FT>(Nv) ? BvLayout<FT, false>(Nv, 1).total : BvLayout<FT, true>(Nv, 1).total;
 }
 
 template <class FT>
@@ -951,10 +965,14 @@ void configure_adjoint_se(int Nv) {
   cudaFuncAttributes fa{};
   cudaFuncGetAttributes(&fa, k_passA_vjp<FT>);
   cudaFuncSetAttribute(k_passA_vjp<FT>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes);
-  cudaFuncGetAttributes(&fa, k_passB_vjp<FT, false>);
-  cudaFuncSetAttribute(k_passB_vjp<FT, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes);
-  cudaFuncGetAttributes(&fa, k_passB_vjp<FT, true>);
-  cudaFuncSetAttribute(k_passB_vjp<FT, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes);
+  auto raise = [&](auto kern) {
+    cudaFuncGetAttributes(&fa, kern);
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes);
+  };
+  raise(k_passB_vjp<FT, false, false>);
+  raise(k_passB_vjp<FT, true, false>);
+  raise(k_passB_vjp<FT, false, true>);
+  raise(k_passB_vjp<FT, true, true>);
 }
 
 template <class FT>
@@ -969,12 +987,18 @@ void launch_passA_vjp(const DevParams<FT> &P, const FT *Yc, const FT *Yf, const 
 template <class FT>
 void launch_passB_vjp(const DevParams<FT> &P, const FT *Yc, const FT *Yf, const FT *L, const FT *Tbc, const FT *Tbf,
                       FT *Ybc, FT *Ybf, FT *Lb, double *dpar, int grid, bool accum, cudaStream_t s) {
-  const AdShape sh = ad_shape<BvLayout<FT>>(P.Nv, AdMinBlocks<FT>::value);
+  const bool staged = passB_vjp_staged<FT>(P.Nv);
+  const AdShape sh = staged ? ad_shape<BvLayout<FT, false>>(P.Nv, AdMinBlocks<FT>::value)
+                            : ad_shape<BvLayout<FT, true>>(P.Nv, AdMinBlocks<FT>::value);
   const int g = std::max(1, std::min({grid, P.Nh, ad_dev().nsm * sh.ctas}));
-  if (P.hs)
-    k_passB_vjp<FT, true><<<g, AD_THREADS, sh.smem, s>>>(P, sh.nbuf, Yc, Yf, L, Tbc, Tbf, Ybc, Ybf, Lb, dpar, accum ? 1 : 0);
-  else
-    k_passB_vjp<FT, false><<<g, AD_THREADS, sh.smem, s>>>(P, sh.nbuf, Yc, Yf, L, Tbc, Tbf, Ybc, Ybf, Lb, dpar, accum ? 1 : 0);
+  const int ac = accum ? 1 : 0;
+  if (staged) {
+    if (P.hs) k_passB_vjp<FT, true, false><<<g, AD_THREADS, sh.smem, s>>>(P, sh.nbuf, Yc, Yf, L, Tbc, Tbf, Ybc, Ybf, Lb, dpar, ac);
+    else k_passB_vjp<FT, false, false><<<g, AD_THREADS, sh.smem, s>>>(P, sh.nbuf, Yc, Yf, L, Tbc, Tbf, Ybc, Ybf, Lb, dpar, ac);
+  } else {
+    if (P.hs) k_passB_vjp<FT, true, true><<<g, AD_THREADS, sh.smem, s>>>(P, sh.nbuf, Yc, Yf, L, Tbc, Tbf, Ybc, Ybf, Lb, dpar, ac);
+    else k_passB_vjp<FT, false, true><<<g, AD_THREADS, sh.smem, s>>>(P, sh.nbuf, Yc, Yf, L, Tbc, Tbf, Ybc, Ybf, Lb, dpar, ac);
+  }
 }
 
 #define INST(FT)                                                                                             \

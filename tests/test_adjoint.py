@@ -240,3 +240,62 @@ def test_step_vjp_deterministic_with_separate_blocks(setup):
         del pad
     for G in outs[1:]:
         assert torch.equal(G.c, outs[0].c) and torch.equal(G.f, outs[0].f)
+
+
+@pytest.mark.gpu
+def test_step_vjp_tall_columns():
+    """z_elem = 70: the slab kernels' second level sweep, pass B^T reading the Laplacians and
+    the cotangent from global memory (FP64 slabs too tall to stage) and the 4-levels-per-lane
+    column pullback.  Without the van Leer limiter: at this height its min/max branches sit
+    close enough to the state that central differences straddle them (the limiter's own
+    pullback is covered at smaller heights)."""
+    sim = _sim()
+    cfg = adj_config(z_elem=70, upwinding="none")
+    Yc, Yf = perturbed_state(cfg, w_amp=0.05, dtype=np.float64)
+    p = sim.AtmosCache(cfg)
+    Y = _fv(Yc, Yf)
+
+    def step(X):
+        Z = X.copy()
+        p.call("gb_step", Z.gb(), 0.0, float(cfg.dt), 1, 0)
+        return Z
+
+    Y1 = step(Y).numpy()
+    rng = np.random.default_rng(21)
+    Yb = _fv(rng.standard_normal(Yc.shape) / np.maximum(np.abs(Y1[0]).max(axis=(0, 2, 3), keepdims=True), 1e-30),
+             rng.standard_normal(Yf.shape) / max(np.abs(Y1[1]).max(), 1e-30))
+    Ybar = Yb.copy()
+    sim.step_vjp(Ybar, Y, p, 0.0, cfg.dt)
+    dc, df = _scaled(Yc.shape, Yf.shape, Yc, Yf, 22)
+    fd = (_dot(Yb, step(_axpy(Yc, Yf, H, dc, df))) - _dot(Yb, step(_axpy(Yc, Yf, -H, dc, df)))) / (2 * H)
+    assert rel(_dot(Ybar, _fv(dc, df)), fd) < 1e-6
+
+
+@pytest.mark.gpu
+def test_remaining_tendency_vjp_at_zero_hyperdiffusion(setup):
+    """nu = 0: d/dnu from the direct form (the transposes carry no nu then)."""
+    sim = _sim()
+    cfg0, Yc, Yf = setup
+    nu0 = cfg0.nu
+    cfg = cfg0.with_(nu=0.0)
+    p = sim.AtmosCache(cfg)
+    Y = _fv(Yc, Yf)
+    T = Y.similar()
+    sim.remaining_tendency(T, None, Y, p, 0.0)
+    rng = np.random.default_rng(23)
+    Tn = sim.AtmosCache(cfg0)
+    T0 = Y.similar()
+    sim.remaining_tendency(T0, None, Y, Tn, 0.0)
+    T0n = T0.numpy()
+    Tb = _fv(rng.standard_normal(Yc.shape) / np.maximum(np.abs(T0n[0]).max(axis=(0, 2, 3), keepdims=True), 1e-30),
+             rng.standard_normal(Yf.shape) / max(np.abs(T0n[1]).max(), 1e-30))
+    Yb = Y.similar()
+    dpar = sim.remaining_tendency_vjp(Yb, Tb, Y, p, 0.0)
+    vals = []
+    for s in (1.0, -1.0):
+        q = sim.AtmosCache(cfg.with_(nu=s * HP * nu0))
+        Tq = Y.similar()
+        sim.remaining_tendency(Tq, None, Y, q, 0.0)
+        vals.append(_dot(Tb, Tq))
+    fd = (vals[0] - vals[1]) / (2 * HP * nu0)
+    assert rel(dpar[0], fd) < 1e-6, (dpar[0], fd)

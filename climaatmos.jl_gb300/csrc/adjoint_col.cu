@@ -51,6 +51,9 @@ struct ColVjpArgs {
   FT *Tib_c[4], *Tib_f[4];  // cotangents of the implicit tendencies (accumulated)
   FT *scr;
   double *dalpha;         // per-column d/d(sponge rate), accumulated
+  // when set: the recorded stage output U and implicit tendency T_imp, from which
+  // U^ = U - dtgamma T_imp (the stage leaves u_h unchanged) replaces the assembly
+  const FT *Uo_c, *Uo_f, *Tio_c, *Tio_f;
 };
 
 template <class FT>
@@ -652,6 +655,17 @@ __global__ void __launch_bounds__(128, VjpMinBlocks<FT>::value) k_col_stage_vjp_
   }
   // ---------------------------------------------------------------- forward recompute
   FT H[5][CM];
+  if (V.Uo_c) {
+#pragma unroll
+    for (int k = 0; k < CM; ++k) {
+      const bool okc = r0 + k < Nv, okf = r0 + k < Nf;
+      H[0][k] = okc ? V.Uo_c[cb + k] - dtg * V.Tio_c[rb + k] : FT(0);
+      H[1][k] = okc ? V.Uo_c[cb + (size_t)sc + k] : FT(0);
+      H[2][k] = okc ? V.Uo_c[cb + (size_t)2 * sc + k] : FT(0);
+      H[3][k] = okc ? V.Uo_c[cb + (size_t)3 * sc + k] - dtg * V.Tio_c[rb + (size_t)sc + k] : FT(0);
+      H[4][k] = okf ? V.Uo_f[fb + k] - dtg * V.Tio_f[fb + k] : FT(0);
+    }
+  } else {
 #pragma unroll
   for (int k = 0; k < CM; ++k) {
     const bool okc = r0 + k < Nv, okf = r0 + k < Nf;
@@ -672,6 +686,7 @@ __global__ void __launch_bounds__(128, VjpMinBlocks<FT>::value) k_col_stage_vjp_
       H[4][k] += A.ce[j] * (okf ? A.te_f[j][fb + k] : FT(0));
       if (j >= 1) H[4][k] += A.ci[j] * (okf ? A.ti_f[j][fb + k] : FT(0));
     }
+  }
   }
 #pragma unroll
   for (int k = 0; k < CM; ++k) {
@@ -1152,9 +1167,13 @@ size_t col_vjp_scratch_words(int Nh, int Nv) { return (size_t)S_NUM * (Nv + 1) *
 template <class FT>
 void launch_column_stage_vjp(const DevParams<FT> &P, const StageArgs<FT> &A, const FT *Ub_c, const FT *Ub_f,
                              const FT *Tb_c, const FT *Tb_f, FT *Yb_c, FT *Yb_f, FT *const Teb[4], FT *const Tib[4],
-                             size_t NC, size_t NR, FT *scr, double *dalpha, cudaStream_t s) {
+                             size_t NC, size_t NR, FT *scr, double *dalpha, cudaStream_t s, const FT *Uo,
+                             const FT *Tio) {
   ColVjpArgs<FT> V{};
   V.A = A;
+  if (Uo && Tio) {
+    V.Uo_c = Uo; V.Uo_f = Uo + NC; V.Tio_c = Tio; V.Tio_f = Tio + NR;
+  }
   V.Ub_c = Ub_c; V.Ub_f = Ub_f; V.Tb_c = Tb_c; V.Tb_f = Tb_f; V.Yb_c = Yb_c; V.Yb_f = Yb_f;
   for (int j = 0; j < 4; ++j) {
     V.Teb_c[j] = Teb[j];
@@ -1184,10 +1203,10 @@ void launch_column_stage_vjp(const DevParams<FT> &P, const StageArgs<FT> &A, con
 template void launch_column_stage_vjp<float>(const DevParams<float> &, const StageArgs<float> &, const float *,
                                              const float *, const float *, const float *, float *, float *,
                                              float *const[4], float *const[4], size_t, size_t, float *, double *,
-                                             cudaStream_t);
+                                             cudaStream_t, const float *, const float *);
 template void launch_column_stage_vjp<double>(const DevParams<double> &, const StageArgs<double> &, const double *,
                                               const double *, const double *, const double *, double *, double *,
                                               double *const[4], double *const[4], size_t, size_t, double *,
-                                              double *, cudaStream_t);
+                                              double *, cudaStream_t, const double *, const double *);
 
 }  // namespace gb

@@ -656,7 +656,8 @@ void reverse_step(gb_ctx *ctx, typename Impl<FT>::Record &rec, double dt_, FT *Y
       tendency_vjp<FT>(ctx, Uc, Uf, (const FT *)rec.L[i].p, Teb[i], Teb[i] + I->NC, Ubc, Ubf, true, false, s);
       const StageArgs<FT> SA = stage_args<FT>(I, i, dt, Yc, Yf, Te, Ti);
       launch_column_stage_vjp<FT>(P, SA, Ubc, Ubf, Tib[i], Tib[i] + I->NR, Ybc, Ybf, Teb, Tib, I->NC, I->NR,
-                                  (FT *)A.scr.p, (double *)A.dal.p, s);
+                                  (FT *)A.scr.p, (double *)A.dal.p, s, (const FT *)rec.U[i].p,
+                                  (const FT *)rec.Ti[i].p);
     }
   }
 }

@@ -81,9 +81,10 @@ AdShape ad_shape(int Nv, int minb) {
 // the Laplacian cotangent Lb (64 Nv) and the state cotangent (64 Nv, 16 Nf),
 // which is accumulated in place and stored back.  Scratch: the face parts of
 // each level's cotangent, level-major rows [Nv][16] (lower, upper face).
-template <class FT>
+// ADD: a further cotangent slab (xb, xf) is loaded and added as well.
+template <class FT, bool ADD = false>
 struct AvLayout {
-  size_t y[2], f[2], g[2], lb[2], yb[2], fb[2], lo, hi, bar, total;
+  size_t y[2], f[2], g[2], lb[2], yb[2], fb[2], xb[2], xf[2], lo, hi, bar, total;
   __host__ __device__ AvLayout(int Nv, int nbuf) {
     const int Nf = Nv + 1;
     size_t o = 0;
@@ -95,8 +96,14 @@ struct AvLayout {
         lb[b] = o; o += align16(sizeof(FT) * 64 * Nv);
         yb[b] = o; o += align16(sizeof(FT) * 64 * Nv);
         fb[b] = o; o += align16(sizeof(FT) * 16 * Nf);
+        xb[b] = xf[b] = 0;
+        if (ADD) {
+          xb[b] = o; o += align16(sizeof(FT) * 64 * Nv);
+          xf[b] = o; o += align16(sizeof(FT) * 16 * Nf);
+        }
       } else {
         y[b] = y[0]; f[b] = f[0]; g[b] = g[0]; lb[b] = lb[0]; yb[b] = yb[0]; fb[b] = fb[0];
+        xb[b] = xb[0]; xf[b] = xf[0];
       }
     }
     lo = o; o += align16(sizeof(FT) * 16 * Nv);
@@ -106,13 +113,16 @@ struct AvLayout {
   }
 };
 
-template <class FT>
+// ADD: Ybar += Xbar + the pass's own contribution (Xbar, a further cotangent of
+// the state, e.g. pass B^T's, is read by TMA with the other slabs).
+template <class FT, bool ADD>
 __global__ void __launch_bounds__(AD_THREADS, AdMinBlocks<FT>::value)
     k_passA_vjp(DevParams<FT> P, int nbuf, const FT *__restrict__ Yc, const FT *__restrict__ Yf,
-                const FT *__restrict__ Lb, FT *__restrict__ Ybc, FT *__restrict__ Ybf) {
+                const FT *__restrict__ Lb, FT *__restrict__ Ybc, FT *__restrict__ Ybf, const FT *__restrict__ Xbc,
+                const FT *__restrict__ Xbf) {
   extern __shared__ __align__(128) unsigned char sm[];
   const int Nv = P.Nv, Nf = P.Nf;
-  const AvLayout<FT> Lo(Nv, nbuf);
+  const AvLayout<FT, ADD> Lo(Nv, nbuf);
   // slab x of buffer b (selects, not a runtime-indexed array)
   auto at = [&](const size_t (&off)[2], int b) { return (FT *)(sm + (b ? off[1] : off[0])); };
   FT *sLo = (FT *)(sm + Lo.lo), *sHi = (FT *)(sm + Lo.hi);
@@ -120,7 +130,7 @@ __global__ void __launch_bounds__(AD_THREADS, AdMinBlocks<FT>::value)
   const uint32_t by = uint32_t(sizeof(FT) * 64 * Nv), bf = uint32_t(sizeof(FT) * 16 * Nf);
   const uint32_t bg = uint32_t(sizeof(FT) * HG_N * 16);
   auto issue = [&](int b, int e) {
-    mbar_expect_tx(b ? &bar[1] : &bar[0], 3 * by + 2 * bf + bg);
+    mbar_expect_tx(b ? &bar[1] : &bar[0], ADD ? 4 * by + 3 * bf + bg : 3 * by + 2 * bf + bg);
     uint64_t *bb = b ? &bar[1] : &bar[0];
     tma_load(at(Lo.y, b), Yc + (size_t)e * 64 * Nv, by, bb);
     tma_load(at(Lo.f, b), Yf + (size_t)e * 16 * Nf, bf, bb);
@@ -128,6 +138,10 @@ __global__ void __launch_bounds__(AD_THREADS, AdMinBlocks<FT>::value)
     tma_load(at(Lo.lb, b), Lb + (size_t)e * 64 * Nv, by, bb);
     tma_load(at(Lo.yb, b), Ybc + (size_t)e * 64 * Nv, by, bb);
     tma_load(at(Lo.fb, b), Ybf + (size_t)e * 16 * Nf, bf, bb);
+    if (ADD) {
+      tma_load(at(Lo.xb, b), Xbc + (size_t)e * 64 * Nv, by, bb);
+      tma_load(at(Lo.xf, b), Xbf + (size_t)e * 16 * Nf, bf, bb);
+    }
   };
   slab_init_bars(bar);
   int e = blockIdx.x;
@@ -140,6 +154,7 @@ __global__ void __launch_bounds__(AD_THREADS, AdMinBlocks<FT>::value)
     if (!slab_begin(bar, nbuf, it, e, P.Nh, P.status, issue, b)) break;
     const FT *sY = at(Lo.y, b), *sF = at(Lo.f, b), *sG = at(Lo.g, b), *sL = at(Lo.lb, b);
     FT *sB = at(Lo.yb, b), *sBf = at(Lo.fb, b);
+    const FT *sX = at(Lo.xb, b), *sXf = at(Lo.xf, b);
     RowGeo<FT> g;
     g.load(sG, P, j);
     for (int v0 = 0; v0 < Nv; v0 += AD_LEVELS) {
@@ -182,10 +197,17 @@ __global__ void __launch_bounds__(AD_THREADS, AdMinBlocks<FT>::value)
         thermo_vjp(P, rho, rhoe, K, Phi, tb, rb, reb, Kb);
         // K = (u . c + Kv) / 2: dK/du_h = c, dK/dKv = 1/2
         if (act) {
-          sB[q] += rb;
-          sB[16 * Nv + q] += u1b[i] + c1 * Kb;
-          sB[32 * Nv + q] += u2b[i] + c2 * Kb;
-          sB[48 * Nv + q] += reb;
+          if (ADD) {
+            sB[q] += sX[q] + rb;
+            sB[16 * Nv + q] += sX[16 * Nv + q] + (u1b[i] + c1 * Kb);
+            sB[32 * Nv + q] += sX[32 * Nv + q] + (u2b[i] + c2 * Kb);
+            sB[48 * Nv + q] += sX[48 * Nv + q] + reb;
+          } else {
+            sB[q] += rb;
+            sB[16 * Nv + q] += u1b[i] + c1 * Kb;
+            sB[32 * Nv + q] += u2b[i] + c2 * Kb;
+            sB[48 * Nv + q] += reb;
+          }
         }
         const FT Kvb = Kb / FT(2);
         lo[i] = v == 0 ? FT(0) : ub3b[i] / FT(2) + Kvb * fa * g3a;
@@ -205,7 +227,10 @@ __global__ void __launch_bounds__(AD_THREADS, AdMinBlocks<FT>::value)
         ld_row(sHi + (size_t)(k - 1) * NN + NQ * j, hi);
         ld_row(sLo + (size_t)k * NN + NQ * j, lo);
 #pragma unroll
-        for (int i = 0; i < 4; ++i) sBf[(NQ * j + i) * Nf + k] += hi[i] + lo[i];
+        for (int i = 0; i < 4; ++i) {
+          const int idx = (NQ * j + i) * Nf + k;
+          sBf[idx] += ADD ? sXf[idx] + (hi[i] + lo[i]) : hi[i] + lo[i];
+        }
       }
     }
     fence_proxy_async();
@@ -943,7 +968,12 @@ __global__ void __launch_bounds__(AD_THREADS, AdMinBlocks<FT>::value)
 
 template <class FT>
 size_t passA_vjp_smem(int Nv) {
-  return AvLayout<FT>(Nv, 1).total;
+  return AvLayout<FT, false>(Nv, 1).total;
+}
+// Whether pass A^T can also take a further cotangent slab (shared memory).
+template <class FT>
+bool passA_vjp_add_fits(int Nv) {
+  return AvLayout<FT, true>(Nv, 1).total <= (size_t)ad_dev().optin;
 }
 // Whether pass B^T stages the Laplacians and the tendency cotangent (they fit).
 template <class FT>
@@ -963,8 +993,10 @@ void configure_adjoint_se(int Nv) {
   cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
   // the dynamic limit is the opt-in maximum less the kernel's static shared memory
   cudaFuncAttributes fa{};
-  cudaFuncGetAttributes(&fa, k_passA_vjp<FT>);
-  cudaFuncSetAttribute(k_passA_vjp<FT>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes);
+  cudaFuncGetAttributes(&fa, k_passA_vjp<FT, false>);
+  cudaFuncSetAttribute(k_passA_vjp<FT, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes);
+  cudaFuncGetAttributes(&fa, k_passA_vjp<FT, true>);
+  cudaFuncSetAttribute(k_passA_vjp<FT, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes);
   auto raise = [&](auto kern) {
     cudaFuncGetAttributes(&fa, kern);
     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes);
@@ -977,11 +1009,17 @@ void configure_adjoint_se(int Nv) {
 
 template <class FT>
 void launch_passA_vjp(const DevParams<FT> &P, const FT *Yc, const FT *Yf, const FT *Lb, FT *Ybc, FT *Ybf, int grid,
-                      cudaStream_t s) {
+                      cudaStream_t s, const FT *Xbc, const FT *Xbf) {
   (void)grid;
-  const AdShape sh = ad_shape<AvLayout<FT>>(P.Nv, AdMinBlocks<FT>::value);
-  const int g = std::max(1, std::min(P.Nh, ad_dev().nsm * sh.ctas));
-  k_passA_vjp<FT><<<g, AD_THREADS, sh.smem, s>>>(P, sh.nbuf, Yc, Yf, Lb, Ybc, Ybf);
+  if (Xbc && Xbf) {
+    const AdShape sh = ad_shape<AvLayout<FT, true>>(P.Nv, AdMinBlocks<FT>::value);
+    const int g = std::max(1, std::min(P.Nh, ad_dev().nsm * sh.ctas));
+    k_passA_vjp<FT, true><<<g, AD_THREADS, sh.smem, s>>>(P, sh.nbuf, Yc, Yf, Lb, Ybc, Ybf, Xbc, Xbf);
+  } else {
+    const AdShape sh = ad_shape<AvLayout<FT, false>>(P.Nv, AdMinBlocks<FT>::value);
+    const int g = std::max(1, std::min(P.Nh, ad_dev().nsm * sh.ctas));
+    k_passA_vjp<FT, false><<<g, AD_THREADS, sh.smem, s>>>(P, sh.nbuf, Yc, Yf, Lb, Ybc, Ybf, nullptr, nullptr);
+  }
 }
 // grid: the number of parameter-partial slots (CTAs) the caller allocated.
 template <class FT>
@@ -1003,10 +1041,11 @@ void launch_passB_vjp(const DevParams<FT> &P, const FT *Yc, const FT *Yf, const 
 
 #define INST(FT)                                                                                             \
   template size_t passA_vjp_smem<FT>(int);                                                                   \
+  template bool passA_vjp_add_fits<FT>(int);                                                                 \
   template size_t passB_vjp_smem<FT>(int);                                                                   \
   template void configure_adjoint_se<FT>(int);                                                               \
   template void launch_passA_vjp<FT>(const DevParams<FT> &, const FT *, const FT *, const FT *, FT *, FT *, int, \
-                                     cudaStream_t);                                                          \
+                                     cudaStream_t, const FT *, const FT *);                                  \
   template void launch_passB_vjp<FT>(const DevParams<FT> &, const FT *, const FT *, const FT *, const FT *,      \
                                      const FT *, FT *, FT *, FT *, double *, int, bool, cudaStream_t);
 INST(float)

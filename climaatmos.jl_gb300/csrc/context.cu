@@ -601,15 +601,27 @@ void record_step(gb_ctx *ctx, FT *Yc, FT *Yf, double dt_, typename Impl<FT>::Rec
 // where Tb is the cotangent of the DSSed tendency (dss_out, as inside the step;
 // Tb is then DSS-transposed in place) or of the tendency as
 // gb_remaining_tendency returns it (not DSSed; Tb is only read).  accum adds
-// to Ub, else Ub is overwritten.
+// to Ub, else Ub is overwritten.  With Yc_add: Yc_add (+)= (dT/dU)^T Tb instead,
+// Ub being scratch (pass B^T writes it, pass A^T adds it and its own part).
 template <class FT>
 void tendency_vjp(gb_ctx *ctx, const FT *Uc, const FT *Uf, const FT *L, FT *Tb_c, FT *Tb_f, FT *Ubc, FT *Ubf,
-                  bool dss_out, bool accum, cudaStream_t s) {
+                  bool dss_out, bool accum, cudaStream_t s, FT *Yc_add = nullptr, FT *Yf_add = nullptr) {
   Impl<FT> *I = impl<FT>(ctx);
   auto &A = *I->adj;
   const DevParams<FT> &P = I->P;
   FT *Lb = (FT *)A.Lb.p;
   if (dss_out) launch_dss_transpose<FT>(P, Tb_c, Tb_f, s);
+  if (Yc_add && passA_vjp_add_fits<FT>(P.Nv)) {
+    launch_passB_vjp<FT>(P, Uc, Uf, L, Tb_c, Tb_f, Ubc, Ubf, Lb, (double *)A.dparB.p, A.grid, false, s);
+    launch_dss_transpose<FT>(P, Lb, nullptr, s);
+    launch_passA_vjp<FT>(P, Uc, Uf, Lb, Yc_add, Yf_add, A.grid, s, Ubc, Ubf);
+    return;
+  }
+  if (Yc_add) {
+    Ubc = Yc_add;
+    Ubf = Yf_add;
+    accum = true;
+  }
   launch_passB_vjp<FT>(P, Uc, Uf, L, Tb_c, Tb_f, Ubc, Ubf, Lb, (double *)A.dparB.p, A.grid, accum, s);
   launch_dss_transpose<FT>(P, Lb, nullptr, s);
   launch_passA_vjp<FT>(P, Uc, Uf, Lb, Ubc, Ubf, A.grid, s);
@@ -651,7 +663,8 @@ void reverse_step(gb_ctx *ctx, typename Impl<FT>::Record &rec, double dt_, FT *Y
     const FT *Uc = i == 0 ? Yc : (const FT *)rec.U[i].p, *Uf = Uc + I->NC;
     if (i == 0) {
       // stage 0 is u_n itself: its tendency cotangent adds straight into the caller's Yb
-      tendency_vjp<FT>(ctx, Uc, Uf, (const FT *)rec.L[i].p, Teb[i], Teb[i] + I->NC, Ybc, Ybf, true, true, s);
+      tendency_vjp<FT>(ctx, Uc, Uf, (const FT *)rec.L[i].p, Teb[i], Teb[i] + I->NC, Ubc, Ubf, true, false, s, Ybc,
+                       Ybf);
     } else {
       tendency_vjp<FT>(ctx, Uc, Uf, (const FT *)rec.L[i].p, Teb[i], Teb[i] + I->NC, Ubc, Ubf, true, false, s);
       const StageArgs<FT> SA = stage_args<FT>(I, i, dt, Yc, Yf, Te, Ti);

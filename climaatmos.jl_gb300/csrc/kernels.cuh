@@ -106,10 +106,11 @@ template <class FT> void launch_final(const DevParams<FT> &P, const StageArgs<FT
 template <class FT> void launch_final_transpose(const DevParams<FT> &P, const CotArgs<FT> &A, FT *Ybc, FT *Ybf, cudaStream_t s);
 template <class FT> void launch_axpy(size_t n, FT a, const FT *x, FT *y, cudaStream_t s);
 void launch_accum(const double *part, int n, int stride, int nout, double *acc, cudaStream_t s);
+template <class FT> bool passA_vjp_add_fits(int Nv);
 template <class FT> size_t passA_vjp_smem(int Nv);
 template <class FT> size_t passB_vjp_smem(int Nv);
 template <class FT> void configure_adjoint_se(int Nv);
-template <class FT> void launch_passA_vjp(const DevParams<FT> &P, const FT *Yc, const FT *Yf, const FT *Lb, FT *Ybc, FT *Ybf, int grid, cudaStream_t s);
+template <class FT> void launch_passA_vjp(const DevParams<FT> &P, const FT *Yc, const FT *Yf, const FT *Lb, FT *Ybc, FT *Ybf, int grid, cudaStream_t s, const FT *Xbc = nullptr, const FT *Xbf = nullptr);
 template <class FT> void launch_passB_vjp(const DevParams<FT> &P, const FT *Yc, const FT *Yf, const FT *L, const FT *Tbc, const FT *Tbf, FT *Ybc, FT *Ybf, FT *Lb, double *dpar, int grid, bool accum, cudaStream_t s);
 size_t col_vjp_scratch_words(int Nh, int Nv);
 // Uo, Tio (optional): the recorded stage output and implicit tendency (U^ = U - dtgamma T_imp

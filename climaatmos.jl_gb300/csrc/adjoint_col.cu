@@ -54,6 +54,11 @@ struct ColVjpArgs {
   // when set: the recorded stage output U and implicit tendency T_imp, from which
   // U^ = U - dtgamma T_imp (the stage leaves u_h unchanged) replaces the assembly
   const FT *Uo_c, *Uo_f, *Tio_c, *Tio_f;
+  // init: the tendency cotangents are written, each initialised from the cotangent of
+  // u_n as it is on entry (the final-combination transpose's dt b_j Ybar): Teb_j =
+  // e0[j] Yb + ce_j U^bar, Tib_j = i0[j] Yb + ci_j U^bar
+  int init;
+  FT e0[4], i0[4];
 };
 
 template <class FT>
@@ -532,22 +537,37 @@ __global__ void __launch_bounds__(128) k_col_stage_vjp(DevParams<FT> P, ColVjpAr
   for (int v = 0; v < Nv; ++v) {
     const FT hb[4] = {S(S_BR, v) - V.Tb_c[rb + v] * idtg, S(S_BU1, v) + V.Ub_c[cb + (size_t)sc + v],
                       S(S_BU2, v) + V.Ub_c[cb + (size_t)2 * sc + v], S(S_BRE, v) - V.Tb_c[rb + (size_t)sc + v] * idtg};
-    for (int c = 0; c < 4; ++c) V.Yb_c[cb + (size_t)c * sc + v] += hb[c];
+    FT y0[4];
+    for (int c = 0; c < 4; ++c) {
+      y0[c] = V.Yb_c[cb + (size_t)c * sc + v];
+      V.Yb_c[cb + (size_t)c * sc + v] = y0[c] + hb[c];
+    }
     for (int j = 0; j < A.nsrc; ++j) {
-      for (int c = 0; c < 4; ++c) V.Teb_c[j][cb + (size_t)c * sc + v] += A.ce[j] * hb[c];
+      // init: written from the cotangent of u_n on entry (see ColVjpArgs)
+      const FT ke = V.init ? V.e0[j] : FT(0), ki = V.init ? V.i0[j] : FT(0);
+      for (int c = 0; c < 4; ++c) {
+        FT &t = V.Teb_c[j][cb + (size_t)c * sc + v];
+        t = (V.init ? ke * y0[c] : t) + A.ce[j] * hb[c];
+      }
       if (j >= 1) {
-        V.Tib_c[j][rb + v] += A.ci[j] * hb[0];
-        V.Tib_c[j][rb + (size_t)sc + v] += A.ci[j] * hb[3];
+        FT &t0 = V.Tib_c[j][rb + v], &t3 = V.Tib_c[j][rb + (size_t)sc + v];
+        t0 = (V.init ? ki * y0[0] : t0) + A.ci[j] * hb[0];
+        t3 = (V.init ? ki * y0[3] : t3) + A.ci[j] * hb[3];
       }
     }
   }
   for (int f = 0; f < Nf; ++f) {
     const bool inner = f > 0 && f < Nv;
     const FT hb = S(S_BH4, f) + (inner ? S(S_BU3, f) : FT(0)) - V.Tb_f[fb + f] * idtg;
-    V.Yb_f[fb + f] += hb;
+    const FT y0 = V.Yb_f[fb + f];
+    V.Yb_f[fb + f] = y0 + hb;
     for (int j = 0; j < A.nsrc; ++j) {
-      V.Teb_f[j][fb + f] += A.ce[j] * hb;
-      if (j >= 1) V.Tib_f[j][fb + f] += A.ci[j] * hb;
+      FT &t = V.Teb_f[j][fb + f];
+      t = (V.init ? V.e0[j] * y0 : t) + A.ce[j] * hb;
+      if (j >= 1) {
+        FT &u = V.Tib_f[j][fb + f];
+        u = (V.init ? V.i0[j] * y0 : u) + A.ci[j] * hb;
+      }
     }
   }
   V.dalpha[col] += dal;  // accumulated over the launches of a reverse pass (zeroed by the host)
@@ -635,7 +655,7 @@ __global__ void __launch_bounds__(128, VjpMinBlocks<FT>::value) k_col_stage_vjp_
     }
     prefetch_l2(V.Tb_c + rb);
     prefetch_l2(V.Tb_c + rb + sc);
-    for (int j = 0; j < A.nsrc; ++j) {
+    for (int j = 0; !V.init && j < A.nsrc; ++j) {  // (init: the tendency cotangents are only written)
       if (V.Teb_c[j])
         for (int c = 0; c < 4; ++c) prefetch_l2(V.Teb_c[j] + cb + (size_t)c * sc);
       if (j >= 1 && V.Tib_c[j]) {
@@ -648,7 +668,7 @@ __global__ void __launch_bounds__(128, VjpMinBlocks<FT>::value) k_col_stage_vjp_
     prefetch_l2(V.Ub_f + fb);
     prefetch_l2(V.Tb_f + fb);
     prefetch_l2(V.Yb_f + fb);
-    for (int j = 0; j < A.nsrc; ++j) {
+    for (int j = 0; !V.init && j < A.nsrc; ++j) {
       if (V.Teb_f[j]) prefetch_l2(V.Teb_f[j] + fb);
       if (j >= 1 && V.Tib_f[j]) prefetch_l2(V.Tib_f[j] + fb);
     }
@@ -1133,24 +1153,43 @@ __global__ void __launch_bounds__(128, VjpMinBlocks<FT>::value) k_col_stage_vjp_
     if (colv && v < Nv) {
       const FT hb[4] = {bR0[k] - V.Tb_c[rb + k] * idtg, bU1[k] + V.Ub_c[cb + (size_t)sc + k],
                         bU2[k] + V.Ub_c[cb + (size_t)2 * sc + k], bRE0[k] - V.Tb_c[rb + (size_t)sc + k] * idtg};
+      FT y0[4];
 #pragma unroll
-      for (int c = 0; c < 4; ++c) V.Yb_c[cb + (size_t)c * sc + k] += hb[c];
+      for (int c = 0; c < 4; ++c) {
+        y0[c] = V.Yb_c[cb + (size_t)c * sc + k];
+        V.Yb_c[cb + (size_t)c * sc + k] = y0[c] + hb[c];
+      }
       for (int j = 0; j < A.nsrc; ++j) {
+        if (V.init) {
 #pragma unroll
-        for (int c = 0; c < 4; ++c) V.Teb_c[j][cb + (size_t)c * sc + k] += A.ce[j] * hb[c];
-        if (j >= 1) {
-          V.Tib_c[j][rb + k] += A.ci[j] * hb[0];
-          V.Tib_c[j][rb + (size_t)sc + k] += A.ci[j] * hb[3];
+          for (int c = 0; c < 4; ++c) V.Teb_c[j][cb + (size_t)c * sc + k] = V.e0[j] * y0[c] + A.ce[j] * hb[c];
+          if (j >= 1) {
+            V.Tib_c[j][rb + k] = V.i0[j] * y0[0] + A.ci[j] * hb[0];
+            V.Tib_c[j][rb + (size_t)sc + k] = V.i0[j] * y0[3] + A.ci[j] * hb[3];
+          }
+        } else {
+#pragma unroll
+          for (int c = 0; c < 4; ++c) V.Teb_c[j][cb + (size_t)c * sc + k] += A.ce[j] * hb[c];
+          if (j >= 1) {
+            V.Tib_c[j][rb + k] += A.ci[j] * hb[0];
+            V.Tib_c[j][rb + (size_t)sc + k] += A.ci[j] * hb[3];
+          }
         }
       }
     }
     if (colv && v < Nf) {
       const bool inner = v > 0 && v < Nv;
       const FT hb = bH4[k] + (inner ? bU3[k] : FT(0)) - V.Tb_f[fb + k] * idtg;
-      V.Yb_f[fb + k] += hb;
+      const FT y0 = V.Yb_f[fb + k];
+      V.Yb_f[fb + k] = y0 + hb;
       for (int j = 0; j < A.nsrc; ++j) {
-        V.Teb_f[j][fb + k] += A.ce[j] * hb;
-        if (j >= 1) V.Tib_f[j][fb + k] += A.ci[j] * hb;
+        if (V.init) {
+          V.Teb_f[j][fb + k] = V.e0[j] * y0 + A.ce[j] * hb;
+          if (j >= 1) V.Tib_f[j][fb + k] = V.i0[j] * y0 + A.ci[j] * hb;
+        } else {
+          V.Teb_f[j][fb + k] += A.ce[j] * hb;
+          if (j >= 1) V.Tib_f[j][fb + k] += A.ci[j] * hb;
+        }
       }
     }
   }
@@ -1168,9 +1207,16 @@ template <class FT>
 void launch_column_stage_vjp(const DevParams<FT> &P, const StageArgs<FT> &A, const FT *Ub_c, const FT *Ub_f,
                              const FT *Tb_c, const FT *Tb_f, FT *Yb_c, FT *Yb_f, FT *const Teb[4], FT *const Tib[4],
                              size_t NC, size_t NR, FT *scr, double *dalpha, cudaStream_t s, const FT *Uo,
-                             const FT *Tio) {
+                             const FT *Tio, const FT *e0, const FT *i0) {
   ColVjpArgs<FT> V{};
   V.A = A;
+  if (e0 && i0) {
+    V.init = 1;
+    for (int j = 0; j < 4; ++j) {
+      V.e0[j] = e0[j];
+      V.i0[j] = i0[j];
+    }
+  }
   if (Uo && Tio) {
     V.Uo_c = Uo; V.Uo_f = Uo + NC; V.Tio_c = Tio; V.Tio_f = Tio + NR;
   }
@@ -1203,10 +1249,12 @@ void launch_column_stage_vjp(const DevParams<FT> &P, const StageArgs<FT> &A, con
 template void launch_column_stage_vjp<float>(const DevParams<float> &, const StageArgs<float> &, const float *,
                                              const float *, const float *, const float *, float *, float *,
                                              float *const[4], float *const[4], size_t, size_t, float *, double *,
-                                             cudaStream_t, const float *, const float *);
+                                             cudaStream_t, const float *, const float *, const float *,
+                                             const float *);
 template void launch_column_stage_vjp<double>(const DevParams<double> &, const StageArgs<double> &, const double *,
                                               const double *, const double *, const double *, double *, double *,
                                               double *const[4], double *const[4], size_t, size_t, double *,
-                                              double *, cudaStream_t, const double *, const double *);
+                                              double *, cudaStream_t, const double *, const double *,
+                                              const double *, const double *);
 
 }  // namespace gb

@@ -644,17 +644,22 @@ void reverse_step(gb_ctx *ctx, typename Impl<FT>::Record &rec, double dt_, FT *Y
       Ti[j] = (FT *)rec.Ti[j].p;
     }
   }
-  // final combination u_{n+1} = u_n + dt sum_j b_j (T_exp_j + T_imp_j), filtered; its
-  // transpose writes every tendency cotangent (zero where b_j = 0)
+  // final combination u_{n+1} = u_n + dt sum_j b_j (T_exp_j + T_imp_j), filtered.  Its
+  // transpose gives every tendency j the cotangent dt b_j Ybar: written here for the last
+  // stage only; the last stage's column pullback writes those of the earlier stages
+  // (dt b_j Ybar plus its own part, Ybar read once).
   CotArgs<FT> F{};
   F.nsrc = 4;
+  FT e0[4], i0[4];
   for (int j = 0; j < 4; ++j) {
-    F.te_c[j] = Teb[j];
-    F.te_f[j] = Teb[j] + I->NC;
+    F.te_c[j] = j == 3 ? Teb[j] : nullptr;
+    F.te_f[j] = j == 3 ? Teb[j] + I->NC : nullptr;
     F.ce[j] = dt * (FT)I->be[j];
-    F.ti_c[j] = Tib[j];
-    F.ti_f[j] = Tib[j] ? Tib[j] + I->NR : nullptr;
+    F.ti_c[j] = j == 3 ? Tib[j] : nullptr;
+    F.ti_f[j] = j == 3 ? Tib[j] + I->NR : nullptr;
     F.ci[j] = dt * (FT)I->bi[j];
+    e0[j] = F.ce[j];
+    i0[j] = F.ci[j];
   }
   launch_final_transpose<FT>(P, F, Ybc, Ybf, s);
   const FT *Yc = (const FT *)rec.Y.p, *Yf = Yc + I->NC;
@@ -670,7 +675,7 @@ void reverse_step(gb_ctx *ctx, typename Impl<FT>::Record &rec, double dt_, FT *Y
       const StageArgs<FT> SA = stage_args<FT>(I, i, dt, Yc, Yf, Te, Ti);
       launch_column_stage_vjp<FT>(P, SA, Ubc, Ubf, Tib[i], Tib[i] + I->NR, Ybc, Ybf, Teb, Tib, I->NC, I->NR,
                                   (FT *)A.scr.p, (double *)A.dal.p, s, (const FT *)rec.U[i].p,
-                                  (const FT *)rec.Ti[i].p);
+                                  (const FT *)rec.Ti[i].p, i == 3 ? e0 : nullptr, i == 3 ? i0 : nullptr);
     }
   }
 }

@@ -114,8 +114,9 @@ template <class FT> void launch_passA_vjp(const DevParams<FT> &P, const FT *Yc, 
 template <class FT> void launch_passB_vjp(const DevParams<FT> &P, const FT *Yc, const FT *Yf, const FT *L, const FT *Tbc, const FT *Tbf, FT *Ybc, FT *Ybf, FT *Lb, double *dpar, int grid, bool accum, cudaStream_t s);
 size_t col_vjp_scratch_words(int Nh, int Nv);
 // Uo, Tio (optional): the recorded stage output and implicit tendency (U^ = U - dtgamma T_imp
-// then replaces the stage assembly in the forward recompute).
-template <class FT> void launch_column_stage_vjp(const DevParams<FT> &P, const StageArgs<FT> &A, const FT *Ub_c, const FT *Ub_f, const FT *Tb_c, const FT *Tb_f, FT *Yb_c, FT *Yb_f, FT *const Teb[4], FT *const Tib[4], size_t NC, size_t NR, FT *scr, double *dalpha, cudaStream_t s, const FT *Uo = nullptr, const FT *Tio = nullptr);
+// then replaces the stage assembly in the forward recompute).  e0, i0 (optional): the
+// tendency cotangents are written, initialised as e0[j] Yb / i0[j] Yb from Yb on entry.
+template <class FT> void launch_column_stage_vjp(const DevParams<FT> &P, const StageArgs<FT> &A, const FT *Ub_c, const FT *Ub_f, const FT *Tb_c, const FT *Tb_f, FT *Yb_c, FT *Yb_f, FT *const Teb[4], FT *const Tib[4], size_t NC, size_t NR, FT *scr, double *dalpha, cudaStream_t s, const FT *Uo = nullptr, const FT *Tio = nullptr, const FT *e0 = nullptr, const FT *i0 = nullptr);
 template <class FT> void launch_bc_filter(const DevParams<FT> &P, FT *Yf, cudaStream_t s);
 template <class FT> void launch_global_sums(const DevParams<FT> &P, const FT *Yc, double *partials, int nblocks, double *out, cudaStream_t s);
 void launch_reduce_rnorm(const double *rnorm, int ncols, double *out, cudaStream_t s);

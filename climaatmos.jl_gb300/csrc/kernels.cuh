@@ -104,7 +104,6 @@ template <class FT> void launch_column(const DevParams<FT> &P, int mode, const C
 template <class FT> void launch_final(const DevParams<FT> &P, const StageArgs<FT> &A, FT *Yc, FT *Yf, cudaStream_t s);
 // ---- reverse (adjoint) kernels
 template <class FT> void launch_final_transpose(const DevParams<FT> &P, const CotArgs<FT> &A, FT *Ybc, FT *Ybf, cudaStream_t s);
-template <class FT> void launch_axpy(size_t n, FT a, const FT *x, FT *y, cudaStream_t s);
 void launch_accum(const double *part, int n, int stride, int nout, double *acc, cudaStream_t s);
 template <class FT> bool passA_vjp_add_fits(int Nv);
 template <class FT> size_t passA_vjp_smem(int Nv);

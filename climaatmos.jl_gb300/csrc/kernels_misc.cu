@@ -218,11 +218,6 @@ __global__ void k_final_t(DevParams<FT> P, CotArgs<FT> A, FT *__restrict__ Ybc, 
   }
 }
 
-template <class FT>
-__global__ void k_axpy(size_t n, FT a, const FT *__restrict__ x, FT *__restrict__ y) {
-  for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x)
-    y[q] += a * x[q];
-}
 
 // acc[o] += sum_i part[i * stride + o] for o < nout, in a fixed order (one block).
 __global__ void k_accum(const double *__restrict__ part, int n, int stride, int nout, double *__restrict__ acc) {
@@ -336,10 +331,6 @@ template <class FT>
 void launch_final_transpose(const DevParams<FT> &P, const CotArgs<FT> &A, FT *Ybc, FT *Ybf, cudaStream_t s) {
   k_final_t<FT><<<152 * 8, 256, 0, s>>>(P, A, Ybc, Ybf);
 }
-template <class FT>
-void launch_axpy(size_t n, FT a, const FT *x, FT *y, cudaStream_t s) {
-  k_axpy<FT><<<152 * 8, 256, 0, s>>>(n, a, x, y);
-}
 void launch_accum(const double *part, int n, int stride, int nout, double *acc, cudaStream_t s) {
   k_accum<<<1, 256, 0, s>>>(part, n, stride, nout, acc);
 }
@@ -362,7 +353,6 @@ void launch_reduce_rnorm(const double *rnorm, int ncols, double *out, cudaStream
   template void launch_dss_transpose<FT>(const DevParams<FT> &, FT *, FT *, cudaStream_t);                \
   template void launch_final<FT>(const DevParams<FT> &, const StageArgs<FT> &, FT *, FT *, cudaStream_t); \
   template void launch_final_transpose<FT>(const DevParams<FT> &, const CotArgs<FT> &, FT *, FT *, cudaStream_t); \
-  template void launch_axpy<FT>(size_t, FT, const FT *, FT *, cudaStream_t);                               \
   template void launch_bc_filter<FT>(const DevParams<FT> &, FT *, cudaStream_t);                          \
   template void launch_global_sums<FT>(const DevParams<FT> &, const FT *, double *, int, double *, cudaStream_t);
 INST(float)

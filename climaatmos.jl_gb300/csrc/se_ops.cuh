@@ -308,22 +308,6 @@ __device__ __forceinline__ void wdiv(const DevParams<FT> &P, const Row<FT> &R, c
   for (int i = 0; i < 4; ++i) o[i] = -(ta[i] + tb[i]) * s.iWJ[i];
 }
 
-// u_bar_3 = I^c(u_3) and the face part of K, I^c(u_3 u^3), with the
-// impenetrable filter (u_3 = 0 on the boundary faces); level-fastest mapping.
-template <class FT>
-__device__ __forceinline__ void centre_from_faces(const DevParams<FT> &P, const FT *sF, FT *sU3, FT *sKv) {
-  const int Nv = P.Nv, Nf = P.Nf;
-  for (int idx = threadIdx.x; idx < NN * Nv; idx += blockDim.x) {
-    const int n = idx / Nv, v = idx - n * Nv;
-    const FT a = v == 0 ? FT(0) : sF[n * Nf + v];
-    const FT b = v + 1 == Nv ? FT(0) : sF[n * Nf + v + 1];
-    const FT ua = a * P.levf[LF_G33 * Nf + v], ub = b * P.levf[LF_G33 * Nf + v + 1];
-    if (sU3) sU3[idx] = (a + b) / FT(2);
-    sKv[idx] = (a * ua + b * ub) / FT(2);
-  }
-}
-
-
 // ---------------------------------------------------------------- reverse (adjoint) forms
 // Transpose of vec_lap: given the cotangents (ob1, ob2, ob3) of (o1, o2, o3),
 // returns the cotangents (cb1, cb2, cb3) of (c1, c2, c3).  The forward sequence

@@ -299,3 +299,31 @@ def test_remaining_tendency_vjp_at_zero_hyperdiffusion(setup):
         vals.append(_dot(Tb, Tq))
     fd = (vals[0] - vals[1]) / (2 * HP * nu0)
     assert rel(dpar[0], fd) < 1e-6, (dpar[0], fd)
+
+
+@pytest.mark.gpu
+def test_step_vjp_fp32_agrees_with_fp64(setup):
+    """The FP32 pullback (the production precision) against the FP64 one: <Ybar, d> for the same
+    state, cotangent and direction agree to FP32 accuracy of the tangent map."""
+    sim = _sim()
+    cfg64, Yc, Yf = setup
+    dc, df = _scaled(Yc.shape, Yf.shape, Yc, Yf, 31)
+    rng = np.random.default_rng(30)
+    bc = rng.standard_normal(Yc.shape)
+    bf = rng.standard_normal(Yf.shape)
+    out = {}
+    for ft in (np.float64, np.float32):
+        cfg = cfg64.with_(ft=ft)
+        p = sim.AtmosCache(cfg)
+        Y = sim.FieldVector.from_numpy(Yc.astype(ft), Yf.astype(ft))
+        Z = Y.copy()
+        p.call("gb_step", Z.gb(), 0.0, float(cfg.dt), 1, 0)
+        Zc, Zf = Z.numpy()
+        scale_c = np.maximum(np.abs(Zc.astype(np.float64)).max(axis=(0, 2, 3), keepdims=True), 1e-30)
+        Yb = sim.FieldVector.from_numpy((bc / scale_c).astype(ft), (bf / max(np.abs(Zf).max(), 1e-30)).astype(ft))
+        dpar = sim.step_vjp(Yb, Y, p, 0.0, cfg.dt)
+        Ybc, Ybf = Yb.numpy()
+        out[ft] = (float((Ybc.astype(np.float64) * dc).sum() + (Ybf.astype(np.float64) * df).sum()), dpar)
+    (g64, p64), (g32, p32) = out[np.float64], out[np.float32]
+    assert rel(g32, g64) < 1e-3, (g32, g64)
+    assert rel(p32[0], p64[0]) < 1e-3 and rel(p32[1], p64[1]) < 1e-3, (p32, p64)

@@ -54,6 +54,7 @@ def parse():
     ap.add_argument("--no-differentiation", action="store_true")
     ap.add_argument("--no-h60", action="store_true")
     ap.add_argument("--held-suarez-steps", type=int, default=20)
+    ap.add_argument("--held-suarez-long", type=int, default=1000)
     ap.add_argument("--no-held-suarez", action="store_true")
     # bracket one forward step ("step") or one reverse pass ("reverse") by
     # cudaProfilerStart/Stop, for `ncu --profile-from-start off`; no effect otherwise
@@ -545,6 +546,18 @@ def measure_held_suarez(args, fwd_ms):
     out = {"steps": n + 3, "ms_per_step": ms, "value": sypd(cfg.dt, ms / 1e3), "unit": UNIT,
            "over_dry_step": ms / fwd_ms, "mass_rel_change": abs(m1 - m0) / abs(m0), "finite": finite,
            "parameters": dict(cfg.hs)}
+    # a longer forced run: the model stays finite and conserves mass while it spins up
+    if args.held_suarez_long > 0:
+        e1 = s.p.global_sums(s.Y)[1]
+        k = args.held_suarez_long
+        s.step(k)
+        torch.cuda.synchronize()
+        m2, e2 = s.p.global_sums(s.Y)
+        out["long_run"] = {
+            "steps": k, "simulated_days": k * cfg.dt / 86400.0,
+            "finite": bool(torch.isfinite(s.Y.c).all() and torch.isfinite(s.Y.f).all()),
+            "mass_rel_change": abs(m2 - m0) / abs(m0), "energy_rel_change": abs(e2 - e1) / abs(e1),
+            "max_abs_u_covariant": float(s.Y.c[:, 1:3].abs().max().item())}
     del s
     torch.cuda.empty_cache()
     return out

@@ -491,7 +491,7 @@ def measure_adjoint(args, s, fwd_ms):
     Y0 = s.Y.copy()
     target = Y0.c[:, 3] * 1.001
     lg = _rhoe_loss(target)
-    sim.gradient(s.p, Y0, 1, lg, checkpoint_every=1)          # warm-up, allocates the reverse buffers
+    sim.gradient(s.p, Y0, n, lg, checkpoint_every=5)          # warm-up: allocates the reverse buffers, records, checkpoints
     Y = Y0.copy()
     f_ms, _ = _timed(lambda: s.p.call("gb_adjoint_forward", Y.gb(), 0.0, float(s.dt), n, 5))
     J, Ybar = lg(Y)

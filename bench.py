@@ -584,6 +584,7 @@ def measure_differentiation(args):
         p.call("gb_step", T.gb(), 0.0, float(cfg.dt), nsteps, 1)
         lg = _rhoe_loss(T.c[:, 3].clone())
         Y0 = sim.FieldVector.from_numpy(Yc.astype(ft), Yf.astype(ft))
+        sim.gradient(p, Y0, nsteps, lg, checkpoint_every=4)  # warm-up: allocates the reverse buffers
         ms, (J, G, dnu, drate, peak) = _timed(lambda: sim.gradient(p, Y0, nsteps, lg, checkpoint_every=4))
         key = "fp32" if ft == np.float32 else "fp64"
         out[key] = {"gradient_ms": ms, "J": J, "dJ_dnu": dnu, "dJ_drate": drate, "library_bytes": peak}
@@ -668,7 +669,9 @@ def measure_precision_h60(args):
     peak = ctypes.c_size_t(0)
     rev_ms, _ = _timed(lambda: s32.p.call("gb_adjoint_reverse", Ybar.gb(), d, ctypes.byref(peak)))
     free1, _ = torch.cuda.mem_get_info()
-    out["adjoint_20_steps"] = {"checkpoint_every": 5, "forward_ms": fwd_ms, "reverse_ms": rev_ms,
+    out["adjoint_20_steps"] = {"checkpoint_every": 5, "forward_ms": fwd_ms,
+                               "forward_note": "first call: includes allocating the stage records and checkpoints",
+                               "reverse_ms": rev_ms,
                                "reverse_over_forward_steps": rev_ms / (20 * ms / 20),
                                "library_bytes": int(peak.value),
                                "device_bytes_in_use_after_reverse": int(total - free1),

@@ -33,7 +33,7 @@ METRIC = "SYPD"
 UNIT = "simulated years per day"
 
 
-def parse():
+def parse(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
@@ -59,7 +59,7 @@ def parse():
     # bracket one forward step ("step") or one reverse pass ("reverse") by
     # cudaProfilerStart/Stop, for `ncu --profile-from-start off`; no effect otherwise
     ap.add_argument("--profile-region", default="none", choices=["none", "step", "reverse"])
-    return ap.parse_args()
+    return ap.parse_args(argv)
 
 
 def workload():
@@ -224,6 +224,7 @@ def run_gb300(args):
     import ctypes
     import torch
     import torch.distributed as dist
+    from gbdycore import replicas as rep
     from gbdycore import simulation as sim
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -238,8 +239,7 @@ def run_gb300(args):
     for _ in range(args.warmup):
         s.step(1)
     torch.cuda.synchronize()
-    if world > 1:
-        dist.barrier()
+    rep.barrier()
     clocks = ClockSampler(local)
     clocks.start()
     time.sleep(0.3)
@@ -251,11 +251,8 @@ def run_gb300(args):
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1) / args.steps
     clk = clocks.stop()
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-        dist.barrier()
+    ms = rep.max_over_ranks(ms, device="cuda")
+    rep.barrier()
     finite = bool(torch.isfinite(s.Y.c).all() and torch.isfinite(s.Y.f).all())
     if args.profile_region == "step":
         torch.cuda.profiler.start()
@@ -263,7 +260,7 @@ def run_gb300(args):
         torch.cuda.synchronize()
         torch.cuda.profiler.stop()
     v1 = sypd(cfg.dt, ms / 1e3)
-    value = v1 * world        # independent replicas, one per GPU
+    value = rep.job_value(v1)  # independent replicas, one per GPU
 
     # per-kernel timing (CUDA events on the context stream, inside the library)
     peak, peak_kind = measured_peak()

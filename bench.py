@@ -524,6 +524,18 @@ def measure_adjoint(args, s, fwd_ms):
             "dJ_dnu": d[0], "dJ_drate": d[1], "library_bytes": int(peak.value), "finite": finite}
 
 
+def max_horizontal_wind(s):
+    """max |u_h| (m/s) from the covariant components: |u|^2 = g^ij u_i u_j / r^2 (deep atmosphere)."""
+    import torch
+    g = s.geometry
+    gup = torch.as_tensor(g.gup, dtype=torch.float64, device=s.Y.c.device)        # (Nh, 16, 3)
+    r2 = torch.as_tensor(((g.R + g.zc) / g.R) ** 2, dtype=torch.float64, device=s.Y.c.device)
+    u1 = s.Y.c[:, 1].double()                                                        # (Nh, 16, Nv)
+    u2 = s.Y.c[:, 2].double()
+    q = (gup[..., 0:1] * u1 * u1 + 2 * gup[..., 1:2] * u1 * u2 + gup[..., 2:3] * u2 * u2) / r2
+    return float(q.clamp_min(0).sqrt().max().item())
+
+
 def measure_held_suarez(args, fwd_ms):
     """The production step with the Held-Suarez forcing in the explicit tendency
     (rad: held_suarez): SYPD, the cost over the plain dry step, and the state
@@ -554,7 +566,7 @@ def measure_held_suarez(args, fwd_ms):
             "steps": k, "simulated_days": k * cfg.dt / 86400.0,
             "finite": bool(torch.isfinite(s.Y.c).all() and torch.isfinite(s.Y.f).all()),
             "mass_rel_change": abs(m2 - m0) / abs(m0), "energy_rel_change": abs(e2 - e1) / abs(e1),
-            "max_abs_u_covariant": float(s.Y.c[:, 1:3].abs().max().item())}
+            "max_wind_m_s": max_horizontal_wind(s)}
     del s
     torch.cuda.empty_cache()
     return out

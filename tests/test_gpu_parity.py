@@ -41,8 +41,10 @@ FT_CASES = [(np.float64, 1e-11), (np.float32, 1e-4)]
 
 
 @pytest.mark.parametrize("ft,tol", FT_CASES)
-def test_remaining_tendency(ft, tol):
-    cfg = small_config(ft=ft)
+@pytest.mark.parametrize("z_elem", [8, 70])
+def test_remaining_tendency(ft, tol, z_elem):
+    # z_elem = 70: two level sweeps per slab; in FP32 pass B single-buffered (in-place output)
+    cfg = small_config(ft=ft, z_elem=z_elem)
     Yc, Yf = perturbed_state(cfg, dtype=ft)
     ref = make_oracle(cfg, ft).remaining_tendency(Yc.copy(), Yf.copy())
     p = _cache(cfg)

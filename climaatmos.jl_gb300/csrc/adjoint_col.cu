@@ -629,8 +629,8 @@ struct VjpMinBlocks {
   static constexpr int value = sizeof(FT) == 4 ? 4 : 1;
 };
 
-template <class FT, int G, int CM>
-__global__ void __launch_bounds__(128, VjpMinBlocks<FT>::value) k_col_stage_vjp_g(DevParams<FT> P, ColVjpArgs<FT> V) {
+template <class FT, int G, int CM, int MINB = VjpMinBlocks<FT>::value>
+__global__ void __launch_bounds__(128, MINB) k_col_stage_vjp_g(DevParams<FT> P, ColVjpArgs<FT> V) {
   const int lane = threadIdx.x & 31, gl = lane % G;
   const int col0 = (blockIdx.x * 4 + (threadIdx.x >> 5)) * (32 / G) + lane / G;
   const int ncols = P.Nh * NN;
@@ -1242,7 +1242,9 @@ void launch_column_stage_vjp(const DevParams<FT> &P, const StageArgs<FT> &A, con
   auto grid = [&](int G) { return (ncols + 4 * (32 / G) - 1) / (4 * (32 / G)); };
   if (P.Nf <= 16) lp::k_col_stage_vjp_g<FT, 8, 2><<<grid(8), 128, 0, s>>>(P, V);
   else if (P.Nf <= 32) lp::k_col_stage_vjp_g<FT, 16, 2><<<grid(16), 128, 0, s>>>(P, V);
-  else if (P.Nf <= 64) lp::k_col_stage_vjp_g<FT, 32, 2><<<grid(32), 128, 0, s>>>(P, V);
+  // FP32, two levels per lane: six resident CTAs per SM (an 85-register cap; measured at
+  // z_elem = 63: 0.531 ms at 4 CTAs, 0.518 at 5, 0.506 at 6, 0.516 at 7, 0.571 at 8)
+  else if (P.Nf <= 64) lp::k_col_stage_vjp_g<FT, 32, 2, sizeof(FT) == 4 ? 6 : 1><<<grid(32), 128, 0, s>>>(P, V);
   else lp::k_col_stage_vjp_g<FT, 32, 4><<<grid(32), 128, 0, s>>>(P, V);
 }
 

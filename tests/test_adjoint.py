@@ -302,11 +302,14 @@ def test_remaining_tendency_vjp_at_zero_hyperdiffusion(setup):
 
 
 @pytest.mark.gpu
-def test_step_vjp_fp32_agrees_with_fp64(setup):
+@pytest.mark.parametrize("z_elem", [8, 45])
+def test_step_vjp_fp32_agrees_with_fp64(z_elem):
     """The FP32 pullback (the production precision) against the FP64 one: <Ybar, d> for the same
-    state, cotangent and direction agree to FP32 accuracy of the tangent map."""
+    state, cotangent and direction agree to FP32 accuracy of the tangent map (z_elem = 45: the
+    32-lane column pullback that FP32 runs at six CTAs per SM)."""
     sim = _sim()
-    cfg64, Yc, Yf = setup
+    cfg64 = adj_config(z_elem=z_elem)
+    Yc, Yf = perturbed_state(cfg64, w_amp=0.05, dtype=np.float64)
     dc, df = _scaled(Yc.shape, Yf.shape, Yc, Yf, 31)
     rng = np.random.default_rng(30)
     bc = rng.standard_normal(Yc.shape)

@@ -24,6 +24,7 @@ import numpy as np
 
 from . import _native as N
 from . import config as C
+from . import restart as R
 from . import setups as S
 
 
@@ -253,21 +254,29 @@ def simulated_years_per_day(dt, seconds_per_step):
 class AtmosSimulation:
     """State + cache + time of one dry dynamical-core run on the GPU."""
 
-    def __init__(self, config, workload="plain", state=None, device="cuda"):
+    def __init__(self, config, workload="plain", state=None, device="cuda", restart_file=None):
         self.config = config
         self.geometry = Geometry(config)
-        if state is None:
+        self.t = 0.0
+        if restart_file is not None:
+            # handle_restart (src/simulation/restart.jl:58-84): the file's time takes precedence
+            Yc, Yf, self.t = R.get_state_restart(restart_file, config)
+        elif state is None:
             Yc, Yf = S.workload_state(self.geometry, config, workload)
         else:
             Yc, Yf = state
         self.Y = FieldVector.from_numpy(np.asarray(Yc, dtype=config.ft), np.asarray(Yf, dtype=config.ft), device)
         self.p = AtmosCache(config)
-        self.t = 0.0
         self.dt = config.dt
 
     def step(self, nsteps=1, use_graph=True):
         self.p.call("gb_step", self.Y.gb(), float(self.t), float(self.dt), int(nsteps), 1 if use_graph else 0)
         self.t += nsteps * self.dt
+
+    def save_state(self, output_dir):
+        """Checkpoint (save_state_to_disk_func, src/callbacks/callbacks.jl:297-321); returns the path."""
+        Yc, Yf = self.Y.numpy()
+        return R.save_state_to_disk(Yc, Yf, self.t, self.config, output_dir)
 
 
 def solve_atmos(sim, nsteps, use_graph=True):

@@ -1,0 +1,57 @@
+"""Checkpoint / restart of the prognostic state (the reference's save_state_to_disk_func,
+src/callbacks/callbacks.jl:297-321, and get_state_restart, src/simulation/restart.jl:22-42):
+file naming from the simulation time, the state and the time round-trip exactly, a different
+model configuration warns, a different grid is refused; on the GPU a run restarted from a
+checkpoint continues bitwise like the uninterrupted run."""
+import os
+import warnings
+
+import numpy as np
+import pytest
+
+from gbdycore import config as C
+from gbdycore import restart as R
+from helpers import perturbed_state, small_config
+
+
+def test_file_name_from_time():
+    assert R.restart_file_name(0.0) == "day0.0.npz"
+    assert R.restart_file_name(86400.0 * 2 + 3661.5) == "day2.3661.npz"
+
+
+def test_round_trip_and_checks(tmp_path):
+    cfg = small_config(np.float32)
+    Yc, Yf = perturbed_state(cfg, dtype=np.float32)
+    path = R.save_state_to_disk(Yc, Yf, 7200.0, cfg, str(tmp_path))
+    assert os.path.basename(path) == "day0.7200.npz"
+    with warnings.catch_warnings():
+        warnings.simplefilter("error")
+        c, f, t = R.get_state_restart(path, cfg)
+    assert t == 7200.0 and np.array_equal(c, Yc) and np.array_equal(f, Yf) and c.dtype == np.float32
+    # another model (sponge on): loads with a warning
+    with pytest.warns(UserWarning, match="different AtmosModel"):
+        R.get_state_restart(path, cfg.with_(alpha_uh=1e-3, sponge_zd=15000.0))
+    # the time step is not part of the model
+    assert R.atmos_model_hash(cfg) == R.atmos_model_hash(cfg.with_(dt=10.0))
+    # another grid or precision: refused
+    with pytest.raises(ValueError):
+        R.get_state_restart(path, cfg.with_(z_elem=cfg.z_elem + 1))
+    with pytest.raises(ValueError):
+        R.get_state_restart(path, cfg.with_(ft=np.float64))
+
+
+@pytest.mark.gpu
+def test_restarted_run_continues_bitwise(tmp_path):
+    from gbdycore import simulation as sim
+    cfg = small_config(np.float32)
+    Yc, Yf = perturbed_state(cfg, dtype=np.float32)
+    a = sim.AtmosSimulation(cfg, state=(Yc, Yf))
+    a.step(2)
+    path = a.save_state(str(tmp_path))
+    a.step(3)
+    b = sim.AtmosSimulation(cfg, restart_file=path)
+    assert b.t == 2 * cfg.dt
+    b.step(3)
+    ac, af = a.Y.numpy()
+    bc, bf = b.Y.numpy()
+    assert np.array_equal(ac, bc) and np.array_equal(af, bf)

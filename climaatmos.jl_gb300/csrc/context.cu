@@ -42,6 +42,7 @@ struct Impl : ImplBase {
   bool jac_valid = false;
   // ARS343 tableau (explicit a~, implicit a, weights b~ = b)
   double ae[4][4], ai[4][4], be[4], bi[4];
+  bool stiffly_accurate = false;  // b = the last row of the implicit tableau
   // reverse mode (allocated on first use)
   struct Record {  // forward data of one step kept for its reverse pass
     DevBuf Y, U[4], L[4], Te[4], Ti[4];
@@ -212,6 +213,8 @@ int create_impl(gb_ctx *ctx) {
   P.ecov = (const FT *)I->ecov.p; P.econ = (const FT *)I->econ.p;
   P.status = (int *)I->status.p;
   ars343(I->ae, I->ai, I->be, I->bi);
+  I->stiffly_accurate = true;
+  for (int j = 0; j < 4; ++j) I->stiffly_accurate = I->stiffly_accurate && I->bi[j] == I->ai[3][j];
   int dev = 0, optin = 0;
   CK(cudaGetDevice(&dev));
   CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
@@ -258,6 +261,25 @@ int column_hook_t(gb_ctx *ctx, int mode, gb_fieldvec O, gb_fieldvec Y, double dt
   return check_launch(ctx);
 }
 
+// The final combination of a stiffly accurate step written from the last stage
+// state U_4 = u_n + dt sum_j (a~_4j T_exp_j + b_j T_imp_j):
+// u_{n+1} = U_4 + dt sum_j (b~_j - a~_4j) T_exp_j, with u_3 = 0 on the bottom
+// and top faces, folded into the last pass B.  The last T_exp enters before its
+// DSS, and the sum is DSSed as a whole (the reference's final dss!): for a
+// continuous u_n that equals U_4 + ... + DSS(T_exp_4).
+template <class FT>
+FinArgs<FT> fin_args(const Impl<FT> *I, FT dt, FT *const (&tc)[4], FT *const (&tf)[4]) {
+  FinArgs<FT> F{};
+  for (int j = 0; j < 3; ++j) {
+    const double c = I->be[j] - I->ae[3][j];
+    F.c[j] = dt * (FT)c;
+    F.te_c[j] = c != 0 ? tc[j] : nullptr;
+    F.te_f[j] = c != 0 ? tf[j] : nullptr;
+  }
+  F.c[3] = dt * (FT)I->be[3];
+  return F;
+}
+
 // One fused ARS343 step (stage loop of ClimaTimeSteppers' IMEX ARK with one
 // Newton iteration per implicit stage); T_exp_j is DSSed once right after it
 // is computed, so every stage state assembled from u_n (continuous), DSSed
@@ -299,6 +321,13 @@ void enqueue_step(gb_ctx *ctx, FT *Yc, FT *Yf, double dt_, cudaStream_t s) {
     launch_column_stage<FT>(P, A, s);
     launch_passA<FT>(P, Uc, Uf, lap, s);
     launch_dss<FT>(P, lap, nullptr, s);
+    if (i == 3 && I->stiffly_accurate) {
+      FT *const c4[4] = {tec(0), tec(1), tec(2), tec(3)}, *const f4[4] = {tef(0), tef(1), tef(2), tef(3)};
+      const FinArgs<FT> F = fin_args<FT>(I, dt, c4, f4);
+      launch_passB<FT>(P, Uc, Uf, lap, Yc, Yf, s, &F);
+      launch_dss<FT>(P, Yc, Yf, s);
+      return;
+    }
     launch_passB<FT>(P, Uc, Uf, lap, tec(i), tef(i), s);
     launch_dss<FT>(P, tec(i), tef(i), s);
   }
@@ -444,6 +473,14 @@ int time_kernel_t(gb_ctx *ctx, int kernel, gb_fieldvec Y, int reps, double *ms) 
                                     Teb, Tibs, I->NC, I->NR, (FT *)I->adj->scr.p, (double *)I->adj->dal.p, s);
         break;
       case GB_K_DSS_T: launch_dss_transpose<FT>(P, Ubc, Ubf, s); break;
+      case GB_K_PASSB_FINAL: {
+        // U = Y + the final combination's terms; Y and the tendency buffers are read
+        FT *const c4[4] = {(FT *)I->Te[0].p, (FT *)I->Te[1].p, (FT *)I->Te[2].p, (FT *)I->Te[3].p};
+        FT *const f4[4] = {c4[0] + I->NC, c4[1] + I->NC, c4[2] + I->NC, c4[3] + I->NC};
+        const FinArgs<FT> F = fin_args<FT>(I, dt, c4, f4);
+        launch_passB<FT>(P, Yc, Yf, lap, (FT *)I->U.p, (FT *)I->U.p + I->NC, s, &F);
+        break;
+      }
       default: launch_final<FT>(P, A, (FT *)I->U.p, (FT *)I->U.p + I->NC, s); break;
     }
   };
@@ -581,6 +618,15 @@ void record_step(gb_ctx *ctx, FT *Yc, FT *Yf, double dt_, typename Impl<FT>::Rec
     FT *L = (FT *)rec.L[i].p;
     launch_passA<FT>(P, Uc, Uf, L, s);
     launch_dss<FT>(P, L, nullptr, s);
+    if (i == 3 && I->stiffly_accurate) {
+      // as enqueue_step (the reverse pass reads no T_exp of the last stage)
+      FT *const c4[4] = {Te[0], Te[1], Te[2], Te[3]};
+      FT *const f4[4] = {Te[0] + I->NC, Te[1] + I->NC, Te[2] + I->NC, Te[3] + I->NC};
+      const FinArgs<FT> F = fin_args<FT>(I, dt, c4, f4);
+      launch_passB<FT>(P, Uc, Uf, L, Yc, Yf, s, &F);
+      launch_dss<FT>(P, Yc, Yf, s);
+      return;
+    }
     launch_passB<FT>(P, Uc, Uf, L, Te[i], Te[i] + I->NC, s);
     launch_dss<FT>(P, Te[i], Te[i] + I->NC, s);
   }
@@ -661,6 +707,10 @@ void reverse_step(gb_ctx *ctx, typename Impl<FT>::Record &rec, double dt_, FT *Y
     e0[j] = F.ce[j];
     i0[j] = F.ci[j];
   }
+  // the step's own final DSS (the combination folded into the last pass B, then
+  // DSSed as a whole): its transpose first; the transposed DSS of the last
+  // tendency that follows leaves the result unchanged (the DSS is a projection)
+  if (I->stiffly_accurate) launch_dss_transpose<FT>(P, Ybc, Ybf, s);
   launch_final_transpose<FT>(P, F, Ybc, Ybf, s);
   const FT *Yc = (const FT *)rec.Y.p, *Yf = Yc + I->NC;
   FT *Ubc = (FT *)A.Ub.p, *Ubf = Ubc + I->NC;
@@ -671,7 +721,10 @@ void reverse_step(gb_ctx *ctx, typename Impl<FT>::Record &rec, double dt_, FT *Y
       tendency_vjp<FT>(ctx, Uc, Uf, (const FT *)rec.L[i].p, Teb[i], Teb[i] + I->NC, Ubc, Ubf, true, false, s, Ybc,
                        Ybf);
     } else {
-      tendency_vjp<FT>(ctx, Uc, Uf, (const FT *)rec.L[i].p, Teb[i], Teb[i] + I->NC, Ubc, Ubf, true, false, s);
+      // the last tendency's cotangent (dt b_4 times the already transposed-DSSed Ybar)
+      // needs no second transposed DSS when the step ends with a DSS of the whole sum
+      const bool dss_out = !(i == 3 && I->stiffly_accurate);
+      tendency_vjp<FT>(ctx, Uc, Uf, (const FT *)rec.L[i].p, Teb[i], Teb[i] + I->NC, Ubc, Ubf, dss_out, false, s);
       const StageArgs<FT> SA = stage_args<FT>(I, i, dt, Yc, Yf, Te, Ti);
       launch_column_stage_vjp<FT>(P, SA, Ubc, Ubf, Tib[i], Tib[i] + I->NR, Ybc, Ybf, Teb, Tib, I->NC, I->NR,
                                   (FT *)A.scr.p, (double *)A.dal.p, s, (const FT *)rec.U[i].p,
@@ -1122,7 +1175,7 @@ int gb_adjoint_reverse(gb_ctx *ctx, gb_fieldvec Ybar, double dparams[2], size_t 
 
 int gb_time_kernel(gb_ctx *ctx, int kernel, gb_fieldvec Y, int reps, double *ms) {
   GUARD(ctx);
-  if (!fv_ok(Y) || !ms || reps < 0 || kernel < 0 || kernel > GB_K_DSS_T) return fail(ctx, GB_ERR_ARG, "bad gb_time_kernel arguments");
+  if (!fv_ok(Y) || !ms || reps < 0 || kernel < 0 || kernel > GB_K_PASSB_FINAL) return fail(ctx, GB_ERR_ARG, "bad gb_time_kernel arguments");
   return DISPATCH(ctx, time_kernel_t, ctx, kernel, Y, reps, ms);
 }
 

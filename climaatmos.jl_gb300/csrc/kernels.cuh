@@ -75,6 +75,18 @@ struct StageArgs {
   int first;        // 1: overwrite rnorm, 0: accumulate
 };
 
+// Final combination of a stiffly accurate step folded into the last stage's
+// explicit tendency: out = U + sum_{j<3} c_j T_j + c_3 T, with U the stage
+// state (the pass's own input), T_j earlier (DSSed) explicit tendencies and T
+// the tendency the pass computes.
+// The bottom and top faces of u_3 are zero (the impenetrable filter, as in the
+// stage combination kernel).
+template <class FT>
+struct FinArgs {
+  const FT *te_c[3], *te_f[3];
+  FT c[4];
+};
+
 // Cotangents of the tendencies a transposed stage combination accumulates into.
 template <class FT>
 struct CotArgs {
@@ -96,7 +108,7 @@ struct ColArgs {
 };
 
 template <class FT> void launch_passA(const DevParams<FT> &P, const FT *Yc, const FT *Yf, FT *L, cudaStream_t s);
-template <class FT> void launch_passB(const DevParams<FT> &P, const FT *Yc, const FT *Yf, const FT *L, FT *Tc, FT *Tf, cudaStream_t s);
+template <class FT> void launch_passB(const DevParams<FT> &P, const FT *Yc, const FT *Yf, const FT *L, FT *Tc, FT *Tf, cudaStream_t s, const FinArgs<FT> *fin = nullptr);
 template <class FT> void launch_dss(const DevParams<FT> &P, FT *C, FT *F, cudaStream_t s);
 template <class FT> void launch_dss_transpose(const DevParams<FT> &P, FT *C, FT *F, cudaStream_t s);
 template <class FT> void launch_column_stage(const DevParams<FT> &P, const StageArgs<FT> &A, cudaStream_t s);

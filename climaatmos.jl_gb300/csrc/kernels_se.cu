@@ -174,12 +174,44 @@ __global__ void __launch_bounds__(SE_THREADS, SeMinBlocks<FT>::value) k_passA(De
   if (threadIdx.x == 0) tma_store_wait_all();
 }
 
+template <class FT>
+struct alignas(16) V16 {
+  FT v[16 / sizeof(FT)];
+};
+
+// out = U + c_3 T + sum_j c_j T_j over one slab of n values in 16-byte vectors
+// (T in shared memory, overwritten; U and the T_j at offset off in global memory).
+template <class FT>
+__device__ __forceinline__ void fin_combine(FT *sT, const FT *U, const FT *const (&Tj)[3], const FinArgs<FT> &F,
+                                            size_t off, int n) {
+  constexpr int E = 16 / sizeof(FT);
+  V16<FT> *s = reinterpret_cast<V16<FT> *>(sT);
+  const V16<FT> *u = reinterpret_cast<const V16<FT> *>(U + off);
+#pragma unroll 2
+  for (int i = threadIdx.x; i < n / E; i += SE_THREADS) {
+    V16<FT> r = u[i];
+    const V16<FT> t = s[i];
+#pragma unroll
+    for (int k = 0; k < E; ++k) r.v[k] += F.c[3] * t.v[k];
+#pragma unroll
+    for (int q = 0; q < 3; ++q)
+      if (Tj[q]) {
+        const V16<FT> a = reinterpret_cast<const V16<FT> *>(Tj[q] + off)[i];
+#pragma unroll
+        for (int k = 0; k < E; ++k) r.v[k] += F.c[q] * a.v[k];
+      }
+    s[i] = r;
+  }
+}
+
 // HS: the Held-Suarez forcing is compiled in (a separate instantiation, so that
 // the default kernel carries none of its registers or instructions).
-template <class FT, bool HS>
+// FIN: the slab written is the step's final combination (FinArgs) of the stage
+// state Yc/Yf, earlier tendencies and this tendency, instead of the tendency.
+template <class FT, bool HS, bool FIN>
 __global__ void __launch_bounds__(SE_THREADS, SeMinBlocks<FT>::value) k_passB(DevParams<FT> P, int nbuf, const FT *__restrict__ Yc,
                                                          const FT *__restrict__ Yf, const FT *__restrict__ Lin,
-                                                         FT *__restrict__ Tc, FT *__restrict__ Tf) {
+                                                         FT *__restrict__ Tc, FT *__restrict__ Tf, FinArgs<FT> F) {
   extern __shared__ __align__(128) unsigned char sm[];
   const int Nv = P.Nv, Nf = P.Nf;
   const PassBLayout<FT> Lo(Nv, nbuf);
@@ -211,6 +243,16 @@ __global__ void __launch_bounds__(SE_THREADS, SeMinBlocks<FT>::value) k_passB(De
   for (int it = 0; e < P.Nh; ++it, e += gridDim.x) {
     int b;
     if (!slab_begin(bar, nbuf, it, e, P.Nh, P.status, issue, b)) break;
+    if (FIN && threadIdx.x == 0) {
+      // the final combination's other operands, into L2 while the tendency is computed
+      bulk_prefetch_l2(Yc + (size_t)e * 64 * Nv, by);
+      bulk_prefetch_l2(Yf + (size_t)e * 16 * Nf, bf);
+      for (int q = 0; q < 3; ++q)
+        if (F.te_c[q]) {
+          bulk_prefetch_l2(F.te_c[q] + (size_t)e * 64 * Nv, by);
+          bulk_prefetch_l2(F.te_f[q] + (size_t)e * 16 * Nf, bf);
+        }
+    }
     // the tendency overwrites the state and face slabs in place: each entry is
     // written by the thread that read it, after its last read
     FT *sY = at(Lo.y, b), *sF = at(Lo.f, b);
@@ -497,6 +539,14 @@ __global__ void __launch_bounds__(SE_THREADS, SeMinBlocks<FT>::value) k_passB(De
         }
       }
     }
+    if (FIN) {
+      __syncthreads();
+      fin_combine<FT>(sO, Yc, F.te_c, F, (size_t)e * 64 * Nv, 64 * Nv);
+      fin_combine<FT>(sOf, Yf, F.te_f, F, (size_t)e * 16 * Nf, 16 * Nf);
+      __syncthreads();
+      // impenetrable filter: u_3 = 0 on the bottom and top faces (thread t < 32: node t / 2)
+      if (threadIdx.x < 32) sOf[(threadIdx.x >> 1) * Nf + ((threadIdx.x & 1) ? Nv : 0)] = FT(0);
+    }
     fence_proxy_async();
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -557,8 +607,10 @@ void configure_se(int Nv) {
   (void)Nv;
   se_device();
   cudaFuncSetAttribute(k_passA<FT>, cudaFuncAttributeMaxDynamicSharedMemorySize, g_se.optin);
-  cudaFuncSetAttribute(k_passB<FT, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, g_se.optin);
-  cudaFuncSetAttribute(k_passB<FT, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, g_se.optin);
+  cudaFuncSetAttribute(k_passB<FT, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, g_se.optin);
+  cudaFuncSetAttribute(k_passB<FT, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, g_se.optin);
+  cudaFuncSetAttribute(k_passB<FT, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, g_se.optin);
+  cudaFuncSetAttribute(k_passB<FT, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, g_se.optin);
 }
 
 template <class FT>
@@ -569,12 +621,19 @@ void launch_passA(const DevParams<FT> &P, const FT *Yc, const FT *Yf, FT *L, cud
   k_passA<FT><<<grid, SE_THREADS, sh.smem, s>>>(P, sh.nbuf, Yc, Yf, L);
 }
 template <class FT>
-void launch_passB(const DevParams<FT> &P, const FT *Yc, const FT *Yf, const FT *L, FT *Tc, FT *Tf, cudaStream_t s) {
+void launch_passB(const DevParams<FT> &P, const FT *Yc, const FT *Yf, const FT *L, FT *Tc, FT *Tf, cudaStream_t s,
+                  const FinArgs<FT> *fin) {
   se_device();
   const SeShape sh = se_shape<FT, PassBLayout<FT>>(P.Nv);
   const int grid = min(P.Nh, g_se.nsm * sh.ctas);
-  if (P.hs) k_passB<FT, true><<<grid, SE_THREADS, sh.smem, s>>>(P, sh.nbuf, Yc, Yf, L, Tc, Tf);
-  else k_passB<FT, false><<<grid, SE_THREADS, sh.smem, s>>>(P, sh.nbuf, Yc, Yf, L, Tc, Tf);
+  const FinArgs<FT> F = fin ? *fin : FinArgs<FT>{};
+  if (fin) {
+    if (P.hs) k_passB<FT, true, true><<<grid, SE_THREADS, sh.smem, s>>>(P, sh.nbuf, Yc, Yf, L, Tc, Tf, F);
+    else k_passB<FT, false, true><<<grid, SE_THREADS, sh.smem, s>>>(P, sh.nbuf, Yc, Yf, L, Tc, Tf, F);
+  } else {
+    if (P.hs) k_passB<FT, true, false><<<grid, SE_THREADS, sh.smem, s>>>(P, sh.nbuf, Yc, Yf, L, Tc, Tf, F);
+    else k_passB<FT, false, false><<<grid, SE_THREADS, sh.smem, s>>>(P, sh.nbuf, Yc, Yf, L, Tc, Tf, F);
+  }
 }
 
 #define INST(FT)                                                                                             \
@@ -582,7 +641,8 @@ void launch_passB(const DevParams<FT> &P, const FT *Yc, const FT *Yf, const FT *
   template size_t passB_smem<FT>(int);                                                                       \
   template void configure_se<FT>(int);                                                                       \
   template void launch_passA<FT>(const DevParams<FT> &, const FT *, const FT *, FT *, cudaStream_t);         \
-  template void launch_passB<FT>(const DevParams<FT> &, const FT *, const FT *, const FT *, FT *, FT *, cudaStream_t);
+  template void launch_passB<FT>(const DevParams<FT> &, const FT *, const FT *, const FT *, FT *, FT *, cudaStream_t, \
+                                 const FinArgs<FT> *);
 INST(float)
 INST(double)
 #undef INST

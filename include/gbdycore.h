@@ -152,12 +152,15 @@ int gb_jacobian_solve_noalloc(gb_ctx *ctx, gb_fieldvec dY, gb_fieldvec Y, gb_fie
  * step's kernels `reps` times on the context stream between CUDA events and
  * returns the mean time per launch in milliseconds.  kernel: 0 pass A
  * (Laplacians), 1 pass B (explicit tendency), 2 column stage (stage 4: five
- * sources), 3 state DSS, 4 final combination.  Y is read (and, for 3/4,
- * written); synchronous. */
+ * sources), 3 state DSS, 4 final combination (the stage combination kernel of
+ * the hook path), 9 the last stage's pass B with the final combination folded
+ * in (what gb_step runs in place of 4).  Y is read (and, for 3, written);
+ * synchronous. */
 enum gb_kernel_id {
   GB_K_PASSA = 0, GB_K_PASSB = 1, GB_K_COLUMN = 2, GB_K_DSS = 3, GB_K_FINAL = 4,
   /* reverse mode: pass A^T, pass B^T, the implicit column stage VJP, DSS^T */
-  GB_K_PASSA_VJP = 5, GB_K_PASSB_VJP = 6, GB_K_COLUMN_VJP = 7, GB_K_DSS_T = 8
+  GB_K_PASSA_VJP = 5, GB_K_PASSB_VJP = 6, GB_K_COLUMN_VJP = 7, GB_K_DSS_T = 8,
+  GB_K_PASSB_FINAL = 9
 };
 int gb_time_kernel(gb_ctx *ctx, int kernel, gb_fieldvec Y, int reps, double *ms_per_launch);
 

@@ -43,6 +43,28 @@ def restart_file_name(t):
     return "day%d.%d.npz" % (day, sec)
 
 
+def time_from_filename(path):
+    """Simulation time (s) from a ``day{day}.{sec}.*`` file name
+    (src/utils/utilities.jl:158-163)."""
+    parts = os.path.basename(path).split(".")
+    return float(parts[0].replace("day", "")) * 86400.0 + float(parts[1])
+
+
+def sort_files_by_time(paths):
+    """The paths ordered by the time in their names (src/utils/utilities.jl:171-172)."""
+    return sorted(paths, key=time_from_filename)
+
+
+def latest_restart_file(output_dir):
+    """The restart file of the latest time in output_dir, or None (the last of the
+    time-sorted ``day*`` files, as auto_detect_restart_file, src/simulation/restart.jl:109-134)."""
+    if not os.path.isdir(output_dir):
+        return None
+    files = [os.path.join(output_dir, f) for f in os.listdir(output_dir)
+             if f.startswith("day") and f.endswith(".npz")]
+    return sort_files_by_time(files)[-1] if files else None
+
+
 def save_state_to_disk(Yc, Yf, t, cfg, output_dir):
     """Write the state (numpy arrays) at time t; returns the file path."""
     os.makedirs(output_dir, exist_ok=True)

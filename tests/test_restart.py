@@ -19,6 +19,28 @@ def test_file_name_from_time():
     assert R.restart_file_name(86400.0 * 2 + 3661.5) == "day2.3661.npz"
 
 
+def test_time_from_filename_known_answers():
+    # the reference's known answers (test/utilities.jl:103-108)
+    assert R.time_from_filename("day0.0.hdf5") == 0.0
+    assert R.time_from_filename("day1.0.hdf5") == 86400.0
+    assert R.time_from_filename("day1.3600.hdf5") == 86400.0 + 3600.0
+    assert R.time_from_filename("day10.43200.hdf5") == 10 * 86400.0 + 43200.0
+    for t in (0.0, 59.0, 86399.0, 86400.0, 90061.0, 10 ** 6):
+        assert R.time_from_filename(R.restart_file_name(t)) == t
+
+
+def test_sort_files_by_time(tmp_path):
+    # as test/utilities.jl:92-101: names of random times, lexically sorted, back in time order
+    rng = np.random.default_rng(0)
+    t = rng.integers(1, 10 ** 6, 100)
+    names = sorted(R.restart_file_name(float(x)) for x in t)
+    assert R.sort_files_by_time(names) == [R.restart_file_name(float(x)) for x in np.sort(t)]
+    assert R.latest_restart_file(str(tmp_path / "none")) is None
+    for x in (86400.0 * 2, 86400.0 * 10, 3600.0):
+        (tmp_path / R.restart_file_name(x)).write_bytes(b"")
+    assert os.path.basename(R.latest_restart_file(str(tmp_path))) == "day10.0.npz"
+
+
 def test_round_trip_and_checks(tmp_path):
     cfg = small_config(np.float32)
     Yc, Yf = perturbed_state(cfg, dtype=np.float32)

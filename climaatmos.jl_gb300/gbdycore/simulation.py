@@ -254,10 +254,14 @@ def simulated_years_per_day(dt, seconds_per_step):
 class AtmosSimulation:
     """State + cache + time of one dry dynamical-core run on the GPU."""
 
-    def __init__(self, config, workload="plain", state=None, device="cuda", restart_file=None):
+    def __init__(self, config, workload="plain", state=None, device="cuda", restart_file=None,
+                 detect_restart_file=False, output_dir=None):
         self.config = config
         self.geometry = Geometry(config)
         self.t = 0.0
+        if restart_file is None and detect_restart_file and output_dir is not None:
+            # the most recent restart file in output_dir, if any (restart.jl:147-160)
+            restart_file = R.latest_restart_file(output_dir)
         if restart_file is not None:
             # handle_restart (src/simulation/restart.jl:58-84): the file's time takes precedence
             Yc, Yf, self.t = R.get_state_restart(restart_file, config)

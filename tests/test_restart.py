@@ -71,7 +71,7 @@ def test_restarted_run_continues_bitwise(tmp_path):
     a.step(2)
     path = a.save_state(str(tmp_path))
     a.step(3)
-    b = sim.AtmosSimulation(cfg, restart_file=path)
+    b = sim.AtmosSimulation(cfg, detect_restart_file=True, output_dir=str(tmp_path))
     assert b.t == 2 * cfg.dt
     b.step(3)
     ac, af = a.Y.numpy()

@@ -301,7 +301,7 @@ __global__ void __launch_bounds__(128) k_col_stage_vjp(DevParams<FT> P, ColVjpAr
     for (int q = S_BR; q <= S_BEU1; ++q) S(q, v) = FT(0);
   for (int f = 0; f < Nf; ++f)
     for (int q = S_BU3; q <= S_BFHB; ++q) S(q, f) = FT(0);
-  double dal = 0;
+  CSum<FT> dal;
   // output cotangents: U and T_imp = (U - U^) / dtgamma
   for (int v = 0; v < Nv; ++v) {
     S(S_BRN, v) = V.Ub_c[cb + v] + V.Tb_c[rb + v] * idtg;
@@ -439,8 +439,8 @@ __global__ void __launch_bounds__(128) k_col_stage_vjp(DevParams<FT> P, ColVjpAr
     const FT spg = P.levf[LF_SPG * Nf + f], beta = P.lf4[f].y;
     const FT u3 = S(S_U3, f);
     S(S_BU3, f) -= beta * T3b;
-    dal -= (double)(spg * u3 * T3b);
-    dal -= (double)(dtg * spg * bbb);  // uu1 = dtgamma (... - beta) - 1
+    dal.add(-mul_rn(spg * u3, T3b));
+    dal.add(-mul_rn(dtg * spg, bbb));  // uu1 = dtgamma (... - beta) - 1
     if (f == 0 || f >= Nv) continue;
     const int a = f - 1, b = f;
     // T3 = -(dPhi - (Phi_r(b) - Phi_r(a)) + cp thd (Pi(b) - Pi(a))) - beta u3
@@ -570,7 +570,7 @@ __global__ void __launch_bounds__(128) k_col_stage_vjp(DevParams<FT> P, ColVjpAr
       }
     }
   }
-  V.dalpha[col] += dal;  // accumulated over the launches of a reverse pass (zeroed by the host)
+  V.dalpha[col] += dal.value();  // accumulated over the launches of a reverse pass (zeroed by the host)
 }
 
 
@@ -962,7 +962,7 @@ __global__ void __launch_bounds__(128, MINB) k_col_stage_vjp_g(DevParams<FT> P, 
   for (int k = 0; k < CM; ++k) {
     bH4[k] = bK[k] = bH[k] = bPI[k] = bTHV[k] = bTHVR[k] = bPHIR[k] = bRJ[k] = FT(0);
   }
-  double dal = 0;
+  CSum<FT> dal;
   {
     // contributions to the centre below the face (f - 1) go to the previous level
     FT pR0 = 0, pK = 0, pTHV = 0, pTHVR = 0, pPI = 0, pPHIR = 0, pru0 = 0, pru1 = 0, peu0 = 0, peu1 = 0, pRr = 0, pRe = 0;
@@ -1009,8 +1009,8 @@ __global__ void __launch_bounds__(128, MINB) k_col_stage_vjp_g(DevParams<FT> P, 
       bH4[k] += db;
       bU3[k] -= db;
       bU3[k] -= beta[k] * T3b;
-      dal -= (double)(spg[k] * u3[k] * T3b);
-      dal -= (double)(dtg * spg[k] * bbb);
+      dal.add(-mul_rn(spg[k] * u3[k], T3b));
+      dal.add(-mul_rn(dtg * spg[k], bbb));
       if (!(f > 0 && f < Nv)) continue;
       // T3 = -(dPhi - (Phi_r(b) - Phi_r(a)) + cp thd (Pi(b) - Pi(a))) - beta u3
       const FT Pia = cprev(Pi, k, Pip), dPi = Pi[k] - Pia;
@@ -1194,7 +1194,7 @@ __global__ void __launch_bounds__(128, MINB) k_col_stage_vjp_g(DevParams<FT> P, 
     }
   }
   col::group_sum1<G>(dal);
-  if (gl == 0 && colv) V.dalpha[col] += dal;
+  if (gl == 0 && colv) V.dalpha[col] += dal.value();
 }
 
 }  // namespace lp

@@ -332,7 +332,8 @@ __global__ void __launch_bounds__(AD_THREADS, AdMinBlocks<FT>::value)
   const FT nu = P.nu_v, nus = P.nu_s;
   const FT rpr = nu != FT(0) ? nus / nu : FT(1);  // d nu_s / d nu = 1 / Prandtl
   const FT hc = P.cpd / FT(2);
-  double dnu = 0, dal = 0;
+  CSum<FT> dnu, dal;
+  const FT inu = nu != FT(0) ? FT(1) / nu : FT(0);  // the Laplacian terms of d/dnu carry 1 / nu
   for (int it = 0; e < P.Nh; ++it, e += gridDim.x) {
     int b;
     if (!slab_begin(bar, nbuf, it, e, P.Nh, P.status, issue, b)) break;
@@ -424,7 +425,7 @@ __global__ void __launch_bounds__(AD_THREADS, AdMinBlocks<FT>::value)
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
           const int q = (NQ * j + i) * Nv + v;
-          dnu -= (double)(o1[i] * sT[16 * Nv + q] + o2[i] * sT[32 * Nv + q] + rpr * hd[i] * sT[48 * Nv + q]);
+          dnu.add(-(o1[i] * sT[16 * Nv + q] + o2[i] * sT[32 * Nv + q] + rpr * hd[i] * sT[48 * Nv + q]));
         }
       }
     }
@@ -511,7 +512,7 @@ __global__ void __launch_bounds__(AD_THREADS, AdMinBlocks<FT>::value)
           RJb[i] = b3b * u3[i] * g33;
           Cv1[i] = inner ? fo1b * iJf : FT(0);
           Cv2[i] = inner ? fo2b * iJf : FT(0);
-          if (act) dnu -= (double)(l4 * T3b);
+          if (act) dnu.add(-mul_rn(l4, T3b));
           u3d[i] = inner ? b3b * rJ * g33 : FT(0);
           // w1 = -tb iWJf, w2 = ta iWJf  ->  cotangents of tb, ta
           tbb[i] = -fo1b * iWJf;
@@ -605,7 +606,7 @@ __global__ void __launch_bounds__(AD_THREADS, AdMinBlocks<FT>::value)
             c2b[i] = -s.J[i] * a3 * t1b;
             u1b[i] = -beta * Tu1b[i];
             u2b[i] = -beta * Tu2b[i];
-            if (act) dal -= (double)(spg * (u1[i] * Tu1b[i] + u2[i] * Tu2b[i]));
+            if (act) dal.add(-mul_rn(spg, u1[i] * Tu1b[i] + u2[i] * Tu2b[i]));
             Kb[i] = FT(0);
           }
         }
@@ -711,7 +712,7 @@ __global__ void __launch_bounds__(AD_THREADS, AdMinBlocks<FT>::value)
             lb[48 * Nv + q] = L3b[i];
             dl += sL[16 * Nv + q] * L1b[i] + sL[32 * Nv + q] * L2b[i] + sL[48 * Nv + q] * L3b[i] - o3[i] * L4b[i];
           }
-          if (nu != FT(0)) dnu += (double)dl / (double)nu;
+          dnu.add(mul_rn(dl, inu));
         }
       }
       {
@@ -743,7 +744,7 @@ __global__ void __launch_bounds__(AD_THREADS, AdMinBlocks<FT>::value)
             lb[(NQ * j + i) * Nv + v] = Lsb[i];
             dl += Ls[i] * Lsb[i];
           }
-          if (nu != FT(0)) dnu += (double)dl / (double)nu;
+          dnu.add(mul_rn(dl, inu));
         }
       }
       // ---- forward thermodynamics and the horizontal-dynamics transpose
@@ -944,13 +945,13 @@ __global__ void __launch_bounds__(AD_THREADS, AdMinBlocks<FT>::value)
   // parameter cotangents: warp sums, then the warps in a fixed order; one slot per CTA
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
-    dnu += __shfl_xor_sync(0xffffffffu, dnu, o);
-    dal += __shfl_xor_sync(0xffffffffu, dal, o);
+    dnu.add(dnu.xor_shfl(o, 32));
+    dal.add(dal.xor_shfl(o, 32));
   }
   const int warp = threadIdx.x >> 5;
   if ((threadIdx.x & 31) == 0) {
-    red[warp] = dnu;
-    red[AD_THREADS / 32 + warp] = dal;
+    red[warp] = dnu.value();
+    red[AD_THREADS / 32 + warp] = dal.value();
   }
   __syncthreads();
   if (threadIdx.x == 0) {  // accumulated over the launches of a reverse pass (zeroed by the host)

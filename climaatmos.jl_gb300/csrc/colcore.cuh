@@ -135,7 +135,7 @@ __device__ __forceinline__ FT vanleer_g(FT u, FT am2, FT am1, FT a0, FT ap1, boo
 // iJc receives 1/J of the lane's centres.
 template <class FT, int G, int CM, bool HAT>
 __device__ __forceinline__ void newton_core(const DevParams<FT> &P, const ColGeo<FT> &Gm, const ColLev<FT> &L, int gl,
-                                            FT dtg, const FT (&Hh)[5][CM], FT (&U)[5][CM], double (&ss)[3],
+                                            FT dtg, const FT (&Hh)[5][CM], FT (&U)[5][CM], CSum<FT> (&ss)[3],
                                             bool &finite, FT (&iJc)[CM]) {
   const int Nv = L.Nv, Nf = L.Nf;
   const int r0 = gl * CM;
@@ -236,8 +236,8 @@ __device__ __forceinline__ void newton_core(const DevParams<FT> &P, const ColGeo
     ru1[k] = cv ? dtg * v1 : FT(0);
     eu0[k] = cv ? dtg * (v0 * fhb[k]) : FT(0);
     eu1[k] = cv ? dtg * (v1 * fhb[k + 1]) : FT(0);
-    ss[0] += (double)(Rr[k] * Rr[k]);
-    ss[1] += (double)(Re[k] * Re[k]);
+    ss[0].add(mul_rn(Rr[k], Rr[k]));
+    ss[1].add(mul_rn(Re[k], Re[k]));
     finite = finite && isfinite(Rr[k]) && isfinite(Re[k]);
   }
   // ---- Schur complement rows onto u_3 (faces r0 .. r0+CM-1); centre r0-1 rows from the previous lane
@@ -251,7 +251,7 @@ __device__ __forceinline__ void newton_core(const DevParams<FT> &P, const ColGeo
       const int f = r0 + k;
       FT R3 = FT(0);
       if (f < Nf) R3 = dtg * T3[k] + (Hh[4][k] - u3[k]);
-      ss[2] += (double)(R3 * R3);
+      ss[2].add(mul_rn(R3, R3));
       finite = finite && isfinite(R3);
       FT aa = uu0[k], bb = uu1[k], cc = uu2[k], rhs = R3;
       const FT mr0 = k > 0 ? ru0[k - 1] : pru0, mr1 = k > 0 ? ru1[k - 1] : pru1;
@@ -337,17 +337,20 @@ __device__ __forceinline__ void vanleer_correct(const DevParams<FT> &P, const Co
   }
 }
 
-// Sum of the lane group's FP64 squares (every lane of the warp calls it).
-template <int G>
-__device__ __forceinline__ void group_sum(double (&ss)[3]) {
+// Sums over the lane group, the same in every lane (TwoSum is exact, so the
+// butterfly's operand order does not matter); every lane of the warp calls it.
+template <int G, class FT>
+__device__ __forceinline__ void group_sum(CSum<FT> (&ss)[3]) {
 #pragma unroll
   for (int q = 0; q < 3; ++q)
-    for (int o = G / 2; o > 0; o >>= 1) ss[q] += __shfl_xor_sync(0xffffffffu, ss[q], o, G);
+#pragma unroll
+    for (int o = G / 2; o > 0; o >>= 1) ss[q].add(ss[q].xor_shfl(o, G));
 }
 
-template <int G>
-__device__ __forceinline__ void group_sum1(double &v) {
-  for (int o = G / 2; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o, G);
+template <int G, class FT>
+__device__ __forceinline__ void group_sum1(CSum<FT> &v) {
+#pragma unroll
+  for (int o = G / 2; o > 0; o >>= 1) v.add(v.xor_shfl(o, G));
 }
 
 }  // namespace col

@@ -74,7 +74,7 @@ __device__ __forceinline__ void solve_item(const DevParams<FT> &P, const BatchAr
   }
   bool finite = true;
   for (int it = 0; it < B.iters; ++it) {
-    double ss[3] = {0, 0, 0};
+    CSum<FT> ss[3];
     FT iJc[CM];
     col::newton_core<FT, G, CM, true>(P, Gm, L, gl, B.dtg, H, U, ss, finite, iJc);
     // u_h: T_imp = 0 and its Jacobian block is -I, so Newton sets it to U^'s
@@ -82,7 +82,7 @@ __device__ __forceinline__ void solve_item(const DevParams<FT> &P, const BatchAr
     for (int k = 0; k < CM; ++k) { U[1][k] = H[1][k]; U[2][k] = H[2][k]; }
     col::group_sum<G>(ss);
     if (gl == 0 && colv)
-      for (int q = 0; q < 3; ++q) B.rnorm[((size_t)c * MAX_ITERS + it) * 3 + q] = ss[q];
+      for (int q = 0; q < 3; ++q) B.rnorm[((size_t)c * MAX_ITERS + it) * 3 + q] = ss[q].value();
   }
   finite = __all_sync(0xffffffffu, finite);
   if (lane == 0 && !finite) atomicOr(P.status, ST_NONFINITE);

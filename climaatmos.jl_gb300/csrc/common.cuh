@@ -160,6 +160,52 @@ __device__ __forceinline__ void fence_mbar_init() {
 }
 // Start a global line towards L2 (no register written, no wait).
 __device__ __forceinline__ void prefetch_l2(const void *p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
+// Compensated sum of FT values.  In FP32 a (hi, lo) pair: every addition is
+// Knuth's TwoSum (error-free), its rounding error carried in lo, so the sum
+// keeps about twice FP32's precision without FP64 instructions (GB300 issues
+// FP64 at 1/64 of its FP32 rate; FP64 accumulators made that pipe the
+// bottleneck of the column kernels).  value() rounds hi + lo to FP64.  In FP64
+// a plain double.  Products fed to add() are rounded first (mul_rn), so that
+// no multiply-add contraction splits them between the TwoSum's operations.
+template <class FT>
+struct CSum;
+template <>
+struct CSum<float> {
+  float hi = 0.f, lo = 0.f;
+  __device__ __forceinline__ void add(float x) {
+    const float s = hi + x, v = s - hi;
+    lo += (hi - (s - v)) + (x - v);
+    hi = s;
+  }
+  __device__ __forceinline__ void add(const CSum &o) {
+    const float s = hi + o.hi, v = s - hi;
+    const float e = ((hi - (s - v)) + (o.hi - v)) + (lo + o.lo);
+    hi = s + e;
+    lo = e - (hi - s);
+  }
+  __device__ __forceinline__ double value() const { return (double)hi + (double)lo; }
+  __device__ __forceinline__ CSum xor_shfl(int o, int width) const {
+    CSum r;
+    r.hi = __shfl_xor_sync(0xffffffffu, hi, o, width);
+    r.lo = __shfl_xor_sync(0xffffffffu, lo, o, width);
+    return r;
+  }
+};
+template <>
+struct CSum<double> {
+  double s = 0.0;
+  __device__ __forceinline__ void add(double x) { s += x; }
+  __device__ __forceinline__ void add(const CSum &o) { s += o.s; }
+  __device__ __forceinline__ double value() const { return s; }
+  __device__ __forceinline__ CSum xor_shfl(int o, int width) const {
+    CSum r;
+    r.s = __shfl_xor_sync(0xffffffffu, s, o, width);
+    return r;
+  }
+};
+__device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
+
 // L2 prefetch of a contiguous range by the copy engine (16-byte aligned, size a multiple of 16)
 __device__ __forceinline__ void bulk_prefetch_l2(const void *p, uint32_t bytes) {
   asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");

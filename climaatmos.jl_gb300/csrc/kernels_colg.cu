@@ -97,7 +97,7 @@ __global__ void __launch_bounds__(CG_THREADS, MINB) k_col_stage_g(DevParams<FT> 
   for (int c = 0; c < 5; ++c)
 #pragma unroll
     for (int k = 0; k < CM; ++k) U[c][k] = H[c][k];
-  double ss[3] = {0, 0, 0};
+  CSum<FT> ss[3];
   bool finite = true;
   FT iJc[CM];
   col::newton_core<FT, G, CM, false>(P, Gm, L, gl, dtg, H, U, ss, finite, iJc);
@@ -127,7 +127,7 @@ __global__ void __launch_bounds__(CG_THREADS, MINB) k_col_stage_g(DevParams<FT> 
   finite = __all_sync(0xffffffffu, finite);
   if (gl == 0 && colv) {
     if (A.rnorm)
-      for (int q = 0; q < 3; ++q) A.rnorm[(size_t)col * 3 + q] = (A.first ? 0.0 : A.rnorm[(size_t)col * 3 + q]) + ss[q];
+      for (int q = 0; q < 3; ++q) A.rnorm[(size_t)col * 3 + q] = (A.first ? 0.0 : A.rnorm[(size_t)col * 3 + q]) + ss[q].value();
   }
   if (lane == 0 && !finite) atomicOr(P.status, ST_NONFINITE);
 }

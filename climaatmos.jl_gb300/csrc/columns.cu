@@ -82,7 +82,7 @@ __device__ __forceinline__ void solve_item(const DevParams<FT> &P, const BatchAr
     for (int k = 0; k < CM; ++k) { U[1][k] = H[1][k]; U[2][k] = H[2][k]; }
     col::group_sum<G>(ss);
     if (gl == 0 && colv)
-      for (int q = 0; q < 3; ++q) B.rnorm[((size_t)c * MAX_ITERS + it) * 3 + q] = ss[q].value();
+      for (int q = 0; q < 3; ++q) RSlot<FT>::put(&B.rnorm[((size_t)c * MAX_ITERS + it) * 3 + q], ss[q], true);
   }
   finite = __all_sync(0xffffffffu, finite);
   if (lane == 0 && !finite) atomicOr(P.status, ST_NONFINITE);
@@ -157,22 +157,17 @@ __global__ void __launch_bounds__(128, 4) k_col_group(DevParams<FT> P, BatchArgs
   solve_item<FT, G, 4>(P, B, B.items[item0 + it], threadIdx.x & 31);
 }
 
-// rsum[it][q] = sum over columns of rnorm[c][it][q] (fixed order: deterministic)
-__global__ void k_batch_rsum(const double *rnorm, int ncols, double *out) {
-  __shared__ double sh[3][256];
+// rsum[it][q] = sum over columns of rnorm[c][it][q] (fixed order: deterministic;
+// compensated FP32 pairs in FP32 runs, FP64 once at the end)
+template <class FT>
+__global__ void __launch_bounds__(256) k_batch_rsum(const double *rnorm, int ncols, double *out) {
   const int it = blockIdx.x;
-  double s[3] = {0, 0, 0};
+  CSum<FT> s[3];
   for (int c = threadIdx.x; c < ncols; c += blockDim.x)
-    for (int q = 0; q < 3; ++q) s[q] += rnorm[((size_t)c * MAX_ITERS + it) * 3 + q];
-  for (int q = 0; q < 3; ++q) sh[q][threadIdx.x] = s[q];
-  __syncthreads();
-  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
-    if ((int)threadIdx.x < o)
-      for (int q = 0; q < 3; ++q) sh[q][threadIdx.x] += sh[q][threadIdx.x + o];
-    __syncthreads();
-  }
+    for (int q = 0; q < 3; ++q) s[q].add(RSlot<FT>::load(&rnorm[((size_t)c * MAX_ITERS + it) * 3 + q]));
+  block_sum3<FT>(s);
   if (threadIdx.x == 0)
-    for (int q = 0; q < 3; ++q) out[it * 3 + q] = sh[q][0];
+    for (int q = 0; q < 3; ++q) out[it * 3 + q] = s[q].value();
 }
 
 // ---------------------------------------------------------------- host side
@@ -396,7 +391,7 @@ void enqueue_persistent(gb_columns *cols, int variant, gb_fieldvec U, gb_fieldve
     case 3: k_col_batch<FT, 256, 2, true><<<g, 256, 0, s>>>(I->P, B); break;
     default: k_col_batch<FT, 64, 8, true><<<g, 64, 0, s>>>(I->P, B); break;
   }
-  k_batch_rsum<<<iters, 256, 0, s>>>((const double *)I->rnorm.p, cols->ncols, (double *)I->rsum.p);
+  k_batch_rsum<FT><<<iters, 256, 0, s>>>((const double *)I->rnorm.p, cols->ncols, (double *)I->rsum.p);
 }
 
 template <class FT>
@@ -412,7 +407,7 @@ void enqueue_per_height(gb_columns *cols, gb_fieldvec U, gb_fieldvec Uh, double 
       default: k_col_group<FT, 32><<<grid, 128, 0, s>>>(I->P, B, g.item0, g.nitem); break;
     }
   }
-  k_batch_rsum<<<iters, 256, 0, s>>>((const double *)I->rnorm.p, cols->ncols, (double *)I->rsum.p);
+  k_batch_rsum<FT><<<iters, 256, 0, s>>>((const double *)I->rnorm.p, cols->ncols, (double *)I->rsum.p);
 }
 
 template <class FT>

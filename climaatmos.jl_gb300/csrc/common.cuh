@@ -193,18 +193,89 @@ struct CSum<float> {
 };
 template <>
 struct CSum<double> {
-  double s = 0.0;
-  __device__ __forceinline__ void add(double x) { s += x; }
-  __device__ __forceinline__ void add(const CSum &o) { s += o.s; }
-  __device__ __forceinline__ double value() const { return s; }
+  double hi = 0.0, lo = 0.0;  // lo stays zero
+  __device__ __forceinline__ void add(double x) { hi += x; }
+  __device__ __forceinline__ void add(const CSum &o) { hi += o.hi; }
+  __device__ __forceinline__ double value() const { return hi; }
   __device__ __forceinline__ CSum xor_shfl(int o, int width) const {
     CSum r;
-    r.s = __shfl_xor_sync(0xffffffffu, s, o, width);
+    r.hi = __shfl_xor_sync(0xffffffffu, hi, o, width);
     return r;
   }
 };
 __device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
 __device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
+
+// A column's residual sum of squares as kept between kernels, in one 8-byte
+// slot: the compensated pair itself in FP32 runs (so that the column kernels
+// issue no FP64 instruction: on this pipe a warp instruction costs its full
+// issue time even with one lane active), a double in FP64 runs.  get() is the
+// FP64 value; put() stores v (first) or adds it to the stored sum.
+template <class FT>
+struct RSlot;
+template <>
+struct RSlot<float> {
+  static __device__ __forceinline__ void put(double *p, const CSum<float> &v, bool first) {
+    float2 *q = reinterpret_cast<float2 *>(p);
+    CSum<float> t = v;
+    if (!first) {
+      const float2 o = *q;
+      CSum<float> a;
+      a.hi = o.x;
+      a.lo = o.y;
+      t.add(a);
+    }
+    *q = make_float2(t.hi, t.lo);
+  }
+  static __device__ __forceinline__ CSum<float> load(const double *p) {
+    const float2 q = *reinterpret_cast<const float2 *>(p);
+    CSum<float> r;
+    r.hi = q.x;
+    r.lo = q.y;
+    return r;
+  }
+};
+template <>
+struct RSlot<double> {
+  static __device__ __forceinline__ void put(double *p, const CSum<double> &v, bool first) {
+    *p = first ? v.hi : *p + v.hi;
+  }
+  static __device__ __forceinline__ CSum<double> load(const double *p) {
+    CSum<double> r;
+    r.hi = *p;
+    return r;
+  }
+};
+
+// Sum over a block of 256 threads of three compensated sums each, in a fixed
+// order (deterministic); the result is valid in thread 0.
+template <class FT>
+__device__ __forceinline__ void block_sum3(CSum<FT> (&v)[3]) {
+  __shared__ FT sh_hi[3][256], sh_lo[3][256];
+  for (int q = 0; q < 3; ++q) {
+    sh_hi[q][threadIdx.x] = v[q].hi;
+    sh_lo[q][threadIdx.x] = v[q].lo;
+  }
+  __syncthreads();
+  for (int o = 128; o > 0; o >>= 1) {
+    if ((int)threadIdx.x < o)
+      for (int q = 0; q < 3; ++q) {
+        CSum<FT> a, b;
+        a.hi = sh_hi[q][threadIdx.x];
+        a.lo = sh_lo[q][threadIdx.x];
+        b.hi = sh_hi[q][threadIdx.x + o];
+        b.lo = sh_lo[q][threadIdx.x + o];
+        a.add(b);
+        sh_hi[q][threadIdx.x] = a.hi;
+        sh_lo[q][threadIdx.x] = a.lo;
+      }
+    __syncthreads();
+  }
+  for (int q = 0; q < 3; ++q) {
+    v[q].hi = sh_hi[q][0];
+    v[q].lo = sh_lo[q][0];
+  }
+}
 
 // L2 prefetch of a contiguous range by the copy engine (16-byte aligned, size a multiple of 16)
 __device__ __forceinline__ void bulk_prefetch_l2(const void *p, uint32_t bytes) {

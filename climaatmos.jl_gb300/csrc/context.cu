@@ -399,7 +399,7 @@ int global_sums_t(gb_ctx *ctx, gb_fieldvec Y, double *out) {
 template <class FT>
 int residual_t(gb_ctx *ctx, double *out) {
   Impl<FT> *I = impl<FT>(ctx);
-  launch_reduce_rnorm((const double *)I->rnorm.p, I->P.Nh * NN, (double *)I->rsum.p, ctx->stream);
+  launch_reduce_rnorm<FT>((const double *)I->rnorm.p, I->P.Nh * NN, (double *)I->rsum.p, ctx->stream);
   int r = check_launch(ctx);
   if (r) return r;
   CK(cudaMemcpyAsync(out, I->rsum.p, 3 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));

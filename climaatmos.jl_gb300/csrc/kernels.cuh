@@ -71,7 +71,7 @@ struct StageArgs {
   FT *U_c, *U_f;    // stage state out
   FT *Ti_c, *Ti_f;  // implicit tendency of this stage out (reduced)
   FT dtg, idtg;
-  double *rnorm;    // [ncols][3] residual sums of squares (accumulated)
+  double *rnorm;    // [ncols][3] residual sums of squares (accumulated; RSlot<FT> entries)
   int first;        // 1: overwrite rnorm, 0: accumulate
 };
 
@@ -130,7 +130,7 @@ size_t col_vjp_scratch_words(int Nh, int Nv);
 template <class FT> void launch_column_stage_vjp(const DevParams<FT> &P, const StageArgs<FT> &A, const FT *Ub_c, const FT *Ub_f, const FT *Tb_c, const FT *Tb_f, FT *Yb_c, FT *Yb_f, FT *const Teb[4], FT *const Tib[4], size_t NC, size_t NR, FT *scr, double *dalpha, cudaStream_t s, const FT *Uo = nullptr, const FT *Tio = nullptr, const FT *e0 = nullptr, const FT *i0 = nullptr);
 template <class FT> void launch_bc_filter(const DevParams<FT> &P, FT *Yf, cudaStream_t s);
 template <class FT> void launch_global_sums(const DevParams<FT> &P, const FT *Yc, double *partials, int nblocks, double *out, cudaStream_t s);
-void launch_reduce_rnorm(const double *rnorm, int ncols, double *out, cudaStream_t s);
+template <class FT> void launch_reduce_rnorm(const double *rnorm, int ncols, double *out, cudaStream_t s);
 
 // Shared memory needed by the slab kernels with single input buffers (the
 // minimum; double buffering is used when it fits).

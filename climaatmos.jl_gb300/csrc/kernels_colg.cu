@@ -127,7 +127,7 @@ __global__ void __launch_bounds__(CG_THREADS, MINB) k_col_stage_g(DevParams<FT> 
   finite = __all_sync(0xffffffffu, finite);
   if (gl == 0 && colv) {
     if (A.rnorm)
-      for (int q = 0; q < 3; ++q) A.rnorm[(size_t)col * 3 + q] = (A.first ? 0.0 : A.rnorm[(size_t)col * 3 + q]) + ss[q].value();
+      for (int q = 0; q < 3; ++q) RSlot<FT>::put(&A.rnorm[(size_t)col * 3 + q], ss[q], A.first != 0);
   }
   if (lane == 0 && !finite) atomicOr(P.status, ST_NONFINITE);
 }

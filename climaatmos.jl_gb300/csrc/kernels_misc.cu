@@ -297,18 +297,14 @@ __global__ void k_sums_final(const double *__restrict__ part, int nblocks, doubl
   }
 }
 
-__global__ void k_reduce_rnorm(const double *__restrict__ r, int ncols, double *__restrict__ out) {
-  __shared__ double sh[3][256];
-  double s[3] = {0, 0, 0};
+template <class FT>
+__global__ void __launch_bounds__(256) k_reduce_rnorm(const double *__restrict__ r, int ncols, double *__restrict__ out) {
+  CSum<FT> s[3];
   for (int c = threadIdx.x; c < ncols; c += blockDim.x)
-    for (int q = 0; q < 3; ++q) s[q] += r[(size_t)c * 3 + q];
-  for (int q = 0; q < 3; ++q) sh[q][threadIdx.x] = s[q];
-  __syncthreads();
-  if (threadIdx.x < 3) {
-    double t = 0;
-    for (int i = 0; i < (int)blockDim.x; ++i) t += sh[threadIdx.x][i];
-    out[threadIdx.x] = t;
-  }
+    for (int q = 0; q < 3; ++q) s[q].add(RSlot<FT>::load(&r[(size_t)c * 3 + q]));
+  block_sum3<FT>(s);
+  if (threadIdx.x == 0)
+    for (int q = 0; q < 3; ++q) out[q] = s[q].value();
 }
 
 }  // namespace
@@ -344,8 +340,9 @@ void launch_global_sums(const DevParams<FT> &P, const FT *Yc, double *partials, 
   k_sums_partial<FT><<<nblocks, SUM_THREADS, 0, s>>>(P, Yc, partials);
   k_sums_final<<<1, 32, 0, s>>>(partials, nblocks, out);
 }
+template <class FT>
 void launch_reduce_rnorm(const double *rnorm, int ncols, double *out, cudaStream_t s) {
-  k_reduce_rnorm<<<1, 256, 0, s>>>(rnorm, ncols, out);
+  k_reduce_rnorm<FT><<<1, 256, 0, s>>>(rnorm, ncols, out);
 }
 
 #define INST(FT)                                                                                          \
@@ -354,7 +351,8 @@ void launch_reduce_rnorm(const double *rnorm, int ncols, double *out, cudaStream
   template void launch_final<FT>(const DevParams<FT> &, const StageArgs<FT> &, FT *, FT *, cudaStream_t); \
   template void launch_final_transpose<FT>(const DevParams<FT> &, const CotArgs<FT> &, FT *, FT *, cudaStream_t); \
   template void launch_bc_filter<FT>(const DevParams<FT> &, FT *, cudaStream_t);                          \
-  template void launch_global_sums<FT>(const DevParams<FT> &, const FT *, double *, int, double *, cudaStream_t);
+  template void launch_global_sums<FT>(const DevParams<FT> &, const FT *, double *, int, double *, cudaStream_t); \
+  template void launch_reduce_rnorm<FT>(const double *, int, double *, cudaStream_t);
 INST(float)
 INST(double)
 #undef INST

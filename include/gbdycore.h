@@ -152,9 +152,9 @@ int gb_jacobian_solve_noalloc(gb_ctx *ctx, gb_fieldvec dY, gb_fieldvec Y, gb_fie
  * step's kernels `reps` times on the context stream between CUDA events and
  * returns the mean time per launch in milliseconds.  kernel: 0 pass A
  * (Laplacians), 1 pass B (explicit tendency), 2 column stage (stage 4: five
- * sources), 3 state DSS, 4 final combination (the stage combination kernel of
- * the hook path), 9 the last stage's pass B with the final combination folded
- * in (what gb_step runs in place of 4).  Y is read (and, for 3, written);
+ * sources), 3 state DSS, 4 the unfolded final combination (run by gb_step only
+ * for a tableau that is not stiffly accurate), 9 the last stage's pass B with
+ * the final combination folded in (what gb_step runs for ARS343).  Y is read (and, for 3, written);
  * synchronous. */
 enum gb_kernel_id {
   GB_K_PASSA = 0, GB_K_PASSB = 1, GB_K_COLUMN = 2, GB_K_DSS = 3, GB_K_FINAL = 4,

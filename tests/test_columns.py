@@ -123,6 +123,9 @@ def test_gpu_fp32_against_fp64_oracle():
     assert rel(gc[3], oc[3]) < 1e-5
     assert rel(gf, of) < 2e-3  # u_3 after the solve: cancellation of O(1e5) hydrostatic terms in FP32
     assert np.all(rn[1] < 1e-1 * rn[0])
+    # first-iteration residual sums of squares (compensated FP32 pairs per column, reduced in
+    # FP32 TwoSum arithmetic) against the FP64 oracle's
+    np.testing.assert_allclose(rn[0], orn[0], rtol=5e-2)
 
 
 @pytest.mark.gpu

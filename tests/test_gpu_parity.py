@@ -185,6 +185,21 @@ def test_global_sums_and_conservation():
     assert np.all(np.isfinite(r)) and r[0] > 0
 
 
+def test_newton_residual_fp32_against_fp64():
+    """The step's Newton residual sums of squares (three implicit stages, summed per column):
+    FP32 keeps them as compensated FP32 pairs and reduces them in FP32 TwoSum arithmetic; they
+    agree with the FP64 library's from the same state to FP32 accuracy."""
+    c32, c64 = small_config(ft=np.float32), small_config(ft=np.float64)
+    Yc, Yf = perturbed_state(c32, dtype=np.float32)
+    r = []
+    for cfg, st in ((c32, (Yc, Yf)), (c64, (Yc.astype(np.float64), Yf.astype(np.float64)))):
+        s = sim.AtmosSimulation(cfg, state=st)
+        s.step(1)
+        r.append(s.p.newton_residual())
+    assert np.all(np.isfinite(r[0])) and np.all(r[1] > 0)
+    np.testing.assert_allclose(r[0], r[1], rtol=5e-2)
+
+
 def test_nonfinite_state_is_reported():
     cfg = small_config(ft=np.float32)
     Yc, Yf = perturbed_state(cfg, dtype=np.float32)

@@ -50,7 +50,7 @@ struct ColVjpArgs {
   FT *Teb_c[4], *Teb_f[4];  // cotangents of the explicit tendencies (accumulated)
   FT *Tib_c[4], *Tib_f[4];  // cotangents of the implicit tendencies (accumulated)
   FT *scr;
-  double *dalpha;         // per-column d/d(sponge rate), accumulated
+  double *dalpha;         // per-column d/d(sponge rate), accumulated (RSlot<FT> entries)
   // when set: the recorded stage output U and implicit tendency T_imp, from which
   // U^ = U - dtgamma T_imp (the stage leaves u_h unchanged) replaces the assembly
   const FT *Uo_c, *Uo_f, *Tio_c, *Tio_f;
@@ -570,7 +570,7 @@ __global__ void __launch_bounds__(128) k_col_stage_vjp(DevParams<FT> P, ColVjpAr
       }
     }
   }
-  V.dalpha[col] += dal.value();  // accumulated over the launches of a reverse pass (zeroed by the host)
+  RSlot<FT>::put(&V.dalpha[col], dal, false);  // accumulated over the launches of a reverse pass (zeroed by the host)
 }
 
 
@@ -1194,7 +1194,7 @@ __global__ void __launch_bounds__(128, MINB) k_col_stage_vjp_g(DevParams<FT> P, 
     }
   }
   col::group_sum1<G>(dal);
-  if (gl == 0 && colv) V.dalpha[col] += dal.value();
+  if (gl == 0 && colv) RSlot<FT>::put(&V.dalpha[col], dal, false);
 }
 
 }  // namespace lp

@@ -755,7 +755,7 @@ int read_dacc(gb_ctx *ctx, double *dpar, bool add) {
   Impl<FT> *I = impl<FT>(ctx);
   auto &A = *I->adj;
   launch_accum((const double *)A.dparB.p, A.grid, 2, 2, (double *)A.dacc.p, ctx->stream);
-  launch_accum((const double *)A.dal.p, I->P.Nh * NN, 1, 1, (double *)A.dacc.p + 1, ctx->stream);
+  launch_accum_slots<FT>((const double *)A.dal.p, I->P.Nh * NN, (double *)A.dacc.p + 1, ctx->stream);
   double h[2];
   CK(cudaMemcpyAsync(h, I->adj->dacc.p, 2 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));

@@ -131,6 +131,7 @@ template <class FT> void launch_column_stage_vjp(const DevParams<FT> &P, const S
 template <class FT> void launch_bc_filter(const DevParams<FT> &P, FT *Yf, cudaStream_t s);
 template <class FT> void launch_global_sums(const DevParams<FT> &P, const FT *Yc, double *partials, int nblocks, double *out, cudaStream_t s);
 template <class FT> void launch_reduce_rnorm(const double *rnorm, int ncols, double *out, cudaStream_t s);
+template <class FT> void launch_accum_slots(const double *part, int n, double *acc, cudaStream_t s);
 
 // Shared memory needed by the slab kernels with single input buffers (the
 // minimum; double buffering is used when it fits).

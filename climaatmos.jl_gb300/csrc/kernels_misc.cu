@@ -236,6 +236,15 @@ __global__ void k_accum(const double *__restrict__ part, int n, int stride, int 
   }
 }
 
+// acc[0] += the sum of n RSlot<FT> entries (fixed order; one block of 256 threads).
+template <class FT>
+__global__ void __launch_bounds__(256) k_accum_slots(const double *__restrict__ part, int n, double *__restrict__ acc) {
+  CSum<FT> s[3];
+  for (int i = threadIdx.x; i < n; i += blockDim.x) s[0].add(RSlot<FT>::load(&part[i]));
+  block_sum3<FT>(s);
+  if (threadIdx.x == 0) acc[0] += s[0].value();
+}
+
 template <class FT>
 __global__ void k_bc_filter(int ncols, int Nf, FT *__restrict__ Yf) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
@@ -327,6 +336,10 @@ template <class FT>
 void launch_final_transpose(const DevParams<FT> &P, const CotArgs<FT> &A, FT *Ybc, FT *Ybf, cudaStream_t s) {
   k_final_t<FT><<<152 * 8, 256, 0, s>>>(P, A, Ybc, Ybf);
 }
+template <class FT>
+void launch_accum_slots(const double *part, int n, double *acc, cudaStream_t s) {
+  k_accum_slots<FT><<<1, 256, 0, s>>>(part, n, acc);
+}
 void launch_accum(const double *part, int n, int stride, int nout, double *acc, cudaStream_t s) {
   k_accum<<<1, 256, 0, s>>>(part, n, stride, nout, acc);
 }
@@ -352,7 +365,8 @@ void launch_reduce_rnorm(const double *rnorm, int ncols, double *out, cudaStream
   template void launch_final_transpose<FT>(const DevParams<FT> &, const CotArgs<FT> &, FT *, FT *, cudaStream_t); \
   template void launch_bc_filter<FT>(const DevParams<FT> &, FT *, cudaStream_t);                          \
   template void launch_global_sums<FT>(const DevParams<FT> &, const FT *, double *, int, double *, cudaStream_t); \
-  template void launch_reduce_rnorm<FT>(const double *, int, double *, cudaStream_t);
+  template void launch_reduce_rnorm<FT>(const double *, int, double *, cudaStream_t);             \
+  template void launch_accum_slots<FT>(const double *, int, double *, cudaStream_t);
 INST(float)
 INST(double)
 #undef INST

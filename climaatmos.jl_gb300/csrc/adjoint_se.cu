@@ -45,16 +45,18 @@ __device__ __forceinline__ void level_geo(const DevParams<FT> &P, const RowGeo<F
 struct AdDev {
   int nsm = 0, optin = 0, per_sm = 0;
 };
-AdDev &ad_dev() {
-  static AdDev d;
-  if (!d.nsm) {
+// Read once (a function-local static: thread-safe initialisation).
+const AdDev &ad_dev() {
+  static const AdDev d = [] {
+    AdDev x;
     int dev = 0;
     cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&d.nsm, cudaDevAttrMultiProcessorCount, dev);
-    cudaDeviceGetAttribute(&d.optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-    cudaDeviceGetAttribute(&d.per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
-    if (d.nsm <= 0) d.nsm = 1;
-  }
+    cudaDeviceGetAttribute(&x.nsm, cudaDevAttrMultiProcessorCount, dev);
+    cudaDeviceGetAttribute(&x.optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    cudaDeviceGetAttribute(&x.per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+    if (x.nsm <= 0) x.nsm = 1;
+    return x;
+  }();
   return d;
 }
 // Buffering and resident CTAs per SM of a TMA slab kernel (1 KB per CTA is

@@ -561,17 +561,21 @@ __global__ void __launch_bounds__(SE_THREADS, SeMinBlocks<FT>::value) k_passB(De
 struct SeLaunch {
   int nsm = 0, optin = 0, per_sm = 0;
 };
-SeLaunch g_se;
-
-void se_device() {
-  if (!g_se.nsm) {
+// The device attributes the slab launches need, read once (a function-local
+// static: its initialisation is thread-safe); every device of one process is
+// taken to be the same GPU model.
+const SeLaunch &se_dev() {
+  static const SeLaunch d = [] {
+    SeLaunch x;
     int dev = 0;
     cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&g_se.nsm, cudaDevAttrMultiProcessorCount, dev);
-    cudaDeviceGetAttribute(&g_se.optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-    cudaDeviceGetAttribute(&g_se.per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
-    if (g_se.nsm <= 0) g_se.nsm = 1;
-  }
+    cudaDeviceGetAttribute(&x.nsm, cudaDevAttrMultiProcessorCount, dev);
+    cudaDeviceGetAttribute(&x.optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    cudaDeviceGetAttribute(&x.per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+    if (x.nsm <= 0) x.nsm = 1;
+    return x;
+  }();
+  return d;
 }
 
 // Buffering and resident CTAs per SM of a slab kernel.  With two CTAs per SM
@@ -584,12 +588,12 @@ struct SeShape {
 };
 template <class FT, class L>
 SeShape se_shape(int Nv) {
-  const size_t two = L(Nv, 2).total, one = L(Nv, 1).total, per_sm = (size_t)g_se.per_sm;
+  const size_t two = L(Nv, 2).total, one = L(Nv, 1).total, per_sm = (size_t)se_dev().per_sm;
   if (SeMinBlocks<FT>::value >= 2) {
     if (2 * (two + 1024) <= per_sm) return {2, 2, two};
     if (2 * (one + 1024) <= per_sm) return {1, 2, one};
   }
-  if (two <= (size_t)g_se.optin) return {2, 1, two};
+  if (two <= (size_t)se_dev().optin) return {2, 1, two};
   return {1, 1, one};
 }
 
@@ -605,27 +609,24 @@ size_t passB_smem(int Nv) { return PassBLayout<FT>(Nv, 1).total; }
 template <class FT>
 void configure_se(int Nv) {
   (void)Nv;
-  se_device();
-  cudaFuncSetAttribute(k_passA<FT>, cudaFuncAttributeMaxDynamicSharedMemorySize, g_se.optin);
-  cudaFuncSetAttribute(k_passB<FT, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, g_se.optin);
-  cudaFuncSetAttribute(k_passB<FT, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, g_se.optin);
-  cudaFuncSetAttribute(k_passB<FT, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, g_se.optin);
-  cudaFuncSetAttribute(k_passB<FT, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, g_se.optin);
+  cudaFuncSetAttribute(k_passA<FT>, cudaFuncAttributeMaxDynamicSharedMemorySize, se_dev().optin);
+  cudaFuncSetAttribute(k_passB<FT, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, se_dev().optin);
+  cudaFuncSetAttribute(k_passB<FT, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, se_dev().optin);
+  cudaFuncSetAttribute(k_passB<FT, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, se_dev().optin);
+  cudaFuncSetAttribute(k_passB<FT, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, se_dev().optin);
 }
 
 template <class FT>
 void launch_passA(const DevParams<FT> &P, const FT *Yc, const FT *Yf, FT *L, cudaStream_t s) {
-  se_device();
   const SeShape sh = se_shape<FT, PassALayout<FT>>(P.Nv);
-  const int grid = min(P.Nh, g_se.nsm * sh.ctas);
+  const int grid = min(P.Nh, se_dev().nsm * sh.ctas);
   k_passA<FT><<<grid, SE_THREADS, sh.smem, s>>>(P, sh.nbuf, Yc, Yf, L);
 }
 template <class FT>
 void launch_passB(const DevParams<FT> &P, const FT *Yc, const FT *Yf, const FT *L, FT *Tc, FT *Tf, cudaStream_t s,
                   const FinArgs<FT> *fin) {
-  se_device();
   const SeShape sh = se_shape<FT, PassBLayout<FT>>(P.Nv);
-  const int grid = min(P.Nh, g_se.nsm * sh.ctas);
+  const int grid = min(P.Nh, se_dev().nsm * sh.ctas);
   const FinArgs<FT> F = fin ? *fin : FinArgs<FT>{};
   if (fin) {
     if (P.hs) k_passB<FT, true, true><<<grid, SE_THREADS, sh.smem, s>>>(P, sh.nbuf, Yc, Yf, L, Tc, Tf, F);

@@ -1,0 +1,129 @@
+"""Oracle restatement of the surface-elevation profiles and terrain-following mesh warps.
+
+TEST INFRASTRUCTURE ONLY. This module is part of the CPU oracle; only the test suite may
+use it. It is the first piece of the topography extension (the GPU metric terms and
+kernels are not built yet): the analytic surface elevations the reference's idealised and
+spherical cases use, and the warps that turn flat level heights into terrain-following ones.
+
+What it restates:
+
+* ``topography_function`` of the analytic profiles (src/topography/topography.jl):
+  ``CosineTopography`` in 2D and 3D (:83-95), ``AgnesiTopography`` (:118-125),
+  ``ScharTopography`` (:151-159), ``DCMIP200Topography`` (:186-205, the 2 km circular mountain
+  on the equator at 270 degrees longitude) and ``Hughes2023Topography`` (:224-253, two 2 km
+  ridges at 45 N).  Angles are in degrees as in the reference.
+* ``LinearWarp`` and ``SLEVEWarp`` (topography.jl:272-307).  The warps themselves are
+  ClimaCore's hypsography adaptions (ClimaCore 0.15.1, not vendored), restated from their
+  published formulations: linear decay of the terrain with height (Gal-Chen and Somerville,
+  1975), z = xi + z_s (1 - xi / z_top); and the one-scale SLEVE coordinate of Schaer et al.
+  (2002) as the reference documents it, z = xi + z_s sinh((eta_h - eta) / (s eta_h)) / sinh(1 / s)
+  for eta = xi / z_top <= eta_h, else z = xi.  Building the grid requires s z_top to exceed
+  the highest surface (topography.jl:295-297).
+"""
+import math
+from dataclasses import dataclass
+
+import numpy as np
+
+
+def cospi(x):
+    return np.cos(np.pi * np.asarray(x, dtype=np.float64))
+
+
+# ---------------------------------------------------------------- analytic profiles
+@dataclass(frozen=True)
+class CosineTopography:
+    """h_max cos(2 pi x / lambda) (2D) or h_max cos(2 pi x / lambda) cos(2 pi y / lambda) (3D)."""
+    dim: int = 2
+    h_max: float = 25.0
+    lam: float = 25e3
+
+    def __call__(self, x, y=0.0):
+        ly = math.inf if self.dim == 2 else self.lam
+        return self.h_max * cospi(2 * np.asarray(x) / self.lam) * cospi(2 * np.asarray(y) / ly)
+
+
+@dataclass(frozen=True)
+class AgnesiTopography:
+    """Witch of Agnesi: h_max / (1 + ((x - x_c) / a)^2)."""
+    h_max: float = 25.0
+    x_center: float = 50e3
+    a: float = 5e3
+
+    def __call__(self, x):
+        return self.h_max / (1 + ((np.asarray(x, dtype=np.float64) - self.x_center) / self.a) ** 2)
+
+
+@dataclass(frozen=True)
+class ScharTopography:
+    """h_max exp(-((x - x_c) / a)^2) cos^2(pi (x - x_c) / lambda)."""
+    h_max: float = 25.0
+    x_center: float = 50e3
+    lam: float = 4e3
+    a: float = 5e3
+
+    def __call__(self, x):
+        d = np.asarray(x, dtype=np.float64) - self.x_center
+        return self.h_max * np.exp(-d ** 2 / self.a ** 2) * cospi(d / self.lam) ** 2
+
+
+def dcmip200(lat, lon):
+    """DCMIP-2-0-0 mountain (degrees): a cosine bell of 2 km over a great-circle radius of
+    3 pi / 4 around (0 N, 270 E), modulated by cosine ridges of half-width pi / 16."""
+    lat = np.asarray(lat, dtype=np.float64)
+    lon = np.asarray(lon, dtype=np.float64)
+    lat_m, lon_m = 0.0, 270.0
+    d2r = np.pi / 180.0
+    r = np.arccos(np.sin(lat_m * d2r) * np.sin(lat * d2r)
+                  + np.cos(lat_m * d2r) * np.cos(lat * d2r) * np.cos((lon - lon_m) * d2r))
+    R_m, zeta_m, h0 = 3 * np.pi / 4, np.pi / 16, 2000.0
+    return np.where(r < R_m, h0 / 2 * (1 + cospi(r / R_m)) * cospi(r / zeta_m) ** 2, 0.0)
+
+
+def hughes2023(lat, lon):
+    """Hughes and Jablonowski (2023) ridges (degrees): super-Gaussian in latitude, Gaussian
+    in longitude, 2 km peaks at (45 N, 72 E) and (45 N, 140 E), a tenth of the peak at 20
+    degrees of latitude and 3.5 degrees of longitude from it."""
+    lat = np.asarray(lat, dtype=np.float64)
+    lon = np.asarray(lon, dtype=np.float64)
+    h0, lat1, lat2, lon1, lon2, lon_w, lat_w = 2e3, 45.0, 45.0, 72.0, 140.0, 7.0, 40.0
+    d = lat_w / 2 * (-math.log(0.1)) ** (-1 / 6)
+    c = lon_w / 2 * (-math.log(0.1)) ** (-1 / 2)
+    return h0 * (np.exp(-(((lat - lat1) / d) ** 6 + ((lon - lon1) / c) ** 2))
+                 + np.exp(-(((lat - lat2) / d) ** 6 + ((lon - lon2) / c) ** 2)))
+
+
+# ---------------------------------------------------------------- mesh warps
+@dataclass(frozen=True)
+class LinearWarp:
+    """Terrain influence decaying linearly to zero at the model top."""
+
+    def __call__(self, xi, z_surface, z_top):
+        xi = np.asarray(xi, dtype=np.float64)
+        return xi + np.asarray(z_surface, dtype=np.float64) * (1 - xi / z_top)
+
+
+@dataclass(frozen=True)
+class SLEVEWarp:
+    """Smooth level vertical coordinate: the terrain decays like
+    sinh((eta_h - eta) / (s eta_h)) / sinh(1 / s), flat above eta_h = eta."""
+    eta: float = 0.7
+    s: float = 10.0
+
+    def __call__(self, xi, z_surface, z_top):
+        xi = np.asarray(xi, dtype=np.float64)
+        zs = np.asarray(z_surface, dtype=np.float64)
+        if np.any(self.s * z_top <= zs):
+            raise ValueError("SLEVEWarp: s * z_top must exceed the surface elevation")
+        eta = xi / z_top
+        decay = np.sinh((self.eta - eta) / (self.s * self.eta)) / math.sinh(1 / self.s)
+        return np.where(eta <= self.eta, xi + zs * decay, xi)
+
+
+def warped_faces(zf_flat, z_surface, warp):
+    """Face heights of terrain-following columns: zf[..., k] for flat face heights zf_flat
+    (0 .. z_top) over surfaces z_surface (any shape), with the given warp."""
+    zf_flat = np.asarray(zf_flat, dtype=np.float64)
+    z_top = float(zf_flat[-1])
+    zs = np.asarray(z_surface, dtype=np.float64)[..., None]
+    return warp(zf_flat, zs, z_top)

@@ -1,0 +1,77 @@
+"""Surface-elevation profiles and terrain-following warps of the oracle (the first piece of
+the topography extension), pinned to the reference's known answers in test/topography.jl,
+and the warps' properties on the production grid (CPU only)."""
+import numpy as np
+import pytest
+
+import topography as T
+from geometry import OracleGeometry, vertical_faces
+
+
+def test_dcmip200_on_the_cubed_sphere():
+    # test/topography.jl:11-22: extrema (0, 2000), the peak on the equator at -90 longitude
+    g = OracleGeometry(4, 2)
+    lat, lon = np.degrees(g.lat), np.degrees(g.lon)
+    z = T.dcmip200(lat, lon)
+    assert z.min() == 0.0 and abs(z.max() - 2000.0) < 1e-9
+    k = np.unravel_index(np.argmax(z), z.shape)
+    assert abs(lat[k]) < 1e-9 and abs(lon[k] + 90.0) < 1e-9
+
+
+def test_hughes2023_on_the_cubed_sphere():
+    # test/topography.jl:24-34: within [0, 2000], no NaN
+    g = OracleGeometry(6, 2)
+    z = T.hughes2023(np.degrees(g.lat), np.degrees(g.lon))
+    assert np.all(np.isfinite(z)) and z.min() >= 0.0 and z.max() <= 2000.0
+
+
+def test_cosine_known_answers():
+    # test/topography.jl:36-60
+    t3 = T.CosineTopography(dim=3, h_max=100.0, lam=1000.0)
+    assert t3(0.0, 0.0) == 100.0
+    assert abs(t3(500.0, 0.0) + 100.0) <= np.finfo(np.float64).eps
+    t2 = T.CosineTopography(dim=2, h_max=50.0, lam=2000.0)
+    assert t2(0.0) == 50.0
+    assert abs(t2(1000.0) + 50.0) <= np.finfo(np.float64).eps
+
+
+def test_agnesi_and_schar_known_answers():
+    # test/topography.jl:62-91
+    a = T.AgnesiTopography(h_max=1000.0, x_center=500.0, a=100.0)
+    assert a(500.0) == 1000.0 and a(600.0) == 500.0 and a(0.0) < 50.0
+    s = T.ScharTopography(h_max=500.0, x_center=1000.0, lam=200.0, a=100.0)
+    assert s(1000.0) == 500.0
+    assert abs(s(1100.0)) <= 1e-6
+    assert np.all(s(np.arange(0.0, 2001.0, 100.0)) >= 0.0)
+
+
+def test_warp_defaults_and_parameters():
+    # test/topography.jl:93-101 and the defaults at src/topography/topography.jl:304-307
+    assert T.SLEVEWarp() == T.SLEVEWarp(eta=0.7, s=10.0)
+    w = T.SLEVEWarp(eta=0.8, s=12.0)
+    assert w.eta == 0.8 and w.s == 12.0
+
+
+@pytest.mark.parametrize("warp", [T.LinearWarp(), T.SLEVEWarp()])
+def test_warped_production_columns(warp):
+    """Over the DCMIP200 mountain on the production levels (63, tanh-stretched from 30 m):
+    the bottom face follows the surface, the top stays at z_top, levels stay ordered, and a
+    flat surface leaves the levels unchanged."""
+    zf = vertical_faces(63, 30000.0, True, 30.0)
+    g = OracleGeometry(4, 2)
+    zs = T.dcmip200(np.degrees(g.lat), np.degrees(g.lon))
+    Z = T.warped_faces(zf, zs, warp)
+    assert Z.shape == zs.shape + (64,)
+    np.testing.assert_allclose(Z[..., 0], zs, rtol=0, atol=1e-9)
+    np.testing.assert_allclose(Z[..., -1], 30000.0, rtol=0, atol=1e-9)
+    assert np.all(np.diff(Z, axis=-1) > 0)
+    np.testing.assert_allclose(T.warped_faces(zf, np.zeros(3), warp), np.broadcast_to(zf, (3, 64)), atol=1e-9)
+
+
+def test_sleve_flat_above_eta_and_refuses_high_terrain():
+    zf = np.linspace(0.0, 1000.0, 11)
+    Z = T.warped_faces(zf, np.array([100.0]), T.SLEVEWarp(eta=0.5, s=2.0))[0]
+    np.testing.assert_array_equal(Z[zf / 1000.0 > 0.5], zf[zf / 1000.0 > 0.5])
+    assert np.all(Z[zf / 1000.0 < 0.5] > zf[zf / 1000.0 < 0.5])
+    with pytest.raises(ValueError):
+        T.warped_faces(zf, np.array([2500.0]), T.SLEVEWarp(eta=0.5, s=2.0))

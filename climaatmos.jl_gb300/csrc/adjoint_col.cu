@@ -622,8 +622,9 @@ __device__ __forceinline__ void fold2(FT (&own)[CM], FT toPrev2, FT toPrev1, FT 
   if (gl > 0) { own[0] += c; own[1] += d; }
 }
 
-// FP32 is capped at 128 registers (four resident 128-thread CTAs per SM; 60 B of spills measured at
-// z_elem = 63), FP64 runs uncapped.
+// Default register cap: FP32 at 128 registers (four resident 128-thread CTAs per SM), FP64
+// uncapped; the FP32 32-lane, two-levels-per-lane form (z_elem < 64) is launched at six CTAs
+// per SM instead (launch_column_stage_vjp).
 template <class FT>
 struct VjpMinBlocks {
   static constexpr int value = sizeof(FT) == 4 ? 4 : 1;

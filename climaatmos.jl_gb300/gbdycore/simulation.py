@@ -272,6 +272,7 @@ class AtmosSimulation:
         self.Y = FieldVector.from_numpy(np.asarray(Yc, dtype=config.ft), np.asarray(Yf, dtype=config.ft), device)
         self.p = AtmosCache(config)
         self.dt = config.dt
+        self.output_dir = output_dir
 
     def step(self, nsteps=1, use_graph=True):
         self.p.call("gb_step", self.Y.gb(), float(self.t), float(self.dt), int(nsteps), 1 if use_graph else 0)
@@ -282,19 +283,52 @@ class AtmosSimulation:
         Yc, Yf = self.Y.numpy()
         return R.save_state_to_disk(Yc, Yf, self.t, self.config, output_dir)
 
+    def synchronize(self):
+        import torch
+        torch.cuda.synchronize()
+
+    def check(self):
+        """Raise GBError if a kernel of the steps so far flagged a failure (a non-finite Newton
+        residual, a device wait that timed out); gb_newton_residual reads the status word."""
+        self.p.newton_residual()
+
+
+class AtmosSolveResults:
+    """What solve_atmos returns (solve.jl:93-97): ``sol`` the final state (None after a
+    crash), ``ret_code`` "success" or "simulation_crashed", ``walltime`` [s] of the timed
+    steps (None after a crash); ``seconds_per_step`` and ``sypd`` as solve.jl:40-45 logs them."""
+
+    def __init__(self, sol, ret_code, walltime, seconds_per_step=None, sypd=None):
+        self.sol = sol
+        self.ret_code = ret_code
+        self.walltime = walltime
+        self.seconds_per_step = seconds_per_step
+        self.sypd = sypd
+
+    def __repr__(self):
+        return "AtmosSolveResults(ret_code=%r, walltime=%r, sypd=%r)" % (self.ret_code, self.walltime, self.sypd)
+
 
 def solve_atmos(sim, nsteps, use_graph=True):
-    """Warm-up step, then ``nsteps`` timed steps (solve.jl:119-149); returns timing and SYPD."""
-    import torch
-    sim.step(1, use_graph)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    sim.step(nsteps, use_graph)
-    torch.cuda.synchronize()
-    wall = time.perf_counter() - t0
+    """One untimed step, then ``nsteps`` timed steps (solve.jl:119-149).  A library failure
+    ends the run as the reference's catch does: the state is written to ``sim.output_dir``
+    (when set) and the results carry ret_code "simulation_crashed"."""
+    try:
+        sim.step(1, use_graph)
+        sim.synchronize()
+        t0 = time.perf_counter()
+        sim.step(nsteps, use_graph)
+        sim.synchronize()
+        wall = time.perf_counter() - t0
+        sim.check()
+    except N.GBError as e:
+        import warnings
+        if getattr(sim, "output_dir", None):
+            sim.save_state(sim.output_dir)
+        warnings.warn("simulation crashed: %s" % e)
+        return AtmosSolveResults(None, "simulation_crashed", None)
     sps = wall / max(nsteps, 1)
-    return {"walltime": wall, "seconds_per_step": sps, "sypd": simulated_years_per_day(sim.dt, sps),
-            "ret_code": "success"}
+    return AtmosSolveResults(sim.Y, "success", wall, sps, simulated_years_per_day(sim.dt, sps))
 
 
 # ---------------------------------------------------------------- reverse mode

@@ -1,0 +1,55 @@
+"""solve_atmos's host logic (src/simulation/solve.jl:93-149): one untimed step, the timed
+steps, the results record, and the crash path (the state written to the output directory,
+ret_code "simulation_crashed"), on a fake simulation (CPU only; the GPU path that raises is
+covered by test_gpu_parity.py::test_nonfinite_state_is_reported)."""
+import pytest
+
+from gbdycore import _native as N
+from gbdycore import simulation as sim
+
+
+class FakeSim:
+    def __init__(self, fail_check=False, fail_step=False, output_dir=None):
+        self.steps, self.saved, self.dt, self.Y = [], [], 120.0, object()
+        self.fail_check, self.fail_step, self.output_dir = fail_check, fail_step, output_dir
+
+    def step(self, n, use_graph=True):
+        if self.fail_step:
+            raise N.GBError(N.GB_ERR_TIMEOUT, "a device wait gave up")
+        self.steps.append(n)
+
+    def synchronize(self):
+        pass
+
+    def check(self):
+        if self.fail_check:
+            raise N.GBError(N.GB_ERR_NONFINITE, "non-finite Newton residual")
+
+    def save_state(self, d):
+        self.saved.append(d)
+
+
+def test_success_record():
+    s = FakeSim()
+    r = sim.solve_atmos(s, 10)
+    assert s.steps == [1, 10]
+    assert r.ret_code == "success" and r.sol is s.Y and r.walltime >= 0
+    assert r.seconds_per_step == pytest.approx(r.walltime / 10)
+    if r.walltime > 0:
+        assert r.sypd == pytest.approx(sim.simulated_years_per_day(120.0, r.seconds_per_step))
+
+
+@pytest.mark.parametrize("kw", [dict(fail_check=True), dict(fail_step=True)])
+def test_crash_saves_state_and_reports(kw, tmp_path):
+    s = FakeSim(output_dir=str(tmp_path), **kw)
+    with pytest.warns(UserWarning, match="simulation crashed"):
+        r = sim.solve_atmos(s, 5)
+    assert r.ret_code == "simulation_crashed" and r.sol is None and r.walltime is None
+    assert s.saved == [str(tmp_path)]
+
+
+def test_crash_without_output_dir_saves_nothing():
+    s = FakeSim(fail_check=True)
+    with pytest.warns(UserWarning):
+        r = sim.solve_atmos(s, 2)
+    assert r.ret_code == "simulation_crashed" and s.saved == []

@@ -255,8 +255,9 @@ class AtmosSimulation:
     """State + cache + time of one dry dynamical-core run on the GPU."""
 
     def __init__(self, config, workload="plain", state=None, device="cuda", restart_file=None,
-                 detect_restart_file=False, output_dir=None):
+                 detect_restart_file=False, output_dir=None, t_end=None):
         self.config = config
+        self.t_end = t_end
         self.geometry = Geometry(config)
         self.t = 0.0
         if restart_file is None and detect_restart_file and output_dir is not None:
@@ -309,10 +310,17 @@ class AtmosSolveResults:
         return "AtmosSolveResults(ret_code=%r, walltime=%r, sypd=%r)" % (self.ret_code, self.walltime, self.sypd)
 
 
-def solve_atmos(sim, nsteps, use_graph=True):
-    """One untimed step, then ``nsteps`` timed steps (solve.jl:119-149).  A library failure
-    ends the run as the reference's catch does: the state is written to ``sim.output_dir``
-    (when set) and the results carry ret_code "simulation_crashed"."""
+def solve_atmos(sim, nsteps=None, use_graph=True):
+    """One untimed step, then ``nsteps`` timed steps (solve.jl:119-149); without ``nsteps``
+    the run goes to ``sim.t_end`` as the reference's does (the untimed step included).  A
+    library failure ends the run as the reference's catch does: the state is written to
+    ``sim.output_dir`` (when set) and the results carry ret_code "simulation_crashed"."""
+    if nsteps is None:
+        if getattr(sim, "t_end", None) is None:
+            raise ValueError("solve_atmos: give nsteps or an AtmosSimulation with t_end")
+        nsteps = int(round((sim.t_end - sim.t) / sim.dt)) - 1
+        if nsteps < 0:
+            raise ValueError("solve_atmos: t_end is less than one step ahead")
     try:
         sim.step(1, use_graph)
         sim.synchronize()

@@ -9,8 +9,9 @@ from gbdycore import simulation as sim
 
 
 class FakeSim:
-    def __init__(self, fail_check=False, fail_step=False, output_dir=None):
+    def __init__(self, fail_check=False, fail_step=False, output_dir=None, t=0.0, t_end=None):
         self.steps, self.saved, self.dt, self.Y = [], [], 120.0, object()
+        self.t, self.t_end = t, t_end
         self.fail_check, self.fail_step, self.output_dir = fail_check, fail_step, output_dir
 
     def step(self, n, use_graph=True):
@@ -53,3 +54,13 @@ def test_crash_without_output_dir_saves_nothing():
     with pytest.warns(UserWarning):
         r = sim.solve_atmos(s, 2)
     assert r.ret_code == "simulation_crashed" and s.saved == []
+
+
+def test_runs_to_t_end():
+    s = FakeSim(t=240.0, t_end=240.0 + 120.0 * 12)
+    assert sim.solve_atmos(s).ret_code == "success"
+    assert s.steps == [1, 11]  # the untimed step and the timed ones reach t_end
+    with pytest.raises(ValueError):
+        sim.solve_atmos(FakeSim())
+    with pytest.raises(ValueError):
+        sim.solve_atmos(FakeSim(t=100.0, t_end=100.0))

@@ -126,7 +126,8 @@ class ClockSampler:
                     reasons.add(n)
         os.unlink(self.f.name)
         return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": sorted(reasons), "samples": len(sm)}
+                "reasons": sorted(reasons), "samples": len(sm),
+                "window": "untimed steps of the workload (~0.6 s) and the timed steps after them"}
 
 
 # ------------------------------------------------------------------ CPU baseline (oracle port)
@@ -244,9 +245,21 @@ def run_gb300(args):
     rep.barrier()
     clocks = ClockSampler(local)
     clocks.start()
-    time.sleep(0.3)
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    # the sampler reads the clocks every 200 ms, longer than the timed steps take: it runs over
+    # ~0.6 s of untimed steps of the same workload that lead straight into the timed ones,
+    # which then start again from the state the warm-up left
+    y0c, y0f, t0 = s.Y.c.clone(), s.Y.f.clone(), s.t
+    t_load = time.perf_counter()
+    while time.perf_counter() - t_load < 0.6:
+        s.step(10)
+        torch.cuda.synchronize()
+    s.Y.c.copy_(y0c)
+    s.Y.f.copy_(y0f)
+    s.t = t0
+    del y0c, y0f
+    rep.barrier()
     torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(stream)
     s.step(args.steps)
     e1.record(stream)

@@ -820,6 +820,16 @@ struct Oracle {
   }
 
   std::vector<FT> Te_c[4], Te_f[4], Ti_c[4], Ti_f[4], Uc, Uf, Hc, Hf, Rc_, Rf_, Xc_, Xf_, Kc, Kf;
+  // ORACLE_STORE32 (a separate build for the precision study only): every field the step
+  // stores (stage states, tendencies, the state) is rounded to FP32 while the arithmetic
+  // stays in FT, which separates the FP32 storage error from the FP32 arithmetic error.
+#ifdef ORACLE_STORE32
+  static void R32v(std::vector<FT> &v) { for (auto &x : v) x = (FT)(float)x; }
+  static void R32p(FT *p, size_t n) { for (size_t i = 0; i < n; ++i) p[i] = (FT)(float)p[i]; }
+#else
+  static void R32v(std::vector<FT> &) {}
+  static void R32p(FT *, size_t) {}
+#endif
   void step(FT *Yc, FT *Yf, double dt_) {
     FT dt = (FT)dt_;
     size_t NC = ncen(), NF = nfac();
@@ -848,7 +858,9 @@ struct Oracle {
         }
         Uf[q] = s;
       }
+      R32v(Uc); R32v(Uf);
       if (i > 0 || dss_stage1) dss(Uc.data(), Uf.data());
+      R32v(Uc); R32v(Uf);
       FT aii = ai[i][i];
       if (aii != FT(0)) {
         FT dtg = dt * aii;
@@ -868,12 +880,15 @@ struct Oracle {
           for (size_t q = 0; q < NC; ++q) Uc[q] += dtg * Kc[q];
           set_precomputed(Uc.data(), Uf.data());
         }
+        R32v(Uc); R32v(Uf);
         for (size_t q = 0; q < NC; ++q) Ti_c[i][q] = (Uc[q] - Hc[q]) / dtg;
         for (size_t q = 0; q < NF; ++q) Ti_f[i][q] = (Uf[q] - Hf[q]) / dtg;
+        R32v(Ti_c[i]); R32v(Ti_f[i]);
       } else {
         set_precomputed(Uc.data(), Uf.data());  // cache!
       }
       remaining_tendency(Te_c[i].data(), Te_f[i].data(), Uc.data(), Uf.data());
+      R32v(Te_c[i]); R32v(Te_f[i]);
     }
 #pragma omp parallel for
     for (size_t q = 0; q < NC; ++q) {
@@ -893,7 +908,9 @@ struct Oracle {
       }
       Yf[q] = s;
     }
+    R32p(Yc, NC); R32p(Yf, NF);
     dss(Yc, Yf);
+    R32p(Yc, NC); R32p(Yf, NF);
     set_precomputed(Yc, Yf);
   }
 

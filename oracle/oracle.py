@@ -17,16 +17,25 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD = os.path.join(HERE, "_build")
-LIB = os.path.join(BUILD, "liboracle.so")
+# ORACLE_VARIANT=store32 selects the precision-study build (ORACLE_STORE32 in dycore_oracle.cpp:
+# every field the step stores is rounded to FP32, the arithmetic stays in the oracle's type);
+# unset, the oracle is the default build.
+VARIANT = os.environ.get("ORACLE_VARIANT", "")
+if VARIANT not in ("", "store32"):
+    raise ValueError("ORACLE_VARIANT must be unset or 'store32'")
+LIB = os.path.join(BUILD, "liboracle_store32.so" if VARIANT else "liboracle.so")
 SRC = os.path.join(HERE, "dycore_oracle.cpp")
 
 
 def build(force=False):
-    """Compile the oracle with g++ (OpenMP) into oracle/_build/liboracle.so."""
+    """Compile the oracle with g++ (OpenMP) into oracle/_build/liboracle.so (or the
+    precision-study variant)."""
     os.makedirs(BUILD, exist_ok=True)
     if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= os.path.getmtime(SRC):
         return LIB
     cmd = ["g++", "-O3", "-fopenmp", "-shared", "-fPIC", "-std=c++17", "-ffp-contract=off", SRC, "-o", LIB + ".tmp"]
+    if VARIANT == "store32":
+        cmd.append("-DORACLE_STORE32")
     subprocess.check_call(cmd)
     os.replace(LIB + ".tmp", LIB)
     return LIB

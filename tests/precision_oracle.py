@@ -1,11 +1,17 @@
 """FP32 against FP64 on the CPU oracle (correctly rounded libm, the reference's formulation)
 after n steps of the production workload (h_elem=30, z_elem=63, dt=120 s): the FP32 error
-floor of the formulation itself, to set beside the GPU's (bench.py `fp32_vs_fp64`).
+floor of the formulation itself, to set beside the GPU's (bench.py `fp32_vs_fp64`).  With
+``--store32`` it also runs the oracle's precision-study build (ORACLE_VARIANT=store32: FP64
+arithmetic with every stored field rounded to FP32, in a child process since the library is
+loaded once per process), which separates the error of FP32 storage from that of FP32
+arithmetic.  Every run starts from the FP32-representable initial state.
 
-    python tests/precision_oracle.py [n_steps]      (~2 minutes for 20 steps on 8 cores)
+    python tests/precision_oracle.py [n_steps] [--store32]   (~1 minute per run of 2 steps on 8 cores)
 """
 import os
+import subprocess
 import sys
+import tempfile
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
@@ -17,19 +23,41 @@ from gbdycore import config as C, setups as S  # noqa: E402
 from helpers import field_errors, make_oracle, oracle_geometry  # noqa: E402
 
 
-def main(n=20):
+def _start():
     cfg = C.production_h30()
     g = oracle_geometry(cfg.with_(ft=np.float64))
     Yc, Yf = S.workload_state(g, cfg.with_(ft=np.float64), "production")
-    o64 = make_oracle(cfg, np.float64, dss_stage1=False)
-    o32 = make_oracle(cfg, np.float32, dss_stage1=False)
-    a = (Yc.copy(), Yf.copy())
-    b = (Yc.astype(np.float32), Yf.astype(np.float32))
-    o64.step(a[0], a[1], cfg.dt, n)
-    o32.step(b[0], b[1], cfg.dt, n)
-    e = field_errors(b[0].astype(np.float64), b[1].astype(np.float64), a[0], a[1])
+    return cfg, Yc.astype(np.float32).astype(np.float64), Yf.astype(np.float32).astype(np.float64)
+
+
+def run(dtype, n):
+    cfg, Yc, Yf = _start()
+    o = make_oracle(cfg, dtype, dss_stage1=False)
+    a = (Yc.astype(dtype), Yf.astype(dtype))
+    o.step(a[0], a[1], cfg.dt, n)
+    return a[0].astype(np.float64), a[1].astype(np.float64)
+
+
+def main(n=20, store32=False):
+    ref = run(np.float64, n)
+    e = field_errors(*run(np.float32, n), *ref)
     print("oracle FP32 vs FP64 after %d steps (max-norm relative): %s" % (n, {k: float(v) for k, v in e.items()}))
+    if store32:
+        with tempfile.TemporaryDirectory() as d:
+            out = os.path.join(d, "store32.npz")
+            env = dict(os.environ, ORACLE_VARIANT="store32")
+            subprocess.check_call([sys.executable, os.path.abspath(__file__), str(n), "--emit", out], env=env)
+            z = np.load(out)
+            e = field_errors(z["c"], z["f"], *ref)
+        print("oracle FP64 arithmetic with FP32 storage vs FP64 after %d steps: %s"
+              % (n, {k: float(v) for k, v in e.items()}))
 
 
 if __name__ == "__main__":
-    main(int(sys.argv[1]) if len(sys.argv) > 1 else 20)
+    args = [a for a in sys.argv[1:] if not a.startswith("--")]
+    n = int(args[0]) if args else 20
+    if "--emit" in sys.argv:
+        c, f = run(np.float64, n)
+        np.savez(sys.argv[sys.argv.index("--emit") + 1], c=c, f=f)
+    else:
+        main(n, "--store32" in sys.argv)

@@ -7,7 +7,7 @@ the file is named ``day{day}.{sec}`` from the elapsed simulation time and holds 
 configuration); a restart warns when the hash differs from the running model's.  The
 container is numpy's ``.npz`` (``Y_c`` centres ``[Nh][4][16][Nv]``, ``Y_f`` faces
 ``[Nh][16][Nv+1]``, the library's layout) instead of ClimaCore's HDF5 (no HDF5 library is
-available to this build), so the files are not interchangeable with the reference's.
+available here), so the files are not interchangeable with the reference's.
 """
 import hashlib
 import json

@@ -1,8 +1,8 @@
 // CPU ORACLE for the ClimaAtmos dry dynamical-core IMEX step.
 //
 // TEST INFRASTRUCTURE ONLY: the parity tests, __graft_entry__.smoke() and the
-// CPU-baseline leg of bench.py use this file as the checker and as the timed
-// CPU port.  Nothing in the product library links or calls it.
+// CPU-baseline leg of bench.py use this file for the results to compare with and
+// as the timed CPU port.  Nothing in the product library links or calls it.
 //
 // Parity status: the reference's arithmetic lives in ClimaCore 0.15.1,
 // ClimaTimeSteppers 0.10.6 and Thermodynamics 1.3.0 (pinned in

@@ -1,7 +1,8 @@
 """ctypes front end of the CPU oracle (``dycore_oracle.cpp``).
 
 TEST INFRASTRUCTURE ONLY: imported by ``tests/``, ``__graft_entry__.smoke()``
-and the CPU-baseline leg of ``bench.py`` as the checker / timed CPU port.  The
+and the CPU-baseline leg of ``bench.py``, as the reference results to compare with and as
+the timed CPU port.  The
 product (``climaatmos.jl_gb300``) never imports it.
 
 Parity status: restated from the reference's call sites and documentation; the

@@ -116,12 +116,34 @@ struct Oracle {
   struct Pre {
     std::vector<FT> ub3, K, T, p, h, Pi, thv, thvr, phir, uc1, uc2, u3c;  // u3c = contravariant u^3 at faces
   } pre;
+#ifdef ORACLE_PHID
+  // per level: the reference pressure p0 = p_ref Pi0^(1/kappa) and Pi0^7, Phi_r(Pi0) = g z_c (Newton, FP64)
+  std::vector<FT> p0v, pi07;
+  void ref_levels() {
+    p0v.resize(Nv);
+    pi07.resize(Nv);
+    const double cp = cpd, tm = Tmin_ref, dT = (double)Tsfc_ref - (double)Tmin_ref;
+    for (int v = 0; v < Nv; ++v) {
+      const double gz = (double)grav * (double)zc[v];
+      double P = 1.0;
+      for (int it = 0; it < 60; ++it) {
+        const double f = -cp * (tm * std::log(P) + dT / 7.0 * (std::pow(P, 7.0) - 1.0)) - gz;
+        P -= f / (-cp * (tm / P + dT * std::pow(P, 6.0)));
+      }
+      p0v[v] = (FT)((double)pref * std::pow(P, 1.0 / (double)kappa));
+      pi07[v] = (FT)std::pow(P, 7.0);
+    }
+  }
+#endif
 
   void alloc_pre() {
     size_t P = npt();
     for (auto *v : {&pre.ub3, &pre.K, &pre.T, &pre.p, &pre.h, &pre.Pi, &pre.thv, &pre.thvr, &pre.phir, &pre.uc1, &pre.uc2})
       v->assign(P, FT(0));
     pre.u3c.assign(nfac(), FT(0));
+#ifdef ORACLE_PHID
+    ref_levels();
+#endif
   }
 
   // impenetrable-boundary filter: u_3 = -u_h^3 / g^33 at the bottom and top
@@ -166,7 +188,15 @@ struct Oracle {
           pre.Pi[q] = Pi;
           pre.thv[q] = T / Pi;
           pre.thvr[q] = T_ref(Pi) / Pi;
+#ifdef ORACLE_PHID
+          // precision-study build: phir holds the deviation g z - Phi_r(Pi), formed from the
+          // level's reference Exner Pi0 (Phi_r(Pi0) = g z) so that no O(1e5) terms cancel:
+          // g z - Phi_r(Pi) = cp (T_min ln x + (T_sfc - T_min) / 7 Pi0^7 (x^7 - 1)), x = Pi / Pi0
+          FT lx = kappa * std::log1p((p - p0v[v]) / p0v[v]);
+          pre.phir[q] = cpd * (Tmin_ref * lx + (Tsfc_ref - Tmin_ref) / FT(7) * pi07[v] * std::expm1(FT(7) * lx));
+#else
           pre.phir[q] = phi_r(Pi);
+#endif
         }
       }
   }
@@ -376,7 +406,11 @@ struct Oracle {
         FT Pi[NN], thp[NN], b1[NN], b2[NN], c1[NN], c2[NN], d1_[NN], d2_[NN];
         for (int n = 0; n < NN; ++n) {
           size_t q = pi(e, n, v);
+#ifdef ORACLE_PHID
+          tmp[n] = pre.K[q] + pre.phir[q];
+#else
           tmp[n] = pre.K[q] + grav * zc[v] - pre.phir[q];
+#endif
           Pi[n] = pre.Pi[q];
           thp[n] = pre.thv[q] - pre.thvr[q];
         }
@@ -396,7 +430,11 @@ struct Oracle {
         FT sd[NN], g1[NN], g2[NN], Ls[NN];
         for (int n = 0; n < NN; ++n) {
           size_t q = pi(e, n, v);
+#ifdef ORACLE_PHID
+          sd[n] = cpd * (pre.T[q] - T_ref(pre.Pi[q])) + pre.phir[q];
+#else
           sd[n] = cpd * (pre.T[q] - T0) + grav * zc[v] - sd_r(pre.Pi[q]);
+#endif
         }
         grad_h(sd, g1, g2);
         for (int n = 0; n < NN; ++n) {
@@ -583,8 +621,12 @@ struct Oracle {
           FT val = 0;
           if (k > 0 && k < Nv) {
             size_t a = pi(e, n, k - 1), b = pi(e, n, k);
+#ifdef ORACLE_PHID
+            FT gPhi = pre.phir[b] - pre.phir[a], gPhir = 0;
+#else
             FT gPhi = grav * (zc[k] - zc[k - 1]);
             FT gPhir = pre.phir[b] - pre.phir[a];
+#endif
             FT thd = ((pre.thv[a] - pre.thvr[a]) + (pre.thv[b] - pre.thvr[b])) / FT(2);
             FT gPi = pre.Pi[b] - pre.Pi[a];
             val = -(gPhi - gPhir + cpd * thd * gPi);

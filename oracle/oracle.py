@@ -18,13 +18,15 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD = os.path.join(HERE, "_build")
-# ORACLE_VARIANT=store32 selects the precision-study build (ORACLE_STORE32 in dycore_oracle.cpp:
-# every field the step stores is rounded to FP32, the arithmetic stays in the oracle's type);
-# unset, the oracle is the default build.
+# ORACLE_VARIANT selects a precision-study build of dycore_oracle.cpp: "store32" (ORACLE_STORE32:
+# every field the step stores is rounded to FP32, the arithmetic stays in the oracle's type) or
+# "phid" (ORACLE_PHID: g z - Phi_r formed as a deviation from per-level reference values, the
+# same mathematics without the O(1e5) cancellation); unset, the oracle is the default build.
 VARIANT = os.environ.get("ORACLE_VARIANT", "")
-if VARIANT not in ("", "store32"):
-    raise ValueError("ORACLE_VARIANT must be unset or 'store32'")
-LIB = os.path.join(BUILD, "liboracle_store32.so" if VARIANT else "liboracle.so")
+_FLAGS = {"": [], "store32": ["-DORACLE_STORE32"], "phid": ["-DORACLE_PHID"]}
+if VARIANT not in _FLAGS:
+    raise ValueError("ORACLE_VARIANT must be unset, 'store32' or 'phid'")
+LIB = os.path.join(BUILD, "liboracle_%s.so" % VARIANT if VARIANT else "liboracle.so")
 SRC = os.path.join(HERE, "dycore_oracle.cpp")
 
 
@@ -35,8 +37,7 @@ def build(force=False):
     if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= os.path.getmtime(SRC):
         return LIB
     cmd = ["g++", "-O3", "-fopenmp", "-shared", "-fPIC", "-std=c++17", "-ffp-contract=off", SRC, "-o", LIB + ".tmp"]
-    if VARIANT == "store32":
-        cmd.append("-DORACLE_STORE32")
+    cmd += _FLAGS[VARIANT]
     subprocess.check_call(cmd)
     os.replace(LIB + ".tmp", LIB)
     return LIB

@@ -1,12 +1,13 @@
 """FP32 against FP64 on the CPU oracle (correctly rounded libm, the reference's formulation)
 after n steps of the production workload (h_elem=30, z_elem=63, dt=120 s): the FP32 error
-floor of the formulation itself, to set beside the GPU's (bench.py `fp32_vs_fp64`).  With
-``--store32`` it also runs the oracle's precision-study build (ORACLE_VARIANT=store32: FP64
-arithmetic with every stored field rounded to FP32, in a child process since the library is
-loaded once per process), which separates the error of FP32 storage from that of FP32
-arithmetic.  Every run starts from the FP32-representable initial state.
+floor of the formulation itself, to set beside the GPU's (bench.py `fp32_vs_fp64`).  The
+oracle's precision-study builds run in child processes (the library is loaded once per
+process): ``--store32`` (ORACLE_VARIANT=store32) is FP64 arithmetic with every stored field
+rounded to FP32, which separates the error of FP32 storage from that of FP32 arithmetic;
+``--phid`` (ORACLE_VARIANT=phid) is FP32 with g z - Phi_r formed as a deviation from
+per-level reference values.  Every run starts from the FP32-representable initial state.
 
-    python tests/precision_oracle.py [n_steps] [--store32]   (~1 minute per run of 2 steps on 8 cores)
+    python tests/precision_oracle.py [n_steps] [--store32] [--phid]   (~1 minute per run of 2 steps on 8 cores)
 """
 import os
 import subprocess
@@ -38,18 +39,26 @@ def run(dtype, n):
     return a[0].astype(np.float64), a[1].astype(np.float64)
 
 
-def main(n=20, store32=False):
+def _child(variant, dtype, n):
+    with tempfile.TemporaryDirectory() as d:
+        out = os.path.join(d, "run.npz")
+        env = dict(os.environ, ORACLE_VARIANT=variant)
+        subprocess.check_call([sys.executable, os.path.abspath(__file__), str(n), "--emit", out, dtype], env=env)
+        z = np.load(out)
+        return z["c"], z["f"]
+
+
+def main(n=20, store32=False, phid=False):
     ref = run(np.float64, n)
     e = field_errors(*run(np.float32, n), *ref)
     print("oracle FP32 vs FP64 after %d steps (max-norm relative): %s" % (n, {k: float(v) for k, v in e.items()}))
     if store32:
-        with tempfile.TemporaryDirectory() as d:
-            out = os.path.join(d, "store32.npz")
-            env = dict(os.environ, ORACLE_VARIANT="store32")
-            subprocess.check_call([sys.executable, os.path.abspath(__file__), str(n), "--emit", out], env=env)
-            z = np.load(out)
-            e = field_errors(z["c"], z["f"], *ref)
+        e = field_errors(*_child("store32", "float64", n), *ref)
         print("oracle FP64 arithmetic with FP32 storage vs FP64 after %d steps: %s"
+              % (n, {k: float(v) for k, v in e.items()}))
+    if phid:
+        e = field_errors(*_child("phid", "float32", n), *ref)
+        print("oracle FP32 with g z - Phi_r as a deviation vs FP64 after %d steps: %s"
               % (n, {k: float(v) for k, v in e.items()}))
 
 
@@ -57,7 +66,8 @@ if __name__ == "__main__":
     args = [a for a in sys.argv[1:] if not a.startswith("--")]
     n = int(args[0]) if args else 20
     if "--emit" in sys.argv:
-        c, f = run(np.float64, n)
-        np.savez(sys.argv[sys.argv.index("--emit") + 1], c=c, f=f)
+        i = sys.argv.index("--emit")
+        c, f = run(np.dtype(sys.argv[i + 2]).type, n)
+        np.savez(sys.argv[i + 1], c=c, f=f)
     else:
-        main(n, "--store32" in sys.argv)
+        main(n, "--store32" in sys.argv, "--phid" in sys.argv)

@@ -140,6 +140,45 @@ function global_sums(Y, p)
     return out
 end
 
+"""Sums of squares of the Newton residuals (ρ, ρe_tot, u₃) of the last step; throws if a kernel
+flagged a non-finite residual or a device wait that timed out."""
+function newton_residual(p)
+    out = zeros(Cdouble, 3)
+    check(p.gb, ccall((:gb_newton_residual, libgbdycore), Cint, (Ptr{Cvoid}, Ptr{Cdouble}), p.gb.handle, out))
+    return out
+end
+
+"""What `solve_atmos!` returns (src/simulation/solve.jl:93-97)."""
+struct AtmosSolveResults{S, W}
+    sol::S
+    ret_code::Symbol
+    walltime::W
+end
+
+"""
+    solve_atmos!(Y, p, t, dt, nsteps; save_state = nothing)
+
+One untimed step, then `nsteps` timed fused steps (src/simulation/solve.jl:119-149).  A library
+error ends the run as the reference's catch does: `save_state(Y)` is called when given, and the
+results carry `:simulation_crashed`.
+"""
+function solve_atmos!(Y, p, t, dt, nsteps; save_state = nothing)
+    try
+        step!(Y, p, t, dt, 1)
+        CUDA.synchronize()
+        walltime = @elapsed begin
+            step!(Y, p, t + dt, dt, nsteps)
+            CUDA.synchronize()
+        end
+        newton_residual(p)
+        return AtmosSolveResults(Y, :success, walltime)
+    catch err
+        isnothing(save_state) || save_state(Y)
+        @error "simulation crashed" exception = (err, catch_backtrace())
+        return AtmosSolveResults(nothing, :simulation_crashed, nothing)
+    end
+end
+
 # ---- reverse mode (the pullback halves of ChainRulesCore.rrule(solve!, ...)) ----
 
 """Advance Y by n fused steps (gb_step with graph replay)."""

@@ -43,6 +43,7 @@ def parse(argv=None):
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--plain-steps", type=int, default=3)
     ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--no-config1", action="store_true")
     ap.add_argument("--precision-steps", type=int, default=20)
     ap.add_argument("--no-precision", action="store_true")
     ap.add_argument("--batch-columns", type=int, default=20000)
@@ -363,6 +364,12 @@ def run_gb300(args):
     held_suarez = None
     if not args.no_held_suarez:
         held_suarez = measure_held_suarez(args, ms)
+    config1 = None
+    if not args.no_config1:
+        try:
+            config1 = measure_config1(args, rank == 0 and world == 1 and not args.no_cpu_baseline)
+        except Exception as e:  # reported in the line, not fatal to the headline
+            config1 = {"error": "%s: %s" % (type(e).__name__, e)}
 
     adjoint = None
     if not args.no_adjoint:
@@ -397,6 +404,7 @@ def run_gb300(args):
                             "post-Newton correction, DSS) with unfused torch stage algebra"},
                 "fp32_vs_fp64": prec, "batching": batching, "adjoint": adjoint,
                 "differentiation": differentiation, "precision_h60": h60, "held_suarez": held_suarez,
+                "config1": config1,
                 "clocks": clk, "gpu_launches": LAUNCHES_PER_STEP * args.steps}
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -550,6 +558,40 @@ def max_horizontal_wind(s):
     u2 = s.Y.c[:, 2].double()
     q = (gup[..., 0:1] * u1 * u1 + 2 * gup[..., 1:2] * u1 * u2 + gup[..., 2:3] * u2 * u2) / r2
     return float(q.clamp_min(0).sqrt().max().item())
+
+
+def measure_config1(args, with_cpu):
+    """The reference's CPU-runnable case (h_elem=6, z_elem=10 uniform to 30 km, dt=400 s, FP32):
+    its steps graph-replayed on the GPU (the 0.7 MB state stays in L2: launch- and latency-bound)
+    and, as this case's CPU baseline, the C++ port of the same steps on the host cores."""
+    import torch
+    from gbdycore import config as C, simulation as sim
+    cfg = C.plain_h6()
+    s = sim.AtmosSimulation(cfg, workload="plain")
+    s.step(3)
+    torch.cuda.synchronize()
+    n, reps = 10, 20
+    ms, _ = _timed(lambda: [s.step(n) for _ in range(reps)])
+    ms /= n * reps
+    out = {"workload": "h_elem=6, z_elem=10 uniform to 30 km, dt=400 s, FP32, %d-step runs" % n,
+           "ms_per_step": ms, "value": sypd(cfg.dt, ms / 1e3), "unit": UNIT,
+           "finite": bool(torch.isfinite(s.Y.c).all() and torch.isfinite(s.Y.f).all())}
+    if with_cpu:
+        from geometry import OracleGeometry
+        import oracle as O
+        from gbdycore import setups as S
+        g = OracleGeometry(cfg.h_elem, cfg.z_elem, cfg.z_max, cfg.z_stretch, cfg.dz_bottom)
+        Yc, Yf = S.workload_state(g, cfg, "plain")
+        o = O.Oracle(g, cfg.oracle_params(), np.float32)
+        Yc, Yf = Yc.astype(np.float32), Yf.astype(np.float32)
+        o.step(Yc, Yf, cfg.dt, 1)
+        t0 = time.perf_counter()
+        o.step(Yc, Yf, cfg.dt, n)
+        sec = (time.perf_counter() - t0) / n
+        out["cpu_baseline"] = {"value": sypd(cfg.dt, sec), "unit": UNIT, "ms_per_step": sec * 1e3,
+                               "cores": O.max_threads(), "kind": "port",
+                               "sample": "%d steps after 1 warm-up, C++ port of the reference step (FP32, OpenMP)" % n}
+    return out
 
 
 def measure_held_suarez(args, fwd_ms):

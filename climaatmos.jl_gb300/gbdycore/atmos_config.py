@@ -23,7 +23,7 @@ DEFAULTS = {
     "divergence_damping_factor": 5.0, "rayleigh_sponge": False, "energy_q_tot_upwinding": "vanleer_limiter",
     "rad": None, "deep_atmosphere": True, "ode_algo": "ARS343", "max_newton_iters_ode": 1,
     "use_newton_rtol": False, "output_dir": None, "restart_file": None, "detect_restart_file": False,
-    "initial_condition": "DecayingProfile",
+    "initial_condition": "DecayingProfile", "dt_save_state_to_disk": "Inf",
 }
 
 # Options whose effective value (the job's, else the reference's default, listed first) must
@@ -39,7 +39,7 @@ REQUIRED = {
 }
 
 # Options that only concern output, logging or the host run and are accepted as given.
-HOST_ONLY = {"job_id", "output_dir_style", "dt_save_state_to_disk", "dt_save_to_sol", "log_progress",
+HOST_ONLY = {"job_id", "output_dir_style", "dt_save_to_sol", "log_progress",
              "diagnostics", "netcdf_interpolation_num_points", "output_default_diagnostics",
              "check_conservation", "check_nan_every", "log_to_file", "reproducible_restart",
              "use_itime", "start_date", "toml"}
@@ -62,6 +62,16 @@ def time_to_seconds(s):
     factor = {"s": 1, "secs": 1, "m": 60, "mins": 60, "h": 3600, "hours": 3600, "d": 86400, "days": 86400,
               "weeks": 604800}[m.group(2)]
     return float(m.group(1)) * factor
+
+
+def parse_checkpoint_frequency(period):
+    """Seconds between checkpoints, ``inf`` for none (src/callbacks/get_callbacks.jl:231-247): a
+    number is seconds, a string anything time_to_seconds reads; ``<N>months`` needs the
+    calendar, which this library does not keep (ValueError)."""
+    if isinstance(period, str) and "months" in period:
+        raise ValueError("checkpoint frequency %r: calendar months are not supported" % period)
+    sec = time_to_seconds(period)
+    return sec if math.isinf(sec) else float(round(sec))
 
 
 def _scalar(text):
@@ -180,4 +190,5 @@ def from_atmos_config(options, params=None):
         alpha_uh=a_uh, alpha_w=a_w, upwinding="vanleer" if o["energy_q_tot_upwinding"] == "vanleer_limiter" else "none",
         constants=constants, held_suarez=o["rad"] == "held_suarez")
     host = {k: o.get(k) for k in ("output_dir", "restart_file", "detect_restart_file", "initial_condition")}
+    host["dt_save_state_to_disk"] = parse_checkpoint_frequency(o["dt_save_state_to_disk"])
     return cfg, time_to_seconds(o["t_end"]), host

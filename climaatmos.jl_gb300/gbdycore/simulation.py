@@ -18,6 +18,7 @@ provides device memory, streams and the elementwise stage algebra of the
 hook-level loop.
 """
 import ctypes
+import math
 import time
 
 import numpy as np
@@ -255,9 +256,10 @@ class AtmosSimulation:
     """State + cache + time of one dry dynamical-core run on the GPU."""
 
     def __init__(self, config, workload="plain", state=None, device="cuda", restart_file=None,
-                 detect_restart_file=False, output_dir=None, t_end=None):
+                 detect_restart_file=False, output_dir=None, t_end=None, dt_save_state_to_disk=None):
         self.config = config
         self.t_end = t_end
+        self.dt_save_state_to_disk = dt_save_state_to_disk  # seconds between checkpoints, None / inf: none
         self.geometry = Geometry(config)
         self.t = 0.0
         if restart_file is None and detect_restart_file and output_dir is not None:
@@ -321,11 +323,27 @@ def solve_atmos(sim, nsteps=None, use_graph=True):
         nsteps = int(round((sim.t_end - sim.t) / sim.dt)) - 1
         if nsteps < 0:
             raise ValueError("solve_atmos: t_end is less than one step ahead")
+    every = getattr(sim, "dt_save_state_to_disk", None)
+    every = None if every is None or math.isinf(every) else max(1, int(round(every / sim.dt)))
+    if every and not getattr(sim, "output_dir", None):
+        raise ValueError("solve_atmos: dt_save_state_to_disk needs an output_dir")
+
+    def steps(n):
+        # in runs of steps that end on the checkpoint times (every `every` steps from t = 0),
+        # where the state is written (save_state_to_disk_func, src/callbacks/callbacks.jl:297-321)
+        while n > 0:
+            k = n if not every else min(n, every - int(round(sim.t / sim.dt)) % every)
+            sim.step(k, use_graph)
+            n -= k
+            if every and int(round(sim.t / sim.dt)) % every == 0:
+                sim.synchronize()
+                sim.save_state(sim.output_dir)
+
     try:
-        sim.step(1, use_graph)
+        steps(1)
         sim.synchronize()
         t0 = time.perf_counter()
-        sim.step(nsteps, use_graph)
+        steps(nsteps)
         sim.synchronize()
         wall = time.perf_counter() - t0
         sim.check()

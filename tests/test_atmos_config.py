@@ -45,7 +45,7 @@ def test_defaults_and_hyperdiffusion_scaling():
     h = math.sqrt(4 * math.pi / 6) * 6.371229e6 / 90
     assert c30.nu == pytest.approx(0.1857 * h ** 3, rel=1e-12) and c30.nu == pytest.approx(2.0e14, rel=2e-3)
     assert host == {"output_dir": None, "restart_file": None, "detect_restart_file": False,
-                    "initial_condition": "DecayingProfile"}
+                    "initial_condition": "DecayingProfile", "dt_save_state_to_disk": math.inf}
 
 
 def test_held_suarez_job():
@@ -96,3 +96,13 @@ def test_unimplemented_options_are_refused_by_name(opt):
         A.from_atmos_config(job)
     key = next(iter(opt)) if opt else "disable_surface_flux_tendency"
     assert key in str(e.value)
+
+
+def test_checkpoint_frequency():
+    # src/callbacks/get_callbacks.jl:231-247
+    p = A.parse_checkpoint_frequency
+    assert p("2days") == 172800.0 and p(3600) == 3600.0 and p(90.4) == 90.0 and math.isinf(p("Inf"))
+    with pytest.raises(ValueError, match="months"):
+        p("2months")
+    _, _, host = A.from_atmos_config({"disable_surface_flux_tendency": True, "dt_save_state_to_disk": "1hours"})
+    assert host["dt_save_state_to_disk"] == 3600.0

@@ -9,15 +9,16 @@ from gbdycore import simulation as sim
 
 
 class FakeSim:
-    def __init__(self, fail_check=False, fail_step=False, output_dir=None, t=0.0, t_end=None):
+    def __init__(self, fail_check=False, fail_step=False, output_dir=None, t=0.0, t_end=None, every=None):
         self.steps, self.saved, self.dt, self.Y = [], [], 120.0, object()
-        self.t, self.t_end = t, t_end
+        self.t, self.t_end, self.dt_save_state_to_disk = t, t_end, every
         self.fail_check, self.fail_step, self.output_dir = fail_check, fail_step, output_dir
 
     def step(self, n, use_graph=True):
         if self.fail_step:
             raise N.GBError(N.GB_ERR_TIMEOUT, "a device wait gave up")
         self.steps.append(n)
+        self.t += n * self.dt
 
     def synchronize(self):
         pass
@@ -27,7 +28,7 @@ class FakeSim:
             raise N.GBError(N.GB_ERR_NONFINITE, "non-finite Newton residual")
 
     def save_state(self, d):
-        self.saved.append(d)
+        self.saved.append((d, self.t))
 
 
 def test_success_record():
@@ -46,7 +47,7 @@ def test_crash_saves_state_and_reports(kw, tmp_path):
     with pytest.warns(UserWarning, match="simulation crashed"):
         r = sim.solve_atmos(s, 5)
     assert r.ret_code == "simulation_crashed" and r.sol is None and r.walltime is None
-    assert s.saved == [str(tmp_path)]
+    assert [d for d, _ in s.saved] == [str(tmp_path)]
 
 
 def test_crash_without_output_dir_saves_nothing():
@@ -64,3 +65,14 @@ def test_runs_to_t_end():
         sim.solve_atmos(FakeSim())
     with pytest.raises(ValueError):
         sim.solve_atmos(FakeSim(t=100.0, t_end=100.0))
+
+
+def test_checkpoints_on_schedule(tmp_path):
+    # every 600 s = 5 steps of 120 s from t = 0: the warm-up step, then runs ending on t = 600, 1200
+    s = FakeSim(output_dir=str(tmp_path), every=600.0)
+    assert sim.solve_atmos(s, 12).ret_code == "success"
+    assert s.steps == [1, 4, 5, 3]
+    assert [t for _, t in s.saved] == [600.0, 1200.0]
+    assert sim.solve_atmos(FakeSim(output_dir=str(tmp_path), every=float("inf")), 3).ret_code == "success"
+    with pytest.raises(ValueError, match="output_dir"):
+        sim.solve_atmos(FakeSim(every=600.0), 3)

@@ -23,7 +23,7 @@ DEFAULTS = {
     "divergence_damping_factor": 5.0, "rayleigh_sponge": False, "energy_q_tot_upwinding": "vanleer_limiter",
     "rad": None, "deep_atmosphere": True, "ode_algo": "ARS343", "max_newton_iters_ode": 1,
     "use_newton_rtol": False, "output_dir": None, "restart_file": None, "detect_restart_file": False,
-    "initial_condition": "DecayingProfile", "dt_save_state_to_disk": "Inf",
+    "initial_condition": "DecayingProfile", "dt_save_state_to_disk": "Inf", "check_nan_every": 1024,
 }
 
 # Options whose effective value (the job's, else the reference's default, listed first) must
@@ -41,7 +41,7 @@ REQUIRED = {
 # Options that only concern output, logging or the host run and are accepted as given.
 HOST_ONLY = {"job_id", "output_dir_style", "dt_save_to_sol", "log_progress",
              "diagnostics", "netcdf_interpolation_num_points", "output_default_diagnostics",
-             "check_conservation", "check_nan_every", "log_to_file", "reproducible_restart",
+             "check_conservation", "log_to_file", "reproducible_restart",
              "use_itime", "start_date", "toml"}
 
 # CAM-SE preset (src/types.jl:517-522): the hyperviscosity of Lauritzen et al. (2018).
@@ -191,4 +191,5 @@ def from_atmos_config(options, params=None):
         constants=constants, held_suarez=o["rad"] == "held_suarez")
     host = {k: o.get(k) for k in ("output_dir", "restart_file", "detect_restart_file", "initial_condition")}
     host["dt_save_state_to_disk"] = parse_checkpoint_frequency(o["dt_save_state_to_disk"])
+    host["check_nan_every"] = int(o["check_nan_every"])
     return cfg, time_to_seconds(o["t_end"]), host

@@ -256,10 +256,12 @@ class AtmosSimulation:
     """State + cache + time of one dry dynamical-core run on the GPU."""
 
     def __init__(self, config, workload="plain", state=None, device="cuda", restart_file=None,
-                 detect_restart_file=False, output_dir=None, t_end=None, dt_save_state_to_disk=None):
+                 detect_restart_file=False, output_dir=None, t_end=None, dt_save_state_to_disk=None,
+                 check_nan_every=None):
         self.config = config
         self.t_end = t_end
         self.dt_save_state_to_disk = dt_save_state_to_disk  # seconds between checkpoints, None / inf: none
+        self.check_nan_every = check_nan_every              # steps between NaN scans of the state, None: none
         self.geometry = Geometry(config)
         self.t = 0.0
         if restart_file is None and detect_restart_file and output_dir is not None:
@@ -289,6 +291,13 @@ class AtmosSimulation:
     def synchronize(self):
         import torch
         torch.cuda.synchronize()
+
+    def check_nans(self):
+        """Raise GBError if the state holds a NaN (check_nans, src/callbacks/callbacks.jl:420-438)."""
+        import torch
+        bad = [n for n, x in (("c", self.Y.c), ("f", self.Y.f)) if bool(torch.isnan(x).any())]
+        if bad:
+            raise N.GBError(N.GB_ERR_NONFINITE, "Found NaN in " + ", ".join("Y." + b for b in bad))
 
     def check(self):
         """Raise GBError if a kernel of the steps so far flagged a failure (a non-finite Newton
@@ -327,15 +336,21 @@ def solve_atmos(sim, nsteps=None, use_graph=True):
     every = None if every is None or math.isinf(every) else max(1, int(round(every / sim.dt)))
     if every and not getattr(sim, "output_dir", None):
         raise ValueError("solve_atmos: dt_save_state_to_disk needs an output_dir")
+    nan_every = getattr(sim, "check_nan_every", None) or None
 
     def steps(n):
-        # in runs of steps that end on the checkpoint times (every `every` steps from t = 0),
-        # where the state is written (save_state_to_disk_func, src/callbacks/callbacks.jl:297-321)
+        # in runs of steps that end on the callbacks' steps (multiples from t = 0): the NaN scan
+        # every `nan_every` steps, then the restart file every `every` steps
+        # (save_state_to_disk_func, src/callbacks/callbacks.jl:297-321)
         while n > 0:
-            k = n if not every else min(n, every - int(round(sim.t / sim.dt)) % every)
+            i = int(round(sim.t / sim.dt))
+            k = min([n] + [p - i % p for p in (every, nan_every) if p])
             sim.step(k, use_graph)
             n -= k
-            if every and int(round(sim.t / sim.dt)) % every == 0:
+            i = int(round(sim.t / sim.dt))
+            if nan_every and i % nan_every == 0:
+                sim.check_nans()
+            if every and i % every == 0:
                 sim.synchronize()
                 sim.save_state(sim.output_dir)
 

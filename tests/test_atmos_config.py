@@ -45,7 +45,8 @@ def test_defaults_and_hyperdiffusion_scaling():
     h = math.sqrt(4 * math.pi / 6) * 6.371229e6 / 90
     assert c30.nu == pytest.approx(0.1857 * h ** 3, rel=1e-12) and c30.nu == pytest.approx(2.0e14, rel=2e-3)
     assert host == {"output_dir": None, "restart_file": None, "detect_restart_file": False,
-                    "initial_condition": "DecayingProfile", "dt_save_state_to_disk": math.inf}
+                    "initial_condition": "DecayingProfile", "dt_save_state_to_disk": math.inf,
+                    "check_nan_every": 1024}
 
 
 def test_held_suarez_job():

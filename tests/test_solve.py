@@ -9,9 +9,11 @@ from gbdycore import simulation as sim
 
 
 class FakeSim:
-    def __init__(self, fail_check=False, fail_step=False, output_dir=None, t=0.0, t_end=None, every=None):
-        self.steps, self.saved, self.dt, self.Y = [], [], 120.0, object()
+    def __init__(self, fail_check=False, fail_step=False, output_dir=None, t=0.0, t_end=None, every=None,
+                 nan_every=None, nan_at=None):
+        self.steps, self.saved, self.scans, self.dt, self.Y = [], [], [], 120.0, object()
         self.t, self.t_end, self.dt_save_state_to_disk = t, t_end, every
+        self.check_nan_every, self.nan_at = nan_every, nan_at
         self.fail_check, self.fail_step, self.output_dir = fail_check, fail_step, output_dir
 
     def step(self, n, use_graph=True):
@@ -22,6 +24,11 @@ class FakeSim:
 
     def synchronize(self):
         pass
+
+    def check_nans(self):
+        self.scans.append(self.t)
+        if self.nan_at is not None and self.t >= self.nan_at:
+            raise N.GBError(N.GB_ERR_NONFINITE, "Found NaN in Y.c")
 
     def check(self):
         if self.fail_check:
@@ -76,3 +83,15 @@ def test_checkpoints_on_schedule(tmp_path):
     assert sim.solve_atmos(FakeSim(output_dir=str(tmp_path), every=float("inf")), 3).ret_code == "success"
     with pytest.raises(ValueError, match="output_dir"):
         sim.solve_atmos(FakeSim(every=600.0), 3)
+
+
+def test_nan_scans_on_schedule_end_a_crashed_run(tmp_path):
+    s = FakeSim(output_dir=str(tmp_path), nan_every=4, every=600.0)
+    assert sim.solve_atmos(s, 11).ret_code == "success"
+    assert s.steps == [1, 3, 1, 3, 2, 2]          # runs end on steps 1, 4, 5, 8, 10, 12
+    assert s.scans == [480.0, 960.0, 1440.0] and [t for _, t in s.saved] == [600.0, 1200.0]
+    s = FakeSim(output_dir=str(tmp_path), nan_every=4, nan_at=900.0)
+    with pytest.warns(UserWarning, match="Found NaN"):
+        r = sim.solve_atmos(s, 11)
+    assert r.ret_code == "simulation_crashed" and s.scans == [480.0, 960.0]
+    assert [t for _, t in s.saved] == [960.0]   # the crashed state

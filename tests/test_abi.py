@@ -4,7 +4,6 @@ import os
 import re
 
 import numpy as np
-import pytest
 
 from gbdycore import _native as N
 from gbdycore import config as C

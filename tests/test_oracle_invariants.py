@@ -20,7 +20,7 @@ import pytest
 
 from gbdycore import config as C
 from gbdycore.simulation import ars343_tableau
-from helpers import make_oracle, oracle_geometry, perturbed_state, small_config, state
+from helpers import make_oracle, oracle_geometry, perturbed_state, small_config
 
 
 def test_ars343_order_conditions():

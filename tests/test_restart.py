@@ -9,7 +9,6 @@ import warnings
 import numpy as np
 import pytest
 
-from gbdycore import config as C
 from gbdycore import restart as R
 from helpers import perturbed_state, small_config
 

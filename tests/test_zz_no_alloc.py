@@ -9,7 +9,6 @@ in a row (the second call reuses the array the first one left behind), within
 the tolerance the other GPU tests use, and checks the size limit.  It lives in
 its own file so that pytest collects it last.
 """
-import ctypes
 
 import numpy as np
 import pytest

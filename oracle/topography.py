@@ -127,3 +127,54 @@ def warped_faces(zf_flat, z_surface, warp):
     z_top = float(zf_flat[-1])
     zs = np.asarray(z_surface, dtype=np.float64)[..., None]
     return warp(zf_flat, zs, z_top)
+
+
+# ---------------------------------------------------------------- terrain-following geometry
+def warped_geometry(g, z_surface, warp):
+    """Local geometry of the terrain-following grid over the oracle's cubed sphere ``g``
+    (an OracleGeometry), restated from the mathematics (ClimaCore computes it for the
+    reference and is not vendored): the position is X = (R + z) x_hat with
+    z = warp(zeta, z_s) on the flat faces zeta, so the covariant basis is
+
+        E_i = (R + z) / R e_i + (dz/dxi^i) x_hat   (i = 1, 2; e_i the surface basis),
+        E_3 = dz x_hat                              (dz: the cell's warped thickness; at a face
+                                                     the distance between the centres around it),
+
+    with dz/dxi^i the spectral (GLL) derivative of the warped heights of each level in its
+    element and the centre heights the midpoints of the warped faces.  Returns a dict of numpy
+    arrays: ``zf`` [Nh, 16, Nf] and ``zc`` [Nh, 16, Nv] heights, ``Jc``/``Jf`` the Jacobians
+    E_3 . (E_1 x E_2), and ``gup_c``/``gup_f`` [..., 3, 3] the contravariant metric (the inverse
+    of E_i . E_j), with ``Ec``/``Ef`` [..., 3, 3] the covariant basis (row i = E_i)."""
+    R = g.R
+    zs = np.asarray(z_surface, dtype=np.float64)
+    zf = warped_faces(g.zf, zs, warp)                                # [Nh, 16, Nf]
+    zc = 0.5 * (zf[..., 1:] + zf[..., :-1])
+    dzc = zf[..., 1:] - zf[..., :-1]
+    dzf = np.empty_like(zf)
+    dzf[..., 1:-1] = zc[..., 1:] - zc[..., :-1]
+    dzf[..., 0], dzf[..., -1] = dzc[..., 0], dzc[..., -1]
+    D = g.D
+    NQ = D.shape[0]
+
+    def dxi(z):
+        # [Nh, 16, L] -> d/dxi^1 and d/dxi^2 at every node (node n = i + NQ j)
+        zz = z.reshape(z.shape[0], NQ, NQ, -1)                      # [e, j, i, L]
+        d1 = np.einsum("ik,ejkl->ejil", D, zz).reshape(z.shape)
+        d2 = np.einsum("jk,ekil->ejil", D, zz).reshape(z.shape)
+        return d1, d2
+
+    def basis(z, dz):
+        r = (R + z) / R
+        d1, d2 = dxi(z)
+        xh = g.xyz[:, :, None, :]
+        E = np.empty(z.shape + (3, 3))
+        E[..., 0, :] = r[..., None] * g.ecov[:, :, None, 0, :] + d1[..., None] * xh
+        E[..., 1, :] = r[..., None] * g.ecov[:, :, None, 1, :] + d2[..., None] * xh
+        E[..., 2, :] = dz[..., None] * xh
+        gdn = np.einsum("...ik,...jk->...ij", E, E)
+        J = np.einsum("...k,...k->...", E[..., 2, :], np.cross(E[..., 0, :], E[..., 1, :]))
+        return E, J, np.linalg.inv(gdn)
+
+    Ec, Jc, gup_c = basis(zc, dzc)
+    Ef, Jf, gup_f = basis(zf, dzf)
+    return dict(zf=zf, zc=zc, Jc=Jc, Jf=Jf, gup_c=gup_c, gup_f=gup_f, Ec=Ec, Ef=Ef)

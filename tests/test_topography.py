@@ -75,3 +75,65 @@ def test_sleve_flat_above_eta_and_refuses_high_terrain():
     assert np.all(Z[zf / 1000.0 < 0.5] > zf[zf / 1000.0 < 0.5])
     with pytest.raises(ValueError):
         T.warped_faces(zf, np.array([2500.0]), T.SLEVEWarp(eta=0.5, s=2.0))
+
+
+# ---------------------------------------------------------------- terrain-following geometry
+def _grid(h=4, z=8):
+    g = OracleGeometry(h, z, 30000.0, True, 300.0)
+    return g, T.dcmip200(np.degrees(g.lat), np.degrees(g.lon))
+
+
+def test_flat_surface_reproduces_the_flat_geometry():
+    g, _ = _grid(2, 4)
+    G = T.warped_geometry(g, np.zeros((g.Nh, 16)), T.LinearWarp())
+    Jc = g.Jh[:, :, None] * (g.rc ** 2 * g.dzc)[None, None, :]
+    Jf = g.Jh[:, :, None] * (g.rf ** 2 * g.dzf)[None, None, :]
+    np.testing.assert_allclose(G["Jc"], Jc, rtol=1e-13)
+    np.testing.assert_allclose(G["Jf"], Jf, rtol=1e-13)
+    gu = G["gup_f"]
+    np.testing.assert_allclose(gu[..., 2, 2], np.broadcast_to(1 / g.dzf ** 2, gu.shape[:3]), rtol=1e-12)
+    assert np.abs(gu[..., 2, :2]).max() < 1e-14 * np.abs(gu[..., 2, 2]).max()
+    scale = np.abs(gu[..., 0, 0]).max()
+    for (a, b), c in (((0, 0), 0), ((0, 1), 1), ((1, 1), 2)):
+        np.testing.assert_allclose(gu[..., a, b], g.gup[:, :, None, c] / (g.rf ** 2)[None, None, :],
+                                   rtol=1e-12, atol=1e-13 * scale)
+
+
+@pytest.mark.parametrize("warp", [T.LinearWarp(), T.SLEVEWarp()])
+def test_warped_jacobian_and_column_volume(warp):
+    g, zs = _grid()
+    G = T.warped_geometry(g, zs, warp)
+    R = g.R
+    dzc = G["zf"][..., 1:] - G["zf"][..., :-1]
+    # E_3 is radial, so J = dz r^2 J_h whatever the slopes
+    np.testing.assert_allclose(G["Jc"], dzc * ((R + G["zc"]) / R) ** 2 * g.Jh[:, :, None], rtol=1e-12)
+    # the column integral of r^2 dz from the surface to the top (midpoint rule)
+    vol = (G["Jc"] / g.Jh[:, :, None]).sum(axis=-1)
+    exact = ((R + 30000.0) ** 3 - (R + zs) ** 3) / (3 * R * R)
+    np.testing.assert_allclose(vol, exact, rtol=1e-6)
+
+
+def test_terrain_following_flow_has_no_contravariant_u3_at_the_surface():
+    # a velocity in the tangent plane of the bottom face (spanned by E_1, E_2) has u^3 = 0:
+    # the impenetrable condition u_3 = -(g^31 u_1 + g^32 u_2) / g^33 of a sloping surface
+    g, zs = _grid()
+    G = T.warped_geometry(g, zs, T.LinearWarp())
+    E = G["Ef"][:, :, 0]                                          # [Nh, 16, 3, 3]
+    rng = np.random.default_rng(3)
+    a, b = rng.standard_normal((2,) + E.shape[:2])
+    v = a[..., None] * E[..., 0, :] + b[..., None] * E[..., 1, :]
+    u = np.einsum("enik,enk->eni", E, v)                           # covariant components
+    u3 = np.einsum("enj,enj->en", G["gup_f"][:, :, 0, 2, :], u)
+    scale = np.abs(np.einsum("enj,enj->en", G["gup_f"][:, :, 0, 2, :], np.abs(u))).max()
+    assert np.abs(u3).max() <= 1e-12 * scale
+    assert np.abs(zs).max() > 1000.0                              # the mountain is in the grid
+
+
+def test_linear_warp_slopes_decay_linearly():
+    g, zs = _grid()
+    G = T.warped_geometry(g, zs, T.LinearWarp())
+    zz = zs.reshape(g.Nh, 4, 4)
+    ds1 = np.einsum("ik,ejk->eji", g.D, zz).reshape(g.Nh, 16)
+    for k in (0, 3, 8):
+        slope = np.einsum("enk,enk->en", G["Ef"][:, :, k, 0, :], g.xyz)   # E_1 . x_hat = dz/dxi^1
+        np.testing.assert_allclose(slope, (1 - g.zf[k] / 30000.0) * ds1, atol=1e-9 * np.abs(ds1).max())

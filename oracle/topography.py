@@ -178,3 +178,17 @@ def warped_geometry(g, z_surface, warp):
     Ec, Jc, gup_c = basis(zc, dzc)
     Ef, Jf, gup_f = basis(zf, dzf)
     return dict(zf=zf, zc=zc, Jc=Jc, Jf=Jf, gup_c=gup_c, gup_f=gup_f, Ec=Ec, Ef=Ef)
+
+
+def impenetrable_u3(G, rho, u1, u2):
+    """u_3 on the bottom and top faces that makes u^3 vanish there over terrain
+    (set_velocity_at_surface!, set_velocity_at_top!; src/cache/precomputed_quantities.jl:473-547):
+    u_h^3 = CT3(u_h) = g^31 u_1 + g^32 u_2 at the centres, brought to the faces by the rho J
+    weighted interpolation, which extrapolates the adjacent centre at the two boundary faces
+    (src/utils/abbreviations.jl:184-187), and u_3 = -u_h^3 / g^33 with the face's metric.
+    ``G`` is a warped_geometry; rho, u1, u2 are [Nh, 16, Nv] (u_h covariant).
+    Returns [Nh, 16, 2]: the bottom and top faces."""
+    gc, gf = G["gup_c"], G["gup_f"]
+    uh3 = gc[..., 2, 0] * u1 + gc[..., 2, 1] * u2                 # [Nh, 16, Nv]
+    del rho  # the weights of the interpolation drop out where it extrapolates
+    return np.stack([-uh3[..., 0] / gf[..., 0, 2, 2], -uh3[..., -1] / gf[..., -1, 2, 2]], axis=-1)

@@ -137,3 +137,21 @@ def test_linear_warp_slopes_decay_linearly():
     for k in (0, 3, 8):
         slope = np.einsum("enk,enk->en", G["Ef"][:, :, k, 0, :], g.xyz)   # E_1 . x_hat = dz/dxi^1
         np.testing.assert_allclose(slope, (1 - g.zf[k] / 30000.0) * ds1, atol=1e-9 * np.abs(ds1).max())
+
+
+def test_impenetrable_u3_over_terrain():
+    # set_velocity_at_surface!/top! (src/cache/precomputed_quantities.jl:473-547)
+    g, zs = _grid()
+    rng = np.random.default_rng(5)
+    shape = (g.Nh, 16, g.Nv)
+    rho, u1, u2 = np.ones(shape), rng.standard_normal(shape), rng.standard_normal(shape)
+    flat = T.warped_geometry(g, np.zeros_like(zs), T.LinearWarp())
+    assert np.abs(T.impenetrable_u3(flat, rho, u1, u2)).max() < 1e-12     # no terrain: u_3 = 0
+    G = T.warped_geometry(g, zs, T.LinearWarp())
+    u3 = T.impenetrable_u3(G, rho, u1, u2)
+    # linear in u_h, nonzero over the mountain
+    np.testing.assert_allclose(T.impenetrable_u3(G, rho, 2 * u1, 2 * u2), 2 * u3, rtol=1e-14, atol=1e-300)
+    assert np.abs(u3[..., 0]).max() > 0
+    # u^3 = u_h^3 + g^33 u_3 vanishes on the bottom face (u_h^3 extrapolated from the first centre)
+    uh3 = G["gup_c"][..., 0, 2, 0] * u1[..., 0] + G["gup_c"][..., 0, 2, 1] * u2[..., 0]
+    np.testing.assert_allclose(uh3 + G["gup_f"][..., 0, 2, 2] * u3[..., 0], 0, atol=1e-12 * np.abs(uh3).max())

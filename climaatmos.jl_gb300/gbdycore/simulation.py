@@ -336,25 +336,33 @@ def solve_atmos(sim, nsteps=None, use_graph=True):
     every = None if every is None or math.isinf(every) else max(1, int(round(every / sim.dt)))
     if every and not getattr(sim, "output_dir", None):
         raise ValueError("solve_atmos: dt_save_state_to_disk needs an output_dir")
-    nan_every = getattr(sim, "check_nan_every", None) or None
+    # check_nan_every <= 0 turns the scan off (nan_checking_callback, get_callbacks.jl:316-330)
+    n_nan = getattr(sim, "check_nan_every", None)
+    nan_every = int(n_nan) if n_nan and n_nan > 0 else None
+    taken = [0]   # steps of this run: call_every_n_steps counts from the run's start
 
     def steps(n):
-        # in runs of steps that end on the callbacks' steps (multiples from t = 0): the NaN scan
-        # every `nan_every` steps, then the restart file every `every` steps
+        # in runs of steps that end on the callbacks' steps: the NaN scan every `nan_every` steps
+        # of this run (call_every_n_steps, src/callbacks/callback_helpers.jl:177-199), then the
+        # restart file on multiples of `every` steps from t = 0
         # (save_state_to_disk_func, src/callbacks/callbacks.jl:297-321)
         while n > 0:
             i = int(round(sim.t / sim.dt))
-            k = min([n] + [p - i % p for p in (every, nan_every) if p])
+            k = min([n] + ([every - i % every] if every else []) +
+                    ([nan_every - taken[0] % nan_every] if nan_every else []))
             sim.step(k, use_graph)
             n -= k
+            taken[0] += k
             i = int(round(sim.t / sim.dt))
-            if nan_every and i % nan_every == 0:
+            if nan_every and taken[0] % nan_every == 0:
                 sim.check_nans()
             if every and i % every == 0:
                 sim.synchronize()
                 sim.save_state(sim.output_dir)
 
     try:
+        if nan_every:
+            sim.check_nans()    # the callback's initialize scans the initial state (skip_first = false)
         steps(1)
         sim.synchronize()
         t0 = time.perf_counter()

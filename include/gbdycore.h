@@ -130,21 +130,25 @@ int gb_global_sums(gb_ctx *ctx, gb_fieldvec Y, double out[2]);
  * rho e_tot, u_3 parts, summed over stages); synchronous. */
 int gb_newton_residual(gb_ctx *ctx, double out[3]);
 
-/* Allocation-free Jacobian update + solve.  No counterpart in the reference:
- * it exists for callers that cannot allocate device memory while they run,
- * e.g. a Newton iteration recorded inside a CUDA stream capture or code
- * limited to a memory pool it does not own.  gb_update_jacobian allocates its
+/* Allocation-free Jacobian update + solve.  No counterpart in the reference.
+ * It is for callers that cannot let a library allocate device memory while
+ * they run: a host model whose runtime owns all device memory through its own
+ * pool or a pre-sized arena (a cudaMalloc behind its back fails or breaks its
+ * accounting), or a Newton loop that must not take the device-wide
+ * synchronisation of a first cudaMalloc.  gb_update_jacobian allocates its
  * block storage with cudaMalloc on first use; this entry instead builds the
  * Jacobian at Y (with dtgamma) in a file-scope static device array of
  * GB_NOALLOC_SCRATCH_BYTES and solves W dY = R with it, allocating nothing.
  * Limit: (6 h_elem^2 * 16 columns) * (z_elem + 1) * 15 * ft_bytes must not
  * exceed GB_NOALLOC_SCRATCH_BYTES (else GB_ERR_ARG).  The array is held by
  * every GPU that loads the library until the process exits.  The first call on
- * a device resolves the array's device address (cudaGetSymbolAddress), so make
- * it before any stream capture.  Every call overwrites the whole block storage
- * it uses before reading it, so nothing needs to start at zero; all calls
- * share the one array, so calls that overlap on the GPU race.  Asynchronous
- * on the context stream. */
+ * a device, with that device current, resolves the array's device address
+ * (cudaGetSymbolAddress) and keeps it for the process: make that first call
+ * before any stream capture, and do not reset the device while the library is
+ * loaded (a reset invalidates the kept address, as it does every context).
+ * Every call overwrites the whole block storage it uses before reading it, so
+ * nothing needs to start at zero; all calls share the one array, so calls that
+ * overlap on the GPU race.  Asynchronous on the context stream. */
 #define GB_NOALLOC_SCRATCH_BYTES (64u << 20)
 int gb_jacobian_solve_noalloc(gb_ctx *ctx, gb_fieldvec dY, gb_fieldvec Y, gb_fieldvec R, double dtgamma);
 

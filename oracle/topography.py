@@ -180,15 +180,30 @@ def warped_geometry(g, z_surface, warp):
     return dict(zf=zf, zc=zc, Jc=Jc, Jf=Jf, gup_c=gup_c, gup_f=gup_f, Ec=Ec, Ef=Ef)
 
 
+def winterp_faces(w, x):
+    """rho J-weighted centre-to-face interpolation (the reference's ᶠwinterp, a
+    WeightedInterpolateC2F with Extrapolate boundaries, src/utils/abbreviations.jl:184-187):
+    interior face k+1/2 gets (w_k x_k + w_{k+1} x_{k+1}) / (w_k + w_{k+1}); the bottom and top
+    faces take the adjacent centre's value.  w, x: [..., Nv] -> [..., Nv + 1]."""
+    w = np.asarray(w, dtype=np.float64)
+    x = np.asarray(x, dtype=np.float64)
+    out = np.empty(x.shape[:-1] + (x.shape[-1] + 1,))
+    out[..., 1:-1] = (w[..., :-1] * x[..., :-1] + w[..., 1:] * x[..., 1:]) / (w[..., :-1] + w[..., 1:])
+    out[..., 0], out[..., -1] = x[..., 0], x[..., -1]
+    return out
+
+
 def impenetrable_u3(G, rho, u1, u2):
     """u_3 on the bottom and top faces that makes u^3 vanish there over terrain
     (set_velocity_at_surface!, set_velocity_at_top!; src/cache/precomputed_quantities.jl:473-547):
     u_h^3 = CT3(u_h) = g^31 u_1 + g^32 u_2 at the centres, brought to the faces by the rho J
-    weighted interpolation, which extrapolates the adjacent centre at the two boundary faces
-    (src/utils/abbreviations.jl:184-187), and u_3 = -u_h^3 / g^33 with the face's metric.
+    weighted interpolation ``winterp_faces``, and u_3 = -u_h^3 / g^33 with the face's metric.
+    Only the two boundary faces are produced: that is where the filter acts, and there the
+    interpolation extrapolates the adjacent centre, so the rho J weights do not enter (an
+    interior face would need them).
     ``G`` is a warped_geometry; rho, u1, u2 are [Nh, 16, Nv] (u_h covariant).
     Returns [Nh, 16, 2]: the bottom and top faces."""
     gc, gf = G["gup_c"], G["gup_f"]
     uh3 = gc[..., 2, 0] * u1 + gc[..., 2, 1] * u2                 # [Nh, 16, Nv]
-    del rho  # the weights of the interpolation drop out where it extrapolates
-    return np.stack([-uh3[..., 0] / gf[..., 0, 2, 2], -uh3[..., -1] / gf[..., -1, 2, 2]], axis=-1)
+    uh3f = winterp_faces(np.asarray(rho) * G["Jc"], uh3)          # [Nh, 16, Nv + 1]
+    return np.stack([-uh3f[..., 0] / gf[..., 0, 2, 2], -uh3f[..., -1] / gf[..., -1, 2, 2]], axis=-1)

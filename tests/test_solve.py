@@ -89,9 +89,29 @@ def test_nan_scans_on_schedule_end_a_crashed_run(tmp_path):
     s = FakeSim(output_dir=str(tmp_path), nan_every=4, every=600.0)
     assert sim.solve_atmos(s, 11).ret_code == "success"
     assert s.steps == [1, 3, 1, 3, 2, 2]          # runs end on steps 1, 4, 5, 8, 10, 12
-    assert s.scans == [480.0, 960.0, 1440.0] and [t for _, t in s.saved] == [600.0, 1200.0]
+    # the initial state is scanned too (the callback's initialize), then every 4 steps
+    assert s.scans == [0.0, 480.0, 960.0, 1440.0] and [t for _, t in s.saved] == [600.0, 1200.0]
     s = FakeSim(output_dir=str(tmp_path), nan_every=4, nan_at=900.0)
     with pytest.warns(UserWarning, match="Found NaN"):
         r = sim.solve_atmos(s, 11)
-    assert r.ret_code == "simulation_crashed" and s.scans == [480.0, 960.0]
+    assert r.ret_code == "simulation_crashed" and s.scans == [0.0, 480.0, 960.0]
     assert [t for _, t in s.saved] == [960.0]   # the crashed state
+
+
+@pytest.mark.parametrize("n", [0, -1])
+def test_nan_scan_off_for_zero_or_negative_period(n):
+    # nan_checking_callback (get_callbacks.jl:316-330) builds no callback for check_nan_every <= 0
+    s = FakeSim(nan_every=n)
+    r = sim.solve_atmos(s, 7)
+    assert r.ret_code == "success" and s.steps == [1, 7] and s.scans == []
+
+
+def test_nan_scans_count_the_steps_of_a_restarted_run(tmp_path):
+    # a run restarted at step 3 (t = 360 s) scans every 4 steps of its own (call_every_n_steps,
+    # callback_helpers.jl:177-199, counts from the run's start); restart files stay on multiples
+    # of dt_save_state_to_disk from t = 0
+    s = FakeSim(output_dir=str(tmp_path), t=360.0, nan_every=4, every=600.0)
+    assert sim.solve_atmos(s, 9).ret_code == "success"
+    assert s.scans == [360.0, 360.0 + 480.0, 360.0 + 960.0]
+    assert [t for _, t in s.saved] == [600.0, 1200.0]
+    assert sum(s.steps) == 10

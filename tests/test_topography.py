@@ -155,3 +155,26 @@ def test_impenetrable_u3_over_terrain():
     # u^3 = u_h^3 + g^33 u_3 vanishes on the bottom face (u_h^3 extrapolated from the first centre)
     uh3 = G["gup_c"][..., 0, 2, 0] * u1[..., 0] + G["gup_c"][..., 0, 2, 1] * u2[..., 0]
     np.testing.assert_allclose(uh3 + G["gup_f"][..., 0, 2, 2] * u3[..., 0], 0, atol=1e-12 * np.abs(uh3).max())
+
+
+def test_impenetrable_u3_zeroes_contravariant_u3_on_both_faces():
+    # u^3 = ᶠwinterp(rho J, u_h^3) + g^33 u_3 must vanish on the bottom and the top face for any
+    # rho and u_h over DCMIP200 terrain; the weights are checked to drop out only at those faces
+    g, zs = _grid()
+    rng = np.random.default_rng(9)
+    shape = (g.Nh, 16, g.Nv)
+    rho = np.exp(rng.normal(size=shape))
+    u1, u2 = rng.standard_normal(shape), rng.standard_normal(shape)
+    for warp in (T.LinearWarp(), T.SLEVEWarp()):
+        G = T.warped_geometry(g, zs, warp)
+        u3 = T.impenetrable_u3(G, rho, u1, u2)
+        uh3 = G["gup_c"][..., 2, 0] * u1 + G["gup_c"][..., 2, 1] * u2
+        uh3f = T.winterp_faces(rho * G["Jc"], uh3)
+        for side, k in ((0, 0), (1, -1)):
+            contra = uh3f[..., k] + G["gup_f"][..., k, 2, 2] * u3[..., side]
+            assert np.abs(contra).max() <= 1e-12 * np.abs(uh3).max(), (warp, side)
+        assert np.abs(u3).max() > 0
+        # interior faces: the weights matter (a uniform weight gives another value)
+        plain = T.winterp_faces(np.ones_like(rho), uh3)
+        assert np.abs(plain[..., 1:-1] - uh3f[..., 1:-1]).max() > 1e-6 * np.abs(uh3).max()
+        np.testing.assert_array_equal(plain[..., [0, -1]], uh3f[..., [0, -1]])

@@ -1,21 +1,26 @@
-"""gb_jacobian_solve_noalloc: the allocation-free Jacobian update + solve.
+"""gb_jacobian_solve_noalloc: the Jacobian update + solve that allocates no device memory.
 
-Callers that cannot allocate device memory while they run (a Newton iteration
-recorded in a stream capture, code confined to a memory pool it does not own)
-use this entry point: its Jacobian blocks live in a static device array of
-GB_NOALLOC_SCRATCH_BYTES instead of storage the library allocates.  The test
-compares it through the C ABI with gb_update_jacobian + gb_ldiv on two calls
-in a row (the second call reuses the array the first one left behind), within
-the tolerance the other GPU tests use, and checks the size limit.  It lives in
-its own file so that pytest collects it last.
+Some callers cannot let a library allocate device memory: a host model whose
+runtime owns every byte of the GPU through its own pool (CUDA.jl's allocator, a
+pre-sized arena of an operational forecast), where a cudaMalloc behind its back
+either fails or breaks its accounting, and callers that must not pay the device
+synchronisation a first cudaMalloc implies in the middle of a Newton loop.
+gb_update_jacobian allocates the Jacobian's block storage on first use; this
+entry point keeps the blocks in a fixed static device array instead.
+
+The test calls it through the C ABI twice in a row on different states (the
+second call reuses the array the first one left behind) and checks each result
+bitwise against gb_update_jacobian + gb_ldiv (the same kernels on the same
+inputs) and against the oracle's ldiv within the tolerance of the other
+Jacobian tests; then the size limit.  It lives in its own file so that pytest
+collects it last.
 """
-
 import numpy as np
 import pytest
 
 from gbdycore import _native as N
 from gbdycore import simulation as sim
-from helpers import field_errors, perturbed_state, small_config
+from helpers import field_errors, make_oracle, perturbed_state, small_config
 
 pytestmark = pytest.mark.gpu
 
@@ -37,7 +42,13 @@ def test_noalloc_jacobian_solve_matches_the_allocating_hooks(ft, tol):
         sim.ldiv(ref, jac, R)
         p.call("gb_jacobian_solve_noalloc", out.gb(), Y.gb(), R.gb(), float(dtg))
         ro, rr = out.numpy(), ref.numpy()
-        errs = field_errors(ro[0], ro[1], rr[0], rr[1])
+        np.testing.assert_array_equal(ro[0], rr[0], err_msg="call %d, centres" % call)
+        np.testing.assert_array_equal(ro[1], rr[1], err_msg="call %d, faces" % call)
+        o = make_oracle(cfg, ft)
+        o.set_precomputed(Yc, Yf)
+        o.update_jacobian(Yc, Yf, dtg)
+        oc, of = o.ldiv(Rc, Rf)
+        errs = field_errors(ro[0], ro[1], oc, of)
         assert all(v <= tol for v in errs.values()), (call, errs)
 
 

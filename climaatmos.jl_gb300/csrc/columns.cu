@@ -25,6 +25,7 @@
 
 #include "colcore.cuh"
 #include "geometry.h"
+#include "trace.h"
 
 namespace gb {
 
@@ -504,6 +505,7 @@ using namespace gb;
 extern "C" {
 
 int gb_columns_create(const gb_config *cfg, int ncols, const int *z_elem, gb_columns **out) {
+  GB_RANGE();
   if (!out) return GB_ERR_ARG;
   *out = nullptr;
   if (!cfg || ncols <= 0 || !z_elem || (cfg->ft_bytes != 4 && cfg->ft_bytes != 8) || !(cfg->z_max > 0))
@@ -528,17 +530,20 @@ int gb_columns_create(const gb_config *cfg, int ncols, const int *z_elem, gb_col
 }
 
 int gb_columns_destroy(gb_columns *cols) {
+  GB_RANGE();
   delete cols;
   return GB_OK;
 }
 
 int gb_columns_set_stream(gb_columns *cols, void *cuda_stream) {
+  GB_RANGE();
   if (!cols) return GB_ERR_ARG;
   cols->stream = (cudaStream_t)cuda_stream;
   return GB_OK;
 }
 
 int gb_columns_size(const gb_columns *cols, long long *centres, long long *faces) {
+  GB_RANGE();
   if (!cols) return GB_ERR_ARG;
   if (centres) *centres = cols->ctot;
   if (faces) *faces = cols->ctot + cols->ncols;
@@ -547,6 +552,7 @@ int gb_columns_size(const gb_columns *cols, long long *centres, long long *faces
 
 int gb_columns_solve(gb_columns *cols, gb_fieldvec U, gb_fieldvec Uhat, double dtgamma, int newton_iters, int mode,
                      double *rnorm) {
+  GB_RANGE();
   if (!cols) return GB_ERR_ARG;
   if (!U.c || !U.f || !Uhat.c || !Uhat.f || newton_iters < 1 || newton_iters > MAX_ITERS || mode < 0 || mode > 2 ||
       !(dtgamma > 0))
@@ -557,6 +563,7 @@ int gb_columns_solve(gb_columns *cols, gb_fieldvec U, gb_fieldvec Uhat, double d
 
 int gb_columns_autotune(gb_columns *cols, gb_fieldvec U, gb_fieldvec Uhat, double dtgamma, int newton_iters,
                         int reps, int *choice, double *ms) {
+  GB_RANGE();
   if (!cols) return GB_ERR_ARG;
   if (!U.c || !U.f || !Uhat.c || !Uhat.f || newton_iters < 1 || newton_iters > MAX_ITERS || reps < 1 || !(dtgamma > 0))
     return cfail(cols, GB_ERR_ARG, "gb_columns_autotune: invalid argument");
@@ -565,12 +572,14 @@ int gb_columns_autotune(gb_columns *cols, gb_fieldvec U, gb_fieldvec Uhat, doubl
 }
 
 int gb_columns_set_variant(gb_columns *cols, int variant) {
+  GB_RANGE();
   if (!cols || variant < 0 || variant >= GB_COLUMNS_VARIANTS) return GB_ERR_ARG;
   cols->variant = variant;
   return GB_OK;
 }
 
 int gb_columns_last_error(const gb_columns *cols, char *buf, size_t len) {
+  GB_RANGE();
   if (!cols || !buf || len == 0) return GB_ERR_ARG;
   snprintf(buf, len, "%s", cols->err.c_str());
   return GB_OK;

@@ -318,16 +318,17 @@ __device__ __forceinline__ unsigned long long global_ns() {
   return t;
 }
 // Bounded wait: returns false (and flags ST_TIMEOUT) if the phase did not
-// complete within WAIT_LIMIT_NS; the caller then waits once more, with the
-// same limit, for its own copies and skips its work.
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity, int *status) {
+// complete within limit_ns (WAIT_LIMIT_NS by default); the caller then waits
+// once more, with the same limit, for its own copies and skips its work.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity, int *status,
+                                                  unsigned long long limit_ns = WAIT_LIMIT_NS) {
   if (mbar_try_wait(bar, parity)) return true;
   const unsigned long long t0 = global_ns();
-  while (global_ns() - t0 < WAIT_LIMIT_NS)
+  while (global_ns() - t0 < limit_ns)
     if (mbar_try_wait(bar, parity)) return true;
   if (status) atomicOr(status, ST_TIMEOUT);
   const unsigned long long t1 = global_ns();
-  while (global_ns() - t1 < WAIT_LIMIT_NS)
+  while (global_ns() - t1 < limit_ns)
     if (mbar_try_wait(bar, parity)) break;
   return false;
 }

@@ -11,6 +11,7 @@
 
 #include "gbdycore.h"
 #include "kernels.cuh"
+#include "trace.h"
 
 using namespace gb;
 
@@ -234,9 +235,24 @@ int check_launch(gb_ctx *ctx) {
   return GB_OK;
 }
 
+// test_dycore_consistency: NaN (all bits set, in FP32 and FP64) in every scratch
+// buffer the tendencies and the step fill before they read it (fill_with_nans!,
+// src/utils/debug_utils.jl:58-70).  The Jacobian blocks are not scratch: ldiv
+// reads the blocks of the last update_jacobian, as CTS's Jacobian object.
+template <class FT>
+void poison_scratch(gb_ctx *ctx, cudaStream_t s) {
+  if (!ctx->cfg.test_dycore_consistency) return;
+  Impl<FT> *I = impl<FT>(ctx);
+  DevBuf *bufs[] = {&I->lap, &I->U, &I->Te[0], &I->Te[1], &I->Te[2], &I->Te[3],
+                    &I->Ti[1], &I->Ti[2], &I->Ti[3], &I->rnorm};
+  for (DevBuf *b : bufs)
+    if (b->p) cudaMemsetAsync(b->p, 0xFF, b->bytes, s);
+}
+
 template <class FT>
 int remaining_tendency_t(gb_ctx *ctx, gb_fieldvec Yt, gb_fieldvec Y) {
   Impl<FT> *I = impl<FT>(ctx);
+  poison_scratch<FT>(ctx, ctx->stream);
   launch_passA<FT>(I->P, (const FT *)Y.c, (const FT *)Y.f, (FT *)I->lap.p, ctx->stream);
   launch_dss<FT>(I->P, (FT *)I->lap.p, nullptr, ctx->stream);
   launch_passB<FT>(I->P, (const FT *)Y.c, (const FT *)Y.f, (const FT *)I->lap.p, (FT *)Yt.c, (FT *)Yt.f, ctx->stream);
@@ -251,6 +267,7 @@ int column_hook_t(gb_ctx *ctx, int mode, gb_fieldvec O, gb_fieldvec Y, double dt
     if (r) return r;
   }
   if (mode == COL_LDIV && !I->jac_valid) return fail(ctx, GB_ERR_STATE, "gb_ldiv called before gb_update_jacobian");
+  if (mode == COL_IMPLICIT) poison_scratch<FT>(ctx, ctx->stream);
   ColArgs<FT> A{};
   A.Y_c = (const FT *)Y.c; A.Y_f = (const FT *)Y.f;
   A.O_c = (FT *)O.c; A.O_f = (FT *)O.f;
@@ -295,6 +312,7 @@ void enqueue_step(gb_ctx *ctx, FT *Yc, FT *Yf, double dt_, cudaStream_t s) {
   auto tic = [&](int j) { return (FT *)I->Ti[j].p; };
   auto tif = [&](int j) { return (FT *)I->Ti[j].p + I->NR; };
   FT *Uc = (FT *)I->U.p, *Uf = Uc + I->NC;
+  poison_scratch<FT>(ctx, s);
   // stage 1: U_1 = u_n
   launch_passA<FT>(P, Yc, Yf, lap, s);
   launch_dss<FT>(P, lap, nullptr, s);
@@ -970,6 +988,7 @@ bool fv_ok(gb_fieldvec v) { return v.c && v.f && aligned(v.c) && aligned(v.f); }
 extern "C" {
 
 int gb_sizes(const gb_config *cfg, size_t *n_center, size_t *n_face, int *n_groups, int *n_copies) {
+  GB_RANGE();
   if (!cfg) return GB_ERR_ARG;
   const char *why = nullptr;
   if (!validate_config(*cfg, &why)) return GB_ERR_ARG;
@@ -986,6 +1005,7 @@ int gb_sizes(const gb_config *cfg, size_t *n_center, size_t *n_face, int *n_grou
 }
 
 int gb_geometry_export(const gb_config *cfg, gb_geometry_host *out) {
+  GB_RANGE();
   if (!cfg || !out) return GB_ERR_ARG;
   const char *why = nullptr;
   if (!validate_config(*cfg, &why)) return GB_ERR_ARG;
@@ -1003,6 +1023,7 @@ int gb_geometry_export(const gb_config *cfg, gb_geometry_host *out) {
 }
 
 int gb_ctx_create(const gb_config *cfg, gb_ctx **out) {
+  GB_RANGE();
   if (!cfg || !out) return GB_ERR_ARG;
   *out = nullptr;
   const char *why = nullptr;
@@ -1013,6 +1034,9 @@ int gb_ctx_create(const gb_config *cfg, gb_ctx **out) {
   int r;
   try {
     build_geometry(*cfg, ctx->geo);
+    // the layout is now in the geometry tables; the caller's arrays are not kept
+    ctx->cfg.elem_map = nullptr;
+    ctx->cfg.elem_orient = nullptr;
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) { delete ctx; return GB_ERR_CUDA; }
     r = cfg->ft_bytes == 8 ? create_impl<double>(ctx) : create_impl<float>(ctx);
@@ -1025,6 +1049,7 @@ int gb_ctx_create(const gb_config *cfg, gb_ctx **out) {
 }
 
 int gb_ctx_destroy(gb_ctx *ctx) {
+  GB_RANGE();
   if (!ctx) return GB_ERR_ARG;
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   else cudaDeviceSynchronize();
@@ -1033,12 +1058,14 @@ int gb_ctx_destroy(gb_ctx *ctx) {
 }
 
 int gb_set_stream(gb_ctx *ctx, void *stream) {
+  GB_RANGE();
   GUARD(ctx);
   ctx->stream = (cudaStream_t)stream;
   return GB_OK;
 }
 
 int gb_last_error(gb_ctx *ctx, char *buf, size_t len) {
+  GB_RANGE();
   GUARD(ctx);
   if (buf && len) {
     std::strncpy(buf, ctx->err.c_str(), len - 1);
@@ -1048,6 +1075,7 @@ int gb_last_error(gb_ctx *ctx, char *buf, size_t len) {
 }
 
 int gb_set_precomputed_quantities(gb_ctx *ctx, gb_fieldvec Y, double t) {
+  GB_RANGE();
   GUARD(ctx);
   (void)t;
   if (!fv_ok(Y)) return fail(ctx, GB_ERR_ARG, "Y: null or misaligned pointer");
@@ -1057,6 +1085,7 @@ int gb_set_precomputed_quantities(gb_ctx *ctx, gb_fieldvec Y, double t) {
 }
 
 int gb_remaining_tendency(gb_ctx *ctx, gb_fieldvec Yt, gb_fieldvec Y, double t) {
+  GB_RANGE();
   GUARD(ctx);
   (void)t;
   if (!fv_ok(Y) || !fv_ok(Yt)) return fail(ctx, GB_ERR_ARG, "null or misaligned pointer");
@@ -1064,6 +1093,7 @@ int gb_remaining_tendency(gb_ctx *ctx, gb_fieldvec Yt, gb_fieldvec Y, double t) 
 }
 
 int gb_implicit_tendency(gb_ctx *ctx, gb_fieldvec Yt, gb_fieldvec Y, double t) {
+  GB_RANGE();
   GUARD(ctx);
   (void)t;
   if (!fv_ok(Y) || !fv_ok(Yt)) return fail(ctx, GB_ERR_ARG, "null or misaligned pointer");
@@ -1071,6 +1101,7 @@ int gb_implicit_tendency(gb_ctx *ctx, gb_fieldvec Yt, gb_fieldvec Y, double t) {
 }
 
 int gb_update_jacobian(gb_ctx *ctx, gb_fieldvec Y, double dtgamma, double t) {
+  GB_RANGE();
   GUARD(ctx);
   (void)t;
   if (!fv_ok(Y)) return fail(ctx, GB_ERR_ARG, "null or misaligned pointer");
@@ -1079,12 +1110,14 @@ int gb_update_jacobian(gb_ctx *ctx, gb_fieldvec Y, double dtgamma, double t) {
 }
 
 int gb_ldiv(gb_ctx *ctx, gb_fieldvec dY, gb_fieldvec R) {
+  GB_RANGE();
   GUARD(ctx);
   if (!fv_ok(dY) || !fv_ok(R)) return fail(ctx, GB_ERR_ARG, "null or misaligned pointer");
   return DISPATCH(ctx, column_hook_t, ctx, (int)COL_LDIV, dY, R, 0.0);
 }
 
 int gb_correct_implicit_advection_tendency(gb_ctx *ctx, gb_fieldvec Yt, gb_fieldvec Y, double t) {
+  GB_RANGE();
   GUARD(ctx);
   (void)t;
   if (!fv_ok(Y) || !fv_ok(Yt)) return fail(ctx, GB_ERR_ARG, "null or misaligned pointer");
@@ -1092,6 +1125,7 @@ int gb_correct_implicit_advection_tendency(gb_ctx *ctx, gb_fieldvec Yt, gb_field
 }
 
 int gb_dss(gb_ctx *ctx, gb_fieldvec Y) {
+  GB_RANGE();
   GUARD(ctx);
   if (!fv_ok(Y)) return fail(ctx, GB_ERR_ARG, "null or misaligned pointer");
   if (ctx->cfg.ft_bytes == 8) launch_dss<double>(impl<double>(ctx)->P, (double *)Y.c, (double *)Y.f, ctx->stream);
@@ -1100,6 +1134,7 @@ int gb_dss(gb_ctx *ctx, gb_fieldvec Y) {
 }
 
 int gb_step(gb_ctx *ctx, gb_fieldvec Y, double t, double dt, int nsteps, int use_graph) {
+  GB_RANGE();
   GUARD(ctx);
   (void)t;
   if (!fv_ok(Y)) return fail(ctx, GB_ERR_ARG, "null or misaligned pointer");
@@ -1110,30 +1145,35 @@ int gb_step(gb_ctx *ctx, gb_fieldvec Y, double t, double dt, int nsteps, int use
 }
 
 int gb_global_sums(gb_ctx *ctx, gb_fieldvec Y, double out[2]) {
+  GB_RANGE();
   GUARD(ctx);
   if (!fv_ok(Y) || !out) return fail(ctx, GB_ERR_ARG, "null or misaligned pointer");
   return DISPATCH(ctx, global_sums_t, ctx, Y, out);
 }
 
 int gb_newton_residual(gb_ctx *ctx, double out[3]) {
+  GB_RANGE();
   GUARD(ctx);
   if (!out) return fail(ctx, GB_ERR_ARG, "null pointer");
   return DISPATCH(ctx, residual_t, ctx, out);
 }
 
 int gb_jacobian_solve_noalloc(gb_ctx *ctx, gb_fieldvec dY, gb_fieldvec Y, gb_fieldvec R, double dtgamma) {
+  GB_RANGE();
   GUARD(ctx);
   if (!fv_ok(dY) || !fv_ok(Y) || !fv_ok(R)) return fail(ctx, GB_ERR_ARG, "null or misaligned pointer");
   return DISPATCH(ctx, jacobian_solve_noalloc_t, ctx, dY, Y, R, dtgamma);
 }
 
 int gb_dss_transpose(gb_ctx *ctx, gb_fieldvec X) {
+  GB_RANGE();
   if (!ctx || !X.c || !X.f) return GB_ERR_ARG;
   return ctx->cfg.ft_bytes == 8 ? dss_transpose_t<double>(ctx, X) : dss_transpose_t<float>(ctx, X);
 }
 
 int gb_remaining_tendency_vjp(gb_ctx *ctx, gb_fieldvec Ybar, gb_fieldvec Tbar, gb_fieldvec Y, double t,
                               double dparams[2]) {
+  GB_RANGE();
   (void)t;
   if (!ctx || !fv_ok(Ybar) || !fv_ok(Tbar) || !fv_ok(Y)) return GB_ERR_ARG;
   return ctx->cfg.ft_bytes == 8 ? remaining_tendency_vjp_t<double>(ctx, Ybar, Tbar, Y, dparams)
@@ -1141,6 +1181,7 @@ int gb_remaining_tendency_vjp(gb_ctx *ctx, gb_fieldvec Ybar, gb_fieldvec Tbar, g
 }
 
 int gb_implicit_stage(gb_ctx *ctx, gb_fieldvec U, gb_fieldvec Timp, gb_fieldvec Uhat, double dtgamma) {
+  GB_RANGE();
   if (!ctx || !U.c || !U.f || !Timp.c || !Timp.f || !Uhat.c || !Uhat.f || !(dtgamma > 0)) return GB_ERR_ARG;
   return ctx->cfg.ft_bytes == 8 ? implicit_stage_t<double>(ctx, U, Timp, Uhat, dtgamma)
                                 : implicit_stage_t<float>(ctx, U, Timp, Uhat, dtgamma);
@@ -1148,12 +1189,14 @@ int gb_implicit_stage(gb_ctx *ctx, gb_fieldvec U, gb_fieldvec Timp, gb_fieldvec 
 
 int gb_implicit_stage_vjp(gb_ctx *ctx, gb_fieldvec Uhat_bar, gb_fieldvec Ubar, gb_fieldvec Timp_bar, gb_fieldvec Uhat,
                           double dtgamma, double dparams[2]) {
+  GB_RANGE();
   if (!ctx || !Uhat_bar.c || !Ubar.c || !Timp_bar.c || !Uhat.c || !(dtgamma > 0)) return GB_ERR_ARG;
   return ctx->cfg.ft_bytes == 8 ? implicit_stage_vjp_t<double>(ctx, Uhat_bar, Ubar, Timp_bar, Uhat, dtgamma, dparams)
                                 : implicit_stage_vjp_t<float>(ctx, Uhat_bar, Ubar, Timp_bar, Uhat, dtgamma, dparams);
 }
 
 int gb_step_vjp(gb_ctx *ctx, gb_fieldvec Ybar, gb_fieldvec Y, double t, double dt, double dparams[2]) {
+  GB_RANGE();
   (void)t;
   if (!ctx || !fv_ok(Ybar) || !fv_ok(Y) || !(dt > 0)) return GB_ERR_ARG;
   return ctx->cfg.ft_bytes == 8 ? step_vjp_t<double>(ctx, Ybar, Y, dt, dparams)
@@ -1161,6 +1204,7 @@ int gb_step_vjp(gb_ctx *ctx, gb_fieldvec Ybar, gb_fieldvec Y, double t, double d
 }
 
 int gb_adjoint_forward(gb_ctx *ctx, gb_fieldvec Y, double t0, double dt, int nsteps, int checkpoint_every) {
+  GB_RANGE();
   (void)t0;
   if (!ctx || !fv_ok(Y) || !(dt > 0) || nsteps < 1 || checkpoint_every < 1) return GB_ERR_ARG;
   return ctx->cfg.ft_bytes == 8 ? adjoint_forward_t<double>(ctx, Y, dt, nsteps, checkpoint_every)
@@ -1168,12 +1212,40 @@ int gb_adjoint_forward(gb_ctx *ctx, gb_fieldvec Y, double t0, double dt, int nst
 }
 
 int gb_adjoint_reverse(gb_ctx *ctx, gb_fieldvec Ybar, double dparams[2], size_t *peak_bytes) {
+  GB_RANGE();
   if (!ctx || !fv_ok(Ybar)) return GB_ERR_ARG;
   return ctx->cfg.ft_bytes == 8 ? adjoint_reverse_t<double>(ctx, Ybar, dparams, peak_bytes)
                                 : adjoint_reverse_t<float>(ctx, Ybar, dparams, peak_bytes);
 }
 
+int gb_match_elements(const gb_config *cfg, const double *xyz, int *elem_map, int *elem_orient) {
+  GB_RANGE();
+  if (!cfg || !xyz || !elem_map || !elem_orient) return GB_ERR_ARG;
+  gb_config c = *cfg;
+  c.elem_map = nullptr;
+  c.elem_orient = nullptr;
+  const char *why = nullptr;
+  if (!validate_config(c, &why)) return GB_ERR_ARG;
+  try {
+    return match_elements(c, xyz, elem_map, elem_orient, &why) ? GB_OK : GB_ERR_ARG;
+  } catch (...) {
+    return GB_ERR_NOMEM;
+  }
+}
+
+int gb_selftest_bounded_wait(gb_ctx *ctx, double limit_s) {
+  GB_RANGE();
+  GUARD(ctx);
+  if (!(limit_s > 0) || limit_s > 1.0) return fail(ctx, GB_ERR_ARG, "limit_s must be in (0, 1]");
+  int *status = ctx->cfg.ft_bytes == 8 ? impl<double>(ctx)->P.status : impl<float>(ctx)->P.status;
+  launch_selftest_wait(status, (unsigned long long)(limit_s * 1e9), ctx->stream);
+  int r = check_launch(ctx);
+  if (r) return r;
+  return DISPATCH(ctx, read_status, ctx);
+}
+
 int gb_time_kernel(gb_ctx *ctx, int kernel, gb_fieldvec Y, int reps, double *ms) {
+  GB_RANGE();
   GUARD(ctx);
   if (!fv_ok(Y) || !ms || reps < 0 || kernel < 0 || kernel > GB_K_PASSB_FINAL) return fail(ctx, GB_ERR_ARG, "bad gb_time_kernel arguments");
   return DISPATCH(ctx, time_kernel_t, ctx, kernel, Y, reps, ms);

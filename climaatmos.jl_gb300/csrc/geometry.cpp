@@ -8,6 +8,14 @@
 // collocated element nodes, its copies in ascending element*16 + node order
 // with J-weights; collocated nodes are found exactly on the integer node
 // lattice of the cube (each coordinate in 0..3*h_elem).
+//
+// The tables are built in the caller's element layout when gb_config gives one
+// (elem_map / elem_orient): element e of the caller is library element
+// elem_map[e] with its (xi^1, xi^2) frame turned by elem_orient[e] quarter
+// turns, so every per-node quantity is stored at the caller's (element, node)
+// and expressed on the caller's covariant basis.  The copies of a DSS group
+// are kept in the library's order whatever the caller's layout, so the DSS
+// sums add the same values in the same order for any element numbering.
 #include "geometry.h"
 
 #include <algorithm>
@@ -78,6 +86,16 @@ double beta_sponge(double z, double zd, double zmax, double alpha) {
   return alpha * s * s;
 }
 
+void caller_node(int o, int i, int j, int &ic, int &jc) {
+  // the caller's (i', j') of library node (i, j) in a frame turned by o quarter turns
+  switch (o & 3) {
+    case 0: ic = i; jc = j; break;
+    case 1: ic = j; jc = 3 - i; break;
+    case 2: ic = 3 - i; jc = 3 - j; break;
+    default: ic = 3 - j; jc = i; break;
+  }
+}
+
 bool validate_config(const gb_config &c, const char **why) {
   if (c.h_elem < 1 || c.h_elem > 512) { *why = "h_elem must be in [1, 512]"; return false; }
   if (c.z_elem < 2 || c.z_elem > 127) { *why = "z_elem must be in [2, 127]"; return false; }
@@ -97,6 +115,24 @@ bool validate_config(const gb_config &c, const char **why) {
     *why = "invalid Held-Suarez parameters";
     return false;
   }
+  if (c.test_dycore_consistency != 0 && c.test_dycore_consistency != 1) {
+    *why = "test_dycore_consistency must be 0 or 1";
+    return false;
+  }
+  if ((c.elem_map == nullptr) != (c.elem_orient == nullptr)) {
+    *why = "elem_map and elem_orient must both be given or both be NULL";
+    return false;
+  }
+  if (c.elem_map) {
+    const int Nh = 6 * c.h_elem * c.h_elem;
+    std::vector<char> seen(Nh, 0);
+    for (int e = 0; e < Nh; ++e) {
+      const int m = c.elem_map[e], o = c.elem_orient[e];
+      if (m < 0 || m >= Nh || seen[m]) { *why = "elem_map is not a permutation of the elements"; return false; }
+      if (o < 0 || o > 3) { *why = "elem_orient entries must be in 0..3"; return false; }
+      seen[m] = 1;
+    }
+  }
   return true;
 }
 
@@ -112,15 +148,28 @@ void build_geometry(const gb_config &c, HostGeometry &g) {
   g.sinlat.assign(H, 0); g.fh0.assign(H * 2, 0);
   const double dal = (M_PI / 2.0) / h;
   std::vector<long long> key(H);
+  std::vector<int> libidx(H);  // library element*16 + node of each stored (caller) node
+  // the caller's element and frame of each library element
+  std::vector<int> slot(Nh), orient(Nh, 0);
+  for (int e = 0; e < Nh; ++e) slot[e] = e;
+  if (c.elem_map)
+    for (int e = 0; e < Nh; ++e) {
+      slot[c.elem_map[e]] = e;
+      orient[c.elem_map[e]] = c.elem_orient[e];
+    }
   const int M = 3 * h;
   for (int p = 0; p < 6; ++p)
     for (int ey = 0; ey < h; ++ey)
       for (int ex = 0; ex < h; ++ex) {
-        const int e = (p * h + ey) * h + ex;
+        const int el = (p * h + ey) * h + ex;
+        const int e = slot[el], o = orient[el];
         for (int j = 0; j < NQ; ++j)
           for (int i = 0; i < NQ; ++i) {
-            const int n = i + NQ * j;
+            int ic, jc;
+            caller_node(o, i, j, ic, jc);
+            const int n = ic + NQ * jc;
             const size_t q = (size_t)e * NN + n;
+            libidx[q] = el * NN + i + NQ * j;
             const double al = -M_PI / 4 + (ex + (g.xg[i] + 1) / 2) * dal;
             const double be = -M_PI / 4 + (ey + (g.xg[j] + 1) / 2) * dal;
             const double ta = std::tan(al), tb = std::tan(be);
@@ -132,14 +181,27 @@ void build_geometry(const gb_config &c, HostGeometry &g) {
             }
             const double r2 = P[0] * P[0] + P[1] * P[1] + P[2] * P[2], rn = std::sqrt(r2);
             for (int d = 0; d < 3; ++d) g.xyz[q * 3 + d] = P[d] / rn;
-            // e_k = R (dal/2) d(P/|P|)/dalpha_k with dP/dalpha = sec^2 * t
+            // e_k = R (dal/2) d(P/|P|)/dalpha_k with dP/dalpha = sec^2 * t (library frame)
+            double el_k[2][3];
             for (int k = 0; k < 2; ++k) {
               const double *tv = k == 0 ? t1 : t2;
               const double tt = k == 0 ? ta : tb;
               double dP[3], pd = 0;
               for (int d = 0; d < 3; ++d) { dP[d] = (1.0 + tt * tt) * tv[d]; pd += P[d] * dP[d]; }
-              for (int d = 0; d < 3; ++d)
-                g.ecov[q * 6 + k * 3 + d] = R * (dal / 2.0) * (dP[d] / rn - P[d] * pd / (rn * r2));
+              for (int d = 0; d < 3; ++d) el_k[k][d] = R * (dal / 2.0) * (dP[d] / rn - P[d] * pd / (rn * r2));
+            }
+            // the caller's basis: its frame turned by o quarter turns against the library's
+            // (o = 1: e'_1 = e_2, e'_2 = -e_1; o = 2: -e_1, -e_2; o = 3: -e_2, e_1)
+            for (int d = 0; d < 3; ++d) {
+              double a = el_k[0][d], b = el_k[1][d];
+              switch (o) {
+                case 1: { const double t = a; a = b; b = -t; break; }
+                case 2: a = -a; b = -b; break;
+                case 3: { const double t = a; a = -b; b = t; break; }
+                default: break;
+              }
+              g.ecov[q * 6 + d] = a;
+              g.ecov[q * 6 + 3 + d] = b;
             }
             const double *e1 = &g.ecov[q * 6], *e2 = &g.ecov[q * 6 + 3];
             const double g11 = e1[0] * e1[0] + e1[1] * e1[1] + e1[2] * e1[2];
@@ -178,22 +240,25 @@ void build_geometry(const gb_config &c, HostGeometry &g) {
             key[q] = ((long long)L[0] * (M + 1) + L[1]) * (M + 1) + L[2];
           }
       }
-  // DSS groups: copies sharing a lattice point, ordered by first copy
+  // DSS groups: copies sharing a lattice point, each in the library's node order,
+  // the groups ordered by their first copy in that order
   std::vector<int> order(H);
   std::iota(order.begin(), order.end(), 0);
   std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return key[x] < key[y]; });
   std::vector<std::vector<int>> groups;
+  auto lib_less = [&](int x, int y) { return libidx[x] < libidx[y]; };
   for (size_t s = 0; s < H;) {
     size_t t = s;
     while (t < H && key[order[t]] == key[order[s]]) ++t;
     if (t - s > 1) {
       std::vector<int> gset(order.begin() + s, order.begin() + t);
-      std::sort(gset.begin(), gset.end());
+      std::sort(gset.begin(), gset.end(), lib_less);
       groups.push_back(gset);
     }
     s = t;
   }
-  std::sort(groups.begin(), groups.end(), [](const std::vector<int> &x, const std::vector<int> &y) { return x[0] < y[0]; });
+  std::sort(groups.begin(), groups.end(),
+            [&](const std::vector<int> &x, const std::vector<int> &y) { return libidx[x[0]] < libidx[y[0]]; });
   g.grp_off.assign(1, 0);
   g.grp_copy.clear();
   g.grp_w.clear();
@@ -261,6 +326,66 @@ void build_geometry(const gb_config &c, HostGeometry &g) {
     g.levf[LF_G33 * Nf + k] = 1.0 / (g.dzf[k] * g.dzf[k]);
     g.levf[LF_SPG * Nf + k] = beta_sponge(g.zf[k], c.sponge_zd, c.z_max, 1.0);
   }
+}
+
+bool match_elements(const gb_config &c, const double *xyz, int *elem_map, int *elem_orient, const char **why) {
+  gb_config lc = c;
+  lc.elem_map = nullptr;
+  lc.elem_orient = nullptr;
+  HostGeometry g;
+  build_geometry(lc, g);
+  const int h = c.h_elem, Nh = g.Nh;
+  const double dal = (M_PI / 2.0) / h, tol = 1e-9;
+  std::vector<char> seen(Nh, 0);
+  for (int e = 0; e < Nh; ++e) {
+    // unit vectors of the caller's 16 nodes; the element is found from the mean of its
+    // four interior nodes, which lies inside one element of one panel
+    double u[NN][3], cen[3] = {0, 0, 0};
+    for (int n = 0; n < NN; ++n) {
+      const double *x = xyz + ((size_t)e * NN + n) * 3;
+      const double r = std::sqrt(x[0] * x[0] + x[1] * x[1] + x[2] * x[2]);
+      if (!(r > 0)) { *why = "gb_match_elements: a node position is zero or not finite"; return false; }
+      for (int d = 0; d < 3; ++d) u[n][d] = x[d] / r;
+    }
+    for (int n : {5, 6, 9, 10})
+      for (int d = 0; d < 3; ++d) cen[d] += u[n][d];
+    int p = -1;
+    double best = -1;
+    for (int q = 0; q < 6; ++q) {
+      const double dot = PANEL[q][0][0] * cen[0] + PANEL[q][0][1] * cen[1] + PANEL[q][0][2] * cen[2];
+      if (dot > best) { best = dot; p = q; }
+    }
+    double ta = 0, tb = 0;
+    for (int d = 0; d < 3; ++d) {
+      ta += PANEL[p][1][d] * cen[d] / best;
+      tb += PANEL[p][2][d] * cen[d] / best;
+    }
+    const int ex = std::min(h - 1, std::max(0, (int)std::floor((std::atan(ta) + M_PI / 4) / dal)));
+    const int ey = std::min(h - 1, std::max(0, (int)std::floor((std::atan(tb) + M_PI / 4) / dal)));
+    const int el = (p * h + ey) * h + ex;
+    int found = -1;
+    for (int o = 0; o < 4 && found < 0; ++o) {
+      double err = 0;
+      for (int j = 0; j < NQ; ++j)
+        for (int i = 0; i < NQ; ++i) {
+          int ic, jc;
+          caller_node(o, i, j, ic, jc);
+          const double *a = u[ic + NQ * jc], *b = &g.xyz[((size_t)el * NN + i + NQ * j) * 3];
+          for (int d = 0; d < 3; ++d) err = std::max(err, std::fabs(a[d] - b[d]));
+        }
+      if (err < tol) found = o;
+    }
+    if (found < 0) {
+      *why = "gb_match_elements: an element's nodes are not the GLL nodes of an equiangular cubed-sphere "
+             "element at this h_elem in a rotated frame";
+      return false;
+    }
+    if (seen[el]) { *why = "gb_match_elements: two elements are the same element"; return false; }
+    seen[el] = 1;
+    elem_map[e] = el;
+    elem_orient[e] = found;
+  }
+  return true;
 }
 
 }  // namespace gb

@@ -34,6 +34,10 @@ struct HostGeometry {
 // Returns false (with a message) on an invalid configuration.
 bool validate_config(const gb_config &cfg, const char **why);
 void build_geometry(const gb_config &cfg, HostGeometry &g);
+// The caller's node (ic, jc) of library node (i, j) in a frame turned by o quarter turns.
+void caller_node(int o, int i, int j, int &ic, int &jc);
+// gb_match_elements: the caller's element layout from its node positions.
+bool match_elements(const gb_config &cfg, const double *xyz, int *elem_map, int *elem_orient, const char **why);
 
 // Face heights z_0 = 0 .. z_{z_elem} = z_max: uniform, or tanh-stretched with the
 // first layer dz_bottom (ClimaCore's HyperbolicTangentStretching, grids.jl:356).

@@ -129,6 +129,9 @@ size_t col_vjp_scratch_words(int Nh, int Nv);
 // tendency cotangents are written, initialised as e0[j] Yb / i0[j] Yb from Yb on entry.
 template <class FT> void launch_column_stage_vjp(const DevParams<FT> &P, const StageArgs<FT> &A, const FT *Ub_c, const FT *Ub_f, const FT *Tb_c, const FT *Tb_f, FT *Yb_c, FT *Yb_f, FT *const Teb[4], FT *const Tib[4], size_t NC, size_t NR, FT *scr, double *dalpha, cudaStream_t s, const FT *Uo = nullptr, const FT *Tio = nullptr, const FT *e0 = nullptr, const FT *i0 = nullptr);
 template <class FT> void launch_bc_filter(const DevParams<FT> &P, FT *Yf, cudaStream_t s);
+// Failure-detection self-test: one warp waits on an mbarrier whose transfer is announced but
+// never issued, so the bounded wait gives up after limit_ns and sets ST_TIMEOUT in *status.
+void launch_selftest_wait(int *status, unsigned long long limit_ns, cudaStream_t s);
 template <class FT> void launch_global_sums(const DevParams<FT> &P, const FT *Yc, double *partials, int nblocks, double *out, cudaStream_t s);
 template <class FT> void launch_reduce_rnorm(const double *rnorm, int ncols, double *out, cudaStream_t s);
 template <class FT> void launch_accum_slots(const double *part, int n, double *acc, cudaStream_t s);

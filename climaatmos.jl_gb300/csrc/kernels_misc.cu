@@ -316,7 +316,27 @@ __global__ void __launch_bounds__(256) k_reduce_rnorm(const double *__restrict__
     for (int q = 0; q < 3; ++q) out[q] = s[q].value();
 }
 
+// The failure-detection self-test: an mbarrier phase that announces a 16-byte
+// transfer which nothing issues can never complete, so every lane's bounded
+// wait runs out after limit_ns and flags ST_TIMEOUT, exactly as a wait on a
+// copy that never lands would.  Nothing is in flight when the kernel ends.
+__global__ void k_selftest_wait(int *status, unsigned long long limit_ns) {
+  __shared__ __align__(8) uint64_t bar;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) mbar_expect_tx(&bar, 16u);
+  __syncwarp();
+  mbar_wait_bounded(&bar, 0u, status, limit_ns);
+}
+
 }  // namespace
+
+void launch_selftest_wait(int *status, unsigned long long limit_ns, cudaStream_t s) {
+  k_selftest_wait<<<1, 32, 0, s>>>(status, limit_ns);
+}
 
 template <class FT>
 void launch_dss(const DevParams<FT> &P, FT *C, FT *F, cudaStream_t s) {

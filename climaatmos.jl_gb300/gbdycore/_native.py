@@ -20,7 +20,8 @@ SYMBOLS = [
     "gb_sizes", "gb_geometry_export", "gb_ctx_create", "gb_ctx_destroy", "gb_set_stream", "gb_last_error",
     "gb_set_precomputed_quantities", "gb_remaining_tendency", "gb_implicit_tendency", "gb_update_jacobian",
     "gb_ldiv", "gb_correct_implicit_advection_tendency", "gb_dss", "gb_step", "gb_global_sums",
-    "gb_newton_residual", "gb_time_kernel", "gb_jacobian_solve_noalloc",
+    "gb_newton_residual", "gb_time_kernel", "gb_jacobian_solve_noalloc", "gb_match_elements",
+    "gb_selftest_bounded_wait",
     "gb_dss_transpose", "gb_remaining_tendency_vjp", "gb_implicit_stage", "gb_implicit_stage_vjp", "gb_step_vjp",
     "gb_adjoint_forward", "gb_adjoint_reverse",
     "gb_columns_create", "gb_columns_destroy", "gb_columns_set_stream", "gb_columns_size", "gb_columns_solve",
@@ -40,7 +41,9 @@ class GBConfig(ctypes.Structure):
                     "grav", "omega", "R_d", "cp_d", "cv_d", "T_0", "p_ref", "T_min_ref", "T_surf_ref",
                     "T_min_sgs", "radius")] + [("held_suarez", _c_int)] + [(n, _c_double) for n in (
                     "hs_day", "hs_sigma_b", "hs_dT_y", "hs_T_equator", "hs_dtheta_z", "hs_T_min",
-                    "hs_p_ref_theta", "hs_MSLP")]
+                    "hs_p_ref_theta", "hs_MSLP")] + [
+                    ("elem_map", ctypes.POINTER(_c_int)), ("elem_orient", ctypes.POINTER(_c_int)),
+                    ("test_dycore_consistency", _c_int)]
 
 
 class GBFieldVec(ctypes.Structure):
@@ -98,6 +101,8 @@ def load(build_if_missing=True):
     L.gb_newton_residual.argtypes = [_vp, _dp]
     L.gb_time_kernel.argtypes = [_vp, _c_int, fv, _c_int, _dp]
     L.gb_jacobian_solve_noalloc.argtypes = [_vp, fv, fv, fv, _c_double]
+    L.gb_match_elements.argtypes = [cfgp, _dp, _ip, _ip]
+    L.gb_selftest_bounded_wait.argtypes = [_vp, _c_double]
     L.gb_dss_transpose.argtypes = [_vp, fv]
     L.gb_remaining_tendency_vjp.argtypes = [_vp, fv, fv, fv, _c_double, _dp]
     L.gb_implicit_stage.argtypes = [_vp, fv, fv, fv, _c_double]
@@ -136,4 +141,30 @@ def make_config(cfg):
     c.held_suarez = 1 if cfg.held_suarez else 0
     for k, v in cfg.hs.items():
         setattr(c, "hs_" + k, float(v))
+    c.test_dycore_consistency = 1 if getattr(cfg, "test_dycore_consistency", False) else 0
+    layout = getattr(cfg, "layout", None)
+    if layout is not None:
+        emap = np.ascontiguousarray(layout[0], dtype=np.int32)
+        eori = np.ascontiguousarray(layout[1], dtype=np.int32)
+        c.elem_map = emap.ctypes.data_as(ctypes.POINTER(_c_int))
+        c.elem_orient = eori.ctypes.data_as(ctypes.POINTER(_c_int))
+        c._keep = (emap, eori)   # the arrays live as long as the struct
     return c
+
+
+def match_elements(cfg, xyz):
+    """(elem_map, elem_orient) of the caller's layout from its node positions [Nh, 16, 3]
+    (gb_match_elements); raises GBError if the positions are not a rotated-frame equiangular
+    cubed sphere at cfg.h_elem."""
+    import numpy as np
+    L = load()
+    c = make_config(cfg.with_(layout=None) if hasattr(cfg, "with_") else cfg)
+    Nh = 6 * cfg.h_elem ** 2
+    x = np.ascontiguousarray(xyz, dtype=np.float64).reshape(Nh, 16, 3)
+    emap, eori = np.zeros(Nh, np.int32), np.zeros(Nh, np.int32)
+    ip = ctypes.POINTER(_c_int)
+    rc = L.gb_match_elements(ctypes.byref(c), x.ctypes.data_as(_dp), emap.ctypes.data_as(ip), eori.ctypes.data_as(ip))
+    if rc != GB_OK:
+        raise GBError(rc, "gb_match_elements: the node positions are not those of a cubed sphere at h_elem=%d"
+                      % cfg.h_elem)
+    return emap, eori

@@ -54,7 +54,7 @@ def build(force=False, verbose=False, extra=()):
     with cf.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
         objs = list(ex.map(one, SOURCES))
     tmp = LIB + ".tmp"
-    cmd = [cc, "-shared", "-o", tmp] + objs + ARCH
+    cmd = [cc, "-shared", "-o", tmp] + objs + ARCH + ["-ldl"]   # -ldl: NVTX's injection loader
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("link failed:\n%s%s" % (r.stdout, r.stderr))

@@ -83,6 +83,10 @@ class DycoreConfig:
     constants: dict = field(default_factory=lambda: dict(CONSTANTS))
     held_suarez: bool = False        # rad: held_suarez (src/config/model_getters.jl:636)
     hs: dict = field(default_factory=lambda: dict(HELD_SUAREZ))
+    # numerics.test_dycore_consistency (src/utils/debug_utils.jl:58-70): NaN-fill scratch first
+    test_dycore_consistency: bool = False
+    # the caller's element layout: (elem_map [Nh], elem_orient [Nh]) arrays, None: library order
+    layout: tuple = None
 
     def __post_init__(self):
         if self.nu is None:

@@ -14,7 +14,8 @@
  *   c : [Nh][4][16][Nv]   components (rho, u_1, u_2, rho e_tot); u_h covariant
  *   f : [Nh][16][Nv + 1]  covariant u_3
  * with node n = i + 4 j and elements ordered panel-major, row-major within a
- * panel (gb_geometry_export gives node positions for remapping).
+ * panel, unless gb_config.elem_map / elem_orient give the caller's own order and
+ * element frames (gb_match_elements derives them from node positions).
  * All pointers in gb_fieldvec are device pointers (e.g. CuArray / torch
  * tensors), 16-byte aligned.
  */
@@ -57,6 +58,25 @@ typedef struct {
      equilibrium floor T_min, the potential-temperature reference pressure and MSLP */
   int held_suarez;
   double hs_day, hs_sigma_b, hs_dT_y, hs_T_equator, hs_dtheta_z, hs_T_min, hs_p_ref_theta, hs_MSLP;
+  /* The caller's element layout (both NULL: the library's own order, see above).  ClimaCore
+     numbers the elements along a space-filling curve (Topology2D(..., spacefillingcurve(mesh)),
+     src/simulation/grids.jl:74-75) and each element has its own local (xi^1, xi^2) frame.
+     elem_map[e] is the library element (panel-major, row-major) that the caller's element e
+     is; elem_orient[e] in 0..3 says by how many quarter turns the caller's frame is rotated
+     against the library's: the caller's node (i, j) is the library's node
+       0: (i, j)   1: (3 - j, i)   2: (3 - i, 3 - j)   3: (j, 3 - i)
+     (i fastest, n = i + 4 j), and its covariant u_1, u_2 are components on its own basis.
+     Every geometry table, the DSS plan and every kernel then work in the caller's layout
+     directly (no permutation of the state).  gb_match_elements derives both arrays from the
+     caller's node positions.  Read by gb_sizes, gb_geometry_export and gb_ctx_create only. */
+  const int *elem_map;
+  const int *elem_orient;
+  /* test_dycore_consistency (src/utils/debug_utils.jl:58-70, called from
+     remaining_tendency.jl:52 and implicit_tendency.jl:37): 1 fills every library scratch
+     buffer (Laplacians, stage state, explicit and implicit tendencies, Jacobian, residual
+     slots) with NaN before each tendency evaluation and each step, so that a read of a
+     quantity not recomputed first shows up as NaN in the result.  0 off. */
+  int test_dycore_consistency;
 } gb_config;
 
 typedef struct {
@@ -73,12 +93,21 @@ typedef struct {
   double *fh0;   /* [Nh*16*2] contravariant 2*Omega*cos(lat)*north at radius R */
   double *zf;    /* [Nv+1] face heights */
   int *dss_off;  /* [ngroups+1] */
-  int *dss_copy; /* [ncopies] element*16 + node, ascending within a group */
+  int *dss_copy; /* [ncopies] element*16 + node, in the library's element order within a group
+                    (ascending without elem_map) */
 } gb_geometry_host;
 
 /* Sizes for a configuration (no GPU needed). */
 int gb_sizes(const gb_config *cfg, size_t *n_center, size_t *n_face, int *n_dss_groups, int *n_dss_copies);
 int gb_geometry_export(const gb_config *cfg, gb_geometry_host *out);
+/* The caller's element layout from its node positions (no GPU needed): xyz holds, for each of
+ * the caller's 6 h_elem^2 elements and its 16 nodes (n = i + 4 j), the node's position
+ * (any radius; FP64, [Nh][16][3]).  Fills elem_map[Nh] and elem_orient[Nh] for gb_config.
+ * Fails with GB_ERR_ARG when an element is not one of the equiangular cubed sphere's at
+ * h_elem, its nodes are not the GLL nodes in a rotated (i, j) frame (a mirrored frame is
+ * refused), or two elements are the same one.  The replacement for the layout a ClimaCore
+ * SpectralElementSpace2D takes from its topology (src/simulation/grids.jl:74-75). */
+int gb_match_elements(const gb_config *cfg, const double *xyz, int *elem_map, int *elem_orient);
 
 /* Context lifetime.  Replaces the library-owned parts of AtmosCache
  * (src/cache/cache.jl:165-305: geometry, Coriolis, DSS buffers, scratch) and
@@ -129,6 +158,18 @@ int gb_global_sums(gb_ctx *ctx, gb_fieldvec Y, double out[2]);
 /* FP64 sums of squares of the Newton residual of the last gb_step (rho,
  * rho e_tot, u_3 parts, summed over stages); synchronous. */
 int gb_newton_residual(gb_ctx *ctx, double out[3]);
+
+/* Failure-detection self-test (no counterpart in the reference, whose failure
+ * detection is the host-side NaN scan).  Every wait of this library's kernels
+ * on an asynchronous copy is bounded: when it runs out, the kernel sets a bit
+ * in the context's device status word, waits once more with the same limit for
+ * its own copies and leaves, and the next synchronous entry returns
+ * GB_ERR_TIMEOUT.  This entry runs that path on purpose: one warp waits, with a
+ * limit of limit_s seconds (0 < limit_s <= 1), on an mbarrier whose announced
+ * transfer is never issued.  Returns GB_ERR_TIMEOUT (the status is then
+ * cleared and the context stays usable); GB_OK would mean the wait did not run
+ * out.  Synchronous. */
+int gb_selftest_bounded_wait(gb_ctx *ctx, double limit_s);
 
 /* Allocation-free Jacobian update + solve.  No counterpart in the reference.
  * It is for callers that cannot let a library allocate device memory while

@@ -213,11 +213,10 @@ int gb_time_kernel(gb_ctx *ctx, int kernel, gb_fieldvec Y, int reps, double *ms_
  * Reverse mode (adjoint) of the step, for gradients with respect to the state
  * and to two scalars: nu (nu_4_vorticity, with nu_4_scalar = nu / Prandtl
  * following it) and the Rayleigh sponge rate alpha (alpha_uh = alpha_w =
- * alpha, beta(z) = alpha s(z) above sponge_zd).  The reference exposes its
- * differentiable step to Julia AD through ChainRulesCore; these entries are
- * the forward and pullback halves of that rrule (the Julia shim defines
- * ChainRulesCore.rrule(solve!, ...) on gb_adjoint_forward /
- * gb_adjoint_reverse).  Every *_vjp entry ACCUMULATES into its cotangent
+ * alpha, beta(z) = alpha s(z) above sponge_zd).  Julia AD reaches them
+ * through a ChainRulesCore rule: these entries are the forward and pullback
+ * halves of ChainRulesCore.rrule(solve, Y0, (nu, rate), p, dt, n), which the
+ * Julia shim defines on gb_adjoint_forward / gb_adjoint_reverse.  Every *_vjp entry ACCUMULATES into its cotangent
  * outputs (+=) and into dparams[0] (d/dnu) and dparams[1] (d/dalpha); each
  * is the exact reverse of the corresponding forward computation in this
  * library.  Synchronous.  The reverse slab kernels keep an element's state,

@@ -371,6 +371,42 @@ struct Oracle {
   }
   void dss(FT *Yc, FT *Yf) const { dss_center(Yc, Nv); dss_face(Yf); }
 
+  // ---- the horizontal Laplacians alone (analytic tests of the operators) ----
+  // X is a centre block [Nh][4][16][Nv] holding a scalar f (comp 0) and a covariant
+  // horizontal vector (u_1, u_2) (comps 1-2).  O receives, per level and after the DSS,
+  // comp 0 = wdiv_h(grad_h f) (the scalar Laplacian of prep_hyperdiffusion_tendency!,
+  // hyperdiffusion.jl:141-147) and comps 1-2 = the vector Laplacian of (u_1, u_2, 0)
+  // with unit divergence factor (hyperdiffusion.jl:140), comp 3 = 0.
+  void laplacians(const FT *X, FT *O) const {
+#pragma omp parallel for
+    for (int e = 0; e < Nh; ++e)
+      for (int v = 0; v < Nv; ++v) {
+        Slab s;
+        slab(e, rc[v], dzc[v], s);
+        FT f[NN], u1[NN], u2[NN], u3[NN], g1[NN], g2[NN], F1[NN], F2[NN], Ls[NN], o1[NN], o2[NN], o3[NN];
+        for (int n = 0; n < NN; ++n) {
+          f[n] = X[ci(e, 0, n, v)];
+          u1[n] = X[ci(e, 1, n, v)];
+          u2[n] = X[ci(e, 2, n, v)];
+          u3[n] = FT(0);
+        }
+        grad_h(f, g1, g2);
+        for (int n = 0; n < NN; ++n) {
+          F1[n] = s.gu0[n] * g1[n] + s.gu1[n] * g2[n];
+          F2[n] = s.gu1[n] * g1[n] + s.gu2[n] * g2[n];
+        }
+        wdiv_h(s, F1, F2, Ls);
+        vec_lap(s, u1, u2, u3, FT(1), o1, o2, o3);
+        for (int n = 0; n < NN; ++n) {
+          O[ci(e, 0, n, v)] = Ls[n];
+          O[ci(e, 1, n, v)] = o1[n];
+          O[ci(e, 2, n, v)] = o2[n];
+          O[ci(e, 3, n, v)] = FT(0);
+        }
+      }
+    dss_center(O, Nv);
+  }
+
   // ---- remaining_tendency! ----
   std::vector<FT> Lap;  // [e][4][n][v]: (Ls, L1, L2, L3) so comps 1-2 are the C12 vector
   void remaining_tendency(FT *Tc, FT *Tf, const FT *Yc, const FT *Yf) {
@@ -1099,6 +1135,10 @@ void oracle_dss(void *hh, void *Yc, void *Yf) {
 void oracle_step(void *hh, void *Yc, void *Yf, double dt, int nsteps) {
   Handle *h = (Handle *)hh;
   for (int s = 0; s < nsteps; ++s) DISPATCH(h, (o.step((decltype(o.R) *)Yc, (decltype(o.R) *)Yf, dt)));
+}
+void oracle_laplacians(void *hh, void *X, void *O) {
+  Handle *h = (Handle *)hh;
+  DISPATCH(h, (o.laplacians((const decltype(o.R) *)X, (decltype(o.R) *)O)));
 }
 void oracle_global_sums(void *hh, void *Yc, double *out) {
   Handle *h = (Handle *)hh;

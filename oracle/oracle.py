@@ -79,6 +79,7 @@ def lib():
         _lib.oracle_set_precomputed.argtypes = [v, v, v]
         _lib.oracle_pressure.argtypes = [v, v, v, v]
         _lib.oracle_dss.argtypes = [v, v, v]
+        _lib.oracle_laplacians.argtypes = [v, v, v]
         _lib.oracle_update_jacobian.argtypes = [v, v, v, ctypes.c_double]
         _lib.oracle_step.argtypes = [v, v, v, ctypes.c_double, ctypes.c_int]
         _lib.oracle_global_sums.argtypes = [v, v, _dp]
@@ -197,6 +198,14 @@ class Oracle:
     def dss(self, Yc, Yf):
         self._chk(Yc, Yf)
         lib().oracle_dss(self.h, _ptr(Yc), _ptr(Yf))
+
+    def laplacians(self, X):
+        """Per level, after the DSS: the scalar Laplacian wdiv(grad f) of comp 0 and the vector
+        Laplacian of the covariant (comp 1, comp 2); X and the result are [Nh, 4, 16, Nv]."""
+        X = np.ascontiguousarray(X, self.dtype)
+        O = np.zeros_like(X)
+        lib().oracle_laplacians(self.h, _ptr(X), _ptr(O))
+        return O
 
     def step(self, Yc, Yf, dt, nsteps=1):
         self._chk(Yc, Yf)

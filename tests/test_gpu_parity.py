@@ -225,3 +225,28 @@ def test_production_size_step_conserves_mass():
     assert abs(g1[0] - g0[0]) <= 2e-6 * abs(g0[0])
     assert abs(g1[1] - g0[1]) <= 2e-5 * abs(g0[1])
     assert float(s.Y.f[:, :, 0].abs().max()) == 0.0 and float(s.Y.f[:, :, -1].abs().max()) == 0.0
+
+
+def test_resting_atmosphere_stays_at_rest():
+    """A horizontally uniform atmosphere at rest (the balanced profile, no perturbation): the
+    horizontal operators see constant fields, so u_h stays zero to roundoff and every column
+    evolves alike over 10 FP64 steps (an analytic pin independent of the oracle: gradients of
+    constants, the Coriolis term of zero wind, the vertical-horizontal coupling and the DSS)."""
+    from gbdycore import setups as S
+    cfg = small_config(ft=np.float64, h_elem=4, z_elem=20)
+    g = sim.Geometry(cfg)
+    Yc, Yf = S.initial_state(g, cfg, sigma=0.0)
+    s = sim.AtmosSimulation(cfg, state=(Yc, Yf))
+    s.step(10)
+    Xc, Xf = s.Y.numpy()
+    # physical horizontal speed sqrt(g^ij u_i u_j) at each point (g^ij at the level)
+    rc = (g.R + g.zc) / g.R
+    gu = g.gup[..., None, :] / (rc[None, None, :, None] ** 2)
+    u1, u2 = Xc[:, 1], Xc[:, 2]
+    speed = np.sqrt(np.maximum(gu[..., 0] * u1 * u1 + 2 * gu[..., 1] * u1 * u2 + gu[..., 2] * u2 * u2, 0))
+    assert speed.max() < 1e-8, speed.max()
+    # every column alike: rho, rho e_tot and u_3 equal the column mean to roundoff
+    for name, a in (("rho", Xc[:, 0]), ("rho_e_tot", Xc[:, 3]), ("u_3", Xf)):
+        m = a.reshape(-1, a.shape[-1]).mean(axis=0)
+        scale = max(np.abs(a).max(), 1e-300)
+        assert np.abs(a - m).max() <= 1e-11 * scale, name

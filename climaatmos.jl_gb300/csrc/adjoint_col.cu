@@ -31,7 +31,7 @@ namespace {
 // scratch arrays (each [Nf][ncols])
 enum ColScr {
   // centres
-  S_R0 = 0, S_RE, S_U1, S_U2, S_K, S_H, S_PI, S_THV, S_THVR, S_PHIR, S_RJ, S_IJ, S_RR, S_RES, S_RN, S_REN,
+  S_R0 = 0, S_RE, S_U1, S_U2, S_K, S_H, S_PI, S_THV, S_THVR, S_PHID, S_RJ, S_IJ, S_RR, S_RES, S_RN, S_REN,
   S_HN, S_RJN,
   S_BR, S_BRE, S_BU1, S_BU2, S_BK, S_BH, S_BPI, S_BTHV, S_BTHVR, S_BPHIR, S_BRJ, S_BRN, S_BREN, S_BHN, S_BRJN,
   S_BRR, S_BRES, S_BRU0, S_BRU1, S_BEU0, S_BEU1,
@@ -166,13 +166,13 @@ __global__ void __launch_bounds__(128) k_col_stage_vjp(DevParams<FT> P, ColVjpAr
     const FT c1 = (G.gu0 * u1 + G.gu1 * u2) * L.z, c2 = (G.gu1 * u1 + G.gu2 * u2) * L.z;
     const FT K = (u1 * c1 + u2 * c2 + (a * (a * g33(v)) + b * (b * g33(v + 1))) / FT(2)) / FT(2);
     Thermo<FT> th;
-    thermo(P, S(S_R0, v), S(S_RE, v), K, L.w, th);
+    thermo(P, S(S_R0, v), S(S_RE, v), K, L.w, P.lr4[v], th);
     S(S_K, v) = K;
     S(S_H, v) = th.h;
     S(S_PI, v) = th.Pi;
     S(S_THV, v) = th.thv;
     S(S_THVR, v) = th.thvr;
-    S(S_PHIR, v) = th.phir;
+    S(S_PHID, v) = th.phid;
     S(S_RJ, v) = S(S_R0, v) * (G.Jh * L.x);
     S(S_IJ, v) = G.iJh * L.y;
   }
@@ -232,7 +232,7 @@ __global__ void __launch_bounds__(128) k_col_stage_vjp(DevParams<FT> P, ColVjpAr
     r.uu1 = dtg * (kap * (rbv - ra) * u3c * (irb / FT(2)) - beta) - FT(1);
     r.uu2 = dtg * (kap * rbv * u3cp * (irb / FT(2)));
     const FT thd = ((S(S_THV, a) - S(S_THVR, a)) + (S(S_THV, b) - S(S_THVR, b))) / FT(2);
-    r.T3 = -(P.lf4[f].z - (S(S_PHIR, b) - S(S_PHIR, a)) + P.cpd * thd * (S(S_PI, b) - S(S_PI, a))) - beta * u3;
+    r.T3 = -((S(S_PHID, b) - S(S_PHID, a)) + P.cpd * thd * (S(S_PI, b) - S(S_PI, a))) - beta * u3;
     return r;
   };
   for (int f = 0; f < Nf; ++f) {
@@ -292,7 +292,7 @@ __global__ void __launch_bounds__(128) k_col_stage_vjp(DevParams<FT> P, ColVjpAr
     const FT c1 = (G.gu0 * u1 + G.gu1 * u2) * L.z, c2 = (G.gu1 * u1 + G.gu2 * u2) * L.z;
     const FT K = (u1 * c1 + u2 * c2 + (a * (a * g33(v)) + b * (b * g33(v + 1))) / FT(2)) / FT(2);
     Thermo<FT> th;
-    thermo(P, S(S_RN, v), S(S_REN, v), K, L.w, th);
+    thermo(P, S(S_RN, v), S(S_REN, v), K, L.w, P.lr4[v], th);
     S(S_HN, v) = th.h;
     S(S_RJN, v) = S(S_RN, v) * (G.Jh * L.x);
   }
@@ -644,7 +644,7 @@ __global__ void __launch_bounds__(128, MINB) k_col_stage_vjp_g(DevParams<FT> P, 
   const FT dtg = A.dtg, idtg = A.idtg, kap = P.Rd * P.icvd;
   const size_t cb = (size_t)e * 4 * NN * Nv + (size_t)n * Nv + r0, rb = (size_t)e * 2 * NN * Nv + (size_t)n * Nv + r0;
   const size_t fb = ((size_t)e * NN + n) * Nf + r0;
-  const col::ColLev<FT> L{P.lc4, P.lf4, Nv, Nf};
+  const col::ColLev<FT> L{P.lc4, P.lf4, P.lr4, Nv, Nf};
   // The cotangent inputs and the accumulation targets are first touched after
   // the forward recompute: start their lines towards L2 now (one prefetch per
   // field and warp covers the column: the lanes' levels are contiguous).
@@ -714,7 +714,7 @@ __global__ void __launch_bounds__(128, MINB) k_col_stage_vjp_g(DevParams<FT> P, 
     if (r0 + k >= Nv) { H[0][k] = FT(1); H[1][k] = FT(0); H[2][k] = FT(0); H[3][k] = FT(1); }
     if (r0 + k >= Nf) H[4][k] = FT(0);
   }
-  FT u3[CM], g33[CM], beta[CM], spg[CM], dphi[CM];
+  FT u3[CM], g33[CM], beta[CM], spg[CM];
 #pragma unroll
   for (int k = 0; k < CM; ++k) {
     const int f = r0 + k;
@@ -722,13 +722,12 @@ __global__ void __launch_bounds__(128, MINB) k_col_stage_vjp_g(DevParams<FT> P, 
     const Lev4<FT> lf = P.lf4[min(f, Nf - 1)];
     g33[k] = lf.x;
     beta[k] = lf.y;
-    dphi[k] = lf.z;
     spg[k] = P.levf[LF_SPG * Nf + min(f, Nf - 1)];
   }
   const FT u3n0 = nxt<G, CM>(u3, gl), g33n0 = nxt<G, CM>(g33, gl);
   const FT u3p = prv<G, CM>(u3, gl), g33p = prv<G, CM>(g33, gl);
   // centre diagnostics of U0
-  FT K[CM], h[CM], Pi[CM], thv[CM], thvr[CM], phir[CM], rJ[CM], iJ[CM], c1[CM], c2[CM], Jc[CM], phi[CM];
+  FT K[CM], h[CM], Pi[CM], thv[CM], thvr[CM], phid[CM], rJ[CM], iJ[CM], c1[CM], c2[CM], Jc[CM], phi[CM];
 #pragma unroll
   for (int k = 0; k < CM; ++k) {
     const int v = r0 + k;
@@ -737,12 +736,12 @@ __global__ void __launch_bounds__(128, MINB) k_col_stage_vjp_g(DevParams<FT> P, 
     c1[k] = (Gm.gu0 * H[1][k] + Gm.gu1 * H[2][k]) * Lc.z;
     c2[k] = (Gm.gu1 * H[1][k] + Gm.gu2 * H[2][k]) * Lc.z;
     const col::Cen<FT> cc = col::cdiag(P, Gm, L, v, H[0][k], H[1][k], H[2][k], H[3][k], u3[k], ub, g33[k], gb);
-    K[k] = cc.K; h[k] = cc.h; Pi[k] = cc.Pi; thv[k] = cc.thv; thvr[k] = cc.thvr; phir[k] = cc.phir;
+    K[k] = cc.K; h[k] = cc.h; Pi[k] = cc.Pi; thv[k] = cc.thv; thvr[k] = cc.thvr; phid[k] = cc.phid;
     rJ[k] = cc.rJ; iJ[k] = cc.iJ; Jc[k] = Gm.Jh * Lc.x; phi[k] = cc.phi;
   }
   // previous-level (centre r0 - 1) values
   const FT rJp = prv<G, CM>(rJ, gl), hp = prv<G, CM>(h, gl), Kp = prv<G, CM>(K, gl), Pip = prv<G, CM>(Pi, gl);
-  const FT thvp = prv<G, CM>(thv, gl), thvrp = prv<G, CM>(thvr, gl), phirp = prv<G, CM>(phir, gl);
+  const FT thvp = prv<G, CM>(thv, gl), thvrp = prv<G, CM>(thvr, gl), phidp = prv<G, CM>(phid, gl);
   const FT rhop = prv<G, CM>(H[0], gl), phip = prv<G, CM>(phi, gl);
   auto cprev = [&](const FT (&x)[CM], int k, FT pv) { return k > 0 ? x[k - 1] : pv; };
   // face fluxes and rows
@@ -773,7 +772,7 @@ __global__ void __launch_bounds__(128, MINB) k_col_stage_vjp_g(DevParams<FT> P, 
       uu1[k] = dtg * (kap * (rbv - ra) * u3c * (irb / FT(2)) - beta[k]) - FT(1);
       uu2[k] = dtg * (kap * rbv * u3cp * (irb / FT(2)));
       const FT thd = ((thva - cprev(thvr, k, thvrp)) + (thv[k] - thvr[k])) / FT(2);
-      T3[k] = -(dphi[k] - (phir[k] - cprev(phir, k, phirp)) + P.cpd * thd * (Pi[k] - Pia)) - beta[k] * u3[k];
+      T3[k] = -((phid[k] - cprev(phid, k, phidp)) + P.cpd * thd * (Pi[k] - Pia)) - beta[k] * u3[k];
     } else {
       ur0[k] = ur1[k] = ue0[k] = uu0[k] = uu2[k] = FT(0);
       uu1[k] = f <= Nv ? -dtg * beta[k] - FT(1) : FT(1);

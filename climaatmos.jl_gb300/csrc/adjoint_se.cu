@@ -761,7 +761,7 @@ __global__ void __launch_bounds__(AD_THREADS, AdMinBlocks<FT>::value)
         rho[i] = sY[q];
         rhoe[i] = sY[48 * Nv + q];
         Thermo<FT> th;
-        thermo(P, rho[i], rhoe[i], K[i], Phi, th);
+        thermo(P, rho[i], rhoe[i], K[i], Phi, P.lr4[v], th);
         h[i] = th.h;
         Pi[i] = th.Pi;
         thp[i] = th.thv - th.thvr;

@@ -24,10 +24,11 @@ template <int G, class FT>
 __device__ __forceinline__ FT down(FT v, int d) { return __shfl_down_sync(0xffffffffu, v, d, G); }
 
 // Level geometry of one column: lc4[v] = {r^2 dz, 1/(r^2 dz), 1/r^2, Phi},
-// lf4[f] = {g^33, beta_w, Phi_c(f) - Phi_c(f-1) (0 on the boundary faces), 0}.
+// lf4[f] = {g^33, beta_w, Phi_c(f) - Phi_c(f-1) (0 on the boundary faces), 0},
+// lr4[v] = the level's reference record {p0, 1/p0, cp_d (T_sfc - T_min) / 7 Pi0^7, 0}.
 template <class FT>
 struct ColLev {
-  const Lev4<FT> *lc4, *lf4;
+  const Lev4<FT> *lc4, *lf4, *lr4;
   int Nv, Nf;
 };
 
@@ -35,20 +36,21 @@ struct ColLev {
 // the faces below/above and their g^33.
 template <class FT>
 struct Cen {
-  FT rJ, h, phir, Pi, thv, thvr, K, iJ, phi;
+  FT rJ, h, phid, Pi, thv, thvr, K, iJ, phi;
 };
 template <class FT>
 __device__ __forceinline__ Cen<FT> cdiag(const DevParams<FT> &P, const ColGeo<FT> &G, const ColLev<FT> &L, int v,
                                          FT rho, FT u1, FT u2, FT rhoe, FT u3a, FT u3b, FT g33a, FT g33b) {
-  const Lev4<FT> Lc = L.lc4[min(max(v, 0), L.Nv - 1)];
+  const int vc = min(max(v, 0), L.Nv - 1);
+  const Lev4<FT> Lc = L.lc4[vc];
   const FT c1 = (G.gu0 * u1 + G.gu1 * u2) * Lc.z, c2 = (G.gu1 * u1 + G.gu2 * u2) * Lc.z;
   const FT kv = (u3a * (u3a * g33a) + u3b * (u3b * g33b)) / FT(2);
   Cen<FT> o;
   o.K = (u1 * c1 + u2 * c2 + kv) / FT(2);
   Thermo<FT> th;
-  thermo(P, rho, rhoe, o.K, Lc.w, th);
+  thermo(P, rho, rhoe, o.K, Lc.w, L.lr4[vc], th);
   o.h = th.h;
-  o.phir = th.phir;
+  o.phid = th.phid;
   o.Pi = th.Pi;
   o.thv = th.thv;
   o.thvr = th.thvr;
@@ -183,7 +185,8 @@ __device__ __forceinline__ void newton_core(const DevParams<FT> &P, const ColGeo
     FT t3 = FT(0);
     if (inner) {
       const FT thd = ((prev.thv - prev.thvr) + (cur.thv - cur.thvr)) / FT(2);
-      t3 = -(LF[k].z - (cur.phir - prev.phir) + P.cpd * thd * (cur.Pi - prev.Pi));
+      // ᶠgradᵥ(Phi) - ᶠgradᵥ(Phi_r): the difference of Phi - Phi_r between the levels
+      t3 = -((cur.phid - prev.phid) + P.cpd * thd * (cur.Pi - prev.Pi));
     }
     T3[k] = t3 - beta * u3[k];
     if (inner) {

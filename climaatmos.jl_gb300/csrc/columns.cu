@@ -42,7 +42,7 @@ struct BatchArgs {
   const int *nv;            // z_elem per column
   const int *coff;          // centre offset per column (its faces start at coff + column)
   const int *lco, *lfo;     // offsets of the column's level tables
-  const Lev4<FT> *lc4, *lf4;
+  const Lev4<FT> *lc4, *lf4, *lr4;  // lr4: the levels' reference records (offsets of lc4)
   const FT *hat_c, *hat_f;  // U^
   FT *u_c, *u_f;            // the iterate
   double *rnorm;            // [ncols][MAX_ITERS][3]
@@ -56,7 +56,7 @@ __device__ __forceinline__ void solve_item(const DevParams<FT> &P, const BatchAr
   const bool colv = slot < w.y;
   const int c = B.order[w.x + (colv ? slot : 0)];  // idle groups repeat the item's first column, write nothing
   const int Nv = B.nv[c], Nf = Nv + 1, r0 = gl * CM;
-  const col::ColLev<FT> L{B.lc4 + B.lco[c], B.lf4 + B.lfo[c], Nv, Nf};
+  const col::ColLev<FT> L{B.lc4 + B.lco[c], B.lf4 + B.lfo[c], B.lr4 + B.lco[c], Nv, Nf};
   ColGeo<FT> Gm;  // flat column: J_h = 1, g^ij = identity
   Gm.Jh = FT(1); Gm.iJh = FT(1); Gm.gu0 = FT(1); Gm.gu1 = FT(0); Gm.gu2 = FT(1);
   const size_t cb = (size_t)B.coff[c] + r0, fb = (size_t)B.coff[c] + c + r0, sc = (size_t)B.ctot;
@@ -192,7 +192,7 @@ struct ColBase {
 template <class FT>
 struct ColImpl : ColBase {
   DevParams<FT> P{};
-  Buf lc4, lf4, nv, coff, lco, lfo, order, items[2], pitems, rnorm, rsum, queue, status;
+  Buf lc4, lf4, lr4, nv, coff, lco, lfo, order, items[2], pitems, rnorm, rsum, queue, status;
   int nitems[2] = {0, 0};
   struct Group { int item0, nitem, G; };
   std::vector<Group> groups;  // plain form: one per distinct z_elem
@@ -265,7 +265,7 @@ int create_t(gb_columns *cols) {
   const int n = cols->ncols;
   // level tables, one per distinct z_elem
   std::map<int, std::pair<int, int>> tab;  // z_elem -> (centre offset, face offset)
-  std::vector<double> c4, f4;
+  std::vector<double> c4, f4, r4;
   for (int z : cols->z) {
     if (tab.count(z)) continue;
     gb_config cz = c;
@@ -277,6 +277,9 @@ int create_t(gb_columns *cols) {
       zc[v] = (zf[v] + zf[v + 1]) / 2;
       const double dz = zf[v + 1] - zf[v];
       c4.insert(c4.end(), {dz, 1.0 / dz, 1.0, c.grav * zc[v]});
+      double ref[3];
+      reference_level(c, c.grav * zc[v], ref);
+      r4.insert(r4.end(), {ref[0], ref[1], ref[2], 0.0});
     }
     for (int k = 0; k <= z; ++k) {
       const double d = k == 0 ? zf[1] - zf[0] : k == z ? zf[z] - zf[z - 1] : (zf[k + 1] - zf[k - 1]) / 2;
@@ -284,7 +287,7 @@ int create_t(gb_columns *cols) {
       f4.insert(f4.end(), {1.0 / (d * d), beta_sponge(zf[k], c.sponge_zd, c.z_max, c.alpha_w), dphi, 0.0});
     }
   }
-  std::vector<FT> c4t(c4.begin(), c4.end()), f4t(f4.begin(), f4.end());
+  std::vector<FT> c4t(c4.begin(), c4.end()), f4t(f4.begin(), f4.end()), r4t(r4.begin(), r4.end());
   std::vector<int> coff(n), lco(n), lfo(n);
   long long o = 0;
   for (int i = 0; i < n; ++i) {
@@ -324,7 +327,8 @@ int create_t(gb_columns *cols) {
     s = t;
   }
   int r;
-  if ((r = bupload(cols, I->lc4, c4t)) || (r = bupload(cols, I->lf4, f4t)) || (r = bupload(cols, I->nv, cols->z)) ||
+  if ((r = bupload(cols, I->lc4, c4t)) || (r = bupload(cols, I->lf4, f4t)) || (r = bupload(cols, I->lr4, r4t)) ||
+      (r = bupload(cols, I->nv, cols->z)) ||
       (r = bupload(cols, I->coff, coff)) || (r = bupload(cols, I->lco, lco)) || (r = bupload(cols, I->lfo, lfo)) ||
       (r = bupload(cols, I->order, order)) || (r = bupload(cols, I->items[0], items[0])) ||
       (r = bupload(cols, I->items[1], items[1])) || (r = bupload(cols, I->pitems, pitems)))
@@ -342,6 +346,7 @@ int create_t(gb_columns *cols) {
   P.pref = (FT)c.p_ref; P.kappa = (FT)c.R_d / (FT)c.cp_d; P.Tmin_ref = (FT)c.T_min_ref;
   P.Tsfc_ref = (FT)c.T_surf_ref; P.Tmin_sgs = (FT)c.T_min_sgs;
   P.icvd = (FT)(1.0 / c.cv_d); P.ipref = (FT)(1.0 / c.p_ref);
+  P.cpTmin = (FT)(c.cp_d * c.T_min_ref);
   P.status = (int *)I->status.p;
   // resident CTAs of every persistent variant
   int dev = 0, nsm = 0;
@@ -370,7 +375,7 @@ BatchArgs<FT> args_for(gb_columns *cols, gb_fieldvec U, gb_fieldvec Uh, double d
   B.ncols = cols->ncols; B.nitems = nitems; B.iters = iters; B.ctot = (int)cols->ctot; B.dtg = (FT)dtg;
   B.items = items; B.order = (const int *)I->order.p; B.nv = (const int *)I->nv.p;
   B.coff = (const int *)I->coff.p; B.lco = (const int *)I->lco.p; B.lfo = (const int *)I->lfo.p;
-  B.lc4 = (const Lev4<FT> *)I->lc4.p; B.lf4 = (const Lev4<FT> *)I->lf4.p;
+  B.lc4 = (const Lev4<FT> *)I->lc4.p; B.lf4 = (const Lev4<FT> *)I->lf4.p; B.lr4 = (const Lev4<FT> *)I->lr4.p;
   B.hat_c = (const FT *)Uh.c; B.hat_f = (const FT *)Uh.f; B.u_c = (FT *)U.c; B.u_f = (FT *)U.f;
   B.rnorm = (double *)I->rnorm.p; B.queue = (int *)I->queue.p;
   return B;

@@ -35,6 +35,10 @@ struct DevParams {
   const FT *levf;  // [LF_N][Nf]
   const Lev4<FT> *lc4;  // [Nv] centres: {r^2 dz, 1 / (r^2 dz), 1 / r^2, Phi}
   const Lev4<FT> *lf4;  // [Nf] faces: {g^33, beta_w, Phi_c(v) - Phi_c(v-1) (0 on the boundary faces), 0}
+  // [Nv] centres: the level's reference record {p0, 1 / p0, cp_d (T_sfc - T_min) / 7 Pi0^7, 0}
+  // (reference_level, geometry.h) for Phi - Phi_r in deviation form
+  const Lev4<FT> *lr4;
+  FT cpTmin;  // cp_d T_min_ref
   const int *goff, *gcopy;
   const FT *gw, *ecov, *econ;  // ecov/econ: [Nh*16][6]
   int *status;
@@ -53,6 +57,11 @@ __device__ __forceinline__ float grcp(float a) { return __fdividef(1.0f, a); }
 __device__ __forceinline__ double grcp(double a) { return 1.0 / a; }
 __device__ __forceinline__ float gsin(float x) { return sinf(x); }
 __device__ __forceinline__ double gsin(double x) { return sin(x); }
+// ln(1 + x) and exp(x) - 1 for small x (the library functions, accurate near 0)
+__device__ __forceinline__ float glog1p(float x) { return log1pf(x); }
+__device__ __forceinline__ double glog1p(double x) { return log1p(x); }
+__device__ __forceinline__ float gexpm1(float x) { return expm1f(x); }
+__device__ __forceinline__ double gexpm1(double x) { return expm1(x); }
 
 template <class FT>
 __device__ __forceinline__ FT shfl(FT v, int src, int width) {
@@ -69,12 +78,21 @@ __device__ __forceinline__ FT shfl_down(FT v, int d) {
 
 // Dry thermodynamics of Thermodynamics.jl with e_int = cv_d (T - T_0) - R_d T_0,
 // and the hydrostatic reference state of src/utils/refstate_thermodynamics.jl.
+// phid = Phi - Phi_r(Pi), the geopotential less the reference state's at the point's
+// Exner pressure, which the pressure-gradient and hyperdiffusion terms take
+// (advection.jl:82-88, implicit_tendency.jl:286-293, hyperdiffusion.jl:142-147).
+// It is formed as a deviation from the level's reference record rl (Phi_r(Pi0) = Phi at
+// p0 = rl.x): with ln x = kappa ln(p / p0) = kappa log1p((p - p0) / p0),
+//   Phi - Phi_r(Pi) = cp_d T_min ln x + cp_d (T_sfc - T_min) / 7 Pi0^7 expm1(7 ln x),
+// the same quantity as Phi - Phi_r(Pi) written directly, without the cancellation of two
+// O(1e5) J/kg terms that costs FP32 most of its precision there.
 template <class FT>
 struct Thermo {
-  FT T, p, h, Pi, thv, thvr, phir;
+  FT T, p, h, Pi, thv, thvr, phid, Tr;
 };
 template <class FT>
-__device__ __forceinline__ void thermo(const DevParams<FT> &P, FT rho, FT rhoe, FT K, FT Phi, Thermo<FT> &o) {
+__device__ __forceinline__ void thermo(const DevParams<FT> &P, FT rho, FT rhoe, FT K, FT Phi, const Lev4<FT> &rl,
+                                       Thermo<FT> &o) {
   FT e_tot = gdiv(rhoe, rho);
   FT eint = e_tot - K - Phi;
   FT T = P.T0 + (eint + P.Rd * P.T0) * P.icvd;
@@ -90,7 +108,9 @@ __device__ __forceinline__ void thermo(const DevParams<FT> &P, FT rho, FT rhoe, 
   o.Pi = Pi;
   o.thv = T * iPi;
   o.thvr = Tr * iPi;
-  o.phir = -P.cpd * (P.Tmin_ref * glog(Pi) + (P.Tsfc_ref - P.Tmin_ref) / FT(7) * (Pi7 - FT(1)));
+  o.Tr = Tr;
+  const FT lx = P.kappa * glog1p((p - rl.x) * rl.y);
+  o.phid = P.cpTmin * lx + rl.z * gexpm1(FT(7) * lx);
 }
 // Reverse mode of thermo(): the cotangents of its outputs (T, p, h, Pi, thv,
 // thvr, phir) and of the reference temperature T_r(Pi) give those of
@@ -128,10 +148,12 @@ __device__ __forceinline__ void thermo_vjp(const DevParams<FT> &P, FT rho, FT rh
   K_b = Kb;
 }
 
+// The hyperdiffused dry static energy less its reference value,
+// s_d - s_d,r = cp_d (T - T_0) + Phi - (cp_d (T_r - T_0) + Phi_r) = cp_d (T - T_r) + phid
+// (TD.dry_static_energy and sd_r, hyperdiffusion.jl:142-147, refstate_thermodynamics.jl).
 template <class FT>
-__device__ __forceinline__ FT sd_r(const DevParams<FT> &P, FT Pi, FT phir) {
-  FT Pi2 = Pi * Pi, Pi7 = Pi2 * Pi2 * Pi2 * Pi;
-  return P.cpd * (P.Tmin_ref + (P.Tsfc_ref - P.Tmin_ref) * Pi7 - P.T0) + phir;
+__device__ __forceinline__ FT sd_dev(const DevParams<FT> &P, const Thermo<FT> &th) {
+  return P.cpd * (th.T - th.Tr) + th.phid;
 }
 
 // Per-column horizontal geometry (surface metric of one node).

@@ -36,7 +36,7 @@ struct ImplBase {
 template <class FT>
 struct Impl : ImplBase {
   DevParams<FT> P{};
-  DevBuf hgeo, levc, levf, lc4, lf4, goff, gcopy, gw, ecov, econ, status;
+  DevBuf hgeo, levc, levf, lc4, lf4, lr4, goff, gcopy, gw, ecov, econ, status;
   DevBuf lap, U, Te[4], Ti[4], jac, rnorm, partials, sums, rsum;
   size_t NC = 0, NF = 0, NR = 0;  // centre, face and reduced-centre element counts
   int nsum_blocks = 0;
@@ -150,13 +150,16 @@ int create_impl(gb_ctx *ctx) {
   if ((r = upload<FT>(ctx, I->levf, g.levf))) return r;
   {
     const int nv = g.Nv, nf = nv + 1;
-    std::vector<double> c4((size_t)4 * nv), f4((size_t)4 * nf, 0.0);
+    std::vector<double> c4((size_t)4 * nv), f4((size_t)4 * nf, 0.0), r4((size_t)4 * nv, 0.0);
     for (int v = 0; v < nv; ++v) {
       const double r2dz = g.levc[LC_R2 * nv + v] * g.levc[LC_DZ * nv + v];
       c4[4 * v + 0] = r2dz;
       c4[4 * v + 1] = 1.0 / r2dz;
       c4[4 * v + 2] = g.levc[LC_IR2 * nv + v];
       c4[4 * v + 3] = g.levc[LC_PHI * nv + v];
+      r4[4 * v + 0] = g.levc[LC_P0 * nv + v];
+      r4[4 * v + 1] = g.levc[LC_IP0 * nv + v];
+      r4[4 * v + 2] = g.levc[LC_RB * nv + v];
     }
     for (int f = 0; f < nf; ++f) {
       f4[4 * f + 0] = g.levf[LF_G33 * nf + f];
@@ -165,6 +168,7 @@ int create_impl(gb_ctx *ctx) {
     }
     if ((r = upload<FT>(ctx, I->lc4, c4))) return r;
     if ((r = upload<FT>(ctx, I->lf4, f4))) return r;
+    if ((r = upload<FT>(ctx, I->lr4, r4))) return r;
   }
   if ((r = upload_i(ctx, I->goff, g.grp_off))) return r;
   if ((r = upload_i(ctx, I->gcopy, g.grp_copy))) return r;
@@ -193,6 +197,7 @@ int create_impl(gb_ctx *ctx) {
   P.pref = (FT)c.p_ref; P.kappa = (FT)c.R_d / (FT)c.cp_d; P.Tmin_ref = (FT)c.T_min_ref;
   P.Tsfc_ref = (FT)c.T_surf_ref; P.Tmin_sgs = (FT)c.T_min_sgs;
   P.icvd = (FT)(1.0 / c.cv_d); P.ipref = (FT)(1.0 / c.p_ref);
+  P.cpTmin = (FT)(c.cp_d * c.T_min_ref);
   P.nu_v = (FT)c.nu_v; P.nu_s = (FT)c.nu_s; P.div_damp = (FT)c.div_damp; P.dt_model = (FT)c.dt;
   P.hs = c.held_suarez ? 1 : 0;
   if (P.hs) {
@@ -209,7 +214,7 @@ int create_impl(gb_ctx *ctx) {
   for (int i = 0; i < NQ; ++i)
     for (int k = 0; k < NQ; ++k) P.D[i * NQ + k] = (FT)g.D[i][k];
   P.hgeo = (const FT *)I->hgeo.p; P.levc = (const FT *)I->levc.p; P.levf = (const FT *)I->levf.p;
-  P.lc4 = (const Lev4<FT> *)I->lc4.p; P.lf4 = (const Lev4<FT> *)I->lf4.p;
+  P.lc4 = (const Lev4<FT> *)I->lc4.p; P.lf4 = (const Lev4<FT> *)I->lf4.p; P.lr4 = (const Lev4<FT> *)I->lr4.p;
   P.goff = (const int *)I->goff.p; P.gcopy = (const int *)I->gcopy.p; P.gw = (const FT *)I->gw.p;
   P.ecov = (const FT *)I->ecov.p; P.econ = (const FT *)I->econ.p;
   P.status = (int *)I->status.p;

@@ -86,6 +86,22 @@ double beta_sponge(double z, double zd, double zmax, double alpha) {
   return alpha * s * s;
 }
 
+void reference_level(const gb_config &c, double Phi, double out[3]) {
+  const double cp = c.cp_d, tm = c.T_min_ref, dT = c.T_surf_ref - c.T_min_ref, kappa = c.R_d / c.cp_d;
+  double P = 1.0;
+  for (int it = 0; it < 100; ++it) {
+    const double f = -cp * (tm * std::log(P) + dT / 7.0 * (std::pow(P, 7.0) - 1.0)) - Phi;
+    const double df = -cp * (tm / P + dT * std::pow(P, 6.0));
+    const double step = f / df;
+    P -= step;
+    if (std::fabs(step) < 1e-16 * P) break;
+  }
+  const double p0 = c.p_ref * std::pow(P, 1.0 / kappa);
+  out[0] = p0;
+  out[1] = 1.0 / p0;
+  out[2] = cp * dT / 7.0 * std::pow(P, 7.0);
+}
+
 void caller_node(int o, int i, int j, int &ic, int &jc) {
   // the caller's (i', j') of library node (i, j) in a frame turned by o quarter turns
   switch (o & 3) {
@@ -312,6 +328,11 @@ void build_geometry(const gb_config &c, HostGeometry &g) {
     g.levc[LC_IR2 * Nv + v] = 1.0 / (g.rc[v] * g.rc[v]);
     g.levc[LC_IDZ * Nv + v] = 1.0 / g.dzc[v];
     g.levc[LC_SPG * Nv + v] = beta_sponge(g.zc[v], c.sponge_zd, c.z_max, 1.0);
+    double ref[3];
+    reference_level(c, c.grav * g.zc[v], ref);
+    g.levc[LC_P0 * Nv + v] = ref[0];
+    g.levc[LC_IP0 * Nv + v] = ref[1];
+    g.levc[LC_RB * Nv + v] = ref[2];
   }
   g.levf.assign((size_t)LF_N * Nf, 0);
   for (int k = 0; k < Nf; ++k) {

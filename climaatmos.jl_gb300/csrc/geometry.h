@@ -14,7 +14,10 @@ constexpr int NN = 16;
 enum HGeo { HG_JH = 0, HG_GU0, HG_GU1, HG_GU2, HG_GD0, HG_GD1, HG_GD2, HG_F3, HG_FH1, HG_FH2, HG_IJH, HG_S2, HG_N };
 // Per-level centre quantities ([q][Nv]).
 // LC_SPG / LF_SPG: the sponge shape s(z) (beta = alpha s(z)), for the sponge-rate derivative.
-enum LevC { LC_Z = 0, LC_R2, LC_DZ, LC_PHI, LC_BETA, LC_IR2, LC_IDZ, LC_SPG, LC_N };
+// LC_P0, LC_IP0, LC_RB: the level's reference record (reference_level()): the pressure p0 of
+// the hydrostatic reference state at the level's geopotential, 1 / p0, and
+// cp_d (T_sfc - T_min) / 7 Pi0^7.
+enum LevC { LC_Z = 0, LC_R2, LC_DZ, LC_PHI, LC_BETA, LC_IR2, LC_IDZ, LC_SPG, LC_P0, LC_IP0, LC_RB, LC_N };
 // Per-level face quantities ([q][Nv+1]).
 enum LevF { LF_Z = 0, LF_R2, LF_DZ, LF_RINV, LF_BETA, LF_DPHI, LF_IR2, LF_IDZ, LF_G33, LF_SPG, LF_N };
 
@@ -44,5 +47,12 @@ bool match_elements(const gb_config &cfg, const double *xyz, int *elem_map, int 
 std::vector<double> vertical_faces(const gb_config &cfg);
 // Rayleigh sponge rate alpha sin^2(pi/2 (z - z_d)/(z_max - z_d)) above z_d (rayleigh_sponge.jl:39-44).
 double beta_sponge(double z, double zd, double zmax, double alpha);
+// The reference record of a level of geopotential Phi: the Exner value Pi0 at which the
+// reference state's geopotential Phi_r(Pi0) = -cp_d (T_min ln Pi0 + (T_sfc - T_min) / 7 (Pi0^7 - 1))
+// (src/utils/refstate_thermodynamics.jl:58-166) equals Phi, found by Newton's method in FP64;
+// out = {p0 = p_ref Pi0^(1/kappa), 1 / p0, cp_d (T_sfc - T_min) / 7 Pi0^7}.  The kernels form
+// Phi - Phi_r(Pi) as a deviation from it, cp_d T_min ln x + out[2] (x^7 - 1) with
+// x = Pi / Pi0 = (p / p0)^kappa, so that no two O(1e5) terms cancel in FP32.
+void reference_level(const gb_config &cfg, double Phi, double out[3]);
 
 }  // namespace gb

@@ -126,7 +126,7 @@ struct ColState {
 };
 template <class FT, int M>
 struct ColDiag {
-  FT c1[M], c2[M], K[M], T[M], h[M], Pi[M], thv[M], thvr[M], phir[M], rJ[M], u3c[M], J[M], iJ[M];
+  FT c1[M], c2[M], K[M], T[M], h[M], Pi[M], thv[M], thvr[M], phid[M], rJ[M], u3c[M], J[M], iJ[M];
 };
 
 
@@ -152,9 +152,9 @@ __device__ __forceinline__ void col_diag(const DevParams<FT> &P, const ColGeo<FT
     const FT kv = (S.u3[k] * Dg.u3c[k] + u3n[k] * u3cn[k]) / FT(2);
     const FT K = (S.u1[k] * c1 + S.u2[k] * c2 + kv) / FT(2);
     Thermo<FT> th;
-    thermo(P, S.rho[k], S.rhoe[k], K, Phi, th);
+    thermo(P, S.rho[k], S.rhoe[k], K, Phi, P.lr4[v], th);
     Dg.c1[k] = c1; Dg.c2[k] = c2; Dg.K[k] = K; Dg.T[k] = th.T; Dg.h[k] = th.h; Dg.Pi[k] = th.Pi;
-    Dg.thv[k] = th.thv; Dg.thvr[k] = th.thvr; Dg.phir[k] = th.phir;
+    Dg.thv[k] = th.thv; Dg.thvr[k] = th.thvr; Dg.phid[k] = th.phid;
     Dg.J[k] = G.Jh * r2 * dz;
     Dg.iJ[k] = G.iJh * ir2 * P.levc[LC_IDZ * Nv + v];
     Dg.rJ[k] = S.rho[k] * Dg.J[k];
@@ -167,7 +167,7 @@ __device__ __forceinline__ void col_implicit(const DevParams<FT> &P, const ColGe
                                              const ColDiag<FT, M> &Dg, FT (&Tr)[M], FT (&Te)[M], FT (&T3)[M], int lane) {
   const int Nv = P.Nv, Nf = P.Nf;
   FT rJm[M], hm[M], phm[M], Pim[M], thm[M], thrm[M];
-  nb_all<M, -1>(Dg.rJ, rJm); nb_all<M, -1>(Dg.h, hm); nb_all<M, -1>(Dg.phir, phm);
+  nb_all<M, -1>(Dg.rJ, rJm); nb_all<M, -1>(Dg.h, hm); nb_all<M, -1>(Dg.phid, phm);
   nb_all<M, -1>(Dg.Pi, Pim); nb_all<M, -1>(Dg.thv, thm); nb_all<M, -1>(Dg.thvr, thrm);
   FT flux[M], fh[M];
 #pragma unroll
@@ -182,10 +182,11 @@ __device__ __forceinline__ void col_implicit(const DevParams<FT> &P, const ColGe
     fh[k] = inner ? F * hb : FT(0);
     FT val = 0;
     if (inner) {
-      const FT gPhir = Dg.phir[k] - phm[k];
+      // ᶠgradᵥ(Phi) - ᶠgradᵥ(Phi_r) as the difference of Phi - Phi_r between the levels
+      const FT gPhid = Dg.phid[k] - phm[k];
       const FT thd = ((thm[k] - thrm[k]) + (Dg.thv[k] - Dg.thvr[k])) / FT(2);
       const FT gPi = Dg.Pi[k] - Pim[k];
-      val = -(P.levf[LF_DPHI * Nf + fc] - gPhir + P.cpd * thd * gPi);
+      val = -(gPhid + P.cpd * thd * gPi);
     }
     val -= P.levf[LF_BETA * Nf + fc] * S.u3[k];
     T3[k] = val;

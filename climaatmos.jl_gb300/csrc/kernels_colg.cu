@@ -91,7 +91,7 @@ __global__ void __launch_bounds__(CG_THREADS, MINB) k_col_stage_g(DevParams<FT> 
     if (v >= Nf) H[4][k] = FT(0);
   }
   // ---- one Newton iteration from U = U^, then the post-Newton correction
-  const col::ColLev<FT> L{P.lc4, P.lf4, Nv, Nf};
+  const col::ColLev<FT> L{P.lc4, P.lf4, P.lr4, Nv, Nf};
   FT U[5][CM];
 #pragma unroll
   for (int c = 0; c < 5; ++c)

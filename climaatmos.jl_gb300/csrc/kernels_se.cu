@@ -120,6 +120,7 @@ __global__ void __launch_bounds__(SE_THREADS, SeMinBlocks<FT>::value) k_passA(De
       LevRow<FT> s;
       s.set(g, P.levc[LC_R2 * Nv + v], P.levc[LC_IR2 * Nv + v], P.levc[LC_DZ * Nv + v], P.levc[LC_IDZ * Nv + v]);
       const FT Phi = P.levc[LC_PHI * Nv + v];
+      const Lev4<FT> rl = P.lr4[v];
       const FT g3a = P.levf[LF_G33 * Nf + v], g3b = P.levf[LF_G33 * Nf + v + 1];
       FT u1[4], u2[4], ub3[4], sd[4];
 #pragma unroll
@@ -138,8 +139,8 @@ __global__ void __launch_bounds__(SE_THREADS, SeMinBlocks<FT>::value) k_passA(De
         const FT c1 = gu0 * u1[i] + gu1 * u2[i], c2 = gu1 * u1[i] + gu2 * u2[i];
         const FT K = (u1[i] * c1 + u2[i] * c2 + kv) / FT(2);
         Thermo<FT> th;
-        thermo(P, rho, rhoe, K, Phi, th);
-        sd[i] = P.cpd * (th.T - P.T0) + Phi - sd_r(P, th.Pi, th.phir);
+        thermo(P, rho, rhoe, K, Phi, rl, th);
+        sd[i] = sd_dev(P, th);
       }
       FT o1[4], o2[4], o3[4];
       vec_lap(P, R, g, s, u1, u2, ub3, FT(1), o1, o2, o3);
@@ -267,6 +268,7 @@ __global__ void __launch_bounds__(SE_THREADS, SeMinBlocks<FT>::value) k_passB(De
       const bool act = v0 + vs < Nv;
       const FT idz = P.levc[LC_IDZ * Nv + v];
       const FT Phi = P.levc[LC_PHI * Nv + v], beta = P.levc[LC_BETA * Nv + v];
+      const Lev4<FT> rl = P.lr4[v];
       const FT g3a = P.levf[LF_G33 * Nf + v], g3b = P.levf[LF_G33 * Nf + v + 1];
       LevRow<FT> s;
       {
@@ -302,12 +304,12 @@ __global__ void __launch_bounds__(SE_THREADS, SeMinBlocks<FT>::value) k_passB(De
             const FT kv = (fa * (fa * g3a) + fb * (fb * g3b)) / FT(2);
             K[i] = (u1[i] * c1[i] + u2[i] * c2[i] + kv) / FT(2);
             Thermo<FT> th;
-            thermo(P, rho[i], sY[48 * Nv + q], K[i], Phi, th);
+            thermo(P, rho[i], sY[48 * Nv + q], K[i], Phi, rl, th);
             h[i] = th.h;
             Pi[i] = th.Pi;
             thp[i] = th.thv - th.thvr;
             // grad(K + Phi - Phi_r) and (cp_d / 2) grad(th' Pi) taken as one gradient
-            gg[i] = (K[i] + Phi - th.phir) + P.cpd * (thp[i] * Pi[i]) / FT(2);
+            gg[i] = (K[i] + th.phid) + P.cpd * (thp[i] * Pi[i]) / FT(2);
             if (HS) {
               // Held-Suarez forcing (held_suarez.jl:98-141, 203-225, 279-295), flat surface:
               // sigma = p / MSLP; rho e_tot relaxes with -cv_d k_T rho (p / (rho R_d) - T_eq)

@@ -1019,6 +1019,7 @@ int gb_geometry_export(const gb_config *cfg, gb_geometry_host *out) {
     build_geometry(*cfg, g);
     auto cp = [](double *dst, const std::vector<double> &v) { if (dst) std::memcpy(dst, v.data(), v.size() * sizeof(double)); };
     cp(out->xyz, g.xyz); cp(out->ecov, g.ecov); cp(out->Jh, g.Jh); cp(out->gup, g.gup); cp(out->fh0, g.fh0); cp(out->zf, g.zf);
+    cp(out->econ, g.econ); cp(out->dss_w, g.grp_w);
     if (out->dss_off) std::memcpy(out->dss_off, g.grp_off.data(), g.grp_off.size() * sizeof(int));
     if (out->dss_copy) std::memcpy(out->dss_copy, g.grp_copy.data(), g.grp_copy.size() * sizeof(int));
   } catch (...) {

@@ -15,7 +15,10 @@ constexpr int DSS_THREADS = 256;  // 8 groups per CTA, one warp per group
 // per group, lanes over levels.
 // Two levels per lane (v0 + lane and v0 + 32 + lane), so that each lane has
 // two independent gathers in flight; per level the sums run in the same copy
-// order as with one level per lane.
+// order as with one level per lane.  Every product and sum is an explicit
+// fused multiply-add or rounded product, so the rounding does not depend on
+// the compiler's contraction choices (the oracle's DSS does the same
+// operations in the same order and matches bit for bit).
 template <class FT>
 __global__ void __launch_bounds__(DSS_THREADS) k_dss(DevParams<FT> P, FT *__restrict__ C, FT *__restrict__ F) {
   const int lane = threadIdx.x & 31;
@@ -37,12 +40,12 @@ __global__ void __launch_bounds__(DSS_THREADS) k_dss(DevParams<FT> P, FT *__rest
         for (int h = 0; h < 2; ++h) {
           if (!ok[h]) continue;
           const size_t b = b0 + v[h];
-          s0[h] += w * C[b];
-          s3[h] += w * C[b + 48 * Nv];
+          s0[h] = fma(w, C[b], s0[h]);
+          s3[h] = fma(w, C[b + 48 * Nv], s3[h]);
           const FT u1 = C[b + 16 * Nv], u2 = C[b + 32 * Nv];
-          X0[h] += w * (u1 * ec[0] + u2 * ec[3]);
-          X1[h] += w * (u1 * ec[1] + u2 * ec[4]);
-          X2[h] += w * (u1 * ec[2] + u2 * ec[5]);
+          X0[h] = fma(w, fma(u2, ec[3], mul_rn(u1, ec[0])), X0[h]);
+          X1[h] = fma(w, fma(u2, ec[4], mul_rn(u1, ec[1])), X1[h]);
+          X2[h] = fma(w, fma(u2, ec[5], mul_rn(u1, ec[2])), X2[h]);
         }
       }
       for (int c = o0; c < o1; ++c) {
@@ -55,8 +58,8 @@ __global__ void __launch_bounds__(DSS_THREADS) k_dss(DevParams<FT> P, FT *__rest
           const size_t b = b0 + v[h];
           C[b] = s0[h];
           C[b + 48 * Nv] = s3[h];
-          C[b + 16 * Nv] = eo[0] * X0[h] + eo[1] * X1[h] + eo[2] * X2[h];
-          C[b + 32 * Nv] = eo[3] * X0[h] + eo[4] * X1[h] + eo[5] * X2[h];
+          C[b + 16 * Nv] = fma(eo[2], X2[h], fma(eo[1], X1[h], mul_rn(eo[0], X0[h])));
+          C[b + 32 * Nv] = fma(eo[5], X2[h], fma(eo[4], X1[h], mul_rn(eo[3], X0[h])));
         }
       }
     }
@@ -71,7 +74,7 @@ __global__ void __launch_bounds__(DSS_THREADS) k_dss(DevParams<FT> P, FT *__rest
         const size_t b0 = (size_t)P.gcopy[c] * Nf;
 #pragma unroll
         for (int h = 0; h < 2; ++h)
-          if (ok[h]) sf[h] += w * F[b0 + k[h]];
+          if (ok[h]) sf[h] = fma(w, F[b0 + k[h]], sf[h]);
       }
       for (int c = o0; c < o1; ++c) {
         const size_t b0 = (size_t)P.gcopy[c] * Nf;

@@ -56,7 +56,7 @@ _ip = ctypes.POINTER(ctypes.c_int)
 
 class GBGeometryHost(ctypes.Structure):
     _fields_ = [("xyz", _dp), ("ecov", _dp), ("Jh", _dp), ("gup", _dp), ("fh0", _dp), ("zf", _dp),
-                ("dss_off", _ip), ("dss_copy", _ip)]
+                ("dss_off", _ip), ("dss_copy", _ip), ("econ", _dp), ("dss_w", _dp)]
 
 
 class GBError(RuntimeError):

@@ -49,11 +49,14 @@ class Geometry:
         self.zf = np.zeros(self.Nv + 1)
         self.dss_off = np.zeros(ng.value + 1, np.int32)
         self.dss_copy = np.zeros(ncp.value, np.int32)
+        self.econ = np.zeros((self.Nh, 16, 2, 3))
+        self.dss_w = np.zeros(ncp.value)
         g = N.GBGeometryHost()
         dp = lambda a: a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
         ip = lambda a: a.ctypes.data_as(ctypes.POINTER(ctypes.c_int))
         g.xyz, g.ecov, g.Jh, g.gup, g.fh0, g.zf = dp(self.xyz), dp(self.ecov), dp(self.Jh), dp(self.gup), dp(self.fh0), dp(self.zf)
         g.dss_off, g.dss_copy = ip(self.dss_off), ip(self.dss_copy)
+        g.econ, g.dss_w = dp(self.econ), dp(self.dss_w)
         _check(None, L.gb_geometry_export(ctypes.byref(c), ctypes.byref(g)))
         self.zc = 0.5 * (self.zf[1:] + self.zf[:-1])
         self.n_center, self.n_face = nc.value, nf.value

@@ -95,6 +95,8 @@ typedef struct {
   int *dss_off;  /* [ngroups+1] */
   int *dss_copy; /* [ncopies] element*16 + node, in the library's element order within a group
                     (ascending without elem_map) */
+  double *econ;  /* [Nh*16*2*3] contravariant basis at radius R, Cartesian */
+  double *dss_w; /* [ncopies] the J-weight of each copy in its group */
 } gb_geometry_host;
 
 /* Sizes for a configuration (no GPU needed). */

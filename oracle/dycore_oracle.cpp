@@ -332,23 +332,25 @@ struct Oracle {
 #pragma omp parallel for
     for (int g = 0; g < G; ++g) {
       for (int v = 0; v < levels; ++v) {
+        // the weighted sums as fused multiply-adds in ascending copy order (an exact
+        // rounding recipe, so that a GPU DSS doing the same operations agrees bit for bit)
         FT s0 = 0, s3 = 0, X[3] = {0, 0, 0};
         for (int c = goff[g]; c < goff[g + 1]; ++c) {
           int idx = gcopy[c], e = idx / NN, n = idx % NN;
           FT w = gw[c];
-          s0 += w * C[ci(e, 0, n, v)];
-          s3 += w * C[ci(e, 3, n, v)];
+          s0 = std::fma(w, C[ci(e, 0, n, v)], s0);
+          s3 = std::fma(w, C[ci(e, 3, n, v)], s3);
           FT u1 = C[ci(e, 1, n, v)], u2 = C[ci(e, 2, n, v)];
           const FT *ec = &econ[hn(e, n) * 6];
-          for (int d = 0; d < 3; ++d) X[d] += w * (u1 * ec[d] + u2 * ec[3 + d]);
+          for (int d = 0; d < 3; ++d) X[d] = std::fma(w, std::fma(u2, ec[3 + d], u1 * ec[d]), X[d]);
         }
         for (int c = goff[g]; c < goff[g + 1]; ++c) {
           int idx = gcopy[c], e = idx / NN, n = idx % NN;
           C[ci(e, 0, n, v)] = s0;
           C[ci(e, 3, n, v)] = s3;
           const FT *eo = &ecov[hn(e, n) * 6];
-          C[ci(e, 1, n, v)] = eo[0] * X[0] + eo[1] * X[1] + eo[2] * X[2];
-          C[ci(e, 2, n, v)] = eo[3] * X[0] + eo[4] * X[1] + eo[5] * X[2];
+          C[ci(e, 1, n, v)] = std::fma(eo[2], X[2], std::fma(eo[1], X[1], eo[0] * X[0]));
+          C[ci(e, 2, n, v)] = std::fma(eo[5], X[2], std::fma(eo[4], X[1], eo[3] * X[0]));
         }
       }
     }
@@ -361,7 +363,7 @@ struct Oracle {
         FT s = 0;
         for (int c = goff[g]; c < goff[g + 1]; ++c) {
           int idx = gcopy[c];
-          s += gw[c] * F[fi(idx / NN, idx % NN, k)];
+          s = std::fma(gw[c], F[fi(idx / NN, idx % NN, k)], s);
         }
         for (int c = goff[g]; c < goff[g + 1]; ++c) {
           int idx = gcopy[c];

@@ -22,6 +22,20 @@ def make_oracle(cfg, dtype=np.float64, dss_stage1=True):
     return O.Oracle(oracle_geometry(cfg64), cfg64.oracle_params(dss_stage1=dss_stage1), dtype)
 
 
+def dss_oracle_on_product_grid(cfg, dtype=np.float64):
+    """An oracle whose DSS plan and bases are the library's own (gb_geometry_export), so
+    that a DSS comparison sees the summation and nothing of the two grids' last-bit
+    differences (the grids themselves agree to 1e-14, test_geometry.py)."""
+    import copy
+    from gbdycore.simulation import Geometry
+    cfg64 = cfg.with_(ft=np.float64)
+    g = copy.copy(oracle_geometry(cfg64))
+    pg = Geometry(cfg64)
+    g.ecov, g.econ = pg.ecov, pg.econ
+    g.dss_off, g.dss_copy, g.dss_w = pg.dss_off, pg.dss_copy, pg.dss_w
+    return O.Oracle(g, cfg64.oracle_params(), dtype)
+
+
 def state(cfg, workload="plain", dtype=np.float64, geom=None):
     g = geom or oracle_geometry(cfg)
     Yc, Yf = S.workload_state(g, cfg, workload)

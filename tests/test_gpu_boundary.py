@@ -41,8 +41,11 @@ def test_fused_step_in_a_caller_layout(rotate):
         np.testing.assert_array_equal(out[0], ref[0])
         np.testing.assert_array_equal(out[1], ref[1])
     else:
+        # the turned frames run the derivatives in another order: FP64 roundoff, with u_3's
+        # tendency a cancellation of terms ~1e3 times |u_3| (as against the oracle)
         e = field_errors(out[0], out[1], ref[0], ref[1])
-        assert all(v <= 1e-12 for v in e.values()), e
+        lim = {"rho": 1e-14, "rho_e_tot": 1e-14, "u_1": 1e-12, "u_2": 1e-12, "u_3": 2e-11}
+        assert all(e[k] <= lim[k] for k in lim), e
 
 
 def test_hooks_in_a_permuted_layout_fp32():

@@ -1,9 +1,14 @@
 """GPU parity: every hook and the fused ARS343 step through the C ABI against the CPU oracle.
 
 Tolerances (max-norm error relative to each component's max magnitude):
-  FP64 hooks and steps: <= 1e-11 / 1e-10 (roundoff of a different but
-    equivalent evaluation order: FMA contraction, shuffle-based derivatives,
-    parallel cyclic reduction instead of the Thomas algorithm);
+  FP64 hooks: <= 1e-12 (measured <= 1.1e-13; ldiv 6.6e-15);
+  FP64 steps: rho, rho e_tot <= 1e-14, u_h <= 1e-12 and u_3 <= 2e-11 after three
+    steps on the small grids.  u_3's tendency is the difference of gravity and the
+    vertical pressure gradient, each about g dz, while the test states carry
+    |u_3| ~ 0.05 m/s x dz: FP64 roundoff of those terms is ~1e-12 of max |u_3| per
+    step whatever the evaluation order (the column solve alone agrees to 7e-15, so
+    the order of the tridiagonal solve is not the source).  At the production grid
+    (h_elem 30, z_elem 63) the whole step is held to the 1e-12 target;
   FP32 GPU against the FP32 oracle: <= 1e-4 for tendencies (cancellation in
     the pressure-gradient terms), and the FP32 step against the FP64 oracle
     per prognostic field with the bounds written in each test.
@@ -14,7 +19,7 @@ import torch
 
 from gbdycore import config as C
 from gbdycore import simulation as sim
-from helpers import field_errors, make_oracle, perturbed_state, small_config, state
+from helpers import dss_oracle_on_product_grid, field_errors, make_oracle, perturbed_state, small_config, state
 
 pytestmark = pytest.mark.gpu
 
@@ -37,7 +42,14 @@ def _assert_errs(errs, tol, skip=()):
     assert not bad, "errors above %g: %s (all: %s)" % (tol, bad, errs)
 
 
-FT_CASES = [(np.float64, 1e-11), (np.float32, 1e-4)]
+FT_CASES = [(np.float64, 1e-12), (np.float32, 1e-4)]
+
+
+def _assert_step_fp64(e):
+    """FP64 steps on the small grids (see the module docstring for u_3)."""
+    bad = {k: v for k, v in e.items()
+           if not v <= {"rho": 1e-14, "rho_e_tot": 1e-14, "u_1": 1e-12, "u_2": 1e-12, "u_3": 2e-11}[k]}
+    assert not bad, (bad, e)
 
 
 @pytest.mark.parametrize("ft,tol", FT_CASES)
@@ -76,7 +88,7 @@ def test_implicit_tendency_and_correction(ft, tol):
     assert np.abs(Yt.c[:, :3].cpu().numpy()).max() == 0 and np.abs(Yt.f.cpu().numpy()).max() == 0
 
 
-@pytest.mark.parametrize("ft,tol", [(np.float64, 1e-10), (np.float32, 1e-3)])
+@pytest.mark.parametrize("ft,tol", [(np.float64, 1e-13), (np.float32, 1e-3)])
 def test_jacobian_and_ldiv(ft, tol):
     cfg = small_config(ft=ft, z_elem=40)   # two levels per lane
     Yc, Yf = perturbed_state(cfg, dtype=ft, w_amp=0.3)
@@ -98,21 +110,30 @@ def test_jacobian_and_ldiv(ft, tol):
     _assert_errs(_errs(dY, ref), tol)
 
 
-@pytest.mark.parametrize("ft,tol", [(np.float64, 0.0), (np.float32, 0.0)])
-def test_dss_matches_oracle_bitwise_order(ft, tol):
+@pytest.mark.parametrize("ft", [np.float64, np.float32])
+def test_dss_matches_oracle_bitwise(ft):
+    """The DSS sums every group's copies in one fixed order with an explicit fused
+    multiply-add recipe; the oracle's DSS does the same operations, so on the same grid
+    tables the two agree bit for bit (deterministic, no atomics)."""
     cfg = small_config(ft=ft)
     Yc, Yf = perturbed_state(cfg, dtype=ft)
     rng = np.random.default_rng(2)
     Yc = (Yc * (1 + 1e-3 * rng.normal(size=Yc.shape))).astype(ft)   # break continuity
-    o = make_oracle(cfg, ft)
+    Yf = (Yf + 1e-3 * rng.normal(size=Yf.shape)).astype(ft)
+    o = dss_oracle_on_product_grid(cfg, ft)
     rc, rf = Yc.copy(), Yf.copy()
     o.dss(rc, rf)
     p = _cache(cfg)
     Y = _dev(Yc, Yf)
     sim.dss(Y, p, 0.0)
-    e = _errs(Y, (rc, rf))
-    lim = 1e-14 if ft == np.float64 else 1e-6
-    _assert_errs(e, lim)
+    gc, gf = Y.numpy()
+    np.testing.assert_array_equal(gc, rc)
+    np.testing.assert_array_equal(gf, rf)
+    # and against the independently built oracle grid, to the grids' agreement
+    o2 = make_oracle(cfg, ft)
+    rc2, rf2 = Yc.copy(), Yf.copy()
+    o2.dss(rc2, rf2)
+    _assert_errs(_errs(Y, (rc2, rf2)), 1e-14 if ft == np.float64 else 1e-6)
 
 
 @pytest.mark.parametrize("stretch,z_elem", [(False, 10), (True, 40), (True, 70)])
@@ -124,7 +145,7 @@ def test_fused_step_fp64_matches_oracle(stretch, z_elem):
     o.step(rc, rf, cfg.dt, 3)
     s = sim.AtmosSimulation(cfg, state=(Yc, Yf))
     s.step(3, use_graph=True)
-    _assert_errs(_errs(s.Y, (rc, rf)), 1e-10)
+    _assert_step_fp64(_errs(s.Y, (rc, rf)))
 
 
 def test_hook_loop_matches_fused_step():
@@ -136,7 +157,7 @@ def test_hook_loop_matches_fused_step():
     Y = _dev(Yc, Yf)
     for k in range(2):
         sim.ars343_step_via_hooks(Y, p, k * cfg.dt, cfg.dt)
-    _assert_errs(_errs(Y, a.Y.numpy()), 1e-10)
+    _assert_step_fp64(_errs(Y, a.Y.numpy()))
 
 
 def test_plain_workload_fp32_against_fp64_oracle():
@@ -250,3 +271,33 @@ def test_resting_atmosphere_stays_at_rest():
         m = a.reshape(-1, a.shape[-1]).mean(axis=0)
         scale = max(np.abs(a).max(), 1e-300)
         assert np.abs(a - m).max() <= 1e-11 * scale, name
+
+
+def test_production_step_matches_oracle():
+    """The production grid (h_elem 30, z_elem 63 tanh-stretched from 30 m, dt 120 s, the
+    workload's perturbed state): FP64 steps against the FP64 oracle within the 1e-12
+    target per prognostic field, and FP32 steps against the FP64 oracle."""
+    import oracle as O
+    O.set_threads(O.max_threads())
+    cfg64 = C.production_h30().with_(ft=np.float64)
+    Yc, Yf = state(cfg64, "production")
+    o = make_oracle(cfg64, np.float64, dss_stage1=False)
+    r1 = (Yc.copy(), Yf.copy())
+    o.step(*r1, cfg64.dt, 1)
+    r2 = (r1[0].copy(), r1[1].copy())
+    o.step(*r2, cfg64.dt, 1)
+    s = sim.AtmosSimulation(cfg64, state=(Yc, Yf))
+    s.step(1)
+    e1 = _errs(s.Y, r1)
+    s.step(1)
+    e2 = _errs(s.Y, r2)
+    print("FP64 vs oracle, 1 and 2 steps:", e1, e2)
+    _assert_errs(e1, 1e-12)
+    _assert_errs(e2, 1e-12, skip=("u_3",))
+    assert e2["u_3"] <= 2e-12, e2
+    s32 = sim.AtmosSimulation(C.production_h30(), state=(Yc.astype(np.float32), Yf.astype(np.float32)))
+    s32.step(2)
+    e = _errs(s32.Y, r2)
+    print("FP32 vs FP64 oracle, 2 steps:", e)
+    lim = {"rho": 2e-6, "rho_e_tot": 3e-6, "u_1": 1e-4, "u_2": 1e-4, "u_3": 1e-3}
+    assert all(e[k] <= lim[k] for k in lim), e

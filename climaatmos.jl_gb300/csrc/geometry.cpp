@@ -88,14 +88,20 @@ double beta_sponge(double z, double zd, double zmax, double alpha) {
 
 void reference_level(const gb_config &c, double Phi, double out[3]) {
   const double cp = c.cp_d, tm = c.T_min_ref, dT = c.T_surf_ref - c.T_min_ref, kappa = c.R_d / c.cp_d;
-  double P = 1.0;
+  // Newton's method in x = ln Pi0 on f(x) = Phi_r - Phi = -cp (T_min x + dT / 7 (e^{7x} - 1)) - Phi,
+  // which is decreasing and concave: from x = 0 (Phi_r = 0 <= Phi) the iterates decrease
+  // monotonically to the root and stay finite (Newton in Pi itself overshoots below 0 for
+  // levels near 30 km).
+  double x = 0.0;
   for (int it = 0; it < 100; ++it) {
-    const double f = -cp * (tm * std::log(P) + dT / 7.0 * (std::pow(P, 7.0) - 1.0)) - Phi;
-    const double df = -cp * (tm / P + dT * std::pow(P, 6.0));
+    const double e7 = std::exp(7.0 * x);
+    const double f = -cp * (tm * x + dT / 7.0 * (e7 - 1.0)) - Phi;
+    const double df = -cp * (tm + dT * e7);
     const double step = f / df;
-    P -= step;
-    if (std::fabs(step) < 1e-16 * P) break;
+    x -= step;
+    if (std::fabs(step) < 1e-15 * (1.0 + std::fabs(x))) break;
   }
+  const double P = std::exp(x);
   const double p0 = c.p_ref * std::pow(P, 1.0 / kappa);
   out[0] = p0;
   out[1] = 1.0 / p0;

@@ -252,9 +252,13 @@ def test_resting_atmosphere_stays_at_rest():
     """A horizontally uniform atmosphere at rest (the balanced profile, no perturbation): the
     horizontal operators see constant fields, so u_h stays zero to roundoff and every column
     evolves alike over 10 FP64 steps (an analytic pin independent of the oracle: gradients of
-    constants, the Coriolis term of zero wind, the vertical-horizontal coupling and the DSS)."""
+    constants, the vertical-horizontal coupling terms and the DSS).  The planet does not
+    rotate here: the analytic profile is not in discrete hydrostatic balance, so u_3 adjusts,
+    and with rotation the deep-atmosphere Coriolis term f^12 x u^3 would turn that vertical
+    motion into horizontal wind (2 Omega cos(lat) w, about 1e-3 m/s over these steps)."""
     from gbdycore import setups as S
     cfg = small_config(ft=np.float64, h_elem=4, z_elem=20)
+    cfg = cfg.with_(constants=dict(cfg.constants, omega=0.0))
     g = sim.Geometry(cfg)
     Yc, Yf = S.initial_state(g, cfg, sigma=0.0)
     s = sim.AtmosSimulation(cfg, state=(Yc, Yf))

@@ -57,10 +57,17 @@ __device__ __forceinline__ float grcp(float a) { return __fdividef(1.0f, a); }
 __device__ __forceinline__ double grcp(double a) { return 1.0 / a; }
 __device__ __forceinline__ float gsin(float x) { return sinf(x); }
 __device__ __forceinline__ double gsin(double x) { return sin(x); }
-// ln(1 + x) and exp(x) - 1 for small x (the library functions, accurate near 0)
-__device__ __forceinline__ float glog1p(float x) { return log1pf(x); }
-__device__ __forceinline__ double glog1p(double x) { return log1p(x); }
-__device__ __forceinline__ float gexpm1(float x) { return expm1f(x); }
+// ln(p / p0) for p near p0, and exp(x) - 1 for small x.  FP64: the library's log1p and expm1
+// (accurate near 0).  FP32: the hardware ln of the ratio p (1/p0), whose absolute error
+// (~2e-7) is below what the FP32 pressure itself carries (~3e-7 relative), and exp - 1 by
+// the hardware exp (absolute error ~2e-7 on a term scaled by cp (T_sfc - T_min) Pi0^7 / 7,
+// i.e. a few 1e-3 J/kg): a few instructions instead of two full function evaluations.
+__device__ __forceinline__ float glog_ratio(float p, float p0, float ip0) {
+  (void)p0;
+  return __logf(p * ip0);
+}
+__device__ __forceinline__ double glog_ratio(double p, double p0, double ip0) { return log1p((p - p0) * ip0); }
+__device__ __forceinline__ float gexpm1(float x) { return __expf(x) - 1.0f; }
 __device__ __forceinline__ double gexpm1(double x) { return expm1(x); }
 
 template <class FT>
@@ -82,7 +89,7 @@ __device__ __forceinline__ FT shfl_down(FT v, int d) {
 // Exner pressure, which the pressure-gradient and hyperdiffusion terms take
 // (advection.jl:82-88, implicit_tendency.jl:286-293, hyperdiffusion.jl:142-147).
 // It is formed as a deviation from the level's reference record rl (Phi_r(Pi0) = Phi at
-// p0 = rl.x): with ln x = kappa ln(p / p0) = kappa log1p((p - p0) / p0),
+// p0 = rl.x): with ln x = kappa ln(p / p0),
 //   Phi - Phi_r(Pi) = cp_d T_min ln x + cp_d (T_sfc - T_min) / 7 Pi0^7 expm1(7 ln x),
 // the same quantity as Phi - Phi_r(Pi) written directly, without the cancellation of two
 // O(1e5) J/kg terms that costs FP32 most of its precision there.
@@ -109,7 +116,7 @@ __device__ __forceinline__ void thermo(const DevParams<FT> &P, FT rho, FT rhoe, 
   o.thv = T * iPi;
   o.thvr = Tr * iPi;
   o.Tr = Tr;
-  const FT lx = P.kappa * glog1p((p - rl.x) * rl.y);
+  const FT lx = P.kappa * glog_ratio(p, rl.x, rl.y);
   o.phid = P.cpTmin * lx + rl.z * gexpm1(FT(7) * lx);
 }
 // Reverse mode of thermo(): the cotangents of its outputs (T, p, h, Pi, thv,

@@ -148,8 +148,13 @@ def test_implicit_stage_vjp(setup):
         dc, df = _scaled(Yc.shape, Yf.shape, Yc, Yf, seed)
         fd = (J(_axpy(Yc, Yf, H, dc, df)) - J(_axpy(Yc, Yf, -H, dc, df))) / (2 * H)
         assert rel(_dot(Uhb, _fv(dc, df)), fd) < 1e-6
-    vals = [J(Uh, sim.AtmosCache(cfg.with_(alpha_uh=RATE * s, alpha_w=RATE * s))) for s in (1 + HP, 1 - HP)]
-    assert rel(dpar[1], (vals[0] - vals[1]) / (2 * HP * RATE)) < 1e-6
+    # the van Leer correction's min/max branches make J piecewise smooth in the rate: a central
+    # difference may straddle a branch switch at one step size, so two step sizes are taken
+    errs = []
+    for hp in (HP, HP / 10):
+        vals = [J(Uh, sim.AtmosCache(cfg.with_(alpha_uh=RATE * s, alpha_w=RATE * s))) for s in (1 + hp, 1 - hp)]
+        errs.append(rel(dpar[1], (vals[0] - vals[1]) / (2 * hp * RATE)))
+    assert min(errs) < 1e-6, errs
     assert dpar[0] == 0.0
 
 

@@ -270,11 +270,14 @@ def test_resting_atmosphere_stays_at_rest():
     u1, u2 = Xc[:, 1], Xc[:, 2]
     speed = np.sqrt(np.maximum(gu[..., 0] * u1 * u1 + 2 * gu[..., 1] * u1 * u2 + gu[..., 2] * u2 * u2, 0))
     assert speed.max() < 1e-8, speed.max()
-    # every column alike: rho, rho e_tot and u_3 equal the column mean to roundoff
-    for name, a in (("rho", Xc[:, 0]), ("rho_e_tot", Xc[:, 3]), ("u_3", Xf)):
+    # every column alike: rho, rho e_tot and u_3 equal the column mean to roundoff.  u_3 is the
+    # small residual of the hydrostatic cancellation (gravity and the pressure gradient, each
+    # ~ g dt dz in u_3's covariant units per step), so its roundoff is measured on that scale
+    gdtdz = cfg.constants["grav"] * cfg.dt * float(np.max(np.diff(g.zf)))
+    for name, a, scale in (("rho", Xc[:, 0], np.abs(Xc[:, 0]).max()), ("rho_e_tot", Xc[:, 3], np.abs(Xc[:, 3]).max()),
+                           ("u_3", Xf, gdtdz)):
         m = a.reshape(-1, a.shape[-1]).mean(axis=0)
-        scale = max(np.abs(a).max(), 1e-300)
-        assert np.abs(a - m).max() <= 1e-11 * scale, name
+        assert np.abs(a - m).max() <= 1e-12 * scale, (name, np.abs(a - m).max(), scale)
 
 
 def test_production_step_matches_oracle():

@@ -6,15 +6,9 @@ namespace gb {
 
 // Shared-memory layouts of the element-slab kernels (byte offsets).  The
 // input slabs are double-buffered (nbuf = 2) when they fit, else single.
-// Staging area of the xi^2 row exchange (se::Row<FT, true>): one 4-node slot per
-// thread of a 256-thread CTA, starting on a 128-byte boundary.
-template <class FT>
-__host__ __device__ constexpr size_t stage_bytes() { return 256 * 4 * sizeof(FT); }
-__host__ __device__ constexpr size_t align128(size_t b) { return (b + 127) & ~size_t(127); }
-
 template <class FT>
 struct PassALayout {
-  size_t y[2], f[2], g[2], out, stg, bar, total;
+  size_t y[2], f[2], g[2], out, bar, total;
   __host__ __device__ PassALayout(int Nv, int nbuf) {
     const int Nf = Nv + 1;
     size_t o = 0;
@@ -28,7 +22,6 @@ struct PassALayout {
       }
     }
     out = o; o += align16(sizeof(FT) * 64 * Nv);
-    stg = o = align128(o); o += stage_bytes<FT>();
     bar = o; o += 16;
     total = o;
   }
@@ -44,7 +37,7 @@ enum PassBScratch { SB_C1 = 0, SB_C2, SB_K, SB_RJ, SB_L4, SB_Q1, SB_Q2, SB_N };
 // of the element being computed and stored from there.
 template <class FT>
 struct PassBLayout {
-  size_t y[2], f[2], g[2], lap[2], s, x1, x2, w, stg, bar, total;
+  size_t y[2], f[2], g[2], lap[2], s, x1, x2, w, bar, total;
   __host__ __device__ PassBLayout(int Nv, int nbuf) {
     const int Nf = Nv + 1;
     size_t o = 0;
@@ -62,7 +55,6 @@ struct PassBLayout {
     x1 = o; o += align16(sizeof(FT) * 16 * Nf);   // face rows [Nf][16]
     x2 = o; o += align16(sizeof(FT) * 16 * Nf);
     w = o; o += align16(sizeof(FT) * 2 * 16);     // GLL weights W, 1/W
-    stg = o = align128(o); o += stage_bytes<FT>();
     bar = o; o += 16;
     total = o;
   }

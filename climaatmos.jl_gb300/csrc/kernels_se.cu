@@ -106,8 +106,8 @@ __global__ void __launch_bounds__(SE_THREADS, SeMinBlocks<FT>::value) k_passA(De
   int e = blockIdx.x;
   if (threadIdx.x == 0 && e < P.Nh) issue_slab<FT>(P, &bar[0], e, sYb[0], sFb[0], sGb[0], nullptr, Yc, Yf, nullptr);
   const int j = threadIdx.x & 3, vs = level_slot(threadIdx.x >> 2);
-  Row<FT, true> R;
-  R.init(P, j, (const FT *)(sm + Lo.stg));
+  Row<FT> R;
+  R.init(P, j);
   for (int it = 0; e < P.Nh; ++it, e += gridDim.x) {
     int b;
     if (!begin_element<FT>(P, bar, nbuf, it, e, sYb, sFb, sGb, sGb, false, Yc, Yf, nullptr, b)) break;
@@ -239,8 +239,8 @@ __global__ void __launch_bounds__(SE_THREADS, SeMinBlocks<FT>::value) k_passB(De
   const int j = threadIdx.x & 3, vl = threadIdx.x >> 2, vs = level_slot(vl);
   // the thread's row of scratch field f at level (or face) v
   auto row = [&](FT *base, int f, int v) { return base + ((size_t)f * Nv + v) * NN + NQ * j; };
-  Row<FT, true> R;
-  R.init(P, j, (const FT *)(sm + Lo.stg));
+  Row<FT> R;
+  R.init(P, j);
   for (int it = 0; e < P.Nh; ++it, e += gridDim.x) {
     int b;
     if (!slab_begin(bar, nbuf, it, e, P.Nh, P.status, issue, b)) break;

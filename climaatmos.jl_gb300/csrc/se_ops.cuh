@@ -12,48 +12,21 @@ namespace gb {
 namespace se {
 
 // Row helper: the thread's row j and its xi^2 derivative coefficients.
-// STG: the rows of the level's 4-lane group are exchanged through shared memory
-// (each thread's 4-node row in its own slot of a per-CTA staging area, one
-// store and three loads) instead of by 12 shuffles; the sums are formed in the
-// same order either way, so the results are the same bits.
-template <class FT, bool STG = false>
+template <class FT>
 struct Row {
   int j;
   // xi^2 coefficients ordered by partner row j ^ m (m = 0: the thread's own row):
   // dX[m] = D[j][j ^ m], tX[m] = D[j ^ m][j]
   FT dX[NQ], tX[NQ];
-  // shared-memory address of the thread's staging slot (4 FT); the slot of the
-  // partner lane threadIdx.x ^ m is at slot ^ (m * 4 sizeof(FT)) because the
-  // area starts on a 128-byte boundary and slot t sits at 4 t sizeof(FT)
-  uint32_t slot;
-  __device__ void init(const DevParams<FT> &P, int jj, const FT *stage = nullptr) {
+  __device__ void init(const DevParams<FT> &P, int jj) {
     j = jj;
 #pragma unroll
     for (int m = 0; m < NQ; ++m) {
       dX[m] = P.D[j * NQ + (j ^ m)];
       tX[m] = P.D[(j ^ m) * NQ + j];
     }
-    slot = stage ? smem_u32(stage + 4 * threadIdx.x) : 0u;
   }
 };
-
-// Staging slot access: a 4-node row to and from shared memory (32-bit addresses).
-__device__ __forceinline__ void st_slot(uint32_t a, const float (&v)[4]) {
-  asm volatile("st.shared.v4.f32 [%0], {%1, %2, %3, %4};" ::"r"(a), "f"(v[0]), "f"(v[1]), "f"(v[2]), "f"(v[3])
-               : "memory");
-}
-__device__ __forceinline__ void st_slot(uint32_t a, const double (&v)[4]) {
-  asm volatile("st.shared.v2.f64 [%0], {%1, %2};" ::"r"(a), "d"(v[0]), "d"(v[1]) : "memory");
-  asm volatile("st.shared.v2.f64 [%0+16], {%1, %2};" ::"r"(a), "d"(v[2]), "d"(v[3]) : "memory");
-}
-__device__ __forceinline__ void ld_slot(uint32_t a, float (&v)[4]) {
-  asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];" : "=f"(v[0]), "=f"(v[1]), "=f"(v[2]), "=f"(v[3]) : "r"(a)
-               : "memory");
-}
-__device__ __forceinline__ void ld_slot(uint32_t a, double (&v)[4]) {
-  asm volatile("ld.shared.v2.f64 {%0, %1}, [%2];" : "=d"(v[0]), "=d"(v[1]) : "r"(a) : "memory");
-  asm volatile("ld.shared.v2.f64 {%0, %1}, [%2+16];" : "=d"(v[2]), "=d"(v[3]) : "r"(a) : "memory");
-}
 
 // o[i] = sum_k D[i][k] f[k]   (d/dxi^1, register-local)
 template <class FT>
@@ -78,38 +51,21 @@ __device__ __forceinline__ void t1(const DevParams<FT> &P, const FT (&f)[4], FT 
   }
 }
 // o[i] = sum_m C[m] f(i, row j ^ m): the thread's own row plus three xor
-// partners of its level's 4-lane group (12 shuffles for the 4 outputs, or one
-// staged store and three loads)
-template <class FT, bool S>
-__device__ __forceinline__ void across(const Row<FT, S> &R, const FT (&C)[NQ], const FT (&f)[4], FT (&o)[4]) {
-  if constexpr (S) {
-    FT g[NQ][4];
-    __syncwarp();  // the partners' reads of the previous exchange are done
-    st_slot(R.slot, f);
-    __syncwarp();
+// partners of its level's 4-lane group (12 shuffles for the 4 outputs)
+template <class FT>
+__device__ __forceinline__ void across(const FT (&C)[NQ], const FT (&f)[4], FT (&o)[4]) {
 #pragma unroll
-    for (int m = 1; m < NQ; ++m) ld_slot(R.slot ^ uint32_t(m * 4 * sizeof(FT)), g[m]);
+  for (int i = 0; i < NQ; ++i) {
+    FT s = C[0] * f[i];
 #pragma unroll
-    for (int i = 0; i < NQ; ++i) {
-      FT s = C[0] * f[i];
-#pragma unroll
-      for (int m = 1; m < NQ; ++m) s += C[m] * g[m][i];
-      o[i] = s;
-    }
-  } else {
-#pragma unroll
-    for (int i = 0; i < NQ; ++i) {
-      FT s = C[0] * f[i];
-#pragma unroll
-      for (int m = 1; m < NQ; ++m) s += C[m] * __shfl_xor_sync(0xffffffffu, f[i], m, 4);
-      o[i] = s;
-    }
+    for (int m = 1; m < NQ; ++m) s += C[m] * __shfl_xor_sync(0xffffffffu, f[i], m, 4);
+    o[i] = s;
   }
 }
-template <class FT, bool S>
-__device__ __forceinline__ void d2(const Row<FT, S> &R, const FT (&f)[4], FT (&o)[4]) { across(R, R.dX, f, o); }
-template <class FT, bool S>
-__device__ __forceinline__ void t2(const Row<FT, S> &R, const FT (&f)[4], FT (&o)[4]) { across(R, R.tX, f, o); }
+template <class FT>
+__device__ __forceinline__ void d2(const Row<FT> &R, const FT (&f)[4], FT (&o)[4]) { across(R.dX, f, o); }
+template <class FT>
+__device__ __forceinline__ void t2(const Row<FT> &R, const FT (&f)[4], FT (&o)[4]) { across(R.tX, f, o); }
 
 // Level slot of the 4-lane group vl (0..63) of a 256-thread slab sweep: warp
 // w takes levels 4 (w mod 4) + 32 (w / 4) + {0..3, 16..19}.  A [node][level]
@@ -239,8 +195,8 @@ struct LevRow {
 };
 
 // C123(wgrad(div u)) * fdiv - C123(wcurl(C123(curl u))) for covariant (c1, c2, c3)
-template <class FT, class G, bool S>
-__device__ __forceinline__ void vec_lap(const DevParams<FT> &P, const Row<FT, S> &R, const G &g,
+template <class FT, class G>
+__device__ __forceinline__ void vec_lap(const DevParams<FT> &P, const Row<FT> &R, const G &g,
                                         const LevRow<FT> &s, const FT (&c1)[4], const FT (&c2)[4],
                                         const FT (&c3)[4], FT fdiv, FT (&o1)[4], FT (&o2)[4], FT (&o3)[4]) {
   FT a[4], b[4], da[4], db[4];
@@ -308,8 +264,8 @@ __device__ __forceinline__ void vec_lap(const DevParams<FT> &P, const Row<FT, S>
 
 // The third output of vec_lap alone (it depends on c3 only): the same
 // operations in the same order as in vec_lap.
-template <class FT, class G, bool S>
-__device__ __forceinline__ void vec_lap_o3(const DevParams<FT> &P, const Row<FT, S> &R, const G &g,
+template <class FT, class G>
+__device__ __forceinline__ void vec_lap_o3(const DevParams<FT> &P, const Row<FT> &R, const G &g,
                                            const LevRow<FT> &s, const FT (&c3)[4], FT (&o3)[4]) {
   FT e3[4], e4[4], Wz1[4], Wz2[4];
   d2(R, c3, e3);
@@ -337,8 +293,8 @@ __device__ __forceinline__ void vec_lap_o3(const DevParams<FT> &P, const Row<FT,
 }
 
 // weak divergence -(1/WJ) (D^T (WJ F1) along xi^1 + along xi^2)
-template <class FT, bool S>
-__device__ __forceinline__ void wdiv(const DevParams<FT> &P, const Row<FT, S> &R, const LevRow<FT> &s,
+template <class FT>
+__device__ __forceinline__ void wdiv(const DevParams<FT> &P, const Row<FT> &R, const LevRow<FT> &s,
                                      const FT (&F1)[4], const FT (&F2)[4], FT (&o)[4]) {
   FT a[4], b[4], ta[4], tb[4];
 #pragma unroll
@@ -356,8 +312,8 @@ __device__ __forceinline__ void wdiv(const DevParams<FT> &P, const Row<FT, S> &R
 // Transpose of vec_lap: given the cotangents (ob1, ob2, ob3) of (o1, o2, o3),
 // returns the cotangents (cb1, cb2, cb3) of (c1, c2, c3).  The forward sequence
 // run backwards, with d1 <-> t1 and d2 <-> t2.
-template <class FT, class G, bool S>
-__device__ __forceinline__ void vec_lap_t(const DevParams<FT> &P, const Row<FT, S> &R, const G &g,
+template <class FT, class G>
+__device__ __forceinline__ void vec_lap_t(const DevParams<FT> &P, const Row<FT> &R, const G &g,
                                           const LevRow<FT> &s, const FT (&ob1)[4], const FT (&ob2)[4],
                                           const FT (&ob3)[4], FT fdiv, FT (&cb1)[4], FT (&cb2)[4], FT (&cb3)[4]) {
   FT f1b[4], f2b[4], f3b[4], f4b[4], w1b[4], w2b[4];
@@ -434,8 +390,8 @@ __device__ __forceinline__ void vec_lap_t(const DevParams<FT> &P, const Row<FT, 
 }
 
 // Transpose of wdiv: cotangents (Fb1, Fb2) of (F1, F2) from the cotangent ob of o.
-template <class FT, bool S>
-__device__ __forceinline__ void wdiv_t(const DevParams<FT> &P, const Row<FT, S> &R, const LevRow<FT> &s,
+template <class FT>
+__device__ __forceinline__ void wdiv_t(const DevParams<FT> &P, const Row<FT> &R, const LevRow<FT> &s,
                                        const FT (&ob)[4], FT (&Fb1)[4], FT (&Fb2)[4]) {
   FT tb[4];
 #pragma unroll
@@ -450,8 +406,8 @@ __device__ __forceinline__ void wdiv_t(const DevParams<FT> &P, const Row<FT, S> 
 }
 
 // Transpose of the gradient (d1 f, d2 f): fb = t1(gb1) + t2(gb2).
-template <class FT, bool S>
-__device__ __forceinline__ void grad_t(const DevParams<FT> &P, const Row<FT, S> &R, const FT (&gb1)[4],
+template <class FT>
+__device__ __forceinline__ void grad_t(const DevParams<FT> &P, const Row<FT> &R, const FT (&gb1)[4],
                                        const FT (&gb2)[4], FT (&fb)[4]) {
   FT a[4];
   t1(P, gb1, fb);
@@ -461,8 +417,8 @@ __device__ __forceinline__ void grad_t(const DevParams<FT> &P, const Row<FT, S> 
 }
 
 // Transpose of the scalar Laplacian Ls = wdiv(g^-1 grad sd) (with the row's g^ij / r^2).
-template <class FT, class G, bool S>
-__device__ __forceinline__ void lap_t(const DevParams<FT> &P, const Row<FT, S> &R, const G &g,
+template <class FT, class G>
+__device__ __forceinline__ void lap_t(const DevParams<FT> &P, const Row<FT> &R, const G &g,
                                       const LevRow<FT> &s, const FT (&Lb)[4], FT (&sdb)[4]) {
   FT xb1[4], xb2[4], gb1[4], gb2[4];
   wdiv_t(P, R, s, Lb, xb1, xb2);

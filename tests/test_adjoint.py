@@ -148,13 +148,15 @@ def test_implicit_stage_vjp(setup):
         dc, df = _scaled(Yc.shape, Yf.shape, Yc, Yf, seed)
         fd = (J(_axpy(Yc, Yf, H, dc, df)) - J(_axpy(Yc, Yf, -H, dc, df))) / (2 * H)
         assert rel(_dot(Uhb, _fv(dc, df)), fd) < 1e-6
-    # the van Leer correction's min/max branches make J piecewise smooth in the rate: a central
-    # difference may straddle a branch switch at one step size, so two step sizes are taken
-    errs = []
-    for hp in (HP, HP / 10):
+    # the sponge acts on the top levels only, so J's change with the rate is small against J
+    # itself and a central difference at a small step is round-off bound (measured: 1.6e-6 at
+    # a 1e-4 relative step, 2.1e-5 at 1e-5); larger steps with Richardson extrapolation,
+    # (4 D(h) - D(2h)) / 3, remove the h^2 truncation term instead
+    def D(hp):
         vals = [J(Uh, sim.AtmosCache(cfg.with_(alpha_uh=RATE * s, alpha_w=RATE * s))) for s in (1 + hp, 1 - hp)]
-        errs.append(rel(dpar[1], (vals[0] - vals[1]) / (2 * hp * RATE)))
-    assert min(errs) < 1e-6, errs
+        return (vals[0] - vals[1]) / (2 * hp * RATE)
+    fd = (4 * D(1e-3) - D(2e-3)) / 3
+    assert rel(dpar[1], fd) < 1e-6, (dpar[1], fd)
     assert dpar[0] == 0.0
 
 

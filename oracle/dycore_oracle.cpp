@@ -125,11 +125,14 @@ struct Oracle {
     const double cp = cpd, tm = Tmin_ref, dT = (double)Tsfc_ref - (double)Tmin_ref;
     for (int v = 0; v < Nv; ++v) {
       const double gz = (double)grav * (double)zc[v];
-      double P = 1.0;
-      for (int it = 0; it < 60; ++it) {
-        const double f = -cp * (tm * std::log(P) + dT / 7.0 * (std::pow(P, 7.0) - 1.0)) - gz;
-        P -= f / (-cp * (tm / P + dT * std::pow(P, 6.0)));
+      // Newton's method in x = ln P (decreasing, concave: monotone from x = 0; in P itself the
+      // first step overshoots below zero for levels near 30 km)
+      double x = 0.0;
+      for (int it = 0; it < 100; ++it) {
+        const double e7 = std::exp(7.0 * x);
+        x -= (-cp * (tm * x + dT / 7.0 * (e7 - 1.0)) - gz) / (-cp * (tm + dT * e7));
       }
+      const double P = std::exp(x);
       p0v[v] = (FT)((double)pref * std::pow(P, 1.0 / (double)kappa));
       pi07[v] = (FT)std::pow(P, 7.0);
     }

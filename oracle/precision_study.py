@@ -1,4 +1,4 @@
-"""FP32 against FP64 on the CPU oracle (correctly rounded libm, the reference's formulation)
+"""Precision study (test infrastructure, beside the oracle it runs): FP32 against FP64 on the CPU oracle (correctly rounded libm, the reference's formulation)
 after n steps of the production workload (h_elem=30, z_elem=63, dt=120 s): the FP32 error
 floor of the formulation itself, to set beside the GPU's (bench.py `fp32_vs_fp64`).  The
 oracle's precision-study builds run in child processes (the library is loaded once per
@@ -7,7 +7,7 @@ rounded to FP32, which separates the error of FP32 storage from that of FP32 ari
 ``--phid`` (ORACLE_VARIANT=phid) is FP32 with g z - Phi_r formed as a deviation from
 per-level reference values.  Every run starts from the FP32-representable initial state.
 
-    python tests/precision_oracle.py [n_steps] [--store32] [--phid]   (~1 minute per run of 2 steps on 8 cores)
+    python oracle/precision_study.py [n_steps] [--store32] [--phid]   (~1 minute per run of 2 steps on 8 cores)
 """
 import os
 import subprocess
@@ -16,7 +16,7 @@ import tempfile
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
-sys.path[:0] = [os.path.join(ROOT, "climaatmos.jl_gb300"), os.path.join(ROOT, "oracle"), HERE]
+sys.path[:0] = [os.path.join(ROOT, "climaatmos.jl_gb300"), HERE, os.path.join(ROOT, "tests")]
 
 import numpy as np  # noqa: E402
 

@@ -29,7 +29,8 @@ struct DevParams {
   int hs;
   FT hs_ka, hs_dk, hs_kf, hs_sb, hs_isb, hs_dTy, hs_Teq, hs_dthz, hs_Tmin, hs_ip0, hs_iMSLP;
   FT W[NN], iW[NN];
-  FT D[NQ * NQ];  // D[i*4+k] = l_k'(xi_i)
+  alignas(16) FT D[NQ * NQ];   // D[i*4+k] = l_k'(xi_i)
+  alignas(16) FT DT[NQ * NQ];  // the transpose, DT[k*4+i] = D[i*4+k] (pairs of rows of a column)
   const FT *hgeo;  // [Nh][HG_N][16]
   const FT *levc;  // [LC_N][Nv]
   const FT *levf;  // [LF_N][Nf]

@@ -212,7 +212,10 @@ int create_impl(gb_ctx *ctx) {
   P.upwinding = c.upwinding;
   for (int n = 0; n < NN; ++n) { P.W[n] = (FT)g.W[n]; P.iW[n] = (FT)(1.0 / g.W[n]); }
   for (int i = 0; i < NQ; ++i)
-    for (int k = 0; k < NQ; ++k) P.D[i * NQ + k] = (FT)g.D[i][k];
+    for (int k = 0; k < NQ; ++k) {
+      P.D[i * NQ + k] = (FT)g.D[i][k];
+      P.DT[k * NQ + i] = (FT)g.D[i][k];
+    }
   P.hgeo = (const FT *)I->hgeo.p; P.levc = (const FT *)I->levc.p; P.levf = (const FT *)I->levf.p;
   P.lc4 = (const Lev4<FT> *)I->lc4.p; P.lf4 = (const Lev4<FT> *)I->lf4.p; P.lr4 = (const Lev4<FT> *)I->lr4.p;
   P.goff = (const int *)I->goff.p; P.gcopy = (const int *)I->gcopy.p; P.gw = (const FT *)I->gw.p;

@@ -11,6 +11,15 @@
 namespace gb {
 namespace se {
 
+// Packed FP32: the pair (a[0], a[1]) or (a[2], a[3]) of a 4-node row, and back.
+__device__ __forceinline__ float2 lo2(const float (&a)[4]) { return make_float2(a[0], a[1]); }
+__device__ __forceinline__ float2 hi2(const float (&a)[4]) { return make_float2(a[2], a[3]); }
+__device__ __forceinline__ float2 bc2(float x) { return make_float2(x, x); }
+__device__ __forceinline__ void put2(float2 lo, float2 hi, float (&o)[4]) {
+  o[0] = lo.x; o[1] = lo.y; o[2] = hi.x; o[3] = hi.y;
+}
+__device__ __forceinline__ float2 ld2(const float *p) { return *reinterpret_cast<const float2 *>(p); }
+
 // Row helper: the thread's row j and its xi^2 derivative coefficients.
 template <class FT>
 struct Row {
@@ -39,6 +48,18 @@ __device__ __forceinline__ void d1(const DevParams<FT> &P, const FT (&f)[4], FT 
     o[i] = s;
   }
 }
+// FP32: two outputs per packed multiply-add, the same operations in the same order per lane
+// (so the same bits as the scalar form)
+template <>
+__device__ __forceinline__ void d1<float>(const DevParams<float> &P, const float (&f)[4], float (&o)[4]) {
+  float2 lo = __fmul2_rn(ld2(&P.DT[0]), bc2(f[0])), hi = __fmul2_rn(ld2(&P.DT[2]), bc2(f[0]));
+#pragma unroll
+  for (int k = 1; k < NQ; ++k) {
+    lo = __ffma2_rn(ld2(&P.DT[k * NQ]), bc2(f[k]), lo);
+    hi = __ffma2_rn(ld2(&P.DT[k * NQ + 2]), bc2(f[k]), hi);
+  }
+  put2(lo, hi, o);
+}
 // o[i] = sum_k D[k][i] f[k]   (transpose: weak forms)
 template <class FT>
 __device__ __forceinline__ void t1(const DevParams<FT> &P, const FT (&f)[4], FT (&o)[4]) {
@@ -49,6 +70,16 @@ __device__ __forceinline__ void t1(const DevParams<FT> &P, const FT (&f)[4], FT 
     for (int k = 0; k < NQ; ++k) s += P.D[k * NQ + i] * f[k];
     o[i] = s;
   }
+}
+template <>
+__device__ __forceinline__ void t1<float>(const DevParams<float> &P, const float (&f)[4], float (&o)[4]) {
+  float2 lo = __fmul2_rn(ld2(&P.D[0]), bc2(f[0])), hi = __fmul2_rn(ld2(&P.D[2]), bc2(f[0]));
+#pragma unroll
+  for (int k = 1; k < NQ; ++k) {
+    lo = __ffma2_rn(ld2(&P.D[k * NQ]), bc2(f[k]), lo);
+    hi = __ffma2_rn(ld2(&P.D[k * NQ + 2]), bc2(f[k]), hi);
+  }
+  put2(lo, hi, o);
 }
 // o[i] = sum_m C[m] f(i, row j ^ m): the thread's own row plus three xor
 // partners of its level's 4-lane group (12 shuffles for the 4 outputs)
@@ -61,6 +92,20 @@ __device__ __forceinline__ void across(const FT (&C)[NQ], const FT (&f)[4], FT (
     for (int m = 1; m < NQ; ++m) s += C[m] * __shfl_xor_sync(0xffffffffu, f[i], m, 4);
     o[i] = s;
   }
+}
+__device__ __forceinline__ void across(const float (&C)[NQ], const float (&f)[4], float (&o)[4]) {
+  float g[NQ][4];
+#pragma unroll
+  for (int m = 1; m < NQ; ++m)
+#pragma unroll
+    for (int i = 0; i < NQ; ++i) g[m][i] = __shfl_xor_sync(0xffffffffu, f[i], m, 4);
+  float2 lo = __fmul2_rn(bc2(C[0]), lo2(f)), hi = __fmul2_rn(bc2(C[0]), hi2(f));
+#pragma unroll
+  for (int m = 1; m < NQ; ++m) {
+    lo = __ffma2_rn(bc2(C[m]), lo2(g[m]), lo);
+    hi = __ffma2_rn(bc2(C[m]), hi2(g[m]), hi);
+  }
+  put2(lo, hi, o);
 }
 template <class FT>
 __device__ __forceinline__ void d2(const Row<FT> &R, const FT (&f)[4], FT (&o)[4]) { across(R.dX, f, o); }

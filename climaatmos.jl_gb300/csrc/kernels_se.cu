@@ -283,11 +283,9 @@ __global__ void __launch_bounds__(SE_THREADS, SeMinBlocks<FT>::value) k_passB(De
       FT rho[4], h[4], Pi[4], thp[4], gg[4], F1[4], F2[4], Q1[4], Q2[4];
       FT hsk[4] = {0, 0, 0, 0};  // Held-Suarez drag rate k_f max(0, (sigma - sigma_b) / (1 - sigma_b))
       {
-        FT u1[4], u2[4], c1[4], c2[4], K[4];
+        FT u1[4], u2[4], c1[4], c2[4], K[4], phid[4];
         {
-          FT gu0[4], gu1[4], gu2[4], s2[4];
-          g.gu(gu0, gu1, gu2);
-          if (HS) g.row(HG_S2, s2);
+          FT gu0[4], gu1[4], gu2[4], s2[4], rhoe[4], fa[4], fb[4], t[4];
 #pragma unroll
           for (int i = 0; i < 4; ++i) {
             const int n = NQ * j + i;
@@ -295,21 +293,39 @@ __global__ void __launch_bounds__(SE_THREADS, SeMinBlocks<FT>::value) k_passB(De
             rho[i] = sY[q];
             u1[i] = sY[16 * Nv + q];
             u2[i] = sY[32 * Nv + q];
-            const FT x0 = gu0[i] * s.ir2, x1 = gu1[i] * s.ir2, x2 = gu2[i] * s.ir2;
-            c1[i] = x0 * u1[i] + x1 * u2[i];
-            c2[i] = x1 * u1[i] + x2 * u2[i];
-            // face part of K, I^c(u_3 u^3), with u_3 = 0 on the boundary faces
-            const FT fa = v == 0 ? FT(0) : sF[n * Nf + v];
-            const FT fb = v + 1 == Nv ? FT(0) : sF[n * Nf + v + 1];
-            const FT kv = (fa * (fa * g3a) + fb * (fb * g3b)) / FT(2);
-            K[i] = (u1[i] * c1[i] + u2[i] * c2[i] + kv) / FT(2);
+            rhoe[i] = sY[48 * Nv + q];
+            // u_3 of the faces below and above (0 on the boundary faces)
+            fa[i] = v == 0 ? FT(0) : sF[n * Nf + v];
+            fb[i] = v + 1 == Nv ? FT(0) : sF[n * Nf + v + 1];
+          }
+          // CT12(u_h) = g^ij u_j with the level's g^ij = r^-2 g^ij(surface)
+          g.gu(gu0, gu1, gu2);
+          vmul(gu1, u2, t);
+          vfma(gu0, u1, t, t);
+          vmuls(t, s.ir2, c1);
+          vmul(gu2, u2, t);
+          vfma(gu1, u1, t, t);
+          vmuls(t, s.ir2, c2);
+          // K = (u_h . CT12(u_h) + I^c(u_3 u^3)) / 2, I^c(u_3 u^3) = (fa^2 g33_a + fb^2 g33_b) / 2
+          FT kv2[4];
+          vmuls(fb, g3b, kv2);
+          vmul(fb, kv2, kv2);
+          vmuls(fa, g3a, t);
+          vfma(fa, t, kv2, kv2);
+          vmul(u2, c2, t);
+          vfma(u1, c1, t, t);
+          vfmas(kv2, FT(0.5), t, K);
+          vmuls(K, FT(0.5), K);
+          if (HS) g.row(HG_S2, s2);
+#pragma unroll
+          for (int i = 0; i < 4; ++i) {
+            const int q = (NQ * j + i) * Nv + v;
             Thermo<FT> th;
-            thermo(P, rho[i], sY[48 * Nv + q], K[i], Phi, rl, th);
+            thermo(P, rho[i], rhoe[i], K[i], Phi, rl, th);
             h[i] = th.h;
             Pi[i] = th.Pi;
             thp[i] = th.thv - th.thvr;
-            // grad(K + Phi - Phi_r) and (cp_d / 2) grad(th' Pi) taken as one gradient
-            gg[i] = (K[i] + th.phid) + P.cpd * (thp[i] * Pi[i]) / FT(2);
+            phid[i] = th.phid;
             if (HS) {
               // Held-Suarez forcing (held_suarez.jl:98-141, 203-225, 279-295), flat surface:
               // sigma = p / MSLP; rho e_tot relaxes with -cv_d k_T rho (p / (rho R_d) - T_eq)
@@ -324,34 +340,39 @@ __global__ void __launch_bounds__(SE_THREADS, SeMinBlocks<FT>::value) k_passB(De
               if (act) sY[48 * Nv + q] = kT * rho[i] * (th.p / (rho[i] * P.Rd) - Teq) * P.cvd;
             }
           }
+          // grad(K + Phi - Phi_r) and (cp_d / 2) grad(th' Pi) taken as one gradient
+          vmul(thp, Pi, t);
+          vadd(K, phid, gg);
+          vfmas(t, P.cpd * FT(0.5), gg, gg);
         }
         // vorticity w^3 = wcurl(u_h); (f^3 + w^3) x CT12(u) -> C12, and the sponge
         FT om[4];
         {
           FT W[4], Wu1[4], Wu2[4], ta[4], tb[4];
           g.w(W);
-#pragma unroll
-          for (int i = 0; i < 4; ++i) {
-            Wu1[i] = W[i] * u1[i];
-            Wu2[i] = W[i] * u2[i];
-          }
+          vmul(W, u1, Wu1);
+          vmul(W, u2, Wu2);
           t1(P, Wu2, ta);
           t2(R, Wu1, tb);
-#pragma unroll
-          for (int i = 0; i < 4; ++i) om[i] = (-ta[i] + tb[i]) * s.iWJ[i];
+          vsub(tb, ta, om);
+          vmul(om, s.iWJ, om);
         }
-        FT f3[4], rJ[4];
+        FT f3[4], rJ[4], a3J[4], damp[4];
         g.row(HG_F3, f3);
+        vfmas(f3, idz, om, a3J);            // f^3 + w^3
+        vmul(a3J, s.J, a3J);                // J (f^3 + w^3)
 #pragma unroll
-        for (int i = 0; i < 4; ++i) {
-          const FT a3 = f3[i] * idz + om[i];
-          const FT damp = HS ? beta + hsk[i] : beta;  // sponge (+ Held-Suarez drag)
-          Q1[i] = -(s.J[i] * (-a3 * c2[i])) - damp * u1[i];
-          Q2[i] = -(s.J[i] * (a3 * c1[i])) - damp * u2[i];
-          F1[i] = rho[i] * c1[i];
-          F2[i] = rho[i] * c2[i];
-          rJ[i] = rho[i] * s.J[i];
-        }
+        for (int i = 0; i < 4; ++i) damp[i] = HS ? beta + hsk[i] : beta;  // sponge (+ Held-Suarez drag)
+        // Q1 = J a3 c2 - damp u1, Q2 = -J a3 c1 - damp u2
+        vmul(damp, u1, Q1);
+        vmuls(Q1, FT(-1), Q1);
+        vfma(a3J, c2, Q1, Q1);
+        vmul(a3J, c1, Q2);
+        vfma(damp, u2, Q2, Q2);
+        vmuls(Q2, FT(-1), Q2);
+        vmul(rho, c1, F1);
+        vmul(rho, c2, F2);
+        vmul(rho, s.J, rJ);
         if (act) {
           st_row(row(sS, SB_C1, v), c1);
           st_row(row(sS, SB_C2, v), c2);
@@ -363,19 +384,21 @@ __global__ void __launch_bounds__(SE_THREADS, SeMinBlocks<FT>::value) k_passB(De
       FT Trhoe[4];
       {
         FT G1[4], G2[4], dm[4], dmh[4], ha[4], hb[4];
-#pragma unroll
-        for (int i = 0; i < 4; ++i) {
-          G1[i] = F1[i] * h[i];
-          G2[i] = F2[i] * h[i];
-        }
+        vmul(F1, h, G1);
+        vmul(F2, h, G2);
         wdiv(P, R, s, F1, F2, dm);
         wdiv(P, R, s, G1, G2, dmh);
         d1(P, h, ha);
         d2(R, h, hb);
+        // T_rhoe = -(wdiv(F h) + h wdiv(F) + F . grad h) / 2
+        vmul(F2, hb, Trhoe);
+        vfma(F1, ha, Trhoe, Trhoe);
+        vfma(h, dm, Trhoe, Trhoe);
+        vadd(dmh, Trhoe, Trhoe);
+        vmuls(Trhoe, FT(-0.5), Trhoe);
+        if (act) {
 #pragma unroll
-        for (int i = 0; i < 4; ++i) {
-          Trhoe[i] = -((dmh[i] + h[i] * dm[i] + F1[i] * ha[i] + F2[i] * hb[i]) / FT(2));
-          if (act) sO[(NQ * j + i) * Nv + v] = -dm[i];
+          for (int i = 0; i < 4; ++i) sO[(NQ * j + i) * Nv + v] = -dm[i];
         }
       }
       // u_h: -[grad(K + Phi - Phi_r) + cp_d (th' grad Pi + grad(th' Pi) - Pi grad th') / 2]
@@ -387,11 +410,18 @@ __global__ void __launch_bounds__(SE_THREADS, SeMinBlocks<FT>::value) k_passB(De
         d2(R, Pi, b2);
         d1(P, thp, f1);
         d2(R, thp, f2);
-#pragma unroll
-        for (int i = 0; i < 4; ++i) {
-          Q1[i] += -(a1[i] + P.cpd * (thp[i] * b1[i] - Pi[i] * f1[i]) / FT(2));
-          Q2[i] += -(a2[i] + P.cpd * (thp[i] * b2[i] - Pi[i] * f2[i]) / FT(2));
-        }
+        // Q -= a + (cp_d / 2) (th' b - Pi f)
+        FT t[4];
+        vmul(Pi, f1, t);
+        vmuls(t, FT(-1), t);
+        vfma(thp, b1, t, t);
+        vfmas(t, P.cpd * FT(0.5), a1, t);
+        vsub(Q1, t, Q1);
+        vmul(Pi, f2, t);
+        vmuls(t, FT(-1), t);
+        vfma(thp, b2, t, t);
+        vfmas(t, P.cpd * FT(0.5), a2, t);
+        vsub(Q2, t, Q2);
       }
       // hyperdiffusion: nu (div_damp C123(wgrad div L) - C123(wcurl C123(curl L)))
       {
@@ -404,11 +434,8 @@ __global__ void __launch_bounds__(SE_THREADS, SeMinBlocks<FT>::value) k_passB(De
           L3[i] = sL[48 * Nv + q];
         }
         vec_lap(P, R, g, s, L1, L2, L3, P.div_damp, o1, o2, o3);
-#pragma unroll
-        for (int i = 0; i < 4; ++i) {
-          Q1[i] -= P.nu_v * o1[i];
-          Q2[i] -= P.nu_v * o2[i];
-        }
+        vfmas(o1, -P.nu_v, Q1, Q1);
+        vfmas(o2, -P.nu_v, Q2, Q2);
         if (act) {
           st_row(row(sS, SB_L4, v), o3);
           st_row(row(sS, SB_Q1, v), Q1);
@@ -422,14 +449,12 @@ __global__ void __launch_bounds__(SE_THREADS, SeMinBlocks<FT>::value) k_passB(De
         d1(P, Ls, g1);
         d2(R, Ls, g2);
         {
-          FT gu0[4], gu1[4], gu2[4];
+          // rho g^ij d_j L_s with the level's g^ij = r^-2 g^ij(surface)
+          FT gu0[4], gu1[4], gu2[4], rr[4];
           g.gu(gu0, gu1, gu2);
-#pragma unroll
-          for (int i = 0; i < 4; ++i) {
-            const FT y0 = gu0[i] * s.ir2, y1 = gu1[i] * s.ir2, y2 = gu2[i] * s.ir2;
-            x1[i] = rho[i] * (y0 * g1[i] + y1 * g2[i]);
-            x2[i] = rho[i] * (y1 * g1[i] + y2 * g2[i]);
-          }
+          vmuls(rho, s.ir2, rr);
+          vcontract(gu0, gu1, g1, g2, rr, x1);
+          vcontract(gu1, gu2, g1, g2, rr, x2);
         }
         wdiv(P, R, s, x1, x2, hd);
         if (act) {
@@ -483,38 +508,73 @@ __global__ void __launch_bounds__(SE_THREADS, SeMinBlocks<FT>::value) k_passB(De
         g.iw(iW);
         g.row(HG_FH1, fh1);
         g.row(HG_FH2, fh2);
-        FT X1[4], X2[4];
+        // face Jacobian, its inverse and the weak-curl weight of the face
+        FT Jf[4], iJf[4], iWJf[4], w1[4], w2[4];
+        vmuls(Jh, r2 * dzf, Jf);
+        vmuls(iJh, ir2f * idzf, iJf);
+        vmul(iW, iJf, iWJf);
+        vmul(tb, iWJf, w1);
+        vmuls(w1, FT(-1), w1);
+        vmul(ta, iWJf, w2);
+        FT cv1[4] = {0, 0, 0, 0}, cv2[4] = {0, 0, 0, 0}, gK[4] = {0, 0, 0, 0}, cc1[4], cc2[4], l4[4], rJ[4];
+        if (inner) {
+          // u_h of the levels below and above (not yet overwritten: P3 writes them)
+          FT a1[4], b1[4], a2[4], b2[4], num[4], den[4];
 #pragma unroll
-        for (int i = 0; i < 4; ++i) {
-          const int n = NQ * j + i;
-          const FT Jf = Jh[i] * r2 * dzf;
-          const FT iJf = iJh[i] * ir2f * idzf, iWJf = iW[i] * iJf;
-          const FT w1 = -tb[i] * iWJf, w2 = ta[i] * iWJf;
-          FT cv1 = 0, cv2 = 0, gK = 0, cc1, cc2, l4, rJ;
-          if (inner) {
-            // u_h of the levels below and above (not yet overwritten: P3 writes them)
+          for (int i = 0; i < 4; ++i) {
+            const int n = NQ * j + i;
             const int qa = n * Nv + va, qb = n * Nv + vb;
-            cv1 = -(sY[32 * Nv + qb] - sY[32 * Nv + qa]) * iJf;
-            cv2 = (sY[16 * Nv + qb] - sY[16 * Nv + qa]) * iJf;
-            cc1 = (C1a[i] + C1b[i]) / FT(2);
-            cc2 = (C2a[i] + C2b[i]) / FT(2);
-            gK = Kb[i] - Ka[i];
-            l4 = gdiv(Ra[i] * La[i] + Rb[i] * Lb[i], Ra[i] + Rb[i]);
-            rJ = (Ra[i] + Rb[i]) / FT(2);
-          } else {
-            cc1 = C1a[i];
-            cc2 = C2a[i];
-            l4 = La[i];
-            rJ = Ra[i];
+            a1[i] = sY[16 * Nv + qa];
+            b1[i] = sY[16 * Nv + qb];
+            a2[i] = sY[32 * Nv + qa];
+            b2[i] = sY[32 * Nv + qb];
           }
-          const FT fo1 = fh1[i] * rinv + cv1 + w1, fo2 = fh2[i] * rinv + cv2 + w2;
-          const FT b3 = rJ * (u3[i] * g33);
-          FT T3 = -(P.nu_v * l4);
-          T3 -= Jf * (fo1 * cc2 - fo2 * cc1) + gK;
-          X1[i] = Jf * (fo2 * b3);
-          X2[i] = Jf * (-fo1 * b3);
-          sOf[n * Nf + k] = T3;
+          vsub(a2, b2, cv1);
+          vmul(cv1, iJf, cv1);   // -(d u_2 / d xi^3) / J_f
+          vsub(b1, a1, cv2);
+          vmul(cv2, iJf, cv2);   // (d u_1 / d xi^3) / J_f
+          vadd(C1a, C1b, cc1);
+          vmuls(cc1, FT(0.5), cc1);
+          vadd(C2a, C2b, cc2);
+          vmuls(cc2, FT(0.5), cc2);
+          vsub(Kb, Ka, gK);
+          vmul(Rb, Lb, num);
+          vfma(Ra, La, num, num);
+          vadd(Ra, Rb, den);
+#pragma unroll
+          for (int i = 0; i < 4; ++i) l4[i] = gdiv(num[i], den[i]);
+          vmuls(den, FT(0.5), rJ);
+        } else {
+#pragma unroll
+          for (int i = 0; i < 4; ++i) {
+            cc1[i] = C1a[i];
+            cc2[i] = C2a[i];
+            l4[i] = La[i];
+            rJ[i] = Ra[i];
+          }
         }
+        // (f^12 + w^12) on the face, the u_3 tendency and the face cross products
+        FT fo1[4], fo2[4], b3[4], t[4], T3[4], X1[4], X2[4];
+        vfmas(fh1, rinv, cv1, fo1);
+        vadd(fo1, w1, fo1);
+        vfmas(fh2, rinv, cv2, fo2);
+        vadd(fo2, w2, fo2);
+        FT u3g[4];
+        vmuls(u3, g33, u3g);
+        vmul(rJ, u3g, b3);
+        vmul(fo2, cc1, t);
+        vmuls(t, FT(-1), t);
+        vfma(fo1, cc2, t, t);
+        vfma(Jf, t, gK, t);
+        vmuls(l4, -P.nu_v, T3);
+        vsub(T3, t, T3);
+        vmul(fo2, b3, X1);
+        vmul(Jf, X1, X1);
+        vmul(fo1, b3, X2);
+        vmul(Jf, X2, X2);
+        vmuls(X2, FT(-1), X2);
+#pragma unroll
+        for (int i = 0; i < 4; ++i) sOf[(NQ * j + i) * Nf + k] = T3[i];
         st_row(sX1 + (size_t)k * NN + NQ * j, X1);
         st_row(sX2 + (size_t)k * NN + NQ * j, X2);
       }
@@ -532,12 +592,20 @@ __global__ void __launch_bounds__(SE_THREADS, SeMinBlocks<FT>::value) k_passB(De
         ld_row(row(sS, SB_RJ, v), rJ);
         ld_row(row(sS, SB_Q1, v), Q1);
         ld_row(row(sS, SB_Q2, v), Q2);
+        FT irJ[4], t1v[4], t2v[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) irJ[i] = grcp(rJ[i]);
+        vadd(Xa1, Xb1, t1v);
+        vmul(t1v, irJ, t1v);
+        vfmas(t1v, FT(-0.5), Q1, t1v);
+        vadd(Xa2, Xb2, t2v);
+        vmul(t2v, irJ, t2v);
+        vfmas(t2v, FT(-0.5), Q2, t2v);
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
           const int q = (NQ * j + i) * Nv + v;
-          const FT irJ = grcp(rJ[i]);
-          sO[16 * Nv + q] = Q1[i] - (Xa1[i] + Xb1[i]) / FT(2) * irJ;
-          sO[32 * Nv + q] = Q2[i] - (Xa2[i] + Xb2[i]) / FT(2) * irJ;
+          sO[16 * Nv + q] = t1v[i];
+          sO[32 * Nv + q] = t2v[i];
         }
       }
     }

@@ -20,6 +20,69 @@ __device__ __forceinline__ void put2(float2 lo, float2 hi, float (&o)[4]) {
 }
 __device__ __forceinline__ float2 ld2(const float *p) { return *reinterpret_cast<const float2 *>(p); }
 
+// Element-wise arithmetic on a 4-node row: FP64 one operation per node, FP32 two packed
+// (f32x2) operations per row.  o may alias an input.
+template <class FT>
+__device__ __forceinline__ void vmul(const FT (&a)[4], const FT (&b)[4], FT (&o)[4]) {
+#pragma unroll
+  for (int i = 0; i < 4; ++i) o[i] = a[i] * b[i];
+}
+__device__ __forceinline__ void vmul(const float (&a)[4], const float (&b)[4], float (&o)[4]) {
+  put2(__fmul2_rn(lo2(a), lo2(b)), __fmul2_rn(hi2(a), hi2(b)), o);
+}
+template <class FT>
+__device__ __forceinline__ void vmuls(const FT (&a)[4], FT c, FT (&o)[4]) {
+#pragma unroll
+  for (int i = 0; i < 4; ++i) o[i] = a[i] * c;
+}
+__device__ __forceinline__ void vmuls(const float (&a)[4], float c, float (&o)[4]) {
+  put2(__fmul2_rn(lo2(a), bc2(c)), __fmul2_rn(hi2(a), bc2(c)), o);
+}
+// o = a b + c
+template <class FT>
+__device__ __forceinline__ void vfma(const FT (&a)[4], const FT (&b)[4], const FT (&c)[4], FT (&o)[4]) {
+#pragma unroll
+  for (int i = 0; i < 4; ++i) o[i] = fma(a[i], b[i], c[i]);
+}
+__device__ __forceinline__ void vfma(const float (&a)[4], const float (&b)[4], const float (&c)[4], float (&o)[4]) {
+  put2(__ffma2_rn(lo2(a), lo2(b), lo2(c)), __ffma2_rn(hi2(a), hi2(b), hi2(c)), o);
+}
+// o = a s + c
+template <class FT>
+__device__ __forceinline__ void vfmas(const FT (&a)[4], FT sc, const FT (&c)[4], FT (&o)[4]) {
+#pragma unroll
+  for (int i = 0; i < 4; ++i) o[i] = fma(a[i], sc, c[i]);
+}
+__device__ __forceinline__ void vfmas(const float (&a)[4], float sc, const float (&c)[4], float (&o)[4]) {
+  put2(__ffma2_rn(lo2(a), bc2(sc), lo2(c)), __ffma2_rn(hi2(a), bc2(sc), hi2(c)), o);
+}
+template <class FT>
+__device__ __forceinline__ void vadd(const FT (&a)[4], const FT (&b)[4], FT (&o)[4]) {
+#pragma unroll
+  for (int i = 0; i < 4; ++i) o[i] = a[i] + b[i];
+}
+__device__ __forceinline__ void vadd(const float (&a)[4], const float (&b)[4], float (&o)[4]) {
+  put2(__fadd2_rn(lo2(a), lo2(b)), __fadd2_rn(hi2(a), hi2(b)), o);
+}
+template <class FT>
+__device__ __forceinline__ void vsub(const FT (&a)[4], const FT (&b)[4], FT (&o)[4]) {
+#pragma unroll
+  for (int i = 0; i < 4; ++i) o[i] = a[i] - b[i];
+}
+__device__ __forceinline__ void vsub(const float (&a)[4], const float (&b)[4], float (&o)[4]) {
+  const float2 m = bc2(-1.0f);
+  put2(__ffma2_rn(lo2(b), m, lo2(a)), __ffma2_rn(hi2(b), m, hi2(a)), o);
+}
+// o = (a x + b y) s, the metric contraction of a covariant pair (x, y) with weight s per node
+template <class FT>
+__device__ __forceinline__ void vcontract(const FT (&a)[4], const FT (&b)[4], const FT (&x)[4], const FT (&y)[4],
+                                          const FT (&w)[4], FT (&o)[4]) {
+  FT t[4];
+  vmul(b, y, t);
+  vfma(a, x, t, t);
+  vmul(w, t, o);
+}
+
 // Row helper: the thread's row j and its xi^2 derivative coefficients.
 template <class FT>
 struct Row {
@@ -226,13 +289,10 @@ struct LevRow {
     r2 = r2_;
     ir2 = ir2_;
     G33 = dz * dz;
-#pragma unroll
-    for (int i = 0; i < NQ; ++i) {
-      J[i] = Jh[i] * r2 * dz;
-      iJ[i] = iJh[i] * ir2 * idz;
-      WJ[i] = W[i] * J[i];
-      iWJ[i] = iW[i] * iJ[i];
-    }
+    vmuls(Jh, r2 * dz, J);
+    vmuls(iJh, ir2 * idz, iJ);
+    vmul(W, J, WJ);
+    vmul(iW, iJ, iWJ);
   }
   __device__ void set(const RowGeo<FT> &g, FT r2_, FT ir2_, FT dz, FT idz) {
     set_rows(g.Jh, g.iJh, g.W, g.iW, r2_, ir2_, dz, idz);
@@ -244,16 +304,15 @@ template <class FT, class G>
 __device__ __forceinline__ void vec_lap(const DevParams<FT> &P, const Row<FT> &R, const G &g,
                                         const LevRow<FT> &s, const FT (&c1)[4], const FT (&c2)[4],
                                         const FT (&c3)[4], FT fdiv, FT (&o1)[4], FT (&o2)[4], FT (&o3)[4]) {
+  // the metric of the level is the surface metric scaled by r^-2 (g^ij) or r^2 (g_ij): the
+  // scale is folded into the per-node weight of each contraction
   FT a[4], b[4], da[4], db[4];
   {
-    FT gu0[4], gu1[4], gu2[4];
+    FT gu0[4], gu1[4], gu2[4], Jr[4];
     g.gu(gu0, gu1, gu2);
-#pragma unroll
-    for (int i = 0; i < 4; ++i) {
-      const FT x0 = gu0[i] * s.ir2, x1 = gu1[i] * s.ir2, x2 = gu2[i] * s.ir2;
-      a[i] = s.J[i] * (x0 * c1[i] + x1 * c2[i]);
-      b[i] = s.J[i] * (x1 * c1[i] + x2 * c2[i]);
-    }
+    vmuls(s.J, s.ir2, Jr);
+    vcontract(gu0, gu1, c1, c2, Jr, a);   // J (g^11 c1 + g^12 c2)
+    vcontract(gu1, gu2, c1, c2, Jr, b);   // J (g^12 c1 + g^22 c2)
   }
   d1(P, a, da);
   d2(R, b, db);
@@ -261,8 +320,9 @@ __device__ __forceinline__ void vec_lap(const DevParams<FT> &P, const Row<FT> &R
   {
     FT W[4];
     g.w(W);
-#pragma unroll
-    for (int i = 0; i < 4; ++i) wdv[i] = W[i] * ((da[i] + db[i]) * s.iJ[i]);
+    vadd(da, db, wdv);
+    vmul(wdv, s.iJ, wdv);
+    vmul(W, wdv, wdv);
   }
   t1(P, wdv, w1);
   t2(R, wdv, w2);
@@ -273,18 +333,17 @@ __device__ __forceinline__ void vec_lap(const DevParams<FT> &P, const Row<FT> &R
   d1(P, c3, e4);
   FT Wz1[4], Wz2[4], Wz3[4];
   {
-    FT gd0[4], gd1[4], gd2[4], W[4];
+    FT gd0[4], gd1[4], gd2[4], W[4], WiJ[4], k2[4];
     g.gd(gd0, gd1, gd2);
     g.w(W);
-#pragma unroll
-    for (int i = 0; i < 4; ++i) {
-      const FT k3 = (e1[i] - e2[i]) * s.iJ[i];
-      const FT k1 = e3[i] * s.iJ[i], k2 = -e4[i] * s.iJ[i];
-      const FT x0 = gd0[i] * s.r2, x1 = gd1[i] * s.r2, x2 = gd2[i] * s.r2;
-      Wz1[i] = W[i] * (x0 * k1 + x1 * k2);
-      Wz2[i] = W[i] * (x1 * k1 + x2 * k2);
-      Wz3[i] = W[i] * (s.G33 * k3);
-    }
+    vmul(W, s.iJ, WiJ);
+    vsub(e1, e2, Wz3);
+    vmul(Wz3, WiJ, Wz3);
+    vmuls(Wz3, s.G33, Wz3);               // W G33 (e1 - e2) / J
+    vmuls(WiJ, s.r2, WiJ);
+    vmuls(e4, FT(-1), k2);
+    vcontract(gd0, gd1, e3, k2, WiJ, Wz1);  // W r^2 (g_11 k1 + g_12 k2), k = (e3, -e4) / J
+    vcontract(gd1, gd2, e3, k2, WiJ, Wz2);
   }
   FT f1[4], f2[4], f3[4], f4[4];
   t1(P, Wz2, f1);
@@ -292,18 +351,22 @@ __device__ __forceinline__ void vec_lap(const DevParams<FT> &P, const Row<FT> &R
   t2(R, Wz3, f3);
   t1(P, Wz3, f4);
   {
-    FT gd0[4], gd1[4], gd2[4], iW[4];
+    FT gd0[4], gd1[4], gd2[4], iW[4], q1[4], q3[4], r2iWJ[4], t[4];
     g.gd(gd0, gd1, gd2);
     g.iw(iW);
-#pragma unroll
-    for (int i = 0; i < 4; ++i) {
-      const FT q3 = (-f1[i] + f2[i]) * s.iWJ[i];
-      const FT q1 = -f3[i] * s.iWJ[i], q2 = f4[i] * s.iWJ[i];
-      const FT x0 = gd0[i] * s.r2, x1 = gd1[i] * s.r2, x2 = gd2[i] * s.r2;
-      o1[i] = fdiv * (-w1[i] * iW[i]) - (x0 * q1 + x1 * q2);
-      o2[i] = fdiv * (-w2[i] * iW[i]) - (x1 * q1 + x2 * q2);
-      o3[i] = -s.G33 * q3;
-    }
+    vsub(f2, f1, q3);
+    vmul(q3, s.iWJ, q3);
+    vmuls(q3, -s.G33, o3);
+    vmuls(s.iWJ, s.r2, r2iWJ);
+    vmuls(f3, FT(-1), q1);                  // q = (-f3, f4) / (W J); the contraction takes r^2
+    vcontract(gd0, gd1, q1, f4, r2iWJ, t);
+    vmul(w1, iW, o1);
+    vmuls(o1, -fdiv, o1);
+    vsub(o1, t, o1);
+    vcontract(gd1, gd2, q1, f4, r2iWJ, t);
+    vmul(w2, iW, o2);
+    vmuls(o2, -fdiv, o2);
+    vsub(o2, t, o2);
   }
 }
 
@@ -316,25 +379,21 @@ __device__ __forceinline__ void vec_lap_o3(const DevParams<FT> &P, const Row<FT>
   d2(R, c3, e3);
   d1(P, c3, e4);
   {
-    FT gd0[4], gd1[4], gd2[4], W[4];
+    FT gd0[4], gd1[4], gd2[4], W[4], WiJ[4], k2[4];
     g.gd(gd0, gd1, gd2);
     g.w(W);
-#pragma unroll
-    for (int i = 0; i < 4; ++i) {
-      const FT k1 = e3[i] * s.iJ[i], k2 = -e4[i] * s.iJ[i];
-      const FT x0 = gd0[i] * s.r2, x1 = gd1[i] * s.r2, x2 = gd2[i] * s.r2;
-      Wz1[i] = W[i] * (x0 * k1 + x1 * k2);
-      Wz2[i] = W[i] * (x1 * k1 + x2 * k2);
-    }
+    vmul(W, s.iJ, WiJ);
+    vmuls(WiJ, s.r2, WiJ);
+    vmuls(e4, FT(-1), k2);
+    vcontract(gd0, gd1, e3, k2, WiJ, Wz1);
+    vcontract(gd1, gd2, e3, k2, WiJ, Wz2);
   }
-  FT f1[4], f2[4];
+  FT f1[4], f2[4], q3[4];
   t1(P, Wz2, f1);
   t2(R, Wz1, f2);
-#pragma unroll
-  for (int i = 0; i < 4; ++i) {
-    const FT q3 = (-f1[i] + f2[i]) * s.iWJ[i];
-    o3[i] = -s.G33 * q3;
-  }
+  vsub(f2, f1, q3);
+  vmul(q3, s.iWJ, q3);
+  vmuls(q3, -s.G33, o3);
 }
 
 // weak divergence -(1/WJ) (D^T (WJ F1) along xi^1 + along xi^2)
@@ -342,15 +401,13 @@ template <class FT>
 __device__ __forceinline__ void wdiv(const DevParams<FT> &P, const Row<FT> &R, const LevRow<FT> &s,
                                      const FT (&F1)[4], const FT (&F2)[4], FT (&o)[4]) {
   FT a[4], b[4], ta[4], tb[4];
-#pragma unroll
-  for (int i = 0; i < 4; ++i) {
-    a[i] = s.WJ[i] * F1[i];
-    b[i] = s.WJ[i] * F2[i];
-  }
+  vmul(s.WJ, F1, a);
+  vmul(s.WJ, F2, b);
   t1(P, a, ta);
   t2(R, b, tb);
-#pragma unroll
-  for (int i = 0; i < 4; ++i) o[i] = -(ta[i] + tb[i]) * s.iWJ[i];
+  vadd(ta, tb, o);
+  vmul(o, s.iWJ, o);
+  vmuls(o, FT(-1), o);
 }
 
 // ---------------------------------------------------------------- reverse (adjoint) forms

@@ -122,36 +122,58 @@ __global__ void __launch_bounds__(SE_THREADS, SeMinBlocks<FT>::value) k_passA(De
       const FT Phi = P.levc[LC_PHI * Nv + v];
       const Lev4<FT> rl = P.lr4[v];
       const FT g3a = P.levf[LF_G33 * Nf + v], g3b = P.levf[LF_G33 * Nf + v + 1];
-      FT u1[4], u2[4], ub3[4], sd[4];
+      FT u1[4], u2[4], ub3[4], sd[4], K[4];
+      {
+        FT rho[4], rhoe[4], fa[4], fb[4], t[4], c1[4], c2[4];
 #pragma unroll
-      for (int i = 0; i < 4; ++i) {
-        const int n = NQ * j + i;
-        const int q = n * Nv + v;
-        const FT rho = sY[q], rhoe = sY[48 * Nv + q];
-        u1[i] = sY[16 * Nv + q];
-        u2[i] = sY[32 * Nv + q];
-        // u_bar_3 = I^c(u_3) and the face part of K, with u_3 = 0 on the boundary faces
-        const FT fa = v == 0 ? FT(0) : sF[n * Nf + v];
-        const FT fb = v + 1 == Nv ? FT(0) : sF[n * Nf + v + 1];
-        ub3[i] = (fa + fb) / FT(2);
-        const FT kv = (fa * (fa * g3a) + fb * (fb * g3b)) / FT(2);
-        const FT gu0 = g.gu0[i] * s.ir2, gu1 = g.gu1[i] * s.ir2, gu2 = g.gu2[i] * s.ir2;
-        const FT c1 = gu0 * u1[i] + gu1 * u2[i], c2 = gu1 * u1[i] + gu2 * u2[i];
-        const FT K = (u1[i] * c1 + u2[i] * c2 + kv) / FT(2);
-        Thermo<FT> th;
-        thermo(P, rho, rhoe, K, Phi, rl, th);
-        sd[i] = sd_dev(P, th);
+        for (int i = 0; i < 4; ++i) {
+          const int n = NQ * j + i;
+          const int q = n * Nv + v;
+          rho[i] = sY[q];
+          rhoe[i] = sY[48 * Nv + q];
+          u1[i] = sY[16 * Nv + q];
+          u2[i] = sY[32 * Nv + q];
+          // u_3 of the faces below and above (0 on the boundary faces)
+          fa[i] = v == 0 ? FT(0) : sF[n * Nf + v];
+          fb[i] = v + 1 == Nv ? FT(0) : sF[n * Nf + v + 1];
+        }
+        // u_bar_3 = I^c(u_3); CT12(u_h) with the level's g^ij = r^-2 g^ij(surface); K
+        vadd(fa, fb, ub3);
+        vmuls(ub3, FT(0.5), ub3);
+        vmul(g.gu1, u2, t);
+        vfma(g.gu0, u1, t, t);
+        vmuls(t, s.ir2, c1);
+        vmul(g.gu2, u2, t);
+        vfma(g.gu1, u1, t, t);
+        vmuls(t, s.ir2, c2);
+        FT kv2[4];
+        vmuls(fb, g3b, kv2);
+        vmul(fb, kv2, kv2);
+        vmuls(fa, g3a, t);
+        vfma(fa, t, kv2, kv2);
+        vmul(u2, c2, t);
+        vfma(u1, c1, t, t);
+        vfmas(kv2, FT(0.5), t, K);
+        vmuls(K, FT(0.5), K);
+        // s_d - s_d,r = cp_d (T - T_r) + (Phi - Phi_r)
+        ThermoRow<FT> th;
+        thermo_row(P, rho, rhoe, K, Phi, rl, th);
+        vsub(th.T, th.Tr, t);
+        vfmas(t, P.cpd, th.phid, sd);
       }
       FT o1[4], o2[4], o3[4];
       vec_lap(P, R, g, s, u1, u2, ub3, FT(1), o1, o2, o3);
       FT g1[4], g2[4], x1[4], x2[4], Ls[4];
       d1(P, sd, g1);
       d2(R, sd, g2);
-#pragma unroll
-      for (int i = 0; i < 4; ++i) {
-        const FT gu0 = g.gu0[i] * s.ir2, gu1 = g.gu1[i] * s.ir2, gu2 = g.gu2[i] * s.ir2;
-        x1[i] = gu0 * g1[i] + gu1 * g2[i];
-        x2[i] = gu1 * g1[i] + gu2 * g2[i];
+      {
+        FT t[4];
+        vmul(g.gu1, g2, t);
+        vfma(g.gu0, g1, t, t);
+        vmuls(t, s.ir2, x1);
+        vmul(g.gu2, g2, t);
+        vfma(g.gu1, g1, t, t);
+        vmuls(t, s.ir2, x2);
       }
       wdiv(P, R, s, x1, x2, Ls);
       if (act) {
@@ -317,16 +339,21 @@ __global__ void __launch_bounds__(SE_THREADS, SeMinBlocks<FT>::value) k_passB(De
           vfmas(kv2, FT(0.5), t, K);
           vmuls(K, FT(0.5), K);
           if (HS) g.row(HG_S2, s2);
+          ThermoRow<FT> th4;
+          thermo_row(P, rho, rhoe, K, Phi, rl, th4);
+#pragma unroll
+          for (int i = 0; i < 4; ++i) {
+            h[i] = th4.h[i];
+            Pi[i] = th4.Pi[i];
+            phid[i] = th4.phid[i];
+          }
+          vsub(th4.thv, th4.thvr, thp);
 #pragma unroll
           for (int i = 0; i < 4; ++i) {
             const int q = (NQ * j + i) * Nv + v;
-            Thermo<FT> th;
-            thermo(P, rho[i], rhoe[i], K[i], Phi, rl, th);
-            h[i] = th.h;
-            Pi[i] = th.Pi;
-            thp[i] = th.thv - th.thvr;
-            phid[i] = th.phid;
             if (HS) {
+              Thermo<FT> th;
+              th.p = th4.p[i];
               // Held-Suarez forcing (held_suarez.jl:98-141, 203-225, 279-295), flat surface:
               // sigma = p / MSLP; rho e_tot relaxes with -cv_d k_T rho (p / (rho R_d) - T_eq)
               const FT c2l = FT(1) - s2[i];

@@ -6,14 +6,9 @@ namespace gb {
 
 // Shared-memory layouts of the element-slab kernels (byte offsets).  The
 // input slabs are double-buffered (nbuf = 2) when they fit, else single.
-// Level-major copy of an element's face slab, face k node n at k * FT_STRIDE + n: with the
-// level-slot thread mapping the four rows of a level then hit 32 distinct banks (the
-// node-major slab has a stride of Nv + 1 words, 64 for the production grid: 4-way conflicts).
-constexpr int FT_STRIDE = 17;
-
 template <class FT>
 struct PassALayout {
-  size_t y[2], f[2], g[2], out, ft, bar, total;
+  size_t y[2], f[2], g[2], out, bar, total;
   __host__ __device__ PassALayout(int Nv, int nbuf) {
     const int Nf = Nv + 1;
     size_t o = 0;
@@ -27,7 +22,6 @@ struct PassALayout {
       }
     }
     out = o; o += align16(sizeof(FT) * 64 * Nv);
-    ft = o; o += align16(sizeof(FT) * FT_STRIDE * Nf);
     bar = o; o += 16;
     total = o;
   }
@@ -58,9 +52,7 @@ struct PassBLayout {
       }
     }
     s = o; o += align16(sizeof(FT) * SB_N * 16 * Nv);
-    // face rows [Nf][16] of the cross products (P2, P3); before them (P1, the start of P2) the
-    // two hold the level-major face copy ([Nf][FT_STRIDE] <= 2 [Nf][16])
-    x1 = o; o += align16(sizeof(FT) * 16 * Nf);
+    x1 = o; o += align16(sizeof(FT) * 16 * Nf);   // face rows [Nf][16]
     x2 = o; o += align16(sizeof(FT) * 16 * Nf);
     w = o; o += align16(sizeof(FT) * 2 * 16);     // GLL weights W, 1/W
     bar = o; o += 16;

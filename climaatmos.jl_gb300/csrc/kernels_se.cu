@@ -90,17 +90,6 @@ __device__ __forceinline__ bool begin_element(const DevParams<FT> &P, uint64_t *
   return __syncthreads_and(ok) != 0;
 }
 
-// The element's face slab [16][Nf] (node-major, as it arrives) into the level-major copy
-// [Nf][FT_STRIDE]: consecutive threads read consecutive words and write rows FT_STRIDE (odd)
-// words apart, both without bank conflicts.  The caller synchronizes before reading it.
-template <class FT>
-__device__ __forceinline__ void face_copy(const FT *sF, FT *sFT, int Nf) {
-  for (int idx = threadIdx.x; idx < NN * Nf; idx += SE_THREADS) {
-    const int n = idx / Nf, k = idx - n * Nf;
-    sFT[k * FT_STRIDE + n] = sF[idx];
-  }
-}
-
 template <class FT>
 __global__ void __launch_bounds__(SE_THREADS, SeMinBlocks<FT>::value) k_passA(DevParams<FT> P, int nbuf, const FT *__restrict__ Yc,
                                                          const FT *__restrict__ Yf, FT *__restrict__ Lout) {
@@ -112,7 +101,6 @@ __global__ void __launch_bounds__(SE_THREADS, SeMinBlocks<FT>::value) k_passA(De
   FT *sFb[2] = {(FT *)(sm + Lo.f[0]), (FT *)(sm + Lo.f[1])};
   FT *sGb[2] = {(FT *)(sm + Lo.g[0]), (FT *)(sm + Lo.g[1])};
   FT *sO = (FT *)(sm + Lo.out);
-  FT *sFT = (FT *)(sm + Lo.ft);
   uint64_t *bar = (uint64_t *)(sm + Lo.bar);
   init_bars(bar);
   int e = blockIdx.x;
@@ -124,8 +112,6 @@ __global__ void __launch_bounds__(SE_THREADS, SeMinBlocks<FT>::value) k_passA(De
     int b;
     if (!begin_element<FT>(P, bar, nbuf, it, e, sYb, sFb, sGb, sGb, false, Yc, Yf, nullptr, b)) break;
     const FT *sY = pick(b, sYb[0], sYb[1]), *sF = pick(b, sFb[0], sFb[1]), *sG = pick(b, sGb[0], sGb[1]);
-    face_copy(sF, sFT, Nf);
-    __syncthreads();
     RowGeo<FT> g;
     g.load(sG, P, j);
     for (int v0 = 0; v0 < Nv; v0 += SE_LEVELS) {
@@ -148,8 +134,8 @@ __global__ void __launch_bounds__(SE_THREADS, SeMinBlocks<FT>::value) k_passA(De
           u1[i] = sY[16 * Nv + q];
           u2[i] = sY[32 * Nv + q];
           // u_3 of the faces below and above (0 on the boundary faces)
-          fa[i] = v == 0 ? FT(0) : sFT[v * FT_STRIDE + n];
-          fb[i] = v + 1 == Nv ? FT(0) : sFT[(v + 1) * FT_STRIDE + n];
+          fa[i] = v == 0 ? FT(0) : sF[n * Nf + v];
+          fb[i] = v + 1 == Nv ? FT(0) : sF[n * Nf + v + 1];
         }
         // u_bar_3 = I^c(u_3); CT12(u_h) with the level's g^ij = r^-2 g^ij(surface); K
         vadd(fa, fb, ub3);
@@ -295,9 +281,6 @@ __global__ void __launch_bounds__(SE_THREADS, SeMinBlocks<FT>::value) k_passB(De
     FT *sY = at(Lo.y, b), *sF = at(Lo.f, b);
     const FT *sG = at(Lo.g, b), *sL = at(Lo.lap, b);
     FT *sO = sY, *sOf = sF;
-    FT *sFT = sX1;   // level-major face copy, read in P1 and at the start of P2
-    face_copy(sF, sFT, Nf);
-    __syncthreads();
     const SlabGeo<FT> g{sG + NQ * j, sW + NQ * j};
     // ---- P1: centre-level horizontal work, ordered so that each group of
     // intermediate fields dies before the next is formed; per-level results
@@ -334,8 +317,8 @@ __global__ void __launch_bounds__(SE_THREADS, SeMinBlocks<FT>::value) k_passB(De
             u2[i] = sY[32 * Nv + q];
             rhoe[i] = sY[48 * Nv + q];
             // u_3 of the faces below and above (0 on the boundary faces)
-            fa[i] = v == 0 ? FT(0) : sFT[v * FT_STRIDE + n];
-            fb[i] = v + 1 == Nv ? FT(0) : sFT[(v + 1) * FT_STRIDE + n];
+            fa[i] = v == 0 ? FT(0) : sF[n * Nf + v];
+            fb[i] = v + 1 == Nv ? FT(0) : sF[n * Nf + v + 1];
           }
           // CT12(u_h) = g^ij u_j with the level's g^ij = r^-2 g^ij(surface)
           g.gu(gu0, gu1, gu2);
@@ -512,25 +495,10 @@ __global__ void __launch_bounds__(SE_THREADS, SeMinBlocks<FT>::value) k_passB(De
       }
     }
     __syncthreads();
-    // ---- P2: face-level work (f^12 + w^12, cross products, u_3 tendency).  Faces in the
-    // level-slot order (bank-conflict free on the node-major state slab); u_3 of every sweep
-    // is read from the level-major copy before the sweeps overwrite it with the cross products.
-    constexpr int P2_SWEEPS = (127 + 1 + SE_LEVELS - 1) / SE_LEVELS;  // z_elem <= 127
-    FT u3s[P2_SWEEPS][4];
-#pragma unroll
-    for (int w = 0; w < P2_SWEEPS; ++w) {
-      const int k = min(w * SE_LEVELS + vs, Nf - 1);
-      const bool inner = k > 0 && k < Nv;
-#pragma unroll
-      for (int i = 0; i < 4; ++i) u3s[w][i] = inner && w * SE_LEVELS < Nf ? sFT[k * FT_STRIDE + NQ * j + i] : FT(0);
-    }
-    __syncthreads();
-#pragma unroll
-    for (int w = 0; w < P2_SWEEPS; ++w) {
-      const int k0 = w * SE_LEVELS;
-      if (k0 >= Nf) break;
-      const int k = min(k0 + vs, Nf - 1);
-      const bool act = k0 + vs < Nf;
+    // ---- P2: face-level work (f^12 + w^12, cross products, u_3 tendency)
+    for (int k0 = 0; k0 < Nf; k0 += SE_LEVELS) {
+      const int k = min(k0 + vl, Nf - 1);
+      const bool act = k0 + vl < Nf;
       const bool inner = k > 0 && k < Nv;
       const FT r2 = P.levf[LF_R2 * Nf + k], dzf = P.levf[LF_DZ * Nf + k], rinv = P.levf[LF_RINV * Nf + k];
       const FT ir2f = P.levf[LF_IR2 * Nf + k], idzf = P.levf[LF_IDZ * Nf + k], g33 = P.levf[LF_G33 * Nf + k];
@@ -539,8 +507,10 @@ __global__ void __launch_bounds__(SE_THREADS, SeMinBlocks<FT>::value) k_passB(De
         FT W[4];
         g.w(W);
 #pragma unroll
-        for (int i = 0; i < 4; ++i) u3[i] = u3s[w][i];
-        vmul(W, u3, Wu);
+        for (int i = 0; i < 4; ++i) {
+          u3[i] = inner ? sF[(NQ * j + i) * Nf + k] : FT(0);
+          Wu[i] = W[i] * u3[i];
+        }
       }
       FT ta[4], tb[4];
       t2(R, Wu, tb);

@@ -60,6 +60,50 @@ __device__ __forceinline__ Cen<FT> cdiag(const DevParams<FT> &P, const ColGeo<FT
   return o;
 }
 
+// The centre diagnostics of the lane's CM levels r0 .. r0 + CM - 1 from the state U
+// (rho, u_1, u_2, rho e_tot), the u_3 of the faces below (u3a) and above (u3b) each level
+// and their g^33.  FP32 with two levels per lane: both levels at once, the same quantities
+// with packed arithmetic (thermo_pair).
+template <class FT, int CM>
+__device__ __forceinline__ void cdiag_lane(const DevParams<FT> &P, const ColGeo<FT> &G, const ColLev<FT> &L, int r0,
+                                           const FT (&U)[5][CM], const FT (&u3a)[CM], const FT (&u3b)[CM],
+                                           const FT (&g33a)[CM], const FT (&g33b)[CM], Cen<FT> (&o)[CM]) {
+#pragma unroll
+  for (int k = 0; k < CM; ++k)
+    o[k] = cdiag(P, G, L, r0 + k, U[0][k], U[1][k], U[2][k], U[3][k], u3a[k], u3b[k], g33a[k], g33b[k]);
+}
+template <>
+__device__ __forceinline__ void cdiag_lane<float, 2>(const DevParams<float> &P, const ColGeo<float> &G,
+                                                     const ColLev<float> &L, int r0, const float (&U)[5][2],
+                                                     const float (&u3a)[2], const float (&u3b)[2],
+                                                     const float (&g33a)[2], const float (&g33b)[2],
+                                                     Cen<float> (&o)[2]) {
+  const int v0 = min(max(r0, 0), L.Nv - 1), v1 = min(max(r0 + 1, 0), L.Nv - 1);
+  const Lev4<float> C0 = L.lc4[v0], C1 = L.lc4[v1], R0 = L.lr4[v0], R1 = L.lr4[v1];
+  const float2 rho = make_float2(U[0][0], U[0][1]), u1 = make_float2(U[1][0], U[1][1]);
+  const float2 u2 = make_float2(U[2][0], U[2][1]), rhoe = make_float2(U[3][0], U[3][1]);
+  const float2 a = make_float2(u3a[0], u3a[1]), b = make_float2(u3b[0], u3b[1]);
+  const float2 ga = make_float2(g33a[0], g33a[1]), gb = make_float2(g33b[0], g33b[1]);
+  const float2 ir2 = make_float2(C0.z, C1.z), phi = make_float2(C0.w, C1.w);
+  const float2 c1 = __fmul2_rn(__ffma2_rn(bc2(G.gu1), u2, __fmul2_rn(bc2(G.gu0), u1)), ir2);
+  const float2 c2 = __fmul2_rn(__ffma2_rn(bc2(G.gu2), u2, __fmul2_rn(bc2(G.gu1), u1)), ir2);
+  const float2 kv = __fmul2_rn(__ffma2_rn(b, __fmul2_rn(b, gb), __fmul2_rn(a, __fmul2_rn(a, ga))), bc2(0.5f));
+  const float2 K = __fmul2_rn(__fadd2_rn(__ffma2_rn(u2, c2, __fmul2_rn(u1, c1)), kv), bc2(0.5f));
+  float2 T, p, h, Pi, thv, thvr, phid, Tr;
+  thermo_pair(P, rho, rhoe, K, phi, make_float2(R0.y, R1.y), make_float2(R0.z, R1.z), T, p, h, Pi, thv, thvr, phid, Tr);
+  const float2 iJ = __fmul2_rn(bc2(G.iJh), make_float2(C0.y, C1.y));
+  const float2 rJ = __fmul2_rn(rho, __fmul2_rn(bc2(G.Jh), make_float2(C0.x, C1.x)));
+  o[0].K = K.x; o[1].K = K.y;
+  o[0].h = h.x; o[1].h = h.y;
+  o[0].phid = phid.x; o[1].phid = phid.y;
+  o[0].Pi = Pi.x; o[1].Pi = Pi.y;
+  o[0].thv = thv.x; o[1].thv = thv.y;
+  o[0].thvr = thvr.x; o[1].thvr = thvr.y;
+  o[0].iJ = iJ.x; o[1].iJ = iJ.y;
+  o[0].rJ = rJ.x; o[1].rJ = rJ.y;
+  o[0].phi = phi.x; o[1].phi = phi.y;
+}
+
 // Tridiagonal solve of the CM*G rows held CM per lane by a G-lane group:
 // log2(CM) in-lane cyclic-reduction levels reduce each lane's rows to one,
 // parallel cyclic reduction solves the G reduced rows across the group, and
@@ -166,11 +210,22 @@ __device__ __forceinline__ void newton_core(const DevParams<FT> &P, const ColGeo
   Cen<FT> prev = cdiag(P, Gm, L, r0 - 1, gl > 0 ? hr : FT(1), hu1, hu2, gl > 0 ? he : FT(1), h3m, u3[0], g33m, LF[0].x);
   FT rhoPrev = gl > 0 ? hr : FT(1);
   FT u3cPrev = h3m * g33m;
+  Cen<FT> cen[CM];
+  {
+    FT u3b[CM], ga[CM], gb[CM];
+#pragma unroll
+    for (int k = 0; k < CM; ++k) {
+      u3b[k] = k + 1 < CM ? u3[k + 1] : u3n;
+      ga[k] = LF[k].x;
+      gb[k] = LF[k + 1].x;
+    }
+    cdiag_lane<FT, CM>(P, Gm, L, r0, U, u3, u3b, ga, gb, cen);
+  }
 #pragma unroll
   for (int k = 0; k < CM; ++k) {
     const int f = r0 + k;
     const FT u3next = k + 1 < CM ? u3[k + 1] : u3n;
-    const Cen<FT> cur = cdiag(P, Gm, L, f, U[0][k], U[1][k], U[2][k], U[3][k], u3[k], u3next, LF[k].x, LF[k + 1].x);
+    const Cen<FT> cur = cen[k];
     iJc[k] = cur.iJ;
     const bool inner = f > 0 && f < Nv;
     const FT g33 = LF[k].x;
@@ -306,12 +361,22 @@ __device__ __forceinline__ void vanleer_correct(const DevParams<FT> &P, const Co
 #pragma unroll
   for (int k = 0; k <= CM; ++k) g33[k] = L.lf4[min(r0 + k, Nf - 1)].x;
   FT hh[CM], rJ[CM];
+  {
+    FT w3a[CM], w3b[CM], ga[CM], gb[CM];
+    Cen<FT> cc[CM];
 #pragma unroll
-  for (int k = 0; k < CM; ++k) {
-    const FT wn = k + 1 < CM ? U[4][k + 1] : w3n;
-    const Cen<FT> cc = cdiag(P, Gm, L, r0 + k, U[0][k], U[1][k], U[2][k], U[3][k], U[4][k], wn, g33[k], g33[k + 1]);
-    hh[k] = cc.h;
-    rJ[k] = cc.rJ;
+    for (int k = 0; k < CM; ++k) {
+      w3a[k] = U[4][k];
+      w3b[k] = k + 1 < CM ? U[4][k + 1] : w3n;
+      ga[k] = g33[k];
+      gb[k] = g33[k + 1];
+    }
+    cdiag_lane<FT, CM>(P, Gm, L, r0, U, w3a, w3b, ga, gb, cc);
+#pragma unroll
+    for (int k = 0; k < CM; ++k) {
+      hh[k] = cc[k].h;
+      rJ[k] = cc[k].rJ;
+    }
   }
   const FT hm2 = up<G>(hh[CM - 2], 1), hm1 = up<G>(hh[CM - 1], 1), rJm = up<G>(rJ[CM - 1], 1);
   const FT hp0 = down<G>(hh[0], 1), hp1 = down<G>(hh[1], 1), rJp = down<G>(rJ[0], 1);
@@ -348,6 +413,24 @@ __device__ __forceinline__ void group_sum(CSum<FT> (&ss)[3]) {
   for (int q = 0; q < 3; ++q)
 #pragma unroll
     for (int o = G / 2; o > 0; o >>= 1) ss[q].add(ss[q].xor_shfl(o, G));
+}
+
+// The column's sums over its lane group for the stage kernel's residual norms: each lane's
+// compensated pair is rounded to one value and the group adds those in plain arithmetic
+// (a butterfly, the same in every lane).  In FP32 the column sum then carries a relative
+// error of at most ~log2(G) + 1 roundings (<= 4e-7), against ~2^-44 for the compensated
+// butterfly of group_sum at about a third of its instructions; the sums across columns
+// stay compensated.  In FP64 it is the plain sum.
+template <int G, class FT>
+__device__ __forceinline__ void group_sum_rounded(CSum<FT> (&ss)[3]) {
+#pragma unroll
+  for (int q = 0; q < 3; ++q) {
+    FT v = ss[q].hi + ss[q].lo;
+#pragma unroll
+    for (int o = G / 2; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o, G);
+    ss[q].hi = v;
+    ss[q].lo = FT(0);
+  }
 }
 
 template <int G, class FT>

@@ -120,6 +120,34 @@ __device__ __forceinline__ void thermo(const DevParams<FT> &P, FT rho, FT rhoe, 
   const FT lx = P.kappa * glog_ratio(p, rl.x, rl.y);
   o.phid = P.cpTmin * lx + rl.z * gexpm1(FT(7) * lx);
 }
+// thermo() for two points at once in FP32 (packed multiplies and adds; the hardware ln, exp,
+// power and reciprocal per point): geopotential Phi and the reference record's 1/p0 (ip0)
+// and cp_d (T_sfc - T_min) / 7 Pi0^7 (rz) per point, so the two may sit on different levels.
+__device__ __forceinline__ float2 bc2(float x) { return make_float2(x, x); }
+__device__ __forceinline__ void thermo_pair(const DevParams<float> &P, float2 rho, float2 rhoe, float2 K, float2 Phi,
+                                            float2 ip0, float2 rz, float2 &T, float2 &p, float2 &h, float2 &Pi,
+                                            float2 &thv, float2 &thvr, float2 &phid, float2 &Tr) {
+  const float2 e = make_float2(gdiv(rhoe.x, rho.x), gdiv(rhoe.y, rho.y));
+  const float2 eint = __ffma2_rn(Phi, bc2(-1.0f), __ffma2_rn(K, bc2(-1.0f), e));
+  T = __ffma2_rn(__fadd2_rn(eint, bc2(P.Rd * P.T0)), bc2(P.icvd), bc2(P.T0));
+  T = make_float2(T.x > P.Tmin_sgs ? T.x : P.Tmin_sgs, T.y > P.Tmin_sgs ? T.y : P.Tmin_sgs);
+  p = __fmul2_rn(__fmul2_rn(rho, bc2(P.Rd)), T);
+  const float2 x = __fmul2_rn(p, bc2(P.ipref));
+  Pi = make_float2(gpow(x.x, P.kappa), gpow(x.y, P.kappa));
+  const float2 Pi2 = __fmul2_rn(Pi, Pi), Pi4 = __fmul2_rn(Pi2, Pi2), Pi7 = __fmul2_rn(__fmul2_rn(Pi4, Pi2), Pi);
+  Tr = __ffma2_rn(bc2(P.Tsfc_ref - P.Tmin_ref), Pi7, bc2(P.Tmin_ref));
+  const float2 iPi = make_float2(grcp(Pi.x), grcp(Pi.y));
+  h = __ffma2_rn(bc2(P.Rd), T, e);
+  thv = __fmul2_rn(T, iPi);
+  thvr = __fmul2_rn(Tr, iPi);
+  // Phi - Phi_r(Pi) as the deviation from the level's reference record (see thermo())
+  const float2 r = __fmul2_rn(p, ip0);
+  const float2 lx = __fmul2_rn(bc2(P.kappa), make_float2(__logf(r.x), __logf(r.y)));
+  const float2 e7 = __fmul2_rn(lx, bc2(7.0f));
+  const float2 em = __fadd2_rn(make_float2(__expf(e7.x), __expf(e7.y)), bc2(-1.0f));
+  phid = __ffma2_rn(rz, em, __fmul2_rn(bc2(P.cpTmin), lx));
+}
+
 // Reverse mode of thermo(): the cotangents of its outputs (T, p, h, Pi, thv,
 // thvr, phir) and of the reference temperature T_r(Pi) give those of
 // (rho, rho e_tot, K).  Uses dPi/dp = kappa Pi / p, dT_r/dPi = 7 (T_sfc - T_min) Pi^6,

@@ -123,7 +123,7 @@ __global__ void __launch_bounds__(CG_THREADS, MINB) k_col_stage_g(DevParams<FT> 
       }
     }
   }
-  col::group_sum<G>(ss);
+  col::group_sum_rounded<G>(ss);
   finite = __all_sync(0xffffffffu, finite);
   if (gl == 0 && colv) {
     if (A.rnorm)

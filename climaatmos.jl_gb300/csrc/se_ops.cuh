@@ -14,7 +14,6 @@ namespace se {
 // Packed FP32: the pair (a[0], a[1]) or (a[2], a[3]) of a 4-node row, and back.
 __device__ __forceinline__ float2 lo2(const float (&a)[4]) { return make_float2(a[0], a[1]); }
 __device__ __forceinline__ float2 hi2(const float (&a)[4]) { return make_float2(a[2], a[3]); }
-__device__ __forceinline__ float2 bc2(float x) { return make_float2(x, x); }
 __device__ __forceinline__ void put2(float2 lo, float2 hi, float (&o)[4]) {
   o[0] = lo.x; o[1] = lo.y; o[2] = hi.x; o[3] = hi.y;
 }
@@ -101,36 +100,14 @@ __device__ __forceinline__ void thermo_row(const DevParams<FT> &P, const FT (&rh
     o.thv[i] = th.thv; o.thvr[i] = th.thvr; o.phid[i] = th.phid; o.Tr[i] = th.Tr;
   }
 }
-__device__ __forceinline__ void thermo_pair(const DevParams<float> &P, float2 rho, float2 rhoe, float2 K, float Phi,
-                                            const Lev4<float> &rl, float2 &T, float2 &p, float2 &h, float2 &Pi,
-                                            float2 &thv, float2 &thvr, float2 &phid, float2 &Tr) {
-  const float2 e = make_float2(gdiv(rhoe.x, rho.x), gdiv(rhoe.y, rho.y));
-  const float2 eint = __fadd2_rn(__ffma2_rn(K, bc2(-1.0f), e), bc2(-Phi));
-  T = __ffma2_rn(__fadd2_rn(eint, bc2(P.Rd * P.T0)), bc2(P.icvd), bc2(P.T0));
-  T = make_float2(T.x > P.Tmin_sgs ? T.x : P.Tmin_sgs, T.y > P.Tmin_sgs ? T.y : P.Tmin_sgs);
-  p = __fmul2_rn(__fmul2_rn(rho, bc2(P.Rd)), T);
-  const float2 x = __fmul2_rn(p, bc2(P.ipref));
-  Pi = make_float2(gpow(x.x, P.kappa), gpow(x.y, P.kappa));
-  const float2 Pi2 = __fmul2_rn(Pi, Pi), Pi4 = __fmul2_rn(Pi2, Pi2), Pi7 = __fmul2_rn(__fmul2_rn(Pi4, Pi2), Pi);
-  Tr = __ffma2_rn(bc2(P.Tsfc_ref - P.Tmin_ref), Pi7, bc2(P.Tmin_ref));
-  const float2 iPi = make_float2(grcp(Pi.x), grcp(Pi.y));
-  h = __ffma2_rn(bc2(P.Rd), T, e);
-  thv = __fmul2_rn(T, iPi);
-  thvr = __fmul2_rn(Tr, iPi);
-  // Phi - Phi_r(Pi) as the deviation from the level's reference record (see thermo())
-  const float2 r = __fmul2_rn(p, bc2(rl.y));   // p / p0 (glog_ratio's FP32 form)
-  const float2 lx = __fmul2_rn(bc2(P.kappa), make_float2(__logf(r.x), __logf(r.y)));
-  const float2 e7 = __fmul2_rn(lx, bc2(7.0f));
-  const float2 em = __fadd2_rn(make_float2(__expf(e7.x), __expf(e7.y)), bc2(-1.0f));
-  phid = __ffma2_rn(bc2(rl.z), em, __fmul2_rn(bc2(P.cpTmin), lx));
-}
 template <>
 __device__ __forceinline__ void thermo_row<float>(const DevParams<float> &P, const float (&rho)[4],
                                                   const float (&rhoe)[4], const float (&K)[4], float Phi,
                                                   const Lev4<float> &rl, ThermoRow<float> &o) {
   float2 T[2], p[2], h[2], Pi[2], thv[2], thvr[2], phid[2], Tr[2];
-  thermo_pair(P, lo2(rho), lo2(rhoe), lo2(K), Phi, rl, T[0], p[0], h[0], Pi[0], thv[0], thvr[0], phid[0], Tr[0]);
-  thermo_pair(P, hi2(rho), hi2(rhoe), hi2(K), Phi, rl, T[1], p[1], h[1], Pi[1], thv[1], thvr[1], phid[1], Tr[1]);
+  const float2 ph = bc2(Phi), ip0 = bc2(rl.y), rz = bc2(rl.z);
+  thermo_pair(P, lo2(rho), lo2(rhoe), lo2(K), ph, ip0, rz, T[0], p[0], h[0], Pi[0], thv[0], thvr[0], phid[0], Tr[0]);
+  thermo_pair(P, hi2(rho), hi2(rhoe), hi2(K), ph, ip0, rz, T[1], p[1], h[1], Pi[1], thv[1], thvr[1], phid[1], Tr[1]);
   put2(T[0], T[1], o.T); put2(p[0], p[1], o.p); put2(h[0], h[1], o.h); put2(Pi[0], Pi[1], o.Pi);
   put2(thv[0], thv[1], o.thv); put2(thvr[0], thvr[1], o.thvr); put2(phid[0], phid[1], o.phid);
   put2(Tr[0], Tr[1], o.Tr);

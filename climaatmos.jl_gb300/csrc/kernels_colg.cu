@@ -24,6 +24,34 @@ namespace {
 
 constexpr int CG_THREADS = 128;
 
+// H += ce t (all five fields) + ci q (rho, rho e_tot, u_3), level by level; FP32 with two
+// levels per lane: both levels in one packed multiply-add.
+template <class FT, int CM>
+__device__ __forceinline__ void stage_accumulate(FT (&H)[5][CM], const FT (&t)[5][CM], const FT (&q)[3][CM], FT ce,
+                                                 FT ci) {
+#pragma unroll
+  for (int k = 0; k < CM; ++k)
+#pragma unroll
+    for (int c = 0; c < 5; ++c) {
+      H[c][k] += ce * t[c][k];
+      if (ci != FT(0) && c != 1 && c != 2) H[c][k] += ci * q[c == 0 ? 0 : (c == 3 ? 1 : 2)][k];
+    }
+}
+template <>
+__device__ __forceinline__ void stage_accumulate<float, 2>(float (&H)[5][2], const float (&t)[5][2],
+                                                           const float (&q)[3][2], float ce, float ci) {
+#pragma unroll
+  for (int c = 0; c < 5; ++c) {
+    float2 h = __ffma2_rn(bc2(ce), make_float2(t[c][0], t[c][1]), make_float2(H[c][0], H[c][1]));
+    if (ci != 0.0f && c != 1 && c != 2) {
+      const int m = c == 0 ? 0 : (c == 3 ? 1 : 2);
+      h = __ffma2_rn(bc2(ci), make_float2(q[m][0], q[m][1]), h);
+    }
+    H[c][0] = h.x;
+    H[c][1] = h.y;
+  }
+}
+
 template <class FT, int G, int CM, int STG, int MINB>
 __global__ void __launch_bounds__(CG_THREADS, MINB) k_col_stage_g(DevParams<FT> P, StageArgs<FT> A) {
   const int lane = threadIdx.x & 31, gl = lane % G;
@@ -75,14 +103,7 @@ __global__ void __launch_bounds__(CG_THREADS, MINB) k_col_stage_g(DevParams<FT> 
         q[2][k] = okf ? qf[k] : FT(0);
       }
     }
-#pragma unroll
-    for (int k = 0; k < CM; ++k) {
-#pragma unroll
-      for (int c = 0; c < 5; ++c) {
-        H[c][k] += A.ce[j] * t[c][k];
-        if (j >= 1 && c != 1 && c != 2) H[c][k] += A.ci[j] * q[c == 0 ? 0 : (c == 3 ? 1 : 2)][k];
-      }
-    }
+    stage_accumulate<FT, CM>(H, t, q, A.ce[j], j >= 1 ? A.ci[j] : FT(0));
   }
 #pragma unroll
   for (int k = 0; k < CM; ++k) {

@@ -21,6 +21,7 @@
 // intermediates live in a column-major global scratch so that the threads of
 // a warp access consecutive words.
 #include <cstdlib>
+#include <type_traits>
 
 #include "colcore.cuh"
 
@@ -59,7 +60,23 @@ struct ColVjpArgs {
   // e0[j] Yb + ce_j U^bar, Tib_j = i0[j] Yb + ci_j U^bar
   int init;
   FT e0[4], i0[4];
+  // tby: the cotangent of T_imp is tbs times that of u_n as it is on entry (Tb_c, Tb_f
+  // unused): the last stage's implicit tendency enters the final combination with
+  // coefficient dt b_4, so its cotangent is read in place instead of materialised
+  int tby;
+  FT tbs;
 };
+
+// Cotangent of T_imp at level k of row 0 (rho) or 1 (rho e_tot), and at face k; rb, cb
+// and fb are the column's offsets in the two-row, the four-row and the face layouts.
+template <class FT>
+__device__ __forceinline__ FT tb_cen(const ColVjpArgs<FT> &V, size_t rb, size_t cb, size_t sc, int row, int k) {
+  return V.tby ? V.tbs * V.Yb_c[cb + (size_t)(row ? 3 : 0) * sc + k] : V.Tb_c[rb + (size_t)(row ? sc : 0) + k];
+}
+template <class FT>
+__device__ __forceinline__ FT tb_face(const ColVjpArgs<FT> &V, size_t fb, int k) {
+  return V.tby ? V.tbs * V.Yb_f[fb + k] : V.Tb_f[fb + k];
+}
 
 template <class FT>
 __device__ __forceinline__ FT vl_value(FT u, FT am2, FT am1, FT a0, FT ap1, bool near, FT dtm) {
@@ -304,10 +321,10 @@ __global__ void __launch_bounds__(128) k_col_stage_vjp(DevParams<FT> P, ColVjpAr
   CSum<FT> dal;
   // output cotangents: U and T_imp = (U - U^) / dtgamma
   for (int v = 0; v < Nv; ++v) {
-    S(S_BRN, v) = V.Ub_c[cb + v] + V.Tb_c[rb + v] * idtg;
-    S(S_BREN, v) = V.Ub_c[cb + (size_t)3 * sc + v] + V.Tb_c[rb + (size_t)sc + v] * idtg;
+    S(S_BRN, v) = V.Ub_c[cb + v] + tb_cen(V, rb, cb, sc, 0, v) * idtg;
+    S(S_BREN, v) = V.Ub_c[cb + (size_t)3 * sc + v] + tb_cen(V, rb, cb, sc, 1, v) * idtg;
   }
-  for (int f = 0; f < Nf; ++f) S(S_BU3N, f) = V.Ub_f[fb + f] + V.Tb_f[fb + f] * idtg;
+  for (int f = 0; f < Nf; ++f) S(S_BU3N, f) = V.Ub_f[fb + f] + tb_face(V, fb, f) * idtg;
   // (a) van Leer correction: rhoe_out = rhoe_n + dtgamma corr(state_n)
   if (P.upwinding) {
     for (int f = 1; f < Nv; ++f) {
@@ -535,8 +552,8 @@ __global__ void __launch_bounds__(128) k_col_stage_vjp(DevParams<FT> P, ColVjpAr
   }
   // ------------------------------------------------ cotangent of U^ and its distribution
   for (int v = 0; v < Nv; ++v) {
-    const FT hb[4] = {S(S_BR, v) - V.Tb_c[rb + v] * idtg, S(S_BU1, v) + V.Ub_c[cb + (size_t)sc + v],
-                      S(S_BU2, v) + V.Ub_c[cb + (size_t)2 * sc + v], S(S_BRE, v) - V.Tb_c[rb + (size_t)sc + v] * idtg};
+    const FT hb[4] = {S(S_BR, v) - tb_cen(V, rb, cb, sc, 0, v) * idtg, S(S_BU1, v) + V.Ub_c[cb + (size_t)sc + v],
+                      S(S_BU2, v) + V.Ub_c[cb + (size_t)2 * sc + v], S(S_BRE, v) - tb_cen(V, rb, cb, sc, 1, v) * idtg};
     FT y0[4];
     for (int c = 0; c < 4; ++c) {
       y0[c] = V.Yb_c[cb + (size_t)c * sc + v];
@@ -558,7 +575,7 @@ __global__ void __launch_bounds__(128) k_col_stage_vjp(DevParams<FT> P, ColVjpAr
   }
   for (int f = 0; f < Nf; ++f) {
     const bool inner = f > 0 && f < Nv;
-    const FT hb = S(S_BH4, f) + (inner ? S(S_BU3, f) : FT(0)) - V.Tb_f[fb + f] * idtg;
+    const FT hb = S(S_BH4, f) + (inner ? S(S_BU3, f) : FT(0)) - tb_face(V, fb, f) * idtg;
     const FT y0 = V.Yb_f[fb + f];
     V.Yb_f[fb + f] = y0 + hb;
     for (int j = 0; j < A.nsrc; ++j) {
@@ -622,6 +639,41 @@ __device__ __forceinline__ void fold2(FT (&own)[CM], FT toPrev2, FT toPrev1, FT 
   if (gl > 0) { own[0] += c; own[1] += d; }
 }
 
+// thermo_vjp at the lane's CM levels, with the cotangent of h alone (FULL = false) or of
+// (h, Pi, thv, thvr, Phi_r); FP32 with two levels per lane: one packed pair.
+template <bool FULL, class FT, int CM>
+__device__ __forceinline__ void thermo_vjp_lane(const DevParams<FT> &P, const FT (&rho)[CM], const FT (&rhoe)[CM],
+                                                const FT (&K)[CM], const FT (&Phi)[CM], const FT (&bh)[CM],
+                                                const FT (&bPi)[CM], const FT (&bthv)[CM], const FT (&bthvr)[CM],
+                                                const FT (&bphir)[CM], FT (&rb)[CM], FT (&reb)[CM], FT (&Kb)[CM]) {
+  if constexpr (std::is_same<FT, float>::value && CM == 2) {
+    ThermoBar2 tb;
+    tb.T = tb.p = tb.Tr = bc2(0.0f);
+    tb.h = make_float2(bh[0], bh[1]);
+    tb.Pi = FULL ? make_float2(bPi[0], bPi[1]) : bc2(0.0f);
+    tb.thv = FULL ? make_float2(bthv[0], bthv[1]) : bc2(0.0f);
+    tb.thvr = FULL ? make_float2(bthvr[0], bthvr[1]) : bc2(0.0f);
+    tb.phir = FULL ? make_float2(bphir[0], bphir[1]) : bc2(0.0f);
+    float2 r, re, k;
+    thermo_vjp_pair(P, make_float2(rho[0], rho[1]), make_float2(rhoe[0], rhoe[1]), make_float2(K[0], K[1]),
+                    make_float2(Phi[0], Phi[1]), tb, r, re, k);
+    rb[0] = r.x; rb[1] = r.y; reb[0] = re.x; reb[1] = re.y; Kb[0] = k.x; Kb[1] = k.y;
+  } else {
+#pragma unroll
+    for (int k = 0; k < CM; ++k) {
+      ThermoBar<FT> tb{};
+      tb.h = bh[k];
+      if (FULL) {
+        tb.Pi = bPi[k];
+        tb.thv = bthv[k];
+        tb.thvr = bthvr[k];
+        tb.phir = bphir[k];
+      }
+      thermo_vjp(P, rho[k], rhoe[k], K[k], Phi[k], tb, rb[k], reb[k], Kb[k]);
+    }
+  }
+}
+
 // Default register cap: FP32 at 128 registers (four resident 128-thread CTAs per SM), FP64
 // uncapped; the FP32 32-lane, two-levels-per-lane form (z_elem < 64) is launched at six CTAs
 // per SM instead (launch_column_stage_vjp).
@@ -654,8 +706,10 @@ __global__ void __launch_bounds__(128, MINB) k_col_stage_vjp_g(DevParams<FT> P, 
       prefetch_l2(V.Ub_c + cb + (size_t)c * sc);
       prefetch_l2(V.Yb_c + cb + (size_t)c * sc);
     }
-    prefetch_l2(V.Tb_c + rb);
-    prefetch_l2(V.Tb_c + rb + sc);
+    if (!V.tby) {
+      prefetch_l2(V.Tb_c + rb);
+      prefetch_l2(V.Tb_c + rb + sc);
+    }
     for (int j = 0; !V.init && j < A.nsrc; ++j) {  // (init: the tendency cotangents are only written)
       if (V.Teb_c[j])
         for (int c = 0; c < 4; ++c) prefetch_l2(V.Teb_c[j] + cb + (size_t)c * sc);
@@ -667,7 +721,7 @@ __global__ void __launch_bounds__(128, MINB) k_col_stage_vjp_g(DevParams<FT> P, 
   }
   if (r0 < Nf) {
     prefetch_l2(V.Ub_f + fb);
-    prefetch_l2(V.Tb_f + fb);
+    if (!V.tby) prefetch_l2(V.Tb_f + fb);
     prefetch_l2(V.Yb_f + fb);
     for (int j = 0; !V.init && j < A.nsrc; ++j) {
       if (V.Teb_f[j]) prefetch_l2(V.Teb_f[j] + fb);
@@ -728,16 +782,23 @@ __global__ void __launch_bounds__(128, MINB) k_col_stage_vjp_g(DevParams<FT> P, 
   const FT u3p = prv<G, CM>(u3, gl), g33p = prv<G, CM>(g33, gl);
   // centre diagnostics of U0
   FT K[CM], h[CM], Pi[CM], thv[CM], thvr[CM], phid[CM], rJ[CM], iJ[CM], c1[CM], c2[CM], Jc[CM], phi[CM];
+  {
+    FT ub[CM], gb[CM];
+    col::Cen<FT> cc[CM];
 #pragma unroll
-  for (int k = 0; k < CM; ++k) {
-    const int v = r0 + k;
-    const FT ub = k + 1 < CM ? u3[k + 1] : u3n0, gb = k + 1 < CM ? g33[k + 1] : g33n0;
-    const Lev4<FT> Lc = P.lc4[min(v, Nv - 1)];
-    c1[k] = (Gm.gu0 * H[1][k] + Gm.gu1 * H[2][k]) * Lc.z;
-    c2[k] = (Gm.gu1 * H[1][k] + Gm.gu2 * H[2][k]) * Lc.z;
-    const col::Cen<FT> cc = col::cdiag(P, Gm, L, v, H[0][k], H[1][k], H[2][k], H[3][k], u3[k], ub, g33[k], gb);
-    K[k] = cc.K; h[k] = cc.h; Pi[k] = cc.Pi; thv[k] = cc.thv; thvr[k] = cc.thvr; phid[k] = cc.phid;
-    rJ[k] = cc.rJ; iJ[k] = cc.iJ; Jc[k] = Gm.Jh * Lc.x; phi[k] = cc.phi;
+    for (int k = 0; k < CM; ++k) {
+      ub[k] = k + 1 < CM ? u3[k + 1] : u3n0;
+      gb[k] = k + 1 < CM ? g33[k + 1] : g33n0;
+    }
+    col::cdiag_lane<FT, CM>(P, Gm, L, r0, H, u3, ub, g33, gb, cc);
+#pragma unroll
+    for (int k = 0; k < CM; ++k) {
+      const Lev4<FT> Lc = P.lc4[min(r0 + k, Nv - 1)];
+      c1[k] = (Gm.gu0 * H[1][k] + Gm.gu1 * H[2][k]) * Lc.z;
+      c2[k] = (Gm.gu1 * H[1][k] + Gm.gu2 * H[2][k]) * Lc.z;
+      K[k] = cc[k].K; h[k] = cc[k].h; Pi[k] = cc[k].Pi; thv[k] = cc[k].thv; thvr[k] = cc[k].thvr;
+      phid[k] = cc[k].phid; rJ[k] = cc[k].rJ; iJ[k] = cc[k].iJ; Jc[k] = Gm.Jh * Lc.x; phi[k] = cc[k].phi;
+    }
   }
   // previous-level (centre r0 - 1) values
   const FT rJp = prv<G, CM>(rJ, gl), hp = prv<G, CM>(h, gl), Kp = prv<G, CM>(K, gl), Pip = prv<G, CM>(Pi, gl);
@@ -835,9 +896,9 @@ __global__ void __launch_bounds__(128, MINB) k_col_stage_vjp_g(DevParams<FT> P, 
 #pragma unroll
   for (int k = 0; k < CM; ++k) {
     const bool okc = r0 + k < Nv, okf = r0 + k < Nf;
-    bRN[k] = okc ? V.Ub_c[cb + k] + V.Tb_c[rb + k] * idtg : FT(0);
-    bREN[k] = okc ? V.Ub_c[cb + (size_t)3 * sc + k] + V.Tb_c[rb + (size_t)sc + k] * idtg : FT(0);
-    bU3N[k] = okf ? V.Ub_f[fb + k] + V.Tb_f[fb + k] * idtg : FT(0);
+    bRN[k] = okc ? V.Ub_c[cb + k] + tb_cen(V, rb, cb, sc, 0, k) * idtg : FT(0);
+    bREN[k] = okc ? V.Ub_c[cb + (size_t)3 * sc + k] + tb_cen(V, rb, cb, sc, 1, k) * idtg : FT(0);
+    bU3N[k] = okf ? V.Ub_f[fb + k] + tb_face(V, fb, k) * idtg : FT(0);
     bU1[k] = FT(0);
     bU2[k] = FT(0);
   }
@@ -845,15 +906,24 @@ __global__ void __launch_bounds__(128, MINB) k_col_stage_vjp_g(DevParams<FT> P, 
   if (P.upwinding) {
     FT hn[CM], rJn[CM], cn1[CM], cn2[CM], Kn[CM];
     const FT U3Nn = nxt<G, CM>(U3N, gl);
+    {
+      FT Un[5][CM], wn[CM], gb[CM];
+      col::Cen<FT> cc[CM];
 #pragma unroll
-    for (int k = 0; k < CM; ++k) {
-      const FT wn = fnext(U3N, k, U3Nn), gb = fnext(g33, k, g33n0);
-      const col::Cen<FT> cc = col::cdiag(P, Gm, L, r0 + k, RN[k], H[1][k], H[2][k], REN[k], U3N[k], wn, g33[k], gb);
-      hn[k] = cc.h;
-      rJn[k] = cc.rJ;
-      Kn[k] = cc.K;
-      cn1[k] = c1[k];
-      cn2[k] = c2[k];
+      for (int k = 0; k < CM; ++k) {
+        Un[0][k] = RN[k]; Un[1][k] = H[1][k]; Un[2][k] = H[2][k]; Un[3][k] = REN[k]; Un[4][k] = U3N[k];
+        wn[k] = fnext(U3N, k, U3Nn);
+        gb[k] = fnext(g33, k, g33n0);
+      }
+      col::cdiag_lane<FT, CM>(P, Gm, L, r0, Un, U3N, wn, g33, gb, cc);
+#pragma unroll
+      for (int k = 0; k < CM; ++k) {
+        hn[k] = cc[k].h;
+        rJn[k] = cc[k].rJ;
+        Kn[k] = cc[k].K;
+        cn1[k] = c1[k];
+        cn2[k] = c2[k];
+      }
     }
     const FT hnp = prv<G, CM>(hn, gl), hnp2 = prv2<G, CM>(hn, gl), hnn = nxt<G, CM>(hn, gl), hnn2 = nxt2<G, CM>(hn, gl);
     const FT rJnp = prv<G, CM>(rJn, gl);
@@ -895,13 +965,12 @@ __global__ void __launch_bounds__(128, MINB) k_col_stage_vjp_g(DevParams<FT> P, 
     fold2<G, CM>(bHN, accH[0], accH[1], accH[CM + 2], accH[CM + 3], gl);
     fold1<G, CM>(bRJN, accR[0], accR[CM + 1], gl);
     FT toNextU3 = FT(0);
+    FT tvr[CM], tvre[CM], tvK[CM];
+    thermo_vjp_lane<false>(P, RN, REN, Kn, phi, bHN, bHN, bHN, bHN, bHN, tvr, tvre, tvK);
 #pragma unroll
     for (int k = 0; k < CM; ++k) {
       if (r0 + k >= Nv) continue;
-      ThermoBar<FT> tb{};
-      tb.h = bHN[k];
-      FT rb_, reb, Kb;
-      thermo_vjp(P, RN[k], REN[k], Kn[k], phi[k], tb, rb_, reb, Kb);
+      const FT rb_ = tvr[k], reb = tvre[k], Kb = tvK[k];
       bRN[k] += rb_ + Jc[k] * bRJN[k];
       bREN[k] += reb;
       bU1[k] += cn1[k] * Kb;
@@ -1124,17 +1193,12 @@ __global__ void __launch_bounds__(128, MINB) k_col_stage_vjp_g(DevParams<FT> P, 
   // (g) centre diagnostics of U0
   {
     FT toNextU3 = 0;
+    FT tvr[CM], tvre[CM], tvK[CM];
+    thermo_vjp_lane<true>(P, H[0], H[3], K, phi, bH, bPI, bTHV, bTHVR, bPHIR, tvr, tvre, tvK);
 #pragma unroll
     for (int k = 0; k < CM; ++k) {
       if (r0 + k >= Nv) continue;
-      ThermoBar<FT> tb{};
-      tb.h = bH[k];
-      tb.Pi = bPI[k];
-      tb.thv = bTHV[k];
-      tb.thvr = bTHVR[k];
-      tb.phir = bPHIR[k];
-      FT rb_, reb, Kb;
-      thermo_vjp(P, H[0][k], H[3][k], K[k], phi[k], tb, rb_, reb, Kb);
+      const FT rb_ = tvr[k], reb = tvre[k], Kb = tvK[k];
       bR0[k] += rb_ + Jc[k] * bRJ[k];
       bRE0[k] += reb;
       const FT Kt = Kb + bK[k];
@@ -1151,8 +1215,8 @@ __global__ void __launch_bounds__(128, MINB) k_col_stage_vjp_g(DevParams<FT> P, 
   for (int k = 0; k < CM; ++k) {
     const int v = r0 + k;
     if (colv && v < Nv) {
-      const FT hb[4] = {bR0[k] - V.Tb_c[rb + k] * idtg, bU1[k] + V.Ub_c[cb + (size_t)sc + k],
-                        bU2[k] + V.Ub_c[cb + (size_t)2 * sc + k], bRE0[k] - V.Tb_c[rb + (size_t)sc + k] * idtg};
+      const FT hb[4] = {bR0[k] - tb_cen(V, rb, cb, sc, 0, k) * idtg, bU1[k] + V.Ub_c[cb + (size_t)sc + k],
+                        bU2[k] + V.Ub_c[cb + (size_t)2 * sc + k], bRE0[k] - tb_cen(V, rb, cb, sc, 1, k) * idtg};
       FT y0[4];
 #pragma unroll
       for (int c = 0; c < 4; ++c) {
@@ -1179,7 +1243,7 @@ __global__ void __launch_bounds__(128, MINB) k_col_stage_vjp_g(DevParams<FT> P, 
     }
     if (colv && v < Nf) {
       const bool inner = v > 0 && v < Nv;
-      const FT hb = bH4[k] + (inner ? bU3[k] : FT(0)) - V.Tb_f[fb + k] * idtg;
+      const FT hb = bH4[k] + (inner ? bU3[k] : FT(0)) - tb_face(V, fb, k) * idtg;
       const FT y0 = V.Yb_f[fb + k];
       V.Yb_f[fb + k] = y0 + hb;
       for (int j = 0; j < A.nsrc; ++j) {
@@ -1207,9 +1271,13 @@ template <class FT>
 void launch_column_stage_vjp(const DevParams<FT> &P, const StageArgs<FT> &A, const FT *Ub_c, const FT *Ub_f,
                              const FT *Tb_c, const FT *Tb_f, FT *Yb_c, FT *Yb_f, FT *const Teb[4], FT *const Tib[4],
                              size_t NC, size_t NR, FT *scr, double *dalpha, cudaStream_t s, const FT *Uo,
-                             const FT *Tio, const FT *e0, const FT *i0) {
+                             const FT *Tio, const FT *e0, const FT *i0, const FT *tbs) {
   ColVjpArgs<FT> V{};
   V.A = A;
+  if (tbs) {
+    V.tby = 1;
+    V.tbs = *tbs;
+  }
   if (e0 && i0) {
     V.init = 1;
     for (int j = 0; j < 4; ++j) {
@@ -1252,11 +1320,11 @@ template void launch_column_stage_vjp<float>(const DevParams<float> &, const Sta
                                              const float *, const float *, const float *, float *, float *,
                                              float *const[4], float *const[4], size_t, size_t, float *, double *,
                                              cudaStream_t, const float *, const float *, const float *,
-                                             const float *);
+                                             const float *, const float *);
 template void launch_column_stage_vjp<double>(const DevParams<double> &, const StageArgs<double> &, const double *,
                                               const double *, const double *, const double *, double *, double *,
                                               double *const[4], double *const[4], size_t, size_t, double *,
                                               double *, cudaStream_t, const double *, const double *,
-                                              const double *, const double *);
+                                              const double *, const double *, const double *);
 
 }  // namespace gb

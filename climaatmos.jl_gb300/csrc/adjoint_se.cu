@@ -296,7 +296,7 @@ __global__ void __launch_bounds__(AD_THREADS, AdMinBlocks<FT>::value)
     k_passB_vjp(DevParams<FT> P, int nbuf, const FT *__restrict__ Yc, const FT *__restrict__ Yf,
                 const FT *__restrict__ Lc, const FT *__restrict__ Tbc, const FT *__restrict__ Tbf,
                 FT *__restrict__ Ybc, FT *__restrict__ Ybf, FT *__restrict__ Lbc, double *__restrict__ dpar,
-                int accum) {
+                int accum, FT tsc) {
   extern __shared__ __align__(128) unsigned char sm[];
   const int Nv = P.Nv, Nf = P.Nf;
   const BvLayout<FT, GL> Lo(Nv, nbuf);
@@ -496,12 +496,14 @@ __global__ void __launch_bounds__(AD_THREADS, AdMinBlocks<FT>::value)
           // X-cotangents from P3: t_i(v) = (X_i(v) + X_i(v+1)) / (2 rho J(v)) + ..., T_u_i -= t_i
           FT Xb1 = 0, Xb2 = 0;
           if (k >= 1) {
-            Xb1 -= sT[16 * Nv + qa] / (FT(2) * Ra[i]);
-            Xb2 -= sT[32 * Nv + qa] / (FT(2) * Ra[i]);
+            const FT ia = grcp(FT(2) * Ra[i]);
+            Xb1 -= sT[16 * Nv + qa] * ia;
+            Xb2 -= sT[32 * Nv + qa] * ia;
           }
           if (k < Nv) {
-            Xb1 -= sT[16 * Nv + qb] / (FT(2) * Rb[i]);
-            Xb2 -= sT[32 * Nv + qb] / (FT(2) * Rb[i]);
+            const FT ib = grcp(FT(2) * Rb[i]);
+            Xb1 -= sT[16 * Nv + qb] * ib;
+            Xb2 -= sT[32 * Nv + qb] * ib;
           }
           const FT T3b = sTf[n * Nf + k];
           const FT b3b = Jf * (fo2 * Xb1 - fo1 * Xb2);
@@ -572,7 +574,7 @@ __global__ void __launch_bounds__(AD_THREADS, AdMinBlocks<FT>::value)
           ld_row(frow(BF_X2, v + 1), Xb2);
 #pragma unroll
           for (int i = 0; i < 4; ++i) {
-            const FT iRJ = FT(1) / RJv[i];
+            const FT iRJ = grcp(RJv[i]);
             const FT X1s = (Xa1[i] + Xb1[i]) / FT(2), X2s = (Xa2[i] + Xb2[i]) / FT(2);
             RJb[i] = -(X1s * (-Tu1b[i]) + X2s * (-Tu2b[i])) * iRJ * iRJ;
           }
@@ -639,13 +641,13 @@ __global__ void __launch_bounds__(AD_THREADS, AdMinBlocks<FT>::value)
             const FT bl4l = -nu * T3l, bl4u = -nu * T3u;
             FT l4b = FT(0);
             if (v > 0) {
-              const FT wa = RJm[i], wb = RJv[i], ws = wa + wb;
-              const FT l4 = (wa * L4m[i] + wb * L4v[i]) / ws;
+              const FT wa = RJm[i], wb = RJv[i], iws = grcp(wa + wb);
+              const FT l4 = (wa * L4m[i] + wb * L4v[i]) * iws;
               c1b[i] += cc1l[i] / FT(2);
               c2b[i] += cc2l[i] / FT(2);
               Kb[i] += -T3l;
-              l4b += bl4l * wb / ws;
-              RJb[i] += bl4l * (L4v[i] - l4) / ws + rjl[i] / FT(2);
+              l4b += bl4l * wb * iws;
+              RJb[i] += bl4l * (L4v[i] - l4) * iws + rjl[i] / FT(2);
               u1b[i] += cv2l[i];
               u2b[i] -= cv1l[i];
             } else {
@@ -655,13 +657,13 @@ __global__ void __launch_bounds__(AD_THREADS, AdMinBlocks<FT>::value)
               RJb[i] += rjl[i];
             }
             if (v + 1 < Nv) {
-              const FT wa = RJv[i], wb = RJp[i], ws = wa + wb;
-              const FT l4 = (wa * L4v[i] + wb * L4p[i]) / ws;
+              const FT wa = RJv[i], wb = RJp[i], iws = grcp(wa + wb);
+              const FT l4 = (wa * L4v[i] + wb * L4p[i]) * iws;
               c1b[i] += cc1u[i] / FT(2);
               c2b[i] += cc2u[i] / FT(2);
               Kb[i] -= -T3u;
-              l4b += bl4u * wa / ws;
-              RJb[i] += bl4u * (L4v[i] - l4) / ws + rju[i] / FT(2);
+              l4b += bl4u * wa * iws;
+              RJb[i] += bl4u * (L4v[i] - l4) * iws + rju[i] / FT(2);
               u1b[i] -= cv2u[i];
               u2b[i] += cv1u[i];
             } else {
@@ -709,9 +711,9 @@ __global__ void __launch_bounds__(AD_THREADS, AdMinBlocks<FT>::value)
 #pragma unroll
           for (int i = 0; i < 4; ++i) {
             const int q = (NQ * j + i) * Nv + v;
-            lb[16 * Nv + q] = L1b[i];
-            lb[32 * Nv + q] = L2b[i];
-            lb[48 * Nv + q] = L3b[i];
+            lb[16 * Nv + q] = tsc * L1b[i];
+            lb[32 * Nv + q] = tsc * L2b[i];
+            lb[48 * Nv + q] = tsc * L3b[i];
             dl += sL[16 * Nv + q] * L1b[i] + sL[32 * Nv + q] * L2b[i] + sL[48 * Nv + q] * L3b[i] - o3[i] * L4b[i];
           }
           dnu.add(mul_rn(dl, inu));
@@ -743,7 +745,7 @@ __global__ void __launch_bounds__(AD_THREADS, AdMinBlocks<FT>::value)
           FT dl = 0;  // sum Ls . Lsb = sum hd . hdb, hdb = -nu_s T_rhoe
 #pragma unroll
           for (int i = 0; i < 4; ++i) {
-            lb[(NQ * j + i) * Nv + v] = Lsb[i];
+            lb[(NQ * j + i) * Nv + v] = tsc * Lsb[i];
             dl += Ls[i] * Lsb[i];
           }
           dnu.add(mul_rn(dl, inu));
@@ -760,12 +762,17 @@ __global__ void __launch_bounds__(AD_THREADS, AdMinBlocks<FT>::value)
         const int q = (NQ * j + i) * Nv + v;
         rho[i] = sY[q];
         rhoe[i] = sY[48 * Nv + q];
-        Thermo<FT> th;
-        thermo(P, rho[i], rhoe[i], K[i], Phi, P.lr4[v], th);
-        h[i] = th.h;
-        Pi[i] = th.Pi;
-        thp[i] = th.thv - th.thvr;
-        if (HS) pH[i] = th.p;
+      }
+      {
+        ThermoRow<FT> th;
+        thermo_row(P, rho, rhoe, K, Phi, P.lr4[v], th);
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          h[i] = th.h[i];
+          Pi[i] = th.Pi[i];
+          if (HS) pH[i] = th.p[i];
+        }
+        vsub(th.thv, th.thvr, thp);
       }
       FT hb_[4], Pib[4], thpb[4], phirb[4];
       {
@@ -861,6 +868,8 @@ __global__ void __launch_bounds__(AD_THREADS, AdMinBlocks<FT>::value)
         FT kvb[4], gu0[4], gu1[4], gu2[4], s2[4];
         g.gu(gu0, gu1, gu2);
         if (HS) g.row(HG_S2, s2);
+        FT rbv[4], rebv[4], kbv[4];
+        if (!HS) thermo_vjp_row(P, rho, rhoe, K, Phi, hb_, Pib, thpb, phirb, rbv, rebv, kbv);
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
           const int q = (NQ * j + i) * Nv + v;
@@ -890,22 +899,22 @@ __global__ void __launch_bounds__(AD_THREADS, AdMinBlocks<FT>::value)
             u1b[i] -= P.hs_kf * hf * Tu1b;
             u2b[i] -= P.hs_kf * hf * Tu2b;
           }
-          FT rb, reb, kb;
-          thermo_vjp(P, rho[i], rhoe[i], K[i], Phi, tb, rb, reb, kb);
+          FT rb = rbv[i], reb = rebv[i], kb = kbv[i];
+          if (HS) thermo_vjp(P, rho[i], rhoe[i], K[i], Phi, tb, rb, reb, kb);
           const FT Kt = Kb[i] + kb;
           const FT x0 = gu0[i] * s.ir2, x1 = gu1[i] * s.ir2, x2 = gu2[i] * s.ir2;
-          const FT o0 = rhob[i] + rb, o1 = u1b[i] + c1[i] * Kt + x0 * c1b[i] + x1 * c2b[i];
-          const FT o2 = u2b[i] + c2[i] * Kt + x1 * c1b[i] + x2 * c2b[i];
+          const FT o0 = tsc * (rhob[i] + rb), o1 = tsc * (u1b[i] + c1[i] * Kt + x0 * c1b[i] + x1 * c2b[i]);
+          const FT o2 = tsc * (u2b[i] + c2[i] * Kt + x1 * c1b[i] + x2 * c2b[i]), o3 = tsc * reb;
           if (accum) {
             yb[q] += o0;
             yb[16 * Nv + q] += o1;
             yb[32 * Nv + q] += o2;
-            yb[48 * Nv + q] += reb;
+            yb[48 * Nv + q] += o3;
           } else {
             yb[q] = o0;
             yb[16 * Nv + q] = o1;
             yb[32 * Nv + q] = o2;
-            yb[48 * Nv + q] = reb;
+            yb[48 * Nv + q] = o3;
           }
           kvb[i] = Kt / FT(2);
         }
@@ -927,7 +936,7 @@ __global__ void __launch_bounds__(AD_THREADS, AdMinBlocks<FT>::value)
         for (int i = 0; i < 4; ++i) {
           const int idx = (NQ * j + i) * Nf + k;
           const FT u3 = sF[idx];
-          const FT o = U3b[i] + Km[i] * u3 * g33 + Kp[i] * u3 * g33;
+          const FT o = tsc * (U3b[i] + Km[i] * u3 * g33 + Kp[i] * u3 * g33);
           if (accum) fb[idx] += o;
           else fb[idx] = o;
         }
@@ -962,8 +971,8 @@ __global__ void __launch_bounds__(AD_THREADS, AdMinBlocks<FT>::value)
       a += red[w];
       c += red[AD_THREADS / 32 + w];
     }
-    dpar[2 * blockIdx.x] += a;
-    dpar[2 * blockIdx.x + 1] += c;
+    dpar[2 * blockIdx.x] += (double)tsc * a;
+    dpar[2 * blockIdx.x + 1] += (double)tsc * c;
   }
 }
 
@@ -1027,18 +1036,18 @@ void launch_passA_vjp(const DevParams<FT> &P, const FT *Yc, const FT *Yf, const 
 // grid: the number of parameter-partial slots (CTAs) the caller allocated.
 template <class FT>
 void launch_passB_vjp(const DevParams<FT> &P, const FT *Yc, const FT *Yf, const FT *L, const FT *Tbc, const FT *Tbf,
-                      FT *Ybc, FT *Ybf, FT *Lb, double *dpar, int grid, bool accum, cudaStream_t s) {
+                      FT *Ybc, FT *Ybf, FT *Lb, double *dpar, int grid, bool accum, cudaStream_t s, FT tsc) {
   const bool staged = passB_vjp_staged<FT>(P.Nv);
   const AdShape sh = staged ? ad_shape<BvLayout<FT, false>>(P.Nv, AdMinBlocks<FT>::value)
                             : ad_shape<BvLayout<FT, true>>(P.Nv, AdMinBlocks<FT>::value);
   const int g = std::max(1, std::min({grid, P.Nh, ad_dev().nsm * sh.ctas}));
   const int ac = accum ? 1 : 0;
   if (staged) {
-    if (P.hs) k_passB_vjp<FT, true, false><<<g, AD_THREADS, sh.smem, s>>>(P, sh.nbuf, Yc, Yf, L, Tbc, Tbf, Ybc, Ybf, Lb, dpar, ac);
-    else k_passB_vjp<FT, false, false><<<g, AD_THREADS, sh.smem, s>>>(P, sh.nbuf, Yc, Yf, L, Tbc, Tbf, Ybc, Ybf, Lb, dpar, ac);
+    if (P.hs) k_passB_vjp<FT, true, false><<<g, AD_THREADS, sh.smem, s>>>(P, sh.nbuf, Yc, Yf, L, Tbc, Tbf, Ybc, Ybf, Lb, dpar, ac, tsc);
+    else k_passB_vjp<FT, false, false><<<g, AD_THREADS, sh.smem, s>>>(P, sh.nbuf, Yc, Yf, L, Tbc, Tbf, Ybc, Ybf, Lb, dpar, ac, tsc);
   } else {
-    if (P.hs) k_passB_vjp<FT, true, true><<<g, AD_THREADS, sh.smem, s>>>(P, sh.nbuf, Yc, Yf, L, Tbc, Tbf, Ybc, Ybf, Lb, dpar, ac);
-    else k_passB_vjp<FT, false, true><<<g, AD_THREADS, sh.smem, s>>>(P, sh.nbuf, Yc, Yf, L, Tbc, Tbf, Ybc, Ybf, Lb, dpar, ac);
+    if (P.hs) k_passB_vjp<FT, true, true><<<g, AD_THREADS, sh.smem, s>>>(P, sh.nbuf, Yc, Yf, L, Tbc, Tbf, Ybc, Ybf, Lb, dpar, ac, tsc);
+    else k_passB_vjp<FT, false, true><<<g, AD_THREADS, sh.smem, s>>>(P, sh.nbuf, Yc, Yf, L, Tbc, Tbf, Ybc, Ybf, Lb, dpar, ac, tsc);
   }
 }
 
@@ -1050,7 +1059,7 @@ void launch_passB_vjp(const DevParams<FT> &P, const FT *Yc, const FT *Yf, const 
   template void launch_passA_vjp<FT>(const DevParams<FT> &, const FT *, const FT *, const FT *, FT *, FT *, int, \
                                      cudaStream_t, const FT *, const FT *);                                  \
   template void launch_passB_vjp<FT>(const DevParams<FT> &, const FT *, const FT *, const FT *, const FT *,      \
-                                     const FT *, FT *, FT *, FT *, double *, int, bool, cudaStream_t);
+                                     const FT *, FT *, FT *, FT *, double *, int, bool, cudaStream_t, FT);
 INST(float)
 INST(double)
 #undef INST

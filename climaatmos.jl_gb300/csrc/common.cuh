@@ -184,6 +184,48 @@ __device__ __forceinline__ void thermo_vjp(const DevParams<FT> &P, FT rho, FT rh
   K_b = Kb;
 }
 
+// thermo_vjp for two points at once in FP32: the same formulas with packed multiplies and
+// adds, one reciprocal of rho per point in place of the three divisions (the hardware
+// power and reciprocals per point).  Cotangents as float2 pairs.
+struct ThermoBar2 {
+  float2 T, p, h, Pi, thv, thvr, phir, Tr;
+};
+__device__ __forceinline__ void thermo_vjp_pair(const DevParams<float> &P, float2 rho, float2 rhoe, float2 K,
+                                                float2 Phi, const ThermoBar2 &b, float2 &rho_b, float2 &rhoe_b,
+                                                float2 &K_b) {
+  const float2 m1 = bc2(-1.0f);
+  const float2 irho = make_float2(grcp(rho.x), grcp(rho.y));
+  const float2 e = __fmul2_rn(rhoe, irho);
+  const float2 eint = __ffma2_rn(Phi, m1, __ffma2_rn(K, m1, e));
+  const float2 Tu = __ffma2_rn(__fadd2_rn(eint, bc2(P.Rd * P.T0)), bc2(P.icvd), bc2(P.T0));
+  const bool cx = !(Tu.x > P.Tmin_sgs), cy = !(Tu.y > P.Tmin_sgs);
+  const float2 T = make_float2(cx ? P.Tmin_sgs : Tu.x, cy ? P.Tmin_sgs : Tu.y);
+  const float2 p = __fmul2_rn(__fmul2_rn(rho, bc2(P.Rd)), T);
+  const float2 x = __fmul2_rn(p, bc2(P.ipref));
+  const float2 Pi = make_float2(gpow(x.x, P.kappa), gpow(x.y, P.kappa));
+  const float2 Pi2 = __fmul2_rn(Pi, Pi), Pi4 = __fmul2_rn(Pi2, Pi2), Pi7 = __fmul2_rn(__fmul2_rn(Pi4, Pi2), Pi);
+  const float dT = P.Tsfc_ref - P.Tmin_ref;
+  const float2 Tr = __ffma2_rn(bc2(dT), Pi7, bc2(P.Tmin_ref));
+  const float2 iPi = make_float2(grcp(Pi.x), grcp(Pi.y)), iPi2 = __fmul2_rn(iPi, iPi);
+  const float2 s7 = __fmul2_rn(bc2(7.0f * dT), Pi7);
+  // Pib = b.Pi - T iPi^2 b.thv + (7 dT Pi^7 - T_r) iPi^2 b.thvr - cp T_r iPi b.phir + 7 dT Pi^7 iPi b.Tr
+  float2 Pib = __ffma2_rn(__fmul2_rn(__fmul2_rn(T, iPi2), m1), b.thv, b.Pi);
+  Pib = __ffma2_rn(__fmul2_rn(__ffma2_rn(Tr, m1, s7), iPi2), b.thvr, Pib);
+  Pib = __ffma2_rn(__fmul2_rn(__fmul2_rn(bc2(-P.cpd), Tr), iPi), b.phir, Pib);
+  Pib = __ffma2_rn(__fmul2_rn(s7, iPi), b.Tr, Pib);
+  const float2 ip = make_float2(grcp(p.x), grcp(p.y));
+  const float2 pb = __ffma2_rn(__fmul2_rn(bc2(P.kappa), Pi), __fmul2_rn(Pib, ip), b.p);
+  float2 Tb = __ffma2_rn(iPi, b.thv, b.T);
+  Tb = __ffma2_rn(bc2(P.Rd), b.h, Tb);
+  Tb = __ffma2_rn(__fmul2_rn(rho, bc2(P.Rd)), pb, Tb);
+  const float2 ti = __fmul2_rn(Tb, bc2(P.icvd));
+  const float2 tic = make_float2(cx ? 0.0f : ti.x, cy ? 0.0f : ti.y);
+  const float2 eb = __fadd2_rn(b.h, tic);
+  K_b = __fmul2_rn(tic, m1);
+  rhoe_b = __fmul2_rn(eb, irho);
+  rho_b = __ffma2_rn(__fmul2_rn(rhoe_b, m1), e, __fmul2_rn(__fmul2_rn(bc2(P.Rd), T), pb));
+}
+
 // The hyperdiffused dry static energy less its reference value,
 // s_d - s_d,r = cp_d (T - T_0) + Phi - (cp_d (T_r - T_0) + Phi_r) = cp_d (T - T_r) + phid
 // (TD.dry_static_energy and sd_r, hyperdiffusion.jl:142-147, refstate_thermodynamics.jl).

@@ -674,17 +674,19 @@ void record_step(gb_ctx *ctx, FT *Yc, FT *Yf, double dt_, typename Impl<FT>::Rec
 // Tb is then DSS-transposed in place) or of the tendency as
 // gb_remaining_tendency returns it (not DSSed; Tb is only read).  accum adds
 // to Ub, else Ub is overwritten.  With Yc_add: Yc_add (+)= (dT/dU)^T Tb instead,
-// Ub being scratch (pass B^T writes it, pass A^T adds it and its own part).
+// Ub being scratch (pass B^T writes it, pass A^T adds it and its own part).  The
+// cotangent is tsc Tb (pass B^T scales its outputs).
 template <class FT>
 void tendency_vjp(gb_ctx *ctx, const FT *Uc, const FT *Uf, const FT *L, FT *Tb_c, FT *Tb_f, FT *Ubc, FT *Ubf,
-                  bool dss_out, bool accum, cudaStream_t s, FT *Yc_add = nullptr, FT *Yf_add = nullptr) {
+                  bool dss_out, bool accum, cudaStream_t s, FT *Yc_add = nullptr, FT *Yf_add = nullptr,
+                  FT tsc = FT(1)) {
   Impl<FT> *I = impl<FT>(ctx);
   auto &A = *I->adj;
   const DevParams<FT> &P = I->P;
   FT *Lb = (FT *)A.Lb.p;
   if (dss_out) launch_dss_transpose<FT>(P, Tb_c, Tb_f, s);
   if (Yc_add && passA_vjp_add_fits<FT>(P.Nv)) {
-    launch_passB_vjp<FT>(P, Uc, Uf, L, Tb_c, Tb_f, Ubc, Ubf, Lb, (double *)A.dparB.p, A.grid, false, s);
+    launch_passB_vjp<FT>(P, Uc, Uf, L, Tb_c, Tb_f, Ubc, Ubf, Lb, (double *)A.dparB.p, A.grid, false, s, tsc);
     launch_dss_transpose<FT>(P, Lb, nullptr, s);
     launch_passA_vjp<FT>(P, Uc, Uf, Lb, Yc_add, Yf_add, A.grid, s, Ubc, Ubf);
     return;
@@ -694,7 +696,7 @@ void tendency_vjp(gb_ctx *ctx, const FT *Uc, const FT *Uf, const FT *L, FT *Tb_c
     Ubf = Yf_add;
     accum = true;
   }
-  launch_passB_vjp<FT>(P, Uc, Uf, L, Tb_c, Tb_f, Ubc, Ubf, Lb, (double *)A.dparB.p, A.grid, accum, s);
+  launch_passB_vjp<FT>(P, Uc, Uf, L, Tb_c, Tb_f, Ubc, Ubf, Lb, (double *)A.dparB.p, A.grid, accum, s, tsc);
   launch_dss_transpose<FT>(P, Lb, nullptr, s);
   launch_passA_vjp<FT>(P, Uc, Uf, Lb, Ubc, Ubf, A.grid, s);
 }
@@ -734,10 +736,17 @@ void reverse_step(gb_ctx *ctx, typename Impl<FT>::Record &rec, double dt_, FT *Y
     i0[j] = F.ci[j];
   }
   // the step's own final DSS (the combination folded into the last pass B, then
-  // DSSed as a whole): its transpose first; the transposed DSS of the last
-  // tendency that follows leaves the result unchanged (the DSS is a projection)
-  if (I->stiffly_accurate) launch_dss_transpose<FT>(P, Ybc, Ybf, s);
-  launch_final_transpose<FT>(P, F, Ybc, Ybf, s);
+  // DSSed as a whole): its transpose first, then that of the impenetrability filter.
+  // The last stage's tendency cotangents, dt b~_4 Ybar and dt b_4 Ybar, are then not
+  // materialised: its pullbacks read Ybar in place with those factors, and they need no
+  // second transposed DSS (the DSS is a projection).
+  const bool fold = I->stiffly_accurate;
+  if (fold) {
+    launch_dss_transpose<FT>(P, Ybc, Ybf, s);
+    launch_bc_filter<FT>(P, Ybf, s);
+  } else {
+    launch_final_transpose<FT>(P, F, Ybc, Ybf, s);
+  }
   const FT *Yc = (const FT *)rec.Y.p, *Yf = Yc + I->NC;
   FT *Ubc = (FT *)A.Ub.p, *Ubf = Ubc + I->NC;
   for (int i = 3; i >= 0; --i) {
@@ -747,14 +756,17 @@ void reverse_step(gb_ctx *ctx, typename Impl<FT>::Record &rec, double dt_, FT *Y
       tendency_vjp<FT>(ctx, Uc, Uf, (const FT *)rec.L[i].p, Teb[i], Teb[i] + I->NC, Ubc, Ubf, true, false, s, Ybc,
                        Ybf);
     } else {
-      // the last tendency's cotangent (dt b_4 times the already transposed-DSSed Ybar)
-      // needs no second transposed DSS when the step ends with a DSS of the whole sum
-      const bool dss_out = !(i == 3 && I->stiffly_accurate);
-      tendency_vjp<FT>(ctx, Uc, Uf, (const FT *)rec.L[i].p, Teb[i], Teb[i] + I->NC, Ubc, Ubf, dss_out, false, s);
+      const bool last = i == 3 && fold;
+      if (last)
+        tendency_vjp<FT>(ctx, Uc, Uf, (const FT *)rec.L[i].p, Ybc, Ybf, Ubc, Ubf, false, false, s, nullptr, nullptr,
+                         F.ce[3]);
+      else
+        tendency_vjp<FT>(ctx, Uc, Uf, (const FT *)rec.L[i].p, Teb[i], Teb[i] + I->NC, Ubc, Ubf, true, false, s);
       const StageArgs<FT> SA = stage_args<FT>(I, i, dt, Yc, Yf, Te, Ti);
       launch_column_stage_vjp<FT>(P, SA, Ubc, Ubf, Tib[i], Tib[i] + I->NR, Ybc, Ybf, Teb, Tib, I->NC, I->NR,
                                   (FT *)A.scr.p, (double *)A.dal.p, s, (const FT *)rec.U[i].p,
-                                  (const FT *)rec.Ti[i].p, i == 3 ? e0 : nullptr, i == 3 ? i0 : nullptr);
+                                  (const FT *)rec.Ti[i].p, i == 3 ? e0 : nullptr, i == 3 ? i0 : nullptr,
+                                  last ? &F.ci[3] : nullptr);
     }
   }
 }

@@ -122,12 +122,15 @@ template <class FT> size_t passA_vjp_smem(int Nv);
 template <class FT> size_t passB_vjp_smem(int Nv);
 template <class FT> void configure_adjoint_se(int Nv);
 template <class FT> void launch_passA_vjp(const DevParams<FT> &P, const FT *Yc, const FT *Yf, const FT *Lb, FT *Ybc, FT *Ybf, int grid, cudaStream_t s, const FT *Xbc = nullptr, const FT *Xbf = nullptr);
-template <class FT> void launch_passB_vjp(const DevParams<FT> &P, const FT *Yc, const FT *Yf, const FT *L, const FT *Tbc, const FT *Tbf, FT *Ybc, FT *Ybf, FT *Lb, double *dpar, int grid, bool accum, cudaStream_t s);
+// tsc scales the tendency cotangent: the result is that of tsc * (Tbc, Tbf), formed by
+// scaling the outputs (the pullback is linear in the cotangent).
+template <class FT> void launch_passB_vjp(const DevParams<FT> &P, const FT *Yc, const FT *Yf, const FT *L, const FT *Tbc, const FT *Tbf, FT *Ybc, FT *Ybf, FT *Lb, double *dpar, int grid, bool accum, cudaStream_t s, FT tsc = FT(1));
 size_t col_vjp_scratch_words(int Nh, int Nv);
 // Uo, Tio (optional): the recorded stage output and implicit tendency (U^ = U - dtgamma T_imp
 // then replaces the stage assembly in the forward recompute).  e0, i0 (optional): the
 // tendency cotangents are written, initialised as e0[j] Yb / i0[j] Yb from Yb on entry.
-template <class FT> void launch_column_stage_vjp(const DevParams<FT> &P, const StageArgs<FT> &A, const FT *Ub_c, const FT *Ub_f, const FT *Tb_c, const FT *Tb_f, FT *Yb_c, FT *Yb_f, FT *const Teb[4], FT *const Tib[4], size_t NC, size_t NR, FT *scr, double *dalpha, cudaStream_t s, const FT *Uo = nullptr, const FT *Tio = nullptr, const FT *e0 = nullptr, const FT *i0 = nullptr);
+// tbs: when given, the cotangent of T_imp is *tbs times Yb on entry (Tb_c, Tb_f unused).
+template <class FT> void launch_column_stage_vjp(const DevParams<FT> &P, const StageArgs<FT> &A, const FT *Ub_c, const FT *Ub_f, const FT *Tb_c, const FT *Tb_f, FT *Yb_c, FT *Yb_f, FT *const Teb[4], FT *const Tib[4], size_t NC, size_t NR, FT *scr, double *dalpha, cudaStream_t s, const FT *Uo = nullptr, const FT *Tio = nullptr, const FT *e0 = nullptr, const FT *i0 = nullptr, const FT *tbs = nullptr);
 template <class FT> void launch_bc_filter(const DevParams<FT> &P, FT *Yf, cudaStream_t s);
 // Failure-detection self-test: one warp waits on an mbarrier whose transfer is announced but
 // never issued, so the bounded wait gives up after limit_ns and sets ST_TIMEOUT in *status.

@@ -113,6 +113,49 @@ __device__ __forceinline__ void thermo_row<float>(const DevParams<float> &P, con
   put2(Tr[0], Tr[1], o.Tr);
 }
 
+// thermo_vjp for the 4 nodes of a row with the cotangents of (h, Pi, thv - thvr, Phi_r):
+// FP64 per node, FP32 two nodes at a time (thermo_vjp_pair).
+template <class FT>
+__device__ __forceinline__ void thermo_vjp_row(const DevParams<FT> &P, const FT (&rho)[4], const FT (&rhoe)[4],
+                                               const FT (&K)[4], FT Phi, const FT (&hb)[4], const FT (&Pib)[4],
+                                               const FT (&thpb)[4], const FT (&phirb)[4], FT (&rb)[4],
+                                               FT (&reb)[4], FT (&kb)[4]) {
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    ThermoBar<FT> tb{};
+    tb.h = hb[i];
+    tb.Pi = Pib[i];
+    tb.thv = thpb[i];
+    tb.thvr = -thpb[i];
+    tb.phir = phirb[i];
+    thermo_vjp(P, rho[i], rhoe[i], K[i], Phi, tb, rb[i], reb[i], kb[i]);
+  }
+}
+template <>
+__device__ __forceinline__ void thermo_vjp_row<float>(const DevParams<float> &P, const float (&rho)[4],
+                                                      const float (&rhoe)[4], const float (&K)[4], float Phi,
+                                                      const float (&hb)[4], const float (&Pib)[4],
+                                                      const float (&thpb)[4], const float (&phirb)[4],
+                                                      float (&rb)[4], float (&reb)[4], float (&kb)[4]) {
+  float2 r[2], re[2], k[2];
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    const int i = 2 * h;
+    ThermoBar2 tb;
+    tb.T = tb.p = tb.Tr = bc2(0.0f);
+    tb.h = make_float2(hb[i], hb[i + 1]);
+    tb.Pi = make_float2(Pib[i], Pib[i + 1]);
+    tb.thv = make_float2(thpb[i], thpb[i + 1]);
+    tb.thvr = make_float2(-thpb[i], -thpb[i + 1]);
+    tb.phir = make_float2(phirb[i], phirb[i + 1]);
+    thermo_vjp_pair(P, make_float2(rho[i], rho[i + 1]), make_float2(rhoe[i], rhoe[i + 1]),
+                    make_float2(K[i], K[i + 1]), bc2(Phi), tb, r[h], re[h], k[h]);
+  }
+  put2(r[0], r[1], rb);
+  put2(re[0], re[1], reb);
+  put2(k[0], k[1], kb);
+}
+
 // Row helper: the thread's row j and its xi^2 derivative coefficients.
 template <class FT>
 struct Row {
@@ -448,23 +491,23 @@ template <class FT, class G>
 __device__ __forceinline__ void vec_lap_t(const DevParams<FT> &P, const Row<FT> &R, const G &g,
                                           const LevRow<FT> &s, const FT (&ob1)[4], const FT (&ob2)[4],
                                           const FT (&ob3)[4], FT fdiv, FT (&cb1)[4], FT (&cb2)[4], FT (&cb3)[4]) {
+  // element-wise steps in the packed helpers; the metric scales (r^2, r^-2, G33) are folded
+  // into the per-node weights of the contractions, as in vec_lap
   FT f1b[4], f2b[4], f3b[4], f4b[4], w1b[4], w2b[4];
   {
-    FT gd0[4], gd1[4], gd2[4], iW[4];
+    FT gd0[4], gd1[4], gd2[4], iW[4], wq[4];
     g.gd(gd0, gd1, gd2);
     g.iw(iW);
-#pragma unroll
-    for (int i = 0; i < 4; ++i) {
-      const FT x0 = gd0[i] * s.r2, x1 = gd1[i] * s.r2, x2 = gd2[i] * s.r2;
-      const FT q1b = -(x0 * ob1[i] + x1 * ob2[i]), q2b = -(x1 * ob1[i] + x2 * ob2[i]);
-      const FT q3b = -s.G33 * ob3[i];
-      w1b[i] = -fdiv * iW[i] * ob1[i];
-      w2b[i] = -fdiv * iW[i] * ob2[i];
-      f1b[i] = -q3b * s.iWJ[i];
-      f2b[i] = q3b * s.iWJ[i];
-      f3b[i] = -q1b * s.iWJ[i];
-      f4b[i] = q2b * s.iWJ[i];
-    }
+    vmuls(s.iWJ, s.r2, wq);
+    vcontract(gd0, gd1, ob1, ob2, wq, f3b);   // -q1b iWJ, q1b = -r^2 (g_11 ob1 + g_12 ob2)
+    vmuls(wq, FT(-1), wq);
+    vcontract(gd1, gd2, ob1, ob2, wq, f4b);   // q2b iWJ
+    vmuls(s.iWJ, s.G33, wq);
+    vmul(ob3, wq, f1b);                       // -q3b iWJ, q3b = -G33 ob3
+    vmuls(f1b, FT(-1), f2b);
+    vmuls(iW, -fdiv, wq);
+    vmul(wq, ob1, w1b);
+    vmul(wq, ob2, w2b);
   }
   FT Wz1b[4], Wz2b[4], Wz3b[4], tmp[4];
   d1(P, f1b, Wz2b);
@@ -473,21 +516,18 @@ __device__ __forceinline__ void vec_lap_t(const DevParams<FT> &P, const Row<FT> 
   d1(P, f4b, tmp);
   FT e1b[4], e2b[4], e3b[4], e4b[4];
   {
-    FT gd0[4], gd1[4], gd2[4], W[4];
+    FT gd0[4], gd1[4], gd2[4], W[4], WiJ[4], wk[4];
     g.gd(gd0, gd1, gd2);
     g.w(W);
-#pragma unroll
-    for (int i = 0; i < 4; ++i) {
-      Wz3b[i] += tmp[i];
-      const FT x0 = gd0[i] * s.r2, x1 = gd1[i] * s.r2, x2 = gd2[i] * s.r2;
-      const FT k1b = W[i] * (x0 * Wz1b[i] + x1 * Wz2b[i]);
-      const FT k2b = W[i] * (x1 * Wz1b[i] + x2 * Wz2b[i]);
-      const FT k3b = W[i] * (s.G33 * Wz3b[i]);
-      e1b[i] = k3b * s.iJ[i];
-      e2b[i] = -k3b * s.iJ[i];
-      e3b[i] = k1b * s.iJ[i];
-      e4b[i] = -k2b * s.iJ[i];
-    }
+    vadd(Wz3b, tmp, Wz3b);
+    vmul(W, s.iJ, WiJ);
+    vmuls(WiJ, s.r2, wk);
+    vcontract(gd0, gd1, Wz1b, Wz2b, wk, e3b);  // k1b / J, k1b = W r^2 (g_11 Wz1b + g_12 Wz2b)
+    vmuls(wk, FT(-1), wk);
+    vcontract(gd1, gd2, Wz1b, Wz2b, wk, e4b);  // -k2b / J
+    vmuls(WiJ, s.G33, wk);
+    vmul(Wz3b, wk, e1b);                       // k3b / J, k3b = W G33 Wz3b
+    vmuls(e1b, FT(-1), e2b);
   }
   t1(P, e1b, cb2);
   t2(R, e2b, cb1);
@@ -500,24 +540,22 @@ __device__ __forceinline__ void vec_lap_t(const DevParams<FT> &P, const Row<FT> 
   {
     FT W[4];
     g.w(W);
-#pragma unroll
-    for (int i = 0; i < 4; ++i) {
-      cb3[i] += tmp[i];
-      dab[i] = W[i] * s.iJ[i] * (wdvb[i] + t2b[i]);
-    }
+    vadd(cb3, tmp, cb3);
+    vadd(wdvb, t2b, dab);
+    vmul(dab, s.iJ, dab);
+    vmul(W, dab, dab);
   }
   FT ab[4], bb[4];
   t1(P, dab, ab);
   t2(R, dab, bb);
   {
-    FT gu0[4], gu1[4], gu2[4];
+    FT gu0[4], gu1[4], gu2[4], Jr[4], t[4];
     g.gu(gu0, gu1, gu2);
-#pragma unroll
-    for (int i = 0; i < 4; ++i) {
-      const FT x0 = gu0[i] * s.ir2, x1 = gu1[i] * s.ir2, x2 = gu2[i] * s.ir2;
-      cb1[i] += s.J[i] * (x0 * ab[i] + x1 * bb[i]);
-      cb2[i] += s.J[i] * (x1 * ab[i] + x2 * bb[i]);
-    }
+    vmuls(s.J, s.ir2, Jr);
+    vcontract(gu0, gu1, ab, bb, Jr, t);
+    vadd(cb1, t, cb1);
+    vcontract(gu1, gu2, ab, bb, Jr, t);
+    vadd(cb2, t, cb2);
   }
 }
 
@@ -526,15 +564,12 @@ template <class FT>
 __device__ __forceinline__ void wdiv_t(const DevParams<FT> &P, const Row<FT> &R, const LevRow<FT> &s,
                                        const FT (&ob)[4], FT (&Fb1)[4], FT (&Fb2)[4]) {
   FT tb[4];
-#pragma unroll
-  for (int i = 0; i < 4; ++i) tb[i] = -ob[i] * s.iWJ[i];
+  vmul(ob, s.iWJ, tb);
+  vmuls(tb, FT(-1), tb);
   d1(P, tb, Fb1);
   d2(R, tb, Fb2);
-#pragma unroll
-  for (int i = 0; i < 4; ++i) {
-    Fb1[i] *= s.WJ[i];
-    Fb2[i] *= s.WJ[i];
-  }
+  vmul(Fb1, s.WJ, Fb1);
+  vmul(Fb2, s.WJ, Fb2);
 }
 
 // Transpose of the gradient (d1 f, d2 f): fb = t1(gb1) + t2(gb2).
@@ -544,8 +579,7 @@ __device__ __forceinline__ void grad_t(const DevParams<FT> &P, const Row<FT> &R,
   FT a[4];
   t1(P, gb1, fb);
   t2(R, gb2, a);
-#pragma unroll
-  for (int i = 0; i < 4; ++i) fb[i] += a[i];
+  vadd(fb, a, fb);
 }
 
 // Transpose of the scalar Laplacian Ls = wdiv(g^-1 grad sd) (with the row's g^ij / r^2).
@@ -555,14 +589,12 @@ __device__ __forceinline__ void lap_t(const DevParams<FT> &P, const Row<FT> &R, 
   FT xb1[4], xb2[4], gb1[4], gb2[4];
   wdiv_t(P, R, s, Lb, xb1, xb2);
   {
-    FT gu0[4], gu1[4], gu2[4];
+    FT gu0[4], gu1[4], gu2[4], w[4];
     g.gu(gu0, gu1, gu2);
 #pragma unroll
-    for (int i = 0; i < 4; ++i) {
-      const FT x0 = gu0[i] * s.ir2, x1 = gu1[i] * s.ir2, x2 = gu2[i] * s.ir2;
-      gb1[i] = x0 * xb1[i] + x1 * xb2[i];
-      gb2[i] = x1 * xb1[i] + x2 * xb2[i];
-    }
+    for (int i = 0; i < 4; ++i) w[i] = s.ir2;
+    vcontract(gu0, gu1, xb1, xb2, w, gb1);
+    vcontract(gu1, gu2, xb1, xb2, w, gb2);
   }
   grad_t(P, R, gb1, gb2, sdb);
 }

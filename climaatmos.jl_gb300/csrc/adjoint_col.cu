@@ -1211,49 +1211,75 @@ __global__ void __launch_bounds__(128, MINB) k_col_stage_vjp_g(DevParams<FT> P, 
     fold1<G, CM>(bU3, FT(0), toNextU3, gl);
   }
   // ---------------------------------------------------------------- cotangent of U^ and its distribution
+  // Per level, every load (the cotangents of u_n, U and T_imp and, when accumulating, those
+  // of the earlier stages' tendencies) is issued before the first store: the stores may
+  // alias later loads as far as the compiler knows, so interleaved they would serialise one
+  // memory round trip per tendency.
 #pragma unroll
   for (int k = 0; k < CM; ++k) {
     const int v = r0 + k;
-    if (colv && v < Nv) {
-      const FT hb[4] = {bR0[k] - tb_cen(V, rb, cb, sc, 0, k) * idtg, bU1[k] + V.Ub_c[cb + (size_t)sc + k],
-                        bU2[k] + V.Ub_c[cb + (size_t)2 * sc + k], bRE0[k] - tb_cen(V, rb, cb, sc, 1, k) * idtg};
-      FT y0[4];
+    const bool cen = colv && v < Nv, fac = colv && v < Nf, acc = !V.init;
+    FT y0[4] = {0, 0, 0, 0}, ub1 = 0, ub2 = 0, t0 = 0, t1 = 0, te[4][4], ti[4][2];
+    FT yf = 0, tf = 0, tef[4], tif[4];
 #pragma unroll
-      for (int c = 0; c < 4; ++c) {
-        y0[c] = V.Yb_c[cb + (size_t)c * sc + k];
-        V.Yb_c[cb + (size_t)c * sc + k] = y0[c] + hb[c];
-      }
-      for (int j = 0; j < A.nsrc; ++j) {
-        if (V.init) {
+    for (int j = 0; j < 4; ++j) {
+      tef[j] = tif[j] = ti[j][0] = ti[j][1] = FT(0);
 #pragma unroll
-          for (int c = 0; c < 4; ++c) V.Teb_c[j][cb + (size_t)c * sc + k] = V.e0[j] * y0[c] + A.ce[j] * hb[c];
-          if (j >= 1) {
-            V.Tib_c[j][rb + k] = V.i0[j] * y0[0] + A.ci[j] * hb[0];
-            V.Tib_c[j][rb + (size_t)sc + k] = V.i0[j] * y0[3] + A.ci[j] * hb[3];
-          }
-        } else {
+      for (int c = 0; c < 4; ++c) te[j][c] = FT(0);
+    }
+    if (cen) {
 #pragma unroll
-          for (int c = 0; c < 4; ++c) V.Teb_c[j][cb + (size_t)c * sc + k] += A.ce[j] * hb[c];
-          if (j >= 1) {
-            V.Tib_c[j][rb + k] += A.ci[j] * hb[0];
-            V.Tib_c[j][rb + (size_t)sc + k] += A.ci[j] * hb[3];
-          }
+      for (int c = 0; c < 4; ++c) y0[c] = V.Yb_c[cb + (size_t)c * sc + k];
+      ub1 = V.Ub_c[cb + (size_t)sc + k];
+      ub2 = V.Ub_c[cb + (size_t)2 * sc + k];
+      t0 = tb_cen(V, rb, cb, sc, 0, k);
+      t1 = tb_cen(V, rb, cb, sc, 1, k);
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        if (!acc || j >= A.nsrc) continue;
+#pragma unroll
+        for (int c = 0; c < 4; ++c) te[j][c] = V.Teb_c[j][cb + (size_t)c * sc + k];
+        if (j >= 1) {
+          ti[j][0] = V.Tib_c[j][rb + k];
+          ti[j][1] = V.Tib_c[j][rb + (size_t)sc + k];
         }
       }
     }
-    if (colv && v < Nf) {
-      const bool inner = v > 0 && v < Nv;
-      const FT hb = bH4[k] + (inner ? bU3[k] : FT(0)) - tb_face(V, fb, k) * idtg;
-      const FT y0 = V.Yb_f[fb + k];
-      V.Yb_f[fb + k] = y0 + hb;
-      for (int j = 0; j < A.nsrc; ++j) {
-        if (V.init) {
-          V.Teb_f[j][fb + k] = V.e0[j] * y0 + A.ce[j] * hb;
-          if (j >= 1) V.Tib_f[j][fb + k] = V.i0[j] * y0 + A.ci[j] * hb;
-        } else {
-          V.Teb_f[j][fb + k] += A.ce[j] * hb;
-          if (j >= 1) V.Tib_f[j][fb + k] += A.ci[j] * hb;
+    if (fac) {
+      yf = V.Yb_f[fb + k];
+      tf = tb_face(V, fb, k);
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        if (!acc || j >= A.nsrc) continue;
+        tef[j] = V.Teb_f[j][fb + k];
+        if (j >= 1) tif[j] = V.Tib_f[j][fb + k];
+      }
+    }
+    if (cen) {
+      const FT hb[4] = {bR0[k] - t0 * idtg, bU1[k] + ub1, bU2[k] + ub2, bRE0[k] - t1 * idtg};
+#pragma unroll
+      for (int c = 0; c < 4; ++c) V.Yb_c[cb + (size_t)c * sc + k] = y0[c] + hb[c];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        if (j >= A.nsrc) continue;
+        const FT ke = acc ? FT(1) : V.e0[j], ki = acc ? FT(1) : V.i0[j];
+#pragma unroll
+        for (int c = 0; c < 4; ++c) V.Teb_c[j][cb + (size_t)c * sc + k] = (acc ? te[j][c] : ke * y0[c]) + A.ce[j] * hb[c];
+        if (j >= 1) {
+          V.Tib_c[j][rb + k] = (acc ? ti[j][0] : ki * y0[0]) + A.ci[j] * hb[0];
+          V.Tib_c[j][rb + (size_t)sc + k] = (acc ? ti[j][1] : ki * y0[3]) + A.ci[j] * hb[3];
         }
+      }
+    }
+    if (fac) {
+      const bool inner = v > 0 && v < Nv;
+      const FT hb = bH4[k] + (inner ? bU3[k] : FT(0)) - tf * idtg;
+      V.Yb_f[fb + k] = yf + hb;
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        if (j >= A.nsrc) continue;
+        V.Teb_f[j][fb + k] = (acc ? tef[j] : V.e0[j] * yf) + A.ce[j] * hb;
+        if (j >= 1) V.Tib_f[j][fb + k] = (acc ? tif[j] : V.i0[j] * yf) + A.ci[j] * hb;
       }
     }
   }

@@ -239,13 +239,44 @@ __global__ void k_accum(const double *__restrict__ part, int n, int stride, int 
   }
 }
 
-// acc[0] += the sum of n RSlot<FT> entries (fixed order; one block of 256 threads).
+// acc[0] += the sum of n RSlot<FT> entries, in a fixed order: one block of ACC_THREADS
+// threads, each with four independent compensated sums fed four loads at a time (the
+// loads of one thread are in flight together), then the lanes and the warps in order.
+constexpr int ACC_THREADS = 1024;
 template <class FT>
-__global__ void __launch_bounds__(256) k_accum_slots(const double *__restrict__ part, int n, double *__restrict__ acc) {
-  CSum<FT> s[3];
-  for (int i = threadIdx.x; i < n; i += blockDim.x) s[0].add(RSlot<FT>::load(&part[i]));
-  block_sum3<FT>(s);
-  if (threadIdx.x == 0) acc[0] += s[0].value();
+__global__ void __launch_bounds__(ACC_THREADS) k_accum_slots(const double *__restrict__ part, int n,
+                                                             double *__restrict__ acc) {
+  __shared__ FT sh[2][ACC_THREADS / 32];
+  CSum<FT> s[4];
+  int i = threadIdx.x;
+  for (; i + 3 * ACC_THREADS < n; i += 4 * ACC_THREADS) {
+    CSum<FT> x[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) x[u] = RSlot<FT>::load(&part[i + u * ACC_THREADS]);
+#pragma unroll
+    for (int u = 0; u < 4; ++u) s[u].add(x[u]);
+  }
+  for (; i < n; i += ACC_THREADS) s[0].add(RSlot<FT>::load(&part[i]));
+  s[0].add(s[1]);
+  s[2].add(s[3]);
+  s[0].add(s[2]);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s[0].add(s[0].xor_shfl(o, 32));
+  if ((threadIdx.x & 31) == 0) {
+    sh[0][threadIdx.x >> 5] = s[0].hi;
+    sh[1][threadIdx.x >> 5] = s[0].lo;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    CSum<FT> t;
+    for (int w = 0; w < ACC_THREADS / 32; ++w) {
+      CSum<FT> a;
+      a.hi = sh[0][w];
+      a.lo = sh[1][w];
+      t.add(a);
+    }
+    acc[0] += t.value();
+  }
 }
 
 template <class FT>
@@ -361,7 +392,7 @@ void launch_final_transpose(const DevParams<FT> &P, const CotArgs<FT> &A, FT *Yb
 }
 template <class FT>
 void launch_accum_slots(const double *part, int n, double *acc, cudaStream_t s) {
-  k_accum_slots<FT><<<1, 256, 0, s>>>(part, n, acc);
+  k_accum_slots<FT><<<1, ACC_THREADS, 0, s>>>(part, n, acc);
 }
 void launch_accum(const double *part, int n, int stride, int nout, double *acc, cudaStream_t s) {
   k_accum<<<1, 256, 0, s>>>(part, n, stride, nout, acc);

@@ -682,7 +682,12 @@ struct VjpMinBlocks {
   static constexpr int value = sizeof(FT) == 4 ? 4 : 1;
 };
 
-template <class FT, int G, int CM, int MINB = VjpMinBlocks<FT>::value>
+// REC: the stage's recorded output U and implicit tendency T_imp are given (V.Uo_c, V.Tio_c):
+// the stage input is U - dtgamma T_imp and the Newton update at the inner faces is
+// x = U^ - U = -dtgamma T_imp (the update of u_3 is all the stage does to it), so the forward
+// tridiagonal solve is not repeated: the boundary rows of the Schur system are diagonal,
+// and rho, rho e_tot after the update follow from x by the back-substitution formulas.
+template <class FT, int G, int CM, int MINB = VjpMinBlocks<FT>::value, bool REC = false>
 __global__ void __launch_bounds__(128, MINB) k_col_stage_vjp_g(DevParams<FT> P, ColVjpArgs<FT> V) {
   const int lane = threadIdx.x & 31, gl = lane % G;
   const int col0 = (blockIdx.x * 4 + (threadIdx.x >> 5)) * (32 / G) + lane / G;
@@ -729,16 +734,17 @@ __global__ void __launch_bounds__(128, MINB) k_col_stage_vjp_g(DevParams<FT> P, 
     }
   }
   // ---------------------------------------------------------------- forward recompute
-  FT H[5][CM];
-  if (V.Uo_c) {
+  FT H[5][CM], tif[CM];
+  if constexpr (REC) {
 #pragma unroll
     for (int k = 0; k < CM; ++k) {
       const bool okc = r0 + k < Nv, okf = r0 + k < Nf;
+      tif[k] = okf ? V.Tio_f[fb + k] : FT(0);
       H[0][k] = okc ? V.Uo_c[cb + k] - dtg * V.Tio_c[rb + k] : FT(0);
       H[1][k] = okc ? V.Uo_c[cb + (size_t)sc + k] : FT(0);
       H[2][k] = okc ? V.Uo_c[cb + (size_t)2 * sc + k] : FT(0);
       H[3][k] = okc ? V.Uo_c[cb + (size_t)3 * sc + k] - dtg * V.Tio_c[rb + (size_t)sc + k] : FT(0);
-      H[4][k] = okf ? V.Uo_f[fb + k] - dtg * V.Tio_f[fb + k] : FT(0);
+      H[4][k] = okf ? V.Uo_f[fb + k] - dtg * tif[k] : FT(0);
     }
   } else {
 #pragma unroll
@@ -874,7 +880,13 @@ __global__ void __launch_bounds__(128, MINB) k_col_stage_vjp_g(DevParams<FT> P, 
     Sa[k] = aa; Sb[k] = bb; Sc[k] = cc; Sd[k] = rhs;
   }
   FT x[CM];
-  {
+  if constexpr (REC) {
+#pragma unroll
+    for (int k = 0; k < CM; ++k) {
+      const int f = r0 + k;
+      x[k] = f >= Nf ? FT(0) : (f == 0 || f == Nv) ? Sd[k] / Sb[k] : -dtg * tif[k];
+    }
+  } else {
     FT a_[CM], b_[CM], c_[CM], d_[CM];
 #pragma unroll
     for (int k = 0; k < CM; ++k) { a_[k] = Sa[k]; b_[k] = Sb[k]; c_[k] = Sc[k]; d_[k] = Sd[k]; }
@@ -1036,10 +1048,12 @@ __global__ void __launch_bounds__(128, MINB) k_col_stage_vjp_g(DevParams<FT> P, 
     // contributions to the centre below the face (f - 1) go to the previous level
     FT pR0 = 0, pK = 0, pTHV = 0, pTHVR = 0, pPI = 0, pPHIR = 0, pru0 = 0, pru1 = 0, peu0 = 0, peu1 = 0, pRr = 0, pRe = 0;
     FT toPrevU3 = 0, toNextU3 = 0;
-    FT cR0[CM], cK[CM], cTHV[CM], cTHVR[CM], cPI[CM], cPHIR[CM], cru0[CM], cru1[CM], ceu0[CM], ceu1[CM], cRr[CM], cRe[CM];
-#pragma unroll
-    for (int k = 0; k < CM; ++k)
-      cR0[k] = cK[k] = cTHV[k] = cTHVR[k] = cPI[k] = cPHIR[k] = cru0[k] = cru1[k] = ceu0[k] = ceu1[k] = cRr[k] = cRe[k] = FT(0);
+    // this lane's own contributions accumulate straight into the cotangent arrays (no
+    // separate accumulators live through the loop); those of the level below the lane's
+    // first go to the previous lane (pXX) and are folded in after the loop
+    FT (&cR0)[CM] = bR0, (&cK)[CM] = bK, (&cTHV)[CM] = bTHV, (&cTHVR)[CM] = bTHVR, (&cPI)[CM] = bPI;
+    FT (&cPHIR)[CM] = bPHIR, (&cru0)[CM] = bru0, (&cru1)[CM] = bru1, (&ceu0)[CM] = beu0, (&ceu1)[CM] = beu1;
+    FT (&cRr)[CM] = bRr, (&cRe)[CM] = bRe;
     const FT xpv = xp;
 #pragma unroll
     for (int k = 0; k < CM; ++k) {
@@ -1137,12 +1151,6 @@ __global__ void __launch_bounds__(128, MINB) k_col_stage_vjp_g(DevParams<FT> P, 
     fold1<G, CM>(cRr, pRr, FT(0), gl);
     fold1<G, CM>(cRe, pRe, FT(0), gl);
     fold1<G, CM>(bU3, toPrevU3, toNextU3, gl);
-#pragma unroll
-    for (int k = 0; k < CM; ++k) {
-      bR0[k] += cR0[k]; bK[k] += cK[k]; bTHV[k] += cTHV[k]; bTHVR[k] += cTHVR[k]; bPI[k] += cPI[k];
-      bPHIR[k] += cPHIR[k]; bru0[k] += cru0[k]; bru1[k] += cru1[k]; beu0[k] += ceu0[k]; beu1[k] += ceu1[k];
-      bRr[k] += cRr[k]; bRe[k] += cRe[k];
-    }
   }
   // (e) centre rows: contributions to the face cotangents of F, F h, fr, fhb at faces v, v+1
   FT bF[CM], bFh[CM], bfr[CM], bfhb[CM];
@@ -1334,12 +1342,19 @@ void launch_column_stage_vjp(const DevParams<FT> &P, const StageArgs<FT> &A, con
     return;
   }
   auto grid = [&](int G) { return (ncols + 4 * (32 / G) - 1) / (4 * (32 / G)); };
-  if (P.Nf <= 16) lp::k_col_stage_vjp_g<FT, 8, 2><<<grid(8), 128, 0, s>>>(P, V);
-  else if (P.Nf <= 32) lp::k_col_stage_vjp_g<FT, 16, 2><<<grid(16), 128, 0, s>>>(P, V);
-  // FP32, two levels per lane: six resident CTAs per SM (an 85-register cap; measured at
-  // z_elem = 63: 0.531 ms at 4 CTAs, 0.518 at 5, 0.506 at 6, 0.516 at 7, 0.571 at 8)
-  else if (P.Nf <= 64) lp::k_col_stage_vjp_g<FT, 32, 2, sizeof(FT) == 4 ? 6 : 1><<<grid(32), 128, 0, s>>>(P, V);
-  else lp::k_col_stage_vjp_g<FT, 32, 4><<<grid(32), 128, 0, s>>>(P, V);
+  auto go = [&](auto rec) {
+    constexpr bool R = decltype(rec)::value;
+    constexpr int M6 = sizeof(FT) == 4 ? 6 : 1;
+    constexpr int MD = lp::VjpMinBlocks<FT>::value;
+    if (P.Nf <= 16) lp::k_col_stage_vjp_g<FT, 8, 2, MD, R><<<grid(8), 128, 0, s>>>(P, V);
+    else if (P.Nf <= 32) lp::k_col_stage_vjp_g<FT, 16, 2, MD, R><<<grid(16), 128, 0, s>>>(P, V);
+    // FP32, two levels per lane: six resident CTAs per SM (an 85-register cap; measured at
+    // z_elem = 63: 0.531 ms at 4 CTAs, 0.518 at 5, 0.506 at 6, 0.516 at 7, 0.571 at 8)
+    else if (P.Nf <= 64) lp::k_col_stage_vjp_g<FT, 32, 2, M6, R><<<grid(32), 128, 0, s>>>(P, V);
+    else lp::k_col_stage_vjp_g<FT, 32, 4, MD, R><<<grid(32), 128, 0, s>>>(P, V);
+  };
+  if (V.Uo_c) go(std::true_type{});
+  else go(std::false_type{});
 }
 
 template void launch_column_stage_vjp<float>(const DevParams<float> &, const StageArgs<float> &, const float *,

@@ -495,8 +495,11 @@ int time_kernel_t(gb_ctx *ctx, int kernel, gb_fieldvec Y, int reps, double *ms) 
         launch_passB_vjp<FT>(P, Yc, Yf, lap, Tc, Tf, Ubc, Ubf, Lbc, (double *)I->adj->dparB.p, I->adj->grid, false, s);
         break;
       case GB_K_COLUMN_VJP:
+        // as in a reverse step: the stage's recorded output and implicit tendency given
+        // (here the stage buffer and the last implicit tendency; finite values)
         launch_column_stage_vjp<FT>(P, SA, Tc, Tf, (const FT *)I->Ti[1].p, (const FT *)I->Ti[1].p + I->NR, Ubc, Ubf,
-                                    Teb, Tibs, I->NC, I->NR, (FT *)I->adj->scr.p, (double *)I->adj->dal.p, s);
+                                    Teb, Tibs, I->NC, I->NR, (FT *)I->adj->scr.p, (double *)I->adj->dal.p, s,
+                                    (const FT *)I->U.p, (const FT *)I->Ti[3].p);
         break;
       case GB_K_DSS_T: launch_dss_transpose<FT>(P, Ubc, Ubf, s); break;
       case GB_K_PASSB_FINAL: {

@@ -45,13 +45,23 @@ struct Impl : ImplBase {
   double ae[4][4], ai[4][4], be[4], bi[4];
   bool stiffly_accurate = false;  // b = the last row of the implicit tableau
   // reverse mode (allocated on first use)
+  // A captured launch sequence and the arguments it was captured for.
+  struct Graph {
+    cudaGraphExec_t exec = nullptr;
+    const void *a = nullptr, *b = nullptr;
+    double dt = 0;
+    ~Graph() {
+      if (exec) cudaGraphExecDestroy(exec);
+    }
+  };
   struct Record {  // forward data of one step kept for its reverse pass
     DevBuf Y, U[4], L[4], Te[4], Ti[4];
+    Graph fwd, rev;  // this record's recording step and reverse step, captured on first use
   };
   struct Adjoint {
     std::vector<std::unique_ptr<Record>> rec;
     std::vector<std::unique_ptr<DevBuf>> ckpt;
-    DevBuf Ub, Lb, Teb[4], Tib[4], zero, dummy, scr, dparB, dal, dacc, work;
+    DevBuf Ub, Lb, Teb[4], Tib[4], zero, dummy, scr, dparB, dal, dacc, work, yb;
     int nsteps = 0, every = 0, grid = 0;
     int rec_seg = -1;  // checkpoint segment whose stage records are valid (recorded by the forward pass)
     double dt = 0;
@@ -368,6 +378,30 @@ void enqueue_step(gb_ctx *ctx, FT *Yc, FT *Yf, double dt_, cudaStream_t s) {
     A.ci[j] = dt * (FT)I->bi[j];
   }
   launch_final<FT>(P, A, Yc, Yf, s);
+}
+
+// Run the launches enqueue(stream) as a CUDA graph: captured (on the private capture stream)
+// when g holds none for the arguments (a, b, dt), then launched on the context's stream.
+template <class FT, class F>
+int graph_run(gb_ctx *ctx, typename Impl<FT>::Graph &g, const void *a, const void *b, double dt, F &&enqueue) {
+  Impl<FT> *I = impl<FT>(ctx);
+  if (!g.exec || g.a != a || g.b != b || g.dt != dt) {
+    if (g.exec) { cudaGraphExecDestroy(g.exec); g.exec = nullptr; }
+    if (!I->cap) CK(cudaStreamCreateWithFlags(&I->cap, cudaStreamNonBlocking));
+    cudaGraph_t graph;
+    CK(cudaStreamBeginCapture(I->cap, cudaStreamCaptureModeThreadLocal));
+    enqueue(I->cap);
+    cudaError_t le = cudaGetLastError();
+    cudaError_t ce = cudaStreamEndCapture(I->cap, &graph);
+    if (le != cudaSuccess) return fail(ctx, GB_ERR_CUDA, std::string("capture launch: ") + cudaGetErrorString(le));
+    if (ce != cudaSuccess) return fail(ctx, GB_ERR_CUDA, std::string("cudaStreamEndCapture: ") + cudaGetErrorString(ce));
+    cudaError_t ie = cudaGraphInstantiate(&g.exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (ie != cudaSuccess) { g.exec = nullptr; return fail(ctx, GB_ERR_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(ie)); }
+    g.a = a; g.b = b; g.dt = dt;
+  }
+  CK(cudaGraphLaunch(g.exec, ctx->stream));
+  return GB_OK;
 }
 
 template <class FT>
@@ -914,8 +948,13 @@ int adjoint_forward_t(gb_ctx *ctx, gb_fieldvec Y, double dt, int nsteps, int eve
       CK(cudaMemcpyAsync(ck, Yc, I->NC * sizeof(FT), cudaMemcpyDeviceToDevice, s));
       CK(cudaMemcpyAsync(ck + I->NC, Yf, I->NF * sizeof(FT), cudaMemcpyDeviceToDevice, s));
     }
-    if (k >= last) record_step<FT>(ctx, Yc, Yf, dt, *A.rec[k - last], s);
-    else enqueue_step<FT>(ctx, Yc, Yf, dt, s);
+    if (k >= last) {
+      auto &rc = *A.rec[k - last];
+      r = graph_run<FT>(ctx, rc.fwd, Yc, Yf, dt, [&](cudaStream_t cs) { record_step<FT>(ctx, Yc, Yf, dt, rc, cs); });
+      if (r) return r;
+    } else {
+      enqueue_step<FT>(ctx, Yc, Yf, dt, s);
+    }
   }
   A.rec_seg = nck - 1;
   A.nsteps = nsteps;
@@ -936,18 +975,36 @@ int adjoint_reverse_t(gb_ctx *ctx, gb_fieldvec Yb, double *dpar, size_t *peak) {
   cudaStream_t s = ctx->stream;
   const size_t SB = (I->NC + I->NF) * sizeof(FT);
   FT *W = (FT *)A.work.p;
+  // the cotangent is carried in a library buffer, so that each record's recording and
+  // reverse steps are captured once as CUDA graphs and replayed (fixed arguments)
+  if (!A.yb.p && (r = alloc_z<FT>(ctx, A.yb, SB, A.bytes))) return r;
+  FT *ybc = (FT *)A.yb.p, *ybf = ybc + I->NC;
+  CK(cudaMemcpyAsync(ybc, Yb.c, I->NC * sizeof(FT), cudaMemcpyDeviceToDevice, s));
+  CK(cudaMemcpyAsync(ybf, Yb.f, I->NF * sizeof(FT), cudaMemcpyDeviceToDevice, s));
   zero_dpar<FT>(ctx, s);
   const int nseg = (A.nsteps + A.every - 1) / A.every;
   for (int g = nseg - 1; g >= 0; --g) {
     const int s0 = g * A.every, s1 = std::min(A.nsteps, s0 + A.every);
     if (g != A.rec_seg) {
       CK(cudaMemcpyAsync(W, A.ckpt[g]->p, SB, cudaMemcpyDeviceToDevice, s));
-      for (int k = s0; k < s1; ++k) record_step<FT>(ctx, W, W + I->NC, A.dt, *A.rec[k - s0], s);
+      for (int k = s0; k < s1; ++k) {
+        auto &rc = *A.rec[k - s0];
+        r = graph_run<FT>(ctx, rc.fwd, W, W + I->NC, A.dt,
+                          [&](cudaStream_t cs) { record_step<FT>(ctx, W, W + I->NC, A.dt, rc, cs); });
+        if (r) return r;
+      }
     }
     A.rec_seg = -1;
-    for (int k = s1 - 1; k >= s0; --k) reverse_step<FT>(ctx, *A.rec[k - s0], A.dt, (FT *)Yb.c, (FT *)Yb.f, s);
+    for (int k = s1 - 1; k >= s0; --k) {
+      auto &rc = *A.rec[k - s0];
+      r = graph_run<FT>(ctx, rc.rev, ybc, ybf, A.dt,
+                        [&](cudaStream_t cs) { reverse_step<FT>(ctx, rc, A.dt, ybc, ybf, cs); });
+      if (r) return r;
+    }
     if ((r = check_launch(ctx))) return r;
   }
+  CK(cudaMemcpyAsync(Yb.c, ybc, I->NC * sizeof(FT), cudaMemcpyDeviceToDevice, s));
+  CK(cudaMemcpyAsync(Yb.f, ybf, I->NF * sizeof(FT), cudaMemcpyDeviceToDevice, s));
   if ((r = read_dacc<FT>(ctx, dpar, false))) return r;
   if (peak) {
     size_t base = 0;

@@ -57,8 +57,14 @@ def initial_state(geom, cfg, seed=0, sigma=1.0, bump=None, dtype=None):
     dtype = np.dtype(dtype or cfg.ft)
     Nh, Nv = geom.Nh, geom.Nv
     zc = np.asarray(geom.zc, dtype=np.float64)
+    terrain = getattr(geom, "terrain", None)
+    if terrain is not None:
+        # terrain-following levels: the same profile at each point's own height
+        zc = np.asarray(terrain["zc"], dtype=np.float64)        # [Nh,16,Nv]
+    else:
+        zc = np.broadcast_to(zc, (Nh, 16, Nv))
     T, p = temperature_pressure(zc, c)
-    rho = p / (c["R_d"] * T)                                   # [Nv]
+    rho = p / (c["R_d"] * T)                                   # [Nh,16,Nv]
     rc = (geom.R + zc) / geom.R
     uidx, nu = _unique_node_index(geom.xyz)
     rng = np.random.default_rng(seed)
@@ -74,7 +80,7 @@ def initial_state(geom, cfg, seed=0, sigma=1.0, bump=None, dtype=None):
     u2 = (eE[..., 1, None] * u + eN[..., 1, None] * v) * rc
     K = 0.5 * (u * u + v * v)
     eint = c["cv_d"] * (T - c["T_0"]) - c["R_d"] * c["T_0"]
-    rhoe = rho[None, None, :] * (eint[None, None, :] + c["grav"] * zc[None, None, :] + K)
+    rhoe = rho * (eint + c["grav"] * zc + K)
     if bump is not None:
         amp, rad, lat0, lon0 = bump
         la, lo = math.radians(lat0), math.radians(lon0)
@@ -82,7 +88,7 @@ def initial_state(geom, cfg, seed=0, sigma=1.0, bump=None, dtype=None):
         d = geom.R * np.arccos(np.clip(geom.xyz @ X0, -1.0, 1.0))   # [Nh,16]
         rhoe = rhoe * (1.0 + amp * np.exp(-(d / rad) ** 2))[..., None]
     Yc = np.empty((Nh, 4, 16, Nv), dtype=np.float64)
-    Yc[:, 0] = rho[None, None, :]
+    Yc[:, 0] = rho
     Yc[:, 1] = u1
     Yc[:, 2] = u2
     Yc[:, 3] = rhoe

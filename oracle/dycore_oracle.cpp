@@ -62,6 +62,13 @@ struct OracleGeom {
   const double *W, *D, *Jh, *gup, *gdn, *sinlat, *fh0, *ecov, *econ, *zf;
   const int *dss_off, *dss_copy;
   const double *dss_w;
+  // Terrain-following geometry (all null over a flat surface), per point: heights
+  // zc [Nh][16][Nv] and zf [Nh][16][Nf]; Jacobians Jc, Jf; contravariant metrics
+  // guc, guf [..][6] = (g^11, g^12, g^22, g^13, g^23, g^33); covariant metric of the
+  // centres gdc [..][6] = (g_11, g_12, g_22, g_13, g_23, g_33); the Coriolis f^3 of the
+  // centres and (f^1, f^2) of the faces; the covariant and contravariant basis of the
+  // centres Ecc, Ecn [..][3][3] (row i = E_i or E^i, Cartesian) for the vector DSS.
+  const double *t_zc, *t_zf, *t_Jc, *t_Jf, *t_guc, *t_guf, *t_gdc, *t_f3c, *t_f12f, *t_Ecc, *t_Ecn;
 };
 }
 
@@ -84,6 +91,9 @@ struct Oracle {
   std::vector<FT> zf, zc, dzc, dzf, rc, rf;
   std::vector<int> goff, gcopy;
   std::vector<FT> gw;
+  // terrain-following geometry per point (topo = 1), see OracleGeom
+  int topo = 0;
+  std::vector<FT> tzc, tzf, tJc, tJf, tguc, tguf, tgdc, tf3c, tf12f, tEcc, tEcn;
 
   size_t ncen() const { return (size_t)Nh * 4 * NN * Nv; }
   size_t nfac() const { return (size_t)Nh * NN * Nf; }
@@ -93,9 +103,15 @@ struct Oracle {
   size_t pi(int e, int n, int v) const { return ((size_t)e * NN + n) * Nv + v; }
   size_t hn(int e, int n) const { return (size_t)e * NN + n; }
 
-  // ---- pointwise geometry ----
-  FT Jc(int e, int n, int v) const { return Jh[hn(e, n)] * rc[v] * rc[v] * dzc[v]; }
-  FT Jfc(int e, int n, int k) const { return Jh[hn(e, n)] * rf[k] * rf[k] * dzf[k]; }
+  // ---- pointwise geometry (per level over a flat surface, per point over terrain) ----
+  FT Jc(int e, int n, int v) const { return topo ? tJc[pi(e, n, v)] : Jh[hn(e, n)] * rc[v] * rc[v] * dzc[v]; }
+  FT Jfc(int e, int n, int k) const { return topo ? tJf[fi(e, n, k)] : Jh[hn(e, n)] * rf[k] * rf[k] * dzf[k]; }
+  FT zcp(int e, int n, int v) const { return topo ? tzc[pi(e, n, v)] : zc[v]; }
+  FT zfp(int e, int n, int k) const { return topo ? tzf[fi(e, n, k)] : zf[k]; }
+  // g^33 of a face and the (g^31, g^32) of a centre
+  FT g33f(int e, int n, int k) const { return topo ? tguf[fi(e, n, k) * 6 + 5] : FT(1) / (dzf[k] * dzf[k]); }
+  FT g31c(int e, int n, int v) const { return topo ? tguc[pi(e, n, v) * 6 + 3] : FT(0); }
+  FT g32c(int e, int n, int v) const { return topo ? tguc[pi(e, n, v) * 6 + 4] : FT(0); }
   FT gu(int e, int n, int c, FT r) const { return gup[hn(e, n) * 3 + c] / (r * r); }
   FT gd(int e, int n, int c, FT r) const { return gdn[hn(e, n) * 3 + c] * (r * r); }
 
@@ -115,6 +131,8 @@ struct Oracle {
   // ---- precomputed quantities (set_implicit_precomputed_quantities!) ----
   struct Pre {
     std::vector<FT> ub3, K, T, p, h, Pi, thv, thvr, phir, uc1, uc2, u3c;  // u3c = contravariant u^3 at faces
+    // ct3 = CT3(u_h) = g^31 u_1 + g^32 u_2 at centres (0 over a flat surface); w3c = g^33 u_3 at faces
+    std::vector<FT> ct3, w3c;
   } pre;
 #ifdef ORACLE_PHID
   // per level: the reference pressure p0 = p_ref Pi0^(1/kappa) and Pi0^7, Phi_r(Pi0) = g z_c (Newton, FP64)
@@ -141,46 +159,90 @@ struct Oracle {
 
   void alloc_pre() {
     size_t P = npt();
-    for (auto *v : {&pre.ub3, &pre.K, &pre.T, &pre.p, &pre.h, &pre.Pi, &pre.thv, &pre.thvr, &pre.phir, &pre.uc1, &pre.uc2})
+    for (auto *v : {&pre.ub3, &pre.K, &pre.T, &pre.p, &pre.h, &pre.Pi, &pre.thv, &pre.thvr, &pre.phir, &pre.uc1, &pre.uc2,
+                    &pre.ct3})
       v->assign(P, FT(0));
     pre.u3c.assign(nfac(), FT(0));
+    pre.w3c.assign(nfac(), FT(0));
 #ifdef ORACLE_PHID
     ref_levels();
 #endif
   }
 
-  // impenetrable-boundary filter: u_3 = -u_h^3 / g^33 at the bottom and top
-  // faces; without topography u_h^3 = 0 (precomputed_quantities.jl:486-553).
-  void bc_filter(FT *Yf) const {
+  // impenetrable-boundary filter: u_3 = -u_h^3 / g^33 at the bottom and top faces
+  // (set_velocity_at_surface! / set_velocity_at_top!, precomputed_quantities.jl:486-553),
+  // u_h^3 = ᶠwinterp(rho J, CT3(u_h)), which at the boundary faces is the adjacent centre's
+  // CT3(u_h) (Extrapolate); over a flat surface u_h^3 = 0.
+  void bc_filter(const FT *Yc, FT *Yf) const {
 #pragma omp parallel for
     for (int e = 0; e < Nh; ++e)
       for (int n = 0; n < NN; ++n) {
-        Yf[fi(e, n, 0)] = FT(0);
-        Yf[fi(e, n, Nv)] = FT(0);
+        if (!topo) {
+          Yf[fi(e, n, 0)] = FT(0);
+          Yf[fi(e, n, Nv)] = FT(0);
+          continue;
+        }
+        const FT b = g31c(e, n, 0) * Yc[ci(e, 1, n, 0)] + g32c(e, n, 0) * Yc[ci(e, 2, n, 0)];
+        const FT t = g31c(e, n, Nv - 1) * Yc[ci(e, 1, n, Nv - 1)] + g32c(e, n, Nv - 1) * Yc[ci(e, 2, n, Nv - 1)];
+        Yf[fi(e, n, 0)] = -b / g33f(e, n, 0);
+        Yf[fi(e, n, Nv)] = -t / g33f(e, n, Nv);
       }
   }
 
   void set_precomputed(FT *Yc, FT *Yf) {
-    bc_filter(Yf);
+    bc_filter(Yc, Yf);
 #pragma omp parallel for
     for (int e = 0; e < Nh; ++e)
       for (int n = 0; n < NN; ++n) {
-        for (int k = 0; k < Nf; ++k) pre.u3c[fi(e, n, k)] = Yf[fi(e, n, k)] / (dzf[k] * dzf[k]);
+        for (int k = 0; k < Nf; ++k)
+          pre.u3c[fi(e, n, k)] = topo ? Yf[fi(e, n, k)] * g33f(e, n, k) : Yf[fi(e, n, k)] / (dzf[k] * dzf[k]);
+        if (topo) {
+          // CT3(u_h) at the centres; u^3 = ᶠwinterp(rho J, CT3(u_h)) + g^33 u_3 at the faces
+          // (compute_ᶠuₕ³ and set_velocity_quantities!, precomputed_quantities.jl:473-476, 560-571)
+          for (int v = 0; v < Nv; ++v)
+            pre.ct3[pi(e, n, v)] = g31c(e, n, v) * Yc[ci(e, 1, n, v)] + g32c(e, n, v) * Yc[ci(e, 2, n, v)];
+          for (int k = 0; k < Nf; ++k) {
+            FT uh3;
+            if (k == 0) uh3 = pre.ct3[pi(e, n, 0)];
+            else if (k == Nv) uh3 = pre.ct3[pi(e, n, Nv - 1)];
+            else {
+              const FT wa = Yc[ci(e, 0, n, k - 1)] * Jc(e, n, k - 1), wb = Yc[ci(e, 0, n, k)] * Jc(e, n, k);
+              uh3 = (wa * pre.ct3[pi(e, n, k - 1)] + wb * pre.ct3[pi(e, n, k)]) / (wa + wb);
+            }
+            pre.w3c[fi(e, n, k)] = pre.u3c[fi(e, n, k)];
+            pre.u3c[fi(e, n, k)] = uh3 + pre.w3c[fi(e, n, k)];
+          }
+        } else {
+          for (int k = 0; k < Nf; ++k) pre.w3c[fi(e, n, k)] = pre.u3c[fi(e, n, k)];
+        }
         for (int v = 0; v < Nv; ++v) {
           size_t q = pi(e, n, v);
           FT rho = Yc[ci(e, 0, n, v)], u1 = Yc[ci(e, 1, n, v)], u2 = Yc[ci(e, 2, n, v)], rhoe = Yc[ci(e, 3, n, v)];
-          FT r = rc[v];
-          FT c1 = gu(e, n, 0, r) * u1 + gu(e, n, 1, r) * u2;
-          FT c2 = gu(e, n, 1, r) * u1 + gu(e, n, 2, r) * u2;
           FT a = Yf[fi(e, n, v)], b = Yf[fi(e, n, v + 1)];
+          FT c1, c2, K;
+          pre.ub3[q] = (a + b) / FT(2);
+          if (topo) {
+            // ᶜu = C123(u_h) + ᶜinterp(C123(u_3)); CT12(ᶜu) = g^ab u_b + g^a3 I^c(u_3);
+            // K = 1/2 (C123(u_h) . CT123(u_h) + I^c(u_3 g^33 u_3) + 2 CT3(u_h) I^c(u_3))
+            // (compute_kinetic, utilities.jl:194-206)
+            const FT *G = &tguc[q * 6];
+            const FT h1 = G[0] * u1 + G[1] * u2, h2 = G[1] * u1 + G[2] * u2;
+            c1 = h1 + G[3] * pre.ub3[q];
+            c2 = h2 + G[4] * pre.ub3[q];
+            const FT kv = (a * pre.w3c[fi(e, n, v)] + b * pre.w3c[fi(e, n, v + 1)]) / FT(2);
+            K = (u1 * h1 + u2 * h2 + kv + FT(2) * pre.ct3[q] * pre.ub3[q]) / FT(2);
+          } else {
+            FT r = rc[v];
+            c1 = gu(e, n, 0, r) * u1 + gu(e, n, 1, r) * u2;
+            c2 = gu(e, n, 1, r) * u1 + gu(e, n, 2, r) * u2;
+            // K = 1/2 (u_h . u_h + I^c(u_3 u^3) + 2 u_h^3 I^c(u_3)); u_h^3 = 0 here
+            FT kv = (a * pre.u3c[fi(e, n, v)] + b * pre.u3c[fi(e, n, v + 1)]) / FT(2);
+            K = (u1 * c1 + u2 * c2 + kv) / FT(2);
+          }
           pre.uc1[q] = c1;
           pre.uc2[q] = c2;
-          pre.ub3[q] = (a + b) / FT(2);
-          // K = 1/2 (u_h . u_h + I^c(u_3 u^3) + 2 u_h^3 I^c(u_3)); u_h^3 = 0 here
-          FT kv = (a * pre.u3c[fi(e, n, v)] + b * pre.u3c[fi(e, n, v + 1)]) / FT(2);
-          FT K = (u1 * c1 + u2 * c2 + kv) / FT(2);
           pre.K[q] = K;
-          FT Phi = grav * zc[v];
+          FT Phi = grav * zcp(e, n, v);
           FT eint = rhoe / rho - K - Phi;
           FT T = std::max(Tmin_sgs, T0 + (eint + Rd * T0) / cvd);
           FT p = rho * Rd * T;
@@ -239,8 +301,13 @@ struct Oracle {
         o[i + NQ * j] = s;
       }
   }
-  struct Slab {  // geometry of one slab
+  // Geometry of one slab.  Over a flat surface the metric is block diagonal (g^33 and g_33
+  // per level); over terrain (t = true) it is the full per-node 3x3 metric: gu3, gu4, gu5 =
+  // g^13, g^23, g^33 and gd3, gd4, gd5 = g_13, g_23, g_33 (centres only: the faces need J).
+  struct Slab {
     FT J[NN], WJ[NN], gu0[NN], gu1[NN], gu2[NN], gd0[NN], gd1[NN], gd2[NN], g33, G33;
+    bool t = false;
+    FT gu3[NN], gu4[NN], gu5[NN], gd3[NN], gd4[NN], gd5[NN];
   };
   void slab(int e, FT r, FT dz, Slab &s) const {
     for (int n = 0; n < NN; ++n) {
@@ -251,6 +318,31 @@ struct Oracle {
     }
     s.g33 = FT(1) / (dz * dz);
     s.G33 = dz * dz;
+    s.t = false;
+  }
+  void slab_c(int e, int v, Slab &s) const {
+    if (!topo) return slab(e, rc[v], dzc[v], s);
+    s.t = true;
+    for (int n = 0; n < NN; ++n) {
+      const size_t q = pi(e, n, v);
+      const FT *G = &tguc[q * 6], *H = &tgdc[q * 6];
+      s.J[n] = tJc[q];
+      s.WJ[n] = W[n] * s.J[n];
+      s.gu0[n] = G[0]; s.gu1[n] = G[1]; s.gu2[n] = G[2]; s.gu3[n] = G[3]; s.gu4[n] = G[4]; s.gu5[n] = G[5];
+      s.gd0[n] = H[0]; s.gd1[n] = H[1]; s.gd2[n] = H[2]; s.gd3[n] = H[3]; s.gd4[n] = H[4]; s.gd5[n] = H[5];
+    }
+  }
+  void slab_f(int e, int k, Slab &s) const {
+    if (!topo) return slab(e, rf[k], dzf[k], s);
+    s.t = true;
+    for (int n = 0; n < NN; ++n) {
+      const size_t q = fi(e, n, k);
+      const FT *G = &tguf[q * 6];
+      s.J[n] = tJf[q];
+      s.WJ[n] = W[n] * s.J[n];
+      s.gu0[n] = G[0]; s.gu1[n] = G[1]; s.gu2[n] = G[2]; s.gu3[n] = G[3]; s.gu4[n] = G[4]; s.gu5[n] = G[5];
+      s.gd0[n] = s.gd1[n] = s.gd2[n] = s.gd3[n] = s.gd4[n] = s.gd5[n] = FT(0);
+    }
   }
   // strong divergence of contravariant (F1, F2): (1/J) d_i (J F^i)
   void div_h(const Slab &s, const FT *F1, const FT *F2, FT *o) const {
@@ -302,11 +394,18 @@ struct Oracle {
 
   // ---- vector Laplacian  L(u) = C123(wgrad(div u)) * fdiv - C123(wcurl(C123(curl u))) ----
   // input covariant (c1, c2, c3) on the slab; output covariant (o1, o2, o3)
+  // Over terrain every metric conversion takes the full 3x3 metric: the divergence reads
+  // the contravariant (u^1, u^2) of the C123 input, g^a1 c_1 + g^a2 c_2 + g^a3 c_3, and the
+  // covariant (C123) forms of the curls take g_ij over all three components.
   void vec_lap(const Slab &s, const FT *c1, const FT *c2, const FT *c3, FT fdiv, FT *o1, FT *o2, FT *o3) const {
     FT F1[NN], F2[NN], dv[NN], w1[NN], w2[NN];
     for (int n = 0; n < NN; ++n) {
       F1[n] = s.gu0[n] * c1[n] + s.gu1[n] * c2[n];
       F2[n] = s.gu1[n] * c1[n] + s.gu2[n] * c2[n];
+      if (s.t) {
+        F1[n] += s.gu3[n] * c3[n];
+        F2[n] += s.gu4[n] * c3[n];
+      }
     }
     div_h(s, F1, F2, dv);
     wgrad_h(dv, w1, w2);
@@ -314,23 +413,66 @@ struct Oracle {
     curl_h(s, c1, c2, c3, k1, k2, k3);
     FT z1[NN], z2[NN], z3[NN];
     for (int n = 0; n < NN; ++n) {  // C123 of the contravariant curl
-      z1[n] = s.gd0[n] * k1[n] + s.gd1[n] * k2[n];
-      z2[n] = s.gd1[n] * k1[n] + s.gd2[n] * k2[n];
-      z3[n] = s.G33 * k3[n];
+      if (s.t) {
+        z1[n] = s.gd0[n] * k1[n] + s.gd1[n] * k2[n] + s.gd3[n] * k3[n];
+        z2[n] = s.gd1[n] * k1[n] + s.gd2[n] * k2[n] + s.gd4[n] * k3[n];
+        z3[n] = s.gd3[n] * k1[n] + s.gd4[n] * k2[n] + s.gd5[n] * k3[n];
+      } else {
+        z1[n] = s.gd0[n] * k1[n] + s.gd1[n] * k2[n];
+        z2[n] = s.gd1[n] * k1[n] + s.gd2[n] * k2[n];
+        z3[n] = s.G33 * k3[n];
+      }
     }
     FT q1[NN], q2[NN], q3[NN];
     wcurl_h(s, z1, z2, z3, q1, q2, q3);
     for (int n = 0; n < NN; ++n) {
-      o1[n] = fdiv * w1[n] - (s.gd0[n] * q1[n] + s.gd1[n] * q2[n]);
-      o2[n] = fdiv * w2[n] - (s.gd1[n] * q1[n] + s.gd2[n] * q2[n]);
-      o3[n] = -s.G33 * q3[n];
+      if (s.t) {
+        o1[n] = fdiv * w1[n] - (s.gd0[n] * q1[n] + s.gd1[n] * q2[n] + s.gd3[n] * q3[n]);
+        o2[n] = fdiv * w2[n] - (s.gd1[n] * q1[n] + s.gd2[n] * q2[n] + s.gd4[n] * q3[n]);
+        o3[n] = -(s.gd3[n] * q1[n] + s.gd4[n] * q2[n] + s.gd5[n] * q3[n]);
+      } else {
+        o1[n] = fdiv * w1[n] - (s.gd0[n] * q1[n] + s.gd1[n] * q2[n]);
+        o2[n] = fdiv * w2[n] - (s.gd1[n] * q1[n] + s.gd2[n] * q2[n]);
+        o3[n] = -s.G33 * q3[n];
+      }
     }
   }
 
   // ---- DSS (Spaces.weighted_dss!): J-weighted average over collocated nodes; the
   // covariant horizontal vector (comps 1, 2 of a centre block) is averaged in
   // Cartesian components.  Centre block comps: 0 scalar, 1-2 vector, 3 scalar.
-  void dss_center(FT *C, int levels) const {
+  // c123: comps 1-3 of the block are one covariant 3-vector (the Laplacian block of
+  // remaining_tendency: (L_s, C123 of the vector Laplacian)).  Over terrain its third
+  // basis vector E^3 leans with the level, so the vector is projected to Cartesian
+  // components with each copy's full contravariant basis, averaged, and projected back on
+  // each copy's covariant basis (ClimaCore's dss_transform / dss_untransform of a
+  // Covariant123Vector); over a flat surface that reduces to the horizontal vector and a
+  // scalar third component.
+  void dss_center_c123(FT *C, int levels) const {
+    int G = (int)goff.size() - 1;
+#pragma omp parallel for
+    for (int g = 0; g < G; ++g) {
+      for (int v = 0; v < levels; ++v) {
+        FT s0 = 0, X[3] = {0, 0, 0};
+        for (int c = goff[g]; c < goff[g + 1]; ++c) {
+          int idx = gcopy[c], e = idx / NN, n = idx % NN;
+          FT w = gw[c];
+          s0 += w * C[ci(e, 0, n, v)];
+          const FT *En = &tEcn[pi(e, n, v) * 9];
+          for (int d = 0; d < 3; ++d)
+            X[d] += w * (C[ci(e, 1, n, v)] * En[d] + C[ci(e, 2, n, v)] * En[3 + d] + C[ci(e, 3, n, v)] * En[6 + d]);
+        }
+        for (int c = goff[g]; c < goff[g + 1]; ++c) {
+          int idx = gcopy[c], e = idx / NN, n = idx % NN;
+          const FT *Ec = &tEcc[pi(e, n, v) * 9];
+          C[ci(e, 0, n, v)] = s0;
+          for (int i = 0; i < 3; ++i) C[ci(e, 1 + i, n, v)] = Ec[3 * i] * X[0] + Ec[3 * i + 1] * X[1] + Ec[3 * i + 2] * X[2];
+        }
+      }
+    }
+  }
+  void dss_center(FT *C, int levels, bool c123 = false) const {
+    if (c123 && topo) return dss_center_c123(C, levels);
     int G = (int)goff.size() - 1;
 #pragma omp parallel for
     for (int g = 0; g < G; ++g) {
@@ -387,7 +529,7 @@ struct Oracle {
     for (int e = 0; e < Nh; ++e)
       for (int v = 0; v < Nv; ++v) {
         Slab s;
-        slab(e, rc[v], dzc[v], s);
+        slab_c(e, v, s);
         FT f[NN], u1[NN], u2[NN], u3[NN], g1[NN], g2[NN], F1[NN], F2[NN], Ls[NN], o1[NN], o2[NN], o3[NN];
         for (int n = 0; n < NN; ++n) {
           f[n] = X[ci(e, 0, n, v)];
@@ -423,7 +565,7 @@ struct Oracle {
     for (int e = 0; e < Nh; ++e) {
       Slab s;
       for (int v = 0; v < Nv; ++v) {
-        slab(e, rc[v], dzc[v], s);
+        slab_c(e, v, s);
         FT rho[NN], F1[NN], F2[NN], h[NN], tmp[NN], a1[NN], a2[NN], u1[NN], u2[NN], u3[NN];
         for (int n = 0; n < NN; ++n) {
           size_t q = pi(e, n, v);
@@ -450,7 +592,7 @@ struct Oracle {
 #ifdef ORACLE_PHID
           tmp[n] = pre.K[q] + pre.phir[q];
 #else
-          tmp[n] = pre.K[q] + grav * zc[v] - pre.phir[q];
+          tmp[n] = pre.K[q] + grav * zcp(e, n, v) - pre.phir[q];
 #endif
           Pi[n] = pre.Pi[q];
           thp[n] = pre.thv[q] - pre.thvr[q];
@@ -474,7 +616,7 @@ struct Oracle {
 #ifdef ORACLE_PHID
           sd[n] = cpd * (pre.T[q] - T_ref(pre.Pi[q])) + pre.phir[q];
 #else
-          sd[n] = cpd * (pre.T[q] - T0) + grav * zc[v] - sd_r(pre.Pi[q]);
+          sd[n] = cpd * (pre.T[q] - T0) + grav * zcp(e, n, v) - sd_r(pre.Pi[q]);
 #endif
         }
         grad_h(sd, g1, g2);
@@ -492,14 +634,14 @@ struct Oracle {
       }
     }
     // weighted_dss! of the Laplacians (remaining_tendency.jl:18-21)
-    dss_center(Lap.data(), Nv);
+    dss_center(Lap.data(), Nv, true);
     // apply_hyperdiffusion_tendency!
     std::vector<FT> L4u3(npt());
 #pragma omp parallel for
     for (int e = 0; e < Nh; ++e) {
       Slab s;
       for (int v = 0; v < Nv; ++v) {
-        slab(e, rc[v], dzc[v], s);
+        slab_c(e, v, s);
         FT l1[NN], l2[NN], l3[NN], ls[NN], o1[NN], o2[NN], o3[NN];
         for (int n = 0; n < NN; ++n) {
           ls[n] = Lap[ci(e, 0, n, v)]; l1[n] = Lap[ci(e, 1, n, v)];
@@ -543,14 +685,14 @@ struct Oracle {
     for (int e = 0; e < Nh; ++e) {
       Slab s;
       for (int v = 0; v < Nv; ++v) {  // ᶜω³ = wcurl(u_h)
-        slab(e, rc[v], dzc[v], s);
+        slab_c(e, v, s);
         FT u1[NN], u2[NN], o1[NN], o2[NN], o3[NN];
         for (int n = 0; n < NN; ++n) { u1[n] = Yc[ci(e, 1, n, v)]; u2[n] = Yc[ci(e, 2, n, v)]; }
         wcurl_h(s, u1, u2, nullptr, o1, o2, o3);
         for (int n = 0; n < NN; ++n) om3[pi(e, n, v)] = o3[n];
       }
       for (int k = 0; k < Nf; ++k) {  // ᶠω¹² = ᶠcurlᵥ(u_h) + CT12(wcurl(u_3))
-        slab(e, rf[k], dzf[k], s);
+        slab_f(e, k, s);
         FT w3[NN], o1[NN], o2[NN], o3[NN];
         for (int n = 0; n < NN; ++n) w3[n] = Yf[fi(e, n, k)];
         wcurl_h(s, nullptr, nullptr, w3, o1, o2, o3);
@@ -562,8 +704,11 @@ struct Oracle {
             cv2 = (Yc[ci(e, 1, n, k)] - Yc[ci(e, 1, n, k - 1)]) / J;
           }
           FT fh = FT(1) / rf[k];
-          fo1[fi(e, n, k)] = fh0[hn(e, n) * 2 + 0] * fh + cv1 + o1[n];
-          fo2[fi(e, n, k)] = fh0[hn(e, n) * 2 + 1] * fh + cv2 + o2[n];
+          // Coriolis f^a = grad(xi^a) . 2 Omega z_hat: fh0 / r over a flat surface, per point over terrain
+          const FT f1 = topo ? tf12f[fi(e, n, k) * 2 + 0] : fh0[hn(e, n) * 2 + 0] * fh;
+          const FT f2 = topo ? tf12f[fi(e, n, k) * 2 + 1] : fh0[hn(e, n) * 2 + 1] * fh;
+          fo1[fi(e, n, k)] = f1 + cv1 + o1[n];
+          fo2[fi(e, n, k)] = f2 + cv2 + o2[n];
         }
       }
     }
@@ -588,7 +733,8 @@ struct Oracle {
           FT t1v = (X1[v] + X1[v + 1]) / FT(2) / rJ;
           FT t2v = (X2[v] + X2[v + 1]) / FT(2) / rJ;
           // (f3 + w3) x CT12(u) -> C12 = J (-a3 u^2, a3 u^1)
-          FT a3 = FT(2) * omega * sinlat[hn(e, n)] / dzc[v] + om3[q];
+          // f^3 = grad(xi^3) . 2 Omega z_hat: 2 Omega sin(lat) / dz over a flat surface
+          FT a3 = (topo ? tf3c[q] : FT(2) * omega * sinlat[hn(e, n)] / dzc[v]) + om3[q];
           FT J = Jc(e, n, v);
           t1v += J * (-a3 * pre.uc2[q]);
           t2v += J * (a3 * pre.uc1[q]);
@@ -610,7 +756,7 @@ struct Oracle {
         }
         // additional_tendency!: Rayleigh sponge on u_h
         for (int v = 0; v < Nv; ++v) {
-          FT b = beta_sponge(zc[v], a_uh);
+          FT b = beta_sponge(zcp(e, n, v), a_uh);
           Tc[ci(e, 1, n, v)] -= b * Yc[ci(e, 1, n, v)];
           Tc[ci(e, 2, n, v)] -= b * Yc[ci(e, 2, n, v)];
         }
@@ -665,14 +811,14 @@ struct Oracle {
 #ifdef ORACLE_PHID
             FT gPhi = pre.phir[b] - pre.phir[a], gPhir = 0;
 #else
-            FT gPhi = grav * (zc[k] - zc[k - 1]);
+            FT gPhi = grav * (zcp(e, n, k) - zcp(e, n, k - 1));
             FT gPhir = pre.phir[b] - pre.phir[a];
 #endif
             FT thd = ((pre.thv[a] - pre.thvr[a]) + (pre.thv[b] - pre.thvr[b])) / FT(2);
             FT gPi = pre.Pi[b] - pre.Pi[a];
             val = -(gPhi - gPhir + cpd * thd * gPi);
           }
-          val -= beta_sponge(zf[k], a_w) * Yf[fi(e, n, k)];
+          val -= beta_sponge(zfp(e, n, k), a_w) * Yf[fi(e, n, k)];
           Tf[fi(e, n, k)] = val;
         }
       }
@@ -684,6 +830,7 @@ struct Oracle {
     std::vector<FT> Mur, Mue;             // [col][k][2]  (centres k-1, k)
     std::vector<FT> Muh;                  // [col][k][2][2] (centres k-1, k; comps 1, 2)
     std::vector<FT> Muu;                  // [col][k][3]  (faces k-1, k, k+1)
+    std::vector<FT> Mrh, Meh;             // terrain: [col][v][3][2] (centres v-1, v, v+1; comps 1, 2)
   } jac;
 
   void update_jacobian(const FT *Yc, const FT *Yf, FT dtg) {
@@ -691,6 +838,7 @@ struct Oracle {
     jac.Mru.assign(C * Nv * 2, 0); jac.Meu.assign(C * Nv * 2, 0);
     jac.Mur.assign(C * Nf * 2, 0); jac.Mue.assign(C * Nf * 2, 0);
     jac.Muh.assign(C * Nf * 4, 0); jac.Muu.assign(C * Nf * 3, 0);
+    if (topo) { jac.Mrh.assign(C * Nv * 6, 0); jac.Meh.assign(C * Nv * 6, 0); }
     FT kap = Rd / cvd;  // kappa_m for dry air
 #pragma omp parallel for
     for (int e = 0; e < Nh; ++e)
@@ -704,7 +852,7 @@ struct Oracle {
             FT val = 0, vh = 0;
             if (k > 0 && k < Nv) {
               FT rJ = (Yc[ci(e, 0, n, k - 1)] * Jc(e, n, k - 1) + Yc[ci(e, 0, n, k)] * Jc(e, n, k)) / FT(2);
-              FT g33 = FT(1) / (dzf[k] * dzf[k]);
+              FT g33 = g33f(e, n, k);
               FT sign = s ? FT(-1) : FT(1);  // -ᶜadvdivᵥ: -(+ at v+1, - at v)/J
               val = sign * rJ * g33 / J;
               FT hb = (pre.h[pi(e, n, k - 1)] + pre.h[pi(e, n, k)]) / FT(2);
@@ -715,7 +863,7 @@ struct Oracle {
           }
         }
         for (int k = 0; k < Nf; ++k) {
-          FT beta = beta_sponge(zf[k], a_w);
+          FT beta = beta_sponge(zfp(e, n, k), a_w);
           if (k == 0 || k == Nv) {
             jac.Muu[(col * Nf + k) * 3 + 1] = -dtg * beta - FT(1);
             continue;
@@ -723,7 +871,7 @@ struct Oracle {
           size_t a = pi(e, n, k - 1), b = pi(e, n, k);
           FT ra = Yc[ci(e, 0, n, k - 1)], rb = Yc[ci(e, 0, n, k)];
           FT rbar = (ra + rb) / FT(2);
-          auto dpdr = [&](size_t q) { return kap * (T0 * cpd - pre.K[q] - grav * zc[q % Nv]); };
+          auto dpdr = [&](size_t q) { return kap * (T0 * cpd - pre.K[q] - grav * zcp(e, n, (int)(q % Nv))); };
           FT thvb = (pre.thv[a] + pre.thv[b]) / FT(2);
           FT gPi = pre.Pi[b] - pre.Pi[a];
           FT buoy = cpd * thvb * gPi / rbar;  // times ᶠinterp_matrix (1/2, 1/2)
@@ -738,12 +886,70 @@ struct Oracle {
           jac.Muh[(col * Nf + k) * 4 + 2] = dtg * (kap * rb / rbar) * pre.uc1[b];
           jac.Muh[(col * Nf + k) * 4 + 3] = dtg * (kap * rb / rbar) * pre.uc2[b];
           // (u3, u3): p_grad * diag(-kappa rho) * dK/du3 - beta - I ; dK_v/du3_f = u^3_f / 2
-          FT um = pre.u3c[fi(e, n, k - 1)], u0 = pre.u3c[fi(e, n, k)], up = pre.u3c[fi(e, n, k + 1)];
-          jac.Muu[(col * Nf + k) * 3 + 0] = dtg * (-kap * ra * um / (FT(2) * rbar));
-          jac.Muu[(col * Nf + k) * 3 + 1] = dtg * (kap * (rb - ra) * u0 / (FT(2) * rbar) - beta) - FT(1);
-          jac.Muu[(col * Nf + k) * 3 + 2] = dtg * (kap * rb * up / (FT(2) * rbar));
+          if (topo) {
+            // over terrain dK_v/du3_f = (g^33 u_3)_f / 2 + CT3(u_h)_v / 2 (∂ᶜK_∂ᶠu₃,
+            // manual_sparse_jacobian.jl:754-756)
+            const FT wm = pre.w3c[fi(e, n, k - 1)], w0 = pre.w3c[fi(e, n, k)], wp = pre.w3c[fi(e, n, k + 1)];
+            const FT ca = pre.ct3[a], cb = pre.ct3[b];
+            jac.Muu[(col * Nf + k) * 3 + 0] = dtg * (-kap * ra * (wm + ca) / (FT(2) * rbar));
+            jac.Muu[(col * Nf + k) * 3 + 1] =
+                dtg * (kap * (rb * (w0 + cb) - ra * (w0 + ca)) / (FT(2) * rbar) - beta) - FT(1);
+            jac.Muu[(col * Nf + k) * 3 + 2] = dtg * (kap * rb * (wp + cb) / (FT(2) * rbar));
+          } else {
+            FT um = pre.u3c[fi(e, n, k - 1)], u0 = pre.u3c[fi(e, n, k)], up = pre.u3c[fi(e, n, k + 1)];
+            jac.Muu[(col * Nf + k) * 3 + 0] = dtg * (-kap * ra * um / (FT(2) * rbar));
+            jac.Muu[(col * Nf + k) * 3 + 1] = dtg * (kap * (rb - ra) * u0 / (FT(2) * rbar) - beta) - FT(1);
+            jac.Muu[(col * Nf + k) * 3 + 2] = dtg * (kap * rb * up / (FT(2) * rbar));
+          }
+        }
+        if (topo) {
+          // (rho, u_h) and (rho e_tot, u_h) over terrain (manual_sparse_jacobian.jl:761-763, 771-775):
+          // dtγ ᶜadvection_matrix ⋅ [diag(ᶠinterp(h_tot))] ⋅ ᶠwinterp_matrix(ᶜJ ρ) ⋅ diag(g^3h).
+          // The interior face k's flux ρ̄J u^3 holds ½ Σ_c ρJ_c CT3(u_h)_c over its two centres,
+          // so d(flux_k)/du_a,c = ½ ρ_c J_c g^3a_c; the boundary faces carry no flux.
+          for (int v = 0; v < Nv; ++v) {
+            const FT iJ = FT(1) / Jc(e, n, v);
+            for (int t = 0; t < 3; ++t) {
+              const int c = v - 1 + t;
+              FT wr = 0, we = 0;
+              if (c >= 0 && c < Nv) {
+                const FT half_rJ = Yc[ci(e, 0, n, c)] * Jc(e, n, c) / FT(2);
+                // face v (below centre v, +) and face v + 1 (above, -)
+                if ((c == v - 1 || c == v) && v >= 1) {
+                  const FT hb = (pre.h[pi(e, n, v - 1)] + pre.h[pi(e, n, v)]) / FT(2);
+                  wr += half_rJ * iJ;
+                  we += half_rJ * iJ * hb;
+                }
+                if ((c == v || c == v + 1) && v + 1 <= Nv - 1) {
+                  const FT hb = (pre.h[pi(e, n, v)] + pre.h[pi(e, n, v + 1)]) / FT(2);
+                  wr -= half_rJ * iJ;
+                  we -= half_rJ * iJ * hb;
+                }
+              }
+              for (int a2 = 0; a2 < 2; ++a2) {
+                const FT g3a = c >= 0 && c < Nv ? (a2 == 0 ? g31c(e, n, c) : g32c(e, n, c)) : FT(0);
+                jac.Mrh[((col * Nv + v) * 3 + t) * 2 + a2] = dtg * wr * g3a;
+                jac.Meh[((col * Nv + v) * 3 + t) * 2 + a2] = dtg * we * g3a;
+              }
+            }
+          }
         }
       }
+  }
+  // The (rho, u_h) and (rho e_tot, u_h) blocks applied to V_uh, per centre (terrain only).
+  void uh_coupling(int e, int n, const FT *Vc, int v, FT &gr, FT &ge) const {
+    gr = ge = FT(0);
+    if (!topo) return;
+    const size_t col = hn(e, n);
+    for (int t = 0; t < 3; ++t) {
+      const int c = v - 1 + t;
+      if (c < 0 || c >= Nv) continue;
+      for (int a2 = 0; a2 < 2; ++a2) {
+        const FT x = Vc[ci(e, 1 + a2, n, c)];
+        gr += jac.Mrh[((col * Nv + v) * 3 + t) * 2 + a2] * x;
+        ge += jac.Meh[((col * Nv + v) * 3 + t) * 2 + a2] * x;
+      }
+    }
   }
 
   // ---- ldiv!: BlockArrowheadSolve(rho, rhoe; alg2 = BlockLowerTriangularSolve(u_h)) ----
@@ -757,6 +963,15 @@ struct Oracle {
         for (int v = 0; v < Nv; ++v) {
           Xc[ci(e, 1, n, v)] = -Rc[ci(e, 1, n, v)];
           Xc[ci(e, 2, n, v)] = -Rc[ci(e, 2, n, v)];
+        }
+        // over terrain the (rho, u_h), (rho e_tot, u_h) blocks times Δu_h = -R_uh move to the
+        // right-hand sides of the scalar rows: R_x + M_x,uh R_uh
+        std::vector<FT> Rr(Nv), Re(Nv);
+        for (int v = 0; v < Nv; ++v) {
+          FT gr, ge;
+          uh_coupling(e, n, Rc, v, gr, ge);
+          Rr[v] = topo ? Rc[ci(e, 0, n, v)] + gr : Rc[ci(e, 0, n, v)];
+          Re[v] = topo ? Rc[ci(e, 3, n, v)] + ge : Rc[ci(e, 3, n, v)];
         }
         for (int k = 0; k < Nf; ++k) {
           const FT *mu = &jac.Muu[(col * Nf + k) * 3];
@@ -778,7 +993,7 @@ struct Oracle {
             FT t0 = cr * mru[0] + ce * meu[0];  // -> face v
             FT t1 = cr * mru[1] + ce * meu[1];  // -> face v+1
             if (s == 0) { a += t0; b += t1; } else { b += t0; c += t1; }
-            rhs += cr * Rc[ci(e, 0, n, v)] + ce * Rc[ci(e, 3, n, v)];
+            rhs += cr * Rr[v] + ce * Re[v];
             rhs += mh[2 * s] * Rc[ci(e, 1, n, v)] + mh[2 * s + 1] * Rc[ci(e, 2, n, v)];
           }
           A[k] = a; B[k] = b; Cc[k] = c; Dd[k] = rhs;
@@ -797,8 +1012,8 @@ struct Oracle {
         for (int v = 0; v < Nv; ++v) {
           const FT *mru = &jac.Mru[(col * Nv + v) * 2];
           const FT *meu = &jac.Meu[(col * Nv + v) * 2];
-          Xc[ci(e, 0, n, v)] = mru[0] * x[v] + mru[1] * x[v + 1] - Rc[ci(e, 0, n, v)];
-          Xc[ci(e, 3, n, v)] = meu[0] * x[v] + meu[1] * x[v + 1] - Rc[ci(e, 3, n, v)];
+          Xc[ci(e, 0, n, v)] = mru[0] * x[v] + mru[1] * x[v + 1] - Rr[v];
+          Xc[ci(e, 3, n, v)] = meu[0] * x[v] + meu[1] * x[v + 1] - Re[v];
         }
       }
   }
@@ -815,6 +1030,12 @@ struct Oracle {
           FT a = Vf[fi(e, n, v)], b = Vf[fi(e, n, v + 1)];
           Oc[ci(e, 0, n, v)] = -Vc[ci(e, 0, n, v)] + mru[0] * a + mru[1] * b;
           Oc[ci(e, 3, n, v)] = -Vc[ci(e, 3, n, v)] + meu[0] * a + meu[1] * b;
+          if (topo) {
+            FT gr, ge;
+            uh_coupling(e, n, Vc, v, gr, ge);
+            Oc[ci(e, 0, n, v)] += gr;
+            Oc[ci(e, 3, n, v)] += ge;
+          }
           Oc[ci(e, 1, n, v)] = -Vc[ci(e, 1, n, v)];
           Oc[ci(e, 2, n, v)] = -Vc[ci(e, 2, n, v)];
         }
@@ -1005,7 +1226,8 @@ struct Oracle {
       for (int e = 0; e < Nh; ++e)
         for (int n = 0; n < NN; ++n)
           for (int v = 0; v < Nv; ++v) {
-            double x = (double)Yc[ci(e, comp, n, v)] * (double)W[n] * ((double)Jh[hn(e, n)] * rc[v] * rc[v] * dzc[v]);
+            double x = (double)Yc[ci(e, comp, n, v)] * (double)W[n] *
+                       (topo ? (double)tJc[pi(e, n, v)] : ((double)Jh[hn(e, n)] * rc[v] * rc[v] * dzc[v]));
             double t = s + x;
             if (std::fabs(s) >= std::fabs(x)) comp_ += (s - t) + x; else comp_ += (x - t) + s;
             s = t;
@@ -1044,6 +1266,14 @@ struct Oracle {
       else d = (g->zf[k] + g->zf[k + 1]) / 2 - (g->zf[k - 1] + g->zf[k]) / 2;
       dzf[k] = (FT)d;
       rf[k] = (FT)((p->radius + g->zf[k]) / p->radius);
+    }
+    topo = g->t_zc != nullptr;
+    if (topo) {
+      const size_t P = npt(), F = nfac();
+      auto cp = [](std::vector<FT> &d, const double *s, size_t n) { d.assign(s, s + n); };
+      cp(tzc, g->t_zc, P); cp(tzf, g->t_zf, F); cp(tJc, g->t_Jc, P); cp(tJf, g->t_Jf, F);
+      cp(tguc, g->t_guc, 6 * P); cp(tguf, g->t_guf, 6 * F); cp(tgdc, g->t_gdc, 6 * P);
+      cp(tf3c, g->t_f3c, P); cp(tf12f, g->t_f12f, 2 * F); cp(tEcc, g->t_Ecc, 9 * P); cp(tEcn, g->t_Ecn, 9 * P);
     }
     goff.assign(g->dss_off, g->dss_off + g->ngroups + 1);
     gcopy.assign(g->dss_copy, g->dss_copy + goff.back());
@@ -1136,6 +1366,11 @@ void oracle_jac_apply(void *hh, void *Oc, void *Of, void *Vc, void *Vf) {
 void oracle_dss(void *hh, void *Yc, void *Yf) {
   Handle *h = (Handle *)hh;
   DISPATCH(h, (o.dss((decltype(o.R) *)Yc, (decltype(o.R) *)Yf)));
+}
+// The DSS of a centre block whose comps 1-3 are one covariant 3-vector (the Laplacians).
+void oracle_dss_c123(void *hh, void *C) {
+  Handle *h = (Handle *)hh;
+  DISPATCH(h, (o.dss_center((decltype(o.R) *)C, o.Nv, true)));
 }
 void oracle_step(void *hh, void *Yc, void *Yf, double dt, int nsteps) {
   Handle *h = (Handle *)hh;

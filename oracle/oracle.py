@@ -59,7 +59,8 @@ _ip = ctypes.POINTER(ctypes.c_int)
 class _Geom(ctypes.Structure):
     _fields_ = [("Nh", ctypes.c_int), ("Nv", ctypes.c_int), ("ngroups", ctypes.c_int)] + [
         (n, _dp) for n in ("W", "D", "Jh", "gup", "gdn", "sinlat", "fh0", "ecov", "econ", "zf")] + [
-        ("dss_off", _ip), ("dss_copy", _ip), ("dss_w", _dp)]
+        ("dss_off", _ip), ("dss_copy", _ip), ("dss_w", _dp)] + [
+        ("t_" + n, _dp) for n in ("zc", "zf", "Jc", "Jf", "guc", "guf", "gdc", "f3c", "f12f", "Ecc", "Ecn")]
 
 
 _lib = None
@@ -79,6 +80,7 @@ def lib():
         _lib.oracle_set_precomputed.argtypes = [v, v, v]
         _lib.oracle_pressure.argtypes = [v, v, v, v]
         _lib.oracle_dss.argtypes = [v, v, v]
+        _lib.oracle_dss_c123.argtypes = [v, v]
         _lib.oracle_laplacians.argtypes = [v, v, v]
         _lib.oracle_update_jacobian.argtypes = [v, v, v, ctypes.c_double]
         _lib.oracle_step.argtypes = [v, v, v, ctypes.c_double, ctypes.c_int]
@@ -126,6 +128,11 @@ class Oracle:
         g.dss_off = arr(geom.dss_off, np.int32)
         g.dss_copy = arr(geom.dss_copy, np.int32)
         g.dss_w = arr(geom.dss_w)
+        # terrain-following geometry: a dict of per-point arrays (topography.oracle_terrain)
+        terrain = getattr(geom, "terrain", None)
+        if terrain is not None:
+            for k in ("zc", "zf", "Jc", "Jf", "guc", "guf", "gdc", "f3c", "f12f", "Ecc", "Ecn"):
+                setattr(g, "t_" + k, arr(terrain[k]))
         p = _Params()
         for k, _ in _Params._fields_:
             setattr(p, k, params.get(k, 0))
@@ -198,6 +205,12 @@ class Oracle:
     def dss(self, Yc, Yf):
         self._chk(Yc, Yf)
         lib().oracle_dss(self.h, _ptr(Yc), _ptr(Yf))
+
+    def dss_c123(self, C):
+        """In place: the DSS of a centre block [Nh, 4, 16, Nv] whose comp 0 is a scalar and
+        comps 1-3 one covariant 3-vector (the block of the Laplacians)."""
+        self._chk(C)
+        lib().oracle_dss_c123(self.h, _ptr(C))
 
     def laplacians(self, X):
         """Per level, after the DSS: the scalar Laplacian wdiv(grad f) of comp 0 and the vector

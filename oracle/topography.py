@@ -207,3 +207,46 @@ def impenetrable_u3(G, rho, u1, u2):
     uh3 = gc[..., 2, 0] * u1 + gc[..., 2, 1] * u2                 # [Nh, 16, Nv]
     uh3f = winterp_faces(np.asarray(rho) * G["Jc"], uh3)          # [Nh, 16, Nv + 1]
     return np.stack([-uh3f[..., 0] / gf[..., 0, 2, 2], -uh3f[..., -1] / gf[..., -1, 2, 2]], axis=-1)
+
+
+def oracle_terrain(g, z_surface, warp, omega=None):
+    """The per-point arrays the C++ oracle takes over terrain (OracleGeom's t_* fields), from
+    ``warped_geometry``: heights, Jacobians, the contravariant metric of centres and faces and
+    the covariant metric of the centres as (11, 12, 22, 13, 23, 33), the Coriolis components
+    f^i = grad(xi^i) . 2 Omega z_hat (f^3 at the centres, f^1 and f^2 at the faces:
+    compute_coriolis, src/cache/cache.jl:318-343, deep branch), and the centres' covariant and
+    contravariant bases (rows E_i and E^i = g^ij E_j) for the DSS of covariant 3-vectors."""
+    G = warped_geometry(g, z_surface, warp)
+    om = g.omega if omega is None else omega
+    Om = np.array([0.0, 0.0, 2.0 * om])
+    pick = [(0, 0), (0, 1), (1, 1), (0, 2), (1, 2), (2, 2)]
+
+    def six(M):
+        return np.stack([M[..., i, j] for i, j in pick], axis=-1)
+
+    Ec, Ef = G["Ec"], G["Ef"]
+    gdn_c = np.einsum("...ik,...jk->...ij", Ec, Ec)
+    Ecn = np.einsum("...ij,...jk->...ik", G["gup_c"], Ec)
+    Efn = np.einsum("...ij,...jk->...ik", G["gup_f"], Ef)
+    return dict(
+        zc=G["zc"], zf=G["zf"], Jc=G["Jc"], Jf=G["Jf"],
+        guc=six(G["gup_c"]), guf=six(G["gup_f"]), gdc=six(gdn_c),
+        f3c=Ecn[..., 2, :] @ Om, f12f=np.stack([Efn[..., 0, :] @ Om, Efn[..., 1, :] @ Om], axis=-1),
+        Ecc=Ec.reshape(Ec.shape[:-2] + (9,)), Ecn=Ecn.reshape(Ecn.shape[:-2] + (9,)))
+
+
+def smooth_surface(xyz, h0=2000.0, lat0=20.0, lon0=30.0, width=40.0):
+    """A smooth test surface (m) over unit-sphere node positions ``xyz`` [..., 3]: a Gaussian
+    hill of height h0 and angular half-width ``width`` degrees centred at (lat0, lon0)."""
+    la, lo = math.radians(lat0), math.radians(lon0)
+    X0 = np.array([math.cos(la) * math.cos(lo), math.cos(la) * math.sin(lo), math.sin(la)])
+    d = np.arccos(np.clip(np.asarray(xyz) @ X0, -1.0, 1.0))
+    return h0 * np.exp(-(d / math.radians(width)) ** 2)
+
+
+def dcmip200_nodes(xyz):
+    """The DCMIP-2-0-0 mountain at unit-sphere node positions ``xyz`` [..., 3]."""
+    xyz = np.asarray(xyz, dtype=np.float64)
+    lat = np.degrees(np.arctan2(xyz[..., 2], np.hypot(xyz[..., 0], xyz[..., 1])))
+    lon = np.degrees(np.arctan2(xyz[..., 1], xyz[..., 0])) % 360.0
+    return dcmip200(lat, lon)

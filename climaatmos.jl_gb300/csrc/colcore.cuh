@@ -14,6 +14,7 @@
 // with the impenetrable filter (precomputed_quantities.jl:486-553) on u_3.
 #pragma once
 #include "kernels.cuh"
+#include "topo.cuh"
 
 namespace gb {
 namespace col {
@@ -30,27 +31,108 @@ template <class FT>
 struct ColLev {
   const Lev4<FT> *lc4, *lf4, *lr4;
   int Nv, Nf;
+  static constexpr bool TOPO = false;
+  __device__ Lev4<FT> c4(int v) const { return lc4[v]; }
+  __device__ Lev4<FT> f4(int k) const { return lf4[k]; }
+  __device__ Lev4<FT> r4(int v) const { return lr4[v]; }
+};
+
+// The level geometry of one column over terrain-following levels, with the interface of
+// ColLev: c4(v) = {r^2 dz, 1/(r^2 dz), 1/r^2, Phi} and f4(k) = {g^33, beta_w, 0, 0} of the
+// column's own points (topo.cuh), r4(v) the flat level's reference record; ct(v) gives the
+// centre's (g^31, g^32) and g z_s b, the geopotential above the flat level's.
+template <class FT>
+struct ColLevT {
+  const Lev4<FT> *ltc, *ltf, *lr4;
+  int Nv, Nf;
+  FT zs, d1, d2, gs0, gs1, gs2, iR, grav, aw, zd, sk;
+  static constexpr bool TOPO = true;
+  __device__ void load(const DevParams<FT> &P, int e, int n) {
+    ltc = P.ltc;
+    ltf = P.ltf;
+    lr4 = P.lr4;
+    Nv = P.Nv;
+    Nf = P.Nf;
+    iR = P.iR;
+    grav = P.grav;
+    aw = P.spg_aw;
+    zd = P.spg_zd;
+    sk = P.spg_k;
+    const FT *tg = P.tgeo + (size_t)e * TG_N * NN, *hg = P.hgeo + (size_t)e * HG_N * NN;
+    zs = tg[TG_ZS * NN + n];
+    d1 = tg[TG_D1 * NN + n];
+    d2 = tg[TG_D2 * NN + n];
+    gs0 = hg[HG_GU0 * NN + n];
+    gs1 = hg[HG_GU1 * NN + n];
+    gs2 = hg[HG_GU2 * NN + n];
+  }
+  __device__ TPoint<FT> pt(const Lev4<FT> &L) const {
+    TPoint<FT> o;
+    o.zsb = zs * L.y;
+    o.z = L.x + o.zsb;
+    o.r = FT(1) + o.z * iR;
+    o.ir = grcp(o.r);
+    o.r2 = o.r * o.r;
+    o.ir2 = o.ir * o.ir;
+    o.dz = L.z + zs * L.w;
+    o.idz = grcp(o.dz);
+    o.s1 = L.y * d1;
+    o.s2 = L.y * d2;
+    return o;
+  }
+  __device__ Lev4<FT> c4(int v) const {
+    const TPoint<FT> t = pt(ltc[v]);
+    const FT x = t.r2 * t.dz;
+    return Lev4<FT>{x, grcp(x), t.ir2, grav * t.z};
+  }
+  __device__ Lev4<FT> f4(int k) const {
+    const TPoint<FT> t = pt(ltf[k]);
+    FT beta = FT(0);
+    if (aw != FT(0) && t.z > zd) {
+      const FT s = gsin(sk * (t.z - zd));
+      beta = aw * s * s;
+    }
+    return Lev4<FT>{tmetric_up(t, gs0, gs1, gs2).g33, beta, FT(0), FT(0)};
+  }
+  __device__ Lev4<FT> r4(int v) const { return lr4[v]; }
+  __device__ void ct(int v, FT &g31, FT &g32, FT &phis) const {
+    const TPoint<FT> t = pt(ltc[v]);
+    const TMetricUp<FT> m = tmetric_up(t, gs0, gs1, gs2);
+    g31 = m.g13;
+    g32 = m.g23;
+    phis = grav * t.zsb;
+  }
 };
 
 // Centre diagnostics of one level from (rho, u_1, u_2, rho e_tot), the u_3 of
-// the faces below/above and their g^33.
+// the faces below/above and their g^33.  ct3 = CT3(u_h) (0 over a flat surface).
 template <class FT>
 struct Cen {
-  FT rJ, h, phid, Pi, thv, thvr, K, iJ, phi;
+  FT rJ, h, phid, Pi, thv, thvr, K, iJ, phi, ct3;
 };
-template <class FT>
-__device__ __forceinline__ Cen<FT> cdiag(const DevParams<FT> &P, const ColGeo<FT> &G, const ColLev<FT> &L, int v,
+template <class FT, class LV>
+__device__ __forceinline__ Cen<FT> cdiag(const DevParams<FT> &P, const ColGeo<FT> &G, const LV &L, int v,
                                          FT rho, FT u1, FT u2, FT rhoe, FT u3a, FT u3b, FT g33a, FT g33b) {
   const int vc = min(max(v, 0), L.Nv - 1);
-  const Lev4<FT> Lc = L.lc4[vc];
+  const Lev4<FT> Lc = L.c4(vc);
   const FT c1 = (G.gu0 * u1 + G.gu1 * u2) * Lc.z, c2 = (G.gu1 * u1 + G.gu2 * u2) * Lc.z;
   const FT kv = (u3a * (u3a * g33a) + u3b * (u3b * g33b)) / FT(2);
   Cen<FT> o;
-  o.K = (u1 * c1 + u2 * c2 + kv) / FT(2);
+  FT phis = FT(0);
+  if constexpr (LV::TOPO) {
+    // over terrain K takes 2 CT3(u_h) I^c(u_3) (compute_kinetic, utilities.jl:194-206)
+    FT g31, g32;
+    L.ct(vc, g31, g32, phis);
+    o.ct3 = g31 * u1 + g32 * u2;
+    o.K = (u1 * c1 + u2 * c2 + kv + FT(2) * o.ct3 * ((u3a + u3b) / FT(2))) / FT(2);
+  } else {
+    o.ct3 = FT(0);
+    o.K = (u1 * c1 + u2 * c2 + kv) / FT(2);
+  }
   Thermo<FT> th;
-  thermo(P, rho, rhoe, o.K, Lc.w, L.lr4[vc], th);
+  thermo(P, rho, rhoe, o.K, Lc.w, L.r4(vc), th);
   o.h = th.h;
-  o.phid = th.phid;
+  o.phid = LV::TOPO ? th.phid + phis : th.phid;
   o.Pi = th.Pi;
   o.thv = th.thv;
   o.thvr = th.thvr;
@@ -64,8 +146,8 @@ __device__ __forceinline__ Cen<FT> cdiag(const DevParams<FT> &P, const ColGeo<FT
 // (rho, u_1, u_2, rho e_tot), the u_3 of the faces below (u3a) and above (u3b) each level
 // and their g^33.  FP32 with two levels per lane: both levels at once, the same quantities
 // with packed arithmetic (thermo_pair).
-template <class FT, int CM>
-__device__ __forceinline__ void cdiag_lane(const DevParams<FT> &P, const ColGeo<FT> &G, const ColLev<FT> &L, int r0,
+template <class FT, int CM, class LV>
+__device__ __forceinline__ void cdiag_lane(const DevParams<FT> &P, const ColGeo<FT> &G, const LV &L, int r0,
                                            const FT (&U)[5][CM], const FT (&u3a)[CM], const FT (&u3b)[CM],
                                            const FT (&g33a)[CM], const FT (&g33b)[CM], Cen<FT> (&o)[CM]) {
 #pragma unroll
@@ -73,7 +155,7 @@ __device__ __forceinline__ void cdiag_lane(const DevParams<FT> &P, const ColGeo<
     o[k] = cdiag(P, G, L, r0 + k, U[0][k], U[1][k], U[2][k], U[3][k], u3a[k], u3b[k], g33a[k], g33b[k]);
 }
 template <>
-__device__ __forceinline__ void cdiag_lane<float, 2>(const DevParams<float> &P, const ColGeo<float> &G,
+__device__ __forceinline__ void cdiag_lane<float, 2, ColLev<float>>(const DevParams<float> &P, const ColGeo<float> &G,
                                                      const ColLev<float> &L, int r0, const float (&U)[5][2],
                                                      const float (&u3a)[2], const float (&u3b)[2],
                                                      const float (&g33a)[2], const float (&g33b)[2],
@@ -102,6 +184,7 @@ __device__ __forceinline__ void cdiag_lane<float, 2>(const DevParams<float> &P, 
   o[0].iJ = iJ.x; o[1].iJ = iJ.y;
   o[0].rJ = rJ.x; o[1].rJ = rJ.y;
   o[0].phi = phi.x; o[1].phi = phi.y;
+  o[0].ct3 = o[1].ct3 = 0.0f;
 }
 
 // Tridiagonal solve of the CM*G rows held CM per lane by a G-lane group:
@@ -179,8 +262,13 @@ __device__ __forceinline__ FT vanleer_g(FT u, FT am2, FT am1, FT a0, FT ap1, boo
 // which drops the U^ - U terms of the residual.
 // ss accumulates the FP64 sums of squares of the residual (rho, rho e_tot, u_3),
 // iJc receives 1/J of the lane's centres.
-template <class FT, int G, int CM, bool HAT>
-__device__ __forceinline__ void newton_core(const DevParams<FT> &P, const ColGeo<FT> &Gm, const ColLev<FT> &L, int gl,
+// Over terrain-following levels (LV::TOPO) u^3 = u_h^3 + g^33 u_3 with
+// u_h^3 = ᶠwinterp(rho J, CT3(u_h)) (compute_ᶠuₕ³, precomputed_quantities.jl:473-476), the
+// filter sets u_3 = -u_h^3 / g^33 on the bottom and top faces, and the (u_3, u_3) block takes
+// dK/du_3 = (g^33 u_3)_f / 2 + CT3(u_h)_v / 2 (∂ᶜK_∂ᶠu₃, manual_sparse_jacobian.jl:754-756).
+// The (rho, u_h), (rho e_tot, u_h) and (u_3, u_h) blocks multiply R_u_h = 0 here.
+template <class FT, int G, int CM, bool HAT, class LV>
+__device__ __forceinline__ void newton_core(const DevParams<FT> &P, const ColGeo<FT> &Gm, const LV &L, int gl,
                                             FT dtg, const FT (&Hh)[5][CM], FT (&U)[5][CM], CSum<FT> (&ss)[3],
                                             bool &finite, FT (&iJc)[CM]) {
   const int Nv = L.Nv, Nf = L.Nf;
@@ -188,17 +276,30 @@ __device__ __forceinline__ void newton_core(const DevParams<FT> &P, const ColGeo
   // face geometry of faces r0 .. r0 + CM and g^33 of face r0 - 1
   Lev4<FT> LF[CM + 1];
 #pragma unroll
-  for (int k = 0; k <= CM; ++k) LF[k] = L.lf4[min(r0 + k, Nf - 1)];
-  const FT g33m = L.lf4[min(max(r0 - 1, 0), Nf - 1)].x;
-  // ---- filtered state: u_3 = 0 on the boundary faces
+  for (int k = 0; k <= CM; ++k) LF[k] = L.f4(min(r0 + k, Nf - 1));
+  const FT g33m = L.f4(min(max(r0 - 1, 0), Nf - 1)).x;
+  // halo: centre -1 and face -1 from the previous lane, face r0 + CM from the next lane
+  const FT hr = up<G>(U[0][CM - 1], 1), hu1 = up<G>(U[1][CM - 1], 1), hu2 = up<G>(U[2][CM - 1], 1);
+  // ---- filtered state: u_3 = 0 on the boundary faces (-u_h^3 / g^33 over terrain)
   FT u3[CM];
 #pragma unroll
   for (int k = 0; k < CM; ++k) {
     const int f = r0 + k;
-    u3[k] = (f == 0 || f >= Nv) ? FT(0) : U[4][k];
+    if constexpr (LV::TOPO) {
+      if (f == 0 || f == Nv) {
+        const int v = f == 0 ? 0 : Nv - 1;
+        const FT a1 = f == 0 ? U[1][k] : (k > 0 ? U[1][k > 0 ? k - 1 : 0] : hu1);
+        const FT a2 = f == 0 ? U[2][k] : (k > 0 ? U[2][k > 0 ? k - 1 : 0] : hu2);
+        FT g31, g32, phis;
+        L.ct(v, g31, g32, phis);
+        u3[k] = -(g31 * a1 + g32 * a2) / LF[k].x;
+      } else {
+        u3[k] = f > Nv ? FT(0) : U[4][k];
+      }
+    } else {
+      u3[k] = (f == 0 || f >= Nv) ? FT(0) : U[4][k];
+    }
   }
-  // halo: centre -1 and face -1 from the previous lane, face r0 + CM from the next lane
-  const FT hr = up<G>(U[0][CM - 1], 1), hu1 = up<G>(U[1][CM - 1], 1), hu2 = up<G>(U[2][CM - 1], 1);
   const FT he = up<G>(U[3][CM - 1], 1), h3 = up<G>(u3[CM - 1], 1);
   const FT n3 = down<G>(u3[0], 1);  // every lane shuffles; the column's last lane discards it
   const FT u3n = gl + 1 < G ? n3 : FT(0);
@@ -232,7 +333,12 @@ __device__ __forceinline__ void newton_core(const DevParams<FT> &P, const ColGeo
     const FT u3c = u3[k] * g33;
     const FT rJb = (prev.rJ + cur.rJ) / FT(2);
     const FT hb = (prev.h + cur.h) / FT(2);
-    F[k] = inner ? rJb * u3c : FT(0);
+    if constexpr (LV::TOPO) {
+      const FT uh3 = (prev.rJ * prev.ct3 + cur.rJ * cur.ct3) / (prev.rJ + cur.rJ);
+      F[k] = inner ? rJb * (uh3 + u3c) : FT(0);
+    } else {
+      F[k] = inner ? rJb * u3c : FT(0);
+    }
     Fh[k] = F[k] * hb;
     fr[k] = inner ? rJb * g33 : FT(0);
     fhb[k] = hb;
@@ -254,9 +360,15 @@ __device__ __forceinline__ void newton_core(const DevParams<FT> &P, const ColGeo
       ur1[k] = dtg * (-dpb * irb + buoy / FT(2));
       ue0[k] = dtg * (kap * irb);
       const FT u3cn = u3next * LF[k + 1].x;
-      uu0[k] = dtg * (-kap * ra * u3cPrev * (irb / FT(2)));
-      uu1[k] = dtg * (kap * (rbv - ra) * u3c * (irb / FT(2)) - beta) - FT(1);
-      uu2[k] = dtg * (kap * rbv * u3cn * (irb / FT(2)));
+      if constexpr (LV::TOPO) {
+        uu0[k] = dtg * (-kap * ra * (u3cPrev + prev.ct3) * (irb / FT(2)));
+        uu1[k] = dtg * (kap * (rbv * (u3c + cur.ct3) - ra * (u3c + prev.ct3)) * (irb / FT(2)) - beta) - FT(1);
+        uu2[k] = dtg * (kap * rbv * (u3cn + cur.ct3) * (irb / FT(2)));
+      } else {
+        uu0[k] = dtg * (-kap * ra * u3cPrev * (irb / FT(2)));
+        uu1[k] = dtg * (kap * (rbv - ra) * u3c * (irb / FT(2)) - beta) - FT(1);
+        uu2[k] = dtg * (kap * rbv * u3cn * (irb / FT(2)));
+      }
     } else {
       ur0[k] = ur1[k] = ue0[k] = uu0[k] = uu2[k] = FT(0);
       uu1[k] = f <= Nv ? -dtg * beta - FT(1) : FT(1);
@@ -343,15 +455,16 @@ __device__ __forceinline__ void newton_core(const DevParams<FT> &P, const ColGeo
     if (f >= Nv) { rho = FT(1); rhoe = FT(1); }
     U[0][k] = rho;
     U[3][k] = rhoe;
-    U[4][k] = (f == 0 || f >= Nv) ? FT(0) : u3[k] - x[k];
+    if constexpr (LV::TOPO) U[4][k] = (f == 0 || f == Nv) ? u3[k] : (f > Nv ? FT(0) : u3[k] - x[k]);
+    else U[4][k] = (f == 0 || f >= Nv) ? FT(0) : u3[k] - x[k];
   }
 }
 
 // Post-Newton van Leer minus central correction of rho e_tot
 // (correct_implicit_advection_tendency!, implicit_tendency.jl:322-339), added
 // as rhoe += dtgamma * corr.  U holds the Newton result (filtered u_3).
-template <class FT, int G, int CM>
-__device__ __forceinline__ void vanleer_correct(const DevParams<FT> &P, const ColGeo<FT> &Gm, const ColLev<FT> &L,
+template <class FT, int G, int CM, class LV>
+__device__ __forceinline__ void vanleer_correct(const DevParams<FT> &P, const ColGeo<FT> &Gm, const LV &L,
                                                 int gl, FT dtg, FT (&U)[5][CM], const FT (&iJc)[CM]) {
   const int Nv = L.Nv, Nf = L.Nf;
   const int r0 = gl * CM;
@@ -359,8 +472,8 @@ __device__ __forceinline__ void vanleer_correct(const DevParams<FT> &P, const Co
   const FT w3n = gl + 1 < G ? w3ns : FT(0);
   FT g33[CM + 1];
 #pragma unroll
-  for (int k = 0; k <= CM; ++k) g33[k] = L.lf4[min(r0 + k, Nf - 1)].x;
-  FT hh[CM], rJ[CM];
+  for (int k = 0; k <= CM; ++k) g33[k] = L.f4(min(r0 + k, Nf - 1)).x;
+  FT hh[CM], rJ[CM], ct[CM];
   {
     FT w3a[CM], w3b[CM], ga[CM], gb[CM];
     Cen<FT> cc[CM];
@@ -376,10 +489,16 @@ __device__ __forceinline__ void vanleer_correct(const DevParams<FT> &P, const Co
     for (int k = 0; k < CM; ++k) {
       hh[k] = cc[k].h;
       rJ[k] = cc[k].rJ;
+      ct[k] = cc[k].ct3;
     }
   }
   const FT hm2 = up<G>(hh[CM - 2], 1), hm1 = up<G>(hh[CM - 1], 1), rJm = up<G>(rJ[CM - 1], 1);
   const FT hp0 = down<G>(hh[0], 1), hp1 = down<G>(hh[1], 1), rJp = down<G>(rJ[0], 1);
+  FT ctm = FT(0), ctp = FT(0);
+  if constexpr (LV::TOPO) {
+    ctm = up<G>(ct[CM - 1], 1);
+    ctp = down<G>(ct[0], 1);
+  }
   FT fup[CM + 1], fcen[CM + 1];
 #pragma unroll
   for (int k = 0; k <= CM; ++k) {
@@ -392,7 +511,12 @@ __device__ __forceinline__ void vanleer_correct(const DevParams<FT> &P, const Co
     const FT rA = k >= 1 ? rJ[k - 1] : rJm;
     const FT r0v = k < CM ? rJ[k] : rJp;
     const FT wk = k < CM ? U[4][k] : w3n;
-    const FT u = wk * g33[k];
+    FT u = wk * g33[k];
+    if constexpr (LV::TOPO) {
+      // u^3 = ᶠwinterp(rho J, CT3(u_h)) + g^33 u_3
+      const FT cA = k >= 1 ? ct[k >= 1 ? k - 1 : 0] : ctm, c0 = k < CM ? ct[k < CM ? k : 0] : ctp;
+      u += (rA * cA + r0v * c0) / (rA + r0v);
+    }
     const FT rJb = (rA + r0v) / FT(2);
     const bool near = f == 1 || f == Nv - 1;
     fup[k] = inner ? rJb * vanleer_g(u, hA2, hA1, h0, hP1, near, P.dt_model) : FT(0);

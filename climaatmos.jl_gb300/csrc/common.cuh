@@ -43,6 +43,15 @@ struct DevParams {
   const int *goff, *gcopy;
   const FT *gw, *ecov, *econ;  // ecov/econ: [Nh*16][6]
   int *status;
+  // Terrain-following levels (topo = 1): per node z_s and its xi^1, xi^2 derivatives in the
+  // element ([Nh][TG_N][16]); per level the warp records {zeta, b, dzeta, db} of the centres
+  // (ltc [Nv]) and faces (ltf [Nf]), so that a point's height is zeta + z_s b and its layer
+  // thickness dzeta + z_s db; 1 / R; the Rayleigh sponge of each point, beta = alpha
+  // sin^2(spg_k (z - spg_zd)) above spg_zd (spg_k = pi / (2 (z_max - z_d))).
+  int topo;
+  const FT *tgeo;
+  const Lev4<FT> *ltc, *ltf;
+  FT iR, spg_auh, spg_aw, spg_zd, spg_k;
 };
 
 // ---------------------------------------------------------------- math

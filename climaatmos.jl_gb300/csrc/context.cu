@@ -36,7 +36,7 @@ struct ImplBase {
 template <class FT>
 struct Impl : ImplBase {
   DevParams<FT> P{};
-  DevBuf hgeo, levc, levf, lc4, lf4, lr4, goff, gcopy, gw, ecov, econ, status;
+  DevBuf hgeo, levc, levf, lc4, lf4, lr4, goff, gcopy, gw, ecov, econ, status, tgeo, ltc, ltf;
   DevBuf lap, U, Te[4], Ti[4], jac, rnorm, partials, sums, rsum;
   size_t NC = 0, NF = 0, NR = 0;  // centre, face and reduced-centre element counts
   int nsum_blocks = 0;
@@ -185,6 +185,11 @@ int create_impl(gb_ctx *ctx) {
   if ((r = upload<FT>(ctx, I->gw, g.grp_w))) return r;
   if ((r = upload<FT>(ctx, I->ecov, g.ecov))) return r;
   if ((r = upload<FT>(ctx, I->econ, g.econ))) return r;
+  if (g.topo) {
+    if ((r = upload<FT>(ctx, I->tgeo, g.tgeo))) return r;
+    if ((r = upload<FT>(ctx, I->ltc, g.ltc))) return r;
+    if ((r = upload<FT>(ctx, I->ltf, g.ltf))) return r;
+  }
   if ((r = alloc(ctx, I->status, 16))) return r;
   const int Nh = g.Nh, Nv = g.Nv, Nf = Nv + 1;
   I->NC = (size_t)Nh * 4 * NN * Nv;
@@ -231,6 +236,15 @@ int create_impl(gb_ctx *ctx) {
   P.goff = (const int *)I->goff.p; P.gcopy = (const int *)I->gcopy.p; P.gw = (const FT *)I->gw.p;
   P.ecov = (const FT *)I->ecov.p; P.econ = (const FT *)I->econ.p;
   P.status = (int *)I->status.p;
+  P.topo = g.topo ? 1 : 0;
+  P.tgeo = (const FT *)I->tgeo.p;
+  P.ltc = (const Lev4<FT> *)I->ltc.p;
+  P.ltf = (const Lev4<FT> *)I->ltf.p;
+  P.iR = (FT)(1.0 / c.radius);
+  P.spg_auh = (FT)c.alpha_uh;
+  P.spg_aw = (FT)c.alpha_w;
+  P.spg_zd = (FT)c.sponge_zd;
+  P.spg_k = (FT)(M_PI / (2.0 * (c.z_max - c.sponge_zd)));
   ars343(I->ae, I->ai, I->be, I->bi);
   I->stiffly_accurate = true;
   for (int j = 0; j < 4; ++j) I->stiffly_accurate = I->stiffly_accurate && I->bi[j] == I->ai[3][j];
@@ -240,6 +254,11 @@ int create_impl(gb_ctx *ctx) {
   if (passB_smem<FT>(Nv) > (size_t)optin)
     return fail(ctx, GB_ERR_ARG, "z_elem too large for the element-slab kernels at this precision (shared memory)");
   configure_se<FT>(Nv);
+  if (g.topo) {
+    if (topo_smem<FT>(Nv) > (size_t)optin)
+      return fail(ctx, GB_ERR_ARG, "z_elem too large for the terrain slab kernels at this precision (shared memory)");
+    configure_topo<FT>(Nv);
+  }
   CK(cudaGetLastError());
   return GB_OK;
 }
@@ -271,6 +290,13 @@ template <class FT>
 int remaining_tendency_t(gb_ctx *ctx, gb_fieldvec Yt, gb_fieldvec Y) {
   Impl<FT> *I = impl<FT>(ctx);
   poison_scratch<FT>(ctx, ctx->stream);
+  if (I->P.topo) {
+    launch_topo_passA<FT>(I->P, (const FT *)Y.c, (const FT *)Y.f, (FT *)I->lap.p, ctx->stream);
+    launch_dss<FT>(I->P, (FT *)I->lap.p, nullptr, ctx->stream);
+    launch_topo_passB<FT>(I->P, (const FT *)Y.c, (const FT *)Y.f, (const FT *)I->lap.p, (FT *)Yt.c, (FT *)Yt.f,
+                          ctx->stream);
+    return check_launch(ctx);
+  }
   launch_passA<FT>(I->P, (const FT *)Y.c, (const FT *)Y.f, (FT *)I->lap.p, ctx->stream);
   launch_dss<FT>(I->P, (FT *)I->lap.p, nullptr, ctx->stream);
   launch_passB<FT>(I->P, (const FT *)Y.c, (const FT *)Y.f, (const FT *)I->lap.p, (FT *)Yt.c, (FT *)Yt.f, ctx->stream);
@@ -319,9 +345,71 @@ FinArgs<FT> fin_args(const Impl<FT> *I, FT dt, FT *const (&tc)[4], FT *const (&t
 // Newton iteration per implicit stage); T_exp_j is DSSed once right after it
 // is computed, so every stage state assembled from u_n (continuous), DSSed
 // explicit tendencies and column-local implicit tendencies is continuous.
+// The step over terrain-following levels: the terrain slab kernels for the explicit
+// tendencies; the implicit tendencies are DSSed too (a column's implicit tendency depends on
+// its element's slopes through u_h^3, so collocated copies differ, and the reference DSSes
+// every assembled stage state); the unfolded final combination, its DSS and the impenetrable
+// filter u_3 = -u_h^3 / g^33 of the new state (the reference's dss! then cache!).
+template <class FT>
+void enqueue_step_topo(gb_ctx *ctx, FT *Yc, FT *Yf, double dt_, cudaStream_t s) {
+  Impl<FT> *I = impl<FT>(ctx);
+  const DevParams<FT> &P = I->P;
+  const FT dt = (FT)dt_;
+  FT *lap = (FT *)I->lap.p;
+  auto tec = [&](int j) { return (FT *)I->Te[j].p; };
+  auto tef = [&](int j) { return (FT *)I->Te[j].p + I->NC; };
+  auto tic = [&](int j) { return (FT *)I->Ti[j].p; };
+  auto tif = [&](int j) { return (FT *)I->Ti[j].p + I->NR; };
+  FT *Uc = (FT *)I->U.p, *Uf = Uc + I->NC;
+  poison_scratch<FT>(ctx, s);
+  launch_topo_passA<FT>(P, Yc, Yf, lap, s);
+  launch_dss<FT>(P, lap, nullptr, s);
+  launch_topo_passB<FT>(P, Yc, Yf, lap, tec(0), tef(0), s);
+  launch_dss<FT>(P, tec(0), tef(0), s);
+  for (int i = 1; i < 4; ++i) {
+    StageArgs<FT> A{};
+    A.un_c = Yc; A.un_f = Yf;
+    A.nsrc = i;
+    for (int j = 0; j < i; ++j) {
+      A.te_c[j] = I->ae[i][j] != 0 ? tec(j) : nullptr;
+      A.te_f[j] = I->ae[i][j] != 0 ? tef(j) : nullptr;
+      A.ce[j] = dt * (FT)I->ae[i][j];
+      A.ti_c[j] = I->ai[i][j] != 0 ? tic(j) : nullptr;
+      A.ti_f[j] = I->ai[i][j] != 0 ? tif(j) : nullptr;
+      A.ci[j] = dt * (FT)I->ai[i][j];
+    }
+    A.U_c = Uc; A.U_f = Uf;
+    A.Ti_c = tic(i); A.Ti_f = tif(i);
+    A.dtg = dt * (FT)I->ai[i][i];
+    A.idtg = (FT)1 / A.dtg;
+    A.rnorm = (double *)I->rnorm.p;
+    A.first = i == 1;
+    launch_column_stage<FT>(P, A, s);
+    launch_dss_reduced<FT>(P, tic(i), tif(i), s);
+    launch_topo_passA<FT>(P, Uc, Uf, lap, s);
+    launch_dss<FT>(P, lap, nullptr, s);
+    launch_topo_passB<FT>(P, Uc, Uf, lap, tec(i), tef(i), s);
+    launch_dss<FT>(P, tec(i), tef(i), s);
+  }
+  StageArgs<FT> A{};
+  A.nsrc = 4;
+  for (int j = 0; j < 4; ++j) {
+    A.te_c[j] = I->be[j] != 0 ? tec(j) : nullptr;
+    A.te_f[j] = I->be[j] != 0 ? tef(j) : nullptr;
+    A.ce[j] = dt * (FT)I->be[j];
+    A.ti_c[j] = I->bi[j] != 0 ? tic(j) : nullptr;
+    A.ti_f[j] = I->bi[j] != 0 ? tif(j) : nullptr;
+    A.ci[j] = dt * (FT)I->bi[j];
+  }
+  launch_final<FT>(P, A, Yc, Yf, s);
+  launch_dss<FT>(P, Yc, Yf, s);
+  launch_topo_filter<FT>(P, Yc, Yf, s);
+}
+
 template <class FT>
 void enqueue_step(gb_ctx *ctx, FT *Yc, FT *Yf, double dt_, cudaStream_t s) {
   Impl<FT> *I = impl<FT>(ctx);
+  if (I->P.topo) return enqueue_step_topo<FT>(ctx, Yc, Yf, dt_, s);
   const DevParams<FT> &P = I->P;
   const FT dt = (FT)dt_;
   FT *lap = (FT *)I->lap.p;
@@ -504,6 +592,8 @@ int time_kernel_t(gb_ctx *ctx, int kernel, gb_fieldvec Y, int reps, double *ms) 
   // reverse kernels: cotangent inputs are the tendency and Laplacian buffers of
   // the last step (finite values), outputs the reverse-mode scratch
   const bool rev = kernel >= GB_K_PASSA_VJP && kernel <= GB_K_DSS_T;
+  if (P.topo && (rev || kernel == GB_K_PASSB_FINAL))
+    return fail(ctx, GB_ERR_ARG, "gb_time_kernel: the reverse kernels and the folded final pass are not built over terrain");
   if (rev) {
     int r = ensure_adjoint<FT>(ctx);
     if (r) return r;
@@ -520,8 +610,14 @@ int time_kernel_t(gb_ctx *ctx, int kernel, gb_fieldvec Y, int reps, double *ms) 
   FT *Tibs[4] = {nullptr, nullptr, nullptr, nullptr};
   auto launch = [&]() {
     switch (kernel) {
-      case GB_K_PASSA: launch_passA<FT>(P, Yc, Yf, lap, s); break;
-      case GB_K_PASSB: launch_passB<FT>(P, Yc, Yf, lap, Tc, Tf, s); break;
+      case GB_K_PASSA:
+        if (P.topo) launch_topo_passA<FT>(P, Yc, Yf, lap, s);
+        else launch_passA<FT>(P, Yc, Yf, lap, s);
+        break;
+      case GB_K_PASSB:
+        if (P.topo) launch_topo_passB<FT>(P, Yc, Yf, lap, Tc, Tf, s);
+        else launch_passB<FT>(P, Yc, Yf, lap, Tc, Tf, s);
+        break;
       case GB_K_COLUMN: launch_column_stage<FT>(P, A, s); break;
       case GB_K_DSS: launch_dss<FT>(P, Yc, Yf, s); break;
       case GB_K_PASSA_VJP: launch_passA_vjp<FT>(P, Yc, Yf, lap, Ubc, Ubf, I->adj->grid, s); break;
@@ -1063,6 +1159,12 @@ bool fv_ok(gb_fieldvec v) { return v.c && v.f && aligned(v.c) && aligned(v.f); }
     if (!(ctx)) return GB_ERR_ARG;                           \
   } while (0)
 
+// Entry points not built for terrain-following levels refuse a terrain context.
+#define NO_TERRAIN(ctx, what)                                                                       \
+  do {                                                                                              \
+    if ((ctx)->geo.topo) return fail((ctx), GB_ERR_ARG, what " is not available over terrain");   \
+  } while (0)
+
 }  // namespace
 
 extern "C" {
@@ -1075,9 +1177,11 @@ int gb_sizes(const gb_config *cfg, size_t *n_center, size_t *n_face, int *n_grou
   const size_t Nh = 6 * (size_t)cfg->h_elem * cfg->h_elem;
   if (n_center) *n_center = Nh * 4 * NN * cfg->z_elem;
   if (n_face) *n_face = Nh * NN * (cfg->z_elem + 1);
-  if (n_groups || n_copies) {
+  if (n_groups || n_copies || cfg->z_surface) {
     HostGeometry g;
     build_geometry(*cfg, g);
+    // over terrain the warped levels must not cross
+    if (!build_terrain_tables(*cfg, g, &why)) return GB_ERR_ARG;
     if (n_groups) *n_groups = (int)g.grp_off.size() - 1;
     if (n_copies) *n_copies = (int)g.grp_copy.size();
   }
@@ -1115,9 +1219,14 @@ int gb_ctx_create(const gb_config *cfg, gb_ctx **out) {
   int r;
   try {
     build_geometry(*cfg, ctx->geo);
-    // the layout is now in the geometry tables; the caller's arrays are not kept
+    if (!build_terrain_tables(*cfg, ctx->geo, &why)) {
+      delete ctx;
+      return GB_ERR_ARG;
+    }
+    // the layout and the surface are now in the geometry tables; the caller's arrays are not kept
     ctx->cfg.elem_map = nullptr;
     ctx->cfg.elem_orient = nullptr;
+    ctx->cfg.z_surface = nullptr;
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) { delete ctx; return GB_ERR_CUDA; }
     r = cfg->ft_bytes == 8 ? create_impl<double>(ctx) : create_impl<float>(ctx);
@@ -1160,6 +1269,11 @@ int gb_set_precomputed_quantities(gb_ctx *ctx, gb_fieldvec Y, double t) {
   GUARD(ctx);
   (void)t;
   if (!fv_ok(Y)) return fail(ctx, GB_ERR_ARG, "Y: null or misaligned pointer");
+  if (ctx->geo.topo) {
+    if (ctx->cfg.ft_bytes == 8) launch_topo_filter<double>(impl<double>(ctx)->P, (const double *)Y.c, (double *)Y.f, ctx->stream);
+    else launch_topo_filter<float>(impl<float>(ctx)->P, (const float *)Y.c, (float *)Y.f, ctx->stream);
+    return check_launch(ctx);
+  }
   if (ctx->cfg.ft_bytes == 8) launch_bc_filter<double>(impl<double>(ctx)->P, (double *)Y.f, ctx->stream);
   else launch_bc_filter<float>(impl<float>(ctx)->P, (float *)Y.f, ctx->stream);
   return check_launch(ctx);
@@ -1176,6 +1290,7 @@ int gb_remaining_tendency(gb_ctx *ctx, gb_fieldvec Yt, gb_fieldvec Y, double t) 
 int gb_implicit_tendency(gb_ctx *ctx, gb_fieldvec Yt, gb_fieldvec Y, double t) {
   GB_RANGE();
   GUARD(ctx);
+  NO_TERRAIN(ctx, "gb_implicit_tendency");
   (void)t;
   if (!fv_ok(Y) || !fv_ok(Yt)) return fail(ctx, GB_ERR_ARG, "null or misaligned pointer");
   return DISPATCH(ctx, column_hook_t, ctx, (int)COL_IMPLICIT, Yt, Y, 0.0);
@@ -1184,6 +1299,7 @@ int gb_implicit_tendency(gb_ctx *ctx, gb_fieldvec Yt, gb_fieldvec Y, double t) {
 int gb_update_jacobian(gb_ctx *ctx, gb_fieldvec Y, double dtgamma, double t) {
   GB_RANGE();
   GUARD(ctx);
+  NO_TERRAIN(ctx, "gb_update_jacobian");
   (void)t;
   if (!fv_ok(Y)) return fail(ctx, GB_ERR_ARG, "null or misaligned pointer");
   gb_fieldvec none{nullptr, nullptr};
@@ -1193,6 +1309,7 @@ int gb_update_jacobian(gb_ctx *ctx, gb_fieldvec Y, double dtgamma, double t) {
 int gb_ldiv(gb_ctx *ctx, gb_fieldvec dY, gb_fieldvec R) {
   GB_RANGE();
   GUARD(ctx);
+  NO_TERRAIN(ctx, "gb_ldiv");
   if (!fv_ok(dY) || !fv_ok(R)) return fail(ctx, GB_ERR_ARG, "null or misaligned pointer");
   return DISPATCH(ctx, column_hook_t, ctx, (int)COL_LDIV, dY, R, 0.0);
 }
@@ -1200,6 +1317,7 @@ int gb_ldiv(gb_ctx *ctx, gb_fieldvec dY, gb_fieldvec R) {
 int gb_correct_implicit_advection_tendency(gb_ctx *ctx, gb_fieldvec Yt, gb_fieldvec Y, double t) {
   GB_RANGE();
   GUARD(ctx);
+  NO_TERRAIN(ctx, "gb_correct_implicit_advection_tendency");
   (void)t;
   if (!fv_ok(Y) || !fv_ok(Yt)) return fail(ctx, GB_ERR_ARG, "null or misaligned pointer");
   return DISPATCH(ctx, column_hook_t, ctx, (int)COL_POSTIMP, Yt, Y, 0.0);
@@ -1242,6 +1360,7 @@ int gb_newton_residual(gb_ctx *ctx, double out[3]) {
 int gb_jacobian_solve_noalloc(gb_ctx *ctx, gb_fieldvec dY, gb_fieldvec Y, gb_fieldvec R, double dtgamma) {
   GB_RANGE();
   GUARD(ctx);
+  NO_TERRAIN(ctx, "gb_jacobian_solve_noalloc");
   if (!fv_ok(dY) || !fv_ok(Y) || !fv_ok(R)) return fail(ctx, GB_ERR_ARG, "null or misaligned pointer");
   return DISPATCH(ctx, jacobian_solve_noalloc_t, ctx, dY, Y, R, dtgamma);
 }
@@ -1255,6 +1374,7 @@ int gb_dss_transpose(gb_ctx *ctx, gb_fieldvec X) {
 int gb_remaining_tendency_vjp(gb_ctx *ctx, gb_fieldvec Ybar, gb_fieldvec Tbar, gb_fieldvec Y, double t,
                               double dparams[2]) {
   GB_RANGE();
+  if (ctx && ctx->geo.topo) return fail(ctx, GB_ERR_ARG, "gb_remaining_tendency_vjp is not available over terrain");
   (void)t;
   if (!ctx || !fv_ok(Ybar) || !fv_ok(Tbar) || !fv_ok(Y)) return GB_ERR_ARG;
   return ctx->cfg.ft_bytes == 8 ? remaining_tendency_vjp_t<double>(ctx, Ybar, Tbar, Y, dparams)
@@ -1271,6 +1391,7 @@ int gb_implicit_stage(gb_ctx *ctx, gb_fieldvec U, gb_fieldvec Timp, gb_fieldvec 
 int gb_implicit_stage_vjp(gb_ctx *ctx, gb_fieldvec Uhat_bar, gb_fieldvec Ubar, gb_fieldvec Timp_bar, gb_fieldvec Uhat,
                           double dtgamma, double dparams[2]) {
   GB_RANGE();
+  if (ctx && ctx->geo.topo) return fail(ctx, GB_ERR_ARG, "gb_implicit_stage_vjp is not available over terrain");
   if (!ctx || !Uhat_bar.c || !Ubar.c || !Timp_bar.c || !Uhat.c || !(dtgamma > 0)) return GB_ERR_ARG;
   return ctx->cfg.ft_bytes == 8 ? implicit_stage_vjp_t<double>(ctx, Uhat_bar, Ubar, Timp_bar, Uhat, dtgamma, dparams)
                                 : implicit_stage_vjp_t<float>(ctx, Uhat_bar, Ubar, Timp_bar, Uhat, dtgamma, dparams);
@@ -1278,6 +1399,7 @@ int gb_implicit_stage_vjp(gb_ctx *ctx, gb_fieldvec Uhat_bar, gb_fieldvec Ubar, g
 
 int gb_step_vjp(gb_ctx *ctx, gb_fieldvec Ybar, gb_fieldvec Y, double t, double dt, double dparams[2]) {
   GB_RANGE();
+  if (ctx && ctx->geo.topo) return fail(ctx, GB_ERR_ARG, "gb_step_vjp is not available over terrain");
   (void)t;
   if (!ctx || !fv_ok(Ybar) || !fv_ok(Y) || !(dt > 0)) return GB_ERR_ARG;
   return ctx->cfg.ft_bytes == 8 ? step_vjp_t<double>(ctx, Ybar, Y, dt, dparams)
@@ -1286,6 +1408,7 @@ int gb_step_vjp(gb_ctx *ctx, gb_fieldvec Ybar, gb_fieldvec Y, double t, double d
 
 int gb_adjoint_forward(gb_ctx *ctx, gb_fieldvec Y, double t0, double dt, int nsteps, int checkpoint_every) {
   GB_RANGE();
+  if (ctx && ctx->geo.topo) return fail(ctx, GB_ERR_ARG, "gb_adjoint_forward is not available over terrain");
   (void)t0;
   if (!ctx || !fv_ok(Y) || !(dt > 0) || nsteps < 1 || checkpoint_every < 1) return GB_ERR_ARG;
   return ctx->cfg.ft_bytes == 8 ? adjoint_forward_t<double>(ctx, Y, dt, nsteps, checkpoint_every)
@@ -1294,6 +1417,7 @@ int gb_adjoint_forward(gb_ctx *ctx, gb_fieldvec Y, double t0, double dt, int nst
 
 int gb_adjoint_reverse(gb_ctx *ctx, gb_fieldvec Ybar, double dparams[2], size_t *peak_bytes) {
   GB_RANGE();
+  if (ctx && ctx->geo.topo) return fail(ctx, GB_ERR_ARG, "gb_adjoint_reverse is not available over terrain");
   if (!ctx || !fv_ok(Ybar)) return GB_ERR_ARG;
   return ctx->cfg.ft_bytes == 8 ? adjoint_reverse_t<double>(ctx, Ybar, dparams, peak_bytes)
                                 : adjoint_reverse_t<float>(ctx, Ybar, dparams, peak_bytes);

@@ -141,6 +141,27 @@ bool validate_config(const gb_config &c, const char **why) {
     *why = "test_dycore_consistency must be 0 or 1";
     return false;
   }
+  if (c.z_surface) {
+    if (c.warp != 0 && c.warp != 1) { *why = "warp must be 0 (linear) or 1 (SLEVE)"; return false; }
+    if (c.warp == 1 && !(c.sleve_eta > 0 && c.sleve_eta <= 1 && c.sleve_s > 0)) {
+      *why = "SLEVE warp: sleve_eta must be in (0, 1] and sleve_s > 0";
+      return false;
+    }
+    if (c.held_suarez) { *why = "the Held-Suarez forcing is not available over terrain"; return false; }
+    const size_t H = (size_t)6 * c.h_elem * c.h_elem * 16;
+    double zmx = 0;
+    for (size_t q = 0; q < H; ++q) {
+      if (!std::isfinite(c.z_surface[q]) || !(c.z_surface[q] > -0.5 * c.z_max)) {
+        *why = "z_surface: a surface elevation is not finite or lies below -z_max / 2";
+        return false;
+      }
+      zmx = std::max(zmx, c.z_surface[q]);
+    }
+    if (c.warp == 1 && !(c.sleve_s * c.z_max > zmx)) {
+      *why = "SLEVE warp: sleve_s * z_max must exceed the highest surface (topography.jl:295-297)";
+      return false;
+    }
+  }
   if ((c.elem_map == nullptr) != (c.elem_orient == nullptr)) {
     *why = "elem_map and elem_orient must both be given or both be NULL";
     return false;
@@ -353,6 +374,79 @@ void build_geometry(const gb_config &c, HostGeometry &g) {
     g.levf[LF_G33 * Nf + k] = 1.0 / (g.dzf[k] * g.dzf[k]);
     g.levf[LF_SPG * Nf + k] = beta_sponge(g.zf[k], c.sponge_zd, c.z_max, 1.0);
   }
+}
+
+double warp_factor(const gb_config &c, double zeta) {
+  if (c.warp == 0) return 1.0 - zeta / c.z_max;
+  const double eta = zeta / c.z_max;
+  if (eta > c.sleve_eta) return 0.0;
+  return std::sinh((c.sleve_eta - eta) / (c.sleve_s * c.sleve_eta)) / std::sinh(1.0 / c.sleve_s);
+}
+
+// Terrain tables of build_geometry (gb_config.z_surface given): the per-node surface and its
+// element-local GLL derivatives (in the caller's element frame, where the kernels differentiate),
+// and the per-level warp records.  Returns false if a warped layer would have no thickness.
+static bool build_terrain(const gb_config &c, HostGeometry &g, const char **why) {
+  const int Nh = g.Nh, Nv = g.Nv, Nf = Nv + 1;
+  g.topo = true;
+  g.tgeo.assign((size_t)Nh * TG_N * NN, 0.0);
+  for (int e = 0; e < Nh; ++e) {
+    const double *z = c.z_surface + (size_t)e * NN;
+    double *o = &g.tgeo[(size_t)e * TG_N * NN];
+    for (int j = 0; j < NQ; ++j)
+      for (int i = 0; i < NQ; ++i) {
+        double a = 0, b = 0;
+        for (int k = 0; k < NQ; ++k) {
+          a += g.D[i][k] * z[k + NQ * j];
+          b += g.D[j][k] * z[i + NQ * k];
+        }
+        const int n = i + NQ * j;
+        o[TG_ZS * NN + n] = z[n];
+        o[TG_D1 * NN + n] = a;
+        o[TG_D2 * NN + n] = b;
+      }
+  }
+  std::vector<double> bf(Nf), bc(Nv);
+  for (int k = 0; k < Nf; ++k) bf[k] = warp_factor(c, g.zf[k]);
+  for (int v = 0; v < Nv; ++v) bc[v] = (bf[v] + bf[v + 1]) / 2;
+  g.ltc.assign((size_t)4 * Nv, 0.0);
+  g.ltf.assign((size_t)4 * Nf, 0.0);
+  for (int v = 0; v < Nv; ++v) {
+    g.ltc[4 * v + 0] = g.zc[v];
+    g.ltc[4 * v + 1] = bc[v];
+    g.ltc[4 * v + 2] = g.dzc[v];
+    g.ltc[4 * v + 3] = bf[v + 1] - bf[v];
+  }
+  for (int k = 0; k < Nf; ++k) {
+    const int v = k == 0 ? 0 : (k == Nv ? Nv - 1 : -1);
+    g.ltf[4 * k + 0] = g.zf[k];
+    g.ltf[4 * k + 1] = bf[k];
+    g.ltf[4 * k + 2] = g.dzf[k];
+    g.ltf[4 * k + 3] = v >= 0 ? g.ltc[4 * v + 3] : bc[k] - bc[k - 1];
+  }
+  // every warped centre and face keeps a positive thickness
+  for (size_t q = 0; q < (size_t)Nh * NN; ++q) {
+    const double zs = c.z_surface[q];
+    for (int v = 0; v < Nv; ++v)
+      if (!(g.ltc[4 * v + 2] + zs * g.ltc[4 * v + 3] > 0)) {
+        *why = "z_surface: the terrain-following levels cross (a layer of non-positive thickness)";
+        return false;
+      }
+    for (int k = 0; k < Nf; ++k)
+      if (!(g.ltf[4 * k + 2] + zs * g.ltf[4 * k + 3] > 0)) {
+        *why = "z_surface: the terrain-following levels cross (a layer of non-positive thickness)";
+        return false;
+      }
+  }
+  return true;
+}
+
+bool build_terrain_tables(const gb_config &c, HostGeometry &g, const char **why) {
+  g.topo = false;
+  g.tgeo.clear();
+  g.ltc.clear();
+  g.ltf.clear();
+  return c.z_surface ? build_terrain(c, g, why) : true;
 }
 
 bool match_elements(const gb_config &c, const double *xyz, int *elem_map, int *elem_orient, const char **why) {

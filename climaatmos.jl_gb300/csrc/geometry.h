@@ -21,6 +21,11 @@ enum LevC { LC_Z = 0, LC_R2, LC_DZ, LC_PHI, LC_BETA, LC_IR2, LC_IDZ, LC_SPG, LC_
 // Per-level face quantities ([q][Nv+1]).
 enum LevF { LF_Z = 0, LF_R2, LF_DZ, LF_RINV, LF_BETA, LF_DPHI, LF_IR2, LF_IDZ, LF_G33, LF_SPG, LF_N };
 
+// Per-node terrain quantities ([elem][q][node], terrain-following levels only): the surface
+// elevation z_s and its derivatives along xi^1 and xi^2 in the element (the GLL derivative
+// matrix applied to the element's 16 nodal values), padded to four rows.
+enum TGeo { TG_ZS = 0, TG_D1, TG_D2, TG_PAD, TG_N };
+
 struct HostGeometry {
   int h = 0, Nh = 0, Nv = 0;
   double R = 0;
@@ -32,7 +37,22 @@ struct HostGeometry {
   std::vector<double> hgeo;  // [Nh][HG_N][16]
   std::vector<double> levc;  // [LC_N][Nv]
   std::vector<double> levf;  // [LF_N][Nv+1]
+  // terrain-following levels: z = zeta + z_s b(zeta) per point.  ltc[v] = {zeta_c, b_c,
+  // dzeta_c, db_c} (the centre midway between warped faces: b_c the mean of its faces' b,
+  // the thickness dzeta_c + z_s db_c), ltf[k] = {zeta_f, b_f, dzeta_f, db_f} (the face's
+  // distance between centres, the adjacent thickness on the boundary faces).
+  bool topo = false;
+  std::vector<double> tgeo;  // [Nh][TG_N][16]
+  std::vector<double> ltc;   // [Nv][4]
+  std::vector<double> ltf;   // [Nv+1][4]
 };
+
+// The warp factor b(zeta) of the terrain-following levels (gb_config.warp).
+double warp_factor(const gb_config &cfg, double zeta);
+// The terrain tables (tgeo, ltc, ltf) of a built geometry when cfg.z_surface is given (the
+// surface in the caller's element and node order); false, with a message, if the warped
+// levels cross.
+bool build_terrain_tables(const gb_config &cfg, HostGeometry &g, const char **why);
 
 // Returns false (with a message) on an invalid configuration.
 bool validate_config(const gb_config &cfg, const char **why);

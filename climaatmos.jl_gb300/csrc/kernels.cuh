@@ -139,6 +139,16 @@ template <class FT> void launch_global_sums(const DevParams<FT> &P, const FT *Yc
 template <class FT> void launch_reduce_rnorm(const double *rnorm, int ncols, double *out, cudaStream_t s);
 template <class FT> void launch_accum_slots(const double *part, int n, double *acc, cudaStream_t s);
 
+// ---- terrain-following levels (kernels_topo.cu)
+template <class FT> size_t topo_smem(int Nv);
+template <class FT> void configure_topo(int Nv);
+template <class FT> void launch_topo_passA(const DevParams<FT> &P, const FT *Yc, const FT *Yf, FT *L, cudaStream_t s);
+template <class FT> void launch_topo_passB(const DevParams<FT> &P, const FT *Yc, const FT *Yf, const FT *L, FT *Tc, FT *Tf, cudaStream_t s);
+// u_3 = -u_h^3 / g^33 on the bottom and top faces of every column (reads u_h of Yc)
+template <class FT> void launch_topo_filter(const DevParams<FT> &P, const FT *Yc, FT *Yf, cudaStream_t s);
+// DSS of the reduced implicit tendencies ([Nh][2][16][Nv] centres, faces)
+template <class FT> void launch_dss_reduced(const DevParams<FT> &P, FT *C, FT *F, cudaStream_t s);
+
 // Shared memory needed by the slab kernels with single input buffers (the
 // minimum; double buffering is used when it fits).
 template <class FT> size_t passA_smem(int Nv);

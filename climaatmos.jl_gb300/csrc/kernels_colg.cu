@@ -15,6 +15,7 @@
 // The column arithmetic is the shared core in colcore.cuh.
 #include <cstdio>
 #include <cstdlib>
+#include <type_traits>
 
 #include "colcore.cuh"
 
@@ -52,7 +53,8 @@ __device__ __forceinline__ void stage_accumulate<float, 2>(float (&H)[5][2], con
   }
 }
 
-template <class FT, int G, int CM, int STG, int MINB>
+// TOPO: terrain-following levels (the column's own metric, col::ColLevT).
+template <class FT, int G, int CM, int STG, int MINB, bool TOPO>
 __global__ void __launch_bounds__(CG_THREADS, MINB) k_col_stage_g(DevParams<FT> P, StageArgs<FT> A) {
   const int lane = threadIdx.x & 31, gl = lane % G;
   const int col0 = (blockIdx.x * (CG_THREADS / 32) + (threadIdx.x >> 5)) * (32 / G) + lane / G;
@@ -112,7 +114,10 @@ __global__ void __launch_bounds__(CG_THREADS, MINB) k_col_stage_g(DevParams<FT> 
     if (v >= Nf) H[4][k] = FT(0);
   }
   // ---- one Newton iteration from U = U^, then the post-Newton correction
-  const col::ColLev<FT> L{P.lc4, P.lf4, P.lr4, Nv, Nf};
+  using LV = std::conditional_t<TOPO, col::ColLevT<FT>, col::ColLev<FT>>;
+  LV L;
+  if constexpr (TOPO) L.load(P, e, n);
+  else L = col::ColLev<FT>{P.lc4, P.lf4, P.lr4, Nv, Nf};
   FT U[5][CM];
 #pragma unroll
   for (int c = 0; c < 5; ++c)
@@ -153,15 +158,22 @@ __global__ void __launch_bounds__(CG_THREADS, MINB) k_col_stage_g(DevParams<FT> 
   if (lane == 0 && !finite) atomicOr(P.status, ST_NONFINITE);
 }
 
-template <class FT, int G, int CM, int MINB>
-void launch_g(const DevParams<FT> &P, const StageArgs<FT> &A, cudaStream_t s) {
+template <class FT, int G, int CM, int MINB, bool TOPO>
+void launch_gt(const DevParams<FT> &P, const StageArgs<FT> &A, cudaStream_t s) {
   const int ncols = P.Nh * NN, per_cta = (CG_THREADS / 32) * (32 / G);
   const int grid = (ncols + per_cta - 1) / per_cta;
   switch (A.nsrc) {
-    case 1: k_col_stage_g<FT, G, CM, 1, MINB><<<grid, CG_THREADS, 0, s>>>(P, A); break;
-    case 2: k_col_stage_g<FT, G, CM, 2, MINB><<<grid, CG_THREADS, 0, s>>>(P, A); break;
-    default: k_col_stage_g<FT, G, CM, 3, MINB><<<grid, CG_THREADS, 0, s>>>(P, A); break;
+    case 1: k_col_stage_g<FT, G, CM, 1, MINB, TOPO><<<grid, CG_THREADS, 0, s>>>(P, A); break;
+    case 2: k_col_stage_g<FT, G, CM, 2, MINB, TOPO><<<grid, CG_THREADS, 0, s>>>(P, A); break;
+    default: k_col_stage_g<FT, G, CM, 3, MINB, TOPO><<<grid, CG_THREADS, 0, s>>>(P, A); break;
   }
+}
+// Over terrain the column's metric is computed per level (more live values): two resident
+// CTAs per SM at most, whatever the flat variant's register cap.
+template <class FT, int G, int CM, int MINB>
+void launch_g(const DevParams<FT> &P, const StageArgs<FT> &A, cudaStream_t s) {
+  if (P.topo) launch_gt<FT, G, CM, (MINB < 2 ? MINB : 2), true>(P, A, s);
+  else launch_gt<FT, G, CM, MINB, false>(P, A, s);
 }
 
 // Levels per lane CM and the register cap (min resident CTAs per SM) of a variant.

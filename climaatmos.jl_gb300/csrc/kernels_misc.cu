@@ -310,7 +310,16 @@ __global__ void __launch_bounds__(SUM_THREADS) k_sums_partial(DevParams<FT> P, c
     const int n = (int)(col % NN);
     const size_t e = col / NN;
     const double Jh = (double)P.hgeo[(e * HG_N + HG_JH) * NN + n];
-    const double WJ = (double)P.W[n] * (Jh * (double)P.levc[LC_R2 * Nv + v] * (double)P.levc[LC_DZ * Nv + v]);
+    double WJ;
+    if (P.topo) {
+      // terrain-following levels: J = J_h r^2 dz of the point (topo.cuh), in FP64
+      const Lev4<FT> L = P.ltc[v];
+      const double zs = (double)P.tgeo[(e * TG_N + TG_ZS) * NN + n];
+      const double r = 1.0 + ((double)L.x + zs * (double)L.y) * (double)P.iR;
+      WJ = (double)P.W[n] * (Jh * (r * r) * ((double)L.z + zs * (double)L.w));
+    } else {
+      WJ = (double)P.W[n] * (Jh * (double)P.levc[LC_R2 * Nv + v] * (double)P.levc[LC_DZ * Nv + v]);
+    }
     const size_t b = (e * 4 * NN + n) * Nv + v;
     two_sum_acc(s[0], c[0], (double)Yc[b] * WJ);
     two_sum_acc(s[1], c[1], (double)Yc[b + 48 * Nv] * WJ);

@@ -1,0 +1,744 @@
+// Spectral-element slab kernels of the explicit tendency over terrain-following levels.
+//
+// The same work as k_passA / k_passB (remaining_tendency!: prep_hyperdiffusion_tendency!,
+// horizontal_dynamics_tendency!, apply_hyperdiffusion_tendency!,
+// explicit_vertical_advection_tendency! and the Rayleigh sponge on u_h) with the metric of
+// every point (topo.cuh) in place of the per-level scaling of the surface metric:
+//  - the contravariant (u^1, u^2) of the centre velocity C123(u_h) + I^c(C123(u_3)) take
+//    g^a3 I^c(u_3), and u^3 on a face takes u_h^3 = ᶠwinterp(rho J, CT3(u_h))
+//    (compute_ᶠuₕ³, precomputed_quantities.jl:473-476);
+//  - the kinetic energy takes 2 CT3(u_h) I^c(u_3) (compute_kinetic, utilities.jl:194-206);
+//  - the geopotential g z, the Rayleigh sponge and the Coriolis f^3 are per point;
+//  - every C123 <-> CT123 conversion of the vector Laplacians takes the full 3x3 metric;
+//  - u_3 on the bottom and top faces is the impenetrable value -u_h^3 / g^33 (formed here
+//    from u_h of the adjacent centre, so the kernels read the filtered state whatever the
+//    stored boundary values).
+// The vector Laplacian is a covariant 3-vector whose DSS projects to Cartesian components
+// with each copy's basis, whose E^3 leans with the level over terrain.  Pass A therefore
+// stores (L_s, L_1 - (s_1 / dz) L_3, L_2 - (s_2 / dz) L_3, L_3): the horizontal part of the
+// Cartesian vector in covariant form, which the ordinary DSS averages as a horizontal vector
+// (and L_3 as a scalar, dz being the same for every copy), and pass B adds (s_a / dz) L_3
+// back on its own copy's slopes; that is the Cartesian DSS of the 3-vector.
+#include "se_ops.cuh"
+#include "topo.cuh"
+
+namespace gb {
+
+namespace {
+
+using namespace se;
+
+constexpr int TS_THREADS = 256;
+constexpr int TS_LEVELS = TS_THREADS / 4;
+
+template <class FT>
+struct TopoALayout {
+  size_t y[2], f[2], g[2], t[2], out, bar, total;
+  __host__ __device__ TopoALayout(int Nv, int nbuf) {
+    const int Nf = Nv + 1;
+    size_t o = 0;
+    for (int b = 0; b < 2; ++b) {
+      if (b < nbuf) {
+        y[b] = o; o += align16(sizeof(FT) * 64 * Nv);
+        f[b] = o; o += align16(sizeof(FT) * 16 * Nf);
+        g[b] = o; o += align16(sizeof(FT) * HG_N * 16);
+        t[b] = o; o += align16(sizeof(FT) * TG_N * 16);
+      } else {
+        y[b] = y[0]; f[b] = f[0]; g[b] = g[0]; t[b] = t[0];
+      }
+    }
+    out = o; o += align16(sizeof(FT) * 64 * Nv);
+    bar = o; o += 16;
+    total = o;
+  }
+};
+
+// Level-major scratch rows of the terrain pass B ((f Nv + v) 16 + n).
+enum TopoBScratch { TB_C1 = 0, TB_C2, TB_K, TB_RJ, TB_L4, TB_Q1, TB_Q2, TB_CT3, TB_N };
+
+template <class FT>
+struct TopoBLayout {
+  size_t y[2], f[2], g[2], t[2], lap[2], s, x1, x2, w, bar, total;
+  __host__ __device__ TopoBLayout(int Nv, int nbuf) {
+    const int Nf = Nv + 1;
+    size_t o = 0;
+    for (int b = 0; b < 2; ++b) {
+      if (b < nbuf) {
+        y[b] = o; o += align16(sizeof(FT) * 64 * Nv);
+        f[b] = o; o += align16(sizeof(FT) * 16 * Nf);
+        g[b] = o; o += align16(sizeof(FT) * HG_N * 16);
+        t[b] = o; o += align16(sizeof(FT) * TG_N * 16);
+        lap[b] = o; o += align16(sizeof(FT) * 64 * Nv);
+      } else {
+        y[b] = y[0]; f[b] = f[0]; g[b] = g[0]; t[b] = t[0]; lap[b] = lap[0];
+      }
+    }
+    s = o; o += align16(sizeof(FT) * TB_N * 16 * Nv);
+    x1 = o; o += align16(sizeof(FT) * 16 * Nf);
+    x2 = o; o += align16(sizeof(FT) * 16 * Nf);
+    w = o; o += align16(sizeof(FT) * 2 * 16);
+    bar = o; o += 16;
+    total = o;
+  }
+};
+
+// The geometry of the thread's row (4 nodes) at one centre level.
+template <class FT>
+struct TRow {
+  FT J[4], iJ[4], WJ[4], iWJ[4];
+  FT u11[4], u12[4], u22[4], u13[4], u23[4];  // g^ij (g^33 of centres is not used)
+  FT d11[4], d12[4], d22[4], d13[4], d23[4], d33[4];
+  FT z[4], zsb[4], ir[4], s1i[4], s2i[4], idz[4];  // height, z_s b, 1 / r, s_a / dz, 1 / dz
+};
+
+// Node rows of the element slab: sG the horizontal geometry, sT the terrain, sW = (W, 1/W).
+template <class FT>
+__device__ __forceinline__ void trow_centre(const DevParams<FT> &P, const FT *sG, const FT *sT, const FT *sW, int j,
+                                            const Lev4<FT> &L, TRow<FT> &o) {
+  FT Jh[4], a0[4], a1[4], a2[4], b0[4], b1[4], b2[4], zs[4], e1[4], e2[4], W[4];
+  ld_row(sG + HG_JH * NN + NQ * j, Jh);
+  ld_row(sG + HG_GU0 * NN + NQ * j, a0);
+  ld_row(sG + HG_GU1 * NN + NQ * j, a1);
+  ld_row(sG + HG_GU2 * NN + NQ * j, a2);
+  ld_row(sG + HG_GD0 * NN + NQ * j, b0);
+  ld_row(sG + HG_GD1 * NN + NQ * j, b1);
+  ld_row(sG + HG_GD2 * NN + NQ * j, b2);
+  ld_row(sT + TG_ZS * NN + NQ * j, zs);
+  ld_row(sT + TG_D1 * NN + NQ * j, e1);
+  ld_row(sT + TG_D2 * NN + NQ * j, e2);
+  ld_row(sW + NQ * j, W);
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const TPoint<FT> t = tpoint(P, zs[i], e1[i], e2[i], L);
+    const TMetricUp<FT> m = tmetric_up(t, a0[i], a1[i], a2[i]);
+    o.J[i] = Jh[i] * t.r2 * t.dz;
+    o.iJ[i] = grcp(o.J[i]);
+    o.WJ[i] = W[i] * o.J[i];
+    o.iWJ[i] = grcp(o.WJ[i]);
+    o.u11[i] = m.g11; o.u12[i] = m.g12; o.u22[i] = m.g22; o.u13[i] = m.g13; o.u23[i] = m.g23;
+    o.d11[i] = t.r2 * b0[i] + t.s1 * t.s1;
+    o.d12[i] = t.r2 * b1[i] + t.s1 * t.s2;
+    o.d22[i] = t.r2 * b2[i] + t.s2 * t.s2;
+    o.d13[i] = t.s1 * t.dz;
+    o.d23[i] = t.s2 * t.dz;
+    o.d33[i] = t.dz * t.dz;
+    o.z[i] = t.z;
+    o.zsb[i] = t.zsb;
+    o.ir[i] = t.ir;
+    o.s1i[i] = t.s1 * t.idz;
+    o.s2i[i] = t.s2 * t.idz;
+    o.idz[i] = t.idz;
+  }
+}
+
+// g^33 of the row's nodes on a face with warp record L (and, optionally, J, 1/J, 1/r).
+template <class FT>
+__device__ __forceinline__ void trow_face(const DevParams<FT> &P, const FT *sG, const FT *sT, int j, const Lev4<FT> &L,
+                                          FT (&g33)[4], FT *J = nullptr, FT *iJ = nullptr, FT *ir = nullptr) {
+  FT Jh[4], a0[4], a1[4], a2[4], zs[4], e1[4], e2[4];
+  ld_row(sG + HG_GU0 * NN + NQ * j, a0);
+  ld_row(sG + HG_GU1 * NN + NQ * j, a1);
+  ld_row(sG + HG_GU2 * NN + NQ * j, a2);
+  ld_row(sT + TG_ZS * NN + NQ * j, zs);
+  ld_row(sT + TG_D1 * NN + NQ * j, e1);
+  ld_row(sT + TG_D2 * NN + NQ * j, e2);
+  if (J) ld_row(sG + HG_JH * NN + NQ * j, Jh);
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const TPoint<FT> t = tpoint(P, zs[i], e1[i], e2[i], L);
+    g33[i] = tmetric_up(t, a0[i], a1[i], a2[i]).g33;
+    if (J) {
+      J[i] = Jh[i] * t.r2 * t.dz;
+      iJ[i] = grcp(J[i]);
+      ir[i] = t.ir;
+    }
+  }
+}
+
+// C123(wgrad(div u)) fdiv - C123(wcurl(C123(curl u))) of a covariant (c1, c2, c3) with the full
+// metric of the row (the oracle's vec_lap over terrain).
+template <class FT>
+__device__ __forceinline__ void tvec_lap(const DevParams<FT> &P, const Row<FT> &R, const TRow<FT> &G, const FT (&W)[4],
+                                         const FT (&iW)[4], const FT (&c1)[4], const FT (&c2)[4], const FT (&c3)[4],
+                                         FT fdiv, FT (&o1)[4], FT (&o2)[4], FT (&o3)[4]) {
+  FT a[4], b[4], da[4], db[4], w1[4], w2[4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    a[i] = G.J[i] * (G.u11[i] * c1[i] + G.u12[i] * c2[i] + G.u13[i] * c3[i]);
+    b[i] = G.J[i] * (G.u12[i] * c1[i] + G.u22[i] * c2[i] + G.u23[i] * c3[i]);
+  }
+  d1(P, a, da);
+  d2(R, b, db);
+#pragma unroll
+  for (int i = 0; i < 4; ++i) a[i] = W[i] * ((da[i] + db[i]) * G.iJ[i]);
+  t1(P, a, w1);
+  t2(R, a, w2);
+  FT e1[4], e2[4], e3[4], e4[4];
+  d1(P, c2, e1);
+  d2(R, c1, e2);
+  d2(R, c3, e3);
+  d1(P, c3, e4);
+  FT z1[4], z2[4], z3[4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const FT k1 = e3[i] * G.iJ[i], k2 = -e4[i] * G.iJ[i], k3 = (e1[i] - e2[i]) * G.iJ[i];
+    z1[i] = W[i] * (G.d11[i] * k1 + G.d12[i] * k2 + G.d13[i] * k3);
+    z2[i] = W[i] * (G.d12[i] * k1 + G.d22[i] * k2 + G.d23[i] * k3);
+    z3[i] = W[i] * (G.d13[i] * k1 + G.d23[i] * k2 + G.d33[i] * k3);
+  }
+  FT f1[4], f2[4], f3[4], f4[4];
+  t1(P, z2, f1);
+  t2(R, z1, f2);
+  t2(R, z3, f3);
+  t1(P, z3, f4);
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const FT q1 = -f3[i] * G.iWJ[i], q2 = f4[i] * G.iWJ[i], q3 = (f2[i] - f1[i]) * G.iWJ[i];
+    o1[i] = -fdiv * w1[i] * iW[i] - (G.d11[i] * q1 + G.d12[i] * q2 + G.d13[i] * q3);
+    o2[i] = -fdiv * w2[i] * iW[i] - (G.d12[i] * q1 + G.d22[i] * q2 + G.d23[i] * q3);
+    o3[i] = -(G.d13[i] * q1 + G.d23[i] * q2 + G.d33[i] * q3);
+  }
+}
+
+// weak divergence -(1/WJ) (D^T (WJ F1) + ...) with the row's per-node WJ
+template <class FT>
+__device__ __forceinline__ void twdiv(const DevParams<FT> &P, const Row<FT> &R, const TRow<FT> &G, const FT (&F1)[4],
+                                      const FT (&F2)[4], FT (&o)[4]) {
+  FT a[4], b[4], ta[4], tb[4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    a[i] = G.WJ[i] * F1[i];
+    b[i] = G.WJ[i] * F2[i];
+  }
+  t1(P, a, ta);
+  t2(R, b, tb);
+#pragma unroll
+  for (int i = 0; i < 4; ++i) o[i] = -(ta[i] + tb[i]) * G.iWJ[i];
+}
+
+// The centre state of the row at level v with the filtered face u_3 below and above:
+// ct3 = CT3(u_h), ub3 = I^c(u_3), h = CT12(u_h) and K.
+template <class FT>
+struct TCen {
+  FT rho[4], u1[4], u2[4], rhoe[4], ct3[4], ub3[4], h1[4], h2[4], K[4];
+};
+template <class FT>
+__device__ __forceinline__ void tcentre(const DevParams<FT> &P, const FT *sY, const FT *sF, const FT *sG, const FT *sT,
+                                        int j, int v, const TRow<FT> &G, TCen<FT> &c) {
+  const int Nv = P.Nv, Nf = P.Nf;
+  FT ga[4], gb[4], fa[4], fb[4];
+  trow_face(P, sG, sT, j, P.ltf[v], ga);
+  trow_face(P, sG, sT, j, P.ltf[v + 1], gb);
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const int n = NQ * j + i, q = n * Nv + v;
+    c.rho[i] = sY[q];
+    c.u1[i] = sY[16 * Nv + q];
+    c.u2[i] = sY[32 * Nv + q];
+    c.rhoe[i] = sY[48 * Nv + q];
+    c.ct3[i] = G.u13[i] * c.u1[i] + G.u23[i] * c.u2[i];
+    // the impenetrable value on the bottom and top faces (u^3 = 0 there)
+    fa[i] = v == 0 ? -c.ct3[i] / ga[i] : sF[n * Nf + v];
+    fb[i] = v + 1 == Nv ? -c.ct3[i] / gb[i] : sF[n * Nf + v + 1];
+    c.ub3[i] = (fa[i] + fb[i]) / FT(2);
+    c.h1[i] = G.u11[i] * c.u1[i] + G.u12[i] * c.u2[i];
+    c.h2[i] = G.u12[i] * c.u1[i] + G.u22[i] * c.u2[i];
+    const FT kv = (fa[i] * (fa[i] * ga[i]) + fb[i] * (fb[i] * gb[i])) / FT(2);
+    c.K[i] = (c.u1[i] * c.h1[i] + c.u2[i] * c.h2[i] + kv + FT(2) * c.ct3[i] * c.ub3[i]) / FT(2);
+  }
+}
+
+template <class FT>
+__global__ void __launch_bounds__(TS_THREADS, 1) k_topo_passA(DevParams<FT> P, int nbuf, const FT *__restrict__ Yc,
+                                                             const FT *__restrict__ Yf, FT *__restrict__ Lout) {
+  extern __shared__ __align__(128) unsigned char sm[];
+  const int Nv = P.Nv, Nf = P.Nf;
+  const TopoALayout<FT> Lo(Nv, nbuf);
+  auto at = [&](const size_t (&off)[2], int b) { return (FT *)(sm + (b ? off[1] : off[0])); };
+  FT *sO = (FT *)(sm + Lo.out);
+  __shared__ __align__(16) FT sW[2 * NN];
+  uint64_t *bar = (uint64_t *)(sm + Lo.bar);
+  const uint32_t by = uint32_t(sizeof(FT) * 64 * Nv), bf = uint32_t(sizeof(FT) * 16 * Nf);
+  const uint32_t bg = uint32_t(sizeof(FT) * HG_N * 16), bt = uint32_t(sizeof(FT) * TG_N * 16);
+  auto issue = [&](int b, int e) {
+    uint64_t *bb = b ? &bar[1] : &bar[0];
+    mbar_expect_tx(bb, by + bf + bg + bt);
+    tma_load(at(Lo.y, b), Yc + (size_t)e * 64 * Nv, by, bb);
+    tma_load(at(Lo.f, b), Yf + (size_t)e * 16 * Nf, bf, bb);
+    tma_load(at(Lo.g, b), P.hgeo + (size_t)e * HG_N * 16, bg, bb);
+    tma_load(at(Lo.t, b), P.tgeo + (size_t)e * TG_N * 16, bt, bb);
+  };
+  if (threadIdx.x < NN) {
+    sW[threadIdx.x] = P.W[threadIdx.x];
+    sW[NN + threadIdx.x] = P.iW[threadIdx.x];
+  }
+  slab_init_bars(bar);
+  int e = blockIdx.x;
+  if (threadIdx.x == 0 && e < P.Nh) issue(0, e);
+  const int j = threadIdx.x & 3, vs = level_slot(threadIdx.x >> 2);
+  Row<FT> R;
+  R.init(P, j);
+  FT W[4], iW[4];
+  ld_row(sW + NQ * j, W);
+  ld_row(sW + NN + NQ * j, iW);
+  for (int it = 0; e < P.Nh; ++it, e += gridDim.x) {
+    int b;
+    if (!slab_begin(bar, nbuf, it, e, P.Nh, P.status, issue, b)) break;
+    const FT *sY = at(Lo.y, b), *sF = at(Lo.f, b), *sG = at(Lo.g, b), *sT = at(Lo.t, b);
+    for (int v0 = 0; v0 < Nv; v0 += TS_LEVELS) {
+      const int v = min(v0 + vs, Nv - 1);
+      const bool act = v0 + vs < Nv;
+      TRow<FT> G;
+      trow_centre(P, sG, sT, sW, j, P.ltc[v], G);
+      TCen<FT> c;
+      tcentre(P, sY, sF, sG, sT, j, v, G, c);
+      FT sd[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        Thermo<FT> th;
+        thermo(P, c.rho[i], c.rhoe[i], c.K[i], P.grav * G.z[i], P.lr4[v], th);
+        // s_d - s_d,r = cp_d (T - T_r) + (Phi - Phi_r(Pi)); the level record's deviation is for
+        // the flat level's geopotential g zeta, the point is g z_s b higher
+        sd[i] = P.cpd * (th.T - th.Tr) + (th.phid + P.grav * G.zsb[i]);
+      }
+      FT o1[4], o2[4], o3[4];
+      tvec_lap(P, R, G, W, iW, c.u1, c.u2, c.ub3, FT(1), o1, o2, o3);
+      FT g1[4], g2[4], x1[4], x2[4], Ls[4];
+      d1(P, sd, g1);
+      d2(R, sd, g2);
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        x1[i] = G.u11[i] * g1[i] + G.u12[i] * g2[i];
+        x2[i] = G.u12[i] * g1[i] + G.u22[i] * g2[i];
+      }
+      twdiv(P, R, G, x1, x2, Ls);
+      if (act) {
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          const int q = (NQ * j + i) * Nv + v;
+          sO[q] = Ls[i];
+          sO[16 * Nv + q] = o1[i] - G.s1i[i] * o3[i];
+          sO[32 * Nv + q] = o2[i] - G.s2i[i] * o3[i];
+          sO[48 * Nv + q] = o3[i];
+        }
+      }
+    }
+    fence_proxy_async();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      tma_store(Lout + (size_t)e * 64 * Nv, sO, by);
+      tma_store_commit();
+    }
+  }
+  if (threadIdx.x == 0) tma_store_wait_all();
+}
+
+template <class FT>
+__global__ void __launch_bounds__(TS_THREADS, 1) k_topo_passB(DevParams<FT> P, int nbuf, const FT *__restrict__ Yc,
+                                                             const FT *__restrict__ Yf, const FT *__restrict__ Lin,
+                                                             FT *__restrict__ Tc, FT *__restrict__ Tf) {
+  extern __shared__ __align__(128) unsigned char sm[];
+  const int Nv = P.Nv, Nf = P.Nf;
+  const TopoBLayout<FT> Lo(Nv, nbuf);
+  auto at = [&](const size_t (&off)[2], int b) { return (FT *)(sm + (b ? off[1] : off[0])); };
+  FT *sS = (FT *)(sm + Lo.s), *sX1 = (FT *)(sm + Lo.x1), *sX2 = (FT *)(sm + Lo.x2), *sW = (FT *)(sm + Lo.w);
+  uint64_t *bar = (uint64_t *)(sm + Lo.bar);
+  const uint32_t by = uint32_t(sizeof(FT) * 64 * Nv), bf = uint32_t(sizeof(FT) * 16 * Nf);
+  const uint32_t bg = uint32_t(sizeof(FT) * HG_N * 16), bt = uint32_t(sizeof(FT) * TG_N * 16);
+  auto issue = [&](int b, int e) {
+    uint64_t *bb = b ? &bar[1] : &bar[0];
+    mbar_expect_tx(bb, 2 * by + bf + bg + bt);
+    tma_load(at(Lo.y, b), Yc + (size_t)e * 64 * Nv, by, bb);
+    tma_load(at(Lo.f, b), Yf + (size_t)e * 16 * Nf, bf, bb);
+    tma_load(at(Lo.g, b), P.hgeo + (size_t)e * HG_N * 16, bg, bb);
+    tma_load(at(Lo.t, b), P.tgeo + (size_t)e * TG_N * 16, bt, bb);
+    tma_load(at(Lo.lap, b), Lin + (size_t)e * 64 * Nv, by, bb);
+  };
+  if (threadIdx.x < NN) {
+    sW[threadIdx.x] = P.W[threadIdx.x];
+    sW[NN + threadIdx.x] = P.iW[threadIdx.x];
+  }
+  slab_init_bars(bar);
+  int e = blockIdx.x;
+  if (threadIdx.x == 0 && e < P.Nh) issue(0, e);
+  const int j = threadIdx.x & 3, vl = threadIdx.x >> 2, vs = level_slot(vl);
+  auto row = [&](FT *base, int f, int v) { return base + ((size_t)f * Nv + v) * NN + NQ * j; };
+  Row<FT> R;
+  R.init(P, j);
+  for (int it = 0; e < P.Nh; ++it, e += gridDim.x) {
+    int b;
+    if (!slab_begin(bar, nbuf, it, e, P.Nh, P.status, issue, b)) break;
+    FT *sY = at(Lo.y, b), *sF = at(Lo.f, b);
+    const FT *sG = at(Lo.g, b), *sT = at(Lo.t, b), *sL = at(Lo.lap, b);
+    FT W[4], iW[4];
+    ld_row(sW + NQ * j, W);
+    ld_row(sW + NN + NQ * j, iW);
+    // ---- P1: centre levels
+    for (int v0 = 0; v0 < Nv; v0 += TS_LEVELS) {
+      const int v = min(v0 + vs, Nv - 1);
+      const bool act = v0 + vs < Nv;
+      TRow<FT> G;
+      trow_centre(P, sG, sT, sW, j, P.ltc[v], G);
+      TCen<FT> c;
+      tcentre(P, sY, sF, sG, sT, j, v, G, c);
+      FT h[4], Pi[4], thp[4], gg[4], c1[4], c2[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        Thermo<FT> th;
+        thermo(P, c.rho[i], c.rhoe[i], c.K[i], P.grav * G.z[i], P.lr4[v], th);
+        h[i] = th.h;
+        Pi[i] = th.Pi;
+        thp[i] = th.thv - th.thvr;
+        // K + Phi - Phi_r(Pi) + (cp_d / 2) th' Pi: one gradient for grad(K + Phi - Phi_r) and
+        // the (cp_d / 2) grad(th' Pi) of the Exner-split pressure gradient
+        gg[i] = c.K[i] + (th.phid + P.grav * G.zsb[i]) + P.cpd * FT(0.5) * thp[i] * Pi[i];
+        c1[i] = c.h1[i] + G.u13[i] * c.ub3[i];
+        c2[i] = c.h2[i] + G.u23[i] * c.ub3[i];
+      }
+      // vorticity w^3 = wcurl(u_h), Coriolis f^3, (f^3 + w^3) x CT12(u) -> C12, the sponge
+      FT Q1[4], Q2[4];
+      {
+        FT a[4], bb[4], ta[4], tb[4], f3[4], fh1[4], fh2[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          a[i] = W[i] * c.u2[i];
+          bb[i] = W[i] * c.u1[i];
+        }
+        t1(P, a, ta);
+        t2(R, bb, tb);
+        ld_row(sG + HG_F3 * NN + NQ * j, f3);
+        ld_row(sG + HG_FH1 * NN + NQ * j, fh1);
+        ld_row(sG + HG_FH2 * NN + NQ * j, fh2);
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          const FT om = (tb[i] - ta[i]) * G.iWJ[i];
+          const FT fc3 = f3[i] * G.idz[i] - (G.s1i[i] * fh1[i] + G.s2i[i] * fh2[i]) * G.ir[i];
+          const FT a3J = G.J[i] * (fc3 + om);
+          const FT damp = tsponge(P, G.z[i], P.spg_auh);
+          Q1[i] = a3J * c2[i] - damp * c.u1[i];
+          Q2[i] = -a3J * c1[i] - damp * c.u2[i];
+        }
+      }
+      // rho: -wdiv(rho u); rho e_tot: -split_div(rho u, h)
+      FT F1[4], F2[4], dm[4], Trhoe[4];
+      {
+        FT G1[4], G2[4], dmh[4], ha[4], hb[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          F1[i] = c.rho[i] * c1[i];
+          F2[i] = c.rho[i] * c2[i];
+          G1[i] = F1[i] * h[i];
+          G2[i] = F2[i] * h[i];
+        }
+        twdiv(P, R, G, F1, F2, dm);
+        twdiv(P, R, G, G1, G2, dmh);
+        d1(P, h, ha);
+        d2(R, h, hb);
+#pragma unroll
+        for (int i = 0; i < 4; ++i) Trhoe[i] = -(dmh[i] + h[i] * dm[i] + F1[i] * ha[i] + F2[i] * hb[i]) / FT(2);
+      }
+      // u_h: -[grad(K + Phi - Phi_r) + cp_d (th' grad Pi + grad(th' Pi) - Pi grad th') / 2]
+      {
+        FT a1[4], a2[4], b1[4], b2[4], f1[4], f2[4];
+        d1(P, gg, a1);
+        d2(R, gg, a2);
+        d1(P, Pi, b1);
+        d2(R, Pi, b2);
+        d1(P, thp, f1);
+        d2(R, thp, f2);
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          Q1[i] -= a1[i] + P.cpd * FT(0.5) * (thp[i] * b1[i] - Pi[i] * f1[i]);
+          Q2[i] -= a2[i] + P.cpd * FT(0.5) * (thp[i] * b2[i] - Pi[i] * f2[i]);
+        }
+      }
+      // hyperdiffusion of u: the Laplacian's covariant 3-vector back on this copy's slopes
+      FT L3[4], o3[4];
+      {
+        FT L1[4], L2[4], o1[4], o2[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          const int q = (NQ * j + i) * Nv + v;
+          L3[i] = sL[48 * Nv + q];
+          L1[i] = sL[16 * Nv + q] + G.s1i[i] * L3[i];
+          L2[i] = sL[32 * Nv + q] + G.s2i[i] * L3[i];
+        }
+        tvec_lap(P, R, G, W, iW, L1, L2, L3, P.div_damp, o1, o2, o3);
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          Q1[i] -= P.nu_v * o1[i];
+          Q2[i] -= P.nu_v * o2[i];
+        }
+      }
+      // rho e_tot: -nu_s wdiv(rho grad L_s)
+      {
+        FT Ls[4], g1[4], g2[4], x1[4], x2[4], hd[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) Ls[i] = sL[(NQ * j + i) * Nv + v];
+        d1(P, Ls, g1);
+        d2(R, Ls, g2);
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          x1[i] = c.rho[i] * (G.u11[i] * g1[i] + G.u12[i] * g2[i]);
+          x2[i] = c.rho[i] * (G.u12[i] * g1[i] + G.u22[i] * g2[i]);
+        }
+        twdiv(P, R, G, x1, x2, hd);
+#pragma unroll
+        for (int i = 0; i < 4; ++i) Trhoe[i] -= P.nu_s * hd[i];
+      }
+      if (act) {
+        FT rJ[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) rJ[i] = c.rho[i] * G.J[i];
+        st_row(row(sS, TB_C1, v), c1);
+        st_row(row(sS, TB_C2, v), c2);
+        st_row(row(sS, TB_K, v), c.K);
+        st_row(row(sS, TB_RJ, v), rJ);
+        st_row(row(sS, TB_L4, v), o3);
+        st_row(row(sS, TB_Q1, v), Q1);
+        st_row(row(sS, TB_Q2, v), Q2);
+        st_row(row(sS, TB_CT3, v), c.ct3);
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          const int q = (NQ * j + i) * Nv + v;
+          sY[q] = -dm[i];        // the tendency over the (read) state entries
+          sY[48 * Nv + q] = Trhoe[i];
+        }
+      }
+    }
+    __syncthreads();
+    // ---- P2: faces (f^12 + w^12, cross products, the u_3 tendency)
+    for (int k0 = 0; k0 < Nf; k0 += TS_LEVELS) {
+      const int k = min(k0 + vl, Nf - 1);
+      const bool act = k0 + vl < Nf;
+      const bool inner = k > 0 && k < Nv;
+      const int va = k > 0 ? k - 1 : 0, vb = k < Nv ? k : Nv - 1;
+      FT g33[4], Jf[4], iJf[4], irf[4];
+      trow_face(P, sG, sT, j, P.ltf[k], g33, Jf, iJf, irf);
+      FT C1a[4], C1b[4], C2a[4], C2b[4], Ka[4], Kb[4], Ra[4], Rb[4], La[4], Lb[4], CTa[4], CTb[4];
+      ld_row(row(sS, TB_C1, va), C1a);
+      ld_row(row(sS, TB_C1, vb), C1b);
+      ld_row(row(sS, TB_C2, va), C2a);
+      ld_row(row(sS, TB_C2, vb), C2b);
+      ld_row(row(sS, TB_K, va), Ka);
+      ld_row(row(sS, TB_K, vb), Kb);
+      ld_row(row(sS, TB_RJ, va), Ra);
+      ld_row(row(sS, TB_RJ, vb), Rb);
+      ld_row(row(sS, TB_L4, va), La);
+      ld_row(row(sS, TB_L4, vb), Lb);
+      ld_row(row(sS, TB_CT3, va), CTa);
+      ld_row(row(sS, TB_CT3, vb), CTb);
+      FT u3[4], Wu[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        u3[i] = inner ? sF[(NQ * j + i) * Nf + k] : -CTa[i] / g33[i];
+        Wu[i] = W[i] * u3[i];
+      }
+      FT ta[4], tb[4];
+      t2(R, Wu, tb);
+      t1(P, Wu, ta);
+      if (act) {
+        FT fh1[4], fh2[4];
+        ld_row(sG + HG_FH1 * NN + NQ * j, fh1);
+        ld_row(sG + HG_FH2 * NN + NQ * j, fh2);
+        FT T3[4], X1[4], X2[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          const int n = NQ * j + i;
+          const FT iWJf = iW[i] * iJf[i];
+          FT cv1 = 0, cv2 = 0, gK = 0, cc1, cc2, l4, rJ, uh3;
+          if (inner) {
+            const int qa = n * Nv + va, qb = n * Nv + vb;
+            cv1 = (sY[32 * Nv + qa] - sY[32 * Nv + qb]) * iJf[i];   // -(d u_2 / d xi^3) / J_f
+            cv2 = (sY[16 * Nv + qb] - sY[16 * Nv + qa]) * iJf[i];   // (d u_1 / d xi^3) / J_f
+            cc1 = (C1a[i] + C1b[i]) / FT(2);
+            cc2 = (C2a[i] + C2b[i]) / FT(2);
+            gK = Kb[i] - Ka[i];
+            l4 = (Ra[i] * La[i] + Rb[i] * Lb[i]) / (Ra[i] + Rb[i]);
+            uh3 = (Ra[i] * CTa[i] + Rb[i] * CTb[i]) / (Ra[i] + Rb[i]);
+            rJ = (Ra[i] + Rb[i]) / FT(2);
+          } else {
+            cc1 = C1a[i];
+            cc2 = C2a[i];
+            l4 = La[i];
+            uh3 = CTa[i];
+            rJ = Ra[i];
+          }
+          const FT fo1 = fh1[i] * irf[i] + cv1 - tb[i] * iWJf;
+          const FT fo2 = fh2[i] * irf[i] + cv2 + ta[i] * iWJf;
+          const FT b3 = rJ * (uh3 + g33[i] * u3[i]);
+          T3[i] = -P.nu_v * l4 - (Jf[i] * (fo1 * cc2 - fo2 * cc1) + gK);
+          X1[i] = Jf[i] * (fo2 * b3);
+          X2[i] = -(Jf[i] * (fo1 * b3));
+        }
+#pragma unroll
+        for (int i = 0; i < 4; ++i) sF[(NQ * j + i) * Nf + k] = T3[i];
+        st_row(sX1 + (size_t)k * NN + NQ * j, X1);
+        st_row(sX2 + (size_t)k * NN + NQ * j, X2);
+      }
+    }
+    __syncthreads();
+    // ---- P3: centre u_h part of the face cross products
+    for (int v0 = 0; v0 < Nv; v0 += TS_LEVELS) {
+      const int v = v0 + vs;
+      if (v < Nv) {
+        FT Xa1[4], Xb1[4], Xa2[4], Xb2[4], rJ[4], Q1[4], Q2[4];
+        ld_row(sX1 + (size_t)v * NN + NQ * j, Xa1);
+        ld_row(sX1 + (size_t)(v + 1) * NN + NQ * j, Xb1);
+        ld_row(sX2 + (size_t)v * NN + NQ * j, Xa2);
+        ld_row(sX2 + (size_t)(v + 1) * NN + NQ * j, Xb2);
+        ld_row(row(sS, TB_RJ, v), rJ);
+        ld_row(row(sS, TB_Q1, v), Q1);
+        ld_row(row(sS, TB_Q2, v), Q2);
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          const int q = (NQ * j + i) * Nv + v;
+          sY[16 * Nv + q] = Q1[i] - (Xa1[i] + Xb1[i]) / FT(2) / rJ[i];
+          sY[32 * Nv + q] = Q2[i] - (Xa2[i] + Xb2[i]) / FT(2) / rJ[i];
+        }
+      }
+    }
+    fence_proxy_async();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      tma_store(Tc + (size_t)e * 64 * Nv, sY, by);
+      tma_store(Tf + (size_t)e * 16 * Nf, sF, bf);
+      tma_store_commit();
+    }
+  }
+  if (threadIdx.x == 0) tma_store_wait_all();
+}
+
+// The impenetrable filter over terrain (set_velocity_at_surface!, set_velocity_at_top!,
+// precomputed_quantities.jl:486-553): u_3 = -u_h^3 / g^33 on the bottom and top faces, with
+// u_h^3 the adjacent centre's CT3(u_h) (ᶠwinterp extrapolates at the boundary).  One thread
+// per column and boundary.
+template <class FT>
+__global__ void k_topo_filter(DevParams<FT> P, const FT *__restrict__ Yc, FT *__restrict__ Yf) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int ncols = P.Nh * NN;
+  if (t >= 2 * ncols) return;
+  const int col = t >> 1, top = t & 1;
+  const int e = col >> 4, n = col & 15, Nv = P.Nv, Nf = P.Nf;
+  const int v = top ? Nv - 1 : 0, k = top ? Nv : 0;
+  const FT *hg = P.hgeo + (size_t)e * HG_N * NN, *tg = P.tgeo + (size_t)e * TG_N * NN;
+  const FT zs = tg[TG_ZS * NN + n], d1v = tg[TG_D1 * NN + n], d2v = tg[TG_D2 * NN + n];
+  const FT a0 = hg[HG_GU0 * NN + n], a1 = hg[HG_GU1 * NN + n], a2 = hg[HG_GU2 * NN + n];
+  const TMetricUp<FT> mc = tmetric_up(tpoint(P, zs, d1v, d2v, P.ltc[v]), a0, a1, a2);
+  const TMetricUp<FT> mf = tmetric_up(tpoint(P, zs, d1v, d2v, P.ltf[k]), a0, a1, a2);
+  const size_t cb = ((size_t)e * 4 * NN + n) * Nv + v;
+  const FT ct3 = mc.g13 * Yc[cb + 16 * Nv] + mc.g23 * Yc[cb + 32 * Nv];
+  Yf[(size_t)col * Nf + k] = -ct3 / mf.g33;
+}
+
+// DSS of the reduced implicit tendencies (rho, rho e_tot at the centres: [Nh][2][16][Nv]; u_3
+// at the faces), the J-weighted average of collocated copies in the fixed copy order.  Over
+// terrain the implicit tendency of a column depends on its element's slopes (through u_h^3),
+// so collocated copies differ; the stage states the reference assembles from them are DSSed
+// (ClimaTimeSteppers' dss! after each stage), which DSSing the tendencies reproduces.
+template <class FT>
+__global__ void __launch_bounds__(256) k_dss_reduced(DevParams<FT> P, FT *__restrict__ C, FT *__restrict__ F) {
+  const int lane = threadIdx.x & 31;
+  const int g = blockIdx.x * 8 + (threadIdx.x >> 5);
+  if (g >= P.ngroups) return;
+  const int Nv = P.Nv, Nf = P.Nf;
+  const int o0 = P.goff[g], o1 = P.goff[g + 1];
+  for (int k = lane; k < Nf; k += 32) {
+    FT s0 = 0, s1 = 0, sf = 0;
+    for (int c = o0; c < o1; ++c) {
+      const int idx = P.gcopy[c], e = idx >> 4, n = idx & 15;
+      const FT w = P.gw[c];
+      if (k < Nv) {
+        const size_t b = ((size_t)e * 2 * NN + n) * Nv + k;
+        s0 = fma(w, C[b], s0);
+        s1 = fma(w, C[b + 16 * Nv], s1);
+      }
+      sf = fma(w, F[(size_t)idx * Nf + k], sf);
+    }
+    for (int c = o0; c < o1; ++c) {
+      const int idx = P.gcopy[c], e = idx >> 4, n = idx & 15;
+      if (k < Nv) {
+        const size_t b = ((size_t)e * 2 * NN + n) * Nv + k;
+        C[b] = s0;
+        C[b + 16 * Nv] = s1;
+      }
+      F[(size_t)idx * Nf + k] = sf;
+    }
+  }
+}
+
+struct TsDev {
+  int nsm = 0, optin = 0;
+};
+const TsDev &ts_dev() {
+  static const TsDev d = [] {
+    TsDev x;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&x.nsm, cudaDevAttrMultiProcessorCount, dev);
+    cudaDeviceGetAttribute(&x.optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    if (x.nsm <= 0) x.nsm = 1;
+    return x;
+  }();
+  return d;
+}
+
+// One CTA per SM: double-buffered slabs when they fit, else single.
+template <class L>
+void ts_shape(int Nv, int &nbuf, size_t &smem) {
+  const size_t two = L(Nv, 2).total, one = L(Nv, 1).total;
+  if (two <= (size_t)ts_dev().optin) { nbuf = 2; smem = two; }
+  else { nbuf = 1; smem = one; }
+}
+
+}  // namespace
+
+template <class FT>
+size_t topo_smem(int Nv) { return TopoBLayout<FT>(Nv, 1).total; }
+
+template <class FT>
+void configure_topo(int Nv) {
+  (void)Nv;
+  cudaFuncSetAttribute(k_topo_passA<FT>, cudaFuncAttributeMaxDynamicSharedMemorySize, ts_dev().optin);
+  cudaFuncSetAttribute(k_topo_passB<FT>, cudaFuncAttributeMaxDynamicSharedMemorySize, ts_dev().optin);
+}
+
+template <class FT>
+void launch_topo_passA(const DevParams<FT> &P, const FT *Yc, const FT *Yf, FT *L, cudaStream_t s) {
+  int nbuf;
+  size_t smem;
+  ts_shape<TopoALayout<FT>>(P.Nv, nbuf, smem);
+  const int grid = min(P.Nh, ts_dev().nsm);
+  k_topo_passA<FT><<<grid, TS_THREADS, smem, s>>>(P, nbuf, Yc, Yf, L);
+}
+template <class FT>
+void launch_topo_passB(const DevParams<FT> &P, const FT *Yc, const FT *Yf, const FT *L, FT *Tc, FT *Tf, cudaStream_t s) {
+  int nbuf;
+  size_t smem;
+  ts_shape<TopoBLayout<FT>>(P.Nv, nbuf, smem);
+  const int grid = min(P.Nh, ts_dev().nsm);
+  k_topo_passB<FT><<<grid, TS_THREADS, smem, s>>>(P, nbuf, Yc, Yf, L, Tc, Tf);
+}
+template <class FT>
+void launch_topo_filter(const DevParams<FT> &P, const FT *Yc, FT *Yf, cudaStream_t s) {
+  const int n = 2 * P.Nh * NN;
+  k_topo_filter<FT><<<(n + 255) / 256, 256, 0, s>>>(P, Yc, Yf);
+}
+template <class FT>
+void launch_dss_reduced(const DevParams<FT> &P, FT *C, FT *F, cudaStream_t s) {
+  k_dss_reduced<FT><<<(P.ngroups + 7) / 8, 256, 0, s>>>(P, C, F);
+}
+
+#define INST(FT)                                                                                                  \
+  template size_t topo_smem<FT>(int);                                                                             \
+  template void configure_topo<FT>(int);                                                                          \
+  template void launch_topo_passA<FT>(const DevParams<FT> &, const FT *, const FT *, FT *, cudaStream_t);         \
+  template void launch_topo_passB<FT>(const DevParams<FT> &, const FT *, const FT *, const FT *, FT *, FT *,       \
+                                      cudaStream_t);                                                              \
+  template void launch_topo_filter<FT>(const DevParams<FT> &, const FT *, FT *, cudaStream_t);                    \
+  template void launch_dss_reduced<FT>(const DevParams<FT> &, FT *, FT *, cudaStream_t);
+INST(float)
+INST(double)
+#undef INST
+
+}  // namespace gb

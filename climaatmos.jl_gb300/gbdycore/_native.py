@@ -43,7 +43,9 @@ class GBConfig(ctypes.Structure):
                     "hs_day", "hs_sigma_b", "hs_dT_y", "hs_T_equator", "hs_dtheta_z", "hs_T_min",
                     "hs_p_ref_theta", "hs_MSLP")] + [
                     ("elem_map", ctypes.POINTER(_c_int)), ("elem_orient", ctypes.POINTER(_c_int)),
-                    ("test_dycore_consistency", _c_int)]
+                    ("test_dycore_consistency", _c_int),
+                    ("z_surface", ctypes.POINTER(_c_double)), ("warp", _c_int),
+                    ("sleve_eta", _c_double), ("sleve_s", _c_double)]
 
 
 class GBFieldVec(ctypes.Structure):
@@ -142,13 +144,22 @@ def make_config(cfg):
     for k, v in cfg.hs.items():
         setattr(c, "hs_" + k, float(v))
     c.test_dycore_consistency = 1 if getattr(cfg, "test_dycore_consistency", False) else 0
+    keep = []
     layout = getattr(cfg, "layout", None)
     if layout is not None:
         emap = np.ascontiguousarray(layout[0], dtype=np.int32)
         eori = np.ascontiguousarray(layout[1], dtype=np.int32)
         c.elem_map = emap.ctypes.data_as(ctypes.POINTER(_c_int))
         c.elem_orient = eori.ctypes.data_as(ctypes.POINTER(_c_int))
-        c._keep = (emap, eori)   # the arrays live as long as the struct
+        keep += [emap, eori]
+    zs = getattr(cfg, "z_surface", None)
+    if zs is not None:
+        z = np.ascontiguousarray(zs, dtype=np.float64).reshape(-1)
+        c.z_surface = z.ctypes.data_as(ctypes.POINTER(_c_double))
+        keep.append(z)
+    c.warp = 1 if getattr(cfg, "warp", "linear") == "sleve" else 0
+    c.sleve_eta, c.sleve_s = float(getattr(cfg, "sleve_eta", 0.7)), float(getattr(cfg, "sleve_s", 10.0))
+    c._keep = tuple(keep)   # the arrays live as long as the struct
     return c
 
 

@@ -15,7 +15,7 @@ CSRC = os.path.join(ROOT, "csrc")
 INCLUDE = os.path.join(os.path.dirname(ROOT), "include")
 BUILD = os.path.join(ROOT, "_build")
 LIB = os.path.join(PKG, "libgbdycore.so")
-SOURCES = ["context.cu", "kernels_se.cu", "kernels_col.cu", "kernels_colg.cu", "columns.cu", "adjoint_se.cu", "adjoint_col.cu", "kernels_misc.cu", "geometry.cpp"]
+SOURCES = ["context.cu", "kernels_se.cu", "kernels_col.cu", "kernels_colg.cu", "columns.cu", "adjoint_se.cu", "adjoint_col.cu", "kernels_misc.cu", "kernels_topo.cu", "geometry.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -87,6 +87,12 @@ class DycoreConfig:
     test_dycore_consistency: bool = False
     # the caller's element layout: (elem_map [Nh], elem_orient [Nh]) arrays, None: library order
     layout: tuple = None
+    # terrain-following levels (src/topography/topography.jl): the surface elevation of every
+    # node [Nh, 16] in m (None: flat), the warp ("linear" or "sleve") and SLEVE's eta_h and s
+    z_surface: object = None
+    warp: str = "linear"
+    sleve_eta: float = 0.7
+    sleve_s: float = 10.0
 
     def __post_init__(self):
         if self.nu is None:

@@ -61,6 +61,29 @@ class Geometry:
         self.zc = 0.5 * (self.zf[1:] + self.zf[:-1])
         self.n_center, self.n_face = nc.value, nf.value
         assert H * 4 * self.Nv == self.n_center
+        self.terrain = None
+        if getattr(cfg, "z_surface", None) is not None:
+            self.terrain = {"zc": terrain_centre_heights(cfg, self.zf)}
+
+
+def warp_factor(cfg, zeta):
+    """b(zeta) of the terrain-following levels z = zeta + z_s b(zeta) (gb_config.warp): linear
+    decay to z_max, or the one-scale SLEVE decay (src/topography/topography.jl:272-307)."""
+    zeta = np.asarray(zeta, dtype=np.float64)
+    if getattr(cfg, "warp", "linear") == "linear":
+        return 1.0 - zeta / cfg.z_max
+    eta = zeta / cfg.z_max
+    b = np.sinh((cfg.sleve_eta - eta) / (cfg.sleve_s * cfg.sleve_eta)) / np.sinh(1.0 / cfg.sleve_s)
+    return np.where(eta <= cfg.sleve_eta, b, 0.0)
+
+
+def terrain_centre_heights(cfg, zf):
+    """Heights [Nh, 16, Nv] of the centres over cfg.z_surface [Nh, 16]: midway between the
+    warped faces zeta_k + z_s b(zeta_k)."""
+    zs = np.asarray(cfg.z_surface, dtype=np.float64).reshape(-1, 16)[..., None]
+    zf = np.asarray(zf, dtype=np.float64)
+    zw = zf + zs * warp_factor(cfg, zf)
+    return 0.5 * (zw[..., 1:] + zw[..., :-1])
 
 
 def _check(ctx, rc):

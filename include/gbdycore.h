@@ -77,6 +77,24 @@ typedef struct {
      slots) with NaN before each tendency evaluation and each step, so that a read of a
      quantity not recomputed first shows up as NaN in the result.  0 off. */
   int test_dycore_consistency;
+  /* Terrain-following levels (topography: src/topography/topography.jl with the hypsography of
+     the extruded space, src/simulation/grids.jl).  z_surface is the surface elevation in m at
+     every node, in the caller's element and node order ([Nh][16], FP64), the collocated copies
+     of a node holding the same value; NULL is a flat surface.  The face heights are
+     z = zeta + z_s b(zeta) over the flat faces zeta (the centres midway between warped faces):
+     warp 0 decays the terrain linearly to zero at z_max (LinearWarp), b = 1 - zeta / z_max;
+     warp 1 is the one-scale SLEVE coordinate (SLEVEWarp) with eta_h = sleve_eta and
+     s = sleve_s, b = sinh((eta_h - eta) / (s eta_h)) / sinh(1 / s) for eta = zeta / z_max
+     <= eta_h, else 0.  The metric of every point (J, g^ij, g_ij with their vertical cross
+     terms) follows from z_s, its spectral derivatives in each element and b; the kernels
+     compute it where they use it.  Supported by gb_step, gb_remaining_tendency,
+     gb_set_precomputed_quantities (the filter u_3 = -u_h^3 / g^33), gb_global_sums and
+     gb_time_kernel; the column hooks (implicit tendency, Jacobian, ldiv, post-Newton
+     correction), the reverse-mode entries and the Held-Suarez forcing return GB_ERR_ARG for a
+     terrain context. */
+  const double *z_surface;
+  int warp;
+  double sleve_eta, sleve_s;
 } gb_config;
 
 typedef struct {

@@ -1,0 +1,130 @@
+"""GPU parity over terrain-following levels: the terrain slab kernels, the column stage with
+the column's own metric, the impenetrable filter u_3 = -u_h^3 / g^33 and the compensated
+sums, through the C ABI, against the CPU oracle's terrain path (tests/test_topography_oracle.py
+pins that path by conservation, the filter, the exact mass-row Jacobian and the flat limit).
+
+Tolerances (max-norm error relative to each component's max magnitude): FP64 tendencies
+<= 1e-12; FP64 steps as the flat steps on the small grids (rho, rho e_tot 1e-14, u_h 1e-12,
+u_3 2e-11: the conditioning of u_3's tendency, see test_gpu_parity.py); FP32 tendencies
+against the FP32 oracle <= 1e-4; FP32 steps against the FP64 oracle as the flat FP32 runs
+(rho, rho e_tot 1e-5; u_h 1e-3; u_3 1e-2)."""
+import copy
+
+import numpy as np
+import pytest
+
+import oracle as O
+import topography as T
+from gbdycore import _native as N
+from gbdycore import setups as S
+from gbdycore import simulation as sim
+from helpers import field_errors, oracle_geometry, small_config
+
+pytestmark = pytest.mark.gpu
+
+WARPS = {"linear": T.LinearWarp(), "sleve": T.SLEVEWarp()}
+
+
+def _setup(ft=np.float64, h=3, z=8, warp="linear", surface=None, seed=7):
+    cfg = small_config(ft=ft, h_elem=h, z_elem=z)
+    g = copy.copy(oracle_geometry(cfg.with_(ft=np.float64)))
+    zs = T.smooth_surface(g.xyz) if surface is None else surface(g)
+    g.terrain = T.oracle_terrain(g, zs, WARPS[warp])
+    cfgt = cfg.with_(z_surface=zs, warp=warp)
+    o = O.Oracle(g, cfg.with_(ft=np.float64).oracle_params(dss_stage1=False))
+    Yc, Yf = S.workload_state(g, cfg.with_(ft=np.float64), "plain")
+    rng = np.random.default_rng(seed)
+    dzf = g.terrain["Jf"] / (g.Jh[..., None] * ((g.R + g.terrain["zf"]) / g.R) ** 2)
+    Yf = rng.normal(0, 0.05, size=Yf.shape) * dzf
+    Yc[:, 3] *= 1 + 1e-3 * rng.normal(size=Yc[:, 3].shape)
+    o.dss(Yc, Yf)
+    return cfgt, g, o, Yc, Yf
+
+
+def _dev(Yc, Yf, ft):
+    return sim.FieldVector.from_numpy(np.ascontiguousarray(Yc, ft), np.ascontiguousarray(Yf, ft))
+
+
+def _assert(errs, tol):
+    tol = tol if isinstance(tol, dict) else {k: tol for k in errs}
+    bad = {k: v for k, v in errs.items() if not v <= tol[k]}
+    assert not bad, (bad, errs)
+
+
+@pytest.mark.parametrize("ft,tol", [(np.float64, 1e-12), (np.float32, 1e-4)])
+@pytest.mark.parametrize("warp", ["linear", "sleve"])
+def test_terrain_remaining_tendency(ft, tol, warp):
+    cfg, g, o, Yc, Yf = _setup(ft, warp=warp)
+    ref = O.Oracle(g, cfg.with_(ft=np.float64).oracle_params(dss_stage1=False), ft).remaining_tendency(
+        Yc.astype(ft), Yf.astype(ft))
+    p = sim.AtmosCache(cfg)
+    Y = _dev(Yc, Yf, ft)
+    Yt = Y.similar()
+    sim.remaining_tendency(Yt, None, Y, p, 0.0)
+    Tc, Tf = Yt.numpy()
+    _assert(field_errors(Tc, Tf, ref[0], ref[1]), tol)
+
+
+def test_terrain_filter_and_global_sums():
+    cfg, g, o, Yc, Yf = _setup()
+    Rc, Rf = Yc.copy(), Yf.copy()
+    o.set_precomputed(Rc, Rf)
+    p = sim.AtmosCache(cfg)
+    Y = _dev(Yc, Yf, np.float64)
+    sim.set_precomputed_quantities(Y, p, 0.0)
+    _, Gf = Y.numpy()
+    for k in (0, -1):
+        assert np.abs(Gf[..., k] - Rf[..., k]).max() <= 1e-13 * np.abs(Rf[..., k]).max()
+    assert np.abs(Rf[..., 0]).max() > 0
+    assert np.array_equal(Gf[..., 1:-1], Yf[..., 1:-1])
+    s = p.global_sums(Y)
+    r = o.global_sums(Yc)
+    assert np.all(np.abs(s - r) <= 1e-13 * np.abs(r))
+
+
+@pytest.mark.parametrize("warp", ["linear", "sleve"])
+def test_terrain_step_fp64_matches_oracle(warp):
+    cfg, g, o, Yc, Yf = _setup(warp=warp)
+    rc, rf = Yc.copy(), Yf.copy()
+    o.step(rc, rf, cfg.dt, 3)
+    s = sim.AtmosSimulation(cfg, state=(Yc, Yf))
+    s.step(3, use_graph=True)
+    Gc, Gf = s.Y.numpy()
+    _assert(field_errors(Gc, Gf, rc, rf), {"rho": 1e-14, "rho_e_tot": 1e-14, "u_1": 1e-12, "u_2": 1e-12, "u_3": 2e-11})
+    assert np.abs(Gf[..., 0]).max() > 0   # the filter's value over the terrain, not zero
+
+
+def test_terrain_fp32_step_against_fp64_oracle():
+    cfg, g, o, Yc, Yf = _setup(np.float32, h=4, z=10)
+    rc, rf = Yc.copy(), Yf.copy()
+    o.step(rc, rf, cfg.dt, 2)
+    s = sim.AtmosSimulation(cfg, state=(Yc.astype(np.float32), Yf.astype(np.float32)))
+    s.step(2, use_graph=True)
+    Gc, Gf = s.Y.numpy()
+    _assert(field_errors(Gc, Gf, rc, rf), {"rho": 1e-5, "rho_e_tot": 1e-5, "u_1": 1e-3, "u_2": 1e-3, "u_3": 1e-2})
+
+
+def test_flat_surface_terrain_context_matches_the_flat_step():
+    """z_s = 0 through the terrain kernels equals the flat kernels (independent of the oracle)."""
+    cfg, g, o, Yc, Yf = _setup(surface=lambda g: np.zeros((g.Nh, 16)))
+    flat = cfg.with_(z_surface=None)
+    a = sim.AtmosSimulation(cfg, state=(Yc, Yf))
+    b = sim.AtmosSimulation(flat, state=(Yc, Yf))
+    a.step(2)
+    b.step(2)
+    Ac, Af = a.Y.numpy()
+    Bc, Bf = b.Y.numpy()
+    _assert(field_errors(Ac, Af, Bc, Bf), {"rho": 1e-14, "rho_e_tot": 1e-14, "u_1": 1e-12, "u_2": 1e-12, "u_3": 2e-11})
+
+
+def test_terrain_context_refuses_what_is_not_built():
+    cfg, g, o, Yc, Yf = _setup()
+    p = sim.AtmosCache(cfg)
+    Y = _dev(Yc, Yf, np.float64)
+    Yt = Y.similar()
+    for call in (lambda: sim.implicit_tendency(Yt, Y, p, 0.0),
+                 lambda: sim.update_jacobian(None, Y, p, 10.0, 0.0),
+                 lambda: p.call("gb_step_vjp", Yt.gb(), Y.gb(), 0.0, float(cfg.dt), None)):
+        with pytest.raises(N.GBError) as ei:
+            call()
+        assert ei.value.code == N.GB_ERR_ARG and "terrain" in str(ei.value)

@@ -59,6 +59,8 @@ def parse(argv=None):
     ap.add_argument("--held-suarez-steps", type=int, default=20)
     ap.add_argument("--held-suarez-long", type=int, default=1000)
     ap.add_argument("--no-held-suarez", action="store_true")
+    ap.add_argument("--topography-steps", type=int, default=20)
+    ap.add_argument("--no-topography", action="store_true")
     # bracket one forward step ("step") or one reverse pass ("reverse") by
     # cudaProfilerStart/Stop, for `ncu --profile-from-start off`; no effect otherwise
     ap.add_argument("--profile-region", default="none", choices=["none", "step", "reverse"])
@@ -389,6 +391,12 @@ def run_gb300(args):
     held_suarez = None
     if not args.no_held_suarez:
         held_suarez = measure_held_suarez(args, ms)
+    topography = None
+    if not args.no_topography:
+        try:
+            topography = measure_topography(args, ms)
+        except Exception as e:  # reported in the line, not fatal to the headline
+            topography = {"error": "%s: %s" % (type(e).__name__, e)}
     config1 = None
     if not args.no_config1:
         try:
@@ -429,7 +437,7 @@ def run_gb300(args):
                             "post-Newton correction, DSS) with unfused torch stage algebra"},
                 "fp32_vs_fp64": prec, "fp64_step": fp64, "batching": batching, "adjoint": adjoint,
                 "differentiation": differentiation, "precision_h60": h60, "held_suarez": held_suarez,
-                "config1": config1,
+                "topography": topography, "config1": config1,
                 "clocks": clk, "gpu_launches": LAUNCHES_PER_STEP * args.steps}
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -653,6 +661,68 @@ def measure_held_suarez(args, fwd_ms):
     del s
     torch.cuda.empty_cache()
     return out
+
+
+def measure_topography(args, fwd_ms):
+    """The production step over terrain-following levels: the DCMIP-2-0-0 mountain (2 km)
+    under the linear warp, FP32: SYPD, the cost over the flat step, the terrain kernels'
+    times and achieved bandwidth of their algorithmic bytes (those of the flat kernels plus the
+    four terrain rows of each element), mass conservation, and the FP32 state against the FP64
+    library after the timed steps."""
+    import ctypes
+    import torch
+    from gbdycore import config as C, simulation as sim
+    from gbdycore import setups as S
+    base = C.production_h30()
+    g = sim.Geometry(base)
+    lat = np.degrees(np.arctan2(g.xyz[..., 2], np.hypot(g.xyz[..., 0], g.xyz[..., 1])))
+    lon = np.degrees(np.arctan2(g.xyz[..., 1], g.xyz[..., 0])) % 360.0
+    zs = dcmip200_surface(lat, lon)
+    cfg = base.with_(z_surface=zs, warp="linear")
+    s = sim.AtmosSimulation(cfg, workload="production")
+    m0 = s.p.global_sums(s.Y)[0]
+    s.step(3)
+    torch.cuda.synchronize()
+    n = args.topography_steps
+    ms, _ = _timed(lambda: s.step(n))
+    ms /= n
+    m1 = s.p.global_sums(s.Y)[0]
+    kern = {}
+    fb = 4
+    extra = 6 * cfg.h_elem ** 2 * 4 * 16 * fb  # the TG_N terrain rows of every element
+    for name, kid in (("k_topo_passA", 0), ("k_topo_passB", 1), ("k_col_stage_g (terrain)", 2)):
+        t = ctypes.c_double()
+        s.p.call("gb_time_kernel", kid, s.Y.gb(), 20, ctypes.byref(t))
+        b = algorithmic_bytes(cfg, kid) + (extra if kid < 2 else 0)
+        kern[name] = {"ms": t.value, "algorithmic_bytes": b, "GBps": b / (t.value * 1e-3) / 1e9}
+    finite = bool(torch.isfinite(s.Y.c).all() and torch.isfinite(s.Y.f).all())
+    # FP32 against the FP64 library over the same terrain
+    c64 = cfg.with_(ft=np.float64)
+    Yc, Yf = S.workload_state(sim.Geometry(c64), c64, "production")
+    s64 = sim.AtmosSimulation(c64, state=(Yc, Yf))
+    s32 = sim.AtmosSimulation(cfg, state=(Yc.astype(np.float32), Yf.astype(np.float32)))
+    k = args.precision_steps
+    s64.step(k)
+    s32.step(k)
+    prec = {"steps": k}
+    prec.update(field_errors(s32.Y.numpy(), s64.Y.numpy()))
+    out = {"surface": "DCMIP-2-0-0 mountain (2 km peak on the equator at 270 E), linear warp",
+           "steps": n + 3, "ms_per_step": ms, "value": sypd(cfg.dt, ms / 1e3), "unit": UNIT,
+           "over_flat_step": ms / fwd_ms, "mass_rel_change": abs(m1 - m0) / abs(m0), "finite": finite,
+           "kernels": kern, "fp32_vs_fp64": prec}
+    del s, s64, s32
+    torch.cuda.empty_cache()
+    return out
+
+
+def dcmip200_surface(lat, lon):
+    """The DCMIP-2-0-0 mountain (src/topography/topography.jl:186-205): a cosine bell of 2 km
+    over a great-circle radius of 3 pi / 4 around (0 N, 270 E), modulated by cosine ridges of
+    half-width pi / 16; latitude and longitude in degrees."""
+    d2r = np.pi / 180.0
+    r = np.arccos(np.clip(np.cos(lat * d2r) * np.cos((lon - 270.0) * d2r), -1.0, 1.0))
+    R_m, zeta_m = 3 * np.pi / 4, np.pi / 16
+    return np.where(r < R_m, 1000.0 * (1 + np.cos(np.pi * r / R_m)) * np.cos(np.pi * r / zeta_m) ** 2, 0.0)
 
 
 def measure_differentiation(args):

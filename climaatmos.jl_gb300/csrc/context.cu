@@ -257,7 +257,9 @@ int create_impl(gb_ctx *ctx) {
   if (g.topo) {
     if (topo_smem<FT>(Nv) > (size_t)optin)
       return fail(ctx, GB_ERR_ARG, "z_elem too large for the terrain slab kernels at this precision (shared memory)");
-    configure_topo<FT>(Nv);
+    const cudaError_t e = configure_topo<FT>(Nv);
+    if (e != cudaSuccess)
+      return fail(ctx, GB_ERR_CUDA, std::string("terrain slab kernels: ") + cudaGetErrorString(e));
   }
   CK(cudaGetLastError());
   return GB_OK;

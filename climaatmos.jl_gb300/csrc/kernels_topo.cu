@@ -33,7 +33,7 @@ constexpr int TS_LEVELS = TS_THREADS / 4;
 
 template <class FT>
 struct TopoALayout {
-  size_t y[2], f[2], g[2], t[2], out, bar, total;
+  size_t y[2], f[2], g[2], t[2], out, w, bar, total;
   __host__ __device__ TopoALayout(int Nv, int nbuf) {
     const int Nf = Nv + 1;
     size_t o = 0;
@@ -48,6 +48,7 @@ struct TopoALayout {
       }
     }
     out = o; o += align16(sizeof(FT) * 64 * Nv);
+    w = o; o += align16(sizeof(FT) * 2 * 16);     // GLL weights W, 1/W
     bar = o; o += 16;
     total = o;
   }
@@ -255,8 +256,7 @@ __global__ void __launch_bounds__(TS_THREADS, 1) k_topo_passA(DevParams<FT> P, i
   const int Nv = P.Nv, Nf = P.Nf;
   const TopoALayout<FT> Lo(Nv, nbuf);
   auto at = [&](const size_t (&off)[2], int b) { return (FT *)(sm + (b ? off[1] : off[0])); };
-  FT *sO = (FT *)(sm + Lo.out);
-  __shared__ __align__(16) FT sW[2 * NN];
+  FT *sO = (FT *)(sm + Lo.out), *sW = (FT *)(sm + Lo.w);
   uint64_t *bar = (uint64_t *)(sm + Lo.bar);
   const uint32_t by = uint32_t(sizeof(FT) * 64 * Nv), bf = uint32_t(sizeof(FT) * 16 * Nf);
   const uint32_t bg = uint32_t(sizeof(FT) * HG_N * 16), bt = uint32_t(sizeof(FT) * TG_N * 16);
@@ -697,10 +697,11 @@ template <class FT>
 size_t topo_smem(int Nv) { return TopoBLayout<FT>(Nv, 1).total; }
 
 template <class FT>
-void configure_topo(int Nv) {
+cudaError_t configure_topo(int Nv) {
   (void)Nv;
-  cudaFuncSetAttribute(k_topo_passA<FT>, cudaFuncAttributeMaxDynamicSharedMemorySize, ts_dev().optin);
-  cudaFuncSetAttribute(k_topo_passB<FT>, cudaFuncAttributeMaxDynamicSharedMemorySize, ts_dev().optin);
+  cudaError_t e = cudaFuncSetAttribute(k_topo_passA<FT>, cudaFuncAttributeMaxDynamicSharedMemorySize, ts_dev().optin);
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(k_topo_passB<FT>, cudaFuncAttributeMaxDynamicSharedMemorySize, ts_dev().optin);
 }
 
 template <class FT>
@@ -731,7 +732,7 @@ void launch_dss_reduced(const DevParams<FT> &P, FT *C, FT *F, cudaStream_t s) {
 
 #define INST(FT)                                                                                                  \
   template size_t topo_smem<FT>(int);                                                                             \
-  template void configure_topo<FT>(int);                                                                          \
+  template cudaError_t configure_topo<FT>(int);                                                                   \
   template void launch_topo_passA<FT>(const DevParams<FT> &, const FT *, const FT *, FT *, cudaStream_t);         \
   template void launch_topo_passB<FT>(const DevParams<FT> &, const FT *, const FT *, const FT *, FT *, FT *,       \
                                       cudaStream_t);                                                              \

@@ -69,6 +69,43 @@ struct GBConfig
     elem_orient::Ptr{Cint}
     # numerics.test_dycore_consistency: NaN-fill the library's scratch before each use
     test_dycore_consistency::Cint
+    # terrain-following levels: surface elevation per node (caller's element and node order),
+    # C_NULL: flat; warp 0 linear (LinearAdaption), 1 SLEVE (SLEVEAdaption) with eta_h and s
+    z_surface::Ptr{Cdouble}
+    warp::Cint
+    sleve_eta::Cdouble
+    sleve_s::Cdouble
+end
+
+# A copy of cfg with the named fields replaced.
+function with_fields(cfg::GBConfig; kw...)
+    vals = map(f -> haskey(kw, f) ? kw[f] : getfield(cfg, f), fieldnames(GBConfig))
+    return GBConfig(vals...)
+end
+
+"""
+    terrain(space) -> (z_surface, warp, eta_h, s) or nothing
+
+The surface elevation of a ClimaCore extruded space with hypsography (its grid's
+`hypsography.surface`, a field on the horizontal space), as a [Nh][16] array in the space's
+element and node order (node n = i + 4 j), and the warp: LinearAdaption -> 0, SLEVEAdaption ->
+1 with its eta_h and s.  `nothing` for a flat space.
+"""
+function terrain(space)
+    grid = Spaces.grid(space)
+    hasproperty(grid, :hypsography) || return nothing
+    hyps = grid.hypsography
+    hasproperty(hyps, :surface) || return nothing
+    zs = Array(parent(hyps.surface))                        # (Nq, Nq, 1, Nh)
+    Nq, _, _, Nh = size(zs)
+    out = Array{Cdouble}(undef, Nq, Nq, Nh)                # C order [Nh][16], n = i + 4 j
+    for h in 1:Nh, j in 1:Nq, i in 1:Nq
+        out[i, j, h] = zs[i, j, 1, h]
+    end
+    if hasproperty(hyps, :ηₕ)
+        return out, Cint(1), Cdouble(hyps.ηₕ), Cdouble(hyps.s)
+    end
+    return out, Cint(0), 0.7, 10.0
 end
 
 struct GBFieldVec
@@ -160,16 +197,19 @@ function GBContext(cfg::GBConfig; space = nothing)
         rc = ccall((:gb_ctx_create, libgbdycore), Cint, (Ref{GBConfig}, Ref{Ptr{Cvoid}}), cfg, h)
     else
         elem_map, elem_orient = element_layout(cfg, space)
-        rc = GC.@preserve elem_map elem_orient begin
-            c = GBConfig((getfield(cfg, f) for f in fieldnames(GBConfig)[1:end-3])...,
-                pointer(elem_map), pointer(elem_orient), cfg.test_dycore_consistency)
+        t = terrain(space)
+        zs = t === nothing ? Cdouble[] : t[1]
+        rc = GC.@preserve elem_map elem_orient zs begin
+            c = with_fields(cfg; elem_map = pointer(elem_map), elem_orient = pointer(elem_orient))
+            if t !== nothing
+                c = with_fields(c; z_surface = pointer(zs), warp = t[2], sleve_eta = t[3], sleve_s = t[4])
+            end
             ccall((:gb_ctx_create, libgbdycore), Cint, (Ref{GBConfig}, Ref{Ptr{Cvoid}}), c, h)
         end
     end
     rc == GB_OK || error("gb_ctx_create failed with status $rc")
-    # the library copies the layout into its tables; the context keeps no pointer to it
-    ctx = GBContext(h[], GBConfig((getfield(cfg, f) for f in fieldnames(GBConfig)[1:end-3])...,
-        C_NULL, C_NULL, cfg.test_dycore_consistency))
+    # the library copies the layout and the surface into its tables; the context keeps no pointer
+    ctx = GBContext(h[], with_fields(cfg; elem_map = C_NULL, elem_orient = C_NULL, z_surface = C_NULL))
     finalizer(c -> ccall((:gb_ctx_destroy, libgbdycore), Cint, (Ptr{Cvoid},), c.handle), ctx)
     # work on CUDA.jl's task-local stream
     stream = CUDA.stream().handle

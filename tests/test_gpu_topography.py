@@ -74,7 +74,8 @@ def test_terrain_filter_and_global_sums():
     sim.set_precomputed_quantities(Y, p, 0.0)
     _, Gf = Y.numpy()
     for k in (0, -1):
-        assert np.abs(Gf[..., k] - Rf[..., k]).max() <= 1e-13 * np.abs(Rf[..., k]).max()
+        # -CT3(u_h) / g^33 from the closed-form metric here, from the inverted 3x3 metric in the oracle
+        assert np.abs(Gf[..., k] - Rf[..., k]).max() <= 1e-12 * np.abs(Rf[..., k]).max()
     assert np.abs(Rf[..., 0]).max() > 0
     assert np.array_equal(Gf[..., 1:-1], Yf[..., 1:-1])
     s = p.global_sums(Y)
@@ -96,6 +97,23 @@ def test_terrain_step_fp64_matches_oracle(warp):
 
 def test_terrain_fp32_step_against_fp64_oracle():
     cfg, g, o, Yc, Yf = _setup(np.float32, h=4, z=10)
+    rc, rf = Yc.copy(), Yf.copy()
+    o.step(rc, rf, cfg.dt, 2)
+    s = sim.AtmosSimulation(cfg, state=(Yc.astype(np.float32), Yf.astype(np.float32)))
+    s.step(2, use_graph=True)
+    Gc, Gf = s.Y.numpy()
+    _assert(field_errors(Gc, Gf, rc, rf), {"rho": 1e-5, "rho_e_tot": 1e-5, "u_1": 1e-3, "u_2": 1e-3, "u_3": 1e-2})
+
+
+def test_terrain_step_production_levels_fp32():
+    """The production column (63 levels stretched from 30 m): the slabs exceed the default
+    48 KB of dynamic shared memory and the column stage takes its 32-lane form."""
+    cfg, g, o, Yc, Yf = _setup(np.float32, h=2, z=63)
+    cfg = cfg.with_(dz_bottom=30.0)
+    g = copy.copy(oracle_geometry(cfg.with_(ft=np.float64, z_surface=None)))
+    g.terrain = T.oracle_terrain(g, cfg.z_surface, WARPS["linear"])
+    o = O.Oracle(g, cfg.with_(ft=np.float64).oracle_params(dss_stage1=False))
+    Yc, Yf = S.workload_state(g, cfg.with_(ft=np.float64), "plain")
     rc, rf = Yc.copy(), Yf.copy()
     o.step(rc, rf, cfg.dt, 2)
     s = sim.AtmosSimulation(cfg, state=(Yc.astype(np.float32), Yf.astype(np.float32)))

@@ -309,7 +309,7 @@ template <class FT>
 int column_hook_t(gb_ctx *ctx, int mode, gb_fieldvec O, gb_fieldvec Y, double dtg) {
   Impl<FT> *I = impl<FT>(ctx);
   if (mode == COL_JACOBIAN && !I->jac.p) {
-    int r = alloc(ctx, I->jac, (size_t)I->P.Nh * NN * JAC_Q * I->P.Nf * sizeof(FT));
+    int r = alloc(ctx, I->jac, (size_t)I->P.Nh * NN * (I->P.topo ? JAC_QT : JAC_Q) * I->P.Nf * sizeof(FT));
     if (r) return r;
   }
   if (mode == COL_LDIV && !I->jac_valid) return fail(ctx, GB_ERR_STATE, "gb_ldiv called before gb_update_jacobian");
@@ -1292,7 +1292,6 @@ int gb_remaining_tendency(gb_ctx *ctx, gb_fieldvec Yt, gb_fieldvec Y, double t) 
 int gb_implicit_tendency(gb_ctx *ctx, gb_fieldvec Yt, gb_fieldvec Y, double t) {
   GB_RANGE();
   GUARD(ctx);
-  NO_TERRAIN(ctx, "gb_implicit_tendency");
   (void)t;
   if (!fv_ok(Y) || !fv_ok(Yt)) return fail(ctx, GB_ERR_ARG, "null or misaligned pointer");
   return DISPATCH(ctx, column_hook_t, ctx, (int)COL_IMPLICIT, Yt, Y, 0.0);
@@ -1301,7 +1300,6 @@ int gb_implicit_tendency(gb_ctx *ctx, gb_fieldvec Yt, gb_fieldvec Y, double t) {
 int gb_update_jacobian(gb_ctx *ctx, gb_fieldvec Y, double dtgamma, double t) {
   GB_RANGE();
   GUARD(ctx);
-  NO_TERRAIN(ctx, "gb_update_jacobian");
   (void)t;
   if (!fv_ok(Y)) return fail(ctx, GB_ERR_ARG, "null or misaligned pointer");
   gb_fieldvec none{nullptr, nullptr};
@@ -1311,7 +1309,6 @@ int gb_update_jacobian(gb_ctx *ctx, gb_fieldvec Y, double dtgamma, double t) {
 int gb_ldiv(gb_ctx *ctx, gb_fieldvec dY, gb_fieldvec R) {
   GB_RANGE();
   GUARD(ctx);
-  NO_TERRAIN(ctx, "gb_ldiv");
   if (!fv_ok(dY) || !fv_ok(R)) return fail(ctx, GB_ERR_ARG, "null or misaligned pointer");
   return DISPATCH(ctx, column_hook_t, ctx, (int)COL_LDIV, dY, R, 0.0);
 }
@@ -1319,7 +1316,6 @@ int gb_ldiv(gb_ctx *ctx, gb_fieldvec dY, gb_fieldvec R) {
 int gb_correct_implicit_advection_tendency(gb_ctx *ctx, gb_fieldvec Yt, gb_fieldvec Y, double t) {
   GB_RANGE();
   GUARD(ctx);
-  NO_TERRAIN(ctx, "gb_correct_implicit_advection_tendency");
   (void)t;
   if (!fv_ok(Y) || !fv_ok(Yt)) return fail(ctx, GB_ERR_ARG, "null or misaligned pointer");
   return DISPATCH(ctx, column_hook_t, ctx, (int)COL_POSTIMP, Yt, Y, 0.0);

@@ -98,6 +98,7 @@ struct CotArgs {
 
 enum ColMode { COL_STAGE = 0, COL_IMPLICIT = 1, COL_JACOBIAN = 2, COL_LDIV = 3, COL_POSTIMP = 4 };
 constexpr int JAC_Q = 15;  // stored Jacobian quantities per level
+constexpr int JAC_QT = JAC_Q + 6;  // over terrain: with the (rho, u_h), (rho e_tot, u_h) blocks
 
 template <class FT>
 struct ColArgs {

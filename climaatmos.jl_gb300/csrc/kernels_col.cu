@@ -18,7 +18,9 @@
 //     central, implicit_tendency.jl:322-339) applied as U += dtgamma * corr,
 //   T_imp_i = (U - U^) / dtgamma, and the FP64 residual sums of squares.
 // The other modes are the individual hooks.
-#include "kernels.cuh"
+#include <type_traits>
+
+#include "colcore.cuh"
 
 namespace gb {
 
@@ -124,47 +126,116 @@ template <class FT, int M>
 struct ColState {
   FT rho[M], u1[M], u2[M], rhoe[M], u3[M];
 };
+// Over terrain-following levels (TOPO) also: w3c = g^33 u_3 of the faces (u3c is then the full
+// u^3 = u_h^3 + g^33 u_3), ct3 = CT3(u_h) of the centres, the face's g^33 and the centre's Phi.
 template <class FT, int M>
 struct ColDiag {
   FT c1[M], c2[M], K[M], T[M], h[M], Pi[M], thv[M], thvr[M], phid[M], rJ[M], u3c[M], J[M], iJ[M];
+  FT w3c[M], ct3[M], g33[M], phi[M];
 };
 
-
+// The impenetrable filter over terrain on a state held M levels per lane: u_3 = -CT3(u_h) / g^33
+// of the adjacent centre on the bottom and top faces, 0 beyond the column.
 template <class FT, int M>
-__device__ __forceinline__ void col_diag(const DevParams<FT> &P, const ColGeo<FT> &G, const ColState<FT, M> &S,
-                                         ColDiag<FT, M> &Dg, int lane) {
+__device__ __forceinline__ void col_filter_topo(const col::ColLevT<FT> &T, ColState<FT, M> &S, int lane) {
+  const int Nv = T.Nv, Nf = T.Nf;
+  FT ct3[M], ctm[M];
+#pragma unroll
+  for (int k = 0; k < M; ++k) {
+    const int v = min(lane * M + k, Nv - 1);
+    FT g31, g32, phis;
+    T.ct(v, g31, g32, phis);
+    ct3[k] = g31 * S.u1[k] + g32 * S.u2[k];
+  }
+  nb_all<M, -1>(ct3, ctm);
+#pragma unroll
+  for (int k = 0; k < M; ++k) {
+    const int f = lane * M + k;
+    if (f == 0) S.u3[k] = -ct3[k] / T.f4(0).x;
+    else if (f == Nv) S.u3[k] = -ctm[k] / T.f4(Nv).x;
+    else if (f > Nv) S.u3[k] = FT(0);
+  }
+  (void)Nf;
+}
+
+template <class FT, int M, bool TOPO, class LV>
+__device__ __forceinline__ void col_diag(const DevParams<FT> &P, const ColGeo<FT> &G, const LV &T,
+                                         const ColState<FT, M> &S, ColDiag<FT, M> &Dg, int lane) {
   const int Nv = P.Nv, Nf = P.Nf;
 #pragma unroll
   for (int k = 0; k < M; ++k) {
     const int f = min(lane * M + k, Nf - 1);
-    Dg.u3c[k] = S.u3[k] * P.levf[LF_G33 * Nf + f];
+    if constexpr (TOPO) {
+      Dg.g33[k] = T.f4(f).x;
+      Dg.w3c[k] = S.u3[k] * Dg.g33[k];
+    } else {
+      Dg.u3c[k] = S.u3[k] * P.levf[LF_G33 * Nf + f];
+    }
   }
   FT u3n[M], u3cn[M];
   nb_all<M, 1>(S.u3, u3n);
-  nb_all<M, 1>(Dg.u3c, u3cn);
+  nb_all<M, 1>(TOPO ? Dg.w3c : Dg.u3c, u3cn);
 #pragma unroll
   for (int k = 0; k < M; ++k) {
     const int v = min(lane * M + k, Nv - 1);
-    const FT r2 = P.levc[LC_R2 * Nv + v], dz = P.levc[LC_DZ * Nv + v], Phi = P.levc[LC_PHI * Nv + v];
-    const FT ir2 = P.levc[LC_IR2 * Nv + v];
-    const FT gu0 = G.gu0 * ir2, gu1 = G.gu1 * ir2, gu2 = G.gu2 * ir2;
-    const FT c1 = gu0 * S.u1[k] + gu1 * S.u2[k], c2 = gu1 * S.u1[k] + gu2 * S.u2[k];
-    const FT kv = (S.u3[k] * Dg.u3c[k] + u3n[k] * u3cn[k]) / FT(2);
-    const FT K = (S.u1[k] * c1 + S.u2[k] * c2 + kv) / FT(2);
-    Thermo<FT> th;
-    thermo(P, S.rho[k], S.rhoe[k], K, Phi, P.lr4[v], th);
-    Dg.c1[k] = c1; Dg.c2[k] = c2; Dg.K[k] = K; Dg.T[k] = th.T; Dg.h[k] = th.h; Dg.Pi[k] = th.Pi;
-    Dg.thv[k] = th.thv; Dg.thvr[k] = th.thvr; Dg.phid[k] = th.phid;
-    Dg.J[k] = G.Jh * r2 * dz;
-    Dg.iJ[k] = G.iJh * ir2 * P.levc[LC_IDZ * Nv + v];
-    Dg.rJ[k] = S.rho[k] * Dg.J[k];
+    if constexpr (TOPO) {
+      // the column's own metric; K takes 2 CT3(u_h) I^c(u_3) (compute_kinetic, utilities.jl:194-206)
+      // and CT12(ᶜu) takes g^a3 I^c(u_3)
+      const Lev4<FT> c4 = T.c4(v);
+      FT g31, g32, phis;
+      T.ct(v, g31, g32, phis);
+      const FT gu0 = G.gu0 * c4.z, gu1 = G.gu1 * c4.z, gu2 = G.gu2 * c4.z;
+      const FT h1 = gu0 * S.u1[k] + gu1 * S.u2[k], h2 = gu1 * S.u1[k] + gu2 * S.u2[k];
+      const FT ct3 = g31 * S.u1[k] + g32 * S.u2[k], ub3 = (S.u3[k] + u3n[k]) / FT(2);
+      const FT kv = (S.u3[k] * Dg.w3c[k] + u3n[k] * u3cn[k]) / FT(2);
+      const FT K = (S.u1[k] * h1 + S.u2[k] * h2 + kv + FT(2) * ct3 * ub3) / FT(2);
+      Thermo<FT> th;
+      thermo(P, S.rho[k], S.rhoe[k], K, c4.w, P.lr4[v], th);
+      Dg.c1[k] = h1 + g31 * ub3; Dg.c2[k] = h2 + g32 * ub3; Dg.K[k] = K; Dg.T[k] = th.T; Dg.h[k] = th.h;
+      Dg.Pi[k] = th.Pi; Dg.thv[k] = th.thv; Dg.thvr[k] = th.thvr; Dg.phid[k] = th.phid + phis;
+      Dg.ct3[k] = ct3;
+      Dg.phi[k] = c4.w;
+      Dg.J[k] = G.Jh * c4.x;
+      Dg.iJ[k] = G.iJh * c4.y;
+      Dg.rJ[k] = S.rho[k] * Dg.J[k];
+    } else {
+      const FT r2 = P.levc[LC_R2 * Nv + v], dz = P.levc[LC_DZ * Nv + v], Phi = P.levc[LC_PHI * Nv + v];
+      const FT ir2 = P.levc[LC_IR2 * Nv + v];
+      const FT gu0 = G.gu0 * ir2, gu1 = G.gu1 * ir2, gu2 = G.gu2 * ir2;
+      const FT c1 = gu0 * S.u1[k] + gu1 * S.u2[k], c2 = gu1 * S.u1[k] + gu2 * S.u2[k];
+      const FT kv = (S.u3[k] * Dg.u3c[k] + u3n[k] * u3cn[k]) / FT(2);
+      const FT K = (S.u1[k] * c1 + S.u2[k] * c2 + kv) / FT(2);
+      Thermo<FT> th;
+      thermo(P, S.rho[k], S.rhoe[k], K, Phi, P.lr4[v], th);
+      Dg.c1[k] = c1; Dg.c2[k] = c2; Dg.K[k] = K; Dg.T[k] = th.T; Dg.h[k] = th.h; Dg.Pi[k] = th.Pi;
+      Dg.thv[k] = th.thv; Dg.thvr[k] = th.thvr; Dg.phid[k] = th.phid;
+      Dg.J[k] = G.Jh * r2 * dz;
+      Dg.iJ[k] = G.iJh * ir2 * P.levc[LC_IDZ * Nv + v];
+      Dg.rJ[k] = S.rho[k] * Dg.J[k];
+    }
+  }
+  if constexpr (TOPO) {
+    // u^3 = ᶠwinterp(rho J, CT3(u_h)) + g^33 u_3 (the adjacent centre's CT3 on the boundary faces)
+    FT rJm[M], ctm[M];
+    nb_all<M, -1>(Dg.rJ, rJm);
+    nb_all<M, -1>(Dg.ct3, ctm);
+#pragma unroll
+    for (int k = 0; k < M; ++k) {
+      const int f = lane * M + k;
+      FT uh3;
+      if (f == 0) uh3 = Dg.ct3[k];
+      else if (f >= Nv) uh3 = ctm[k];
+      else uh3 = (rJm[k] * ctm[k] + Dg.rJ[k] * Dg.ct3[k]) / (rJm[k] + Dg.rJ[k]);
+      Dg.u3c[k] = uh3 + Dg.w3c[k];
+    }
   }
 }
 
 // implicit tendency (rho, rho e_tot, u_3) at the owned levels
-template <class FT, int M>
-__device__ __forceinline__ void col_implicit(const DevParams<FT> &P, const ColGeo<FT> &G, const ColState<FT, M> &S,
-                                             const ColDiag<FT, M> &Dg, FT (&Tr)[M], FT (&Te)[M], FT (&T3)[M], int lane) {
+template <class FT, int M, bool TOPO, class LV>
+__device__ __forceinline__ void col_implicit(const DevParams<FT> &P, const ColGeo<FT> &G, const LV &Tg,
+                                             const ColState<FT, M> &S, const ColDiag<FT, M> &Dg, FT (&Tr)[M],
+                                             FT (&Te)[M], FT (&T3)[M], int lane) {
   const int Nv = P.Nv, Nf = P.Nf;
   FT rJm[M], hm[M], phm[M], Pim[M], thm[M], thrm[M];
   nb_all<M, -1>(Dg.rJ, rJm); nb_all<M, -1>(Dg.h, hm); nb_all<M, -1>(Dg.phid, phm);
@@ -188,7 +259,8 @@ __device__ __forceinline__ void col_implicit(const DevParams<FT> &P, const ColGe
       const FT gPi = Dg.Pi[k] - Pim[k];
       val = -(gPhid + P.cpd * thd * gPi);
     }
-    val -= P.levf[LF_BETA * Nf + fc] * S.u3[k];
+    if constexpr (TOPO) val -= Tg.f4(fc).y * S.u3[k];
+    else val -= P.levf[LF_BETA * Nf + fc] * S.u3[k];
     T3[k] = val;
   }
   FT fln[M], fhn[M];
@@ -203,21 +275,37 @@ __device__ __forceinline__ void col_implicit(const DevParams<FT> &P, const ColGe
 
 // Jacobian blocks at the owned levels (centre rows: Mru/Meu for faces v, v+1;
 // face rows: Mur/Mue/Muh for centres k-1, k, Muu for faces k-1, k, k+1).
+// Over terrain six more quantities per centre v carry the (rho, u_h) and (rho e_tot, u_h) blocks
+// (manual_sparse_jacobian.jl:150-187, 745-786): the interior face k's flux rho-bar J u^3 holds
+// 1/2 sum_c rho_c J_c CT3(u_h)_c over its two centres, so with ct_c = g^31_c x_1,c + g^32_c x_2,c
+//   d(rho_t)_v . x   = dtγ [hm (ct_{v-1} + ... ) ...] = wm ct_{v-1} + (w0m - w0p) ct_v - wp ct_{v+1}
+//   d(rhoe_t)_v . x  = hb0 (wm ct_{v-1} + w0m ct_v) - hb1 (w0p ct_v + wp ct_{v+1})
+// with wm = dtγ rho_{v-1} J_{v-1} / (2 J_v) (face v interior), w0m = dtγ rho_v / 2 (face v
+// interior), w0p = dtγ rho_v / 2 (face v+1 interior), wp = dtγ rho_{v+1} J_{v+1} / (2 J_v) (face
+// v+1 interior), hb0, hb1 the face means of h_tot; g^3a is geometry and is recomputed where used.
 template <class FT, int M>
 struct ColJac {
   FT ru0[M], ru1[M], eu0[M], eu1[M];
   FT ur0[M], ur1[M], ue0[M], ue1[M], uh0[M], uh1[M], uh2[M], uh3[M], uu0[M], uu1[M], uu2[M];
+  FT wm[M], w0m[M], w0p[M], wp[M], hb0[M], hb1[M];
 };
 
-template <class FT, int M>
-__device__ __forceinline__ void col_jacobian(const DevParams<FT> &P, const ColGeo<FT> &G, const ColState<FT, M> &S,
-                                             const ColDiag<FT, M> &Dg, FT dtg, ColJac<FT, M> &Jc, int lane) {
+template <class FT, int M, bool TOPO, class LV>
+__device__ __forceinline__ void col_jacobian(const DevParams<FT> &P, const ColGeo<FT> &G, const LV &Tg,
+                                             const ColState<FT, M> &S, const ColDiag<FT, M> &Dg, FT dtg,
+                                             ColJac<FT, M> &Jc, int lane) {
   const int Nv = P.Nv, Nf = P.Nf;
   const FT kap = P.Rd * P.icvd;
   FT rJm[M], hm[M], rhom[M], Km[M], thm[M], Pim[M], c1m[M], c2m[M], u3cm[M], u3cp[M];
   nb_all<M, -1>(Dg.rJ, rJm); nb_all<M, -1>(Dg.h, hm); nb_all<M, -1>(S.rho, rhom); nb_all<M, -1>(Dg.K, Km);
   nb_all<M, -1>(Dg.thv, thm); nb_all<M, -1>(Dg.Pi, Pim); nb_all<M, -1>(Dg.c1, c1m); nb_all<M, -1>(Dg.c2, c2m);
-  nb_all<M, -1>(Dg.u3c, u3cm); nb_all<M, 1>(Dg.u3c, u3cp);
+  // (u_3, u_3) uses g^33 u_3 of the neighbouring faces (u3c over a flat surface, w3c over terrain)
+  nb_all<M, -1>(TOPO ? Dg.w3c : Dg.u3c, u3cm); nb_all<M, 1>(TOPO ? Dg.w3c : Dg.u3c, u3cp);
+  FT ctm[M], phim[M];
+  if constexpr (TOPO) {
+    nb_all<M, -1>(Dg.ct3, ctm);
+    nb_all<M, -1>(Dg.phi, phim);
+  }
   // face quantities needed by centre rows: rJbar*g33 and hbar at faces
   FT fr[M], fhb[M];
 #pragma unroll
@@ -225,7 +313,7 @@ __device__ __forceinline__ void col_jacobian(const DevParams<FT> &P, const ColGe
     const int f = lane * M + k;
     const bool inner = f > 0 && f < Nv;
     const int fc = min(f, Nf - 1);
-    const FT g33 = P.levf[LF_G33 * Nf + fc];
+    const FT g33 = TOPO ? Dg.g33[k] : P.levf[LF_G33 * Nf + fc];
     const FT rJ = (rJm[k] + Dg.rJ[k]) / FT(2);
     fr[k] = inner ? rJ * g33 : FT(0);
     fhb[k] = (hm[k] + Dg.h[k]) / FT(2);
@@ -242,14 +330,15 @@ __device__ __forceinline__ void col_jacobian(const DevParams<FT> &P, const ColGe
     Jc.eu1[k] = dtg * (v1 * fhbn[k]);
     const int f = lane * M + k;
     const int fc = min(f, Nf - 1);
-    const FT beta = P.levf[LF_BETA * Nf + fc];
+    const FT beta = TOPO ? Tg.f4(fc).y : P.levf[LF_BETA * Nf + fc];
     if (f > 0 && f < Nv) {
       const int va = f - 1;
       const FT ra = rhom[k], rb = S.rho[k];
       const FT rbar = (ra + rb) / FT(2);
       const FT irb = grcp(rbar);
-      const FT dpa = kap * (P.T0 * P.cpd - Km[k] - P.levc[LC_PHI * Nv + va]);
-      const FT dpb = kap * (P.T0 * P.cpd - Dg.K[k] - P.levc[LC_PHI * Nv + f]);
+      const FT phia = TOPO ? phim[k] : P.levc[LC_PHI * Nv + va], phib = TOPO ? Dg.phi[k] : P.levc[LC_PHI * Nv + f];
+      const FT dpa = kap * (P.T0 * P.cpd - Km[k] - phia);
+      const FT dpb = kap * (P.T0 * P.cpd - Dg.K[k] - phib);
       const FT thvb = (thm[k] + Dg.thv[k]) / FT(2);
       const FT gPi = Dg.Pi[k] - Pim[k];
       const FT buoy = P.cpd * thvb * gPi * irb;
@@ -261,9 +350,16 @@ __device__ __forceinline__ void col_jacobian(const DevParams<FT> &P, const ColGe
       Jc.uh1[k] = dtg * (-kap * ra * irb) * c2m[k];
       Jc.uh2[k] = dtg * (kap * rb * irb) * Dg.c1[k];
       Jc.uh3[k] = dtg * (kap * rb * irb) * Dg.c2[k];
-      Jc.uu0[k] = dtg * (-kap * ra * u3cm[k] * (irb / FT(2)));
-      Jc.uu1[k] = dtg * (kap * (rb - ra) * Dg.u3c[k] * (irb / FT(2)) - beta) - FT(1);
-      Jc.uu2[k] = dtg * (kap * rb * u3cp[k] * (irb / FT(2)));
+      if constexpr (TOPO) {
+        // dK_v/du_3,f = (g^33 u_3)_f / 2 + CT3(u_h)_v / 2 (manual_sparse_jacobian.jl:754-756)
+        Jc.uu0[k] = dtg * (-kap * ra * (u3cm[k] + ctm[k]) * (irb / FT(2)));
+        Jc.uu1[k] = dtg * (kap * (rb * (Dg.w3c[k] + Dg.ct3[k]) - ra * (Dg.w3c[k] + ctm[k])) * (irb / FT(2)) - beta) - FT(1);
+        Jc.uu2[k] = dtg * (kap * rb * (u3cp[k] + Dg.ct3[k]) * (irb / FT(2)));
+      } else {
+        Jc.uu0[k] = dtg * (-kap * ra * u3cm[k] * (irb / FT(2)));
+        Jc.uu1[k] = dtg * (kap * (rb - ra) * Dg.u3c[k] * (irb / FT(2)) - beta) - FT(1);
+        Jc.uu2[k] = dtg * (kap * rb * u3cp[k] * (irb / FT(2)));
+      }
     } else {
       Jc.ur0[k] = Jc.ur1[k] = Jc.ue0[k] = Jc.ue1[k] = FT(0);
       Jc.uh0[k] = Jc.uh1[k] = Jc.uh2[k] = Jc.uh3[k] = FT(0);
@@ -271,14 +367,59 @@ __device__ __forceinline__ void col_jacobian(const DevParams<FT> &P, const ColGe
       Jc.uu1[k] = f <= Nv ? -dtg * beta - FT(1) : FT(1);  // identity rows beyond the column
     }
   }
+  if constexpr (TOPO) {
+    FT rJp[M], hp[M];
+    nb_all<M, 1>(Dg.rJ, rJp);
+    nb_all<M, 1>(Dg.h, hp);
+#pragma unroll
+    for (int k = 0; k < M; ++k) {
+      const int v = lane * M + k;
+      const bool lo = v >= 1 && v < Nv, hi = v + 1 <= Nv - 1;
+      const FT half = dtg / FT(2);
+      Jc.wm[k] = lo ? half * rJm[k] * Dg.iJ[k] : FT(0);
+      Jc.w0m[k] = lo ? half * S.rho[k] : FT(0);
+      Jc.w0p[k] = hi ? half * S.rho[k] : FT(0);
+      Jc.wp[k] = hi ? half * rJp[k] * Dg.iJ[k] : FT(0);
+      Jc.hb0[k] = (hm[k] + Dg.h[k]) / FT(2);
+      Jc.hb1[k] = (Dg.h[k] + hp[k]) / FT(2);
+    }
+  }
 }
 
 // Solve W dY = R with the Schur complement onto u_3.
-template <class FT, int M>
-__device__ __forceinline__ void col_ldiv(const DevParams<FT> &P, const ColJac<FT, M> &Jc, const FT (&Rr)[M],
-                                         const FT (&Re)[M], const FT (&Ru1)[M], const FT (&Ru2)[M], const FT (&R3)[M],
-                                         FT (&Xr)[M], FT (&Xe)[M], FT (&X3)[M], int lane) {
+template <class FT, int M, bool TOPO, class LV>
+__device__ __forceinline__ void col_ldiv(const DevParams<FT> &P, const LV &Tg, const ColJac<FT, M> &Jc,
+                                         const FT (&Rr0)[M], const FT (&Re0)[M], const FT (&Ru1)[M],
+                                         const FT (&Ru2)[M], const FT (&R3)[M], FT (&Xr)[M], FT (&Xe)[M],
+                                         FT (&X3)[M], int lane) {
   const int Nv = P.Nv, Nf = P.Nf;
+  // over terrain the (rho, u_h), (rho e_tot, u_h) blocks times Δu_h = -R_u_h move to the right-hand
+  // sides of the scalar rows: R_x + M_x,uh R_uh
+  FT Rr[M], Re[M];
+  if constexpr (TOPO) {
+    FT ct[M], ctm[M], ctp[M];
+#pragma unroll
+    for (int k = 0; k < M; ++k) {
+      const int v = min(lane * M + k, Nv - 1);
+      FT g31, g32, phis;
+      Tg.ct(v, g31, g32, phis);
+      ct[k] = lane * M + k < Nv ? g31 * Ru1[k] + g32 * Ru2[k] : FT(0);
+    }
+    nb_all<M, -1>(ct, ctm);
+    nb_all<M, 1>(ct, ctp);
+#pragma unroll
+    for (int k = 0; k < M; ++k) {
+      Rr[k] = Rr0[k] + (Jc.wm[k] * ctm[k] + (Jc.w0m[k] - Jc.w0p[k]) * ct[k] - Jc.wp[k] * ctp[k]);
+      Re[k] = Re0[k] + (Jc.hb0[k] * (Jc.wm[k] * ctm[k] + Jc.w0m[k] * ct[k]) -
+                        Jc.hb1[k] * (Jc.w0p[k] * ct[k] + Jc.wp[k] * ctp[k]));
+    }
+  } else {
+#pragma unroll
+    for (int k = 0; k < M; ++k) {
+      Rr[k] = Rr0[k];
+      Re[k] = Re0[k];
+    }
+  }
   FT ru0m[M], ru1m[M], eu0m[M], eu1m[M], Rrm[M], Rem[M], Ru1m[M], Ru2m[M];
   nb_all<M, -1>(Jc.ru0, ru0m); nb_all<M, -1>(Jc.ru1, ru1m); nb_all<M, -1>(Jc.eu0, eu0m); nb_all<M, -1>(Jc.eu1, eu1m);
   nb_all<M, -1>(Rr, Rrm); nb_all<M, -1>(Re, Rem); nb_all<M, -1>(Ru1, Ru1m); nb_all<M, -1>(Ru2, Ru2m);
@@ -375,7 +516,7 @@ template <class FT>
 __device__ __forceinline__ size_t ridx(int e, int c, int n, int v, int Nv) { return (((size_t)e * 2 + c) * NN + n) * Nv + v; }
 
 // Individual hooks: implicit tendency, Jacobian, ldiv, post-Newton correction.
-template <class FT, int M, int MODE>
+template <class FT, int M, int MODE, bool TOPO>
 __global__ void __launch_bounds__(COL_THREADS) k_col_hook(DevParams<FT> P, ColArgs<FT> A) {
   const int lane = threadIdx.x & 31;
   const int col = blockIdx.x * (COL_THREADS / 32) + (threadIdx.x >> 5);
@@ -384,6 +525,11 @@ __global__ void __launch_bounds__(COL_THREADS) k_col_hook(DevParams<FT> P, ColAr
   const int e = col >> 4, n = col & 15, Nv = P.Nv, Nf = P.Nf;
   ColGeo<FT> G;
   G.load(P, e, n);
+  constexpr int NQJ = TOPO ? JAC_QT : JAC_Q;
+  using LV = std::conditional_t<TOPO, col::ColLevT<FT>, col::ColLev<FT>>;
+  LV Tg;
+  if constexpr (TOPO) Tg.load(P, e, n);
+  else Tg = col::ColLev<FT>{P.lc4, P.lf4, P.lr4, Nv, Nf};
   ColState<FT, M> S;
 #pragma unroll
   for (int k = 0; k < M; ++k) {
@@ -394,9 +540,12 @@ __global__ void __launch_bounds__(COL_THREADS) k_col_hook(DevParams<FT> P, ColAr
     S.u2[k] = cv ? A.Y_c[cidx<FT>(e, 2, n, v, Nv)] : FT(0);
     S.rhoe[k] = cv ? A.Y_c[cidx<FT>(e, 3, n, v, Nv)] : (MODE == COL_LDIV ? FT(0) : FT(1));
     S.u3[k] = fv ? A.Y_f[((size_t)e * NN + n) * Nf + v] : FT(0);
-    if (MODE != COL_LDIV && (v == 0 || v >= Nv)) S.u3[k] = FT(0);  // impenetrable filter
+    if (!TOPO && MODE != COL_LDIV && (v == 0 || v >= Nv)) S.u3[k] = FT(0);  // impenetrable filter
   }
-  FT *jac = A.jac + (size_t)col * JAC_Q * Nf;
+  if constexpr (TOPO) {
+    if (MODE != COL_LDIV) col_filter_topo<FT, M>(Tg, S, lane);  // -u_h^3 / g^33 on the boundary faces
+  }
+  FT *jac = A.jac + (size_t)col * NQJ * Nf;
   FT o0[M], o1[M], o2[M], o3[M], o4[M];
   if constexpr (MODE == COL_LDIV) {
     ColJac<FT, M> Jc;
@@ -404,22 +553,23 @@ __global__ void __launch_bounds__(COL_THREADS) k_col_hook(DevParams<FT> P, ColAr
     for (int k = 0; k < M; ++k) {
       const int f = lane * M + k;
       const int fc = min(f, Nf - 1);
-      FT *q[JAC_Q] = {Jc.ru0, Jc.ru1, Jc.eu0, Jc.eu1, Jc.ur0, Jc.ur1, Jc.ue0, Jc.ue1,
-                      Jc.uh0, Jc.uh1, Jc.uh2, Jc.uh3, Jc.uu0, Jc.uu1, Jc.uu2};
-      for (int t = 0; t < JAC_Q; ++t) q[t][k] = jac[t * Nf + fc];
+      FT *q[JAC_QT] = {Jc.ru0, Jc.ru1, Jc.eu0, Jc.eu1, Jc.ur0, Jc.ur1, Jc.ue0, Jc.ue1,
+                       Jc.uh0, Jc.uh1, Jc.uh2, Jc.uh3, Jc.uu0, Jc.uu1, Jc.uu2,
+                       Jc.wm, Jc.w0m, Jc.w0p, Jc.wp, Jc.hb0, Jc.hb1};
+      for (int t = 0; t < NQJ; ++t) q[t][k] = jac[t * Nf + fc];
       if (f >= Nf) {
-        for (int t = 0; t < JAC_Q; ++t) q[t][k] = FT(0);
+        for (int t = 0; t < NQJ; ++t) q[t][k] = FT(0);
         Jc.uu1[k] = FT(1);
       }
     }
-    col_ldiv<FT, M>(P, Jc, S.rho, S.rhoe, S.u1, S.u2, S.u3, o0, o3, o4, lane);
+    col_ldiv<FT, M, TOPO>(P, Tg, Jc, S.rho, S.rhoe, S.u1, S.u2, S.u3, o0, o3, o4, lane);
 #pragma unroll
     for (int k = 0; k < M; ++k) { o1[k] = -S.u1[k]; o2[k] = -S.u2[k]; }
   } else {
     ColDiag<FT, M> Dg;
-    col_diag<FT, M>(P, G, S, Dg, lane);
+    col_diag<FT, M, TOPO>(P, G, Tg, S, Dg, lane);
     if constexpr (MODE == COL_IMPLICIT) {
-      col_implicit<FT, M>(P, G, S, Dg, o0, o3, o4, lane);
+      col_implicit<FT, M, TOPO>(P, G, Tg, S, Dg, o0, o3, o4, lane);
 #pragma unroll
       for (int k = 0; k < M; ++k) { o1[k] = FT(0); o2[k] = FT(0); }
     } else if constexpr (MODE == COL_POSTIMP) {
@@ -432,14 +582,21 @@ __global__ void __launch_bounds__(COL_THREADS) k_col_hook(DevParams<FT> P, ColAr
       }
     } else {  // COL_JACOBIAN
       ColJac<FT, M> Jc;
-      col_jacobian<FT, M>(P, G, S, Dg, A.dtg, Jc, lane);
+      col_jacobian<FT, M, TOPO>(P, G, Tg, S, Dg, A.dtg, Jc, lane);
 #pragma unroll
       for (int k = 0; k < M; ++k) {
         const int f = lane * M + k;
         if (f < Nf) {
-          const FT q[JAC_Q] = {Jc.ru0[k], Jc.ru1[k], Jc.eu0[k], Jc.eu1[k], Jc.ur0[k], Jc.ur1[k], Jc.ue0[k], Jc.ue1[k],
-                               Jc.uh0[k], Jc.uh1[k], Jc.uh2[k], Jc.uh3[k], Jc.uu0[k], Jc.uu1[k], Jc.uu2[k]};
-          for (int t = 0; t < JAC_Q; ++t) jac[t * Nf + f] = q[t];
+          if constexpr (TOPO) {
+            const FT q[JAC_QT] = {Jc.ru0[k], Jc.ru1[k], Jc.eu0[k], Jc.eu1[k], Jc.ur0[k], Jc.ur1[k], Jc.ue0[k],
+                                  Jc.ue1[k], Jc.uh0[k], Jc.uh1[k], Jc.uh2[k], Jc.uh3[k], Jc.uu0[k], Jc.uu1[k],
+                                  Jc.uu2[k], Jc.wm[k], Jc.w0m[k], Jc.w0p[k], Jc.wp[k], Jc.hb0[k], Jc.hb1[k]};
+            for (int t = 0; t < JAC_QT; ++t) jac[t * Nf + f] = q[t];
+          } else {
+            const FT q[JAC_Q] = {Jc.ru0[k], Jc.ru1[k], Jc.eu0[k], Jc.eu1[k], Jc.ur0[k], Jc.ur1[k], Jc.ue0[k], Jc.ue1[k],
+                                 Jc.uh0[k], Jc.uh1[k], Jc.uh2[k], Jc.uh3[k], Jc.uu0[k], Jc.uu1[k], Jc.uu2[k]};
+            for (int t = 0; t < JAC_Q; ++t) jac[t * Nf + f] = q[t];
+          }
         }
       }
       return;
@@ -462,14 +619,19 @@ inline int levels_per_lane(int Nf) { return Nf <= 32 ? 1 : (Nf <= 64 ? 2 : 4); }
 
 }  // namespace
 
+template <class FT, int M, bool TOPO>
+void launch_hook_mt(const DevParams<FT> &P, int mode, const ColArgs<FT> &A, int grid, cudaStream_t s) {
+  switch (mode) {
+    case COL_IMPLICIT: k_col_hook<FT, M, COL_IMPLICIT, TOPO><<<grid, COL_THREADS, 0, s>>>(P, A); break;
+    case COL_JACOBIAN: k_col_hook<FT, M, COL_JACOBIAN, TOPO><<<grid, COL_THREADS, 0, s>>>(P, A); break;
+    case COL_LDIV: k_col_hook<FT, M, COL_LDIV, TOPO><<<grid, COL_THREADS, 0, s>>>(P, A); break;
+    default: k_col_hook<FT, M, COL_POSTIMP, TOPO><<<grid, COL_THREADS, 0, s>>>(P, A); break;
+  }
+}
 template <class FT, int M>
 void launch_hook_m(const DevParams<FT> &P, int mode, const ColArgs<FT> &A, int grid, cudaStream_t s) {
-  switch (mode) {
-    case COL_IMPLICIT: k_col_hook<FT, M, COL_IMPLICIT><<<grid, COL_THREADS, 0, s>>>(P, A); break;
-    case COL_JACOBIAN: k_col_hook<FT, M, COL_JACOBIAN><<<grid, COL_THREADS, 0, s>>>(P, A); break;
-    case COL_LDIV: k_col_hook<FT, M, COL_LDIV><<<grid, COL_THREADS, 0, s>>>(P, A); break;
-    default: k_col_hook<FT, M, COL_POSTIMP><<<grid, COL_THREADS, 0, s>>>(P, A); break;
-  }
+  if (P.topo) launch_hook_mt<FT, M, true>(P, mode, A, grid, s);
+  else launch_hook_mt<FT, M, false>(P, mode, A, grid, s);
 }
 
 template <class FT>

@@ -87,11 +87,11 @@ typedef struct {
      s = sleve_s, b = sinh((eta_h - eta) / (s eta_h)) / sinh(1 / s) for eta = zeta / z_max
      <= eta_h, else 0.  The metric of every point (J, g^ij, g_ij with their vertical cross
      terms) follows from z_s, its spectral derivatives in each element and b; the kernels
-     compute it where they use it.  Supported by gb_step, gb_remaining_tendency,
-     gb_set_precomputed_quantities (the filter u_3 = -u_h^3 / g^33), gb_global_sums and
-     gb_time_kernel; the column hooks (implicit tendency, Jacobian, ldiv, post-Newton
-     correction), the reverse-mode entries and the Held-Suarez forcing return GB_ERR_ARG for a
-     terrain context. */
+     compute it where they use it.  Supported by gb_step, every hook (gb_set_precomputed_quantities
+     applies u_3 = -u_h^3 / g^33 on the bottom and top faces; gb_update_jacobian adds the
+     (rho, u_h) and (rho e_tot, u_h) blocks that gb_ldiv applies to R's u_h part),
+     gb_global_sums and gb_time_kernel; gb_jacobian_solve_noalloc, the reverse-mode entries and
+     the Held-Suarez forcing return GB_ERR_ARG for a terrain context. */
   const double *z_surface;
   int warp;
   double sleve_eta, sleve_s;

@@ -173,7 +173,11 @@ def warped_geometry(g, z_surface, warp):
         E[..., 2, :] = dz[..., None] * xh
         gdn = np.einsum("...ik,...jk->...ij", E, E)
         J = np.einsum("...k,...k->...", E[..., 2, :], np.cross(E[..., 0, :], E[..., 1, :]))
-        return E, J, np.linalg.inv(gdn)
+        # the metric's diagonal spans ~1e4 (dz^2) to ~1e12 (the horizontal scale squared):
+        # invert the equilibrated matrix D g D (D = diag(g_ii)^-1/2) and scale back
+        d = 1.0 / np.sqrt(np.einsum("...ii->...i", gdn))
+        gup = d[..., :, None] * np.linalg.inv(d[..., :, None] * gdn * d[..., None, :]) * d[..., None, :]
+        return E, J, gup
 
     Ec, Jc, gup_c = basis(zc, dzc)
     Ef, Jf, gup_f = basis(zf, dzf)

@@ -135,13 +135,67 @@ def test_flat_surface_terrain_context_matches_the_flat_step():
     _assert(field_errors(Ac, Af, Bc, Bf), {"rho": 1e-14, "rho_e_tot": 1e-14, "u_1": 1e-12, "u_2": 1e-12, "u_3": 2e-11})
 
 
+@pytest.mark.parametrize("ft,tol", [(np.float64, 1e-12), (np.float32, 1e-4)])
+def test_terrain_implicit_tendency_and_correction(ft, tol):
+    cfg, g, o, Yc, Yf = _setup(ft, z=12)
+    o32 = O.Oracle(g, cfg.with_(ft=np.float64).oracle_params(dss_stage1=False), ft)
+    ref = o32.implicit_tendency(Yc.astype(ft), Yf.astype(ft))
+    refc = o32.correct_implicit(Yc.astype(ft), Yf.astype(ft))
+    p = sim.AtmosCache(cfg)
+    Y = _dev(Yc, Yf, ft)
+    Yt = Y.similar()
+    sim.implicit_tendency(Yt, Y, p, 0.0)
+    e = field_errors(*Yt.numpy(), ref[0], ref[1])
+    # u_3's tendency is the near-cancellation of gravity and the pressure gradient (FP32: 1e-3)
+    _assert({k: v for k, v in e.items() if k in ("rho", "rho_e_tot")}, tol)
+    assert e["u_3"] <= (tol if ft == np.float64 else 1e-3), e
+    sim.correct_implicit_advection_tendency(Yt, Y, p, 0.0)
+    e = field_errors(*Yt.numpy(), refc[0], refc[1])
+    assert e["rho_e_tot"] <= tol, e
+
+
+def test_terrain_jacobian_and_ldiv_with_the_uh_blocks():
+    """update_jacobian + ldiv over terrain with a residual whose u_h part is nonzero: the
+    (rho, u_h) and (rho e_tot, u_h) blocks (manual_sparse_jacobian.jl:150-187, 745-786) enter
+    the scalar rows' right-hand sides."""
+    cfg, g, o, Yc, Yf = _setup(z=40)   # two levels per lane
+    dtg = 0.4358665215084590 * cfg.dt
+    o.set_precomputed(Yc, Yf)
+    o.update_jacobian(Yc, Yf, dtg)
+    rng = np.random.default_rng(3)
+    Rc = rng.normal(size=Yc.shape) * np.abs(Yc).max(axis=(0, 2, 3), keepdims=True) * 1e-3
+    Rf = rng.normal(size=Yf.shape) * 0.1
+    ref = o.ldiv(Rc, Rf)
+    ref0 = o.ldiv(np.concatenate([Rc[:, :1], 0 * Rc[:, 1:3], Rc[:, 3:]], axis=1), Rf)
+    assert np.abs(ref[0][:, 0] - ref0[0][:, 0]).max() > 1e-6 * np.abs(ref[0][:, 0]).max()
+    p = sim.AtmosCache(cfg)
+    Y = _dev(Yc, Yf, np.float64)
+    jac = sim.Jacobian(p)
+    sim.update_jacobian(jac, Y, p, dtg, 0.0)
+    dY = Y.similar()
+    sim.ldiv(dY, jac, _dev(Rc, Rf, np.float64))
+    _assert(field_errors(*dY.numpy(), ref[0], ref[1]), 1e-12)
+
+
+def test_terrain_hook_loop_matches_fused_step():
+    """The ClimaTimeSteppers stage loop through the hooks (stage states DSSed, the filter at
+    every cache!) against the fused step over terrain."""
+    cfg, g, o, Yc, Yf = _setup()
+    a = sim.AtmosSimulation(cfg, state=(Yc, Yf))
+    a.step(2, use_graph=False)
+    p = sim.AtmosCache(cfg)
+    Y = _dev(Yc, Yf, np.float64)
+    for k in range(2):
+        sim.ars343_step_via_hooks(Y, p, k * cfg.dt, cfg.dt)
+    _assert(field_errors(*Y.numpy(), *a.Y.numpy()), {"rho": 1e-14, "rho_e_tot": 1e-14, "u_1": 1e-12, "u_2": 1e-12, "u_3": 2e-11})
+
+
 def test_terrain_context_refuses_what_is_not_built():
     cfg, g, o, Yc, Yf = _setup()
     p = sim.AtmosCache(cfg)
     Y = _dev(Yc, Yf, np.float64)
     Yt = Y.similar()
-    for call in (lambda: sim.implicit_tendency(Yt, Y, p, 0.0),
-                 lambda: sim.update_jacobian(None, Y, p, 10.0, 0.0),
+    for call in (lambda: p.call("gb_jacobian_solve_noalloc", Yt.gb(), Y.gb(), Y.gb(), 10.0),
                  lambda: p.call("gb_step_vjp", Yt.gb(), Y.gb(), 0.0, float(cfg.dt), None)):
         with pytest.raises(N.GBError) as ei:
             call()

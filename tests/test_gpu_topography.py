@@ -74,8 +74,10 @@ def test_terrain_filter_and_global_sums():
     sim.set_precomputed_quantities(Y, p, 0.0)
     _, Gf = Y.numpy()
     for k in (0, -1):
-        # -CT3(u_h) / g^33 from the closed-form metric here, from the inverted 3x3 metric in the oracle
-        assert np.abs(Gf[..., k] - Rf[..., k]).max() <= 1e-12 * np.abs(Rf[..., k]).max()
+        # -CT3(u_h) / g^33 from the closed-form metric here; the oracle forms the metric from
+        # Cartesian basis vectors, where x_hat . e_a rounds to ~1e-16 |e_a| ~ 1e-10 against
+        # slopes of ~1e3: its g^3a carry ~1e-13, and CT3(u_h) = g^31 u_1 + g^32 u_2 partly cancels
+        assert np.abs(Gf[..., k] - Rf[..., k]).max() <= 1e-11 * np.abs(Rf[..., k]).max()
     assert np.abs(Rf[..., 0]).max() > 0
     assert np.array_equal(Gf[..., 1:-1], Yf[..., 1:-1])
     s = p.global_sums(Y)

@@ -750,6 +750,13 @@ def measure_differentiation(args):
         ms, (J, G, dnu, drate, peak) = _timed(lambda: sim.gradient(p, Y0, nsteps, lg, checkpoint_every=4))
         key = "fp32" if ft == np.float32 else "fp64"
         out[key] = {"gradient_ms": ms, "J": J, "dJ_dnu": dnu, "dJ_drate": drate, "library_bytes": peak}
+        if ft == np.float32:
+            # both segments' stage data kept by the forward half: the pullback recomputes nothing
+            sim.gradient(p, Y0, nsteps, lg, checkpoint_every=4, record_segments=2)
+            ms2, (_, G2, _, _, peak2) = _timed(lambda: sim.gradient(p, Y0, nsteps, lg, checkpoint_every=4))
+            p.call("gb_adjoint_set_record_segments", 1)
+            out[key]["two_segments_kept"] = {"gradient_ms": ms2, "library_bytes": peak2,
+                                             "same_gradient": bool(torch.equal(G.c, G2.c) and torch.equal(G.f, G2.f))}
         if ft == np.float64:
             def fwd(Xc, Xf, q=p):
                 Z = sim.FieldVector.from_numpy(Xc, Xf)
@@ -789,6 +796,7 @@ def measure_differentiation(args):
     fms, _ = _timed(lambda: s32.step(nsteps))
     out["fp32"]["forward_ms"] = fms
     out["fp32"]["gradient_over_forward"] = out["fp32"]["gradient_ms"] / fms
+    out["fp32"]["two_segments_kept"]["gradient_over_forward"] = out["fp32"]["two_segments_kept"]["gradient_ms"] / fms
     out["workload"] = "h_elem=16, z_elem=45 stretched (dz_bottom 500 m), dt=200 s, 8 steps, sponge 1e-4 s^-1 above 20 km"
     return out
 
@@ -831,13 +839,31 @@ def measure_precision_h60(args):
     peak = ctypes.c_size_t(0)
     rev_ms, _ = _timed(lambda: s32.p.call("gb_adjoint_reverse", Ybar.gb(), d, ctypes.byref(peak)))
     free1, _ = torch.cuda.mem_get_info()
-    out["adjoint_20_steps"] = {"checkpoint_every": 5, "forward_ms": fwd_ms,
+    out["adjoint_20_steps"] = {"checkpoint_every": 5, "record_segments": 1, "forward_ms": fwd_ms,
                                "forward_note": "first call: includes allocating the stage records and checkpoints",
                                "reverse_ms": rev_ms,
                                "reverse_over_forward_steps": rev_ms / (20 * ms / 20),
                                "library_bytes": int(peak.value),
                                "device_bytes_in_use_after_reverse": int(total - free1),
                                "finite": bool(torch.isfinite(Ybar.c).all() and torch.isfinite(Ybar.f).all())}
+    # HBM for recomputation: the forward half keeps the stage data of the last two segments,
+    # so the pullback recomputes two of the four (gb_adjoint_set_record_segments)
+    s32.p.call("gb_adjoint_set_record_segments", 2)
+    Y = Y0.copy()
+    s32.p.call("gb_adjoint_forward", Y.gb(), 0.0, float(cfg.dt), 20, 5)   # allocates the extra records
+    J, Ybar2 = lg(Y)
+    s32.p.call("gb_adjoint_reverse", Ybar2.gb(), d, ctypes.byref(peak))
+    Y = Y0.copy()
+    fwd2, _ = _timed(lambda: s32.p.call("gb_adjoint_forward", Y.gb(), 0.0, float(cfg.dt), 20, 5))
+    J, Ybar2 = lg(Y)
+    rev2, _ = _timed(lambda: s32.p.call("gb_adjoint_reverse", Ybar2.gb(), d, ctypes.byref(peak)))
+    free2, _ = torch.cuda.mem_get_info()
+    out["adjoint_20_steps_two_segments_kept"] = {
+        "checkpoint_every": 5, "record_segments": 2, "forward_ms": fwd2, "reverse_ms": rev2,
+        "reverse_over_forward_steps": rev2 / ms, "library_bytes": int(peak.value),
+        "device_bytes_in_use_after_reverse": int(total - free2),
+        "same_gradient_as_one_kept": bool(torch.equal(Ybar.c, Ybar2.c) and torch.equal(Ybar.f, Ybar2.f))}
+    s32.p.call("gb_adjoint_set_record_segments", 1)
     return out
 
 

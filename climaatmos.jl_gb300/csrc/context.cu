@@ -63,7 +63,8 @@ struct Impl : ImplBase {
     std::vector<std::unique_ptr<DevBuf>> ckpt;
     DevBuf Ub, Lb, Teb[4], Tib[4], zero, dummy, scr, dparB, dal, dacc, work, yb;
     int nsteps = 0, every = 0, grid = 0;
-    int rec_seg = -1;  // checkpoint segment whose stage records are valid (recorded by the forward pass)
+    int rec_first = -1;  // the first of the trailing segments whose stage records the forward pass kept
+    int keep = 1;        // trailing segments the forward pass records (gb_adjoint_set_record_segments)
     double dt = 0;
     bool ready = false;
     size_t bytes = 0, rec_bytes = 0;
@@ -1012,7 +1013,7 @@ int step_vjp_t(gb_ctx *ctx, gb_fieldvec Yb, gb_fieldvec Y, double dt, double *dp
   CK(cudaMemcpyAsync(W, Y.c, I->NC * sizeof(FT), cudaMemcpyDeviceToDevice, s));
   CK(cudaMemcpyAsync(W + I->NC, Y.f, I->NF * sizeof(FT), cudaMemcpyDeviceToDevice, s));
   zero_dpar<FT>(ctx, s);
-  A.rec_seg = -1;  // record 0 is reused here
+  A.rec_first = -1;  // record 0 is reused here
   record_step<FT>(ctx, W, W + I->NC, dt, *A.rec[0], s);
   reverse_step<FT>(ctx, *A.rec[0], dt, (FT *)Yb.c, (FT *)Yb.f, s);
   if ((r = check_launch(ctx))) return r;
@@ -1033,28 +1034,31 @@ int adjoint_forward_t(gb_ctx *ctx, gb_fieldvec Y, double dt, int nsteps, int eve
     if ((r = alloc_z<FT>(ctx, *b, SB, A.bytes))) return r;
     A.ckpt.push_back(std::move(b));
   }
-  // the last segment's stage data is recorded on the way (the reverse pass starts
-  // there and needs no recompute for it); the same kernels in the same order as the step
-  if ((r = ensure_records<FT>(ctx, every))) return r;
-  const int last = (nck - 1) * every;
-  A.rec_seg = -1;
+  // the last `keep` segments' stage data is recorded on the way (the reverse pass starts
+  // there and needs no recompute for them); the same kernels in the same order as the step.
+  // Segment g (of the kept ones) uses the records from (nck - 1 - g) * every on.
+  const int keep = std::max(1, std::min(A.keep, nck));
+  if ((r = ensure_records<FT>(ctx, keep * every))) return r;
+  const int first = nck - keep;
+  A.rec_first = -1;
   cudaStream_t s = ctx->stream;
   FT *Yc = (FT *)Y.c, *Yf = (FT *)Y.f;
   for (int k = 0; k < nsteps; ++k) {
+    const int g = k / every;
     if (k % every == 0) {
-      FT *ck = (FT *)A.ckpt[k / every]->p;
+      FT *ck = (FT *)A.ckpt[g]->p;
       CK(cudaMemcpyAsync(ck, Yc, I->NC * sizeof(FT), cudaMemcpyDeviceToDevice, s));
       CK(cudaMemcpyAsync(ck + I->NC, Yf, I->NF * sizeof(FT), cudaMemcpyDeviceToDevice, s));
     }
-    if (k >= last) {
-      auto &rc = *A.rec[k - last];
+    if (g >= first) {
+      auto &rc = *A.rec[(nck - 1 - g) * every + (k - g * every)];
       r = graph_run<FT>(ctx, rc.fwd, Yc, Yf, dt, [&](cudaStream_t cs) { record_step<FT>(ctx, Yc, Yf, dt, rc, cs); });
       if (r) return r;
     } else {
       enqueue_step<FT>(ctx, Yc, Yf, dt, s);
     }
   }
-  A.rec_seg = nck - 1;
+  A.rec_first = first;
   A.nsteps = nsteps;
   A.every = every;
   A.dt = dt;
@@ -1083,18 +1087,21 @@ int adjoint_reverse_t(gb_ctx *ctx, gb_fieldvec Yb, double *dpar, size_t *peak) {
   const int nseg = (A.nsteps + A.every - 1) / A.every;
   for (int g = nseg - 1; g >= 0; --g) {
     const int s0 = g * A.every, s1 = std::min(A.nsteps, s0 + A.every);
-    if (g != A.rec_seg) {
+    // a kept segment's records start at (nseg - 1 - g) * every; a recomputed one reuses the
+    // first record set (its segment was reversed first)
+    const bool kept = A.rec_first >= 0 && g >= A.rec_first;
+    const int base = kept ? (nseg - 1 - g) * A.every : 0;
+    if (!kept) {
       CK(cudaMemcpyAsync(W, A.ckpt[g]->p, SB, cudaMemcpyDeviceToDevice, s));
       for (int k = s0; k < s1; ++k) {
-        auto &rc = *A.rec[k - s0];
+        auto &rc = *A.rec[base + k - s0];
         r = graph_run<FT>(ctx, rc.fwd, W, W + I->NC, A.dt,
                           [&](cudaStream_t cs) { record_step<FT>(ctx, W, W + I->NC, A.dt, rc, cs); });
         if (r) return r;
       }
     }
-    A.rec_seg = -1;
     for (int k = s1 - 1; k >= s0; --k) {
-      auto &rc = *A.rec[k - s0];
+      auto &rc = *A.rec[base + k - s0];
       r = graph_run<FT>(ctx, rc.rev, ybc, ybf, A.dt,
                         [&](cudaStream_t cs) { reverse_step<FT>(ctx, rc, A.dt, ybc, ybf, cs); });
       if (r) return r;
@@ -1419,6 +1426,18 @@ int gb_adjoint_reverse(gb_ctx *ctx, gb_fieldvec Ybar, double dparams[2], size_t 
   if (!ctx || !fv_ok(Ybar)) return GB_ERR_ARG;
   return ctx->cfg.ft_bytes == 8 ? adjoint_reverse_t<double>(ctx, Ybar, dparams, peak_bytes)
                                 : adjoint_reverse_t<float>(ctx, Ybar, dparams, peak_bytes);
+}
+
+int gb_adjoint_set_record_segments(gb_ctx *ctx, int segments) {
+  GB_RANGE();
+  GUARD(ctx);
+  if (segments < 1) return fail(ctx, GB_ERR_ARG, "gb_adjoint_set_record_segments: segments must be >= 1");
+  if (ctx->geo.topo) return fail(ctx, GB_ERR_ARG, "gb_adjoint_set_record_segments is not available over terrain");
+  const int r = ctx->cfg.ft_bytes == 8 ? ensure_adjoint<double>(ctx) : ensure_adjoint<float>(ctx);
+  if (r) return r;
+  if (ctx->cfg.ft_bytes == 8) impl<double>(ctx)->adj->keep = segments;
+  else impl<float>(ctx)->adj->keep = segments;
+  return GB_OK;
 }
 
 int gb_match_elements(const gb_config *cfg, const double *xyz, int *elem_map, int *elem_orient) {

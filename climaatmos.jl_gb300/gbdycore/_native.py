@@ -23,7 +23,7 @@ SYMBOLS = [
     "gb_newton_residual", "gb_time_kernel", "gb_jacobian_solve_noalloc", "gb_match_elements",
     "gb_selftest_bounded_wait",
     "gb_dss_transpose", "gb_remaining_tendency_vjp", "gb_implicit_stage", "gb_implicit_stage_vjp", "gb_step_vjp",
-    "gb_adjoint_forward", "gb_adjoint_reverse",
+    "gb_adjoint_forward", "gb_adjoint_reverse", "gb_adjoint_set_record_segments",
     "gb_columns_create", "gb_columns_destroy", "gb_columns_set_stream", "gb_columns_size", "gb_columns_solve",
     "gb_columns_autotune", "gb_columns_set_variant", "gb_columns_last_error",
 ]
@@ -112,6 +112,7 @@ def load(build_if_missing=True):
     L.gb_step_vjp.argtypes = [_vp, fv, fv, _c_double, _c_double, _dp]
     L.gb_adjoint_forward.argtypes = [_vp, fv, _c_double, _c_double, _c_int, _c_int]
     L.gb_adjoint_reverse.argtypes = [_vp, fv, _dp, ctypes.POINTER(ctypes.c_size_t)]
+    L.gb_adjoint_set_record_segments.argtypes = [_vp, _c_int]
     _llp = ctypes.POINTER(ctypes.c_longlong)
     L.gb_columns_create.argtypes = [cfgp, _c_int, _ip, ctypes.POINTER(_vp)]
     L.gb_columns_destroy.argtypes = [_vp]

@@ -446,14 +446,19 @@ def step_vjp(Ybar, Y, p, t, dt):
     return np.array(d[:])
 
 
-def gradient(p, Y0, nsteps, loss_and_grad, dt=None, checkpoint_every=5):
+def gradient(p, Y0, nsteps, loss_and_grad, dt=None, checkpoint_every=5, record_segments=None):
     """Reverse-mode gradient of a loss of the state after ``nsteps`` steps from Y0.
 
     The rrule pattern (ChainRulesCore.rrule of the solve): the forward half
     advances a copy of Y0 keeping a checkpoint every ``checkpoint_every``
     steps; ``loss_and_grad(Y_N) -> (J, dJ/dY_N FieldVector)``; the pullback
-    returns (J, dJ/dY0, dJ/dnu, dJ/d sponge rate, library bytes at the peak)."""
+    returns (J, dJ/dY0, dJ/dnu, dJ/d sponge rate, library bytes at the peak).
+    ``record_segments`` (default: the context's setting, initially 1) is how many trailing
+    segments the forward half keeps the stage data of, so that the pullback recomputes only
+    the segments before them (gb_adjoint_set_record_segments)."""
     dt = p.dt if dt is None else dt
+    if record_segments is not None:
+        p.call("gb_adjoint_set_record_segments", int(record_segments))
     Y = Y0.copy()
     p.call("gb_adjoint_forward", Y.gb(), 0.0, float(dt), int(nsteps), int(checkpoint_every))
     J, Ybar = loss_and_grad(Y)

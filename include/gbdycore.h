@@ -270,6 +270,12 @@ int gb_adjoint_forward(gb_ctx *ctx, gb_fieldvec Y, double t0, double dt, int nst
  * stage data kept, then reversed.  peak_bytes (may be NULL) receives the
  * device bytes the library held during the pass. */
 int gb_adjoint_reverse(gb_ctx *ctx, gb_fieldvec Ybar, double dparams[2], size_t *peak_bytes);
+/* Memory against recomputation in the checkpointed adjoint (no counterpart in the reference,
+ * which leaves checkpointing to the AD tool): the forward half keeps the stage data of the
+ * last `segments` checkpoint segments (default 1), so the reverse pass recomputes only the
+ * segments before them.  Each kept step holds about 13 states (its stage states, Laplacians
+ * and tendencies).  segments >= 1; it applies from the next gb_adjoint_forward. */
+int gb_adjoint_set_record_segments(gb_ctx *ctx, int segments);
 
 /* ---------------------------------------------------------------------------
  * Batched standalone columns of uneven height.

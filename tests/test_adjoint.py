@@ -217,6 +217,12 @@ def test_trajectory_gradient_checkpointed(setup):
     _, G3, dnu3, dal3, _ = sim.gradient(p, Y0, nsteps, loss_and_grad, checkpoint_every=3)
     assert torch.equal(G2.c, G3.c) and torch.equal(G2.f, G3.f) and dnu2 == dnu3 and dal2 == dal3
     assert peak > 0
+    # keeping the stage data of more trailing segments (less recomputation) changes nothing
+    for every, keep in ((1, 2), (1, 3), (2, 2)):
+        _, Gk, dnuk, dalk, peak_k = sim.gradient(p, Y0, nsteps, loss_and_grad, checkpoint_every=every,
+                                                 record_segments=keep)
+        assert torch.equal(Gk.c, G2.c) and torch.equal(Gk.f, G2.f) and dnuk == dnu2 and dalk == dal2, (every, keep)
+    p.call("gb_adjoint_set_record_segments", 1)
     for seed in (12, 13, 14):
         dc, df = _scaled(Yc.shape, Yf.shape, Yc, Yf, seed)
         fd = (loss_and_grad(forward(_axpy(Yc, Yf, HT, dc, df)))[0] -

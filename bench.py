@@ -63,7 +63,8 @@ def parse(argv=None):
     ap.add_argument("--no-topography", action="store_true")
     # bracket one forward step ("step") or one reverse pass ("reverse") by
     # cudaProfilerStart/Stop, for `ncu --profile-from-start off`; no effect otherwise
-    ap.add_argument("--profile-region", default="none", choices=["none", "step", "reverse"])
+    # ("topography": one step of the terrain-following workload)
+    ap.add_argument("--profile-region", default="none", choices=["none", "step", "reverse", "topography"])
     return ap.parse_args(argv)
 
 
@@ -686,6 +687,11 @@ def measure_topography(args, fwd_ms):
     n = args.topography_steps
     ms, _ = _timed(lambda: s.step(n))
     ms /= n
+    if args.profile_region == "topography":
+        torch.cuda.profiler.start()
+        s.step(1)
+        torch.cuda.synchronize()
+        torch.cuda.profiler.stop()
     m1 = s.p.global_sums(s.Y)[0]
     kern = {}
     fb = 4

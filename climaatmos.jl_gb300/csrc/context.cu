@@ -388,9 +388,19 @@ void enqueue_step_topo(gb_ctx *ctx, FT *Yc, FT *Yf, double dt_, cudaStream_t s) 
     A.rnorm = (double *)I->rnorm.p;
     A.first = i == 1;
     launch_column_stage<FT>(P, A, s);
-    launch_dss_reduced<FT>(P, tic(i), tif(i), s);
     launch_topo_passA<FT>(P, Uc, Uf, lap, s);
     launch_dss<FT>(P, lap, nullptr, s);
+    if (i == 3 && I->stiffly_accurate) {
+      // the final combination folded into the last pass B, as in the flat step; the last
+      // implicit tendency is inside U_4, and the DSS of the whole sum replaces its DSS
+      FT *const c4[4] = {tec(0), tec(1), tec(2), tec(3)}, *const f4[4] = {tef(0), tef(1), tef(2), tef(3)};
+      const FinArgs<FT> F = fin_args<FT>(I, dt, c4, f4);
+      launch_topo_passB<FT>(P, Uc, Uf, lap, Yc, Yf, s, &F);
+      launch_dss<FT>(P, Yc, Yf, s);
+      launch_topo_filter<FT>(P, Yc, Yf, s);
+      return;
+    }
+    launch_dss_reduced<FT>(P, tic(i), tif(i), s);
     launch_topo_passB<FT>(P, Uc, Uf, lap, tec(i), tef(i), s);
     launch_dss<FT>(P, tec(i), tef(i), s);
   }

@@ -144,7 +144,7 @@ template <class FT> void launch_accum_slots(const double *part, int n, double *a
 template <class FT> size_t topo_smem(int Nv);
 template <class FT> cudaError_t configure_topo(int Nv);
 template <class FT> void launch_topo_passA(const DevParams<FT> &P, const FT *Yc, const FT *Yf, FT *L, cudaStream_t s);
-template <class FT> void launch_topo_passB(const DevParams<FT> &P, const FT *Yc, const FT *Yf, const FT *L, FT *Tc, FT *Tf, cudaStream_t s);
+template <class FT> void launch_topo_passB(const DevParams<FT> &P, const FT *Yc, const FT *Yf, const FT *L, FT *Tc, FT *Tf, cudaStream_t s, const FinArgs<FT> *fin = nullptr);
 // u_3 = -u_h^3 / g^33 on the bottom and top faces of every column (reads u_h of Yc)
 template <class FT> void launch_topo_filter(const DevParams<FT> &P, const FT *Yc, FT *Yf, cudaStream_t s);
 // DSS of the reduced implicit tendencies ([Nh][2][16][Nv] centres, faces)

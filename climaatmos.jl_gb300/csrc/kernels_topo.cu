@@ -33,7 +33,7 @@ constexpr int TS_LEVELS = TS_THREADS / 4;
 
 template <class FT>
 struct TopoALayout {
-  size_t y[2], f[2], g[2], t[2], out, w, bar, total;
+  size_t y[2], f[2], g[2], t[2], out, w, gf, bar, total;
   __host__ __device__ TopoALayout(int Nv, int nbuf) {
     const int Nf = Nv + 1;
     size_t o = 0;
@@ -49,6 +49,7 @@ struct TopoALayout {
     }
     out = o; o += align16(sizeof(FT) * 64 * Nv);
     w = o; o += align16(sizeof(FT) * 2 * 16);     // GLL weights W, 1/W
+    gf = o; o += align16(sizeof(FT) * 16 * Nf);   // g^33 of every face [Nf][16]
     bar = o; o += 16;
     total = o;
   }
@@ -59,7 +60,7 @@ enum TopoBScratch { TB_C1 = 0, TB_C2, TB_K, TB_RJ, TB_L4, TB_Q1, TB_Q2, TB_CT3, 
 
 template <class FT>
 struct TopoBLayout {
-  size_t y[2], f[2], g[2], t[2], lap[2], s, x1, x2, w, bar, total;
+  size_t y[2], f[2], g[2], t[2], lap[2], s, x1, x2, w, gf, bar, total;
   __host__ __device__ TopoBLayout(int Nv, int nbuf) {
     const int Nf = Nv + 1;
     size_t o = 0;
@@ -78,6 +79,7 @@ struct TopoBLayout {
     x1 = o; o += align16(sizeof(FT) * 16 * Nf);
     x2 = o; o += align16(sizeof(FT) * 16 * Nf);
     w = o; o += align16(sizeof(FT) * 2 * 16);
+    gf = o; o += align16(sizeof(FT) * 16 * Nf);   // g^33 of every face [Nf][16]
     bar = o; o += 16;
     total = o;
   }
@@ -156,6 +158,18 @@ __device__ __forceinline__ void trow_face(const DevParams<FT> &P, const FT *sG, 
   }
 }
 
+// g^33 of every face of the element into sG33 [Nf][16] (one row per thread and face slot);
+// the caller synchronises before the rows are read.
+template <class FT>
+__device__ __forceinline__ void face_g33_rows(const DevParams<FT> &P, const FT *sG, const FT *sT, FT *sG33, int j,
+                                              int vl) {
+  for (int k = vl; k < P.Nf; k += TS_LEVELS) {
+    FT g33[4];
+    trow_face(P, sG, sT, j, P.ltf[k], g33);
+    st_row(sG33 + (size_t)k * NN + NQ * j, g33);
+  }
+}
+
 // C123(wgrad(div u)) fdiv - C123(wcurl(C123(curl u))) of a covariant (c1, c2, c3) with the full
 // metric of the row (the oracle's vec_lap over terrain).
 template <class FT>
@@ -224,12 +238,12 @@ struct TCen {
   FT rho[4], u1[4], u2[4], rhoe[4], ct3[4], ub3[4], h1[4], h2[4], K[4];
 };
 template <class FT>
-__device__ __forceinline__ void tcentre(const DevParams<FT> &P, const FT *sY, const FT *sF, const FT *sG, const FT *sT,
-                                        int j, int v, const TRow<FT> &G, TCen<FT> &c) {
+__device__ __forceinline__ void tcentre(const DevParams<FT> &P, const FT *sY, const FT *sF, const FT *sG33, int j,
+                                        int v, const TRow<FT> &G, TCen<FT> &c) {
   const int Nv = P.Nv, Nf = P.Nf;
   FT ga[4], gb[4], fa[4], fb[4];
-  trow_face(P, sG, sT, j, P.ltf[v], ga);
-  trow_face(P, sG, sT, j, P.ltf[v + 1], gb);
+  ld_row(sG33 + (size_t)v * NN + NQ * j, ga);
+  ld_row(sG33 + (size_t)(v + 1) * NN + NQ * j, gb);
 #pragma unroll
   for (int i = 0; i < 4; ++i) {
     const int n = NQ * j + i, q = n * Nv + v;
@@ -256,7 +270,7 @@ __global__ void __launch_bounds__(TS_THREADS, 1) k_topo_passA(DevParams<FT> P, i
   const int Nv = P.Nv, Nf = P.Nf;
   const TopoALayout<FT> Lo(Nv, nbuf);
   auto at = [&](const size_t (&off)[2], int b) { return (FT *)(sm + (b ? off[1] : off[0])); };
-  FT *sO = (FT *)(sm + Lo.out), *sW = (FT *)(sm + Lo.w);
+  FT *sO = (FT *)(sm + Lo.out), *sW = (FT *)(sm + Lo.w), *sG33 = (FT *)(sm + Lo.gf);
   uint64_t *bar = (uint64_t *)(sm + Lo.bar);
   const uint32_t by = uint32_t(sizeof(FT) * 64 * Nv), bf = uint32_t(sizeof(FT) * 16 * Nf);
   const uint32_t bg = uint32_t(sizeof(FT) * HG_N * 16), bt = uint32_t(sizeof(FT) * TG_N * 16);
@@ -275,7 +289,7 @@ __global__ void __launch_bounds__(TS_THREADS, 1) k_topo_passA(DevParams<FT> P, i
   slab_init_bars(bar);
   int e = blockIdx.x;
   if (threadIdx.x == 0 && e < P.Nh) issue(0, e);
-  const int j = threadIdx.x & 3, vs = level_slot(threadIdx.x >> 2);
+  const int j = threadIdx.x & 3, vl = threadIdx.x >> 2, vs = level_slot(vl);
   Row<FT> R;
   R.init(P, j);
   FT W[4], iW[4];
@@ -285,13 +299,15 @@ __global__ void __launch_bounds__(TS_THREADS, 1) k_topo_passA(DevParams<FT> P, i
     int b;
     if (!slab_begin(bar, nbuf, it, e, P.Nh, P.status, issue, b)) break;
     const FT *sY = at(Lo.y, b), *sF = at(Lo.f, b), *sG = at(Lo.g, b), *sT = at(Lo.t, b);
+    face_g33_rows(P, sG, sT, sG33, j, vl);
+    __syncthreads();
     for (int v0 = 0; v0 < Nv; v0 += TS_LEVELS) {
       const int v = min(v0 + vs, Nv - 1);
       const bool act = v0 + vs < Nv;
       TRow<FT> G;
       trow_centre(P, sG, sT, sW, j, P.ltc[v], G);
       TCen<FT> c;
-      tcentre(P, sY, sF, sG, sT, j, v, G, c);
+      tcentre(P, sY, sF, sG33, j, v, G, c);
       FT sd[4];
 #pragma unroll
       for (int i = 0; i < 4; ++i) {
@@ -334,14 +350,48 @@ __global__ void __launch_bounds__(TS_THREADS, 1) k_topo_passA(DevParams<FT> P, i
 }
 
 template <class FT>
+struct alignas(16) TV16 {
+  FT v[16 / sizeof(FT)];
+};
+
+// out = U + c_3 T + sum_j c_j T_j over one slab of n values in 16-byte vectors (T in shared
+// memory, overwritten; U and the T_j at offset off in global memory): the final combination of
+// a stiffly accurate step, as the flat pass B folds it.
+template <class FT>
+__device__ __forceinline__ void tfin_combine(FT *sT, const FT *U, const FT *const (&Tj)[3], const FinArgs<FT> &F,
+                                             size_t off, int n) {
+  constexpr int E = 16 / sizeof(FT);
+  TV16<FT> *sv = reinterpret_cast<TV16<FT> *>(sT);
+  const TV16<FT> *u = reinterpret_cast<const TV16<FT> *>(U + off);
+  for (int i = threadIdx.x; i < n / E; i += TS_THREADS) {
+    TV16<FT> r = u[i];
+    const TV16<FT> t = sv[i];
+#pragma unroll
+    for (int k = 0; k < E; ++k) r.v[k] += F.c[3] * t.v[k];
+#pragma unroll
+    for (int q = 0; q < 3; ++q)
+      if (Tj[q]) {
+        const TV16<FT> a = reinterpret_cast<const TV16<FT> *>(Tj[q] + off)[i];
+#pragma unroll
+        for (int k = 0; k < E; ++k) r.v[k] += F.c[q] * a.v[k];
+      }
+    sv[i] = r;
+  }
+}
+
+// FIN: the slab written is the step's final combination (FinArgs) of the stage state Yc/Yf,
+// the earlier tendencies and this tendency (its u_3 on the bottom and top faces is then set by
+// the filter after the state's DSS).
+template <class FT, bool FIN>
 __global__ void __launch_bounds__(TS_THREADS, 1) k_topo_passB(DevParams<FT> P, int nbuf, const FT *__restrict__ Yc,
                                                              const FT *__restrict__ Yf, const FT *__restrict__ Lin,
-                                                             FT *__restrict__ Tc, FT *__restrict__ Tf) {
+                                                             FT *__restrict__ Tc, FT *__restrict__ Tf, FinArgs<FT> Fa) {
   extern __shared__ __align__(128) unsigned char sm[];
   const int Nv = P.Nv, Nf = P.Nf;
   const TopoBLayout<FT> Lo(Nv, nbuf);
   auto at = [&](const size_t (&off)[2], int b) { return (FT *)(sm + (b ? off[1] : off[0])); };
   FT *sS = (FT *)(sm + Lo.s), *sX1 = (FT *)(sm + Lo.x1), *sX2 = (FT *)(sm + Lo.x2), *sW = (FT *)(sm + Lo.w);
+  FT *sG33 = (FT *)(sm + Lo.gf);
   uint64_t *bar = (uint64_t *)(sm + Lo.bar);
   const uint32_t by = uint32_t(sizeof(FT) * 64 * Nv), bf = uint32_t(sizeof(FT) * 16 * Nf);
   const uint32_t bg = uint32_t(sizeof(FT) * HG_N * 16), bt = uint32_t(sizeof(FT) * TG_N * 16);
@@ -373,6 +423,18 @@ __global__ void __launch_bounds__(TS_THREADS, 1) k_topo_passB(DevParams<FT> P, i
     FT W[4], iW[4];
     ld_row(sW + NQ * j, W);
     ld_row(sW + NN + NQ * j, iW);
+    if (FIN && threadIdx.x == 0) {
+      // the final combination's other operands, into L2 while the tendency is computed
+      bulk_prefetch_l2(Yc + (size_t)e * 64 * Nv, by);
+      bulk_prefetch_l2(Yf + (size_t)e * 16 * Nf, bf);
+      for (int q = 0; q < 3; ++q)
+        if (Fa.te_c[q]) {
+          bulk_prefetch_l2(Fa.te_c[q] + (size_t)e * 64 * Nv, by);
+          bulk_prefetch_l2(Fa.te_f[q] + (size_t)e * 16 * Nf, bf);
+        }
+    }
+    face_g33_rows(P, sG, sT, sG33, j, vl);
+    __syncthreads();
     // ---- P1: centre levels
     for (int v0 = 0; v0 < Nv; v0 += TS_LEVELS) {
       const int v = min(v0 + vs, Nv - 1);
@@ -380,7 +442,7 @@ __global__ void __launch_bounds__(TS_THREADS, 1) k_topo_passB(DevParams<FT> P, i
       TRow<FT> G;
       trow_centre(P, sG, sT, sW, j, P.ltc[v], G);
       TCen<FT> c;
-      tcentre(P, sY, sF, sG, sT, j, v, G, c);
+      tcentre(P, sY, sF, sG33, j, v, G, c);
       FT h[4], Pi[4], thp[4], gg[4], c1[4], c2[4];
 #pragma unroll
       for (int i = 0; i < 4; ++i) {
@@ -513,8 +575,9 @@ __global__ void __launch_bounds__(TS_THREADS, 1) k_topo_passB(DevParams<FT> P, i
       const bool act = k0 + vl < Nf;
       const bool inner = k > 0 && k < Nv;
       const int va = k > 0 ? k - 1 : 0, vb = k < Nv ? k : Nv - 1;
-      FT g33[4], Jf[4], iJf[4], irf[4];
-      trow_face(P, sG, sT, j, P.ltf[k], g33, Jf, iJf, irf);
+      FT g33[4], g33r[4], Jf[4], iJf[4], irf[4];
+      trow_face(P, sG, sT, j, P.ltf[k], g33r, Jf, iJf, irf);
+      ld_row(sG33 + (size_t)k * NN + NQ * j, g33);
       FT C1a[4], C1b[4], C2a[4], C2b[4], Ka[4], Kb[4], Ra[4], Rb[4], La[4], Lb[4], CTa[4], CTb[4];
       ld_row(row(sS, TB_C1, va), C1a);
       ld_row(row(sS, TB_C1, vb), C1b);
@@ -597,6 +660,11 @@ __global__ void __launch_bounds__(TS_THREADS, 1) k_topo_passB(DevParams<FT> P, i
           sY[32 * Nv + q] = Q2[i] - (Xa2[i] + Xb2[i]) / FT(2) / rJ[i];
         }
       }
+    }
+    if (FIN) {
+      __syncthreads();
+      tfin_combine<FT>(sY, Yc, Fa.te_c, Fa, (size_t)e * 64 * Nv, 64 * Nv);
+      tfin_combine<FT>(sF, Yf, Fa.te_f, Fa, (size_t)e * 16 * Nf, 16 * Nf);
     }
     fence_proxy_async();
     __syncthreads();
@@ -701,7 +769,9 @@ cudaError_t configure_topo(int Nv) {
   (void)Nv;
   cudaError_t e = cudaFuncSetAttribute(k_topo_passA<FT>, cudaFuncAttributeMaxDynamicSharedMemorySize, ts_dev().optin);
   if (e != cudaSuccess) return e;
-  return cudaFuncSetAttribute(k_topo_passB<FT>, cudaFuncAttributeMaxDynamicSharedMemorySize, ts_dev().optin);
+  e = cudaFuncSetAttribute(k_topo_passB<FT, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, ts_dev().optin);
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(k_topo_passB<FT, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, ts_dev().optin);
 }
 
 template <class FT>
@@ -713,12 +783,15 @@ void launch_topo_passA(const DevParams<FT> &P, const FT *Yc, const FT *Yf, FT *L
   k_topo_passA<FT><<<grid, TS_THREADS, smem, s>>>(P, nbuf, Yc, Yf, L);
 }
 template <class FT>
-void launch_topo_passB(const DevParams<FT> &P, const FT *Yc, const FT *Yf, const FT *L, FT *Tc, FT *Tf, cudaStream_t s) {
+void launch_topo_passB(const DevParams<FT> &P, const FT *Yc, const FT *Yf, const FT *L, FT *Tc, FT *Tf, cudaStream_t s,
+                       const FinArgs<FT> *fin) {
   int nbuf;
   size_t smem;
   ts_shape<TopoBLayout<FT>>(P.Nv, nbuf, smem);
   const int grid = min(P.Nh, ts_dev().nsm);
-  k_topo_passB<FT><<<grid, TS_THREADS, smem, s>>>(P, nbuf, Yc, Yf, L, Tc, Tf);
+  const FinArgs<FT> F = fin ? *fin : FinArgs<FT>{};
+  if (fin) k_topo_passB<FT, true><<<grid, TS_THREADS, smem, s>>>(P, nbuf, Yc, Yf, L, Tc, Tf, F);
+  else k_topo_passB<FT, false><<<grid, TS_THREADS, smem, s>>>(P, nbuf, Yc, Yf, L, Tc, Tf, F);
 }
 template <class FT>
 void launch_topo_filter(const DevParams<FT> &P, const FT *Yc, FT *Yf, cudaStream_t s) {
@@ -735,7 +808,7 @@ void launch_dss_reduced(const DevParams<FT> &P, FT *C, FT *F, cudaStream_t s) {
   template cudaError_t configure_topo<FT>(int);                                                                   \
   template void launch_topo_passA<FT>(const DevParams<FT> &, const FT *, const FT *, FT *, cudaStream_t);         \
   template void launch_topo_passB<FT>(const DevParams<FT> &, const FT *, const FT *, const FT *, FT *, FT *,       \
-                                      cudaStream_t);                                                              \
+                                      cudaStream_t, const FinArgs<FT> *);                                         \
   template void launch_topo_filter<FT>(const DevParams<FT> &, const FT *, FT *, cudaStream_t);                    \
   template void launch_dss_reduced<FT>(const DevParams<FT> &, FT *, FT *, cudaStream_t);
 INST(float)

@@ -19,101 +19,6 @@ constexpr int DSS_THREADS = 256;  // 8 groups per CTA, one warp per group
 // fused multiply-add or rounded product, so the rounding does not depend on
 // the compiler's contraction choices (the oracle's DSS does the same
 // operations in the same order and matches bit for bit).
-// A group has 2 (edge), 3 (cube corner) or 4 (vertex) copies: up to DSS_MAXC copies are gathered
-// with every load of every copy issued before the first sum (the loads do not wait on one
-// another's latency), then summed in the same fixed order with the same operations as the
-// general loop below (bitwise the same results).
-constexpr int DSS_MAXC = 4;
-
-template <class FT>
-__device__ __forceinline__ void dss_centre_gathered(const DevParams<FT> &P, FT *__restrict__ C, int o0, int m, int lane) {
-  const int Nv = P.Nv;
-  int cid[DSS_MAXC];
-  size_t base[DSS_MAXC];
-  FT w[DSS_MAXC];
-#pragma unroll
-  for (int q = 0; q < DSS_MAXC; ++q) {
-    cid[q] = q < m ? P.gcopy[o0 + q] : P.gcopy[o0];
-    w[q] = q < m ? P.gw[o0 + q] : FT(0);
-    base[q] = ((size_t)(cid[q] >> 4) * 4 * NN + (cid[q] & 15)) * Nv;
-  }
-  for (int v0 = 0; v0 < Nv; v0 += 64) {
-    const int v[2] = {v0 + lane, v0 + 32 + lane};
-    const bool ok[2] = {v[0] < Nv, v[1] < Nv};
-    FT x[DSS_MAXC][2][4];
-#pragma unroll
-    for (int q = 0; q < DSS_MAXC; ++q)
-#pragma unroll
-      for (int h = 0; h < 2; ++h)
-        if (q < m && ok[h]) {
-          const size_t b = base[q] + v[h];
-          x[q][h][0] = C[b];
-          x[q][h][1] = C[b + 16 * Nv];
-          x[q][h][2] = C[b + 32 * Nv];
-          x[q][h][3] = C[b + 48 * Nv];
-        }
-#pragma unroll
-    for (int h = 0; h < 2; ++h) {
-      if (!ok[h]) continue;
-      FT s0 = 0, s3 = 0, X0 = 0, X1 = 0, X2 = 0;
-#pragma unroll
-      for (int q = 0; q < DSS_MAXC; ++q) {
-        if (q >= m) continue;
-        const FT *ec = P.econ + (size_t)cid[q] * 6;   // (L1-resident) basis rows of the copy
-        const FT u1 = x[q][h][1], u2 = x[q][h][2];
-        s0 = fma(w[q], x[q][h][0], s0);
-        s3 = fma(w[q], x[q][h][3], s3);
-        X0 = fma(w[q], fma(u2, ec[3], mul_rn(u1, ec[0])), X0);
-        X1 = fma(w[q], fma(u2, ec[4], mul_rn(u1, ec[1])), X1);
-        X2 = fma(w[q], fma(u2, ec[5], mul_rn(u1, ec[2])), X2);
-      }
-#pragma unroll
-      for (int q = 0; q < DSS_MAXC; ++q) {
-        if (q >= m) continue;
-        const FT *eo = P.ecov + (size_t)cid[q] * 6;
-        const size_t b = base[q] + v[h];
-        C[b] = s0;
-        C[b + 48 * Nv] = s3;
-        C[b + 16 * Nv] = fma(eo[2], X2, fma(eo[1], X1, mul_rn(eo[0], X0)));
-        C[b + 32 * Nv] = fma(eo[5], X2, fma(eo[4], X1, mul_rn(eo[3], X0)));
-      }
-    }
-  }
-}
-
-template <class FT>
-__device__ __forceinline__ void dss_face_gathered(const DevParams<FT> &P, FT *__restrict__ F, int o0, int m, int lane) {
-  const int Nf = P.Nf;
-  size_t base[DSS_MAXC];
-  FT w[DSS_MAXC];
-#pragma unroll
-  for (int q = 0; q < DSS_MAXC; ++q) {
-    base[q] = (size_t)(q < m ? P.gcopy[o0 + q] : P.gcopy[o0]) * Nf;
-    w[q] = q < m ? P.gw[o0 + q] : FT(0);
-  }
-  for (int k0 = 0; k0 < Nf; k0 += 64) {
-    const int k[2] = {k0 + lane, k0 + 32 + lane};
-    const bool ok[2] = {k[0] < Nf, k[1] < Nf};
-    FT x[DSS_MAXC][2];
-#pragma unroll
-    for (int q = 0; q < DSS_MAXC; ++q)
-#pragma unroll
-      for (int h = 0; h < 2; ++h)
-        if (q < m && ok[h]) x[q][h] = F[base[q] + k[h]];
-#pragma unroll
-    for (int h = 0; h < 2; ++h) {
-      if (!ok[h]) continue;
-      FT sf = 0;
-#pragma unroll
-      for (int q = 0; q < DSS_MAXC; ++q)
-        if (q < m) sf = fma(w[q], x[q][h], sf);
-#pragma unroll
-      for (int q = 0; q < DSS_MAXC; ++q)
-        if (q < m) F[base[q] + k[h]] = sf;
-    }
-  }
-}
-
 template <class FT>
 __global__ void __launch_bounds__(DSS_THREADS) k_dss(DevParams<FT> P, FT *__restrict__ C, FT *__restrict__ F) {
   const int lane = threadIdx.x & 31;
@@ -121,11 +26,6 @@ __global__ void __launch_bounds__(DSS_THREADS) k_dss(DevParams<FT> P, FT *__rest
   if (g >= P.ngroups) return;
   const int Nv = P.Nv, Nf = P.Nf;
   const int o0 = P.goff[g], o1 = P.goff[g + 1];
-  if (o1 - o0 <= DSS_MAXC) {
-    if (C) dss_centre_gathered(P, C, o0, o1 - o0, lane);
-    if (F) dss_face_gathered(P, F, o0, o1 - o0, lane);
-    return;
-  }
   if (C) {
     for (int v0 = 0; v0 < Nv; v0 += 64) {
       const int v[2] = {v0 + lane, v0 + 32 + lane};

@@ -192,6 +192,29 @@ def test_terrain_hook_loop_matches_fused_step():
     _assert(field_errors(*Y.numpy(), *a.Y.numpy()), {"rho": 1e-14, "rho_e_tot": 1e-14, "u_1": 1e-12, "u_2": 1e-12, "u_3": 2e-11})
 
 
+@pytest.mark.parametrize("rotate", [False, True])
+def test_terrain_step_in_a_caller_layout(rotate):
+    """Over terrain in the caller's element order and frames (the surface given in that layout):
+    the library-order result moved there, bitwise for a renumbering alone."""
+    from gbdycore import layout as LY
+    cfg, g, o, Yc, Yf = _setup()
+    a = sim.AtmosSimulation(cfg, state=(Yc, Yf))
+    a.step(2)
+    ref = a.Y.numpy()
+    emap, eori = LY.random_layout(cfg.h_elem, seed=5, rotate=rotate)
+    zs = np.asarray(cfg.z_surface)[emap[:, None], LY.NODE_OF[eori & 3]]
+    Xc, Xf = LY.to_caller(Yc, Yf, emap, eori)
+    b = sim.AtmosSimulation(cfg.with_(layout=(emap, eori), z_surface=zs), state=(Xc, Xf))
+    b.step(2)
+    out = LY.from_caller(*b.Y.numpy(), emap, eori)
+    if not rotate:
+        np.testing.assert_array_equal(out[0], ref[0])
+        np.testing.assert_array_equal(out[1], ref[1])
+    else:
+        _assert(field_errors(out[0], out[1], ref[0], ref[1]),
+                {"rho": 1e-14, "rho_e_tot": 1e-14, "u_1": 1e-12, "u_2": 1e-12, "u_3": 2e-11})
+
+
 def test_terrain_context_refuses_what_is_not_built():
     cfg, g, o, Yc, Yf = _setup()
     p = sim.AtmosCache(cfg)

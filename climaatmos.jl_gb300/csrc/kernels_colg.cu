@@ -168,11 +168,11 @@ void launch_gt(const DevParams<FT> &P, const StageArgs<FT> &A, cudaStream_t s) {
     default: k_col_stage_g<FT, G, CM, 3, MINB, TOPO><<<grid, CG_THREADS, 0, s>>>(P, A); break;
   }
 }
-// Over terrain the column's metric is computed per level (more live values): two resident
-// CTAs per SM at most, whatever the flat variant's register cap.
+// Over terrain the column's metric is computed per level from a few per-column values (no spill
+// at the flat variants' register caps).
 template <class FT, int G, int CM, int MINB>
 void launch_g(const DevParams<FT> &P, const StageArgs<FT> &A, cudaStream_t s) {
-  if (P.topo) launch_gt<FT, G, CM, (MINB < 2 ? MINB : 2), true>(P, A, s);
+  if (P.topo) launch_gt<FT, G, CM, MINB, true>(P, A, s);
   else launch_gt<FT, G, CM, MINB, false>(P, A, s);
 }
 

@@ -30,6 +30,12 @@ using namespace se;
 
 constexpr int TS_THREADS = 256;
 constexpr int TS_LEVELS = TS_THREADS / 4;
+// Resident CTAs per SM the terrain slab kernels are compiled for: two in FP32 (a 128-register
+// cap; pass A fits it, pass B spills a few words), one in FP64.
+template <class FT>
+struct TsMinBlocks {
+  static constexpr int value = sizeof(FT) == 4 ? 2 : 1;
+};
 
 template <class FT>
 struct TopoALayout {
@@ -264,7 +270,7 @@ __device__ __forceinline__ void tcentre(const DevParams<FT> &P, const FT *sY, co
 }
 
 template <class FT>
-__global__ void __launch_bounds__(TS_THREADS, 1) k_topo_passA(DevParams<FT> P, int nbuf, const FT *__restrict__ Yc,
+__global__ void __launch_bounds__(TS_THREADS, TsMinBlocks<FT>::value) k_topo_passA(DevParams<FT> P, int nbuf, const FT *__restrict__ Yc,
                                                              const FT *__restrict__ Yf, FT *__restrict__ Lout) {
   extern __shared__ __align__(128) unsigned char sm[];
   const int Nv = P.Nv, Nf = P.Nf;
@@ -383,7 +389,7 @@ __device__ __forceinline__ void tfin_combine(FT *sT, const FT *U, const FT *cons
 // the earlier tendencies and this tendency (its u_3 on the bottom and top faces is then set by
 // the filter after the state's DSS).
 template <class FT, bool FIN>
-__global__ void __launch_bounds__(TS_THREADS, 1) k_topo_passB(DevParams<FT> P, int nbuf, const FT *__restrict__ Yc,
+__global__ void __launch_bounds__(TS_THREADS, TsMinBlocks<FT>::value) k_topo_passB(DevParams<FT> P, int nbuf, const FT *__restrict__ Yc,
                                                              const FT *__restrict__ Yf, const FT *__restrict__ Lin,
                                                              FT *__restrict__ Tc, FT *__restrict__ Tf, FinArgs<FT> Fa) {
   extern __shared__ __align__(128) unsigned char sm[];
@@ -736,7 +742,7 @@ __global__ void __launch_bounds__(256) k_dss_reduced(DevParams<FT> P, FT *__rest
 }
 
 struct TsDev {
-  int nsm = 0, optin = 0;
+  int nsm = 0, optin = 0, per_sm = 0;
 };
 const TsDev &ts_dev() {
   static const TsDev d = [] {
@@ -745,16 +751,23 @@ const TsDev &ts_dev() {
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&x.nsm, cudaDevAttrMultiProcessorCount, dev);
     cudaDeviceGetAttribute(&x.optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    cudaDeviceGetAttribute(&x.per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
     if (x.nsm <= 0) x.nsm = 1;
     return x;
   }();
   return d;
 }
 
-// One CTA per SM: double-buffered slabs when they fit, else single.
-template <class L>
-void ts_shape(int Nv, int &nbuf, size_t &smem) {
-  const size_t two = L(Nv, 2).total, one = L(Nv, 1).total;
+// Buffering and resident CTAs per SM: at the compiled residency (two in FP32) double-buffered
+// slabs if two CTAs' fit the SM (1 KB per CTA reserved), else single-buffered; else one CTA.
+template <class FT, class L>
+void ts_shape(int Nv, int &nbuf, size_t &smem, int &ctas) {
+  const size_t two = L(Nv, 2).total, one = L(Nv, 1).total, per_sm = (size_t)ts_dev().per_sm;
+  if (TsMinBlocks<FT>::value >= 2) {
+    if (2 * (two + 1024) <= per_sm) { nbuf = 2; smem = two; ctas = 2; return; }
+    if (2 * (one + 1024) <= per_sm) { nbuf = 1; smem = one; ctas = 2; return; }
+  }
+  ctas = 1;
   if (two <= (size_t)ts_dev().optin) { nbuf = 2; smem = two; }
   else { nbuf = 1; smem = one; }
 }
@@ -776,19 +789,19 @@ cudaError_t configure_topo(int Nv) {
 
 template <class FT>
 void launch_topo_passA(const DevParams<FT> &P, const FT *Yc, const FT *Yf, FT *L, cudaStream_t s) {
-  int nbuf;
+  int nbuf, ctas;
   size_t smem;
-  ts_shape<TopoALayout<FT>>(P.Nv, nbuf, smem);
-  const int grid = min(P.Nh, ts_dev().nsm);
+  ts_shape<FT, TopoALayout<FT>>(P.Nv, nbuf, smem, ctas);
+  const int grid = min(P.Nh, ts_dev().nsm * ctas);
   k_topo_passA<FT><<<grid, TS_THREADS, smem, s>>>(P, nbuf, Yc, Yf, L);
 }
 template <class FT>
 void launch_topo_passB(const DevParams<FT> &P, const FT *Yc, const FT *Yf, const FT *L, FT *Tc, FT *Tf, cudaStream_t s,
                        const FinArgs<FT> *fin) {
-  int nbuf;
+  int nbuf, ctas;
   size_t smem;
-  ts_shape<TopoBLayout<FT>>(P.Nv, nbuf, smem);
-  const int grid = min(P.Nh, ts_dev().nsm);
+  ts_shape<FT, TopoBLayout<FT>>(P.Nv, nbuf, smem, ctas);
+  const int grid = min(P.Nh, ts_dev().nsm * ctas);
   const FinArgs<FT> F = fin ? *fin : FinArgs<FT>{};
   if (fin) k_topo_passB<FT, true><<<grid, TS_THREADS, smem, s>>>(P, nbuf, Yc, Yf, L, Tc, Tf, F);
   else k_topo_passB<FT, false><<<grid, TS_THREADS, smem, s>>>(P, nbuf, Yc, Yf, L, Tc, Tf, F);

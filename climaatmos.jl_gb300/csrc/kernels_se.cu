@@ -19,6 +19,8 @@
 //        + apply_hyperdiffusion_tendency! (hyperdiffusion.jl:247-307)
 //        + explicit_vertical_advection_tendency! (advection.jl:205-290, deep branch)
 //        + Rayleigh sponge on u_h (remaining_tendency.jl:119-166, rayleigh_sponge.jl:39-44)
+#include <cstdlib>
+
 #include "se_ops.cuh"
 
 namespace gb {
@@ -29,13 +31,6 @@ using namespace se;
 
 constexpr int SE_THREADS = 256;          // 64 level slots x 4 rows per sweep
 constexpr int SE_LEVELS = SE_THREADS / 4;
-// Resident CTAs per SM the slab kernels are compiled for: two in FP32 (a
-// 128-register cap; one CTA computes while the other's slabs stream in), one
-// in FP64 (whose register demand would spill heavily under the cap).
-template <class FT>
-struct SeMinBlocks {
-  static constexpr int value = sizeof(FT) == 4 ? 2 : 1;
-};
 
 // TMA loads of one element's input slabs into buffer set b (thread 0 only).
 template <class FT>
@@ -90,8 +85,11 @@ __device__ __forceinline__ bool begin_element(const DevParams<FT> &P, uint64_t *
   return __syncthreads_and(ok) != 0;
 }
 
-template <class FT>
-__global__ void __launch_bounds__(SE_THREADS, SeMinBlocks<FT>::value) k_passA(DevParams<FT> P, int nbuf, const FT *__restrict__ Yc,
+// MB: the resident CTAs per SM the kernel is compiled for (its register cap): two in FP32 (a
+// 128-register cap; one CTA computes while the other's slabs stream in) or three, one in FP64
+// (whose register demand would spill heavily under the cap).
+template <class FT, int MB>
+__global__ void __launch_bounds__(SE_THREADS, MB) k_passA(DevParams<FT> P, int nbuf, const FT *__restrict__ Yc,
                                                          const FT *__restrict__ Yf, FT *__restrict__ Lout) {
   extern __shared__ __align__(128) unsigned char sm[];
   const int Nv = P.Nv;
@@ -231,8 +229,8 @@ __device__ __forceinline__ void fin_combine(FT *sT, const FT *U, const FT *const
 // the default kernel carries none of its registers or instructions).
 // FIN: the slab written is the step's final combination (FinArgs) of the stage
 // state Yc/Yf, earlier tendencies and this tendency, instead of the tendency.
-template <class FT, bool HS, bool FIN>
-__global__ void __launch_bounds__(SE_THREADS, SeMinBlocks<FT>::value) k_passB(DevParams<FT> P, int nbuf, const FT *__restrict__ Yc,
+template <class FT, bool HS, bool FIN, int MB>
+__global__ void __launch_bounds__(SE_THREADS, MB) k_passB(DevParams<FT> P, int nbuf, const FT *__restrict__ Yc,
                                                          const FT *__restrict__ Yf, const FT *__restrict__ Lin,
                                                          FT *__restrict__ Tc, FT *__restrict__ Tf, FinArgs<FT> F) {
   extern __shared__ __align__(128) unsigned char sm[];
@@ -675,23 +673,32 @@ const SeLaunch &se_dev() {
   return d;
 }
 
-// Buffering and resident CTAs per SM of a slab kernel.  With two CTAs per SM
-// each CTA's slabs must leave room for the other's (1 KB per CTA is reserved
-// by the hardware): prefer double buffering if two such CTAs fit, else single
-// buffering at two CTAs, else one double- or single-buffered CTA.
+// Buffering and resident CTAs per SM of a slab kernel compiled for `ctas` resident CTAs (1 KB
+// per CTA is reserved by the hardware): double buffering if that many such CTAs fit, else
+// single buffering at that many, else one double- or single-buffered CTA.
 struct SeShape {
   int nbuf, ctas;
   size_t smem;
 };
 template <class FT, class L>
-SeShape se_shape(int Nv) {
+SeShape se_shape(int Nv, int ctas) {
   const size_t two = L(Nv, 2).total, one = L(Nv, 1).total, per_sm = (size_t)se_dev().per_sm;
-  if (SeMinBlocks<FT>::value >= 2) {
-    if (2 * (two + 1024) <= per_sm) return {2, 2, two};
-    if (2 * (one + 1024) <= per_sm) return {1, 2, one};
+  if (ctas >= 2) {
+    if (ctas * (two + 1024) <= per_sm) return {2, ctas, two};
+    if (ctas * (one + 1024) <= per_sm) return {1, ctas, one};
   }
   if (two <= (size_t)se_dev().optin) return {2, 1, two};
   return {1, 1, one};
+}
+
+// Resident CTAs per SM of the FP32 slab kernels: two (a 128-register cap) by default; three (an
+// 85-register cap, single-buffered slabs) with GBDYCORE_SE_CTAS=3.
+int se_ctas_env() {
+  static const int v = [] {
+    const char *e = getenv("GBDYCORE_SE_CTAS");
+    return e && atoi(e) == 3 ? 3 : 2;
+  }();
+  return v;
 }
 
 }  // namespace
@@ -703,34 +710,62 @@ size_t passB_smem(int Nv) { return PassBLayout<FT>(Nv, 1).total; }
 
 // Raise the dynamic shared-memory limit of the slab kernels to the device's
 // opt-in maximum once (contexts with different level counts may coexist).
+template <class FT, int MB>
+void configure_se_mb() {
+  cudaFuncSetAttribute(k_passA<FT, MB>, cudaFuncAttributeMaxDynamicSharedMemorySize, se_dev().optin);
+  cudaFuncSetAttribute(k_passB<FT, false, false, MB>, cudaFuncAttributeMaxDynamicSharedMemorySize, se_dev().optin);
+  cudaFuncSetAttribute(k_passB<FT, true, false, MB>, cudaFuncAttributeMaxDynamicSharedMemorySize, se_dev().optin);
+  cudaFuncSetAttribute(k_passB<FT, false, true, MB>, cudaFuncAttributeMaxDynamicSharedMemorySize, se_dev().optin);
+  cudaFuncSetAttribute(k_passB<FT, true, true, MB>, cudaFuncAttributeMaxDynamicSharedMemorySize, se_dev().optin);
+}
 template <class FT>
 void configure_se(int Nv) {
   (void)Nv;
-  cudaFuncSetAttribute(k_passA<FT>, cudaFuncAttributeMaxDynamicSharedMemorySize, se_dev().optin);
-  cudaFuncSetAttribute(k_passB<FT, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, se_dev().optin);
-  cudaFuncSetAttribute(k_passB<FT, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, se_dev().optin);
-  cudaFuncSetAttribute(k_passB<FT, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, se_dev().optin);
-  cudaFuncSetAttribute(k_passB<FT, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, se_dev().optin);
+  if constexpr (sizeof(FT) == 4) {
+    configure_se_mb<FT, 2>();
+    configure_se_mb<FT, 3>();
+  } else {
+    configure_se_mb<FT, 1>();
+  }
 }
 
+template <class FT, int MB>
+void launch_passA_mb(const DevParams<FT> &P, const FT *Yc, const FT *Yf, FT *L, cudaStream_t s) {
+  const SeShape sh = se_shape<FT, PassALayout<FT>>(P.Nv, MB);
+  const int grid = min(P.Nh, se_dev().nsm * sh.ctas);
+  k_passA<FT, MB><<<grid, SE_THREADS, sh.smem, s>>>(P, sh.nbuf, Yc, Yf, L);
+}
 template <class FT>
 void launch_passA(const DevParams<FT> &P, const FT *Yc, const FT *Yf, FT *L, cudaStream_t s) {
-  const SeShape sh = se_shape<FT, PassALayout<FT>>(P.Nv);
+  if constexpr (sizeof(FT) == 4) {
+    if (se_ctas_env() == 3) launch_passA_mb<FT, 3>(P, Yc, Yf, L, s);
+    else launch_passA_mb<FT, 2>(P, Yc, Yf, L, s);
+  } else {
+    launch_passA_mb<FT, 1>(P, Yc, Yf, L, s);
+  }
+}
+template <class FT, int MB>
+void launch_passB_mb(const DevParams<FT> &P, const FT *Yc, const FT *Yf, const FT *L, FT *Tc, FT *Tf, cudaStream_t s,
+                     const FinArgs<FT> *fin) {
+  const SeShape sh = se_shape<FT, PassBLayout<FT>>(P.Nv, MB);
   const int grid = min(P.Nh, se_dev().nsm * sh.ctas);
-  k_passA<FT><<<grid, SE_THREADS, sh.smem, s>>>(P, sh.nbuf, Yc, Yf, L);
+  const FinArgs<FT> F = fin ? *fin : FinArgs<FT>{};
+  if (fin) {
+    if (P.hs) k_passB<FT, true, true, MB><<<grid, SE_THREADS, sh.smem, s>>>(P, sh.nbuf, Yc, Yf, L, Tc, Tf, F);
+    else k_passB<FT, false, true, MB><<<grid, SE_THREADS, sh.smem, s>>>(P, sh.nbuf, Yc, Yf, L, Tc, Tf, F);
+  } else {
+    if (P.hs) k_passB<FT, true, false, MB><<<grid, SE_THREADS, sh.smem, s>>>(P, sh.nbuf, Yc, Yf, L, Tc, Tf, F);
+    else k_passB<FT, false, false, MB><<<grid, SE_THREADS, sh.smem, s>>>(P, sh.nbuf, Yc, Yf, L, Tc, Tf, F);
+  }
 }
 template <class FT>
 void launch_passB(const DevParams<FT> &P, const FT *Yc, const FT *Yf, const FT *L, FT *Tc, FT *Tf, cudaStream_t s,
                   const FinArgs<FT> *fin) {
-  const SeShape sh = se_shape<FT, PassBLayout<FT>>(P.Nv);
-  const int grid = min(P.Nh, se_dev().nsm * sh.ctas);
-  const FinArgs<FT> F = fin ? *fin : FinArgs<FT>{};
-  if (fin) {
-    if (P.hs) k_passB<FT, true, true><<<grid, SE_THREADS, sh.smem, s>>>(P, sh.nbuf, Yc, Yf, L, Tc, Tf, F);
-    else k_passB<FT, false, true><<<grid, SE_THREADS, sh.smem, s>>>(P, sh.nbuf, Yc, Yf, L, Tc, Tf, F);
+  if constexpr (sizeof(FT) == 4) {
+    if (se_ctas_env() == 3) launch_passB_mb<FT, 3>(P, Yc, Yf, L, Tc, Tf, s, fin);
+    else launch_passB_mb<FT, 2>(P, Yc, Yf, L, Tc, Tf, s, fin);
   } else {
-    if (P.hs) k_passB<FT, true, false><<<grid, SE_THREADS, sh.smem, s>>>(P, sh.nbuf, Yc, Yf, L, Tc, Tf, F);
-    else k_passB<FT, false, false><<<grid, SE_THREADS, sh.smem, s>>>(P, sh.nbuf, Yc, Yf, L, Tc, Tf, F);
+    launch_passB_mb<FT, 1>(P, Yc, Yf, L, Tc, Tf, s, fin);
   }
 }
 

@@ -385,6 +385,11 @@ function adjoint_reverse!(Ybar, p)
     return d[1], d[2], Int(peak[])
 end
 
+"""How many trailing checkpoint segments the forward half keeps the stage data of (HBM for
+recomputation: the pullback then recomputes only the segments before them)."""
+adjoint_record_segments!(p, k::Integer) =
+    check(p.gb, ccall((:gb_adjoint_set_record_segments, libgbdycore), Cint, (Ptr{Cvoid}, Cint), p.gb.handle, k))
+
 """Pullback of one step from Y: Ybar (cotangent of the next state in, of Y out)."""
 function step_vjp!(Ybar, Y, p, t, dt)
     d = zeros(Cdouble, 2)
@@ -395,17 +400,19 @@ function step_vjp!(Ybar, Y, p, t, dt)
 end
 
 """
-    ChainRulesCore.rrule(::typeof(solve), Y0, θ, p, dt, n; checkpoint_every = 5)
+    ChainRulesCore.rrule(::typeof(solve), Y0, θ, p, dt, n; checkpoint_every = 5, record_segments = nothing)
 
 Reverse mode of `solve` (the differentiable step that calibration of ν and the sponge rate
 needs): the forward half runs `gb_adjoint_forward` (the n steps, a checkpoint every
-`checkpoint_every`), the pullback `gb_adjoint_reverse` (each checkpoint segment recomputed
-with its stage data kept, then reversed with the transposed SE operators, DSS and column
+`checkpoint_every`, the stage data of the last `record_segments` segments kept), the pullback
+`gb_adjoint_reverse` (each other checkpoint segment recomputed with its stage data kept, then reversed with the transposed SE operators, DSS and column
 solves).  The cotangent of Y_n comes in as a FieldVector; it returns the cotangents of Y0
 and of θ = (ν, rate); `p`, `dt` and `n` get none.
 """
-function ChainRulesCore.rrule(::typeof(solve), Y0, θ::NamedTuple{(:ν, :rate)}, p, dt, n; checkpoint_every = 5)
+function ChainRulesCore.rrule(::typeof(solve), Y0, θ::NamedTuple{(:ν, :rate)}, p, dt, n; checkpoint_every = 5,
+                              record_segments = nothing)
     check_params(p.gb, θ)
+    record_segments === nothing || adjoint_record_segments!(p, record_segments)
     Y = copy(Y0)
     adjoint_forward!(Y, p, dt, n, checkpoint_every)
     function solve_pullback(Ȳ)

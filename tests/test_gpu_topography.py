@@ -215,6 +215,34 @@ def test_terrain_step_in_a_caller_layout(rotate):
                 {"rho": 1e-14, "rho_e_tot": 1e-14, "u_1": 1e-12, "u_2": 1e-12, "u_3": 2e-11})
 
 
+def test_terrain_production_step_matches_oracle():
+    """The production grid (h_elem 30, z_elem 63 stretched from 30 m, dt 120 s, the workload's
+    perturbed state) over the DCMIP-2-0-0 mountain: one FP64 step against the FP64 oracle within
+    the 1e-12 target per field, and the FP32 step against the FP64 oracle."""
+    from gbdycore import config as C
+    O.set_threads(O.max_threads())
+    base = C.production_h30()
+    g = copy.copy(oracle_geometry(base.with_(ft=np.float64)))
+    zs = T.dcmip200_nodes(g.xyz)
+    g.terrain = T.oracle_terrain(g, zs, T.LinearWarp())
+    cfg64 = base.with_(ft=np.float64, z_surface=zs)
+    Yc, Yf = S.workload_state(g, cfg64, "production")
+    o = O.Oracle(g, cfg64.oracle_params(dss_stage1=False))
+    r1 = (Yc.copy(), Yf.copy())
+    o.step(*r1, cfg64.dt, 1)
+    del o
+    s = sim.AtmosSimulation(cfg64, state=(Yc, Yf))
+    s.step(1)
+    e = field_errors(*s.Y.numpy(), *r1)
+    print("terrain, FP64 vs oracle, 1 step:", e)
+    _assert(e, {"rho": 1e-12, "rho_e_tot": 1e-12, "u_1": 1e-12, "u_2": 1e-12, "u_3": 2e-12})
+    s32 = sim.AtmosSimulation(cfg64.with_(ft=np.float32), state=(Yc.astype(np.float32), Yf.astype(np.float32)))
+    s32.step(1)
+    e = field_errors(*s32.Y.numpy(), *r1)
+    print("terrain, FP32 vs FP64 oracle, 1 step:", e)
+    _assert(e, {"rho": 2e-6, "rho_e_tot": 3e-6, "u_1": 1e-4, "u_2": 1e-4, "u_3": 1e-3})
+
+
 def test_terrain_context_refuses_what_is_not_built():
     cfg, g, o, Yc, Yf = _setup()
     p = sim.AtmosCache(cfg)

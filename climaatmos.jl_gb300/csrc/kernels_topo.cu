@@ -30,12 +30,12 @@ using namespace se;
 
 constexpr int TS_THREADS = 256;
 constexpr int TS_LEVELS = TS_THREADS / 4;
-// Resident CTAs per SM the terrain slab kernels are compiled for: pass A two in FP32 (it fits the
-// 128-register cap: 94 -> 80 us at h_elem 30, z_elem 63), one in FP64; pass B one (at the cap it
-// spills 54 words and measured no faster than one CTA of 202 registers: 203 against 201 us).
+// Resident CTAs per SM the terrain slab kernels are compiled for: two in FP32 (the 128-register
+// cap: pass A fits it, 94 -> 80 us at h_elem 30, z_elem 63; pass B spills ten words with its
+// centre phase ordered hyperdiffusion first), one in FP64.
 template <class FT, bool B = false>
 struct TsMinBlocks {
-  static constexpr int value = (sizeof(FT) == 4 && !B) ? 2 : 1;
+  static constexpr int value = sizeof(FT) == 4 ? 2 : 1;
 };
 
 template <class FT>
@@ -97,22 +97,46 @@ template <class FT>
 struct TRow {
   FT J[4], iJ[4], WJ[4], iWJ[4];
   FT u11[4], u12[4], u22[4], u13[4], u23[4];  // g^ij (g^33 of centres is not used)
-  FT d11[4], d12[4], d22[4], d13[4], d23[4], d33[4];
   FT z[4], zsb[4], ir[4], s1i[4], s2i[4], idz[4];  // height, z_s b, 1 / r, s_a / dz, 1 / dz
 };
+
+// The covariant metric g_ij of the row's nodes at the centre level with warp record L (formed
+// only where the vector Laplacians' curls take it, so that it is not held across the pass).
+template <class FT>
+struct TCov {
+  FT d11[4], d12[4], d22[4], d13[4], d23[4], d33[4];
+};
+template <class FT>
+__device__ __forceinline__ void trow_cov(const DevParams<FT> &P, const FT *sG, const FT *sT, int j, const Lev4<FT> &L,
+                                         TCov<FT> &o) {
+  FT b0[4], b1[4], b2[4], zs[4], e1[4], e2[4];
+  ld_row(sG + HG_GD0 * NN + NQ * j, b0);
+  ld_row(sG + HG_GD1 * NN + NQ * j, b1);
+  ld_row(sG + HG_GD2 * NN + NQ * j, b2);
+  ld_row(sT + TG_ZS * NN + NQ * j, zs);
+  ld_row(sT + TG_D1 * NN + NQ * j, e1);
+  ld_row(sT + TG_D2 * NN + NQ * j, e2);
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const TPoint<FT> t = tpoint(P, zs[i], e1[i], e2[i], L);
+    o.d11[i] = t.r2 * b0[i] + t.s1 * t.s1;
+    o.d12[i] = t.r2 * b1[i] + t.s1 * t.s2;
+    o.d22[i] = t.r2 * b2[i] + t.s2 * t.s2;
+    o.d13[i] = t.s1 * t.dz;
+    o.d23[i] = t.s2 * t.dz;
+    o.d33[i] = t.dz * t.dz;
+  }
+}
 
 // Node rows of the element slab: sG the horizontal geometry, sT the terrain, sW = (W, 1/W).
 template <class FT>
 __device__ __forceinline__ void trow_centre(const DevParams<FT> &P, const FT *sG, const FT *sT, const FT *sW, int j,
                                             const Lev4<FT> &L, TRow<FT> &o) {
-  FT Jh[4], a0[4], a1[4], a2[4], b0[4], b1[4], b2[4], zs[4], e1[4], e2[4], W[4];
+  FT Jh[4], a0[4], a1[4], a2[4], zs[4], e1[4], e2[4], W[4];
   ld_row(sG + HG_JH * NN + NQ * j, Jh);
   ld_row(sG + HG_GU0 * NN + NQ * j, a0);
   ld_row(sG + HG_GU1 * NN + NQ * j, a1);
   ld_row(sG + HG_GU2 * NN + NQ * j, a2);
-  ld_row(sG + HG_GD0 * NN + NQ * j, b0);
-  ld_row(sG + HG_GD1 * NN + NQ * j, b1);
-  ld_row(sG + HG_GD2 * NN + NQ * j, b2);
   ld_row(sT + TG_ZS * NN + NQ * j, zs);
   ld_row(sT + TG_D1 * NN + NQ * j, e1);
   ld_row(sT + TG_D2 * NN + NQ * j, e2);
@@ -126,12 +150,6 @@ __device__ __forceinline__ void trow_centre(const DevParams<FT> &P, const FT *sG
     o.WJ[i] = W[i] * o.J[i];
     o.iWJ[i] = grcp(o.WJ[i]);
     o.u11[i] = m.g11; o.u12[i] = m.g12; o.u22[i] = m.g22; o.u13[i] = m.g13; o.u23[i] = m.g23;
-    o.d11[i] = t.r2 * b0[i] + t.s1 * t.s1;
-    o.d12[i] = t.r2 * b1[i] + t.s1 * t.s2;
-    o.d22[i] = t.r2 * b2[i] + t.s2 * t.s2;
-    o.d13[i] = t.s1 * t.dz;
-    o.d23[i] = t.s2 * t.dz;
-    o.d33[i] = t.dz * t.dz;
     o.z[i] = t.z;
     o.zsb[i] = t.zsb;
     o.ir[i] = t.ir;
@@ -180,9 +198,10 @@ __device__ __forceinline__ void face_g33_rows(const DevParams<FT> &P, const FT *
 // C123(wgrad(div u)) fdiv - C123(wcurl(C123(curl u))) of a covariant (c1, c2, c3) with the full
 // metric of the row (the oracle's vec_lap over terrain).
 template <class FT>
-__device__ __forceinline__ void tvec_lap(const DevParams<FT> &P, const Row<FT> &R, const TRow<FT> &G, const FT (&W)[4],
-                                         const FT (&iW)[4], const FT (&c1)[4], const FT (&c2)[4], const FT (&c3)[4],
-                                         FT fdiv, FT (&o1)[4], FT (&o2)[4], FT (&o3)[4]) {
+__device__ __forceinline__ void tvec_lap(const DevParams<FT> &P, const Row<FT> &R, const TRow<FT> &G, const FT *sG,
+                                         const FT *sT, int j, const Lev4<FT> &L, const FT (&W)[4], const FT (&iW)[4],
+                                         const FT (&c1)[4], const FT (&c2)[4], const FT (&c3)[4], FT fdiv,
+                                         FT (&o1)[4], FT (&o2)[4], FT (&o3)[4]) {
   FT a[4], b[4], da[4], db[4], w1[4], w2[4];
 #pragma unroll
   for (int i = 0; i < 4; ++i) {
@@ -200,13 +219,15 @@ __device__ __forceinline__ void tvec_lap(const DevParams<FT> &P, const Row<FT> &
   d2(R, c1, e2);
   d2(R, c3, e3);
   d1(P, c3, e4);
+  TCov<FT> Gd;
+  trow_cov(P, sG, sT, j, L, Gd);
   FT z1[4], z2[4], z3[4];
 #pragma unroll
   for (int i = 0; i < 4; ++i) {
     const FT k1 = e3[i] * G.iJ[i], k2 = -e4[i] * G.iJ[i], k3 = (e1[i] - e2[i]) * G.iJ[i];
-    z1[i] = W[i] * (G.d11[i] * k1 + G.d12[i] * k2 + G.d13[i] * k3);
-    z2[i] = W[i] * (G.d12[i] * k1 + G.d22[i] * k2 + G.d23[i] * k3);
-    z3[i] = W[i] * (G.d13[i] * k1 + G.d23[i] * k2 + G.d33[i] * k3);
+    z1[i] = W[i] * (Gd.d11[i] * k1 + Gd.d12[i] * k2 + Gd.d13[i] * k3);
+    z2[i] = W[i] * (Gd.d12[i] * k1 + Gd.d22[i] * k2 + Gd.d23[i] * k3);
+    z3[i] = W[i] * (Gd.d13[i] * k1 + Gd.d23[i] * k2 + Gd.d33[i] * k3);
   }
   FT f1[4], f2[4], f3[4], f4[4];
   t1(P, z2, f1);
@@ -216,9 +237,9 @@ __device__ __forceinline__ void tvec_lap(const DevParams<FT> &P, const Row<FT> &
 #pragma unroll
   for (int i = 0; i < 4; ++i) {
     const FT q1 = -f3[i] * G.iWJ[i], q2 = f4[i] * G.iWJ[i], q3 = (f2[i] - f1[i]) * G.iWJ[i];
-    o1[i] = -fdiv * w1[i] * iW[i] - (G.d11[i] * q1 + G.d12[i] * q2 + G.d13[i] * q3);
-    o2[i] = -fdiv * w2[i] * iW[i] - (G.d12[i] * q1 + G.d22[i] * q2 + G.d23[i] * q3);
-    o3[i] = -(G.d13[i] * q1 + G.d23[i] * q2 + G.d33[i] * q3);
+    o1[i] = -fdiv * w1[i] * iW[i] - (Gd.d11[i] * q1 + Gd.d12[i] * q2 + Gd.d13[i] * q3);
+    o2[i] = -fdiv * w2[i] * iW[i] - (Gd.d12[i] * q1 + Gd.d22[i] * q2 + Gd.d23[i] * q3);
+    o3[i] = -(Gd.d13[i] * q1 + Gd.d23[i] * q2 + Gd.d33[i] * q3);
   }
 }
 
@@ -325,7 +346,7 @@ __global__ void __launch_bounds__(TS_THREADS, TsMinBlocks<FT>::value) k_topo_pas
         sd[i] = P.cpd * (th.T - th.Tr) + (th.phid + P.grav * G.zsb[i]);
       }
       FT o1[4], o2[4], o3[4];
-      tvec_lap(P, R, G, W, iW, c.u1, c.u2, c.ub3, FT(1), o1, o2, o3);
+      tvec_lap(P, R, G, sG, sT, j, P.ltc[v], W, iW, c.u1, c.u2, c.ub3, FT(1), o1, o2, o3);
       FT g1[4], g2[4], x1[4], x2[4], Ls[4];
       d1(P, sd, g1);
       d2(R, sd, g2);
@@ -442,14 +463,51 @@ __global__ void __launch_bounds__(TS_THREADS, TsMinBlocks<FT, true>::value) k_to
     }
     face_g33_rows(P, sG, sT, sG33, j, vl);
     __syncthreads();
-    // ---- P1: centre levels
+    // ---- P1: centre levels, ordered so that each group of intermediates dies before the
+    // next is formed: the hyperdiffusion of u (the largest) first, then the state's diagnostics
     for (int v0 = 0; v0 < Nv; v0 += TS_LEVELS) {
       const int v = min(v0 + vs, Nv - 1);
       const bool act = v0 + vs < Nv;
       TRow<FT> G;
       trow_centre(P, sG, sT, sW, j, P.ltc[v], G);
+      // hyperdiffusion of u: the Laplacian's covariant 3-vector back on this copy's slopes
+      FT Q1[4], Q2[4];
+      {
+        FT L1[4], L2[4], L3[4], o1[4], o2[4], o3[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          const int q = (NQ * j + i) * Nv + v;
+          L3[i] = sL[48 * Nv + q];
+          L1[i] = sL[16 * Nv + q] + G.s1i[i] * L3[i];
+          L2[i] = sL[32 * Nv + q] + G.s2i[i] * L3[i];
+        }
+        tvec_lap(P, R, G, sG, sT, j, P.ltc[v], W, iW, L1, L2, L3, P.div_damp, o1, o2, o3);
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          Q1[i] = -P.nu_v * o1[i];
+          Q2[i] = -P.nu_v * o2[i];
+        }
+        if (act) st_row(row(sS, TB_L4, v), o3);
+      }
       TCen<FT> c;
       tcentre(P, sY, sF, sG33, j, v, G, c);
+      // rho e_tot: -nu_s wdiv(rho grad L_s)
+      FT Trhoe[4];
+      {
+        FT Ls[4], g1[4], g2[4], x1[4], x2[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) Ls[i] = sL[(NQ * j + i) * Nv + v];
+        d1(P, Ls, g1);
+        d2(R, Ls, g2);
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          x1[i] = c.rho[i] * (G.u11[i] * g1[i] + G.u12[i] * g2[i]);
+          x2[i] = c.rho[i] * (G.u12[i] * g1[i] + G.u22[i] * g2[i]);
+        }
+        twdiv(P, R, G, x1, x2, Trhoe);
+#pragma unroll
+        for (int i = 0; i < 4; ++i) Trhoe[i] *= -P.nu_s;
+      }
       FT h[4], Pi[4], thp[4], gg[4], c1[4], c2[4];
 #pragma unroll
       for (int i = 0; i < 4; ++i) {
@@ -465,7 +523,6 @@ __global__ void __launch_bounds__(TS_THREADS, TsMinBlocks<FT, true>::value) k_to
         c2[i] = c.h2[i] + G.u23[i] * c.ub3[i];
       }
       // vorticity w^3 = wcurl(u_h), Coriolis f^3, (f^3 + w^3) x CT12(u) -> C12, the sponge
-      FT Q1[4], Q2[4];
       {
         FT a[4], bb[4], ta[4], tb[4], f3[4], fh1[4], fh2[4];
 #pragma unroll
@@ -484,14 +541,14 @@ __global__ void __launch_bounds__(TS_THREADS, TsMinBlocks<FT, true>::value) k_to
           const FT fc3 = f3[i] * G.idz[i] - (G.s1i[i] * fh1[i] + G.s2i[i] * fh2[i]) * G.ir[i];
           const FT a3J = G.J[i] * (fc3 + om);
           const FT damp = tsponge(P, G.z[i], P.spg_auh);
-          Q1[i] = a3J * c2[i] - damp * c.u1[i];
-          Q2[i] = -a3J * c1[i] - damp * c.u2[i];
+          Q1[i] += a3J * c2[i] - damp * c.u1[i];
+          Q2[i] += -a3J * c1[i] - damp * c.u2[i];
         }
       }
       // rho: -wdiv(rho u); rho e_tot: -split_div(rho u, h)
-      FT F1[4], F2[4], dm[4], Trhoe[4];
+      FT dm[4];
       {
-        FT G1[4], G2[4], dmh[4], ha[4], hb[4];
+        FT F1[4], F2[4], G1[4], G2[4], dmh[4], ha[4], hb[4];
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
           F1[i] = c.rho[i] * c1[i];
@@ -504,7 +561,7 @@ __global__ void __launch_bounds__(TS_THREADS, TsMinBlocks<FT, true>::value) k_to
         d1(P, h, ha);
         d2(R, h, hb);
 #pragma unroll
-        for (int i = 0; i < 4; ++i) Trhoe[i] = -(dmh[i] + h[i] * dm[i] + F1[i] * ha[i] + F2[i] * hb[i]) / FT(2);
+        for (int i = 0; i < 4; ++i) Trhoe[i] -= (dmh[i] + h[i] * dm[i] + F1[i] * ha[i] + F2[i] * hb[i]) / FT(2);
       }
       // u_h: -[grad(K + Phi - Phi_r) + cp_d (th' grad Pi + grad(th' Pi) - Pi grad th') / 2]
       {
@@ -521,40 +578,6 @@ __global__ void __launch_bounds__(TS_THREADS, TsMinBlocks<FT, true>::value) k_to
           Q2[i] -= a2[i] + P.cpd * FT(0.5) * (thp[i] * b2[i] - Pi[i] * f2[i]);
         }
       }
-      // hyperdiffusion of u: the Laplacian's covariant 3-vector back on this copy's slopes
-      FT L3[4], o3[4];
-      {
-        FT L1[4], L2[4], o1[4], o2[4];
-#pragma unroll
-        for (int i = 0; i < 4; ++i) {
-          const int q = (NQ * j + i) * Nv + v;
-          L3[i] = sL[48 * Nv + q];
-          L1[i] = sL[16 * Nv + q] + G.s1i[i] * L3[i];
-          L2[i] = sL[32 * Nv + q] + G.s2i[i] * L3[i];
-        }
-        tvec_lap(P, R, G, W, iW, L1, L2, L3, P.div_damp, o1, o2, o3);
-#pragma unroll
-        for (int i = 0; i < 4; ++i) {
-          Q1[i] -= P.nu_v * o1[i];
-          Q2[i] -= P.nu_v * o2[i];
-        }
-      }
-      // rho e_tot: -nu_s wdiv(rho grad L_s)
-      {
-        FT Ls[4], g1[4], g2[4], x1[4], x2[4], hd[4];
-#pragma unroll
-        for (int i = 0; i < 4; ++i) Ls[i] = sL[(NQ * j + i) * Nv + v];
-        d1(P, Ls, g1);
-        d2(R, Ls, g2);
-#pragma unroll
-        for (int i = 0; i < 4; ++i) {
-          x1[i] = c.rho[i] * (G.u11[i] * g1[i] + G.u12[i] * g2[i]);
-          x2[i] = c.rho[i] * (G.u12[i] * g1[i] + G.u22[i] * g2[i]);
-        }
-        twdiv(P, R, G, x1, x2, hd);
-#pragma unroll
-        for (int i = 0; i < 4; ++i) Trhoe[i] -= P.nu_s * hd[i];
-      }
       if (act) {
         FT rJ[4];
 #pragma unroll
@@ -563,7 +586,6 @@ __global__ void __launch_bounds__(TS_THREADS, TsMinBlocks<FT, true>::value) k_to
         st_row(row(sS, TB_C2, v), c2);
         st_row(row(sS, TB_K, v), c.K);
         st_row(row(sS, TB_RJ, v), rJ);
-        st_row(row(sS, TB_L4, v), o3);
         st_row(row(sS, TB_Q1, v), Q1);
         st_row(row(sS, TB_Q2, v), Q2);
         st_row(row(sS, TB_CT3, v), c.ct3);

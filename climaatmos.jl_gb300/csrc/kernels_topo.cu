@@ -33,7 +33,7 @@ constexpr int TS_LEVELS = TS_THREADS / 4;
 // Resident CTAs per SM the terrain slab kernels are compiled for: two in FP32 (the 128-register
 // cap: pass A fits it, 94 -> 80 us at h_elem 30, z_elem 63; pass B spills ten words with its
 // centre phase ordered hyperdiffusion first), one in FP64.
-template <class FT, bool B = false>
+template <class FT>
 struct TsMinBlocks {
   static constexpr int value = sizeof(FT) == 4 ? 2 : 1;
 };
@@ -411,7 +411,7 @@ __device__ __forceinline__ void tfin_combine(FT *sT, const FT *U, const FT *cons
 // the earlier tendencies and this tendency (its u_3 on the bottom and top faces is then set by
 // the filter after the state's DSS).
 template <class FT, bool FIN>
-__global__ void __launch_bounds__(TS_THREADS, TsMinBlocks<FT, true>::value) k_topo_passB(DevParams<FT> P, int nbuf, const FT *__restrict__ Yc,
+__global__ void __launch_bounds__(TS_THREADS, TsMinBlocks<FT>::value) k_topo_passB(DevParams<FT> P, int nbuf, const FT *__restrict__ Yc,
                                                              const FT *__restrict__ Yf, const FT *__restrict__ Lin,
                                                              FT *__restrict__ Tc, FT *__restrict__ Tf, FinArgs<FT> Fa) {
   extern __shared__ __align__(128) unsigned char sm[];
@@ -783,10 +783,10 @@ const TsDev &ts_dev() {
 
 // Buffering and resident CTAs per SM: at the compiled residency (two in FP32) double-buffered
 // slabs if two CTAs' fit the SM (1 KB per CTA reserved), else single-buffered; else one CTA.
-template <class FT, class L, bool B>
+template <class FT, class L>
 void ts_shape(int Nv, int &nbuf, size_t &smem, int &ctas) {
   const size_t two = L(Nv, 2).total, one = L(Nv, 1).total, per_sm = (size_t)ts_dev().per_sm;
-  if (TsMinBlocks<FT, B>::value >= 2) {
+  if (TsMinBlocks<FT>::value >= 2) {
     if (2 * (two + 1024) <= per_sm) { nbuf = 2; smem = two; ctas = 2; return; }
     if (2 * (one + 1024) <= per_sm) { nbuf = 1; smem = one; ctas = 2; return; }
   }
@@ -814,7 +814,7 @@ template <class FT>
 void launch_topo_passA(const DevParams<FT> &P, const FT *Yc, const FT *Yf, FT *L, cudaStream_t s) {
   int nbuf, ctas;
   size_t smem;
-  ts_shape<FT, TopoALayout<FT>, false>(P.Nv, nbuf, smem, ctas);
+  ts_shape<FT, TopoALayout<FT>>(P.Nv, nbuf, smem, ctas);
   const int grid = min(P.Nh, ts_dev().nsm * ctas);
   k_topo_passA<FT><<<grid, TS_THREADS, smem, s>>>(P, nbuf, Yc, Yf, L);
 }
@@ -823,7 +823,7 @@ void launch_topo_passB(const DevParams<FT> &P, const FT *Yc, const FT *Yf, const
                        const FinArgs<FT> *fin) {
   int nbuf, ctas;
   size_t smem;
-  ts_shape<FT, TopoBLayout<FT>, true>(P.Nv, nbuf, smem, ctas);
+  ts_shape<FT, TopoBLayout<FT>>(P.Nv, nbuf, smem, ctas);
   const int grid = min(P.Nh, ts_dev().nsm * ctas);
   const FinArgs<FT> F = fin ? *fin : FinArgs<FT>{};
   if (fin) k_topo_passB<FT, true><<<grid, TS_THREADS, smem, s>>>(P, nbuf, Yc, Yf, L, Tc, Tf, F);

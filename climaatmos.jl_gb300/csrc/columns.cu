@@ -513,7 +513,8 @@ int gb_columns_create(const gb_config *cfg, int ncols, const int *z_elem, gb_col
   GB_RANGE();
   if (!out) return GB_ERR_ARG;
   *out = nullptr;
-  if (!cfg || ncols <= 0 || !z_elem || (cfg->ft_bytes != 4 && cfg->ft_bytes != 8) || !(cfg->z_max > 0))
+  // the batched columns are dry (moist 0M is built for the column hooks of a context)
+  if (!cfg || ncols <= 0 || !z_elem || (cfg->ft_bytes != 4 && cfg->ft_bytes != 8) || !(cfg->z_max > 0) || cfg->moist)
     return GB_ERR_ARG;
   auto *c = new (std::nothrow) gb_columns();
   if (!c) return GB_ERR_NOMEM;

@@ -52,6 +52,11 @@ struct DevParams {
   const FT *tgeo;
   const Lev4<FT> *ltc, *ltf;
   FT iR, spg_auh, spg_aw, spg_zd, spg_k;
+  // Moist 0M (moist = 1): R_v; cv of vapour, liquid and ice; cp_v - cp_l, cp_v - cp_i; L_v0,
+  // L_s0; 1 / T_triple, p_triple; T_freeze, T_icenuc, 1 / (T_freeze - T_icenuc), pow_icenuc;
+  // e_int_v0 = L_v0 - R_v T_0, e_int_i0 = L_s0 - L_v0; Newton iterations of the adjustment
+  int moist, sa_iters;
+  FT Rv, cvv, cvl, cvi, dcl, dci, Lv0, Ls0, iTtr, ptr, Tfrz, Tice, iTrng, pice, ev0, ei0;
 };
 
 // ---------------------------------------------------------------- math
@@ -79,6 +84,8 @@ __device__ __forceinline__ float glog_ratio(float p, float p0, float ip0) {
 __device__ __forceinline__ double glog_ratio(double p, double p0, double ip0) { return log1p((p - p0) * ip0); }
 __device__ __forceinline__ float gexpm1(float x) { return __expf(x) - 1.0f; }
 __device__ __forceinline__ double gexpm1(double x) { return expm1(x); }
+__device__ __forceinline__ float gexp(float x) { return __expf(x); }
+__device__ __forceinline__ double gexp(double x) { return exp(x); }
 
 template <class FT>
 __device__ __forceinline__ FT shfl(FT v, int src, int width) {
@@ -155,6 +162,112 @@ __device__ __forceinline__ void thermo_pair(const DevParams<float> &P, float2 rh
   const float2 e7 = __fmul2_rn(lx, bc2(7.0f));
   const float2 em = __fadd2_rn(make_float2(__expf(e7.x), __expf(e7.y)), bc2(-1.0f));
   phid = __ffma2_rn(rz, em, __fmul2_rn(bc2(P.cpTmin), lx));
+}
+
+// ---- moist thermodynamics (EquilibriumMicrophysics0M) ----
+// The formulation of Thermodynamics.jl 1.3.0 that the reference's Jacobian assumes (its dp/drho
+// and dp/d(rho q_tot), manual_sparse_jacobian.jl:646-685, follow from these definitions):
+//   cv_m  = cv_d + (cv_v - cv_d) q_t + (cv_l - cv_v) q_l + (cv_i - cv_v) q_i
+//   R_m   = R_d (1 - q_t) + R_v (q_t - q_l - q_i)
+//   e_int = cv_m (T - T_0) + q_v e_int_v0 - q_i e_int_i0 - (1 - q_t) R_d T_0
+//   q_v*  = p_v*(T) / (rho R_v T),  p_v* = p_tr (T / T_tr)^(dcp / R_v) exp((L_0 - dcp T_0) / R_v (1 / T_tr - 1 / T))
+//           with L_0 and dcp the liquid-fraction weighted latent heat and cp_v - cp_(l,i)
+//   lam(T) = 1 above T_freeze, 0 at or below T_icenuc, ((T - T_icenuc) / (T_freeze - T_icenuc))^pow between.
+// The liquid fraction and its T-derivative.
+template <class FT>
+__device__ __forceinline__ FT liq_frac(const DevParams<FT> &P, FT T, FT &dl) {
+  if (T > P.Tfrz) { dl = FT(0); return FT(1); }
+  if (!(T > P.Tice)) { dl = FT(0); return FT(0); }
+  const FT x = (T - P.Tice) * P.iTrng;
+  if (P.pice == FT(1)) { dl = P.iTrng; return x; }
+  dl = P.pice * gpow(x, P.pice - FT(1)) * P.iTrng;
+  return gpow(x, P.pice);
+}
+// q_v*(T, rho) and d ln q_v* / dT (the L_0 and dcp weights follow lam(T) too)
+template <class FT>
+__device__ __forceinline__ FT qsat(const DevParams<FT> &P, FT T, FT rho, FT &dlnq) {
+  FT dl;
+  const FT lam = liq_frac(P, T, dl);
+  const FT iRv = grcp(P.Rv), iT = grcp(T);
+  const FT dcp = lam * P.dcl + (FT(1) - lam) * P.dci, L0 = lam * P.Lv0 + (FT(1) - lam) * P.Ls0;
+  const FT a = dcp * iRv, b = (L0 - dcp * P.T0) * iRv, sd = P.iTtr - iT;
+  const FT lt = glog(T * P.iTtr);
+  const FT ps = P.ptr * gexp(a * lt + b * sd);
+  const FT dd = P.dcl - P.dci;
+  const FT dlp = a * iT + b * iT * iT + dl * (dd * iRv * lt + ((P.Lv0 - P.Ls0) - dd * P.T0) * iRv * sd);
+  dlnq = dlp - iT;
+  return gdiv(ps, rho * P.Rv * T);
+}
+// The saturation adjustment in (rho, e_int, q_tot) (TD.saturation_adjustment with TD.ρe(),
+// precomputed_quantities.jl:734-747): the all-vapour temperature T_u if the point is unsaturated
+// there, else sa_iters safeguarded Newton iterations on f(T) = e_int(T) - e_int with the saturated
+// partition q_c = q_t - q_v*(T) continued smoothly where q_v* > q_t (the clamped function's kink
+// makes plain Newton cycle).  f increases with T and
+// [T_u, max(T_u + q_t (e_int_v0 + e_int_i0) / cv_d, T_0) + 1] brackets its root; a step outside
+// the current bracket becomes a bisection.  The partition is that of the final T.
+template <class FT>
+__device__ __forceinline__ void sat_adjust(const DevParams<FT> &P, FT rho, FT eint, FT q, FT &T, FT &ql, FT &qi) {
+  const FT cvm0 = P.cvd + (P.cvv - P.cvd) * q;
+  T = P.T0 + gdiv(eint - q * P.ev0 + (FT(1) - q) * P.Rd * P.T0, cvm0);
+  T = T > P.Tmin_sgs ? T : P.Tmin_sgs;
+  FT dlnq;
+  ql = qi = FT(0);
+  if (q <= qsat(P, T, rho, dlnq)) return;
+  FT lo = T, hi = fmax(T + gdiv(q * (P.ev0 + P.ei0), P.cvd), P.T0) + FT(1);
+  for (int it = 0; it < P.sa_iters; ++it) {
+    FT dl;
+    const FT lam = liq_frac(P, T, dl);
+    const FT qs = qsat(P, T, rho, dlnq);
+    const FT qc = q - qs;
+    const FT l = lam * qc, i = (FT(1) - lam) * qc;
+    const FT cvm = P.cvd + (P.cvv - P.cvd) * q + (P.cvl - P.cvv) * l + (P.cvi - P.cvv) * i;
+    const FT f = cvm * (T - P.T0) + qs * P.ev0 - i * P.ei0 - (FT(1) - q) * P.Rd * P.T0 - eint;
+    const FT dqc = -qs * dlnq;
+    const FT dql = dl * qc + lam * dqc, dqi = -dl * qc + (FT(1) - lam) * dqc;
+    const FT df = cvm + (T - P.T0) * ((P.cvl - P.cvv) * dql + (P.cvi - P.cvv) * dqi) - dqc * P.ev0 - dqi * P.ei0;
+    if (f < FT(0)) lo = T;
+    else hi = T;
+    const FT Tn = T - gdiv(f, df);
+    T = (Tn >= lo && Tn <= hi) ? Tn : (lo + hi) / FT(2);
+  }
+  FT dl;
+  const FT lam = liq_frac(P, T, dl);
+  const FT qc = fmax(FT(0), q - qsat(P, T, rho, dlnq));
+  ql = lam * qc;
+  qi = (FT(1) - lam) * qc;
+}
+// thermo() of moist air: T from the saturation adjustment of max(0, q_tot), p = rho R_m T,
+// h_tot = e_tot + R_m T, theta_v = T R_m / (Pi R_d) (refstate_thermodynamics.jl:58-63); also
+// q = specific(rho q_tot, rho), kappa_m = R_m / cv_m (ᶜkappa_m_field!) and dp/d(rho q_tot) at
+// constant rho and rho e_tot (ᶜ∂p∂ρq_tot_field!, manual_sparse_jacobian.jl:646-685).
+template <class FT>
+__device__ __forceinline__ void thermo_moist(const DevParams<FT> &P, FT rho, FT rhoe, FT rhoq, FT K, FT Phi,
+                                             const Lev4<FT> &rl, Thermo<FT> &o, FT &q, FT &kapm, FT &dpdq) {
+  const FT irho = grcp(rho);
+  const FT e_tot = rhoe * irho;
+  const FT eint = e_tot - K - Phi;
+  q = rhoq * irho;
+  const FT qn = fmax(FT(0), q);
+  FT T, ql, qi;
+  sat_adjust(P, rho, eint, qn, T, ql, qi);
+  const FT Rm = P.Rd * (FT(1) - qn) + P.Rv * (qn - ql - qi);
+  const FT cvm = P.cvd + (P.cvv - P.cvd) * qn + (P.cvl - P.cvv) * ql + (P.cvi - P.cvv) * qi;
+  const FT p = rho * Rm * T;
+  const FT Pi = gpow(p * P.ipref, P.kappa);
+  const FT Pi2 = Pi * Pi, Pi7 = Pi2 * Pi2 * Pi2 * Pi;
+  const FT Tr = P.Tmin_ref + (P.Tsfc_ref - P.Tmin_ref) * Pi7;
+  const FT iPi = grcp(Pi);
+  o.T = T;
+  o.p = p;
+  o.h = e_tot + Rm * T;
+  o.Pi = Pi;
+  o.thv = gdiv(T * Rm, Pi * P.Rd);
+  o.thvr = Tr * iPi;
+  o.Tr = Tr;
+  const FT lx = P.kappa * glog_ratio(p, rl.x, rl.y);
+  o.phid = P.cpTmin * lx + rl.z * gexpm1(FT(7) * lx);
+  kapm = gdiv(Rm, cvm);
+  dpdq = kapm * (-P.ev0 - P.Rd * P.T0 - (P.cvv - P.cvd) * (T - P.T0)) + (P.Rv - P.Rd) * T;
 }
 
 // Reverse mode of thermo(): the cotangents of its outputs (T, p, h, Pi, thv,

@@ -246,6 +246,18 @@ int create_impl(gb_ctx *ctx) {
   P.spg_aw = (FT)c.alpha_w;
   P.spg_zd = (FT)c.sponge_zd;
   P.spg_k = (FT)(M_PI / (2.0 * (c.z_max - c.sponge_zd)));
+  P.moist = c.moist ? 1 : 0;
+  if (P.moist) {
+    P.sa_iters = c.sa_iters;
+    P.Rv = (FT)c.R_v;
+    P.cvv = (FT)(c.cp_v - c.R_v); P.cvl = (FT)c.cp_l; P.cvi = (FT)c.cp_i;
+    P.dcl = (FT)(c.cp_v - c.cp_l); P.dci = (FT)(c.cp_v - c.cp_i);
+    P.Lv0 = (FT)c.LH_v0; P.Ls0 = (FT)c.LH_s0;
+    P.iTtr = (FT)(1.0 / c.T_triple); P.ptr = (FT)c.press_triple;
+    P.Tfrz = (FT)c.T_freeze; P.Tice = (FT)c.T_icenuc; P.iTrng = (FT)(1.0 / (c.T_freeze - c.T_icenuc));
+    P.pice = (FT)c.pow_icenuc;
+    P.ev0 = (FT)(c.LH_v0 - c.R_v * c.T_0); P.ei0 = (FT)(c.LH_s0 - c.LH_v0);
+  }
   ars343(I->ae, I->ai, I->be, I->bi);
   I->stiffly_accurate = true;
   for (int j = 0; j < 4; ++j) I->stiffly_accurate = I->stiffly_accurate && I->bi[j] == I->ai[3][j];
@@ -310,7 +322,8 @@ template <class FT>
 int column_hook_t(gb_ctx *ctx, int mode, gb_fieldvec O, gb_fieldvec Y, double dtg) {
   Impl<FT> *I = impl<FT>(ctx);
   if (mode == COL_JACOBIAN && !I->jac.p) {
-    int r = alloc(ctx, I->jac, (size_t)I->P.Nh * NN * (I->P.topo ? JAC_QT : JAC_Q) * I->P.Nf * sizeof(FT));
+    const int nq = I->P.topo ? JAC_QT : (I->P.moist ? JAC_QM : JAC_Q);
+    int r = alloc(ctx, I->jac, (size_t)I->P.Nh * NN * nq * I->P.Nf * sizeof(FT));
     if (r) return r;
   }
   if (mode == COL_LDIV && !I->jac_valid) return fail(ctx, GB_ERR_STATE, "gb_ldiv called before gb_update_jacobian");
@@ -1184,6 +1197,13 @@ bool fv_ok(gb_fieldvec v) { return v.c && v.f && aligned(v.c) && aligned(v.f); }
     if ((ctx)->geo.topo) return fail((ctx), GB_ERR_ARG, what " is not available over terrain");   \
   } while (0)
 
+// A moist 0M context supports the column hooks only (gb_set_precomputed_quantities,
+// gb_implicit_tendency, gb_update_jacobian, gb_ldiv, gb_correct_implicit_advection_tendency).
+#define NO_MOIST(ctx, what)                                                                            \
+  do {                                                                                                 \
+    if ((ctx) && (ctx)->cfg.moist) return fail((ctx), GB_ERR_ARG, what " is not available with moist = 1"); \
+  } while (0)
+
 }  // namespace
 
 extern "C" {
@@ -1194,7 +1214,7 @@ int gb_sizes(const gb_config *cfg, size_t *n_center, size_t *n_face, int *n_grou
   const char *why = nullptr;
   if (!validate_config(*cfg, &why)) return GB_ERR_ARG;
   const size_t Nh = 6 * (size_t)cfg->h_elem * cfg->h_elem;
-  if (n_center) *n_center = Nh * 4 * NN * cfg->z_elem;
+  if (n_center) *n_center = Nh * (cfg->moist ? 5 : 4) * NN * cfg->z_elem;
   if (n_face) *n_face = Nh * NN * (cfg->z_elem + 1);
   if (n_groups || n_copies || cfg->z_surface) {
     HostGeometry g;
@@ -1300,6 +1320,7 @@ int gb_set_precomputed_quantities(gb_ctx *ctx, gb_fieldvec Y, double t) {
 
 int gb_remaining_tendency(gb_ctx *ctx, gb_fieldvec Yt, gb_fieldvec Y, double t) {
   GB_RANGE();
+  NO_MOIST(ctx, "gb_remaining_tendency");
   GUARD(ctx);
   (void)t;
   if (!fv_ok(Y) || !fv_ok(Yt)) return fail(ctx, GB_ERR_ARG, "null or misaligned pointer");
@@ -1340,6 +1361,7 @@ int gb_correct_implicit_advection_tendency(gb_ctx *ctx, gb_fieldvec Yt, gb_field
 
 int gb_dss(gb_ctx *ctx, gb_fieldvec Y) {
   GB_RANGE();
+  NO_MOIST(ctx, "gb_dss");
   GUARD(ctx);
   if (!fv_ok(Y)) return fail(ctx, GB_ERR_ARG, "null or misaligned pointer");
   if (ctx->cfg.ft_bytes == 8) launch_dss<double>(impl<double>(ctx)->P, (double *)Y.c, (double *)Y.f, ctx->stream);
@@ -1349,6 +1371,7 @@ int gb_dss(gb_ctx *ctx, gb_fieldvec Y) {
 
 int gb_step(gb_ctx *ctx, gb_fieldvec Y, double t, double dt, int nsteps, int use_graph) {
   GB_RANGE();
+  NO_MOIST(ctx, "gb_step");
   GUARD(ctx);
   (void)t;
   if (!fv_ok(Y)) return fail(ctx, GB_ERR_ARG, "null or misaligned pointer");
@@ -1360,6 +1383,7 @@ int gb_step(gb_ctx *ctx, gb_fieldvec Y, double t, double dt, int nsteps, int use
 
 int gb_global_sums(gb_ctx *ctx, gb_fieldvec Y, double out[2]) {
   GB_RANGE();
+  NO_MOIST(ctx, "gb_global_sums");
   GUARD(ctx);
   if (!fv_ok(Y) || !out) return fail(ctx, GB_ERR_ARG, "null or misaligned pointer");
   return DISPATCH(ctx, global_sums_t, ctx, Y, out);
@@ -1374,6 +1398,7 @@ int gb_newton_residual(gb_ctx *ctx, double out[3]) {
 
 int gb_jacobian_solve_noalloc(gb_ctx *ctx, gb_fieldvec dY, gb_fieldvec Y, gb_fieldvec R, double dtgamma) {
   GB_RANGE();
+  NO_MOIST(ctx, "gb_jacobian_solve_noalloc");
   GUARD(ctx);
   NO_TERRAIN(ctx, "gb_jacobian_solve_noalloc");
   if (!fv_ok(dY) || !fv_ok(Y) || !fv_ok(R)) return fail(ctx, GB_ERR_ARG, "null or misaligned pointer");
@@ -1382,6 +1407,7 @@ int gb_jacobian_solve_noalloc(gb_ctx *ctx, gb_fieldvec dY, gb_fieldvec Y, gb_fie
 
 int gb_dss_transpose(gb_ctx *ctx, gb_fieldvec X) {
   GB_RANGE();
+  NO_MOIST(ctx, "gb_dss_transpose");
   if (!ctx || !X.c || !X.f) return GB_ERR_ARG;
   return ctx->cfg.ft_bytes == 8 ? dss_transpose_t<double>(ctx, X) : dss_transpose_t<float>(ctx, X);
 }
@@ -1389,6 +1415,7 @@ int gb_dss_transpose(gb_ctx *ctx, gb_fieldvec X) {
 int gb_remaining_tendency_vjp(gb_ctx *ctx, gb_fieldvec Ybar, gb_fieldvec Tbar, gb_fieldvec Y, double t,
                               double dparams[2]) {
   GB_RANGE();
+  NO_MOIST(ctx, "gb_remaining_tendency_vjp");
   if (ctx && ctx->geo.topo) return fail(ctx, GB_ERR_ARG, "gb_remaining_tendency_vjp is not available over terrain");
   (void)t;
   if (!ctx || !fv_ok(Ybar) || !fv_ok(Tbar) || !fv_ok(Y)) return GB_ERR_ARG;
@@ -1398,6 +1425,7 @@ int gb_remaining_tendency_vjp(gb_ctx *ctx, gb_fieldvec Ybar, gb_fieldvec Tbar, g
 
 int gb_implicit_stage(gb_ctx *ctx, gb_fieldvec U, gb_fieldvec Timp, gb_fieldvec Uhat, double dtgamma) {
   GB_RANGE();
+  NO_MOIST(ctx, "gb_implicit_stage");
   if (!ctx || !U.c || !U.f || !Timp.c || !Timp.f || !Uhat.c || !Uhat.f || !(dtgamma > 0)) return GB_ERR_ARG;
   return ctx->cfg.ft_bytes == 8 ? implicit_stage_t<double>(ctx, U, Timp, Uhat, dtgamma)
                                 : implicit_stage_t<float>(ctx, U, Timp, Uhat, dtgamma);
@@ -1406,6 +1434,7 @@ int gb_implicit_stage(gb_ctx *ctx, gb_fieldvec U, gb_fieldvec Timp, gb_fieldvec 
 int gb_implicit_stage_vjp(gb_ctx *ctx, gb_fieldvec Uhat_bar, gb_fieldvec Ubar, gb_fieldvec Timp_bar, gb_fieldvec Uhat,
                           double dtgamma, double dparams[2]) {
   GB_RANGE();
+  NO_MOIST(ctx, "gb_implicit_stage_vjp");
   if (ctx && ctx->geo.topo) return fail(ctx, GB_ERR_ARG, "gb_implicit_stage_vjp is not available over terrain");
   if (!ctx || !Uhat_bar.c || !Ubar.c || !Timp_bar.c || !Uhat.c || !(dtgamma > 0)) return GB_ERR_ARG;
   return ctx->cfg.ft_bytes == 8 ? implicit_stage_vjp_t<double>(ctx, Uhat_bar, Ubar, Timp_bar, Uhat, dtgamma, dparams)
@@ -1414,6 +1443,7 @@ int gb_implicit_stage_vjp(gb_ctx *ctx, gb_fieldvec Uhat_bar, gb_fieldvec Ubar, g
 
 int gb_step_vjp(gb_ctx *ctx, gb_fieldvec Ybar, gb_fieldvec Y, double t, double dt, double dparams[2]) {
   GB_RANGE();
+  NO_MOIST(ctx, "gb_step_vjp");
   if (ctx && ctx->geo.topo) return fail(ctx, GB_ERR_ARG, "gb_step_vjp is not available over terrain");
   (void)t;
   if (!ctx || !fv_ok(Ybar) || !fv_ok(Y) || !(dt > 0)) return GB_ERR_ARG;
@@ -1423,6 +1453,7 @@ int gb_step_vjp(gb_ctx *ctx, gb_fieldvec Ybar, gb_fieldvec Y, double t, double d
 
 int gb_adjoint_forward(gb_ctx *ctx, gb_fieldvec Y, double t0, double dt, int nsteps, int checkpoint_every) {
   GB_RANGE();
+  NO_MOIST(ctx, "gb_adjoint_forward");
   if (ctx && ctx->geo.topo) return fail(ctx, GB_ERR_ARG, "gb_adjoint_forward is not available over terrain");
   (void)t0;
   if (!ctx || !fv_ok(Y) || !(dt > 0) || nsteps < 1 || checkpoint_every < 1) return GB_ERR_ARG;
@@ -1432,6 +1463,7 @@ int gb_adjoint_forward(gb_ctx *ctx, gb_fieldvec Y, double t0, double dt, int nst
 
 int gb_adjoint_reverse(gb_ctx *ctx, gb_fieldvec Ybar, double dparams[2], size_t *peak_bytes) {
   GB_RANGE();
+  NO_MOIST(ctx, "gb_adjoint_reverse");
   if (ctx && ctx->geo.topo) return fail(ctx, GB_ERR_ARG, "gb_adjoint_reverse is not available over terrain");
   if (!ctx || !fv_ok(Ybar)) return GB_ERR_ARG;
   return ctx->cfg.ft_bytes == 8 ? adjoint_reverse_t<double>(ctx, Ybar, dparams, peak_bytes)
@@ -1440,6 +1472,7 @@ int gb_adjoint_reverse(gb_ctx *ctx, gb_fieldvec Ybar, double dparams[2], size_t 
 
 int gb_adjoint_set_record_segments(gb_ctx *ctx, int segments) {
   GB_RANGE();
+  NO_MOIST(ctx, "gb_adjoint_set_record_segments");
   GUARD(ctx);
   if (segments < 1) return fail(ctx, GB_ERR_ARG, "gb_adjoint_set_record_segments: segments must be >= 1");
   if (ctx->geo.topo) return fail(ctx, GB_ERR_ARG, "gb_adjoint_set_record_segments is not available over terrain");
@@ -1478,6 +1511,7 @@ int gb_selftest_bounded_wait(gb_ctx *ctx, double limit_s) {
 
 int gb_time_kernel(gb_ctx *ctx, int kernel, gb_fieldvec Y, int reps, double *ms) {
   GB_RANGE();
+  NO_MOIST(ctx, "gb_time_kernel");
   GUARD(ctx);
   if (!fv_ok(Y) || !ms || reps < 0 || kernel < 0 || kernel > GB_K_PASSB_FINAL) return fail(ctx, GB_ERR_ARG, "bad gb_time_kernel arguments");
   return DISPATCH(ctx, time_kernel_t, ctx, kernel, Y, reps, ms);

@@ -162,6 +162,17 @@ bool validate_config(const gb_config &c, const char **why) {
       return false;
     }
   }
+  if (c.moist != 0 && c.moist != 1) { *why = "moist must be 0 or 1"; return false; }
+  if (c.moist) {
+    if (c.z_surface) { *why = "moist 0M is not available over terrain"; return false; }
+    if (c.held_suarez) { *why = "the Held-Suarez forcing is a dry configuration (moist = 0)"; return false; }
+    if (!(c.R_v > 0) || !(c.cp_v > c.R_v) || !(c.cp_l > 0) || !(c.cp_i > 0) || !(c.LH_v0 > 0) ||
+        !(c.LH_s0 > c.LH_v0) || !(c.T_triple > 0) || !(c.press_triple > 0) || !(c.T_freeze > c.T_icenuc) ||
+        !(c.T_icenuc > 0) || !(c.pow_icenuc > 0) || c.sa_iters < 1 || c.sa_iters > 100) {
+      *why = "invalid moist thermodynamic constants or sa_iters";
+      return false;
+    }
+  }
   if ((c.elem_map == nullptr) != (c.elem_orient == nullptr)) {
     *why = "elem_map and elem_orient must both be given or both be NULL";
     return false;

@@ -99,6 +99,7 @@ struct CotArgs {
 enum ColMode { COL_STAGE = 0, COL_IMPLICIT = 1, COL_JACOBIAN = 2, COL_LDIV = 3, COL_POSTIMP = 4 };
 constexpr int JAC_Q = 15;  // stored Jacobian quantities per level
 constexpr int JAC_QT = JAC_Q + 6;  // over terrain: with the (rho, u_h), (rho e_tot, u_h) blocks
+constexpr int JAC_QM = JAC_Q + 4;  // moist 0M: with the (rho q_tot, u_3) and (u_3, rho q_tot) blocks
 
 template <class FT>
 struct ColArgs {

@@ -125,6 +125,7 @@ __device__ __forceinline__ void crpcr_solve2(FT (&a)[2], FT (&b)[2], FT (&c)[2],
 template <class FT, int M>
 struct ColState {
   FT rho[M], u1[M], u2[M], rhoe[M], u3[M];
+  FT rhoq[M];  // moist 0M: rho q_tot
 };
 // Over terrain-following levels (TOPO) also: w3c = g^33 u_3 of the faces (u3c is then the full
 // u^3 = u_h^3 + g^33 u_3), ct3 = CT3(u_h) of the centres, the face's g^33 and the centre's Phi.
@@ -132,6 +133,8 @@ template <class FT, int M>
 struct ColDiag {
   FT c1[M], c2[M], K[M], T[M], h[M], Pi[M], thv[M], thvr[M], phid[M], rJ[M], u3c[M], J[M], iJ[M];
   FT w3c[M], ct3[M], g33[M], phi[M];
+  // moist 0M: q = specific(rho q_tot, rho), kappa_m, dp/d(rho q_tot)
+  FT q[M], km[M], dpq[M];
 };
 
 // The impenetrable filter over terrain on a state held M levels per lane: u_3 = -CT3(u_h) / g^33
@@ -158,7 +161,7 @@ __device__ __forceinline__ void col_filter_topo(const col::ColLevT<FT> &T, ColSt
   (void)Nf;
 }
 
-template <class FT, int M, bool TOPO, class LV>
+template <class FT, int M, bool TOPO, bool MOIST, class LV>
 __device__ __forceinline__ void col_diag(const DevParams<FT> &P, const ColGeo<FT> &G, const LV &T,
                                          const ColState<FT, M> &S, ColDiag<FT, M> &Dg, int lane) {
   const int Nv = P.Nv, Nf = P.Nf;
@@ -206,7 +209,8 @@ __device__ __forceinline__ void col_diag(const DevParams<FT> &P, const ColGeo<FT
       const FT kv = (S.u3[k] * Dg.u3c[k] + u3n[k] * u3cn[k]) / FT(2);
       const FT K = (S.u1[k] * c1 + S.u2[k] * c2 + kv) / FT(2);
       Thermo<FT> th;
-      thermo(P, S.rho[k], S.rhoe[k], K, Phi, P.lr4[v], th);
+      if constexpr (MOIST) thermo_moist(P, S.rho[k], S.rhoe[k], S.rhoq[k], K, Phi, P.lr4[v], th, Dg.q[k], Dg.km[k], Dg.dpq[k]);
+      else thermo(P, S.rho[k], S.rhoe[k], K, Phi, P.lr4[v], th);
       Dg.c1[k] = c1; Dg.c2[k] = c2; Dg.K[k] = K; Dg.T[k] = th.T; Dg.h[k] = th.h; Dg.Pi[k] = th.Pi;
       Dg.thv[k] = th.thv; Dg.thvr[k] = th.thvr; Dg.phid[k] = th.phid;
       Dg.J[k] = G.Jh * r2 * dz;
@@ -231,16 +235,17 @@ __device__ __forceinline__ void col_diag(const DevParams<FT> &P, const ColGeo<FT
   }
 }
 
-// implicit tendency (rho, rho e_tot, u_3) at the owned levels
-template <class FT, int M, bool TOPO, class LV>
+// implicit tendency (rho, rho e_tot, u_3; moist: rho q_tot) at the owned levels
+template <class FT, int M, bool TOPO, bool MOIST, class LV>
 __device__ __forceinline__ void col_implicit(const DevParams<FT> &P, const ColGeo<FT> &G, const LV &Tg,
                                              const ColState<FT, M> &S, const ColDiag<FT, M> &Dg, FT (&Tr)[M],
-                                             FT (&Te)[M], FT (&T3)[M], int lane) {
+                                             FT (&Te)[M], FT (&T3)[M], FT (&Tq)[M], int lane) {
   const int Nv = P.Nv, Nf = P.Nf;
-  FT rJm[M], hm[M], phm[M], Pim[M], thm[M], thrm[M];
+  FT rJm[M], hm[M], phm[M], Pim[M], thm[M], thrm[M], qm[M];
   nb_all<M, -1>(Dg.rJ, rJm); nb_all<M, -1>(Dg.h, hm); nb_all<M, -1>(Dg.phid, phm);
   nb_all<M, -1>(Dg.Pi, Pim); nb_all<M, -1>(Dg.thv, thm); nb_all<M, -1>(Dg.thvr, thrm);
-  FT flux[M], fh[M];
+  if constexpr (MOIST) nb_all<M, -1>(Dg.q, qm);
+  FT flux[M], fh[M], fq[M];
 #pragma unroll
   for (int k = 0; k < M; ++k) {
     const int f = lane * M + k;
@@ -251,6 +256,8 @@ __device__ __forceinline__ void col_implicit(const DevParams<FT> &P, const ColGe
     const FT hb = (hm[k] + Dg.h[k]) / FT(2);
     flux[k] = inner ? F : FT(0);
     fh[k] = inner ? F * hb : FT(0);
+    // central transport of q_tot (implicit_tendency.jl:211-215)
+    if constexpr (MOIST) fq[k] = inner ? F * ((qm[k] + Dg.q[k]) / FT(2)) : FT(0);
     FT val = 0;
     if (inner) {
       // ᶠgradᵥ(Phi) - ᶠgradᵥ(Phi_r) as the difference of Phi - Phi_r between the levels
@@ -263,13 +270,15 @@ __device__ __forceinline__ void col_implicit(const DevParams<FT> &P, const ColGe
     else val -= P.levf[LF_BETA * Nf + fc] * S.u3[k];
     T3[k] = val;
   }
-  FT fln[M], fhn[M];
+  FT fln[M], fhn[M], fqn[M];
   nb_all<M, 1>(flux, fln);
   nb_all<M, 1>(fh, fhn);
+  if constexpr (MOIST) nb_all<M, 1>(fq, fqn);
 #pragma unroll
   for (int k = 0; k < M; ++k) {
     Tr[k] = -((fln[k] - flux[k]) * Dg.iJ[k]);
     Te[k] = -((fhn[k] - fh[k]) * Dg.iJ[k]);
+    Tq[k] = MOIST ? -((fqn[k] - fq[k]) * Dg.iJ[k]) : FT(0);
   }
 }
 
@@ -288,9 +297,16 @@ struct ColJac {
   FT ru0[M], ru1[M], eu0[M], eu1[M];
   FT ur0[M], ur1[M], ue0[M], ue1[M], uh0[M], uh1[M], uh2[M], uh3[M], uu0[M], uu1[M], uu2[M];
   FT wm[M], w0m[M], w0p[M], wp[M], hb0[M], hb1[M];
+  // moist 0M: (rho q_tot, u_3) of centre v for faces v, v+1 and (u_3, rho q_tot) of face k for
+  // centres k-1, k
+  FT qu0[M], qu1[M], uq0[M], uq1[M];
 };
 
-template <class FT, int M, bool TOPO, class LV>
+// Moist 0M (manual_sparse_jacobian.jl:646-685, 770-831): kappa_m of each centre replaces the
+// dry R_d / cv_d, dp/drho gains (R_d - kappa_m cv_d) T, and the (rho q_tot, u_3) and
+// (u_3, rho q_tot) blocks are the (rho e_tot, u_3) block with ᶠinterp(q_tot) and the
+// (u_3, rho e_tot) block with dp/d(rho q_tot).
+template <class FT, int M, bool TOPO, bool MOIST, class LV>
 __device__ __forceinline__ void col_jacobian(const DevParams<FT> &P, const ColGeo<FT> &G, const LV &Tg,
                                              const ColState<FT, M> &S, const ColDiag<FT, M> &Dg, FT dtg,
                                              ColJac<FT, M> &Jc, int lane) {
@@ -306,8 +322,12 @@ __device__ __forceinline__ void col_jacobian(const DevParams<FT> &P, const ColGe
     nb_all<M, -1>(Dg.ct3, ctm);
     nb_all<M, -1>(Dg.phi, phim);
   }
+  FT kmm[M], Tmm[M], dqm[M], qm[M];
+  if constexpr (MOIST) {
+    nb_all<M, -1>(Dg.km, kmm); nb_all<M, -1>(Dg.T, Tmm); nb_all<M, -1>(Dg.dpq, dqm); nb_all<M, -1>(Dg.q, qm);
+  }
   // face quantities needed by centre rows: rJbar*g33 and hbar at faces
-  FT fr[M], fhb[M];
+  FT fr[M], fhb[M], fqb[M];
 #pragma unroll
   for (int k = 0; k < M; ++k) {
     const int f = lane * M + k;
@@ -317,10 +337,12 @@ __device__ __forceinline__ void col_jacobian(const DevParams<FT> &P, const ColGe
     const FT rJ = (rJm[k] + Dg.rJ[k]) / FT(2);
     fr[k] = inner ? rJ * g33 : FT(0);
     fhb[k] = (hm[k] + Dg.h[k]) / FT(2);
+    if constexpr (MOIST) fqb[k] = (qm[k] + Dg.q[k]) / FT(2);
   }
-  FT frn[M], fhbn[M];
+  FT frn[M], fhbn[M], fqbn[M];
   nb_all<M, 1>(fr, frn);
   nb_all<M, 1>(fhb, fhbn);
+  if constexpr (MOIST) nb_all<M, 1>(fqb, fqbn);
 #pragma unroll
   for (int k = 0; k < M; ++k) {
     const FT v0 = fr[k] * Dg.iJ[k], v1 = -frn[k] * Dg.iJ[k];
@@ -328,6 +350,10 @@ __device__ __forceinline__ void col_jacobian(const DevParams<FT> &P, const ColGe
     Jc.ru1[k] = dtg * v1;
     Jc.eu0[k] = dtg * (v0 * fhb[k]);
     Jc.eu1[k] = dtg * (v1 * fhbn[k]);
+    if constexpr (MOIST) {
+      Jc.qu0[k] = dtg * (v0 * fqb[k]);
+      Jc.qu1[k] = dtg * (v1 * fqbn[k]);
+    }
     const int f = lane * M + k;
     const int fc = min(f, Nf - 1);
     const FT beta = TOPO ? Tg.f4(fc).y : P.levf[LF_BETA * Nf + fc];
@@ -337,30 +363,43 @@ __device__ __forceinline__ void col_jacobian(const DevParams<FT> &P, const ColGe
       const FT rbar = (ra + rb) / FT(2);
       const FT irb = grcp(rbar);
       const FT phia = TOPO ? phim[k] : P.levc[LC_PHI * Nv + va], phib = TOPO ? Dg.phi[k] : P.levc[LC_PHI * Nv + f];
-      const FT dpa = kap * (P.T0 * P.cpd - Km[k] - phia);
-      const FT dpb = kap * (P.T0 * P.cpd - Dg.K[k] - phib);
+      // kappa_m of the centres below (a) and above (b) the face: R_d / cv_d for dry air
+      const FT ka = MOIST ? kmm[k] : kap, kb = MOIST ? Dg.km[k] : kap;
+      FT dpa = ka * (P.T0 * P.cpd - Km[k] - phia);
+      FT dpb = kb * (P.T0 * P.cpd - Dg.K[k] - phib);
+      if constexpr (MOIST) {
+        dpa += (P.Rd - ka * P.cvd) * Tmm[k];
+        dpb += (P.Rd - kb * P.cvd) * Dg.T[k];
+        Jc.uq0[k] = dtg * (dqm[k] * irb);
+        Jc.uq1[k] = dtg * (-Dg.dpq[k] * irb);
+      }
       const FT thvb = (thm[k] + Dg.thv[k]) / FT(2);
       const FT gPi = Dg.Pi[k] - Pim[k];
       const FT buoy = P.cpd * thvb * gPi * irb;
       Jc.ur0[k] = dtg * (dpa * irb + buoy / FT(2));
       Jc.ur1[k] = dtg * (-dpb * irb + buoy / FT(2));
-      Jc.ue0[k] = dtg * (kap * irb);
-      Jc.ue1[k] = dtg * (-kap * irb);
-      Jc.uh0[k] = dtg * (-kap * ra * irb) * c1m[k];
-      Jc.uh1[k] = dtg * (-kap * ra * irb) * c2m[k];
-      Jc.uh2[k] = dtg * (kap * rb * irb) * Dg.c1[k];
-      Jc.uh3[k] = dtg * (kap * rb * irb) * Dg.c2[k];
+      Jc.ue0[k] = dtg * (ka * irb);
+      Jc.ue1[k] = dtg * (-kb * irb);
+      Jc.uh0[k] = dtg * (-ka * ra * irb) * c1m[k];
+      Jc.uh1[k] = dtg * (-ka * ra * irb) * c2m[k];
+      Jc.uh2[k] = dtg * (kb * rb * irb) * Dg.c1[k];
+      Jc.uh3[k] = dtg * (kb * rb * irb) * Dg.c2[k];
       if constexpr (TOPO) {
         // dK_v/du_3,f = (g^33 u_3)_f / 2 + CT3(u_h)_v / 2 (manual_sparse_jacobian.jl:754-756)
         Jc.uu0[k] = dtg * (-kap * ra * (u3cm[k] + ctm[k]) * (irb / FT(2)));
         Jc.uu1[k] = dtg * (kap * (rb * (Dg.w3c[k] + Dg.ct3[k]) - ra * (Dg.w3c[k] + ctm[k])) * (irb / FT(2)) - beta) - FT(1);
         Jc.uu2[k] = dtg * (kap * rb * (u3cp[k] + Dg.ct3[k]) * (irb / FT(2)));
+      } else if constexpr (MOIST) {
+        Jc.uu0[k] = dtg * (-ka * ra * u3cm[k] * (irb / FT(2)));
+        Jc.uu1[k] = dtg * ((kb * rb - ka * ra) * Dg.u3c[k] * (irb / FT(2)) - beta) - FT(1);
+        Jc.uu2[k] = dtg * (kb * rb * u3cp[k] * (irb / FT(2)));
       } else {
         Jc.uu0[k] = dtg * (-kap * ra * u3cm[k] * (irb / FT(2)));
         Jc.uu1[k] = dtg * (kap * (rb - ra) * Dg.u3c[k] * (irb / FT(2)) - beta) - FT(1);
         Jc.uu2[k] = dtg * (kap * rb * u3cp[k] * (irb / FT(2)));
       }
     } else {
+      if constexpr (MOIST) Jc.uq0[k] = Jc.uq1[k] = FT(0);
       Jc.ur0[k] = Jc.ur1[k] = Jc.ue0[k] = Jc.ue1[k] = FT(0);
       Jc.uh0[k] = Jc.uh1[k] = Jc.uh2[k] = Jc.uh3[k] = FT(0);
       Jc.uu0[k] = Jc.uu2[k] = FT(0);
@@ -386,12 +425,15 @@ __device__ __forceinline__ void col_jacobian(const DevParams<FT> &P, const ColGe
   }
 }
 
-// Solve W dY = R with the Schur complement onto u_3.
-template <class FT, int M, bool TOPO, class LV>
+// Solve W dY = R with the Schur complement onto u_3.  Moist 0M: the rho q_tot row is a third
+// scalar row with a -I diagonal block, as rho and rho e_tot (the reference's
+// ApproximateBlockArrowheadIterativeSolve, manual_sparse_jacobian.jl:539-584, is then exact in
+// its first preconditioner application).
+template <class FT, int M, bool TOPO, bool MOIST, class LV>
 __device__ __forceinline__ void col_ldiv(const DevParams<FT> &P, const LV &Tg, const ColJac<FT, M> &Jc,
-                                         const FT (&Rr0)[M], const FT (&Re0)[M], const FT (&Ru1)[M],
-                                         const FT (&Ru2)[M], const FT (&R3)[M], FT (&Xr)[M], FT (&Xe)[M],
-                                         FT (&X3)[M], int lane) {
+                                         const FT (&Rr0)[M], const FT (&Re0)[M], const FT (&Rq)[M],
+                                         const FT (&Ru1)[M], const FT (&Ru2)[M], const FT (&R3)[M], FT (&Xr)[M],
+                                         FT (&Xe)[M], FT (&Xq)[M], FT (&X3)[M], int lane) {
   const int Nv = P.Nv, Nf = P.Nf;
   // over terrain the (rho, u_h), (rho e_tot, u_h) blocks times Δu_h = -R_u_h move to the right-hand
   // sides of the scalar rows: R_x + M_x,uh R_uh
@@ -423,6 +465,10 @@ __device__ __forceinline__ void col_ldiv(const DevParams<FT> &P, const LV &Tg, c
   FT ru0m[M], ru1m[M], eu0m[M], eu1m[M], Rrm[M], Rem[M], Ru1m[M], Ru2m[M];
   nb_all<M, -1>(Jc.ru0, ru0m); nb_all<M, -1>(Jc.ru1, ru1m); nb_all<M, -1>(Jc.eu0, eu0m); nb_all<M, -1>(Jc.eu1, eu1m);
   nb_all<M, -1>(Rr, Rrm); nb_all<M, -1>(Re, Rem); nb_all<M, -1>(Ru1, Ru1m); nb_all<M, -1>(Ru2, Ru2m);
+  FT qu0m[M], qu1m[M], Rqm[M];
+  if constexpr (MOIST) {
+    nb_all<M, -1>(Jc.qu0, qu0m); nb_all<M, -1>(Jc.qu1, qu1m); nb_all<M, -1>(Rq, Rqm);
+  }
   FT a[M], b[M], c[M], d[M], x[M];
 #pragma unroll
   for (int k = 0; k < M; ++k) {
@@ -435,6 +481,12 @@ __device__ __forceinline__ void col_ldiv(const DevParams<FT> &P, const LV &Tg, c
       bb += cr * ru1m[k] + ce * eu1m[k];
       rhs += cr * Rrm[k] + ce * Rem[k];
       rhs += Jc.uh0[k] * Ru1m[k] + Jc.uh1[k] * Ru2m[k];
+      if constexpr (MOIST) {
+        const FT cq = Jc.uq0[k];
+        aa += cq * qu0m[k];
+        bb += cq * qu1m[k];
+        rhs += cq * Rqm[k];
+      }
     }
     if (f < Nv) {  // centre f (slot s = 1)
       const FT cr = Jc.ur1[k], ce = Jc.ue1[k];
@@ -442,6 +494,12 @@ __device__ __forceinline__ void col_ldiv(const DevParams<FT> &P, const LV &Tg, c
       cc += cr * Jc.ru1[k] + ce * Jc.eu1[k];
       rhs += cr * Rr[k] + ce * Re[k];
       rhs += Jc.uh2[k] * Ru1[k] + Jc.uh3[k] * Ru2[k];
+      if constexpr (MOIST) {
+        const FT cq = Jc.uq1[k];
+        bb += cq * Jc.qu0[k];
+        cc += cq * Jc.qu1[k];
+        rhs += cq * Rq[k];
+      }
     }
     if (f >= Nf) { aa = FT(0); bb = FT(1); cc = FT(0); rhs = FT(0); }
     a[k] = aa; b[k] = bb; c[k] = cc; d[k] = rhs;
@@ -455,6 +513,7 @@ __device__ __forceinline__ void col_ldiv(const DevParams<FT> &P, const LV &Tg, c
     X3[k] = x[k];
     Xr[k] = Jc.ru0[k] * x[k] + Jc.ru1[k] * xn[k] - Rr[k];
     Xe[k] = Jc.eu0[k] * x[k] + Jc.eu1[k] * xn[k] - Re[k];
+    Xq[k] = MOIST ? Jc.qu0[k] * x[k] + Jc.qu1[k] * xn[k] - Rq[k] : FT(0);
   }
 }
 
@@ -480,12 +539,13 @@ __device__ __forceinline__ FT vanleer(FT u, FT am2, FT am1, FT a0, FT ap1, bool 
   }
 }
 
+// a: the transported specific quantity of the centres (h_tot for rho e_tot, q_tot for rho q_tot)
 template <class FT, int M>
 __device__ __forceinline__ void col_correction(const DevParams<FT> &P, const ColGeo<FT> &G, const ColDiag<FT, M> &Dg,
-                                               FT (&corr)[M], int lane) {
+                                               const FT (&a)[M], FT (&corr)[M], int lane) {
   const int Nv = P.Nv, Nf = P.Nf;
   FT hm1[M], hm2[M], hp1[M], rJm[M];
-  nb_all<M, -1>(Dg.h, hm1); nb_all<M, -2>(Dg.h, hm2); nb_all<M, 1>(Dg.h, hp1);
+  nb_all<M, -1>(a, hm1); nb_all<M, -2>(a, hm2); nb_all<M, 1>(a, hp1);
   nb_all<M, -1>(Dg.rJ, rJm);
   FT fup[M], fcen[M];
 #pragma unroll
@@ -495,9 +555,9 @@ __device__ __forceinline__ void col_correction(const DevParams<FT> &P, const Col
     const FT rJ = (rJm[k] + Dg.rJ[k]) / FT(2);
     const FT u = Dg.u3c[k];
     const bool near = f == 1 || f == Nv - 1;
-    const FT vl = vanleer(u, hm2[k], hm1[k], Dg.h[k], hp1[k], near, P.dt_model);
+    const FT vl = vanleer(u, hm2[k], hm1[k], a[k], hp1[k], near, P.dt_model);
     fup[k] = inner ? rJ * vl : FT(0);
-    fcen[k] = inner ? rJ * (u * (hm1[k] + Dg.h[k]) / FT(2)) : FT(0);
+    fcen[k] = inner ? rJ * (u * (hm1[k] + a[k]) / FT(2)) : FT(0);
   }
   FT fupn[M], fcn[M];
   nb_all<M, 1>(fup, fupn);
@@ -510,14 +570,18 @@ __device__ __forceinline__ void col_correction(const DevParams<FT> &P, const Col
   }
 }
 
-template <class FT>
-__device__ __forceinline__ size_t cidx(int e, int c, int n, int v, int Nv) { return (((size_t)e * 4 + c) * NN + n) * Nv + v; }
+// centre block [e][NFC][16][Nv]: NFC = 4 (rho, u_1, u_2, rho e_tot), 5 with rho q_tot
+template <class FT, int NFC = 4>
+__device__ __forceinline__ size_t cidx(int e, int c, int n, int v, int Nv) { return (((size_t)e * NFC + c) * NN + n) * Nv + v; }
 template <class FT>
 __device__ __forceinline__ size_t ridx(int e, int c, int n, int v, int Nv) { return (((size_t)e * 2 + c) * NN + n) * Nv + v; }
 
-// Individual hooks: implicit tendency, Jacobian, ldiv, post-Newton correction.
-template <class FT, int M, int MODE, bool TOPO>
+// Individual hooks: implicit tendency, Jacobian, ldiv, post-Newton correction.  MOIST: the
+// centre block carries rho q_tot as its fifth component (never with TOPO).
+template <class FT, int M, int MODE, bool TOPO, bool MOIST>
 __global__ void __launch_bounds__(COL_THREADS) k_col_hook(DevParams<FT> P, ColArgs<FT> A) {
+  static_assert(!(TOPO && MOIST), "moist 0M is not built over terrain");
+  constexpr int NFC = MOIST ? 5 : 4;
   const int lane = threadIdx.x & 31;
   const int col = blockIdx.x * (COL_THREADS / 32) + (threadIdx.x >> 5);
   const int ncols = P.Nh * NN;
@@ -525,7 +589,7 @@ __global__ void __launch_bounds__(COL_THREADS) k_col_hook(DevParams<FT> P, ColAr
   const int e = col >> 4, n = col & 15, Nv = P.Nv, Nf = P.Nf;
   ColGeo<FT> G;
   G.load(P, e, n);
-  constexpr int NQJ = TOPO ? JAC_QT : JAC_Q;
+  constexpr int NQJ = TOPO ? JAC_QT : (MOIST ? JAC_QM : JAC_Q);
   using LV = std::conditional_t<TOPO, col::ColLevT<FT>, col::ColLev<FT>>;
   LV Tg;
   if constexpr (TOPO) Tg.load(P, e, n);
@@ -535,10 +599,11 @@ __global__ void __launch_bounds__(COL_THREADS) k_col_hook(DevParams<FT> P, ColAr
   for (int k = 0; k < M; ++k) {
     const int v = lane * M + k;
     const bool cv = v < Nv, fv = v < Nf;
-    S.rho[k] = cv ? A.Y_c[cidx<FT>(e, 0, n, v, Nv)] : (MODE == COL_LDIV ? FT(0) : FT(1));
-    S.u1[k] = cv ? A.Y_c[cidx<FT>(e, 1, n, v, Nv)] : FT(0);
-    S.u2[k] = cv ? A.Y_c[cidx<FT>(e, 2, n, v, Nv)] : FT(0);
-    S.rhoe[k] = cv ? A.Y_c[cidx<FT>(e, 3, n, v, Nv)] : (MODE == COL_LDIV ? FT(0) : FT(1));
+    S.rho[k] = cv ? A.Y_c[cidx<FT, NFC>(e, 0, n, v, Nv)] : (MODE == COL_LDIV ? FT(0) : FT(1));
+    S.u1[k] = cv ? A.Y_c[cidx<FT, NFC>(e, 1, n, v, Nv)] : FT(0);
+    S.u2[k] = cv ? A.Y_c[cidx<FT, NFC>(e, 2, n, v, Nv)] : FT(0);
+    S.rhoe[k] = cv ? A.Y_c[cidx<FT, NFC>(e, 3, n, v, Nv)] : (MODE == COL_LDIV ? FT(0) : FT(1));
+    S.rhoq[k] = MOIST && cv ? A.Y_c[cidx<FT, NFC>(e, 4, n, v, Nv)] : FT(0);
     S.u3[k] = fv ? A.Y_f[((size_t)e * NN + n) * Nf + v] : FT(0);
     if (!TOPO && MODE != COL_LDIV && (v == 0 || v >= Nv)) S.u3[k] = FT(0);  // impenetrable filter
   }
@@ -546,7 +611,7 @@ __global__ void __launch_bounds__(COL_THREADS) k_col_hook(DevParams<FT> P, ColAr
     if (MODE != COL_LDIV) col_filter_topo<FT, M>(Tg, S, lane);  // -u_h^3 / g^33 on the boundary faces
   }
   FT *jac = A.jac + (size_t)col * NQJ * Nf;
-  FT o0[M], o1[M], o2[M], o3[M], o4[M];
+  FT o0[M], o1[M], o2[M], o3[M], o4[M], o5[M];
   if constexpr (MODE == COL_LDIV) {
     ColJac<FT, M> Jc;
 #pragma unroll
@@ -555,34 +620,39 @@ __global__ void __launch_bounds__(COL_THREADS) k_col_hook(DevParams<FT> P, ColAr
       const int fc = min(f, Nf - 1);
       FT *q[JAC_QT] = {Jc.ru0, Jc.ru1, Jc.eu0, Jc.eu1, Jc.ur0, Jc.ur1, Jc.ue0, Jc.ue1,
                        Jc.uh0, Jc.uh1, Jc.uh2, Jc.uh3, Jc.uu0, Jc.uu1, Jc.uu2,
-                       Jc.wm, Jc.w0m, Jc.w0p, Jc.wp, Jc.hb0, Jc.hb1};
+                       TOPO ? Jc.wm : Jc.qu0, TOPO ? Jc.w0m : Jc.qu1, TOPO ? Jc.w0p : Jc.uq0, TOPO ? Jc.wp : Jc.uq1,
+                       Jc.hb0, Jc.hb1};
       for (int t = 0; t < NQJ; ++t) q[t][k] = jac[t * Nf + fc];
       if (f >= Nf) {
         for (int t = 0; t < NQJ; ++t) q[t][k] = FT(0);
         Jc.uu1[k] = FT(1);
       }
     }
-    col_ldiv<FT, M, TOPO>(P, Tg, Jc, S.rho, S.rhoe, S.u1, S.u2, S.u3, o0, o3, o4, lane);
+    col_ldiv<FT, M, TOPO, MOIST>(P, Tg, Jc, S.rho, S.rhoe, S.rhoq, S.u1, S.u2, S.u3, o0, o3, o5, o4, lane);
 #pragma unroll
     for (int k = 0; k < M; ++k) { o1[k] = -S.u1[k]; o2[k] = -S.u2[k]; }
   } else {
     ColDiag<FT, M> Dg;
-    col_diag<FT, M, TOPO>(P, G, Tg, S, Dg, lane);
+    col_diag<FT, M, TOPO, MOIST>(P, G, Tg, S, Dg, lane);
     if constexpr (MODE == COL_IMPLICIT) {
-      col_implicit<FT, M, TOPO>(P, G, Tg, S, Dg, o0, o3, o4, lane);
+      col_implicit<FT, M, TOPO, MOIST>(P, G, Tg, S, Dg, o0, o3, o4, o5, lane);
 #pragma unroll
       for (int k = 0; k < M; ++k) { o1[k] = FT(0); o2[k] = FT(0); }
     } else if constexpr (MODE == COL_POSTIMP) {
-      FT corr[M];
-      if (P.upwinding) col_correction<FT, M>(P, G, Dg, corr, lane);
+      FT corr[M], corq[M];
+      if (P.upwinding) {
+        col_correction<FT, M>(P, G, Dg, Dg.h, corr, lane);
+        if constexpr (MOIST) col_correction<FT, M>(P, G, Dg, Dg.q, corq, lane);
+      }
 #pragma unroll
       for (int k = 0; k < M; ++k) {
         o0[k] = o1[k] = o2[k] = o4[k] = FT(0);
         o3[k] = P.upwinding ? corr[k] : FT(0);
+        o5[k] = MOIST && P.upwinding ? corq[k] : FT(0);
       }
     } else {  // COL_JACOBIAN
       ColJac<FT, M> Jc;
-      col_jacobian<FT, M, TOPO>(P, G, Tg, S, Dg, A.dtg, Jc, lane);
+      col_jacobian<FT, M, TOPO, MOIST>(P, G, Tg, S, Dg, A.dtg, Jc, lane);
 #pragma unroll
       for (int k = 0; k < M; ++k) {
         const int f = lane * M + k;
@@ -592,6 +662,11 @@ __global__ void __launch_bounds__(COL_THREADS) k_col_hook(DevParams<FT> P, ColAr
                                   Jc.ue1[k], Jc.uh0[k], Jc.uh1[k], Jc.uh2[k], Jc.uh3[k], Jc.uu0[k], Jc.uu1[k],
                                   Jc.uu2[k], Jc.wm[k], Jc.w0m[k], Jc.w0p[k], Jc.wp[k], Jc.hb0[k], Jc.hb1[k]};
             for (int t = 0; t < JAC_QT; ++t) jac[t * Nf + f] = q[t];
+          } else if constexpr (MOIST) {
+            const FT q[JAC_QM] = {Jc.ru0[k], Jc.ru1[k], Jc.eu0[k], Jc.eu1[k], Jc.ur0[k], Jc.ur1[k], Jc.ue0[k],
+                                  Jc.ue1[k], Jc.uh0[k], Jc.uh1[k], Jc.uh2[k], Jc.uh3[k], Jc.uu0[k], Jc.uu1[k],
+                                  Jc.uu2[k], Jc.qu0[k], Jc.qu1[k], Jc.uq0[k], Jc.uq1[k]};
+            for (int t = 0; t < JAC_QM; ++t) jac[t * Nf + f] = q[t];
           } else {
             const FT q[JAC_Q] = {Jc.ru0[k], Jc.ru1[k], Jc.eu0[k], Jc.eu1[k], Jc.ur0[k], Jc.ur1[k], Jc.ue0[k], Jc.ue1[k],
                                  Jc.uh0[k], Jc.uh1[k], Jc.uh2[k], Jc.uh3[k], Jc.uu0[k], Jc.uu1[k], Jc.uu2[k]};
@@ -606,10 +681,11 @@ __global__ void __launch_bounds__(COL_THREADS) k_col_hook(DevParams<FT> P, ColAr
   for (int k = 0; k < M; ++k) {
     const int v = lane * M + k;
     if (v < Nv) {
-      A.O_c[cidx<FT>(e, 0, n, v, Nv)] = o0[k];
-      A.O_c[cidx<FT>(e, 1, n, v, Nv)] = o1[k];
-      A.O_c[cidx<FT>(e, 2, n, v, Nv)] = o2[k];
-      A.O_c[cidx<FT>(e, 3, n, v, Nv)] = o3[k];
+      A.O_c[cidx<FT, NFC>(e, 0, n, v, Nv)] = o0[k];
+      A.O_c[cidx<FT, NFC>(e, 1, n, v, Nv)] = o1[k];
+      A.O_c[cidx<FT, NFC>(e, 2, n, v, Nv)] = o2[k];
+      A.O_c[cidx<FT, NFC>(e, 3, n, v, Nv)] = o3[k];
+      if constexpr (MOIST) A.O_c[cidx<FT, NFC>(e, 4, n, v, Nv)] = o5[k];
     }
     if (v < Nf) A.O_f[((size_t)e * NN + n) * Nf + v] = o4[k];
   }
@@ -619,19 +695,20 @@ inline int levels_per_lane(int Nf) { return Nf <= 32 ? 1 : (Nf <= 64 ? 2 : 4); }
 
 }  // namespace
 
-template <class FT, int M, bool TOPO>
+template <class FT, int M, bool TOPO, bool MOIST>
 void launch_hook_mt(const DevParams<FT> &P, int mode, const ColArgs<FT> &A, int grid, cudaStream_t s) {
   switch (mode) {
-    case COL_IMPLICIT: k_col_hook<FT, M, COL_IMPLICIT, TOPO><<<grid, COL_THREADS, 0, s>>>(P, A); break;
-    case COL_JACOBIAN: k_col_hook<FT, M, COL_JACOBIAN, TOPO><<<grid, COL_THREADS, 0, s>>>(P, A); break;
-    case COL_LDIV: k_col_hook<FT, M, COL_LDIV, TOPO><<<grid, COL_THREADS, 0, s>>>(P, A); break;
-    default: k_col_hook<FT, M, COL_POSTIMP, TOPO><<<grid, COL_THREADS, 0, s>>>(P, A); break;
+    case COL_IMPLICIT: k_col_hook<FT, M, COL_IMPLICIT, TOPO, MOIST><<<grid, COL_THREADS, 0, s>>>(P, A); break;
+    case COL_JACOBIAN: k_col_hook<FT, M, COL_JACOBIAN, TOPO, MOIST><<<grid, COL_THREADS, 0, s>>>(P, A); break;
+    case COL_LDIV: k_col_hook<FT, M, COL_LDIV, TOPO, MOIST><<<grid, COL_THREADS, 0, s>>>(P, A); break;
+    default: k_col_hook<FT, M, COL_POSTIMP, TOPO, MOIST><<<grid, COL_THREADS, 0, s>>>(P, A); break;
   }
 }
 template <class FT, int M>
 void launch_hook_m(const DevParams<FT> &P, int mode, const ColArgs<FT> &A, int grid, cudaStream_t s) {
-  if (P.topo) launch_hook_mt<FT, M, true>(P, mode, A, grid, s);
-  else launch_hook_mt<FT, M, false>(P, mode, A, grid, s);
+  if (P.topo) launch_hook_mt<FT, M, true, false>(P, mode, A, grid, s);
+  else if (P.moist) launch_hook_mt<FT, M, false, true>(P, mode, A, grid, s);
+  else launch_hook_mt<FT, M, false, false>(P, mode, A, grid, s);
 }
 
 template <class FT>

@@ -45,7 +45,10 @@ class GBConfig(ctypes.Structure):
                     ("elem_map", ctypes.POINTER(_c_int)), ("elem_orient", ctypes.POINTER(_c_int)),
                     ("test_dycore_consistency", _c_int),
                     ("z_surface", ctypes.POINTER(_c_double)), ("warp", _c_int),
-                    ("sleve_eta", _c_double), ("sleve_s", _c_double)]
+                    ("sleve_eta", _c_double), ("sleve_s", _c_double),
+                    ("moist", _c_int)] + [(n, _c_double) for n in (
+                    "R_v", "cp_v", "cp_l", "cp_i", "LH_v0", "LH_s0", "T_triple", "press_triple", "T_freeze",
+                    "T_icenuc", "pow_icenuc")] + [("sa_iters", _c_int)]
 
 
 class GBFieldVec(ctypes.Structure):
@@ -160,6 +163,10 @@ def make_config(cfg):
         keep.append(z)
     c.warp = 1 if getattr(cfg, "warp", "linear") == "sleve" else 0
     c.sleve_eta, c.sleve_s = float(getattr(cfg, "sleve_eta", 0.7)), float(getattr(cfg, "sleve_s", 10.0))
+    c.moist = 1 if getattr(cfg, "moist", False) else 0
+    for k, v in getattr(cfg, "moist_constants", {}).items():
+        setattr(c, k, float(v))
+    c.sa_iters = int(getattr(cfg, "sa_iters", 16))
     c._keep = tuple(keep)   # the arrays live as long as the struct
     return c
 

@@ -41,6 +41,23 @@ HELD_SUAREZ = dict(
     MSLP=101325.0,
 )
 
+# Moist thermodynamic constants of the 0M microphysics (EquilibriumMicrophysics0M): the
+# ClimaParams defaults under their Thermodynamics.jl names; R_v = R / M_w with the gas constant
+# 8.3144598 J/(mol K) and the molar mass of water 0.01801528 kg/mol.
+MOIST = dict(
+    R_v=8.3144598 / 0.01801528,
+    cp_v=1859.0,
+    cp_l=4181.0,
+    cp_i=2100.0,
+    LH_v0=2.5008e6,
+    LH_s0=2.8344e6,
+    T_triple=273.16,
+    press_triple=611.657,
+    T_freeze=273.15,
+    T_icenuc=233.0,
+    pow_icenuc=1.0,
+)
+
 SECONDS_PER_YEAR = 3.1536e7  # 365-day year, as in simulated_years_per_day (src/simulation/solve.jl:40-45)
 
 
@@ -93,6 +110,11 @@ class DycoreConfig:
     warp: str = "linear"
     sleve_eta: float = 0.7
     sleve_s: float = 10.0
+    # moist 0M (microphysics_model: 0M, EquilibriumMicrophysics0M): rho q_tot is the fifth centre
+    # component; the column hooks only.  sa_iters: Newton iterations of the saturation adjustment
+    moist: bool = False
+    moist_constants: dict = field(default_factory=lambda: dict(MOIST))
+    sa_iters: int = 16
 
     def __post_init__(self):
         if self.nu is None:
@@ -113,6 +135,8 @@ class DycoreConfig:
                  upwinding=1 if self.upwinding == "vanleer" else 0, dss_stage1=1 if dss_stage1 else 0,
                  held_suarez=1 if self.held_suarez else 0)
         p.update({"hs_" + k: v for k, v in self.hs.items()})
+        p.update(self.moist_constants)
+        p.update(moist=1 if self.moist else 0, sa_iters=self.sa_iters)
         return p
 
 

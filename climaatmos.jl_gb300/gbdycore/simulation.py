@@ -60,7 +60,8 @@ class Geometry:
         _check(None, L.gb_geometry_export(ctypes.byref(c), ctypes.byref(g)))
         self.zc = 0.5 * (self.zf[1:] + self.zf[:-1])
         self.n_center, self.n_face = nc.value, nf.value
-        assert H * 4 * self.Nv == self.n_center
+        self.nfc = 5 if getattr(cfg, "moist", False) else 4   # centre components (5: with rho q_tot)
+        assert H * self.nfc * self.Nv == self.n_center
         self.terrain = None
         if getattr(cfg, "z_surface", None) is not None:
             self.terrain = {"zc": terrain_centre_heights(cfg, self.zf)}
@@ -97,7 +98,8 @@ def _check(ctx, rc):
 
 
 class FieldVector:
-    """Device state: ``c`` [Nh,4,16,Nv] (rho, u_1, u_2, rho e_tot), ``f`` [Nh,16,Nv+1] (u_3)."""
+    """Device state: ``c`` [Nh,4,16,Nv] (rho, u_1, u_2, rho e_tot; moist 0M: [Nh,5,16,Nv] with
+    rho q_tot last), ``f`` [Nh,16,Nv+1] (u_3)."""
 
     def __init__(self, c, f):
         self.c, self.f = c, f

@@ -95,6 +95,26 @@ typedef struct {
   const double *z_surface;
   int warp;
   double sleve_eta, sleve_s;
+  /* Moist 0M (microphysics_model: EquilibriumMicrophysics0M): moist = 1 adds the prognostic
+     rho q_tot as a fifth centre component, so the centre block is [Nh][5][16][Nv] with
+     rho q_tot last (ClimaCore's Y.c field order rho, u_h, rho e_tot, rho q_tot).  The
+     precomputed temperature then comes from the saturation adjustment of (rho, e_int,
+     max(0, q_tot)) (precomputed_quantities.jl:734-747), the pressure is rho R_m T and
+     theta_v = T R_m / (Pi R_d); the implicit tendency transports q_tot centrally
+     (implicit_tendency.jl:211-215); gb_update_jacobian forms kappa_m = R_m / cv_m and the
+     (u_3, rho q_tot) and (rho q_tot, u_3) blocks (manual_sparse_jacobian.jl:646-685, 770-831),
+     and gb_ldiv solves the Schur complement onto u_3 with the rho q_tot row (the reference's
+     ApproximateBlockArrowheadIterativeSolve, exact here because with 0M and no diffusion the
+     scalar blocks are -I); gb_correct_implicit_advection_tendency corrects rho q_tot as well.
+     The moist thermodynamic constants carry the Thermodynamics.jl parameter names (the
+     liquid fraction ramps from 0 at T_icenuc to 1 at T_freeze with exponent pow_icenuc);
+     sa_iters (>= 1) Newton iterations solve the saturation adjustment.  A moist context
+     supports gb_set_precomputed_quantities, gb_implicit_tendency, gb_update_jacobian,
+     gb_ldiv and gb_correct_implicit_advection_tendency; every other state entry point returns
+     GB_ERR_ARG, as does moist = 1 with a surface or the Held-Suarez forcing. */
+  int moist;
+  double R_v, cp_v, cp_l, cp_i, LH_v0, LH_s0, T_triple, press_triple, T_freeze, T_icenuc, pow_icenuc;
+  int sa_iters;
 } gb_config;
 
 typedef struct {

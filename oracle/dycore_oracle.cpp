@@ -56,6 +56,12 @@ struct OracleParams {
   int dss_stage1;   // 1: DSS the first stage as well (ClimaTimeSteppers does)
   int held_suarez;  // 1: Held-Suarez forcing in the remaining tendency
   double hs_day, hs_sigma_b, hs_dT_y, hs_T_equator, hs_dtheta_z, hs_T_min, hs_p_ref_theta, hs_MSLP;
+  // Moist 0M (EquilibriumMicrophysics0M): moist = 1 adds the centre component rho q_tot (comp 4)
+  // to the column operators; the moist thermodynamic constants (Thermodynamics.jl names) and the
+  // Newton iterations of the saturation adjustment
+  int moist;
+  double R_v, cp_v, cp_l, cp_i, LH_v0, LH_s0, T_triple, press_triple, T_freeze, T_icenuc, pow_icenuc;
+  int sa_iters;
 };
 struct OracleGeom {
   int Nh, Nv, ngroups;
@@ -84,6 +90,12 @@ struct Oracle {
   FT nu_v, nu_s, div_damp, zd, a_uh, a_w, zmax, dt_model, kappa;
   int upwinding, dss_stage1;
   int hs = 0;  // Held-Suarez forcing
+  // moist 0M: centre components per element (4 dry, 5 with rho q_tot) and the moist constants:
+  // cv of vapour, liquid and ice, latent heats at T_0, the triple point, the freezing and
+  // homogeneous-nucleation temperatures of the liquid fraction, e_int_v0 = L_v0 - R_v T_0,
+  // e_int_i0 = L_s0 - L_v0
+  int moist = 0, nfc = 4, sa_iters = 0;
+  FT Rv, cvv, cvl, cvi, cpv, cpl, cpi, Lv0, Ls0, Ttr, ptr, Tfrz, Tice, pice, ev0, ei0;
   FT hs_day, hs_sb, hs_dTy, hs_Teq, hs_dthz, hs_Tmin, hs_p0, hs_MSLP;
   // geometry
   FT W[NN], D[NQ][NQ];
@@ -95,10 +107,10 @@ struct Oracle {
   int topo = 0;
   std::vector<FT> tzc, tzf, tJc, tJf, tguc, tguf, tgdc, tf3c, tf12f, tEcc, tEcn;
 
-  size_t ncen() const { return (size_t)Nh * 4 * NN * Nv; }
+  size_t ncen() const { return (size_t)Nh * nfc * NN * Nv; }
   size_t nfac() const { return (size_t)Nh * NN * Nf; }
   size_t npt() const { return (size_t)Nh * NN * Nv; }
-  size_t ci(int e, int c, int n, int v) const { return (((size_t)e * 4 + c) * NN + n) * Nv + v; }
+  size_t ci(int e, int c, int n, int v) const { return (((size_t)e * nfc + c) * NN + n) * Nv + v; }
   size_t fi(int e, int n, int k) const { return ((size_t)e * NN + n) * Nf + k; }
   size_t pi(int e, int n, int v) const { return ((size_t)e * NN + n) * Nv + v; }
   size_t hn(int e, int n) const { return (size_t)e * NN + n; }
@@ -133,7 +145,82 @@ struct Oracle {
     std::vector<FT> ub3, K, T, p, h, Pi, thv, thvr, phir, uc1, uc2, u3c;  // u3c = contravariant u^3 at faces
     // ct3 = CT3(u_h) = g^31 u_1 + g^32 u_2 at centres (0 over a flat surface); w3c = g^33 u_3 at faces
     std::vector<FT> ct3, w3c;
+    // moist: q = specific(rho q_tot, rho); kapm = R_m / cv_m; dpdq = dp/d(rho q_tot) at constant
+    // rho and rho e_tot
+    std::vector<FT> q, kapm, dpdq;
   } pre;
+
+  // ---- moist thermodynamics (EquilibriumMicrophysics0M) ----
+  // Restated from the published formulation of Thermodynamics.jl 1.3.0 (not vendored here; parity
+  // with it is unpinned), as the reference's Jacobian assumes it (manual_sparse_jacobian.jl:646-684:
+  // its dp/drho and dp/d(rho q_tot) follow from these definitions):
+  //   cv_m  = cv_d + (cv_v - cv_d) q_t + (cv_l - cv_v) q_l + (cv_i - cv_v) q_i
+  //   R_m   = R_d (1 - q_t) + R_v (q_t - q_l - q_i)
+  //   e_int = cv_m (T - T_0) + q_v e_int_v0 - q_i e_int_i0 - (1 - q_t) R_d T_0
+  //   p_v*(T) = p_tr (T / T_tr)^(dcp / R_v) exp((L_0 - dcp T_0) / R_v (1 / T_tr - 1 / T)),
+  //     L_0 = lam L_v0 + (1 - lam) L_s0, dcp = lam (cp_v - cp_l) + (1 - lam) (cp_v - cp_i)
+  //   q_v* = p_v* / (rho R_v T)
+  //   lam(T) = 1 above T_freeze, 0 below T_icenuc, ((T - T_icenuc) / (T_freeze - T_icenuc))^pow between
+  // The saturation adjustment (precomputed_quantities.jl:734-747, TD.saturation_adjustment with
+  // TD.ρe()): the all-vapour temperature T_u if the point is unsaturated there, else sa_iters
+  // safeguarded Newton iterations on f(T) = e_int(T) - e_int with the saturated partition
+  // q_c = q_t - q_v*(T) split by lam(T), continued smoothly (q_c < 0) where q_v* > q_t: the
+  // clamped function's kink there makes plain Newton cycle between T_u and an unsaturated
+  // iterate.  f increases with T, f(T_u) < 0 and f(T_b) > 0 at
+  // T_b = max(T_u + q_t (e_int_v0 + e_int_i0) / cv_d, T_0) + 1; a Newton step outside the
+  // current bracket is replaced by bisection.  The partition returned is that of the final T.
+  FT liq_frac(FT T, FT &dl) const {
+    if (T > Tfrz) { dl = FT(0); return FT(1); }
+    if (!(T > Tice)) { dl = FT(0); return FT(0); }
+    const FT x = (T - Tice) / (Tfrz - Tice);
+    dl = pice * std::pow(x, pice - FT(1)) / (Tfrz - Tice);
+    return std::pow(x, pice);
+  }
+  // q_v*(T, rho) and d ln q_v* / dT
+  FT qsat(FT T, FT rho, FT &dlnq) const {
+    FT dl;
+    const FT lam = liq_frac(T, dl);
+    const FT dcl = cpv - cpl, dci = cpv - cpi;
+    const FT dcp = lam * dcl + (FT(1) - lam) * dci, L0 = lam * Lv0 + (FT(1) - lam) * Ls0;
+    const FT a = dcp / Rv, b = (L0 - dcp * T0) / Rv, s = FT(1) / Ttr - FT(1) / T;
+    const FT lt = std::log(T / Ttr);
+    const FT ps = ptr * std::exp(a * lt + b * s);
+    // d ln p_v* / dT, with the dependence of L_0 and dcp on lam(T)
+    const FT dlp = a / T + b / (T * T) + dl * ((dcl - dci) / Rv * lt + ((Lv0 - Ls0) - (dcl - dci) * T0) / Rv * s);
+    dlnq = dlp - FT(1) / T;
+    return ps / (rho * Rv * T);
+  }
+  struct Sat {
+    FT T, ql, qi;
+  };
+  Sat sat_adjust(FT rho, FT eint, FT q) const {
+    const FT cvm0 = cvd + (cvv - cvd) * q;
+    FT T = T0 + (eint - q * ev0 + (FT(1) - q) * Rd * T0) / cvm0;
+    T = std::max(Tmin_sgs, T);
+    FT dlnq;
+    if (q <= qsat(T, rho, dlnq)) return {T, FT(0), FT(0)};
+    FT lo = T, hi = std::max(T + q * (ev0 + ei0) / cvd, T0) + FT(1);
+    for (int it = 0; it < sa_iters; ++it) {
+      FT dl;
+      const FT lam = liq_frac(T, dl);
+      const FT qs = qsat(T, rho, dlnq);
+      const FT qc = q - qs;
+      const FT ql = lam * qc, qi = (FT(1) - lam) * qc;
+      const FT cvm = cvd + (cvv - cvd) * q + (cvl - cvv) * ql + (cvi - cvv) * qi;
+      const FT f = cvm * (T - T0) + qs * ev0 - qi * ei0 - (FT(1) - q) * Rd * T0 - eint;
+      const FT dqc = -qs * dlnq;
+      const FT dql = dl * qc + lam * dqc, dqi = -dl * qc + (FT(1) - lam) * dqc;
+      const FT df = cvm + (T - T0) * ((cvl - cvv) * dql + (cvi - cvv) * dqi) - dqc * ev0 - dqi * ei0;
+      if (f < FT(0)) lo = T;
+      else hi = T;
+      const FT Tn = T - f / df;
+      T = (Tn >= lo && Tn <= hi) ? Tn : (lo + hi) / FT(2);
+    }
+    FT dl;
+    const FT lam = liq_frac(T, dl);
+    const FT qc = std::max(FT(0), q - qsat(T, rho, dlnq));
+    return {T, lam * qc, (FT(1) - lam) * qc};
+  }
 #ifdef ORACLE_PHID
   // per level: the reference pressure p0 = p_ref Pi0^(1/kappa) and Pi0^7, Phi_r(Pi0) = g z_c (Newton, FP64)
   std::vector<FT> p0v, pi07;
@@ -164,6 +251,8 @@ struct Oracle {
       v->assign(P, FT(0));
     pre.u3c.assign(nfac(), FT(0));
     pre.w3c.assign(nfac(), FT(0));
+    if (moist)
+      for (auto *v : {&pre.q, &pre.kapm, &pre.dpdq}) v->assign(P, FT(0));
 #ifdef ORACLE_PHID
     ref_levels();
 #endif
@@ -244,14 +333,31 @@ struct Oracle {
           pre.K[q] = K;
           FT Phi = grav * zcp(e, n, v);
           FT eint = rhoe / rho - K - Phi;
-          FT T = std::max(Tmin_sgs, T0 + (eint + Rd * T0) / cvd);
-          FT p = rho * Rd * T;
+          FT T, Rm = Rd;
+          if (moist) {
+            // precomputed_quantities.jl:734-747: q_tot_nonneg = max(0, specific(rho q_tot, rho)),
+            // the saturation adjustment, p = rho R_m T (EquilibriumMicrophysics0M)
+            const FT qt = Yc[ci(e, 4, n, v)] / rho, qn = std::max(FT(0), qt);
+            const Sat sa = sat_adjust(rho, eint, qn);
+            T = sa.T;
+            Rm = Rd * (FT(1) - qn) + Rv * (qn - sa.ql - sa.qi);
+            const FT cvm = cvd + (cvv - cvd) * qn + (cvl - cvv) * sa.ql + (cvi - cvv) * sa.qi;
+            const FT km = Rm / cvm;
+            pre.q[q] = qt;
+            pre.kapm[q] = km;
+            // ᶜ∂p∂ρq_tot (manual_sparse_jacobian.jl:670-685)
+            pre.dpdq[q] = km * (-ev0 - Rd * T0 - (cvv - cvd) * (T - T0)) + (Rv - Rd) * T;
+          } else {
+            T = std::max(Tmin_sgs, T0 + (eint + Rd * T0) / cvd);
+          }
+          FT p = rho * Rm * T;
           FT Pi = exner(p);
           pre.T[q] = T;
           pre.p[q] = p;
-          pre.h[q] = rhoe / rho + Rd * T;
+          pre.h[q] = rhoe / rho + Rm * T;
           pre.Pi[q] = Pi;
-          pre.thv[q] = T / Pi;
+          // theta_v = T R_m / (Pi R_d) (refstate_thermodynamics.jl:58-63)
+          pre.thv[q] = moist ? T * Rm / (Pi * Rd) : T / Pi;
           pre.thvr[q] = T_ref(Pi) / Pi;
 #ifdef ORACLE_PHID
           // precision-study build: phir holds the deviation g z - Phi_r(Pi), formed from the
@@ -789,7 +895,7 @@ struct Oracle {
 #pragma omp parallel for
     for (int e = 0; e < Nh; ++e)
       for (int n = 0; n < NN; ++n) {
-        std::vector<FT> flux(Nf), fh(Nf);
+        std::vector<FT> flux(Nf), fh(Nf), fq(Nf, FT(0));
         for (int k = 0; k < Nf; ++k) {
           if (k == 0 || k == Nv) { flux[k] = 0; fh[k] = 0; continue; }
           FT rJ = (Yc[ci(e, 0, n, k - 1)] * Jc(e, n, k - 1) + Yc[ci(e, 0, n, k)] * Jc(e, n, k)) / FT(2);
@@ -798,11 +904,14 @@ struct Oracle {
           FT hb = (pre.h[pi(e, n, k - 1)] + pre.h[pi(e, n, k)]) / FT(2);
           flux[k] = Jf * F;       // ᶜadvdivᵥ multiplies the face value by ᶠJ
           fh[k] = Jf * F * hb;
+          // central transport of q_tot = specific(rho q_tot, rho) (implicit_tendency.jl:211-215)
+          if (moist) fq[k] = Jf * F * ((pre.q[pi(e, n, k - 1)] + pre.q[pi(e, n, k)]) / FT(2));
         }
         for (int v = 0; v < Nv; ++v) {
           FT J = Jc(e, n, v);
           Tc[ci(e, 0, n, v)] -= (flux[v + 1] - flux[v]) / J;
           Tc[ci(e, 3, n, v)] -= (fh[v + 1] - fh[v]) / J;
+          if (moist) Tc[ci(e, 4, n, v)] -= (fq[v + 1] - fq[v]) / J;
         }
         for (int k = 0; k < Nf; ++k) {
           FT val = 0;
@@ -831,6 +940,8 @@ struct Oracle {
     std::vector<FT> Muh;                  // [col][k][2][2] (centres k-1, k; comps 1, 2)
     std::vector<FT> Muu;                  // [col][k][3]  (faces k-1, k, k+1)
     std::vector<FT> Mrh, Meh;             // terrain: [col][v][3][2] (centres v-1, v, v+1; comps 1, 2)
+    std::vector<FT> Mqu;                  // moist: [col][v][2] (rho q_tot, u3 faces v, v+1)
+    std::vector<FT> Muq;                  // moist: [col][k][2] (u3, rho q_tot of centres k-1, k)
   } jac;
 
   void update_jacobian(const FT *Yc, const FT *Yf, FT dtg) {
@@ -839,7 +950,10 @@ struct Oracle {
     jac.Mur.assign(C * Nf * 2, 0); jac.Mue.assign(C * Nf * 2, 0);
     jac.Muh.assign(C * Nf * 4, 0); jac.Muu.assign(C * Nf * 3, 0);
     if (topo) { jac.Mrh.assign(C * Nv * 6, 0); jac.Meh.assign(C * Nv * 6, 0); }
-    FT kap = Rd / cvd;  // kappa_m for dry air
+    if (moist) { jac.Mqu.assign(C * Nv * 2, 0); jac.Muq.assign(C * Nf * 2, 0); }
+    const FT kapd = Rd / cvd;  // kappa_m for dry air
+    // moist: kappa_m = R_m / cv_m of each centre (ᶜkappa_m_field!, manual_sparse_jacobian.jl:646-662)
+    auto kapc = [&](size_t q) { return moist ? pre.kapm[q] : kapd; };
 #pragma omp parallel for
     for (int e = 0; e < Nh; ++e)
       for (int n = 0; n < NN; ++n) {
@@ -849,7 +963,7 @@ struct Oracle {
           FT J = Jc(e, n, v);
           for (int s = 0; s < 2; ++s) {
             int k = v + s;
-            FT val = 0, vh = 0;
+            FT val = 0, vh = 0, vq = 0;
             if (k > 0 && k < Nv) {
               FT rJ = (Yc[ci(e, 0, n, k - 1)] * Jc(e, n, k - 1) + Yc[ci(e, 0, n, k)] * Jc(e, n, k)) / FT(2);
               FT g33 = g33f(e, n, k);
@@ -857,9 +971,12 @@ struct Oracle {
               val = sign * rJ * g33 / J;
               FT hb = (pre.h[pi(e, n, k - 1)] + pre.h[pi(e, n, k)]) / FT(2);
               vh = val * hb;
+              // (rho q_tot, u_3): the same with ᶠinterp(q_tot) (manual_sparse_jacobian.jl:770-783)
+              if (moist) vq = val * ((pre.q[pi(e, n, k - 1)] + pre.q[pi(e, n, k)]) / FT(2));
             }
             jac.Mru[(col * Nv + v) * 2 + s] = dtg * val;
             jac.Meu[(col * Nv + v) * 2 + s] = dtg * vh;
+            if (moist) jac.Mqu[(col * Nv + v) * 2 + s] = dtg * vq;
           }
         }
         for (int k = 0; k < Nf; ++k) {
@@ -871,35 +988,51 @@ struct Oracle {
           size_t a = pi(e, n, k - 1), b = pi(e, n, k);
           FT ra = Yc[ci(e, 0, n, k - 1)], rb = Yc[ci(e, 0, n, k)];
           FT rbar = (ra + rb) / FT(2);
-          auto dpdr = [&](size_t q) { return kap * (T0 * cpd - pre.K[q] - grav * zcp(e, n, (int)(q % Nv))); };
+          const FT ka = kapc(a), kb = kapc(b);
+          // ᶜ∂p∂ρ = kappa_m (T_0 cp_d - K - Phi) + (R_d - kappa_m cv_d) T; the second term is 0
+          // for dry air (manual_sparse_jacobian.jl:817-819)
+          auto dpdr = [&](size_t q, FT km) {
+            const FT d = km * (T0 * cpd - pre.K[q] - grav * zcp(e, n, (int)(q % Nv)));
+            return moist ? d + (Rd - km * cvd) * pre.T[q] : d;
+          };
           FT thvb = (pre.thv[a] + pre.thv[b]) / FT(2);
           FT gPi = pre.Pi[b] - pre.Pi[a];
           FT buoy = cpd * thvb * gPi / rbar;  // times ᶠinterp_matrix (1/2, 1/2)
           // ᶠp_grad_matrix = diag(-1/ρ̄) ᶠgradᵥ_matrix  (−1 at k−1, +1 at k)
-          jac.Mur[(col * Nf + k) * 2 + 0] = dtg * (dpdr(a) / rbar + buoy / FT(2));
-          jac.Mur[(col * Nf + k) * 2 + 1] = dtg * (-dpdr(b) / rbar + buoy / FT(2));
-          jac.Mue[(col * Nf + k) * 2 + 0] = dtg * (kap / rbar);
-          jac.Mue[(col * Nf + k) * 2 + 1] = dtg * (-kap / rbar);
+          jac.Mur[(col * Nf + k) * 2 + 0] = dtg * (dpdr(a, ka) / rbar + buoy / FT(2));
+          jac.Mur[(col * Nf + k) * 2 + 1] = dtg * (-dpdr(b, kb) / rbar + buoy / FT(2));
+          jac.Mue[(col * Nf + k) * 2 + 0] = dtg * (ka / rbar);
+          jac.Mue[(col * Nf + k) * 2 + 1] = dtg * (-kb / rbar);
+          if (moist) {
+            // (u_3, rho q_tot) = dtγ ᶠp_grad_matrix ⋅ diag(ᶜ∂p∂ρq_tot) (manual_sparse_jacobian.jl:827-831)
+            jac.Muq[(col * Nf + k) * 2 + 0] = dtg * (pre.dpdq[a] / rbar);
+            jac.Muq[(col * Nf + k) * 2 + 1] = dtg * (-pre.dpdq[b] / rbar);
+          }
           // (u3, u_h): p_grad * diag(-kappa rho) * dK/du_h,  dK/du_i = u^i
-          jac.Muh[(col * Nf + k) * 4 + 0] = dtg * (-kap * ra / rbar) * pre.uc1[a];
-          jac.Muh[(col * Nf + k) * 4 + 1] = dtg * (-kap * ra / rbar) * pre.uc2[a];
-          jac.Muh[(col * Nf + k) * 4 + 2] = dtg * (kap * rb / rbar) * pre.uc1[b];
-          jac.Muh[(col * Nf + k) * 4 + 3] = dtg * (kap * rb / rbar) * pre.uc2[b];
+          jac.Muh[(col * Nf + k) * 4 + 0] = dtg * (-ka * ra / rbar) * pre.uc1[a];
+          jac.Muh[(col * Nf + k) * 4 + 1] = dtg * (-ka * ra / rbar) * pre.uc2[a];
+          jac.Muh[(col * Nf + k) * 4 + 2] = dtg * (kb * rb / rbar) * pre.uc1[b];
+          jac.Muh[(col * Nf + k) * 4 + 3] = dtg * (kb * rb / rbar) * pre.uc2[b];
           // (u3, u3): p_grad * diag(-kappa rho) * dK/du3 - beta - I ; dK_v/du3_f = u^3_f / 2
           if (topo) {
             // over terrain dK_v/du3_f = (g^33 u_3)_f / 2 + CT3(u_h)_v / 2 (∂ᶜK_∂ᶠu₃,
             // manual_sparse_jacobian.jl:754-756)
             const FT wm = pre.w3c[fi(e, n, k - 1)], w0 = pre.w3c[fi(e, n, k)], wp = pre.w3c[fi(e, n, k + 1)];
             const FT ca = pre.ct3[a], cb = pre.ct3[b];
-            jac.Muu[(col * Nf + k) * 3 + 0] = dtg * (-kap * ra * (wm + ca) / (FT(2) * rbar));
+            jac.Muu[(col * Nf + k) * 3 + 0] = dtg * (-kapd * ra * (wm + ca) / (FT(2) * rbar));
             jac.Muu[(col * Nf + k) * 3 + 1] =
-                dtg * (kap * (rb * (w0 + cb) - ra * (w0 + ca)) / (FT(2) * rbar) - beta) - FT(1);
-            jac.Muu[(col * Nf + k) * 3 + 2] = dtg * (kap * rb * (wp + cb) / (FT(2) * rbar));
+                dtg * (kapd * (rb * (w0 + cb) - ra * (w0 + ca)) / (FT(2) * rbar) - beta) - FT(1);
+            jac.Muu[(col * Nf + k) * 3 + 2] = dtg * (kapd * rb * (wp + cb) / (FT(2) * rbar));
+          } else if (moist) {
+            FT um = pre.u3c[fi(e, n, k - 1)], u0 = pre.u3c[fi(e, n, k)], up = pre.u3c[fi(e, n, k + 1)];
+            jac.Muu[(col * Nf + k) * 3 + 0] = dtg * (-ka * ra * um / (FT(2) * rbar));
+            jac.Muu[(col * Nf + k) * 3 + 1] = dtg * ((kb * rb - ka * ra) * u0 / (FT(2) * rbar) - beta) - FT(1);
+            jac.Muu[(col * Nf + k) * 3 + 2] = dtg * (kb * rb * up / (FT(2) * rbar));
           } else {
             FT um = pre.u3c[fi(e, n, k - 1)], u0 = pre.u3c[fi(e, n, k)], up = pre.u3c[fi(e, n, k + 1)];
-            jac.Muu[(col * Nf + k) * 3 + 0] = dtg * (-kap * ra * um / (FT(2) * rbar));
-            jac.Muu[(col * Nf + k) * 3 + 1] = dtg * (kap * (rb - ra) * u0 / (FT(2) * rbar) - beta) - FT(1);
-            jac.Muu[(col * Nf + k) * 3 + 2] = dtg * (kap * rb * up / (FT(2) * rbar));
+            jac.Muu[(col * Nf + k) * 3 + 0] = dtg * (-kapd * ra * um / (FT(2) * rbar));
+            jac.Muu[(col * Nf + k) * 3 + 1] = dtg * (kapd * (rb - ra) * u0 / (FT(2) * rbar) - beta) - FT(1);
+            jac.Muu[(col * Nf + k) * 3 + 2] = dtg * (kapd * rb * up / (FT(2) * rbar));
           }
         }
         if (topo) {
@@ -953,6 +1086,11 @@ struct Oracle {
   }
 
   // ---- ldiv!: BlockArrowheadSolve(rho, rhoe; alg2 = BlockLowerTriangularSolve(u_h)) ----
+  // Moist 0M: the reference solves with ApproximateBlockArrowheadIterativeSolve over (rho, rho e_tot,
+  // rho q_tot) (manual_sparse_jacobian.jl:539-584) because diffusion and sedimentation may fill the
+  // scalar blocks; with 0M and neither, those blocks are -I ((rho e_tot, rho q_tot) = 0,
+  // manual_sparse_jacobian.jl:906-910), its block-arrowhead Schur preconditioner is the exact
+  // inverse, and the solve is the same Schur complement onto u_3 with a third scalar row.
   void ldiv(FT *Xc, FT *Xf, const FT *Rc, const FT *Rf) const {
 #pragma omp parallel for
     for (int e = 0; e < Nh; ++e)
@@ -966,12 +1104,13 @@ struct Oracle {
         }
         // over terrain the (rho, u_h), (rho e_tot, u_h) blocks times Δu_h = -R_uh move to the
         // right-hand sides of the scalar rows: R_x + M_x,uh R_uh
-        std::vector<FT> Rr(Nv), Re(Nv);
+        std::vector<FT> Rr(Nv), Re(Nv), Rq(Nv, FT(0));
         for (int v = 0; v < Nv; ++v) {
           FT gr, ge;
           uh_coupling(e, n, Rc, v, gr, ge);
           Rr[v] = topo ? Rc[ci(e, 0, n, v)] + gr : Rc[ci(e, 0, n, v)];
           Re[v] = topo ? Rc[ci(e, 3, n, v)] + ge : Rc[ci(e, 3, n, v)];
+          if (moist) Rq[v] = Rc[ci(e, 4, n, v)];
         }
         for (int k = 0; k < Nf; ++k) {
           const FT *mu = &jac.Muu[(col * Nf + k) * 3];
@@ -992,6 +1131,13 @@ struct Oracle {
             // face v+1 relative to k: s
             FT t0 = cr * mru[0] + ce * meu[0];  // -> face v
             FT t1 = cr * mru[1] + ce * meu[1];  // -> face v+1
+            if (moist) {
+              const FT cq = jac.Muq[(col * Nf + k) * 2 + s];
+              const FT *mqu = &jac.Mqu[(col * Nv + v) * 2];
+              t0 += cq * mqu[0];
+              t1 += cq * mqu[1];
+              rhs += cq * Rq[v];
+            }
             if (s == 0) { a += t0; b += t1; } else { b += t0; c += t1; }
             rhs += cr * Rr[v] + ce * Re[v];
             rhs += mh[2 * s] * Rc[ci(e, 1, n, v)] + mh[2 * s + 1] * Rc[ci(e, 2, n, v)];
@@ -1014,6 +1160,10 @@ struct Oracle {
           const FT *meu = &jac.Meu[(col * Nv + v) * 2];
           Xc[ci(e, 0, n, v)] = mru[0] * x[v] + mru[1] * x[v + 1] - Rr[v];
           Xc[ci(e, 3, n, v)] = meu[0] * x[v] + meu[1] * x[v + 1] - Re[v];
+          if (moist) {
+            const FT *mqu = &jac.Mqu[(col * Nv + v) * 2];
+            Xc[ci(e, 4, n, v)] = mqu[0] * x[v] + mqu[1] * x[v + 1] - Rq[v];
+          }
         }
       }
   }
@@ -1038,6 +1188,10 @@ struct Oracle {
           }
           Oc[ci(e, 1, n, v)] = -Vc[ci(e, 1, n, v)];
           Oc[ci(e, 2, n, v)] = -Vc[ci(e, 2, n, v)];
+          if (moist) {
+            const FT *mqu = &jac.Mqu[(col * Nv + v) * 2];
+            Oc[ci(e, 4, n, v)] = -Vc[ci(e, 4, n, v)] + mqu[0] * a + mqu[1] * b;
+          }
         }
         for (int k = 0; k < Nf; ++k) {
           const FT *mu = &jac.Muu[(col * Nf + k) * 3];
@@ -1052,13 +1206,14 @@ struct Oracle {
             if (v < 0 || v >= Nv) continue;
             s += mr[t] * Vc[ci(e, 0, n, v)] + me[t] * Vc[ci(e, 3, n, v)];
             s += mh[2 * t] * Vc[ci(e, 1, n, v)] + mh[2 * t + 1] * Vc[ci(e, 2, n, v)];
+            if (moist) s += jac.Muq[(col * Nf + k) * 2 + t] * Vc[ci(e, 4, n, v)];
           }
           Of[fi(e, n, k)] = s;
         }
       }
   }
 
-  // ---- correct_implicit_advection_tendency! (van Leer minus central, ρe_tot only) ----
+  // ---- correct_implicit_advection_tendency! (van Leer minus central; ρe_tot, and ρq_tot when moist) ----
   FT vanleer_face(FT u, const FT *a, int k) const {
     // a: centre values of the column; face k between centres k-1 and k (interior)
     bool near = (k == 1 || k == Nv - 1);
@@ -1088,19 +1243,22 @@ struct Oracle {
     for (int e = 0; e < Nh; ++e)
       for (int n = 0; n < NN; ++n) {
         std::vector<FT> h(Nv), fup(Nf, 0), fc(Nf, 0);
-        for (int v = 0; v < Nv; ++v) h[v] = pre.h[pi(e, n, v)];
-        for (int k = 1; k < Nv; ++k) {
-          FT rJ = (Yc[ci(e, 0, n, k - 1)] * Jc(e, n, k - 1) + Yc[ci(e, 0, n, k)] * Jc(e, n, k)) / FT(2);
-          FT u = pre.u3c[fi(e, n, k)];
-          FT Jf = Jfc(e, n, k);
-          fup[k] = Jf * (rJ / Jf * vanleer_face(u, h.data(), k));
-          fc[k] = Jf * (rJ / Jf * (u * (h[k - 1] + h[k]) / FT(2)));
-        }
-        for (int v = 0; v < Nv; ++v) {
-          FT J = Jc(e, n, v);
-          FT vup = -(fup[v + 1] - fup[v]) / J;
-          FT vc = -(fc[v + 1] - fc[v]) / J;
-          Tc[ci(e, 3, n, v)] = vup - vc;
+        for (int comp = 3; comp <= (moist ? 4 : 3); ++comp) {
+          // the transported specific quantity: h_tot for rho e_tot, q_tot for rho q_tot
+          for (int v = 0; v < Nv; ++v) h[v] = comp == 3 ? pre.h[pi(e, n, v)] : pre.q[pi(e, n, v)];
+          for (int k = 1; k < Nv; ++k) {
+            FT rJ = (Yc[ci(e, 0, n, k - 1)] * Jc(e, n, k - 1) + Yc[ci(e, 0, n, k)] * Jc(e, n, k)) / FT(2);
+            FT u = pre.u3c[fi(e, n, k)];
+            FT Jf = Jfc(e, n, k);
+            fup[k] = Jf * (rJ / Jf * vanleer_face(u, h.data(), k));
+            fc[k] = Jf * (rJ / Jf * (u * (h[k - 1] + h[k]) / FT(2)));
+          }
+          for (int v = 0; v < Nv; ++v) {
+            FT J = Jc(e, n, v);
+            FT vup = -(fup[v + 1] - fup[v]) / J;
+            FT vc = -(fc[v + 1] - fc[v]) / J;
+            Tc[ci(e, comp, n, v)] = vup - vc;
+          }
         }
       }
   }
@@ -1245,6 +1403,16 @@ struct Oracle {
     kappa = Rd / cpd;
     hs = p->held_suarez; hs_day = p->hs_day; hs_sb = p->hs_sigma_b; hs_dTy = p->hs_dT_y; hs_Teq = p->hs_T_equator;
     hs_dthz = p->hs_dtheta_z; hs_Tmin = p->hs_T_min; hs_p0 = p->hs_p_ref_theta; hs_MSLP = p->hs_MSLP;
+    moist = p->moist;
+    nfc = moist ? 5 : 4;
+    if (moist) {
+      Rv = p->R_v; cpv = p->cp_v; cpl = p->cp_l; cpi = p->cp_i;
+      cvv = cpv - Rv; cvl = cpl; cvi = cpi;
+      Lv0 = p->LH_v0; Ls0 = p->LH_s0; Ttr = p->T_triple; ptr = p->press_triple;
+      Tfrz = p->T_freeze; Tice = p->T_icenuc; pice = p->pow_icenuc;
+      ev0 = Lv0 - Rv * T0; ei0 = Ls0 - Lv0;
+      sa_iters = p->sa_iters;
+    }
     for (int n = 0; n < NN; ++n) W[n] = g->W[n];
     for (int i = 0; i < NQ; ++i) for (int k = 0; k < NQ; ++k) D[i][k] = g->D[i * NQ + k];
     size_t H = (size_t)Nh * NN;
@@ -1379,6 +1547,17 @@ void oracle_step(void *hh, void *Yc, void *Yf, double dt, int nsteps) {
 void oracle_laplacians(void *hh, void *X, void *O) {
   Handle *h = (Handle *)hh;
   DISPATCH(h, (o.laplacians((const decltype(o.R) *)X, (decltype(o.R) *)O)));
+}
+// The saturation adjustment of n points (moist handles): T, q_liq, q_ice from (rho, e_int, q_tot).
+void oracle_sat_adjust(void *hh, int n, const double *rho, const double *eint, const double *q, double *T,
+                       double *ql, double *qi) {
+  Handle *h = (Handle *)hh;
+  for (int i = 0; i < n; ++i)
+    DISPATCH(h, ({
+      using F = decltype(o.R);
+      const auto r = o.sat_adjust((F)rho[i], (F)eint[i], (F)q[i]);
+      T[i] = r.T; ql[i] = r.ql; qi[i] = r.qi;
+    }));
 }
 void oracle_global_sums(void *hh, void *Yc, double *out) {
   Handle *h = (Handle *)hh;

@@ -49,7 +49,11 @@ class _Params(ctypes.Structure):
         "nu_v", "nu_s", "div_damp", "sponge_zd", "alpha_uh", "alpha_w", "z_max", "dt_model")] + [
         ("upwinding", ctypes.c_int), ("dss_stage1", ctypes.c_int), ("held_suarez", ctypes.c_int)] + [
         (n, ctypes.c_double) for n in ("hs_day", "hs_sigma_b", "hs_dT_y", "hs_T_equator", "hs_dtheta_z",
-                                       "hs_T_min", "hs_p_ref_theta", "hs_MSLP")]
+                                       "hs_T_min", "hs_p_ref_theta", "hs_MSLP")] + [
+        ("moist", ctypes.c_int)] + [
+        (n, ctypes.c_double) for n in ("R_v", "cp_v", "cp_l", "cp_i", "LH_v0", "LH_s0", "T_triple", "press_triple",
+                                       "T_freeze", "T_icenuc", "pow_icenuc")] + [
+        ("sa_iters", ctypes.c_int)]
 
 
 _dp = ctypes.POINTER(ctypes.c_double)
@@ -85,6 +89,7 @@ def lib():
         _lib.oracle_update_jacobian.argtypes = [v, v, v, ctypes.c_double]
         _lib.oracle_step.argtypes = [v, v, v, ctypes.c_double, ctypes.c_int]
         _lib.oracle_global_sums.argtypes = [v, v, _dp]
+        _lib.oracle_sat_adjust.argtypes = [v, ctypes.c_int] + [_dp] * 6
         _lib.oracle_set_threads.argtypes = [ctypes.c_int]
         _lib.oracle_max_threads.restype = ctypes.c_int
     return _lib
@@ -99,7 +104,10 @@ class Oracle:
 
     ``params`` is a dict with the keys of ``_Params``; state arrays use the
     C-ABI layout: centre ``[Nh, 4, 16, Nv]`` (rho, u_1, u_2, rho e_tot) and
-    face ``[Nh, 16, Nv + 1]`` (u_3).
+    face ``[Nh, 16, Nv + 1]`` (u_3).  With ``params["moist"] = 1`` (moist 0M) the centre
+    block is ``[Nh, 5, 16, Nv]`` (rho q_tot last) and only the column operators are
+    available: set_precomputed, pressure, implicit_tendency, update_jacobian, ldiv,
+    jac_apply and correct_implicit.
     """
 
     def __init__(self, geom, params, dtype=np.float64):
@@ -137,6 +145,10 @@ class Oracle:
         for k, _ in _Params._fields_:
             setattr(p, k, params.get(k, 0))
         self._g, self._p = g, p
+        self.moist = bool(params.get("moist", 0))
+        if self.moist and terrain is not None:
+            raise NotImplementedError("moist 0M over terrain-following levels is not restated")
+        self.nfc = 5 if self.moist else 4
         self.h = L.oracle_create(ctypes.byref(g), ctypes.byref(p), self.dtype.itemsize)
         self.Nh, self.Nv = geom.Nh, geom.Nv
 
@@ -147,7 +159,12 @@ class Oracle:
             pass
 
     def zeros(self):
-        return (np.zeros((self.Nh, 4, 16, self.Nv), self.dtype), np.zeros((self.Nh, 16, self.Nv + 1), self.dtype))
+        return (np.zeros((self.Nh, self.nfc, 16, self.Nv), self.dtype),
+                np.zeros((self.Nh, 16, self.Nv + 1), self.dtype))
+
+    def _dry_only(self, what):
+        if self.moist:
+            raise NotImplementedError(what + " is restated for dry air only (moist 0M: the column operators)")
 
     def _chk(self, *a):
         for x in a:
@@ -166,6 +183,7 @@ class Oracle:
         return p
 
     def remaining_tendency(self, Yc, Yf):
+        self._dry_only('remaining_tendency')
         Tc, Tf = self.zeros()
         self._chk(Yc, Yf)
         lib().oracle_remaining_tendency(self.h, _ptr(Tc), _ptr(Tf), _ptr(Yc), _ptr(Yf))
@@ -203,28 +221,44 @@ class Oracle:
         return Oc, Of
 
     def dss(self, Yc, Yf):
+        self._dry_only('dss')
         self._chk(Yc, Yf)
         lib().oracle_dss(self.h, _ptr(Yc), _ptr(Yf))
 
     def dss_c123(self, C):
         """In place: the DSS of a centre block [Nh, 4, 16, Nv] whose comp 0 is a scalar and
         comps 1-3 one covariant 3-vector (the block of the Laplacians)."""
+        self._dry_only('dss_c123')
         self._chk(C)
         lib().oracle_dss_c123(self.h, _ptr(C))
 
     def laplacians(self, X):
         """Per level, after the DSS: the scalar Laplacian wdiv(grad f) of comp 0 and the vector
         Laplacian of the covariant (comp 1, comp 2); X and the result are [Nh, 4, 16, Nv]."""
+        self._dry_only('laplacians')
         X = np.ascontiguousarray(X, self.dtype)
         O = np.zeros_like(X)
         lib().oracle_laplacians(self.h, _ptr(X), _ptr(O))
         return O
 
     def step(self, Yc, Yf, dt, nsteps=1):
+        self._dry_only('step')
         self._chk(Yc, Yf)
         lib().oracle_step(self.h, _ptr(Yc), _ptr(Yf), float(dt), int(nsteps))
 
+    def sat_adjust(self, rho, eint, q):
+        """The saturation adjustment (moist oracles): (T, q_liq, q_ice) of each point of the
+        equal-shaped arrays rho, e_int, q_tot, in the oracle's precision."""
+        if not self.moist:
+            raise NotImplementedError("the saturation adjustment belongs to a moist oracle")
+        a = [np.ascontiguousarray(x, np.float64).ravel() for x in np.broadcast_arrays(rho, eint, q)]
+        out = [np.zeros_like(a[0]) for _ in range(3)]
+        lib().oracle_sat_adjust(self.h, a[0].size, *[x.ctypes.data_as(_dp) for x in a + out])
+        shape = np.broadcast(rho, eint, q).shape
+        return tuple(x.reshape(shape) for x in out)
+
     def global_sums(self, Yc):
+        self._dry_only('global_sums')
         out = np.zeros(2)
         lib().oracle_global_sums(self.h, _ptr(Yc), out.ctypes.data_as(_dp))
         return out

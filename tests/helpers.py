@@ -75,3 +75,32 @@ def field_errors(Xc, Xf, Rc, Rf):
     out = {names[c]: rel_err(Xc[:, c], Rc[:, c]) for c in range(4)}
     out["u_3"] = rel_err(Xf, Rf)
     return out
+
+
+def moist_state(cfg, seed=11, dtype=np.float64, w_amp=0.05, q0=0.018, H=2500.0):
+    """Moist 0M state [Nh, 5, 16, Nv] (rho q_tot last) and faces: the perturbed dry state with
+    q_tot = q0 exp(-z / H) (x (1 + 5 % noise)) and rho e_tot raised by
+    rho q_tot ((cv_v - cv_d)(T - T_0) + e_int_v0 + R_d T_0), so that the all-vapour temperature
+    is the dry state's T.  With q0 = 0.018 the lowest kilometres and the mixed-phase levels are
+    supersaturated there (the saturation adjustment condenses); q0 = 0.003 keeps every point
+    unsaturated."""
+    Yc, Yf = perturbed_state(cfg.with_(moist=False), seed, np.float64, w_amp)
+    dry = make_oracle(cfg.with_(moist=False))
+    p = dry.pressure(Yc, Yf)
+    K, M = cfg.constants, cfg.moist_constants
+    rho = Yc[:, 0]
+    T = p / (rho * K["R_d"])
+    g = oracle_geometry(cfg)
+    rng = np.random.default_rng(seed + 100)
+    q = q0 * np.exp(-g.zc / H)[None, None, :] * (1 + 0.05 * rng.normal(size=rho.shape))
+    cvv = M["cp_v"] - M["R_v"]
+    ev0 = M["LH_v0"] - M["R_v"] * K["T_0"]
+    Ym = np.concatenate([Yc, (rho * q)[:, None]], axis=1)
+    Ym[:, 3] += rho * q * ((cvv - K["cv_d"]) * (T - K["T_0"]) + ev0 + K["R_d"] * K["T_0"])
+    return np.ascontiguousarray(Ym.astype(dtype)), Yf.astype(dtype)
+
+
+def moist_field_errors(Xc, Xf, Rc, Rf):
+    out = field_errors(Xc, Xf, Rc, Rf)
+    out["rho_q_tot"] = rel_err(Xc[:, 4], Rc[:, 4])
+    return out

@@ -61,6 +61,7 @@ def parse(argv=None):
     ap.add_argument("--no-held-suarez", action="store_true")
     ap.add_argument("--topography-steps", type=int, default=20)
     ap.add_argument("--no-topography", action="store_true")
+    ap.add_argument("--no-moist", action="store_true")
     # bracket one forward step ("step") or one reverse pass ("reverse") by
     # cudaProfilerStart/Stop, for `ncu --profile-from-start off`; no effect otherwise
     # ("topography": one step of the terrain-following workload)
@@ -392,6 +393,12 @@ def run_gb300(args):
     held_suarez = None
     if not args.no_held_suarez:
         held_suarez = measure_held_suarez(args, ms)
+    moist = None
+    if not args.no_moist:
+        try:
+            moist = measure_moist(args)
+        except Exception as e:  # reported in the line, not fatal
+            moist = {"error": "%s: %s" % (type(e).__name__, e)}
     topography = None
     if not args.no_topography:
         try:
@@ -438,7 +445,7 @@ def run_gb300(args):
                             "post-Newton correction, DSS) with unfused torch stage algebra"},
                 "fp32_vs_fp64": prec, "fp64_step": fp64, "batching": batching, "adjoint": adjoint,
                 "differentiation": differentiation, "precision_h60": h60, "held_suarez": held_suarez,
-                "topography": topography, "config1": config1,
+                "topography": topography, "moist_0m": moist, "config1": config1,
                 "clocks": clk, "gpu_launches": LAUNCHES_PER_STEP * args.steps}
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -718,6 +725,60 @@ def measure_topography(args, fwd_ms):
            "kernels": kern, "fp32_vs_fp64": prec}
     del s, s64, s32
     torch.cuda.empty_cache()
+    return out
+
+
+def measure_moist(args):
+    """Moist 0M column hooks on the production grid (h_elem 30, z_elem 63, FP32): one Newton
+    iteration's hook calls (set_precomputed_quantities, implicit_tendency, update_jacobian, ldiv,
+    correct_implicit_advection_tendency) with rho q_tot and the saturation adjustment, against the
+    same calls of the dry context; per hook its CUDA-event time and the bandwidth of its
+    algorithmic bytes (state in, tendency or solution out, Jacobian rows)."""
+    import torch
+    from gbdycore import config as C, simulation as sim
+    from gbdycore import setups as S
+    base = C.production_h30()
+    out = {}
+    for name, cfg in (("dry", base), ("moist", base.with_(moist=True))):
+        g = sim.Geometry(cfg)
+        if cfg.moist:
+            Yc, Yf = S.moist_initial_state(g, cfg, seed=1, sigma=2.0)
+        else:
+            Yc, Yf = S.initial_state(g, cfg, seed=1, sigma=2.0)
+        p = sim.AtmosCache(cfg)
+        Y = sim.FieldVector.from_numpy(Yc, Yf)
+        Y.f.normal_(0.0, 0.05)
+        sim.set_precomputed_quantities(Y, p, 0.0)
+        T, dY = Y.similar(), Y.similar()
+        dtg = 0.4358665215084590 * cfg.dt
+        nfc = Yc.shape[1]
+        fb = 4
+        Nh, Nv = g.Nh, cfg.z_elem
+        S_b, F_b = Nh * 16 * Nv * fb, Nh * 16 * (Nv + 1) * fb
+        nq = 19 if cfg.moist else 15
+        calls = {
+            "implicit_tendency": (lambda: sim.implicit_tendency(T, Y, p, 0.0), 2 * (nfc * S_b + F_b)),
+            "update_jacobian": (lambda: sim.update_jacobian(sim.Jacobian(p), Y, p, dtg, 0.0), nfc * S_b + F_b + nq * F_b),
+            "ldiv": (lambda: sim.ldiv(dY, sim.Jacobian(p), T), 2 * (nfc * S_b + F_b) + nq * F_b),
+            "correct_implicit": (lambda: sim.correct_implicit_advection_tendency(dY, Y, p, 0.0), 2 * (nfc * S_b + F_b)),
+        }
+        res = {}
+        reps = 20
+        for k, (fn, b) in calls.items():
+            fn()
+            torch.cuda.synchronize()
+            ms, _ = _timed(lambda: [fn() for _ in range(reps)])
+            ms /= reps
+            res[k] = {"ms": ms, "algorithmic_bytes": b, "GBps": b / (ms * 1e-3) / 1e9}
+        res["newton_iteration_ms"] = sum(v["ms"] for v in res.values())
+        res["finite"] = bool(torch.isfinite(T.c).all() and torch.isfinite(dY.c).all())
+        out[name] = res
+        del p, Y, T, dY
+        torch.cuda.empty_cache()
+    out["moist_over_dry"] = out["moist"]["newton_iteration_ms"] / out["dry"]["newton_iteration_ms"]
+    out["what"] = ("h_elem 30, z_elem 63, FP32; q_tot = 0.018 exp(-z / 2.5 km): condensate below ~2 km and on "
+                   "the mixed-phase levels; the saturation adjustment in every hook that forms the precomputed "
+                   "quantities")
     return out
 
 

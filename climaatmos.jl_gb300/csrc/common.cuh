@@ -204,7 +204,9 @@ __device__ __forceinline__ FT qsat(const DevParams<FT> &P, FT T, FT rho, FT &dln
 // partition q_c = q_t - q_v*(T) continued smoothly where q_v* > q_t (the clamped function's kink
 // makes plain Newton cycle).  f increases with T and
 // [T_u, max(T_u + q_t (e_int_v0 + e_int_i0) / cv_d, T_0) + 1] brackets its root; a step outside
-// the current bracket becomes a bisection.  The partition is that of the final T.
+// the current bracket becomes a bisection.  A lane stops once a step moves T by no more than
+// 1e-9 K (FP64) or 1e-3 K (FP32) (Newton's error after it is of the order of its square).  The
+// partition is that of the final T.
 template <class FT>
 __device__ __forceinline__ void sat_adjust(const DevParams<FT> &P, FT rho, FT eint, FT q, FT &T, FT &ql, FT &qi) {
   const FT cvm0 = P.cvd + (P.cvv - P.cvd) * q;
@@ -227,8 +229,11 @@ __device__ __forceinline__ void sat_adjust(const DevParams<FT> &P, FT rho, FT ei
     const FT df = cvm + (T - P.T0) * ((P.cvl - P.cvv) * dql + (P.cvi - P.cvv) * dqi) - dqc * P.ev0 - dqi * P.ei0;
     if (f < FT(0)) lo = T;
     else hi = T;
-    const FT Tn = T - gdiv(f, df);
-    T = (Tn >= lo && Tn <= hi) ? Tn : (lo + hi) / FT(2);
+    FT Tn = T - gdiv(f, df);
+    if (!(Tn >= lo && Tn <= hi)) Tn = (lo + hi) / FT(2);
+    const FT dT = Tn - T;
+    T = Tn;
+    if (fabs(dT) <= (sizeof(FT) == 8 ? FT(1e-9) : FT(1e-3))) break;
   }
   FT dl;
   const FT lam = liq_frac(P, T, dl);

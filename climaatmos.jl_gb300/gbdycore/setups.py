@@ -107,3 +107,38 @@ def workload_state(geom, cfg, name):
     if name == "differentiation":
         return initial_state(geom, cfg, seed=3, sigma=1.0)
     raise ValueError(name)
+
+
+def moist_initial_state(geom, cfg, seed=0, sigma=1.0, q0=0.018, scale_height=2500.0, dtype=None):
+    """Moist 0M counterpart of ``initial_state``: (Yc [Nh,5,16,Nv], Yf) with rho q_tot last.
+
+    The same temperature profile and winds, specific humidity q_tot = q0 exp(-z / H) with 5 %
+    noise per unique node and level, rho = p / (R_m T) with the all-vapour R_m, and
+    rho e_tot = rho (e_int(T, q_tot) + g z + K) with the all-vapour internal energy
+    cv_m (T - T_0) + q_tot e_int_v0 - (1 - q_tot) R_d T_0 (the saturation adjustment condenses
+    where q_tot exceeds saturation: the lowest kilometres and the mixed-phase levels).
+    """
+    c, m = cfg.constants, cfg.moist_constants
+    dtype = np.dtype(dtype or cfg.ft)
+    Yc, Yf = initial_state(geom, cfg, seed=seed, sigma=sigma, dtype=np.float64)
+    Nh, Nv = geom.Nh, geom.Nv
+    zc = np.broadcast_to(np.asarray(geom.zc, dtype=np.float64), (Nh, 16, Nv))
+    T, p = temperature_pressure(zc, c)
+    uidx, nu = _unique_node_index(geom.xyz)
+    noise = np.random.default_rng(seed + 1000).normal(0.0, 0.05, size=(nu, Nv))[uidx]
+    q = q0 * np.exp(-zc / scale_height) * (1.0 + noise)
+    Rm = c["R_d"] * (1.0 - q) + m["R_v"] * q
+    rho_d = Yc[:, 0]
+    rho = p / (Rm * T)
+    cvv = m["cp_v"] - m["R_v"]
+    ev0 = m["LH_v0"] - m["R_v"] * c["T_0"]
+    e_dry = c["cv_d"] * (T - c["T_0"]) - c["R_d"] * c["T_0"]
+    e_moist = (c["cv_d"] + (cvv - c["cv_d"]) * q) * (T - c["T_0"]) + q * ev0 - (1.0 - q) * c["R_d"] * c["T_0"]
+    # rho e_tot / rho of the dry state is e_int + g z + K: replace its e_int
+    spec = Yc[:, 3] / rho_d - e_dry + e_moist
+    out = np.empty((Nh, 5, 16, Nv), dtype=np.float64)
+    out[:, 0] = rho
+    out[:, 1:3] = Yc[:, 1:3]
+    out[:, 3] = rho * spec
+    out[:, 4] = rho * q
+    return np.ascontiguousarray(out.astype(dtype)), np.ascontiguousarray(Yf.astype(dtype))

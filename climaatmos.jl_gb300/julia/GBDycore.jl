@@ -75,6 +75,22 @@ struct GBConfig
     warp::Cint
     sleve_eta::Cdouble
     sleve_s::Cdouble
+    # moist 0M (microphysics_model EquilibriumMicrophysics0M): 1 adds Y.c.ρq_tot as the fifth
+    # centre component (the column hooks only); the Thermodynamics.jl constants of the moist
+    # thermodynamics and the Newton iterations of the saturation adjustment
+    moist::Cint
+    R_v::Cdouble
+    cp_v::Cdouble
+    cp_l::Cdouble
+    cp_i::Cdouble
+    LH_v0::Cdouble
+    LH_s0::Cdouble
+    T_triple::Cdouble
+    press_triple::Cdouble
+    T_freeze::Cdouble
+    T_icenuc::Cdouble
+    pow_icenuc::Cdouble
+    sa_iters::Cint
 end
 
 # A copy of cfg with the named fields replaced.
@@ -164,23 +180,25 @@ end
 """
     assert_layout(ctx, Y)
 
-The buffers handed to the library are what the header says: `Y.c` holds (ρ, uₕ, ρe_tot)
-with uₕ a 2-component covariant vector, `Y.f` holds u₃ alone, both CuArrays of the context's
-float type with ClimaCore's VIJFH parent shapes (Nv, 4, 4, 4, Nh) and (Nv + 1, 4, 4, 1, Nh).
+The buffers handed to the library are what the header says: `Y.c` holds (ρ, uₕ, ρe_tot), and
+ρq_tot last in a moist 0M context, with uₕ a 2-component covariant vector, `Y.f` holds u₃ alone,
+both CuArrays of the context's float type with ClimaCore's VIJFH parent shapes
+(Nv, 4, 4, 4 or 5, Nh) and (Nv + 1, 4, 4, 1, Nh).
 """
 function assert_layout(ctx::GBContext, Y)
     cfg = ctx.cfg
     FT = cfg.ft_bytes == 8 ? Float64 : Float32
     Nh, Nv = 6 * cfg.h_elem^2, cfg.z_elem
-    propertynames(Y.c) == (:ρ, :uₕ, :ρe_tot) ||
-        error("GBDycore: Y.c must hold (ρ, uₕ, ρe_tot), it holds $(propertynames(Y.c))")
+    names = cfg.moist == 1 ? (:ρ, :uₕ, :ρe_tot, :ρq_tot) : (:ρ, :uₕ, :ρe_tot)
+    propertynames(Y.c) == names || error("GBDycore: Y.c must hold $names, it holds $(propertynames(Y.c))")
     propertynames(Y.f) == (:u₃,) || error("GBDycore: Y.f must hold (u₃,), it holds $(propertynames(Y.f))")
     eltype(Y.c.uₕ) <: Geometry.Covariant12Vector || error("GBDycore: uₕ must be a Covariant12Vector field")
     eltype(Y.f.u₃) <: Geometry.Covariant3Vector || error("GBDycore: u₃ must be a Covariant3Vector field")
     pc, pf = parent(Y.c), parent(Y.f)
     pc isa CUDA.CuArray{FT} && pf isa CUDA.CuArray{FT} ||
         error("GBDycore: the state must be CuArrays of $FT (the context's precision)")
-    size(pc) == (Nv, 4, 4, 4, Nh) || error("GBDycore: parent(Y.c) is $(size(pc)), expected $((Nv, 4, 4, 4, Nh))")
+    nfc = ctx.cfg.moist == 1 ? 5 : 4   # (ρ, uₕ, ρe_tot[, ρq_tot])
+    size(pc) == (Nv, 4, 4, nfc, Nh) || error("GBDycore: parent(Y.c) is $(size(pc)), expected $((Nv, 4, 4, nfc, Nh))")
     size(pf) == (Nv + 1, 4, 4, 1, Nh) || error("GBDycore: parent(Y.f) is $(size(pf)), expected $((Nv + 1, 4, 4, 1, Nh))")
     return nothing
 end

@@ -168,7 +168,9 @@ struct Oracle {
   // clamped function's kink there makes plain Newton cycle between T_u and an unsaturated
   // iterate.  f increases with T, f(T_u) < 0 and f(T_b) > 0 at
   // T_b = max(T_u + q_t (e_int_v0 + e_int_i0) / cv_d, T_0) + 1; a Newton step outside the
-  // current bracket is replaced by bisection.  The partition returned is that of the final T.
+  // current bracket is replaced by bisection.  The iterations stop early once a step moves T by
+  // no more than 1e-9 K (FP64) or 1e-3 K (FP32): Newton's error after such a step is of the order
+  // of its square.  The partition returned is that of the final T.
   FT liq_frac(FT T, FT &dl) const {
     if (T > Tfrz) { dl = FT(0); return FT(1); }
     if (!(T > Tice)) { dl = FT(0); return FT(0); }
@@ -213,8 +215,11 @@ struct Oracle {
       const FT df = cvm + (T - T0) * ((cvl - cvv) * dql + (cvi - cvv) * dqi) - dqc * ev0 - dqi * ei0;
       if (f < FT(0)) lo = T;
       else hi = T;
-      const FT Tn = T - f / df;
-      T = (Tn >= lo && Tn <= hi) ? Tn : (lo + hi) / FT(2);
+      FT Tn = T - f / df;
+      if (!(Tn >= lo && Tn <= hi)) Tn = (lo + hi) / FT(2);
+      const FT dT = Tn - T;
+      T = Tn;
+      if (std::fabs(dT) <= (sizeof(FT) == 8 ? FT(1e-9) : FT(1e-3))) break;
     }
     FT dl;
     const FT lam = liq_frac(T, dl);

@@ -4,10 +4,11 @@ The centre block carries rho q_tot as its fifth component.  Each hook runs throu
 the implicit tendency (central transport of q_tot, moist pressure from the saturation
 adjustment), the post-Newton correction, the Jacobian with kappa_m and the (u_3, rho q_tot),
 (rho q_tot, u_3) blocks, and ldiv with the rho q_tot row.  Tolerances (max-norm error relative
-to each component's max magnitude): FP64 <= 1e-11 (the saturation adjustment's Newton iterations
-and the device's fused multiply-adds against the oracle's unfused arithmetic); FP32 against the
-FP32 oracle <= 1e-3 for the tendencies (the device's hardware exp/log in q_v* against the C
-library's, amplified by the pressure-gradient cancellation), and the solve to <= 1e-3."""
+to each component's max magnitude): FP64 <= 2e-12 (measured: the implicit tendency's u_3 row
+3e-13 at z_elem 12 and 6e-13 at 63, the pressure-gradient difference of two terms each ~g dz;
+every other row and ldiv <= 3e-14); FP32 against the FP32 oracle <= 1e-3 (measured: u_3's
+tendency 2.5e-4, the device's hardware exp/log in q_v* against the C library's amplified by the
+same cancellation; every other row and ldiv <= 5e-6)."""
 import numpy as np
 import pytest
 
@@ -27,7 +28,7 @@ def _assert(errs, tol):
     assert not bad, "errors above %g: %s (all: %s)" % (tol, bad, errs)
 
 
-FT_CASES = [(np.float64, 1e-11), (np.float32, 1e-3)]
+FT_CASES = [(np.float64, 2e-12), (np.float32, 1e-3)]
 
 
 @pytest.mark.parametrize("ft,tol", FT_CASES)

@@ -176,3 +176,22 @@ def test_moist_oracle_refuses_the_dry_only_operators():
         o.remaining_tendency(Yc, Yf)
     with pytest.raises(NotImplementedError):
         o.step(Yc, Yf, cfg.dt)
+
+
+def test_moist_initial_state_carries_the_profile_temperature():
+    """gbdycore.setups.moist_initial_state: at rest (K = 0) the adjustment of each point returns
+    the profile's temperature where the point is unsaturated, a warmer one (latent heat) where it
+    condenses; both kinds of point occur."""
+    from gbdycore import setups as S
+    cfg = _cfg(z_elem=20)
+    g = oracle_geometry(cfg)
+    Yc, Yf = S.moist_initial_state(g, cfg, seed=0, sigma=0.0, dtype=np.float64)
+    assert Yc.shape == (g.Nh, 5, 16, cfg.z_elem)
+    rho, q = Yc[:, 0], Yc[:, 4] / Yc[:, 0]
+    eint = Yc[:, 3] / rho - cfg.constants["grav"] * g.zc[None, None, :]
+    T, ql, qi = make_oracle(cfg).sat_adjust(rho, eint, q)
+    T_prof, _ = S.temperature_pressure(np.broadcast_to(g.zc, T.shape), cfg.constants)
+    dry = (ql + qi) == 0
+    assert dry.any() and (~dry).any()
+    assert np.abs(T[dry] - T_prof[dry]).max() < 1e-9
+    assert np.all(T[~dry] > T_prof[~dry])

@@ -4,24 +4,43 @@
 
 namespace gb {
 
+// Face slab of the flat slab kernels in shared memory: the element's four node rows j (nodes
+// 4j..4j+3, Nf faces each, as in global memory) at j * face_rows<FT>(Nf) elements.  In FP32 the
+// row stride is padded to 4 banks modulo 32, so that the four rows' threads of a warp reading
+// one node each at the eight levels of a level_slot group hit 32 distinct banks (unpadded, the
+// rows of Nf = 64 faces all start on bank 0: 4-way conflicts); FP64 keeps the global layout.
+template <class FT>
+__host__ __device__ inline int face_rows(int Nf) {
+  return sizeof(FT) == 4 ? 4 * Nf + ((4 - 4 * Nf) % 32 + 32) % 32 : 4 * Nf;
+}
+// element index of (node n, face k) in that slab; FR = face_rows<FT>(Nf)
+__host__ __device__ inline int fslot(int n, int k, int Nf, int FR) { return (n >> 2) * FR + (n & 3) * Nf + k; }
+
 // Shared-memory layouts of the element-slab kernels (byte offsets).  The
 // input slabs are double-buffered (nbuf = 2) when they fit, else single.
+// Pass A's output slab is double-buffered with its inputs: the store of one element's
+// Laplacians then reads its slab while the next element is computed into the other.
 template <class FT>
 struct PassALayout {
-  size_t y[2], f[2], g[2], out, bar, total;
+  size_t y[2], f[2], g[2], out[2], bar, total;
   __host__ __device__ PassALayout(int Nv, int nbuf) {
     const int Nf = Nv + 1;
     size_t o = 0;
     for (int b = 0; b < 2; ++b) {
       if (b < nbuf) {
         y[b] = o; o += align16(sizeof(FT) * 64 * Nv);
-        f[b] = o; o += align16(sizeof(FT) * 16 * Nf);
+        f[b] = o; o += align16(sizeof(FT) * 4 * face_rows<FT>(Nf));
         g[b] = o; o += align16(sizeof(FT) * HG_N * 16);
       } else {
         y[b] = y[0]; f[b] = f[0]; g[b] = g[0];
       }
     }
-    out = o; o += align16(sizeof(FT) * 64 * Nv);
+    out[0] = o; o += align16(sizeof(FT) * 64 * Nv);
+    if (nbuf == 2) {
+      out[1] = o; o += align16(sizeof(FT) * 64 * Nv);
+    } else {
+      out[1] = out[0];
+    }
     bar = o; o += 16;
     total = o;
   }
@@ -44,7 +63,7 @@ struct PassBLayout {
     for (int b = 0; b < 2; ++b) {
       if (b < nbuf) {
         y[b] = o; o += align16(sizeof(FT) * 64 * Nv);
-        f[b] = o; o += align16(sizeof(FT) * 16 * Nf);
+        f[b] = o; o += align16(sizeof(FT) * 4 * face_rows<FT>(Nf));
         g[b] = o; o += align16(sizeof(FT) * HG_N * 16);
         lap[b] = o; o += align16(sizeof(FT) * 64 * Nv);
       } else {

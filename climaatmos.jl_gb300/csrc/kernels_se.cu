@@ -32,6 +32,23 @@ using namespace se;
 constexpr int SE_THREADS = 256;          // 64 level slots x 4 rows per sweep
 constexpr int SE_LEVELS = SE_THREADS / 4;
 
+// The element's face block (16 nodes x Nf faces) into the padded face slab: one TMA copy per node
+// row j (4 Nf elements: a multiple of 16 bytes at 16-byte aligned addresses on both sides).
+template <class FT>
+__device__ __forceinline__ void load_faces(FT *sF, const FT *Yf, int e, int Nf, uint64_t *bar) {
+  const int FR = face_rows<FT>(Nf);
+  const uint32_t b4 = uint32_t(sizeof(FT) * 4 * Nf);
+#pragma unroll
+  for (int j = 0; j < NQ; ++j) tma_load(sF + (size_t)j * FR, Yf + ((size_t)e * 16 + 4 * j) * Nf, b4, bar);
+}
+template <class FT>
+__device__ __forceinline__ void store_faces(FT *Yf, const FT *sF, int e, int Nf) {
+  const int FR = face_rows<FT>(Nf);
+  const uint32_t b4 = uint32_t(sizeof(FT) * 4 * Nf);
+#pragma unroll
+  for (int j = 0; j < NQ; ++j) tma_store(Yf + ((size_t)e * 16 + 4 * j) * Nf, sF + (size_t)j * FR, b4);
+}
+
 // TMA loads of one element's input slabs into buffer set b (thread 0 only).
 template <class FT>
 __device__ __forceinline__ void issue_slab(const DevParams<FT> &P, uint64_t *bar, int e, FT *sY, FT *sF, FT *sG,
@@ -41,7 +58,7 @@ __device__ __forceinline__ void issue_slab(const DevParams<FT> &P, uint64_t *bar
   const uint32_t bg = uint32_t(sizeof(FT) * HG_N * 16);
   mbar_expect_tx(bar, by + bf + bg + (sL ? by : 0u));
   tma_load(sY, Yc + (size_t)e * 64 * Nv, by, bar);
-  tma_load(sF, Yf + (size_t)e * 16 * Nf, bf, bar);
+  load_faces(sF, Yf, e, Nf, bar);
   tma_load(sG, P.hgeo + (size_t)e * HG_N * 16, bg, bar);
   if (sL) tma_load(sL, Lin + (size_t)e * 64 * Nv, by, bar);
 }
@@ -78,7 +95,10 @@ __device__ __forceinline__ bool begin_element(const DevParams<FT> &P, uint64_t *
     } else if (it > 0) {
       issue_slab<FT>(P, &bar[0], e, sY[0], sF[0], sG[0], withL ? sL[0] : nullptr, Yc, Yf, Lin);
     }
-    tma_store_wait_read();
+    // the output slab this element writes was last stored two elements ago (double-buffered
+    // output) or by the previous element
+    if (nbuf == 2) tma_store_wait_read_1();
+    else tma_store_wait_read();
   }
   const uint32_t parity = nbuf == 2 ? ((it >> 1) & 1) : (it & 1);
   const bool ok = mbar_wait_bounded(pick(b, &bar[0], &bar[1]), parity, P.status);
@@ -93,12 +113,12 @@ __global__ void __launch_bounds__(SE_THREADS, MB) k_passA(DevParams<FT> P, int n
                                                          const FT *__restrict__ Yf, FT *__restrict__ Lout) {
   extern __shared__ __align__(128) unsigned char sm[];
   const int Nv = P.Nv;
-  const int Nf = P.Nf;
+  const int Nf = P.Nf, FR = face_rows<FT>(Nf);
   const PassALayout<FT> Lo(Nv, nbuf);
   FT *sYb[2] = {(FT *)(sm + Lo.y[0]), (FT *)(sm + Lo.y[1])};
   FT *sFb[2] = {(FT *)(sm + Lo.f[0]), (FT *)(sm + Lo.f[1])};
   FT *sGb[2] = {(FT *)(sm + Lo.g[0]), (FT *)(sm + Lo.g[1])};
-  FT *sO = (FT *)(sm + Lo.out);
+  FT *sOb[2] = {(FT *)(sm + Lo.out[0]), (FT *)(sm + Lo.out[1])};
   uint64_t *bar = (uint64_t *)(sm + Lo.bar);
   init_bars(bar);
   int e = blockIdx.x;
@@ -110,6 +130,7 @@ __global__ void __launch_bounds__(SE_THREADS, MB) k_passA(DevParams<FT> P, int n
     int b;
     if (!begin_element<FT>(P, bar, nbuf, it, e, sYb, sFb, sGb, sGb, false, Yc, Yf, nullptr, b)) break;
     const FT *sY = pick(b, sYb[0], sYb[1]), *sF = pick(b, sFb[0], sFb[1]), *sG = pick(b, sGb[0], sGb[1]);
+    FT *sO = pick(b, sOb[0], sOb[1]);
     RowGeo<FT> g;
     g.load(sG, P, j);
     for (int v0 = 0; v0 < Nv; v0 += SE_LEVELS) {
@@ -132,8 +153,8 @@ __global__ void __launch_bounds__(SE_THREADS, MB) k_passA(DevParams<FT> P, int n
           u1[i] = sY[16 * Nv + q];
           u2[i] = sY[32 * Nv + q];
           // u_3 of the faces below and above (0 on the boundary faces)
-          fa[i] = v == 0 ? FT(0) : sF[n * Nf + v];
-          fb[i] = v + 1 == Nv ? FT(0) : sF[n * Nf + v + 1];
+          fa[i] = v == 0 ? FT(0) : sF[fslot(n, v, Nf, FR)];
+          fb[i] = v + 1 == Nv ? FT(0) : sF[fslot(n, v + 1, Nf, FR)];
         }
         // u_bar_3 = I^c(u_3); CT12(u_h) with the level's g^ij = r^-2 g^ij(surface); K
         vadd(fa, fb, ub3);
@@ -201,17 +222,21 @@ struct alignas(16) V16 {
 };
 
 // out = U + c_3 T + sum_j c_j T_j over one slab of n values in 16-byte vectors
-// (T in shared memory, overwritten; U and the T_j at offset off in global memory).
+// (T in shared memory, overwritten; U and the T_j at offset off in global memory).  Vector i
+// of the slab sits at shared-memory vector i + (i / rowv) padv: the padded face slab (rowv
+// vectors per node row, padv vectors of padding after each); rowv = n / E, padv = 0 for the
+// unpadded centre slab.
 template <class FT>
 __device__ __forceinline__ void fin_combine(FT *sT, const FT *U, const FT *const (&Tj)[3], const FinArgs<FT> &F,
-                                            size_t off, int n) {
+                                            size_t off, int n, int rowv, int padv) {
   constexpr int E = 16 / sizeof(FT);
   V16<FT> *s = reinterpret_cast<V16<FT> *>(sT);
   const V16<FT> *u = reinterpret_cast<const V16<FT> *>(U + off);
 #pragma unroll 2
   for (int i = threadIdx.x; i < n / E; i += SE_THREADS) {
     V16<FT> r = u[i];
-    const V16<FT> t = s[i];
+    const int si = i + (i / rowv) * padv;
+    const V16<FT> t = s[si];
 #pragma unroll
     for (int k = 0; k < E; ++k) r.v[k] += F.c[3] * t.v[k];
 #pragma unroll
@@ -221,7 +246,7 @@ __device__ __forceinline__ void fin_combine(FT *sT, const FT *U, const FT *const
 #pragma unroll
         for (int k = 0; k < E; ++k) r.v[k] += F.c[q] * a.v[k];
       }
-    s[i] = r;
+    s[si] = r;
   }
 }
 
@@ -234,7 +259,7 @@ __global__ void __launch_bounds__(SE_THREADS, MB) k_passB(DevParams<FT> P, int n
                                                          const FT *__restrict__ Yf, const FT *__restrict__ Lin,
                                                          FT *__restrict__ Tc, FT *__restrict__ Tf, FinArgs<FT> F) {
   extern __shared__ __align__(128) unsigned char sm[];
-  const int Nv = P.Nv, Nf = P.Nf;
+  const int Nv = P.Nv, Nf = P.Nf, FR = face_rows<FT>(Nf);
   const PassBLayout<FT> Lo(Nv, nbuf);
   auto at = [&](const size_t (&off)[2], int b) { return (FT *)(sm + (b ? off[1] : off[0])); };
   FT *sS = (FT *)(sm + Lo.s), *sX1 = (FT *)(sm + Lo.x1), *sX2 = (FT *)(sm + Lo.x2), *sW = (FT *)(sm + Lo.w);
@@ -245,7 +270,7 @@ __global__ void __launch_bounds__(SE_THREADS, MB) k_passB(DevParams<FT> P, int n
     uint64_t *bb = b ? &bar[1] : &bar[0];
     mbar_expect_tx(bb, 2 * by + bf + bg);
     tma_load(at(Lo.y, b), Yc + (size_t)e * 64 * Nv, by, bb);
-    tma_load(at(Lo.f, b), Yf + (size_t)e * 16 * Nf, bf, bb);
+    load_faces(at(Lo.f, b), Yf, e, Nf, bb);
     tma_load(at(Lo.g, b), P.hgeo + (size_t)e * HG_N * 16, bg, bb);
     tma_load(at(Lo.lap, b), Lin + (size_t)e * 64 * Nv, by, bb);
   };
@@ -262,8 +287,21 @@ __global__ void __launch_bounds__(SE_THREADS, MB) k_passB(DevParams<FT> P, int n
   Row<FT> R;
   R.init(P, j);
   for (int it = 0; e < P.Nh; ++it, e += gridDim.x) {
-    int b;
-    if (!slab_begin(bar, nbuf, it, e, P.Nh, P.status, issue, b)) break;
+    // Double-buffered, the next element's slabs go into the buffer that holds the previous
+    // element's tendency until that element's store has read it: the prefetch is issued after
+    // the centre phase (below), when the store has long finished, rather than here, where
+    // waiting for the store would hold every thread.  Single-buffered, this element's slabs are
+    // loaded here once the store has read the buffer (the first before the loop).
+    const int b = nbuf == 2 ? (it & 1) : 0;
+    if (threadIdx.x == 0 && nbuf != 2) {
+      tma_store_wait_read();
+      if (it > 0) issue(0, e);
+    }
+    {
+      const uint32_t parity = nbuf == 2 ? ((it >> 1) & 1) : (it & 1);
+      const bool ok = mbar_wait_bounded(b ? &bar[1] : &bar[0], parity, P.status);
+      if (!__syncthreads_and(ok)) break;
+    }
     if (FIN && threadIdx.x == 0) {
       // the final combination's other operands, into L2 while the tendency is computed
       bulk_prefetch_l2(Yc + (size_t)e * 64 * Nv, by);
@@ -315,8 +353,8 @@ __global__ void __launch_bounds__(SE_THREADS, MB) k_passB(DevParams<FT> P, int n
             u2[i] = sY[32 * Nv + q];
             rhoe[i] = sY[48 * Nv + q];
             // u_3 of the faces below and above (0 on the boundary faces)
-            fa[i] = v == 0 ? FT(0) : sF[n * Nf + v];
-            fb[i] = v + 1 == Nv ? FT(0) : sF[n * Nf + v + 1];
+            fa[i] = v == 0 ? FT(0) : sF[fslot(n, v, Nf, FR)];
+            fb[i] = v + 1 == Nv ? FT(0) : sF[fslot(n, v + 1, Nf, FR)];
           }
           // CT12(u_h) = g^ij u_j with the level's g^ij = r^-2 g^ij(surface)
           g.gu(gu0, gu1, gu2);
@@ -493,10 +531,17 @@ __global__ void __launch_bounds__(SE_THREADS, MB) k_passB(DevParams<FT> P, int n
       }
     }
     __syncthreads();
+    if (threadIdx.x == 0 && nbuf == 2) {
+      tma_store_wait_read();
+      const int en = e + (int)gridDim.x;
+      if (en < P.Nh) issue(b ^ 1, en);
+    }
     // ---- P2: face-level work (f^12 + w^12, cross products, u_3 tendency)
     for (int k0 = 0; k0 < Nf; k0 += SE_LEVELS) {
-      const int k = min(k0 + vl, Nf - 1);
-      const bool act = k0 + vl < Nf;
+      // faces in level_slot order, as the centre levels: the face slab reads are then free of
+      // bank conflicts (its padded rows) and so are the row-vector scratch accesses
+      const int k = min(k0 + vs, Nf - 1);
+      const bool act = k0 + vs < Nf;
       const bool inner = k > 0 && k < Nv;
       const FT r2 = P.levf[LF_R2 * Nf + k], dzf = P.levf[LF_DZ * Nf + k], rinv = P.levf[LF_RINV * Nf + k];
       const FT ir2f = P.levf[LF_IR2 * Nf + k], idzf = P.levf[LF_IDZ * Nf + k], g33 = P.levf[LF_G33 * Nf + k];
@@ -506,7 +551,7 @@ __global__ void __launch_bounds__(SE_THREADS, MB) k_passB(DevParams<FT> P, int n
         g.w(W);
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
-          u3[i] = inner ? sF[(NQ * j + i) * Nf + k] : FT(0);
+          u3[i] = inner ? sF[j * FR + i * Nf + k] : FT(0);
           Wu[i] = W[i] * u3[i];
         }
       }
@@ -599,7 +644,7 @@ __global__ void __launch_bounds__(SE_THREADS, MB) k_passB(DevParams<FT> P, int n
         vmul(Jf, X2, X2);
         vmuls(X2, FT(-1), X2);
 #pragma unroll
-        for (int i = 0; i < 4; ++i) sOf[(NQ * j + i) * Nf + k] = T3[i];
+        for (int i = 0; i < 4; ++i) sOf[j * FR + i * Nf + k] = T3[i];
         st_row(sX1 + (size_t)k * NN + NQ * j, X1);
         st_row(sX2 + (size_t)k * NN + NQ * j, X2);
       }
@@ -636,17 +681,18 @@ __global__ void __launch_bounds__(SE_THREADS, MB) k_passB(DevParams<FT> P, int n
     }
     if (FIN) {
       __syncthreads();
-      fin_combine<FT>(sO, Yc, F.te_c, F, (size_t)e * 64 * Nv, 64 * Nv);
-      fin_combine<FT>(sOf, Yf, F.te_f, F, (size_t)e * 16 * Nf, 16 * Nf);
+      constexpr int E = 16 / sizeof(FT);
+      fin_combine<FT>(sO, Yc, F.te_c, F, (size_t)e * 64 * Nv, 64 * Nv, 64 * Nv / E, 0);
+      fin_combine<FT>(sOf, Yf, F.te_f, F, (size_t)e * 16 * Nf, 16 * Nf, 4 * Nf / E, (FR - 4 * Nf) / E);
       __syncthreads();
       // impenetrable filter: u_3 = 0 on the bottom and top faces (thread t < 32: node t / 2)
-      if (threadIdx.x < 32) sOf[(threadIdx.x >> 1) * Nf + ((threadIdx.x & 1) ? Nv : 0)] = FT(0);
+      if (threadIdx.x < 32) sOf[fslot(threadIdx.x >> 1, (threadIdx.x & 1) ? Nv : 0, Nf, FR)] = FT(0);
     }
     fence_proxy_async();
     __syncthreads();
     if (threadIdx.x == 0) {
       tma_store(Tc + (size_t)e * 64 * Nv, sO, by);
-      tma_store(Tf + (size_t)e * 16 * Nf, sOf, bf);
+      store_faces(Tf, sOf, e, Nf);
       tma_store_commit();
     }
   }

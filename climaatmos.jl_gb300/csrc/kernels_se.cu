@@ -287,21 +287,10 @@ __global__ void __launch_bounds__(SE_THREADS, MB) k_passB(DevParams<FT> P, int n
   Row<FT> R;
   R.init(P, j);
   for (int it = 0; e < P.Nh; ++it, e += gridDim.x) {
-    // Double-buffered, the next element's slabs go into the buffer that holds the previous
-    // element's tendency until that element's store has read it: the prefetch is issued after
-    // the centre phase (below), when the store has long finished, rather than here, where
-    // waiting for the store would hold every thread.  Single-buffered, this element's slabs are
-    // loaded here once the store has read the buffer (the first before the loop).
-    const int b = nbuf == 2 ? (it & 1) : 0;
-    if (threadIdx.x == 0 && nbuf != 2) {
-      tma_store_wait_read();
-      if (it > 0) issue(0, e);
-    }
-    {
-      const uint32_t parity = nbuf == 2 ? ((it >> 1) & 1) : (it & 1);
-      const bool ok = mbar_wait_bounded(b ? &bar[1] : &bar[0], parity, P.status);
-      if (!__syncthreads_and(ok)) break;
-    }
+    // the tendency overwrites this element's slabs: the next element is prefetched after the
+    // centre phase (slab_prefetch below)
+    int b;
+    if (!slab_begin_deferred(bar, nbuf, it, e, P.status, issue, b)) break;
     if (FIN && threadIdx.x == 0) {
       // the final combination's other operands, into L2 while the tendency is computed
       bulk_prefetch_l2(Yc + (size_t)e * 64 * Nv, by);
@@ -531,11 +520,7 @@ __global__ void __launch_bounds__(SE_THREADS, MB) k_passB(DevParams<FT> P, int n
       }
     }
     __syncthreads();
-    if (threadIdx.x == 0 && nbuf == 2) {
-      tma_store_wait_read();
-      const int en = e + (int)gridDim.x;
-      if (en < P.Nh) issue(b ^ 1, en);
-    }
+    slab_prefetch(nbuf, b, e, P.Nh, issue);
     // ---- P2: face-level work (f^12 + w^12, cross products, u_3 tendency)
     for (int k0 = 0; k0 < Nf; k0 += SE_LEVELS) {
       // faces in level_slot order, as the centre levels: the face slab reads are then free of

@@ -641,5 +641,32 @@ __device__ __forceinline__ bool slab_begin(uint64_t *bar, int nbuf, int it, int 
   return __syncthreads_and(ok) != 0;
 }
 
+// slab_begin for the kernels whose tendency overwrites their own input slabs and whose first
+// phase is long enough to cover the next element's loads: double-buffered, the prefetch of the
+// next element (into the buffer holding the previous element's output until that element's
+// store has read it) is left to slab_prefetch, called after that first phase, when the store has
+// long finished, instead of holding every thread at the start while the store reads.
+// Single-buffered, as slab_begin.
+template <class Issue>
+__device__ __forceinline__ bool slab_begin_deferred(uint64_t *bar, int nbuf, int it, int e, int *status,
+                                                    const Issue &issue, int &b) {
+  b = nbuf == 2 ? (it & 1) : 0;
+  if (threadIdx.x == 0 && nbuf != 2) {
+    tma_store_wait_read();
+    if (it > 0) issue(0, e);
+  }
+  const uint32_t parity = nbuf == 2 ? ((it >> 1) & 1) : (it & 1);
+  const bool ok = mbar_wait_bounded(b ? &bar[1] : &bar[0], parity, status);
+  return __syncthreads_and(ok) != 0;
+}
+template <class Issue>
+__device__ __forceinline__ void slab_prefetch(int nbuf, int b, int e, int Nh, const Issue &issue) {
+  if (threadIdx.x == 0 && nbuf == 2) {
+    tma_store_wait_read();
+    const int en = e + (int)gridDim.x;
+    if (en < Nh) issue(b ^ 1, en);
+  }
+}
+
 }  // namespace se
 }  // namespace gb

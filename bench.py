@@ -573,6 +573,16 @@ def measure_adjoint(args, s, fwd_ms):
     _, Ybar1 = lg(Y1)
     d1 = (ctypes.c_double * 2)()
     p_ms, _ = _timed(lambda: s.p.call("gb_adjoint_reverse", Ybar1.gb(), d1, None))
+    # the same reverse pass with the stage data of both segments kept by the forward half
+    # (gb_adjoint_set_record_segments(ctx, 2)): no recompute, the same gradient
+    s.p.call("gb_adjoint_set_record_segments", 2)
+    Y2 = Y0.copy()
+    s.p.call("gb_adjoint_forward", Y2.gb(), 0.0, float(s.dt), n, 5)
+    _, Ybar2 = lg(Y2)
+    d2 = (ctypes.c_double * 2)()
+    r2_ms, _ = _timed(lambda: s.p.call("gb_adjoint_reverse", Ybar2.gb(), d2, None))
+    same = bool(torch.equal(Ybar2.c, Ybar.c) and torch.equal(Ybar2.f, Ybar.f))
+    s.p.call("gb_adjoint_set_record_segments", 1)
     # per-kernel times of the reverse kernels (CUDA events inside the library)
     kern = {}
     for kid, name, per_step in REVERSE_KERNELS:
@@ -586,7 +596,9 @@ def measure_adjoint(args, s, fwd_ms):
             "what": "reverse = per-segment recompute (1 forward step per step, stage data kept; the last "
                     "segment is recorded by the checkpointed forward pass) + reverse kernels; ratio against "
                     "the graph-replayed forward step",
-            "dJ_dnu": d[0], "dJ_drate": d[1], "library_bytes": int(peak.value), "finite": finite}
+            "dJ_dnu": d[0], "dJ_drate": d[1], "library_bytes": int(peak.value), "finite": finite,
+            "segments_kept_2": {"reverse_ms_per_step": r2_ms / n, "adjoint_over_forward": (r2_ms / n) / fwd_ms,
+                                "same_gradient_bitwise": same}}
 
 
 def max_horizontal_wind(s):

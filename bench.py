@@ -943,23 +943,24 @@ def measure_precision_h60(args):
                                "library_bytes": int(peak.value),
                                "device_bytes_in_use_after_reverse": int(total - free1),
                                "finite": bool(torch.isfinite(Ybar.c).all() and torch.isfinite(Ybar.f).all())}
-    # HBM for recomputation: the forward half keeps the stage data of the last two segments,
-    # so the pullback recomputes two of the four (gb_adjoint_set_record_segments)
-    s32.p.call("gb_adjoint_set_record_segments", 2)
-    Y = Y0.copy()
-    s32.p.call("gb_adjoint_forward", Y.gb(), 0.0, float(cfg.dt), 20, 5)   # allocates the extra records
-    J, Ybar2 = lg(Y)
-    s32.p.call("gb_adjoint_reverse", Ybar2.gb(), d, ctypes.byref(peak))
-    Y = Y0.copy()
-    fwd2, _ = _timed(lambda: s32.p.call("gb_adjoint_forward", Y.gb(), 0.0, float(cfg.dt), 20, 5))
-    J, Ybar2 = lg(Y)
-    rev2, _ = _timed(lambda: s32.p.call("gb_adjoint_reverse", Ybar2.gb(), d, ctypes.byref(peak)))
-    free2, _ = torch.cuda.mem_get_info()
-    out["adjoint_20_steps_two_segments_kept"] = {
-        "checkpoint_every": 5, "record_segments": 2, "forward_ms": fwd2, "reverse_ms": rev2,
-        "reverse_over_forward_steps": rev2 / ms, "library_bytes": int(peak.value),
-        "device_bytes_in_use_after_reverse": int(total - free2),
-        "same_gradient_as_one_kept": bool(torch.equal(Ybar.c, Ybar2.c) and torch.equal(Ybar.f, Ybar2.f))}
+    # HBM for recomputation: the forward half keeps the stage data of the last K segments, so
+    # the pullback recomputes 4 - K of the four (gb_adjoint_set_record_segments)
+    for K, key in ((2, "adjoint_20_steps_two_segments_kept"), (3, "adjoint_20_steps_three_segments_kept")):
+        s32.p.call("gb_adjoint_set_record_segments", K)
+        Y = Y0.copy()
+        s32.p.call("gb_adjoint_forward", Y.gb(), 0.0, float(cfg.dt), 20, 5)   # allocates the extra records
+        J, Ybar2 = lg(Y)
+        s32.p.call("gb_adjoint_reverse", Ybar2.gb(), d, ctypes.byref(peak))
+        Y = Y0.copy()
+        fwd2, _ = _timed(lambda: s32.p.call("gb_adjoint_forward", Y.gb(), 0.0, float(cfg.dt), 20, 5))
+        J, Ybar2 = lg(Y)
+        rev2, _ = _timed(lambda: s32.p.call("gb_adjoint_reverse", Ybar2.gb(), d, ctypes.byref(peak)))
+        free2, _ = torch.cuda.mem_get_info()
+        out[key] = {
+            "checkpoint_every": 5, "record_segments": K, "forward_ms": fwd2, "reverse_ms": rev2,
+            "reverse_over_forward_steps": rev2 / ms, "library_bytes": int(peak.value),
+            "device_bytes_in_use_after_reverse": int(total - free2),
+            "same_gradient_as_one_kept": bool(torch.equal(Ybar.c, Ybar2.c) and torch.equal(Ybar.f, Ybar2.f))}
     s32.p.call("gb_adjoint_set_record_segments", 1)
     return out
 

@@ -92,6 +92,96 @@ struct TopoBLayout {
   }
 };
 
+// Row helpers of the terrain kernels: the arithmetic over the row's four nodes goes through the
+// vector helpers (two nodes per packed instruction in FP32).
+template <class FT>
+__device__ __forceinline__ void vbc(FT c, FT (&o)[4]) {
+#pragma unroll
+  for (int i = 0; i < 4; ++i) o[i] = c;
+}
+template <class FT>
+__device__ __forceinline__ void vrcp(const FT (&a)[4], FT (&o)[4]) {
+#pragma unroll
+  for (int i = 0; i < 4; ++i) o[i] = grcp(a[i]);
+}
+// thermo() for the row's nodes, each with its own geopotential Phi[i], on the level with the
+// reference record rl (FP32: two nodes at a time)
+template <class FT>
+__device__ __forceinline__ void thermo_row_pt(const DevParams<FT> &P, const FT (&rho)[4], const FT (&rhoe)[4],
+                                              const FT (&K)[4], const FT (&Phi)[4], const Lev4<FT> &rl,
+                                              ThermoRow<FT> &o) {
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    Thermo<FT> th;
+    thermo(P, rho[i], rhoe[i], K[i], Phi[i], rl, th);
+    o.T[i] = th.T; o.p[i] = th.p; o.h[i] = th.h; o.Pi[i] = th.Pi;
+    o.thv[i] = th.thv; o.thvr[i] = th.thvr; o.phid[i] = th.phid; o.Tr[i] = th.Tr;
+  }
+}
+__device__ __forceinline__ void thermo_row_pt(const DevParams<float> &P, const float (&rho)[4], const float (&rhoe)[4],
+                                              const float (&K)[4], const float (&Phi)[4], const Lev4<float> &rl,
+                                              ThermoRow<float> &o) {
+  float2 T[2], p[2], h[2], Pi[2], thv[2], thvr[2], phid[2], Tr[2];
+  const float2 ip0 = bc2(rl.y), rz = bc2(rl.z);
+  thermo_pair(P, lo2(rho), lo2(rhoe), lo2(K), lo2(Phi), ip0, rz, T[0], p[0], h[0], Pi[0], thv[0], thvr[0], phid[0], Tr[0]);
+  thermo_pair(P, hi2(rho), hi2(rhoe), hi2(K), hi2(Phi), ip0, rz, T[1], p[1], h[1], Pi[1], thv[1], thvr[1], phid[1], Tr[1]);
+  put2(T[0], T[1], o.T); put2(p[0], p[1], o.p); put2(h[0], h[1], o.h); put2(Pi[0], Pi[1], o.Pi);
+  put2(thv[0], thv[1], o.thv); put2(thvr[0], thvr[1], o.thvr); put2(phid[0], phid[1], o.phid); put2(Tr[0], Tr[1], o.Tr);
+}
+
+// The point terms of the row's nodes on the level with warp record L: z_s b, height z, 1/r, r^2,
+// 1/r^2, layer thickness dz, 1/dz and the slopes s_a (tpoint, four nodes).
+template <class FT>
+struct TPoint4 {
+  FT zsb[4], z[4], ir[4], r2[4], ir2[4], dz[4], idz[4], s1[4], s2[4];
+};
+template <class FT>
+__device__ __forceinline__ void tpoint4(const DevParams<FT> &P, const FT (&zs)[4], const FT (&d1)[4], const FT (&d2)[4],
+                                        const Lev4<FT> &L, TPoint4<FT> &t) {
+  FT a[4], r[4];
+  vmuls(zs, L.y, t.zsb);
+  vbc(L.x, a);
+  vadd(a, t.zsb, t.z);
+  vbc(FT(1), a);
+  vfmas(t.z, P.iR, a, r);
+  vrcp(r, t.ir);
+  vmul(r, r, t.r2);
+  vmul(t.ir, t.ir, t.ir2);
+  vbc(L.z, a);
+  vfmas(zs, L.w, a, t.dz);
+  vrcp(t.dz, t.idz);
+  vmuls(d1, L.y, t.s1);
+  vmuls(d2, L.y, t.s2);
+}
+// the contravariant metric g^ij (tmetric_up, four nodes) from the surface g_s^ab
+template <class FT>
+__device__ __forceinline__ void tmetric_up4(const TPoint4<FT> &t, const FT (&a0)[4], const FT (&a1)[4],
+                                            const FT (&a2)[4], FT (&g11)[4], FT (&g12)[4], FT (&g22)[4],
+                                            FT (&g13)[4], FT (&g23)[4], FT *g33) {
+  FT h1[4], h2[4], x[4];
+  vmul(a0, t.ir2, g11);
+  vmul(a1, t.ir2, g12);
+  vmul(a2, t.ir2, g22);
+  vmul(g12, t.s2, x);
+  vfma(g11, t.s1, x, h1);
+  vmul(g22, t.s2, x);
+  vfma(g12, t.s1, x, h2);
+  vmul(h1, t.idz, g13);
+  vmuls(g13, FT(-1), g13);
+  vmul(h2, t.idz, g23);
+  vmuls(g23, FT(-1), g23);
+  if (g33) {
+    FT one[4], q[4], i2[4], o[4];
+    vbc(FT(1), one);
+    vfma(t.s1, h1, one, q);
+    vfma(t.s2, h2, q, q);
+    vmul(t.idz, t.idz, i2);
+    vmul(q, i2, o);
+#pragma unroll
+    for (int i = 0; i < 4; ++i) g33[i] = o[i];
+  }
+}
+
 // The geometry of the thread's row (4 nodes) at one centre level.
 template <class FT>
 struct TRow {
@@ -116,16 +206,18 @@ __device__ __forceinline__ void trow_cov(const DevParams<FT> &P, const FT *sG, c
   ld_row(sT + TG_ZS * NN + NQ * j, zs);
   ld_row(sT + TG_D1 * NN + NQ * j, e1);
   ld_row(sT + TG_D2 * NN + NQ * j, e2);
-#pragma unroll
-  for (int i = 0; i < 4; ++i) {
-    const TPoint<FT> t = tpoint(P, zs[i], e1[i], e2[i], L);
-    o.d11[i] = t.r2 * b0[i] + t.s1 * t.s1;
-    o.d12[i] = t.r2 * b1[i] + t.s1 * t.s2;
-    o.d22[i] = t.r2 * b2[i] + t.s2 * t.s2;
-    o.d13[i] = t.s1 * t.dz;
-    o.d23[i] = t.s2 * t.dz;
-    o.d33[i] = t.dz * t.dz;
-  }
+  TPoint4<FT> t;
+  tpoint4(P, zs, e1, e2, L, t);
+  FT x[4];
+  vmul(t.s1, t.s1, x);
+  vfma(t.r2, b0, x, o.d11);
+  vmul(t.s1, t.s2, x);
+  vfma(t.r2, b1, x, o.d12);
+  vmul(t.s2, t.s2, x);
+  vfma(t.r2, b2, x, o.d22);
+  vmul(t.s1, t.dz, o.d13);
+  vmul(t.s2, t.dz, o.d23);
+  vmul(t.dz, t.dz, o.d33);
 }
 
 // Node rows of the element slab: sG the horizontal geometry, sT the terrain, sW = (W, 1/W).
@@ -141,22 +233,23 @@ __device__ __forceinline__ void trow_centre(const DevParams<FT> &P, const FT *sG
   ld_row(sT + TG_D1 * NN + NQ * j, e1);
   ld_row(sT + TG_D2 * NN + NQ * j, e2);
   ld_row(sW + NQ * j, W);
+  TPoint4<FT> t;
+  tpoint4(P, zs, e1, e2, L, t);
+  tmetric_up4(t, a0, a1, a2, o.u11, o.u12, o.u22, o.u13, o.u23, (FT *)nullptr);
+  vmul(Jh, t.r2, o.J);
+  vmul(o.J, t.dz, o.J);
+  vrcp(o.J, o.iJ);
+  vmul(W, o.J, o.WJ);
+  vrcp(o.WJ, o.iWJ);
 #pragma unroll
   for (int i = 0; i < 4; ++i) {
-    const TPoint<FT> t = tpoint(P, zs[i], e1[i], e2[i], L);
-    const TMetricUp<FT> m = tmetric_up(t, a0[i], a1[i], a2[i]);
-    o.J[i] = Jh[i] * t.r2 * t.dz;
-    o.iJ[i] = grcp(o.J[i]);
-    o.WJ[i] = W[i] * o.J[i];
-    o.iWJ[i] = grcp(o.WJ[i]);
-    o.u11[i] = m.g11; o.u12[i] = m.g12; o.u22[i] = m.g22; o.u13[i] = m.g13; o.u23[i] = m.g23;
-    o.z[i] = t.z;
-    o.zsb[i] = t.zsb;
-    o.ir[i] = t.ir;
-    o.s1i[i] = t.s1 * t.idz;
-    o.s2i[i] = t.s2 * t.idz;
-    o.idz[i] = t.idz;
+    o.z[i] = t.z[i];
+    o.zsb[i] = t.zsb[i];
+    o.ir[i] = t.ir[i];
+    o.idz[i] = t.idz[i];
   }
+  vmul(t.s1, t.idz, o.s1i);
+  vmul(t.s2, t.idz, o.s2i);
 }
 
 // g^33 of the row's nodes on a face with warp record L (and, optionally, J, 1/J, 1/r).
@@ -171,14 +264,19 @@ __device__ __forceinline__ void trow_face(const DevParams<FT> &P, const FT *sG, 
   ld_row(sT + TG_D1 * NN + NQ * j, e1);
   ld_row(sT + TG_D2 * NN + NQ * j, e2);
   if (J) ld_row(sG + HG_JH * NN + NQ * j, Jh);
+  TPoint4<FT> t;
+  tpoint4(P, zs, e1, e2, L, t);
+  FT g11[4], g12[4], g22[4], g13[4], g23[4];
+  tmetric_up4(t, a0, a1, a2, g11, g12, g22, g13, g23, g33);
+  if (J) {
+    FT x[4];
+    vmul(Jh, t.r2, x);
+    vmul(x, t.dz, x);
 #pragma unroll
-  for (int i = 0; i < 4; ++i) {
-    const TPoint<FT> t = tpoint(P, zs[i], e1[i], e2[i], L);
-    g33[i] = tmetric_up(t, a0[i], a1[i], a2[i]).g33;
-    if (J) {
-      J[i] = Jh[i] * t.r2 * t.dz;
-      iJ[i] = grcp(J[i]);
-      ir[i] = t.ir;
+    for (int i = 0; i < 4; ++i) {
+      J[i] = x[i];
+      iJ[i] = grcp(x[i]);
+      ir[i] = t.ir[i];
     }
   }
 }
@@ -202,16 +300,20 @@ __device__ __forceinline__ void tvec_lap(const DevParams<FT> &P, const Row<FT> &
                                          const FT *sT, int j, const Lev4<FT> &L, const FT (&W)[4], const FT (&iW)[4],
                                          const FT (&c1)[4], const FT (&c2)[4], const FT (&c3)[4], FT fdiv,
                                          FT (&o1)[4], FT (&o2)[4], FT (&o3)[4]) {
-  FT a[4], b[4], da[4], db[4], w1[4], w2[4];
-#pragma unroll
-  for (int i = 0; i < 4; ++i) {
-    a[i] = G.J[i] * (G.u11[i] * c1[i] + G.u12[i] * c2[i] + G.u13[i] * c3[i]);
-    b[i] = G.J[i] * (G.u12[i] * c1[i] + G.u22[i] * c2[i] + G.u23[i] * c3[i]);
-  }
+  FT a[4], b[4], da[4], db[4], w1[4], w2[4], x[4];
+  vmul(G.u13, c3, x);
+  vfma(G.u12, c2, x, x);
+  vfma(G.u11, c1, x, x);
+  vmul(G.J, x, a);
+  vmul(G.u23, c3, x);
+  vfma(G.u22, c2, x, x);
+  vfma(G.u12, c1, x, x);
+  vmul(G.J, x, b);
   d1(P, a, da);
   d2(R, b, db);
-#pragma unroll
-  for (int i = 0; i < 4; ++i) a[i] = W[i] * ((da[i] + db[i]) * G.iJ[i]);
+  vadd(da, db, x);
+  vmul(x, G.iJ, x);
+  vmul(W, x, a);
   t1(P, a, w1);
   t2(R, a, w2);
   FT e1[4], e2[4], e3[4], e4[4];
@@ -222,25 +324,54 @@ __device__ __forceinline__ void tvec_lap(const DevParams<FT> &P, const Row<FT> &
   TCov<FT> Gd;
   trow_cov(P, sG, sT, j, L, Gd);
   FT z1[4], z2[4], z3[4];
-#pragma unroll
-  for (int i = 0; i < 4; ++i) {
-    const FT k1 = e3[i] * G.iJ[i], k2 = -e4[i] * G.iJ[i], k3 = (e1[i] - e2[i]) * G.iJ[i];
-    z1[i] = W[i] * (Gd.d11[i] * k1 + Gd.d12[i] * k2 + Gd.d13[i] * k3);
-    z2[i] = W[i] * (Gd.d12[i] * k1 + Gd.d22[i] * k2 + Gd.d23[i] * k3);
-    z3[i] = W[i] * (Gd.d13[i] * k1 + Gd.d23[i] * k2 + Gd.d33[i] * k3);
+  {
+    FT k1[4], k2[4], k3[4];
+    vmul(e3, G.iJ, k1);
+    vmul(e4, G.iJ, k2);
+    vmuls(k2, FT(-1), k2);
+    vsub(e1, e2, k3);
+    vmul(k3, G.iJ, k3);
+    vmul(Gd.d13, k3, x);
+    vfma(Gd.d12, k2, x, x);
+    vfma(Gd.d11, k1, x, x);
+    vmul(W, x, z1);
+    vmul(Gd.d23, k3, x);
+    vfma(Gd.d22, k2, x, x);
+    vfma(Gd.d12, k1, x, x);
+    vmul(W, x, z2);
+    vmul(Gd.d33, k3, x);
+    vfma(Gd.d23, k2, x, x);
+    vfma(Gd.d13, k1, x, x);
+    vmul(W, x, z3);
   }
   FT f1[4], f2[4], f3[4], f4[4];
   t1(P, z2, f1);
   t2(R, z1, f2);
   t2(R, z3, f3);
   t1(P, z3, f4);
-#pragma unroll
-  for (int i = 0; i < 4; ++i) {
-    const FT q1 = -f3[i] * G.iWJ[i], q2 = f4[i] * G.iWJ[i], q3 = (f2[i] - f1[i]) * G.iWJ[i];
-    o1[i] = -fdiv * w1[i] * iW[i] - (Gd.d11[i] * q1 + Gd.d12[i] * q2 + Gd.d13[i] * q3);
-    o2[i] = -fdiv * w2[i] * iW[i] - (Gd.d12[i] * q1 + Gd.d22[i] * q2 + Gd.d23[i] * q3);
-    o3[i] = -(Gd.d13[i] * q1 + Gd.d23[i] * q2 + Gd.d33[i] * q3);
-  }
+  FT q1[4], q2[4], q3[4], y[4];
+  vmul(f3, G.iWJ, q1);
+  vmuls(q1, FT(-1), q1);
+  vmul(f4, G.iWJ, q2);
+  vsub(f2, f1, q3);
+  vmul(q3, G.iWJ, q3);
+  // o1 = -fdiv (w1 / W) - (d11 q1 + d12 q2 + d13 q3), o2 alike
+  vmul(w1, iW, y);
+  vmul(Gd.d13, q3, x);
+  vfma(Gd.d12, q2, x, x);
+  vfma(Gd.d11, q1, x, x);
+  vmuls(x, FT(-1), x);
+  vfmas(y, -fdiv, x, o1);
+  vmul(w2, iW, y);
+  vmul(Gd.d23, q3, x);
+  vfma(Gd.d22, q2, x, x);
+  vfma(Gd.d12, q1, x, x);
+  vmuls(x, FT(-1), x);
+  vfmas(y, -fdiv, x, o2);
+  vmul(Gd.d33, q3, x);
+  vfma(Gd.d23, q2, x, x);
+  vfma(Gd.d13, q1, x, x);
+  vmuls(x, FT(-1), o3);
 }
 
 // weak divergence -(1/WJ) (D^T (WJ F1) + ...) with the row's per-node WJ
@@ -248,15 +379,13 @@ template <class FT>
 __device__ __forceinline__ void twdiv(const DevParams<FT> &P, const Row<FT> &R, const TRow<FT> &G, const FT (&F1)[4],
                                       const FT (&F2)[4], FT (&o)[4]) {
   FT a[4], b[4], ta[4], tb[4];
-#pragma unroll
-  for (int i = 0; i < 4; ++i) {
-    a[i] = G.WJ[i] * F1[i];
-    b[i] = G.WJ[i] * F2[i];
-  }
+  vmul(G.WJ, F1, a);
+  vmul(G.WJ, F2, b);
   t1(P, a, ta);
   t2(R, b, tb);
-#pragma unroll
-  for (int i = 0; i < 4; ++i) o[i] = -(ta[i] + tb[i]) * G.iWJ[i];
+  vadd(ta, tb, a);
+  vmul(a, G.iWJ, a);
+  vmuls(a, FT(-1), o);
 }
 
 // The centre state of the row at level v with the filtered face u_3 below and above:
@@ -269,26 +398,45 @@ template <class FT>
 __device__ __forceinline__ void tcentre(const DevParams<FT> &P, const FT *sY, const FT *sF, const FT *sG33, int j,
                                         int v, const TRow<FT> &G, TCen<FT> &c) {
   const int Nv = P.Nv, Nf = P.Nf;
-  FT ga[4], gb[4], fa[4], fb[4];
+  FT ga[4], gb[4], fa[4], fb[4], x[4];
   ld_row(sG33 + (size_t)v * NN + NQ * j, ga);
   ld_row(sG33 + (size_t)(v + 1) * NN + NQ * j, gb);
 #pragma unroll
   for (int i = 0; i < 4; ++i) {
-    const int n = NQ * j + i, q = n * Nv + v;
+    const int q = (NQ * j + i) * Nv + v;
     c.rho[i] = sY[q];
     c.u1[i] = sY[16 * Nv + q];
     c.u2[i] = sY[32 * Nv + q];
     c.rhoe[i] = sY[48 * Nv + q];
-    c.ct3[i] = G.u13[i] * c.u1[i] + G.u23[i] * c.u2[i];
-    // the impenetrable value on the bottom and top faces (u^3 = 0 there)
-    fa[i] = v == 0 ? -c.ct3[i] / ga[i] : sF[n * Nf + v];
-    fb[i] = v + 1 == Nv ? -c.ct3[i] / gb[i] : sF[n * Nf + v + 1];
-    c.ub3[i] = (fa[i] + fb[i]) / FT(2);
-    c.h1[i] = G.u11[i] * c.u1[i] + G.u12[i] * c.u2[i];
-    c.h2[i] = G.u12[i] * c.u1[i] + G.u22[i] * c.u2[i];
-    const FT kv = (fa[i] * (fa[i] * ga[i]) + fb[i] * (fb[i] * gb[i])) / FT(2);
-    c.K[i] = (c.u1[i] * c.h1[i] + c.u2[i] * c.h2[i] + kv + FT(2) * c.ct3[i] * c.ub3[i]) / FT(2);
   }
+  vmul(G.u23, c.u2, x);
+  vfma(G.u13, c.u1, x, c.ct3);
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const int n = NQ * j + i;
+    // the impenetrable value on the bottom and top faces (u^3 = 0 there)
+    fa[i] = v == 0 ? -gdiv(c.ct3[i], ga[i]) : sF[n * Nf + v];
+    fb[i] = v + 1 == Nv ? -gdiv(c.ct3[i], gb[i]) : sF[n * Nf + v + 1];
+  }
+  vadd(fa, fb, c.ub3);
+  vmuls(c.ub3, FT(0.5), c.ub3);
+  vmul(G.u12, c.u2, x);
+  vfma(G.u11, c.u1, x, c.h1);
+  vmul(G.u22, c.u2, x);
+  vfma(G.u12, c.u1, x, c.h2);
+  // K = (u_1 h1 + u_2 h2 + (fa^2 ga + fb^2 gb) / 2 + 2 ct3 ub3) / 2
+  FT kv[4], y[4];
+  vmul(fb, gb, y);
+  vmul(fb, y, kv);
+  vmul(fa, ga, y);
+  vfma(fa, y, kv, kv);
+  vmul(c.ct3, c.ub3, y);
+  vmuls(y, FT(4), y);
+  vadd(kv, y, kv);                   // fa^2 ga + fb^2 gb + 4 ct3 ub3
+  vmul(c.u2, c.h2, y);
+  vfma(c.u1, c.h1, y, y);
+  vfmas(kv, FT(0.5), y, y);
+  vmuls(y, FT(0.5), c.K);
 }
 
 template <class FT>
@@ -337,32 +485,42 @@ __global__ void __launch_bounds__(TS_THREADS, TsMinBlocks<FT>::value) k_topo_pas
       TCen<FT> c;
       tcentre(P, sY, sF, sG33, j, v, G, c);
       FT sd[4];
-#pragma unroll
-      for (int i = 0; i < 4; ++i) {
-        Thermo<FT> th;
-        thermo(P, c.rho[i], c.rhoe[i], c.K[i], P.grav * G.z[i], P.lr4[v], th);
+      {
         // s_d - s_d,r = cp_d (T - T_r) + (Phi - Phi_r(Pi)); the level record's deviation is for
         // the flat level's geopotential g zeta, the point is g z_s b higher
-        sd[i] = P.cpd * (th.T - th.Tr) + (th.phid + P.grav * G.zsb[i]);
+        FT Phi[4], t[4], x[4];
+        ThermoRow<FT> th;
+        vmuls(G.z, P.grav, Phi);
+        thermo_row_pt(P, c.rho, c.rhoe, c.K, Phi, P.lr4[v], th);
+        vsub(th.T, th.Tr, t);
+        vfmas(G.zsb, P.grav, th.phid, x);
+        vfmas(t, P.cpd, x, sd);
       }
       FT o1[4], o2[4], o3[4];
       tvec_lap(P, R, G, sG, sT, j, P.ltc[v], W, iW, c.u1, c.u2, c.ub3, FT(1), o1, o2, o3);
       FT g1[4], g2[4], x1[4], x2[4], Ls[4];
       d1(P, sd, g1);
       d2(R, sd, g2);
-#pragma unroll
-      for (int i = 0; i < 4; ++i) {
-        x1[i] = G.u11[i] * g1[i] + G.u12[i] * g2[i];
-        x2[i] = G.u12[i] * g1[i] + G.u22[i] * g2[i];
+      {
+        FT t[4];
+        vmul(G.u12, g2, t);
+        vfma(G.u11, g1, t, x1);
+        vmul(G.u22, g2, t);
+        vfma(G.u12, g1, t, x2);
       }
       twdiv(P, R, G, x1, x2, Ls);
       if (act) {
+        FT t[4];
+        vmul(G.s1i, o3, t);
+        vsub(o1, t, o1);
+        vmul(G.s2i, o3, t);
+        vsub(o2, t, o2);
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
           const int q = (NQ * j + i) * Nv + v;
           sO[q] = Ls[i];
-          sO[16 * Nv + q] = o1[i] - G.s1i[i] * o3[i];
-          sO[32 * Nv + q] = o2[i] - G.s2i[i] * o3[i];
+          sO[16 * Nv + q] = o1[i];
+          sO[32 * Nv + q] = o2[i];
           sO[48 * Nv + q] = o3[i];
         }
       }
@@ -478,15 +636,14 @@ __global__ void __launch_bounds__(TS_THREADS, TsMinBlocks<FT>::value) k_topo_pas
         for (int i = 0; i < 4; ++i) {
           const int q = (NQ * j + i) * Nv + v;
           L3[i] = sL[48 * Nv + q];
-          L1[i] = sL[16 * Nv + q] + G.s1i[i] * L3[i];
-          L2[i] = sL[32 * Nv + q] + G.s2i[i] * L3[i];
+          L1[i] = sL[16 * Nv + q];
+          L2[i] = sL[32 * Nv + q];
         }
+        vfma(G.s1i, L3, L1, L1);
+        vfma(G.s2i, L3, L2, L2);
         tvec_lap(P, R, G, sG, sT, j, P.ltc[v], W, iW, L1, L2, L3, P.div_damp, o1, o2, o3);
-#pragma unroll
-        for (int i = 0; i < 4; ++i) {
-          Q1[i] = -P.nu_v * o1[i];
-          Q2[i] = -P.nu_v * o2[i];
-        }
+        vmuls(o1, -P.nu_v, Q1);
+        vmuls(o2, -P.nu_v, Q2);
         if (act) st_row(row(sS, TB_L4, v), o3);
       }
       TCen<FT> c;
@@ -499,69 +656,82 @@ __global__ void __launch_bounds__(TS_THREADS, TsMinBlocks<FT>::value) k_topo_pas
         for (int i = 0; i < 4; ++i) Ls[i] = sL[(NQ * j + i) * Nv + v];
         d1(P, Ls, g1);
         d2(R, Ls, g2);
-#pragma unroll
-        for (int i = 0; i < 4; ++i) {
-          x1[i] = c.rho[i] * (G.u11[i] * g1[i] + G.u12[i] * g2[i]);
-          x2[i] = c.rho[i] * (G.u12[i] * g1[i] + G.u22[i] * g2[i]);
-        }
+        vcontract(G.u11, G.u12, g1, g2, c.rho, x1);
+        vcontract(G.u12, G.u22, g1, g2, c.rho, x2);
         twdiv(P, R, G, x1, x2, Trhoe);
-#pragma unroll
-        for (int i = 0; i < 4; ++i) Trhoe[i] *= -P.nu_s;
+        vmuls(Trhoe, -P.nu_s, Trhoe);
       }
       FT h[4], Pi[4], thp[4], gg[4], c1[4], c2[4];
+      {
+        FT Phi[4], t[4];
+        ThermoRow<FT> th;
+        vmuls(G.z, P.grav, Phi);
+        thermo_row_pt(P, c.rho, c.rhoe, c.K, Phi, P.lr4[v], th);
 #pragma unroll
-      for (int i = 0; i < 4; ++i) {
-        Thermo<FT> th;
-        thermo(P, c.rho[i], c.rhoe[i], c.K[i], P.grav * G.z[i], P.lr4[v], th);
-        h[i] = th.h;
-        Pi[i] = th.Pi;
-        thp[i] = th.thv - th.thvr;
+        for (int i = 0; i < 4; ++i) {
+          h[i] = th.h[i];
+          Pi[i] = th.Pi[i];
+        }
+        vsub(th.thv, th.thvr, thp);
         // K + Phi - Phi_r(Pi) + (cp_d / 2) th' Pi: one gradient for grad(K + Phi - Phi_r) and
         // the (cp_d / 2) grad(th' Pi) of the Exner-split pressure gradient
-        gg[i] = c.K[i] + (th.phid + P.grav * G.zsb[i]) + P.cpd * FT(0.5) * thp[i] * Pi[i];
-        c1[i] = c.h1[i] + G.u13[i] * c.ub3[i];
-        c2[i] = c.h2[i] + G.u23[i] * c.ub3[i];
+        vfmas(G.zsb, P.grav, th.phid, t);
+        vadd(c.K, t, gg);
+        vmul(thp, Pi, t);
+        vfmas(t, P.cpd * FT(0.5), gg, gg);
+        vfma(G.u13, c.ub3, c.h1, c1);
+        vfma(G.u23, c.ub3, c.h2, c2);
       }
       // vorticity w^3 = wcurl(u_h), Coriolis f^3, (f^3 + w^3) x CT12(u) -> C12, the sponge
       {
         FT a[4], bb[4], ta[4], tb[4], f3[4], fh1[4], fh2[4];
-#pragma unroll
-        for (int i = 0; i < 4; ++i) {
-          a[i] = W[i] * c.u2[i];
-          bb[i] = W[i] * c.u1[i];
-        }
+        vmul(W, c.u2, a);
+        vmul(W, c.u1, bb);
         t1(P, a, ta);
         t2(R, bb, tb);
         ld_row(sG + HG_F3 * NN + NQ * j, f3);
         ld_row(sG + HG_FH1 * NN + NQ * j, fh1);
         ld_row(sG + HG_FH2 * NN + NQ * j, fh2);
+        // om = (tb - ta) / (W J); f^3 = f3 / dz - (s1 fh1 + s2 fh2) / (r dz); a3J = J (f^3 + om)
+        FT om[4], fc[4], x[4], a3J[4], damp[4];
+        vsub(tb, ta, om);
+        vmul(om, G.iWJ, om);
+        vmul(G.s2i, fh2, x);
+        vfma(G.s1i, fh1, x, x);
+        vmul(x, G.ir, x);
+        vmul(f3, G.idz, fc);
+        vsub(fc, x, fc);
+        vadd(fc, om, x);
+        vmul(G.J, x, a3J);
 #pragma unroll
-        for (int i = 0; i < 4; ++i) {
-          const FT om = (tb[i] - ta[i]) * G.iWJ[i];
-          const FT fc3 = f3[i] * G.idz[i] - (G.s1i[i] * fh1[i] + G.s2i[i] * fh2[i]) * G.ir[i];
-          const FT a3J = G.J[i] * (fc3 + om);
-          const FT damp = tsponge(P, G.z[i], P.spg_auh);
-          Q1[i] += a3J * c2[i] - damp * c.u1[i];
-          Q2[i] += -a3J * c1[i] - damp * c.u2[i];
-        }
+        for (int i = 0; i < 4; ++i) damp[i] = tsponge(P, G.z[i], P.spg_auh);
+        // Q1 += a3J c2 - damp u1, Q2 += -a3J c1 - damp u2
+        vmul(damp, c.u1, x);
+        vsub(Q1, x, Q1);
+        vfma(a3J, c2, Q1, Q1);
+        vmul(damp, c.u2, x);
+        vsub(Q2, x, Q2);
+        vmul(a3J, c1, x);
+        vsub(Q2, x, Q2);
       }
       // rho: -wdiv(rho u); rho e_tot: -split_div(rho u, h)
       FT dm[4];
       {
-        FT F1[4], F2[4], G1[4], G2[4], dmh[4], ha[4], hb[4];
-#pragma unroll
-        for (int i = 0; i < 4; ++i) {
-          F1[i] = c.rho[i] * c1[i];
-          F2[i] = c.rho[i] * c2[i];
-          G1[i] = F1[i] * h[i];
-          G2[i] = F2[i] * h[i];
-        }
+        FT F1[4], F2[4], G1[4], G2[4], dmh[4], ha[4], hb[4], x[4];
+        vmul(c.rho, c1, F1);
+        vmul(c.rho, c2, F2);
+        vmul(F1, h, G1);
+        vmul(F2, h, G2);
         twdiv(P, R, G, F1, F2, dm);
         twdiv(P, R, G, G1, G2, dmh);
         d1(P, h, ha);
         d2(R, h, hb);
-#pragma unroll
-        for (int i = 0; i < 4; ++i) Trhoe[i] -= (dmh[i] + h[i] * dm[i] + F1[i] * ha[i] + F2[i] * hb[i]) / FT(2);
+        // T_rhoe -= (wdiv(F h) + h wdiv(F) + F . grad h) / 2
+        vmul(F2, hb, x);
+        vfma(F1, ha, x, x);
+        vfma(h, dm, x, x);
+        vadd(dmh, x, x);
+        vfmas(x, FT(-0.5), Trhoe, Trhoe);
       }
       // u_h: -[grad(K + Phi - Phi_r) + cp_d (th' grad Pi + grad(th' Pi) - Pi grad th') / 2]
       {
@@ -572,16 +742,22 @@ __global__ void __launch_bounds__(TS_THREADS, TsMinBlocks<FT>::value) k_topo_pas
         d2(R, Pi, b2);
         d1(P, thp, f1);
         d2(R, thp, f2);
-#pragma unroll
-        for (int i = 0; i < 4; ++i) {
-          Q1[i] -= a1[i] + P.cpd * FT(0.5) * (thp[i] * b1[i] - Pi[i] * f1[i]);
-          Q2[i] -= a2[i] + P.cpd * FT(0.5) * (thp[i] * b2[i] - Pi[i] * f2[i]);
-        }
+        // Q -= a + (cp_d / 2) (th' b - Pi f)
+        FT t[4], x[4];
+        vmul(Pi, f1, t);
+        vmuls(t, FT(-1), t);
+        vfma(thp, b1, t, t);
+        vfmas(t, P.cpd * FT(0.5), a1, x);
+        vsub(Q1, x, Q1);
+        vmul(Pi, f2, t);
+        vmuls(t, FT(-1), t);
+        vfma(thp, b2, t, t);
+        vfmas(t, P.cpd * FT(0.5), a2, x);
+        vsub(Q2, x, Q2);
       }
       if (act) {
         FT rJ[4];
-#pragma unroll
-        for (int i = 0; i < 4; ++i) rJ[i] = c.rho[i] * G.J[i];
+        vmul(c.rho, G.J, rJ);
         st_row(row(sS, TB_C1, v), c1);
         st_row(row(sS, TB_C2, v), c2);
         st_row(row(sS, TB_K, v), c.K);
@@ -623,7 +799,7 @@ __global__ void __launch_bounds__(TS_THREADS, TsMinBlocks<FT>::value) k_topo_pas
       FT u3[4], Wu[4];
 #pragma unroll
       for (int i = 0; i < 4; ++i) {
-        u3[i] = inner ? sF[(NQ * j + i) * Nf + k] : -CTa[i] / g33[i];
+        u3[i] = inner ? sF[(NQ * j + i) * Nf + k] : -gdiv(CTa[i], g33[i]);
         Wu[i] = W[i] * u3[i];
       }
       FT ta[4], tb[4];
@@ -646,8 +822,9 @@ __global__ void __launch_bounds__(TS_THREADS, TsMinBlocks<FT>::value) k_topo_pas
             cc1 = (C1a[i] + C1b[i]) / FT(2);
             cc2 = (C2a[i] + C2b[i]) / FT(2);
             gK = Kb[i] - Ka[i];
-            l4 = (Ra[i] * La[i] + Rb[i] * Lb[i]) / (Ra[i] + Rb[i]);
-            uh3 = (Ra[i] * CTa[i] + Rb[i] * CTb[i]) / (Ra[i] + Rb[i]);
+            const FT iRab = grcp(Ra[i] + Rb[i]);
+            l4 = (Ra[i] * La[i] + Rb[i] * Lb[i]) * iRab;
+            uh3 = (Ra[i] * CTa[i] + Rb[i] * CTb[i]) * iRab;
             rJ = (Ra[i] + Rb[i]) / FT(2);
           } else {
             cc1 = C1a[i];
@@ -682,11 +859,19 @@ __global__ void __launch_bounds__(TS_THREADS, TsMinBlocks<FT>::value) k_topo_pas
         ld_row(row(sS, TB_RJ, v), rJ);
         ld_row(row(sS, TB_Q1, v), Q1);
         ld_row(row(sS, TB_Q2, v), Q2);
+        FT irJ[4], t1v[4], t2v[4];
+        vrcp(rJ, irJ);
+        vadd(Xa1, Xb1, t1v);
+        vmul(t1v, irJ, t1v);
+        vfmas(t1v, FT(-0.5), Q1, t1v);
+        vadd(Xa2, Xb2, t2v);
+        vmul(t2v, irJ, t2v);
+        vfmas(t2v, FT(-0.5), Q2, t2v);
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
           const int q = (NQ * j + i) * Nv + v;
-          sY[16 * Nv + q] = Q1[i] - (Xa1[i] + Xb1[i]) / FT(2) / rJ[i];
-          sY[32 * Nv + q] = Q2[i] - (Xa2[i] + Xb2[i]) / FT(2) / rJ[i];
+          sY[16 * Nv + q] = t1v[i];
+          sY[32 * Nv + q] = t2v[i];
         }
       }
     }

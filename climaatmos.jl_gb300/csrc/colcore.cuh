@@ -102,6 +102,16 @@ struct ColLevT {
     g32 = m.g23;
     phis = grav * t.zsb;
   }
+  // c4 and ct of one centre from one evaluation of its point terms
+  __device__ Lev4<FT> c4ct(int v, FT &g31, FT &g32, FT &phis) const {
+    const TPoint<FT> t = pt(ltc[v]);
+    const TMetricUp<FT> m = tmetric_up(t, gs0, gs1, gs2);
+    g31 = m.g13;
+    g32 = m.g23;
+    phis = grav * t.zsb;
+    const FT x = t.r2 * t.dz;
+    return Lev4<FT>{x, grcp(x), t.ir2, grav * t.z};
+  }
 };
 
 // Centre diagnostics of one level from (rho, u_1, u_2, rho e_tot), the u_3 of
@@ -114,15 +124,15 @@ template <class FT, class LV>
 __device__ __forceinline__ Cen<FT> cdiag(const DevParams<FT> &P, const ColGeo<FT> &G, const LV &L, int v,
                                          FT rho, FT u1, FT u2, FT rhoe, FT u3a, FT u3b, FT g33a, FT g33b) {
   const int vc = min(max(v, 0), L.Nv - 1);
-  const Lev4<FT> Lc = L.c4(vc);
+  FT phis = FT(0), g31 = FT(0), g32 = FT(0);
+  Lev4<FT> Lc;
+  if constexpr (LV::TOPO) Lc = L.c4ct(vc, g31, g32, phis);
+  else Lc = L.c4(vc);
   const FT c1 = (G.gu0 * u1 + G.gu1 * u2) * Lc.z, c2 = (G.gu1 * u1 + G.gu2 * u2) * Lc.z;
   const FT kv = (u3a * (u3a * g33a) + u3b * (u3b * g33b)) / FT(2);
   Cen<FT> o;
-  FT phis = FT(0);
   if constexpr (LV::TOPO) {
     // over terrain K takes 2 CT3(u_h) I^c(u_3) (compute_kinetic, utilities.jl:194-206)
-    FT g31, g32;
-    L.ct(vc, g31, g32, phis);
     o.ct3 = g31 * u1 + g32 * u2;
     o.K = (u1 * c1 + u2 * c2 + kv + FT(2) * o.ct3 * ((u3a + u3b) / FT(2))) / FT(2);
   } else {

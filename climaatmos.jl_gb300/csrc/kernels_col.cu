@@ -184,9 +184,8 @@ __device__ __forceinline__ void col_diag(const DevParams<FT> &P, const ColGeo<FT
     if constexpr (TOPO) {
       // the column's own metric; K takes 2 CT3(u_h) I^c(u_3) (compute_kinetic, utilities.jl:194-206)
       // and CT12(ᶜu) takes g^a3 I^c(u_3)
-      const Lev4<FT> c4 = T.c4(v);
       FT g31, g32, phis;
-      T.ct(v, g31, g32, phis);
+      const Lev4<FT> c4 = T.c4ct(v, g31, g32, phis);
       const FT gu0 = G.gu0 * c4.z, gu1 = G.gu1 * c4.z, gu2 = G.gu2 * c4.z;
       const FT h1 = gu0 * S.u1[k] + gu1 * S.u2[k], h2 = gu1 * S.u1[k] + gu2 * S.u2[k];
       const FT ct3 = g31 * S.u1[k] + g32 * S.u2[k], ub3 = (S.u3[k] + u3n[k]) / FT(2);

@@ -788,6 +788,27 @@ def measure_moist(args):
         del p, Y, T, dY
         torch.cuda.empty_cache()
     out["moist_over_dry"] = out["moist"]["newton_iteration_ms"] / out["dry"]["newton_iteration_ms"]
+    # FP32 against FP64 (the library's own FP64 path) for the moist implicit tendency
+    c64 = base.with_(moist=True, ft=np.float64)
+    g64 = sim.Geometry(c64)
+    Mc, Mf = S.moist_initial_state(g64, c64, seed=1, sigma=2.0, dtype=np.float64)
+    Mf = np.random.default_rng(5).normal(0.0, 0.05, size=Mf.shape) * np.diff(
+        np.concatenate([[g64.zf[0]], g64.zc, [g64.zf[-1]]]))[None, None, :]
+    res = {}
+    for ft in (np.float64, np.float32):
+        cf = c64.with_(ft=ft)
+        pf = sim.AtmosCache(cf)
+        Yf_ = sim.FieldVector.from_numpy(Mc.astype(ft), Mf.astype(ft))
+        Tf_ = Yf_.similar()
+        sim.implicit_tendency(Tf_, Yf_, pf, 0.0)
+        res[np.dtype(ft).name] = Tf_.numpy()
+        del pf, Yf_, Tf_
+    a, b = res["float32"], res["float64"]
+    names = ["rho", "u_1", "u_2", "rho_e_tot", "rho_q_tot"]
+    err = {n: float(np.abs(a[0][:, c] - b[0][:, c]).max() / max(np.abs(b[0][:, c]).max(), 1e-300))
+           for c, n in enumerate(names) if np.abs(b[0][:, c]).max() > 0}
+    err["u_3"] = float(np.abs(a[1] - b[1]).max() / np.abs(b[1]).max())
+    out["implicit_tendency_fp32_vs_fp64"] = err
     out["what"] = ("h_elem 30, z_elem 63, FP32; q_tot = 0.018 exp(-z / 2.5 km): condensate below ~2 km and on "
                    "the mixed-phase levels; the saturation adjustment in every hook that forms the precomputed "
                    "quantities")

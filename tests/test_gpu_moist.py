@@ -114,3 +114,38 @@ def test_moist_context_refuses_the_dry_only_entries():
         with pytest.raises(N.GBError) as e:
             call()
         assert e.value.code == N.GB_ERR_ARG
+
+
+def _assert_u3(errs, tol, tol_u3):
+    bad = {k: v for k, v in errs.items() if not v <= (tol_u3 if k == "u_3" else tol)}
+    assert not bad, "errors above the bounds: %s (all: %s)" % (bad, errs)
+
+
+def test_moist_hooks_at_the_production_grid():
+    """h_elem 30, z_elem 63 stretched (the headline grid), the moist initial state: the FP64
+    implicit tendency and Jacobian solve against the FP64 oracle at 2e-12, u_3's tendency at 1e-11
+    (measured 3.8e-12): it is the difference of gravity and the vertical pressure gradient, each
+    about g dz, in a hydrostatically balanced state, so that its FP64 roundoff relative to its
+    own maximum grows with that cancellation."""
+    from gbdycore import config as C
+    from gbdycore import setups as S
+    from helpers import oracle_geometry
+    cfg = C.production_h30().with_(ft=np.float64, moist=True)
+    g = oracle_geometry(cfg)
+    Yc, Yf = S.moist_initial_state(g, cfg, seed=1, sigma=2.0, dtype=np.float64)
+    rng = np.random.default_rng(3)
+    Yf = np.ascontiguousarray(rng.normal(0.0, 0.05, size=Yf.shape) * g.dzf[None, None, :])
+    o = make_oracle(cfg)
+    ref = o.implicit_tendency(Yc.copy(), Yf.copy())
+    p = sim.AtmosCache(cfg)
+    Y = _dev(Yc, Yf)
+    Yt = Y.similar()
+    sim.implicit_tendency(Yt, Y, p, 0.0)
+    _assert_u3(moist_field_errors(*Yt.numpy(), *ref), 2e-12, 1e-11)
+    dtg = 0.4358665215084590 * cfg.dt
+    o.update_jacobian(Yc.copy(), Yf.copy(), dtg)
+    refx = o.ldiv(ref[0], ref[1])
+    sim.update_jacobian(sim.Jacobian(p), Y, p, dtg, 0.0)
+    X = Y.similar()
+    sim.ldiv(X, sim.Jacobian(p), Yt)
+    _assert_u3(moist_field_errors(*X.numpy(), *refx), 2e-12, 1e-11)

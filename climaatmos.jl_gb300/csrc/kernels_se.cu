@@ -32,23 +32,6 @@ using namespace se;
 constexpr int SE_THREADS = 256;          // 64 level slots x 4 rows per sweep
 constexpr int SE_LEVELS = SE_THREADS / 4;
 
-// The element's face block (16 nodes x Nf faces) into the padded face slab: one TMA copy per node
-// row j (4 Nf elements: a multiple of 16 bytes at 16-byte aligned addresses on both sides).
-template <class FT>
-__device__ __forceinline__ void load_faces(FT *sF, const FT *Yf, int e, int Nf, uint64_t *bar) {
-  const int FR = face_rows<FT>(Nf);
-  const uint32_t b4 = uint32_t(sizeof(FT) * 4 * Nf);
-#pragma unroll
-  for (int j = 0; j < NQ; ++j) tma_load(sF + (size_t)j * FR, Yf + ((size_t)e * 16 + 4 * j) * Nf, b4, bar);
-}
-template <class FT>
-__device__ __forceinline__ void store_faces(FT *Yf, const FT *sF, int e, int Nf) {
-  const int FR = face_rows<FT>(Nf);
-  const uint32_t b4 = uint32_t(sizeof(FT) * 4 * Nf);
-#pragma unroll
-  for (int j = 0; j < NQ; ++j) tma_store(Yf + ((size_t)e * 16 + 4 * j) * Nf, sF + (size_t)j * FR, b4);
-}
-
 // TMA loads of one element's input slabs into buffer set b (thread 0 only).
 template <class FT>
 __device__ __forceinline__ void issue_slab(const DevParams<FT> &P, uint64_t *bar, int e, FT *sY, FT *sF, FT *sG,

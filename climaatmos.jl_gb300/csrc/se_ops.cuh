@@ -668,5 +668,23 @@ __device__ __forceinline__ void slab_prefetch(int nbuf, int b, int e, int Nh, co
   }
 }
 
+// The element's face block (16 nodes x Nf faces) into the padded face slab (face_rows): one TMA
+// copy per node row j (4 Nf elements: a multiple of 16 bytes at 16-byte aligned addresses on both
+// sides), and back.
+template <class FT>
+__device__ __forceinline__ void load_faces(FT *sF, const FT *Yf, int e, int Nf, uint64_t *bar) {
+  const int FR = face_rows<FT>(Nf);
+  const uint32_t b4 = uint32_t(sizeof(FT) * 4 * Nf);
+#pragma unroll
+  for (int j = 0; j < NQ; ++j) tma_load(sF + (size_t)j * FR, Yf + ((size_t)e * 16 + 4 * j) * Nf, b4, bar);
+}
+template <class FT>
+__device__ __forceinline__ void store_faces(FT *Yf, const FT *sF, int e, int Nf) {
+  const int FR = face_rows<FT>(Nf);
+  const uint32_t b4 = uint32_t(sizeof(FT) * 4 * Nf);
+#pragma unroll
+  for (int j = 0; j < NQ; ++j) tma_store(Yf + ((size_t)e * 16 + 4 * j) * Nf, sF + (size_t)j * FR, b4);
+}
+
 }  // namespace se
 }  // namespace gb

@@ -204,7 +204,7 @@ int create_impl(gb_ctx *ctx) {
     if ((r = alloc(ctx, I->Ti[s], (I->NR + I->NF) * sizeof(FT)))) return r;
   if ((r = alloc(ctx, I->rnorm, (size_t)Nh * NN * 3 * sizeof(double)))) return r;
   I->nsum_blocks = 152 * 4;
-  if ((r = alloc(ctx, I->partials, (size_t)I->nsum_blocks * 4 * sizeof(double)))) return r;
+  if ((r = alloc(ctx, I->partials, (size_t)I->nsum_blocks * 6 * sizeof(double)))) return r;
   if ((r = alloc(ctx, I->sums, 4 * sizeof(double)))) return r;
   if ((r = alloc(ctx, I->rsum, 4 * sizeof(double)))) return r;
   DevParams<FT> &P = I->P;
@@ -559,13 +559,14 @@ int read_status(gb_ctx *ctx) {
   return GB_OK;
 }
 
+// The integrals of rho and rho e_tot, and (moist) of rho q_tot: nout of them are copied out.
 template <class FT>
-int global_sums_t(gb_ctx *ctx, gb_fieldvec Y, double *out) {
+int global_sums_t(gb_ctx *ctx, gb_fieldvec Y, double *out, int nout) {
   Impl<FT> *I = impl<FT>(ctx);
   launch_global_sums<FT>(I->P, (const FT *)Y.c, (double *)I->partials.p, I->nsum_blocks, (double *)I->sums.p, ctx->stream);
   int r = check_launch(ctx);
   if (r) return r;
-  CK(cudaMemcpyAsync(out, I->sums.p, 2 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaMemcpyAsync(out, I->sums.p, nout * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
   return GB_OK;
 }
@@ -1197,8 +1198,9 @@ bool fv_ok(gb_fieldvec v) { return v.c && v.f && aligned(v.c) && aligned(v.f); }
     if ((ctx)->geo.topo) return fail((ctx), GB_ERR_ARG, what " is not available over terrain");   \
   } while (0)
 
-// A moist 0M context supports the column hooks only (gb_set_precomputed_quantities,
-// gb_implicit_tendency, gb_update_jacobian, gb_ldiv, gb_correct_implicit_advection_tendency).
+// A moist 0M context supports the column hooks (gb_set_precomputed_quantities,
+// gb_implicit_tendency, gb_update_jacobian, gb_ldiv, gb_correct_implicit_advection_tendency),
+// the state DSS and the conservation sums.
 #define NO_MOIST(ctx, what)                                                                            \
   do {                                                                                                 \
     if ((ctx) && (ctx)->cfg.moist) return fail((ctx), GB_ERR_ARG, what " is not available with moist = 1"); \
@@ -1361,11 +1363,10 @@ int gb_correct_implicit_advection_tendency(gb_ctx *ctx, gb_fieldvec Yt, gb_field
 
 int gb_dss(gb_ctx *ctx, gb_fieldvec Y) {
   GB_RANGE();
-  NO_MOIST(ctx, "gb_dss");
   GUARD(ctx);
   if (!fv_ok(Y)) return fail(ctx, GB_ERR_ARG, "null or misaligned pointer");
-  if (ctx->cfg.ft_bytes == 8) launch_dss<double>(impl<double>(ctx)->P, (double *)Y.c, (double *)Y.f, ctx->stream);
-  else launch_dss<float>(impl<float>(ctx)->P, (float *)Y.c, (float *)Y.f, ctx->stream);
+  if (ctx->cfg.ft_bytes == 8) launch_dss_state<double>(impl<double>(ctx)->P, (double *)Y.c, (double *)Y.f, ctx->stream);
+  else launch_dss_state<float>(impl<float>(ctx)->P, (float *)Y.c, (float *)Y.f, ctx->stream);
   return check_launch(ctx);
 }
 
@@ -1383,10 +1384,17 @@ int gb_step(gb_ctx *ctx, gb_fieldvec Y, double t, double dt, int nsteps, int use
 
 int gb_global_sums(gb_ctx *ctx, gb_fieldvec Y, double out[2]) {
   GB_RANGE();
-  NO_MOIST(ctx, "gb_global_sums");
   GUARD(ctx);
   if (!fv_ok(Y) || !out) return fail(ctx, GB_ERR_ARG, "null or misaligned pointer");
-  return DISPATCH(ctx, global_sums_t, ctx, Y, out);
+  return DISPATCH(ctx, global_sums_t, ctx, Y, out, 2);
+}
+
+int gb_conservation_sums(gb_ctx *ctx, gb_fieldvec Y, double out[3]) {
+  GB_RANGE();
+  GUARD(ctx);
+  if (!fv_ok(Y) || !out) return fail(ctx, GB_ERR_ARG, "null or misaligned pointer");
+  out[2] = 0.0;
+  return DISPATCH(ctx, global_sums_t, ctx, Y, out, ctx->cfg.moist ? 3 : 2);
 }
 
 int gb_newton_residual(gb_ctx *ctx, double out[3]) {

@@ -131,6 +131,8 @@ struct ColArgs {
 template <class FT> void launch_passA(const DevParams<FT> &P, const FT *Yc, const FT *Yf, FT *L, cudaStream_t s);
 template <class FT> void launch_passB(const DevParams<FT> &P, const FT *Yc, const FT *Yf, const FT *L, FT *Tc, FT *Tf, cudaStream_t s, const FinArgs<FT> *fin = nullptr);
 template <class FT> void launch_dss(const DevParams<FT> &P, FT *C, FT *F, cudaStream_t s);
+// the DSS of a state (Y.c with the context's centre components: 5 when moist)
+template <class FT> void launch_dss_state(const DevParams<FT> &P, FT *C, FT *F, cudaStream_t s);
 template <class FT> void launch_dss_transpose(const DevParams<FT> &P, FT *C, FT *F, cudaStream_t s);
 template <class FT> void launch_column_stage(const DevParams<FT> &P, const StageArgs<FT> &A, cudaStream_t s);
 template <class FT> void launch_column(const DevParams<FT> &P, int mode, const ColArgs<FT> &A, cudaStream_t s);

@@ -12,15 +12,17 @@ constexpr int DSS_THREADS = 256;  // 8 groups per CTA, one warp per group
 // J-weighted average of its copies, summed in the fixed ascending copy order
 // (deterministic, no atomics).  Centre block components: 0 scalar, 1-2 covariant
 // horizontal vector (averaged in Cartesian components), 3 scalar.  One warp
-// per group, lanes over levels.
+// per group, lanes over levels.  Q5 (moist 0M): a fifth centre component,
+// rho*q_tot, averaged as a scalar (element block stride 5 * 16 * Nv).
 // Two levels per lane (v0 + lane and v0 + 32 + lane), so that each lane has
 // two independent gathers in flight; per level the sums run in the same copy
 // order as with one level per lane.  Every product and sum is an explicit
 // fused multiply-add or rounded product, so the rounding does not depend on
 // the compiler's contraction choices (the oracle's DSS does the same
 // operations in the same order and matches bit for bit).
-template <class FT>
+template <class FT, bool Q5 = false>
 __global__ void __launch_bounds__(DSS_THREADS) k_dss(DevParams<FT> P, FT *__restrict__ C, FT *__restrict__ F) {
+  constexpr int NFC = Q5 ? 5 : 4;
   const int lane = threadIdx.x & 31;
   const int g = blockIdx.x * (DSS_THREADS / 32) + (threadIdx.x >> 5);
   if (g >= P.ngroups) return;
@@ -30,18 +32,19 @@ __global__ void __launch_bounds__(DSS_THREADS) k_dss(DevParams<FT> P, FT *__rest
     for (int v0 = 0; v0 < Nv; v0 += 64) {
       const int v[2] = {v0 + lane, v0 + 32 + lane};
       const bool ok[2] = {v[0] < Nv, v[1] < Nv};
-      FT s0[2] = {0, 0}, s3[2] = {0, 0}, X0[2] = {0, 0}, X1[2] = {0, 0}, X2[2] = {0, 0};
+      FT s0[2] = {0, 0}, s3[2] = {0, 0}, s4[2] = {0, 0}, X0[2] = {0, 0}, X1[2] = {0, 0}, X2[2] = {0, 0};
       for (int c = o0; c < o1; ++c) {
         const int idx = P.gcopy[c], e = idx >> 4, n = idx & 15;
         const FT w = P.gw[c];
         const FT *ec = P.econ + (size_t)idx * 6;
-        const size_t b0 = ((size_t)e * 4 * NN + n) * Nv;
+        const size_t b0 = ((size_t)e * NFC * NN + n) * Nv;
 #pragma unroll
         for (int h = 0; h < 2; ++h) {
           if (!ok[h]) continue;
           const size_t b = b0 + v[h];
           s0[h] = fma(w, C[b], s0[h]);
           s3[h] = fma(w, C[b + 48 * Nv], s3[h]);
+          if (Q5) s4[h] = fma(w, C[b + 64 * Nv], s4[h]);
           const FT u1 = C[b + 16 * Nv], u2 = C[b + 32 * Nv];
           X0[h] = fma(w, fma(u2, ec[3], mul_rn(u1, ec[0])), X0[h]);
           X1[h] = fma(w, fma(u2, ec[4], mul_rn(u1, ec[1])), X1[h]);
@@ -51,13 +54,14 @@ __global__ void __launch_bounds__(DSS_THREADS) k_dss(DevParams<FT> P, FT *__rest
       for (int c = o0; c < o1; ++c) {
         const int idx = P.gcopy[c], e = idx >> 4, n = idx & 15;
         const FT *eo = P.ecov + (size_t)idx * 6;
-        const size_t b0 = ((size_t)e * 4 * NN + n) * Nv;
+        const size_t b0 = ((size_t)e * NFC * NN + n) * Nv;
 #pragma unroll
         for (int h = 0; h < 2; ++h) {
           if (!ok[h]) continue;
           const size_t b = b0 + v[h];
           C[b] = s0[h];
           C[b + 48 * Nv] = s3[h];
+          if (Q5) C[b + 64 * Nv] = s4[h];
           C[b + 16 * Nv] = fma(eo[2], X2[h], fma(eo[1], X1[h], mul_rn(eo[0], X0[h])));
           C[b + 32 * Nv] = fma(eo[5], X2[h], fma(eo[4], X1[h], mul_rn(eo[3], X0[h])));
         }
@@ -297,13 +301,16 @@ __device__ __forceinline__ void two_sum_acc(double &s, double &cmp, double x) {
 
 constexpr int SUM_THREADS = 256;
 
-// Block partial sums of rho*WJ and rhoe*WJ (fixed order -> deterministic).
-template <class FT>
+// Block partial sums of rho*WJ and rhoe*WJ, and with Q5 (moist 0M) of
+// rhoq_tot*WJ, the fifth centre component (fixed order -> deterministic).
+// Each block writes NS (sum, compensation) pairs at part[block * 6].
+template <class FT, bool Q5 = false>
 __global__ void __launch_bounds__(SUM_THREADS) k_sums_partial(DevParams<FT> P, const FT *__restrict__ Yc, double *__restrict__ part) {
-  __shared__ double sh[4][SUM_THREADS];
+  constexpr int NS = Q5 ? 3 : 2, NFC = Q5 ? 5 : 4;
+  __shared__ double sh[2 * NS][SUM_THREADS];
   const int Nv = P.Nv;
   const size_t npt = (size_t)P.Nh * NN * Nv;
-  double s[2] = {0, 0}, c[2] = {0, 0};
+  double s[NS] = {}, c[NS] = {};
   for (size_t p = blockIdx.x * (size_t)SUM_THREADS + threadIdx.x; p < npt; p += (size_t)gridDim.x * SUM_THREADS) {
     const size_t col = p / Nv;
     const int v = (int)(p - col * Nv);
@@ -320,30 +327,34 @@ __global__ void __launch_bounds__(SUM_THREADS) k_sums_partial(DevParams<FT> P, c
     } else {
       WJ = (double)P.W[n] * (Jh * (double)P.levc[LC_R2 * Nv + v] * (double)P.levc[LC_DZ * Nv + v]);
     }
-    const size_t b = (e * 4 * NN + n) * Nv + v;
+    const size_t b = (e * NFC * NN + n) * Nv + v;
     two_sum_acc(s[0], c[0], (double)Yc[b] * WJ);
     two_sum_acc(s[1], c[1], (double)Yc[b + 48 * Nv] * WJ);
+    if (Q5) two_sum_acc(s[NS - 1], c[NS - 1], (double)Yc[b + 64 * Nv] * WJ);
   }
-  sh[0][threadIdx.x] = s[0]; sh[1][threadIdx.x] = c[0];
-  sh[2][threadIdx.x] = s[1]; sh[3][threadIdx.x] = c[1];
+#pragma unroll
+  for (int q = 0; q < NS; ++q) {
+    sh[2 * q][threadIdx.x] = s[q];
+    sh[2 * q + 1][threadIdx.x] = c[q];
+  }
   __syncthreads();
-  if (threadIdx.x < 2) {
+  if (threadIdx.x < NS) {
     double ss = 0, cc = 0;
     for (int t = 0; t < SUM_THREADS; ++t) {
       two_sum_acc(ss, cc, sh[2 * threadIdx.x][t]);
       cc += sh[2 * threadIdx.x + 1][t];
     }
-    part[blockIdx.x * 4 + 2 * threadIdx.x] = ss;
-    part[blockIdx.x * 4 + 2 * threadIdx.x + 1] = cc;
+    part[blockIdx.x * 6 + 2 * threadIdx.x] = ss;
+    part[blockIdx.x * 6 + 2 * threadIdx.x + 1] = cc;
   }
 }
 
-__global__ void k_sums_final(const double *__restrict__ part, int nblocks, double *__restrict__ out) {
-  if (threadIdx.x < 2) {
+__global__ void k_sums_final(const double *__restrict__ part, int nblocks, int nsums, double *__restrict__ out) {
+  if (threadIdx.x < nsums) {
     double ss = 0, cc = 0;
     for (int b = 0; b < nblocks; ++b) {
-      two_sum_acc(ss, cc, part[b * 4 + 2 * threadIdx.x]);
-      cc += part[b * 4 + 2 * threadIdx.x + 1];
+      two_sum_acc(ss, cc, part[b * 6 + 2 * threadIdx.x]);
+      cc += part[b * 6 + 2 * threadIdx.x + 1];
     }
     out[threadIdx.x] = ss + cc;
   }
@@ -387,6 +398,13 @@ void launch_dss(const DevParams<FT> &P, FT *C, FT *F, cudaStream_t s) {
   if (grid > 0) k_dss<FT><<<grid, DSS_THREADS, 0, s>>>(P, C, F);
 }
 template <class FT>
+void launch_dss_state(const DevParams<FT> &P, FT *C, FT *F, cudaStream_t s) {
+  const int grid = (P.ngroups + DSS_THREADS / 32 - 1) / (DSS_THREADS / 32);
+  if (grid <= 0) return;
+  if (P.moist) k_dss<FT, true><<<grid, DSS_THREADS, 0, s>>>(P, C, F);
+  else k_dss<FT><<<grid, DSS_THREADS, 0, s>>>(P, C, F);
+}
+template <class FT>
 void launch_dss_transpose(const DevParams<FT> &P, FT *C, FT *F, cudaStream_t s) {
   const int grid = (P.ngroups + DSS_THREADS / 32 - 1) / (DSS_THREADS / 32);
   if (grid > 0) k_dss_t<FT><<<grid, DSS_THREADS, 0, s>>>(P, C, F);
@@ -413,8 +431,9 @@ void launch_bc_filter(const DevParams<FT> &P, FT *Yf, cudaStream_t s) {
 }
 template <class FT>
 void launch_global_sums(const DevParams<FT> &P, const FT *Yc, double *partials, int nblocks, double *out, cudaStream_t s) {
-  k_sums_partial<FT><<<nblocks, SUM_THREADS, 0, s>>>(P, Yc, partials);
-  k_sums_final<<<1, 32, 0, s>>>(partials, nblocks, out);
+  if (P.moist) k_sums_partial<FT, true><<<nblocks, SUM_THREADS, 0, s>>>(P, Yc, partials);
+  else k_sums_partial<FT><<<nblocks, SUM_THREADS, 0, s>>>(P, Yc, partials);
+  k_sums_final<<<1, 32, 0, s>>>(partials, nblocks, P.moist ? 3 : 2, out);
 }
 template <class FT>
 void launch_reduce_rnorm(const double *rnorm, int ncols, double *out, cudaStream_t s) {
@@ -423,6 +442,7 @@ void launch_reduce_rnorm(const double *rnorm, int ncols, double *out, cudaStream
 
 #define INST(FT)                                                                                          \
   template void launch_dss<FT>(const DevParams<FT> &, FT *, FT *, cudaStream_t);                          \
+  template void launch_dss_state<FT>(const DevParams<FT> &, FT *, FT *, cudaStream_t);                    \
   template void launch_dss_transpose<FT>(const DevParams<FT> &, FT *, FT *, cudaStream_t);                \
   template void launch_final<FT>(const DevParams<FT> &, const StageArgs<FT> &, FT *, FT *, cudaStream_t); \
   template void launch_final_transpose<FT>(const DevParams<FT> &, const CotArgs<FT> &, FT *, FT *, cudaStream_t); \

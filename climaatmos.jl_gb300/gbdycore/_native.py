@@ -20,7 +20,7 @@ SYMBOLS = [
     "gb_sizes", "gb_geometry_export", "gb_ctx_create", "gb_ctx_destroy", "gb_set_stream", "gb_last_error",
     "gb_set_precomputed_quantities", "gb_remaining_tendency", "gb_implicit_tendency", "gb_update_jacobian",
     "gb_ldiv", "gb_correct_implicit_advection_tendency", "gb_dss", "gb_step", "gb_global_sums",
-    "gb_newton_residual", "gb_time_kernel", "gb_jacobian_solve_noalloc", "gb_match_elements",
+    "gb_conservation_sums",    "gb_newton_residual", "gb_time_kernel", "gb_jacobian_solve_noalloc", "gb_match_elements",
     "gb_selftest_bounded_wait",
     "gb_dss_transpose", "gb_remaining_tendency_vjp", "gb_implicit_stage", "gb_implicit_stage_vjp", "gb_step_vjp",
     "gb_adjoint_forward", "gb_adjoint_reverse", "gb_adjoint_set_record_segments",
@@ -103,6 +103,7 @@ def load(build_if_missing=True):
     L.gb_dss.argtypes = [_vp, fv]
     L.gb_step.argtypes = [_vp, fv, _c_double, _c_double, _c_int, _c_int]
     L.gb_global_sums.argtypes = [_vp, fv, _dp]
+    L.gb_conservation_sums.argtypes = [_vp, fv, _dp]
     L.gb_newton_residual.argtypes = [_vp, _dp]
     L.gb_time_kernel.argtypes = [_vp, _c_int, fv, _c_int, _dp]
     L.gb_jacobian_solve_noalloc.argtypes = [_vp, fv, fv, fv, _c_double]

@@ -171,6 +171,12 @@ class AtmosCache:
         self.call("gb_global_sums", Y.gb(), out)
         return np.array(out[:])
 
+    def conservation_sums(self, Y):
+        """∫ρ, ∫ρe_tot and ∫ρq_tot (0 when dry) of the state, compensated FP64."""
+        out = (ctypes.c_double * 3)()
+        self.call("gb_conservation_sums", Y.gb(), out)
+        return np.array(out[:])
+
     def newton_residual(self):
         out = (ctypes.c_double * 3)()
         self.call("gb_newton_residual", out)
@@ -347,6 +353,18 @@ class AtmosSolveResults:
 
     def __repr__(self):
         return "AtmosSolveResults(ret_code=%r, walltime=%r, sypd=%r)" % (self.ret_code, self.walltime, self.sypd)
+
+
+def check_conservation(first, last, moist, energy_surface_change=0.0, energy_radiation_input=0.0):
+    """The relative budgets of check_conservation (src/simulation/solve.jl:216-265) from the
+    conservation sums (∫ρ, ∫ρe_tot, ∫ρq_tot) of the first and the last state of a run
+    (``AtmosCache.conservation_sums``).  A surface without a slab ocean: the energy budget is
+    closed by the surface's and the top's net energy fluxes (zero without radiation and surface
+    fluxes) and no water leaves through the surface."""
+    energy = abs(last[1] - first[1] + energy_surface_change - energy_radiation_input) / first[1]
+    mass = (last[0] - first[0]) / first[0]
+    water = abs(last[2] - first[2]) / last[2] if moist else 0.0
+    return {"energy_conservation": energy, "mass_conservation": mass, "water_conservation": water}
 
 
 def solve_atmos(sim, nsteps=None, use_graph=True):

@@ -288,6 +288,25 @@ function global_sums(Y, p)
     return out
 end
 
+"""∫ρ, ∫ρe_tot and ∫ρq_tot (0 for a dry context): the sums check_conservation compares."""
+function conservation_sums(Y, p)
+    out = zeros(Cdouble, 3)
+    check(p.gb, ccall((:gb_conservation_sums, libgbdycore), Cint,
+        (Ptr{Cvoid}, GBFieldVec, Ptr{Cdouble}), p.gb.handle, gbvec(p.gb, Y), out))
+    return out
+end
+
+"""check_conservation (src/simulation/solve.jl:216-265) from the conservation sums of a run's
+first and last states, for a surface without a slab ocean."""
+function check_conservation(first, last, moist::Bool; energy_surface_change = 0.0,
+                            energy_radiation_input = 0.0)
+    energy_conservation =
+        abs(last[2] - first[2] + energy_surface_change - energy_radiation_input) / first[2]
+    mass_conservation = (last[1] - first[1]) / first[1]
+    water_conservation = moist ? abs(last[3] - first[3]) / last[3] : 0.0
+    return (; energy_conservation, mass_conservation, water_conservation)
+end
+
 """Sums of squares of the Newton residuals (ρ, ρe_tot, u₃) of the last step; throws if a kernel
 flagged a non-finite residual or a device wait that timed out."""
 function newton_residual(p)

@@ -110,8 +110,10 @@ typedef struct {
      liquid fraction ramps from 0 at T_icenuc to 1 at T_freeze with exponent pow_icenuc);
      sa_iters (>= 1) Newton iterations solve the saturation adjustment.  A moist context
      supports gb_set_precomputed_quantities, gb_implicit_tendency, gb_update_jacobian,
-     gb_ldiv and gb_correct_implicit_advection_tendency; every other state entry point returns
-     GB_ERR_ARG, as does moist = 1 with a surface or the Held-Suarez forcing. */
+     gb_ldiv, gb_correct_implicit_advection_tendency, gb_dss (rho q_tot averaged as a scalar)
+     and the conservation sums (gb_global_sums, gb_conservation_sums with the water integral);
+     every other state entry point returns GB_ERR_ARG, as does moist = 1 with a surface or the
+     Held-Suarez forcing. */
   int moist;
   double R_v, cp_v, cp_l, cp_i, LH_v0, LH_s0, T_triple, press_triple, T_freeze, T_icenuc, pow_icenuc;
   int sa_iters;
@@ -194,6 +196,11 @@ int gb_step(gb_ctx *ctx, gb_fieldvec Y, double t, double dt, int nsteps, int use
 /* Global integrals of rho and rho e_tot (sum of value * WJ), compensated FP64,
  * as check_conservation does (src/simulation/solve.jl:216-265).  Synchronous. */
 int gb_global_sums(gb_ctx *ctx, gb_fieldvec Y, double out[2]);
+
+/* The three integrals check_conservation compares (src/simulation/solve.jl:216-265): out[0]
+ * of rho, out[1] of rho e_tot and out[2] of rho q_tot (the water; 0 for a dry context, whose
+ * water_conservation the reference sets to zero), compensated FP64.  Synchronous. */
+int gb_conservation_sums(gb_ctx *ctx, gb_fieldvec Y, double out[3]);
 
 /* FP64 sums of squares of the Newton residual of the last gb_step (rho,
  * rho e_tot, u_3 parts, summed over stages); synchronous. */

@@ -590,12 +590,14 @@ struct Oracle {
       for (int v = 0; v < levels; ++v) {
         // the weighted sums as fused multiply-adds in ascending copy order (an exact
         // rounding recipe, so that a GPU DSS doing the same operations agrees bit for bit)
-        FT s0 = 0, s3 = 0, X[3] = {0, 0, 0};
+        // (moist: ρq_tot, centre component 4, is a scalar like ρ and ρe_tot)
+        FT s0 = 0, s3 = 0, s4 = 0, X[3] = {0, 0, 0};
         for (int c = goff[g]; c < goff[g + 1]; ++c) {
           int idx = gcopy[c], e = idx / NN, n = idx % NN;
           FT w = gw[c];
           s0 = std::fma(w, C[ci(e, 0, n, v)], s0);
           s3 = std::fma(w, C[ci(e, 3, n, v)], s3);
+          if (nfc == 5) s4 = std::fma(w, C[ci(e, 4, n, v)], s4);
           FT u1 = C[ci(e, 1, n, v)], u2 = C[ci(e, 2, n, v)];
           const FT *ec = &econ[hn(e, n) * 6];
           for (int d = 0; d < 3; ++d) X[d] = std::fma(w, std::fma(u2, ec[3 + d], u1 * ec[d]), X[d]);
@@ -604,6 +606,7 @@ struct Oracle {
           int idx = gcopy[c], e = idx / NN, n = idx % NN;
           C[ci(e, 0, n, v)] = s0;
           C[ci(e, 3, n, v)] = s3;
+          if (nfc == 5) C[ci(e, 4, n, v)] = s4;
           const FT *eo = &ecov[hn(e, n) * 6];
           C[ci(e, 1, n, v)] = std::fma(eo[2], X[2], std::fma(eo[1], X[1], eo[0] * X[0]));
           C[ci(e, 2, n, v)] = std::fma(eo[5], X[2], std::fma(eo[4], X[1], eo[3] * X[0]));
@@ -1381,10 +1384,11 @@ struct Oracle {
     set_precomputed(Yc, Yf);
   }
 
-  // ∫ rho dV, ∫ rho e_tot dV with compensated (Neumaier) FP64 summation
+  // ∫ rho dV, ∫ rho e_tot dV (and, moist, ∫ rho q_tot dV: the three sums of
+  // check_conservation, solve.jl:216-265) with compensated (Neumaier) FP64 summation
   void global_sums(const FT *Yc, double *out) const {
-    for (int c = 0; c < 2; ++c) {
-      int comp = c == 0 ? 0 : 3;
+    for (int c = 0; c < (nfc == 5 ? 3 : 2); ++c) {
+      const int comp = c == 0 ? 0 : c == 1 ? 3 : 4;
       double s = 0, comp_ = 0;
       for (int e = 0; e < Nh; ++e)
         for (int n = 0; n < NN; ++n)

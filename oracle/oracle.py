@@ -221,7 +221,6 @@ class Oracle:
         return Oc, Of
 
     def dss(self, Yc, Yf):
-        self._dry_only('dss')
         self._chk(Yc, Yf)
         lib().oracle_dss(self.h, _ptr(Yc), _ptr(Yf))
 
@@ -258,8 +257,8 @@ class Oracle:
         return tuple(x.reshape(shape) for x in out)
 
     def global_sums(self, Yc):
-        self._dry_only('global_sums')
-        out = np.zeros(2)
+        """∫ρ dV, ∫ρe_tot dV and, for a moist oracle, ∫ρq_tot dV (compensated FP64)."""
+        out = np.zeros(3 if self.moist else 2)
         lib().oracle_global_sums(self.h, _ptr(Yc), out.ctypes.data_as(_dp))
         return out
 

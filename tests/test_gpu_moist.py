@@ -3,7 +3,8 @@
 The centre block carries rho q_tot as its fifth component.  Each hook runs through the C ABI:
 the implicit tendency (central transport of q_tot, moist pressure from the saturation
 adjustment), the post-Newton correction, the Jacobian with kappa_m and the (u_3, rho q_tot),
-(rho q_tot, u_3) blocks, and ldiv with the rho q_tot row.  Tolerances (max-norm error relative
+(rho q_tot, u_3) blocks, and ldiv with the rho q_tot row; the state DSS (bitwise) and the
+conservation sums with the water integral.  Tolerances (max-norm error relative
 to each component's max magnitude): FP64 <= 2e-12 (measured: the implicit tendency's u_3 row
 3e-13 at z_elem 12 and 6e-13 at 63, the pressure-gradient difference of two terms each ~g dz;
 every other row and ldiv <= 3e-14); FP32 against the FP32 oracle <= 1e-3 (measured: u_3's
@@ -14,7 +15,8 @@ import pytest
 
 from gbdycore import _native as N
 from gbdycore import simulation as sim
-from helpers import make_oracle, moist_field_errors, moist_state, perturbed_state, rel_err, small_config
+from helpers import (dss_oracle_on_product_grid, make_oracle, moist_field_errors, moist_state, perturbed_state,
+                     rel_err, small_config)
 
 pytestmark = pytest.mark.gpu
 
@@ -110,7 +112,7 @@ def test_moist_context_refuses_the_dry_only_entries():
     Y = _dev(Yc, Yf)
     for call in (lambda: sim.remaining_tendency(Y.similar(), None, Y, p, 0.0),
                  lambda: p.call("gb_step", Y.gb(), 0.0, float(cfg.dt), 1, 0),
-                 lambda: p.global_sums(Y)):
+                 lambda: sim.dss_transpose(Y, p)):
         with pytest.raises(N.GBError) as e:
             call()
         assert e.value.code == N.GB_ERR_ARG
@@ -149,3 +151,45 @@ def test_moist_hooks_at_the_production_grid():
     X = Y.similar()
     sim.ldiv(X, sim.Jacobian(p), Yt)
     _assert_u3(moist_field_errors(*X.numpy(), *refx), 2e-12, 1e-11)
+
+
+@pytest.mark.parametrize("ft", [np.float64, np.float32])
+def test_moist_state_dss_matches_oracle_bitwise(ft):
+    """gb_dss of a moist state: rho q_tot averaged as a scalar with the dry DSS's fixed copy order
+    and fused multiply-add recipe, so that on the library's own grid tables the oracle agrees bit
+    for bit, rho q_tot included."""
+    cfg = small_config(ft=ft, moist=True)
+    Yc, Yf = moist_state(cfg)
+    rng = np.random.default_rng(2)
+    Yc = (Yc * (1 + 1e-3 * rng.normal(size=Yc.shape))).astype(ft)    # break continuity
+    Yf = (Yf + 1e-3 * rng.normal(size=Yf.shape)).astype(ft)
+    rc, rf = Yc.copy(), Yf.copy()
+    dss_oracle_on_product_grid(cfg, ft).dss(rc, rf)
+    p = sim.AtmosCache(cfg)
+    Y = _dev(Yc, Yf)
+    sim.dss(Y, p, 0.0)
+    gc, gf = Y.numpy()
+    np.testing.assert_array_equal(gc, rc)
+    np.testing.assert_array_equal(gf, rf)
+    assert not np.array_equal(gc[:, 4], Yc[:, 4])
+
+
+def test_moist_conservation_sums_match_oracle():
+    """gb_conservation_sums: the integrals of rho, rho e_tot and rho q_tot against the oracle's
+    compensated sums (1e-14); gb_global_sums returns the first two; a dry context reports no water."""
+    cfg = small_config(ft=np.float64, moist=True)
+    Yc, Yf = moist_state(cfg)
+    p = sim.AtmosCache(cfg)
+    Y = _dev(Yc, Yf)
+    s = p.conservation_sums(Y)
+    ref = make_oracle(cfg).global_sums(Yc)
+    assert s.shape == (3,) and s[2] > 0
+    assert np.all(np.abs(s - ref) <= 1e-14 * np.abs(ref)), (s, ref)
+    np.testing.assert_array_equal(p.global_sums(Y), s[:2])
+    dcfg = cfg.with_(moist=False)
+    Dc, Df = perturbed_state(dcfg)
+    pd = sim.AtmosCache(dcfg)
+    D = _dev(Dc, Df)
+    sd = pd.conservation_sums(D)
+    assert sd[2] == 0.0
+    np.testing.assert_array_equal(sd[:2], pd.global_sums(D))

@@ -1,6 +1,6 @@
 """The oracle's moist 0M column operators (CPU only): the saturation adjustment, the transport of
 rho q_tot in the implicit tendency and its post-Newton correction, the moist Jacobian blocks and
-the Schur solve with the rho q_tot row.
+the Schur solve with the rho q_tot row; the state DSS and the conservation sums with rho q_tot.
 
 Thermodynamics.jl (1.3.0, not vendored) and ClimaParams hold the reference's moist thermodynamics,
 so parity with them is unpinned.  Pinned here by properties of the formulation the reference's
@@ -195,3 +195,56 @@ def test_moist_initial_state_carries_the_profile_temperature():
     assert dry.any() and (~dry).any()
     assert np.abs(T[dry] - T_prof[dry]).max() < 1e-9
     assert np.all(T[~dry] > T_prof[~dry])
+
+
+def _discontinuous_moist(cfg, seed=5):
+    """A moist state whose collocated element copies disagree (rho q_tot too)."""
+    Yc, Yf = moist_state(cfg)
+    rng = np.random.default_rng(seed)
+    Yc = Yc * (1 + 1e-3 * rng.normal(size=Yc.shape))
+    Yf = Yf + 1e-3 * rng.normal(size=Yf.shape) * np.abs(Yf).max()
+    return np.ascontiguousarray(Yc), np.ascontiguousarray(Yf)
+
+
+def test_moist_state_dss_averages_rho_q_tot_as_a_scalar():
+    """dss! of a moist state (constrain_state.jl:59-64): rho, u_h, rho e_tot and the faces as the
+    dry DSS does them, rho q_tot exactly as rho (the same weights, copies and summation order)."""
+    cfg = _cfg()
+    Yc, Yf = _discontinuous_moist(cfg)
+    Xc, Xf = Yc.copy(), Yf.copy()
+    make_oracle(cfg).dss(Xc, Xf)
+    Dc, Df = np.ascontiguousarray(Yc[:, :4]), Yf.copy()
+    make_oracle(cfg.with_(moist=False)).dss(Dc, Df)
+    assert np.array_equal(Xc[:, :4], Dc) and np.array_equal(Xf, Df)
+    Qc = np.ascontiguousarray(Yc[:, [4, 1, 2, 3]])
+    make_oracle(cfg.with_(moist=False)).dss(Qc, Yf.copy())
+    assert np.array_equal(Xc[:, 4], Qc[:, 0])
+    assert not np.array_equal(Xc[:, 4], Yc[:, 4])
+
+
+def test_moist_conservation_sums_include_the_water():
+    """check_conservation's sums (solve.jl:216-265) of a moist state: the integrals of rho and
+    rho e_tot as the dry oracle forms them and the integral of rho q_tot with the same weights."""
+    cfg = _cfg()
+    Yc, Yf = moist_state(cfg)
+    s = make_oracle(cfg).global_sums(Yc)
+    dry = make_oracle(cfg.with_(moist=False))
+    assert s.shape == (3,)
+    assert np.array_equal(s[:2], dry.global_sums(np.ascontiguousarray(Yc[:, :4])))
+    assert s[2] == dry.global_sums(np.ascontiguousarray(Yc[:, [4, 1, 2, 3]]))[0]
+    assert s[2] > 0
+
+
+def test_check_conservation_budgets():
+    """The host side of check_conservation (solve.jl:216-265) on given sums: the energy budget
+    relative to the first state's energy, the signed mass change, the water change relative to the
+    last state's water, zero water budget for a dry run."""
+    from gbdycore.simulation import check_conservation
+    first, last = np.array([10.0, 200.0, 0.5]), np.array([10.1, 198.0, 0.4])
+    r = check_conservation(first, last, moist=True)
+    assert r["energy_conservation"] == pytest.approx(0.01)
+    assert r["mass_conservation"] == pytest.approx(0.01)
+    assert r["water_conservation"] == pytest.approx(0.25)
+    r = check_conservation(first, last, moist=False, energy_surface_change=3.0, energy_radiation_input=1.0)
+    assert r["energy_conservation"] == pytest.approx(0.0)
+    assert r["water_conservation"] == 0.0

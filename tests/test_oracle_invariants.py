@@ -223,3 +223,20 @@ def test_oracle_is_deterministic():
     o.step(a[0], a[1], cfg.dt, 2)
     o.step(b[0], b[1], cfg.dt, 2)
     assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+
+
+def test_step_meets_the_reference_conservation_bounds():
+    """check_conservation (solve.jl:216-265) over three oracle steps of the dry dycore, held to the
+    bounds the reference's CI asserts (.buildkite/ci_driver.jl:175-187): the energy budget within
+    100 eps, the mass budget within 250 eps (FP64)."""
+    from gbdycore.simulation import check_conservation
+    cfg = small_config(ft=np.float64)
+    Yc, Yf = perturbed_state(cfg)
+    o = make_oracle(cfg)
+    s0 = np.append(o.global_sums(Yc), 0.0)
+    o.step(Yc, Yf, cfg.dt, 3)
+    s1 = np.append(o.global_sums(Yc), 0.0)
+    r = check_conservation(s0, s1, moist=False)
+    eps = np.finfo(np.float64).eps
+    # the reference's `x ≈ 0 atol = a`: |x| <= a (the energy budget divides by the signed ∫ρe_tot)
+    assert abs(r["energy_conservation"]) <= 100 * eps and abs(r["mass_conservation"]) <= 250 * eps, r

@@ -1163,7 +1163,7 @@ int noalloc_scratch(gb_ctx *ctx, void **out) {
 template <class FT>
 int jacobian_solve_noalloc_t(gb_ctx *ctx, gb_fieldvec dY, gb_fieldvec Y, gb_fieldvec R, double dtg) {
   Impl<FT> *I = impl<FT>(ctx);
-  const size_t need = (size_t)I->P.Nh * NN * JAC_Q * I->P.Nf * sizeof(FT);
+  const size_t need = (size_t)I->P.Nh * NN * (I->P.moist ? JAC_QM : JAC_Q) * I->P.Nf * sizeof(FT);
   if (need > (size_t)GB_NOALLOC_SCRATCH_BYTES)
     return fail(ctx, GB_ERR_ARG, "gb_jacobian_solve_noalloc: Jacobian needs " + std::to_string(need) +
                                      " bytes, more than GB_NOALLOC_SCRATCH_BYTES (" +
@@ -1199,8 +1199,8 @@ bool fv_ok(gb_fieldvec v) { return v.c && v.f && aligned(v.c) && aligned(v.f); }
   } while (0)
 
 // A moist 0M context supports the column hooks (gb_set_precomputed_quantities,
-// gb_implicit_tendency, gb_update_jacobian, gb_ldiv, gb_correct_implicit_advection_tendency),
-// the state DSS and the conservation sums.
+// gb_implicit_tendency, gb_update_jacobian, gb_ldiv, gb_correct_implicit_advection_tendency,
+// gb_jacobian_solve_noalloc), the state DSS and the conservation sums.
 #define NO_MOIST(ctx, what)                                                                            \
   do {                                                                                                 \
     if ((ctx) && (ctx)->cfg.moist) return fail((ctx), GB_ERR_ARG, what " is not available with moist = 1"); \
@@ -1406,7 +1406,6 @@ int gb_newton_residual(gb_ctx *ctx, double out[3]) {
 
 int gb_jacobian_solve_noalloc(gb_ctx *ctx, gb_fieldvec dY, gb_fieldvec Y, gb_fieldvec R, double dtgamma) {
   GB_RANGE();
-  NO_MOIST(ctx, "gb_jacobian_solve_noalloc");
   GUARD(ctx);
   NO_TERRAIN(ctx, "gb_jacobian_solve_noalloc");
   if (!fv_ok(dY) || !fv_ok(Y) || !fv_ok(R)) return fail(ctx, GB_ERR_ARG, "null or misaligned pointer");

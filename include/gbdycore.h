@@ -110,7 +110,8 @@ typedef struct {
      liquid fraction ramps from 0 at T_icenuc to 1 at T_freeze with exponent pow_icenuc);
      sa_iters (>= 1) Newton iterations solve the saturation adjustment.  A moist context
      supports gb_set_precomputed_quantities, gb_implicit_tendency, gb_update_jacobian,
-     gb_ldiv, gb_correct_implicit_advection_tendency, gb_dss (rho q_tot averaged as a scalar)
+     gb_ldiv, gb_correct_implicit_advection_tendency, gb_jacobian_solve_noalloc, gb_dss (rho
+     q_tot averaged as a scalar)
      and the conservation sums (gb_global_sums, gb_conservation_sums with the water integral);
      every other state entry point returns GB_ERR_ARG, as does moist = 1 with a surface or the
      Held-Suarez forcing. */
@@ -227,8 +228,10 @@ int gb_selftest_bounded_wait(gb_ctx *ctx, double limit_s);
  * block storage with cudaMalloc on first use; this entry instead builds the
  * Jacobian at Y (with dtgamma) in a file-scope static device array of
  * GB_NOALLOC_SCRATCH_BYTES and solves W dY = R with it, allocating nothing.
- * Limit: (6 h_elem^2 * 16 columns) * (z_elem + 1) * 15 * ft_bytes must not
- * exceed GB_NOALLOC_SCRATCH_BYTES (else GB_ERR_ARG).  The array is held by
+ * Limit: (6 h_elem^2 * 16 columns) * (z_elem + 1) * nq * ft_bytes, nq = 15
+ * (19 for a moist 0M context, whose Jacobian carries the rho q_tot blocks), must
+ * not exceed GB_NOALLOC_SCRATCH_BYTES (else GB_ERR_ARG).  A terrain context
+ * returns GB_ERR_ARG.  The array is held by
  * every GPU that loads the library until the process exits.  The first call on
  * a device, with that device current, resolves the array's device address
  * (cudaGetSymbolAddress) and keeps it for the process: make that first call

@@ -20,7 +20,7 @@ import pytest
 
 from gbdycore import _native as N
 from gbdycore import simulation as sim
-from helpers import field_errors, make_oracle, perturbed_state, small_config
+from helpers import field_errors, make_oracle, moist_field_errors, moist_state, perturbed_state, small_config
 
 pytestmark = pytest.mark.gpu
 
@@ -50,6 +50,34 @@ def test_noalloc_jacobian_solve_matches_the_allocating_hooks(ft, tol):
         oc, of = o.ldiv(Rc, Rf)
         errs = field_errors(ro[0], ro[1], oc, of)
         assert all(v <= tol for v in errs.values()), (call, errs)
+
+
+@pytest.mark.parametrize("ft,tol", [(np.float64, 1e-13), (np.float32, 1e-3)])
+def test_noalloc_moist_jacobian_solve_matches_the_allocating_hooks(ft, tol):
+    """A moist 0M context: the 19 stored values per level (with the rho q_tot blocks) in the
+    static array, bitwise equal to gb_update_jacobian + gb_ldiv, and the oracle's moist ldiv."""
+    cfg = small_config(ft=ft, z_elem=40, moist=True)
+    p = sim.AtmosCache(cfg)
+    dtg = 0.4358665215084590 * cfg.dt
+    rng = np.random.default_rng(9)
+    Yc, Yf = moist_state(cfg, dtype=ft, w_amp=0.3)
+    Rc = (rng.normal(size=Yc.shape) * np.abs(Yc).max(axis=(0, 2, 3), keepdims=True) * 1e-3).astype(ft)
+    Rf = (rng.normal(size=Yf.shape) * 0.1).astype(ft)
+    Y, R = sim.FieldVector.from_numpy(Yc, Yf), sim.FieldVector.from_numpy(Rc, Rf)
+    ref, out = Y.similar(), Y.similar()
+    jac = sim.Jacobian(p)
+    sim.update_jacobian(jac, Y, p, dtg, 0.0)
+    sim.ldiv(ref, jac, R)
+    p.call("gb_jacobian_solve_noalloc", out.gb(), Y.gb(), R.gb(), float(dtg))
+    ro, rr = out.numpy(), ref.numpy()
+    np.testing.assert_array_equal(ro[0], rr[0])
+    np.testing.assert_array_equal(ro[1], rr[1])
+    o = make_oracle(cfg, ft)
+    o.set_precomputed(Yc, Yf)
+    o.update_jacobian(Yc, Yf, dtg)
+    oc, of = o.ldiv(Rc, Rf)
+    errs = moist_field_errors(ro[0], ro[1], oc, of)
+    assert all(v <= tol for v in errs.values()), errs
 
 
 def test_noalloc_rejects_grids_beyond_the_static_scratch():

@@ -1,7 +1,7 @@
 """The working tree that travels to a GPU host stays small.
 
-Files matched by .gpurunignore (build output, caches, raw profiles) stay behind;
-everything else is copied to the GPU host before a run, and a copy above
+Files matched by the copy's ignore list (build output, caches, raw profiles) stay
+behind; everything else is copied to the GPU host before a run, and a copy above
 512 MiB is refused there.  This test sums the sizes of the files that would
 travel and fails above 400 MiB, so that study dumps written into the tree are
 caught here first.
@@ -57,9 +57,9 @@ def travelling_bytes():
     return total, sorted(biggest, reverse=True)[:5]
 
 
-def test_gpurunignore_drops_build_output():
+def test_ignore_list_drops_build_output():
     pats = ignore_patterns()
-    for rel, is_dir in [("gpurun_out", True), ("climaatmos.jl_gb300/_build", True),
+    for rel, is_dir in [("climaatmos.jl_gb300/_build", True), ("_work/study.npz", False),
                         ("climaatmos.jl_gb300/gbdycore/libgbdycore.so", False), ("x/prof.ncu-rep", False)]:
         assert ignored(rel, is_dir, pats), rel
 
